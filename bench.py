@@ -1,0 +1,359 @@
+"""Benchmark of the exciton path: BSE build + lowest-exciton solve on one GB300.
+
+Metric: exciton solves/s (BSE build + lowest-10 solve) on the 2D hexagonal w=12, 60x60x1, 4v+4c system
+(BSE dimension 57,600, Rytova-Keldysh r0 = 40 A), in the mixed-precision form (matrix-free operator,
+split-BF16 tensor-core contraction, FP64 Rayleigh-Ritz and final refinement).  One step is one full
+solve: H(k) and bands for the 3600 k-points, V(k,k') table, operator set-up, block eigensolve.  Inputs
+are seeded synthetic systems (no dataset).  L2 is flushed (256 MB write) between timed steps.
+
+Also reported: the same solve in the plain FP64 GPU form (dense FP64 build + FP64 operator), timed
+once, with the largest exciton-energy difference between the two; the end-to-end time through the C
+ABI with host buffers; the live-timed roofline of the dominant kernel; a CPU baseline (the oracle's C
+restatement of the reference's element-by-element build and dense matvec, OpenMP on the host cores,
+timed on a bounded row sample and scaled to one solve).
+
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference] [--workload NAME]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "BSE build+solve s & exciton solves/s vs FP64 GPU path at 1e-5 eV error"
+UNIT = "solves/s"
+WORKLOADS = {
+    "hex12_60x60": "2D hexagonal w=12, |R|<=3a (37 R), 60x60x1 k-mesh, 4v+4c, BSE dim 57600, V2DRK r0=40 A, "
+                   "lowest 10 excitons",
+    "hex8_24x24": "2D hexagonal w=8, |R|<=3a (37 R), 24x24x1 k-mesh, 2v+2c, BSE dim 2304, V2DRK r0=40 A, "
+                  "lowest 10 excitons",
+    "cubic16_16x16x16": "simple cubic w=16, |R|<=2a (33 R), 16^3 k-mesh, 3v+3c, BSE dim 36864, V3DL eps=8, "
+                        "lowest 20 excitons",
+}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_rank{gpu_index}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return None
+
+
+def flush_l2(torch, buf):
+    buf.fill_(1.0)
+
+
+def cpu_baseline_sample(sysm, p, fp64_matvec_columns, budget_s=12.0):
+    """Time the oracle's C restatement (element-by-element build and dense matvec, OpenMP) on a bounded
+    row sample of this workload and scale it to one full solve.  Returns the cpu_baseline object."""
+    import ctypes
+
+    import __graft_entry__ as g
+    from oracle import wtb_oracle as O
+
+    g.build_oracle()
+    lib = ctypes.CDLL(g.ORACLE_SO)
+
+    class Coul(ctypes.Structure):
+        _fields_ = [("coultype", ctypes.c_int), ("ngrid", ctypes.c_int * 3), ("ktol", ctypes.c_double),
+                    ("ediel", ctypes.c_double * 3), ("ez", ctypes.c_double), ("w", ctypes.c_double),
+                    ("r0", ctypes.c_double), ("lc", ctypes.c_double), ("rlat", ctypes.c_double * 9)]
+
+    cp = Coul()
+    cp.coultype = {"V2DRK": 6, "V3DL": 2, "V3D": 1}[p.coultype]
+    for i in range(3):
+        cp.ngrid[i] = p.ngrid[i]
+        cp.ediel[i] = p.ediel[i]
+    cp.ktol, cp.ez, cp.w, cp.r0, cp.lc = p.ktol, p.ez, p.w_coul, p.r0, p.lc
+    for i in range(9):
+        cp.rlat[i] = float(sysm.rlat.reshape(-1)[i])
+    nk = p.nk
+    # bands on the host for the sample: only the rows' k-points and all k-points' bands are needed
+    kpt = O.monhkhorst_pack(p.ngrid[0], p.ngrid[1], p.ngrid[2], p.mshift, sysm.rlat)
+    t0 = time.perf_counter()
+    eigv, vec, _ = O.bands(sysm, p, kpt)
+    t_bands = time.perf_counter() - t0
+    dim = p.dim
+    eigv = np.ascontiguousarray(eigv)
+    vec = np.ascontiguousarray(vec)
+    kpt = np.ascontiguousarray(kpt)
+    nthreads = lib.oracle_num_threads()
+    # build: grow the row sample until it takes about half the budget
+    rows = 8
+    while True:
+        out = np.zeros((rows, dim), dtype=np.complex128)
+        t0 = time.perf_counter()
+        lib.oracle_build_rows(nk, p.nc, p.nv, sysm.w90basis, eigv.ctypes.data_as(ctypes.c_void_p),
+                              vec.ctypes.data_as(ctypes.c_void_p), kpt.ctypes.data_as(ctypes.c_void_p),
+                              ctypes.byref(cp), ctypes.c_long(0), ctypes.c_long(rows),
+                              out.ctypes.data_as(ctypes.c_void_p))
+        tb = time.perf_counter() - t0
+        if tb > budget_s / 4 or rows >= dim:
+            break
+        rows = min(dim, rows * 4)
+    elems = sum(dim - i for i in range(rows))
+    t_build = tb / elems * (dim * (dim + 1) / 2.0)
+    # dense matvec on a row block of the (dense, complex(8)) matrix: the operation a Krylov-Schur step applies
+    Hblk = np.ascontiguousarray(out + 0.0)
+    x = np.ones((dim, 1), dtype=np.complex128)
+    y = np.zeros((rows, 1), dtype=np.complex128)
+    t0 = time.perf_counter()
+    reps = 0
+    while time.perf_counter() - t0 < budget_s / 4:
+        lib.oracle_dense_mv(ctypes.c_long(rows), ctypes.c_long(dim), Hblk.ctypes.data_as(ctypes.c_void_p),
+                            x.ctypes.data_as(ctypes.c_void_p), 1, y.ctypes.data_as(ctypes.c_void_p))
+        reps += 1
+    t_mv = (time.perf_counter() - t0) / reps * (dim / rows)
+    t_total = t_bands + t_build + fp64_matvec_columns * t_mv
+    return {"value": 1.0 / t_total, "unit": UNIT, "cores": int(nthreads), "kind": "port",
+            "sample": (f"oracle C restatement: bands {t_bands:.2f} s (all {nk} k-points, LAPACK zheev), "
+                       f"element-by-element build of rows 0..{rows} of {dim} scaled to the upper triangle "
+                       f"({t_build:.1f} s), dense complex(8) matvec of that row block scaled to the full "
+                       f"matrix ({t_mv:.3f} s/column) x {fp64_matvec_columns} columns (the FP64 GPU solve's "
+                       f"matvec count); projected {t_total:.1f} s per solve"),
+            "projected_s_per_solve": t_total}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    from wtb_gb300 import synthetic as S
+
+    sysm, p = S.workload(args.workload)
+    vals = []
+    last = None
+    for i in range(args.warmup + args.steps):
+        cb = cpu_baseline_sample(sysm, p, fp64_matvec_columns=args.ref_matvecs, budget_s=args.ref_budget)
+        if i >= args.warmup:
+            vals.append(cb["value"])
+        last = cb
+    v = float(np.mean(vals))
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded H(R))", "impl": "reference",
+            "config": {"workload": args.workload, "description": WORKLOADS.get(args.workload, args.workload)},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": last["cores"], "kind": last["kind"],
+                             "sample": last["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--workload", default="hex12_60x60")
+    ap.add_argument("--precision", default="bf16x3")
+    ap.add_argument("--tol", type=float, default=1e-6)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU form")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--ref-matvecs", type=int, default=800)
+    ap.add_argument("--ref-budget", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    from wtb_gb300 import api
+    from wtb_gb300 import synthetic as S
+
+    # one independent replica of the workload per GPU (systems are independent; no collective)
+    sysm, p = S.workload(args.workload)
+    ctx = api.Context(local)
+    ctx.set_hr(sysm)
+    stream = torch.cuda.ExternalStream(api.lib().wtb_ctx_stream(ctx._h))
+    l2buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
+    solve_kw = dict(precision=args.precision, op="matfree", tol=args.tol)
+    for _ in range(args.warmup):
+        ctx.bsesolver(p, **solve_kw)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    api.lib().wtb_profile_enable(ctx._h, 1)
+    launches0 = api.kernel_launch_count()
+    last = None
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        flush_l2(torch, l2buf)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            ev[i][0].record(stream)
+        last = ctx.bsesolver(p, **solve_kw)
+        with torch.cuda.stream(stream):
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+    launches = api.kernel_launch_count() - launches0
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    tot_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([tot_ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot_ms = float(t.item())
+    import ctypes
+
+    tms, nl, fl, by = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double(), ctypes.c_double()
+    api.lib().wtb_profile_read(ctx._h, ctypes.byref(tms), ctypes.byref(nl), ctypes.byref(fl), ctypes.byref(by))
+    api.lib().wtb_profile_enable(ctx._h, 0)
+    value = world * args.steps / (tot_ms / 1000.0)
+
+    # end to end through the C ABI with host buffers: H(R) host -> device, Ws/acts/HE device -> host
+    e2e_ms = []
+    for i in range(max(1, min(args.steps, 3))):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.set_hr(sysm)
+        out = ctx.bsesolver(p, want_vectors=True, **solve_kw)
+        torch.cuda.synchronize()
+        e2e_ms.append(1000.0 * (time.perf_counter() - t0))
+    h2d = sysm.hop.nbytes + sysm.ihop.nbytes + sysm.rvec.astype(np.int32).nbytes + \
+        sysm.ffactor.astype(np.int32).nbytes + 9 * 8
+    d2h = p.dim * 8 + p.dim * 8 * 8 + p.dim * p.nev * 16
+    e2e = world * 1000.0 / float(np.mean(e2e_ms))
+
+    peaks = measured_peaks()
+    g_ms = tms.value / max(nl.value, 1)
+    g_flops = fl.value / max(nl.value, 1)
+    peak_t = peaks.get("bf16_tflops_sustained") if peaks else 1700.0
+    achieved = g_flops / (g_ms * 1e-3) / 1e12 if g_ms > 0 else None
+    roofline = {"bound": "tensor", "kernel": "tc_gemm_kernel (tcgen05 split-BF16 V x Z contraction)",
+                "achieved": achieved, "peak": peak_t, "unit": "TFLOP/s",
+                "frac": (achieved / peak_t) if achieved else None,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)" if peaks else "fallback",
+                "traffic": None, "launches_timed": int(nl.value), "avg_launch_ms": g_ms,
+                "flops_per_launch": g_flops, "algorithmic_bytes_per_launch": by.value / max(nl.value, 1),
+                "share_of_step": (tms.value / tot_ms) if tot_ms > 0 else None}
+    if args.precision not in ("bf16x3", "bf16x6"):
+        roofline["bound"] = "simt"
+    tr = os.path.join(ROOT, "profiles", "tc_gemm_traffic.json")
+    if os.path.exists(tr):
+        try:
+            roofline["traffic"] = json.load(open(tr)).get(args.workload)
+        except Exception:
+            pass
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tot_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16x3+f32 operator, f64 Rayleigh-Ritz" if args.precision == "bf16x3"
+            else args.precision, "data": "synthetic (seeded H(R))",
+            "config": {"workload": args.workload, "description": WORKLOADS.get(args.workload, args.workload),
+                       "operator": "matrix-free", "precision": args.precision, "eigensolver_tol": args.tol,
+                       "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}"},
+            "build_plus_solve_s": tot_ms / args.steps / 1000.0,
+            "solver": {"iterations": last["timings"]["iterations"],
+                       "matvec_columns": last["timings"]["matvec_columns"],
+                       "max_rel_residual": last["timings"]["max_rel_residual"],
+                       "fp64_refine_shift_eV": last["timings"]["refine_shift_max"],
+                       "stage_ms": {k: last["timings"][k] for k in ("t_bands_ms", "t_build_ms", "t_solve_ms",
+                                                                     "t_optics_ms", "t_total_ms")}},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches), "roofline": roofline, "clocks": clk}
+
+    fp64_cols = args.ref_matvecs
+    if rank == 0 and not args.no_fp64:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ref64 = ctx.bsesolver(p, precision="fp64", op="dense", tol=args.tol)
+        torch.cuda.synchronize()
+        t64 = time.perf_counter() - t0
+        dE = float(np.max(np.abs(ref64["E"] - last["E"])))
+        fp64_cols = int(ref64["timings"]["matvec_columns"])
+        line["fp64_gpu_form"] = {"build_plus_solve_s": t64, "solves_per_s": 1.0 / t64,
+                                 "speedup_mixed_vs_fp64": t64 / (tot_ms / args.steps / 1000.0),
+                                 "max_abs_dE_eV_mixed_vs_fp64": dE,
+                                 "iterations": ref64["timings"]["iterations"], "matvec_columns": fp64_cols,
+                                 "stage_ms": {k: ref64["timings"][k] for k in ("t_bands_ms", "t_build_ms",
+                                                                                "t_solve_ms", "t_total_ms")}}
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline_sample(sysm, p, fp64_cols, budget_s=args.ref_budget)
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,186 @@
+/*
+ * wtb_gpu.h -- C ABI of the GB300 exciton path (libwtb_gb300.so).
+ *
+ * The entry points replace the Fortran subroutines of the WTB exciton path one for one; each
+ * declaration names the reference interface it stands in for (file:line inside the WTB sources).
+ * Conventions shared by every call:
+ *   - plain pointers and sizes only; arrays use Fortran column-major order and complex(8) is
+ *     interleaved (re, im) double, i.e. C99 `double _Complex`;
+ *   - the caller allocates every output array; host pointers are used only during the call;
+ *   - every function returns a status code (WTB_OK = 0); wtb_last_error() returns the text the
+ *     reference would have printed before its STOP;
+ *   - a context binds one CUDA device and one stream; it is not thread-safe (one per host thread).
+ */
+#ifndef WTB_GPU_H
+#define WTB_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct wtb_ctx wtb_ctx;
+
+/* status codes */
+#define WTB_OK 0
+#define WTB_EBADARG 1   /* invalid argument / band window outside the occupied or empty states */
+#define WTB_ENOMEM 2    /* device allocation failed */
+#define WTB_ENOCONV 3   /* eigensolver did not converge within maxit */
+#define WTB_ETIMEOUT 4  /* a bounded device wait gave up; the kernel returned early */
+#define WTB_ENAN 5      /* non-finite value in the input or the iteration */
+#define WTB_ECUDA 6     /* CUDA runtime error */
+#define WTB_ESTATE 7    /* call made before the state it needs (e.g. no H(R) set) */
+#define WTB_ENODEV 8    /* no usable CUDA device / kernels missing for this device */
+
+/* arithmetic of the BSE operator (the Rayleigh-Ritz, orthogonalisation and final refinement are FP64 in
+ * every mode) */
+#define WTB_PREC_FP64 0   /* plain FP64 form: FP64 operator, FP64 iteration */
+#define WTB_PREC_FP32 1   /* FP32 operator (CUDA cores), FP32 iteration vectors */
+#define WTB_PREC_BF16X3 2 /* split-BF16 tensor-core operator, 3 slice products, FP32 accumulation */
+#define WTB_PREC_BF16X6 3 /* split-BF16 tensor-core operator, 6 slice products (~FP32 accuracy) */
+
+/* how the BSE operator is applied */
+#define WTB_OP_DENSE 0   /* dense Hamiltonian built in HBM, dense matvecs */
+#define WTB_OP_MATFREE 1 /* V(k,k') table and band vectors only; the matvec recomputes the kernel */
+
+/* Coulomb potentials (COULOMB_POT key; select case at src/module_bse.F90:49-72) */
+#define WTB_V2DK 0
+#define WTB_V3D 1
+#define WTB_V3DL 2
+#define WTB_V2DT 3
+#define WTB_V2DT2 4
+#define WTB_V2DOH 5
+#define WTB_V2DRK 6
+#define WTB_V1DT 7
+#define WTB_V0DT 8
+
+/* Run keys of bsesolver/bsedielraw (src/module_bse.F90:2023-2026, :835; defaults at
+ * src/module_input.F90:54-122).  Matches a Fortran bind(C) derived type field by field. */
+typedef struct wtb_bse_params {
+  int ngrid[3];      /* NGX NGY NGZ */
+  int nc, nv;        /* NBANDSC NBANDSV */
+  double mshift[3];  /* SHIFT_1..3 */
+  int coultype;      /* WTB_V2DRK, ... */
+  int renorm;        /* RNMD (imagrenorm) */
+  double ktol;       /* KTOL */
+  double ediel[3];   /* EDIEL_T EDIEL EDIEL_B */
+  double ez, w_coul, r0, lc; /* EDIEL_Z W_COUL R_0 LC */
+  double cshift;     /* CSHIFT: optics denominator and Lorentzian width */
+  double ebse0, ebsef; /* ENSPECI ENSPECF */
+  int numbse;        /* NESPEC */
+  int nev;           /* number of excitons (the reference hard-codes 100) */
+  int precision;     /* WTB_PREC_* */
+  int op;            /* WTB_OP_* */
+  double tol;        /* relative residual target of the eigensolver (SLEPc uses 1e-8) */
+  int maxit;         /* iteration cap (SLEPc uses 200) */
+  int block;         /* eigensolver block size, 0 = automatic */
+} wtb_bse_params;
+
+/* Per-call measurements filled by the solver entry points (may be NULL). */
+typedef struct wtb_timings {
+  double t_bands_ms, t_build_ms, t_solve_ms, t_optics_ms, t_total_ms;
+  int iterations, matvec_columns;
+  double max_rel_residual;
+  double refine_shift_max; /* max |E_refined - E_iteration| in eV from the FP64 final step */
+  int kernel_launches;
+} wtb_timings;
+
+/* ---------------------------------------------------------------------------------------------- */
+/* context */
+int wtb_ctx_create(wtb_ctx** ctx, int device);
+int wtb_ctx_destroy(wtb_ctx* ctx);
+const char* wtb_last_error(const wtb_ctx* ctx);
+int wtb_version(void);
+
+/* Replaces the module globals filled by hamiltonian_input_read
+ * (src/module_hamiltonian.F90:8-31, :35-194): w90basis, nvec, ffactor, rvec, hopmatrices,
+ * ihopmatrices, rlat, efermi, scs and systype ("NP" doubles the spectrum, src/module_bse.F90:875-879).
+ *   rvec        nvec x 3, integer lattice coordinates      (rvec(iR,d))
+ *   hopmatrices nvec x w x w, Re H_mn(R) at (iR,m,n)        (hopmatrices(iR,m,n))
+ *   rlat        3 x 3, rlat(i,:) = lattice vector a_i        (Angstrom) */
+int wtb_set_hr(wtb_ctx* ctx, int w90basis, int nvec, const int* rvec, const int* ffactor,
+               const double* hopmatrices, const double* ihopmatrices, const double* rlat, double efermi,
+               double scs, int systype_np);
+
+/* Replaces eigsys (src/module_hamiltonian.F90:200-320) with its full argument list: H(k) Fourier sum,
+ * Hermitian eigensolve, autovetores(i,:) = i-th eigenvector, nocp = #(E <= 0), scissor scs above nocp.
+ * Stateless: runs on the process-wide default context (device 0).  `exc` and `nthreads` are accepted
+ * and ignored, as in the reference. */
+int wtb_eigsys(int nthreads, double scs, double exc, int* nocp, const int* ffactor, double kx, double ky,
+               double kz, int w90basis, int nvec, const double* rlat, const int* rvec, const double* hopmatrices,
+               const double* ihopmatrices, double efermi, double* energias, double* autovetores);
+
+/* Replaces monhkhorst_pack (src/module_kmesh.F90:338-386): kpt is n1*n2*n3 x 3. Host computation. */
+int wtb_monhkhorst_pack(int n1, int n2, int n3, const double* shift, const double* rlat1, const double* rlat2,
+                        const double* rlat3, double* kpt);
+
+/* Replaces the eigsys loop of bsesolver (src/module_bse.F90:2230-2245) plus the band checks of
+ * quantumnumbers2 (src/module_math.F90:362-368): eigv(nk, nv+nc), vector(nk, nv+nc, w), nocpk(nk).
+ * Any output pointer may be NULL; the bands stay resident on the device for later calls. */
+int wtb_eigsys_mesh(wtb_ctx* ctx, int nk, const double* kpt, int nv, int nc, double* eigv, double* vector,
+                    int* nocpk);
+
+/* Replaces the scalar potentials of module_coulomb (v2dk, vcoul, v3diel, v2dt, v2dt2, v2dohono, v2drk,
+ * v0dt; src/module_coulomb.F90:11-387) evaluated for every pair: V(n1, n2) with V(i,j) = v(kpt1(i,:),
+ * kpt2(j,:)). */
+int wtb_coulomb_table(wtb_ctx* ctx, const wtb_bse_params* p, int n1, const double* kpt1, int n2,
+                      const double* kpt2, double* V);
+
+/* Replaces the optsp/hlm loop of bsesolver (src/module_bse.F90:2317-2348; src/module_optics.F90:12-167):
+ * hr(dim, 5) = hrx, hry, hrz, hrsp, hrsm for the bands of the last wtb_eigsys_mesh/wtb_bsesolver call. */
+int wtb_optsp(wtb_ctx* ctx, const wtb_bse_params* p, double* hr);
+
+/* Replaces the matrizelbse build loop and Hermitian mirror (src/module_bse.F90:24-83, :2392-2415):
+ * builds the dense BSE Hamiltonian on the device in p->precision (FP64 or FP32) from the bands of the
+ * last wtb_eigsys_mesh call.  If hbse is not NULL the dim x dim complex(8) matrix is copied out. */
+int wtb_bse_build(wtb_ctx* ctx, const wtb_bse_params* p, double* hbse);
+
+/* Applies the BSE operator of the last band set-up without storing it (or from the dense build):
+ * Y(dim, ncol) = H X(dim, ncol), complex(8), 1 <= ncol <= 32, in p->op / p->precision.  The operator is
+ * the one the matrizelbse loop assembles (src/module_bse.F90:24-83, :2392-2415); this entry lets a caller
+ * drive its own eigensolver, as the reference hands hbse to SLEPc (src/module_slepc_solver.F90:44-74). */
+int wtb_bse_matvec(wtb_ctx* ctx, const wtb_bse_params* p, int ncol, const double* X, double* Y);
+
+/* Replaces slepc_solver(HX, EX, HE, NX, NE) (src/module_slepc_solver.F90:12-97): the lowest NE eigenpairs
+ * of the dense Hermitian NX x NX matrix HX (host, complex(8)); EX(NE), HE(NX, NE).  tol 1e-8 relative
+ * residual and 200 iterations as in the reference, FP64 throughout. */
+int wtb_slepc_solver(wtb_ctx* ctx, const double* HX, double* EX, double* HE, int NX, int NE);
+
+/* Replaces dielbsev/dielbsep (src/module_bse.F90:171-245): activity(i) = |sum_j A(j,i) h(j)|^2 (pair = 0)
+ * or Re[(sum_j A(j,i) h1(j)) conj(sum_j A(j,i) h2(j))] (pair = 1) for i <= dimse1, zero above. */
+int wtb_dielbse(wtb_ctx* ctx, int dimse, int dimse1, const double* excitonvec, const double* hopt1,
+                const double* hopt2, int pair, double* activity);
+
+/* Replaces bsesolver (src/module_bse.F90:2023-2594) without its text files: mesh, bands, optics, BSE
+ * operator, lowest p->nev excitons, oscillator strengths.  Outputs (each may be NULL):
+ *   Ws(dim)      exciton energies, rows past nev set to 0 (the reference leaves them unassigned)
+ *   acts(dim, 8) xx yy zz xy xz yz sp sm activities, rows past nev zero
+ *   HE(dim, nev) exciton eigenvectors (complex(8)) */
+int wtb_bsesolver(wtb_ctx* ctx, const wtb_bse_params* p, double* Ws, double* acts, double* HE, wtb_timings* t);
+
+/* Replaces bsedielraw (src/module_bse.F90:835-1036 with optdiel, avgsme and imagrenorm,
+ * src/module_optics.F90:171-401): dielf(numbse, 3, 6) = (omega, eps1, eps2) for xx yy zz xy xz yz from
+ * the dimse rows of Ws and acts(dimse, 6). */
+int wtb_bsedielraw(wtb_ctx* ctx, const wtb_bse_params* p, int dimse, const double* Ws, const double* acts,
+                   double* dielf);
+
+/* Replaces bseoptprop (src/module_bse.F90:3766-3931, formulas :5075-5124): props(numbse, 6, 5) =
+ * refractive index, extinction coefficient, reflectivity, absorption coefficient, energy-loss function. */
+int wtb_bseoptprop(wtb_ctx* ctx, int numbse, const double* dielf, double* props);
+
+/* Number of CUDA kernels this library has launched in the process (instrumentation for benchmarks). */
+long long wtb_kernel_launch_count(void);
+
+/* The cudaStream_t the context launches on (for CUDA events recorded by a caller). */
+void* wtb_ctx_stream(wtb_ctx* ctx);
+
+/* Live timing of the operator's dominant kernel (the V x Z contraction of the matrix-free operator):
+ * when enabled, CUDA events bracket each launch on the context's stream.  wtb_profile_read returns the
+ * summed device time, the launch count, and the algorithmic flops and bytes of those launches. */
+int wtb_profile_enable(wtb_ctx* ctx, int on);
+int wtb_profile_read(wtb_ctx* ctx, double* total_ms, long long* launches, double* flops, double* bytes);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WTB_GPU_H */

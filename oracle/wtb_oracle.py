@@ -1,0 +1,488 @@
+"""CPU FP64 oracle for the exciton path -- TEST INFRASTRUCTURE ONLY.
+
+This module restates, in numpy/scipy, the arithmetic of the reference's exciton path so that the
+GPU implementation can be checked against it.  Only ``tests/``, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` may import it; the product path never does.
+
+Parity status: UNPINNED by reference outputs.  The reference ships no tests, no golden vectors and
+no expected outputs, and it cannot be compiled here (Fortran, MPI, PETSc/SLEPc and MKL are absent).
+The oracle is anchored instead on (a) a line-by-line restatement of the reference routines cited in
+each docstring, including their single-precision constants and roundings, (b) analytic known-answer
+tests (tests/test_oracle.py), and (c) LAPACK ZHEEV itself (scipy.linalg.lapack.zheev, the same
+routine the reference calls for the per-k problem).  Third-party arithmetic the reference links
+but does not ship: SLEPc/PETSc 3.22.2 Krylov-Schur (replaced here by dense ``zheevd`` or ARPACK
+``eigsh`` on the same matrix) and LAPACK ``ZHEEV`` from MKL/OpenBLAS.
+
+Index conventions (0-based here, 1-based in the reference):
+  exciton basis I = k*nc*nv + c*nv + v, c in [0,nc) is band slot nv+c, v in [0,nv) is slot v
+  (``quantumnumbers2``, src/module_math.F90:352-379).
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.linalg
+import scipy.linalg.lapack as lapack
+
+F32 = np.float32
+PI_F32 = float(F32(np.arccos(F32(-1.0))))            # acos(-1.) single precision
+CIC = -float(F32(F32(0.0904756) * F32(1000.0)))      # -(0.0904756)*10**(3), src/module_coulomb.F90:15
+GAMA = float(F32(180.90))                            # e^2/e0, src/module_optics.F90:196
+HC = float(F32(19.746e-6))                           # src/module_bse.F90:5111
+SQRT2_F32 = float(F32(np.sqrt(F32(2.0))))            # sqrt(2.0) in abscoef, src/module_bse.F90:5113
+INV_SQRT2_F32 = float(F32(F32(1.0) / F32(np.sqrt(F32(2.0)))))  # 1.0/sqrt(2.), src/module_bse.F90:2328
+RENORM_SHIFT = float(F32(0.15))                      # factor=0.15, src/module_optics.F90:345
+ALPHA1_V2DK = float(F32(1.76))                       # src/module_coulomb.F90:17
+
+
+class OracleError(RuntimeError):
+    """Raised where the reference executes STOP."""
+
+
+# ----------------------------------------------------------------------------- lattice helpers
+def prodvec(v1, v2):
+    """src/module_math.F90:129-134."""
+    return np.array([v1[1] * v2[2] - v1[2] * v2[1], v1[2] * v2[0] - v1[0] * v2[2],
+                     v1[0] * v2[1] - v1[1] * v2[0]])
+
+
+def vcell2D(rlat):
+    """|a1 x a2|, src/module_math.F90:143-149."""
+    vx = prodvec(rlat[0], rlat[1])
+    return float(np.sqrt(vx[0] ** 2 + vx[1] ** 2 + vx[2] ** 2))
+
+
+def vcell3D(rlat):
+    """|(a1 x a2) . a3|, src/module_math.F90:153-160."""
+    vx = prodvec(rlat[0], rlat[1])
+    return abs(float(vx[0] * rlat[2, 0] + vx[1] * rlat[2, 1] + vx[2] * rlat[2, 2]))
+
+
+def alat2D(rlat):
+    """src/module_math.F90:184-192."""
+    s = [float(np.sqrt(np.sum(rlat[i] ** 2))) for i in range(3)]
+    return 0.5 * (s[0] + s[1])
+
+
+def recvec(a1, a2, a3):
+    """b_i = 2*pi/vol * (a_j x a_k) with single-precision pi, src/module_kmesh.F90:391-407."""
+    v23, v31, v12 = prodvec(a2, a3), prodvec(a3, a1), prodvec(a1, a2)
+    vol = abs(a1[0] * v23[0] + a1[1] * v23[1] + a1[2] * v23[2])
+    f = (2.0 * PI_F32) / vol
+    return f * v23, f * v31, f * v12
+
+
+def monhkhorst_pack(n1, n2, n3, shift, rlat):
+    """Gamma-anchored mesh, i outer, j, l inner (src/module_kmesh.F90:338-386)."""
+    b1, b2, b3 = recvec(rlat[0], rlat[1], rlat[2])
+    ks = np.array([b1[d] * shift[0] + b2[d] * shift[1] + b3[d] * shift[2] for d in range(3)])
+    kpt = np.empty((n1 * n2 * n3, 3))
+    c = 0
+    for i in range(n1):
+        for j in range(n2):
+            for l in range(n3):
+                for d in range(3):
+                    kpt[c, d] = (b1[d] / n1) * i + (b2[d] / n2) * j + (b3[d] / n3) * l + ks[d]
+                c += 1
+    return kpt
+
+
+# ----------------------------------------------------------------------------- H(k) and eigsys
+def _phases_f32(kpt, rvec, rlat):
+    """phi_R = k.R rounded to single precision by cmplx(0.0, ...) (src/module_hamiltonian.F90:240-244).
+
+    kpt (Nk,3) -> (Nk, nR) float64 holding float32 values."""
+    Rx = rvec[:, 0] * rlat[0, 0] + rvec[:, 1] * rlat[1, 0] + rvec[:, 2] * rlat[2, 0]
+    Ry = rvec[:, 0] * rlat[0, 1] + rvec[:, 1] * rlat[1, 1] + rvec[:, 2] * rlat[2, 1]
+    Rz = rvec[:, 0] * rlat[0, 2] + rvec[:, 1] * rlat[1, 2] + rvec[:, 2] * rlat[2, 2]
+    kpt = np.atleast_2d(kpt)
+    phi = kpt[:, 0:1] * Rx[None] + kpt[:, 1:2] * Ry[None] + kpt[:, 2:3] * Rz[None]
+    return phi.astype(F32).astype(np.float64)
+
+
+def hk_matrix(k, sysm):
+    """H(k) = sum_R e^{i phi_R} (H_re + i H_im)(R)/ndegen - E_F I (src/module_hamiltonian.F90:246-259)."""
+    phi = _phases_f32(np.asarray(k)[None], sysm.rvec, sysm.rlat)[0]
+    e = np.exp(1j * phi)
+    H = np.einsum("r,rmn->mn", e / sysm.ffactor.astype(np.float64), sysm.hop + 1j * sysm.ihop)
+    H = H - sysm.efermi * np.eye(sysm.w90basis)
+    return H
+
+
+def eigsys(k, sysm, nocp_in=None):
+    """One k-point: ZHEEV('V','L') then transpose, nocp, scissor (src/module_hamiltonian.F90:200-320).
+
+    Returns (energias (w,), autovetores (w,w) with row i = eigenvector i, nocp)."""
+    H = hk_matrix(k, sysm)
+    w, v, info = lapack.zheev(H, compute_v=1, lower=1)
+    if info > 0:
+        raise OracleError("The algorithm failed to compute eigenvalues.")
+    energias = np.array(w, dtype=np.float64)
+    autovetores = np.array(v.T)
+    pos = np.flatnonzero(energias > 0.0)
+    nocp = int(pos[0]) if len(pos) else (sysm.w90basis if nocp_in is None else nocp_in)
+    energias[nocp:] += sysm.scs
+    return energias, autovetores, nocp
+
+
+def gauge_fix(vec):
+    """Rotate each eigenvector (rows of ``vec``) so its first component is real and >= 0.
+
+    ZHEEV('L') leaves the first component real (ZHETRD('L') keeps e1 invariant); its sign is free
+    and every output of the path is invariant under a sign flip, so this is the comparison gauge."""
+    v = np.array(vec)
+    a = v[..., 0]
+    ph = np.where(np.abs(a) > 0, np.conj(a) / np.where(np.abs(a) > 0, np.abs(a), 1.0), 1.0)
+    return v * ph[..., None]
+
+
+def bands(sysm, p, kpt):
+    """The eigsys loop of bsesolver (src/module_bse.F90:2230-2245) plus quantumnumbers2's checks.
+
+    Returns eigv (Nk, nv+nc), vector (Nk, nv+nc, w), nocpk (Nk,)."""
+    Nk = len(kpt)
+    w = sysm.w90basis
+    eigv = np.empty((Nk, p.nv + p.nc))
+    vec = np.empty((Nk, p.nv + p.nc, w), dtype=np.complex128)
+    nocpk = np.empty(Nk, dtype=np.int64)
+    for i in range(Nk):
+        e, v, nocp = eigsys(kpt[i], sysm)
+        nocpk[i] = nocp
+        if p.nv > nocp:
+            raise OracleError("Number of valence states higher then ocuppied states")
+        if p.nc > w - nocp:
+            raise OracleError("Number of conduction states higher then unocuppied states")
+        eigv[i] = e[nocp - p.nv: nocp + p.nc]
+        vec[i] = v[nocp - p.nv: nocp + p.nc]
+    return eigv, vec, nocpk
+
+
+# ----------------------------------------------------------------------------- Coulomb potentials
+def _modk(k1, k2):
+    """modvec, src/module_math.F90:221-225."""
+    d = k1 - k2
+    return np.sqrt(d[..., 0] ** 2 + d[..., 1] ** 2 + d[..., 2] ** 2)
+
+
+def coulomb_table(kpt1, kpt2, p, rlat):
+    """V(k,k') for every pair, vectorised restatement of module_coulomb (src/module_coulomb.F90).
+
+    Supported: V2DRK (:286-350), V3DL (:98-131), V3D (:64-94), V2DK (:11-60), V2DOH (:354-387),
+    V2DT (:135-193), V2DT2 (:243-282), V0DT (:197-238)."""
+    k1 = np.asarray(kpt1)[:, None, :]
+    k2 = np.asarray(kpt2)[None, :, :]
+    modk = _modk(k1, k2)
+    ng = int(p.ngrid[0] * p.ngrid[1] * p.ngrid[2])
+    tol = p.ktol
+    small = modk < tol
+    safe = np.where(small, 1.0, modk)
+    ct = p.coultype
+    ed = p.ediel
+    if ct == "V2DRK":
+        vc = vcell2D(rlat)
+        vbz = 1.0 / (ng * vc)
+        epar, et, eb = ed[1], ed[0], ed[2]
+        eta = np.sqrt(epar / p.ez)
+        kappa = np.sqrt(epar * p.ez)
+        pb = (eb - kappa) / (eb + kappa)
+        pt = (et - kappa) / (et + kappa)
+        aux1 = (1.0 - (pb * pt * np.exp(-2.0 * safe * eta * p.lc))) * kappa
+        aux2 = (1.0 - (pt * np.exp(-eta * safe * p.lc))) * (1.0 - (pb * np.exp(-eta * safe * p.lc)))
+        aux3 = p.r0 * safe * np.exp(-safe * p.w_coul)
+        ew = (aux1 / aux2) + aux3
+        V = (vbz * CIC) * np.exp(-safe * p.w_coul) * (1.0 / ew) * (1.0 / safe)
+        return np.where(small, 0.0, V)
+    if ct in ("V3DL", "V3D"):
+        vc = vcell3D(rlat)
+        vbz = 1.0 / (ng * vc)
+        e = ed[1] if ct == "V3DL" else 1.0
+        V = vbz * (CIC / e) * (1.0 / (safe * safe))
+        return np.where(small, 0.0, V)
+    if ct == "V2DK":
+        a0 = alat2D(rlat)
+        vc = vcell2D(rlat)
+        r0 = ((ed[1] - 1.0) * p.lc) / (ed[0] + ed[2])
+        vbz = 1.0 / (ng * vc)
+        g1 = float(p.ngrid[0] * p.ngrid[1])
+        auxi = (2.0 * PI_F32 * r0) / (a0 * np.sqrt(g1))
+        e = (ed[0] + ed[2]) / 2.0
+        v0 = vbz * (CIC / e) * (a0 * np.sqrt(g1) / (2.0 * PI_F32)) * (ALPHA1_V2DK + auxi * 1.0 + 0.0 * auxi ** 2)
+        V = vbz * (CIC / e) * (1.0 / (safe * (1 + (r0 * safe))))
+        return np.where(small, v0, V)
+    if ct == "V2DOH":
+        vc = vcell2D(rlat)
+        vbz = 1.0 / (ng * vc)
+        V = (vbz * CIC) * np.exp(-p.w_coul * safe) * (1.0 / (p.ez * safe))
+        return np.where(small, 0.0, V)
+    if ct == "V2DT":
+        vc = vcell3D(rlat)
+        vbz = 1.0 / (ng * vc)
+        d = k1 - k2
+        gz = np.abs(d[..., 2])
+        gpar = np.sqrt(d[..., 0] ** 2 + d[..., 1] ** 2)
+        rc = 0.5 * rlat[2, 2]
+        c1 = (gpar < tol) & (gz < tol)
+        c2 = (gpar < tol) & (gz >= tol)
+        m2 = np.where(modk > 0, modk, 1.0) ** 2
+        v1 = (vbz * CIC) * (-0.5 * rc * rc)
+        v2 = (vbz * CIC) * (1.0 / m2) * (1.0 - np.cos(gz * rc) - (gz * rc * np.sin(gz * rc)))
+        gp = np.where(gpar > 0, gpar, 1.0)
+        aux1 = gz / gp
+        aux2 = gpar * rc
+        aux3 = gz * rc
+        v3 = (vbz * CIC) * (1.0 / m2) * (1.0 + (np.exp(-aux2) * (aux1 * np.sin(aux3) - np.cos(aux3))))
+        return np.where(c1, v1, np.where(c2, v2, v3))
+    if ct == "V2DT2":
+        vc = vcell3D(rlat)
+        vbz = 1.0 / (ng * vc)
+        d = k1 - k2
+        qxy = np.sqrt(d[..., 0] ** 2 + d[..., 1] ** 2)
+        V = (vbz * CIC) * (1.0 / (safe * safe)) * (1.0 - np.exp(-0.5 * qxy * p.lc) * np.cos(0.5 * p.lc * d[..., 2]))
+        return np.where(small, 0.0, V)
+    if ct == "V0DT":
+        vc = vcell3D(rlat)
+        vbz = 1.0 / (ng * vc)
+        cr = 0.5 * min(float(np.sqrt(np.sum(rlat[i] ** 2))) for i in range(3))
+        V = (vbz * CIC) * (1.0 / (safe * safe)) * (1.0 - np.cos(cr * safe))
+        return np.where(small, (vbz * CIC) * 0.5 * cr * cr, V)
+    raise OracleError("Wrong Coulomb Potential")
+
+
+# ----------------------------------------------------------------------------- BSE build
+def basis(nk, nc, nv):
+    """stt of quantumnumbers2: returns (k, c_slot, v_slot) arrays of length dim (0-based slots)."""
+    I = np.arange(nk * nc * nv)
+    k = I // (nc * nv)
+    c = (I // nv) % nc
+    v = I % nv
+    return k, nv + c, v
+
+
+def bse_build(eigv, vec, kpt, p, rlat):
+    """Dense hbse: upper triangle by matrizelbse (src/module_bse.F90:24-83) then the Hermitian mirror
+    (src/module_bse.F90:2392-2415).  Vectorised: element (i,j) is V(k_i,k_j)*<c_i|c_j>*<v_i|v_j>, the
+    diagonal is (E_c - E_v) + V(k_i,k_i)."""
+    nk = len(kpt)
+    kk, cs, vs = basis(nk, p.nc, p.nv)
+    V = coulomb_table(kpt, kpt, p, rlat)
+    Cv = vec[kk, cs]          # (dim, w)
+    Vv = vec[kk, vs]
+    gc = np.conj(Cv) @ Cv.T   # <c_i|c_j>
+    gv = np.conj(Vv) @ Vv.T   # <v_i|v_j>  (v_i^* . v_j, not the textbook <v_j|v_i>)
+    H = V[kk[:, None], kk[None, :]] * gc * gv
+    dE = eigv[kk, cs] - eigv[kk, vs]
+    d = np.arange(len(kk))
+    H[d, d] = dE + V[kk, kk]
+    iu = np.triu_indices(len(kk), 1)
+    H[iu[1], iu[0]] = np.conj(H[iu[0], iu[1]])
+    return H
+
+
+def bse_matvec_factored(x, eigv, vec, kpt, p, rlat, V=None):
+    """Matrix-free y = H x through V(k,k') and the orbital factorisation; same operator as bse_build."""
+    nk = len(kpt)
+    nc, nv = p.nc, p.nv
+    if V is None:
+        V = coulomb_table(kpt, kpt, p, rlat)
+    C = vec[:, nv:nv + nc]        # (nk, nc, w)
+    Vb = vec[:, :nv]              # (nk, nv, w)
+    X = x.reshape(nk, nc, nv, -1)
+    Z = np.einsum("kco,kvp,kcvb->kopb", C, Vb, X)
+    T = np.einsum("kq,qopb->kopb", V, Z)
+    Y = np.einsum("kco,kvp,kopb->kcvb", np.conj(C), np.conj(Vb), T)
+    dE = (eigv[:, nv:nv + nc][:, :, None] - eigv[:, :nv][:, None, :])
+    Y += dE[..., None] * X
+    return Y.reshape(x.shape)
+
+
+def slepc_solver(HX, NE):
+    """Lowest NE eigenpairs of the dense Hermitian HX (stands in for SLEPc Krylov-Schur,
+    src/module_slepc_solver.F90:12-97; EPS_SMALLEST_MAGNITUDE equals smallest-algebraic for the
+    positive BSE spectra used here).  Returns (EX (NE,), HE (dim, NE))."""
+    n = HX.shape[0]
+    w, v = scipy.linalg.eigh(HX, subset_by_index=[0, min(NE, n) - 1], driver="evr")
+    return w, v
+
+
+# ----------------------------------------------------------------------------- optics
+def hlm(k, sysm):
+    """dH/dk_alpha = sum_R i R_alpha e^{i phi_R} H(R)/ndegen, on-site diagonal of H(R=0) removed,
+    R_alpha and phi rounded to single precision (src/module_optics.F90:12-108)."""
+    rvec, rlat = sysm.rvec, sysm.rlat
+    phi = _phases_f32(np.asarray(k)[None], rvec, rlat)[0]
+    Rx = (rvec[:, 0] * rlat[0, 0] + rvec[:, 1] * rlat[1, 0] + rvec[:, 2] * rlat[2, 0]).astype(F32).astype(np.float64)
+    Ry = (rvec[:, 0] * rlat[0, 1] + rvec[:, 1] * rlat[1, 1] + rvec[:, 2] * rlat[2, 1]).astype(F32).astype(np.float64)
+    Rz = (rvec[:, 0] * rlat[0, 2] + rvec[:, 1] * rlat[1, 2] + rvec[:, 2] * rlat[2, 2]).astype(F32).astype(np.float64)
+    Hc = (sysm.hop + 1j * sysm.ihop).copy()
+    for i in range(len(rvec)):
+        if np.all(rvec[i] == 0):
+            Hc[i][np.diag_indices(sysm.w90basis)] = 0.0
+    e = np.exp(1j * phi) / sysm.ffactor
+    hx = np.einsum("r,rmn->mn", 1j * Rx * e, Hc)
+    hy = np.einsum("r,rmn->mn", 1j * Ry * e, Hc)
+    hz = np.einsum("r,rmn->mn", 1j * Rz * e, Hc)
+    return hx, hy, hz
+
+
+def optsp_all(eigv, vec, kpt, sysm, p):
+    """hr_alpha for every basis state (src/module_bse.F90:2317-2348 calling optsp,
+    src/module_optics.F90:113-167).  factor = 1./esp is assigned to a real variable, so the scaling is
+    Re(1/(E_c - E_v + i*float32(CSHIFT))).  Returns hrx, hry, hrz, hrsp, hrsm (dim,) complex."""
+    nk = len(kpt)
+    nc, nv = p.nc, p.nv
+    dim = nk * nc * nv
+    out = np.empty((3, dim), dtype=np.complex128)
+    s32 = float(F32(p.cshift))
+    for k in range(nk):
+        hs = hlm(kpt[k], sysm)
+        for c in range(nc):
+            for v in range(nv):
+                I = k * nc * nv + c * nv + v
+                cv = vec[k, nv + c]
+                vv = vec[k, v]
+                esp = (eigv[k, nv + c] - eigv[k, v]) + 1j * s32
+                factor = (1.0 / esp).real
+                for a in range(3):
+                    out[a, I] = factor * (np.conj(cv) @ (hs[a] @ vv))
+    hrsp = (out[0] + 1j * out[1]) * INV_SQRT2_F32
+    hrsm = (out[0] - 1j * out[1]) * INV_SQRT2_F32
+    return out[0], out[1], out[2], hrsp, hrsm
+
+
+def dielbsev(A, hopt, dim):
+    """act(i) = |sum_j A(j,i) h(j)|^2 for i <= nev, zero beyond (src/module_bse.F90:201-245)."""
+    act = np.zeros(dim)
+    s = A.T @ hopt
+    act[:A.shape[1]] = (s * np.conj(s)).real
+    return act
+
+
+def dielbsep(A, h1, h2, dim):
+    """act(i) = Re[(sum A h1)(sum A h2)^*] (src/module_bse.F90:171-196)."""
+    act = np.zeros(dim)
+    s1 = A.T @ h1
+    s2 = A.T @ h2
+    act[:A.shape[1]] = (s1 * np.conj(s2)).real
+    return act
+
+
+# ----------------------------------------------------------------------------- spectrum
+def avgsme(E):
+    """10 * (sum_{i>=2} (E_i - E_{i-1})) / ndim (src/module_optics.F90:313-335)."""
+    s = 0.0
+    for i in range(1, len(E)):
+        s = s + E[i] - E[i - 1]
+    return 10.0 * (s / float(len(E)))
+
+
+def optdiel_grid(rtype, vc, ngrid, elux, E, f, sme):
+    """optdiel for a vector of photon energies (src/module_optics.F90:171-255)."""
+    baux = float(F32(ngrid[0] * ngrid[1] * ngrid[2])) * vc
+    caux = GAMA / (baux * 1.0)
+    delta = 1.0 if rtype == 1 else 0.0
+    smef = avgsme(E) + sme
+    ex = E[None, :]
+    el = np.asarray(elux)[:, None]
+    eaux = ((el - ex) ** 2) + (smef ** 2)
+    rpart = np.sum(f[None, :] * ((ex - el) / eaux), axis=1)
+    ipart = np.sum(f[None, :] * (smef / eaux), axis=1)
+    return delta + rpart * caux, ipart * caux
+
+
+def imagrenorm(E1, dielf):
+    """In-place baseline renormalisation of dielf[:,2] (src/module_optics.F90:338-401)."""
+    aux = E1 - RENORM_SHIFT
+    if aux <= 0.0:
+        return dielf
+    n = dielf.shape[0]
+    ibegin = 0
+    for i in range(n):
+        if dielf[i, 0] <= aux:
+            ibegin = i
+        else:
+            break
+    if ibegin + 1 >= n:
+        return dielf
+    aux3 = dielf[ibegin + 1, 2]
+    dielf[: ibegin + 1, 2] = 0.0
+    t = dielf[ibegin + 1:, 2] - aux3
+    dielf[ibegin + 1:, 2] = np.where(t < 0.0, 0.0, t)
+    return dielf
+
+
+COMPONENTS = ("xx", "yy", "zz", "xy", "xz", "yz")
+
+
+def bsedielraw(Ws, acts, ngrid, rlat, p, spinf=1.0):
+    """epsilon(omega) for the six components (src/module_bse.F90:835-1036).
+
+    ``Ws`` and ``acts`` are the dim-row arrays that bsesolver writes (rows past nev hold E = 0 and
+    zero activities).  Returns dict comp -> (numbse, 3) array [omega, spinf*eps1, spinf*eps2]."""
+    vc = vcell3D(rlat)
+    N = int(p.numbse)
+    j = np.arange(N, dtype=np.float64)
+    elux = p.ebse0 + ((p.ebsef - p.ebse0) * j) / (float(N) - 1.0)
+    out = {}
+    for comp in COMPONENTS:
+        rtype = 1 if comp in ("xx", "yy", "zz") else 0
+        r, im = optdiel_grid(rtype, vc, ngrid, elux, Ws, acts[comp], p.cshift)
+        d = np.stack([elux, r, im], axis=1)
+        if p.renorm:
+            imagrenorm(Ws[0], d)
+        d[:, 1] *= spinf
+        d[:, 2] *= spinf
+        out[comp] = d
+    return out
+
+
+def abscoef(e1, e2, efoton):
+    """alpha = sqrt(2)*omega/hc*sqrt(|eps| - eps1) (src/module_bse.F90:5107-5114)."""
+    aux = np.sqrt(e1 * e1 + e2 * e2)
+    return (SQRT2_F32 * efoton) * (1.0 / HC) * np.sqrt(aux - e1)
+
+
+def optprops(e1, e2, omega):
+    """refractive index, extinction, reflectivity, absorption, loss (src/module_bse.F90:5075-5124)."""
+    aux = np.sqrt(e1 * e1 + e2 * e2)
+    n = np.sqrt((aux + e1) / 2.0)
+    kap = np.sqrt((aux - e1) / 2.0)
+    refl = ((n - 1.0) ** 2 + kap * kap) / ((n + 1.0) ** 2 + kap * kap)
+    return {"refr": n, "ext": kap, "refl": refl, "abs": abscoef(e1, e2, omega),
+            "eloss": e2 / (e1 * e1 + e2 * e2)}
+
+
+# ----------------------------------------------------------------------------- whole path
+def bsesolver(sysm, p, dense_solver=True, nev=None, with_vectors=False):
+    """The bsesolver path (src/module_bse.F90:2023-2594) for the oracle: mesh -> eigsys -> optics ->
+    build -> lowest nev -> oscillator strengths.  Returns a dict with Ws (dim,), acts, E (nev,), A."""
+    nev = p.nev if nev is None else nev
+    kpt = monhkhorst_pack(p.ngrid[0], p.ngrid[1], p.ngrid[2], p.mshift, sysm.rlat)
+    eigv, vec, nocpk = bands(sysm, p, kpt)
+    hrx, hry, hrz, hrsp, hrsm = optsp_all(eigv, vec, kpt, sysm, p)
+    dim = p.dim
+    if dense_solver:
+        H = bse_build(eigv, vec, kpt, p, sysm.rlat)
+        E, A = slepc_solver(H, nev)
+    else:
+        import scipy.sparse.linalg as sla
+        V = coulomb_table(kpt, kpt, p, sysm.rlat)
+        op = sla.LinearOperator((dim, dim), dtype=np.complex128,
+                                matvec=lambda x: bse_matvec_factored(x.reshape(-1, 1), eigv, vec, kpt, p,
+                                                                     sysm.rlat, V).ravel())
+        E, A = sla.eigsh(op, k=nev, which="SA", tol=1e-12)
+        o = np.argsort(E)
+        E, A = E[o], A[:, o]
+    Ws = np.zeros(dim)
+    Ws[:nev] = E
+    acts = {"xx": dielbsev(A, hrx, dim), "yy": dielbsev(A, hry, dim), "zz": dielbsev(A, hrz, dim),
+            "xy": dielbsep(A, hrx, hry, dim), "xz": dielbsep(A, hrx, hrz, dim),
+            "yz": dielbsep(A, hry, hrz, dim), "sp": dielbsev(A, hrsp, dim), "sm": dielbsev(A, hrsm, dim)}
+    out = {"kpt": kpt, "eigv": eigv, "vec": vec, "nocpk": nocpk, "E": E, "Ws": Ws, "acts": acts,
+           "hr": np.stack([hrx, hry, hrz, hrsp, hrsm])}
+    if with_vectors:
+        out["A"] = A
+    return out
+
+
+def round_f15_4(x):
+    """The 7F15.4 text handoff of bse_opt_diel.dat (src/module_bse.F90:2556-2567)."""
+    return np.round(np.asarray(x, dtype=np.float64), 4)

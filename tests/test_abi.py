@@ -1,0 +1,51 @@
+"""The C-ABI library: loads without a GPU and exports every entry point include/wtb_gpu.h declares."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    text = open(os.path.join(ROOT, "include", "wtb_gpu.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[a-z_ ]+\**\s*\**(wtb_[a-z0-9_]+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    for n in ("wtb_ctx_create", "wtb_set_hr", "wtb_eigsys", "wtb_bsesolver", "wtb_slepc_solver", "wtb_bsedielraw",
+              "wtb_bseoptprop", "wtb_bse_build", "wtb_coulomb_table", "wtb_dielbse", "wtb_monhkhorst_pack"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(built):
+    lib = ctypes.CDLL(os.path.join(ROOT, "wtb_gb300", "libwtb_gb300.so"))
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_host_only_entry_points(built):
+    """monhkhorst_pack is host arithmetic: matches the package's mesh without a GPU."""
+    import numpy as np
+
+    from wtb_gb300 import api, synthetic
+
+    rlat = synthetic.hex_lattice()
+    k = api.monhkhorst_pack(5, 4, 1, [0.1, 0.0, 0.0], rlat[0], rlat[1], rlat[2])
+    ref = synthetic.monkhorst_pack((5, 4, 1), rlat, (0.1, 0.0, 0.0))
+    np.testing.assert_allclose(k, ref, rtol=0, atol=1e-14)
+
+
+def test_no_device_is_an_error_not_a_fallback(built):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from wtb_gb300 import api
+
+    with pytest.raises(api.WTBError) as e:
+        api.Context(0)
+    assert e.value.code == api.WTB_ENODEV

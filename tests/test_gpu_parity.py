@@ -1,0 +1,236 @@
+"""Parity of the CUDA path (through the C ABI) against the FP64 oracle on seeded systems.
+
+Tolerances: integer outputs exact; per-k band energies 1e-11 eV; band vectors 1e-9 (after the
+first-component-real gauge, sign included); V table and FP64 dense build 1e-12 relative; FP32 build
+2e-6 of the largest element; exciton energies 1e-5 eV (the acceptance bound) in every precision mode;
+spectra 1e-4 relative L2.
+"""
+import numpy as np
+import pytest
+
+from oracle import wtb_oracle as O
+from wtb_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+MODES = [("fp64", "dense"), ("fp32", "dense"), ("fp64", "matfree"), ("fp32", "matfree"), ("bf16x3", "matfree"),
+         ("bf16x6", "matfree")]
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def small():
+    sysm, p = S.workload("hex8_6x6")
+    ref = O.bsesolver(sysm, p, with_vectors=True)
+    return sysm, p, ref
+
+
+@pytest.fixture(scope="module")
+def c1():
+    sysm, p = S.workload("hex8_24x24")
+    ref = O.bsesolver(sysm, p, with_vectors=False)
+    return sysm, p, ref
+
+
+def test_bands_match_zheev(ctx, small):
+    sysm, p, ref = small
+    ctx.set_hr(sysm)
+    eigv, vec, nocp = ctx.eigsys_mesh(ref["kpt"], p.nv, p.nc)
+    np.testing.assert_array_equal(nocp, ref["nocpk"])
+    np.testing.assert_allclose(eigv, ref["eigv"], rtol=0, atol=1e-11)
+    np.testing.assert_allclose(vec, O.gauge_fix(ref["vec"]), rtol=0, atol=1e-9)
+    # ZHEEV('L') leaves the first component real: the oracle's vectors equal ours up to a sign
+    assert np.max(np.abs(ref["vec"][..., 0].imag)) < 1e-12
+
+
+def test_eigsys_reference_argument_list(built, small):
+    from wtb_gb300 import api
+
+    sysm, p, ref = small
+    k = ref["kpt"][7]
+    nocp, e, av = api.eigsys(1, sysm.scs, 0.0, 0, sysm.ffactor, k[0], k[1], k[2], sysm.w90basis, sysm.nvec,
+                             sysm.rlat, sysm.rvec, sysm.hop, sysm.ihop, sysm.efermi)
+    e_ref, av_ref, nocp_ref = O.eigsys(k, sysm)
+    assert nocp == nocp_ref
+    np.testing.assert_allclose(e, e_ref, atol=1e-11)
+    np.testing.assert_allclose(av, O.gauge_fix(av_ref), atol=1e-9)
+
+
+def test_scissor_shift(ctx, small):
+    sysm, p, ref = small
+    s2 = sysm.copy()
+    s2.scs = 0.37
+    ctx.set_hr(s2)
+    eigv, _, _ = ctx.eigsys_mesh(ref["kpt"], p.nv, p.nc)
+    e_ref, _, nocp = O.eigsys(ref["kpt"][3], s2)
+    np.testing.assert_allclose(eigv[3], e_ref[nocp - p.nv: nocp + p.nc], atol=1e-11)
+    ctx.set_hr(sysm)
+
+
+@pytest.mark.parametrize("coultype", ["V2DRK", "V3DL", "V3D", "V2DK", "V2DOH", "V2DT", "V2DT2", "V0DT"])
+def test_coulomb_table(ctx, small, coultype):
+    sysm, p, ref = small
+    ctx.set_hr(sysm)
+    q = S.BSEParams(**{**p.__dict__})
+    q.coultype = coultype
+    q.ediel = (1.5, 4.0, 2.0)
+    q.ez, q.w_coul, q.r0, q.lc = 2.0, 0.7, 35.0, 6.0
+    kpt = ref["kpt"]
+    V = ctx.coulomb_table(q, kpt)
+    Vref = O.coulomb_table(kpt, kpt, q, sysm.rlat)
+    np.testing.assert_allclose(V, Vref, rtol=1e-12, atol=1e-14 * np.abs(Vref).max())
+
+
+def test_optics_matrix_elements(ctx, small):
+    sysm, p, ref = small
+    ctx.set_hr(sysm)
+    ctx.eigsys_mesh(ref["kpt"], p.nv, p.nc)
+    hr = ctx.optsp(p)
+    h_ref = np.stack(O.optsp_all(ref["eigv"], O.gauge_fix(ref["vec"]), ref["kpt"], sysm, p))
+    np.testing.assert_allclose(hr, h_ref, rtol=0, atol=1e-10 * np.abs(h_ref).max())
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32", 2e-6)])
+def test_dense_build(ctx, small, precision, tol):
+    sysm, p, ref = small
+    ctx.set_hr(sysm)
+    ctx.eigsys_mesh(ref["kpt"], p.nv, p.nc)
+    H = ctx.bse_build(p, precision=precision)
+    Href = O.bse_build(ref["eigv"], O.gauge_fix(ref["vec"]), ref["kpt"], p, sysm.rlat)
+    assert np.abs(H - H.conj().T).max() == 0.0
+    np.testing.assert_allclose(H, Href, rtol=0, atol=tol * np.abs(Href).max())
+
+
+MATVEC_TOL = {("fp64", "dense"): 1e-13, ("fp32", "dense"): 2e-6, ("fp64", "matfree"): 1e-13,
+              ("fp32", "matfree"): 2e-6, ("bf16x3", "matfree"): 2e-4, ("bf16x6", "matfree"): 2e-6}
+
+
+@pytest.mark.parametrize("precision,op", MODES)
+@pytest.mark.parametrize("ncol", [1, 5, 16, 20])
+def test_operator_matvec(ctx, small, precision, op, ncol):
+    """Every operator variant against the oracle's dense FP64 matrix, relative to ||H x||."""
+    sysm, p, ref = small
+    ctx.set_hr(sysm)
+    ctx.eigsys_mesh(ref["kpt"], p.nv, p.nc)
+    Href = O.bse_build(ref["eigv"], O.gauge_fix(ref["vec"]), ref["kpt"], p, sysm.rlat)
+    rng = np.random.default_rng(ncol)
+    X = rng.normal(size=(p.dim, ncol)) + 1j * rng.normal(size=(p.dim, ncol))
+    Y = ctx.bse_matvec(p, X, precision=precision, op=op)
+    Yref = Href @ X
+    err = np.linalg.norm(Y - Yref, axis=0) / np.linalg.norm(Yref, axis=0)
+    assert err.max() <= MATVEC_TOL[(precision, op)], err
+
+
+def test_slepc_solver_dense(ctx, small):
+    sysm, p, ref = small
+    Href = O.bse_build(ref["eigv"], ref["vec"], ref["kpt"], p, sysm.rlat)
+    EX, HE = ctx.slepc_solver(Href, 6)
+    w = np.linalg.eigvalsh(Href)[:6]
+    np.testing.assert_allclose(EX, w, atol=1e-9)
+    R = Href @ HE - HE * EX[None, :]
+    assert np.linalg.norm(R, axis=0).max() < 1e-7 * np.abs(EX).max()
+
+
+@pytest.mark.parametrize("precision,op", MODES)
+def test_bsesolver_small(ctx, small, precision, op):
+    sysm, p, ref = small
+    ctx.set_hr(sysm)
+    out = ctx.bsesolver(p, precision=precision, op=op, tol=1e-8 if precision == "fp64" else 1e-6)
+    np.testing.assert_allclose(out["E"], ref["E"], rtol=0, atol=1e-5)
+    assert np.all(out["Ws"][p.nev:] == 0.0)
+    dim = p.dim
+    for c in ("xx", "yy", "zz"):
+        assert np.all(out["acts"][c][p.nev:] == 0.0)
+
+
+@pytest.mark.parametrize("precision,op", MODES)
+def test_bsesolver_hex8_24x24(ctx, c1, precision, op):
+    """dim 2304, 10 excitons: energies within 1e-5 eV and the spectrum within 1e-4 relative L2."""
+    sysm, p, ref = c1
+    ctx.set_hr(sysm)
+    out = ctx.bsesolver(p, precision=precision, op=op, tol=1e-8 if precision == "fp64" else 1e-6)
+    err = np.abs(out["E"] - ref["E"])
+    assert err.max() <= 1e-5, err
+    spec = O.bsedielraw(out["Ws"], out["acts"], p.ngrid, sysm.rlat, p)
+    spec_ref = O.bsedielraw(ref["Ws"], ref["acts"], p.ngrid, sysm.rlat, p)
+    for c in ("xx", "yy", "zz"):
+        assert rel_l2(spec[c][:, 2], spec_ref[c][:, 2]) <= 1e-4, c
+
+
+def test_spectrum_kernel(ctx, c1):
+    sysm, p, ref = c1
+    ctx.set_hr(sysm)
+    d = ctx.bsedielraw(p, ref["Ws"], ref["acts"])
+    d_ref = O.bsedielraw(ref["Ws"], ref["acts"], p.ngrid, sysm.rlat, p)
+    for c in O.COMPONENTS:
+        np.testing.assert_allclose(d[c], d_ref[c], rtol=1e-10, atol=1e-12 * max(1.0, np.abs(d_ref[c]).max()))
+
+
+def test_optprops_kernel(ctx, c1):
+    sysm, p, ref = c1
+    ctx.set_hr(sysm)
+    d_ref = O.bsedielraw(ref["Ws"], ref["acts"], p.ngrid, sysm.rlat, p)
+    props = ctx.bseoptprop(d_ref)
+    for c in O.COMPONENTS:
+        om, e1, e2 = d_ref[c][:, 0], d_ref[c][:, 1], d_ref[c][:, 2]
+        pr = O.optprops(e1, e2, om)
+        for nm in ("refr", "ext", "refl", "abs", "eloss"):
+            np.testing.assert_allclose(props[nm][c], pr[nm], rtol=1e-12, atol=1e-12)
+
+
+def test_dielbse(ctx, small):
+    sysm, p, ref = small
+    A = ref["A"]
+    hr = ref["hr"]
+    act = ctx.dielbse(p.dim, A.shape[1], A, hr[0])
+    np.testing.assert_allclose(act, O.dielbsev(A, hr[0], p.dim), rtol=1e-12, atol=1e-14)
+    act = ctx.dielbse(p.dim, A.shape[1], A, hr[0], hr[1])
+    np.testing.assert_allclose(act, O.dielbsep(A, hr[0], hr[1], p.dim), rtol=1e-12, atol=1e-14)
+
+
+def test_error_band_window(ctx, small):
+    from wtb_gb300 import api
+
+    sysm, p, ref = small
+    ctx.set_hr(sysm)
+    q = S.BSEParams(**{**p.__dict__})
+    q.nv = sysm.w90basis // 2 + 1
+    q.nc = 1
+    with pytest.raises(api.WTBError) as e:
+        ctx.bsesolver(q)
+    assert e.value.code == api.WTB_EBADARG
+    assert "valence states higher" in str(e.value)
+
+
+def test_error_arguments(ctx, small):
+    from wtb_gb300 import api
+
+    sysm, p, ref = small
+    ctx.set_hr(sysm)
+    q = S.BSEParams(**{**p.__dict__})
+    q.ktol = 0.0
+    with pytest.raises(api.WTBError) as e:
+        ctx.bsesolver(q)
+    assert e.value.code == api.WTB_EBADARG
+    q = S.BSEParams(**{**p.__dict__})
+    q.nev = p.dim + 1
+    with pytest.raises(api.WTBError) as e:
+        ctx.bsesolver(q)
+    assert e.value.code == api.WTB_EBADARG
+    bad = sysm.copy()
+    bad.hop[0, 0, 0] = np.nan
+    with pytest.raises(api.WTBError) as e:
+        ctx.set_hr(bad)
+    assert e.value.code == api.WTB_ENAN
+    ctx.set_hr(sysm)
+
+
+def test_determinism_fp64(ctx, small):
+    sysm, p, ref = small
+    ctx.set_hr(sysm)
+    a = ctx.bsesolver(p, precision="fp64", op="dense", tol=1e-8)
+    b = ctx.bsesolver(p, precision="fp64", op="dense", tol=1e-8)
+    assert np.array_equal(a["E"], b["E"])

@@ -1,0 +1,215 @@
+"""The FP64 oracle on the CPU: known-answer tests, invariants, the golden fixtures, and the C restatement.
+
+The reference ships no tests or golden outputs for this path; these checks pin the oracle by
+(1) single-precision constants and roundings read off the reference sources, (2) analytic known answers
+(no Coulomb interaction => excitons are the lowest transition energies; Lorentzian sum rule; gauge
+behaviour of eigenvalues versus oscillator strengths), (3) agreement of two independent restatements
+(vectorised numpy and the element-by-element C loop), and (4) committed golden fixtures.
+"""
+import ctypes
+import os
+
+import numpy as np
+import pytest
+
+from oracle import wtb_oracle as O
+from wtb_gb300 import synthetic as S
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def small():
+    sysm, p = S.workload("hex8_6x6")
+    kpt = O.monhkhorst_pack(*p.ngrid, p.mshift, sysm.rlat)
+    eigv, vec, nocp = O.bands(sysm, p, kpt)
+    return sysm, p, kpt, eigv, vec, nocp
+
+
+def test_single_precision_constants():
+    assert O.CIC == -90.47559356689453
+    assert O.PI_F32 == 3.1415927410125732
+    assert O.GAMA == 180.89999389648438
+    assert O.INV_SQRT2_F32 == 0.7071067690849304
+    assert O.RENORM_SHIFT == 0.15000000596046448
+    assert O.HC == float(np.float32(19.746e-6))
+
+
+def test_mesh_is_gamma_anchored_k_outer():
+    rlat = S.hex_lattice()
+    k = O.monhkhorst_pack(3, 2, 1, (0.0, 0.0, 0.0), rlat)
+    assert np.all(k[0] == 0.0)
+    b1, b2, _ = O.recvec(*rlat)
+    np.testing.assert_allclose(k[1], b2 / 2, atol=1e-15)     # (i=0, j=1): j runs inside i
+    np.testing.assert_allclose(k[2], b1 / 3, atol=1e-15)
+    np.testing.assert_allclose(k, S.monkhorst_pack((3, 2, 1), rlat), atol=1e-15)
+    # reciprocal vectors use single-precision pi: a_i . b_j = 2*pi_f32 delta_ij
+    np.testing.assert_allclose(rlat @ np.array([b1, b2, O.recvec(*rlat)[2]]).T, 2 * O.PI_F32 * np.eye(3), atol=1e-12)
+
+
+def test_eigsys_zheev_gauge_and_occupation(small):
+    sysm, p, kpt, eigv, vec, nocp = small
+    e, v, n = O.eigsys(kpt[5], sysm)
+    assert np.all(np.diff(e) >= 0)
+    np.testing.assert_allclose(v @ v.conj().T, np.eye(sysm.w90basis), atol=1e-12)
+    assert np.max(np.abs(v[:, 0].imag)) < 1e-12          # first component real (ZHETRD('L') keeps e1)
+    assert n == np.sum(e <= 0) == sysm.w90basis // 2
+    H = O.hk_matrix(kpt[5], sysm)
+    np.testing.assert_allclose(H @ v.T, v.T * e[None, :], atol=1e-11)
+
+
+def test_scissor_above_fermi_level(small):
+    sysm, p, kpt, *_ = small
+    s2 = sysm.copy()
+    s2.scs = 0.4
+    e0, _, n0 = O.eigsys(kpt[3], sysm)
+    e1, _, n1 = O.eigsys(kpt[3], s2)
+    assert n0 == n1
+    np.testing.assert_allclose(e1[:n0], e0[:n0])
+    np.testing.assert_allclose(e1[n0:], e0[n0:] + 0.4)
+
+
+def test_band_window_errors(small):
+    sysm, p, kpt, *_ = small
+    q = S.BSEParams(**{**p.__dict__})
+    q.nv = sysm.w90basis // 2 + 1
+    with pytest.raises(O.OracleError, match="valence states higher"):
+        O.bands(sysm, q, kpt)
+    q = S.BSEParams(**{**p.__dict__})
+    q.nc = sysm.w90basis // 2 + 1
+    with pytest.raises(O.OracleError, match="conduction states higher"):
+        O.bands(sysm, q, kpt)
+
+
+def test_no_interaction_gives_transition_energies(small):
+    """With V = 0 (KTOL larger than every |k - k'|) the excitons are the lowest E_c - E_v."""
+    sysm, p, kpt, eigv, vec, _ = small
+    q = S.BSEParams(**{**p.__dict__})
+    q.ktol = 1e6
+    H = O.bse_build(eigv, vec, kpt, q, sysm.rlat)
+    E, _ = O.slepc_solver(H, 6)
+    kk, cs, vs = O.basis(len(kpt), p.nc, p.nv)
+    dE = np.sort(eigv[kk, cs] - eigv[kk, vs])[:6]
+    np.testing.assert_allclose(E, dE, atol=1e-12)
+
+
+def test_hermitian_and_matrix_free_equal_dense(small):
+    sysm, p, kpt, eigv, vec, _ = small
+    H = O.bse_build(eigv, vec, kpt, p, sysm.rlat)
+    assert np.abs(H - H.conj().T).max() == 0.0
+    x = np.random.default_rng(3).normal(size=(p.dim, 4)) + 1j
+    np.testing.assert_allclose(O.bse_matvec_factored(x, eigv, vec, kpt, p, sysm.rlat), H @ x, atol=1e-12)
+
+
+def test_phase_gauge_changes_oscillators_not_energies(small):
+    """Per-(k, band) phases leave the exciton energies unchanged but change |sum_j A_j h_j|^2
+    (no conjugate on A in dielbsev); a sign flip leaves both unchanged."""
+    sysm, p, kpt, eigv, vec, _ = small
+    rng = np.random.default_rng(9)
+    ph = np.exp(1j * rng.uniform(0, 2 * np.pi, vec.shape[:2]))
+    vec2 = vec * ph[..., None]
+    sgn = np.where(rng.uniform(size=vec.shape[:2]) < 0.5, -1.0, 1.0)
+    vec3 = vec * sgn[..., None]
+    res = []
+    for v in (vec, vec2, vec3):
+        H = O.bse_build(eigv, v, kpt, p, sysm.rlat)
+        E, A = O.slepc_solver(H, 3)
+        h = O.optsp_all(eigv, v, kpt, sysm, p)[0]
+        res.append((E, O.dielbsev(A, h, p.dim)[:3]))
+    np.testing.assert_allclose(res[1][0], res[0][0], atol=1e-12)
+    np.testing.assert_allclose(res[2][0], res[0][0], atol=1e-12)
+    np.testing.assert_allclose(res[2][1], res[0][1], rtol=1e-9, atol=1e-14)
+    assert np.max(np.abs(res[1][1] - res[0][1])) > 1e-6 * np.max(res[0][1])
+
+
+def test_optsp_real_part_scaling(small):
+    """optsp assigns 1./esp to a real: h = <c|dH|v> * Re(1/(dE + i*CSHIFT_f32))."""
+    sysm, p, kpt, eigv, vec, _ = small
+    hx = O.optsp_all(eigv, vec, kpt, sysm, p)[0]
+    dx, _, _ = O.hlm(kpt[0], sysm)
+    c, v = vec[0, p.nv], vec[0, 0]
+    de = eigv[0, p.nv] - eigv[0, 0]
+    s = float(np.float32(p.cshift))
+    np.testing.assert_allclose(hx[0], (np.conj(c) @ dx @ v) * de / (de * de + s * s), rtol=1e-13)
+
+
+def test_lorentzian_sum_rule():
+    """Integral of eps2 over the window equals C * sum_n f_n [atan((b-E_n)/g) - atan((a-E_n)/g)], with the
+    width g = CSHIFT + avgsme (renormalisation off)."""
+    p = S.BSEParams(ngrid=(4, 4, 1), nc=1, nv=1, numbse=40001, ebse0=-20.0, ebsef=25.0, cshift=0.05, renorm=False)
+    rlat = S.hex_lattice()
+    Ws = np.array([1.5, 2.0, 2.5])
+    f = np.array([1.0, 0.5, 0.25])
+    acts = {c: f for c in O.COMPONENTS}
+    d = O.bsedielraw(Ws, acts, p.ngrid, rlat, p)["xx"]
+    C = O.GAMA / (16 * O.vcell3D(rlat))
+    g = p.cshift + O.avgsme(Ws)
+    assert abs(g - (0.05 + 10.0 * 1.0 / 3.0)) < 1e-14
+    expect = C * np.sum(f * (np.arctan((p.ebsef - Ws) / g) - np.arctan((p.ebse0 - Ws) / g)))
+    integral = np.trapezoid(d[:, 2], d[:, 0])
+    assert abs(integral - expect) / expect < 1e-6
+
+
+def test_zero_tail_narrows_the_width():
+    """Rows past nev hold E = 0 (quirk of the file handoff): avgsme telescopes to -10 E_1 / dim."""
+    Ws = np.zeros(1000)
+    Ws[:3] = [1.5, 2.0, 2.5]
+    assert abs(O.avgsme(Ws) - (-10.0 * 1.5 / 1000)) < 1e-15
+
+
+def test_imagrenorm_baseline():
+    d = np.zeros((10, 3))
+    d[:, 0] = np.linspace(0, 0.9, 10)
+    d[:, 2] = np.linspace(1.0, 2.0, 10)
+    O.imagrenorm(0.56, d)          # E1 - 0.15_f32 = 0.41 -> last omega below is index 4 (omega = 0.4)
+    assert np.all(d[:5, 2] == 0.0)
+    np.testing.assert_allclose(d[5:, 2], np.linspace(1.0, 2.0, 10)[5:] - np.linspace(1.0, 2.0, 10)[5])
+    d2 = np.ones((5, 3))
+    O.imagrenorm(0.1, d2)          # E1 - 0.15 <= 0: untouched
+    assert np.all(d2 == 1.0)
+
+
+@pytest.mark.parametrize("name", ["hex8_6x6", "hex8_24x24"])
+def test_golden_fixtures(name):
+    from tests.golden.make_golden import input_digest
+
+    g = np.load(os.path.join(HERE, "golden", name + ".npz"))
+    sysm, p = S.workload(name)
+    assert str(g["digest"]) == input_digest(sysm), "the seeded input generator changed"
+    r = O.bsesolver(sysm, p)
+    np.testing.assert_allclose(r["E"], g["E"], atol=1e-11)
+    np.testing.assert_allclose(r["eigv"], g["eigv"], atol=1e-12)
+    spec = O.bsedielraw(r["Ws"], r["acts"], p.ngrid, sysm.rlat, p)
+    for c in ("xx", "yy", "zz"):
+        np.testing.assert_allclose(spec[c], g["spec_" + c], rtol=1e-8, atol=1e-10)
+
+
+def test_c_restatement_matches_numpy(built, small):
+    """The element-by-element C loop (the timed CPU baseline) equals the vectorised oracle."""
+    import __graft_entry__ as g
+
+    sysm, p, kpt, eigv, vec, _ = small
+    lib = ctypes.CDLL(g.ORACLE_SO)
+
+    class Coul(ctypes.Structure):
+        _fields_ = [("coultype", ctypes.c_int), ("ngrid", ctypes.c_int * 3), ("ktol", ctypes.c_double),
+                    ("ediel", ctypes.c_double * 3), ("ez", ctypes.c_double), ("w", ctypes.c_double),
+                    ("r0", ctypes.c_double), ("lc", ctypes.c_double), ("rlat", ctypes.c_double * 9)]
+
+    cp = Coul()
+    cp.coultype = 6
+    for i in range(3):
+        cp.ngrid[i] = p.ngrid[i]
+        cp.ediel[i] = p.ediel[i]
+    cp.ktol, cp.ez, cp.w, cp.r0, cp.lc = p.ktol, p.ez, p.w_coul, p.r0, p.lc
+    for i in range(9):
+        cp.rlat[i] = sysm.rlat.reshape(-1)[i]
+    dim = p.dim
+    out = np.zeros((dim, dim), dtype=np.complex128)
+    e, v, k = np.ascontiguousarray(eigv), np.ascontiguousarray(vec), np.ascontiguousarray(kpt)
+    lib.oracle_build_rows(len(kpt), p.nc, p.nv, sysm.w90basis, e.ctypes.data_as(ctypes.c_void_p),
+                          v.ctypes.data_as(ctypes.c_void_p), k.ctypes.data_as(ctypes.c_void_p), ctypes.byref(cp),
+                          ctypes.c_long(0), ctypes.c_long(dim), out.ctypes.data_as(ctypes.c_void_p))
+    H = O.bse_build(eigv, vec, kpt, p, sysm.rlat)
+    iu = np.triu_indices(dim)
+    np.testing.assert_allclose(out[iu], H[iu], rtol=0, atol=1e-14)

@@ -1,0 +1,307 @@
+"""Python mirror of the WTB exciton-path interface over the C ABI of libwtb_gb300.so.
+
+The names and argument meanings follow the Fortran subroutines the library replaces
+(``eigsys``, ``monhkhorst_pack``, ``bsesolver``, ``slepc_solver``, ``dielbsev``/``dielbsep``,
+``bsedielraw``, ``bseoptprop`` and the ``module_coulomb`` potentials); arrays cross the boundary in
+Fortran column-major order exactly as the Fortran caller would pass them.  There is no CPU
+fallback: if the shared library is missing, importing this module raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from .synthetic import BSEParams, TBSystem
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libwtb_gb300.so")
+
+WTB_OK, WTB_EBADARG, WTB_ENOMEM, WTB_ENOCONV, WTB_ETIMEOUT, WTB_ENAN, WTB_ECUDA, WTB_ESTATE, WTB_ENODEV = range(9)
+STATUS_NAMES = {0: "WTB_OK", 1: "WTB_EBADARG", 2: "WTB_ENOMEM", 3: "WTB_ENOCONV", 4: "WTB_ETIMEOUT",
+                5: "WTB_ENAN", 6: "WTB_ECUDA", 7: "WTB_ESTATE", 8: "WTB_ENODEV"}
+PREC = {"fp64": 0, "fp32": 1, "bf16x3": 2, "bf16x6": 3}
+OPS = {"dense": 0, "matfree": 1}
+COULTYPES = {"V2DK": 0, "V3D": 1, "V3DL": 2, "V2DT": 3, "V2DT2": 4, "V2DOH": 5, "V2DRK": 6, "V1DT": 7, "V0DT": 8}
+COMPONENTS = ("xx", "yy", "zz", "xy", "xz", "yz", "sp", "sm")
+
+
+class WTBError(RuntimeError):
+    """A non-zero status from the library; ``code`` is the WTB_* status, the text is the reference's."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {message}")
+        self.code = code
+
+
+class CParams(C.Structure):
+    _fields_ = [("ngrid", C.c_int * 3), ("nc", C.c_int), ("nv", C.c_int), ("mshift", C.c_double * 3),
+                ("coultype", C.c_int), ("renorm", C.c_int), ("ktol", C.c_double), ("ediel", C.c_double * 3),
+                ("ez", C.c_double), ("w_coul", C.c_double), ("r0", C.c_double), ("lc", C.c_double),
+                ("cshift", C.c_double), ("ebse0", C.c_double), ("ebsef", C.c_double), ("numbse", C.c_int),
+                ("nev", C.c_int), ("precision", C.c_int), ("op", C.c_int), ("tol", C.c_double),
+                ("maxit", C.c_int), ("block", C.c_int)]
+
+
+class CTimings(C.Structure):
+    _fields_ = [("t_bands_ms", C.c_double), ("t_build_ms", C.c_double), ("t_solve_ms", C.c_double),
+                ("t_optics_ms", C.c_double), ("t_total_ms", C.c_double), ("iterations", C.c_int),
+                ("matvec_columns", C.c_int), ("max_rel_residual", C.c_double), ("refine_shift_max", C.c_double),
+                ("kernel_launches", C.c_int)]
+
+
+def _load():
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with __graft_entry__.build(); there is no CPU fallback")
+    lib = C.CDLL(LIB_PATH)
+    P = C.c_void_p
+    dp = C.POINTER(C.c_double)
+    ip = C.POINTER(C.c_int)
+    sigs = {
+        "wtb_ctx_create": [C.POINTER(P), C.c_int],
+        "wtb_ctx_destroy": [P],
+        "wtb_set_hr": [P, C.c_int, C.c_int, ip, ip, dp, dp, dp, C.c_double, C.c_double, C.c_int],
+        "wtb_eigsys": [C.c_int, C.c_double, C.c_double, ip, ip, C.c_double, C.c_double, C.c_double, C.c_int,
+                       C.c_int, dp, ip, dp, dp, C.c_double, dp, dp],
+        "wtb_monhkhorst_pack": [C.c_int, C.c_int, C.c_int, dp, dp, dp, dp, dp],
+        "wtb_eigsys_mesh": [P, C.c_int, dp, C.c_int, C.c_int, dp, dp, ip],
+        "wtb_coulomb_table": [P, C.POINTER(CParams), C.c_int, dp, C.c_int, dp, dp],
+        "wtb_optsp": [P, C.POINTER(CParams), dp],
+        "wtb_bse_build": [P, C.POINTER(CParams), dp],
+        "wtb_bse_matvec": [P, C.POINTER(CParams), C.c_int, dp, dp],
+        "wtb_slepc_solver": [P, dp, dp, dp, C.c_int, C.c_int],
+        "wtb_dielbse": [P, C.c_int, C.c_int, dp, dp, dp, C.c_int, dp],
+        "wtb_bsesolver": [P, C.POINTER(CParams), dp, dp, dp, C.POINTER(CTimings)],
+        "wtb_bsedielraw": [P, C.POINTER(CParams), C.c_int, dp, dp, dp],
+        "wtb_bseoptprop": [P, C.c_int, dp, dp],
+    }
+    for name, args in sigs.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    lib.wtb_last_error.argtypes = [P]
+    lib.wtb_last_error.restype = C.c_char_p
+    lib.wtb_version.restype = C.c_int
+    lib.wtb_kernel_launch_count.restype = C.c_longlong
+    lib.wtb_ctx_stream.argtypes = [P]
+    lib.wtb_ctx_stream.restype = C.c_void_p
+    lib.wtb_profile_enable.argtypes = [P, C.c_int]
+    lib.wtb_profile_enable.restype = C.c_int
+    lib.wtb_profile_read.argtypes = [P, dp, C.POINTER(C.c_longlong), dp, dp]
+    lib.wtb_profile_read.restype = C.c_int
+    return lib
+
+
+_lib = _load()
+
+
+def lib():
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int)) if a is not None else None
+
+
+def _f64(a):
+    return np.asfortranarray(np.asarray(a, dtype=np.float64))
+
+
+def _c128(a):
+    return np.asfortranarray(np.asarray(a, dtype=np.complex128))
+
+
+def cparams(p: BSEParams, precision="fp64", op="dense", tol=0.0, maxit=0, block=0) -> CParams:
+    c = CParams()
+    for i in range(3):
+        c.ngrid[i] = int(p.ngrid[i])
+        c.mshift[i] = float(p.mshift[i])
+        c.ediel[i] = float(p.ediel[i])
+    c.nc, c.nv = int(p.nc), int(p.nv)
+    c.coultype = COULTYPES[p.coultype] if isinstance(p.coultype, str) else int(p.coultype)
+    c.renorm = 1 if p.renorm else 0
+    c.ktol, c.ez, c.w_coul, c.r0, c.lc = float(p.ktol), float(p.ez), float(p.w_coul), float(p.r0), float(p.lc)
+    c.cshift, c.ebse0, c.ebsef = float(p.cshift), float(p.ebse0), float(p.ebsef)
+    c.numbse, c.nev = int(p.numbse), int(p.nev)
+    c.precision = PREC[precision] if isinstance(precision, str) else int(precision)
+    c.op = OPS[op] if isinstance(op, str) else int(op)
+    c.tol, c.maxit, c.block = float(tol), int(maxit), int(block)
+    return c
+
+
+def kernel_launch_count() -> int:
+    return int(_lib.wtb_kernel_launch_count())
+
+
+def monhkhorst_pack(n1, n2, n3, shift, rlat1, rlat2, rlat3):
+    """monhkhorst_pack (src/module_kmesh.F90:338-386): returns kpt (n1*n2*n3, 3)."""
+    kpt = np.zeros((n1 * n2 * n3, 3), order="F")
+    r = _lib.wtb_monhkhorst_pack(n1, n2, n3, _dp(_f64(shift)), _dp(_f64(rlat1)), _dp(_f64(rlat2)),
+                                 _dp(_f64(rlat3)), _dp(kpt))
+    if r:
+        raise WTBError(r, "monhkhorst_pack: bad arguments")
+    return np.ascontiguousarray(kpt)
+
+
+def eigsys(nthreads, scs, exc, nocp, ffactor, kx, ky, kz, w90basis, nvec, rlat, rvec, hopmatrices, ihopmatrices,
+           efermi):
+    """eigsys (src/module_hamiltonian.F90:200-320), same argument list; H(R) arrays with the reference's
+    shapes: rvec (nvec,3), hopmatrices (nvec,w,w).  Returns (nocp, energias (w,), autovetores (w,w))."""
+    n = C.c_int(int(nocp))
+    en = np.zeros(w90basis)
+    av = np.zeros((w90basis, w90basis), dtype=np.complex128, order="F")
+    ff = np.asfortranarray(np.asarray(ffactor, dtype=np.int32))
+    rv = np.asfortranarray(np.asarray(rvec, dtype=np.int32))
+    r = _lib.wtb_eigsys(int(nthreads), float(scs), float(exc), C.byref(n), _ip(ff), float(kx), float(ky), float(kz),
+                        int(w90basis), int(nvec), _dp(_f64(rlat)), _ip(rv), _dp(_f64(hopmatrices)),
+                        _dp(_f64(ihopmatrices)), float(efermi), _dp(en), _dp(av))
+    if r:
+        raise WTBError(r, "eigsys failed")
+    return n.value, en, av
+
+
+class Context:
+    """One device context (``wtb_ctx``); owns device buffers and the stream."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        r = _lib.wtb_ctx_create(C.byref(h), int(device))
+        if r:
+            raise WTBError(r, "no usable CUDA device")
+        self._h = h
+        self.system: TBSystem | None = None
+
+    def close(self):
+        if self._h:
+            _lib.wtb_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, r, what):
+        if r:
+            msg = _lib.wtb_last_error(self._h)
+            raise WTBError(r, f"{what}: {msg.decode() if msg else ''}")
+
+    # -------------------------------------------------------------------- module_hamiltonian globals
+    def set_hr(self, s: TBSystem):
+        rv = np.asfortranarray(s.rvec.astype(np.int32))
+        ff = np.asfortranarray(s.ffactor.astype(np.int32))
+        self._chk(_lib.wtb_set_hr(self._h, int(s.w90basis), int(s.nvec), _ip(rv), _ip(ff), _dp(_f64(s.hop)),
+                                  _dp(_f64(s.ihop)), _dp(_f64(s.rlat)), float(s.efermi), float(s.scs),
+                                  1 if s.systype == "NP" else 0), "wtb_set_hr")
+        self.system = s
+
+    def eigsys_mesh(self, kpt, nv, nc):
+        """Band loop of bsesolver: returns eigv (nk, nv+nc), vector (nk, nv+nc, w), nocpk (nk,)."""
+        kpt = np.asarray(kpt, dtype=np.float64)
+        nk = kpt.shape[0]
+        w = self.system.w90basis
+        eigv = np.zeros((nk, nv + nc), order="F")
+        vec = np.zeros((nk, nv + nc, w), dtype=np.complex128, order="F")
+        nocp = np.zeros(nk, dtype=np.int32)
+        self._chk(_lib.wtb_eigsys_mesh(self._h, nk, _dp(_f64(kpt)), int(nv), int(nc), _dp(eigv), _dp(vec), _ip(nocp)),
+                  "wtb_eigsys_mesh")
+        return np.ascontiguousarray(eigv), np.ascontiguousarray(vec), nocp
+
+    def coulomb_table(self, p: BSEParams, kpt1, kpt2=None):
+        kpt1 = np.asarray(kpt1, dtype=np.float64)
+        kpt2 = kpt1 if kpt2 is None else np.asarray(kpt2, dtype=np.float64)
+        V = np.zeros((len(kpt1), len(kpt2)), order="F")
+        cp = cparams(p)
+        self._chk(_lib.wtb_coulomb_table(self._h, C.byref(cp), len(kpt1), _dp(_f64(kpt1)), len(kpt2),
+                                         _dp(_f64(kpt2)), _dp(V)), "wtb_coulomb_table")
+        return np.ascontiguousarray(V)
+
+    def optsp(self, p: BSEParams):
+        dim = p.dim
+        hr = np.zeros((dim, 5), dtype=np.complex128, order="F")
+        cp = cparams(p)
+        self._chk(_lib.wtb_optsp(self._h, C.byref(cp), _dp(hr)), "wtb_optsp")
+        return hr.T.copy()
+
+    def bse_build(self, p: BSEParams, precision="fp64"):
+        dim = p.dim
+        H = np.zeros((dim, dim), dtype=np.complex128, order="F")
+        cp = cparams(p, precision=precision)
+        self._chk(_lib.wtb_bse_build(self._h, C.byref(cp), _dp(H)), "wtb_bse_build")
+        return H
+
+    def bse_matvec(self, p: BSEParams, X, precision="fp64", op="matfree"):
+        """Y = H X for the bands of the last set-up (X: dim x ncol complex)."""
+        X = _c128(X)
+        if X.ndim == 1:
+            X = X.reshape(-1, 1, order="F")
+        Y = np.zeros_like(X, order="F")
+        cp = cparams(p, precision=precision, op=op)
+        self._chk(_lib.wtb_bse_matvec(self._h, C.byref(cp), X.shape[1], _dp(X), _dp(Y)), "wtb_bse_matvec")
+        return Y
+
+    def slepc_solver(self, HX, NE):
+        HX = _c128(HX)
+        NX = HX.shape[0]
+        EX = np.zeros(NE)
+        HE = np.zeros((NX, NE), dtype=np.complex128, order="F")
+        self._chk(_lib.wtb_slepc_solver(self._h, _dp(HX), _dp(EX), _dp(HE), NX, NE), "wtb_slepc_solver")
+        return EX, HE
+
+    def dielbse(self, dimse, dimse1, excitonvec, hopt1, hopt2=None):
+        A = _c128(excitonvec)[:, :dimse1]
+        A = np.asfortranarray(A)
+        h1 = _c128(hopt1)
+        h2 = _c128(hopt2) if hopt2 is not None else None
+        act = np.zeros(dimse)
+        self._chk(_lib.wtb_dielbse(self._h, dimse, dimse1, _dp(A), _dp(h1), _dp(h2), 1 if h2 is not None else 0,
+                                   _dp(act)), "wtb_dielbse")
+        return act
+
+    def bsesolver(self, p: BSEParams, precision="fp64", op="dense", tol=0.0, maxit=0, block=0,
+                  want_vectors=False):
+        """The bsesolver path; returns dict with Ws (dim,), acts {comp: (dim,)}, E (nev,), timings, HE."""
+        dim = p.dim
+        Ws = np.zeros(dim)
+        acts = np.zeros((dim, 8), order="F")
+        HE = np.zeros((dim, p.nev), dtype=np.complex128, order="F") if want_vectors else None
+        t = CTimings()
+        cp = cparams(p, precision=precision, op=op, tol=tol, maxit=maxit, block=block)
+        self._chk(_lib.wtb_bsesolver(self._h, C.byref(cp), _dp(Ws), _dp(acts), _dp(HE), C.byref(t)),
+                  "wtb_bsesolver")
+        out = {"Ws": Ws, "E": Ws[: p.nev].copy(), "acts": {c: acts[:, i].copy() for i, c in enumerate(COMPONENTS)},
+               "timings": {f: getattr(t, f) for f, _ in CTimings._fields_}}
+        if want_vectors:
+            out["HE"] = HE
+        return out
+
+    def bsedielraw(self, p: BSEParams, Ws, acts):
+        """Returns dict comp -> (numbse, 3) [omega, eps1, eps2] for xx yy zz xy xz yz."""
+        Ws = np.asarray(Ws, dtype=np.float64)
+        dimse = len(Ws)
+        A = np.zeros((dimse, 6), order="F")
+        for i, cname in enumerate(COMPONENTS[:6]):
+            A[:, i] = acts[cname]
+        dielf = np.zeros((p.numbse, 3, 6), order="F")
+        cp = cparams(p)
+        self._chk(_lib.wtb_bsedielraw(self._h, C.byref(cp), dimse, _dp(_f64(Ws)), _dp(A), _dp(dielf)),
+                  "wtb_bsedielraw")
+        return {cname: dielf[:, :, i].copy() for i, cname in enumerate(COMPONENTS[:6])}
+
+    def bseoptprop(self, dielf: dict):
+        n = next(iter(dielf.values())).shape[0]
+        D = np.zeros((n, 3, 6), order="F")
+        for i, cname in enumerate(COMPONENTS[:6]):
+            D[:, :, i] = dielf[cname]
+        props = np.zeros((n, 6, 5), order="F")
+        self._chk(_lib.wtb_bseoptprop(self._h, n, _dp(D), _dp(props)), "wtb_bseoptprop")
+        names = ("refr", "ext", "refl", "abs", "eloss")
+        return {nm: {cname: props[:, i, q].copy() for i, cname in enumerate(COMPONENTS[:6])}
+                for q, nm in enumerate(names)}

@@ -1,0 +1,530 @@
+// Wannier Fourier sum H(k) = sum_R e^{ik.R} H(R)/ndegen - E_F I, Hermitian eigensolve, gauge fix and
+// band window, one CTA per k-point; plus the velocity matrix elements of optsp/hlm and the V(k,k')
+// table.  Follows eigsys (src/module_hamiltonian.F90:200-320), the bsesolver band loop
+// (src/module_bse.F90:2230-2245), hlm/optsp (src/module_optics.F90:12-167) and module_coulomb.
+//
+// Eigensolver: cyclic two-sided Jacobi for complex Hermitian matrices with the round-robin (circle)
+// pair ordering, so the n/2 rotations of a step touch disjoint rows/columns and are applied by all
+// threads at once.  The matrix and the accumulated rotations live in shared memory (w <= 64).
+// Gauge: every eigenvector is rotated so its first component is real and >= 0, the gauge ZHEEV('L')
+// produces up to a sign (the Householder reflectors of ZHETRD('L') leave e1 invariant).
+#include "wtb_internal.h"
+
+namespace wtb {
+
+namespace {
+
+constexpr int kHkThreads = 128;
+
+__device__ __forceinline__ double cabs2(zd a) { return a.re * a.re + a.im * a.im; }
+
+// Cartesian component a of R = r1 a1 + r2 a2 + r3 a3, evaluated as separately rounded products and
+// sums (no fused multiply-add) so that the single-precision rounding below sees the same double as the
+// reference's expression rvec(i,1)*rlat(1,a)+rvec(i,2)*rlat(2,a)+rvec(i,3)*rlat(3,a).
+__device__ __forceinline__ double rcart(int r1, int r2, int r3, const double* rl, int a) {
+  return __dadd_rn(__dadd_rn(__dmul_rn((double)r1, rl[a]), __dmul_rn((double)r2, rl[3 + a])),
+                   __dmul_rn((double)r3, rl[6 + a]));
+}
+
+// phi_R = kx*Rx + ky*Ry + kz*Rz rounded to single precision (cmplx(0.0, ...) in the reference,
+// src/module_hamiltonian.F90:240-244); unfused so the float rounding is reproducible.
+__device__ __forceinline__ double phase_f32(const int* rvec, int nR, int iR, const double* rl, double kx, double ky,
+                                            double kz) {
+  const int r1 = rvec[iR], r2 = rvec[nR + iR], r3 = rvec[2 * nR + iR];
+  const double phi = __dadd_rn(__dadd_rn(__dmul_rn(kx, rcart(r1, r2, r3, rl, 0)), __dmul_rn(ky, rcart(r1, r2, r3, rl, 1))),
+                               __dmul_rn(kz, rcart(r1, r2, r3, rl, 2)));
+  return (double)__double2float_rn(phi);
+}
+
+__device__ __forceinline__ double rcomp_f32(const int* rvec, int nR, int iR, const double* rl, int a) {
+  const int r1 = rvec[iR], r2 = rvec[nR + iR], r3 = rvec[2 * nR + iR];
+  return (double)__double2float_rn(rcart(r1, r2, r3, rl, a));
+}
+
+// Round-robin partner table: position i of step t.
+__device__ __forceinline__ int rr_player(int i, int t, int n) { return i == 0 ? 0 : ((i - 1 + t) % (n - 1)) + 1; }
+
+// Jacobi eigen-decomposition of the n x n (n even) Hermitian matrix A (shared, ld = n); V receives the
+// eigenvectors as columns.  All threads of the block participate.
+__device__ void jacobi_shared(zd* A, zd* V, int n, int nreal, double* rc, double* rs, zd* rph, int* rp, int* rq,
+                              int* flag, double* red) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < n * n; e += nt) V[e] = mk<double>((e / n) == (e % n) ? 1.0 : 0.0, 0.0);
+  __syncthreads();
+  const int half = n / 2;
+  for (int sweep = 0; sweep < 40; ++sweep) {
+    // convergence test: off-diagonal Frobenius norm against the diagonal
+    if (tid == 0) {
+      red[0] = 0.0;
+      red[1] = 0.0;
+    }
+    __syncthreads();
+    double off = 0.0, dia = 0.0;
+    for (int e = tid; e < n * n; e += nt) {
+      const int r = e / n, c = e % n;
+      if (r == c)
+        dia += A[e].re * A[e].re;
+      else
+        off += cabs2(A[e]);
+    }
+    atomicAdd(&red[0], off);
+    atomicAdd(&red[1], dia);
+    __syncthreads();
+    const double offn = red[0], dian = red[1];
+    __syncthreads();
+    if (offn <= 1e-32 * dian || offn == 0.0) break;
+    for (int t = 0; t < n - 1; ++t) {
+      if (tid < half) {
+        int p = rr_player(tid, t, n), q = rr_player(n - 1 - tid, t, n);
+        if (p > q) {
+          int tmp = p;
+          p = q;
+          q = tmp;
+        }
+        const zd apq = A[p * n + q];
+        const double app = A[p * n + p].re, aqq = A[q * n + q].re;
+        const double b = sqrt(cabs2(apq));
+        double c = 1.0, s = 0.0;
+        zd ph = mk<double>(1.0, 0.0);
+        int act = 0;
+        if (b > 1e-300 && b > 1e-18 * (fabs(app) + fabs(aqq))) {
+          ph = mk<double>(apq.re / b, apq.im / b);
+          const double zeta = (aqq - app) / (2.0 * b);
+          double tt;
+          if (fabs(zeta) > 1e150)
+            tt = 0.5 / zeta;
+          else
+            tt = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+          c = 1.0 / sqrt(1.0 + tt * tt);
+          s = tt * c;
+          act = 1;
+        }
+        rc[tid] = c;
+        rs[tid] = s;
+        rph[tid] = ph;
+        rp[tid] = p;
+        rq[tid] = q;
+        flag[tid] = act;
+      }
+      __syncthreads();
+      // rows: A_p. <- c A_p. - s e^{i phi} A_q. ; A_q. <- s A_p. + c e^{i phi} A_q.
+      for (int e = tid; e < half * n; e += nt) {
+        const int j = e / n, col = e % n;
+        if (!flag[j]) continue;
+        const int p = rp[j], q = rq[j];
+        const double c = rc[j], s = rs[j];
+        const zd ph = rph[j];
+        const zd ap = A[p * n + col], aq = A[q * n + col];
+        const zd phq = cmul(ph, aq);
+        A[p * n + col] = mk<double>(c * ap.re - s * phq.re, c * ap.im - s * phq.im);
+        A[q * n + col] = mk<double>(s * ap.re + c * phq.re, s * ap.im + c * phq.im);
+      }
+      __syncthreads();
+      // columns of A and V: A_.p <- c A_.p - s e^{-i phi} A_.q ; A_.q <- s A_.p + c e^{-i phi} A_.q
+      for (int e = tid; e < half * n * 2; e += nt) {
+        const int which = e / (half * n);
+        const int ee = e % (half * n);
+        const int j = ee / n, row = ee % n;
+        if (!flag[j]) continue;
+        zd* M = which ? V : A;
+        const int p = rp[j], q = rq[j];
+        const double c = rc[j], s = rs[j];
+        const zd phc = mk<double>(rph[j].re, -rph[j].im);
+        const zd ap = M[row * n + p], aq = M[row * n + q];
+        const zd phq = cmul(phc, aq);
+        M[row * n + p] = mk<double>(c * ap.re - s * phq.re, c * ap.im - s * phq.im);
+        M[row * n + q] = mk<double>(s * ap.re + c * phq.re, s * ap.im + c * phq.im);
+      }
+      __syncthreads();
+      if (tid < half && flag[tid]) {
+        const int p = rp[tid], q = rq[tid];
+        A[p * n + q] = mk<double>(0.0, 0.0);
+        A[q * n + p] = mk<double>(0.0, 0.0);
+        A[p * n + p].im = 0.0;
+        A[q * n + q].im = 0.0;
+      }
+      __syncthreads();
+    }
+  }
+  (void)nreal;
+}
+
+__global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict__ hr, const int* __restrict__ rvec,
+                                                            const int* __restrict__ ndegen, int nR, int w,
+                                                            const double* __restrict__ rlat, double efermi, double scs,
+                                                            const double* __restrict__ kpt, int nk, int nv, int nc,
+                                                            double* eig_all, zd* vec_all, double* eig_win,
+                                                            zd* vec_win, int* nocp_out, DevStatus* st) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int k = blockIdx.x;
+  if (k >= nk) return;
+  const int n = (w + 1) & ~1;
+  zd* A = reinterpret_cast<zd*>(smem_raw);
+  zd* V = A + n * n;
+  zd* eph = V + n * n;  // nR phases
+  double* rc = reinterpret_cast<double*>(eph + nR);
+  double* rs = rc + 32;
+  zd* rph = reinterpret_cast<zd*>(rs + 32);
+  double* red = reinterpret_cast<double*>(rph + 32);
+  double* ev = red + 4;  // n eigenvalues
+  int* rp = reinterpret_cast<int*>(ev + 64);
+  int* rq = rp + 32;
+  int* flag = rq + 32;
+  int* rank = flag + 32;  // n
+  __shared__ double rl[9];
+  __shared__ int s_nocp;
+  const int tid = threadIdx.x;
+  if (tid < 9) rl[tid] = rlat[tid];
+  __syncthreads();
+  const double kx = kpt[3 * k], ky = kpt[3 * k + 1], kz = kpt[3 * k + 2];
+  for (int r = tid; r < nR; r += blockDim.x) {
+    const double phi = phase_f32(rvec, nR, r, rl, kx, ky, kz);
+    double sn, cs;
+    sincos(phi, &sn, &cs);
+    const double inv = 1.0 / (double)ndegen[r];
+    eph[r] = mk<double>(cs * inv, sn * inv);
+  }
+  __syncthreads();
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    const int m = e / n, c = e % n;
+    zd acc = mk<double>(0.0, 0.0);
+    if (m < w && c < w) {
+      for (int r = 0; r < nR; ++r) cfma(acc, eph[r], hr[((size_t)r * w + m) * w + c]);
+      if (m == c) acc.re -= efermi;
+    }
+    A[e] = acc;
+  }
+  __syncthreads();
+  // Hermitian by construction up to rounding: symmetrise so the rotations see an exact Hermitian matrix
+  for (int e = tid; e < n * n; e += blockDim.x) {
+    const int m = e / n, c = e % n;
+    if (m < c) {
+      const zd a = A[m * n + c], b = A[c * n + m];
+      const zd h = mk<double>(0.5 * (a.re + b.re), 0.5 * (a.im - b.im));
+      A[m * n + c] = h;
+      A[c * n + m] = mk<double>(h.re, -h.im);
+    } else if (m == c) {
+      A[e].im = 0.0;
+    }
+  }
+  __syncthreads();
+  jacobi_shared(A, V, n, w, rc, rs, rph, rp, rq, flag, red);
+  // ascending order of the w real eigenvalues (the padding index w, if any, is excluded)
+  if (tid < w) ev[tid] = A[tid * n + tid].re;
+  __syncthreads();
+  if (tid < w) {
+    int r = 0;
+    const double x = ev[tid];
+    for (int j = 0; j < w; ++j) r += (ev[j] < x) || (ev[j] == x && j < tid);
+    rank[tid] = r;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    int cnt = 0;
+    for (int j = 0; j < w; ++j) cnt += (ev[j] <= 0.0);
+    s_nocp = cnt;  // = index of the first E > 0 in ascending order
+  }
+  __syncthreads();
+  const int nocp = s_nocp;
+  // outputs: eigenvalue j goes to position rank[j]; eigenvector = column j of V, gauge fixed
+  for (int e = tid; e < w * w; e += blockDim.x) {
+    const int j = e / w, o = e % w;
+    const zd a0 = V[0 * n + j];
+    const double m0 = sqrt(cabs2(a0));
+    zd g = mk<double>(1.0, 0.0);
+    if (m0 > 0.0) g = mk<double>(a0.re / m0, -a0.im / m0);
+    zd val = cmul(V[o * n + j], g);
+    if (o == 0) val = mk<double>(m0, 0.0);
+    const int r = rank[j];
+    if (vec_all) vec_all[((size_t)k * w + r) * w + o] = val;
+    const int s = r - (nocp - nv);
+    if (vec_win && s >= 0 && s < nv + nc) vec_win[((size_t)k * (nv + nc) + s) * w + o] = val;
+  }
+  if (tid < w) {
+    const int r = rank[tid];
+    const double e = ev[tid] + (r >= nocp ? scs : 0.0);
+    if (eig_all) eig_all[(size_t)k * w + r] = e;
+    const int s = r - (nocp - nv);
+    if (eig_win && s >= 0 && s < nv + nc) eig_win[(size_t)k * (nv + nc) + s] = e;
+  }
+  if (tid == 0) {
+    if (nocp_out) nocp_out[k] = nocp;
+    if (eig_win) {
+      if (nv > nocp) dev_fail(st, 101, k);            // valence window below the occupied states
+      else if (nc > w - nocp) dev_fail(st, 102, k);   // conduction window above the empty states
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------- optics (hlm + optsp)
+__global__ void __launch_bounds__(kHkThreads) optics_kernel(const zd* __restrict__ hr, const int* __restrict__ rvec,
+                                                            const int* __restrict__ ndegen, int nR, int w,
+                                                            const double* __restrict__ rlat,
+                                                            const double* __restrict__ kpt, int nk, int nv, int nc,
+                                                            const double* __restrict__ eig_win,
+                                                            const zd* __restrict__ vec_win, float s32,
+                                                            zd* __restrict__ hout) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int k = blockIdx.x;
+  if (k >= nk) return;
+  const int tid = threadIdx.x;
+  const int nb = nv + nc;
+  zd* M = reinterpret_cast<zd*>(smem_raw);   // w*w
+  zd* B = M + w * w;                         // nb*w band vectors
+  zd* Mv = B + nb * w;                       // nv*w
+  zd* eph = Mv + nv * w;                     // nR
+  double* Ra = reinterpret_cast<double*>(eph + nR);  // nR
+  __shared__ double rl[9];
+  if (tid < 9) rl[tid] = rlat[tid];
+  for (int e = tid; e < nb * w; e += blockDim.x) B[e] = vec_win[(size_t)k * nb * w + e];
+  __syncthreads();
+  const double kx = kpt[3 * k], ky = kpt[3 * k + 1], kz = kpt[3 * k + 2];
+  for (int r = tid; r < nR; r += blockDim.x) {
+    const double phi = phase_f32(rvec, nR, r, rl, kx, ky, kz);
+    double sn, cs;
+    sincos(phi, &sn, &cs);
+    const double inv = 1.0 / (double)ndegen[r];
+    eph[r] = mk<double>(cs * inv, sn * inv);
+  }
+  const int dimk = nc * nv;
+  const size_t dim = (size_t)nk * dimk;
+  zd hxyz[3][1];
+  (void)hxyz;
+  for (int a = 0; a < 3; ++a) {
+    __syncthreads();
+    for (int r = tid; r < nR; r += blockDim.x) Ra[r] = rcomp_f32(rvec, nR, r, rl, a);
+    __syncthreads();
+    // M = sum_R i R_a e^{i phi} H(R)/ndegen; the on-site diagonal at R = 0 is removed (R_a = 0 there)
+    for (int e = tid; e < w * w; e += blockDim.x) {
+      const int m = e / w, c = e % w;
+      zd acc = mk<double>(0.0, 0.0);
+      for (int r = 0; r < nR; ++r) {
+        const bool r0 = rvec[r] == 0 && rvec[nR + r] == 0 && rvec[2 * nR + r] == 0;
+        if (r0 && m == c) continue;
+        const zd f = mk<double>(-Ra[r] * eph[r].im, Ra[r] * eph[r].re);  // i R_a e
+        cfma(acc, f, hr[((size_t)r * w + m) * w + c]);
+      }
+      M[e] = acc;
+    }
+    __syncthreads();
+    for (int e = tid; e < nv * w; e += blockDim.x) {
+      const int v = e / w, m = e % w;
+      zd acc = mk<double>(0.0, 0.0);
+      for (int c = 0; c < w; ++c) cfma(acc, M[m * w + c], B[v * w + c]);
+      Mv[e] = acc;
+    }
+    __syncthreads();
+    for (int e = tid; e < dimk; e += blockDim.x) {
+      const int c = e / nv, v = e % nv;
+      zd acc = mk<double>(0.0, 0.0);
+      for (int m = 0; m < w; ++m) cfmac(acc, B[(nv + c) * w + m], Mv[v * w + m]);
+      // factor = Re(1/(E_c - E_v + i*CSHIFT_f32)) (a complex assigned to a real in optsp)
+      const double de = eig_win[(size_t)k * nb + nv + c] - eig_win[(size_t)k * nb + v];
+      const double sf = (double)s32;
+      const double factor = de / (de * de + sf * sf);
+      hout[a * dim + (size_t)k * dimk + e] = cscale(acc, factor);
+    }
+  }
+  __syncthreads();
+  const double isq = (double)0.70710677f;  // 1.0/sqrt(2.) in single precision
+  for (int e = tid; e < dimk; e += blockDim.x) {
+    const size_t I = (size_t)k * dimk + e;
+    const zd hx = hout[I], hy = hout[dim + I];
+    hout[3 * dim + I] = mk<double>((hx.re - hy.im) * isq, (hx.im + hy.re) * isq);
+    hout[4 * dim + I] = mk<double>((hx.re + hy.im) * isq, (hx.im - hy.re) * isq);
+  }
+}
+
+// ----------------------------------------------------------------------------- Coulomb table
+__host__ __device__ __forceinline__ double vecsize3(const double* a) { return sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]); }
+
+struct CoulConst {
+  int type;
+  double vbz, tol, cic;
+  double eta, kappa, pb, pt, r0, w, lc, ez;  // V2DRK / V2DOH / V2DT2
+  double ed;                                 // V3DL / V2DK
+  double v2dk_r0, v2dk_small;                // V2DK
+  double rc;                                 // V2DT / V0DT
+};
+
+__global__ void coulomb_kernel(CoulConst cc, const double* __restrict__ k1, int n1, const double* __restrict__ k2,
+                               int n2, double* __restrict__ V, int ldv) {
+  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long)n1 * n2) return;
+  const int i = (int)(e / n2), j = (int)(e % n2);
+  const double dx = k1[3 * i] - k2[3 * j], dy = k1[3 * i + 1] - k2[3 * j + 1], dz = k1[3 * i + 2] - k2[3 * j + 2];
+  const double modk = sqrt(dx * dx + dy * dy + dz * dz);
+  double v = 0.0;
+  const double vc = cc.vbz * cc.cic;
+  switch (cc.type) {
+    case CT_V2DRK:
+      if (!(modk < cc.tol)) {
+        const double aux1 = (1.0 - (cc.pb * cc.pt * exp(-2.0 * modk * cc.eta * cc.lc))) * cc.kappa;
+        const double aux2 = (1.0 - (cc.pt * exp(-cc.eta * modk * cc.lc))) * (1.0 - (cc.pb * exp(-cc.eta * modk * cc.lc)));
+        const double aux3 = cc.r0 * modk * exp(-modk * cc.w);
+        const double ew = (aux1 / aux2) + aux3;
+        v = vc * exp(-modk * cc.w) * (1.0 / ew) * (1.0 / modk);
+      }
+      break;
+    case CT_V3DL:
+    case CT_V3D:
+      if (!(modk < cc.tol)) v = cc.vbz * (cc.cic / cc.ed) * (1.0 / (modk * modk));
+      break;
+    case CT_V2DK:
+      if (modk < cc.tol)
+        v = cc.v2dk_small;
+      else
+        v = cc.vbz * (cc.cic / cc.ed) * (1.0 / (modk * (1 + (cc.v2dk_r0 * modk))));
+      break;
+    case CT_V2DOH:
+      if (!(modk < cc.tol)) v = vc * exp(-cc.w * modk) * (1.0 / (cc.ez * modk));
+      break;
+    case CT_V2DT: {
+      const double gz = fabs(dz), gpar = sqrt(dx * dx + dy * dy), rc = cc.rc;
+      if (gpar < cc.tol && gz < cc.tol) {
+        v = vc * (-0.5 * rc * rc);
+      } else if (gpar < cc.tol) {
+        v = vc * (1.0 / (modk * modk)) * (1.0 - cos(gz * rc) - (gz * rc * sin(gz * rc)));
+      } else {
+        const double aux1 = gz / gpar, aux2 = gpar * rc, aux3 = gz * rc;
+        v = vc * (1.0 / (modk * modk)) * (1.0 + (exp(-aux2) * (aux1 * sin(aux3) - cos(aux3))));
+      }
+      break;
+    }
+    case CT_V2DT2:
+      if (!(modk < cc.tol)) {
+        const double qxy = sqrt(dx * dx + dy * dy);
+        v = vc * (1.0 / (modk * modk)) * (1.0 - exp(-0.5 * qxy * cc.lc) * cos(0.5 * cc.lc * dz));
+      }
+      break;
+    case CT_V0DT:
+      if (modk < cc.tol)
+        v = vc * 0.5 * cc.rc * cc.rc;
+      else
+        v = vc * (1.0 / (modk * modk)) * (1.0 - cos(cc.rc * modk));
+      break;
+    default:
+      v = 0.0;
+  }
+  V[(size_t)i * ldv + j] = v;
+}
+
+__global__ void transition_kernel(const double* __restrict__ eig_win, int nk, int nv, int nc, double* dE) {
+  const long I = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long dim = (long)nk * nc * nv;
+  if (I >= dim) return;
+  const int k = (int)(I / (nc * nv)), c = (int)((I / nv) % nc), v = (int)(I % nv);
+  dE[I] = eig_win[(size_t)k * (nv + nc) + nv + c] - eig_win[(size_t)k * (nv + nc) + v];
+}
+
+}  // namespace
+
+cudaError_t launch_hk_eig(const zd* hr, const int* rvec, const int* ndegen, int nR, int w, const double* rlat_rm,
+                          double efermi, double scs, const double* kpt, int nk, int nv, int nc, double* eig_all,
+                          zd* vec_all, double* eig_win, zd* vec_win, int* nocp, DevStatus* st, cudaStream_t s) {
+  if (w > 64 || w < 1) return cudaErrorInvalidValue;
+  const int n = (w + 1) & ~1;
+  const size_t smem = (size_t)2 * n * n * sizeof(zd) + nR * sizeof(zd) + 32 * 2 * sizeof(double) + 32 * sizeof(zd) +
+                      4 * sizeof(double) + 64 * sizeof(double) + 32 * 3 * sizeof(int) + 64 * sizeof(int) + 64;
+  cudaError_t e = cudaFuncSetAttribute(hk_eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  hk_eig_kernel<<<nk, kHkThreads, smem, s>>>(hr, rvec, ndegen, nR, w, rlat_rm, efermi, scs, kpt, nk, nv, nc, eig_all,
+                                             vec_all, eig_win, vec_win, nocp, st); ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_optics(const zd* hr, const int* rvec, const int* ndegen, int nR, int w, const double* rlat_rm,
+                          const double* kpt, int nk, int nv, int nc, const double* eig_win, const zd* vec_win,
+                          double cshift, zd* hout, cudaStream_t s) {
+  const int nb = nv + nc;
+  const size_t smem = (size_t)(w * w + nb * w + nv * w + nR) * sizeof(zd) + nR * sizeof(double) + 16;
+  cudaError_t e = cudaFuncSetAttribute(optics_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  optics_kernel<<<nk, kHkThreads, smem, s>>>(hr, rvec, ndegen, nR, w, rlat_rm, kpt, nk, nv, nc, eig_win, vec_win,
+                                             (float)cshift, hout); ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_coulomb(const CoulParams& p, const double* kpt1, int n1, const double* kpt2, int n2, double* V,
+                           int ldv, cudaStream_t s) {
+  const double* r = p.rlat;
+  auto cross = [](const double* a, const double* b, double* o) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+  };
+  double vx[3];
+  cross(r, r + 3, vx);
+  const double vc2 = sqrt(vx[0] * vx[0] + vx[1] * vx[1] + vx[2] * vx[2]);          // vcell2D
+  const double vc3 = fabs(vx[0] * r[6] + vx[1] * r[7] + vx[2] * r[8]);             // vcell3D
+  const long ng = (long)p.ngrid[0] * p.ngrid[1] * p.ngrid[2];
+  CoulConst cc{};
+  cc.type = p.type;
+  cc.tol = p.ktol;
+  cc.cic = -(double)(0.0904756f * 1000.0f);  // -(0.0904756)*10**(3) evaluated in single precision
+  cc.r0 = p.r0;
+  cc.w = p.w;
+  cc.lc = p.lc;
+  cc.ez = p.ez;
+  const double pi32 = (double)3.14159274101257324f;
+  switch (p.type) {
+    case CT_V2DRK: {
+      cc.vbz = 1.0 / (ng * vc2);
+      const double epar = p.ediel[1], et = p.ediel[0], eb = p.ediel[2];
+      cc.eta = sqrt(epar / p.ez);
+      cc.kappa = sqrt(epar * p.ez);
+      cc.pb = (eb - cc.kappa) / (eb + cc.kappa);
+      cc.pt = (et - cc.kappa) / (et + cc.kappa);
+      break;
+    }
+    case CT_V3DL:
+      cc.vbz = 1.0 / (ng * vc3);
+      cc.ed = p.ediel[1];
+      break;
+    case CT_V3D:
+      cc.vbz = 1.0 / (ng * vc3);
+      cc.ed = 1.0;
+      break;
+    case CT_V2DK: {
+      const double a0 = 0.5 * (vecsize3(r) + vecsize3(r + 3));
+      cc.vbz = 1.0 / (ng * vc2);
+      cc.v2dk_r0 = ((p.ediel[1] - 1.0) * p.lc) / (p.ediel[0] + p.ediel[2]);
+      const double g1 = (double)(p.ngrid[0] * p.ngrid[1]);
+      const double auxi = (2. * pi32 * cc.v2dk_r0) / (a0 * sqrt(g1));
+      cc.ed = (p.ediel[0] + p.ediel[2]) / (2.0);
+      cc.v2dk_small = cc.vbz * (cc.cic / cc.ed) * (a0 * sqrt(g1) / (2. * pi32)) *
+                      ((double)1.76f + auxi * 1.0 + 0.0 * auxi * auxi);
+      break;
+    }
+    case CT_V2DOH:
+      cc.vbz = 1.0 / (ng * vc2);
+      break;
+    case CT_V2DT:
+      cc.vbz = 1.0 / (ng * vc3);
+      cc.rc = 0.5 * r[8];
+      break;
+    case CT_V2DT2:
+      cc.vbz = 1.0 / (ng * vc3);
+      break;
+    case CT_V0DT: {
+      cc.vbz = 1.0 / (ng * vc3);
+      const double s1 = vecsize3(r), s2 = vecsize3(r + 3), s3 = vecsize3(r + 6);
+      cc.rc = 0.5 * fmin(s1, fmin(s2, s3));
+      break;
+    }
+    default:
+      return cudaErrorInvalidValue;
+  }
+  const long tot = (long)n1 * n2;
+  const int th = 256;
+  coulomb_kernel<<<(unsigned)((tot + th - 1) / th), th, 0, s>>>(cc, kpt1, n1, kpt2, n2, V, ldv); ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_transition_energies(const double* eig_win, int nk, int nv, int nc, double* dE, cudaStream_t s) {
+  const long dim = (long)nk * nc * nv;
+  transition_kernel<<<(unsigned)((dim + 255) / 256), 256, 0, s>>>(eig_win, nk, nv, nc, dE); ++g_launch_count;
+  return cudaGetLastError();
+}
+
+}  // namespace wtb

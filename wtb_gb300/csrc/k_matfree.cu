@@ -1,0 +1,297 @@
+// Matrix-free BSE operator pieces.
+//
+// With I = (k,c,v) and the band vectors C[k][c][o], Vb[k][v][p] (o, p orbitals) the operator of the
+// dense build factorises as
+//     (H x)[k,c,v] = dE[k,c,v] x[k,c,v] + sum_{o,p} conj(C[k,c,o]) conj(Vb[k,v,p]) T[k,o,p]
+//     T[k,o,p]     = sum_k' V(k,k') Z[k',o,p]
+//     Z[k',o,p]    = sum_{c',v'} C[k',c',o] Vb[k',v',p] x[k',c',v']
+// (same operator as matrizelbse, src/module_bse.F90:24-83, including V(k,k) times the orbital overlaps
+// on the same k-point, which vanish by orthonormality).  The gather kernel forms Z, the real
+// Nk x Nk by Nk x (2 w^2 nb) contraction T = V Z runs on the tensor cores (tcgen05, split-BF16) or on
+// the CUDA cores (FP32/FP64), and the scatter kernel forms y.
+//
+// Z is stored transposed and K-major for the contraction: zt[slice][n][k'] with
+// n = ((b*w + o)*w + p)*2 + (0 re | 1 im); T is row-major t[k][n].
+#include <cuda_bf16.h>
+
+#include "wtb_internal.h"
+
+namespace wtb {
+
+namespace {
+
+template <class Z>
+struct ZStore;
+template <>
+struct ZStore<float> {
+  __device__ static void put(float* base, long slice_stride, int nslices, long off, float v) {
+    (void)slice_stride;
+    (void)nslices;
+    base[off] = v;
+  }
+};
+template <>
+struct ZStore<double> {
+  __device__ static void put(double* base, long slice_stride, int nslices, long off, double v) {
+    (void)slice_stride;
+    (void)nslices;
+    base[off] = v;
+  }
+};
+template <>
+struct ZStore<uint16_t> {
+  // split v = hi + mid + lo with each part rounded to bfloat16
+  __device__ static void put(uint16_t* base, long slice_stride, int nslices, long off, float v) {
+    float r = v;
+    for (int s = 0; s < nslices; ++s) {
+      const __nv_bfloat16 h = __float2bfloat16_rn(r);
+      base[s * slice_stride + off] = __bfloat16_as_ushort(h);
+      r = r - __bfloat162float(h);
+    }
+  }
+};
+
+template <class S, class Z>
+__global__ void __launch_bounds__(256) mf_gather_kernel(const cplx<S>* __restrict__ X, int ldx, int c0,
+                                                        const zd* __restrict__ vec_win, int nk, int nv, int nc, int w,
+                                                        int KT, Z* __restrict__ zt, int ldk, int nslices,
+                                                        long slice_stride) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nb = nv + nc, ncv = nc * nv;
+  const int kt0 = blockIdx.x * KT;
+  const int b = blockIdx.y;
+  const int tkn = min(KT, nk - kt0);
+  cplx<S>* Cs = reinterpret_cast<cplx<S>*>(smem_raw);  // [KT][nc][w]
+  cplx<S>* Vs = Cs + KT * nc * w;                      // [KT][nv][w]
+  cplx<S>* xs = Vs + KT * nv * w;                      // [KT][ncv]
+  cplx<S>* Y1 = xs + KT * ncv;                         // [KT][nc][w]
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < KT * nb * w; e += nt) {
+    const int kk = e / (nb * w), s = (e / w) % nb, o = e % w;
+    zd a = mk<double>(0.0, 0.0);
+    if (kk < tkn) a = vec_win[((size_t)(kt0 + kk) * nb + s) * w + o];
+    const cplx<S> as = mk<S>((S)a.re, (S)a.im);
+    if (s < nv)
+      Vs[(kk * nv + s) * w + o] = as;
+    else
+      Cs[(kk * nc + s - nv) * w + o] = as;
+  }
+  for (int e = tid; e < KT * ncv; e += nt) {
+    const int kk = e / ncv, cv = e % ncv;
+    xs[e] = kk < tkn ? X[((size_t)(kt0 + kk) * ncv + cv) * ldx + c0 + b] : mk<S>(0, 0);
+  }
+  __syncthreads();
+  // Y1[k'][c'][p] = sum_v' Vb[k'][v'][p] x[k'][c'][v']
+  for (int e = tid; e < KT * nc * w; e += nt) {
+    const int kk = e / (nc * w), c = (e / w) % nc, p = e % w;
+    cplx<S> acc = mk<S>(0, 0);
+    for (int v = 0; v < nv; ++v) cfma(acc, Vs[(kk * nv + v) * w + p], xs[kk * ncv + c * nv + v]);
+    Y1[e] = acc;
+  }
+  __syncthreads();
+  // Z[k'][o][p] = sum_c' C[k'][c'][o] Y1[k'][c'][p]; k' fastest across threads -> coalesced rows of zt
+  const long nbase = (long)b * w * w * 2;
+  for (int e = tid; e < KT * w * w; e += nt) {
+    const int kk = e % KT, op = e / KT;
+    if (kk >= tkn) continue;
+    const int o = op / w, p = op % w;
+    cplx<S> acc = mk<S>(0, 0);
+    for (int c = 0; c < nc; ++c) cfma(acc, Cs[(kk * nc + c) * w + o], Y1[(kk * nc + c) * w + p]);
+    const long n = nbase + (long)op * 2;
+    const long off = n * ldk + kt0 + kk;
+    ZStore<Z>::put(zt, slice_stride, nslices, off, acc.re);
+    ZStore<Z>::put(zt, slice_stride, nslices, off + ldk, acc.im);
+  }
+}
+
+template <class S, class T>
+__global__ void __launch_bounds__(128) mf_scatter_kernel(const T* __restrict__ Tm, int ldt,
+                                                         const cplx<S>* __restrict__ X, int ldx,
+                                                         const zd* __restrict__ vec_win, const double* __restrict__ dE,
+                                                         int nk, int nv, int nc, int w, int nb, int nbg,
+                                                         cplx<S>* __restrict__ Y, int ldy, int c0) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int k = blockIdx.x;
+  const int b0 = blockIdx.y * nbg;
+  const int nbl = min(nbg, nb - b0);
+  const int nbnd = nv + nc, ncv = nc * nv;
+  cplx<S>* Cs = reinterpret_cast<cplx<S>*>(smem_raw);  // [nc][w]
+  cplx<S>* Vs = Cs + nc * w;                           // [nv][w]
+  cplx<S>* U = Vs + nv * w;                            // [nbg][w][nv]
+  T* Ts = reinterpret_cast<T*>(U + nbg * w * nv);     // [nbg][w][w][2]
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < nbnd * w; e += nt) {
+    const int s = e / w, o = e % w;
+    const zd a = vec_win[((size_t)k * nbnd + s) * w + o];
+    const cplx<S> as = mk<S>((S)a.re, (S)a.im);
+    if (s < nv)
+      Vs[s * w + o] = as;
+    else
+      Cs[(s - nv) * w + o] = as;
+  }
+  const int row = nbl * w * w * 2;
+  const T* trow = Tm + (size_t)k * ldt + (size_t)b0 * w * w * 2;
+  for (int e = tid; e < row; e += nt) Ts[e] = trow[e];
+  __syncthreads();
+  // U[b][o][v] = sum_p conj(Vb[v][p]) T[b][o][p]
+  for (int e = tid; e < nbl * w * nv; e += nt) {
+    const int bb = e / (w * nv), o = (e / nv) % w, v = e % nv;
+    cplx<S> acc = mk<S>(0, 0);
+    const T* tp = Ts + ((size_t)bb * w + o) * w * 2;
+    for (int p = 0; p < w; ++p) cfmac(acc, Vs[v * w + p], mk<S>((S)tp[2 * p], (S)tp[2 * p + 1]));
+    U[e] = acc;
+  }
+  __syncthreads();
+  // y[c][v][b] = dE x + sum_o conj(C[c][o]) U[b][o][v]
+  for (int e = tid; e < ncv * nbl; e += nt) {
+    const int cv = e / nbl, bb = e % nbl;
+    const int c = cv / nv, v = cv % nv;
+    cplx<S> acc = mk<S>(0, 0);
+    for (int o = 0; o < w; ++o) cfmac(acc, Cs[c * w + o], U[((size_t)bb * w + o) * nv + v]);
+    const size_t I = (size_t)k * ncv + cv;
+    const cplx<S> x = X[I * ldx + c0 + b0 + bb];
+    const S d = (S)dE[I];
+    acc.re += d * x.re;
+    acc.im += d * x.im;
+    Y[I * ldy + c0 + b0 + bb] = acc;
+  }
+}
+
+// C[M][N] = A[M][K] * B[N][K]^T, real, CUDA cores.  64 x 64 CTA tile, 4 x 4 per thread, K step 16.
+template <class S>
+__global__ void __launch_bounds__(256) simt_gemm_tn_kernel(const S* __restrict__ A, int lda, const S* __restrict__ B,
+                                                           int ldb, S* __restrict__ C, int ldc, int M, int N, int K) {
+  constexpr int BM = 64, BN = 64, BK = 16;
+  __shared__ S As[BK][BM + 4];
+  __shared__ S Bs[BK][BN + 4];
+  const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  S acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0;
+  for (int k0 = 0; k0 < K; k0 += BK) {
+    for (int e = tid; e < BM * BK; e += 256) {
+      const int r = e / BK, kk = e % BK;
+      const int gm = m0 + r, gn = n0 + r, gk = k0 + kk;
+      As[kk][r] = (gm < M && gk < K) ? A[(size_t)gm * lda + gk] : (S)0;
+      Bs[kk][r] = (gn < N && gk < K) ? B[(size_t)gn * ldb + gk] : (S)0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; ++kk) {
+      S a[4], bv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bv[j] = Bs[kk][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], bv[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int gm = m0 + ty * 4 + i, gn = n0 + tx * 4 + j;
+      if (gm < M && gn < N) C[(size_t)gm * ldc + gn] = acc[i][j];
+    }
+}
+
+__global__ void split_bf16_kernel(const double* __restrict__ V, int ldv, int rows, int cols, uint16_t* __restrict__ out,
+                                  int ldo, long slice_stride, int nslices) {
+  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long)rows * cols) return;
+  const int r = (int)(e / cols), c = (int)(e % cols);
+  double x = V[(size_t)r * ldv + c];
+  for (int s = 0; s < nslices; ++s) {
+    const __nv_bfloat16 h = __float2bfloat16_rn((float)x);
+    out[s * slice_stride + (size_t)r * ldo + c] = __bfloat16_as_ushort(h);
+    x = x - (double)__bfloat162float(h);
+  }
+}
+
+__global__ void round_f32_kernel(const double* __restrict__ V, int ldv, int rows, int cols, float* __restrict__ out,
+                                 int ldo) {
+  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long)rows * cols) return;
+  const int r = (int)(e / cols), c = (int)(e % cols);
+  out[(size_t)r * ldo + c] = (float)V[(size_t)r * ldv + c];
+}
+
+}  // namespace
+
+template <class S, class Z>
+cudaError_t launch_mf_gather(const cplx<S>* X, int ldx, int c0, int nb, const zd* vec_win, int nk, int nv, int nc,
+                             int w, Z* zt, int ldk, int nslices, long slice_stride, cudaStream_t s) {
+  int KT = 32;
+  auto smem_of = [&](int kt) { return (size_t)(2 * kt * nc * w + kt * nv * w + kt * nc * nv) * sizeof(cplx<S>); };
+  while (KT > 4 && smem_of(KT) > 160 * 1024) KT /= 2;
+  const size_t smem = smem_of(KT);
+  cudaError_t e = cudaFuncSetAttribute(mf_gather_kernel<S, Z>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  dim3 grid((nk + KT - 1) / KT, nb);
+  mf_gather_kernel<S, Z><<<grid, 256, smem, s>>>(X, ldx, c0, vec_win, nk, nv, nc, w, KT, zt, ldk, nslices,
+                                                 slice_stride); ++g_launch_count;
+  return cudaGetLastError();
+}
+
+template <class S, class T>
+cudaError_t launch_mf_scatter(const T* Tm, int ldt, const cplx<S>* X, int ldx, const zd* vec_win, const double* dE,
+                              int nk, int nv, int nc, int w, int nb, cplx<S>* Y, int ldy, int c0, cudaStream_t s) {
+  int nbg = nb;
+  auto smem_of = [&](int g) {
+    return (size_t)((nc + nv) * w + g * w * nv) * sizeof(cplx<S>) + (size_t)g * w * w * 2 * sizeof(T) + 16;
+  };
+  while (nbg > 1 && smem_of(nbg) > 96 * 1024) nbg = (nbg + 1) / 2;
+  const size_t smem = smem_of(nbg);
+  cudaError_t e = cudaFuncSetAttribute(mf_scatter_kernel<S, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  dim3 grid(nk, (nb + nbg - 1) / nbg);
+  mf_scatter_kernel<S, T><<<grid, 128, smem, s>>>(Tm, ldt, X, ldx, vec_win, dE, nk, nv, nc, w, nb, nbg, Y, ldy, c0); ++g_launch_count;
+  return cudaGetLastError();
+}
+
+template <class S>
+cudaError_t launch_simt_gemm_tn(const S* A, int lda, const S* B, int ldb, S* C, int ldc, int M, int N, int K,
+                                cudaStream_t s) {
+  dim3 grid((N + 63) / 64, (M + 63) / 64);
+  simt_gemm_tn_kernel<S><<<grid, 256, 0, s>>>(A, lda, B, ldb, C, ldc, M, N, K); ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_split_bf16(const double* V, int ldv, int rows, int cols, uint16_t* out, int ldo, long slice_stride,
+                              int nslices, cudaStream_t s) {
+  const long n = (long)rows * cols;
+  split_bf16_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(V, ldv, rows, cols, out, ldo, slice_stride, nslices); ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_round_f32(const double* V, int ldv, int rows, int cols, float* out, int ldo, cudaStream_t s) {
+  const long n = (long)rows * cols;
+  round_f32_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(V, ldv, rows, cols, out, ldo); ++g_launch_count;
+  return cudaGetLastError();
+}
+
+template cudaError_t launch_mf_gather<float, float>(const cplx<float>*, int, int, int, const zd*, int, int, int, int,
+                                                    float*, int, int, long, cudaStream_t);
+template cudaError_t launch_mf_gather<float, uint16_t>(const cplx<float>*, int, int, int, const zd*, int, int, int,
+                                                       int, uint16_t*, int, int, long, cudaStream_t);
+template cudaError_t launch_mf_gather<double, double>(const cplx<double>*, int, int, int, const zd*, int, int, int,
+                                                      int, double*, int, int, long, cudaStream_t);
+template cudaError_t launch_mf_scatter<float, float>(const float*, int, const cplx<float>*, int, const zd*,
+                                                     const double*, int, int, int, int, int, cplx<float>*, int, int,
+                                                     cudaStream_t);
+template cudaError_t launch_mf_scatter<double, double>(const double*, int, const cplx<double>*, int, const zd*,
+                                                       const double*, int, int, int, int, int, cplx<double>*, int, int,
+                                                       cudaStream_t);
+template cudaError_t launch_simt_gemm_tn<float>(const float*, int, const float*, int, float*, int, int, int, int,
+                                                cudaStream_t);
+template cudaError_t launch_simt_gemm_tn<double>(const double*, int, const double*, int, double*, int, int, int, int,
+                                                 cudaStream_t);
+
+}  // namespace wtb

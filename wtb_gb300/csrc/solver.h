@@ -1,0 +1,144 @@
+// Lowest-exciton eigensolver (replaces SLEPc Krylov-Schur in slepc_solver,
+// src/module_slepc_solver.F90:12-97) and the BSE operators it drives.
+#pragma once
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "wtb_internal.h"
+
+namespace wtb {
+
+// Device allocation with grow-only reuse.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  cudaError_t ensure(size_t n, bool zero = false) {
+    if (n <= bytes && p) {
+      if (zero) return cudaMemset(p, 0, n);
+      return cudaSuccess;
+    }
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&p, n ? n : 16);
+    if (e != cudaSuccess) return e;
+    bytes = n;
+    if (zero) return cudaMemset(p, 0, n);
+    return cudaSuccess;
+  }
+  template <class T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
+};
+
+struct Workspace {
+  std::map<std::string, std::unique_ptr<DevBuf>> bufs;
+  template <class T>
+  T* get(const std::string& name, size_t count, cudaError_t* err, bool zero = false) {
+    auto& b = bufs[name];
+    if (!b) b.reset(new DevBuf());
+    *err = b->ensure(count * sizeof(T), zero);
+    return b->as<T>();
+  }
+};
+
+template <class S>
+struct Operator {
+  virtual ~Operator() {}
+  // Y[:, c0:c0+ncol] = H X[:, c0:c0+ncol]
+  virtual cudaError_t apply(const cplx<S>* X, int ldx, int c0, int ncol, cplx<S>* Y, int ldy, cudaStream_t s) = 0;
+  long matvec_columns = 0;
+};
+
+template <class S>
+struct DenseOperator : Operator<S> {
+  const cplx<S>* H = nullptr;
+  int dim = 0;
+  cudaError_t apply(const cplx<S>* X, int ldx, int c0, int ncol, cplx<S>* Y, int ldy, cudaStream_t s) override {
+    this->matvec_columns += ncol;
+    return launch_dense_mv<S>(H, dim, X + c0, ldx, Y + c0, ldy, ncol, s);
+  }
+};
+
+enum GemmKind { GEMM_TC_BF16 = 0, GEMM_SIMT_F32 = 1, GEMM_SIMT_F64 = 2 };
+
+// Event pairs around the contraction launches (enabled by wtb_profile_enable).
+struct KernelProfile {
+  bool on = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+  double total_ms = 0.0, flops = 0.0, bytes = 0.0;
+  long long launches = 0;
+  void flush() {
+    for (auto& pr : pending) {
+      float ms = 0.f;
+      if (cudaEventSynchronize(pr.second) == cudaSuccess && cudaEventElapsedTime(&ms, pr.first, pr.second) == cudaSuccess)
+        total_ms += ms;
+      cudaEventDestroy(pr.first);
+      cudaEventDestroy(pr.second);
+    }
+    pending.clear();
+  }
+  void reset() {
+    flush();
+    total_ms = flops = bytes = 0.0;
+    launches = 0;
+  }
+};
+
+// Matrix-free operator: gather (Z), contraction (T = V Z), scatter (y).  S = iteration precision.
+template <class S>
+struct MatFreeOperator : Operator<S> {
+  int nk = 0, nv = 0, nc = 0, w = 0, nbmax = 16;
+  const zd* vec_win = nullptr;
+  const double* dE = nullptr;
+  GemmKind kind = GEMM_SIMT_F32;
+  int nslices = 2, npairs = 3;
+  int pa[8] = {0}, pb[8] = {0};
+  int Mpad = 0, Kpad = 0, Npad = 0;
+  // contraction operands
+  const uint16_t* Vs = nullptr;   // [nslices][Mpad][Kpad] bf16
+  uint16_t* Zs = nullptr;         // [nslices][Npad][Kpad] bf16
+  const S* Vr = nullptr;          // [nk][Kpad] (SIMT)
+  S* Zr = nullptr;                // [Npad][Kpad] (SIMT)
+  void* Tm = nullptr;             // [Mpad][Npad] float (TC) or S (SIMT)
+  DevStatus* st = nullptr;
+  KernelProfile* prof = nullptr;
+  std::map<int, TcGemmPlan*> plans;  // keyed by N of the chunk
+  std::string* msg = nullptr;
+  ~MatFreeOperator() override {
+    for (auto& kv : plans) tc_gemm_plan_destroy(kv.second);
+  }
+  cudaError_t apply(const cplx<S>* X, int ldx, int c0, int ncol, cplx<S>* Y, int ldy, cudaStream_t s) override;
+};
+
+struct SolveStats {
+  int iterations = 0;
+  long matvec_columns = 0;
+  double max_rel_residual = 0.0;
+  double refine_shift_max = 0.0;
+  int launches = 0;
+};
+
+// Lowest nev eigenpairs of the Hermitian operator.  diag = its diagonal (preconditioner and start
+// vectors).  Output: E (host, nev) and the FP64 eigenvectors Xout (device, dim x nev row-major).
+template <class S>
+int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, double tol, int maxit,
+                 Workspace& ws, DevStatus* st, cudaStream_t s, std::vector<double>* E, zd* Xout, SolveStats* stats,
+                 std::string* msg);
+
+// extra launchers used by the solver
+cudaError_t launch_jacobi_eig_f32(zd* A, int lda, int n, double* evals, zd* evecs, int ldv, int sweeps,
+                                  DevStatus* st, cudaStream_t s);
+cudaError_t launch_mark_dropped(zd* G, int ldg, int n, const int* keep, cudaStream_t s);
+cudaError_t launch_select_lowest(const double* diag, int dim, int m, int* idx, cudaStream_t s);
+template <class S>
+cudaError_t launch_init_guess(cplx<S>* X, int ldx, int dim, int m, const int* idx, unsigned seed, cudaStream_t s);
+void tc_gemm_set_valid(TcGemmPlan* p, int m_valid, int n_valid);
+
+}  // namespace wtb

@@ -1,0 +1,905 @@
+// C ABI of libwtb_gb300 (declared in include/wtb_gpu.h): the context, the state the Fortran modules
+// kept in globals, and the entry points that stand in for eigsys, monhkhorst_pack, the module_coulomb
+// potentials, matrizelbse's build loop, slepc_solver, dielbsev/dielbsep, bsesolver, bsedielraw and
+// bseoptprop.  Everything numeric runs in the CUDA kernels of this library; host code only moves
+// arguments, checks them, and orchestrates launches on the context's stream.
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+#include "solver.h"
+
+namespace wtb {
+long long g_launch_count = 0;
+}
+
+using namespace wtb;
+
+struct wtb_ctx {
+  int device = 0;
+  cudaStream_t s = nullptr;
+  std::string msg;
+  DevStatus* st = nullptr;
+  Workspace ws;
+  // H(R)
+  bool have_hr = false;
+  int w = 0, nR = 0, systype_np = 0;
+  double efermi = 0.0, scs = 0.0;
+  double rlat_rm[9] = {0};
+  // bands of the last mesh
+  bool have_bands = false;
+  int nk = 0, nv = 0, nc = 0;
+  int ngrid[3] = {0, 0, 0};
+  std::vector<double> kpt;  // nk x 3 row-major
+  // last BSE operator data (for wtb_optsp)
+  bool have_hr_optics = false;
+  KernelProfile prof;
+};
+
+namespace {
+
+int set_err(wtb_ctx* c, int code, const std::string& m) {
+  if (c) c->msg = m;
+  return code;
+}
+
+#define CKC(x)                                                                   \
+  do {                                                                           \
+    cudaError_t e__ = (x);                                                       \
+    if (e__ != cudaSuccess) {                                                    \
+      if (e__ == cudaErrorMemoryAllocation)                                      \
+        return set_err(c, WTB_ENOMEM, std::string(#x) + ": " + cudaGetErrorString(e__)); \
+      return set_err(c, WTB_ECUDA, std::string(#x) + ": " + cudaGetErrorString(e__));    \
+    }                                                                            \
+  } while (0)
+
+#define CKR(x)             \
+  do {                     \
+    int r__ = (x);         \
+    if (r__) return r__;   \
+  } while (0)
+
+// Reads and clears the device status word; maps kernel-side failures to the reference's STOP texts.
+int check_status(wtb_ctx* c) {
+  DevStatus h;
+  CKC(cudaStreamSynchronize(c->s));
+  CKC(cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
+  if (!h.code) return WTB_OK;
+  CKC(cudaMemset(c->st, 0, sizeof(DevStatus)));
+  switch (h.code) {
+    case 101:
+      return set_err(c, WTB_EBADARG, "Number of valence states higher then ocuppied states (k-point " +
+                                         std::to_string(h.info + 1) + ")");
+    case 102:
+      return set_err(c, WTB_EBADARG, "Number of conduction states higher then unocuppied states (k-point " +
+                                         std::to_string(h.info + 1) + ")");
+    case 201:
+      return set_err(c, WTB_ENOCONV, "The algorithm failed to compute eigenvalues.");
+    default:
+      if (h.code >= 400 && h.code < 500)
+        return set_err(c, WTB_ETIMEOUT, "a bounded device wait timed out (code " + std::to_string(h.code) + ")");
+      return set_err(c, WTB_ECUDA, "device status " + std::to_string(h.code));
+  }
+}
+
+int prep_device(wtb_ctx* c) {
+  CKC(cudaSetDevice(c->device));
+  return WTB_OK;
+}
+
+double vcell3D(const double* r) {
+  const double vx0 = r[1] * r[5] - r[2] * r[4], vx1 = r[2] * r[3] - r[0] * r[5], vx2 = r[0] * r[4] - r[1] * r[3];
+  return std::fabs(vx0 * r[6] + vx1 * r[7] + vx2 * r[8]);
+}
+
+// Gamma-anchored mesh, i outer, j, l inner; reciprocal vectors with single-precision pi
+// (monhkhorst_pack + recvec, src/module_kmesh.F90:338-407).  kpt row-major nk x 3.
+void mp_mesh(int n1, int n2, int n3, const double* shift, const double* a1, const double* a2, const double* a3,
+             double* kpt) {
+  auto cross = [](const double* u, const double* v, double* o) {
+    o[0] = u[1] * v[2] - u[2] * v[1];
+    o[1] = u[2] * v[0] - u[0] * v[2];
+    o[2] = u[0] * v[1] - u[1] * v[0];
+  };
+  double v23[3], v31[3], v12[3];
+  cross(a2, a3, v23);
+  cross(a3, a1, v31);
+  cross(a1, a2, v12);
+  const double vol = std::fabs(a1[0] * v23[0] + a1[1] * v23[1] + a1[2] * v23[2]);
+  const double pi32 = (double)3.14159274101257324f;
+  const double f = (2.0 * pi32) / vol;
+  double b1[3], b2[3], b3[3], ks[3];
+  for (int d = 0; d < 3; ++d) {
+    b1[d] = f * v23[d];
+    b2[d] = f * v31[d];
+    b3[d] = f * v12[d];
+  }
+  for (int d = 0; d < 3; ++d) ks[d] = b1[d] * shift[0] + b2[d] * shift[1] + b3[d] * shift[2];
+  long cnt = 0;
+  for (int i = 0; i < n1; ++i)
+    for (int j = 0; j < n2; ++j)
+      for (int l = 0; l < n3; ++l) {
+        for (int d = 0; d < 3; ++d)
+          kpt[3 * cnt + d] = (b1[d] / (double)n1) * (double)i + (b2[d] / (double)n2) * (double)j +
+                             (b3[d] / (double)n3) * (double)l + ks[d];
+        ++cnt;
+      }
+}
+
+__global__ void transpose_z_kernel(const zd* __restrict__ A, int rows, int cols, int lda, zd* __restrict__ B,
+                                   int conj) {
+  // B (column-major rows x cols) = A (row-major rows x cols, ld lda)
+  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long)rows * cols) return;
+  const long r = e % rows, cc = e / rows;
+  zd v = A[r * lda + cc];
+  if (conj) v.im = -v.im;
+  B[cc * rows + r] = v;
+}
+
+template <class S>
+__global__ void conj_convert_kernel(const cplx<S>* __restrict__ A, long n, zd* __restrict__ B) {
+  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  B[e] = mk<double>((double)A[e].re, -(double)A[e].im);
+}
+
+__global__ void conj_inplace_kernel(zd* A, long n) {
+  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < n) A[e].im = -A[e].im;
+}
+
+__global__ void diag_real_kernel(const zd* __restrict__ H, int n, double* __restrict__ d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) d[i] = H[(size_t)i * n + i].re;
+}
+
+__global__ void __launch_bounds__(256) dielbse_kernel(const zd* __restrict__ A, int dimse, const zd* __restrict__ h1,
+                                                      const zd* __restrict__ h2, int pair, double* __restrict__ act) {
+  // one CTA per exciton n; A column-major (column n contiguous)
+  __shared__ double red[4][256];
+  const int n = blockIdx.x;
+  zd s1 = mk<double>(0, 0), s2 = mk<double>(0, 0);
+  for (int j = threadIdx.x; j < dimse; j += blockDim.x) {
+    const zd a = A[(size_t)n * dimse + j];
+    cfma(s1, a, h1[j]);
+    if (pair) cfma(s2, a, h2[j]);
+  }
+  red[0][threadIdx.x] = s1.re;
+  red[1][threadIdx.x] = s1.im;
+  red[2][threadIdx.x] = s2.re;
+  red[3][threadIdx.x] = s2.im;
+  __syncthreads();
+  for (int off = 128; off > 0; off >>= 1) {
+    if (threadIdx.x < off)
+      for (int q = 0; q < 4; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + off];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double ar = red[0][0], ai = red[1][0];
+    if (pair)
+      act[n] = ar * red[2][0] + ai * red[3][0];
+    else
+      act[n] = ar * ar + ai * ai;
+  }
+}
+
+__global__ void expand_acts_kernel(const double* __restrict__ osc, int nev, int dim, double* __restrict__ acts) {
+  // acts(dim, 8) column-major; rows past nev are zero
+  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long)dim * 8) return;
+  const int a = (int)(e / dim);
+  const long i = e % dim;
+  acts[e] = i < nev ? osc[(size_t)a * nev + i] : 0.0;
+}
+
+int upload_bands(wtb_ctx* c, int nk, const double* kpt_rm, int nv, int nc) {
+  cudaError_t err;
+  double* dk = c->ws.get<double>("kpt", (size_t)nk * 3, &err);
+  CKC(err);
+  CKC(cudaMemcpyAsync(dk, kpt_rm, sizeof(double) * nk * 3, cudaMemcpyHostToDevice, c->s));
+  const int w = c->w, nb = nv + nc;
+  double* eig_all = c->ws.get<double>("eig_all", (size_t)nk * w, &err);
+  CKC(err);
+  zd* vec_all = c->ws.get<zd>("vec_all", (size_t)nk * w * w, &err);
+  CKC(err);
+  double* eig_win = c->ws.get<double>("eig_win", (size_t)nk * (nb > 0 ? nb : 1), &err);
+  CKC(err);
+  zd* vec_win = c->ws.get<zd>("vec_win", (size_t)nk * (nb > 0 ? nb : 1) * w, &err);
+  CKC(err);
+  int* nocp = c->ws.get<int>("nocp", nk, &err);
+  CKC(err);
+  CKC(launch_hk_eig(c->ws.get<zd>("hr", 0, &err), c->ws.get<int>("rvec", 0, &err), c->ws.get<int>("ndegen", 0, &err),
+                    c->nR, w, c->ws.get<double>("rlat", 0, &err), c->efermi, c->scs, dk, nk, nv, nc, eig_all, vec_all,
+                    nb > 0 ? eig_win : nullptr, nb > 0 ? vec_win : nullptr, nocp, c->st, c->s));
+  CKR(check_status(c));
+  c->nk = nk;
+  c->nv = nv;
+  c->nc = nc;
+  c->kpt.assign(kpt_rm, kpt_rm + (size_t)nk * 3);
+  c->have_bands = nb > 0;
+  return WTB_OK;
+}
+
+int validate_params(wtb_ctx* c, const wtb_bse_params* p) {
+  if (!p) return set_err(c, WTB_EBADARG, "params is NULL");
+  if (p->ngrid[0] < 1 || p->ngrid[1] < 1 || p->ngrid[2] < 1) return set_err(c, WTB_EBADARG, "ngrid must be >= 1");
+  if (p->nc < 1 || p->nv < 1) return set_err(c, WTB_EBADARG, "nc and nv must be >= 1");
+  if (p->coultype < 0 || p->coultype > 8 || p->coultype == WTB_V1DT)
+    return set_err(c, WTB_EBADARG, "Wrong Coulomb Potential");
+  if (!(p->ktol > 0.0)) return set_err(c, WTB_EBADARG, "KTOL must be > 0 (V(k,k) is singular otherwise)");
+  if (p->precision < 0 || p->precision > 3 || p->op < 0 || p->op > 1)
+    return set_err(c, WTB_EBADARG, "unknown precision or operator mode");
+  if (p->op == WTB_OP_DENSE && p->precision >= WTB_PREC_BF16X3)
+    return set_err(c, WTB_EBADARG, "split-BF16 precision is available for the matrix-free operator only");
+  return WTB_OK;
+}
+
+CoulParams coul_of(wtb_ctx* c, const wtb_bse_params* p) {
+  CoulParams cp{};
+  cp.type = p->coultype;
+  for (int d = 0; d < 3; ++d) {
+    cp.ngrid[d] = p->ngrid[d];
+    cp.ediel[d] = p->ediel[d];
+  }
+  cp.ktol = p->ktol;
+  cp.ez = p->ez;
+  cp.w = p->w_coul;
+  cp.r0 = p->r0;
+  cp.lc = p->lc;
+  std::memcpy(cp.rlat, c->rlat_rm, sizeof(cp.rlat));
+  return cp;
+}
+
+int auto_block(const wtb_bse_params* p, int dim, bool fp64) {
+  int m = p->block > 0 ? p->block : std::max(p->nev + 6, (3 * p->nev + 1) / 2);
+  if (p->block <= 0) m = (m + 7) / 8 * 8;
+  const int cap = fp64 ? 26 : 32;
+  if (m > cap) m = cap;
+  if (m < p->nev) m = p->nev;
+  if (m > dim) m = dim;
+  return m;
+}
+
+// The BSE operator selected by p (dense FP64/FP32, or matrix-free FP64/FP32/split-BF16) over the bands of
+// the context; exactly one of o64 / o32 is set.
+struct OpBundle {
+  std::unique_ptr<Operator<double>> o64;
+  std::unique_ptr<Operator<float>> o32;
+  std::string msg;
+  const double* dE = nullptr;
+  int dim = 0;
+};
+
+int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob) {
+  const int nk = c->nk, nv = c->nv, nc = c->nc, w = c->w;
+  const int dim = nk * nc * nv;
+  cudaError_t err;
+  const zd* vec_win = c->ws.get<zd>("vec_win", 0, &err);
+  double* dE = c->ws.get<double>("dE", dim, &err);
+  CKC(err);
+  CKC(launch_transition_energies(c->ws.get<double>("eig_win", 0, &err), nk, nv, nc, dE, c->s));
+  const int Kpad = (nk + 63) / 64 * 64, Mpad = (nk + 127) / 128 * 128;
+  double* V = c->ws.get<double>("V", (size_t)Mpad * Kpad, &err, true);
+  CKC(err);
+  const double* kd = c->ws.get<double>("kpt", 0, &err);
+  CKC(launch_coulomb(coul_of(c, p), kd, nk, kd, nk, V, Kpad, c->s));
+  ob->dE = dE;
+  ob->dim = dim;
+  const bool fp64 = p->precision == WTB_PREC_FP64;
+  if (p->op == WTB_OP_DENSE) {
+    if (fp64) {
+      zd* H = c->ws.get<zd>("H64", (size_t)dim * dim, &err);
+      CKC(err);
+      CKC(launch_bse_build<double>(vec_win, dE, V, Kpad, nk, nv, nc, w, H, c->s));
+      auto op = new DenseOperator<double>();
+      op->H = H;
+      op->dim = dim;
+      ob->o64.reset(op);
+    } else {
+      zf* H = c->ws.get<zf>("H32", (size_t)dim * dim, &err);
+      CKC(err);
+      CKC(launch_bse_build<float>(vec_win, dE, V, Kpad, nk, nv, nc, w, H, c->s));
+      auto op = new DenseOperator<float>();
+      op->H = H;
+      op->dim = dim;
+      ob->o32.reset(op);
+    }
+    return WTB_OK;
+  }
+  const int N = 2 * w * w * nbmax;
+  const int Npad = (N + 255) / 256 * 256;
+  if (fp64) {
+    auto op = new MatFreeOperator<double>();
+    ob->o64.reset(op);
+    op->kind = GEMM_SIMT_F64;
+    op->nk = nk; op->nv = nv; op->nc = nc; op->w = w; op->nbmax = nbmax;
+    op->vec_win = vec_win; op->dE = dE; op->st = c->st; op->msg = &ob->msg; op->prof = &c->prof;
+    op->Kpad = Kpad; op->Mpad = Mpad; op->Npad = Npad;
+    op->Vr = V;
+    op->Zr = c->ws.get<double>("Zr64", (size_t)Npad * Kpad, &err, true);
+    op->Tm = c->ws.get<double>("T64", (size_t)Mpad * Npad, &err);
+    CKC(err);
+    return WTB_OK;
+  }
+  auto op = new MatFreeOperator<float>();
+  ob->o32.reset(op);
+  op->nk = nk; op->nv = nv; op->nc = nc; op->w = w; op->nbmax = nbmax;
+  op->vec_win = vec_win; op->dE = dE; op->st = c->st; op->msg = &ob->msg; op->prof = &c->prof;
+  op->Kpad = Kpad; op->Mpad = Mpad; op->Npad = Npad;
+  if (p->precision == WTB_PREC_FP32) {
+    op->kind = GEMM_SIMT_F32;
+    float* Vf = c->ws.get<float>("V32", (size_t)Mpad * Kpad, &err, true);
+    CKC(err);
+    CKC(launch_round_f32(V, Kpad, nk, nk, Vf, Kpad, c->s));
+    op->Vr = Vf;
+    op->Zr = c->ws.get<float>("Zr32", (size_t)Npad * Kpad, &err, true);
+    op->Tm = c->ws.get<float>("T32", (size_t)Mpad * Npad, &err);
+    CKC(err);
+    return WTB_OK;
+  }
+  if (!tc_gemm_available()) return set_err(c, WTB_ENODEV, "the split-BF16 tensor-core path needs an sm_103 device");
+  op->kind = GEMM_TC_BF16;
+  const bool x6 = p->precision == WTB_PREC_BF16X6;
+  op->nslices = x6 ? 3 : 2;
+  op->npairs = x6 ? 6 : 3;
+  const int pa6[6] = {0, 0, 1, 0, 1, 2}, pb6[6] = {0, 1, 0, 2, 1, 0};
+  for (int i = 0; i < op->npairs; ++i) {
+    op->pa[i] = pa6[i];
+    op->pb[i] = pb6[i];
+  }
+  uint16_t* Vs = c->ws.get<uint16_t>("Vbf", (size_t)op->nslices * Mpad * Kpad, &err, true);
+  CKC(err);
+  CKC(launch_split_bf16(V, Kpad, nk, nk, Vs, Kpad, (long)Mpad * Kpad, op->nslices, c->s));
+  op->Vs = Vs;
+  op->Zs = c->ws.get<uint16_t>("Zbf", (size_t)op->nslices * Npad * Kpad, &err, true);
+  op->Tm = c->ws.get<float>("Tbf", (size_t)Mpad * Npad, &err);
+  CKC(err);
+  return WTB_OK;
+}
+
+// Solve with the operator selected by p; leaves E and the FP64 eigenvectors (dim x nev row-major, "Xout").
+int run_solve(wtb_ctx* c, const wtb_bse_params* p, std::vector<double>* E, wtb_timings* t, SolveStats* stats) {
+  const int dim = c->nk * c->nc * c->nv;
+  cudaError_t err;
+  cudaEvent_t ev[3];
+  for (auto& e : ev) CKC(cudaEventCreate(&e));
+  CKC(cudaEventRecord(ev[0], c->s));
+  const bool fp64 = p->precision == WTB_PREC_FP64;
+  const int m = auto_block(p, dim, fp64);
+  const double tol = p->tol > 0 ? p->tol : (fp64 ? 1e-8 : 1e-6);
+  const int maxit = p->maxit > 0 ? p->maxit : 200;
+  zd* Xout = c->ws.get<zd>("Xout", (size_t)dim * p->nev, &err);
+  CKC(err);
+  OpBundle ob;
+  CKR(make_operator(c, p, std::min(m, 16), &ob));
+  CKC(cudaEventRecord(ev[1], c->s));
+  int rc;
+  std::string msg;
+  if (ob.o64)
+    rc = lobpcg_solve<double>(*ob.o64, ob.dE, dim, p->nev, m, tol, maxit, c->ws, c->st, c->s, E, Xout, stats, &msg);
+  else
+    rc = lobpcg_solve<float>(*ob.o32, ob.dE, dim, p->nev, m, tol, maxit, c->ws, c->st, c->s, E, Xout, stats, &msg);
+  if (!ob.msg.empty()) msg += " (" + ob.msg + ")";
+  CKC(cudaEventRecord(ev[2], c->s));
+  CKC(cudaEventSynchronize(ev[2]));
+  float t01 = 0, t12 = 0;
+  cudaEventElapsedTime(&t01, ev[0], ev[1]);
+  cudaEventElapsedTime(&t12, ev[1], ev[2]);
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (t) {
+    t->t_build_ms = t01;
+    t->t_solve_ms = t12;
+  }
+  if (rc != WTB_OK) {
+    int sc = check_status(c);
+    if (sc != WTB_OK && rc == WTB_ECUDA) return sc;
+    return set_err(c, rc, msg);
+  }
+  return check_status(c);
+}
+
+std::mutex g_default_mu;
+wtb_ctx* g_default = nullptr;
+
+}  // namespace
+
+// ================================================================================================ C ABI
+extern "C" {
+
+int wtb_version(void) { return 10000; }
+
+const char* wtb_last_error(const wtb_ctx* ctx) { return ctx ? ctx->msg.c_str() : "no context"; }
+
+int wtb_ctx_create(wtb_ctx** out, int device) {
+  if (!out) return WTB_EBADARG;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device || device < 0) return WTB_ENODEV;
+  wtb_ctx* c = new wtb_ctx();
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&c->st, sizeof(DevStatus)) != cudaSuccess || cudaMemset(c->st, 0, sizeof(DevStatus)) != cudaSuccess) {
+    delete c;
+    return WTB_ENODEV;
+  }
+  *out = c;
+  return WTB_OK;
+}
+
+int wtb_ctx_destroy(wtb_ctx* c) {
+  if (!c) return WTB_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->s);
+  c->prof.reset();
+  c->ws.bufs.clear();
+  if (c->st) cudaFree(c->st);
+  if (c->s) cudaStreamDestroy(c->s);
+  delete c;
+  return WTB_OK;
+}
+
+int wtb_set_hr(wtb_ctx* c, int w90basis, int nvec, const int* rvec, const int* ffactor, const double* hop,
+               const double* ihop, const double* rlat, double efermi, double scs, int systype_np) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (w90basis < 1 || w90basis > 64) return set_err(c, WTB_EBADARG, "w90basis must be in 1..64");
+  if (nvec < 1 || !rvec || !ffactor || !hop || !ihop || !rlat) return set_err(c, WTB_EBADARG, "missing H(R) arrays");
+  const int w = w90basis;
+  std::vector<zd> hr((size_t)nvec * w * w);
+  for (int iR = 0; iR < nvec; ++iR) {
+    if (ffactor[iR] <= 0) return set_err(c, WTB_EBADARG, "ffactor (ndegen) must be positive");
+    for (int m = 0; m < w; ++m)
+      for (int n = 0; n < w; ++n) {
+        const size_t f = (size_t)iR + (size_t)nvec * (m + (size_t)w * n);
+        const double re = hop[f], im = ihop[f];
+        if (!std::isfinite(re) || !std::isfinite(im)) return set_err(c, WTB_ENAN, "non-finite entry in H(R)");
+        hr[((size_t)iR * w + m) * w + n] = mk<double>(re, im);
+      }
+  }
+  double rl[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) rl[3 * i + j] = rlat[i + 3 * j];
+  if (!std::isfinite(efermi) || !std::isfinite(scs)) return set_err(c, WTB_ENAN, "non-finite efermi or scs");
+  cudaError_t err;
+  zd* dh = c->ws.get<zd>("hr", hr.size(), &err);
+  CKC(err);
+  int* dr = c->ws.get<int>("rvec", (size_t)nvec * 3, &err);
+  CKC(err);
+  int* dn = c->ws.get<int>("ndegen", nvec, &err);
+  CKC(err);
+  double* dl = c->ws.get<double>("rlat", 9, &err);
+  CKC(err);
+  CKC(cudaMemcpyAsync(dh, hr.data(), hr.size() * sizeof(zd), cudaMemcpyHostToDevice, c->s));
+  CKC(cudaMemcpyAsync(dr, rvec, sizeof(int) * nvec * 3, cudaMemcpyHostToDevice, c->s));
+  CKC(cudaMemcpyAsync(dn, ffactor, sizeof(int) * nvec, cudaMemcpyHostToDevice, c->s));
+  CKC(cudaMemcpyAsync(dl, rl, sizeof(rl), cudaMemcpyHostToDevice, c->s));
+  CKC(cudaStreamSynchronize(c->s));
+  c->w = w;
+  c->nR = nvec;
+  c->efermi = efermi;
+  c->scs = scs;
+  c->systype_np = systype_np;
+  std::memcpy(c->rlat_rm, rl, sizeof(rl));
+  c->have_hr = true;
+  c->have_bands = false;
+  return WTB_OK;
+}
+
+int wtb_monhkhorst_pack(int n1, int n2, int n3, const double* shift, const double* rlat1, const double* rlat2,
+                        const double* rlat3, double* kpt) {
+  if (n1 < 1 || n2 < 1 || n3 < 1 || !shift || !rlat1 || !rlat2 || !rlat3 || !kpt) return WTB_EBADARG;
+  const long nk = (long)n1 * n2 * n3;
+  std::vector<double> k((size_t)nk * 3);
+  mp_mesh(n1, n2, n3, shift, rlat1, rlat2, rlat3, k.data());
+  for (long i = 0; i < nk; ++i)
+    for (int d = 0; d < 3; ++d) kpt[i + nk * d] = k[3 * i + d];  // kpt(nk, 3) column-major
+  return WTB_OK;
+}
+
+int wtb_eigsys(int nthreads, double scs, double exc, int* nocp, const int* ffactor, double kx, double ky, double kz,
+               int w90basis, int nvec, const double* rlat, const int* rvec, const double* hop, const double* ihop,
+               double efermi, double* energias, double* autovetores) {
+  (void)nthreads;
+  (void)exc;
+  std::lock_guard<std::mutex> lock(g_default_mu);
+  if (!g_default) {
+    int r = wtb_ctx_create(&g_default, 0);
+    if (r) return r;
+  }
+  wtb_ctx* c = g_default;
+  CKR(wtb_set_hr(c, w90basis, nvec, rvec, ffactor, hop, ihop, rlat, efermi, scs, 0));
+  const double k[3] = {kx, ky, kz};
+  CKR(upload_bands(c, 1, k, 0, 0));
+  const int w = w90basis;
+  cudaError_t err;
+  std::vector<double> e(w);
+  std::vector<zd> v((size_t)w * w);
+  int cnt = 0;
+  CKC(cudaMemcpy(e.data(), c->ws.get<double>("eig_all", 0, &err), sizeof(double) * w, cudaMemcpyDeviceToHost));
+  CKC(cudaMemcpy(v.data(), c->ws.get<zd>("vec_all", 0, &err), sizeof(zd) * w * w, cudaMemcpyDeviceToHost));
+  CKC(cudaMemcpy(&cnt, c->ws.get<int>("nocp", 0, &err), sizeof(int), cudaMemcpyDeviceToHost));
+  if (cnt < w) {
+    if (nocp) *nocp = cnt;
+  } else if (nocp) {
+    // no positive eigenvalue: the reference leaves nocp as passed in and adds scs above it
+    for (int i = *nocp; i < w; ++i)
+      if (i >= 0) e[i] += scs;
+  }
+  for (int i = 0; i < w; ++i) {
+    if (energias) energias[i] = e[i];
+    if (autovetores)
+      for (int j = 0; j < w; ++j) {
+        autovetores[2 * (i + (size_t)w * j)] = v[(size_t)i * w + j].re;
+        autovetores[2 * (i + (size_t)w * j) + 1] = v[(size_t)i * w + j].im;
+      }
+  }
+  return WTB_OK;
+}
+
+int wtb_eigsys_mesh(wtb_ctx* c, int nk, const double* kpt, int nv, int nc, double* eigv, double* vector, int* nocpk) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (!c->have_hr) return set_err(c, WTB_ESTATE, "H(R) not set (call wtb_set_hr first)");
+  if (nk < 1 || !kpt || nv < 1 || nc < 1) return set_err(c, WTB_EBADARG, "bad mesh or band window");
+  if (nv + nc > c->w) return set_err(c, WTB_EBADARG, "nv + nc exceeds w90basis");
+  std::vector<double> k((size_t)nk * 3);
+  for (int i = 0; i < nk; ++i)
+    for (int d = 0; d < 3; ++d) k[3 * i + d] = kpt[i + (size_t)nk * d];
+  CKR(upload_bands(c, nk, k.data(), nv, nc));
+  const int nb = nv + nc, w = c->w;
+  cudaError_t err;
+  if (eigv) {
+    std::vector<double> e((size_t)nk * nb);
+    CKC(cudaMemcpy(e.data(), c->ws.get<double>("eig_win", 0, &err), e.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < nk; ++i)
+      for (int j = 0; j < nb; ++j) eigv[i + (size_t)nk * j] = e[(size_t)i * nb + j];
+  }
+  if (vector) {
+    std::vector<zd> v((size_t)nk * nb * w);
+    CKC(cudaMemcpy(v.data(), c->ws.get<zd>("vec_win", 0, &err), v.size() * sizeof(zd), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < nk; ++i)
+      for (int j = 0; j < nb; ++j)
+        for (int o = 0; o < w; ++o) {
+          const size_t f = (size_t)i + (size_t)nk * (j + (size_t)nb * o);
+          vector[2 * f] = v[((size_t)i * nb + j) * w + o].re;
+          vector[2 * f + 1] = v[((size_t)i * nb + j) * w + o].im;
+        }
+  }
+  if (nocpk) CKC(cudaMemcpy(nocpk, c->ws.get<int>("nocp", 0, &err), sizeof(int) * nk, cudaMemcpyDeviceToHost));
+  return WTB_OK;
+}
+
+int wtb_coulomb_table(wtb_ctx* c, const wtb_bse_params* p, int n1, const double* kpt1, int n2, const double* kpt2,
+                      double* V) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (!c->have_hr) return set_err(c, WTB_ESTATE, "lattice not set (call wtb_set_hr first)");
+  if (!p || n1 < 1 || n2 < 1 || !kpt1 || !kpt2 || !V) return set_err(c, WTB_EBADARG, "bad arguments");
+  if (p->coultype < 0 || p->coultype > 8 || p->coultype == WTB_V1DT)
+    return set_err(c, WTB_EBADARG, "Wrong Coulomb Potential");
+  std::vector<double> a((size_t)n1 * 3), b((size_t)n2 * 3);
+  for (int i = 0; i < n1; ++i)
+    for (int d = 0; d < 3; ++d) a[3 * i + d] = kpt1[i + (size_t)n1 * d];
+  for (int i = 0; i < n2; ++i)
+    for (int d = 0; d < 3; ++d) b[3 * i + d] = kpt2[i + (size_t)n2 * d];
+  cudaError_t err;
+  double* da = c->ws.get<double>("ct_a", a.size(), &err);
+  double* db = c->ws.get<double>("ct_b", b.size(), &err);
+  double* dv = c->ws.get<double>("ct_v", (size_t)n1 * n2, &err);
+  CKC(err);
+  CKC(cudaMemcpyAsync(da, a.data(), a.size() * sizeof(double), cudaMemcpyHostToDevice, c->s));
+  CKC(cudaMemcpyAsync(db, b.data(), b.size() * sizeof(double), cudaMemcpyHostToDevice, c->s));
+  // V(i,j) column-major = row-major table of (kpt2, kpt1); every potential depends on k1 - k2 through
+  // even functions, so V is symmetric under the swap
+  CKC(launch_coulomb(coul_of(c, p), db, n2, da, n1, dv, n1, c->s));
+  CKC(cudaMemcpyAsync(V, dv, sizeof(double) * n1 * n2, cudaMemcpyDeviceToHost, c->s));
+  return check_status(c);
+}
+
+static int ensure_bands_for(wtb_ctx* c, const wtb_bse_params* p) {
+  const int nk = p->ngrid[0] * p->ngrid[1] * p->ngrid[2];
+  std::vector<double> k((size_t)nk * 3);
+  mp_mesh(p->ngrid[0], p->ngrid[1], p->ngrid[2], p->mshift, c->rlat_rm, c->rlat_rm + 3, c->rlat_rm + 6, k.data());
+  CKR(upload_bands(c, nk, k.data(), p->nv, p->nc));
+  for (int d = 0; d < 3; ++d) c->ngrid[d] = p->ngrid[d];
+  return WTB_OK;
+}
+
+static int compute_optics(wtb_ctx* c, const wtb_bse_params* p) {
+  cudaError_t err;
+  const int dim = c->nk * c->nc * c->nv;
+  zd* hout = c->ws.get<zd>("hrvel", (size_t)5 * dim, &err);
+  CKC(err);
+  CKC(launch_optics(c->ws.get<zd>("hr", 0, &err), c->ws.get<int>("rvec", 0, &err), c->ws.get<int>("ndegen", 0, &err),
+                    c->nR, c->w, c->ws.get<double>("rlat", 0, &err), c->ws.get<double>("kpt", 0, &err), c->nk, c->nv,
+                    c->nc, c->ws.get<double>("eig_win", 0, &err), c->ws.get<zd>("vec_win", 0, &err), p->cshift, hout,
+                    c->s));
+  c->have_hr_optics = true;
+  return WTB_OK;
+}
+
+int wtb_optsp(wtb_ctx* c, const wtb_bse_params* p, double* hr) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (!c->have_bands) return set_err(c, WTB_ESTATE, "no bands (call wtb_eigsys_mesh or wtb_bsesolver first)");
+  if (!p) return set_err(c, WTB_EBADARG, "params is NULL");
+  CKR(compute_optics(c, p));
+  const int dim = c->nk * c->nc * c->nv;
+  cudaError_t err;
+  if (hr)
+    CKC(cudaMemcpyAsync(hr, c->ws.get<zd>("hrvel", 0, &err), sizeof(zd) * 5 * dim, cudaMemcpyDeviceToHost, c->s));
+  return check_status(c);
+}
+
+int wtb_bse_build(wtb_ctx* c, const wtb_bse_params* p, double* hbse) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (!c->have_bands) return set_err(c, WTB_ESTATE, "no bands (call wtb_eigsys_mesh first)");
+  if (!p) return set_err(c, WTB_EBADARG, "params is NULL");
+  if (p->coultype < 0 || p->coultype > 8 || p->coultype == WTB_V1DT)
+    return set_err(c, WTB_EBADARG, "Wrong Coulomb Potential");
+  if (!(p->ktol > 0.0)) return set_err(c, WTB_EBADARG, "KTOL must be > 0");
+  if (p->precision != WTB_PREC_FP64 && p->precision != WTB_PREC_FP32)
+    return set_err(c, WTB_EBADARG, "the dense build stores FP64 or FP32");
+  const int nk = c->nk, nv = c->nv, nc = c->nc, w = c->w;
+  const long dim = (long)nk * nc * nv;
+  cudaError_t err;
+  double* dE = c->ws.get<double>("dE", dim, &err);
+  CKC(err);
+  CKC(launch_transition_energies(c->ws.get<double>("eig_win", 0, &err), nk, nv, nc, dE, c->s));
+  const int Kpad = (nk + 63) / 64 * 64;
+  double* V = c->ws.get<double>("V", (size_t)((nk + 127) / 128 * 128) * Kpad, &err, true);
+  CKC(err);
+  const double* kd = c->ws.get<double>("kpt", 0, &err);
+  CKC(launch_coulomb(coul_of(c, p), kd, nk, kd, nk, V, Kpad, c->s));
+  const zd* vw = c->ws.get<zd>("vec_win", 0, &err);
+  zd* staging = nullptr;
+  if (p->precision == WTB_PREC_FP64) {
+    zd* H = c->ws.get<zd>("H64", (size_t)dim * dim, &err);
+    CKC(err);
+    CKC(launch_bse_build<double>(vw, dE, V, Kpad, nk, nv, nc, w, H, c->s));
+    if (hbse) {
+      staging = c->ws.get<zd>("Hout", (size_t)dim * dim, &err);
+      CKC(err);
+      conj_convert_kernel<double><<<(unsigned)((dim * dim + 255) / 256), 256, 0, c->s>>>(H, dim * dim, staging); ++g_launch_count;
+    }
+  } else {
+    zf* H = c->ws.get<zf>("H32", (size_t)dim * dim, &err);
+    CKC(err);
+    CKC(launch_bse_build<float>(vw, dE, V, Kpad, nk, nv, nc, w, H, c->s));
+    if (hbse) {
+      staging = c->ws.get<zd>("Hout", (size_t)dim * dim, &err);
+      CKC(err);
+      conj_convert_kernel<float><<<(unsigned)((dim * dim + 255) / 256), 256, 0, c->s>>>(H, dim * dim, staging); ++g_launch_count;
+    }
+  }
+  CKC(cudaGetLastError());
+  if (hbse) CKC(cudaMemcpyAsync(hbse, staging, sizeof(zd) * dim * dim, cudaMemcpyDeviceToHost, c->s));
+  return check_status(c);
+}
+
+int wtb_slepc_solver(wtb_ctx* c, const double* HX, double* EX, double* HE, int NX, int NE) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (!HX || NX < 1 || NE < 1 || NE > NX) return set_err(c, WTB_EBADARG, "bad matrix size or NE");
+  cudaError_t err;
+  const long n2 = (long)NX * NX;
+  zd* H = c->ws.get<zd>("slepc_H", n2, &err);
+  double* d = c->ws.get<double>("slepc_d", NX, &err);
+  zd* X = c->ws.get<zd>("slepc_X", (size_t)NX * NE, &err);
+  zd* HEd = c->ws.get<zd>("slepc_HE", (size_t)NX * NE, &err);
+  CKC(err);
+  CKC(cudaMemcpyAsync(H, HX, sizeof(zd) * n2, cudaMemcpyHostToDevice, c->s));
+  // column-major HX read row-major is H^T = conj(H)
+  conj_inplace_kernel<<<(unsigned)((n2 + 255) / 256), 256, 0, c->s>>>(H, n2); ++g_launch_count;
+  diag_real_kernel<<<(NX + 255) / 256, 256, 0, c->s>>>(H, NX, d); ++g_launch_count;
+  CKC(cudaGetLastError());
+  DenseOperator<double> op;
+  op.H = H;
+  op.dim = NX;
+  wtb_bse_params p{};
+  p.nev = NE;
+  const int m = auto_block(&p, NX, true);
+  std::vector<double> E;
+  SolveStats stats;
+  std::string msg;
+  int rc = lobpcg_solve<double>(op, d, NX, NE, m, 1e-8, 200, c->ws, c->st, c->s, &E, X, &stats, &msg);
+  if (rc != WTB_OK) return set_err(c, rc, msg);
+  for (int i = 0; i < NE; ++i)
+    if (EX) EX[i] = E[i];
+  if (HE) {
+    transpose_z_kernel<<<(unsigned)(((long)NX * NE + 255) / 256), 256, 0, c->s>>>(X, NX, NE, NE, HEd, 0); ++g_launch_count;
+    CKC(cudaGetLastError());
+    CKC(cudaMemcpyAsync(HE, HEd, sizeof(zd) * NX * NE, cudaMemcpyDeviceToHost, c->s));
+  }
+  return check_status(c);
+}
+
+int wtb_dielbse(wtb_ctx* c, int dimse, int dimse1, const double* excitonvec, const double* hopt1, const double* hopt2,
+                int pair, double* activity) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (dimse < 1 || dimse1 < 0 || dimse1 > dimse || !excitonvec || !hopt1 || (pair && !hopt2) || !activity)
+    return set_err(c, WTB_EBADARG, "bad arguments");
+  cudaError_t err;
+  zd* A = c->ws.get<zd>("db_A", (size_t)dimse * std::max(dimse1, 1), &err);
+  zd* h1 = c->ws.get<zd>("db_h1", dimse, &err);
+  zd* h2 = c->ws.get<zd>("db_h2", dimse, &err);
+  double* act = c->ws.get<double>("db_act", dimse, &err, true);
+  CKC(err);
+  CKC(cudaMemcpyAsync(A, excitonvec, sizeof(zd) * dimse * dimse1, cudaMemcpyHostToDevice, c->s));
+  CKC(cudaMemcpyAsync(h1, hopt1, sizeof(zd) * dimse, cudaMemcpyHostToDevice, c->s));
+  if (pair) CKC(cudaMemcpyAsync(h2, hopt2, sizeof(zd) * dimse, cudaMemcpyHostToDevice, c->s));
+  if (dimse1 > 0) {
+    dielbse_kernel<<<dimse1, 256, 0, c->s>>>(A, dimse, h1, h2, pair, act); ++g_launch_count;
+    CKC(cudaGetLastError());
+  }
+  CKC(cudaMemcpyAsync(activity, act, sizeof(double) * dimse, cudaMemcpyDeviceToHost, c->s));
+  return check_status(c);
+}
+
+int wtb_bsesolver(wtb_ctx* c, const wtb_bse_params* p, double* Ws, double* acts, double* HE, wtb_timings* t) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (!c->have_hr) return set_err(c, WTB_ESTATE, "H(R) not set (call wtb_set_hr first)");
+  CKR(validate_params(c, p));
+  if (p->nv + p->nc > c->w) return set_err(c, WTB_EBADARG, "nv + nc exceeds w90basis");
+  const long dim = (long)p->ngrid[0] * p->ngrid[1] * p->ngrid[2] * p->nc * p->nv;
+  if (p->nev < 1 || p->nev > dim) return set_err(c, WTB_EBADARG, "nev must be between 1 and the BSE dimension");
+  cudaEvent_t e0, e1, e2;
+  CKC(cudaEventCreate(&e0));
+  CKC(cudaEventCreate(&e1));
+  CKC(cudaEventCreate(&e2));
+  CKC(cudaEventRecord(e0, c->s));
+  CKR(ensure_bands_for(c, p));
+  CKR(compute_optics(c, p));
+  CKC(cudaEventRecord(e1, c->s));
+  std::vector<double> E;
+  SolveStats stats;
+  wtb_timings tt{};
+  CKR(run_solve(c, p, &E, &tt, &stats));
+  cudaError_t err;
+  const int nev = p->nev;
+  double* osc = c->ws.get<double>("osc", (size_t)8 * nev, &err);
+  double* part = c->ws.get<double>("osc_part", (size_t)((dim + 255) / 256) * nev * 10, &err);
+  CKC(err);
+  cudaEvent_t e3;
+  CKC(cudaEventCreate(&e3));
+  CKC(cudaEventRecord(e3, c->s));
+  CKC(launch_oscillators(c->ws.get<zd>("Xout", 0, &err), nev, nev, (int)dim, c->ws.get<zd>("hrvel", 0, &err), osc, part,
+                         (int)((dim + 255) / 256), c->s));
+  if (acts) {
+    double* dacts = c->ws.get<double>("acts", (size_t)dim * 8, &err);
+    CKC(err);
+    expand_acts_kernel<<<(unsigned)((dim * 8 + 255) / 256), 256, 0, c->s>>>(osc, nev, (int)dim, dacts); ++g_launch_count;
+    CKC(cudaMemcpyAsync(acts, dacts, sizeof(double) * dim * 8, cudaMemcpyDeviceToHost, c->s));
+  }
+  if (HE) {
+    zd* staging = c->ws.get<zd>("HEout", (size_t)dim * nev, &err);
+    CKC(err);
+    transpose_z_kernel<<<(unsigned)((dim * nev + 255) / 256), 256, 0, c->s>>>(c->ws.get<zd>("Xout", 0, &err), (int)dim,
+                                                                            nev, nev, staging, 0); ++g_launch_count;
+    CKC(cudaMemcpyAsync(HE, staging, sizeof(zd) * dim * nev, cudaMemcpyDeviceToHost, c->s));
+  }
+  CKC(cudaEventRecord(e2, c->s));
+  CKC(cudaEventSynchronize(e2));
+  if (Ws) {
+    for (long i = 0; i < dim; ++i) Ws[i] = 0.0;
+    for (int i = 0; i < nev; ++i) Ws[i] = E[i];
+  }
+  if (t) {
+    float a = 0, b = 0, d = 0;
+    cudaEventElapsedTime(&a, e0, e1);
+    cudaEventElapsedTime(&b, e0, e2);
+    cudaEventElapsedTime(&d, e3, e2);
+    *t = tt;
+    t->t_bands_ms = a;
+    t->t_optics_ms = d;
+    t->t_total_ms = b;
+    t->iterations = stats.iterations;
+    t->matvec_columns = (int)stats.matvec_columns;
+    t->max_rel_residual = stats.max_rel_residual;
+    t->refine_shift_max = stats.refine_shift_max;
+    t->kernel_launches = (int)g_launch_count;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  cudaEventDestroy(e3);
+  return check_status(c);
+}
+
+int wtb_bsedielraw(wtb_ctx* c, const wtb_bse_params* p, int dimse, const double* Ws, const double* acts,
+                   double* dielf) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (!c->have_hr) return set_err(c, WTB_ESTATE, "lattice not set (call wtb_set_hr first)");
+  if (!p || dimse < 1 || !Ws || !acts || !dielf || p->numbse < 2) return set_err(c, WTB_EBADARG, "bad arguments");
+  cudaError_t err;
+  double* dW = c->ws.get<double>("sp_W", dimse, &err);
+  double* df = c->ws.get<double>("sp_f", (size_t)6 * dimse, &err);
+  double* dd = c->ws.get<double>("sp_d", (size_t)18 * p->numbse, &err);
+  double* dp = c->ws.get<double>("sp_p", 16, &err);
+  CKC(err);
+  CKC(cudaMemcpyAsync(dW, Ws, sizeof(double) * dimse, cudaMemcpyHostToDevice, c->s));
+  CKC(cudaMemcpyAsync(df, acts, sizeof(double) * 6 * dimse, cudaMemcpyHostToDevice, c->s));
+  const int ng = p->ngrid[0] * p->ngrid[1] * p->ngrid[2];
+  CKC(launch_spectrum(dW, dimse, df, p->cshift, vcell3D(c->rlat_rm), ng, p->ebse0, p->ebsef, p->numbse, p->renorm,
+                      c->systype_np ? 2.0 : 1.0, dd, dp, 1, c->s));
+  CKC(cudaMemcpyAsync(dielf, dd, sizeof(double) * 18 * p->numbse, cudaMemcpyDeviceToHost, c->s));
+  return check_status(c);
+}
+
+int wtb_bseoptprop(wtb_ctx* c, int numbse, const double* dielf, double* props) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (numbse < 1 || !dielf || !props) return set_err(c, WTB_EBADARG, "bad arguments");
+  cudaError_t err;
+  double* dd = c->ws.get<double>("op_d", (size_t)18 * numbse, &err);
+  double* dp = c->ws.get<double>("op_p", (size_t)30 * numbse, &err);
+  CKC(err);
+  CKC(cudaMemcpyAsync(dd, dielf, sizeof(double) * 18 * numbse, cudaMemcpyHostToDevice, c->s));
+  CKC(launch_optprops(dd, numbse, dp, c->s));
+  CKC(cudaMemcpyAsync(props, dp, sizeof(double) * 30 * numbse, cudaMemcpyDeviceToHost, c->s));
+  return check_status(c);
+}
+
+int wtb_bse_matvec(wtb_ctx* c, const wtb_bse_params* p, int ncol, const double* X, double* Y) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (!c->have_bands) return set_err(c, WTB_ESTATE, "no bands (call wtb_eigsys_mesh or wtb_bsesolver first)");
+  if (!p || ncol < 1 || ncol > 32 || !X || !Y) return set_err(c, WTB_EBADARG, "bad arguments (1 <= ncol <= 32)");
+  if (p->precision < 0 || p->precision > 3 || p->op < 0 || p->op > 1)
+    return set_err(c, WTB_EBADARG, "unknown precision or operator mode");
+  if (p->op == WTB_OP_DENSE && p->precision >= WTB_PREC_BF16X3)
+    return set_err(c, WTB_EBADARG, "split-BF16 precision is available for the matrix-free operator only");
+  if (!(p->ktol > 0.0)) return set_err(c, WTB_EBADARG, "KTOL must be > 0");
+  const int dim = c->nk * c->nc * c->nv;
+  cudaError_t err;
+  zd* xc = c->ws.get<zd>("mv_xc", (size_t)dim * ncol, &err);
+  zd* x64 = c->ws.get<zd>("mv_x64", (size_t)dim * ncol, &err);
+  zd* y64 = c->ws.get<zd>("mv_y64", (size_t)dim * ncol, &err);
+  zf* x32 = c->ws.get<zf>("mv_x32", (size_t)dim * ncol, &err);
+  zf* y32 = c->ws.get<zf>("mv_y32", (size_t)dim * ncol, &err);
+  CKC(err);
+  OpBundle ob;
+  CKR(make_operator(c, p, std::min(ncol, 16), &ob));
+  CKC(cudaMemcpyAsync(xc, X, sizeof(zd) * dim * ncol, cudaMemcpyHostToDevice, c->s));
+  const unsigned nbk = (unsigned)(((long)dim * ncol + 255) / 256);
+  // column-major X (dim x ncol) seen as row-major X^T (ncol x dim) -> row-major X
+  transpose_z_kernel<<<nbk, 256, 0, c->s>>>(xc, ncol, dim, dim, x64, 0); ++g_launch_count;
+  if (ob.o64) {
+    CKC(ob.o64->apply(x64, ncol, 0, ncol, y64, ncol, c->s));
+  } else {
+    CKC((launch_convert_cols<double, float>(x64, ncol, x32, ncol, ncol, dim, c->s)));
+    CKC(ob.o32->apply(x32, ncol, 0, ncol, y32, ncol, c->s));
+    CKC((launch_convert_cols<float, double>(y32, ncol, y64, ncol, ncol, dim, c->s)));
+  }
+  transpose_z_kernel<<<nbk, 256, 0, c->s>>>(y64, dim, ncol, ncol, xc, 0); ++g_launch_count;
+  CKC(cudaGetLastError());
+  CKC(cudaMemcpyAsync(Y, xc, sizeof(zd) * dim * ncol, cudaMemcpyDeviceToHost, c->s));
+  return check_status(c);
+}
+
+long long wtb_kernel_launch_count(void) { return g_launch_count; }
+
+void* wtb_ctx_stream(wtb_ctx* c) { return c ? (void*)c->s : nullptr; }
+
+int wtb_profile_enable(wtb_ctx* c, int on) {
+  if (!c) return WTB_EBADARG;
+  c->prof.reset();
+  c->prof.on = on != 0;
+  return WTB_OK;
+}
+
+int wtb_profile_read(wtb_ctx* c, double* total_ms, long long* launches, double* flops, double* bytes) {
+  if (!c) return WTB_EBADARG;
+  c->prof.flush();
+  if (total_ms) *total_ms = c->prof.total_ms;
+  if (launches) *launches = c->prof.launches;
+  if (flops) *flops = c->prof.flops;
+  if (bytes) *bytes = c->prof.bytes;
+  return WTB_OK;
+}
+
+}  // extern "C"
