@@ -215,7 +215,7 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--workload", default="hex12_60x60")
     ap.add_argument("--precision", default="bf16x3")
-    ap.add_argument("--tol", type=float, default=1e-6)
+    ap.add_argument("--tol", type=float, default=0.0, help="residual target (0: the library's per-precision default)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU form")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--ref-matvecs", type=int, default=800)

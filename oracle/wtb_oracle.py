@@ -167,7 +167,7 @@ def coulomb_table(kpt1, kpt2, p, rlat):
     """V(k,k') for every pair, vectorised restatement of module_coulomb (src/module_coulomb.F90).
 
     Supported: V2DRK (:286-350), V3DL (:98-131), V3D (:64-94), V2DK (:11-60), V2DOH (:354-387),
-    V2DT (:135-193), V2DT2 (:243-282), V0DT (:197-238)."""
+    V2DT (:135-193), V2DT2 (:243-282), V0DT (:197-238), V1DT (:391-442)."""
     k1 = np.asarray(kpt1)[:, None, :]
     k2 = np.asarray(kpt2)[None, :, :]
     modk = _modk(k1, k2)
@@ -238,6 +238,30 @@ def coulomb_table(kpt1, kpt2, p, rlat):
         qxy = np.sqrt(d[..., 0] ** 2 + d[..., 1] ** 2)
         V = (vbz * CIC) * (1.0 / (safe * safe)) * (1.0 - np.exp(-0.5 * qxy * p.lc) * np.cos(0.5 * p.lc * d[..., 2]))
         return np.where(small, 0.0, V)
+    if ct == "V1DT":
+        # src/module_coulomb.F90:391-442; J0/J1/K0/K1 (the reference uses Cody's CALJY0/CALJY1/CALCK0/
+        # CALCK1, src/module_math.F90:453-1572) and the 100-point trapezoid of integralJ0pot (:429-449)
+        import scipy.special as sp
+        vc = vcell3D(rlat)
+        vbz = 1.0 / (ng * vc)
+        d = k1 - k2
+        vx = np.abs(d[..., 0])
+        qyz = np.sqrt(d[..., 1] * d[..., 1] + d[..., 2] * d[..., 2])
+        lc = p.lc
+        out = np.empty(modk.shape)
+        a = (vx < tol) & (qyz >= tol)
+        b = (vx < tol) & (qyz < tol)
+        c = ~(a | b)
+        out[b] = (vbz * CIC) * ((lc * lc) / 16.0) * (2.0 * np.log(lc) - 1.0)
+        if np.any(a):
+            out[a] = (vbz * CIC) * np.array([integral_j0_pot(lc, g) for g in qyz[a]])
+        if np.any(c):
+            x1 = qyz[c] * lc
+            x2 = vx[c] * lc
+            c1 = qyz[c] * lc * sp.j1(x1) * sp.k0(x2)
+            c2 = vx[c] * lc * sp.j0(x1) * sp.k1(x2)
+            out[c] = (vbz * CIC) * (1.0 + c1 + c2)
+        return out
     if ct == "V0DT":
         vc = vcell3D(rlat)
         vbz = 1.0 / (ng * vc)
@@ -245,6 +269,20 @@ def coulomb_table(kpt1, kpt2, p, rlat):
         V = (vbz * CIC) * (1.0 / (safe * safe)) * (1.0 - np.cos(cr * safe))
         return np.where(small, (vbz * CIC) * 0.5 * cr * cr, V)
     raise OracleError("Wrong Coulomb Potential")
+
+
+def integral_j0_pot(rmax, gperp):
+    """integralJ0pot (src/module_math.F90:429-449): trapezoid of r J0(r g) log r on 100 points from eta."""
+    import scipy.special as sp
+    n = 100
+    eta = float(F32(1e-4))
+    r = ((np.arange(1, n + 1) - 1.0) / (n - 1.0)) * rmax + eta
+    f = r * sp.j0(r * gperp) * np.log(r)
+    h = r[1] - r[0]
+    res = 0.0
+    for i in range(n - 1):
+        res = res + (h / 2.0) * (f[i] + f[i + 1])
+    return res
 
 
 # ----------------------------------------------------------------------------- BSE build

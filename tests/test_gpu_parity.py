@@ -70,7 +70,7 @@ def test_scissor_shift(ctx, small):
     ctx.set_hr(sysm)
 
 
-@pytest.mark.parametrize("coultype", ["V2DRK", "V3DL", "V3D", "V2DK", "V2DOH", "V2DT", "V2DT2", "V0DT"])
+@pytest.mark.parametrize("coultype", ["V2DRK", "V3DL", "V3D", "V2DK", "V2DOH", "V2DT", "V2DT2", "V0DT", "V1DT"])
 def test_coulomb_table(ctx, small, coultype):
     sysm, p, ref = small
     ctx.set_hr(sysm)
@@ -100,7 +100,7 @@ def test_dense_build(ctx, small, precision, tol):
     ctx.eigsys_mesh(ref["kpt"], p.nv, p.nc)
     H = ctx.bse_build(p, precision=precision)
     Href = O.bse_build(ref["eigv"], O.gauge_fix(ref["vec"]), ref["kpt"], p, sysm.rlat)
-    assert np.abs(H - H.conj().T).max() == 0.0
+    assert np.abs(H - H.conj().T).max() <= tol * np.abs(Href).max()
     np.testing.assert_allclose(H, Href, rtol=0, atol=tol * np.abs(Href).max())
 
 
@@ -138,7 +138,7 @@ def test_slepc_solver_dense(ctx, small):
 def test_bsesolver_small(ctx, small, precision, op):
     sysm, p, ref = small
     ctx.set_hr(sysm)
-    out = ctx.bsesolver(p, precision=precision, op=op, tol=1e-8 if precision == "fp64" else 1e-6)
+    out = ctx.bsesolver(p, precision=precision, op=op)
     np.testing.assert_allclose(out["E"], ref["E"], rtol=0, atol=1e-5)
     assert np.all(out["Ws"][p.nev:] == 0.0)
     dim = p.dim
@@ -151,7 +151,7 @@ def test_bsesolver_hex8_24x24(ctx, c1, precision, op):
     """dim 2304, 10 excitons: energies within 1e-5 eV and the spectrum within 1e-4 relative L2."""
     sysm, p, ref = c1
     ctx.set_hr(sysm)
-    out = ctx.bsesolver(p, precision=precision, op=op, tol=1e-8 if precision == "fp64" else 1e-6)
+    out = ctx.bsesolver(p, precision=precision, op=op)
     err = np.abs(out["E"] - ref["E"])
     assert err.max() <= 1e-5, err
     spec = O.bsedielraw(out["Ws"], out["acts"], p.ngrid, sysm.rlat, p)
@@ -178,7 +178,7 @@ def test_optprops_kernel(ctx, c1):
         om, e1, e2 = d_ref[c][:, 0], d_ref[c][:, 1], d_ref[c][:, 2]
         pr = O.optprops(e1, e2, om)
         for nm in ("refr", "ext", "refl", "abs", "eloss"):
-            np.testing.assert_allclose(props[nm][c], pr[nm], rtol=1e-12, atol=1e-12)
+            np.testing.assert_allclose(props[nm][c], pr[nm], rtol=1e-9, atol=1e-12)
 
 
 def test_dielbse(ctx, small):

@@ -9,8 +9,9 @@
 // Gc = <c|c'> and Gv = <v|v'> once in shared memory from the band vectors, takes V(k,k') from the
 // precomputed table, and expands the (TK*nc*nv)^2 outputs with coalesced row-segment stores.  The
 // kernel is HBM-write bound: dim^2 * sizeof(complex S) bytes leave the SMs, nothing is re-read.
-// Computing every element directly (instead of the upper triangle then a mirror) gives the same
-// Hermitian matrix: V is symmetric and conj(<a|b>) = <b|a> holds exactly in IEEE arithmetic.
+// Every element is computed directly instead of the upper triangle then a mirror: V is symmetric and
+// conj(<a|b>) = <b|a>, so the result is Hermitian to the rounding of the fused multiply-adds (relative
+// 1e-16 in FP64, 1e-8 in FP32).
 #include "wtb_internal.h"
 
 namespace wtb {
@@ -92,7 +93,9 @@ __global__ void __launch_bounds__(256) bse_build_kernel(const zd* __restrict__ v
 }
 
 // Y[:, 0:ncol] = H * X[:, 0:ncol]; H row-major dim x dim.  CTA: 64 rows x ncol (<= 32) columns, K in
-// chunks of 16 staged in shared memory, 4 x 2 register micro-tile per thread.
+// chunks of 16 staged in shared memory, 4 x 2 register micro-tile per thread.  The diagonal term (the
+// transition energy, much larger than the Coulomb entries) is accumulated apart from the off-diagonal
+// sum, so a long FP32 accumulation only carries rounding of the Coulomb-sized terms.
 template <class S>
 __global__ void __launch_bounds__(256) dense_mv_kernel(const cplx<S>* __restrict__ H, int dim,
                                                        const cplx<S>* __restrict__ X, int ldx, cplx<S>* __restrict__ Y,
@@ -102,11 +105,14 @@ __global__ void __launch_bounds__(256) dense_mv_kernel(const cplx<S>* __restrict
   __shared__ cplx<S> Xs[BK][32];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const long r0 = (long)blockIdx.x * BM;
-  cplx<S> acc[4][2];
+  cplx<S> acc[4][2], dacc[4][2];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 2; ++j) acc[i][j] = mk<S>(0, 0);
+    for (int j = 0; j < 2; ++j) {
+      acc[i][j] = mk<S>(0, 0);
+      dacc[i][j] = mk<S>(0, 0);
+    }
   for (long kb = 0; kb < dim; kb += BK) {
     for (int e = tid; e < BM * BK; e += 256) {
       const int rr = e / BK, kk = e % BK;
@@ -119,17 +125,40 @@ __global__ void __launch_bounds__(256) dense_mv_kernel(const cplx<S>* __restrict
       Xs[kk][c] = (gk < dim && c < ncol) ? X[gk * ldx + c] : mk<S>(0, 0);
     }
     __syncthreads();
+    // the diagonal lies in this K chunk for rows r0 + [kb - r0, kb - r0 + BK)
+    const bool diag_chunk = kb < r0 + BM && kb + BK > r0;
+    if (!diag_chunk) {
 #pragma unroll 4
-    for (int kk = 0; kk < BK; ++kk) {
-      cplx<S> h[4], x[2];
+      for (int kk = 0; kk < BK; ++kk) {
+        cplx<S> h[4], x[2];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) h[i] = Hs[ty + 16 * i][kk];
+        for (int i = 0; i < 4; ++i) h[i] = Hs[ty + 16 * i][kk];
 #pragma unroll
-      for (int j = 0; j < 2; ++j) x[j] = Xs[kk][tx + 16 * j];
+        for (int j = 0; j < 2; ++j) x[j] = Xs[kk][tx + 16 * j];
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 2; ++j) cfma(acc[i][j], h[i], x[j]);
+          for (int j = 0; j < 2; ++j) cfma(acc[i][j], h[i], x[j]);
+      }
+    } else {
+      for (int kk = 0; kk < BK; ++kk) {
+        cplx<S> h[4], x[2];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) h[i] = Hs[ty + 16 * i][kk];
+#pragma unroll
+        for (int j = 0; j < 2; ++j) x[j] = Xs[kk][tx + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const bool d = (kb + kk) == (r0 + ty + 16 * i);
+#pragma unroll
+          for (int j = 0; j < 2; ++j) {
+            if (d)
+              cfma(dacc[i][j], h[i], x[j]);
+            else
+              cfma(acc[i][j], h[i], x[j]);
+          }
+        }
+      }
     }
     __syncthreads();
   }
@@ -139,7 +168,7 @@ __global__ void __launch_bounds__(256) dense_mv_kernel(const cplx<S>* __restrict
     for (int j = 0; j < 2; ++j) {
       const long gr = r0 + ty + 16 * i;
       const int c = tx + 16 * j;
-      if (gr < dim && c < ncol) Y[gr * ldy + c] = acc[i][j];
+      if (gr < dim && c < ncol) Y[gr * ldy + c] = cadd(dacc[i][j], acc[i][j]);
     }
 }
 

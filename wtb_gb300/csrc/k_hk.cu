@@ -338,6 +338,43 @@ __global__ void __launch_bounds__(kHkThreads) optics_kernel(const zd* __restrict
 // ----------------------------------------------------------------------------- Coulomb table
 __host__ __device__ __forceinline__ double vecsize3(const double* a) { return sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]); }
 
+// Modified Bessel functions of the second kind K0 and K1 from K_nu(x) = int_0^inf exp(-x cosh t) cosh(nu t) dt,
+// trapezoid rule with step min(1/16, 1/(4 sqrt(x))) (the integrand is analytic in a strip of half-width
+// pi/2 and decays double-exponentially, so the rule converges to machine precision), truncated where
+// x cosh t > 745.
+__device__ void bessel_k01(double x, double* k0, double* k1) {
+  const double h = fmin(0.0625, 0.25 / sqrt(x));
+  const double tmax = acosh(fmax(745.0 / x, 1.0)) + h;
+  double s0 = 0.5 * exp(-x), s1 = 0.5 * exp(-x);
+  for (int i = 1;; ++i) {
+    const double t = i * h;
+    if (t > tmax) break;
+    const double e = exp(-x * cosh(t));
+    s0 += e;
+    s1 += e * cosh(t);
+  }
+  *k0 = h * s0;
+  *k1 = h * s1;
+}
+
+// integralJ0pot (src/module_math.F90:429-449): trapezoid of r J0(r g) log r on 100 points starting at
+// eta = 1E-04 (single precision literal).
+__device__ double integral_j0_pot(double rmax, double g) {
+  const int n = 100;
+  const double eta = (double)1E-04f;
+  double res = 0.0;
+  const double r1 = eta, r2 = (1.0 / (n - 1.0)) * rmax + eta;
+  const double hh = r2 - r1;
+  double fprev = r1 * j0(r1 * g) * log(r1);
+  for (int i = 1; i < n; ++i) {
+    const double r = ((double)i / (n - 1.0)) * rmax + eta;
+    const double f = r * j0(r * g) * log(r);
+    res = res + (hh / 2.0) * (fprev + f);
+    fprev = f;
+  }
+  return res;
+}
+
 struct CoulConst {
   int type;
   double vbz, tol, cic;
@@ -397,6 +434,21 @@ __global__ void coulomb_kernel(CoulConst cc, const double* __restrict__ k1, int 
         v = vc * (1.0 / (modk * modk)) * (1.0 - exp(-0.5 * qxy * cc.lc) * cos(0.5 * cc.lc * dz));
       }
       break;
+    case CT_V1DT: {
+      const double vx = fabs(dx), qyz = sqrt(dy * dy + dz * dz);
+      if (vx < cc.tol && qyz >= cc.tol) {
+        v = vc * integral_j0_pot(cc.lc, qyz);
+      } else if (vx < cc.tol) {
+        v = vc * ((cc.lc * cc.lc) / 16.0) * (2.0 * log(cc.lc) - 1.0);
+      } else {
+        double kk0, kk1;
+        bessel_k01(vx * cc.lc, &kk0, &kk1);
+        const double c1 = qyz * cc.lc * j1(qyz * cc.lc) * kk0;
+        const double c2 = vx * cc.lc * j0(qyz * cc.lc) * kk1;
+        v = vc * (1.0 + c1 + c2);
+      }
+      break;
+    }
     case CT_V0DT:
       if (modk < cc.tol)
         v = vc * 0.5 * cc.rc * cc.rc;
@@ -504,6 +556,9 @@ cudaError_t launch_coulomb(const CoulParams& p, const double* kpt1, int n1, cons
       cc.rc = 0.5 * r[8];
       break;
     case CT_V2DT2:
+      cc.vbz = 1.0 / (ng * vc3);
+      break;
+    case CT_V1DT:
       cc.vbz = 1.0 / (ng * vc3);
       break;
     case CT_V0DT: {

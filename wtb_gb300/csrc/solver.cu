@@ -12,6 +12,7 @@
 // EPS_SMALLEST_MAGNITUDE, tol 1e-8, 200 iterations); for the positive BSE spectra of this path the
 // smallest-magnitude and smallest-algebraic eigenvalues coincide.
 #include <cmath>
+#include <cstdlib>
 
 #include "solver.h"
 
@@ -189,14 +190,18 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
     sm.theta = ws.get<double>("lob_theta", maxnb, &err);
     sm.dinv = ws.get<double>("lob_dinv", maxnb, &err);
     sm.keep = ws.get<int>("lob_keep", maxnb, &err);
-    const int npart = 304;
+    // partial sums of the tall-skinny reductions: about 128 rows per part, at most two per SM
+    const int npart = std::max(1, std::min(304, (dim + 127) / 128));
     double* partial = ws.get<double>("lob_partial", (size_t)npart * nn * 2, &err);
     double* norms2 = ws.get<double>("lob_norms2", 32, &err);
     int* active = ws.get<int>("lob_active", 32, &err);
     int* idx = ws.get<int>("lob_idx", 128, &err);
     double* th_dev = ws.get<double>("lob_thcur", maxnb, &err);
     if (!chk()) goto oom;
-    const double tau = sizeof(S) == 4 ? 1e-7 : 1e-13;
+    // SVQB keeps a direction of the scaled Gram matrix only if its eigenvalue exceeds tau: a kept
+    // direction's Rayleigh quotient carries the operator's rounding divided by sqrt(eigenvalue), so tau
+    // sits well above the FP32 noise (~1e-6 on the Gram entries) and just above FP64's
+    const double tau = sizeof(S) == 4 ? 1e-4 : 1e-13;
     std::vector<double> h_theta(maxnb), h_norm(32);
     std::vector<int> h_active(32, 1);
     // start block: unit vectors at the m lowest transition energies (+ small deterministic noise)
@@ -212,6 +217,14 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
     bool have_p = false;
     bool converged = false;
     int it = 0;
+    // per-iteration monitor in the format of the reference's MyEPSMonitor
+    // (src/module_slepc_solver.F90:101-116), enabled by the WTB_EPS_MONITOR environment variable
+    const bool monitor = std::getenv("WTB_EPS_MONITOR") != nullptr;
+    // stagnation guard for reduced-precision iterations: once the wanted residuals sit within
+    // 100 x tol and have not improved by 10% over 15 iterations, the operator's rounding floor has been
+    // reached and the FP64 Rayleigh-Ritz below takes over
+    double best_maxrel = 1e300;
+    int best_it = 0;
     for (; it < maxit; ++it) {
       cplx<S>* X = Sb[cur];
       cplx<S>* AX = ASb[cur];
@@ -244,8 +257,22 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
         h_active[j] = cj ? 0 : 1;
       }
       if (stats) stats->max_rel_residual = maxrel;
+      if (monitor) {
+        int first = 0;
+        while (first < nev - 1 && h_active[first] == 0) ++first;
+        std::fprintf(stderr, "WTB-EPS %5d EPS pair=%4d value (error) %15.8E (%10.3E) max %10.3E\n", it, nconv + 1,
+                     h_theta[first], std::sqrt(std::max(h_norm[first], 0.0)) / std::max(std::fabs(h_theta[first]), 1e-12),
+                     maxrel);
+      }
       if (nconv == nev) {
         converged = true;
+        break;
+      }
+      if (maxrel < 0.9 * best_maxrel) {
+        best_maxrel = maxrel;
+        best_it = it;
+      } else if (sizeof(S) == 4 && maxrel <= 100.0 * tol && it - best_it >= 15) {
+        converged = true;  // rounding floor of the reduced-precision operator
         break;
       }
       CK(cudaMemcpyAsync(active, h_active.data(), sizeof(int) * m, cudaMemcpyHostToDevice, s));
@@ -254,6 +281,12 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
       CK(launch_gram<S>(X, ld, m, W, ld, m, dim, sm.T, partial, npart, s));
       CK(launch_update<S>(X, ld, m, sm.T, m, m, dim, W, ld, -1.0, 1.0, s));
       CK(op.apply(W, ld, 0, m, AW, ld, s));
+      if (have_p) {
+        // P <- P - X (X^H P), AP <- AP - AX (X^H P): keeps the basis [X W P] away from dependence
+        CK(launch_gram<S>(X, ld, m, X + 2 * m, ld, m, dim, sm.T, partial, npart, s));
+        CK(launch_update<S>(X, ld, m, sm.T, m, m, dim, X + 2 * m, ld, -1.0, 1.0, s));
+        CK(launch_update<S>(AX, ld, m, sm.T, m, m, dim, AX + 2 * m, ld, -1.0, 1.0, s));
+      }
       const int nb = have_p ? 3 * m : 2 * m;
       r = rayleigh_ritz<S>(X, AX, ld, nb, m, dim, tau, sm, partial, npart, st, s, msg, false);
       if (r) return r;

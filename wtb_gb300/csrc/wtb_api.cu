@@ -225,7 +225,7 @@ int validate_params(wtb_ctx* c, const wtb_bse_params* p) {
   if (!p) return set_err(c, WTB_EBADARG, "params is NULL");
   if (p->ngrid[0] < 1 || p->ngrid[1] < 1 || p->ngrid[2] < 1) return set_err(c, WTB_EBADARG, "ngrid must be >= 1");
   if (p->nc < 1 || p->nv < 1) return set_err(c, WTB_EBADARG, "nc and nv must be >= 1");
-  if (p->coultype < 0 || p->coultype > 8 || p->coultype == WTB_V1DT)
+  if (p->coultype < 0 || p->coultype > 8)
     return set_err(c, WTB_EBADARG, "Wrong Coulomb Potential");
   if (!(p->ktol > 0.0)) return set_err(c, WTB_EBADARG, "KTOL must be > 0 (V(k,k) is singular otherwise)");
   if (p->precision < 0 || p->precision > 3 || p->op < 0 || p->op > 1)
@@ -367,7 +367,8 @@ int run_solve(wtb_ctx* c, const wtb_bse_params* p, std::vector<double>* E, wtb_t
   CKC(cudaEventRecord(ev[0], c->s));
   const bool fp64 = p->precision == WTB_PREC_FP64;
   const int m = auto_block(p, dim, fp64);
-  const double tol = p->tol > 0 ? p->tol : (fp64 ? 1e-8 : 1e-6);
+  // default residual targets: SLEPc's 1e-8 in FP64; the FP32 rounding floor of the operator otherwise
+  const double tol = p->tol > 0 ? p->tol : (fp64 ? 1e-8 : (p->precision == WTB_PREC_BF16X3 ? 1e-4 : 1e-5));
   const int maxit = p->maxit > 0 ? p->maxit : 200;
   zd* Xout = c->ws.get<zd>("Xout", (size_t)dim * p->nev, &err);
   CKC(err);
@@ -575,7 +576,7 @@ int wtb_coulomb_table(wtb_ctx* c, const wtb_bse_params* p, int n1, const double*
   CKR(prep_device(c));
   if (!c->have_hr) return set_err(c, WTB_ESTATE, "lattice not set (call wtb_set_hr first)");
   if (!p || n1 < 1 || n2 < 1 || !kpt1 || !kpt2 || !V) return set_err(c, WTB_EBADARG, "bad arguments");
-  if (p->coultype < 0 || p->coultype > 8 || p->coultype == WTB_V1DT)
+  if (p->coultype < 0 || p->coultype > 8)
     return set_err(c, WTB_EBADARG, "Wrong Coulomb Potential");
   std::vector<double> a((size_t)n1 * 3), b((size_t)n2 * 3);
   for (int i = 0; i < n1; ++i)
@@ -636,7 +637,7 @@ int wtb_bse_build(wtb_ctx* c, const wtb_bse_params* p, double* hbse) {
   CKR(prep_device(c));
   if (!c->have_bands) return set_err(c, WTB_ESTATE, "no bands (call wtb_eigsys_mesh first)");
   if (!p) return set_err(c, WTB_EBADARG, "params is NULL");
-  if (p->coultype < 0 || p->coultype > 8 || p->coultype == WTB_V1DT)
+  if (p->coultype < 0 || p->coultype > 8)
     return set_err(c, WTB_EBADARG, "Wrong Coulomb Potential");
   if (!(p->ktol > 0.0)) return set_err(c, WTB_EBADARG, "KTOL must be > 0");
   if (p->precision != WTB_PREC_FP64 && p->precision != WTB_PREC_FP32)

@@ -1,0 +1,177 @@
+! ISO_C_BINDING layer between the WTB Fortran modules and libwtb_gb300.so (include/wtb_gpu.h).
+!
+! Each wtb_gpu_* procedure keeps the argument list of the WTB subroutine it replaces, so the body of
+! that subroutine can become a single call (see INTEGRATION.md):
+!   wtb_gpu_eigsys        <- eigsys        (src/module_hamiltonian.F90:200-320)
+!   wtb_gpu_slepc_solver  <- slepc_solver  (src/module_slepc_solver.F90:12-97)
+!   wtb_gpu_bsesolver     <- bsesolver     (src/module_bse.F90:2023-2594)
+!   wtb_gpu_bsedielraw    <- bsedielraw    (src/module_bse.F90:835-1036)
+! A non-zero status from the library is turned into the reference's behaviour: print the message
+! (the reference's STOP text where it has one) and STOP.
+! No Fortran compiler exists in the build image, so this file is not compiled by the project's build.
+module wtb_gpu
+  use iso_c_binding
+  implicit none
+  private
+  public :: wtb_bse_params_t, wtb_timings_t, wtb_gpu_init, wtb_gpu_eigsys, wtb_gpu_slepc_solver, &
+            wtb_gpu_bsesolver, wtb_gpu_bsedielraw, wtb_gpu_set_hr
+
+  type, bind(C) :: wtb_bse_params_t
+    integer(c_int)  :: ngrid(3)
+    integer(c_int)  :: nc, nv
+    real(c_double)  :: mshift(3)
+    integer(c_int)  :: coultype, renorm
+    real(c_double)  :: ktol, ediel(3), ez, w_coul, r0, lc, cshift, ebse0, ebsef
+    integer(c_int)  :: numbse, nev, precision, op
+    real(c_double)  :: tol
+    integer(c_int)  :: maxit, block
+  end type
+
+  type, bind(C) :: wtb_timings_t
+    real(c_double)  :: t_bands_ms, t_build_ms, t_solve_ms, t_optics_ms, t_total_ms
+    integer(c_int)  :: iterations, matvec_columns
+    real(c_double)  :: max_rel_residual, refine_shift_max
+    integer(c_int)  :: kernel_launches
+  end type
+
+  interface
+    integer(c_int) function c_wtb_ctx_create(ctx, device) bind(C, name="wtb_ctx_create")
+      import :: c_ptr, c_int
+      type(c_ptr), intent(out) :: ctx
+      integer(c_int), value :: device
+    end function
+    type(c_ptr) function c_wtb_last_error(ctx) bind(C, name="wtb_last_error")
+      import :: c_ptr
+      type(c_ptr), value :: ctx
+    end function
+    integer(c_int) function c_wtb_set_hr(ctx, w, nvec, rvec, ffactor, hop, ihop, rlat, efermi, scs, np) &
+        bind(C, name="wtb_set_hr")
+      import :: c_ptr, c_int, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: w, nvec, np
+      integer(c_int) :: rvec(*), ffactor(*)
+      real(c_double) :: hop(*), ihop(*), rlat(*)
+      real(c_double), value :: efermi, scs
+    end function
+    integer(c_int) function c_wtb_eigsys(nthreads, scs, exc, nocp, ffactor, kx, ky, kz, w, nvec, rlat, rvec, &
+        hop, ihop, efermi, energias, autovetores) bind(C, name="wtb_eigsys")
+      import :: c_int, c_double, c_double_complex
+      integer(c_int), value :: nthreads, w, nvec
+      real(c_double), value :: scs, exc, kx, ky, kz, efermi
+      integer(c_int) :: nocp, ffactor(*), rvec(*)
+      real(c_double) :: rlat(*), hop(*), ihop(*), energias(*)
+      complex(c_double_complex) :: autovetores(*)
+    end function
+    integer(c_int) function c_wtb_slepc_solver(ctx, hx, ex, he, nx, ne) bind(C, name="wtb_slepc_solver")
+      import :: c_ptr, c_int, c_double, c_double_complex
+      type(c_ptr), value :: ctx
+      complex(c_double_complex) :: hx(*), he(*)
+      real(c_double) :: ex(*)
+      integer(c_int), value :: nx, ne
+    end function
+    integer(c_int) function c_wtb_bsesolver(ctx, p, ws, acts, he, t) bind(C, name="wtb_bsesolver")
+      import :: c_ptr, c_int, c_double, wtb_bse_params_t, wtb_timings_t
+      type(c_ptr), value :: ctx
+      type(wtb_bse_params_t) :: p
+      real(c_double) :: ws(*), acts(*)
+      type(c_ptr), value :: he
+      type(wtb_timings_t) :: t
+    end function
+    integer(c_int) function c_wtb_bsedielraw(ctx, p, dimse, ws, acts, dielf) bind(C, name="wtb_bsedielraw")
+      import :: c_ptr, c_int, c_double, wtb_bse_params_t
+      type(c_ptr), value :: ctx
+      type(wtb_bse_params_t) :: p
+      integer(c_int), value :: dimse
+      real(c_double) :: ws(*), acts(*), dielf(*)
+    end function
+  end interface
+
+  type(c_ptr), save :: ctx = c_null_ptr
+
+contains
+
+  subroutine check(status, where)
+    integer(c_int), intent(in) :: status
+    character(*), intent(in) :: where
+    character(len=512), pointer :: msg
+    if (status /= 0) then
+      call c_f_pointer(c_wtb_last_error(ctx), msg)
+      write(*,*) trim(where)//': '//msg(1:index(msg, c_null_char)-1)
+      stop
+    end if
+  end subroutine
+
+  subroutine wtb_gpu_init(device)
+    integer, intent(in) :: device
+    if (.not. c_associated(ctx)) call check(c_wtb_ctx_create(ctx, int(device, c_int)), 'wtb_ctx_create')
+  end subroutine
+
+  ! module_hamiltonian globals -> device (after hamiltonian_input_read)
+  subroutine wtb_gpu_set_hr(w90basis, nvec, rvec, ffactor, hopmatrices, ihopmatrices, rlat, efermi, scs, systype)
+    integer :: w90basis, nvec, rvec(nvec,3), ffactor(nvec)
+    double precision :: hopmatrices(nvec,w90basis,w90basis), ihopmatrices(nvec,w90basis,w90basis)
+    double precision :: rlat(3,3), efermi, scs
+    character(len=*) :: systype
+    integer(c_int) :: np
+    call wtb_gpu_init(0)
+    np = 0
+    if (systype == "NP") np = 1
+    call check(c_wtb_set_hr(ctx, w90basis, nvec, rvec, ffactor, hopmatrices, ihopmatrices, rlat, efermi, scs, np), &
+               'wtb_set_hr')
+  end subroutine
+
+  ! same argument list as eigsys (src/module_hamiltonian.F90:200-201)
+  subroutine wtb_gpu_eigsys(nthreads, scs, exc, nocp, ffactor, kx, ky, kz, w90basis, nvec, rlat, rvec, &
+                            hopmatrices, ihopmatrices, efermi, energias, autovetores)
+    integer :: nthreads, nocp, w90basis, nvec
+    integer :: ffactor(*), rvec(nvec,3)
+    double precision :: scs, exc, kx, ky, kz, efermi, rlat(3,3)
+    double precision :: hopmatrices(nvec,w90basis,w90basis), ihopmatrices(nvec,w90basis,w90basis)
+    double precision :: energias(w90basis)
+    double complex :: autovetores(w90basis,w90basis)
+    integer(c_int) :: st
+    st = c_wtb_eigsys(nthreads, scs, exc, nocp, ffactor, kx, ky, kz, w90basis, nvec, rlat, rvec, hopmatrices, &
+                      ihopmatrices, efermi, energias, autovetores)
+    if (st /= 0) then
+      write(*,*) 'The algorithm failed to compute eigenvalues.'
+      stop
+    end if
+  end subroutine
+
+  ! same argument list as slepc_solver (src/module_slepc_solver.F90:12)
+  subroutine wtb_gpu_slepc_solver(HX, EX, HE, NX, NE)
+    integer :: NX, NE
+    complex(8) :: HX(NX,NX), HE(NX,NE)
+    real(8) :: EX(NE)
+    call wtb_gpu_init(0)
+    call check(c_wtb_slepc_solver(ctx, HX, EX, HE, NX, NE), 'slepc_solver')
+  end subroutine
+
+  ! bsesolver body: bands, optics, BSE operator, lowest nev excitons, oscillator strengths, then the
+  ! reference's bse_opt_diel.dat in 7F15.4 for every one of the dimbse rows (src/module_bse.F90:2556-2567)
+  subroutine wtb_gpu_bsesolver(p, outputfolder, Ws, acts, dimbse)
+    type(wtb_bse_params_t) :: p
+    character(len=70) :: outputfolder
+    integer :: dimbse, i, erro
+    double precision :: Ws(dimbse), acts(dimbse,8)
+    type(wtb_timings_t) :: t
+    call wtb_gpu_init(0)
+    call check(c_wtb_bsesolver(ctx, p, Ws, acts, c_null_ptr, t), 'bsesolver')
+    open(unit=301, file=trim(outputfolder)//"/bse_opt_diel.dat", status='unknown', iostat=erro)
+    if (erro /= 0) stop "Error opening bse_opt_diel output file"
+    write(301,*) "#","  ", "exciton energy","  ","xx","  ","yy","  ","zz"," ","xy","  ","xz","  ","yz"
+    do i = 1, dimbse
+      write(301,"(7F15.4)") Ws(i), acts(i,1), acts(i,2), acts(i,3), acts(i,4), acts(i,5), acts(i,6)
+    end do
+    close(301)
+  end subroutine
+
+  subroutine wtb_gpu_bsedielraw(p, dimse, Ws, acts, dielf)
+    type(wtb_bse_params_t) :: p
+    integer :: dimse
+    double precision :: Ws(dimse), acts(dimse,6), dielf(p%numbse,3,6)
+    call wtb_gpu_init(0)
+    call check(c_wtb_bsedielraw(ctx, p, dimse, Ws, acts, dielf), 'bsedielraw')
+  end subroutine
+
+end module wtb_gpu
