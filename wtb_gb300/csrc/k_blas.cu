@@ -5,6 +5,8 @@
 // CTA sums them), so repeated runs give identical bits.  Small matrices (<= 112 x 112, the projected
 // problems of the Rayleigh-Ritz step) are complex(8) in global memory; their eigen-decomposition runs in
 // one CTA by cyclic Jacobi in precision S.
+#include <algorithm>
+
 #include "wtb_internal.h"
 
 namespace wtb {
@@ -14,48 +16,49 @@ namespace {
 // ----------------------------------------------------------------------------- gram: out = A^H B
 constexpr int kGramTile = 16;
 
-template <class S>
+template <class S, int TI>
 __global__ void __launch_bounds__(256) gram_partial_kernel(const cplx<S>* __restrict__ A, int lda, int p,
                                                            const cplx<S>* __restrict__ B, int ldb, int q, int nrow,
                                                            double* __restrict__ partial, int rows_per_part) {
-  // output tile of this CTA: rows [bi*96, ...) x cols [bj*96, ...) -- the launcher keeps p, q <= 96
+  // the p x q output is covered by a 16 x 16 thread grid with TI x TI entries per thread (16 TI >= p, q)
   constexpr int RT = 8;  // rows of A/B staged per step
-  __shared__ cplx<S> As[RT][96];
-  __shared__ cplx<S> Bs[RT][96];
+  constexpr int W = 16 * TI;
+  __shared__ cplx<S> As[RT][W];
+  __shared__ cplx<S> Bs[RT][W];
   const int tid = threadIdx.x, tx = tid % kGramTile, ty = tid / kGramTile;
   const long r_begin = (long)blockIdx.x * rows_per_part;
   const long r_end = min((long)nrow, r_begin + rows_per_part);
-  cplx<S> acc[6][6];
+  cplx<S> acc[TI][TI];
 #pragma unroll
-  for (int a = 0; a < 6; ++a)
+  for (int a = 0; a < TI; ++a)
 #pragma unroll
-    for (int b = 0; b < 6; ++b) acc[a][b] = mk<S>(0, 0);
+    for (int b = 0; b < TI; ++b) acc[a][b] = mk<S>(0, 0);
   for (long r0 = r_begin; r0 < r_end; r0 += RT) {
-    for (int e = tid; e < RT * 96; e += 256) {
-      const int rr = e / 96, c = e % 96;
+    for (int e = tid; e < RT * W; e += 256) {
+      const int rr = e / W, c = e % W;
       const long gr = r0 + rr;
       As[rr][c] = (gr < r_end && c < p) ? A[gr * lda + c] : mk<S>(0, 0);
       Bs[rr][c] = (gr < r_end && c < q) ? B[gr * ldb + c] : mk<S>(0, 0);
     }
     __syncthreads();
     for (int rr = 0; rr < RT; ++rr) {
-      cplx<S> a[6], b[6];
+      cplx<S> a[TI], b[TI];
 #pragma unroll
-      for (int i = 0; i < 6; ++i) a[i] = As[rr][ty + kGramTile * i];
+      for (int i = 0; i < TI; ++i) a[i] = As[rr][ty + kGramTile * i];
 #pragma unroll
-      for (int j = 0; j < 6; ++j) b[j] = Bs[rr][tx + kGramTile * j];
+      for (int j = 0; j < TI; ++j) b[j] = Bs[rr][tx + kGramTile * j];
 #pragma unroll
-      for (int i = 0; i < 6; ++i)
+      for (int i = 0; i < TI; ++i)
 #pragma unroll
-        for (int j = 0; j < 6; ++j) cfmac(acc[i][j], a[i], b[j]);
+        for (int j = 0; j < TI; ++j) cfmac(acc[i][j], a[i], b[j]);
     }
     __syncthreads();
   }
   double* out = partial + (size_t)blockIdx.x * p * q * 2;
 #pragma unroll
-  for (int i = 0; i < 6; ++i)
+  for (int i = 0; i < TI; ++i)
 #pragma unroll
-    for (int j = 0; j < 6; ++j) {
+    for (int j = 0; j < TI; ++j) {
       const int ii = ty + kGramTile * i, jj = tx + kGramTile * j;
       if (ii < p && jj < q) {
         out[2 * (ii * q + jj)] = (double)acc[i][j].re;
@@ -64,12 +67,23 @@ __global__ void __launch_bounds__(256) gram_partial_kernel(const cplx<S>* __rest
     }
 }
 
-__global__ void sum_partials_kernel(const double* __restrict__ partial, int npart, int n, double* __restrict__ out) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= n) return;
+// out[e] = sum over b of partial[b][e]: a CTA owns 32 consecutive e; its 8 warps take every 8th part
+// (lane = e, so reads coalesce), then the 8 warp sums are added in a fixed order.
+__global__ void __launch_bounds__(256) sum_partials_kernel(const double* __restrict__ partial, int npart, int n,
+                                                           double* __restrict__ out) {
+  __shared__ double red[8][33];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int e = blockIdx.x * 32 + lane;
   double s = 0.0;
-  for (int b = 0; b < npart; ++b) s += partial[(size_t)b * n + e];
-  out[e] = s;
+  if (e < n)
+    for (int b = warp; b < npart; b += 8) s += partial[(size_t)b * n + e];
+  red[warp][lane] = s;
+  __syncthreads();
+  if (warp == 0 && e < n) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += red[w][lane];
+    out[e] = t;
+  }
 }
 
 // ----------------------------------------------------------------------------- update: Out = beta Out + S C
@@ -167,23 +181,25 @@ __global__ void convert_cols_kernel(const cplx<Sa>* __restrict__ A, int lda, cpl
 // ----------------------------------------------------------------------------- small Jacobi eigensolver
 __device__ __forceinline__ int rr_player(int i, int t, int n) { return i == 0 ? 0 : ((i - 1 + t) % (n - 1)) + 1; }
 
+// One CTA; each warp owns rotation pairs j = warp, warp + nwarps, ... of the round-robin step.  Its lanes
+// walk the n columns (row update) and then the n rows (column update) of that pair, so no thread does
+// integer division in the inner loops; rotation parameters stay in registers between the two phases,
+// and a step needs two block barriers.
 template <class S>
 __global__ void __launch_bounds__(512) jacobi_small_kernel(zd* A, int lda, int nin, double* evals, zd* evecs,
                                                            int ldv, int max_sweeps, DevStatus* st) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int kMaxPairsPerWarp = 4;  // half <= 64 pairs over 16 warps
   const int n = (nin + 1) & ~1;
   const int half = n / 2;
+  // leading dimension n + 1: a column walk then strides 2(n+1) words and spreads over the banks
+  const int ldm = n + 1;
   cplx<S>* M = reinterpret_cast<cplx<S>*>(smem_raw);
-  cplx<S>* Vv = M + n * n;
-  S* rc = reinterpret_cast<S*>(Vv + n * n);
-  S* rs = rc + 64;
-  cplx<S>* rph = reinterpret_cast<cplx<S>*>(rs + 64);
-  int* rp = reinterpret_cast<int*>(rph + 64);
-  int* rq = rp + 64;
-  int* flag = rq + 64;
-  double* ev = reinterpret_cast<double*>(flag + 64);
+  cplx<S>* Vv = M + n * ldm;
+  double* ev = reinterpret_cast<double*>(Vv + n * ldm);
   int* rank = reinterpret_cast<int*>(ev + 128);
   const int tid = threadIdx.x, nt = blockDim.x;
+  const int warp = tid >> 5, lane = tid & 31, nwarps = nt >> 5;
   for (int e = tid; e < n * n; e += nt) {
     const int r = e / n, c = e % n;
     cplx<S> v = mk<S>(0, 0);
@@ -193,8 +209,8 @@ __global__ void __launch_bounds__(512) jacobi_small_kernel(zd* A, int lda, int n
       v = mk<S>((S)(0.5 * (a.re + b.re)), (S)(0.5 * (a.im - b.im)));
       if (r == c) v.im = 0;
     }
-    M[e] = v;
-    Vv[e] = mk<S>(r == c ? (S)1 : (S)0, 0);
+    M[r * ldm + c] = v;
+    Vv[r * ldm + c] = mk<S>(r == c ? (S)1 : (S)0, 0);
   }
   __syncthreads();
   const S tiny = sizeof(S) == 4 ? (S)1e-30 : (S)1e-300;
@@ -206,17 +222,19 @@ __global__ void __launch_bounds__(512) jacobi_small_kernel(zd* A, int lda, int n
   const double epsa = sizeof(S) == 4 ? 4e-7 : 4e-16;
   __shared__ int notconv;
   __shared__ unsigned long long s_scale;
+  __shared__ double s_off;
   if (tid == 0) s_scale = 0ull;
   __syncthreads();
   for (int i = tid; i < nin; i += nt) {
-    const double d = fabs((double)M[i * n + i].re);
-    if (d < 1e29) atomicMax(&s_scale, __double_as_longlong(d));  // non-negative doubles order as integers
+    const double d = fabs((double)M[i * ldm + i].re);
+    if (d < 1e29) atomicMax(&s_scale, (unsigned long long)__double_as_longlong(d));  // non-negative doubles order as integers
   }
   __syncthreads();
-  const double floor2 = (epsa * __longlong_as_double(s_scale)) * (epsa * __longlong_as_double(s_scale));
-  // Jacobi converges quadratically; once a sweep no longer halves the off-diagonal norm the rotations
-  // are working on rounding noise and the sweep loop stops as well
-  __shared__ double s_off;
+  const double scale = __longlong_as_double((long long)s_scale);
+  const double floor2 = (epsa * scale) * (epsa * scale);
+  // Jacobi converges quadratically; once a sweep no longer shrinks the off-diagonal mass and that mass
+  // is at the rounding floor, the sweep loop stops as well
+  const double noise = (sizeof(S) == 4 ? 1e-6 : 1e-14) * scale;
   double prev_off = 1e300;
   for (int sweep = 0; sweep < max_sweeps; ++sweep) {
     if (tid == 0) {
@@ -229,95 +247,105 @@ __global__ void __launch_bounds__(512) jacobi_small_kernel(zd* A, int lda, int n
     for (int e = tid; e < n * n; e += nt) {
       const int r = e / n, c = e % n;
       if (r == c) continue;
-      const double m2 = (double)M[e].re * M[e].re + (double)M[e].im * M[e].im;
-      const double dd = fabs((double)M[r * n + r].re * (double)M[c * n + c].re);
+      const cplx<S> me = M[r * ldm + c];
+      const double m2 = (double)me.re * me.re + (double)me.im * me.im;
+      const double dd = fabs((double)M[r * ldm + r].re * (double)M[c * ldm + c].re);
       off += m2;
       if (m2 > eps2 * dd && m2 > floor2 && m2 > 1e-280) mine = 1;
     }
     if (mine) atomicOr(&notconv, 1);
     for (int o = 16; o > 0; o >>= 1) off += __shfl_xor_sync(0xffffffffu, off, o);
-    if ((tid & 31) == 0) atomicAdd(&s_off, off);
+    if (lane == 0) atomicAdd(&s_off, off);
     __syncthreads();
     const int nc = notconv;
     const double offn = s_off;
-    __syncthreads();
     if (!nc) break;
-    // stagnation at the rounding floor: off-diagonal mass already at noise level and no longer shrinking
-    const double noise = (sizeof(S) == 4 ? 1e-6 : 1e-14) * __longlong_as_double(s_scale);
     if (sweep >= 2 && offn > 0.25 * prev_off && offn <= noise * noise * (double)n * n) break;
     prev_off = offn;
     if (sizeof(S) == 8 && sweep == max_sweeps - 1 && tid == 0) dev_fail(st, 201, n);
     for (int t = 0; t < n - 1; ++t) {
-      if (tid < half) {
-        int p = rr_player(tid, t, n), q = rr_player(n - 1 - tid, t, n);
+      __syncthreads();
+      int pp[kMaxPairsPerWarp], qq[kMaxPairsPerWarp];
+      S cc[kMaxPairsPerWarp], ss[kMaxPairsPerWarp];
+      cplx<S> ph[kMaxPairsPerWarp];
+      bool act[kMaxPairsPerWarp];
+#pragma unroll
+      for (int k = 0; k < kMaxPairsPerWarp; ++k) {
+        const int j = warp + k * nwarps;
+        act[k] = false;
+        if (j >= half) continue;
+        // round-robin (circle) pairing of step t: position i holds player (i - 1 + t) mod (n - 1) + 1
+        int p = j == 0 ? 0 : ((j - 1 + t) % (n - 1)) + 1;
+        int q = ((n - 2 - j + t) % (n - 1)) + 1;
         if (p > q) {
           const int tmp = p;
           p = q;
           q = tmp;
         }
-        const cplx<S> apq = M[p * n + q];
-        const S app = M[p * n + p].re, aqq = M[q * n + q].re;
+        pp[k] = p;
+        qq[k] = q;
+        const cplx<S> apq = M[p * ldm + q];
+        const S app = M[p * ldm + p].re, aqq = M[q * ldm + q].re;
         const S b = sqrt(apq.re * apq.re + apq.im * apq.im);
-        S c = 1, s = 0;
-        cplx<S> ph = mk<S>(1, 0);
-        int act = 0;
         if (b > tiny) {
-          ph = mk<S>(apq.re / b, apq.im / b);
+          ph[k] = mk<S>(apq.re / b, apq.im / b);
           const S zeta = (aqq - app) / (2 * b);
           S tt;
           if (fabs(zeta) > (S)1e15)
             tt = (S)0.5 / zeta;
           else
             tt = (zeta >= 0 ? (S)1 : (S)-1) / (fabs(zeta) + sqrt((S)1 + zeta * zeta));
-          c = (S)1 / sqrt((S)1 + tt * tt);
-          s = tt * c;
-          act = 1;
+          cc[k] = (S)1 / sqrt((S)1 + tt * tt);
+          ss[k] = tt * cc[k];
+          act[k] = true;
         }
-        rc[tid] = c;
-        rs[tid] = s;
-        rph[tid] = ph;
-        rp[tid] = p;
-        rq[tid] = q;
-        flag[tid] = act;
+      }
+      __syncwarp();
+      // rows: A_p. <- c A_p. - s e^{i phi} A_q. ; A_q. <- s A_p. + c e^{i phi} A_q.
+#pragma unroll
+      for (int k = 0; k < kMaxPairsPerWarp; ++k) {
+        if (!act[k]) continue;
+        const int p = pp[k], q = qq[k];
+        const S c = cc[k], s = ss[k];
+        for (int col = lane; col < n; col += 32) {
+          const cplx<S> ap = M[p * ldm + col], aq = M[q * ldm + col];
+          const cplx<S> phq = cmul(ph[k], aq);
+          M[p * ldm + col] = mk<S>(c * ap.re - s * phq.re, c * ap.im - s * phq.im);
+          M[q * ldm + col] = mk<S>(s * ap.re + c * phq.re, s * ap.im + c * phq.im);
+        }
       }
       __syncthreads();
-      for (int e = tid; e < half * n; e += nt) {
-        const int j = e / n, col = e % n;
-        if (!flag[j]) continue;
-        const int p = rp[j], q = rq[j];
-        const S c = rc[j], s = rs[j];
-        const cplx<S> ap = M[p * n + col], aq = M[q * n + col];
-        const cplx<S> phq = cmul(rph[j], aq);
-        M[p * n + col] = mk<S>(c * ap.re - s * phq.re, c * ap.im - s * phq.im);
-        M[q * n + col] = mk<S>(s * ap.re + c * phq.re, s * ap.im + c * phq.im);
+      // columns of A and V: A_.p <- c A_.p - s e^{-i phi} A_.q ; A_.q <- s A_.p + c e^{-i phi} A_.q
+#pragma unroll
+      for (int k = 0; k < kMaxPairsPerWarp; ++k) {
+        if (!act[k]) continue;
+        const int p = pp[k], q = qq[k];
+        const S c = cc[k], s = ss[k];
+        const cplx<S> phc = mk<S>(ph[k].re, -ph[k].im);
+        for (int row = lane; row < n; row += 32) {
+          cplx<S> ap = M[row * ldm + p], aq = M[row * ldm + q];
+          cplx<S> phq = cmul(phc, aq);
+          M[row * ldm + p] = mk<S>(c * ap.re - s * phq.re, c * ap.im - s * phq.im);
+          M[row * ldm + q] = mk<S>(s * ap.re + c * phq.re, s * ap.im + c * phq.im);
+          ap = Vv[row * ldm + p];
+          aq = Vv[row * ldm + q];
+          phq = cmul(phc, aq);
+          Vv[row * ldm + p] = mk<S>(c * ap.re - s * phq.re, c * ap.im - s * phq.im);
+          Vv[row * ldm + q] = mk<S>(s * ap.re + c * phq.re, s * ap.im + c * phq.im);
+        }
+        __syncwarp();
+        if (lane == 0) {
+          M[p * ldm + q] = mk<S>(0, 0);
+          M[q * ldm + p] = mk<S>(0, 0);
+          M[p * ldm + p].im = 0;
+          M[q * ldm + q].im = 0;
+        }
       }
-      __syncthreads();
-      for (int e = tid; e < half * n * 2; e += nt) {
-        const int which = e / (half * n);
-        const int ee = e % (half * n);
-        const int j = ee / n, row = ee % n;
-        if (!flag[j]) continue;
-        cplx<S>* X = which ? Vv : M;
-        const int p = rp[j], q = rq[j];
-        const S c = rc[j], s = rs[j];
-        const cplx<S> phc = mk<S>(rph[j].re, -rph[j].im);
-        const cplx<S> ap = X[row * n + p], aq = X[row * n + q];
-        const cplx<S> phq = cmul(phc, aq);
-        X[row * n + p] = mk<S>(c * ap.re - s * phq.re, c * ap.im - s * phq.im);
-        X[row * n + q] = mk<S>(s * ap.re + c * phq.re, s * ap.im + c * phq.im);
-      }
-      __syncthreads();
-      if (tid < half && flag[tid]) {
-        const int p = rp[tid], q = rq[tid];
-        M[p * n + q] = mk<S>(0, 0);
-        M[q * n + p] = mk<S>(0, 0);
-        M[p * n + p].im = 0;
-        M[q * n + q].im = 0;
-      }
-      __syncthreads();
     }
+    __syncthreads();
   }
-  if (tid < nin) ev[tid] = (double)M[tid * n + tid].re;
+  __syncthreads();
+  if (tid < nin) ev[tid] = (double)M[tid * ldm + tid].re;
   __syncthreads();
   if (tid < nin) {
     int r = 0;
@@ -329,7 +357,7 @@ __global__ void __launch_bounds__(512) jacobi_small_kernel(zd* A, int lda, int n
   if (tid < nin) evals[rank[tid]] = ev[tid];
   for (int e = tid; e < nin * nin; e += nt) {
     const int row = e / nin, j = e % nin;
-    const cplx<S> v = Vv[row * n + j];
+    const cplx<S> v = Vv[row * ldm + j];
     evecs[(size_t)row * ldv + rank[j]] = mk<double>((double)v.re, (double)v.im);
   }
 }
@@ -396,24 +424,30 @@ __device__ __forceinline__ double hash_noise(unsigned a, unsigned b, unsigned se
 }
 
 // X0 = unit vectors at the m smallest diagonal entries (lowest transition energies) plus a small
-// deterministic perturbation; one CTA selects the m indices by repeated arg-min.
-__global__ void __launch_bounds__(1024) select_lowest_kernel(const double* __restrict__ diag, int dim, int m,
-                                                             int* __restrict__ idx) {
-  __shared__ double bv[1024];
-  __shared__ int bi[1024];
+// deterministic perturbation.  Selection in two levels: each CTA takes the m smallest of its slice by
+// repeated arg-min (ties to the lower index), then one CTA repeats that over the CTAs' candidates.
+__global__ void __launch_bounds__(256) select_lowest_kernel(const double* __restrict__ val, const int* __restrict__ ids,
+                                                            int count, int m, double* __restrict__ out_val,
+                                                            int* __restrict__ out_idx) {
+  __shared__ double bv[256];
+  __shared__ int bi[256];
   __shared__ int chosen[128];
   const int tid = threadIdx.x;
+  const int per = (count + gridDim.x - 1) / gridDim.x;
+  const int r0 = blockIdx.x * per, r1 = min(count, r0 + per);
   for (int s = 0; s < m; ++s) {
     double best = 1e300;
     int besti = 0x7fffffff;
-    for (int r = tid; r < dim; r += blockDim.x) {
+    for (int r = r0 + tid; r < r1; r += blockDim.x) {
+      const int id = ids ? ids[r] : r;
+      if (id < 0) continue;
       bool used = false;
-      for (int t = 0; t < s; ++t) used |= (chosen[t] == r);
+      for (int t = 0; t < s; ++t) used |= (chosen[t] == id);
       if (used) continue;
-      const double d = diag[r];
-      if (d < best || (d == best && r < besti)) {
+      const double d = val[r];
+      if (d < best || (d == best && id < besti)) {
         best = d;
-        besti = r;
+        besti = id;
       }
     }
     bv[tid] = best;
@@ -432,7 +466,8 @@ __global__ void __launch_bounds__(1024) select_lowest_kernel(const double* __res
     }
     if (tid == 0) {
       chosen[s] = bi[0];
-      idx[s] = bi[0];
+      out_val[blockIdx.x * m + s] = bv[0];
+      out_idx[blockIdx.x * m + s] = bi[0] == 0x7fffffff ? -1 : bi[0];
     }
     __syncthreads();
   }
@@ -458,9 +493,18 @@ cudaError_t launch_gram(const cplx<S>* A, int lda, int p, const cplx<S>* B, int 
                         double* partial, int npart, cudaStream_t s) {
   if (p > 96 || q > 96) return cudaErrorInvalidValue;
   const int rpp = (nrow + npart - 1) / npart;
-  gram_partial_kernel<S><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp); ++g_launch_count;
+  const int ti = (std::max(p, q) + 15) / 16;
+  switch (ti) {
+    case 1: gram_partial_kernel<S, 1><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp); break;
+    case 2: gram_partial_kernel<S, 2><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp); break;
+    case 3: gram_partial_kernel<S, 3><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp); break;
+    case 4: gram_partial_kernel<S, 4><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp); break;
+    case 5: gram_partial_kernel<S, 5><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp); break;
+    default: gram_partial_kernel<S, 6><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp); break;
+  }
+  ++g_launch_count;
   const int n = p * q * 2;
-  sum_partials_kernel<<<(n + 255) / 256, 256, 0, s>>>(partial, npart, n, reinterpret_cast<double*>(out)); ++g_launch_count;
+  sum_partials_kernel<<<(n + 31) / 32, 256, 0, s>>>(partial, npart, n, reinterpret_cast<double*>(out)); ++g_launch_count;
   return cudaGetLastError();
 }
 
@@ -486,7 +530,7 @@ cudaError_t launch_residual(const cplx<S>* AX, int ldax, const cplx<S>* X, int l
   if (m > 32) return cudaErrorInvalidValue;
   residual_kernel<S><<<npart, 256, 0, s>>>(AX, ldax, X, ldx, theta, m, nrow, R, ldr, partial); ++g_launch_count;
   // partial is [npart][32]; sum column-wise
-  sum_partials_kernel<<<1, 32, 0, s>>>(partial, npart, 32, norms2); ++g_launch_count;
+  sum_partials_kernel<<<1, 256, 0, s>>>(partial, npart, 32, norms2); ++g_launch_count;
   return cudaGetLastError();
 }
 
@@ -517,8 +561,8 @@ template <class S>
 static cudaError_t jacobi_launch(zd* A, int lda, int n, double* evals, zd* evecs, int ldv, int sweeps,
                                  DevStatus* st, cudaStream_t s) {
   const int np = (n + 1) & ~1;
-  const size_t smem = (size_t)2 * np * np * sizeof(cplx<S>) + 64 * 2 * sizeof(S) + 64 * sizeof(cplx<S>) +
-                      64 * 3 * sizeof(int) + 128 * sizeof(double) + 128 * sizeof(int) + 64;
+  if (np / 2 > 64) return cudaErrorInvalidValue;
+  const size_t smem = (size_t)2 * np * (np + 1) * sizeof(cplx<S>) + 128 * sizeof(double) + 128 * sizeof(int) + 64;
   if (smem > 220 * 1024) return cudaErrorInvalidValue;
   cudaError_t e = cudaFuncSetAttribute(jacobi_small_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -563,9 +607,12 @@ cudaError_t launch_mark_dropped(zd* G, int ldg, int n, const int* keep, cudaStre
   return cudaGetLastError();
 }
 
-cudaError_t launch_select_lowest(const double* diag, int dim, int m, int* idx, cudaStream_t s) {
+// idx needs room for 64 * m + m ints (candidates then the result), idx[64 m .. 64 m + m) holds the answer.
+cudaError_t launch_select_lowest(const double* diag, int dim, int m, int* idx, double* cand_val, cudaStream_t s) {
   if (m > 128) return cudaErrorInvalidValue;
-  select_lowest_kernel<<<1, 1024, 0, s>>>(diag, dim, m, idx); ++g_launch_count;
+  const int g = std::max(1, std::min(64, (dim + 1023) / 1024));
+  select_lowest_kernel<<<g, 256, 0, s>>>(diag, nullptr, dim, m, cand_val, idx); ++g_launch_count;
+  select_lowest_kernel<<<1, 256, 0, s>>>(cand_val, idx, g * m, m, cand_val + 64 * m, idx + 64 * m); ++g_launch_count;
   return cudaGetLastError();
 }
 

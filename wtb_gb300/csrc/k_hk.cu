@@ -41,15 +41,16 @@ __device__ __forceinline__ double rcomp_f32(const int* rvec, int nR, int iR, con
   return (double)__double2float_rn(rcart(r1, r2, r3, rl, a));
 }
 
-// Round-robin partner table: position i of step t.
-__device__ __forceinline__ int rr_player(int i, int t, int n) { return i == 0 ? 0 : ((i - 1 + t) % (n - 1)) + 1; }
-
-// Jacobi eigen-decomposition of the n x n (n even) Hermitian matrix A (shared, ld = n); V receives the
-// eigenvectors as columns.  All threads of the block participate.
-__device__ void jacobi_shared(zd* A, zd* V, int n, int nreal, double* rc, double* rs, zd* rph, int* rp, int* rq,
-                              int* flag, double* red) {
+// Jacobi eigen-decomposition of the n x n (n even, n <= 64) Hermitian matrix A (shared, leading
+// dimension ld = n + 1 so column walks spread over the shared-memory banks); V receives the eigenvectors
+// as columns.  Round-robin (circle) ordering: the n/2 rotations of a step touch disjoint rows/columns,
+// so all threads apply them element by element (for w of 8..22 orbitals the elements of a step keep
+// the block's 128 threads busier than one warp per rotation would).
+__device__ void jacobi_shared(zd* A, zd* V, int n, double* rc, double* rs, zd* rph, int* rp, int* rq, int* flag,
+                              double* red) {
   const int tid = threadIdx.x, nt = blockDim.x;
-  for (int e = tid; e < n * n; e += nt) V[e] = mk<double>((e / n) == (e % n) ? 1.0 : 0.0, 0.0);
+  const int ld = n + 1;
+  for (int e = tid; e < n * n; e += nt) V[(e / n) * ld + e % n] = mk<double>((e / n) == (e % n) ? 1.0 : 0.0, 0.0);
   __syncthreads();
   const int half = n / 2;
   for (int sweep = 0; sweep < 40; ++sweep) {
@@ -63,9 +64,9 @@ __device__ void jacobi_shared(zd* A, zd* V, int n, int nreal, double* rc, double
     for (int e = tid; e < n * n; e += nt) {
       const int r = e / n, c = e % n;
       if (r == c)
-        dia += A[e].re * A[e].re;
+        dia += A[r * ld + c].re * A[r * ld + c].re;
       else
-        off += cabs2(A[e]);
+        off += cabs2(A[r * ld + c]);
     }
     atomicAdd(&red[0], off);
     atomicAdd(&red[1], dia);
@@ -75,14 +76,15 @@ __device__ void jacobi_shared(zd* A, zd* V, int n, int nreal, double* rc, double
     if (offn <= 1e-32 * dian || offn == 0.0) break;
     for (int t = 0; t < n - 1; ++t) {
       if (tid < half) {
-        int p = rr_player(tid, t, n), q = rr_player(n - 1 - tid, t, n);
+        int p = tid == 0 ? 0 : ((tid - 1 + t) % (n - 1)) + 1;
+        int q = ((n - 2 - tid + t) % (n - 1)) + 1;
         if (p > q) {
-          int tmp = p;
+          const int tmp = p;
           p = q;
           q = tmp;
         }
-        const zd apq = A[p * n + q];
-        const double app = A[p * n + p].re, aqq = A[q * n + q].re;
+        const zd apq = A[p * ld + q];
+        const double app = A[p * ld + p].re, aqq = A[q * ld + q].re;
         const double b = sqrt(cabs2(apq));
         double c = 1.0, s = 0.0;
         zd ph = mk<double>(1.0, 0.0);
@@ -113,11 +115,10 @@ __device__ void jacobi_shared(zd* A, zd* V, int n, int nreal, double* rc, double
         if (!flag[j]) continue;
         const int p = rp[j], q = rq[j];
         const double c = rc[j], s = rs[j];
-        const zd ph = rph[j];
-        const zd ap = A[p * n + col], aq = A[q * n + col];
-        const zd phq = cmul(ph, aq);
-        A[p * n + col] = mk<double>(c * ap.re - s * phq.re, c * ap.im - s * phq.im);
-        A[q * n + col] = mk<double>(s * ap.re + c * phq.re, s * ap.im + c * phq.im);
+        const zd ap = A[p * ld + col], aq = A[q * ld + col];
+        const zd phq = cmul(rph[j], aq);
+        A[p * ld + col] = mk<double>(c * ap.re - s * phq.re, c * ap.im - s * phq.im);
+        A[q * ld + col] = mk<double>(s * ap.re + c * phq.re, s * ap.im + c * phq.im);
       }
       __syncthreads();
       // columns of A and V: A_.p <- c A_.p - s e^{-i phi} A_.q ; A_.q <- s A_.p + c e^{-i phi} A_.q
@@ -130,23 +131,22 @@ __device__ void jacobi_shared(zd* A, zd* V, int n, int nreal, double* rc, double
         const int p = rp[j], q = rq[j];
         const double c = rc[j], s = rs[j];
         const zd phc = mk<double>(rph[j].re, -rph[j].im);
-        const zd ap = M[row * n + p], aq = M[row * n + q];
+        const zd ap = M[row * ld + p], aq = M[row * ld + q];
         const zd phq = cmul(phc, aq);
-        M[row * n + p] = mk<double>(c * ap.re - s * phq.re, c * ap.im - s * phq.im);
-        M[row * n + q] = mk<double>(s * ap.re + c * phq.re, s * ap.im + c * phq.im);
+        M[row * ld + p] = mk<double>(c * ap.re - s * phq.re, c * ap.im - s * phq.im);
+        M[row * ld + q] = mk<double>(s * ap.re + c * phq.re, s * ap.im + c * phq.im);
       }
       __syncthreads();
       if (tid < half && flag[tid]) {
         const int p = rp[tid], q = rq[tid];
-        A[p * n + q] = mk<double>(0.0, 0.0);
-        A[q * n + p] = mk<double>(0.0, 0.0);
-        A[p * n + p].im = 0.0;
-        A[q * n + q].im = 0.0;
+        A[p * ld + q] = mk<double>(0.0, 0.0);
+        A[q * ld + p] = mk<double>(0.0, 0.0);
+        A[p * ld + p].im = 0.0;
+        A[q * ld + q].im = 0.0;
       }
       __syncthreads();
     }
   }
-  (void)nreal;
 }
 
 __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict__ hr, const int* __restrict__ rvec,
@@ -159,9 +159,10 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
   const int k = blockIdx.x;
   if (k >= nk) return;
   const int n = (w + 1) & ~1;
+  const int ld = n + 1;
   zd* A = reinterpret_cast<zd*>(smem_raw);
-  zd* V = A + n * n;
-  zd* eph = V + n * n;  // nR phases
+  zd* V = A + n * ld;
+  zd* eph = V + n * ld;  // nR phases
   double* rc = reinterpret_cast<double*>(eph + nR);
   double* rs = rc + 32;
   zd* rph = reinterpret_cast<zd*>(rs + 32);
@@ -192,25 +193,25 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
       for (int r = 0; r < nR; ++r) cfma(acc, eph[r], hr[((size_t)r * w + m) * w + c]);
       if (m == c) acc.re -= efermi;
     }
-    A[e] = acc;
+    A[m * ld + c] = acc;
   }
   __syncthreads();
-  // Hermitian by construction up to rounding: symmetrise so the rotations see an exact Hermitian matrix
+  // ZHEEV('V','L') reads the lower triangle and the real part of the diagonal only: the matrix that is
+  // diagonalised is the Hermitian completion of the lower triangle (identical to H(k) when the H(R) set
+  // is Hermitian-consistent; a perturbation of an upper-triangle entry does not reach the eigensolve)
   for (int e = tid; e < n * n; e += blockDim.x) {
     const int m = e / n, c = e % n;
-    if (m < c) {
-      const zd a = A[m * n + c], b = A[c * n + m];
-      const zd h = mk<double>(0.5 * (a.re + b.re), 0.5 * (a.im - b.im));
-      A[m * n + c] = h;
-      A[c * n + m] = mk<double>(h.re, -h.im);
+    if (m > c) {
+      const zd a = A[m * ld + c];
+      A[c * ld + m] = mk<double>(a.re, -a.im);
     } else if (m == c) {
-      A[e].im = 0.0;
+      A[m * ld + c].im = 0.0;
     }
   }
   __syncthreads();
-  jacobi_shared(A, V, n, w, rc, rs, rph, rp, rq, flag, red);
+  jacobi_shared(A, V, n, rc, rs, rph, rp, rq, flag, red);
   // ascending order of the w real eigenvalues (the padding index w, if any, is excluded)
-  if (tid < w) ev[tid] = A[tid * n + tid].re;
+  if (tid < w) ev[tid] = A[tid * ld + tid].re;
   __syncthreads();
   if (tid < w) {
     int r = 0;
@@ -229,11 +230,11 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
   // outputs: eigenvalue j goes to position rank[j]; eigenvector = column j of V, gauge fixed
   for (int e = tid; e < w * w; e += blockDim.x) {
     const int j = e / w, o = e % w;
-    const zd a0 = V[0 * n + j];
+    const zd a0 = V[0 * ld + j];
     const double m0 = sqrt(cabs2(a0));
     zd g = mk<double>(1.0, 0.0);
     if (m0 > 0.0) g = mk<double>(a0.re / m0, -a0.im / m0);
-    zd val = cmul(V[o * n + j], g);
+    zd val = cmul(V[o * ld + j], g);
     if (o == 0) val = mk<double>(m0, 0.0);
     const int r = rank[j];
     if (vec_all) vec_all[((size_t)k * w + r) * w + o] = val;
@@ -384,12 +385,9 @@ struct CoulConst {
   double rc;                                 // V2DT / V0DT
 };
 
-__global__ void coulomb_kernel(CoulConst cc, const double* __restrict__ k1, int n1, const double* __restrict__ k2,
-                               int n2, double* __restrict__ V, int ldv) {
-  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= (long)n1 * n2) return;
-  const int i = (int)(e / n2), j = (int)(e % n2);
-  const double dx = k1[3 * i] - k2[3 * j], dy = k1[3 * i + 1] - k2[3 * j + 1], dz = k1[3 * i + 2] - k2[3 * j + 2];
+// The selected potential for the k-point difference (dx, dy, dz) = k1 - k2 (modvec, then the switch of
+// matrizelbse, src/module_bse.F90:49-72).
+__device__ double coulomb_of(const CoulConst& cc, double dx, double dy, double dz) {
   const double modk = sqrt(dx * dx + dy * dy + dz * dz);
   double v = 0.0;
   const double vc = cc.vbz * cc.cic;
@@ -458,7 +456,43 @@ __global__ void coulomb_kernel(CoulConst cc, const double* __restrict__ k1, int 
     default:
       v = 0.0;
   }
-  V[(size_t)i * ldv + j] = v;
+  return v;
+}
+
+__global__ void coulomb_kernel(CoulConst cc, const double* __restrict__ k1, int n1, const double* __restrict__ k2,
+                               int n2, double* __restrict__ V, int ldv) {
+  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long)n1 * n2) return;
+  const int i = (int)(e / n2), j = (int)(e % n2);
+  const double dx = k1[3 * i] - k2[3 * j], dy = k1[3 * i + 1] - k2[3 * j + 1], dz = k1[3 * i + 2] - k2[3 * j + 2];
+  V[(size_t)i * ldv + j] = coulomb_of(cc, dx, dy, dz);
+}
+
+// On a Monkhorst-Pack mesh k = (i/n1) b1 + (j/n2) b2 + (l/n3) b3 + shift, so k - k' depends on the index
+// differences only and every potential of module_coulomb is a function of k - k': the (2n1-1)(2n2-1)(2n3-1)
+// distinct values are evaluated once and then spread over the Nk x Nk table.
+__global__ void coulomb_stencil_kernel(CoulConst cc, const double* __restrict__ bl, int n1, int n2, int n3,
+                                       double* __restrict__ st) {
+  const int s1 = 2 * n1 - 1, s2 = 2 * n2 - 1, s3 = 2 * n3 - 1;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= s1 * s2 * s3) return;
+  const int di = e / (s2 * s3) - (n1 - 1), dj = (e / s3) % s2 - (n2 - 1), dl = e % s3 - (n3 - 1);
+  double d[3];
+  for (int a = 0; a < 3; ++a)
+    d[a] = (bl[a] / (double)n1) * (double)di + (bl[3 + a] / (double)n2) * (double)dj + (bl[6 + a] / (double)n3) * (double)dl;
+  st[e] = coulomb_of(cc, d[0], d[1], d[2]);
+}
+
+__global__ void coulomb_expand_kernel(const double* __restrict__ st, int n1, int n2, int n3, double* __restrict__ V,
+                                      int ldv) {
+  const long nk = (long)n1 * n2 * n3;
+  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nk * nk) return;
+  const int k = (int)(e / nk), kp = (int)(e % nk);
+  const int i = k / (n2 * n3), j = (k / n3) % n2, l = k % n3;
+  const int ip = kp / (n2 * n3), jp = (kp / n3) % n2, lp = kp % n3;
+  const int s2 = 2 * n2 - 1, s3 = 2 * n3 - 1;
+  V[(size_t)k * ldv + kp] = st[((i - ip + n1 - 1) * s2 + (j - jp + n2 - 1)) * s3 + (l - lp + n3 - 1)];
 }
 
 __global__ void transition_kernel(const double* __restrict__ eig_win, int nk, int nv, int nc, double* dE) {
@@ -476,7 +510,7 @@ cudaError_t launch_hk_eig(const zd* hr, const int* rvec, const int* ndegen, int 
                           zd* vec_all, double* eig_win, zd* vec_win, int* nocp, DevStatus* st, cudaStream_t s) {
   if (w > 64 || w < 1) return cudaErrorInvalidValue;
   const int n = (w + 1) & ~1;
-  const size_t smem = (size_t)2 * n * n * sizeof(zd) + nR * sizeof(zd) + 32 * 2 * sizeof(double) + 32 * sizeof(zd) +
+  const size_t smem = (size_t)2 * n * (n + 1) * sizeof(zd) + nR * sizeof(zd) + 32 * 2 * sizeof(double) + 32 * sizeof(zd) +
                       4 * sizeof(double) + 64 * sizeof(double) + 32 * 3 * sizeof(int) + 64 * sizeof(int) + 64;
   cudaError_t e = cudaFuncSetAttribute(hk_eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -497,8 +531,31 @@ cudaError_t launch_optics(const zd* hr, const int* rvec, const int* ndegen, int 
   return cudaGetLastError();
 }
 
+static bool coul_const(const CoulParams& p, CoulConst* out);
+
 cudaError_t launch_coulomb(const CoulParams& p, const double* kpt1, int n1, const double* kpt2, int n2, double* V,
                            int ldv, cudaStream_t s) {
+  CoulConst cc{};
+  if (!coul_const(p, &cc)) return cudaErrorInvalidValue;
+  const long tot = (long)n1 * n2;
+  const int th = 256;
+  coulomb_kernel<<<(unsigned)((tot + th - 1) / th), th, 0, s>>>(cc, kpt1, n1, kpt2, n2, V, ldv); ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_coulomb_mesh(const CoulParams& p, const double* bl, double* stencil, double* V, int ldv,
+                                cudaStream_t s) {
+  CoulConst cc{};
+  if (!coul_const(p, &cc)) return cudaErrorInvalidValue;
+  const int n1 = p.ngrid[0], n2 = p.ngrid[1], n3 = p.ngrid[2];
+  const int ns = (2 * n1 - 1) * (2 * n2 - 1) * (2 * n3 - 1);
+  coulomb_stencil_kernel<<<(ns + 127) / 128, 128, 0, s>>>(cc, bl, n1, n2, n3, stencil); ++g_launch_count;
+  const long nk = (long)n1 * n2 * n3;
+  coulomb_expand_kernel<<<(unsigned)((nk * nk + 255) / 256), 256, 0, s>>>(stencil, n1, n2, n3, V, ldv); ++g_launch_count;
+  return cudaGetLastError();
+}
+
+static bool coul_const(const CoulParams& p, CoulConst* out) {
   const double* r = p.rlat;
   auto cross = [](const double* a, const double* b, double* o) {
     o[0] = a[1] * b[2] - a[2] * b[1];
@@ -568,12 +625,10 @@ cudaError_t launch_coulomb(const CoulParams& p, const double* kpt1, int n1, cons
       break;
     }
     default:
-      return cudaErrorInvalidValue;
+      return false;
   }
-  const long tot = (long)n1 * n2;
-  const int th = 256;
-  coulomb_kernel<<<(unsigned)((tot + th - 1) / th), th, 0, s>>>(cc, kpt1, n1, kpt2, n2, V, ldv); ++g_launch_count;
-  return cudaGetLastError();
+  *out = cc;
+  return true;
 }
 
 cudaError_t launch_transition_energies(const double* eig_win, int nk, int nv, int nc, double* dE, cudaStream_t s) {

@@ -40,7 +40,8 @@ cudaError_t MatFreeOperator<S>::apply(const cplx<S>* X, int ldx, int c0, int nco
         e = launch_mf_gather<float, uint16_t>(X, ldx, c0 + b0, nb, vec_win, nk, nv, nc, w, Zs, Kpad, nslices,
                                               (long)Npad * Kpad, s);
         if (e != cudaSuccess) return e;
-        auto it = plans.find(N);
+        const long key = (long)N * 16 + npairs;
+        auto it = plans.find(key);
         TcGemmPlan* plan = nullptr;
         if (it == plans.end()) {
           std::string m2;
@@ -50,7 +51,7 @@ cudaError_t MatFreeOperator<S>::apply(const cplx<S>* X, int ldx, int c0, int nco
             return cudaErrorInvalidValue;
           }
           tc_gemm_set_valid(plan, nk, N);
-          plans[N] = plan;
+          plans[key] = plan;
         } else {
           plan = it->second;
         }
@@ -150,7 +151,7 @@ int rayleigh_ritz(const cplx<S>* Sb, const cplx<S>* ASb, int ld, int nb, int m, 
 template <class S>
 int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, double tol, int maxit, Workspace& ws,
                  DevStatus* st, cudaStream_t s, std::vector<double>* E, zd* Xout, SolveStats* stats,
-                 std::string* msg) {
+                 std::string* msg, double tol_refine) {
   if (m < nev) m = nev;
   if (m > dim) m = dim;
   if (nev < 1 || nev > dim) {
@@ -195,7 +196,8 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
     double* partial = ws.get<double>("lob_partial", (size_t)npart * nn * 2, &err);
     double* norms2 = ws.get<double>("lob_norms2", 32, &err);
     int* active = ws.get<int>("lob_active", 32, &err);
-    int* idx = ws.get<int>("lob_idx", 128, &err);
+    int* idx = ws.get<int>("lob_idx", 65 * 128, &err);
+    double* cand = ws.get<double>("lob_cand", 65 * 128, &err);
     double* th_dev = ws.get<double>("lob_thcur", maxnb, &err);
     if (!chk()) goto oom;
     // SVQB keeps a direction of the scaled Gram matrix only if its eigenvalue exceeds tau: a kept
@@ -205,8 +207,8 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
     std::vector<double> h_theta(maxnb), h_norm(32);
     std::vector<int> h_active(32, 1);
     // start block: unit vectors at the m lowest transition energies (+ small deterministic noise)
-    CK(launch_select_lowest(diag, dim, m, idx, s));
-    CK(launch_init_guess<S>(Sb[0], ld, dim, m, idx, 12345u, s));
+    CK(launch_select_lowest(diag, dim, m, idx, cand, s));
+    CK(launch_init_guess<S>(Sb[0], ld, dim, m, idx + 64 * m, 12345u, s));
     CK(op.apply(Sb[0], ld, 0, m, ASb[0], ld, s));
     int r = rayleigh_ritz<S>(Sb[0], ASb[0], ld, m, m, dim, tau, sm, partial, npart, st, s, msg, false);
     if (r) return r;
@@ -265,6 +267,24 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
                      maxrel);
       }
       if (nconv == nev) {
+        if (tol_refine > 0.0 && tol_refine < tol && op.begin_refine()) {
+          // second phase: the accurate operator; AX is recomputed and the search directions P (built
+          // with the cheaper operator) are dropped
+          tol = tol_refine;
+          tol_refine = 0.0;
+          CK(op.apply(X, ld, 0, m, AX, ld, s));
+          have_p = false;
+          best_maxrel = 1e300;
+          best_it = it;
+          r = rayleigh_ritz<S>(X, AX, ld, m, m, dim, tau, sm, partial, npart, st, s, msg, false);
+          if (r) return r;
+          const int nxt = cur ^ 1;
+          CK(launch_update<S>(X, ld, m, sm.C, m, m, dim, Sb[nxt], ld, 1.0, 0.0, s));
+          CK(launch_update<S>(AX, ld, m, sm.C, m, m, dim, ASb[nxt], ld, 1.0, 0.0, s));
+          CK(cudaMemcpyAsync(th_dev, sm.theta, sizeof(double) * m, cudaMemcpyDeviceToDevice, s));
+          cur = nxt;
+          continue;
+        }
         converged = true;
         break;
       }
@@ -312,7 +332,9 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
       zd* X64 = ws.get<zd>("fin_X", (size_t)dim * 2 * mm, &err);
       zd* T64 = ws.get<zd>("fin_T", (size_t)dim * mm, &err);
       if (!chk()) goto oom;
-      // fresh H X (the iteration's AX is a running linear combination)
+      // fresh H X in the operator's most accurate arithmetic (the iteration's AX is a running linear
+      // combination of cheaper applications)
+      op.begin_refine();
       CK(op.apply(X, ld, 0, mm, AXs, ld, s));
       CK((launch_convert_cols<S, double>(X, ld, X64, 2 * mm, mm, dim, s)));
       CK((launch_convert_cols<S, double>(AXs, ld, X64 + mm, 2 * mm, mm, dim, s)));
@@ -361,8 +383,9 @@ oom:
 }
 
 template int lobpcg_solve<float>(Operator<float>&, const double*, int, int, int, double, int, Workspace&, DevStatus*,
-                                 cudaStream_t, std::vector<double>*, zd*, SolveStats*, std::string*);
+                                 cudaStream_t, std::vector<double>*, zd*, SolveStats*, std::string*, double);
 template int lobpcg_solve<double>(Operator<double>&, const double*, int, int, int, double, int, Workspace&,
-                                  DevStatus*, cudaStream_t, std::vector<double>*, zd*, SolveStats*, std::string*);
+                                  DevStatus*, cudaStream_t, std::vector<double>*, zd*, SolveStats*, std::string*,
+                                  double);
 
 }  // namespace wtb

@@ -53,6 +53,8 @@ struct Operator {
   virtual ~Operator() {}
   // Y[:, c0:c0+ncol] = H X[:, c0:c0+ncol]
   virtual cudaError_t apply(const cplx<S>* X, int ldx, int c0, int ncol, cplx<S>* Y, int ldy, cudaStream_t s) = 0;
+  // switches the operator to its most accurate arithmetic; returns false if it has only one
+  virtual bool begin_refine() { return false; }
   long matvec_columns = 0;
 };
 
@@ -99,6 +101,7 @@ struct MatFreeOperator : Operator<S> {
   const double* dE = nullptr;
   GemmKind kind = GEMM_SIMT_F32;
   int nslices = 2, npairs = 3;
+  int npairs_refine = 0;  // > npairs: slice products used by begin_refine() (needs nslices = 3)
   int pa[8] = {0}, pb[8] = {0};
   int Mpad = 0, Kpad = 0, Npad = 0;
   // contraction operands
@@ -109,12 +112,17 @@ struct MatFreeOperator : Operator<S> {
   void* Tm = nullptr;             // [Mpad][Npad] float (TC) or S (SIMT)
   DevStatus* st = nullptr;
   KernelProfile* prof = nullptr;
-  std::map<int, TcGemmPlan*> plans;  // keyed by N of the chunk
+  std::map<long, TcGemmPlan*> plans;  // keyed by (N of the chunk, slice products)
   std::string* msg = nullptr;
   ~MatFreeOperator() override {
     for (auto& kv : plans) tc_gemm_plan_destroy(kv.second);
   }
   cudaError_t apply(const cplx<S>* X, int ldx, int c0, int ncol, cplx<S>* Y, int ldy, cudaStream_t s) override;
+  bool begin_refine() override {
+    if (npairs_refine <= npairs) return false;
+    npairs = npairs_refine;
+    return true;
+  }
 };
 
 struct SolveStats {
@@ -127,16 +135,18 @@ struct SolveStats {
 
 // Lowest nev eigenpairs of the Hermitian operator.  diag = its diagonal (preconditioner and start
 // vectors).  Output: E (host, nev) and the FP64 eigenvectors Xout (device, dim x nev row-major).
+// tol_refine > 0: once tol is met, switch the operator to its accurate arithmetic (begin_refine) and
+// continue to tol_refine.
 template <class S>
 int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, double tol, int maxit,
                  Workspace& ws, DevStatus* st, cudaStream_t s, std::vector<double>* E, zd* Xout, SolveStats* stats,
-                 std::string* msg);
+                 std::string* msg, double tol_refine = 0.0);
 
 // extra launchers used by the solver
 cudaError_t launch_jacobi_eig_f32(zd* A, int lda, int n, double* evals, zd* evecs, int ldv, int sweeps,
                                   DevStatus* st, cudaStream_t s);
 cudaError_t launch_mark_dropped(zd* G, int ldg, int n, const int* keep, cudaStream_t s);
-cudaError_t launch_select_lowest(const double* diag, int dim, int m, int* idx, cudaStream_t s);
+cudaError_t launch_select_lowest(const double* diag, int dim, int m, int* idx, double* cand_val, cudaStream_t s);
 template <class S>
 cudaError_t launch_init_guess(cplx<S>* X, int ldx, int dim, int m, const int* idx, unsigned seed, cudaStream_t s);
 void tc_gemm_set_valid(TcGemmPlan* p, int m_valid, int n_valid);

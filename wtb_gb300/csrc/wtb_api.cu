@@ -31,6 +31,9 @@ struct wtb_ctx {
   int nk = 0, nv = 0, nc = 0;
   int ngrid[3] = {0, 0, 0};
   std::vector<double> kpt;  // nk x 3 row-major
+  // the k-points are the Monkhorst-Pack mesh of ngrid (set by the solver entry points); a caller-supplied
+  // k-point list (wtb_eigsys_mesh) clears it and the V(k,k') table is then evaluated pair by pair
+  bool mesh_mp = false;
   // last BSE operator data (for wtb_optsp)
   bool have_hr_optics = false;
   KernelProfile prof;
@@ -251,6 +254,44 @@ CoulParams coul_of(wtb_ctx* c, const wtb_bse_params* p) {
   return cp;
 }
 
+// V(k,k') for the bands of the context into V (leading dimension ldv)
+int coulomb_table_into(wtb_ctx* c, const wtb_bse_params* p, double* V, int ldv) {
+  cudaError_t err;
+  const int nk = c->nk;
+  const bool mp = c->mesh_mp && p->ngrid[0] == c->ngrid[0] && p->ngrid[1] == c->ngrid[1] &&
+                  p->ngrid[2] == c->ngrid[2] && (long)p->ngrid[0] * p->ngrid[1] * p->ngrid[2] == nk;
+  if (mp) {
+    // reciprocal vectors exactly as the mesh was built (recvec, src/module_kmesh.F90:391-407)
+    const double* r = c->rlat_rm;
+    auto cross = [](const double* u, const double* v, double* o) {
+      o[0] = u[1] * v[2] - u[2] * v[1];
+      o[1] = u[2] * v[0] - u[0] * v[2];
+      o[2] = u[0] * v[1] - u[1] * v[0];
+    };
+    double v23[3], v31[3], v12[3], bl[9];
+    cross(r + 3, r + 6, v23);
+    cross(r + 6, r, v31);
+    cross(r, r + 3, v12);
+    const double vol = std::fabs(r[0] * v23[0] + r[1] * v23[1] + r[2] * v23[2]);
+    const double f = (2.0 * (double)3.14159274101257324f) / vol;
+    for (int d = 0; d < 3; ++d) {
+      bl[d] = f * v23[d];
+      bl[3 + d] = f * v31[d];
+      bl[6 + d] = f * v12[d];
+    }
+    double* dbl = c->ws.get<double>("recip", 9, &err);
+    const long ns = (2L * p->ngrid[0] - 1) * (2L * p->ngrid[1] - 1) * (2L * p->ngrid[2] - 1);
+    double* stn = c->ws.get<double>("vstencil", ns, &err);
+    CKC(err);
+    CKC(cudaMemcpyAsync(dbl, bl, sizeof(bl), cudaMemcpyHostToDevice, c->s));
+    CKC(launch_coulomb_mesh(coul_of(c, p), dbl, stn, V, ldv, c->s));
+  } else {
+    const double* kd = c->ws.get<double>("kpt", 0, &err);
+    CKC(launch_coulomb(coul_of(c, p), kd, nk, kd, nk, V, ldv, c->s));
+  }
+  return WTB_OK;
+}
+
 int auto_block(const wtb_bse_params* p, int dim, bool fp64) {
   int m = p->block > 0 ? p->block : std::max(p->nev + 6, (3 * p->nev + 1) / 2);
   if (p->block <= 0) m = (m + 7) / 8 * 8;
@@ -282,8 +323,7 @@ int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob) 
   const int Kpad = (nk + 63) / 64 * 64, Mpad = (nk + 127) / 128 * 128;
   double* V = c->ws.get<double>("V", (size_t)Mpad * Kpad, &err, true);
   CKC(err);
-  const double* kd = c->ws.get<double>("kpt", 0, &err);
-  CKC(launch_coulomb(coul_of(c, p), kd, nk, kd, nk, V, Kpad, c->s));
+  CKR(coulomb_table_into(c, p, V, Kpad));
   ob->dE = dE;
   ob->dim = dim;
   const bool fp64 = p->precision == WTB_PREC_FP64;
@@ -341,10 +381,13 @@ int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob) 
   if (!tc_gemm_available()) return set_err(c, WTB_ENODEV, "the split-BF16 tensor-core path needs an sm_103 device");
   op->kind = GEMM_TC_BF16;
   const bool x6 = p->precision == WTB_PREC_BF16X6;
-  op->nslices = x6 ? 3 : 2;
+  // three slices in both modes: bf16x3 iterates with the 3 leading slice products and applies all 6
+  // for the final refinement
+  op->nslices = 3;
   op->npairs = x6 ? 6 : 3;
+  op->npairs_refine = 6;
   const int pa6[6] = {0, 0, 1, 0, 1, 2}, pb6[6] = {0, 1, 0, 2, 1, 0};
-  for (int i = 0; i < op->npairs; ++i) {
+  for (int i = 0; i < 6; ++i) {
     op->pa[i] = pa6[i];
     op->pb[i] = pb6[i];
   }
@@ -367,8 +410,12 @@ int run_solve(wtb_ctx* c, const wtb_bse_params* p, std::vector<double>* E, wtb_t
   CKC(cudaEventRecord(ev[0], c->s));
   const bool fp64 = p->precision == WTB_PREC_FP64;
   const int m = auto_block(p, dim, fp64);
-  // default residual targets: SLEPc's 1e-8 in FP64; the FP32 rounding floor of the operator otherwise
-  const double tol = p->tol > 0 ? p->tol : (fp64 ? 1e-8 : (p->precision == WTB_PREC_BF16X3 ? 1e-4 : 1e-5));
+  // residual targets: SLEPc's 1e-8 in FP64; 1e-5 (about the FP32 rounding floor of the operator) otherwise.
+  // bf16x3 runs in two phases: its 3-product operator to 1e-4, then the 6-product operator to the target.
+  const bool two_phase = p->op == WTB_OP_MATFREE && p->precision == WTB_PREC_BF16X3;
+  const double tol_final = p->tol > 0 ? p->tol : (fp64 ? 1e-8 : 1e-5);
+  const double tol = two_phase ? std::max(tol_final, 1e-4) : tol_final;
+  const double tol_refine = two_phase && tol_final < tol ? tol_final : 0.0;
   const int maxit = p->maxit > 0 ? p->maxit : 200;
   zd* Xout = c->ws.get<zd>("Xout", (size_t)dim * p->nev, &err);
   CKC(err);
@@ -380,7 +427,8 @@ int run_solve(wtb_ctx* c, const wtb_bse_params* p, std::vector<double>* E, wtb_t
   if (ob.o64)
     rc = lobpcg_solve<double>(*ob.o64, ob.dE, dim, p->nev, m, tol, maxit, c->ws, c->st, c->s, E, Xout, stats, &msg);
   else
-    rc = lobpcg_solve<float>(*ob.o32, ob.dE, dim, p->nev, m, tol, maxit, c->ws, c->st, c->s, E, Xout, stats, &msg);
+    rc = lobpcg_solve<float>(*ob.o32, ob.dE, dim, p->nev, m, tol, maxit, c->ws, c->st, c->s, E, Xout, stats, &msg,
+                             tol_refine);
   if (!ob.msg.empty()) msg += " (" + ob.msg + ")";
   CKC(cudaEventRecord(ev[2], c->s));
   CKC(cudaEventSynchronize(ev[2]));
@@ -547,6 +595,7 @@ int wtb_eigsys_mesh(wtb_ctx* c, int nk, const double* kpt, int nv, int nc, doubl
   for (int i = 0; i < nk; ++i)
     for (int d = 0; d < 3; ++d) k[3 * i + d] = kpt[i + (size_t)nk * d];
   CKR(upload_bands(c, nk, k.data(), nv, nc));
+  c->mesh_mp = false;
   const int nb = nv + nc, w = c->w;
   cudaError_t err;
   if (eigv) {
@@ -603,6 +652,7 @@ static int ensure_bands_for(wtb_ctx* c, const wtb_bse_params* p) {
   mp_mesh(p->ngrid[0], p->ngrid[1], p->ngrid[2], p->mshift, c->rlat_rm, c->rlat_rm + 3, c->rlat_rm + 6, k.data());
   CKR(upload_bands(c, nk, k.data(), p->nv, p->nc));
   for (int d = 0; d < 3; ++d) c->ngrid[d] = p->ngrid[d];
+  c->mesh_mp = true;
   return WTB_OK;
 }
 
@@ -651,8 +701,7 @@ int wtb_bse_build(wtb_ctx* c, const wtb_bse_params* p, double* hbse) {
   const int Kpad = (nk + 63) / 64 * 64;
   double* V = c->ws.get<double>("V", (size_t)((nk + 127) / 128 * 128) * Kpad, &err, true);
   CKC(err);
-  const double* kd = c->ws.get<double>("kpt", 0, &err);
-  CKC(launch_coulomb(coul_of(c, p), kd, nk, kd, nk, V, Kpad, c->s));
+  CKR(coulomb_table_into(c, p, V, Kpad));
   const zd* vw = c->ws.get<zd>("vec_win", 0, &err);
   zd* staging = nullptr;
   if (p->precision == WTB_PREC_FP64) {

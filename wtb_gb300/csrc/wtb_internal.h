@@ -101,6 +101,10 @@ cudaError_t launch_optics(const zd* hr, const int* rvec, const int* ndegen, int 
 // V(k,k') table, double, leading dimension ldv (>= nk), zero padding left as is.
 cudaError_t launch_coulomb(const CoulParams& p, const double* kpt1, int n1, const double* kpt2, int n2,
                            double* V, int ldv, cudaStream_t s);
+// The same table on a Monkhorst-Pack mesh from the reciprocal vectors bl (3 x 3 row-major), through the
+// (2n1-1)(2n2-1)(2n3-1) distinct values of k - k' (stencil scratch of that size).
+cudaError_t launch_coulomb_mesh(const CoulParams& p, const double* bl, double* stencil, double* V, int ldv,
+                                cudaStream_t s);
 // Transition energies dE[I] = E_c - E_v.
 cudaError_t launch_transition_energies(const double* eig_win, int nk, int nv, int nc, double* dE, cudaStream_t s);
 
