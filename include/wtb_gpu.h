@@ -167,6 +167,18 @@ int wtb_bsedielraw(wtb_ctx* ctx, const wtb_bse_params* p, int dimse, const doubl
  * refractive index, extinction coefficient, reflectivity, absorption coefficient, energy-loss function. */
 int wtb_bseoptprop(wtb_ctx* ctx, int numbse, const double* dielf, double* props);
 
+/* Allocation-free variant of wtb_dielbse, for callers that cannot allocate device memory: their device
+ * memory belongs to another allocator (a framework's caching pool, a host program's preallocated arena)
+ * or they must not pay cudaMalloc's implicit device synchronisation.  It has no counterpart in the
+ * reference.  Every pointer is a device pointer owned by the caller: excitonvec(dimse, dimse1) and
+ * hopt1/hopt2(dimse) complex(8) in Fortran order, activity(dimse) real(8); stream may be NULL.  The
+ * partial sums live in one fixed 2 MiB device array per GPU (held until the process exits), so
+ * ceil(dimse/1024) * dimse1 * 4 must not exceed 262144; larger calls return WTB_EBADARG (reason on stderr).
+ * All calls share that array: calls that overlap on the GPU race and must be ordered.  The first call on
+ * a device looks up the array's address; make it before any stream capture. */
+int wtb_dielbse_noalloc(int dimse, int dimse1, const double* excitonvec, const double* hopt1,
+                        const double* hopt2, int pair, double* activity, void* stream);
+
 /* Number of CUDA kernels this library has launched in the process (instrumentation for benchmarks). */
 long long wtb_kernel_launch_count(void);
 
