@@ -38,6 +38,8 @@ WORKLOADS = {
                   "lowest 10 excitons",
     "cubic16_16x16x16": "simple cubic w=16, |R|<=2a (33 R), 16^3 k-mesh, 3v+3c, BSE dim 36864, V3DL eps=8, "
                         "lowest 20 excitons",
+    "batch64": "64 independent 2D hexagonal w=8 systems (on-site strain U(-0.2,0.2) eV), n x n meshes n in 12..36, "
+               "(nv,nc) in {(2,2),(3,3)}, BSE dim 676..11664, lowest 6 excitons each",
 }
 
 
@@ -207,6 +209,63 @@ def run_reference(args):
     return 0
 
 
+def run_batch(args, torch, api, S, world, local):
+    """systems/s over the 64-system batch: one step = the whole batch through wtb_batch_bsesolver (its
+    workers' streams overlap on the device; the call returns when every system is done)."""
+    from wtb_gb300 import batch as B
+
+    everything = S.strained_batch(nsys=64)
+    rank = int(os.environ.get("RANK", "0"))
+    # the 64 systems are split across ranks by the longest-processing-time partition (no collective on the
+    # data path; only the step time is reduced)
+    part = B.lpt_partition([B.system_cost(p, s.w90basis) for s, p in everything], world)[rank]
+    items = [everything[i] for i in part]
+    b = api.Batch(local, nworkers=args.workers)
+    kw = dict(precision=args.precision, op="matfree", tol=args.tol)
+    for _ in range(args.warmup):
+        b.bsesolver(items, **kw)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = api.kernel_launch_count()
+    side = torch.cuda.Stream()
+    ms = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(side)
+        out, _ = b.bsesolver(items, **kw)
+        e1.record(side)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    launches = api.kernel_launch_count() - launches0
+    clk = clocks.stop()
+    tot = sum(ms)
+    b.close()
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([tot], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot = float(t.item())
+    value = len(everything) * args.steps / (tot / 1000.0)
+    h2d = sum(s.hop.nbytes + s.ihop.nbytes for s, _ in items)
+    d2h = sum(p.dim * 8 * 9 for _, p in items)
+    line = {"metric": "exciton systems/s (BSE build + lowest-6 solve, 64-system batch)", "value": value,
+            "unit": "systems/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": tot / args.steps, "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
+            "dtype": args.precision, "data": "synthetic (seeded H(R))",
+            "config": {"workload": "batch64", "systems_this_rank": len(items), "sharding": "LPT over ranks", "description": WORKLOADS["batch64"], "workers": args.workers,
+                       "precision": args.precision, "l2": "inputs and operators of 64 systems exceed L2 per step",
+                       "timing": "events on a side stream around the blocking batch call"},
+            "e2e": {"value": value, "unit": "systems/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches), "clocks": clk,
+            "iterations": {"max": max(o["iterations"] for o in out), "mean": float(np.mean([o["iterations"] for o in out]))}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -220,6 +279,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--ref-matvecs", type=int, default=800)
     ap.add_argument("--ref-budget", type=float, default=12.0)
+    ap.add_argument("--workers", type=int, default=8, help="batch64: concurrent contexts")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -235,6 +295,11 @@ def main():
     from wtb_gb300 import api
     from wtb_gb300 import synthetic as S
 
+    if args.workload == "batch64":
+        r = run_batch(args, torch, api, S, world, local)
+        if world > 1:
+            dist.destroy_process_group()
+        return r
     # one independent replica of the workload per GPU (systems are independent; no collective)
     sysm, p = S.workload(args.workload)
     ctx = api.Context(local)

@@ -179,6 +179,65 @@ int wtb_bseoptprop(wtb_ctx* ctx, int numbse, const double* dielf, double* props)
 int wtb_dielbse_noalloc(int dimse, int dimse1, const double* excitonvec, const double* hopt1,
                         const double* hopt2, int pair, double* activity, void* stream);
 
+/* Reverse-mode gradient of a loss L(E, f) through the last wtb_bsesolver call, which it requires (same
+ * parameters, p->nev <= 16).  E_n are the exciton energies and f_n = |sum_j A(j,n) hrx(j)|^2 the xx
+ * activities of that call (dielbsev, src/module_bse.F90:201-245).  Inputs: dL_dE(nev), dL_dfxx(nev) (either
+ * may be NULL = zero).  Outputs (each may be NULL): dL_dhop, dL_dihop (nvec, w, w) in the layout of
+ * hopmatrices/ihopmatrices (wtb_set_hr), and dL_dr0 (the R_0 screening length of V2DRK; 0 for the other
+ * potentials).  The forward arithmetic differentiated is that of eigsys (src/module_hamiltonian.F90:200-320,
+ * with the first-component-real eigenvector gauge and ZHEEV('L') reading the lower triangle), matrizelbse
+ * (src/module_bse.F90:24-83), v2drk (src/module_coulomb.F90:286-350) and hlm/optsp
+ * (src/module_optics.F90:12-167).  Degenerate excitons (|E_m - E_n| < 1e-9 eV) or degenerate bands have
+ * no individual derivative; their mutual terms are dropped.  Not in the reference (it has no gradients).
+ * t->iterations = iterations of the adjoint linear solve, t->t_total_ms = device time. */
+int wtb_bse_backward(wtb_ctx* ctx, const wtb_bse_params* p, const double* dL_dE, const double* dL_dfxx,
+                     double* dL_dhop, double* dL_dihop, double* dL_dr0, wtb_timings* t);
+
+/* Least-squares spectrum loss L = sum_j (spinf eps2_xx(omega_j) - target_j)^2 on the omega grid of p
+ * (ebse0..ebsef, numbse points), with eps2_xx the Lorentzian sum of bsedielraw (src/module_bse.F90:835-1036,
+ * optdiel/avgsme src/module_optics.F90:171-335, no imagrenorm) over the dimse rows whose first nev hold the
+ * exciton energies E and activities fxx (rows past nev are zero).  Returns L, dL/dE(nev) and dL/dfxx(nev)
+ * (either may be NULL), the cotangents wtb_bse_backward takes.  1 <= nev <= 64. */
+int wtb_spectrum_loss(wtb_ctx* ctx, const wtb_bse_params* p, int dimse, int nev, const double* E,
+                      const double* fxx, const double* target, double* L, double* dL_dE, double* dL_dfxx);
+
+/* ---------------------------------------------------------------------------------------------- */
+/* batches of independent systems (strain variants, meshes of uneven size) */
+
+/* One system's H(R), with the argument meanings of wtb_set_hr (hamiltonian_input_read,
+ * src/module_hamiltonian.F90:35-194).  The arrays are read during wtb_batch_bsesolver only. */
+typedef struct wtb_system {
+  int w90basis, nvec;
+  const int* rvec;             /* nvec x 3 */
+  const int* ffactor;          /* nvec */
+  const double* hopmatrices;   /* nvec x w x w */
+  const double* ihopmatrices;  /* nvec x w x w */
+  const double* rlat;          /* 3 x 3 */
+  double efermi, scs;
+  int systype_np;
+} wtb_system;
+
+typedef struct wtb_batch wtb_batch;
+
+/* A pool of nworkers contexts on one device, each with its own stream and host thread, so that the solves of
+ * several small systems overlap on the GPU.  The reference runs one bsesolver per process and input; a batch
+ * of independent inputs is what its strain scans and mesh-convergence series do by relaunching it. */
+int wtb_batch_create(wtb_batch** batch, int device, int nworkers);
+int wtb_batch_destroy(wtb_batch* batch);
+
+/* wtb_bsesolver for nsys independent systems: system i uses sys[i] and p[i] (p[i].nev <= nev_stride).  Systems
+ * are handed to the workers largest first (cost ~ Nk^2 w^2 nev of the matrix-free operator).  Outputs, for the
+ * first p[i].nev excitons of system i:
+ *   E[i * nev_stride + n]               exciton energies (eV)
+ *   act[(i * 8 + a) * nev_stride + n]   activities a = xx yy zz xy xz yz sp sm (dielbsev/dielbsep)
+ *   status[i]                           WTB_OK or the system's error (text: wtb_batch_error(batch, i))
+ *   iterations[i]                       eigensolver iterations (may be NULL)
+ * Returns WTB_OK when every system succeeded, else the first failing system's status.  wall_ms (may be NULL)
+ * is the host wall time of the whole batch. */
+int wtb_batch_bsesolver(wtb_batch* batch, int nsys, const wtb_system* sys, const wtb_bse_params* p, int nev_stride,
+                        double* E, double* act, int* status, int* iterations, double* wall_ms);
+const char* wtb_batch_error(const wtb_batch* batch, int i);
+
 /* Number of CUDA kernels this library has launched in the process (instrumentation for benchmarks). */
 long long wtb_kernel_launch_count(void);
 

@@ -41,6 +41,25 @@ def make(name):
     print(name, r["E"])
 
 
+def make_fit_target(name="hex8_36x36", r0_true=44.0, noise=1e-3, seed=2024):
+    """Target xx absorption spectrum of the fitting case: the oracle's spinf * eps2_xx at the perturbed
+    screening length r0_true plus seeded N(0, noise) noise (no imagrenorm)."""
+    sysm, p = S.workload(name)
+    p.r0 = r0_true
+    r = O.bsesolver(sysm, p, dense_solver=False)
+    spinf = 2.0 if sysm.systype == "NP" else 1.0
+    spec = O.bsedielraw(r["Ws"], r["acts"], p.ngrid, sysm.rlat, p, spinf=spinf)
+    p.renorm = False
+    spec_raw = O.bsedielraw(r["Ws"], r["acts"], p.ngrid, sysm.rlat, p, spinf=spinf)
+    rng = np.random.default_rng(seed)
+    target = spec_raw["xx"][:, 2] + rng.normal(0.0, noise, p.numbse)
+    np.savez_compressed(os.path.join(HERE, name + "_fit_target.npz"), digest=np.array(input_digest(sysm)),
+                        r0_true=np.array(r0_true), E=r["E"], fxx=r["acts"]["xx"][: p.nev], target=target,
+                        spec_xx_renorm=spec["xx"][:, 2])
+    print(name, "fit target at r0 =", r0_true, r["E"])
+
+
 if __name__ == "__main__":
     for n in ("hex8_6x6", "hex8_24x24"):
         make(n)
+    make_fit_target()

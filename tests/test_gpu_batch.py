@@ -1,0 +1,67 @@
+"""wtb_batch_* against single-context solves and the oracle (independent systems solved concurrently).
+
+Tolerances: batch vs single-context solve of the same system 1e-9 eV (the same kernels on another stream;
+only the order of a floating-point reduction in the small eigensolver's stopping test may differ); against
+the oracle 1e-5 eV, activities 1e-4 relative to the largest."""
+import numpy as np
+import pytest
+
+from oracle import wtb_oracle as O
+from wtb_gb300 import api
+from wtb_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def items():
+    full = S.strained_batch(nsys=64)
+    # the 6 smallest systems of the C4 batch keep the test short
+    order = sorted(range(len(full)), key=lambda i: full[i][1].dim)
+    return [full[i] for i in order[:6]]
+
+
+@pytest.mark.parametrize("prec", ["fp64", "bf16x3"])
+def test_batch_matches_single_context(ctx, items, prec):
+    b = api.Batch(0, nworkers=4)
+    try:
+        out, wall = b.bsesolver(items, precision=prec, op="matfree")
+    finally:
+        b.close()
+    assert wall > 0
+    for (s, p), o in zip(items, out):
+        assert o["status"] == 0 and o["iterations"] > 0
+        ctx.set_hr(s)
+        ref = ctx.bsesolver(p, precision=prec, op="matfree")
+        np.testing.assert_allclose(o["E"], ref["E"], atol=1e-9)
+        for c in ("xx", "yy", "sp"):
+            np.testing.assert_allclose(o["acts"][c], ref["acts"][c][: p.nev], atol=1e-9 * max(1.0, np.abs(ref["acts"][c]).max()))
+
+
+def test_batch_against_oracle(items):
+    b = api.Batch(0, nworkers=3)
+    try:
+        out, _ = b.bsesolver(items[:3], precision="bf16x3", op="matfree")
+    finally:
+        b.close()
+    for (s, p), o in zip(items[:3], out):
+        ref = O.bsesolver(s, p)
+        np.testing.assert_allclose(o["E"], ref["E"], atol=1e-5)
+        fx = ref["acts"]["xx"][: p.nev]
+        np.testing.assert_allclose(o["acts"]["xx"], fx, atol=1e-4 * np.abs(fx).max())
+
+
+def test_batch_reports_failing_system_and_finishes_the_rest(items):
+    bad_s, bad_p = items[0][0].copy(), items[0][1]
+    bad_s.efermi = -1e3  # no occupied band: "Number of valence states higher then ocuppied states"
+    batch = [items[1], (bad_s, bad_p), items[2]]
+    b = api.Batch(0, nworkers=2)
+    try:
+        out, _ = b.bsesolver(batch, precision="bf16x3", op="matfree", raise_on_error=False)
+        with pytest.raises(api.WTBError):
+            b.bsesolver(batch, precision="bf16x3", op="matfree")
+    finally:
+        b.close()
+    assert out[0]["status"] == 0 and out[2]["status"] == 0
+    assert out[1]["status"] != 0
+    assert "valence" in out[1]["error"]

@@ -22,6 +22,7 @@ LIB_PATH = os.path.join(_HERE, "libwtb_gb300.so")
 WTB_OK, WTB_EBADARG, WTB_ENOMEM, WTB_ENOCONV, WTB_ETIMEOUT, WTB_ENAN, WTB_ECUDA, WTB_ESTATE, WTB_ENODEV = range(9)
 STATUS_NAMES = {0: "WTB_OK", 1: "WTB_EBADARG", 2: "WTB_ENOMEM", 3: "WTB_ENOCONV", 4: "WTB_ETIMEOUT",
                 5: "WTB_ENAN", 6: "WTB_ECUDA", 7: "WTB_ESTATE", 8: "WTB_ENODEV"}
+STATUS = {v: k for k, v in STATUS_NAMES.items()}
 PREC = {"fp64": 0, "fp32": 1, "bf16x3": 2, "bf16x6": 3}
 OPS = {"dense": 0, "matfree": 1}
 COULTYPES = {"V2DK": 0, "V3D": 1, "V3DL": 2, "V2DT": 3, "V2DT2": 4, "V2DOH": 5, "V2DRK": 6, "V1DT": 7, "V0DT": 8}
@@ -43,6 +44,12 @@ class CParams(C.Structure):
                 ("cshift", C.c_double), ("ebse0", C.c_double), ("ebsef", C.c_double), ("numbse", C.c_int),
                 ("nev", C.c_int), ("precision", C.c_int), ("op", C.c_int), ("tol", C.c_double),
                 ("maxit", C.c_int), ("block", C.c_int)]
+
+
+class CSystem(C.Structure):
+    _fields_ = [("w90basis", C.c_int), ("nvec", C.c_int), ("rvec", C.POINTER(C.c_int)), ("ffactor", C.POINTER(C.c_int)),
+                ("hopmatrices", C.POINTER(C.c_double)), ("ihopmatrices", C.POINTER(C.c_double)),
+                ("rlat", C.POINTER(C.c_double)), ("efermi", C.c_double), ("scs", C.c_double), ("systype_np", C.c_int)]
 
 
 class CTimings(C.Structure):
@@ -76,11 +83,18 @@ def _load():
         "wtb_bsesolver": [P, C.POINTER(CParams), dp, dp, dp, C.POINTER(CTimings)],
         "wtb_bsedielraw": [P, C.POINTER(CParams), C.c_int, dp, dp, dp],
         "wtb_bseoptprop": [P, C.c_int, dp, dp],
+        "wtb_bse_backward": [P, C.POINTER(CParams), dp, dp, dp, dp, dp, C.POINTER(CTimings)],
+        "wtb_spectrum_loss": [P, C.POINTER(CParams), C.c_int, C.c_int, dp, dp, dp, dp, dp, dp],
+        "wtb_batch_create": [C.POINTER(P), C.c_int, C.c_int],
+        "wtb_batch_destroy": [P],
+        "wtb_batch_bsesolver": [P, C.c_int, C.POINTER(CSystem), C.POINTER(CParams), C.c_int, dp, dp, ip, ip, dp],
     }
     for name, args in sigs.items():
         f = getattr(lib, name)
         f.argtypes = args
         f.restype = C.c_int
+    lib.wtb_batch_error.argtypes = [P, C.c_int]
+    lib.wtb_batch_error.restype = C.c_char_p
     lib.wtb_last_error.argtypes = [P]
     lib.wtb_last_error.restype = C.c_char_p
     lib.wtb_version.restype = C.c_int
@@ -282,6 +296,38 @@ class Context:
             out["HE"] = HE
         return out
 
+    def bse_backward(self, p: BSEParams, dL_dE=None, dL_dfxx=None, precision="fp64"):
+        """Gradient of L(E, f_xx) through the last bsesolver call (same p and precision): returns dict with
+        dhop, dihop (nvec, w, w), dr0 and the timings.  dL_dE / dL_dfxx: (nev,) or None (zero)."""
+        s = self.system
+        dh = np.zeros((s.nvec, s.w90basis, s.w90basis), order="F")
+        di = np.zeros_like(dh, order="F")
+        dr0 = C.c_double(0.0)
+        t = CTimings()
+        cp = cparams(p, precision=precision, op="matfree")
+        a = None if dL_dE is None else np.ascontiguousarray(dL_dE, dtype=np.float64)
+        b = None if dL_dfxx is None else np.ascontiguousarray(dL_dfxx, dtype=np.float64)
+        self._chk(_lib.wtb_bse_backward(self._h, C.byref(cp), _dp(a), _dp(b), _dp(dh), _dp(di),
+                                        C.cast(C.byref(dr0), C.POINTER(C.c_double)), C.byref(t)),
+                  "wtb_bse_backward")
+        return {"dhop": np.array(dh), "dihop": np.array(di), "dr0": dr0.value,
+                "timings": {f: getattr(t, f) for f, _ in CTimings._fields_}}
+
+    def spectrum_loss(self, p: BSEParams, dimse, E, fxx, target):
+        """L = sum_j (spinf eps2_xx(omega_j) - target_j)^2 and its cotangents (dL/dE, dL/dfxx)."""
+        E = np.ascontiguousarray(E, dtype=np.float64)
+        f = np.ascontiguousarray(fxx, dtype=np.float64)
+        tg = np.ascontiguousarray(target, dtype=np.float64)
+        nev = len(E)
+        L = C.c_double(0.0)
+        gE = np.zeros(nev)
+        gf = np.zeros(nev)
+        cp = cparams(p)
+        self._chk(_lib.wtb_spectrum_loss(self._h, C.byref(cp), int(dimse), nev, _dp(E), _dp(f), _dp(tg),
+                                         C.cast(C.byref(L), C.POINTER(C.c_double)), _dp(gE), _dp(gf)),
+                  "wtb_spectrum_loss")
+        return L.value, gE, gf
+
     def bsedielraw(self, p: BSEParams, Ws, acts):
         """Returns dict comp -> (numbse, 3) [omega, eps1, eps2] for xx yy zz xy xz yz."""
         Ws = np.asarray(Ws, dtype=np.float64)
@@ -305,3 +351,59 @@ class Context:
         names = ("refr", "ext", "refl", "abs", "eloss")
         return {nm: {cname: props[:, i, q].copy() for i, cname in enumerate(COMPONENTS[:6])}
                 for q, nm in enumerate(names)}
+
+
+class Batch:
+    """A pool of ``nworkers`` contexts on one device solving independent systems concurrently
+    (``wtb_batch_*``)."""
+
+    def __init__(self, device: int = 0, nworkers: int = 8):
+        h = C.c_void_p()
+        r = _lib.wtb_batch_create(C.byref(h), int(device), int(nworkers))
+        if r:
+            raise WTBError(r, "wtb_batch_create failed")
+        self._h = h
+
+    def close(self):
+        if self._h:
+            _lib.wtb_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def bsesolver(self, items, precision="bf16x3", op="matfree", tol=0.0, maxit=0, raise_on_error=True):
+        """items: list of (TBSystem, BSEParams).  Returns (list of dicts {E, acts, status, error, iterations},
+        host wall ms of the batch)."""
+        n = len(items)
+        nev_stride = max(p.nev for _, p in items) if n else 1
+        keep = []
+        systems = (CSystem * max(n, 1))()
+        params = (CParams * max(n, 1))()
+        for i, (s, p) in enumerate(items):
+            arrs = (np.asfortranarray(s.rvec.astype(np.int32)), np.asfortranarray(s.ffactor.astype(np.int32)),
+                    _f64(s.hop), _f64(s.ihop), _f64(s.rlat))
+            keep.append(arrs)
+            systems[i] = CSystem(int(s.w90basis), int(s.nvec), _ip(arrs[0]), _ip(arrs[1]), _dp(arrs[2]), _dp(arrs[3]),
+                                 _dp(arrs[4]), float(s.efermi), float(s.scs), 1 if s.systype == "NP" else 0)
+            params[i] = cparams(p, precision=precision, op=op, tol=tol, maxit=maxit)
+        E = np.zeros((n, nev_stride))
+        acts = np.zeros((n, 8, nev_stride))
+        status = np.zeros(n, dtype=np.int32)
+        iters = np.zeros(n, dtype=np.int32)
+        wall = np.zeros(1)
+        r = _lib.wtb_batch_bsesolver(self._h, n, systems, params, nev_stride, _dp(E), _dp(acts), _ip(status),
+                                     _ip(iters), _dp(wall))
+        out = []
+        for i, (_, p) in enumerate(items):
+            err = _lib.wtb_batch_error(self._h, i)
+            out.append({"E": E[i, :p.nev].copy(),
+                        "acts": {c: acts[i, a, :p.nev].copy() for a, c in enumerate(COMPONENTS)},
+                        "status": int(status[i]), "error": err.decode() if err else "", "iterations": int(iters[i])})
+        if r and raise_on_error:
+            bad = next(i for i in range(n) if status[i])
+            raise WTBError(int(r), f"wtb_batch_bsesolver: system {bad}: {out[bad]['error']}")
+        return out, float(wall[0])

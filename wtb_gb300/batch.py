@@ -1,8 +1,9 @@
 """Batches of independent exciton systems (strain variants, k-meshes of uneven size).
 
 Systems are independent, so a batch shards across GPUs with no data-path collective: each rank solves
-the systems a longest-processing-time-first partition assigns to it (cost ~ dim^3 of the dense problem
-it replaces) and the results are gathered on the host.  One rank drives one GPU.
+the systems a longest-processing-time-first partition assigns to it (cost model ``system_cost``) and the
+results are gathered on the host.  One rank drives one GPU; on that GPU ``api.Batch`` overlaps the
+rank's systems on several streams.
 """
 from __future__ import annotations
 
@@ -10,9 +11,14 @@ import heapq
 from typing import Callable, Sequence
 
 
-def system_cost(p) -> float:
-    """Relative cost of one system: the dense-equivalent dim^3 (the reference's ZHEEV scaling)."""
-    return float(p.dim) ** 3
+def system_cost(p, w: int | None = None) -> float:
+    """Relative cost of one system.  With the orbital count w: the matrix-free operator's Nk^2 w^2 nev
+    (its V x Z contraction dominates; the same model orders the work of wtb_batch_bsesolver).  Without it:
+    the dense-equivalent dim^3 (the reference's ZHEEV scaling)."""
+    if w is None:
+        return float(p.dim) ** 3
+    nk = float(p.ngrid[0] * p.ngrid[1] * p.ngrid[2])
+    return nk * nk * float(w) ** 2 * max(int(p.nev), 1) + nk * p.nc * p.nv * 1e3
 
 
 def lpt_partition(costs: Sequence[float], nranks: int) -> list[list[int]]:

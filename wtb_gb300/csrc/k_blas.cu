@@ -236,7 +236,8 @@ __global__ void __launch_bounds__(512) jacobi_small_kernel(zd* A, int lda, int n
   // is at the rounding floor, the sweep loop stops as well
   const double noise = (sizeof(S) == 4 ? 1e-6 : 1e-14) * scale;
   double prev_off = 1e300;
-  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+  int sweeps_done = 0;
+  for (int sweep = 0; sweep < max_sweeps; ++sweep, ++sweeps_done) {
     if (tid == 0) {
       notconv = 0;
       s_off = 0.0;
@@ -345,6 +346,10 @@ __global__ void __launch_bounds__(512) jacobi_small_kernel(zd* A, int lda, int n
     __syncthreads();
   }
   __syncthreads();
+  if (tid == 0) {
+    atomicAdd(&st->small_sweeps, sweeps_done);
+    atomicAdd(&st->small_calls, 1);
+  }
   if (tid < nin) ev[tid] = (double)M[tid * ldm + tid].re;
   __syncthreads();
   if (tid < nin) {
@@ -513,7 +518,7 @@ cudaError_t launch_update(const cplx<S>* Sx, int lds, int nin, const zd* C, int 
                           cplx<S>* Out, int ldo, double alpha, double beta, cudaStream_t s) {
   if (nout > 256 || nin * nout > 8192) return cudaErrorInvalidValue;
   const size_t smem = (size_t)nin * nout * sizeof(cplx<S>);
-  cudaError_t e = cudaFuncSetAttribute(update_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(update_kernel<S>), (size_t)smem);
   if (e != cudaSuccess) return e;
   const int rows_per_blk = 256 / nout;
   long nblk = (nrow + rows_per_blk - 1) / rows_per_blk;
@@ -564,7 +569,7 @@ static cudaError_t jacobi_launch(zd* A, int lda, int n, double* evals, zd* evecs
   if (np / 2 > 64) return cudaErrorInvalidValue;
   const size_t smem = (size_t)2 * np * (np + 1) * sizeof(cplx<S>) + 128 * sizeof(double) + 128 * sizeof(int) + 64;
   if (smem > 220 * 1024) return cudaErrorInvalidValue;
-  cudaError_t e = cudaFuncSetAttribute(jacobi_small_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(jacobi_small_kernel<S>), (size_t)smem);
   if (e != cudaSuccess) return e;
   jacobi_small_kernel<S><<<1, 512, smem, s>>>(A, lda, n, evals, evecs, ldv, sweeps, st); ++g_launch_count;
   return cudaGetLastError();

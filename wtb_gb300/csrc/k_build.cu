@@ -187,7 +187,7 @@ cudaError_t launch_bse_build(const zd* vec_win, const double* dE, const double* 
   };
   while (TK > 1 && smem_of(TK) > 200 * 1024) --TK;
   const size_t smem = smem_of(TK);
-  cudaError_t e = cudaFuncSetAttribute(bse_build_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(bse_build_kernel<S>), (size_t)smem);
   if (e != cudaSuccess) return e;
   const int nblk = (nk + TK - 1) / TK;
   dim3 grid(nblk, nblk);

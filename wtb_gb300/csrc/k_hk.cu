@@ -378,6 +378,7 @@ __device__ double integral_j0_pot(double rmax, double g) {
 
 struct CoulConst {
   int type;
+  int deriv_r0;
   double vbz, tol, cic;
   double eta, kappa, pb, pt, r0, w, lc, ez;  // V2DRK / V2DOH / V2DT2
   double ed;                                 // V3DL / V2DK
@@ -388,6 +389,7 @@ struct CoulConst {
 // The selected potential for the k-point difference (dx, dy, dz) = k1 - k2 (modvec, then the switch of
 // matrizelbse, src/module_bse.F90:49-72).
 __device__ double coulomb_of(const CoulConst& cc, double dx, double dy, double dz) {
+  if (cc.deriv_r0 && cc.type != CT_V2DRK) return 0.0;  // only V2DRK reads the R_0 key
   const double modk = sqrt(dx * dx + dy * dy + dz * dz);
   double v = 0.0;
   const double vc = cc.vbz * cc.cic;
@@ -399,6 +401,7 @@ __device__ double coulomb_of(const CoulConst& cc, double dx, double dy, double d
         const double aux3 = cc.r0 * modk * exp(-modk * cc.w);
         const double ew = (aux1 / aux2) + aux3;
         v = vc * exp(-modk * cc.w) * (1.0 / ew) * (1.0 / modk);
+        if (cc.deriv_r0) v = -v * (modk * exp(-modk * cc.w)) / ew;  // d/dr0: ew depends on r0 through aux3
       }
       break;
     case CT_V3DL:
@@ -512,7 +515,7 @@ cudaError_t launch_hk_eig(const zd* hr, const int* rvec, const int* ndegen, int 
   const int n = (w + 1) & ~1;
   const size_t smem = (size_t)2 * n * (n + 1) * sizeof(zd) + nR * sizeof(zd) + 32 * 2 * sizeof(double) + 32 * sizeof(zd) +
                       4 * sizeof(double) + 64 * sizeof(double) + 32 * 3 * sizeof(int) + 64 * sizeof(int) + 64;
-  cudaError_t e = cudaFuncSetAttribute(hk_eig_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(hk_eig_kernel), (size_t)smem);
   if (e != cudaSuccess) return e;
   hk_eig_kernel<<<nk, kHkThreads, smem, s>>>(hr, rvec, ndegen, nR, w, rlat_rm, efermi, scs, kpt, nk, nv, nc, eig_all,
                                              vec_all, eig_win, vec_win, nocp, st); ++g_launch_count;
@@ -524,7 +527,7 @@ cudaError_t launch_optics(const zd* hr, const int* rvec, const int* ndegen, int 
                           double cshift, zd* hout, cudaStream_t s) {
   const int nb = nv + nc;
   const size_t smem = (size_t)(w * w + nb * w + nv * w + nR) * sizeof(zd) + nR * sizeof(double) + 16;
-  cudaError_t e = cudaFuncSetAttribute(optics_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(optics_kernel), (size_t)smem);
   if (e != cudaSuccess) return e;
   optics_kernel<<<nk, kHkThreads, smem, s>>>(hr, rvec, ndegen, nR, w, rlat_rm, kpt, nk, nv, nc, eig_win, vec_win,
                                              (float)cshift, hout); ++g_launch_count;
@@ -569,6 +572,7 @@ static bool coul_const(const CoulParams& p, CoulConst* out) {
   const long ng = (long)p.ngrid[0] * p.ngrid[1] * p.ngrid[2];
   CoulConst cc{};
   cc.type = p.type;
+  cc.deriv_r0 = p.deriv_r0;
   cc.tol = p.ktol;
   cc.cic = -(double)(0.0904756f * 1000.0f);  // -(0.0904756)*10**(3) evaluated in single precision
   cc.r0 = p.r0;

@@ -232,6 +232,9 @@ __global__ void __launch_bounds__(128) mf_scatter_kernel(const T* __restrict__ T
 }
 
 // C[M][N] = A[M][K] * B[N][K]^T, real, CUDA cores.  64 x 64 CTA tile, 4 x 4 per thread, K step 16.
+// Products are accumulated over 256-wide K ranges and the range sums added into a second accumulator:
+// one running sum over all of K (K = Nk up to a few thousand) lets FP32 rounding errors add up
+// coherently for the smooth, one-signed operands of this contraction.
 template <class S>
 __global__ void __launch_bounds__(256) simt_gemm_tn_kernel(const S* __restrict__ A, int lda, const S* __restrict__ B,
                                                            int ldb, S* __restrict__ C, int ldc, int M, int N, int K) {
@@ -240,12 +243,21 @@ __global__ void __launch_bounds__(256) simt_gemm_tn_kernel(const S* __restrict__
   __shared__ S Bs[BK][BN + 4];
   const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-  S acc[4][4];
+  S acc[4][4], tot[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0;
+    for (int j = 0; j < 4; ++j) acc[i][j] = tot[i][j] = 0;
   for (int k0 = 0; k0 < K; k0 += BK) {
+    if (k0 % 256 == 0) {
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          tot[i][j] += acc[i][j];
+          acc[i][j] = 0;
+        }
+    }
     for (int e = tid; e < BM * BK; e += 256) {
       const int r = e / BK, kk = e % BK;
       const int gm = m0 + r, gn = n0 + r, gk = k0 + kk;
@@ -272,7 +284,7 @@ __global__ void __launch_bounds__(256) simt_gemm_tn_kernel(const S* __restrict__
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const int gm = m0 + ty * 4 + i, gn = n0 + tx * 4 + j;
-      if (gm < M && gn < N) C[(size_t)gm * ldc + gn] = acc[i][j];
+      if (gm < M && gn < N) C[(size_t)gm * ldc + gn] = tot[i][j] + acc[i][j];
     }
 }
 
@@ -306,8 +318,7 @@ cudaError_t launch_mf_gather(const cplx<S>* X, int ldx, int c0, int nb, const zd
     const size_t smem = (size_t)(2 * 32 * nc * w + 32 * nv * w + 32 * nc * nv) * sizeof(zf) +
                         (size_t)2 * w * w * 33 * sizeof(float);
     if (smem <= 200 * 1024 && ldk % 32 == 0) {
-      cudaError_t e = cudaFuncSetAttribute(mf_gather_bf16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)smem);
+      cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(mf_gather_bf16_kernel), (size_t)smem);
       if (e != cudaSuccess) return e;
       dim3 grid((nk + 31) / 32, nb);
       mf_gather_bf16_kernel<<<grid, 256, smem, s>>>(reinterpret_cast<const zf*>(X), ldx, c0, vec_win, nk, nv, nc, w,
@@ -320,7 +331,7 @@ cudaError_t launch_mf_gather(const cplx<S>* X, int ldx, int c0, int nb, const zd
   auto smem_of = [&](int kt) { return (size_t)(2 * kt * nc * w + kt * nv * w + kt * nc * nv) * sizeof(cplx<S>); };
   while (KT > 4 && smem_of(KT) > 160 * 1024) KT /= 2;
   const size_t smem = smem_of(KT);
-  cudaError_t e = cudaFuncSetAttribute(mf_gather_kernel<S, Z>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(mf_gather_kernel<S, Z>), (size_t)smem);
   if (e != cudaSuccess) return e;
   dim3 grid((nk + KT - 1) / KT, nb);
   mf_gather_kernel<S, Z><<<grid, 256, smem, s>>>(X, ldx, c0, vec_win, nk, nv, nc, w, KT, zt, ldk, nslices,
@@ -337,7 +348,7 @@ cudaError_t launch_mf_scatter(const T* Tm, int ldt, const cplx<S>* X, int ldx, c
   };
   while (nbg > 1 && smem_of(nbg) > 96 * 1024) nbg = (nbg + 1) / 2;
   const size_t smem = smem_of(nbg);
-  cudaError_t e = cudaFuncSetAttribute(mf_scatter_kernel<S, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(mf_scatter_kernel<S, T>), (size_t)smem);
   if (e != cudaSuccess) return e;
   dim3 grid(nk, (nb + nbg - 1) / nbg);
   mf_scatter_kernel<S, T><<<grid, 128, smem, s>>>(Tm, ldt, X, ldx, vec_win, dE, nk, nv, nc, w, nb, nbg, Y, ldy, c0); ++g_launch_count;

@@ -8,11 +8,13 @@
 //
 // CTA tile 128 x 256, K step 64 (one 128-byte swizzle atom of bf16), 4-stage TMA pipeline:
 //   warp 0 lane 0   TMA producer (cp.async.bulk.tensor.3d, mbarrier complete_tx)
-//   warp 1 lane 0   MMA issuer (tcgen05.mma.cta_group::1.kind::f16, accumulator in TMEM, 256 columns)
+//   warp 1 lane 0   MMA issuer (tcgen05.mma.cta_group::1.kind::f16, two 256-column accumulators in TMEM)
 //   warp 2          TMEM allocator
 //   warps 4..7      epilogue (tcgen05.ld 32x32b, lane = row) -> fp32 rows in global memory
 // Every mbarrier wait is bounded (2 s of %globaltimer); a wait that gives up sets the device status
 // word and an abort flag, the other roles stop at their next wait, and TMEM is freed before exit.
+#include <algorithm>
+
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -26,7 +28,9 @@ constexpr int BM = 128, BN = 256, BK = 64, STAGES = 4;
 constexpr int A_BYTES = BM * BK * 2;
 constexpr int B_BYTES = BN * BK * 2;
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int TMEM_COLS = 256;
+// room for two FP32 accumulators of BN columns: in split runs even K blocks go to the first, odd ones to
+// the second, and the epilogue adds them (halves the number of MMA accumulation steps each one takes)
+constexpr int TMEM_COLS = 2 * BN;
 constexpr unsigned long long kTimeoutNs = 2000000000ull;
 constexpr uint32_t kIdesc = (1u << 4)                       // D format: f32
                             | (1u << 7)                     // A format: bf16
@@ -37,6 +41,9 @@ constexpr size_t kSmemBytes = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
 
 struct TcArgs {
   int K, kblocks, m_valid, n_valid, ldc, npairs;
+  int kb0, kbn;    // this launch covers K blocks [kb0, kb0 + kbn)
+  int accumulate;  // 1: C += result (a later K range of a split run), 0: C = result
+  int dual;        // 1: even/odd K blocks in two accumulators (split runs), 0: one accumulator
   int pa[8], pb[8];
   float* C;
   DevStatus* st;
@@ -160,7 +167,7 @@ __global__ void __launch_bounds__(256, 1) tc_gemm_kernel(const __grid_constant__
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
-  const int total = args.npairs * args.kblocks;
+  const int total = args.npairs * args.kbn;
 
   volatile int* issued = abort_flag + 1;    // TMA stages issued by the producer
   volatile int* consumed = abort_flag + 2;  // stages whose loads the MMA issuer has seen land
@@ -174,7 +181,7 @@ __global__ void __launch_bounds__(256, 1) tc_gemm_kernel(const __grid_constant__
           dev_fail(args.st, 401, it);
           break;
         }
-        const int pair = it / args.kblocks, kb = it % args.kblocks;
+        const int pair = it / args.kbn, kb = args.kb0 + it % args.kbn;
         uint8_t* sa = base + s * STAGE_BYTES;
         uint8_t* sb = sa + A_BYTES;
         mbar_expect_tx(&full[s], STAGE_BYTES);
@@ -198,10 +205,15 @@ __global__ void __launch_bounds__(256, 1) tc_gemm_kernel(const __grid_constant__
         const uint32_t sa = smem_u32(base + s * STAGE_BYTES);
         const uint32_t sb = sa + A_BYTES;
         const uint64_t da = sw128_desc(sa), db = sw128_desc(sb);
+        const int kl = it % args.kbn;  // K block within this launch's range
+        const int ai = args.dual ? (kl & 1) : 0;  // accumulator of this K block
+        const uint32_t acc_col = (uint32_t)(ai * BN);
+        const bool first = args.dual ? (it < 2 && kl == it) : (it == 0);  // its first block in pair 0
 #pragma unroll
         for (int kk = 0; kk < BK / 16; ++kk) {
           // advance 16 bf16 = 32 bytes along K inside the swizzle atom: +2 in the encoded address
-          umma_bf16(tmem, da + (uint64_t)(2 * kk), db + (uint64_t)(2 * kk), kIdesc, (it > 0 || kk > 0) ? 1u : 0u);
+          umma_bf16(tmem + acc_col, da + (uint64_t)(2 * kk), db + (uint64_t)(2 * kk), kIdesc,
+                    (!first || kk > 0) ? 1u : 0u);
         }
         umma_commit(&empty[s]);
       }
@@ -219,10 +231,17 @@ __global__ void __launch_bounds__(256, 1) tc_gemm_kernel(const __grid_constant__
       const int wq = warp & 3;
       const int row = m0 + wq * 32 + lane;
       const uint32_t lane_addr = tmem + ((uint32_t)(wq * 32) << 16);
+      const bool two = args.dual && args.kbn > 1;  // the second accumulator holds the odd K blocks
 #pragma unroll 1
       for (int j = 0; j < BN / 32; ++j) {
         uint32_t r[32];
         tmem_ld32(lane_addr + (uint32_t)(j * 32), r);
+        if (two) {
+          uint32_t r2[32];
+          tmem_ld32(lane_addr + (uint32_t)(BN + j * 32), r2);
+#pragma unroll
+          for (int q = 0; q < 32; ++q) r[q] = __float_as_uint(__uint_as_float(r[q]) + __uint_as_float(r2[q]));
+        }
         const int col0 = n0 + j * 32;
         if (row < args.m_valid) {
           float* dst = args.C + (size_t)row * args.ldc + col0;
@@ -231,11 +250,18 @@ __global__ void __launch_bounds__(256, 1) tc_gemm_kernel(const __grid_constant__
             for (int q = 0; q < 8; ++q) {
               float4 v = make_float4(__uint_as_float(r[4 * q]), __uint_as_float(r[4 * q + 1]),
                                      __uint_as_float(r[4 * q + 2]), __uint_as_float(r[4 * q + 3]));
+              if (args.accumulate) {
+                const float4 o = reinterpret_cast<const float4*>(dst)[q];
+                v.x += o.x;
+                v.y += o.y;
+                v.z += o.z;
+                v.w += o.w;
+              }
               reinterpret_cast<float4*>(dst)[q] = v;
             }
           } else {
             for (int q = 0; q < 32; ++q)
-              if (col0 + q < args.n_valid) dst[q] = __uint_as_float(r[q]);
+              if (col0 + q < args.n_valid) dst[q] = __uint_as_float(r[q]) + (args.accumulate ? dst[q] : 0.f);
           }
         }
       }
@@ -253,14 +279,15 @@ __global__ void __launch_bounds__(256, 1) tc_gemm_kernel(const __grid_constant__
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
+  // a function-local static is initialised once, thread-safely
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
     cudaDriverEntryPointQueryResult q;
     void* p = nullptr;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  }
+      return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    return nullptr;
+  }();
   return fn;
 }
 
@@ -320,6 +347,10 @@ int tc_gemm_plan_create(TcGemmPlan** plan, const uint16_t* A, int M, int K, long
   }
   p->args.K = K;
   p->args.kblocks = K / BK;
+  p->args.kb0 = 0;
+  p->args.kbn = K / BK;
+  p->args.accumulate = 0;
+  p->args.dual = 0;
   p->args.ldc = ldc;
   p->args.npairs = npairs;
   for (int i = 0; i < npairs; ++i) {
@@ -330,15 +361,12 @@ int tc_gemm_plan_create(TcGemmPlan** plan, const uint16_t* A, int M, int K, long
   p->args.m_valid = M;
   p->args.n_valid = N;
   p->grid = dim3(N / BN, M / BM);
-  static bool attr = false;
-  if (!attr) {
-    if (cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemBytes) !=
-        cudaSuccess) {
-      *msg = "tc_gemm: shared memory attribute rejected";
-      delete p;
-      return WTB_ECUDA;
-    }
-    attr = true;
+  // per device and thread-safe in the runtime; plans are cached, so this runs once per operator shape
+  if (raise_smem_limit(reinterpret_cast<const void*>(tc_gemm_kernel), (size_t)kSmemBytes) !=
+      cudaSuccess) {
+    *msg = "tc_gemm: shared memory attribute rejected";
+    delete p;
+    return WTB_ECUDA;
   }
   *plan = p;
   return WTB_OK;
@@ -351,8 +379,35 @@ void tc_gemm_set_valid(TcGemmPlan* p, int m_valid, int n_valid) {
 
 cudaError_t tc_gemm_run(TcGemmPlan* plan, DevStatus* st, cudaStream_t s) {
   plan->args.st = st;
+  plan->args.kb0 = 0;
+  plan->args.kbn = plan->args.kblocks;
+  plan->args.accumulate = 0;
+  plan->args.dual = 0;
   tc_gemm_kernel<<<plan->grid, 256, kSmemBytes, s>>>(plan->mapA, plan->mapB, plan->args); ++g_launch_count;
   return cudaGetLastError();
+}
+
+// The tensor cores add each MMA's products into the FP32 accumulator with a rounding that does not average
+// out over a long K: with a smooth right-hand side and a one-signed V the error of a full-K accumulation
+// grows with K and shifts Rayleigh quotients coherently.  This run splits K into ranges of kb_chunk blocks
+// (one launch each), accumulates each range afresh in TMEM with its even and odd K blocks in two
+// accumulators, and adds the results to C in FP32 round-to-nearest in the epilogue, which cuts that error
+// by twice the number of ranges.  Launches are ordered on the stream, so the read-modify-write of C is
+// race-free.
+cudaError_t tc_gemm_run_split(TcGemmPlan* plan, DevStatus* st, cudaStream_t s, int kb_chunk) {
+  if (kb_chunk < 1 || kb_chunk > plan->args.kblocks) kb_chunk = plan->args.kblocks;
+  plan->args.st = st;
+  for (int kb0 = 0; kb0 < plan->args.kblocks; kb0 += kb_chunk) {
+    TcArgs a = plan->args;
+    a.kb0 = kb0;
+    a.kbn = std::min(kb_chunk, plan->args.kblocks - kb0);
+    a.accumulate = kb0 > 0 ? 1 : 0;
+    a.dual = 1;
+    tc_gemm_kernel<<<plan->grid, 256, kSmemBytes, s>>>(plan->mapA, plan->mapB, a); ++g_launch_count;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 void tc_gemm_plan_destroy(TcGemmPlan* plan) { delete plan; }

@@ -56,14 +56,17 @@ cudaError_t MatFreeOperator<S>::apply(const cplx<S>* X, int ldx, int c0, int nco
           plan = it->second;
         }
         cudaEvent_t ea = nullptr, eb = nullptr;
-        if (prof && prof->on) {
+        // the live profile covers the iteration's contraction launches (the final split run is a
+        // different launch configuration and is left out of it)
+        const bool profiled = prof && prof->on && !final_apply;
+        if (profiled) {
           cudaEventCreate(&ea);
           cudaEventCreate(&eb);
           cudaEventRecord(ea, s);
         }
-        e = tc_gemm_run(plan, st, s);
+        e = final_apply ? tc_gemm_run_split(plan, st, s, kchunk_final) : tc_gemm_run(plan, st, s);
         if (e != cudaSuccess) return e;
-        if (prof && prof->on) {
+        if (profiled) {
           cudaEventRecord(eb, s);
           prof->pending.emplace_back(ea, eb);
           prof->launches += 1;
@@ -100,6 +103,40 @@ cudaError_t MatFreeOperator<S>::apply(const cplx<S>* X, int ldx, int c0, int nco
     }
   }
   return cudaSuccess;
+}
+
+template <class S>
+cudaError_t MatFreeOperator<S>::contract(const cplx<S>* X, int ldx, int ncol, cudaStream_t s) {
+  if (ncol > nbmax) return cudaErrorInvalidValue;
+  const int N = 2 * w * w * ncol;
+  if (kind == GEMM_TC_BF16) {
+    if constexpr (sizeof(S) == 4) {
+      cudaError_t e = launch_mf_gather<float, uint16_t>(X, ldx, 0, ncol, vec_win, nk, nv, nc, w, Zs, Kpad, nslices,
+                                                        (long)Npad * Kpad, s);
+      if (e != cudaSuccess) return e;
+      const long key = (long)N * 16 + npairs;
+      TcGemmPlan* plan = nullptr;
+      auto it = plans.find(key);
+      if (it == plans.end()) {
+        std::string m2;
+        if (tc_gemm_plan_create(&plan, Vs, Mpad, Kpad, (long)Mpad * Kpad, nslices, Zs, Npad, (long)Npad * Kpad,
+                                nslices, reinterpret_cast<float*>(Tm), Npad, npairs, pa, pb, &m2) != WTB_OK) {
+          if (msg) *msg = m2;
+          return cudaErrorInvalidValue;
+        }
+        tc_gemm_set_valid(plan, nk, N);
+        plans[key] = plan;
+      } else {
+        plan = it->second;
+      }
+      return tc_gemm_run(plan, st, s);
+    } else {
+      return cudaErrorInvalidValue;
+    }
+  }
+  cudaError_t e = launch_mf_gather<S, S>(X, ldx, 0, ncol, vec_win, nk, nv, nc, w, Zr, Kpad, 1, 0, s);
+  if (e != cudaSuccess) return e;
+  return launch_simt_gemm_tn<S>(Vr, Kpad, Zr, Kpad, reinterpret_cast<S*>(Tm), Npad, nk, N, Kpad, s);
 }
 
 template struct MatFreeOperator<float>;
@@ -227,6 +264,13 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
     // reached and the FP64 Rayleigh-Ritz below takes over
     double best_maxrel = 1e300;
     int best_it = 0;
+    // breakdown guard: near the operator's rounding floor the running AX drifts from H X and LOBPCG can
+    // lose consistency (Ritz values falling far below the spectrum).  The block with the lowest residual of
+    // the current phase is kept; a residual that grows 10x past it after reaching 100 x tol restores it.
+    cplx<S>* Xbest = ws.get<cplx<S>>("lob_Xbest", (size_t)dim * m, &err);
+    if (!chk()) goto oom;
+    double saved_rel = 1e300;
+    int restarts = 0;
     for (; it < maxit; ++it) {
       cplx<S>* X = Sb[cur];
       cplx<S>* AX = ASb[cur];
@@ -262,9 +306,40 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
       if (monitor) {
         int first = 0;
         while (first < nev - 1 && h_active[first] == 0) ++first;
-        std::fprintf(stderr, "WTB-EPS %5d EPS pair=%4d value (error) %15.8E (%10.3E) max %10.3E\n", it, nconv + 1,
-                     h_theta[first], std::sqrt(std::max(h_norm[first], 0.0)) / std::max(std::fabs(h_theta[first]), 1e-12),
-                     maxrel);
+        std::fprintf(stderr, "WTB-EPS %5d EPS pair=%4d value (error) %15.8E (%10.3E) max %10.3E  small %d/%d\n", it,
+                     nconv + 1, h_theta[first],
+                     std::sqrt(std::max(h_norm[first], 0.0)) / std::max(std::fabs(h_theta[first]), 1e-12), maxrel,
+                     hst.small_sweeps, hst.small_calls);
+      }
+      // restart from X alone: fresh AX, no search directions, Rayleigh-Ritz on X
+      auto restart_from_x = [&]() -> int {
+        CK(op.apply(X, ld, 0, m, AX, ld, s));
+        have_p = false;
+        best_maxrel = 1e300;
+        best_it = it;
+        int rr = rayleigh_ritz<S>(X, AX, ld, m, m, dim, tau, sm, partial, npart, st, s, msg, false);
+        if (rr) return rr;
+        const int nxt = cur ^ 1;
+        CK(launch_update<S>(X, ld, m, sm.C, m, m, dim, Sb[nxt], ld, 1.0, 0.0, s));
+        CK(launch_update<S>(AX, ld, m, sm.C, m, m, dim, ASb[nxt], ld, 1.0, 0.0, s));
+        CK(cudaMemcpyAsync(th_dev, sm.theta, sizeof(double) * m, cudaMemcpyDeviceToDevice, s));
+        cur = nxt;
+        return WTB_OK;
+      };
+      if (maxrel < saved_rel) {
+        saved_rel = maxrel;
+        CK(launch_copy_cols<S>(X, ld, Xbest, m, m, dim, s));
+      } else if (saved_rel <= 100.0 * tol && maxrel > 10.0 * saved_rel) {
+        CK(launch_copy_cols<S>(Xbest, m, X, ld, m, dim, s));
+        if (saved_rel <= tol || ++restarts > 2) {
+          // the best block goes to the final Rayleigh-Ritz (which re-applies the operator)
+          converged = saved_rel <= 100.0 * tol;
+          break;
+        }
+        r = restart_from_x();
+        if (r) return r;
+        saved_rel = 1e300;
+        continue;
       }
       if (nconv == nev) {
         if (tol_refine > 0.0 && tol_refine < tol && op.begin_refine()) {
@@ -272,17 +347,9 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
           // with the cheaper operator) are dropped
           tol = tol_refine;
           tol_refine = 0.0;
-          CK(op.apply(X, ld, 0, m, AX, ld, s));
-          have_p = false;
-          best_maxrel = 1e300;
-          best_it = it;
-          r = rayleigh_ritz<S>(X, AX, ld, m, m, dim, tau, sm, partial, npart, st, s, msg, false);
+          r = restart_from_x();
           if (r) return r;
-          const int nxt = cur ^ 1;
-          CK(launch_update<S>(X, ld, m, sm.C, m, m, dim, Sb[nxt], ld, 1.0, 0.0, s));
-          CK(launch_update<S>(AX, ld, m, sm.C, m, m, dim, ASb[nxt], ld, 1.0, 0.0, s));
-          CK(cudaMemcpyAsync(th_dev, sm.theta, sizeof(double) * m, cudaMemcpyDeviceToDevice, s));
-          cur = nxt;
+          saved_rel = 1e300;
           continue;
         }
         converged = true;
@@ -335,7 +402,10 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
       // fresh H X in the operator's most accurate arithmetic (the iteration's AX is a running linear
       // combination of cheaper applications)
       op.begin_refine();
-      CK(op.apply(X, ld, 0, mm, AXs, ld, s));
+      op.set_final(true);
+      const cudaError_t fe = op.apply(X, ld, 0, mm, AXs, ld, s);
+      op.set_final(false);
+      CK(fe);
       CK((launch_convert_cols<S, double>(X, ld, X64, 2 * mm, mm, dim, s)));
       CK((launch_convert_cols<S, double>(AXs, ld, X64 + mm, 2 * mm, mm, dim, s)));
       r = rayleigh_ritz<double>(X64, X64 + mm, 2 * mm, mm, mm, dim, 1e-13, sm, partial, npart, st, s, msg, true);

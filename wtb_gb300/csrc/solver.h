@@ -37,14 +37,24 @@ struct DevBuf {
   }
 };
 
+// Named device buffers.  get() sets *err only when an allocation fails, so one check after a run of
+// get() calls sees any failure in the run (callers start with err = cudaSuccess).
 struct Workspace {
   std::map<std::string, std::unique_ptr<DevBuf>> bufs;
   template <class T>
   T* get(const std::string& name, size_t count, cudaError_t* err, bool zero = false) {
     auto& b = bufs[name];
     if (!b) b.reset(new DevBuf());
-    *err = b->ensure(count * sizeof(T), zero);
+    const cudaError_t e = b->ensure(count * sizeof(T), zero);
+    if (e != cudaSuccess) *err = e;
     return b->as<T>();
+  }
+  // an existing buffer of at least count elements, or nullptr
+  template <class T>
+  T* find(const std::string& name, size_t count) const {
+    auto it = bufs.find(name);
+    if (it == bufs.end() || !it->second || !it->second->p || it->second->bytes < count * sizeof(T)) return nullptr;
+    return it->second->as<T>();
   }
 };
 
@@ -55,6 +65,9 @@ struct Operator {
   virtual cudaError_t apply(const cplx<S>* X, int ldx, int c0, int ncol, cplx<S>* Y, int ldy, cudaStream_t s) = 0;
   // switches the operator to its most accurate arithmetic; returns false if it has only one
   virtual bool begin_refine() { return false; }
+  // on: the next applications define the reported eigenvalues (final Rayleigh-Ritz); an operator may use
+  // a slower, more accurate accumulation for them
+  virtual void set_final(bool on) { (void)on; }
   long matvec_columns = 0;
 };
 
@@ -118,11 +131,18 @@ struct MatFreeOperator : Operator<S> {
     for (auto& kv : plans) tc_gemm_plan_destroy(kv.second);
   }
   cudaError_t apply(const cplx<S>* X, int ldx, int c0, int ncol, cplx<S>* Y, int ldy, cudaStream_t s) override;
+  // gather + contraction only: leaves T = V Z(X[:, 0:ncol]) in Tm (row k, column ((b w + o) w + p) 2 + ri,
+  // leading dimension Npad; float for the tensor-core kind, S otherwise); ncol <= nbmax
+  cudaError_t contract(const cplx<S>* X, int ldx, int ncol, cudaStream_t s);
   bool begin_refine() override {
     if (npairs_refine <= npairs) return false;
     npairs = npairs_refine;
     return true;
   }
+  // tensor-core kind: K blocks per accumulation range in the final applications (0: one range)
+  int kchunk_final = 4;
+  bool final_apply = false;
+  void set_final(bool on) override { final_apply = on; }
 };
 
 struct SolveStats {

@@ -4,40 +4,33 @@
 // bseoptprop.  Everything numeric runs in the CUDA kernels of this library; host code only moves
 // arguments, checks them, and orchestrates launches on the context's stream.
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 
-#include "solver.h"
+#include "ctx.h"
 
 namespace wtb {
-long long g_launch_count = 0;
+std::atomic<long long> g_launch_count{0};
+
+cudaError_t raise_smem_limit(const void* func, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> limit;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = limit[{func, dev}];
+  if (bytes <= cur) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
+}
 }
 
 using namespace wtb;
 
-struct wtb_ctx {
-  int device = 0;
-  cudaStream_t s = nullptr;
-  std::string msg;
-  DevStatus* st = nullptr;
-  Workspace ws;
-  // H(R)
-  bool have_hr = false;
-  int w = 0, nR = 0, systype_np = 0;
-  double efermi = 0.0, scs = 0.0;
-  double rlat_rm[9] = {0};
-  // bands of the last mesh
-  bool have_bands = false;
-  int nk = 0, nv = 0, nc = 0;
-  int ngrid[3] = {0, 0, 0};
-  std::vector<double> kpt;  // nk x 3 row-major
-  // the k-points are the Monkhorst-Pack mesh of ngrid (set by the solver entry points); a caller-supplied
-  // k-point list (wtb_eigsys_mesh) clears it and the V(k,k') table is then evaluated pair by pair
-  bool mesh_mp = false;
-  // last BSE operator data (for wtb_optsp)
-  bool have_hr_optics = false;
-  KernelProfile prof;
-};
 
 namespace {
 
@@ -197,7 +190,7 @@ __global__ void expand_acts_kernel(const double* __restrict__ osc, int nev, int 
 }
 
 int upload_bands(wtb_ctx* c, int nk, const double* kpt_rm, int nv, int nc) {
-  cudaError_t err;
+  cudaError_t err = cudaSuccess;
   double* dk = c->ws.get<double>("kpt", (size_t)nk * 3, &err);
   CKC(err);
   CKC(cudaMemcpyAsync(dk, kpt_rm, sizeof(double) * nk * 3, cudaMemcpyHostToDevice, c->s));
@@ -221,6 +214,7 @@ int upload_bands(wtb_ctx* c, int nk, const double* kpt_rm, int nv, int nc) {
   c->nc = nc;
   c->kpt.assign(kpt_rm, kpt_rm + (size_t)nk * 3);
   c->have_bands = nb > 0;
+  c->have_solve = false;  // the stored excitons belong to the previous bands
   return WTB_OK;
 }
 
@@ -254,9 +248,11 @@ CoulParams coul_of(wtb_ctx* c, const wtb_bse_params* p) {
   return cp;
 }
 
-// V(k,k') for the bands of the context into V (leading dimension ldv)
-int coulomb_table_into(wtb_ctx* c, const wtb_bse_params* p, double* V, int ldv) {
-  cudaError_t err;
+// V(k,k') (or dV/dr0) for the bands of the context into V (leading dimension ldv)
+int coulomb_table_into(wtb_ctx* c, const wtb_bse_params* p, double* V, int ldv, bool deriv_r0 = false) {
+  cudaError_t err = cudaSuccess;
+  CoulParams cpar = coul_of(c, p);
+  cpar.deriv_r0 = deriv_r0 ? 1 : 0;
   const int nk = c->nk;
   const bool mp = c->mesh_mp && p->ngrid[0] == c->ngrid[0] && p->ngrid[1] == c->ngrid[1] &&
                   p->ngrid[2] == c->ngrid[2] && (long)p->ngrid[0] * p->ngrid[1] * p->ngrid[2] == nk;
@@ -284,10 +280,10 @@ int coulomb_table_into(wtb_ctx* c, const wtb_bse_params* p, double* V, int ldv) 
     double* stn = c->ws.get<double>("vstencil", ns, &err);
     CKC(err);
     CKC(cudaMemcpyAsync(dbl, bl, sizeof(bl), cudaMemcpyHostToDevice, c->s));
-    CKC(launch_coulomb_mesh(coul_of(c, p), dbl, stn, V, ldv, c->s));
+    CKC(launch_coulomb_mesh(cpar, dbl, stn, V, ldv, c->s));
   } else {
     const double* kd = c->ws.get<double>("kpt", 0, &err);
-    CKC(launch_coulomb(coul_of(c, p), kd, nk, kd, nk, V, ldv, c->s));
+    CKC(launch_coulomb(cpar, kd, nk, kd, nk, V, ldv, c->s));
   }
   return WTB_OK;
 }
@@ -302,28 +298,21 @@ int auto_block(const wtb_bse_params* p, int dim, bool fp64) {
   return m;
 }
 
-// The BSE operator selected by p (dense FP64/FP32, or matrix-free FP64/FP32/split-BF16) over the bands of
-// the context; exactly one of o64 / o32 is set.
-struct OpBundle {
-  std::unique_ptr<Operator<double>> o64;
-  std::unique_ptr<Operator<float>> o32;
-  std::string msg;
-  const double* dE = nullptr;
-  int dim = 0;
-};
-
-int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob) {
+// tag: suffix of the buffers holding the V table and its forms (a second operator, e.g. the dV/dr0 one,
+// must not overwrite the first); deriv_r0: build the operator of dV/dr0 with no diagonal term.
+int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob, const std::string& tag = "",
+                  bool deriv_r0 = false) {
   const int nk = c->nk, nv = c->nv, nc = c->nc, w = c->w;
   const int dim = nk * nc * nv;
-  cudaError_t err;
+  cudaError_t err = cudaSuccess;
   const zd* vec_win = c->ws.get<zd>("vec_win", 0, &err);
-  double* dE = c->ws.get<double>("dE", dim, &err);
+  double* dE = c->ws.get<double>(deriv_r0 ? "dE0" : "dE", dim, &err, deriv_r0);
   CKC(err);
-  CKC(launch_transition_energies(c->ws.get<double>("eig_win", 0, &err), nk, nv, nc, dE, c->s));
+  if (!deriv_r0) CKC(launch_transition_energies(c->ws.get<double>("eig_win", 0, &err), nk, nv, nc, dE, c->s));
   const int Kpad = (nk + 63) / 64 * 64, Mpad = (nk + 127) / 128 * 128;
-  double* V = c->ws.get<double>("V", (size_t)Mpad * Kpad, &err, true);
+  double* V = c->ws.get<double>("V" + tag, (size_t)Mpad * Kpad, &err, true);
   CKC(err);
-  CKR(coulomb_table_into(c, p, V, Kpad));
+  CKR(coulomb_table_into(c, p, V, Kpad, deriv_r0));
   ob->dE = dE;
   ob->dim = dim;
   const bool fp64 = p->precision == WTB_PREC_FP64;
@@ -369,7 +358,7 @@ int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob) 
   op->Kpad = Kpad; op->Mpad = Mpad; op->Npad = Npad;
   if (p->precision == WTB_PREC_FP32) {
     op->kind = GEMM_SIMT_F32;
-    float* Vf = c->ws.get<float>("V32", (size_t)Mpad * Kpad, &err, true);
+    float* Vf = c->ws.get<float>("V32" + tag, (size_t)Mpad * Kpad, &err, true);
     CKC(err);
     CKC(launch_round_f32(V, Kpad, nk, nk, Vf, Kpad, c->s));
     op->Vr = Vf;
@@ -391,20 +380,21 @@ int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob) 
     op->pa[i] = pa6[i];
     op->pb[i] = pb6[i];
   }
-  uint16_t* Vs = c->ws.get<uint16_t>("Vbf", (size_t)op->nslices * Mpad * Kpad, &err, true);
+  uint16_t* Vs = c->ws.get<uint16_t>("Vbf" + tag, (size_t)op->nslices * Mpad * Kpad, &err, true);
   CKC(err);
   CKC(launch_split_bf16(V, Kpad, nk, nk, Vs, Kpad, (long)Mpad * Kpad, op->nslices, c->s));
   op->Vs = Vs;
   op->Zs = c->ws.get<uint16_t>("Zbf", (size_t)op->nslices * Npad * Kpad, &err, true);
   op->Tm = c->ws.get<float>("Tbf", (size_t)Mpad * Npad, &err);
   CKC(err);
+  if (const char* kc = std::getenv("WTB_FINAL_KCHUNK")) op->kchunk_final = std::atoi(kc);
   return WTB_OK;
 }
 
 // Solve with the operator selected by p; leaves E and the FP64 eigenvectors (dim x nev row-major, "Xout").
 int run_solve(wtb_ctx* c, const wtb_bse_params* p, std::vector<double>* E, wtb_timings* t, SolveStats* stats) {
   const int dim = c->nk * c->nc * c->nv;
-  cudaError_t err;
+  cudaError_t err = cudaSuccess;
   cudaEvent_t ev[3];
   for (auto& e : ev) CKC(cudaEventCreate(&e));
   CKC(cudaEventRecord(ev[0], c->s));
@@ -452,6 +442,20 @@ std::mutex g_default_mu;
 wtb_ctx* g_default = nullptr;
 
 }  // namespace
+
+namespace wtb {
+int ctx_set_err(wtb_ctx* c, int code, const std::string& m) { return set_err(c, code, m); }
+double ctx_vcell3d(const wtb_ctx* c) { return vcell3D(c->rlat_rm); }
+int ctx_check_status(wtb_ctx* c) { return check_status(c); }
+CoulParams ctx_coul_params(wtb_ctx* c, const wtb_bse_params* p) { return coul_of(c, p); }
+int ctx_coulomb_table(wtb_ctx* c, const wtb_bse_params* p, double* V, int ldv, bool deriv_r0) {
+  return coulomb_table_into(c, p, V, ldv, deriv_r0);
+}
+int ctx_make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob, const std::string& tag,
+                      bool deriv_r0) {
+  return make_operator(c, p, nbmax, ob, tag, deriv_r0);
+}
+}  // namespace wtb
 
 // ================================================================================================ C ABI
 extern "C" {
@@ -509,7 +513,7 @@ int wtb_set_hr(wtb_ctx* c, int w90basis, int nvec, const int* rvec, const int* f
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) rl[3 * i + j] = rlat[i + 3 * j];
   if (!std::isfinite(efermi) || !std::isfinite(scs)) return set_err(c, WTB_ENAN, "non-finite efermi or scs");
-  cudaError_t err;
+  cudaError_t err = cudaSuccess;
   zd* dh = c->ws.get<zd>("hr", hr.size(), &err);
   CKC(err);
   int* dr = c->ws.get<int>("rvec", (size_t)nvec * 3, &err);
@@ -531,6 +535,7 @@ int wtb_set_hr(wtb_ctx* c, int w90basis, int nvec, const int* rvec, const int* f
   std::memcpy(c->rlat_rm, rl, sizeof(rl));
   c->have_hr = true;
   c->have_bands = false;
+  c->have_solve = false;
   return WTB_OK;
 }
 
@@ -560,7 +565,7 @@ int wtb_eigsys(int nthreads, double scs, double exc, int* nocp, const int* ffact
   const double k[3] = {kx, ky, kz};
   CKR(upload_bands(c, 1, k, 0, 0));
   const int w = w90basis;
-  cudaError_t err;
+  cudaError_t err = cudaSuccess;
   std::vector<double> e(w);
   std::vector<zd> v((size_t)w * w);
   int cnt = 0;
@@ -597,7 +602,7 @@ int wtb_eigsys_mesh(wtb_ctx* c, int nk, const double* kpt, int nv, int nc, doubl
   CKR(upload_bands(c, nk, k.data(), nv, nc));
   c->mesh_mp = false;
   const int nb = nv + nc, w = c->w;
-  cudaError_t err;
+  cudaError_t err = cudaSuccess;
   if (eigv) {
     std::vector<double> e((size_t)nk * nb);
     CKC(cudaMemcpy(e.data(), c->ws.get<double>("eig_win", 0, &err), e.size() * sizeof(double), cudaMemcpyDeviceToHost));
@@ -632,7 +637,7 @@ int wtb_coulomb_table(wtb_ctx* c, const wtb_bse_params* p, int n1, const double*
     for (int d = 0; d < 3; ++d) a[3 * i + d] = kpt1[i + (size_t)n1 * d];
   for (int i = 0; i < n2; ++i)
     for (int d = 0; d < 3; ++d) b[3 * i + d] = kpt2[i + (size_t)n2 * d];
-  cudaError_t err;
+  cudaError_t err = cudaSuccess;
   double* da = c->ws.get<double>("ct_a", a.size(), &err);
   double* db = c->ws.get<double>("ct_b", b.size(), &err);
   double* dv = c->ws.get<double>("ct_v", (size_t)n1 * n2, &err);
@@ -657,7 +662,7 @@ static int ensure_bands_for(wtb_ctx* c, const wtb_bse_params* p) {
 }
 
 static int compute_optics(wtb_ctx* c, const wtb_bse_params* p) {
-  cudaError_t err;
+  cudaError_t err = cudaSuccess;
   const int dim = c->nk * c->nc * c->nv;
   zd* hout = c->ws.get<zd>("hrvel", (size_t)5 * dim, &err);
   CKC(err);
@@ -666,6 +671,7 @@ static int compute_optics(wtb_ctx* c, const wtb_bse_params* p) {
                     c->nc, c->ws.get<double>("eig_win", 0, &err), c->ws.get<zd>("vec_win", 0, &err), p->cshift, hout,
                     c->s));
   c->have_hr_optics = true;
+  c->have_solve = false;  // hrvel now follows p->cshift; wtb_bsesolver sets it again after its solve
   return WTB_OK;
 }
 
@@ -676,7 +682,7 @@ int wtb_optsp(wtb_ctx* c, const wtb_bse_params* p, double* hr) {
   if (!p) return set_err(c, WTB_EBADARG, "params is NULL");
   CKR(compute_optics(c, p));
   const int dim = c->nk * c->nc * c->nv;
-  cudaError_t err;
+  cudaError_t err = cudaSuccess;
   if (hr)
     CKC(cudaMemcpyAsync(hr, c->ws.get<zd>("hrvel", 0, &err), sizeof(zd) * 5 * dim, cudaMemcpyDeviceToHost, c->s));
   return check_status(c);
@@ -694,7 +700,7 @@ int wtb_bse_build(wtb_ctx* c, const wtb_bse_params* p, double* hbse) {
     return set_err(c, WTB_EBADARG, "the dense build stores FP64 or FP32");
   const int nk = c->nk, nv = c->nv, nc = c->nc, w = c->w;
   const long dim = (long)nk * nc * nv;
-  cudaError_t err;
+  cudaError_t err = cudaSuccess;
   double* dE = c->ws.get<double>("dE", dim, &err);
   CKC(err);
   CKC(launch_transition_energies(c->ws.get<double>("eig_win", 0, &err), nk, nv, nc, dE, c->s));
@@ -732,7 +738,7 @@ int wtb_slepc_solver(wtb_ctx* c, const double* HX, double* EX, double* HE, int N
   if (!c) return WTB_EBADARG;
   CKR(prep_device(c));
   if (!HX || NX < 1 || NE < 1 || NE > NX) return set_err(c, WTB_EBADARG, "bad matrix size or NE");
-  cudaError_t err;
+  cudaError_t err = cudaSuccess;
   const long n2 = (long)NX * NX;
   zd* H = c->ws.get<zd>("slepc_H", n2, &err);
   double* d = c->ws.get<double>("slepc_d", NX, &err);
@@ -771,7 +777,7 @@ int wtb_dielbse(wtb_ctx* c, int dimse, int dimse1, const double* excitonvec, con
   CKR(prep_device(c));
   if (dimse < 1 || dimse1 < 0 || dimse1 > dimse || !excitonvec || !hopt1 || (pair && !hopt2) || !activity)
     return set_err(c, WTB_EBADARG, "bad arguments");
-  cudaError_t err;
+  cudaError_t err = cudaSuccess;
   zd* A = c->ws.get<zd>("db_A", (size_t)dimse * std::max(dimse1, 1), &err);
   zd* h1 = c->ws.get<zd>("db_h1", dimse, &err);
   zd* h2 = c->ws.get<zd>("db_h2", dimse, &err);
@@ -808,7 +814,7 @@ int wtb_bsesolver(wtb_ctx* c, const wtb_bse_params* p, double* Ws, double* acts,
   SolveStats stats;
   wtb_timings tt{};
   CKR(run_solve(c, p, &E, &tt, &stats));
-  cudaError_t err;
+  cudaError_t err = cudaSuccess;
   const int nev = p->nev;
   double* osc = c->ws.get<double>("osc", (size_t)8 * nev, &err);
   double* part = c->ws.get<double>("osc_part", (size_t)((dim + 255) / 256) * nev * 10, &err);
@@ -837,6 +843,9 @@ int wtb_bsesolver(wtb_ctx* c, const wtb_bse_params* p, double* Ws, double* acts,
     for (long i = 0; i < dim; ++i) Ws[i] = 0.0;
     for (int i = 0; i < nev; ++i) Ws[i] = E[i];
   }
+  c->have_solve = true;
+  c->last_p = *p;
+  c->last_E = E;
   if (t) {
     float a = 0, b = 0, d = 0;
     cudaEventElapsedTime(&a, e0, e1);
@@ -850,7 +859,7 @@ int wtb_bsesolver(wtb_ctx* c, const wtb_bse_params* p, double* Ws, double* acts,
     t->matvec_columns = (int)stats.matvec_columns;
     t->max_rel_residual = stats.max_rel_residual;
     t->refine_shift_max = stats.refine_shift_max;
-    t->kernel_launches = (int)g_launch_count;
+    t->kernel_launches = (int)g_launch_count.load();
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -865,7 +874,7 @@ int wtb_bsedielraw(wtb_ctx* c, const wtb_bse_params* p, int dimse, const double*
   CKR(prep_device(c));
   if (!c->have_hr) return set_err(c, WTB_ESTATE, "lattice not set (call wtb_set_hr first)");
   if (!p || dimse < 1 || !Ws || !acts || !dielf || p->numbse < 2) return set_err(c, WTB_EBADARG, "bad arguments");
-  cudaError_t err;
+  cudaError_t err = cudaSuccess;
   double* dW = c->ws.get<double>("sp_W", dimse, &err);
   double* df = c->ws.get<double>("sp_f", (size_t)6 * dimse, &err);
   double* dd = c->ws.get<double>("sp_d", (size_t)18 * p->numbse, &err);
@@ -884,7 +893,7 @@ int wtb_bseoptprop(wtb_ctx* c, int numbse, const double* dielf, double* props) {
   if (!c) return WTB_EBADARG;
   CKR(prep_device(c));
   if (numbse < 1 || !dielf || !props) return set_err(c, WTB_EBADARG, "bad arguments");
-  cudaError_t err;
+  cudaError_t err = cudaSuccess;
   double* dd = c->ws.get<double>("op_d", (size_t)18 * numbse, &err);
   double* dp = c->ws.get<double>("op_p", (size_t)30 * numbse, &err);
   CKC(err);
@@ -905,7 +914,7 @@ int wtb_bse_matvec(wtb_ctx* c, const wtb_bse_params* p, int ncol, const double* 
     return set_err(c, WTB_EBADARG, "split-BF16 precision is available for the matrix-free operator only");
   if (!(p->ktol > 0.0)) return set_err(c, WTB_EBADARG, "KTOL must be > 0");
   const int dim = c->nk * c->nc * c->nv;
-  cudaError_t err;
+  cudaError_t err = cudaSuccess;
   zd* xc = c->ws.get<zd>("mv_xc", (size_t)dim * ncol, &err);
   zd* x64 = c->ws.get<zd>("mv_x64", (size_t)dim * ncol, &err);
   zd* y64 = c->ws.get<zd>("mv_y64", (size_t)dim * ncol, &err);
@@ -914,6 +923,9 @@ int wtb_bse_matvec(wtb_ctx* c, const wtb_bse_params* p, int ncol, const double* 
   CKC(err);
   OpBundle ob;
   CKR(make_operator(c, p, std::min(ncol, 16), &ob));
+  // a single application: the operator's accurate accumulation, as in the eigensolver's final step
+  if (ob.o64) ob.o64->set_final(true);
+  if (ob.o32) ob.o32->set_final(true);
   CKC(cudaMemcpyAsync(xc, X, sizeof(zd) * dim * ncol, cudaMemcpyHostToDevice, c->s));
   const unsigned nbk = (unsigned)(((long)dim * ncol + 255) / 256);
   // column-major X (dim x ncol) seen as row-major X^T (ncol x dim) -> row-major X
@@ -931,7 +943,7 @@ int wtb_bse_matvec(wtb_ctx* c, const wtb_bse_params* p, int ncol, const double* 
   return check_status(c);
 }
 
-long long wtb_kernel_launch_count(void) { return g_launch_count; }
+long long wtb_kernel_launch_count(void) { return g_launch_count.load(); }
 
 void* wtb_ctx_stream(wtb_ctx* c) { return c ? (void*)c->s : nullptr; }
 

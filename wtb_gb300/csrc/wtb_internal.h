@@ -8,6 +8,7 @@
 //   dense H     H[I][J] row-major; Hermitian, so its column-major image is conj(H)
 //   V table     V[k][k'] real, padded rows/cols for the tensor-core GEMM
 #pragma once
+#include <atomic>
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
@@ -71,7 +72,8 @@ typedef cplx<float> zf;
 struct DevStatus {
   int code;
   int info;
-  int pad[2];
+  int small_sweeps;  // Jacobi sweeps of the projected eigenproblems since the last reset (instrumentation)
+  int small_calls;   // and their number
 };
 
 __device__ __forceinline__ void dev_fail(DevStatus* st, int code, int info) {
@@ -86,6 +88,7 @@ struct CoulParams {
   int ngrid[3];
   double ktol, ediel[3], ez, w, r0, lc;
   double rlat[9];  // row-major rlat[i][j] = component j of a_(i+1)
+  int deriv_r0;    // 1: the table holds dV/dr0 (R_0 key) instead of V
 };
 
 // ----------------------------------------------------------------------------- kernels (launchers)
@@ -165,6 +168,8 @@ int tc_gemm_plan_create(TcGemmPlan** plan, const uint16_t* A, int M, int K, long
                         const uint16_t* B, int N, long b_slice_stride, int nb_slices, float* C, int ldc,
                         int npairs, const int* pair_a, const int* pair_b, std::string* msg);
 cudaError_t tc_gemm_run(TcGemmPlan* plan, DevStatus* st, cudaStream_t s);
+// the same product with K split into ranges of kb_chunk 64-wide blocks, summed in FP32 round-to-nearest
+cudaError_t tc_gemm_run_split(TcGemmPlan* plan, DevStatus* st, cudaStream_t s, int kb_chunk);
 void tc_gemm_plan_destroy(TcGemmPlan* plan);
 int tc_gemm_available();
 
@@ -177,7 +182,13 @@ cudaError_t launch_spectrum(const double* Ws, int nrows, const double* f /*[6][n
                             double* partial, int npart, cudaStream_t s);
 cudaError_t launch_optprops(const double* dielf, int nesp, double* props, cudaStream_t s);
 
-// Every launcher adds the number of kernels it started (reported as gpu_launches by the benchmark).
-extern long long g_launch_count;
+// Raises (never lowers) a kernel's dynamic shared-memory limit on the current device.  Launchers run on
+// several host threads at once (batch workers): setting the limit to each launch's own need would let one
+// thread lower it under another thread's larger launch.
+cudaError_t raise_smem_limit(const void* func, size_t bytes);
+
+// Every launcher adds the number of kernels it started (reported as gpu_launches by the benchmark);
+// atomic because batch workers drive several contexts from several host threads.
+extern std::atomic<long long> g_launch_count;
 
 }  // namespace wtb
