@@ -73,4 +73,6 @@ def test_fit_screening_length_to_target_spectrum(ctx):
         if abs(rb - ra) < 1e-3:
             break
     assert abs(rb - r0_true) < 0.3, rb
-    assert Lb < 0.1 * L0
+    # the target's noise alone leaves numbse * 1e-6 = 1e-3 in the loss
+    noise_floor = p.numbse * 1e-6
+    assert Lb < L0 and Lb < 1.2 * noise_floor, (Lb, L0)

@@ -7,6 +7,7 @@
 // one CTA by cyclic Jacobi in precision S.
 #include <algorithm>
 
+#include "small_eig.cuh"
 #include "wtb_internal.h"
 
 namespace wtb {
@@ -181,191 +182,6 @@ __global__ void convert_cols_kernel(const cplx<Sa>* __restrict__ A, int lda, cpl
 // ----------------------------------------------------------------------------- small Jacobi eigensolver
 __device__ __forceinline__ int rr_player(int i, int t, int n) { return i == 0 ? 0 : ((i - 1 + t) % (n - 1)) + 1; }
 
-// One CTA; each warp owns rotation pairs j = warp, warp + nwarps, ... of the round-robin step.  Its lanes
-// walk the n columns (row update) and then the n rows (column update) of that pair, so no thread does
-// integer division in the inner loops; rotation parameters stay in registers between the two phases,
-// and a step needs two block barriers.
-template <class S>
-__global__ void __launch_bounds__(512) jacobi_small_kernel(zd* A, int lda, int nin, double* evals, zd* evecs,
-                                                           int ldv, int max_sweeps, DevStatus* st) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  constexpr int kMaxPairsPerWarp = 4;  // half <= 64 pairs over 16 warps
-  const int n = (nin + 1) & ~1;
-  const int half = n / 2;
-  // leading dimension n + 1: a column walk then strides 2(n+1) words and spreads over the banks
-  const int ldm = n + 1;
-  cplx<S>* M = reinterpret_cast<cplx<S>*>(smem_raw);
-  cplx<S>* Vv = M + n * ldm;
-  double* ev = reinterpret_cast<double*>(Vv + n * ldm);
-  int* rank = reinterpret_cast<int*>(ev + 128);
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int warp = tid >> 5, lane = tid & 31, nwarps = nt >> 5;
-  for (int e = tid; e < n * n; e += nt) {
-    const int r = e / n, c = e % n;
-    cplx<S> v = mk<S>(0, 0);
-    if (r < nin && c < nin) {
-      // Hermitian part of the input
-      const zd a = A[(size_t)r * lda + c], b = A[(size_t)c * lda + r];
-      v = mk<S>((S)(0.5 * (a.re + b.re)), (S)(0.5 * (a.im - b.im)));
-      if (r == c) v.im = 0;
-    }
-    M[r * ldm + c] = v;
-    Vv[r * ldm + c] = mk<S>(r == c ? (S)1 : (S)0, 0);
-  }
-  __syncthreads();
-  const S tiny = sizeof(S) == 4 ? (S)1e-30 : (S)1e-300;
-  // classical per-pair criterion |a_pq| <= eps sqrt(|a_pp a_qq|): independent of the scale of other
-  // entries (dropped directions carry a large marker on the diagonal)
-  // or |a_pq| <= eps_abs * scale, scale = largest unmarked diagonal magnitude (the rounding floor of the
-  // rotations, which the relative test cannot reach for eigenvalues far below the norm)
-  const double eps2 = sizeof(S) == 4 ? 1e-12 : 1e-30;
-  const double epsa = sizeof(S) == 4 ? 4e-7 : 4e-16;
-  __shared__ int notconv;
-  __shared__ unsigned long long s_scale;
-  __shared__ double s_off;
-  if (tid == 0) s_scale = 0ull;
-  __syncthreads();
-  for (int i = tid; i < nin; i += nt) {
-    const double d = fabs((double)M[i * ldm + i].re);
-    if (d < 1e29) atomicMax(&s_scale, (unsigned long long)__double_as_longlong(d));  // non-negative doubles order as integers
-  }
-  __syncthreads();
-  const double scale = __longlong_as_double((long long)s_scale);
-  const double floor2 = (epsa * scale) * (epsa * scale);
-  // Jacobi converges quadratically; once a sweep no longer shrinks the off-diagonal mass and that mass
-  // is at the rounding floor, the sweep loop stops as well
-  const double noise = (sizeof(S) == 4 ? 1e-6 : 1e-14) * scale;
-  double prev_off = 1e300;
-  int sweeps_done = 0;
-  for (int sweep = 0; sweep < max_sweeps; ++sweep, ++sweeps_done) {
-    if (tid == 0) {
-      notconv = 0;
-      s_off = 0.0;
-    }
-    __syncthreads();
-    int mine = 0;
-    double off = 0.0;
-    for (int e = tid; e < n * n; e += nt) {
-      const int r = e / n, c = e % n;
-      if (r == c) continue;
-      const cplx<S> me = M[r * ldm + c];
-      const double m2 = (double)me.re * me.re + (double)me.im * me.im;
-      const double dd = fabs((double)M[r * ldm + r].re * (double)M[c * ldm + c].re);
-      off += m2;
-      if (m2 > eps2 * dd && m2 > floor2 && m2 > 1e-280) mine = 1;
-    }
-    if (mine) atomicOr(&notconv, 1);
-    for (int o = 16; o > 0; o >>= 1) off += __shfl_xor_sync(0xffffffffu, off, o);
-    if (lane == 0) atomicAdd(&s_off, off);
-    __syncthreads();
-    const int nc = notconv;
-    const double offn = s_off;
-    if (!nc) break;
-    if (sweep >= 2 && offn > 0.25 * prev_off && offn <= noise * noise * (double)n * n) break;
-    prev_off = offn;
-    if (sizeof(S) == 8 && sweep == max_sweeps - 1 && tid == 0) dev_fail(st, 201, n);
-    for (int t = 0; t < n - 1; ++t) {
-      __syncthreads();
-      int pp[kMaxPairsPerWarp], qq[kMaxPairsPerWarp];
-      S cc[kMaxPairsPerWarp], ss[kMaxPairsPerWarp];
-      cplx<S> ph[kMaxPairsPerWarp];
-      bool act[kMaxPairsPerWarp];
-#pragma unroll
-      for (int k = 0; k < kMaxPairsPerWarp; ++k) {
-        const int j = warp + k * nwarps;
-        act[k] = false;
-        if (j >= half) continue;
-        // round-robin (circle) pairing of step t: position i holds player (i - 1 + t) mod (n - 1) + 1
-        int p = j == 0 ? 0 : ((j - 1 + t) % (n - 1)) + 1;
-        int q = ((n - 2 - j + t) % (n - 1)) + 1;
-        if (p > q) {
-          const int tmp = p;
-          p = q;
-          q = tmp;
-        }
-        pp[k] = p;
-        qq[k] = q;
-        const cplx<S> apq = M[p * ldm + q];
-        const S app = M[p * ldm + p].re, aqq = M[q * ldm + q].re;
-        const S b = sqrt(apq.re * apq.re + apq.im * apq.im);
-        if (b > tiny) {
-          ph[k] = mk<S>(apq.re / b, apq.im / b);
-          const S zeta = (aqq - app) / (2 * b);
-          S tt;
-          if (fabs(zeta) > (S)1e15)
-            tt = (S)0.5 / zeta;
-          else
-            tt = (zeta >= 0 ? (S)1 : (S)-1) / (fabs(zeta) + sqrt((S)1 + zeta * zeta));
-          cc[k] = (S)1 / sqrt((S)1 + tt * tt);
-          ss[k] = tt * cc[k];
-          act[k] = true;
-        }
-      }
-      __syncwarp();
-      // rows: A_p. <- c A_p. - s e^{i phi} A_q. ; A_q. <- s A_p. + c e^{i phi} A_q.
-#pragma unroll
-      for (int k = 0; k < kMaxPairsPerWarp; ++k) {
-        if (!act[k]) continue;
-        const int p = pp[k], q = qq[k];
-        const S c = cc[k], s = ss[k];
-        for (int col = lane; col < n; col += 32) {
-          const cplx<S> ap = M[p * ldm + col], aq = M[q * ldm + col];
-          const cplx<S> phq = cmul(ph[k], aq);
-          M[p * ldm + col] = mk<S>(c * ap.re - s * phq.re, c * ap.im - s * phq.im);
-          M[q * ldm + col] = mk<S>(s * ap.re + c * phq.re, s * ap.im + c * phq.im);
-        }
-      }
-      __syncthreads();
-      // columns of A and V: A_.p <- c A_.p - s e^{-i phi} A_.q ; A_.q <- s A_.p + c e^{-i phi} A_.q
-#pragma unroll
-      for (int k = 0; k < kMaxPairsPerWarp; ++k) {
-        if (!act[k]) continue;
-        const int p = pp[k], q = qq[k];
-        const S c = cc[k], s = ss[k];
-        const cplx<S> phc = mk<S>(ph[k].re, -ph[k].im);
-        for (int row = lane; row < n; row += 32) {
-          cplx<S> ap = M[row * ldm + p], aq = M[row * ldm + q];
-          cplx<S> phq = cmul(phc, aq);
-          M[row * ldm + p] = mk<S>(c * ap.re - s * phq.re, c * ap.im - s * phq.im);
-          M[row * ldm + q] = mk<S>(s * ap.re + c * phq.re, s * ap.im + c * phq.im);
-          ap = Vv[row * ldm + p];
-          aq = Vv[row * ldm + q];
-          phq = cmul(phc, aq);
-          Vv[row * ldm + p] = mk<S>(c * ap.re - s * phq.re, c * ap.im - s * phq.im);
-          Vv[row * ldm + q] = mk<S>(s * ap.re + c * phq.re, s * ap.im + c * phq.im);
-        }
-        __syncwarp();
-        if (lane == 0) {
-          M[p * ldm + q] = mk<S>(0, 0);
-          M[q * ldm + p] = mk<S>(0, 0);
-          M[p * ldm + p].im = 0;
-          M[q * ldm + q].im = 0;
-        }
-      }
-    }
-    __syncthreads();
-  }
-  __syncthreads();
-  if (tid == 0) {
-    atomicAdd(&st->small_sweeps, sweeps_done);
-    atomicAdd(&st->small_calls, 1);
-  }
-  if (tid < nin) ev[tid] = (double)M[tid * ldm + tid].re;
-  __syncthreads();
-  if (tid < nin) {
-    int r = 0;
-    const double x = ev[tid];
-    for (int j = 0; j < nin; ++j) r += (ev[j] < x) || (ev[j] == x && j < tid);
-    rank[tid] = r;
-  }
-  __syncthreads();
-  if (tid < nin) evals[rank[tid]] = ev[tid];
-  for (int e = tid; e < nin * nin; e += nt) {
-    const int row = e / nin, j = e % nin;
-    const cplx<S> v = Vv[row * ldm + j];
-    evecs[(size_t)row * ldv + rank[j]] = mk<double>((double)v.re, (double)v.im);
-  }
-}
 
 // ----------------------------------------------------------------------------- small helpers
 __global__ void small_gemm_kernel(const zd* __restrict__ A, int lda, int transA, const zd* __restrict__ B, int ldb,
@@ -383,40 +199,9 @@ __global__ void small_gemm_kernel(const zd* __restrict__ A, int lda, int transA,
   C[(size_t)i * ldc + j] = acc;
 }
 
-__global__ void svqb_scale_kernel(const zd* __restrict__ M, int ldm, int n, double* dinv) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double d = M[(size_t)i * ldm + i].re;
-  dinv[i] = d > 1e-300 ? 1.0 / sqrt(d) : 0.0;
-}
 
-__global__ void scale_sym_kernel(zd* M, int ldm, int n, const double* __restrict__ dinv) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= n * n) return;
-  const int i = e / n, j = e % n;
-  M[(size_t)i * ldm + j] = cscale(M[(size_t)i * ldm + j], dinv[i] * dinv[j]);
-}
 
-// B[:, j] = dinv .* U[:, j] / sqrt(lam_j) for lam_j > tau * lam_max; dropped columns are zero and
-// flagged by a negative entry in rank_flags[j] (consumed by mark_dropped_kernel).
-__global__ void svqb_basis_kernel(const double* __restrict__ dinv, const zd* __restrict__ U, int ldu,
-                                  const double* __restrict__ lam, int n, double tau, zd* __restrict__ B, int ldb,
-                                  int* keep) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= n * n) return;
-  const int i = e / n, j = e % n;
-  const double lmax = lam[n - 1];
-  const bool k = lam[j] > tau * lmax && lam[j] > 0.0;
-  if (i == 0) keep[j] = k ? 1 : 0;
-  B[(size_t)i * ldb + j] = k ? cscale(U[(size_t)i * ldu + j], dinv[i] / sqrt(lam[j])) : mk<double>(0.0, 0.0);
-}
 
-__global__ void mark_dropped_kernel(zd* G, int ldg, int n, const int* __restrict__ keep) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= n * n) return;
-  const int i = e / n, j = e % n;
-  if (!keep[i] || !keep[j]) G[(size_t)i * ldg + j] = mk<double>(i == j ? 1e30 : 0.0, 0.0);
-}
 
 __device__ __forceinline__ double hash_noise(unsigned a, unsigned b, unsigned seed) {
   unsigned h = a * 2654435761u ^ (b + 0x9e3779b9u + (seed << 6) + (seed >> 2));
@@ -488,6 +273,177 @@ __global__ void init_guess_kernel(cplx<S>* X, int ldx, int dim, int m, const int
   double im = 1e-3 * hash_noise((unsigned)r, (unsigned)j + 7919u, seed);
   if (idx[j] == r) re += 1.0;
   X[r * ldx + j] = mk<S>((S)re, (S)im);
+}
+
+// Lowest nwant eigenpairs of the Hermitian part of the leading n x n block of Ag (n = *nptr if nptr, capped
+// at nmax), in precision S, by the tridiagonal route of small_eig.cuh.  evals[k] ascending; evecs (nmax rows,
+// leading dimension ldv): column k for k < min(nwant, n); rows >= n and the columns of missing eigenpairs
+// are zero, and a missing eigenvalue is 1e30 (a direction the orthonormalisation dropped).
+template <class S>
+__global__ void __launch_bounds__(256) heev_small_kernel(const zd* __restrict__ Ag, int lda, const int* __restrict__ nptr,
+                                                         int nmax, int nwant, double* __restrict__ evals,
+                                                         zd* __restrict__ evecs, int ldv) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = nptr ? min(max(*nptr, 0), nmax) : nmax;
+  const int nw = min(nwant, n);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int lds = n + 1;
+  cplx<S>* A = reinterpret_cast<cplx<S>*>(smem_raw);
+  cplx<S>* p = A + (size_t)n * lds;
+  cplx<S>* tau = p + nmax;
+  S* d = reinterpret_cast<S*>(tau + nmax);
+  S* e = d + nmax;
+  S* e2 = e + nmax;
+  S* lam = e2 + nmax;
+  S* red = lam + nmax;
+  S* Z = red + 4;
+  S* Dv = Z + (size_t)nmax * nwant;
+  S* Lv = Dv + (size_t)nmax * nwant;
+  int* cl = reinterpret_cast<int*>(Lv + (size_t)nmax * nwant);
+  int* flag = cl + nwant;
+  for (int q = tid; q < n * n; q += nt) {
+    const int r = q / n, c = q % n;
+    const zd a = Ag[(size_t)r * lda + c], b = Ag[(size_t)c * lda + r];
+    A[(size_t)r * lds + c] = mk<S>((S)(0.5 * (a.re + b.re)), r == c ? (S)0 : (S)(0.5 * (a.im - b.im)));
+  }
+  __syncthreads();
+  if (n > 0) {
+    tridiag_cta<S>(A, lds, n, d, e, tau, p, flag);
+    cplx<S>* U = reinterpret_cast<cplx<S>*>(Dv);
+    tridiag_eigvecs_cta<S>(A, lds, n, nw, d, e, tau, e2, lam, Z, Dv, Lv, cl, U, nw > 0 ? nw : 1, red);
+    for (int q = tid; q < nmax * nwant; q += nt) {
+      const int r = q / nwant, k = q % nwant;
+      zd v = mk<double>(0.0, 0.0);
+      if (r < n && k < nw) {
+        const cplx<S> u = U[(size_t)r * nw + k];
+        v = mk<double>((double)u.re, (double)u.im);
+      }
+      evecs[(size_t)r * ldv + k] = v;
+    }
+    for (int k = tid; k < nwant; k += nt) evals[k] = k < nw ? (double)lam[k] : 1e30;
+  } else {
+    for (int q = tid; q < nmax * nwant; q += nt) evecs[(size_t)(q / nwant) * ldv + q % nwant] = mk<double>(0.0, 0.0);
+    for (int k = tid; k < nwant; k += nt) evals[k] = 1e30;
+  }
+}
+
+// Orthonormalising basis of the Gram matrix M = S^H S (n x n, complex(8)) by pivoted Cholesky in precision S:
+// with D = diag(M) and Ms = D^-1/2 M D^-1/2, pivots are taken largest residual diagonal first while it exceeds
+// drop (relative to Ms's unit diagonal); for the r chosen columns P, Ms[P,P] = R^H R and
+// B = D_P^-1/2 R^-1 makes S B orthonormal.  B (n x n, leading dimension ldb) holds those r columns first and
+// zeros elsewhere; *r_out = r.  Dropped columns are numerically in the span of the kept ones (the
+// directions SVQB drops by eigenvalue are dropped here by residual norm).
+template <class S>
+__global__ void __launch_bounds__(256) pchol_basis_kernel(const zd* __restrict__ Mg, int ldm, int n, double drop,
+                                                          zd* __restrict__ B, int ldb, int* __restrict__ r_out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int lds = n + 1;
+  cplx<S>* W = reinterpret_cast<cplx<S>*>(smem_raw);  // residual matrix (original index order)
+  cplx<S>* R = W + (size_t)n * lds;                    // R[k][original column], rows in pivot order
+  S* dinv = reinterpret_cast<S*>(R + (size_t)n * lds);
+  int* perm = reinterpret_cast<int*>(dinv + n);
+  int* chosen = perm + n;
+  __shared__ int s_r, s_piv;
+  for (int i = tid; i < n; i += nt) {
+    const double m = Mg[(size_t)i * ldm + i].re;
+    dinv[i] = m > 1e-300 ? (S)(1.0 / sqrt(m)) : (S)0;
+    chosen[i] = 0;
+  }
+  __syncthreads();
+  for (int q = tid; q < n * n; q += nt) {
+    const int i = q / n, j = q % n;
+    const zd a = Mg[(size_t)i * ldm + j], b = Mg[(size_t)j * ldm + i];
+    const S sc = dinv[i] * dinv[j];
+    W[(size_t)i * lds + j] = mk<S>((S)(0.5 * (a.re + b.re)) * sc, i == j ? (S)0 : (S)(0.5 * (a.im - b.im)) * sc);
+  }
+  if (tid == 0) s_r = n;
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    if (warp == 0) {
+      S best = (S)-1;
+      int bi = -1;
+      for (int i = lane; i < n; i += 32) {
+        const S v = chosen[i] ? (S)-1 : W[(size_t)i * lds + i].re;
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const S ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi >= 0 && (bi < 0 || oi < bi))) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      if (lane == 0) {
+        if (bi < 0 || !(best > (S)drop)) {
+          s_r = k;
+          s_piv = -1;
+        } else {
+          s_piv = bi;
+          perm[k] = bi;
+          chosen[bi] = 1;
+        }
+      }
+    }
+    __syncthreads();
+    const int pv = s_piv;
+    if (pv < 0) break;
+    const S rkk = sqrt(W[(size_t)pv * lds + pv].re);
+    // row k of R: R[k][j] = W[pv][j] / rkk for the unchosen j, rkk at the pivot
+    for (int j = tid; j < n; j += nt) {
+      cplx<S> v = mk<S>(0, 0);
+      if (j == pv)
+        v = mk<S>(rkk, 0);
+      else if (!chosen[j])
+        v = mk<S>(W[(size_t)pv * lds + j].re / rkk, W[(size_t)pv * lds + j].im / rkk);
+      R[(size_t)k * lds + j] = v;
+    }
+    __syncthreads();
+    // Schur complement on the unchosen rows and columns: W[i][j] -= conj(R[k][i]) R[k][j]
+    for (int q = tid; q < n * n; q += nt) {
+      const int i = q / n, j = q % n;
+      if (chosen[i] || chosen[j]) continue;
+      const cplx<S> ri = R[(size_t)k * lds + i], rj = R[(size_t)k * lds + j];
+      cplx<S>& w = W[(size_t)i * lds + j];
+      w.re -= ri.re * rj.re + ri.im * rj.im;
+      w.im -= ri.re * rj.im - ri.im * rj.re;
+    }
+    __syncthreads();
+  }
+  const int r = s_r;
+  // R^-1 (r x r, upper triangular in pivot order), one thread per column c, stored over W's rows
+  cplx<S>* Ri = W;  // Ri[k][c], leading dimension lds
+  for (int c = tid; c < r; c += nt) {
+    for (int k = c + 1; k < r; ++k) Ri[(size_t)k * lds + c] = mk<S>(0, 0);
+    const S rcc = R[(size_t)c * lds + perm[c]].re;
+    Ri[(size_t)c * lds + c] = mk<S>((S)1 / rcc, 0);
+    for (int k = c - 1; k >= 0; --k) {
+      cplx<S> acc = mk<S>(0, 0);
+      for (int l = k + 1; l <= c; ++l) cfma(acc, R[(size_t)k * lds + perm[l]], Ri[(size_t)l * lds + c]);
+      const S rkk = R[(size_t)k * lds + perm[k]].re;
+      Ri[(size_t)k * lds + c] = mk<S>(-acc.re / rkk, -acc.im / rkk);
+    }
+  }
+  __syncthreads();
+  // B[perm[k]][c] = dinv[perm[k]] Ri[k][c] (k <= c < r); everything else zero
+  for (int q = tid; q < n * n; q += nt) {
+    const int i = q / n, c = q % n;
+    B[(size_t)i * ldb + c] = mk<double>(0.0, 0.0);
+  }
+  __syncthreads();
+  for (int q = tid; q < r * r; q += nt) {
+    const int k = q / r, c = q % r;
+    if (k > c) continue;
+    const int i = perm[k];
+    const cplx<S> v = Ri[(size_t)k * lds + c];
+    B[(size_t)i * ldb + c] = mk<double>((double)v.re * (double)dinv[i], (double)v.im * (double)dinv[i]);
+  }
+  if (tid == 0) *r_out = r;
 }
 
 }  // namespace
@@ -562,28 +518,38 @@ cudaError_t launch_convert_cols(const cplx<Sa>* A, int lda, cplx<Sb>* B, int ldb
   return cudaGetLastError();
 }
 
+
+
+
 template <class S>
-static cudaError_t jacobi_launch(zd* A, int lda, int n, double* evals, zd* evecs, int ldv, int sweeps,
-                                 DevStatus* st, cudaStream_t s) {
-  const int np = (n + 1) & ~1;
-  if (np / 2 > 64) return cudaErrorInvalidValue;
-  const size_t smem = (size_t)2 * np * (np + 1) * sizeof(cplx<S>) + 128 * sizeof(double) + 128 * sizeof(int) + 64;
+cudaError_t launch_heev_small(const zd* A, int lda, const int* nptr, int nmax, int nwant, double* evals, zd* evecs,
+                              int ldv, cudaStream_t s) {
+  if (nmax < 1 || nmax > 96 || nwant < 0 || nwant > nmax) return cudaErrorInvalidValue;
+  const size_t smem = (size_t)nmax * (nmax + 1) * sizeof(cplx<S>) + (size_t)2 * nmax * sizeof(cplx<S>) +
+                      (size_t)(4 * nmax + 4) * sizeof(S) + (size_t)3 * nmax * nwant * sizeof(S) +
+                      (size_t)(nwant + 4) * sizeof(int) + 64;
   if (smem > 220 * 1024) return cudaErrorInvalidValue;
-  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(jacobi_small_kernel<S>), (size_t)smem);
+  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(heev_small_kernel<S>), smem);
   if (e != cudaSuccess) return e;
-  jacobi_small_kernel<S><<<1, 512, smem, s>>>(A, lda, n, evals, evecs, ldv, sweeps, st); ++g_launch_count;
+  heev_small_kernel<S><<<1, 256, smem, s>>>(A, lda, nptr, nmax, nwant, evals, evecs, ldv); ++g_launch_count;
   return cudaGetLastError();
 }
 
-cudaError_t launch_jacobi_eig(zd* A, int lda, int n, double* evals, zd* evecs, int ldv, int sweeps, DevStatus* st,
-                              cudaStream_t s) {
-  return jacobi_launch<double>(A, lda, n, evals, evecs, ldv, sweeps, st, s);
+template <class S>
+cudaError_t launch_pchol_basis(const zd* M, int ldm, int n, double drop, zd* B, int ldb, int* r_out, cudaStream_t s) {
+  if (n < 1 || n > 96) return cudaErrorInvalidValue;
+  const size_t smem = (size_t)2 * n * (n + 1) * sizeof(cplx<S>) + (size_t)n * sizeof(S) + (size_t)2 * n * sizeof(int) + 64;
+  if (smem > 220 * 1024) return cudaErrorInvalidValue;
+  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(pchol_basis_kernel<S>), smem);
+  if (e != cudaSuccess) return e;
+  pchol_basis_kernel<S><<<1, 256, smem, s>>>(M, ldm, n, drop, B, ldb, r_out); ++g_launch_count;
+  return cudaGetLastError();
 }
 
-cudaError_t launch_jacobi_eig_f32(zd* A, int lda, int n, double* evals, zd* evecs, int ldv, int sweeps,
-                                  DevStatus* st, cudaStream_t s) {
-  return jacobi_launch<float>(A, lda, n, evals, evecs, ldv, sweeps, st, s);
-}
+template cudaError_t launch_heev_small<float>(const zd*, int, const int*, int, int, double*, zd*, int, cudaStream_t);
+template cudaError_t launch_heev_small<double>(const zd*, int, const int*, int, int, double*, zd*, int, cudaStream_t);
+template cudaError_t launch_pchol_basis<float>(const zd*, int, int, double, zd*, int, int*, cudaStream_t);
+template cudaError_t launch_pchol_basis<double>(const zd*, int, int, double, zd*, int, int*, cudaStream_t);
 
 cudaError_t launch_small_gemm(const zd* A, int lda, int transA, const zd* B, int ldb, zd* C, int ldc, int m, int n,
                               int k, cudaStream_t s) {
@@ -591,26 +557,9 @@ cudaError_t launch_small_gemm(const zd* A, int lda, int transA, const zd* B, int
   return cudaGetLastError();
 }
 
-cudaError_t launch_svqb_scale(const zd* M, int ldm, int n, double* dinv, cudaStream_t s) {
-  svqb_scale_kernel<<<1, 128, 0, s>>>(M, ldm, n, dinv); ++g_launch_count;
-  return cudaGetLastError();
-}
 
-cudaError_t launch_scale_sym(zd* M, int ldm, int n, const double* dinv, cudaStream_t s) {
-  scale_sym_kernel<<<(n * n + 255) / 256, 256, 0, s>>>(M, ldm, n, dinv); ++g_launch_count;
-  return cudaGetLastError();
-}
 
-cudaError_t launch_svqb_basis(const double* dinv, const zd* U, int ldu, const double* lam, int n, double tau, zd* B,
-                              int ldb, int* keep, cudaStream_t s) {
-  svqb_basis_kernel<<<(n * n + 255) / 256, 256, 0, s>>>(dinv, U, ldu, lam, n, tau, B, ldb, keep); ++g_launch_count;
-  return cudaGetLastError();
-}
 
-cudaError_t launch_mark_dropped(zd* G, int ldg, int n, const int* keep, cudaStream_t s) {
-  mark_dropped_kernel<<<(n * n + 255) / 256, 256, 0, s>>>(G, ldg, n, keep); ++g_launch_count;
-  return cudaGetLastError();
-}
 
 // idx needs room for 64 * m + m ints (candidates then the result), idx[64 m .. 64 m + m) holds the answer.
 cudaError_t launch_select_lowest(const double* diag, int dim, int m, int* idx, double* cand_val, cudaStream_t s) {

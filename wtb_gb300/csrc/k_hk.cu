@@ -8,6 +8,7 @@
 // threads at once.  The matrix and the accumulated rotations live in shared memory (w <= 64).
 // Gauge: every eigenvector is rotated so its first component is real and >= 0, the gauge ZHEEV('L')
 // produces up to a sign (the Householder reflectors of ZHETRD('L') leave e1 invariant).
+#include "small_eig.cuh"
 #include "wtb_internal.h"
 
 namespace wtb {
@@ -41,114 +42,6 @@ __device__ __forceinline__ double rcomp_f32(const int* rvec, int nR, int iR, con
   return (double)__double2float_rn(rcart(r1, r2, r3, rl, a));
 }
 
-// Jacobi eigen-decomposition of the n x n (n even, n <= 64) Hermitian matrix A (shared, leading
-// dimension ld = n + 1 so column walks spread over the shared-memory banks); V receives the eigenvectors
-// as columns.  Round-robin (circle) ordering: the n/2 rotations of a step touch disjoint rows/columns,
-// so all threads apply them element by element (for w of 8..22 orbitals the elements of a step keep
-// the block's 128 threads busier than one warp per rotation would).
-__device__ void jacobi_shared(zd* A, zd* V, int n, double* rc, double* rs, zd* rph, int* rp, int* rq, int* flag,
-                              double* red) {
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int ld = n + 1;
-  for (int e = tid; e < n * n; e += nt) V[(e / n) * ld + e % n] = mk<double>((e / n) == (e % n) ? 1.0 : 0.0, 0.0);
-  __syncthreads();
-  const int half = n / 2;
-  for (int sweep = 0; sweep < 40; ++sweep) {
-    // convergence test: off-diagonal Frobenius norm against the diagonal
-    if (tid == 0) {
-      red[0] = 0.0;
-      red[1] = 0.0;
-    }
-    __syncthreads();
-    double off = 0.0, dia = 0.0;
-    for (int e = tid; e < n * n; e += nt) {
-      const int r = e / n, c = e % n;
-      if (r == c)
-        dia += A[r * ld + c].re * A[r * ld + c].re;
-      else
-        off += cabs2(A[r * ld + c]);
-    }
-    atomicAdd(&red[0], off);
-    atomicAdd(&red[1], dia);
-    __syncthreads();
-    const double offn = red[0], dian = red[1];
-    __syncthreads();
-    if (offn <= 1e-32 * dian || offn == 0.0) break;
-    for (int t = 0; t < n - 1; ++t) {
-      if (tid < half) {
-        int p = tid == 0 ? 0 : ((tid - 1 + t) % (n - 1)) + 1;
-        int q = ((n - 2 - tid + t) % (n - 1)) + 1;
-        if (p > q) {
-          const int tmp = p;
-          p = q;
-          q = tmp;
-        }
-        const zd apq = A[p * ld + q];
-        const double app = A[p * ld + p].re, aqq = A[q * ld + q].re;
-        const double b = sqrt(cabs2(apq));
-        double c = 1.0, s = 0.0;
-        zd ph = mk<double>(1.0, 0.0);
-        int act = 0;
-        if (b > 1e-300 && b > 1e-18 * (fabs(app) + fabs(aqq))) {
-          ph = mk<double>(apq.re / b, apq.im / b);
-          const double zeta = (aqq - app) / (2.0 * b);
-          double tt;
-          if (fabs(zeta) > 1e150)
-            tt = 0.5 / zeta;
-          else
-            tt = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-          c = 1.0 / sqrt(1.0 + tt * tt);
-          s = tt * c;
-          act = 1;
-        }
-        rc[tid] = c;
-        rs[tid] = s;
-        rph[tid] = ph;
-        rp[tid] = p;
-        rq[tid] = q;
-        flag[tid] = act;
-      }
-      __syncthreads();
-      // rows: A_p. <- c A_p. - s e^{i phi} A_q. ; A_q. <- s A_p. + c e^{i phi} A_q.
-      for (int e = tid; e < half * n; e += nt) {
-        const int j = e / n, col = e % n;
-        if (!flag[j]) continue;
-        const int p = rp[j], q = rq[j];
-        const double c = rc[j], s = rs[j];
-        const zd ap = A[p * ld + col], aq = A[q * ld + col];
-        const zd phq = cmul(rph[j], aq);
-        A[p * ld + col] = mk<double>(c * ap.re - s * phq.re, c * ap.im - s * phq.im);
-        A[q * ld + col] = mk<double>(s * ap.re + c * phq.re, s * ap.im + c * phq.im);
-      }
-      __syncthreads();
-      // columns of A and V: A_.p <- c A_.p - s e^{-i phi} A_.q ; A_.q <- s A_.p + c e^{-i phi} A_.q
-      for (int e = tid; e < half * n * 2; e += nt) {
-        const int which = e / (half * n);
-        const int ee = e % (half * n);
-        const int j = ee / n, row = ee % n;
-        if (!flag[j]) continue;
-        zd* M = which ? V : A;
-        const int p = rp[j], q = rq[j];
-        const double c = rc[j], s = rs[j];
-        const zd phc = mk<double>(rph[j].re, -rph[j].im);
-        const zd ap = M[row * ld + p], aq = M[row * ld + q];
-        const zd phq = cmul(phc, aq);
-        M[row * ld + p] = mk<double>(c * ap.re - s * phq.re, c * ap.im - s * phq.im);
-        M[row * ld + q] = mk<double>(s * ap.re + c * phq.re, s * ap.im + c * phq.im);
-      }
-      __syncthreads();
-      if (tid < half && flag[tid]) {
-        const int p = rp[tid], q = rq[tid];
-        A[p * ld + q] = mk<double>(0.0, 0.0);
-        A[q * ld + p] = mk<double>(0.0, 0.0);
-        A[p * ld + p].im = 0.0;
-        A[q * ld + q].im = 0.0;
-      }
-      __syncthreads();
-    }
-  }
-}
-
 __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict__ hr, const int* __restrict__ rvec,
                                                             const int* __restrict__ ndegen, int nR, int w,
                                                             const double* __restrict__ rlat, double efermi, double scs,
@@ -158,20 +51,23 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int k = blockIdx.x;
   if (k >= nk) return;
-  const int n = (w + 1) & ~1;
+  const int n = w;
   const int ld = n + 1;
   zd* A = reinterpret_cast<zd*>(smem_raw);
-  zd* V = A + n * ld;
-  zd* eph = V + n * ld;  // nR phases
-  double* rc = reinterpret_cast<double*>(eph + nR);
-  double* rs = rc + 32;
-  zd* rph = reinterpret_cast<zd*>(rs + 32);
-  double* red = reinterpret_cast<double*>(rph + 32);
-  double* ev = red + 4;  // n eigenvalues
-  int* rp = reinterpret_cast<int*>(ev + 64);
-  int* rq = rp + 32;
-  int* flag = rq + 32;
-  int* rank = flag + 32;  // n
+  zd* eph = A + n * ld;  // nR phases
+  zd* p = eph + nR;      // n
+  zd* tau = p + n;       // n
+  double* d = reinterpret_cast<double*>(tau + n);
+  double* e = d + n;
+  double* e2 = e + n;
+  double* lam = e2 + n;
+  double* red = lam + n;  // 4
+  double* Z = red + 4;    // n * n
+  double* Dv = Z + n * n; // n * n, then Lv n * n; the eigenvectors U (n x n complex) reuse both
+  double* Lv = Dv + n * n;
+  int* cl = reinterpret_cast<int*>(Lv + n * n);
+  int* flag = cl + n;
+  zd* U = reinterpret_cast<zd*>(Dv);
   __shared__ double rl[9];
   __shared__ int s_nocp;
   const int tid = threadIdx.x;
@@ -186,67 +82,51 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
     eph[r] = mk<double>(cs * inv, sn * inv);
   }
   __syncthreads();
-  for (int e = tid; e < n * n; e += blockDim.x) {
-    const int m = e / n, c = e % n;
-    zd acc = mk<double>(0.0, 0.0);
-    if (m < w && c < w) {
-      for (int r = 0; r < nR; ++r) cfma(acc, eph[r], hr[((size_t)r * w + m) * w + c]);
-      if (m == c) acc.re -= efermi;
-    }
-    A[m * ld + c] = acc;
-  }
-  __syncthreads();
   // ZHEEV('V','L') reads the lower triangle and the real part of the diagonal only: the matrix that is
   // diagonalised is the Hermitian completion of the lower triangle (identical to H(k) when the H(R) set
   // is Hermitian-consistent; a perturbation of an upper-triangle entry does not reach the eigensolve)
-  for (int e = tid; e < n * n; e += blockDim.x) {
-    const int m = e / n, c = e % n;
-    if (m > c) {
-      const zd a = A[m * ld + c];
-      A[c * ld + m] = mk<double>(a.re, -a.im);
-    } else if (m == c) {
-      A[m * ld + c].im = 0.0;
+  for (int q = tid; q < n * n; q += blockDim.x) {
+    const int m = q / n, c = q % n;
+    if (m < c) continue;
+    zd acc = mk<double>(0.0, 0.0);
+    for (int r = 0; r < nR; ++r) cfma(acc, eph[r], hr[((size_t)r * w + m) * w + c]);
+    if (m == c) {
+      acc.re -= efermi;
+      acc.im = 0.0;
     }
+    A[m * ld + c] = acc;
+    if (m != c) A[c * ld + m] = mk<double>(acc.re, -acc.im);
   }
   __syncthreads();
-  jacobi_shared(A, V, n, rc, rs, rph, rp, rq, flag, red);
-  // ascending order of the w real eigenvalues (the padding index w, if any, is excluded)
-  if (tid < w) ev[tid] = A[tid * ld + tid].re;
-  __syncthreads();
-  if (tid < w) {
-    int r = 0;
-    const double x = ev[tid];
-    for (int j = 0; j < w; ++j) r += (ev[j] < x) || (ev[j] == x && j < tid);
-    rank[tid] = r;
-  }
-  __syncthreads();
+  tridiag_cta<double>(A, ld, n, d, e, tau, p, flag);
+  tridiag_eigvecs_cta<double>(A, ld, n, n, d, e, tau, e2, lam, Z, Dv, Lv, cl, U, n, red);
   if (tid == 0) {
     int cnt = 0;
-    for (int j = 0; j < w; ++j) cnt += (ev[j] <= 0.0);
+    for (int j = 0; j < n; ++j) cnt += (lam[j] <= 0.0);
     s_nocp = cnt;  // = index of the first E > 0 in ascending order
   }
   __syncthreads();
   const int nocp = s_nocp;
-  // outputs: eigenvalue j goes to position rank[j]; eigenvector = column j of V, gauge fixed
-  for (int e = tid; e < w * w; e += blockDim.x) {
-    const int j = e / w, o = e % w;
-    const zd a0 = V[0 * ld + j];
+  // outputs in ascending order; eigenvector j = column j of U, rotated so that its first component is real
+  // and >= 0 (ZHEEV('L') returns it real; the sign does not reach any output)
+  for (int q = tid; q < w * w; q += blockDim.x) {
+    const int j = q / w, o = q % w;
+    const zd a0 = U[0 * n + j];
     const double m0 = sqrt(cabs2(a0));
     zd g = mk<double>(1.0, 0.0);
     if (m0 > 0.0) g = mk<double>(a0.re / m0, -a0.im / m0);
-    zd val = cmul(V[o * ld + j], g);
+    zd val = cmul(U[o * n + j], g);
     if (o == 0) val = mk<double>(m0, 0.0);
-    const int r = rank[j];
-    if (vec_all) vec_all[((size_t)k * w + r) * w + o] = val;
-    const int s = r - (nocp - nv);
-    if (vec_win && s >= 0 && s < nv + nc) vec_win[((size_t)k * (nv + nc) + s) * w + o] = val;
+    if (vec_all) vec_all[((size_t)k * w + j) * w + o] = val;
+    const int sl = j - (nocp - nv);
+    if (vec_win && sl >= 0 && sl < nv + nc) vec_win[((size_t)k * (nv + nc) + sl) * w + o] = val;
   }
   if (tid < w) {
-    const int r = rank[tid];
-    const double e = ev[tid] + (r >= nocp ? scs : 0.0);
-    if (eig_all) eig_all[(size_t)k * w + r] = e;
-    const int s = r - (nocp - nv);
-    if (eig_win && s >= 0 && s < nv + nc) eig_win[(size_t)k * (nv + nc) + s] = e;
+    const int j = tid;
+    const double ev = lam[j] + (j >= nocp ? scs : 0.0);
+    if (eig_all) eig_all[(size_t)k * w + j] = ev;
+    const int sl = j - (nocp - nv);
+    if (eig_win && sl >= 0 && sl < nv + nc) eig_win[(size_t)k * (nv + nc) + sl] = ev;
   }
   if (tid == 0) {
     if (nocp_out) nocp_out[k] = nocp;
@@ -512,9 +392,11 @@ cudaError_t launch_hk_eig(const zd* hr, const int* rvec, const int* ndegen, int 
                           double efermi, double scs, const double* kpt, int nk, int nv, int nc, double* eig_all,
                           zd* vec_all, double* eig_win, zd* vec_win, int* nocp, DevStatus* st, cudaStream_t s) {
   if (w > 64 || w < 1) return cudaErrorInvalidValue;
-  const int n = (w + 1) & ~1;
-  const size_t smem = (size_t)2 * n * (n + 1) * sizeof(zd) + nR * sizeof(zd) + 32 * 2 * sizeof(double) + 32 * sizeof(zd) +
-                      4 * sizeof(double) + 64 * sizeof(double) + 32 * 3 * sizeof(int) + 64 * sizeof(int) + 64;
+  const int n = w;
+  // A, phases, p, tau (complex); d, e, e2, lam, red; Z, Dv, Lv (n x n each); cluster ids and flag
+  const size_t smem = (size_t)(n * (n + 1) + nR + 2 * n) * sizeof(zd) + (size_t)(4 * n + 4 + 3 * n * n) * sizeof(double) +
+                      (size_t)(n + 4) * sizeof(int) + 64;
+  if (smem > 220 * 1024) return cudaErrorInvalidValue;
   cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(hk_eig_kernel), (size_t)smem);
   if (e != cudaSuccess) return e;
   hk_eig_kernel<<<nk, kHkThreads, smem, s>>>(hr, rvec, ndegen, nR, w, rlat_rm, efermi, scs, kpt, nk, nv, nc, eig_all,

@@ -1,0 +1,286 @@
+// CTA-cooperative eigensolver for small Hermitian matrices held in shared memory (n <= 96): the projected
+// problems of the block eigensolver and the per-k band problems.
+//
+// Method (the route of LAPACK's ZHEEV: ZHETRD + a tridiagonal eigensolver + back-transformation; here with
+// bisection and inverse iteration for the tridiagonal stage because their work is independent per
+// eigenpair and spreads over the CTA's threads):
+//   1. Householder reduction to a real symmetric tridiagonal T = Q^H A Q with Q = H_0 H_1 ... H_{n-2},
+//      H_j = I - tau_j v_j v_j^H (the lower-triangle convention of ZHETD2; v_j[0] = 1), three barriers a step;
+//   2. the k-th smallest eigenvalue of T by Sturm-count bisection, one thread per eigenvalue;
+//   3. its eigenvector z_k by inverse iteration (L D L^T of T - lam_k I with safeguarded pivots, three
+//      solves from a fixed pseudo-random start), one thread per eigenvector, then modified Gram-Schmidt
+//      inside each cluster of close eigenvalues (one warp per cluster);
+//   4. u_k = Q z_k, one warp per eigenvector (no block barrier: each warp owns its vectors).
+// An unreduced tridiagonal matrix has distinct eigenvalues; (near-)degenerate ones come from (near-)zero
+// off-diagonal entries, for which independent inverse iterations from different starts give independent
+// vectors of the eigenspace, made orthonormal by step 3's Gram-Schmidt.
+#pragma once
+#include "wtb_internal.h"
+
+namespace wtb {
+
+template <class S>
+__device__ __forceinline__ S warp_allsum(S v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <class S>
+__device__ __forceinline__ S fast_div(S a, S b) {
+  return a / b;
+}
+template <>
+__device__ __forceinline__ float fast_div<float>(float a, float b) {
+  return __fdividef(a, b);
+}
+
+// Step 1.  A: n x n Hermitian (both triangles), row-major with leading dimension lda, in shared memory; it is
+// overwritten: column j below the diagonal holds v_j.  d[n], e[n-1] receive T; tau[n-1] the reflector scalars;
+// p[n] is scratch.  All threads of the block call it.
+template <class S>
+__device__ void tridiag_cta(cplx<S>* A, int lda, int n, S* d, S* e, cplx<S>* tau, cplx<S>* p, int* flag) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  for (int j = 0; j < n - 1; ++j) {
+    const int L = n - 1 - j;
+    cplx<S>* vcol = A + (size_t)(j + 1) * lda + j;  // v_j[i] = vcol[i * lda]
+    if (warp == 0) {
+      S sig = 0;
+      for (int i = 1 + lane; i < L; i += 32) {
+        const cplx<S> x = vcol[(size_t)i * lda];
+        sig += x.re * x.re + x.im * x.im;
+      }
+      sig = warp_allsum(sig);
+      const cplx<S> alpha = vcol[0];
+      bool skip = false;
+      S beta;
+      cplx<S> t = mk<S>(0, 0), sc = mk<S>(0, 0);
+      if (sig == (S)0 && alpha.im == (S)0) {
+        skip = true;
+        beta = alpha.re;
+      } else {
+        const S an = sqrt(alpha.re * alpha.re + alpha.im * alpha.im + sig);
+        beta = alpha.re >= (S)0 ? -an : an;
+        t = mk<S>((beta - alpha.re) / beta, -alpha.im / beta);
+        const S dr = alpha.re - beta, di = alpha.im, dd = dr * dr + di * di;
+        sc = mk<S>(dr / dd, -di / dd);  // 1 / (alpha - beta)
+      }
+      if (!skip)
+        for (int i = 1 + lane; i < L; i += 32) vcol[(size_t)i * lda] = cmul(vcol[(size_t)i * lda], sc);
+      if (lane == 0) {
+        vcol[0] = mk<S>(1, 0);
+        e[j] = beta;
+        tau[j] = t;
+        d[j] = A[(size_t)j * lda + j].re;
+        flag[0] = skip ? 1 : 0;
+      }
+    }
+    __syncthreads();
+    const bool skip = flag[0] != 0;
+    if (skip) {
+      __syncthreads();  // every thread has read the flag before warp 0 rewrites it
+      continue;
+    }
+    const cplx<S> tj = tau[j];
+    // p = tau A22 v (A22 = rows/columns j+1..n-1), one warp per row
+    for (int r = warp; r < L; r += nw) {
+      const cplx<S>* row = A + (size_t)(j + 1 + r) * lda + (j + 1);
+      cplx<S> acc = mk<S>(0, 0);
+      for (int c = lane; c < L; c += 32) cfma(acc, row[c], vcol[(size_t)c * lda]);
+      acc.re = warp_allsum(acc.re);
+      acc.im = warp_allsum(acc.im);
+      if (lane == 0) p[r] = cmul(tj, acc);
+    }
+    __syncthreads();
+    // K = -1/2 tau (p^H v), every warp for itself; w = p + K v;  A22 -= v w^H + w v^H
+    cplx<S> sdot = mk<S>(0, 0);
+    for (int c = lane; c < L; c += 32) cfmac(sdot, p[c], vcol[(size_t)c * lda]);
+    sdot.re = warp_allsum(sdot.re);
+    sdot.im = warp_allsum(sdot.im);
+    const cplx<S> K = cmul(mk<S>((S)-0.5 * tj.re, (S)-0.5 * tj.im), sdot);
+    for (int q = tid; q < L * L; q += nt) {
+      const int r = q / L, c = q - r * L;
+      const cplx<S> vr = vcol[(size_t)r * lda], vc = vcol[(size_t)c * lda];
+      const cplx<S> wr = mk<S>(p[r].re + K.re * vr.re - K.im * vr.im, p[r].im + K.re * vr.im + K.im * vr.re);
+      const cplx<S> wc = mk<S>(p[c].re + K.re * vc.re - K.im * vc.im, p[c].im + K.re * vc.im + K.im * vc.re);
+      // v_r conj(w_c) + w_r conj(v_c)
+      const S re = vr.re * wc.re + vr.im * wc.im + wr.re * vc.re + wr.im * vc.im;
+      const S im = vr.im * wc.re - vr.re * wc.im + wr.im * vc.re - wr.re * vc.im;
+      cplx<S>& a = A[(size_t)(j + 1 + r) * lda + (j + 1 + c)];
+      a.re -= re;
+      a.im -= im;
+    }
+    __syncthreads();
+  }
+  if (tid == 0) d[n - 1] = A[(size_t)(n - 1) * lda + (n - 1)].re;
+  __syncthreads();
+}
+
+// Number of eigenvalues of T below x (Sturm count of T - x I, pivots safeguarded by pivmin).
+template <class S>
+__device__ __forceinline__ int sturm_count(const S* d, const S* e2, int n, S x, S pivmin) {
+  S q = d[0] - x;
+  if (fabs(q) < pivmin) q = -pivmin;
+  int c = q < (S)0;
+  for (int i = 1; i < n; ++i) {
+    q = (d[i] - x) - fast_div<S>(e2[i - 1], q);
+    if (fabs(q) < pivmin) q = -pivmin;
+    c += q < (S)0;
+  }
+  return c;
+}
+
+// Steps 2-4 after tridiag_cta.  Computes the nwant lowest eigenpairs: lam[k] ascending, U[i * ldu + k] the
+// eigenvectors of A (complex, in shared memory).  Scratch (shared): e2[n], Z[n * nwant], Dv[n * nwant],
+// Lv[n * nwant] (Lv directly after Dv: U may alias Dv with ldu = nwant, both being dead by step 4),
+// cl[nwant] (ints), red[4].
+template <class S>
+__device__ void tridiag_eigvecs_cta(const cplx<S>* A, int lda, int n, int nwant, const S* d, const S* e,
+                                    const cplx<S>* tau, S* e2, S* lam, S* Z, S* Dv, S* Lv, int* cl, cplx<S>* U,
+                                    int ldu, S* red) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  const S eps = sizeof(S) == 4 ? (S)5.96e-8 : (S)1.11e-16;
+  for (int i = tid; i < n - 1; i += nt) e2[i] = e[i] * e[i];
+  // Gershgorin interval and the scale of T (one warp)
+  if (warp == 0) {
+    S lo = d[0], hi = d[0], emax2 = 0;
+    for (int i = lane; i < n; i += 32) {
+      const S r = (i > 0 ? fabs(e[i - 1]) : (S)0) + (i < n - 1 ? fabs(e[i]) : (S)0);
+      lo = fmin(lo, d[i] - r);
+      hi = fmax(hi, d[i] + r);
+      if (i < n - 1) emax2 = fmax(emax2, e[i] * e[i]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+      hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+      emax2 = fmax(emax2, __shfl_xor_sync(0xffffffffu, emax2, o));
+    }
+    if (lane == 0) {
+      const S tn = fmax(fabs(lo), fabs(hi));
+      const S tiny = sizeof(S) == 4 ? (S)1e-30 : (S)1e-290;
+      const S pivmin = fmax(emax2, (S)1) * tiny;
+      red[0] = lo - (S)2 * eps * tn - pivmin;
+      red[1] = hi + (S)2 * eps * tn + pivmin;
+      red[2] = fmax(tn, tiny);
+      red[3] = pivmin;
+    }
+  }
+  __syncthreads();
+  const S tnorm = red[2], pivmin = red[3];
+  // step 2: bisection
+  for (int k = tid; k < nwant; k += nt) {
+    S a = red[0], b = red[1];
+    for (int it = 0; it < 256; ++it) {
+      const S mid = (S)0.5 * (a + b);
+      if (b - a <= (S)2 * eps * fmax(fabs(a), fabs(b)) + pivmin || mid <= a || mid >= b) break;
+      if (sturm_count<S>(d, e2, n, mid, pivmin) > k)
+        b = mid;
+      else
+        a = mid;
+    }
+    lam[k] = (S)0.5 * (a + b);
+  }
+  __syncthreads();
+  // step 3: inverse iteration, one thread per eigenvector; column k of Z, Dv, Lv (stride nwant)
+  const S tiny = eps * tnorm;
+  for (int k = tid; k < nwant; k += nt) {
+    const S lk = lam[k];
+    S Dp = d[0] - lk;
+    if (fabs(Dp) < tiny) Dp = tiny;
+    Dv[k] = Dp;
+    for (int i = 1; i < n; ++i) {
+      const S l = e[i - 1] / Dp;
+      Lv[(size_t)(i - 1) * nwant + k] = l;
+      Dp = (d[i] - lk) - l * e[i - 1];
+      if (fabs(Dp) < tiny) Dp = tiny;
+      Dv[(size_t)i * nwant + k] = Dp;
+    }
+    // start: deterministic pseudo-random entries in [-1, 1) (distinct for every k)
+    for (int i = 0; i < n; ++i) {
+      unsigned h = (unsigned)(i + 1) * 2654435761u ^ (unsigned)(k + 7) * 2246822519u;
+      h ^= h >> 15;
+      h *= 0x2c1b3c6du;
+      h ^= h >> 12;
+      Z[(size_t)i * nwant + k] = (S)((double)(h & 0xffffffu) / 8388608.0 - 1.0);
+    }
+    for (int pass = 0; pass < 3; ++pass) {
+      // L y = b (in place), y /= D, L^T x = y (in place)
+      S y = Z[k];
+      for (int i = 1; i < n; ++i) {
+        const S v = Z[(size_t)i * nwant + k] - Lv[(size_t)(i - 1) * nwant + k] * y;
+        Z[(size_t)i * nwant + k] = v;
+        y = v;
+      }
+      for (int i = 0; i < n; ++i) Z[(size_t)i * nwant + k] /= Dv[(size_t)i * nwant + k];
+      S x = Z[(size_t)(n - 1) * nwant + k];
+      for (int i = n - 2; i >= 0; --i) {
+        const S v = Z[(size_t)i * nwant + k] - Lv[(size_t)i * nwant + k] * x;
+        Z[(size_t)i * nwant + k] = v;
+        x = v;
+      }
+      S nrm = 0, mx = 0;
+      for (int i = 0; i < n; ++i) mx = fmax(mx, fabs(Z[(size_t)i * nwant + k]));
+      if (!(mx > (S)0)) mx = (S)1;
+      for (int i = 0; i < n; ++i) {
+        const S v = Z[(size_t)i * nwant + k] / mx;
+        nrm += v * v;
+      }
+      const S sc = (S)1 / (mx * sqrt(nrm));
+      for (int i = 0; i < n; ++i) Z[(size_t)i * nwant + k] *= sc;
+    }
+    // cluster start: the first index of the run of eigenvalues closer than 1e-3 ||T|| to their neighbour
+    int s0 = k;
+    while (s0 > 0 && lam[s0] - lam[s0 - 1] <= (S)1e-3 * tnorm) --s0;
+    cl[k] = s0;
+  }
+  __syncthreads();
+  // modified Gram-Schmidt inside each cluster, one warp per cluster (clusters are contiguous runs)
+  for (int k0 = warp; k0 < nwant; k0 += nw) {
+    if (cl[k0] != k0) continue;  // not a cluster start
+    int k1 = k0 + 1;
+    while (k1 < nwant && cl[k1] == k0) ++k1;
+    for (int jv = k0 + 1; jv < k1; ++jv) {
+      for (int iv = k0; iv < jv; ++iv) {
+        S dot = 0;
+        for (int i = lane; i < n; i += 32) dot += Z[(size_t)i * nwant + iv] * Z[(size_t)i * nwant + jv];
+        dot = warp_allsum(dot);
+        for (int i = lane; i < n; i += 32) Z[(size_t)i * nwant + jv] -= dot * Z[(size_t)i * nwant + iv];
+        __syncwarp();
+      }
+      S nrm = 0;
+      for (int i = lane; i < n; i += 32) nrm += Z[(size_t)i * nwant + jv] * Z[(size_t)i * nwant + jv];
+      nrm = warp_allsum(nrm);
+      const S sc = nrm > (S)0 ? (S)1 / sqrt(nrm) : (S)0;
+      for (int i = lane; i < n; i += 32) Z[(size_t)i * nwant + jv] *= sc;
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  // step 4: u_k = H_0 (H_1 (... H_{n-2} z_k)), one warp per eigenvector
+  for (int k = warp; k < nwant; k += nw) {
+    for (int i = lane; i < n; i += 32) U[(size_t)i * ldu + k] = mk<S>(Z[(size_t)i * nwant + k], 0);
+    __syncwarp();
+    for (int j = n - 2; j >= 0; --j) {
+      const cplx<S> tj = tau[j];
+      if (tj.re == (S)0 && tj.im == (S)0) continue;
+      const cplx<S>* vcol = A + (size_t)(j + 1) * lda + j;
+      const int L = n - 1 - j;
+      cplx<S> dot = mk<S>(0, 0);
+      for (int i = lane; i < L; i += 32) cfmac(dot, vcol[(size_t)i * lda], U[(size_t)(j + 1 + i) * ldu + k]);
+      dot.re = warp_allsum(dot.re);
+      dot.im = warp_allsum(dot.im);
+      const cplx<S> f = cmul(tj, dot);
+      for (int i = lane; i < L; i += 32) {
+        const cplx<S> v = vcol[(size_t)i * lda];
+        cplx<S>& u = U[(size_t)(j + 1 + i) * ldu + k];
+        u.re -= f.re * v.re - f.im * v.im;
+        u.im -= f.re * v.im + f.im * v.re;
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+}
+
+}  // namespace wtb

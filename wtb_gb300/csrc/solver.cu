@@ -3,8 +3,10 @@
 // LOBPCG (Knyazev's locally optimal block preconditioned CG) with
 //   - the diagonal (transition-energy) preconditioner |diag(H) - theta|^-1, floored;
 //   - soft locking: converged columns keep their place in X but get no new search direction;
-//   - SVQB orthonormalisation of the basis [X W P] (eigen-decomposition of its scaled Gram matrix,
-//     directions with eigenvalue below tau * max dropped) followed by Rayleigh-Ritz;
+//   - orthonormalisation of the basis [X W P] by pivoted Cholesky of its scaled Gram matrix (directions
+//     whose residual norm falls below tau are dropped) followed by Rayleigh-Ritz on the kept directions,
+//     whose small eigenproblem is solved by Householder tridiagonalisation, bisection and inverse
+//     iteration on one CTA (small_eig.cuh);
 //   - all projected (3m x 3m) matrices kept in complex(8) on the device.
 // The iteration vectors are in precision S.  In every mode the last step is an FP64 Rayleigh-Ritz on
 // the final block with a freshly applied operator: FP64 Gram matrices, FP64 eigen-decomposition, FP64
@@ -144,14 +146,6 @@ template struct MatFreeOperator<double>;
 
 namespace {
 
-template <class S>
-cudaError_t jacobi_for(zd* A, int lda, int n, double* ev, zd* U, int ldu, DevStatus* st, cudaStream_t s) {
-  if constexpr (sizeof(S) == 4)
-    return launch_jacobi_eig_f32(A, lda, n, ev, U, ldu, 60, st, s);
-  else
-    return launch_jacobi_eig(A, lda, n, ev, U, ldu, 60, st, s);
-}
-
 struct Small {
   zd *M, *G, *B, *Gp, *U, *Y, *C, *T;
   double *lam, *theta, *dinv;
@@ -159,26 +153,27 @@ struct Small {
 };
 
 // Rayleigh-Ritz on the basis Sb (dim x nb, ld) with ASb = H Sb: returns C (nb x m) and theta (m).
+// Orthonormalisation: pivoted Cholesky of the scaled Gram matrix (directions whose residual diagonal falls
+// below tau are dropped; the r kept ones come first in B); the projected r x r problem B^H G B is solved
+// by the tridiagonal route (small_eig.cuh).  The small problems run in precision S, or FP64 for
+// small_in_fp64.  A missing Ritz pair (r < m) has theta = 1e30 and a zero column in C.
 template <class S>
 int rayleigh_ritz(const cplx<S>* Sb, const cplx<S>* ASb, int ld, int nb, int m, int dim, double tau, Small& sm,
                   double* partial, int npart, DevStatus* st, cudaStream_t s, std::string* msg,
                   bool small_in_fp64) {
+  (void)st;
   CK(launch_gram<S>(Sb, ld, nb, Sb, ld, nb, dim, sm.M, partial, npart, s));
   CK(launch_gram<S>(Sb, ld, nb, ASb, ld, nb, dim, sm.G, partial, npart, s));
-  CK(launch_svqb_scale(sm.M, nb, nb, sm.dinv, s));
-  CK(launch_scale_sym(sm.M, nb, nb, sm.dinv, s));
   if (small_in_fp64)
-    CK(launch_jacobi_eig(sm.M, nb, nb, sm.lam, sm.U, nb, 60, st, s));
+    CK(launch_pchol_basis<double>(sm.M, nb, nb, tau, sm.B, nb, sm.keep, s));
   else
-    CK(jacobi_for<S>(sm.M, nb, nb, sm.lam, sm.U, nb, st, s));
-  CK(launch_svqb_basis(sm.dinv, sm.U, nb, sm.lam, nb, tau, sm.B, nb, sm.keep, s));
+    CK(launch_pchol_basis<S>(sm.M, nb, nb, tau, sm.B, nb, sm.keep, s));
   CK(launch_small_gemm(sm.G, nb, 0, sm.B, nb, sm.T, nb, nb, nb, nb, s));
   CK(launch_small_gemm(sm.B, nb, 1, sm.T, nb, sm.Gp, nb, nb, nb, nb, s));
-  CK(launch_mark_dropped(sm.Gp, nb, nb, sm.keep, s));
   if (small_in_fp64)
-    CK(launch_jacobi_eig(sm.Gp, nb, nb, sm.theta, sm.Y, nb, 60, st, s));
+    CK(launch_heev_small<double>(sm.Gp, nb, sm.keep, nb, m, sm.theta, sm.Y, nb, s));
   else
-    CK(jacobi_for<S>(sm.Gp, nb, nb, sm.theta, sm.Y, nb, st, s));
+    CK(launch_heev_small<S>(sm.Gp, nb, sm.keep, nb, m, sm.theta, sm.Y, nb, s));
   CK(launch_small_gemm(sm.B, nb, 0, sm.Y, nb, sm.C, m, nb, m, nb, s));
   return WTB_OK;
 }
@@ -306,10 +301,9 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
       if (monitor) {
         int first = 0;
         while (first < nev - 1 && h_active[first] == 0) ++first;
-        std::fprintf(stderr, "WTB-EPS %5d EPS pair=%4d value (error) %15.8E (%10.3E) max %10.3E  small %d/%d\n", it,
-                     nconv + 1, h_theta[first],
-                     std::sqrt(std::max(h_norm[first], 0.0)) / std::max(std::fabs(h_theta[first]), 1e-12), maxrel,
-                     hst.small_sweeps, hst.small_calls);
+        std::fprintf(stderr, "WTB-EPS %5d EPS pair=%4d value (error) %15.8E (%10.3E) max %10.3E\n", it, nconv + 1,
+                     h_theta[first], std::sqrt(std::max(h_norm[first], 0.0)) / std::max(std::fabs(h_theta[first]), 1e-12),
+                     maxrel);
       }
       // restart from X alone: fresh AX, no search directions, Rayleigh-Ritz on X
       auto restart_from_x = [&]() -> int {

@@ -163,9 +163,11 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
                  std::string* msg, double tol_refine = 0.0);
 
 // extra launchers used by the solver
-cudaError_t launch_jacobi_eig_f32(zd* A, int lda, int n, double* evals, zd* evecs, int ldv, int sweeps,
-                                  DevStatus* st, cudaStream_t s);
-cudaError_t launch_mark_dropped(zd* G, int ldg, int n, const int* keep, cudaStream_t s);
+template <class S>
+cudaError_t launch_heev_small(const zd* A, int lda, const int* nptr, int nmax, int nwant, double* evals, zd* evecs,
+                              int ldv, cudaStream_t s);
+template <class S>
+cudaError_t launch_pchol_basis(const zd* M, int ldm, int n, double drop, zd* B, int ldb, int* r_out, cudaStream_t s);
 cudaError_t launch_select_lowest(const double* diag, int dim, int m, int* idx, double* cand_val, cudaStream_t s);
 template <class S>
 cudaError_t launch_init_guess(cplx<S>* X, int ldx, int dim, int m, const int* idx, unsigned seed, cudaStream_t s);

@@ -72,8 +72,7 @@ typedef cplx<float> zf;
 struct DevStatus {
   int code;
   int info;
-  int small_sweeps;  // Jacobi sweeps of the projected eigenproblems since the last reset (instrumentation)
-  int small_calls;   // and their number
+  int pad[2];
 };
 
 __device__ __forceinline__ void dev_fail(DevStatus* st, int code, int info) {
@@ -138,14 +137,8 @@ cudaError_t launch_copy_cols(const cplx<S>* A, int lda, cplx<S>* B, int ldb, int
 template <class Sa, class Sb>
 cudaError_t launch_convert_cols(const cplx<Sa>* A, int lda, cplx<Sb>* B, int ldb, int ncol, int nrow,
                                 cudaStream_t s);
-cudaError_t launch_jacobi_eig(zd* A, int lda, int n, double* evals, zd* evecs, int ldv, int sweeps,
-                              DevStatus* st, cudaStream_t s);
 cudaError_t launch_small_gemm(const zd* A, int lda, int transA, const zd* B, int ldb, zd* C, int ldc, int m, int n,
                               int k, cudaStream_t s);
-cudaError_t launch_svqb_scale(const zd* M, int ldm, int n, double* dinv, cudaStream_t s);
-cudaError_t launch_svqb_basis(const double* dinv, const zd* U, int ldu, const double* lam, int n, double tau,
-                              zd* B, int ldb, int* keep, cudaStream_t s);
-cudaError_t launch_scale_sym(zd* M, int ldm, int n, const double* dinv, cudaStream_t s);
 
 // ----------------------------------------------------------------------------- matrix-free operator
 // Z[n][k'] with n = ((b*w + o)*w + p)*2 + ri (K-major for the V*Z contraction).
