@@ -104,76 +104,79 @@ __global__ void __launch_bounds__(256) mf_gather_kernel(const cplx<S>* __restric
   }
 }
 
-// bf16-slice variant: the Z tile of this CTA is staged in shared memory and each slice is written as
-// 16-byte vectors of 8 consecutive k' (the K-major rows of zt are 128-byte aligned, kt0 is a multiple of
-// 32).  Columns k' >= nk inside the tile are zero (x is zero there).
-__global__ void __launch_bounds__(256) mf_gather_bf16_kernel(const zf* __restrict__ X, int ldx, int c0,
+// bf16-slice variant: one CTA per tile of 8 consecutive k' and all nb block columns.  The X rows of the tile
+// (nb contiguous columns each) and the tile's band vectors are read once; Y1 = Vb x is staged in shared
+// memory; each thread then forms Z[k'][o][p][b] for its (b, o, p) items over the 8 k' of the tile and writes
+// the re and im rows of every slice as one 16-byte vector of 8 bf16 (the K-major rows of zt are 16-byte
+// aligned: ldk and the tile start are multiples of 8).  k' >= nk inside the last tile give zeros (x = 0).
+constexpr int kGatherKT = 8;
+__global__ void __launch_bounds__(256) mf_gather_bf16_kernel(const zf* __restrict__ X, int ldx, int c0, int nbc,
                                                              const zd* __restrict__ vec_win, int nk, int nv, int nc,
                                                              int w, uint16_t* __restrict__ zt, int ldk, int nslices,
                                                              long slice_stride) {
-  constexpr int KT = 32;
+  constexpr int KT = kGatherKT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int nb = nv + nc, ncv = nc * nv;
+  const int nbnd = nv + nc, ncv = nc * nv, ww = w * w;
   const int kt0 = blockIdx.x * KT;
-  const int b = blockIdx.y;
   const int tkn = min(KT, nk - kt0);
   zf* Cs = reinterpret_cast<zf*>(smem_raw);  // [KT][nc][w]
   zf* Vs = Cs + KT * nc * w;                 // [KT][nv][w]
-  zf* xs = Vs + KT * nv * w;                 // [KT][ncv]
-  zf* Y1 = xs + KT * ncv;                    // [KT][nc][w]
-  float* Zs = reinterpret_cast<float*>(Y1 + KT * nc * w);  // [2 w^2][KT + 1]
+  zf* xs = Vs + KT * nv * w;                 // [KT][ncv][nbc]
+  zf* Y1 = xs + KT * ncv * nbc;              // [KT][nc][w][nbc]
   const int tid = threadIdx.x, nt = blockDim.x;
-  for (int e = tid; e < KT * nb * w; e += nt) {
-    const int kk = e / (nb * w), sb = (e / w) % nb, o = e % w;
+  for (int e = tid; e < KT * nbnd * w; e += nt) {
+    const int kk = e / (nbnd * w), sb = (e / w) % nbnd, o = e % w;
     zd a = mk<double>(0.0, 0.0);
-    if (kk < tkn) a = vec_win[((size_t)(kt0 + kk) * nb + sb) * w + o];
+    if (kk < tkn) a = vec_win[((size_t)(kt0 + kk) * nbnd + sb) * w + o];
     const zf as = mk<float>((float)a.re, (float)a.im);
     if (sb < nv)
       Vs[(kk * nv + sb) * w + o] = as;
     else
       Cs[(kk * nc + sb - nv) * w + o] = as;
   }
-  for (int e = tid; e < KT * ncv; e += nt) {
-    const int kk = e / ncv, cv = e % ncv;
-    xs[e] = kk < tkn ? X[((size_t)(kt0 + kk) * ncv + cv) * ldx + c0 + b] : mk<float>(0.f, 0.f);
+  for (int e = tid; e < KT * ncv * nbc; e += nt) {
+    const int b = e % nbc, r = e / nbc;  // r = kk * ncv + cv
+    const int kk = r / ncv;
+    xs[e] = kk < tkn ? X[((size_t)kt0 * ncv + r) * ldx + c0 + b] : mk<float>(0.f, 0.f);
   }
   __syncthreads();
-  for (int e = tid; e < KT * nc * w; e += nt) {
-    const int kk = e / (nc * w), c = (e / w) % nc, p = e % w;
+  // Y1[kk][c][p][b] = sum_v Vb[kk][v][p] x[kk][c][v][b]
+  for (int e = tid; e < KT * nc * w * nbc; e += nt) {
+    const int b = e % nbc, p = (e / nbc) % w, c = (e / (nbc * w)) % nc, kk = e / (nbc * w * nc);
     zf acc = mk<float>(0.f, 0.f);
-    for (int v = 0; v < nv; ++v) cfma(acc, Vs[(kk * nv + v) * w + p], xs[kk * ncv + c * nv + v]);
+    for (int v = 0; v < nv; ++v) cfma(acc, Vs[(kk * nv + v) * w + p], xs[(kk * ncv + c * nv + v) * nbc + b]);
     Y1[e] = acc;
   }
   __syncthreads();
-  const int ww = w * w;
-  for (int e = tid; e < KT * ww; e += nt) {
-    const int kk = e % KT, op = e / KT;
-    const int o = op / w, p = op % w;
-    zf acc = mk<float>(0.f, 0.f);
-    for (int c = 0; c < nc; ++c) cfma(acc, Cs[(kk * nc + c) * w + o], Y1[(kk * nc + c) * w + p]);
-    Zs[(2 * op) * (KT + 1) + kk] = acc.re;
-    Zs[(2 * op + 1) * (KT + 1) + kk] = acc.im;
-  }
-  __syncthreads();
-  // 2 w^2 rows x 4 chunks of 8 k' each; a chunk becomes one 16-byte store per slice
-  const long nbase = (long)b * ww * 2;
-  for (int e = tid; e < 2 * ww * (KT / 8); e += nt) {
-    const int row = e / (KT / 8), ch = e % (KT / 8);
-    float r[8];
+  // items (b, o, p): Z over the tile's 8 k', re and im rows, every slice
+  for (int it = tid; it < nbc * ww; it += nt) {
+    const int b = it / ww, op = it % ww, o = op / w, p = op % w;
+    float zr[KT], zi[KT];
 #pragma unroll
-    for (int q = 0; q < 8; ++q) r[q] = Zs[row * (KT + 1) + ch * 8 + q];
-    const long off = (nbase + row) * ldk + kt0 + ch * 8;
+    for (int kk = 0; kk < KT; ++kk) {
+      zf acc = mk<float>(0.f, 0.f);
+      for (int c = 0; c < nc; ++c)
+        cfma(acc, Cs[(kk * nc + c) * w + o], Y1[((kk * nc + c) * w + p) * nbc + b]);
+      zr[kk] = acc.re;
+      zi[kk] = acc.im;
+    }
+    const long row = ((long)(b * w + o) * w + p) * 2;
+    const long off_re = row * ldk + kt0, off_im = off_re + ldk;
     for (int sl = 0; sl < nslices; ++sl) {
-      uint32_t packed[4];
+      uint32_t pr[4], pi[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        const __nv_bfloat16 h0 = __float2bfloat16_rn(r[2 * q]);
-        const __nv_bfloat16 h1 = __float2bfloat16_rn(r[2 * q + 1]);
-        r[2 * q] -= __bfloat162float(h0);
-        r[2 * q + 1] -= __bfloat162float(h1);
-        packed[q] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+        const __nv_bfloat16 r0 = __float2bfloat16_rn(zr[2 * q]), r1 = __float2bfloat16_rn(zr[2 * q + 1]);
+        const __nv_bfloat16 i0 = __float2bfloat16_rn(zi[2 * q]), i1 = __float2bfloat16_rn(zi[2 * q + 1]);
+        zr[2 * q] -= __bfloat162float(r0);
+        zr[2 * q + 1] -= __bfloat162float(r1);
+        zi[2 * q] -= __bfloat162float(i0);
+        zi[2 * q + 1] -= __bfloat162float(i1);
+        pr[q] = (uint32_t)__bfloat16_as_ushort(r0) | ((uint32_t)__bfloat16_as_ushort(r1) << 16);
+        pi[q] = (uint32_t)__bfloat16_as_ushort(i0) | ((uint32_t)__bfloat16_as_ushort(i1) << 16);
       }
-      *reinterpret_cast<uint4*>(zt + sl * slice_stride + off) = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+      *reinterpret_cast<uint4*>(zt + sl * slice_stride + off_re) = make_uint4(pr[0], pr[1], pr[2], pr[3]);
+      *reinterpret_cast<uint4*>(zt + sl * slice_stride + off_im) = make_uint4(pi[0], pi[1], pi[2], pi[3]);
     }
   }
 }
@@ -315,14 +318,15 @@ template <class S, class Z>
 cudaError_t launch_mf_gather(const cplx<S>* X, int ldx, int c0, int nb, const zd* vec_win, int nk, int nv, int nc,
                              int w, Z* zt, int ldk, int nslices, long slice_stride, cudaStream_t s) {
   if constexpr (sizeof(S) == 4 && sizeof(Z) == 2) {
-    const size_t smem = (size_t)(2 * 32 * nc * w + 32 * nv * w + 32 * nc * nv) * sizeof(zf) +
-                        (size_t)2 * w * w * 33 * sizeof(float);
-    if (smem <= 200 * 1024 && ldk % 32 == 0) {
-      cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(mf_gather_bf16_kernel), (size_t)smem);
+    const int KT = kGatherKT;
+    const size_t smem = (size_t)(KT * nc * w + KT * nv * w + KT * nc * nv * nb + KT * nc * w * nb) * sizeof(zf);
+    if (smem <= 200 * 1024 && ldk % KT == 0 && slice_stride % 8 == 0) {
+      cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(mf_gather_bf16_kernel), smem);
       if (e != cudaSuccess) return e;
-      dim3 grid((nk + 31) / 32, nb);
-      mf_gather_bf16_kernel<<<grid, 256, smem, s>>>(reinterpret_cast<const zf*>(X), ldx, c0, vec_win, nk, nv, nc, w,
-                                                    reinterpret_cast<uint16_t*>(zt), ldk, nslices, slice_stride);
+      mf_gather_bf16_kernel<<<(nk + KT - 1) / KT, 256, smem, s>>>(reinterpret_cast<const zf*>(X), ldx, c0, nb,
+                                                                   vec_win, nk, nv, nc, w,
+                                                                   reinterpret_cast<uint16_t*>(zt), ldk, nslices,
+                                                                   slice_stride);
       ++g_launch_count;
       return cudaGetLastError();
     }

@@ -14,6 +14,9 @@
 // An unreduced tridiagonal matrix has distinct eigenvalues; (near-)degenerate ones come from (near-)zero
 // off-diagonal entries, for which independent inverse iterations from different starts give independent
 // vectors of the eigenspace, made orthonormal by step 3's Gram-Schmidt.
+// In FP64 the bisection runs in FP32 and only supplies shifts: the FP64 eigenvalues are Rayleigh quotients
+// of the FP64 inverse-iteration vectors, and inside a cluster the Rayleigh-Ritz values of T on the cluster's
+// vectors (an FP64 instruction costs a warp far more than an FP32 one on this GPU).
 #pragma once
 #include "wtb_internal.h"
 
@@ -24,6 +27,11 @@ __device__ __forceinline__ S warp_allsum(S v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
+}
+
+template <class S>
+__device__ __forceinline__ S tiny_of() {
+  return sizeof(S) == 4 ? (S)1e-30 : (S)1e-290;
 }
 
 template <class S>
@@ -168,22 +176,57 @@ __device__ void tridiag_eigvecs_cta(const cplx<S>* A, int lda, int n, int nwant,
   }
   __syncthreads();
   const S tnorm = red[2], pivmin = red[3];
-  // step 2: bisection
-  for (int k = tid; k < nwant; k += nt) {
-    S a = red[0], b = red[1];
-    for (int it = 0; it < 256; ++it) {
-      const S mid = (S)0.5 * (a + b);
-      if (b - a <= (S)2 * eps * fmax(fabs(a), fabs(b)) + pivmin || mid <= a || mid >= b) break;
-      if (sturm_count<S>(d, e2, n, mid, pivmin) > k)
-        b = mid;
-      else
-        a = mid;
+  // step 2: bisection.  In FP64 it runs in FP32 on the rounded T (an FP64 instruction costs a warp dozens of
+  // FP32 ones on this part); the FP32 eigenvalue is then only the shift of the FP64 inverse iteration, and
+  // the FP64 eigenvalue is the Rayleigh quotient of the FP64 vector (step 3).
+  if constexpr (sizeof(S) == 8) {
+    float* df = reinterpret_cast<float*>(Z);  // Z is free until step 3
+    float* e2f = df + n;
+    for (int i = tid; i < n; i += nt) {
+      df[i] = (float)d[i];
+      if (i < n - 1) e2f[i] = (float)e2[i];
     }
-    lam[k] = (S)0.5 * (a + b);
+    __syncthreads();
+    const float epsf = 5.96e-8f;
+    const float pivf = fmaxf((float)(pivmin / tiny_of<S>() * 1e-30), 1e-30f);
+    for (int k = tid; k < nwant; k += nt) {
+      float a = (float)red[0], b = (float)red[1];
+      const float w0 = b - a;
+      a -= 4.f * epsf * fabsf(w0) + pivf;
+      b += 4.f * epsf * fabsf(w0) + pivf;
+      for (int it = 0; it < 128; ++it) {
+        const float mid = 0.5f * (a + b);
+        if (b - a <= 2.f * epsf * fmaxf(fabsf(a), fabsf(b)) + pivf || mid <= a || mid >= b) break;
+        if (sturm_count<float>(df, e2f, n, mid, pivf) > k)
+          b = mid;
+        else
+          a = mid;
+      }
+      lam[k] = (S)(0.5f * (a + b));
+    }
+  } else {
+    for (int k = tid; k < nwant; k += nt) {
+      S a = red[0], b = red[1];
+      for (int it = 0; it < 256; ++it) {
+        const S mid = (S)0.5 * (a + b);
+        if (b - a <= (S)2 * eps * fmax(fabs(a), fabs(b)) + pivmin || mid <= a || mid >= b) break;
+        if (sturm_count<S>(d, e2, n, mid, pivmin) > k)
+          b = mid;
+        else
+          a = mid;
+      }
+      lam[k] = (S)0.5 * (a + b);
+    }
   }
   __syncthreads();
   // step 3: inverse iteration, one thread per eigenvector; column k of Z, Dv, Lv (stride nwant)
   const S tiny = eps * tnorm;
+  // clusters from the (shift) eigenvalues: runs closer than 1e-3 ||T|| to their neighbour
+  for (int k = tid; k < nwant; k += nt) {
+    int s0 = k;
+    while (s0 > 0 && lam[s0] - lam[s0 - 1] <= (S)1e-3 * tnorm) --s0;
+    cl[k] = s0;
+  }
   for (int k = tid; k < nwant; k += nt) {
     const S lk = lam[k];
     S Dp = d[0] - lk;
@@ -229,10 +272,6 @@ __device__ void tridiag_eigvecs_cta(const cplx<S>* A, int lda, int n, int nwant,
       const S sc = (S)1 / (mx * sqrt(nrm));
       for (int i = 0; i < n; ++i) Z[(size_t)i * nwant + k] *= sc;
     }
-    // cluster start: the first index of the run of eigenvalues closer than 1e-3 ||T|| to their neighbour
-    int s0 = k;
-    while (s0 > 0 && lam[s0] - lam[s0 - 1] <= (S)1e-3 * tnorm) --s0;
-    cl[k] = s0;
   }
   __syncthreads();
   // modified Gram-Schmidt inside each cluster, one warp per cluster (clusters are contiguous runs)
@@ -257,6 +296,107 @@ __device__ void tridiag_eigvecs_cta(const cplx<S>* A, int lda, int n, int nwant,
     }
   }
   __syncthreads();
+  if constexpr (sizeof(S) == 8) {
+    // FP64 eigenvalues: Rayleigh quotients z^T T z; inside a cluster the Rayleigh-Ritz of T on the cluster's
+    // vectors (one warp per cluster; the small symmetric problem by cyclic Jacobi on lane 0; its matrices
+    // use the dead L D L^T storage at offset k0 n, which clusters starting at different k0 cannot overlap)
+    for (int k0 = warp; k0 < nwant; k0 += nw) {
+      if (cl[k0] != k0) continue;
+      int k1 = k0 + 1;
+      while (k1 < nwant && cl[k1] == k0) ++k1;
+      const int kc = k1 - k0;
+      S* Tc = Dv + (size_t)k0 * n;
+      S* Yc = Lv + (size_t)k0 * n;
+      for (int a = 0; a < kc; ++a)
+        for (int b = a; b < kc; ++b) {
+          S acc = 0;
+          for (int i = lane; i < n; i += 32) {
+            S tz = d[i] * Z[(size_t)i * nwant + k0 + b];
+            if (i > 0) tz += e[i - 1] * Z[(size_t)(i - 1) * nwant + k0 + b];
+            if (i < n - 1) tz += e[i] * Z[(size_t)(i + 1) * nwant + k0 + b];
+            acc += Z[(size_t)i * nwant + k0 + a] * tz;
+          }
+          acc = warp_allsum(acc);
+          if (lane == 0) {
+            Tc[a * kc + b] = acc;
+            Tc[b * kc + a] = acc;
+          }
+        }
+      __syncwarp();
+      if (kc == 1 || kc > 32) {
+        // a single vector, or a cluster too large for the in-register rotation: Rayleigh quotients
+        if (lane == 0)
+          for (int a = 0; a < kc; ++a) lam[k0 + a] = Tc[a * kc + a];
+        __syncwarp();
+        continue;
+      }
+      if (lane == 0) {
+        for (int a = 0; a < kc; ++a)
+          for (int b = 0; b < kc; ++b) Yc[a * kc + b] = a == b ? (S)1 : (S)0;
+        for (int sweep = 0; sweep < 30; ++sweep) {
+          S off = 0, dia = 0;
+          for (int a = 0; a < kc; ++a) {
+            dia += Tc[a * kc + a] * Tc[a * kc + a];
+            for (int b = a + 1; b < kc; ++b) off += Tc[a * kc + b] * Tc[a * kc + b];
+          }
+          if (off <= (S)1e-32 * dia) break;
+          for (int a = 0; a < kc - 1; ++a)
+            for (int b = a + 1; b < kc; ++b) {
+              const S apq = Tc[a * kc + b];
+              if (fabs(apq) <= (S)1e-300) continue;
+              const S zeta = (Tc[b * kc + b] - Tc[a * kc + a]) / (2 * apq);
+              const S t = (zeta >= 0 ? (S)1 : (S)-1) / (fabs(zeta) + sqrt((S)1 + zeta * zeta));
+              const S c = (S)1 / sqrt((S)1 + t * t), sn = t * c;
+              for (int q = 0; q < kc; ++q) {  // columns a, b
+                const S xa = Tc[q * kc + a], xb = Tc[q * kc + b];
+                Tc[q * kc + a] = c * xa - sn * xb;
+                Tc[q * kc + b] = sn * xa + c * xb;
+              }
+              for (int q = 0; q < kc; ++q) {  // rows a, b
+                const S xa = Tc[a * kc + q], xb = Tc[b * kc + q];
+                Tc[a * kc + q] = c * xa - sn * xb;
+                Tc[b * kc + q] = sn * xa + c * xb;
+              }
+              for (int q = 0; q < kc; ++q) {
+                const S ya = Yc[q * kc + a], yb = Yc[q * kc + b];
+                Yc[q * kc + a] = c * ya - sn * yb;
+                Yc[q * kc + b] = sn * ya + c * yb;
+              }
+            }
+        }
+        // ascending order: selection sort of the diagonal, columns of Yc follow
+        for (int a = 0; a < kc; ++a) {
+          int mi = a;
+          for (int b = a + 1; b < kc; ++b)
+            if (Tc[b * kc + b] < Tc[mi * kc + mi]) mi = b;
+          if (mi != a) {
+            const S t = Tc[a * kc + a];
+            Tc[a * kc + a] = Tc[mi * kc + mi];
+            Tc[mi * kc + mi] = t;
+            for (int q = 0; q < kc; ++q) {
+              const S y = Yc[q * kc + a];
+              Yc[q * kc + a] = Yc[q * kc + mi];
+              Yc[q * kc + mi] = y;
+            }
+          }
+          lam[k0 + a] = Tc[a * kc + a];
+        }
+      }
+      __syncwarp();
+      // Z_c <- Z_c Yc, row by row (each lane owns rows)
+      for (int i = lane; i < n; i += 32) {
+        S zrow[32];
+        for (int b = 0; b < kc; ++b) zrow[b] = Z[(size_t)i * nwant + k0 + b];
+        for (int a = 0; a < kc; ++a) {
+          S acc = 0;
+          for (int b = 0; b < kc; ++b) acc += zrow[b] * Yc[b * kc + a];
+          Z[(size_t)i * nwant + k0 + a] = acc;
+        }
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+  }
   // step 4: u_k = H_0 (H_1 (... H_{n-2} z_k)), one warp per eigenvector
   for (int k = warp; k < nwant; k += nw) {
     for (int i = lane; i < n; i += 32) U[(size_t)i * ldu + k] = mk<S>(Z[(size_t)i * nwant + k], 0);
