@@ -1,11 +1,12 @@
 // Batches of independent exciton systems on one GPU.
 //
-// A system of the strain/mesh scans is small (dim 576..11,664): its eigensolve is a chain of short
-// kernels and host round trips that leaves most of the 152 SMs idle.  The batch therefore runs several
-// systems at once: each worker owns a context (its own stream, device buffers and status word) and a host
-// thread, and takes the next system from a queue sorted largest first (longest-processing-time order, so
-// the tail of the batch is made of short jobs).  Kernels of different workers overlap on the device;
-// nothing is shared between workers except the read-only inputs and the per-system output slots.
+// A system of the strain/mesh scans is small (dim 576..11,664): its solve is a chain of short kernels (one
+// graph launch for the eigensolve) that leaves most of the 152 SMs idle.  The batch therefore runs several
+// systems at once: every system slot owns a context (its own stream, device buffers, status word and cached
+// eigensolver graph), and nworkers host threads take the next system from a queue sorted largest first
+// (longest-processing-time order, so the tail of the batch is made of short jobs).  Kernels of different
+// systems overlap on the device; nothing is shared between them except the read-only inputs and the
+// per-system output slots.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -17,7 +18,10 @@
 
 struct wtb_batch {
   int device = 0;
-  std::vector<wtb_ctx*> workers;
+  int nworkers = 1;
+  // one context per system slot: its buffers, stream and cached eigensolver graph persist across calls, so
+  // solving the same batch again relaunches each system's graph without capturing it again
+  std::vector<wtb_ctx*> slots;
   std::vector<std::string> errors;  // per system of the last call
 };
 
@@ -32,25 +36,18 @@ double system_cost(const wtb_system& s, const wtb_bse_params& p) {
 
 extern "C" int wtb_batch_create(wtb_batch** out, int device, int nworkers) {
   if (!out || nworkers < 1 || nworkers > 64) return WTB_EBADARG;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) return WTB_ENODEV;
   auto* b = new wtb_batch();
   b->device = device;
-  for (int i = 0; i < nworkers; ++i) {
-    wtb_ctx* c = nullptr;
-    const int r = wtb_ctx_create(&c, device);
-    if (r != WTB_OK) {
-      for (wtb_ctx* w : b->workers) wtb_ctx_destroy(w);
-      delete b;
-      return r;
-    }
-    b->workers.push_back(c);
-  }
+  b->nworkers = nworkers;
   *out = b;
   return WTB_OK;
 }
 
 extern "C" int wtb_batch_destroy(wtb_batch* b) {
   if (!b) return WTB_OK;
-  for (wtb_ctx* w : b->workers) wtb_ctx_destroy(w);
+  for (wtb_ctx* w : b->slots) wtb_ctx_destroy(w);
   delete b;
   return WTB_OK;
 }
@@ -72,11 +69,18 @@ extern "C" int wtb_batch_bsesolver(wtb_batch* b, int nsys, const wtb_system* sys
   for (int i = 0; i < nsys; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(),
                    [&](int x, int y) { return system_cost(sys[x], p[x]) > system_cost(sys[y], p[y]); });
+  while ((int)b->slots.size() < nsys) {
+    wtb_ctx* c = nullptr;
+    const int r = wtb_ctx_create(&c, b->device);
+    if (r != WTB_OK) return r;
+    b->slots.push_back(c);
+  }
   std::atomic<int> next{0};
-  auto work = [&](wtb_ctx* c) {
+  auto work = [&]() {
     std::vector<double> Ws, acts;
     for (int q = next.fetch_add(1); q < nsys; q = next.fetch_add(1)) {
       const int i = order[q];
+      wtb_ctx* c = b->slots[i];
       const wtb_system& s = sys[i];
       int r = wtb_set_hr(c, s.w90basis, s.nvec, s.rvec, s.ffactor, s.hopmatrices, s.ihopmatrices, s.rlat, s.efermi,
                          s.scs, s.systype_np);
@@ -104,10 +108,10 @@ extern "C" int wtb_batch_bsesolver(wtb_batch* b, int nsys, const wtb_system* sys
       if (r != WTB_OK) b->errors[i] = wtb_last_error(c);
     }
   };
-  const int nw = std::min<int>((int)b->workers.size(), std::max(nsys, 1));
+  const int nw = std::min(b->nworkers, std::max(nsys, 1));
   std::vector<std::thread> threads;
-  for (int w = 1; w < nw; ++w) threads.emplace_back(work, b->workers[w]);
-  work(b->workers[0]);
+  for (int w = 1; w < nw; ++w) threads.emplace_back(work);
+  work();
   for (auto& th : threads) th.join();
   if (wall_ms) wall_ms[0] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   for (int i = 0; i < nsys; ++i)

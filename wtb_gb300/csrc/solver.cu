@@ -14,6 +14,8 @@
 // EPS_SMALLEST_MAGNITUDE, tol 1e-8, 200 iterations); for the positive BSE spectra of this path the
 // smallest-magnitude and smallest-algebraic eigenvalues coincide.
 #include <cmath>
+#include <cstring>
+#include <functional>
 #include <cstdlib>
 
 #include "solver.h"
@@ -60,7 +62,7 @@ cudaError_t MatFreeOperator<S>::apply(const cplx<S>* X, int ldx, int c0, int nco
         cudaEvent_t ea = nullptr, eb = nullptr;
         // the live profile covers the iteration's contraction launches (the final split run is a
         // different launch configuration and is left out of it)
-        const bool profiled = prof && prof->on && !final_apply;
+        const bool profiled = prof && prof->on && !final_apply && !this->capturing;
         if (profiled) {
           cudaEventCreate(&ea);
           cudaEventCreate(&eb);
@@ -68,6 +70,7 @@ cudaError_t MatFreeOperator<S>::apply(const cplx<S>* X, int ldx, int c0, int nco
         }
         e = final_apply ? tc_gemm_run_split(plan, st, s, kchunk_final) : tc_gemm_run(plan, st, s);
         if (e != cudaSuccess) return e;
+
         if (profiled) {
           cudaEventRecord(eb, s);
           prof->pending.emplace_back(ea, eb);
@@ -85,14 +88,15 @@ cudaError_t MatFreeOperator<S>::apply(const cplx<S>* X, int ldx, int c0, int nco
       e = launch_mf_gather<S, S>(X, ldx, c0 + b0, nb, vec_win, nk, nv, nc, w, Zr, Kpad, 1, 0, s);
       if (e != cudaSuccess) return e;
       cudaEvent_t ea = nullptr, eb = nullptr;
-      if (prof && prof->on) {
+      const bool profiled = prof && prof->on && !this->capturing;
+      if (profiled) {
         cudaEventCreate(&ea);
         cudaEventCreate(&eb);
         cudaEventRecord(ea, s);
       }
       e = launch_simt_gemm_tn<S>(Vr, Kpad, Zr, Kpad, reinterpret_cast<S*>(Tm), Npad, nk, N, Kpad, s);
       if (e != cudaSuccess) return e;
-      if (prof && prof->on) {
+      if (profiled) {
         cudaEventRecord(eb, s);
         prof->pending.emplace_back(ea, eb);
         prof->launches += 1;
@@ -102,6 +106,52 @@ cudaError_t MatFreeOperator<S>::apply(const cplx<S>* X, int ldx, int c0, int nco
       e = launch_mf_scatter<S, S>(reinterpret_cast<const S*>(Tm), Npad, X, ldx, vec_win, dE, nk, nv, nc, w, nb, Y, ldy,
                                   c0 + b0, s);
       if (e != cudaSuccess) return e;
+    }
+  }
+  return cudaSuccess;
+}
+
+template <class S>
+cudaError_t MatFreeOperator<S>::time_contraction(int reps, int ncol, cudaStream_t s) {
+  if (!prof) return cudaSuccess;
+  const int N = 2 * w * w * std::min(ncol, nbmax);
+  const int np = npairs0 > 0 ? npairs0 : npairs;
+  TcGemmPlan* plan = nullptr;
+  if (kind == GEMM_TC_BF16) {
+    const long key = (long)N * 16 + np;
+    auto it = plans.find(key);
+    if (it == plans.end()) {
+      std::string m2;
+      if (tc_gemm_plan_create(&plan, Vs, Mpad, Kpad, (long)Mpad * Kpad, nslices, Zs, Npad, (long)Npad * Kpad, nslices,
+                              reinterpret_cast<float*>(Tm), Npad, np, pa, pb, &m2) != WTB_OK)
+        return cudaErrorInvalidValue;
+      tc_gemm_set_valid(plan, nk, N);
+      plans[key] = plan;
+    } else {
+      plan = it->second;
+    }
+  }
+  for (int r = 0; r < reps; ++r) {
+    cudaEvent_t ea, eb;
+    cudaError_t e = cudaEventCreate(&ea);
+    if (e != cudaSuccess) return e;
+    e = cudaEventCreate(&eb);
+    if (e != cudaSuccess) return e;
+    cudaEventRecord(ea, s);
+    if (plan)
+      e = tc_gemm_run(plan, st, s);
+    else
+      e = launch_simt_gemm_tn<S>(Vr, Kpad, Zr, Kpad, reinterpret_cast<S*>(Tm), Npad, nk, N, Kpad, s);
+    if (e != cudaSuccess) return e;
+    cudaEventRecord(eb, s);
+    prof->pending.emplace_back(ea, eb);
+    prof->launches += 1;
+    if (plan) {
+      prof->flops += 2.0 * nk * (double)N * nk * np;
+      prof->bytes += 2.0 * nslices * ((double)nk * nk + (double)N * nk) + 4.0 * nk * (double)N;
+    } else {
+      prof->flops += 2.0 * nk * (double)N * nk;
+      prof->bytes += sizeof(S) * ((double)nk * nk + (double)N * nk + (double)nk * N);
     }
   }
   return cudaSuccess;
@@ -180,6 +230,187 @@ int rayleigh_ritz(const cplx<S>* Sb, const cplx<S>* ASb, int ld, int nb, int m, 
 
 }  // namespace
 
+// ------------------------------------------------------------------------------------------------
+// Device-resident loop.  One solve is one CUDA graph: set-up, a WHILE node whose body is one LOBPCG
+// iteration (bf16x3: a second WHILE node for the 6-product phase, after a static switch block), then the
+// final FP64 Rayleigh-Ritz.  The decisions the host used to take every iteration (soft locking,
+// convergence, the stagnation and breakdown guards, the iteration cap) are taken by lob_control_kernel,
+// which sets the loop's condition with cudaGraphSetConditional; the host synchronises once per solve.
+// The basis is always [X W P] (3m columns): W and P start at zero and the pivoted-Cholesky
+// orthonormalisation drops zero columns, so the first iteration needs no separate 2m-column path.
+
+struct LobCtl {
+  int it, total_it, nconv, stop, converged, restore, save, failed, best_it, pad[3];
+  double maxrel, best_maxrel, saved_rel, tol;
+};
+
+__global__ void lob_ctl_reset_kernel(LobCtl* c, double tol, int keep_total) {
+  c->it = 0;
+  if (!keep_total) {
+    c->total_it = 0;
+    c->failed = 0;
+  }
+  c->nconv = 0;
+  c->stop = 0;
+  c->converged = 0;
+  c->restore = 0;
+  c->save = 0;
+  c->best_it = 0;
+  c->maxrel = 1e300;
+  c->best_maxrel = 1e300;
+  c->saved_rel = 1e300;
+  c->tol = tol;
+}
+
+// One warp.  rel_j = ||r_j|| / |theta_j|; converged columns leave the active set (soft locking).
+//  - breakdown guard: near the operator's rounding floor the running AX drifts from H X and LOBPCG can lose
+//    consistency (Ritz values falling far below the spectrum): the block with the lowest residual of the
+//    phase is kept (save), and a residual 10x above it after reaching 100 x tol restores it and ends the
+//    phase (restore);
+//  - stagnation guard (reduced precision): residuals within 100 x tol that have not improved by 10% over
+//    15 iterations are at the operator's rounding floor; the FP64 Rayleigh-Ritz takes over;
+//  - the iteration cap, a non-finite residual and a device status word end the loop as well.
+// Monitor lines follow the reference's MyEPSMonitor (src/module_slepc_solver.F90:101-116).
+__global__ void lob_control_kernel(LobCtl* c, const double* __restrict__ norms2, const double* __restrict__ theta,
+                                   int m, int nev, int maxit, int reduced, int* __restrict__ active,
+                                   const DevStatus* __restrict__ st, cudaGraphConditionalHandle h, int monitor) {
+  const int lane = threadIdx.x;
+  const double tol = c->tol;
+  double rel = 0.0;
+  int conv = 1, bad = 0;
+  if (lane < m) {
+    const double rn = sqrt(fmax(norms2[lane], 0.0));
+    const double th = theta[lane];
+    bad = !(isfinite(rn) && isfinite(th));
+    rel = rn / fmax(fabs(th), 1e-12);
+    conv = rel <= tol;
+    active[lane] = conv ? 0 : 1;
+  }
+  double mr = lane < nev ? rel : 0.0;
+  int nc = lane < nev ? conv : 0;
+  int first = lane < nev && !conv ? lane : 1 << 20;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+    nc += __shfl_xor_sync(0xffffffffu, nc, o);
+    bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    first = min(first, __shfl_xor_sync(0xffffffffu, first, o));
+  }
+  if (lane != 0) return;
+  int stop = 0;
+  c->save = 0;
+  if (st->code) {
+    stop = 1;
+  } else if (bad) {
+    c->failed = WTB_ENAN;
+    stop = 1;
+  } else {
+    c->maxrel = mr;
+    c->nconv = nc;
+    if (mr < c->saved_rel) {
+      c->saved_rel = mr;
+      c->save = 1;
+    } else if (c->saved_rel <= 100.0 * tol && mr > 10.0 * c->saved_rel) {
+      c->restore = 1;
+      c->converged = 1;
+      stop = 1;
+    }
+    if (!stop && nc == nev) {
+      c->converged = 1;
+      stop = 1;
+    }
+    if (!stop) {
+      if (mr < 0.9 * c->best_maxrel) {
+        c->best_maxrel = mr;
+        c->best_it = c->it;
+      } else if (reduced && mr <= 100.0 * tol && c->it - c->best_it >= 15) {
+        c->converged = 1;
+        stop = 1;
+      }
+    }
+    if (!stop && c->total_it >= maxit) stop = 1;
+  }
+  if (monitor) {
+    const int f = first < nev ? first : nev - 1;
+    printf("WTB-EPS %5d EPS pair=%4d value (error) %15.8E (%10.3E) max %10.3E\n", c->total_it, nc + 1, theta[f],
+           sqrt(fmax(norms2[f], 0.0)) / fmax(fabs(theta[f]), 1e-12), mr);
+  }
+  if (!stop) {
+    c->it += 1;
+    c->total_it += 1;
+  }
+  c->stop = stop;
+  cudaGraphSetConditional(h, stop ? 0u : 1u);
+}
+
+// dst[:, 0:ncol] = src[:, 0:ncol] when *flag is set
+template <class S>
+__global__ void cond_copy_kernel(const int* __restrict__ flag, const cplx<S>* __restrict__ src, int lds,
+                                 cplx<S>* __restrict__ dst, int ldd, int ncol, int nrow) {
+  if (!*flag) return;
+  const long n = (long)nrow * ncol;
+  for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
+    const long r = e / ncol;
+    const int c = (int)(e % ncol);
+    dst[r * ldd + c] = src[r * lds + c];
+  }
+}
+
+// In place, row by row (one warp per row): X <- [X W P] C and P <- [W P] C[m:3m, :] for the basis and for
+// its image under H (the row is read into registers before any of it is written).
+template <class S>
+__global__ void __launch_bounds__(256) lob_update_kernel(cplx<S>* __restrict__ Sb, cplx<S>* __restrict__ ASb, int ld,
+                                                         int m, const zd* __restrict__ C, int dim) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cplx<S>* Cs = reinterpret_cast<cplx<S>*>(smem_raw);  // [3m][m]
+  const int nb = 3 * m;
+  for (int e = threadIdx.x; e < nb * m; e += blockDim.x) Cs[e] = mk<S>((S)C[e].re, (S)C[e].im);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (long r = (long)blockIdx.x * nw + warp; r < dim; r += (long)gridDim.x * nw) {
+    for (int which = 0; which < 2; ++which) {
+      cplx<S>* row = (which ? ASb : Sb) + r * ld;
+      cplx<S> v[3];
+#pragma unroll
+      for (int q = 0; q < 3; ++q) v[q] = lane + 32 * q < nb ? row[lane + 32 * q] : mk<S>(0, 0);
+      cplx<S> x = mk<S>(0, 0), pn = mk<S>(0, 0);
+      const int j = lane < m ? lane : 0;
+      for (int i = 0; i < nb; ++i) {
+        const int q = i >> 5;
+        const cplx<S> src = q == 0 ? v[0] : (q == 1 ? v[1] : v[2]);
+        const cplx<S> ri = mk<S>(__shfl_sync(0xffffffffu, src.re, i & 31), __shfl_sync(0xffffffffu, src.im, i & 31));
+        const cplx<S> c = Cs[i * m + j];
+        cfma(x, ri, c);
+        if (i >= m) cfma(pn, ri, c);
+      }
+      __syncwarp();
+      if (lane < m) {
+        row[lane] = x;
+        row[2 * m + lane] = pn;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+struct CaptureSeg {
+  cudaStream_t s;
+  cudaError_t begin(cudaGraph_t g, const std::vector<cudaGraphNode_t>& deps) {
+    return cudaStreamBeginCaptureToGraph(s, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(),
+                                         cudaStreamCaptureModeRelaxed);
+  }
+  cudaError_t end(std::vector<cudaGraphNode_t>* tail) {
+    cudaStreamCaptureStatus cs;
+    const cudaGraphNode_t* d = nullptr;
+    size_t nd = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(s, &cs, nullptr, nullptr, &d, nullptr, &nd);
+    if (tail && e == cudaSuccess) tail->assign(d, d + nd);
+    cudaGraph_t g2 = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(s, &g2);
+    return e != cudaSuccess ? e : e2;
+  }
+};
+
 template <class S>
 int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, double tol, int maxit, Workspace& ws,
                  DevStatus* st, cudaStream_t s, std::vector<double>* E, zd* Xout, SolveStats* stats,
@@ -191,259 +422,309 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
     return WTB_EBADARG;
   }
   const int ld = 3 * m;
-  const int maxnb = 3 * m;
-  if (maxnb > (sizeof(S) == 4 ? 96 : 78)) {
+  const int nb = 3 * m;
+  if (nb > (sizeof(S) == 4 ? 96 : 78) || m > 32) {
     if (msg) *msg = "eigensolver block too large (3*block must be <= 96 in FP32, <= 78 in FP64)";
     return WTB_EBADARG;
   }
   cudaError_t err = cudaSuccess;
-  auto chk = [&](void) { return err == cudaSuccess; };
-  cplx<S>* Sb[2];
-  cplx<S>* ASb[2];
-  Sb[0] = ws.get<cplx<S>>("lob_S0", (size_t)dim * ld, &err, true);
-  if (!chk()) goto oom;
-  Sb[1] = ws.get<cplx<S>>("lob_S1", (size_t)dim * ld, &err, true);
-  if (!chk()) goto oom;
-  ASb[0] = ws.get<cplx<S>>("lob_AS0", (size_t)dim * ld, &err, true);
-  if (!chk()) goto oom;
-  ASb[1] = ws.get<cplx<S>>("lob_AS1", (size_t)dim * ld, &err, true);
-  if (!chk()) goto oom;
-  {
-    Small sm;
-    const size_t nn = (size_t)maxnb * maxnb;
-    sm.M = ws.get<zd>("lob_M", nn, &err);
-    sm.G = ws.get<zd>("lob_G", nn, &err);
-    sm.B = ws.get<zd>("lob_B", nn, &err);
-    sm.Gp = ws.get<zd>("lob_Gp", nn, &err);
-    sm.U = ws.get<zd>("lob_U", nn, &err);
-    sm.Y = ws.get<zd>("lob_Y", nn, &err);
-    sm.C = ws.get<zd>("lob_C", nn, &err);
-    sm.T = ws.get<zd>("lob_T", nn, &err);
-    sm.lam = ws.get<double>("lob_lam", maxnb, &err);
-    sm.theta = ws.get<double>("lob_theta", maxnb, &err);
-    sm.dinv = ws.get<double>("lob_dinv", maxnb, &err);
-    sm.keep = ws.get<int>("lob_keep", maxnb, &err);
-    // partial sums of the tall-skinny reductions: about 128 rows per part, at most two per SM
-    const int npart = std::max(1, std::min(304, (dim + 127) / 128));
-    double* partial = ws.get<double>("lob_partial", (size_t)npart * nn * 2, &err);
-    double* norms2 = ws.get<double>("lob_norms2", 32, &err);
-    int* active = ws.get<int>("lob_active", 32, &err);
-    int* idx = ws.get<int>("lob_idx", 65 * 128, &err);
-    double* cand = ws.get<double>("lob_cand", 65 * 128, &err);
-    double* th_dev = ws.get<double>("lob_thcur", maxnb, &err);
-    if (!chk()) goto oom;
-    // SVQB keeps a direction of the scaled Gram matrix only if its eigenvalue exceeds tau: a kept
-    // direction's Rayleigh quotient carries the operator's rounding divided by sqrt(eigenvalue), so tau
-    // sits well above the FP32 noise (~1e-6 on the Gram entries) and just above FP64's
-    const double tau = sizeof(S) == 4 ? 1e-4 : 1e-13;
-    std::vector<double> h_theta(maxnb), h_norm(32);
-    std::vector<int> h_active(32, 1);
-    // start block: unit vectors at the m lowest transition energies (+ small deterministic noise)
-    CK(launch_select_lowest(diag, dim, m, idx, cand, s));
-    CK(launch_init_guess<S>(Sb[0], ld, dim, m, idx + 64 * m, 12345u, s));
-    CK(op.apply(Sb[0], ld, 0, m, ASb[0], ld, s));
-    int r = rayleigh_ritz<S>(Sb[0], ASb[0], ld, m, m, dim, tau, sm, partial, npart, st, s, msg, false);
+  cplx<S>* Sb = ws.get<cplx<S>>("lob_S", (size_t)dim * ld, &err, true);
+  cplx<S>* ASb = ws.get<cplx<S>>("lob_AS", (size_t)dim * ld, &err, true);
+  cplx<S>* Xbest = ws.get<cplx<S>>("lob_Xbest", (size_t)dim * m, &err);
+  Small sm;
+  const size_t nn = (size_t)nb * nb;
+  sm.M = ws.get<zd>("lob_M", nn, &err);
+  sm.G = ws.get<zd>("lob_G", nn, &err);
+  sm.B = ws.get<zd>("lob_B", nn, &err);
+  sm.Gp = ws.get<zd>("lob_Gp", nn, &err);
+  sm.U = nullptr;
+  sm.Y = ws.get<zd>("lob_Y", nn, &err);
+  sm.C = ws.get<zd>("lob_C", nn, &err);
+  sm.T = ws.get<zd>("lob_T", nn, &err);
+  sm.lam = nullptr;
+  sm.dinv = nullptr;
+  sm.theta = ws.get<double>("lob_theta", nb, &err);
+  sm.keep = ws.get<int>("lob_keep", nb, &err);
+  // partial sums of the tall-skinny reductions: about 128 rows per part, at most two per SM
+  const int npart = std::max(1, std::min(304, (dim + 127) / 128));
+  double* partial = ws.get<double>("lob_partial", (size_t)npart * nn * 2, &err);
+  double* norms2 = ws.get<double>("lob_norms2", 32, &err);
+  int* active = ws.get<int>("lob_active", 32, &err);
+  int* idx = ws.get<int>("lob_idx", 65 * 128, &err);
+  double* cand = ws.get<double>("lob_cand", 65 * 128, &err);
+  double* th_dev = ws.get<double>("lob_thcur", nb, &err);
+  LobCtl* ctl = ws.get<LobCtl>("lob_ctl", 1, &err);
+  zd* X64 = ws.get<zd>("fin_X", (size_t)dim * 2 * m, &err);
+  zd* T64 = ws.get<zd>("fin_T", (size_t)dim * m, &err);
+  if (err != cudaSuccess) {
+    if (msg) *msg = std::string("device allocation failed: ") + cudaGetErrorString(err);
+    return WTB_ENOMEM;
+  }
+  cplx<S>* X = Sb;
+  cplx<S>* W = Sb + m;
+  cplx<S>* P = Sb + 2 * m;
+  cplx<S>* AX = ASb;
+  cplx<S>* AW = ASb + m;
+  cplx<S>* AP = ASb + 2 * m;
+  // orthonormalisation threshold: a kept direction's Rayleigh quotient carries the operator's rounding
+  // divided by its residual norm, so tau sits well above the FP32 noise and just above FP64's
+  const double tau = sizeof(S) == 4 ? 1e-4 : 1e-13;
+  const bool reduced = sizeof(S) == 4;
+  const bool monitor = std::getenv("WTB_EPS_MONITOR") != nullptr;
+  const bool two_phase = tol_refine > 0.0 && tol_refine < tol;
+  const size_t upd_smem = (size_t)nb * m * sizeof(cplx<S>);
+  const int upd_grid = std::max(1, std::min(152 * 8, (dim + 7) / 8));
+  const unsigned cp_grid = (unsigned)std::max(1, std::min(152 * 4, (int)(((long)dim * m + 255) / 256)));
+
+  // the pieces of one iteration, as stream launches (captured below)
+  auto rr_and_update = [&]() -> int {
+    int r = rayleigh_ritz<S>(Sb, ASb, ld, nb, m, dim, tau, sm, partial, npart, st, s, msg, false);
     if (r) return r;
-    CK(launch_update<S>(Sb[0], ld, m, sm.C, m, m, dim, Sb[1], ld, 1.0, 0.0, s));
-    CK(launch_update<S>(ASb[0], ld, m, sm.C, m, m, dim, ASb[1], ld, 1.0, 0.0, s));
+    lob_update_kernel<S><<<upd_grid, 256, upd_smem, s>>>(Sb, ASb, ld, m, sm.C, dim);
+    ++g_launch_count;
+    CK(cudaGetLastError());
     CK(cudaMemcpyAsync(th_dev, sm.theta, sizeof(double) * m, cudaMemcpyDeviceToDevice, s));
-    int cur = 1;
-    bool have_p = false;
-    bool converged = false;
-    int it = 0;
-    // per-iteration monitor in the format of the reference's MyEPSMonitor
-    // (src/module_slepc_solver.F90:101-116), enabled by the WTB_EPS_MONITOR environment variable
-    const bool monitor = std::getenv("WTB_EPS_MONITOR") != nullptr;
-    // stagnation guard for reduced-precision iterations: once the wanted residuals sit within
-    // 100 x tol and have not improved by 10% over 15 iterations, the operator's rounding floor has been
-    // reached and the FP64 Rayleigh-Ritz below takes over
-    double best_maxrel = 1e300;
-    int best_it = 0;
-    // breakdown guard: near the operator's rounding floor the running AX drifts from H X and LOBPCG can
-    // lose consistency (Ritz values falling far below the spectrum).  The block with the lowest residual of
-    // the current phase is kept; a residual that grows 10x past it after reaching 100 x tol restores it.
-    cplx<S>* Xbest = ws.get<cplx<S>>("lob_Xbest", (size_t)dim * m, &err);
-    if (!chk()) goto oom;
-    double saved_rel = 1e300;
-    int restarts = 0;
-    for (; it < maxit; ++it) {
-      cplx<S>* X = Sb[cur];
-      cplx<S>* AX = ASb[cur];
-      cplx<S>* W = X + m;
-      cplx<S>* AW = AX + m;
-      CK(launch_residual<S>(AX, ld, X, ld, th_dev, m, dim, W, ld, partial, npart, norms2, s));
-      CK(cudaMemcpyAsync(h_norm.data(), norms2, sizeof(double) * m, cudaMemcpyDeviceToHost, s));
-      CK(cudaMemcpyAsync(h_theta.data(), th_dev, sizeof(double) * m, cudaMemcpyDeviceToHost, s));
-      CK(cudaStreamSynchronize(s));
-      DevStatus hst;
-      CK(cudaMemcpy(&hst, st, sizeof(hst), cudaMemcpyDeviceToHost));
-      if (hst.code) {
-        if (msg) *msg = "device status " + std::to_string(hst.code) + " during the eigensolve";
-        return hst.code >= 400 && hst.code < 500 ? WTB_ETIMEOUT : WTB_ENOCONV;
-      }
-      int nconv = 0;
-      double maxrel = 0.0;
-      for (int j = 0; j < m; ++j) {
-        const double rn = std::sqrt(std::max(h_norm[j], 0.0));
-        if (!std::isfinite(rn) || !std::isfinite(h_theta[j])) {
-          if (msg) *msg = "non-finite residual in the eigensolve";
-          return WTB_ENAN;
-        }
-        const double rel = rn / std::max(std::fabs(h_theta[j]), 1e-12);
-        const bool cj = rel <= tol;
-        if (j < nev) {
-          nconv += cj;
-          maxrel = std::max(maxrel, rel);
-        }
-        h_active[j] = cj ? 0 : 1;
-      }
-      if (stats) stats->max_rel_residual = maxrel;
-      if (monitor) {
-        int first = 0;
-        while (first < nev - 1 && h_active[first] == 0) ++first;
-        std::fprintf(stderr, "WTB-EPS %5d EPS pair=%4d value (error) %15.8E (%10.3E) max %10.3E\n", it, nconv + 1,
-                     h_theta[first], std::sqrt(std::max(h_norm[first], 0.0)) / std::max(std::fabs(h_theta[first]), 1e-12),
-                     maxrel);
-      }
-      // restart from X alone: fresh AX, no search directions, Rayleigh-Ritz on X
-      auto restart_from_x = [&]() -> int {
-        CK(op.apply(X, ld, 0, m, AX, ld, s));
-        have_p = false;
-        best_maxrel = 1e300;
-        best_it = it;
-        int rr = rayleigh_ritz<S>(X, AX, ld, m, m, dim, tau, sm, partial, npart, st, s, msg, false);
-        if (rr) return rr;
-        const int nxt = cur ^ 1;
-        CK(launch_update<S>(X, ld, m, sm.C, m, m, dim, Sb[nxt], ld, 1.0, 0.0, s));
-        CK(launch_update<S>(AX, ld, m, sm.C, m, m, dim, ASb[nxt], ld, 1.0, 0.0, s));
-        CK(cudaMemcpyAsync(th_dev, sm.theta, sizeof(double) * m, cudaMemcpyDeviceToDevice, s));
-        cur = nxt;
-        return WTB_OK;
-      };
-      if (maxrel < saved_rel) {
-        saved_rel = maxrel;
-        CK(launch_copy_cols<S>(X, ld, Xbest, m, m, dim, s));
-      } else if (saved_rel <= 100.0 * tol && maxrel > 10.0 * saved_rel) {
-        CK(launch_copy_cols<S>(Xbest, m, X, ld, m, dim, s));
-        if (saved_rel <= tol || ++restarts > 2) {
-          // the best block goes to the final Rayleigh-Ritz (which re-applies the operator)
-          converged = saved_rel <= 100.0 * tol;
-          break;
-        }
-        r = restart_from_x();
-        if (r) return r;
-        saved_rel = 1e300;
-        continue;
-      }
-      if (nconv == nev) {
-        if (tol_refine > 0.0 && tol_refine < tol && op.begin_refine()) {
-          // second phase: the accurate operator; AX is recomputed and the search directions P (built
-          // with the cheaper operator) are dropped
-          tol = tol_refine;
-          tol_refine = 0.0;
-          r = restart_from_x();
-          if (r) return r;
-          saved_rel = 1e300;
-          continue;
-        }
-        converged = true;
-        break;
-      }
-      if (maxrel < 0.9 * best_maxrel) {
-        best_maxrel = maxrel;
-        best_it = it;
-      } else if (sizeof(S) == 4 && maxrel <= 100.0 * tol && it - best_it >= 15) {
-        converged = true;  // rounding floor of the reduced-precision operator
-        break;
-      }
-      CK(cudaMemcpyAsync(active, h_active.data(), sizeof(int) * m, cudaMemcpyHostToDevice, s));
-      CK(launch_precond<S>(W, ld, diag, th_dev, active, m, dim, s));
-      // W <- W - X (X^H W)
-      CK(launch_gram<S>(X, ld, m, W, ld, m, dim, sm.T, partial, npart, s));
-      CK(launch_update<S>(X, ld, m, sm.T, m, m, dim, W, ld, -1.0, 1.0, s));
-      CK(op.apply(W, ld, 0, m, AW, ld, s));
-      if (have_p) {
-        // P <- P - X (X^H P), AP <- AP - AX (X^H P): keeps the basis [X W P] away from dependence
-        CK(launch_gram<S>(X, ld, m, X + 2 * m, ld, m, dim, sm.T, partial, npart, s));
-        CK(launch_update<S>(X, ld, m, sm.T, m, m, dim, X + 2 * m, ld, -1.0, 1.0, s));
-        CK(launch_update<S>(AX, ld, m, sm.T, m, m, dim, AX + 2 * m, ld, -1.0, 1.0, s));
-      }
-      const int nb = have_p ? 3 * m : 2 * m;
-      r = rayleigh_ritz<S>(X, AX, ld, nb, m, dim, tau, sm, partial, npart, st, s, msg, false);
-      if (r) return r;
-      const int nxt = cur ^ 1;
-      // new X, AX from the whole basis; new P, AP from its W and P parts
-      CK(launch_update<S>(X, ld, nb, sm.C, m, m, dim, Sb[nxt], ld, 1.0, 0.0, s));
-      CK(launch_update<S>(AX, ld, nb, sm.C, m, m, dim, ASb[nxt], ld, 1.0, 0.0, s));
-      CK(launch_update<S>(X + m, ld, nb - m, sm.C + (size_t)m * m, m, m, dim, Sb[nxt] + 2 * m, ld, 1.0, 0.0, s));
-      CK(launch_update<S>(AX + m, ld, nb - m, sm.C + (size_t)m * m, m, m, dim, ASb[nxt] + 2 * m, ld, 1.0, 0.0, s));
-      CK(cudaMemcpyAsync(th_dev, sm.theta, sizeof(double) * m, cudaMemcpyDeviceToDevice, s));
-      cur = nxt;
-      have_p = true;
+    return WTB_OK;
+  };
+  auto check_and_decide = [&](cudaGraphConditionalHandle h) -> int {
+    CK(launch_residual<S>(AX, ld, X, ld, th_dev, m, dim, W, ld, partial, npart, norms2, s));
+    lob_control_kernel<<<1, 32, 0, s>>>(ctl, norms2, th_dev, m, nev, maxit, reduced ? 1 : 0, active, st, h,
+                                        monitor ? 1 : 0);
+    ++g_launch_count;
+    CK(cudaGetLastError());
+    cond_copy_kernel<S><<<cp_grid, 256, 0, s>>>(&ctl->save, X, ld, Xbest, m, m, dim);
+    ++g_launch_count;
+    CK(cudaGetLastError());
+    return WTB_OK;
+  };
+  auto restart_from_x = [&](cudaGraphConditionalHandle h) -> int {
+    CK(cudaMemset2DAsync(W, sizeof(cplx<S>) * ld, 0, sizeof(cplx<S>) * 2 * m, dim, s));
+    CK(cudaMemset2DAsync(AW, sizeof(cplx<S>) * ld, 0, sizeof(cplx<S>) * 2 * m, dim, s));
+    CK(op.apply(X, ld, 0, m, AX, ld, s));
+    int r = rr_and_update();
+    if (r) return r;
+    return check_and_decide(h);
+  };
+  auto iteration = [&](cudaGraphConditionalHandle h) -> int {
+    CK(launch_precond<S>(W, ld, diag, th_dev, active, m, dim, s));
+    // W <- W - X (X^H W);  P <- P - X (X^H P), AP <- AP - AX (X^H P)
+    CK(launch_gram<S>(X, ld, m, W, ld, m, dim, sm.T, partial, npart, s));
+    CK(launch_update<S>(X, ld, m, sm.T, m, m, dim, W, ld, -1.0, 1.0, s));
+    CK(op.apply(W, ld, 0, m, AW, ld, s));
+    CK(launch_gram<S>(X, ld, m, P, ld, m, dim, sm.T, partial, npart, s));
+    CK(launch_update<S>(X, ld, m, sm.T, m, m, dim, P, ld, -1.0, 1.0, s));
+    CK(launch_update<S>(AX, ld, m, sm.T, m, m, dim, AP, ld, -1.0, 1.0, s));
+    int r = rr_and_update();
+    if (r) return r;
+    return check_and_decide(h);
+  };
+
+  // the graph of this solve is reused when nothing it was captured with has changed
+  std::vector<uint64_t> sig = {(uint64_t)dim, (uint64_t)nev, (uint64_t)m, (uint64_t)maxit, (uint64_t)sizeof(S),
+                               (uint64_t)(uintptr_t)diag, (uint64_t)(uintptr_t)Xout, (uint64_t)(uintptr_t)st,
+                               (uint64_t)(uintptr_t)s, (uint64_t)(uintptr_t)Sb, (uint64_t)(uintptr_t)ASb,
+                               (uint64_t)(uintptr_t)Xbest, (uint64_t)(uintptr_t)sm.M, (uint64_t)(uintptr_t)sm.G,
+                               (uint64_t)(uintptr_t)sm.B, (uint64_t)(uintptr_t)sm.Gp, (uint64_t)(uintptr_t)sm.Y,
+                               (uint64_t)(uintptr_t)sm.C, (uint64_t)(uintptr_t)sm.T, (uint64_t)(uintptr_t)sm.theta,
+                               (uint64_t)(uintptr_t)sm.keep, (uint64_t)(uintptr_t)partial, (uint64_t)(uintptr_t)norms2,
+                               (uint64_t)(uintptr_t)active, (uint64_t)(uintptr_t)idx, (uint64_t)(uintptr_t)cand,
+                               (uint64_t)(uintptr_t)th_dev, (uint64_t)(uintptr_t)ctl, (uint64_t)(uintptr_t)X64,
+                               (uint64_t)(uintptr_t)T64, (uint64_t)monitor};
+  {
+    uint64_t tb, tr;
+    std::memcpy(&tb, &tol, 8);
+    std::memcpy(&tr, &tol_refine, 8);
+    sig.push_back(tb);
+    sig.push_back(tr);
+  }
+  op.signature(&sig);
+  uint64_t key = 1469598103934665603ull;  // FNV-1a over the signature words
+  for (uint64_t v : sig)
+    for (int b = 0; b < 8; ++b) {
+      key ^= (v >> (8 * b)) & 0xffu;
+      key *= 1099511628211ull;
     }
-    if (stats) {
-      stats->iterations = it;
-      stats->launches = 0;
+  if (key == 0) key = 1;
+  long long body_launches[2] = {0, 0};
+  int rc = WTB_OK;
+  if (ws.graph_exec && ws.graph_key == key) {
+    body_launches[0] = ws.graph_body_launches[0];
+    body_launches[1] = ws.graph_body_launches[1];
+    g_launch_count += ws.graph_launches;  // one pass of every captured kernel; the bodies' repeats are added below
+    if (cudaGraphLaunch(ws.graph_exec, s) != cudaSuccess) {
+      if (msg) *msg = "graph launch failed";
+      return WTB_ECUDA;
     }
-    // ---------------------------------------------------------------- final FP64 Rayleigh-Ritz
-    {
-      cplx<S>* X = Sb[cur];
-      cplx<S>* AXs = ASb[cur];
-      const int mm = m;
-      zd* X64 = ws.get<zd>("fin_X", (size_t)dim * 2 * mm, &err);
-      zd* T64 = ws.get<zd>("fin_T", (size_t)dim * mm, &err);
-      if (!chk()) goto oom;
-      // fresh H X in the operator's most accurate arithmetic (the iteration's AX is a running linear
-      // combination of cheaper applications)
+  } else {
+  ws.drop_graph();
+  const long long captured0 = g_launch_count.load();
+  cudaGraph_t G = nullptr;
+  cudaGraphExec_t GX = nullptr;
+  CK(cudaGraphCreate(&G, 0));
+  CaptureSeg cap{s};
+  std::vector<cudaGraphNode_t> tail;
+  // kernels captured into each loop body (the launch counter counts captured kernels; the bodies then run
+  // once per iteration)
+  auto segment = [&](cudaGraph_t g, const std::vector<cudaGraphNode_t>& deps, std::vector<cudaGraphNode_t>* out,
+                     const std::function<int()>& body) -> int {
+    cudaError_t e = cap.begin(g, deps);
+    if (e != cudaSuccess) {
+      if (msg) *msg = std::string("graph capture: ") + cudaGetErrorString(e);
+      return WTB_ECUDA;
+    }
+    op.capturing = true;
+    int r = body();
+    op.capturing = false;
+    e = cap.end(out);
+    if (r == WTB_OK && e != cudaSuccess) {
+      if (msg) *msg = std::string("graph capture: ") + cudaGetErrorString(e);
+      r = WTB_ECUDA;
+    }
+    return r;
+  };
+  auto add_while = [&](const std::vector<cudaGraphNode_t>& deps, cudaGraphConditionalHandle h, cudaGraphNode_t* node,
+                       cudaGraph_t* body) -> int {
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    CK(cudaGraphAddNode(node, G, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(), &np));
+    *body = np.conditional.phGraph_out[0];
+    return WTB_OK;
+  };
+  do {
+    cudaGraphConditionalHandle h1 = 0, h2 = 0;
+    if (cudaGraphConditionalHandleCreate(&h1, G, 0, cudaGraphCondAssignDefault) != cudaSuccess ||
+        (two_phase && cudaGraphConditionalHandleCreate(&h2, G, 0, cudaGraphCondAssignDefault) != cudaSuccess)) {
+      if (msg) *msg = "graph conditional handle creation failed";
+      rc = WTB_ECUDA;
+      break;
+    }
+    // set-up: unit vectors at the m lowest transition energies (+ deterministic noise), W = P = 0
+    rc = segment(G, {}, &tail, [&]() -> int {
+      lob_ctl_reset_kernel<<<1, 1, 0, s>>>(ctl, tol, 0);
+      ++g_launch_count;
+      CK(cudaMemset2DAsync(Sb, sizeof(cplx<S>) * ld, 0, sizeof(cplx<S>) * ld, dim, s));
+      CK(launch_select_lowest(diag, dim, m, idx, cand, s));
+      CK(launch_init_guess<S>(X, ld, dim, m, idx + 64 * m, 12345u, s));
+      return restart_from_x(h1);
+    });
+    if (rc) break;
+    cudaGraphNode_t wn;
+    cudaGraph_t body;
+    if ((rc = add_while(tail, h1, &wn, &body))) break;
+    long long c0 = g_launch_count.load();
+    if ((rc = segment(body, {}, nullptr, [&]() { return iteration(h1); }))) break;
+    body_launches[0] = g_launch_count.load() - c0;
+    tail.assign(1, wn);
+    if (two_phase) {
+      // second phase: the accurate operator; fresh AX from the (best) block, search directions dropped
+      op.begin_refine();
+      rc = segment(G, tail, &tail, [&]() -> int {
+        cond_copy_kernel<S><<<cp_grid, 256, 0, s>>>(&ctl->restore, Xbest, m, X, ld, m, dim);
+        ++g_launch_count;
+        lob_ctl_reset_kernel<<<1, 1, 0, s>>>(ctl, tol_refine, 1);
+        ++g_launch_count;
+        return restart_from_x(h2);
+      });
+      if (rc) break;
+      if ((rc = add_while(tail, h2, &wn, &body))) break;
+      c0 = g_launch_count.load();
+      if ((rc = segment(body, {}, nullptr, [&]() { return iteration(h2); }))) break;
+      body_launches[1] = g_launch_count.load() - c0;
+      tail.assign(1, wn);
+    }
+    // final FP64 Rayleigh-Ritz on a fresh application of the operator's most accurate arithmetic (the
+    // iteration's AX is a running linear combination of cheaper applications)
+    rc = segment(G, tail, &tail, [&]() -> int {
+      cond_copy_kernel<S><<<cp_grid, 256, 0, s>>>(&ctl->restore, Xbest, m, X, ld, m, dim);
+      ++g_launch_count;
       op.begin_refine();
       op.set_final(true);
-      const cudaError_t fe = op.apply(X, ld, 0, mm, AXs, ld, s);
+      const cudaError_t fe = op.apply(X, ld, 0, m, AX, ld, s);
       op.set_final(false);
       CK(fe);
-      CK((launch_convert_cols<S, double>(X, ld, X64, 2 * mm, mm, dim, s)));
-      CK((launch_convert_cols<S, double>(AXs, ld, X64 + mm, 2 * mm, mm, dim, s)));
-      r = rayleigh_ritz<double>(X64, X64 + mm, 2 * mm, mm, mm, dim, 1e-13, sm, partial, npart, st, s, msg, true);
+      CK((launch_convert_cols<S, double>(X, ld, X64, 2 * m, m, dim, s)));
+      CK((launch_convert_cols<S, double>(AX, ld, X64 + m, 2 * m, m, dim, s)));
+      int r = rayleigh_ritz<double>(X64, X64 + m, 2 * m, m, m, dim, 1e-13, sm, partial, npart, st, s, msg, true);
       if (r) return r;
       // Xout = X64 C[:, :nev]; residual = (AX64 C - Xout theta)
-      CK(launch_update<double>(X64, 2 * mm, mm, sm.C, mm, nev, dim, Xout, nev, 1.0, 0.0, s));
-      CK(launch_update<double>(X64 + mm, 2 * mm, mm, sm.C, mm, nev, dim, T64, nev, 1.0, 0.0, s));
+      CK(launch_update<double>(X64, 2 * m, m, sm.C, m, nev, dim, Xout, nev, 1.0, 0.0, s));
+      CK(launch_update<double>(X64 + m, 2 * m, m, sm.C, m, nev, dim, T64, nev, 1.0, 0.0, s));
       CK(launch_residual<double>(T64, nev, Xout, nev, sm.theta, nev, dim, T64, nev, partial, npart, norms2, s));
-      std::vector<double> th(nev);
-      CK(cudaMemcpyAsync(th.data(), sm.theta, sizeof(double) * nev, cudaMemcpyDeviceToHost, s));
-      CK(cudaMemcpyAsync(h_norm.data(), norms2, sizeof(double) * nev, cudaMemcpyDeviceToHost, s));
-      CK(cudaStreamSynchronize(s));
-      DevStatus hst;
-      CK(cudaMemcpy(&hst, st, sizeof(hst), cudaMemcpyDeviceToHost));
-      if (hst.code) {
-        if (msg) *msg = "device status " + std::to_string(hst.code) + " in the final Rayleigh-Ritz";
-        return hst.code >= 400 && hst.code < 500 ? WTB_ETIMEOUT : WTB_ENOCONV;
-      }
-      double maxrel = 0.0, shift = 0.0;
-      for (int j = 0; j < nev; ++j) {
-        const double rel = std::sqrt(std::max(h_norm[j], 0.0)) / std::max(std::fabs(th[j]), 1e-12);
-        if (!std::isfinite(rel) || !std::isfinite(th[j])) {
-          if (msg) *msg = "non-finite eigenpair after the final Rayleigh-Ritz";
-          return WTB_ENAN;
-        }
-        maxrel = std::max(maxrel, rel);
-        shift = std::max(shift, std::fabs(th[j] - h_theta[j]));
-      }
-      *E = th;
-      if (stats) {
-        stats->max_rel_residual = maxrel;
-        stats->refine_shift_max = shift;
-        stats->matvec_columns = op.matvec_columns;
-      }
+      return WTB_OK;
+    });
+    if (rc) break;
+    if (cudaGraphInstantiate(&GX, G, 0) != cudaSuccess) {
+      if (msg) *msg = "graph instantiation failed";
+      rc = WTB_ECUDA;
+      break;
     }
-    if (!converged) {
-      if (msg) *msg = "eigensolver did not converge in " + std::to_string(maxit) + " iterations";
-      return WTB_ENOCONV;
+    if (cudaGraphLaunch(GX, s) != cudaSuccess) {
+      if (msg) *msg = "graph launch failed";
+      rc = WTB_ECUDA;
+      break;
     }
-    return WTB_OK;
+  } while (false);
+  if (rc) {
+    if (GX) cudaGraphExecDestroy(GX);
+    if (G) cudaGraphDestroy(G);
+    return rc;
   }
-oom:
-  if (msg) *msg = std::string("device allocation failed: ") + cudaGetErrorString(err);
-  return WTB_ENOMEM;
+  ws.graph = G;
+  ws.graph_exec = GX;
+  ws.graph_key = key;
+  ws.graph_body_launches[0] = body_launches[0];
+  ws.graph_body_launches[1] = body_launches[1];
+  ws.graph_launches = g_launch_count.load() - captured0;
+  }
+  std::vector<double> th(nev), th_it(nev), nrm(nev);
+  LobCtl hc;
+  CK(cudaMemcpyAsync(th.data(), sm.theta, sizeof(double) * nev, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(th_it.data(), th_dev, sizeof(double) * nev, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(nrm.data(), norms2, sizeof(double) * nev, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&hc, ctl, sizeof(hc), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  DevStatus hst;
+  CK(cudaMemcpy(&hst, st, sizeof(hst), cudaMemcpyDeviceToHost));
+  {
+    const int it2 = two_phase ? hc.it : 0, it1 = hc.total_it - it2;
+    g_launch_count += body_launches[0] * (it1 - 1) + (two_phase ? body_launches[1] * (it2 - 1) : 0);
+  }
+  if (stats) {
+    stats->iterations = hc.total_it;
+    stats->launches = 0;
+    stats->matvec_columns = (long)m * (hc.total_it + (two_phase ? 3 : 2));
+  }
+  if (hst.code) {
+    if (msg) *msg = "device status " + std::to_string(hst.code) + " during the eigensolve";
+    return hst.code >= 400 && hst.code < 500 ? WTB_ETIMEOUT : WTB_ENOCONV;
+  }
+  if (hc.failed == WTB_ENAN) {
+    if (msg) *msg = "non-finite residual in the eigensolve";
+    return WTB_ENAN;
+  }
+  double maxrel = 0.0, shift = 0.0;
+  for (int j = 0; j < nev; ++j) {
+    const double rel = std::sqrt(std::max(nrm[j], 0.0)) / std::max(std::fabs(th[j]), 1e-12);
+    if (!std::isfinite(rel) || !std::isfinite(th[j])) {
+      if (msg) *msg = "non-finite eigenpair after the final Rayleigh-Ritz";
+      return WTB_ENAN;
+    }
+    maxrel = std::max(maxrel, rel);
+    shift = std::max(shift, std::fabs(th[j] - th_it[j]));
+  }
+  *E = th;
+  if (stats) {
+    stats->max_rel_residual = maxrel;
+    stats->refine_shift_max = shift;
+  }
+  if (!hc.converged) {
+    if (msg) *msg = "eigensolver did not converge in " + std::to_string(maxit) + " iterations";
+    return WTB_ENOCONV;
+  }
+  return WTB_OK;
 }
 
 template int lobpcg_solve<float>(Operator<float>&, const double*, int, int, int, double, int, Workspace&, DevStatus*,

@@ -1,6 +1,7 @@
 // Lowest-exciton eigensolver (replaces SLEPc Krylov-Schur in slepc_solver,
 // src/module_slepc_solver.F90:12-97) and the BSE operators it drives.
 #pragma once
+#include <cstdint>
 #include <map>
 #include <memory>
 #include <string>
@@ -39,8 +40,23 @@ struct DevBuf {
 
 // Named device buffers.  get() sets *err only when an allocation fails, so one check after a run of
 // get() calls sees any failure in the run (callers start with err = cudaSuccess).
+// The workspace also keeps the last eigensolver graph (instantiated), reused while its signature (sizes,
+// parameters, operator configuration and every device address it was captured with) is unchanged.
 struct Workspace {
   std::map<std::string, std::unique_ptr<DevBuf>> bufs;
+  uint64_t graph_key = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  long long graph_body_launches[2] = {0, 0};
+  long long graph_launches = 0;  // kernels captured in the whole graph
+  void drop_graph() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (graph) cudaGraphDestroy(graph);
+    graph_exec = nullptr;
+    graph = nullptr;
+    graph_key = 0;
+  }
+  ~Workspace() { drop_graph(); }
   template <class T>
   T* get(const std::string& name, size_t count, cudaError_t* err, bool zero = false) {
     auto& b = bufs[name];
@@ -68,6 +84,10 @@ struct Operator {
   // on: the next applications define the reported eigenvalues (final Rayleigh-Ritz); an operator may use
   // a slower, more accurate accumulation for them
   virtual void set_final(bool on) { (void)on; }
+  // true while launches are being captured into a graph (no event timing then)
+  bool capturing = false;
+  // everything a captured application depends on besides buffer contents (configuration and addresses)
+  virtual void signature(std::vector<uint64_t>* sig) const = 0;
   long matvec_columns = 0;
 };
 
@@ -78,6 +98,11 @@ struct DenseOperator : Operator<S> {
   cudaError_t apply(const cplx<S>* X, int ldx, int c0, int ncol, cplx<S>* Y, int ldy, cudaStream_t s) override {
     this->matvec_columns += ncol;
     return launch_dense_mv<S>(H, dim, X + c0, ldx, Y + c0, ldy, ncol, s);
+  }
+  void signature(std::vector<uint64_t>* sig) const override {
+    sig->push_back(1);
+    sig->push_back((uint64_t)(uintptr_t)H);
+    sig->push_back((uint64_t)dim);
   }
 };
 
@@ -139,6 +164,19 @@ struct MatFreeOperator : Operator<S> {
     npairs = npairs_refine;
     return true;
   }
+  void signature(std::vector<uint64_t>* sig) const override {
+    const uint64_t v[] = {2, (uint64_t)kind, (uint64_t)nk, (uint64_t)nv, (uint64_t)nc, (uint64_t)w, (uint64_t)nbmax,
+                          (uint64_t)nslices, (uint64_t)npairs, (uint64_t)npairs_refine, (uint64_t)kchunk_final,
+                          (uint64_t)Mpad, (uint64_t)Kpad, (uint64_t)Npad, (uint64_t)(uintptr_t)vec_win,
+                          (uint64_t)(uintptr_t)dE, (uint64_t)(uintptr_t)Vs, (uint64_t)(uintptr_t)Zs,
+                          (uint64_t)(uintptr_t)Vr, (uint64_t)(uintptr_t)Zr, (uint64_t)(uintptr_t)Tm,
+                          (uint64_t)(uintptr_t)st};
+    sig->insert(sig->end(), v, v + sizeof(v) / sizeof(v[0]));
+  }
+  // launches the contraction of an ncol-column application (the first phase's slice products) reps times
+  // with CUDA events around each, into prof (the eigensolve itself runs as one graph launch)
+  int npairs0 = 0;
+  cudaError_t time_contraction(int reps, int ncol, cudaStream_t s);
   // tensor-core kind: K blocks per accumulation range in the final applications (0: one range)
   int kchunk_final = 4;
   bool final_apply = false;

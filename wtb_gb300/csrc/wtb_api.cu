@@ -374,6 +374,7 @@ int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob, 
   // for the final refinement
   op->nslices = 3;
   op->npairs = x6 ? 6 : 3;
+  op->npairs0 = op->npairs;
   op->npairs_refine = 6;
   const int pa6[6] = {0, 0, 1, 0, 1, 2}, pb6[6] = {0, 1, 0, 2, 1, 0};
   for (int i = 0; i < 6; ++i) {
@@ -422,6 +423,15 @@ int run_solve(wtb_ctx* c, const wtb_bse_params* p, std::vector<double>* E, wtb_t
   if (!ob.msg.empty()) msg += " (" + ob.msg + ")";
   CKC(cudaEventRecord(ev[2], c->s));
   CKC(cudaEventSynchronize(ev[2]));
+  // the eigensolve is one graph launch: the live profile of the contraction is taken after it, on the same
+  // operator data (three launches of the iteration-phase contraction, CUDA events on the context's stream)
+  if (rc == WTB_OK && c->prof.on && p->op == WTB_OP_MATFREE) {
+    if (ob.o64) {
+      if (auto* mf = dynamic_cast<MatFreeOperator<double>*>(ob.o64.get())) CKC(mf->time_contraction(3, m, c->s));
+    } else if (auto* mf = dynamic_cast<MatFreeOperator<float>*>(ob.o32.get())) {
+      CKC(mf->time_contraction(3, m, c->s));
+    }
+  }
   float t01 = 0, t12 = 0;
   cudaEventElapsedTime(&t01, ev[0], ev[1]);
   cudaEventElapsedTime(&t12, ev[1], ev[2]);
