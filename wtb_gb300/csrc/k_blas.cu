@@ -327,123 +327,91 @@ __global__ void __launch_bounds__(256) heev_small_kernel(const zd* __restrict__ 
   }
 }
 
-// Orthonormalising basis of the Gram matrix M = S^H S (n x n, complex(8)) by pivoted Cholesky in precision S:
-// with D = diag(M) and Ms = D^-1/2 M D^-1/2, pivots are taken largest residual diagonal first while it exceeds
-// drop (relative to Ms's unit diagonal); for the r chosen columns P, Ms[P,P] = R^H R and
+// Orthonormalising basis of the Gram matrix M = S^H S (n x n, complex(8)) by Cholesky in precision S, in the
+// basis's own order ([X W P]: the current block first) with deflation: with D = diag(M) and
+// Ms = D^-1/2 M D^-1/2, column k is kept when its residual diagonal (its squared distance from the span of the
+// kept columns before it) exceeds drop, and dropped otherwise.  For the r kept columns P, Ms[P,P] = R^H R and
 // B = D_P^-1/2 R^-1 makes S B orthonormal.  B (n x n, leading dimension ldb) holds those r columns first and
-// zeros elsewhere; *r_out = r.  Dropped columns are numerically in the span of the kept ones (the
-// directions SVQB drops by eigenvalue are dropped here by residual norm).
+// zeros elsewhere; *r_out = r.  Two barriers a step; the CTA is a 16 x 16 thread grid over the trailing matrix.
 template <class S>
 __global__ void __launch_bounds__(256) pchol_basis_kernel(const zd* __restrict__ Mg, int ldm, int n, double drop,
                                                           zd* __restrict__ B, int ldb, int* __restrict__ r_out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x, nt = blockDim.x, tx = tid & 15, ty = tid >> 4;
   const int lds = n + 1;
-  cplx<S>* W = reinterpret_cast<cplx<S>*>(smem_raw);  // residual matrix (original index order)
-  cplx<S>* R = W + (size_t)n * lds;                    // R[k][original column], rows in pivot order
+  cplx<S>* W = reinterpret_cast<cplx<S>*>(smem_raw);  // residual matrix
+  cplx<S>* R = W + (size_t)n * lds;                    // R[k][column], rows in kept order
   S* dinv = reinterpret_cast<S*>(R + (size_t)n * lds);
   int* perm = reinterpret_cast<int*>(dinv + n);
-  int* chosen = perm + n;
-  __shared__ int s_r, s_piv;
+  __shared__ int s_r;
   for (int i = tid; i < n; i += nt) {
     const double m = Mg[(size_t)i * ldm + i].re;
     dinv[i] = m > 1e-300 ? (S)(1.0 / sqrt(m)) : (S)0;
-    chosen[i] = 0;
   }
   __syncthreads();
-  for (int q = tid; q < n * n; q += nt) {
-    const int i = q / n, j = q % n;
-    const zd a = Mg[(size_t)i * ldm + j], b = Mg[(size_t)j * ldm + i];
-    const S sc = dinv[i] * dinv[j];
-    W[(size_t)i * lds + j] = mk<S>((S)(0.5 * (a.re + b.re)) * sc, i == j ? (S)0 : (S)(0.5 * (a.im - b.im)) * sc);
-  }
-  if (tid == 0) s_r = n;
-  __syncthreads();
-  for (int k = 0; k < n; ++k) {
-    if (warp == 0) {
-      S best = (S)-1;
-      int bi = -1;
-      for (int i = lane; i < n; i += 32) {
-        const S v = chosen[i] ? (S)-1 : W[(size_t)i * lds + i].re;
-        if (v > best) {
-          best = v;
-          bi = i;
-        }
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const S ob = __shfl_xor_sync(0xffffffffu, best, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (ob > best || (ob == best && oi >= 0 && (bi < 0 || oi < bi))) {
-          best = ob;
-          bi = oi;
-        }
-      }
-      if (lane == 0) {
-        if (bi < 0 || !(best > (S)drop)) {
-          s_r = k;
-          s_piv = -1;
-        } else {
-          s_piv = bi;
-          perm[k] = bi;
-          chosen[bi] = 1;
-        }
-      }
+  for (int i = ty; i < n; i += 16)
+    for (int j = tx; j < n; j += 16) {
+      const zd a = Mg[(size_t)i * ldm + j], b = Mg[(size_t)j * ldm + i];
+      const S sc = dinv[i] * dinv[j];
+      W[(size_t)i * lds + j] = mk<S>((S)(0.5 * (a.re + b.re)) * sc, i == j ? (S)0 : (S)(0.5 * (a.im - b.im)) * sc);
     }
-    __syncthreads();
-    const int pv = s_piv;
-    if (pv < 0) break;
-    const S rkk = sqrt(W[(size_t)pv * lds + pv].re);
-    // row k of R: R[k][j] = W[pv][j] / rkk for the unchosen j, rkk at the pivot
+  __syncthreads();
+  int r = 0;  // kept so far (uniform across the block)
+  for (int k = 0; k < n; ++k) {
+    const S dk = W[(size_t)k * lds + k].re;
+    if (!(dk > (S)drop)) continue;  // uniform decision: every thread reads the same settled value
+    const S rkk = sqrt(dk), irk = (S)1 / rkk;
+    // row r of R: columns k+1.. of the residual row k, scaled
     for (int j = tid; j < n; j += nt) {
       cplx<S> v = mk<S>(0, 0);
-      if (j == pv)
+      if (j == k)
         v = mk<S>(rkk, 0);
-      else if (!chosen[j])
-        v = mk<S>(W[(size_t)pv * lds + j].re / rkk, W[(size_t)pv * lds + j].im / rkk);
-      R[(size_t)k * lds + j] = v;
+      else if (j > k)
+        v = mk<S>(W[(size_t)k * lds + j].re * irk, W[(size_t)k * lds + j].im * irk);
+      R[(size_t)r * lds + j] = v;
     }
+    if (tid == 0) perm[r] = k;
     __syncthreads();
-    // Schur complement on the unchosen rows and columns: W[i][j] -= conj(R[k][i]) R[k][j]
-    for (int q = tid; q < n * n; q += nt) {
-      const int i = q / n, j = q % n;
-      if (chosen[i] || chosen[j]) continue;
-      const cplx<S> ri = R[(size_t)k * lds + i], rj = R[(size_t)k * lds + j];
-      cplx<S>& w = W[(size_t)i * lds + j];
-      w.re -= ri.re * rj.re + ri.im * rj.im;
-      w.im -= ri.re * rj.im - ri.im * rj.re;
+    // Schur complement on the trailing block: W[i][j] -= conj(R[r][i]) R[r][j]
+    for (int i = k + 1 + ty; i < n; i += 16) {
+      const cplx<S> ri = R[(size_t)r * lds + i];
+      for (int j = k + 1 + tx; j < n; j += 16) {
+        const cplx<S> rj = R[(size_t)r * lds + j];
+        cplx<S>& w = W[(size_t)i * lds + j];
+        w.re -= ri.re * rj.re + ri.im * rj.im;
+        w.im -= ri.re * rj.im - ri.im * rj.re;
+      }
     }
+    ++r;
     __syncthreads();
   }
-  const int r = s_r;
-  // R^-1 (r x r, upper triangular in pivot order), one thread per column c, stored over W's rows
-  cplx<S>* Ri = W;  // Ri[k][c], leading dimension lds
+  if (tid == 0) s_r = r;
+  __syncthreads();
+  // R^-1 (r x r, upper triangular in kept order), one thread per column c, stored over W's rows
+  cplx<S>* Ri = W;
   for (int c = tid; c < r; c += nt) {
     for (int k = c + 1; k < r; ++k) Ri[(size_t)k * lds + c] = mk<S>(0, 0);
-    const S rcc = R[(size_t)c * lds + perm[c]].re;
-    Ri[(size_t)c * lds + c] = mk<S>((S)1 / rcc, 0);
+    Ri[(size_t)c * lds + c] = mk<S>((S)1 / R[(size_t)c * lds + perm[c]].re, 0);
     for (int k = c - 1; k >= 0; --k) {
       cplx<S> acc = mk<S>(0, 0);
       for (int l = k + 1; l <= c; ++l) cfma(acc, R[(size_t)k * lds + perm[l]], Ri[(size_t)l * lds + c]);
-      const S rkk = R[(size_t)k * lds + perm[k]].re;
-      Ri[(size_t)k * lds + c] = mk<S>(-acc.re / rkk, -acc.im / rkk);
+      const S irkk = (S)1 / R[(size_t)k * lds + perm[k]].re;
+      Ri[(size_t)k * lds + c] = mk<S>(-acc.re * irkk, -acc.im * irkk);
     }
   }
   __syncthreads();
   // B[perm[k]][c] = dinv[perm[k]] Ri[k][c] (k <= c < r); everything else zero
-  for (int q = tid; q < n * n; q += nt) {
-    const int i = q / n, c = q % n;
-    B[(size_t)i * ldb + c] = mk<double>(0.0, 0.0);
-  }
+  for (int i = ty; i < n; i += 16)
+    for (int c = tx; c < n; c += 16) B[(size_t)i * ldb + c] = mk<double>(0.0, 0.0);
   __syncthreads();
-  for (int q = tid; q < r * r; q += nt) {
-    const int k = q / r, c = q % r;
-    if (k > c) continue;
-    const int i = perm[k];
-    const cplx<S> v = Ri[(size_t)k * lds + c];
-    B[(size_t)i * ldb + c] = mk<double>((double)v.re * (double)dinv[i], (double)v.im * (double)dinv[i]);
-  }
-  if (tid == 0) *r_out = r;
+  for (int k = ty; k < r; k += 16)
+    for (int c = tx; c < r; c += 16) {
+      if (k > c) continue;
+      const int i = perm[k];
+      const cplx<S> v = Ri[(size_t)k * lds + c];
+      B[(size_t)i * ldb + c] = mk<double>((double)v.re * (double)dinv[i], (double)v.im * (double)dinv[i]);
+    }
+  if (tid == 0) *r_out = s_r;
 }
 
 }  // namespace
@@ -538,7 +506,7 @@ cudaError_t launch_heev_small(const zd* A, int lda, const int* nptr, int nmax, i
 template <class S>
 cudaError_t launch_pchol_basis(const zd* M, int ldm, int n, double drop, zd* B, int ldb, int* r_out, cudaStream_t s) {
   if (n < 1 || n > 96) return cudaErrorInvalidValue;
-  const size_t smem = (size_t)2 * n * (n + 1) * sizeof(cplx<S>) + (size_t)n * sizeof(S) + (size_t)2 * n * sizeof(int) + 64;
+  const size_t smem = (size_t)2 * n * (n + 1) * sizeof(cplx<S>) + (size_t)n * sizeof(S) + (size_t)n * sizeof(int) + 64;
   if (smem > 220 * 1024) return cudaErrorInvalidValue;
   cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(pchol_basis_kernel<S>), smem);
   if (e != cudaSuccess) return e;

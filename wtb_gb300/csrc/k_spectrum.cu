@@ -17,10 +17,14 @@ namespace {
 
 constexpr int kOscRows = 256;
 
-// partial[blk][n][5] = sum over this block's rows of A[j][n] * h_a[j]
+// Partial sums s_a(n) = sum_r A(r, n) h_a(r) over a CTA's kOscRows rows, a = x y z sp sm.  The eight warps
+// take interleaved rows, a lane takes exciton n (lanes beyond nev idle; nev > 32 loops), and the warps'
+// sums are added in a fixed order through shared memory: the FP64 work is spread over the SM's four
+// schedulers instead of the few threads of one warp.
 __global__ void __launch_bounds__(256) osc_partial_kernel(const zd* __restrict__ A, int lda, int nev, int dim,
                                                           const zd* __restrict__ hr, double* __restrict__ partial) {
   __shared__ zd hs[5][kOscRows];
+  __shared__ double red[8][32][10];
   const int r0 = blockIdx.x * kOscRows;
   const int nr = min(kOscRows, dim - r0);
   for (int e = threadIdx.x; e < 5 * kOscRows; e += blockDim.x) {
@@ -28,18 +32,32 @@ __global__ void __launch_bounds__(256) osc_partial_kernel(const zd* __restrict__
     hs[a][r] = r < nr ? hr[(size_t)a * dim + r0 + r] : mk<double>(0.0, 0.0);
   }
   __syncthreads();
-  for (int n = threadIdx.x; n < nev; n += blockDim.x) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int n0 = 0; n0 < nev; n0 += 32) {
+    const int n = n0 + lane;
     zd acc[5];
+#pragma unroll
     for (int a = 0; a < 5; ++a) acc[a] = mk<double>(0.0, 0.0);
-    for (int r = 0; r < nr; ++r) {
-      const zd x = A[(size_t)(r0 + r) * lda + n];
-      for (int a = 0; a < 5; ++a) cfma(acc[a], x, hs[a][r]);
-    }
-    double* out = partial + ((size_t)blockIdx.x * nev + n) * 10;
+    if (n < nev)
+      for (int r = warp; r < nr; r += 8) {
+        const zd x = A[(size_t)(r0 + r) * lda + n];
+#pragma unroll
+        for (int a = 0; a < 5; ++a) cfma(acc[a], x, hs[a][r]);
+      }
+#pragma unroll
     for (int a = 0; a < 5; ++a) {
-      out[2 * a] = acc[a].re;
-      out[2 * a + 1] = acc[a].im;
+      red[warp][lane][2 * a] = acc[a].re;
+      red[warp][lane][2 * a + 1] = acc[a].im;
     }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 32 * 10; e += blockDim.x) {
+      const int l = e / 10, q = e % 10;
+      if (n0 + l >= nev) continue;
+      double t = 0.0;
+      for (int w = 0; w < 8; ++w) t += red[w][l][q];
+      partial[((size_t)blockIdx.x * nev + n0 + l) * 10 + q] = t;
+    }
+    __syncthreads();
   }
 }
 

@@ -90,14 +90,12 @@ __device__ void tridiag_cta(cplx<S>* A, int lda, int n, S* d, S* e, cplx<S>* tau
       continue;
     }
     const cplx<S> tj = tau[j];
-    // p = tau A22 v (A22 = rows/columns j+1..n-1), one warp per row
-    for (int r = warp; r < L; r += nw) {
+    // p = tau A22 v (A22 = rows/columns j+1..n-1), one thread per row (no reduction on the critical path)
+    for (int r = tid; r < L; r += nt) {
       const cplx<S>* row = A + (size_t)(j + 1 + r) * lda + (j + 1);
       cplx<S> acc = mk<S>(0, 0);
-      for (int c = lane; c < L; c += 32) cfma(acc, row[c], vcol[(size_t)c * lda]);
-      acc.re = warp_allsum(acc.re);
-      acc.im = warp_allsum(acc.im);
-      if (lane == 0) p[r] = cmul(tj, acc);
+      for (int c = 0; c < L; ++c) cfma(acc, row[c], vcol[(size_t)c * lda]);
+      p[r] = cmul(tj, acc);
     }
     __syncthreads();
     // K = -1/2 tau (p^H v), every warp for itself; w = p + K v;  A22 -= v w^H + w v^H
@@ -228,16 +226,19 @@ __device__ void tridiag_eigvecs_cta(const cplx<S>* A, int lda, int n, int nwant,
     cl[k] = s0;
   }
   for (int k = tid; k < nwant; k += nt) {
+    // Dv holds the reciprocal pivots (one division per pivot; the solves multiply)
     const S lk = lam[k];
     S Dp = d[0] - lk;
     if (fabs(Dp) < tiny) Dp = tiny;
-    Dv[k] = Dp;
+    S Dr = (S)1 / Dp;
+    Dv[k] = Dr;
     for (int i = 1; i < n; ++i) {
-      const S l = e[i - 1] / Dp;
+      const S l = e[i - 1] * Dr;
       Lv[(size_t)(i - 1) * nwant + k] = l;
       Dp = (d[i] - lk) - l * e[i - 1];
       if (fabs(Dp) < tiny) Dp = tiny;
-      Dv[(size_t)i * nwant + k] = Dp;
+      Dr = (S)1 / Dp;
+      Dv[(size_t)i * nwant + k] = Dr;
     }
     // start: deterministic pseudo-random entries in [-1, 1) (distinct for every k)
     for (int i = 0; i < n; ++i) {
@@ -255,7 +256,7 @@ __device__ void tridiag_eigvecs_cta(const cplx<S>* A, int lda, int n, int nwant,
         Z[(size_t)i * nwant + k] = v;
         y = v;
       }
-      for (int i = 0; i < n; ++i) Z[(size_t)i * nwant + k] /= Dv[(size_t)i * nwant + k];
+      for (int i = 0; i < n; ++i) Z[(size_t)i * nwant + k] *= Dv[(size_t)i * nwant + k];
       S x = Z[(size_t)(n - 1) * nwant + k];
       for (int i = n - 2; i >= 0; --i) {
         const S v = Z[(size_t)i * nwant + k] - Lv[(size_t)i * nwant + k] * x;
@@ -265,11 +266,12 @@ __device__ void tridiag_eigvecs_cta(const cplx<S>* A, int lda, int n, int nwant,
       S nrm = 0, mx = 0;
       for (int i = 0; i < n; ++i) mx = fmax(mx, fabs(Z[(size_t)i * nwant + k]));
       if (!(mx > (S)0)) mx = (S)1;
+      const S imx = (S)1 / mx;
       for (int i = 0; i < n; ++i) {
-        const S v = Z[(size_t)i * nwant + k] / mx;
+        const S v = Z[(size_t)i * nwant + k] * imx;
         nrm += v * v;
       }
-      const S sc = (S)1 / (mx * sqrt(nrm));
+      const S sc = imx / sqrt(nrm);
       for (int i = 0; i < n; ++i) Z[(size_t)i * nwant + k] *= sc;
     }
   }

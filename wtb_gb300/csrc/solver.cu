@@ -3,8 +3,9 @@
 // LOBPCG (Knyazev's locally optimal block preconditioned CG) with
 //   - the diagonal (transition-energy) preconditioner |diag(H) - theta|^-1, floored;
 //   - soft locking: converged columns keep their place in X but get no new search direction;
-//   - orthonormalisation of the basis [X W P] by pivoted Cholesky of its scaled Gram matrix (directions
-//     whose residual norm falls below tau are dropped) followed by Rayleigh-Ritz on the kept directions,
+//   - orthonormalisation of the basis [X W P] by Cholesky of its scaled Gram matrix in the basis's order with
+//     deflation (directions whose residual norm falls below tau are dropped) followed by Rayleigh-Ritz on the
+//     kept directions,
 //     whose small eigenproblem is solved by Householder tridiagonalisation, bisection and inverse
 //     iteration on one CTA (small_eig.cuh);
 //   - all projected (3m x 3m) matrices kept in complex(8) on the device.
@@ -203,8 +204,9 @@ struct Small {
 };
 
 // Rayleigh-Ritz on the basis Sb (dim x nb, ld) with ASb = H Sb: returns C (nb x m) and theta (m).
-// Orthonormalisation: pivoted Cholesky of the scaled Gram matrix (directions whose residual diagonal falls
-// below tau are dropped; the r kept ones come first in B); the projected r x r problem B^H G B is solved
+// Orthonormalisation: Cholesky of the scaled Gram matrix in [X W P] order with deflation (directions whose
+// residual diagonal falls below tau are dropped; the r kept ones come first in B); the projected r x r
+// problem B^H G B is solved
 // by the tridiagonal route (small_eig.cuh).  The small problems run in precision S, or FP64 for
 // small_in_fp64.  A missing Ritz pair (r < m) has theta = 1e30 and a zero column in C.
 template <class S>
@@ -236,7 +238,7 @@ int rayleigh_ritz(const cplx<S>* Sb, const cplx<S>* ASb, int ld, int nb, int m, 
 // final FP64 Rayleigh-Ritz.  The decisions the host used to take every iteration (soft locking,
 // convergence, the stagnation and breakdown guards, the iteration cap) are taken by lob_control_kernel,
 // which sets the loop's condition with cudaGraphSetConditional; the host synchronises once per solve.
-// The basis is always [X W P] (3m columns): W and P start at zero and the pivoted-Cholesky
+// The basis is always [X W P] (3m columns): W and P start at zero and the Cholesky
 // orthonormalisation drops zero columns, so the first iteration needs no separate 2m-column path.
 
 struct LobCtl {
@@ -273,7 +275,8 @@ __global__ void lob_ctl_reset_kernel(LobCtl* c, double tol, int keep_total) {
 // Monitor lines follow the reference's MyEPSMonitor (src/module_slepc_solver.F90:101-116).
 __global__ void lob_control_kernel(LobCtl* c, const double* __restrict__ norms2, const double* __restrict__ theta,
                                    int m, int nev, int maxit, int reduced, int* __restrict__ active,
-                                   const DevStatus* __restrict__ st, cudaGraphConditionalHandle h, int monitor) {
+                                   const DevStatus* __restrict__ st, cudaGraphConditionalHandle h, int in_graph,
+                                   int monitor) {
   const int lane = threadIdx.x;
   const double tol = c->tol;
   double rel = 0.0;
@@ -340,7 +343,7 @@ __global__ void lob_control_kernel(LobCtl* c, const double* __restrict__ norms2,
     c->total_it += 1;
   }
   c->stop = stop;
-  cudaGraphSetConditional(h, stop ? 0u : 1u);
+  if (in_graph) cudaGraphSetConditional(h, stop ? 0u : 1u);
 }
 
 // dst[:, 0:ncol] = src[:, 0:ncol] when *flag is set
@@ -356,39 +359,57 @@ __global__ void cond_copy_kernel(const int* __restrict__ flag, const cplx<S>* __
   }
 }
 
-// In place, row by row (one warp per row): X <- [X W P] C and P <- [W P] C[m:3m, :] for the basis and for
-// its image under H (the row is read into registers before any of it is written).
+// In place: X <- [X W P] C and P <- [W P] C[m:3m, :] for the basis and for its image under H.  A CTA stages
+// kUpdRows rows of the block in shared memory (so the in-place writes cannot overtake reads), then threads
+// (row, group of four output columns) form their outputs from the staged row and C.
+constexpr int kUpdRows = 32;
 template <class S>
 __global__ void __launch_bounds__(256) lob_update_kernel(cplx<S>* __restrict__ Sb, cplx<S>* __restrict__ ASb, int ld,
                                                          int m, const zd* __restrict__ C, int dim) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  cplx<S>* Cs = reinterpret_cast<cplx<S>*>(smem_raw);  // [3m][m]
   const int nb = 3 * m;
+  cplx<S>* Cs = reinterpret_cast<cplx<S>*>(smem_raw);  // [3m][m]
+  cplx<S>* Rs = Cs + nb * m;                           // [kUpdRows][3m]
   for (int e = threadIdx.x; e < nb * m; e += blockDim.x) Cs[e] = mk<S>((S)C[e].re, (S)C[e].im);
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (long r = (long)blockIdx.x * nw + warp; r < dim; r += (long)gridDim.x * nw) {
+  const int ngrp = (m + 3) >> 2;       // groups of 4 output columns
+  const int items = kUpdRows * ngrp;   // (row, group) pairs per pass
+  for (long r0 = (long)blockIdx.x * kUpdRows; r0 < dim; r0 += (long)gridDim.x * kUpdRows) {
+    const int nr = (int)min((long)kUpdRows, dim - r0);
     for (int which = 0; which < 2; ++which) {
-      cplx<S>* row = (which ? ASb : Sb) + r * ld;
-      cplx<S> v[3];
+      cplx<S>* base = (which ? ASb : Sb) + r0 * ld;
+      __syncthreads();
+      for (int e = threadIdx.x; e < nr * nb; e += blockDim.x) {
+        const int rr = e / nb, c = e - rr * nb;
+        Rs[rr * nb + c] = base[(size_t)rr * ld + c];
+      }
+      __syncthreads();
+      for (int it = threadIdx.x; it < items; it += blockDim.x) {
+        const int rr = it / ngrp, g = it - rr * ngrp;
+        if (rr >= nr) continue;
+        const int j0 = g * 4;
+        cplx<S> x[4], pn[4];
 #pragma unroll
-      for (int q = 0; q < 3; ++q) v[q] = lane + 32 * q < nb ? row[lane + 32 * q] : mk<S>(0, 0);
-      cplx<S> x = mk<S>(0, 0), pn = mk<S>(0, 0);
-      const int j = lane < m ? lane : 0;
-      for (int i = 0; i < nb; ++i) {
-        const int q = i >> 5;
-        const cplx<S> src = q == 0 ? v[0] : (q == 1 ? v[1] : v[2]);
-        const cplx<S> ri = mk<S>(__shfl_sync(0xffffffffu, src.re, i & 31), __shfl_sync(0xffffffffu, src.im, i & 31));
-        const cplx<S> c = Cs[i * m + j];
-        cfma(x, ri, c);
-        if (i >= m) cfma(pn, ri, c);
+        for (int q = 0; q < 4; ++q) x[q] = pn[q] = mk<S>(0, 0);
+        const cplx<S>* row = Rs + rr * nb;
+        for (int i = 0; i < nb; ++i) {
+          const cplx<S> ri = row[i];
+          const cplx<S>* crow = Cs + i * m + j0;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            if (j0 + q < m) {
+              cfma(x[q], ri, crow[q]);
+              if (i >= m) cfma(pn[q], ri, crow[q]);
+            }
+          }
+        }
+        cplx<S>* out = base + (size_t)rr * ld;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (j0 + q < m) {
+            out[j0 + q] = x[q];
+            out[2 * m + j0 + q] = pn[q];
+          }
       }
-      __syncwarp();
-      if (lane < m) {
-        row[lane] = x;
-        row[2 * m + lane] = pn;
-      }
-      __syncwarp();
     }
   }
 }
@@ -472,14 +493,19 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
   const bool reduced = sizeof(S) == 4;
   const bool monitor = std::getenv("WTB_EPS_MONITOR") != nullptr;
   const bool two_phase = tol_refine > 0.0 && tol_refine < tol;
-  const size_t upd_smem = (size_t)nb * m * sizeof(cplx<S>);
-  const int upd_grid = std::max(1, std::min(152 * 8, (dim + 7) / 8));
+  // WTB_SOLVER_STREAM: the same kernels launched directly on the stream, the host reading the loop state
+  // between iterations (for kernel-level profilers, which do not replay kernels inside conditional graph
+  // bodies); the default runs the whole solve as one graph launch
+  const bool stream_mode = std::getenv("WTB_SOLVER_STREAM") != nullptr;
+  const size_t upd_smem = (size_t)(nb * m + kUpdRows * nb) * sizeof(cplx<S>);
+  const int upd_grid = std::max(1, std::min(152 * 8, (dim + kUpdRows - 1) / kUpdRows));
   const unsigned cp_grid = (unsigned)std::max(1, std::min(152 * 4, (int)(((long)dim * m + 255) / 256)));
 
   // the pieces of one iteration, as stream launches (captured below)
   auto rr_and_update = [&]() -> int {
     int r = rayleigh_ritz<S>(Sb, ASb, ld, nb, m, dim, tau, sm, partial, npart, st, s, msg, false);
     if (r) return r;
+    CK(raise_smem_limit(reinterpret_cast<const void*>(lob_update_kernel<S>), upd_smem));
     lob_update_kernel<S><<<upd_grid, 256, upd_smem, s>>>(Sb, ASb, ld, m, sm.C, dim);
     ++g_launch_count;
     CK(cudaGetLastError());
@@ -489,7 +515,7 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
   auto check_and_decide = [&](cudaGraphConditionalHandle h) -> int {
     CK(launch_residual<S>(AX, ld, X, ld, th_dev, m, dim, W, ld, partial, npart, norms2, s));
     lob_control_kernel<<<1, 32, 0, s>>>(ctl, norms2, th_dev, m, nev, maxit, reduced ? 1 : 0, active, st, h,
-                                        monitor ? 1 : 0);
+                                        stream_mode ? 0 : 1, monitor ? 1 : 0);
     ++g_launch_count;
     CK(cudaGetLastError());
     cond_copy_kernel<S><<<cp_grid, 256, 0, s>>>(&ctl->save, X, ld, Xbest, m, m, dim);
@@ -518,7 +544,65 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
     if (r) return r;
     return check_and_decide(h);
   };
+  // final FP64 Rayleigh-Ritz on a fresh application of the operator's most accurate arithmetic (the
+  // iteration's AX is a running linear combination of cheaper applications)
+  std::function<int()> final_step = [&]() -> int {
+    cond_copy_kernel<S><<<cp_grid, 256, 0, s>>>(&ctl->restore, Xbest, m, X, ld, m, dim);
+    ++g_launch_count;
+    op.begin_refine();
+    op.set_final(true);
+    const cudaError_t fe = op.apply(X, ld, 0, m, AX, ld, s);
+    op.set_final(false);
+    CK(fe);
+    CK((launch_convert_cols<S, double>(X, ld, X64, 2 * m, m, dim, s)));
+    CK((launch_convert_cols<S, double>(AX, ld, X64 + m, 2 * m, m, dim, s)));
+    int r = rayleigh_ritz<double>(X64, X64 + m, 2 * m, m, m, dim, 1e-13, sm, partial, npart, st, s, msg, true);
+    if (r) return r;
+    // Xout = X64 C[:, :nev]; residual = (AX64 C - Xout theta)
+    CK(launch_update<double>(X64, 2 * m, m, sm.C, m, nev, dim, Xout, nev, 1.0, 0.0, s));
+    CK(launch_update<double>(X64 + m, 2 * m, m, sm.C, m, nev, dim, T64, nev, 1.0, 0.0, s));
+    CK(launch_residual<double>(T64, nev, Xout, nev, sm.theta, nev, dim, T64, nev, partial, npart, norms2, s));
+    return WTB_OK;
+  };
 
+  int rc = WTB_OK;
+  long long body_launches[2] = {0, 0};
+  if (stream_mode) {
+    auto stopped = [&](bool* stop) -> int {
+      int h = 0;
+      CK(cudaMemcpyAsync(&h, &ctl->stop, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      *stop = h != 0;
+      return WTB_OK;
+    };
+    auto run_loop = [&]() -> int {
+      for (;;) {
+        bool stop = false;
+        int r = stopped(&stop);
+        if (r) return r;
+        if (stop) return WTB_OK;
+        r = iteration(0);
+        if (r) return r;
+      }
+    };
+    lob_ctl_reset_kernel<<<1, 1, 0, s>>>(ctl, tol, 0);
+    ++g_launch_count;
+    CK(cudaMemset2DAsync(Sb, sizeof(cplx<S>) * ld, 0, sizeof(cplx<S>) * ld, dim, s));
+    CK(launch_select_lowest(diag, dim, m, idx, cand, s));
+    CK(launch_init_guess<S>(X, ld, dim, m, idx + 64 * m, 12345u, s));
+    if ((rc = restart_from_x(0))) return rc;
+    if ((rc = run_loop())) return rc;
+    if (two_phase) {
+      op.begin_refine();
+      cond_copy_kernel<S><<<cp_grid, 256, 0, s>>>(&ctl->restore, Xbest, m, X, ld, m, dim);
+      ++g_launch_count;
+      lob_ctl_reset_kernel<<<1, 1, 0, s>>>(ctl, tol_refine, 1);
+      ++g_launch_count;
+      if ((rc = restart_from_x(0))) return rc;
+      if ((rc = run_loop())) return rc;
+    }
+    if ((rc = final_step())) return rc;
+  } else {
   // the graph of this solve is reused when nothing it was captured with has changed
   std::vector<uint64_t> sig = {(uint64_t)dim, (uint64_t)nev, (uint64_t)m, (uint64_t)maxit, (uint64_t)sizeof(S),
                                (uint64_t)(uintptr_t)diag, (uint64_t)(uintptr_t)Xout, (uint64_t)(uintptr_t)st,
@@ -545,8 +629,6 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
       key *= 1099511628211ull;
     }
   if (key == 0) key = 1;
-  long long body_launches[2] = {0, 0};
-  int rc = WTB_OK;
   if (ws.graph_exec && ws.graph_key == key) {
     body_launches[0] = ws.graph_body_launches[0];
     body_launches[1] = ws.graph_body_launches[1];
@@ -635,26 +717,7 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
       body_launches[1] = g_launch_count.load() - c0;
       tail.assign(1, wn);
     }
-    // final FP64 Rayleigh-Ritz on a fresh application of the operator's most accurate arithmetic (the
-    // iteration's AX is a running linear combination of cheaper applications)
-    rc = segment(G, tail, &tail, [&]() -> int {
-      cond_copy_kernel<S><<<cp_grid, 256, 0, s>>>(&ctl->restore, Xbest, m, X, ld, m, dim);
-      ++g_launch_count;
-      op.begin_refine();
-      op.set_final(true);
-      const cudaError_t fe = op.apply(X, ld, 0, m, AX, ld, s);
-      op.set_final(false);
-      CK(fe);
-      CK((launch_convert_cols<S, double>(X, ld, X64, 2 * m, m, dim, s)));
-      CK((launch_convert_cols<S, double>(AX, ld, X64 + m, 2 * m, m, dim, s)));
-      int r = rayleigh_ritz<double>(X64, X64 + m, 2 * m, m, m, dim, 1e-13, sm, partial, npart, st, s, msg, true);
-      if (r) return r;
-      // Xout = X64 C[:, :nev]; residual = (AX64 C - Xout theta)
-      CK(launch_update<double>(X64, 2 * m, m, sm.C, m, nev, dim, Xout, nev, 1.0, 0.0, s));
-      CK(launch_update<double>(X64 + m, 2 * m, m, sm.C, m, nev, dim, T64, nev, 1.0, 0.0, s));
-      CK(launch_residual<double>(T64, nev, Xout, nev, sm.theta, nev, dim, T64, nev, partial, npart, norms2, s));
-      return WTB_OK;
-    });
+    rc = segment(G, tail, &tail, final_step);
     if (rc) break;
     if (cudaGraphInstantiate(&GX, G, 0) != cudaSuccess) {
       if (msg) *msg = "graph instantiation failed";
@@ -679,16 +742,17 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
   ws.graph_body_launches[1] = body_launches[1];
   ws.graph_launches = g_launch_count.load() - captured0;
   }
+  }
   std::vector<double> th(nev), th_it(nev), nrm(nev);
   LobCtl hc;
   CK(cudaMemcpyAsync(th.data(), sm.theta, sizeof(double) * nev, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(th_it.data(), th_dev, sizeof(double) * nev, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(nrm.data(), norms2, sizeof(double) * nev, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(&hc, ctl, sizeof(hc), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
   DevStatus hst;
-  CK(cudaMemcpy(&hst, st, sizeof(hst), cudaMemcpyDeviceToHost));
-  {
+  CK(cudaMemcpyAsync(&hst, st, sizeof(hst), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (!stream_mode) {
     const int it2 = two_phase ? hc.it : 0, it1 = hc.total_it - it2;
     g_launch_count += body_launches[0] * (it1 - 1) + (two_phase ? body_launches[1] * (it2 - 1) : 0);
   }

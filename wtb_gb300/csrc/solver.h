@@ -11,16 +11,18 @@
 
 namespace wtb {
 
-// Device allocation with grow-only reuse.
+// Device allocation with grow-only reuse.  Zeroing is ordered on the owner's stream: the legacy default
+// stream has no ordering with the (non-blocking) context streams, so a cudaMemset there could land in the
+// middle of later work on the context's stream.
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
   ~DevBuf() {
     if (p) cudaFree(p);
   }
-  cudaError_t ensure(size_t n, bool zero = false) {
+  cudaError_t ensure(size_t n, bool zero, cudaStream_t s) {
     if (n <= bytes && p) {
-      if (zero) return cudaMemset(p, 0, n);
+      if (zero) return cudaMemsetAsync(p, 0, n, s);
       return cudaSuccess;
     }
     if (p) cudaFree(p);
@@ -29,7 +31,7 @@ struct DevBuf {
     cudaError_t e = cudaMalloc(&p, n ? n : 16);
     if (e != cudaSuccess) return e;
     bytes = n;
-    if (zero) return cudaMemset(p, 0, n);
+    if (zero) return cudaMemsetAsync(p, 0, n, s);
     return cudaSuccess;
   }
   template <class T>
@@ -44,6 +46,7 @@ struct DevBuf {
 // parameters, operator configuration and every device address it was captured with) is unchanged.
 struct Workspace {
   std::map<std::string, std::unique_ptr<DevBuf>> bufs;
+  cudaStream_t stream = nullptr;  // the owner's stream (zeroing is ordered on it)
   uint64_t graph_key = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -61,7 +64,7 @@ struct Workspace {
   T* get(const std::string& name, size_t count, cudaError_t* err, bool zero = false) {
     auto& b = bufs[name];
     if (!b) b.reset(new DevBuf());
-    const cudaError_t e = b->ensure(count * sizeof(T), zero);
+    const cudaError_t e = b->ensure(count * sizeof(T), zero, stream);
     if (e != cudaSuccess) *err = e;
     return b->as<T>();
   }

@@ -58,10 +58,11 @@ int set_err(wtb_ctx* c, int code, const std::string& m) {
 // Reads and clears the device status word; maps kernel-side failures to the reference's STOP texts.
 int check_status(wtb_ctx* c) {
   DevStatus h;
+  CKC(cudaMemcpyAsync(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost, c->s));
   CKC(cudaStreamSynchronize(c->s));
-  CKC(cudaMemcpy(&h, c->st, sizeof(h), cudaMemcpyDeviceToHost));
   if (!h.code) return WTB_OK;
-  CKC(cudaMemset(c->st, 0, sizeof(DevStatus)));
+  CKC(cudaMemsetAsync(c->st, 0, sizeof(DevStatus), c->s));
+  CKC(cudaStreamSynchronize(c->s));
   switch (h.code) {
     case 101:
       return set_err(c, WTB_EBADARG, "Number of valence states higher then ocuppied states (k-point " +
@@ -481,10 +482,12 @@ int wtb_ctx_create(wtb_ctx** out, int device) {
   wtb_ctx* c = new wtb_ctx();
   c->device = device;
   if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->s, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaMalloc(&c->st, sizeof(DevStatus)) != cudaSuccess || cudaMemset(c->st, 0, sizeof(DevStatus)) != cudaSuccess) {
+      cudaMalloc(&c->st, sizeof(DevStatus)) != cudaSuccess ||
+      cudaMemsetAsync(c->st, 0, sizeof(DevStatus), c->s) != cudaSuccess || cudaStreamSynchronize(c->s) != cudaSuccess) {
     delete c;
     return WTB_ENODEV;
   }
+  c->ws.stream = c->s;
   *out = c;
   return WTB_OK;
 }
@@ -579,9 +582,9 @@ int wtb_eigsys(int nthreads, double scs, double exc, int* nocp, const int* ffact
   std::vector<double> e(w);
   std::vector<zd> v((size_t)w * w);
   int cnt = 0;
-  CKC(cudaMemcpy(e.data(), c->ws.get<double>("eig_all", 0, &err), sizeof(double) * w, cudaMemcpyDeviceToHost));
-  CKC(cudaMemcpy(v.data(), c->ws.get<zd>("vec_all", 0, &err), sizeof(zd) * w * w, cudaMemcpyDeviceToHost));
-  CKC(cudaMemcpy(&cnt, c->ws.get<int>("nocp", 0, &err), sizeof(int), cudaMemcpyDeviceToHost));
+  CKC(cudaMemcpyAsync(e.data(), c->ws.get<double>("eig_all", 0, &err), sizeof(double) * w, cudaMemcpyDeviceToHost, c->s));
+  CKC(cudaMemcpyAsync(v.data(), c->ws.get<zd>("vec_all", 0, &err), sizeof(zd) * w * w, cudaMemcpyDeviceToHost, c->s));
+  CKC(cudaMemcpyAsync(&cnt, c->ws.get<int>("nocp", 0, &err), sizeof(int), cudaMemcpyDeviceToHost, c->s));
   if (cnt < w) {
     if (nocp) *nocp = cnt;
   } else if (nocp) {
@@ -615,13 +618,13 @@ int wtb_eigsys_mesh(wtb_ctx* c, int nk, const double* kpt, int nv, int nc, doubl
   cudaError_t err = cudaSuccess;
   if (eigv) {
     std::vector<double> e((size_t)nk * nb);
-    CKC(cudaMemcpy(e.data(), c->ws.get<double>("eig_win", 0, &err), e.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    CKC(cudaMemcpyAsync(e.data(), c->ws.get<double>("eig_win", 0, &err), e.size() * sizeof(double), cudaMemcpyDeviceToHost, c->s));
     for (int i = 0; i < nk; ++i)
       for (int j = 0; j < nb; ++j) eigv[i + (size_t)nk * j] = e[(size_t)i * nb + j];
   }
   if (vector) {
     std::vector<zd> v((size_t)nk * nb * w);
-    CKC(cudaMemcpy(v.data(), c->ws.get<zd>("vec_win", 0, &err), v.size() * sizeof(zd), cudaMemcpyDeviceToHost));
+    CKC(cudaMemcpyAsync(v.data(), c->ws.get<zd>("vec_win", 0, &err), v.size() * sizeof(zd), cudaMemcpyDeviceToHost, c->s));
     for (int i = 0; i < nk; ++i)
       for (int j = 0; j < nb; ++j)
         for (int o = 0; o < w; ++o) {
@@ -630,7 +633,7 @@ int wtb_eigsys_mesh(wtb_ctx* c, int nk, const double* kpt, int nv, int nc, doubl
           vector[2 * f + 1] = v[((size_t)i * nb + j) * w + o].im;
         }
   }
-  if (nocpk) CKC(cudaMemcpy(nocpk, c->ws.get<int>("nocp", 0, &err), sizeof(int) * nk, cudaMemcpyDeviceToHost));
+  if (nocpk) CKC(cudaMemcpyAsync(nocpk, c->ws.get<int>("nocp", 0, &err), sizeof(int) * nk, cudaMemcpyDeviceToHost, c->s));
   return WTB_OK;
 }
 

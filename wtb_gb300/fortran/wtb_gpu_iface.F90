@@ -84,6 +84,22 @@ module wtb_gpu
       integer(c_int), value :: dimse
       real(c_double) :: ws(*), acts(*), dielf(*)
     end function
+    integer(c_int) function c_wtb_spectrum_loss(ctx, p, dimse, nev, e, fxx, target, l, dl_de, dl_df) &
+        bind(C, name="wtb_spectrum_loss")
+      import :: c_ptr, c_int, c_double, wtb_bse_params_t
+      type(c_ptr), value :: ctx
+      type(wtb_bse_params_t) :: p
+      integer(c_int), value :: dimse, nev
+      real(c_double) :: e(*), fxx(*), target(*), l, dl_de(*), dl_df(*)
+    end function
+    integer(c_int) function c_wtb_bse_backward(ctx, p, dl_de, dl_df, dl_dhop, dl_dihop, dl_dr0, t) &
+        bind(C, name="wtb_bse_backward")
+      import :: c_ptr, c_int, c_double, wtb_bse_params_t, wtb_timings_t
+      type(c_ptr), value :: ctx
+      type(wtb_bse_params_t) :: p
+      real(c_double) :: dl_de(*), dl_df(*), dl_dhop(*), dl_dihop(*), dl_dr0
+      type(wtb_timings_t) :: t
+    end function
   end interface
 
   type(c_ptr), save :: ctx = c_null_ptr
@@ -172,6 +188,21 @@ contains
     double precision :: Ws(dimse), acts(dimse,6), dielf(p%numbse,3,6)
     call wtb_gpu_init(0)
     call check(c_wtb_bsedielraw(ctx, p, dimse, Ws, acts, dielf), 'bsedielraw')
+  end subroutine
+
+  ! gradient of L = sum_j (spinf eps2_xx(omega_j) - target_j)^2 with respect to H(R) and R_0, through the last
+  ! wtb_gpu_bsesolver call (same p): dL_dhop/dL_dihop have the layout of hopmatrices/ihopmatrices
+  subroutine wtb_gpu_spectrum_gradient(p, dimbse, Ws, acts, target, loss, dl_dhop, dl_dihop, dl_dr0, nvec, w90basis)
+    type(wtb_bse_params_t) :: p
+    integer :: dimbse, nvec, w90basis
+    double precision :: Ws(dimbse), acts(dimbse,8), target(p%numbse), loss, dl_dr0
+    double precision :: dl_dhop(nvec,w90basis,w90basis), dl_dihop(nvec,w90basis,w90basis)
+    double precision :: dl_de(p%nev), dl_df(p%nev)
+    type(wtb_timings_t) :: t
+    call wtb_gpu_init(0)
+    call check(c_wtb_spectrum_loss(ctx, p, dimbse, p%nev, Ws, acts(1:p%nev,1), target, loss, dl_de, dl_df), &
+               'spectrum_loss')
+    call check(c_wtb_bse_backward(ctx, p, dl_de, dl_df, dl_dhop, dl_dihop, dl_dr0, t), 'bse_backward')
   end subroutine
 
 end module wtb_gpu
