@@ -397,36 +397,67 @@ __global__ void __launch_bounds__(128) adj_eig_kernel(const zd* __restrict__ vec
   }
 }
 
-// dL/dhop(R,m,n), dL/dihop(R,m,n) (Fortran layout (nvec, w, w)) from G_k and Mbar_k.
-__global__ void adj_fourier_kernel(const zd* __restrict__ G, const zd* __restrict__ Mbar, const int* __restrict__ rvec,
-                                   const int* __restrict__ ndegen, int nR, int w, const double* __restrict__ rlat,
-                                   const double* __restrict__ kpt, int nk, double* __restrict__ dhop,
-                                   double* __restrict__ dihop) {
+// e^{i phi_kR} / ndegen_R for every (k, R), once (the forward's float32-rounded phase)
+__global__ void adj_phase_kernel(const int* __restrict__ rvec, const int* __restrict__ ndegen, int nR,
+                                 const double* __restrict__ rlat, const double* __restrict__ kpt, int nk,
+                                 zd* __restrict__ eph) {
   __shared__ double rl[9];
   if (threadIdx.x < 9) rl[threadIdx.x] = rlat[threadIdx.x];
   __syncthreads();
+  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long)nk * nR) return;
+  const int k = (int)(e / nR), r = (int)(e % nR);
+  double sn, cs;
+  sincos(phase_adj(rvec, nR, r, rl, kpt + 3 * k), &sn, &cs);
+  const double inv = 1.0 / (double)ndegen[r];
+  eph[e] = mk<double>(cs * inv, sn * inv);
+}
+
+// Partial sums over the k-points of chunk blockIdx.y of dL/dhop(R,m,n) and dL/dihop(R,m,n) from G_k and Mbar_k:
+// dH/dhop = e^{i phi}/nd, dH/dihop = i e^{i phi}/nd, dM/dhop = i R_x e^{i phi}/nd, dM/dihop = -R_x e^{i phi}/nd.
+__global__ void adj_fourier_partial_kernel(const zd* __restrict__ G, const zd* __restrict__ Mbar,
+                                           const zd* __restrict__ eph, const int* __restrict__ rvec, int nR, int w,
+                                           const double* __restrict__ rlat, int nk, int kchunk,
+                                           double* __restrict__ part) {
+  __shared__ double rl[9];
+  if (threadIdx.x < 9) rl[threadIdx.x] = rlat[threadIdx.x];
+  __syncthreads();
+  const int ent = nR * w * w;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= nR * w * w) return;
+  if (e >= ent) return;
   const int r = e / (w * w), m = (e / w) % w, n = e % w;
   const bool onsite = rvec[r] == 0 && rvec[nR + r] == 0 && rvec[2 * nR + r] == 0 && m == n;
   const double rx = (double)__double2float_rn(rcart_adj(rvec[r], rvec[nR + r], rvec[2 * nR + r], rl, 0));
-  const double inv = 1.0 / (double)ndegen[r];
+  const int k0 = blockIdx.y * kchunk, k1 = min(nk, k0 + kchunk);
   double gh = 0.0, gi = 0.0;
-  for (int k = 0; k < nk; ++k) {
-    const double phi = phase_adj(rvec, nR, r, rl, kpt + 3 * k);
-    double sn, cs;
-    sincos(phi, &sn, &cs);
+  for (int k = k0; k < k1; ++k) {
+    const zd ep = eph[(size_t)k * nR + r];
+    const double cs = ep.re, sn = ep.im;  // already divided by ndegen
     const zd g = G[((size_t)k * w + m) * w + n];
-    // dH/dhop = e^{i phi}/nd, dH/dihop = i e^{i phi}/nd; Re(conj(g) z)
-    gh += (g.re * cs + g.im * sn) * inv;
-    gi += (g.re * (-sn) + g.im * cs) * inv;
+    gh += g.re * cs + g.im * sn;
+    gi += g.im * cs - g.re * sn;
     if (!onsite) {
       const zd mb = Mbar[((size_t)k * w + m) * w + n];
-      // dM/dhop = i R_x e^{i phi}/nd = R_x (-sin, cos)/nd ; dM/dihop = -R_x e^{i phi}/nd
-      gh += rx * (mb.re * (-sn) + mb.im * cs) * inv;
-      gi += -rx * (mb.re * cs + mb.im * sn) * inv;
+      gh += rx * (mb.im * cs - mb.re * sn);
+      gi -= rx * (mb.re * cs + mb.im * sn);
     }
   }
+  part[((size_t)blockIdx.y * ent + e) * 2] = gh;
+  part[((size_t)blockIdx.y * ent + e) * 2 + 1] = gi;
+}
+
+// chunks summed in a fixed order into the Fortran layout (nvec, w, w)
+__global__ void adj_fourier_reduce_kernel(const double* __restrict__ part, int nchunk, int nR, int w,
+                                          double* __restrict__ dhop, double* __restrict__ dihop) {
+  const int ent = nR * w * w;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ent) return;
+  double gh = 0.0, gi = 0.0;
+  for (int c = 0; c < nchunk; ++c) {
+    gh += part[((size_t)c * ent + e) * 2];
+    gi += part[((size_t)c * ent + e) * 2 + 1];
+  }
+  const int r = e / (w * w), m = (e / w) % w, n = e % w;
   const size_t f = (size_t)r + (size_t)nR * (m + (size_t)w * n);
   dhop[f] = gh;
   dihop[f] = gi;
@@ -702,9 +733,21 @@ int backward_impl(wtb_ctx* c, const wtb_bse_params* p, Operator<S>& op, MatFreeO
     ++g_launch_count;
     CKA(cudaGetLastError());
   }
-  adj_fourier_kernel<<<(nR * w * w + 127) / 128, 128, 0, s>>>(Gk, Mbar, rvec, ndegen, nR, w, rlat, kpt, nk, dh, di);
-  ++g_launch_count;
-  CKA(cudaGetLastError());
+  {
+    // k split into chunks so that nR w^2 entries x chunks fill the GPU; phases computed once per (k, R)
+    const int ent = nR * w * w;
+    const int kchunk = std::max(16, (int)(((long)nk * ent + 152L * 2048 - 1) / (152L * 2048)));
+    const int nchunk = (nk + kchunk - 1) / kchunk;
+    zd* eph = c->ws.get<zd>("adj_eph", (size_t)nk * nR, &err);
+    double* fpart = c->ws.get<double>("adj_fpart", (size_t)nchunk * ent * 2, &err);
+    if (err != cudaSuccess) return ctx_set_err(c, WTB_ENOMEM, "adjoint workspace");
+    adj_phase_kernel<<<(unsigned)(((long)nk * nR + 255) / 256), 256, 0, s>>>(rvec, ndegen, nR, rlat, kpt, nk, eph);
+    adj_fourier_partial_kernel<<<dim3((ent + 127) / 128, nchunk), 128, 0, s>>>(Gk, Mbar, eph, rvec, nR, w, rlat, nk,
+                                                                                 kchunk, fpart);
+    adj_fourier_reduce_kernel<<<(ent + 255) / 256, 256, 0, s>>>(fpart, nchunk, nR, w, dh, di);
+    g_launch_count += 3;
+    CKA(cudaGetLastError());
+  }
   if (dhop) CKA(cudaMemcpyAsync(dhop, dh, sizeof(double) * nR * w * w, cudaMemcpyDeviceToHost, s));
   if (dihop) CKA(cudaMemcpyAsync(dihop, di, sizeof(double) * nR * w * w, cudaMemcpyDeviceToHost, s));
   // dL/dr0 = Re sum_n y_n^H H' A_n, H' the operator of dV/dr0 (no diagonal)

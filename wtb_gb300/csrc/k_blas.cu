@@ -129,17 +129,19 @@ __global__ void __launch_bounds__(256) residual_kernel(const cplx<S>* __restrict
   __shared__ double red[8][32];
   const int tid = threadIdx.x;
   const int j = tid % 32, rr = tid / 32;  // 8 rows per step, up to 32 columns
-  double acc = 0.0;
+  // a thread's few dozen rows are summed in S (FP64 instructions are scarce on this GPU), the partial sums
+  // in FP64
+  S acc = 0;
   if (j < m) {
     const S th = (S)theta[j];
     for (long r = (long)blockIdx.x * 8 + rr; r < nrow; r += (long)gridDim.x * 8) {
       const cplx<S> ax = AX[r * ldax + j], x = X[r * ldx + j];
       const cplx<S> v = mk<S>(ax.re - th * x.re, ax.im - th * x.im);
       R[r * ldr + j] = v;
-      acc += (double)v.re * (double)v.re + (double)v.im * (double)v.im;
+      acc += v.re * v.re + v.im * v.im;
     }
   }
-  red[rr][j] = acc;
+  red[rr][j] = (double)acc;
   __syncthreads();
   if (rr == 0) {
     double s = 0.0;
@@ -160,11 +162,11 @@ __global__ void precond_kernel(cplx<S>* __restrict__ R, int ldr, const double* _
     v = mk<S>(0, 0);
     return;
   }
-  const double th = theta[j];
-  double d = diag[r] - th;
-  const double fl = 1e-2 * fmax(fabs(th), 1e-3);
+  const S th = (S)theta[j];
+  S d = (S)diag[r] - th;
+  const S fl = (S)1e-2 * (fabs(th) > (S)1e-3 ? fabs(th) : (S)1e-3);
   if (fabs(d) < fl) d = fl;
-  const S inv = (S)(1.0 / fabs(d));
+  const S inv = (S)1 / fabs(d);
   v = mk<S>(v.re * inv, v.im * inv);
 }
 
@@ -184,24 +186,26 @@ __device__ __forceinline__ int rr_player(int i, int t, int n) { return i == 0 ? 
 
 
 // ----------------------------------------------------------------------------- small helpers
+// C = op(A) B for the small projected matrices (complex(8) storage), in arithmetic T: FP32 when the projected
+// problem is solved in FP32 (FP64 instructions are scarce on this GPU), FP64 for the final FP64 step
+template <class T>
 __global__ void small_gemm_kernel(const zd* __restrict__ A, int lda, int transA, const zd* __restrict__ B, int ldb,
                                   zd* __restrict__ C, int ldc, int m, int n, int k) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= m * n) return;
   const int i = e / n, j = e % n;
-  zd acc = mk<double>(0.0, 0.0);
+  cplx<T> acc = mk<T>(0, 0);
   for (int l = 0; l < k; ++l) {
+    const zd a = transA ? A[(size_t)l * lda + i] : A[(size_t)i * lda + l];
+    const zd b = B[(size_t)l * ldb + j];
+    const cplx<T> at = mk<T>((T)a.re, (T)a.im), bt = mk<T>((T)b.re, (T)b.im);
     if (transA)
-      cfmac(acc, A[(size_t)l * lda + i], B[(size_t)l * ldb + j]);
+      cfmac(acc, at, bt);
     else
-      cfma(acc, A[(size_t)i * lda + l], B[(size_t)l * ldb + j]);
+      cfma(acc, at, bt);
   }
-  C[(size_t)i * ldc + j] = acc;
+  C[(size_t)i * ldc + j] = mk<double>((double)acc.re, (double)acc.im);
 }
-
-
-
-
 
 __device__ __forceinline__ double hash_noise(unsigned a, unsigned b, unsigned seed) {
   unsigned h = a * 2654435761u ^ (b + 0x9e3779b9u + (seed << 6) + (seed >> 2));
@@ -486,9 +490,6 @@ cudaError_t launch_convert_cols(const cplx<Sa>* A, int lda, cplx<Sb>* B, int ldb
   return cudaGetLastError();
 }
 
-
-
-
 template <class S>
 cudaError_t launch_heev_small(const zd* A, int lda, const int* nptr, int nmax, int nwant, double* evals, zd* evecs,
                               int ldv, cudaStream_t s) {
@@ -520,14 +521,14 @@ template cudaError_t launch_pchol_basis<float>(const zd*, int, int, double, zd*,
 template cudaError_t launch_pchol_basis<double>(const zd*, int, int, double, zd*, int, int*, cudaStream_t);
 
 cudaError_t launch_small_gemm(const zd* A, int lda, int transA, const zd* B, int ldb, zd* C, int ldc, int m, int n,
-                              int k, cudaStream_t s) {
-  small_gemm_kernel<<<(m * n + 127) / 128, 128, 0, s>>>(A, lda, transA, B, ldb, C, ldc, m, n, k); ++g_launch_count;
+                              int k, cudaStream_t s, bool fp32) {
+  if (fp32)
+    small_gemm_kernel<float><<<(m * n + 127) / 128, 128, 0, s>>>(A, lda, transA, B, ldb, C, ldc, m, n, k);
+  else
+    small_gemm_kernel<double><<<(m * n + 127) / 128, 128, 0, s>>>(A, lda, transA, B, ldb, C, ldc, m, n, k);
+  ++g_launch_count;
   return cudaGetLastError();
 }
-
-
-
-
 
 // idx needs room for 64 * m + m ints (candidates then the result), idx[64 m .. 64 m + m) holds the answer.
 cudaError_t launch_select_lowest(const double* diag, int dim, int m, int* idx, double* cand_val, cudaStream_t s) {

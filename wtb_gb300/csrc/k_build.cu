@@ -96,20 +96,21 @@ __global__ void __launch_bounds__(256) bse_build_kernel(const zd* __restrict__ v
 // chunks of 16 staged in shared memory, 4 x 2 register micro-tile per thread.  The diagonal term (the
 // transition energy, much larger than the Coulomb entries) is accumulated apart from the off-diagonal
 // sum, so a long FP32 accumulation only carries rounding of the Coulomb-sized terms.
-template <class S>
+template <class S, int BM, int TC>
 __global__ void __launch_bounds__(256) dense_mv_kernel(const cplx<S>* __restrict__ H, int dim,
                                                        const cplx<S>* __restrict__ X, int ldx, cplx<S>* __restrict__ Y,
                                                        int ldy, int ncol) {
-  constexpr int BM = 64, BK = 16;
+  // 16 x 16 threads: a thread owns rows ty + 16 i (i < BM/16) and columns tx + 16 j (j < TC)
+  constexpr int BK = 16, RI = BM / 16, NC = 16 * TC;
   __shared__ cplx<S> Hs[BM][BK + 1];
-  __shared__ cplx<S> Xs[BK][32];
+  __shared__ cplx<S> Xs[BK][NC];
   const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
   const long r0 = (long)blockIdx.x * BM;
-  cplx<S> acc[4][2], dacc[4][2];
+  cplx<S> acc[RI][TC], dacc[RI][TC];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < RI; ++i)
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
+    for (int j = 0; j < TC; ++j) {
       acc[i][j] = mk<S>(0, 0);
       dacc[i][j] = mk<S>(0, 0);
     }
@@ -119,8 +120,8 @@ __global__ void __launch_bounds__(256) dense_mv_kernel(const cplx<S>* __restrict
       const long gr = r0 + rr, gk = kb + kk;
       Hs[rr][kk] = (gr < dim && gk < dim) ? H[gr * dim + gk] : mk<S>(0, 0);
     }
-    for (int e = tid; e < BK * 32; e += 256) {
-      const int kk = e / 32, c = e % 32;
+    for (int e = tid; e < BK * NC; e += 256) {
+      const int kk = e / NC, c = e % NC;
       const long gk = kb + kk;
       Xs[kk][c] = (gk < dim && c < ncol) ? X[gk * ldx + c] : mk<S>(0, 0);
     }
@@ -130,29 +131,29 @@ __global__ void __launch_bounds__(256) dense_mv_kernel(const cplx<S>* __restrict
     if (!diag_chunk) {
 #pragma unroll 4
       for (int kk = 0; kk < BK; ++kk) {
-        cplx<S> h[4], x[2];
+        cplx<S> h[RI], x[TC];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) h[i] = Hs[ty + 16 * i][kk];
+        for (int i = 0; i < RI; ++i) h[i] = Hs[ty + 16 * i][kk];
 #pragma unroll
-        for (int j = 0; j < 2; ++j) x[j] = Xs[kk][tx + 16 * j];
+        for (int j = 0; j < TC; ++j) x[j] = Xs[kk][tx + 16 * j];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < RI; ++i)
 #pragma unroll
-          for (int j = 0; j < 2; ++j) cfma(acc[i][j], h[i], x[j]);
+          for (int j = 0; j < TC; ++j) cfma(acc[i][j], h[i], x[j]);
       }
     } else {
       for (int kk = 0; kk < BK; ++kk) {
-        cplx<S> h[4], x[2];
+        cplx<S> h[RI], x[TC];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) h[i] = Hs[ty + 16 * i][kk];
+        for (int i = 0; i < RI; ++i) h[i] = Hs[ty + 16 * i][kk];
 #pragma unroll
-        for (int j = 0; j < 2; ++j) x[j] = Xs[kk][tx + 16 * j];
+        for (int j = 0; j < TC; ++j) x[j] = Xs[kk][tx + 16 * j];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const bool d = (kb + kk) == (r0 + ty + 16 * i);
+        for (int i = 0; i < RI; ++i) {
+          const bool dg = (kb + kk) == (r0 + ty + 16 * i);
 #pragma unroll
-          for (int j = 0; j < 2; ++j) {
-            if (d)
+          for (int j = 0; j < TC; ++j) {
+            if (dg)
               cfma(dacc[i][j], h[i], x[j]);
             else
               cfma(acc[i][j], h[i], x[j]);
@@ -163,9 +164,9 @@ __global__ void __launch_bounds__(256) dense_mv_kernel(const cplx<S>* __restrict
     __syncthreads();
   }
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < RI; ++i)
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
+    for (int j = 0; j < TC; ++j) {
       const long gr = r0 + ty + 16 * i;
       const int c = tx + 16 * j;
       if (gr < dim && c < ncol) Y[gr * ldy + c] = cadd(dacc[i][j], acc[i][j]);
@@ -198,9 +199,22 @@ cudaError_t launch_bse_build(const zd* vec_win, const double* dE, const double* 
 template <class S>
 cudaError_t launch_dense_mv(const cplx<S>* H, int dim, const cplx<S>* X, int ldx, cplx<S>* Y, int ldy, int ncol,
                             cudaStream_t s) {
+  // column tiles of 16 or 32 (no FMAs on padding columns); 32-row tiles when 64-row ones would leave SMs idle
+  const bool small = (dim + 63) / 64 < 2 * 152;
   for (int c0 = 0; c0 < ncol; c0 += 32) {
     const int nc = ncol - c0 < 32 ? ncol - c0 : 32;
-    dense_mv_kernel<S><<<(dim + 63) / 64, 256, 0, s>>>(H, dim, X + c0, ldx, Y + c0, ldy, nc); ++g_launch_count;
+    if (nc <= 16) {
+      if (small)
+        dense_mv_kernel<S, 32, 1><<<(dim + 31) / 32, 256, 0, s>>>(H, dim, X + c0, ldx, Y + c0, ldy, nc);
+      else
+        dense_mv_kernel<S, 64, 1><<<(dim + 63) / 64, 256, 0, s>>>(H, dim, X + c0, ldx, Y + c0, ldy, nc);
+    } else {
+      if (small)
+        dense_mv_kernel<S, 32, 2><<<(dim + 31) / 32, 256, 0, s>>>(H, dim, X + c0, ldx, Y + c0, ldy, nc);
+      else
+        dense_mv_kernel<S, 64, 2><<<(dim + 63) / 64, 256, 0, s>>>(H, dim, X + c0, ldx, Y + c0, ldy, nc);
+    }
+    ++g_launch_count;
   }
   return cudaGetLastError();
 }

@@ -148,9 +148,10 @@ __global__ void __launch_bounds__(256) mf_gather_bf16_kernel(const zf* __restric
     Y1[e] = acc;
   }
   __syncthreads();
-  // items (b, o, p): Z over the tile's 8 k', re and im rows, every slice
+  // items (b, o, p), b fastest across lanes (Y1 reads are then consecutive in shared memory): Z over the
+  // tile's 8 k', re and im rows, every slice
   for (int it = tid; it < nbc * ww; it += nt) {
-    const int b = it / ww, op = it % ww, o = op / w, p = op % w;
+    const int b = it % nbc, op = it / nbc, o = op / w, p = op % w;
     float zr[KT], zi[KT];
 #pragma unroll
     for (int kk = 0; kk < KT; ++kk) {
@@ -291,16 +292,18 @@ __global__ void __launch_bounds__(256) simt_gemm_tn_kernel(const S* __restrict__
     }
 }
 
+// x = x0 + x1 + x2 with every part rounded to bf16: three 8-bit significands hold the 24 bits of the FP32
+// rounding of x, so the split runs in FP32 after one conversion (FP64 instructions are scarce on this GPU)
 __global__ void split_bf16_kernel(const double* __restrict__ V, int ldv, int rows, int cols, uint16_t* __restrict__ out,
                                   int ldo, long slice_stride, int nslices) {
   const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= (long)rows * cols) return;
   const int r = (int)(e / cols), c = (int)(e % cols);
-  double x = V[(size_t)r * ldv + c];
+  float x = (float)V[(size_t)r * ldv + c];
   for (int s = 0; s < nslices; ++s) {
-    const __nv_bfloat16 h = __float2bfloat16_rn((float)x);
+    const __nv_bfloat16 h = __float2bfloat16_rn(x);
     out[s * slice_stride + (size_t)r * ldo + c] = __bfloat16_as_ushort(h);
-    x = x - (double)__bfloat162float(h);
+    x = x - __bfloat162float(h);
   }
 }
 

@@ -85,20 +85,32 @@ __global__ void osc_final_kernel(const double* __restrict__ partial, int nblk, i
 }
 
 // smef = CSHIFT + 10 * (sum_{i>=1} (E_i - E_{i-1})) / nrows  (fixed-order tree reduction)
+// Also records in smef[1] the end of the last row with a nonzero activity in any component: rows past it add
+// exactly zero to every Lorentzian sum (bsesolver leaves the rows past nev at zero).
 __global__ void __launch_bounds__(1024) avgsme_kernel(const double* __restrict__ Ws, int nrows, double sme,
-                                                      double* __restrict__ smef) {
+                                                      const double* __restrict__ f, double* __restrict__ smef) {
   __shared__ double red[1024];
+  __shared__ int s_last;
+  if (threadIdx.x == 0) s_last = 0;
   double acc = 0.0;
   const int chunk = (nrows + blockDim.x - 1) / blockDim.x;
   const int i0 = threadIdx.x * chunk;
+  int last = 0;
   for (int i = max(i0, 1); i < min(nrows, i0 + chunk); ++i) acc = acc + Ws[i] - Ws[i - 1];
+  for (int i = i0; i < min(nrows, i0 + chunk); ++i)
+    for (int c = 0; c < 6; ++c)
+      if (f[(size_t)c * nrows + i] != 0.0) last = i + 1;
   red[threadIdx.x] = acc;
   __syncthreads();
+  if (last) atomicMax(&s_last, last);
   for (int off = blockDim.x / 2; off > 0; off >>= 1) {
     if (threadIdx.x < off) red[threadIdx.x] += red[threadIdx.x + off];
     __syncthreads();
   }
-  if (threadIdx.x == 0) smef[0] = 10.0 * (red[0] / (double)nrows) + sme;
+  if (threadIdx.x == 0) {
+    smef[0] = 10.0 * (red[0] / (double)nrows) + sme;
+    smef[1] = (double)s_last;
+  }
 }
 
 __global__ void lorentz_kernel(const double* __restrict__ Ws, int nrows, const double* __restrict__ f,
@@ -109,9 +121,10 @@ __global__ void lorentz_kernel(const double* __restrict__ Ws, int nrows, const d
   const int comp = e / nesp, j = e % nesp;
   const double elux = e0 + ((ef - e0) * (double)j) / ((double)nesp - 1.0);
   const double smef = smef_p[0];
+  const int nuse = min(nrows, (int)smef_p[1]);
   const double* fc = f + (size_t)comp * nrows;
   double rpart = 0.0, ipart = 0.0;
-  for (int i = 0; i < nrows; ++i) {
+  for (int i = 0; i < nuse; ++i) {
     const double fi = fc[i];
     if (fi == 0.0) continue;  // zero activities add exactly zero (the denominator is >= gamma^2 > 0)
     const double ex = Ws[i];
@@ -207,7 +220,7 @@ cudaError_t launch_spectrum(const double* Ws, int nrows, const double* f, double
                             double ef, int nesp, int renorm, double spinf, double* dielf, double* partial, int npart,
                             cudaStream_t s) {
   (void)npart;
-  avgsme_kernel<<<1, 1024, 0, s>>>(Ws, nrows, sme, partial); ++g_launch_count;
+  avgsme_kernel<<<1, 1024, 0, s>>>(Ws, nrows, sme, f, partial); ++g_launch_count;
   const double baux = (double)(float)ng * vc;  // real(ngrid product) * vc
   const double caux = (double)180.90f / (baux * 1.0);
   lorentz_kernel<<<(6 * nesp + 127) / 128, 128, 0, s>>>(Ws, nrows, f, partial, caux, e0, ef, nesp, dielf); ++g_launch_count;

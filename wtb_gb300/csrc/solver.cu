@@ -220,13 +220,16 @@ int rayleigh_ritz(const cplx<S>* Sb, const cplx<S>* ASb, int ld, int nb, int m, 
     CK(launch_pchol_basis<double>(sm.M, nb, nb, tau, sm.B, nb, sm.keep, s));
   else
     CK(launch_pchol_basis<S>(sm.M, nb, nb, tau, sm.B, nb, sm.keep, s));
-  CK(launch_small_gemm(sm.G, nb, 0, sm.B, nb, sm.T, nb, nb, nb, nb, s));
-  CK(launch_small_gemm(sm.B, nb, 1, sm.T, nb, sm.Gp, nb, nb, nb, nb, s));
+  // the projected matrix B^H G B stays FP64 (its rounding would mix near-degenerate Ritz vectors); the basis
+  // combination C = B Y may run in FP32 when the iteration does
+  const bool f32 = !small_in_fp64 && sizeof(S) == 4;
+  CK(launch_small_gemm(sm.G, nb, 0, sm.B, nb, sm.T, nb, nb, nb, nb, s, false));
+  CK(launch_small_gemm(sm.B, nb, 1, sm.T, nb, sm.Gp, nb, nb, nb, nb, s, false));
   if (small_in_fp64)
     CK(launch_heev_small<double>(sm.Gp, nb, sm.keep, nb, m, sm.theta, sm.Y, nb, s));
   else
     CK(launch_heev_small<S>(sm.Gp, nb, sm.keep, nb, m, sm.theta, sm.Y, nb, s));
-  CK(launch_small_gemm(sm.B, nb, 0, sm.Y, nb, sm.C, m, nb, m, nb, s));
+  CK(launch_small_gemm(sm.B, nb, 0, sm.Y, nb, sm.C, m, nb, m, nb, s, f32));
   return WTB_OK;
 }
 

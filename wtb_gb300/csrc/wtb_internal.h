@@ -138,7 +138,7 @@ template <class Sa, class Sb>
 cudaError_t launch_convert_cols(const cplx<Sa>* A, int lda, cplx<Sb>* B, int ldb, int ncol, int nrow,
                                 cudaStream_t s);
 cudaError_t launch_small_gemm(const zd* A, int lda, int transA, const zd* B, int ldb, zd* C, int ldc, int m, int n,
-                              int k, cudaStream_t s);
+                              int k, cudaStream_t s, bool fp32 = false);
 
 // ----------------------------------------------------------------------------- matrix-free operator
 // Z[n][k'] with n = ((b*w + o)*w + p)*2 + ri (K-major for the V*Z contraction).
