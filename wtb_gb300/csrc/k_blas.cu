@@ -1,10 +1,11 @@
 // Tall-skinny block kernels and small dense eigen-decompositions for the block eigensolver.
 //
 // Block vectors are dim x ncol, row-major with leading dimension ld, in the iteration precision S
-// (float or double).  Reductions over dim run in two fixed-order passes (per-CTA partials, then one
-// CTA sums them), so repeated runs give identical bits.  Small matrices (<= 112 x 112, the projected
+// (float or double).  Reductions over dim run in two fixed-order passes (per-part partials, then one
+// CTA per system sums them), so repeated runs give identical bits.  Small matrices (<= 96 x 96, the projected
 // problems of the Rayleigh-Ritz step) are complex(8) in global memory; their eigen-decomposition runs in
-// one CTA by cyclic Jacobi in precision S.
+// one CTA per system (small_eig.cuh).  Every kernel takes a BatchMap: one system, or a ragged batch of
+// independent systems in one concatenated row space.
 #include <algorithm>
 
 #include "small_eig.cuh"
@@ -20,15 +21,18 @@ constexpr int kGramTile = 16;
 template <class S, int TI>
 __global__ void __launch_bounds__(256) gram_partial_kernel(const cplx<S>* __restrict__ A, int lda, int p,
                                                            const cplx<S>* __restrict__ B, int ldb, int q, int nrow,
-                                                           double* __restrict__ partial, int rows_per_part) {
-  // the p x q output is covered by a 16 x 16 thread grid with TI x TI entries per thread (16 TI >= p, q)
+                                                           double* __restrict__ partial, int rows_per_part,
+                                                           BatchMap bm) {
+  // the p x q output is covered by a 16 x 16 thread grid with TI x TI entries per thread (16 TI >= p, q);
+  // one CTA per reduction part
   constexpr int RT = 8;  // rows of A/B staged per step
   constexpr int W = 16 * TI;
   __shared__ cplx<S> As[RT][W];
   __shared__ cplx<S> Bs[RT][W];
   const int tid = threadIdx.x, tx = tid % kGramTile, ty = tid / kGramTile;
-  const long r_begin = (long)blockIdx.x * rows_per_part;
-  const long r_end = min((long)nrow, r_begin + rows_per_part);
+  long r_begin, r_end;
+  const int sys = bm_part(bm, blockIdx.x, nrow, rows_per_part, &r_begin, &r_end);
+  if (bm_frozen(bm, sys)) return;
   cplx<S> acc[TI][TI];
 #pragma unroll
   for (int a = 0; a < TI; ++a)
@@ -68,16 +72,25 @@ __global__ void __launch_bounds__(256) gram_partial_kernel(const cplx<S>* __rest
     }
 }
 
-// out[e] = sum over b of partial[b][e]: a CTA owns 32 consecutive e; its 8 warps take every 8th part
-// (lane = e, so reads coalesce), then the 8 warp sums are added in a fixed order.
+// out[e] = sum over b of partial[b][e] over the parts of system blockIdx.y (out at a stride of out_stride per
+// system): a CTA owns 32 consecutive e; its 8 warps take every 8th part (lane = e, so reads coalesce), then the
+// 8 warp sums are added in a fixed order.
 __global__ void __launch_bounds__(256) sum_partials_kernel(const double* __restrict__ partial, int npart, int n,
-                                                           double* __restrict__ out) {
+                                                           double* __restrict__ out, BatchMap bm, long out_stride) {
   __shared__ double red[8][33];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int e = blockIdx.x * 32 + lane;
+  const int sys = blockIdx.y;
+  if (bm_frozen(bm, sys)) return;
+  int b0 = 0, nbp = npart;
+  if (bm.sys_parts) {
+    b0 = bm.sys_parts[sys].x;
+    nbp = bm.sys_parts[sys].y;
+  }
+  out += (size_t)sys * out_stride;
   double s = 0.0;
   if (e < n)
-    for (int b = warp; b < npart; b += 8) s += partial[(size_t)b * n + e];
+    for (int b = warp; b < nbp; b += 8) s += partial[(size_t)(b0 + b) * n + e];
   red[warp][lane] = s;
   __syncthreads();
   if (warp == 0 && e < n) {
@@ -88,35 +101,50 @@ __global__ void __launch_bounds__(256) sum_partials_kernel(const double* __restr
 }
 
 // ----------------------------------------------------------------------------- update: Out = beta Out + S C
+// Row tiles of kTileRows rows, tile-strided over the grid; C of the tile's system is staged in shared memory
+// (again only when the system changes from one tile to the next).
 template <class S>
 __global__ void __launch_bounds__(256) update_kernel(const cplx<S>* __restrict__ Sx, int lds, int nin,
                                                      const zd* __restrict__ C, int ldc, int nout, int nrow,
-                                                     cplx<S>* __restrict__ Out, int ldo, S alpha, S beta) {
+                                                     cplx<S>* __restrict__ Out, int ldo, S alpha, S beta,
+                                                     BatchMap bm, long c_stride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cplx<S>* Cs = reinterpret_cast<cplx<S>*>(smem_raw);  // nin x nout
   const int tid = threadIdx.x;
-  for (int e = tid; e < nin * nout; e += blockDim.x) {
-    const int i = e / nout, j = e % nout;
-    const zd c = C[(size_t)i * ldc + j];
-    Cs[e] = mk<S>((S)c.re, (S)c.im);
-  }
-  __syncthreads();
   const int rows_per_blk = blockDim.x / nout;
   const int rr = tid / nout, j = tid % nout;
-  if (rr >= rows_per_blk) return;
-  for (long r = (long)blockIdx.x * rows_per_blk + rr; r < nrow; r += (long)gridDim.x * rows_per_blk) {
-    cplx<S> acc = mk<S>(0, 0);
-    const cplx<S>* srow = Sx + r * lds;
-    for (int i = 0; i < nin; ++i) cfma(acc, srow[i], Cs[i * nout + j]);
-    acc.re *= alpha;
-    acc.im *= alpha;
-    cplx<S>* o = Out + r * ldo + j;
-    if (beta != (S)0) {
-      const cplx<S> old = *o;
-      acc.re += beta * old.re;
-      acc.im += beta * old.im;
+  const long ntile = ((long)nrow + kTileRows - 1) / kTileRows;
+  int staged = -1;
+  for (long t = blockIdx.x; t < ntile; t += gridDim.x) {
+    const int sys = bm_sys_of_row(bm, t * kTileRows);  // uniform over the CTA
+    if (bm_frozen(bm, sys)) continue;
+    if (sys != staged) {
+      __syncthreads();
+      const zd* Cq = C + (size_t)sys * c_stride;
+      for (int e = tid; e < nin * nout; e += blockDim.x) {
+        const int i = e / nout, jj = e % nout;
+        const zd c = Cq[(size_t)i * ldc + jj];
+        Cs[e] = mk<S>((S)c.re, (S)c.im);
+      }
+      __syncthreads();
+      staged = sys;
     }
-    *o = acc;
+    if (rr >= rows_per_blk) continue;
+    const long r1 = min((long)nrow, (t + 1) * kTileRows);
+    for (long r = t * kTileRows + rr; r < r1; r += rows_per_blk) {
+      cplx<S> acc = mk<S>(0, 0);
+      const cplx<S>* srow = Sx + r * lds;
+      for (int i = 0; i < nin; ++i) cfma(acc, srow[i], Cs[i * nout + j]);
+      acc.re *= alpha;
+      acc.im *= alpha;
+      cplx<S>* o = Out + r * ldo + j;
+      if (beta != (S)0) {
+        const cplx<S> old = *o;
+        acc.re += beta * old.re;
+        acc.im += beta * old.im;
+      }
+      *o = acc;
+    }
   }
 }
 
@@ -125,16 +153,20 @@ template <class S>
 __global__ void __launch_bounds__(256) residual_kernel(const cplx<S>* __restrict__ AX, int ldax,
                                                        const cplx<S>* __restrict__ X, int ldx,
                                                        const double* __restrict__ theta, int m, int nrow,
-                                                       cplx<S>* __restrict__ R, int ldr, double* __restrict__ partial) {
+                                                       cplx<S>* __restrict__ R, int ldr, double* __restrict__ partial,
+                                                       int rows_per_part, BatchMap bm, long theta_stride) {
   __shared__ double red[8][32];
   const int tid = threadIdx.x;
-  const int j = tid % 32, rr = tid / 32;  // 8 rows per step, up to 32 columns
+  const int j = tid % 32, rr = tid / 32;  // 8 rows per step, up to 32 columns; one CTA per reduction part
+  long r_begin, r_end;
+  const int sys = bm_part(bm, blockIdx.x, nrow, rows_per_part, &r_begin, &r_end);
+  if (bm_frozen(bm, sys)) return;
   // a thread's few dozen rows are summed in S (FP64 instructions are scarce on this GPU), the partial sums
   // in FP64
   S acc = 0;
   if (j < m) {
-    const S th = (S)theta[j];
-    for (long r = (long)blockIdx.x * 8 + rr; r < nrow; r += (long)gridDim.x * 8) {
+    const S th = (S)theta[(size_t)sys * theta_stride + j];
+    for (long r = r_begin + rr; r < r_end; r += 8) {
       const cplx<S> ax = AX[r * ldax + j], x = X[r * ldx + j];
       const cplx<S> v = mk<S>(ax.re - th * x.re, ax.im - th * x.im);
       R[r * ldr + j] = v;
@@ -152,17 +184,20 @@ __global__ void __launch_bounds__(256) residual_kernel(const cplx<S>* __restrict
 
 template <class S>
 __global__ void precond_kernel(cplx<S>* __restrict__ R, int ldr, const double* __restrict__ diag,
-                               const double* __restrict__ theta, const int* __restrict__ active, int m, int nrow) {
+                               const double* __restrict__ theta, const int* __restrict__ active, int m, int nrow,
+                               BatchMap bm, long theta_stride) {
   const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= (long)nrow * m) return;
   const long r = e / m;
   const int j = (int)(e % m);
+  const int sys = bm_sys_of_row(bm, r);
+  if (bm_frozen(bm, sys)) return;
   cplx<S>& v = R[r * ldr + j];
-  if (!active[j]) {
+  if (!active[32 * sys + j]) {
     v = mk<S>(0, 0);
     return;
   }
-  const S th = (S)theta[j];
+  const S th = (S)theta[(size_t)sys * theta_stride + j];
   S d = (S)diag[r] - th;
   const S fl = (S)1e-2 * (fabs(th) > (S)1e-3 ? fabs(th) : (S)1e-3);
   if (fabs(d) < fl) d = fl;
@@ -181,30 +216,42 @@ __global__ void convert_cols_kernel(const cplx<Sa>* __restrict__ A, int lda, cpl
   B[r * ldb + j] = mk<Sb>((Sb)a.re, (Sb)a.im);
 }
 
-// ----------------------------------------------------------------------------- small Jacobi eigensolver
-__device__ __forceinline__ int rr_player(int i, int t, int n) { return i == 0 ? 0 : ((i - 1 + t) % (n - 1)) + 1; }
-
 
 // ----------------------------------------------------------------------------- small helpers
 // C = op(A) B for the small projected matrices (complex(8) storage), in arithmetic T: FP32 when the projected
 // problem is solved in FP32 (FP64 instructions are scarce on this GPU), FP64 for the final FP64 step
+constexpr int kGemmKS = 8;  // lanes per output element of the small products (K split, shuffle sum)
 template <class T>
-__global__ void small_gemm_kernel(const zd* __restrict__ A, int lda, int transA, const zd* __restrict__ B, int ldb,
-                                  zd* __restrict__ C, int ldc, int m, int n, int k) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= m * n) return;
-  const int i = e / n, j = e % n;
+__global__ void __launch_bounds__(128) small_gemm_kernel(const zd* __restrict__ A, int lda, int transA,
+                                                         const zd* __restrict__ B, int ldb, zd* __restrict__ C,
+                                                         int ldc, int m, int n, int k, BatchMap bm, long a_stride,
+                                                         long b_stride, long c_stride) {
+  const int sys = blockIdx.y;  // uniform over the CTA
+  if (bm_frozen(bm, sys)) return;
+  A += (size_t)sys * a_stride;
+  B += (size_t)sys * b_stride;
+  C += (size_t)sys * c_stride;
+  const int t = threadIdx.x & (kGemmKS - 1);
+  const int e = (int)((blockIdx.x * blockDim.x + threadIdx.x) / kGemmKS);
+  const bool ok = e < m * n;  // no early return: every lane reaches the shuffles
+  const int i = ok ? e / n : 0, j = ok ? e % n : 0;
   cplx<T> acc = mk<T>(0, 0);
-  for (int l = 0; l < k; ++l) {
-    const zd a = transA ? A[(size_t)l * lda + i] : A[(size_t)i * lda + l];
-    const zd b = B[(size_t)l * ldb + j];
-    const cplx<T> at = mk<T>((T)a.re, (T)a.im), bt = mk<T>((T)b.re, (T)b.im);
-    if (transA)
-      cfmac(acc, at, bt);
-    else
-      cfma(acc, at, bt);
+  if (ok)
+    for (int l = t; l < k; l += kGemmKS) {
+      const zd a = transA ? A[(size_t)l * lda + i] : A[(size_t)i * lda + l];
+      const zd b = B[(size_t)l * ldb + j];
+      const cplx<T> at = mk<T>((T)a.re, (T)a.im), bt = mk<T>((T)b.re, (T)b.im);
+      if (transA)
+        cfmac(acc, at, bt);
+      else
+        cfma(acc, at, bt);
+    }
+#pragma unroll
+  for (int o = kGemmKS / 2; o > 0; o >>= 1) {
+    acc.re += __shfl_xor_sync(0xffffffffu, acc.re, o);
+    acc.im += __shfl_xor_sync(0xffffffffu, acc.im, o);
   }
-  C[(size_t)i * ldc + j] = mk<double>((double)acc.re, (double)acc.im);
+  if (ok && t == 0) C[(size_t)i * ldc + j] = mk<double>((double)acc.re, (double)acc.im);
 }
 
 __device__ __forceinline__ double hash_noise(unsigned a, unsigned b, unsigned seed) {
@@ -218,17 +265,15 @@ __device__ __forceinline__ double hash_noise(unsigned a, unsigned b, unsigned se
 }
 
 // X0 = unit vectors at the m smallest diagonal entries (lowest transition energies) plus a small
-// deterministic perturbation.  Selection in two levels: each CTA takes the m smallest of its slice by
-// repeated arg-min (ties to the lower index), then one CTA repeats that over the CTAs' candidates.
-__global__ void __launch_bounds__(256) select_lowest_kernel(const double* __restrict__ val, const int* __restrict__ ids,
-                                                            int count, int m, double* __restrict__ out_val,
-                                                            int* __restrict__ out_idx) {
+// deterministic perturbation.  Selection by repeated arg-min over a slice (ties to the lower index): for one
+// large system in two levels (each CTA takes the m smallest of its slice, then one CTA repeats that over the
+// CTAs' candidates); for a batch one CTA per system over all of its rows.
+__device__ void select_m_smallest(const double* __restrict__ val, const int* __restrict__ ids, int r0, int r1, int m,
+                                  double* __restrict__ out_val, int* __restrict__ out_idx) {
   __shared__ double bv[256];
   __shared__ int bi[256];
   __shared__ int chosen[128];
   const int tid = threadIdx.x;
-  const int per = (count + gridDim.x - 1) / gridDim.x;
-  const int r0 = blockIdx.x * per, r1 = min(count, r0 + per);
   for (int s = 0; s < m; ++s) {
     double best = 1e300;
     int besti = 0x7fffffff;
@@ -260,22 +305,52 @@ __global__ void __launch_bounds__(256) select_lowest_kernel(const double* __rest
     }
     if (tid == 0) {
       chosen[s] = bi[0];
-      out_val[blockIdx.x * m + s] = bv[0];
-      out_idx[blockIdx.x * m + s] = bi[0] == 0x7fffffff ? -1 : bi[0];
+      out_val[s] = bv[0];
+      out_idx[s] = bi[0] == 0x7fffffff ? -1 : bi[0];
     }
     __syncthreads();
   }
 }
 
+__global__ void __launch_bounds__(256) select_lowest_kernel(const double* __restrict__ val, const int* __restrict__ ids,
+                                                            int count, int m, double* __restrict__ out_val,
+                                                            int* __restrict__ out_idx) {
+  const int per = (count + gridDim.x - 1) / gridDim.x;
+  const int r0 = blockIdx.x * per, r1 = min(count, r0 + per);
+  select_m_smallest(val, ids, r0, r1, m, out_val + blockIdx.x * m, out_idx + blockIdx.x * m);
+}
+
+// one CTA per system: indices relative to the system's first row, at out_idx + idx_stride q
+__global__ void __launch_bounds__(256) select_lowest_batch_kernel(const double* __restrict__ diag, BatchMap bm, int m,
+                                                                  double* __restrict__ cand_val,
+                                                                  int* __restrict__ out_idx, long idx_stride) {
+  const int q = blockIdx.x;
+  const int2 rw = bm.rows[q];
+  select_m_smallest(diag + rw.x, nullptr, 0, rw.y, m, cand_val + (size_t)q * m, out_idx + (size_t)q * idx_stride);
+}
+
+// rows of every system (nrow in all); the noise depends on the row within its system, so a system gets the
+// same start in a batch as alone; padding rows are zero
 template <class S>
-__global__ void init_guess_kernel(cplx<S>* X, int ldx, int dim, int m, const int* __restrict__ idx, unsigned seed) {
+__global__ void init_guess_kernel(cplx<S>* X, int ldx, int nrow, int m, const int* __restrict__ idx, unsigned seed,
+                                  BatchMap bm, long idx_stride) {
   const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= (long)dim * m) return;
+  if (e >= (long)nrow * m) return;
   const long r = e / m;
   const int j = (int)(e % m);
-  double re = 1e-3 * hash_noise((unsigned)r, (unsigned)j, seed);
-  double im = 1e-3 * hash_noise((unsigned)r, (unsigned)j + 7919u, seed);
-  if (idx[j] == r) re += 1.0;
+  const int sys = bm_sys_of_row(bm, r);
+  long lr = r;
+  if (bm.rows) {
+    const int2 rw = bm.rows[sys];
+    lr = r - rw.x;
+    if (lr >= rw.y) {
+      X[r * ldx + j] = mk<S>(0, 0);
+      return;
+    }
+  }
+  double re = 1e-3 * hash_noise((unsigned)lr, (unsigned)j, seed);
+  double im = 1e-3 * hash_noise((unsigned)lr, (unsigned)j + 7919u, seed);
+  if (idx[(size_t)sys * idx_stride + j] == lr) re += 1.0;
   X[r * ldx + j] = mk<S>((S)re, (S)im);
 }
 
@@ -286,8 +361,15 @@ __global__ void init_guess_kernel(cplx<S>* X, int ldx, int dim, int m, const int
 template <class S>
 __global__ void __launch_bounds__(256) heev_small_kernel(const zd* __restrict__ Ag, int lda, const int* __restrict__ nptr,
                                                          int nmax, int nwant, double* __restrict__ evals,
-                                                         zd* __restrict__ evecs, int ldv) {
+                                                         zd* __restrict__ evecs, int ldv, BatchMap bm, long a_stride,
+                                                         long e_stride, long v_stride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int sys = blockIdx.x;  // one CTA per system
+  if (bm_frozen(bm, sys)) return;
+  Ag += (size_t)sys * a_stride;
+  if (nptr) nptr += sys;
+  evals += (size_t)sys * e_stride;
+  evecs += (size_t)sys * v_stride;
   const int n = nptr ? min(max(*nptr, 0), nmax) : nmax;
   const int nw = min(nwant, n);
   const int tid = threadIdx.x, nt = blockDim.x;
@@ -300,11 +382,13 @@ __global__ void __launch_bounds__(256) heev_small_kernel(const zd* __restrict__ 
   S* e2 = e + nmax;
   S* lam = e2 + nmax;
   S* red = lam + nmax;
+  // Z, Dv, Lv: nwant vectors of stride n + 1 each, regions rounded to an even count (U aliases Dv as complex)
+  const size_t zsz = ((size_t)(nmax + 1) * nwant + 1) & ~(size_t)1;
   S* Z = red + 4;
-  S* Dv = Z + (size_t)nmax * nwant;
-  S* Lv = Dv + (size_t)nmax * nwant;
-  int* cl = reinterpret_cast<int*>(Lv + (size_t)nmax * nwant);
-  int* flag = cl + nwant;
+  S* Dv = Z + zsz;
+  S* Lv = Dv + zsz;
+  int* cl = reinterpret_cast<int*>(Lv + zsz);
+#pragma unroll 4
   for (int q = tid; q < n * n; q += nt) {
     const int r = q / n, c = q % n;
     const zd a = Ag[(size_t)r * lda + c], b = Ag[(size_t)c * lda + r];
@@ -312,14 +396,14 @@ __global__ void __launch_bounds__(256) heev_small_kernel(const zd* __restrict__ 
   }
   __syncthreads();
   if (n > 0) {
-    tridiag_cta<S>(A, lds, n, d, e, tau, p, flag);
+    tridiag_cta<S>(A, lds, n, d, e, tau, p);
     cplx<S>* U = reinterpret_cast<cplx<S>*>(Dv);
-    tridiag_eigvecs_cta<S>(A, lds, n, nw, d, e, tau, e2, lam, Z, Dv, Lv, cl, U, nw > 0 ? nw : 1, red);
+    tridiag_eigvecs_cta<S>(A, lds, n, nw, d, e, tau, e2, lam, Z, Dv, Lv, cl, U, n, red);
     for (int q = tid; q < nmax * nwant; q += nt) {
       const int r = q / nwant, k = q % nwant;
       zd v = mk<double>(0.0, 0.0);
       if (r < n && k < nw) {
-        const cplx<S> u = U[(size_t)r * nw + k];
+        const cplx<S> u = U[(size_t)k * n + r];
         v = mk<double>((double)u.re, (double)u.im);
       }
       evecs[(size_t)r * ldv + k] = v;
@@ -336,17 +420,25 @@ __global__ void __launch_bounds__(256) heev_small_kernel(const zd* __restrict__ 
 // Ms = D^-1/2 M D^-1/2, column k is kept when its residual diagonal (its squared distance from the span of the
 // kept columns before it) exceeds drop, and dropped otherwise.  For the r kept columns P, Ms[P,P] = R^H R and
 // B = D_P^-1/2 R^-1 makes S B orthonormal.  B (n x n, leading dimension ldb) holds those r columns first and
-// zeros elsewhere; *r_out = r.  Two barriers a step; the CTA is a 16 x 16 thread grid over the trailing matrix.
+// zeros elsewhere; *r_out = r.  One barrier a step: the Schur update reads row k of the residual, which that
+// step does not write; the CTA is a 16 x 16 thread grid over the trailing matrix.
 template <class S>
 __global__ void __launch_bounds__(256) pchol_basis_kernel(const zd* __restrict__ Mg, int ldm, int n, double drop,
-                                                          zd* __restrict__ B, int ldb, int* __restrict__ r_out) {
+                                                          zd* __restrict__ B, int ldb, int* __restrict__ r_out,
+                                                          BatchMap bm, long m_stride, long b_stride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int sys = blockIdx.x;  // one CTA per system
+  if (bm_frozen(bm, sys)) return;
+  Mg += (size_t)sys * m_stride;
+  B += (size_t)sys * b_stride;
+  r_out += sys;
   const int tid = threadIdx.x, nt = blockDim.x, tx = tid & 15, ty = tid >> 4;
   const int lds = n + 1;
-  cplx<S>* W = reinterpret_cast<cplx<S>*>(smem_raw);  // residual matrix
-  cplx<S>* R = W + (size_t)n * lds;                    // R[k][column], rows in kept order
+  cplx<S>* W = reinterpret_cast<cplx<S>*>(smem_raw);  // residual matrix, then R in kept order
+  cplx<S>* R = W + (size_t)n * lds;                    // R[k][column], rows in kept order; then R^-1
   S* dinv = reinterpret_cast<S*>(R + (size_t)n * lds);
-  int* perm = reinterpret_cast<int*>(dinv + n);
+  S* rinv = dinv + n;                                  // 1 / R[k][k]
+  int* perm = reinterpret_cast<int*>(rinv + n);
   __shared__ int s_r;
   for (int i = tid; i < n; i += nt) {
     const double m = Mg[(size_t)i * ldm + i].re;
@@ -364,43 +456,58 @@ __global__ void __launch_bounds__(256) pchol_basis_kernel(const zd* __restrict__
   for (int k = 0; k < n; ++k) {
     const S dk = W[(size_t)k * lds + k].re;
     if (!(dk > (S)drop)) continue;  // uniform decision: every thread reads the same settled value
-    const S rkk = sqrt(dk), irk = (S)1 / rkk;
+    const S rkk = sqrt(dk), irk = (S)1 / rkk, idk = irk * irk;
+    const cplx<S>* wk = W + (size_t)k * lds;
     // row r of R: columns k+1.. of the residual row k, scaled
     for (int j = tid; j < n; j += nt) {
       cplx<S> v = mk<S>(0, 0);
       if (j == k)
         v = mk<S>(rkk, 0);
       else if (j > k)
-        v = mk<S>(W[(size_t)k * lds + j].re * irk, W[(size_t)k * lds + j].im * irk);
+        v = mk<S>(wk[j].re * irk, wk[j].im * irk);
       R[(size_t)r * lds + j] = v;
     }
-    if (tid == 0) perm[r] = k;
-    __syncthreads();
-    // Schur complement on the trailing block: W[i][j] -= conj(R[r][i]) R[r][j]
+    if (tid == 0) {
+      perm[r] = k;
+      rinv[r] = irk;
+    }
+    // Schur complement on the trailing block: W[i][j] -= conj(W[k][i]) W[k][j] / dk
     for (int i = k + 1 + ty; i < n; i += 16) {
-      const cplx<S> ri = R[(size_t)r * lds + i];
+      const cplx<S> ri = wk[i];
+      const cplx<S> rs = mk<S>(ri.re * idk, ri.im * idk);
       for (int j = k + 1 + tx; j < n; j += 16) {
-        const cplx<S> rj = R[(size_t)r * lds + j];
+        const cplx<S> rj = wk[j];
         cplx<S>& w = W[(size_t)i * lds + j];
-        w.re -= ri.re * rj.re + ri.im * rj.im;
-        w.im -= ri.re * rj.im - ri.im * rj.re;
+        w.re -= rs.re * rj.re + rs.im * rj.im;
+        w.im -= rs.re * rj.im - rs.im * rj.re;
       }
     }
     ++r;
     __syncthreads();
   }
   if (tid == 0) s_r = r;
+  // R in kept order and compact (Rk[k][l] = R[k][perm[l]], l >= k) over the dead residual matrix
+  cplx<S>* Rk = W;
+  for (int k = ty; k < r; k += 16)
+    for (int l = tx; l < r; l += 16) Rk[(size_t)k * lds + l] = l >= k ? R[(size_t)k * lds + perm[l]] : mk<S>(0, 0);
   __syncthreads();
-  // R^-1 (r x r, upper triangular in kept order), one thread per column c, stored over W's rows
-  cplx<S>* Ri = W;
+  // R^-1 (r x r upper triangular), one thread per column c, over R's rows (dead); two partial sums per
+  // element halve the dependent chain
+  cplx<S>* Ri = R;
   for (int c = tid; c < r; c += nt) {
     for (int k = c + 1; k < r; ++k) Ri[(size_t)k * lds + c] = mk<S>(0, 0);
-    Ri[(size_t)c * lds + c] = mk<S>((S)1 / R[(size_t)c * lds + perm[c]].re, 0);
+    Ri[(size_t)c * lds + c] = mk<S>(rinv[c], 0);
     for (int k = c - 1; k >= 0; --k) {
-      cplx<S> acc = mk<S>(0, 0);
-      for (int l = k + 1; l <= c; ++l) cfma(acc, R[(size_t)k * lds + perm[l]], Ri[(size_t)l * lds + c]);
-      const S irkk = (S)1 / R[(size_t)k * lds + perm[k]].re;
-      Ri[(size_t)k * lds + c] = mk<S>(-acc.re * irkk, -acc.im * irkk);
+      const cplx<S>* rk = Rk + (size_t)k * lds;
+      cplx<S> a0 = mk<S>(0, 0), a1 = mk<S>(0, 0);
+      int l = k + 1;
+      for (; l + 1 <= c; l += 2) {
+        cfma(a0, rk[l], Ri[(size_t)l * lds + c]);
+        cfma(a1, rk[l + 1], Ri[(size_t)(l + 1) * lds + c]);
+      }
+      if (l <= c) cfma(a0, rk[l], Ri[(size_t)l * lds + c]);
+      const S ir = rinv[k];
+      Ri[(size_t)k * lds + c] = mk<S>(-(a0.re + a1.re) * ir, -(a0.im + a1.im) * ir);
     }
   }
   __syncthreads();
@@ -421,57 +528,68 @@ __global__ void __launch_bounds__(256) pchol_basis_kernel(const zd* __restrict__
 }  // namespace
 
 // ----------------------------------------------------------------------------- launchers
+// npart: reduction parts (bm.nparts for a batch map with a part table; else equal row ranges)
 template <class S>
 cudaError_t launch_gram(const cplx<S>* A, int lda, int p, const cplx<S>* B, int ldb, int q, int nrow, zd* out,
-                        double* partial, int npart, cudaStream_t s) {
+                        double* partial, int npart, cudaStream_t s, const BatchMap& bm, long out_stride) {
   if (p > 96 || q > 96) return cudaErrorInvalidValue;
+  if (bm.parts) npart = bm.nparts;
   const int rpp = (nrow + npart - 1) / npart;
   const int ti = (std::max(p, q) + 15) / 16;
   switch (ti) {
-    case 1: gram_partial_kernel<S, 1><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp); break;
-    case 2: gram_partial_kernel<S, 2><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp); break;
-    case 3: gram_partial_kernel<S, 3><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp); break;
-    case 4: gram_partial_kernel<S, 4><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp); break;
-    case 5: gram_partial_kernel<S, 5><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp); break;
-    default: gram_partial_kernel<S, 6><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp); break;
+    case 1: gram_partial_kernel<S, 1><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp, bm); break;
+    case 2: gram_partial_kernel<S, 2><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp, bm); break;
+    case 3: gram_partial_kernel<S, 3><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp, bm); break;
+    case 4: gram_partial_kernel<S, 4><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp, bm); break;
+    case 5: gram_partial_kernel<S, 5><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp, bm); break;
+    default: gram_partial_kernel<S, 6><<<npart, 256, 0, s>>>(A, lda, p, B, ldb, q, nrow, partial, rpp, bm); break;
   }
   ++g_launch_count;
   const int n = p * q * 2;
-  sum_partials_kernel<<<(n + 31) / 32, 256, 0, s>>>(partial, npart, n, reinterpret_cast<double*>(out)); ++g_launch_count;
+  sum_partials_kernel<<<dim3((n + 31) / 32, bm.nsys), 256, 0, s>>>(partial, npart, n, reinterpret_cast<double*>(out),
+                                                                    bm, 2 * out_stride);
+  ++g_launch_count;
   return cudaGetLastError();
 }
 
 template <class S>
 cudaError_t launch_update(const cplx<S>* Sx, int lds, int nin, const zd* C, int ldc, int nout, int nrow,
-                          cplx<S>* Out, int ldo, double alpha, double beta, cudaStream_t s) {
+                          cplx<S>* Out, int ldo, double alpha, double beta, cudaStream_t s, const BatchMap& bm,
+                          long c_stride) {
   if (nout > 256 || nin * nout > 8192) return cudaErrorInvalidValue;
   const size_t smem = (size_t)nin * nout * sizeof(cplx<S>);
   cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(update_kernel<S>), (size_t)smem);
   if (e != cudaSuccess) return e;
-  const int rows_per_blk = 256 / nout;
-  long nblk = (nrow + rows_per_blk - 1) / rows_per_blk;
+  long nblk = ((long)nrow + kTileRows - 1) / kTileRows;
   if (nblk > 152 * 16) nblk = 152 * 16;
-  update_kernel<S><<<(unsigned)nblk, 256, smem, s>>>(Sx, lds, nin, C, ldc, nout, nrow, Out, ldo, (S)alpha,
-                                                     (S)beta); ++g_launch_count;
+  update_kernel<S><<<(unsigned)nblk, 256, smem, s>>>(Sx, lds, nin, C, ldc, nout, nrow, Out, ldo, (S)alpha, (S)beta,
+                                                     bm, c_stride);
+  ++g_launch_count;
   return cudaGetLastError();
 }
 
 template <class S>
 cudaError_t launch_residual(const cplx<S>* AX, int ldax, const cplx<S>* X, int ldx, const double* theta, int m,
-                            int nrow, cplx<S>* R, int ldr, double* partial, int npart, double* norms2,
-                            cudaStream_t s) {
+                            int nrow, cplx<S>* R, int ldr, double* partial, int npart, double* norms2, cudaStream_t s,
+                            const BatchMap& bm, long theta_stride) {
   if (m > 32) return cudaErrorInvalidValue;
-  residual_kernel<S><<<npart, 256, 0, s>>>(AX, ldax, X, ldx, theta, m, nrow, R, ldr, partial); ++g_launch_count;
-  // partial is [npart][32]; sum column-wise
-  sum_partials_kernel<<<1, 256, 0, s>>>(partial, npart, 32, norms2); ++g_launch_count;
+  if (bm.parts) npart = bm.nparts;
+  const int rpp = (nrow + npart - 1) / npart;
+  residual_kernel<S><<<npart, 256, 0, s>>>(AX, ldax, X, ldx, theta, m, nrow, R, ldr, partial, rpp, bm, theta_stride);
+  ++g_launch_count;
+  // partial is [part][32]; summed column-wise per system
+  sum_partials_kernel<<<dim3(1, bm.nsys), 256, 0, s>>>(partial, npart, 32, norms2, bm, 32);
+  ++g_launch_count;
   return cudaGetLastError();
 }
 
 template <class S>
 cudaError_t launch_precond(cplx<S>* R, int ldr, const double* diag, const double* theta, const int* active, int m,
-                           int nrow, cudaStream_t s) {
+                           int nrow, cudaStream_t s, const BatchMap& bm, long theta_stride) {
   const long n = (long)nrow * m;
-  precond_kernel<S><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(R, ldr, diag, theta, active, m, nrow); ++g_launch_count;
+  precond_kernel<S><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(R, ldr, diag, theta, active, m, nrow, bm,
+                                                                theta_stride);
+  ++g_launch_count;
   return cudaGetLastError();
 }
 
@@ -492,40 +610,53 @@ cudaError_t launch_convert_cols(const cplx<Sa>* A, int lda, cplx<Sb>* B, int ldb
 
 template <class S>
 cudaError_t launch_heev_small(const zd* A, int lda, const int* nptr, int nmax, int nwant, double* evals, zd* evecs,
-                              int ldv, cudaStream_t s) {
+                              int ldv, cudaStream_t s, const BatchMap& bm, long a_stride, long e_stride,
+                              long v_stride) {
   if (nmax < 1 || nmax > 96 || nwant < 0 || nwant > nmax) return cudaErrorInvalidValue;
   const size_t smem = (size_t)nmax * (nmax + 1) * sizeof(cplx<S>) + (size_t)2 * nmax * sizeof(cplx<S>) +
-                      (size_t)(4 * nmax + 4) * sizeof(S) + (size_t)3 * nmax * nwant * sizeof(S) +
+                      (size_t)(4 * nmax + 4) * sizeof(S) + (size_t)3 * ((nmax + 1) * nwant + 1) * sizeof(S) +
                       (size_t)(nwant + 4) * sizeof(int) + 64;
   if (smem > 220 * 1024) return cudaErrorInvalidValue;
   cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(heev_small_kernel<S>), smem);
   if (e != cudaSuccess) return e;
-  heev_small_kernel<S><<<1, 256, smem, s>>>(A, lda, nptr, nmax, nwant, evals, evecs, ldv); ++g_launch_count;
+  heev_small_kernel<S><<<bm.nsys, 256, smem, s>>>(A, lda, nptr, nmax, nwant, evals, evecs, ldv, bm, a_stride, e_stride,
+                                                  v_stride);
+  ++g_launch_count;
   return cudaGetLastError();
 }
 
 template <class S>
-cudaError_t launch_pchol_basis(const zd* M, int ldm, int n, double drop, zd* B, int ldb, int* r_out, cudaStream_t s) {
+cudaError_t launch_pchol_basis(const zd* M, int ldm, int n, double drop, zd* B, int ldb, int* r_out, cudaStream_t s,
+                               const BatchMap& bm, long m_stride, long b_stride) {
   if (n < 1 || n > 96) return cudaErrorInvalidValue;
-  const size_t smem = (size_t)2 * n * (n + 1) * sizeof(cplx<S>) + (size_t)n * sizeof(S) + (size_t)n * sizeof(int) + 64;
+  const size_t smem = (size_t)2 * n * (n + 1) * sizeof(cplx<S>) + (size_t)2 * n * sizeof(S) + (size_t)n * sizeof(int) + 64;
   if (smem > 220 * 1024) return cudaErrorInvalidValue;
   cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(pchol_basis_kernel<S>), smem);
   if (e != cudaSuccess) return e;
-  pchol_basis_kernel<S><<<1, 256, smem, s>>>(M, ldm, n, drop, B, ldb, r_out); ++g_launch_count;
+  pchol_basis_kernel<S><<<bm.nsys, 256, smem, s>>>(M, ldm, n, drop, B, ldb, r_out, bm, m_stride, b_stride);
+  ++g_launch_count;
   return cudaGetLastError();
 }
 
-template cudaError_t launch_heev_small<float>(const zd*, int, const int*, int, int, double*, zd*, int, cudaStream_t);
-template cudaError_t launch_heev_small<double>(const zd*, int, const int*, int, int, double*, zd*, int, cudaStream_t);
-template cudaError_t launch_pchol_basis<float>(const zd*, int, int, double, zd*, int, int*, cudaStream_t);
-template cudaError_t launch_pchol_basis<double>(const zd*, int, int, double, zd*, int, int*, cudaStream_t);
+template cudaError_t launch_heev_small<float>(const zd*, int, const int*, int, int, double*, zd*, int, cudaStream_t,
+                                              const BatchMap&, long, long, long);
+template cudaError_t launch_heev_small<double>(const zd*, int, const int*, int, int, double*, zd*, int, cudaStream_t,
+                                               const BatchMap&, long, long, long);
+template cudaError_t launch_pchol_basis<float>(const zd*, int, int, double, zd*, int, int*, cudaStream_t,
+                                               const BatchMap&, long, long);
+template cudaError_t launch_pchol_basis<double>(const zd*, int, int, double, zd*, int, int*, cudaStream_t,
+                                                const BatchMap&, long, long);
 
 cudaError_t launch_small_gemm(const zd* A, int lda, int transA, const zd* B, int ldb, zd* C, int ldc, int m, int n,
-                              int k, cudaStream_t s, bool fp32) {
+                              int k, cudaStream_t s, bool fp32, const BatchMap& bm, long a_stride, long b_stride,
+                              long c_stride) {
+  const dim3 grid((unsigned)(((long)m * n * kGemmKS + 127) / 128), bm.nsys);
   if (fp32)
-    small_gemm_kernel<float><<<(m * n + 127) / 128, 128, 0, s>>>(A, lda, transA, B, ldb, C, ldc, m, n, k);
+    small_gemm_kernel<float><<<grid, 128, 0, s>>>(A, lda, transA, B, ldb, C, ldc, m, n, k, bm, a_stride, b_stride,
+                                                  c_stride);
   else
-    small_gemm_kernel<double><<<(m * n + 127) / 128, 128, 0, s>>>(A, lda, transA, B, ldb, C, ldc, m, n, k);
+    small_gemm_kernel<double><<<grid, 128, 0, s>>>(A, lda, transA, B, ldb, C, ldc, m, n, k, bm, a_stride, b_stride,
+                                                   c_stride);
   ++g_launch_count;
   return cudaGetLastError();
 }
@@ -539,24 +670,36 @@ cudaError_t launch_select_lowest(const double* diag, int dim, int m, int* idx, d
   return cudaGetLastError();
 }
 
+// batch: the m lowest rows of every system, relative indices at idx + idx_stride q (cand_val: nsys * m)
+cudaError_t launch_select_lowest_batch(const double* diag, const BatchMap& bm, int m, int* idx, long idx_stride,
+                                       double* cand_val, cudaStream_t s) {
+  if (m > 128 || !bm.rows) return cudaErrorInvalidValue;
+  select_lowest_batch_kernel<<<bm.nsys, 256, 0, s>>>(diag, bm, m, cand_val, idx, idx_stride); ++g_launch_count;
+  return cudaGetLastError();
+}
+
 template <class S>
-cudaError_t launch_init_guess(cplx<S>* X, int ldx, int dim, int m, const int* idx, unsigned seed, cudaStream_t s) {
-  const long n = (long)dim * m;
-  init_guess_kernel<S><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(X, ldx, dim, m, idx, seed); ++g_launch_count;
+cudaError_t launch_init_guess(cplx<S>* X, int ldx, int nrow, int m, const int* idx, unsigned seed, cudaStream_t s,
+                              const BatchMap& bm, long idx_stride) {
+  const long n = (long)nrow * m;
+  init_guess_kernel<S><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(X, ldx, nrow, m, idx, seed, bm, idx_stride);
+  ++g_launch_count;
   return cudaGetLastError();
 }
 
 #define WTB_INST_BLAS(S)                                                                                          \
   template cudaError_t launch_gram<S>(const cplx<S>*, int, int, const cplx<S>*, int, int, int, zd*, double*, int,  \
-                                      cudaStream_t);                                                              \
+                                      cudaStream_t, const BatchMap&, long);                                       \
   template cudaError_t launch_update<S>(const cplx<S>*, int, int, const zd*, int, int, int, cplx<S>*, int, double, \
-                                        double, cudaStream_t);                                                    \
+                                        double, cudaStream_t, const BatchMap&, long);                             \
   template cudaError_t launch_residual<S>(const cplx<S>*, int, const cplx<S>*, int, const double*, int, int,       \
-                                          cplx<S>*, int, double*, int, double*, cudaStream_t);                    \
+                                          cplx<S>*, int, double*, int, double*, cudaStream_t, const BatchMap&,     \
+                                          long);                                                                   \
   template cudaError_t launch_precond<S>(cplx<S>*, int, const double*, const double*, const int*, int, int,        \
-                                         cudaStream_t);                                                           \
+                                         cudaStream_t, const BatchMap&, long);                                    \
   template cudaError_t launch_copy_cols<S>(const cplx<S>*, int, cplx<S>*, int, int, int, cudaStream_t);           \
-  template cudaError_t launch_init_guess<S>(cplx<S>*, int, int, int, const int*, unsigned, cudaStream_t);
+  template cudaError_t launch_init_guess<S>(cplx<S>*, int, int, int, const int*, unsigned, cudaStream_t,           \
+                                            const BatchMap&, long);
 WTB_INST_BLAS(float)
 WTB_INST_BLAS(double)
 template cudaError_t launch_convert_cols<float, double>(const cplx<float>*, int, cplx<double>*, int, int, int,

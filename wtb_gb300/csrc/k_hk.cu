@@ -62,11 +62,10 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
   double* e2 = e + n;
   double* lam = e2 + n;
   double* red = lam + n;  // 4
-  double* Z = red + 4;    // n * n
-  double* Dv = Z + n * n; // n * n, then Lv n * n; the eigenvectors U (n x n complex) reuse both
-  double* Lv = Dv + n * n;
-  int* cl = reinterpret_cast<int*>(Lv + n * n);
-  int* flag = cl + n;
+  double* Z = red + 4;          // n vectors of stride n + 1
+  double* Dv = Z + n * (n + 1); // the same, then Lv; the eigenvectors U (n x n complex, column j = vector j)
+  double* Lv = Dv + n * (n + 1);  // reuse both
+  int* cl = reinterpret_cast<int*>(Lv + n * (n + 1));
   zd* U = reinterpret_cast<zd*>(Dv);
   __shared__ double rl[9];
   __shared__ int s_nocp;
@@ -98,7 +97,7 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
     if (m != c) A[c * ld + m] = mk<double>(acc.re, -acc.im);
   }
   __syncthreads();
-  tridiag_cta<double>(A, ld, n, d, e, tau, p, flag);
+  tridiag_cta<double>(A, ld, n, d, e, tau, p);
   tridiag_eigvecs_cta<double>(A, ld, n, n, d, e, tau, e2, lam, Z, Dv, Lv, cl, U, n, red);
   if (tid == 0) {
     int cnt = 0;
@@ -111,11 +110,11 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
   // and >= 0 (ZHEEV('L') returns it real; the sign does not reach any output)
   for (int q = tid; q < w * w; q += blockDim.x) {
     const int j = q / w, o = q % w;
-    const zd a0 = U[0 * n + j];
+    const zd a0 = U[j * n];
     const double m0 = sqrt(cabs2(a0));
     zd g = mk<double>(1.0, 0.0);
     if (m0 > 0.0) g = mk<double>(a0.re / m0, -a0.im / m0);
-    zd val = cmul(U[o * n + j], g);
+    zd val = cmul(U[j * n + o], g);
     if (o == 0) val = mk<double>(m0, 0.0);
     if (vec_all) vec_all[((size_t)k * w + j) * w + o] = val;
     const int sl = j - (nocp - nv);
@@ -393,8 +392,8 @@ cudaError_t launch_hk_eig(const zd* hr, const int* rvec, const int* ndegen, int 
                           zd* vec_all, double* eig_win, zd* vec_win, int* nocp, DevStatus* st, cudaStream_t s) {
   if (w > 64 || w < 1) return cudaErrorInvalidValue;
   const int n = w;
-  // A, phases, p, tau (complex); d, e, e2, lam, red; Z, Dv, Lv (n x n each); cluster ids and flag
-  const size_t smem = (size_t)(n * (n + 1) + nR + 2 * n) * sizeof(zd) + (size_t)(4 * n + 4 + 3 * n * n) * sizeof(double) +
+  // A, phases, p, tau (complex); d, e, e2, lam, red; Z, Dv, Lv (n x (n + 1) each); cluster ids
+  const size_t smem = (size_t)(n * (n + 1) + nR + 2 * n) * sizeof(zd) + (size_t)(4 * n + 4 + 3 * n * (n + 1)) * sizeof(double) +
                       (size_t)(n + 4) * sizeof(int) + 64;
   if (smem > 220 * 1024) return cudaErrorInvalidValue;
   cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(hk_eig_kernel), (size_t)smem);

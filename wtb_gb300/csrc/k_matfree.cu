@@ -110,14 +110,13 @@ __global__ void __launch_bounds__(256) mf_gather_kernel(const cplx<S>* __restric
 // the re and im rows of every slice as one 16-byte vector of 8 bf16 (the K-major rows of zt are 16-byte
 // aligned: ldk and the tile start are multiples of 8).  k' >= nk inside the last tile give zeros (x = 0).
 constexpr int kGatherKT = 8;
-__global__ void __launch_bounds__(256) mf_gather_bf16_kernel(const zf* __restrict__ X, int ldx, int c0, int nbc,
-                                                             const zd* __restrict__ vec_win, int nk, int nv, int nc,
-                                                             int w, uint16_t* __restrict__ zt, int ldk, int nslices,
-                                                             long slice_stride) {
+__device__ __forceinline__ void gather_bf16_tile(const zf* __restrict__ X, int ldx, int c0, int nbc,
+                                                 const zd* __restrict__ vec_win, int nk, int nv, int nc, int w,
+                                                 uint16_t* __restrict__ zt, int ldk, int nslices, long slice_stride,
+                                                 int kt0) {
   constexpr int KT = kGatherKT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nbnd = nv + nc, ncv = nc * nv, ww = w * w;
-  const int kt0 = blockIdx.x * KT;
   const int tkn = min(KT, nk - kt0);
   zf* Cs = reinterpret_cast<zf*>(smem_raw);  // [KT][nc][w]
   zf* Vs = Cs + KT * nc * w;                 // [KT][nv][w]
@@ -182,15 +181,32 @@ __global__ void __launch_bounds__(256) mf_gather_bf16_kernel(const zf* __restric
   }
 }
 
+__global__ void __launch_bounds__(256) mf_gather_bf16_kernel(const zf* __restrict__ X, int ldx, int c0, int nbc,
+                                                             const zd* __restrict__ vec_win, int nk, int nv, int nc,
+                                                             int w, uint16_t* __restrict__ zt, int ldk, int nslices,
+                                                             long slice_stride) {
+  gather_bf16_tile(X, ldx, c0, nbc, vec_win, nk, nv, nc, w, zt, ldk, nslices, slice_stride, blockIdx.x * kGatherKT);
+}
+
+// batch: CTA b takes tile tiles[b] = (system, first k-point) of the systems' Z panels; frozen systems are
+// skipped unless all (the final application) are wanted
+__global__ void __launch_bounds__(256) mf_gather_bf16_batch_kernel(const zf* __restrict__ X, int ldx, int c0, int nbc,
+                                                                   const MfSys* __restrict__ sys,
+                                                                   const int2* __restrict__ tiles, int nslices,
+                                                                   const int* __restrict__ frozen) {
+  const int2 t = tiles[blockIdx.x];
+  if (frozen && frozen[t.x]) return;
+  const MfSys& q = sys[t.x];
+  gather_bf16_tile(X + (size_t)q.row0 * ldx, ldx, c0, nbc, q.vec_win, q.nk, q.nv, q.nc, q.w, q.zt, q.ldk, nslices,
+                   q.slice_stride, t.y);
+}
+
 template <class S, class T>
-__global__ void __launch_bounds__(128) mf_scatter_kernel(const T* __restrict__ Tm, int ldt,
-                                                         const cplx<S>* __restrict__ X, int ldx,
-                                                         const zd* __restrict__ vec_win, const double* __restrict__ dE,
-                                                         int nk, int nv, int nc, int w, int nb, int nbg,
-                                                         cplx<S>* __restrict__ Y, int ldy, int c0) {
+__device__ __forceinline__ void scatter_k(const T* __restrict__ Tm, int ldt, const cplx<S>* __restrict__ X, int ldx,
+                                          const zd* __restrict__ vec_win, const double* __restrict__ dE, int nk,
+                                          int nv, int nc, int w, int nb, int nbg, cplx<S>* __restrict__ Y, int ldy,
+                                          int c0, int k, int b0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int k = blockIdx.x;
-  const int b0 = blockIdx.y * nbg;
   const int nbl = min(nbg, nb - b0);
   const int nbnd = nv + nc, ncv = nc * nv;
   cplx<S>* Cs = reinterpret_cast<cplx<S>*>(smem_raw);  // [nc][w]
@@ -233,6 +249,28 @@ __global__ void __launch_bounds__(128) mf_scatter_kernel(const T* __restrict__ T
     acc.im += d * x.im;
     Y[I * ldy + c0 + b0 + bb] = acc;
   }
+}
+
+template <class S, class T>
+__global__ void __launch_bounds__(128) mf_scatter_kernel(const T* __restrict__ Tm, int ldt,
+                                                         const cplx<S>* __restrict__ X, int ldx,
+                                                         const zd* __restrict__ vec_win, const double* __restrict__ dE,
+                                                         int nk, int nv, int nc, int w, int nb, int nbg,
+                                                         cplx<S>* __restrict__ Y, int ldy, int c0) {
+  scatter_k<S, T>(Tm, ldt, X, ldx, vec_win, dE, nk, nv, nc, w, nb, nbg, Y, ldy, c0, blockIdx.x, blockIdx.y * nbg);
+}
+
+// batch: CTA (b, g) takes k-point kpts[b] = (system, k) and column group g
+__global__ void __launch_bounds__(128) mf_scatter_batch_kernel(const zf* __restrict__ X, int ldx,
+                                                               const MfSys* __restrict__ sys,
+                                                               const int2* __restrict__ kpts, int nb, int nbg,
+                                                               zf* __restrict__ Y, int ldy, int c0,
+                                                               const int* __restrict__ frozen) {
+  const int2 t = kpts[blockIdx.x];
+  if (frozen && frozen[t.x]) return;
+  const MfSys& q = sys[t.x];
+  scatter_k<float, float>(q.Tm, q.ldt, X + (size_t)q.row0 * ldx, ldx, q.vec_win, q.dE, q.nk, q.nv, q.nc, q.w, nb, nbg,
+                          Y + (size_t)q.row0 * ldy, ldy, c0, t.y, blockIdx.y * nbg);
 }
 
 // C[M][N] = A[M][K] * B[N][K]^T, real, CUDA cores.  64 x 64 CTA tile, 4 x 4 per thread, K step 16.
@@ -359,6 +397,37 @@ cudaError_t launch_mf_scatter(const T* Tm, int ldt, const cplx<S>* X, int ldx, c
   if (e != cudaSuccess) return e;
   dim3 grid(nk, (nb + nbg - 1) / nbg);
   mf_scatter_kernel<S, T><<<grid, 128, smem, s>>>(Tm, ldt, X, ldx, vec_win, dE, nk, nv, nc, w, nb, nbg, Y, ldy, c0); ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mf_gather_batch(const zf* X, int ldx, int c0, int nb, const MfSys* sys, const int2* tiles,
+                                   int ntiles, int max_nv, int max_nc, int w, int nslices, const int* frozen,
+                                   cudaStream_t s) {
+  const int KT = kGatherKT;
+  const size_t smem =
+      (size_t)(KT * max_nc * w + KT * max_nv * w + KT * max_nc * max_nv * nb + KT * max_nc * w * nb) * sizeof(zf);
+  if (smem > 200 * 1024) return cudaErrorInvalidValue;
+  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(mf_gather_bf16_batch_kernel), smem);
+  if (e != cudaSuccess) return e;
+  mf_gather_bf16_batch_kernel<<<ntiles, 256, smem, s>>>(X, ldx, c0, nb, sys, tiles, nslices, frozen);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mf_scatter_batch(const zf* X, int ldx, const MfSys* sys, const int2* kpts, int nkpts, int max_nv,
+                                    int max_nc, int w, int nb, zf* Y, int ldy, int c0, const int* frozen,
+                                    cudaStream_t s) {
+  int nbg = nb;
+  auto smem_of = [&](int g) {
+    return (size_t)((max_nc + max_nv) * w + g * w * max_nv) * sizeof(zf) + (size_t)g * w * w * 2 * sizeof(float) + 16;
+  };
+  while (nbg > 1 && smem_of(nbg) > 96 * 1024) nbg = (nbg + 1) / 2;
+  const size_t smem = smem_of(nbg);
+  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(mf_scatter_batch_kernel), smem);
+  if (e != cudaSuccess) return e;
+  mf_scatter_batch_kernel<<<dim3(nkpts, (nb + nbg - 1) / nbg), 128, smem, s>>>(X, ldx, sys, kpts, nb, nbg, Y, ldy, c0,
+                                                                              frozen);
+  ++g_launch_count;
   return cudaGetLastError();
 }
 

@@ -14,6 +14,8 @@
 // Every mbarrier wait is bounded (2 s of %globaltimer); a wait that gives up sets the device status
 // word and an abort flag, the other roles stop at their next wait, and TMEM is freed before exit.
 #include <algorithm>
+#include <cstring>
+#include <utility>
 
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -133,9 +135,13 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-__global__ void __launch_bounds__(256, 1) tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA,
-                                                         const __grid_constant__ CUtensorMap mapB, TcArgs args) {
+// One 128 x 256 output tile at (m0, n0) of the product described by args, operands through the tensor maps
+// (kernel parameter or global memory).
+__device__ __forceinline__ void tc_gemm_tile(const CUtensorMap* mapA_p, const CUtensorMap* mapB_p,
+                                             const TcArgs& args, int m0, int n0) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
+  const CUtensorMap& mapA = *mapA_p;
+  const CUtensorMap& mapB = *mapB_p;
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   uint64_t* full = reinterpret_cast<uint64_t*>(base + STAGES * STAGE_BYTES);
   uint64_t* empty = full + STAGES;
@@ -166,7 +172,6 @@ __global__ void __launch_bounds__(256, 1) tc_gemm_kernel(const __grid_constant__
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
   const int total = args.npairs * args.kbn;
 
   volatile int* issued = abort_flag + 1;    // TMA stages issued by the producer
@@ -276,6 +281,48 @@ __global__ void __launch_bounds__(256, 1) tc_gemm_kernel(const __grid_constant__
   if (warp == 2) {
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
   }
+}
+
+__global__ void __launch_bounds__(256, 1) tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA,
+                                                         const __grid_constant__ CUtensorMap mapB, TcArgs args) {
+  tc_gemm_tile(&mapA, &mapB, args, blockIdx.y * BM, blockIdx.x * BN);
+}
+
+// A group of independent products (the operators of a batch of systems): tensor maps and arguments per
+// product in global memory (64-byte aligned), one CTA per output tile (product, row tile, column tile).
+struct TcGroup {
+  CUtensorMap mapA;
+  CUtensorMap mapB;
+  TcArgs args;
+};
+
+// kb_chunk > 0: this launch is range `chunk` of a split run (K blocks [chunk kb_chunk, (chunk + 1) kb_chunk) of
+// each product, added to C from the second range on, even and odd K blocks in two accumulators).  Products of
+// frozen systems are skipped; the CTA returns before it touches shared memory or TMEM.
+__global__ void __launch_bounds__(256, 1) tc_gemm_grouped_kernel(const TcGroup* __restrict__ groups,
+                                                                 const int4* __restrict__ tiles, int npairs,
+                                                                 int chunk, int kb_chunk,
+                                                                 const int* __restrict__ frozen, DevStatus* st) {
+  const int4 t = tiles[blockIdx.x];
+  if (frozen && frozen[t.x]) return;
+  const TcGroup* g = groups + t.x;
+  TcArgs a = g->args;
+  a.npairs = npairs;
+  a.st = st;
+  if (kb_chunk > 0) {
+    const int kb0 = chunk * kb_chunk;
+    if (kb0 >= a.kblocks) return;
+    a.kb0 = kb0;
+    a.kbn = min(kb_chunk, a.kblocks - kb0);
+    a.accumulate = chunk > 0 ? 1 : 0;
+    a.dual = 1;
+  } else {
+    a.kb0 = 0;
+    a.kbn = a.kblocks;
+    a.accumulate = 0;
+    a.dual = 0;
+  }
+  tc_gemm_tile(&g->mapA, &g->mapB, a, t.y * BM, t.z * BN);
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
@@ -411,5 +458,101 @@ cudaError_t tc_gemm_run_split(TcGemmPlan* plan, DevStatus* st, cudaStream_t s, i
 }
 
 void tc_gemm_plan_destroy(TcGemmPlan* plan) { delete plan; }
+
+struct TcGroupPlan {
+  TcGroup* d_groups = nullptr;
+  int4* d_tiles = nullptr;
+  int ntiles = 0;
+  int max_kblocks = 0;
+  ~TcGroupPlan() {
+    if (d_groups) cudaFree(d_groups);
+    if (d_tiles) cudaFree(d_tiles);
+  }
+};
+
+int tc_gemm_group_create(TcGroupPlan** plan, int n, const TcGroupDesc* d, int nslices, int npairs, const int* pair_a,
+                         const int* pair_b, std::string* msg) {
+  if (n < 1 || npairs < 1 || npairs > 8) {
+    *msg = "tc_gemm_group: bad arguments";
+    return WTB_EBADARG;
+  }
+  std::vector<TcGroup> h(n);
+  std::vector<int4> tiles;
+  std::vector<std::pair<int, int>> order;  // (K blocks, product): the longest tiles go first
+  for (int i = 0; i < n; ++i) {
+    const TcGroupDesc& q = d[i];
+    if (q.M % BM || q.N % BN || q.K % BK || q.ldc % 4) {
+      *msg = "tc_gemm_group: unsupported shape";
+      return WTB_EBADARG;
+    }
+    std::memset(&h[i], 0, sizeof(TcGroup));
+    if (!make_map(&h[i].mapA, q.A, q.K, q.M, nslices, BM, msg) || !make_map(&h[i].mapB, q.B, q.K, q.N, nslices, BN, msg))
+      return WTB_ECUDA;
+    TcArgs& a = h[i].args;
+    a.K = q.K;
+    a.kblocks = q.K / BK;
+    a.kb0 = 0;
+    a.kbn = a.kblocks;
+    a.m_valid = q.m_valid;
+    a.n_valid = q.n_valid;
+    a.ldc = q.ldc;
+    a.npairs = npairs;
+    for (int j = 0; j < npairs; ++j) {
+      a.pa[j] = pair_a[j];
+      a.pb[j] = pair_b[j];
+    }
+    a.C = q.C;
+    order.emplace_back(a.kblocks, i);
+  }
+  std::stable_sort(order.begin(), order.end(), [](const std::pair<int, int>& x, const std::pair<int, int>& y) {
+    return x.first > y.first;
+  });
+  int maxkb = 0;
+  for (const auto& o : order) {
+    const TcGroupDesc& q = d[o.second];
+    const int mt = (q.m_valid + BM - 1) / BM, nt = (q.n_valid + BN - 1) / BN;
+    for (int y = 0; y < mt; ++y)
+      for (int x = 0; x < nt; ++x) tiles.push_back(make_int4(o.second, y, x, 0));
+    maxkb = std::max(maxkb, o.first);
+  }
+  if (raise_smem_limit(reinterpret_cast<const void*>(tc_gemm_grouped_kernel), (size_t)kSmemBytes) != cudaSuccess) {
+    *msg = "tc_gemm_group: shared memory attribute rejected";
+    return WTB_ECUDA;
+  }
+  TcGroupPlan* p = new TcGroupPlan();
+  if (cudaMalloc(&p->d_groups, sizeof(TcGroup) * n) != cudaSuccess ||
+      cudaMalloc(&p->d_tiles, sizeof(int4) * tiles.size()) != cudaSuccess ||
+      cudaMemcpy(p->d_groups, h.data(), sizeof(TcGroup) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(p->d_tiles, tiles.data(), sizeof(int4) * tiles.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+    delete p;
+    *msg = "tc_gemm_group: device allocation failed";
+    return WTB_ENOMEM;
+  }
+  p->ntiles = (int)tiles.size();
+  p->max_kblocks = maxkb;
+  *plan = p;
+  return WTB_OK;
+}
+
+cudaError_t tc_gemm_group_run(TcGroupPlan* plan, int npairs, const int* frozen, DevStatus* st, cudaStream_t s) {
+  tc_gemm_grouped_kernel<<<plan->ntiles, 256, kSmemBytes, s>>>(plan->d_groups, plan->d_tiles, npairs, 0, 0, frozen, st);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t tc_gemm_group_run_split(TcGroupPlan* plan, int npairs, const int* frozen, DevStatus* st, cudaStream_t s,
+                                    int kb_chunk) {
+  if (kb_chunk < 1) kb_chunk = plan->max_kblocks;
+  for (int c = 0; c * kb_chunk < plan->max_kblocks; ++c) {
+    tc_gemm_grouped_kernel<<<plan->ntiles, 256, kSmemBytes, s>>>(plan->d_groups, plan->d_tiles, npairs, c, kb_chunk,
+                                                                 frozen, st);
+    ++g_launch_count;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+void tc_gemm_group_destroy(TcGroupPlan* plan) { delete plan; }
 
 }  // namespace wtb

@@ -43,78 +43,116 @@ __device__ __forceinline__ float fast_div<float>(float a, float b) {
   return __fdividef(a, b);
 }
 
-// Step 1.  A: n x n Hermitian (both triangles), row-major with leading dimension lda, in shared memory; it is
-// overwritten: column j below the diagonal holds v_j.  d[n], e[n-1] receive T; tau[n-1] the reflector scalars;
-// p[n] is scratch.  All threads of the block call it.
+// Householder reflector of column j of A (warp 0 alone): from x = conj(row j right of the diagonal) it writes
+// v_j over that row (v_j[0] = 1), beta to e[j], the scalar to tau[j] (zero: column already reduced) and the
+// diagonal entry to d[j].
 template <class S>
-__device__ void tridiag_cta(cplx<S>* A, int lda, int n, S* d, S* e, cplx<S>* tau, cplx<S>* p, int* flag) {
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+__device__ __forceinline__ void reflector_warp(cplx<S>* A, int lda, int n, int j, S* d, S* e, cplx<S>* tau) {
+  const int lane = threadIdx.x & 31;
+  const int L = n - 1 - j;
+  cplx<S>* v = A + (size_t)j * lda + (j + 1);
+  S sig = 0;
+  for (int i = 1 + lane; i < L; i += 32) sig += v[i].re * v[i].re + v[i].im * v[i].im;
+  sig = warp_allsum(sig);
+  const cplx<S> alpha = cconj(v[0]);
+  S beta;
+  cplx<S> t = mk<S>(0, 0), sc = mk<S>(0, 0);
+  if (sig == (S)0 && alpha.im == (S)0) {
+    beta = alpha.re;
+  } else {
+    const S an = sqrt(alpha.re * alpha.re + alpha.im * alpha.im + sig);
+    beta = alpha.re >= (S)0 ? -an : an;
+    t = mk<S>((beta - alpha.re) / beta, -alpha.im / beta);
+    const S dr = alpha.re - beta, di = alpha.im, dd = dr * dr + di * di;
+    sc = mk<S>(dr / dd, -di / dd);  // 1 / (alpha - beta)
+    for (int i = 1 + lane; i < L; i += 32) v[i] = cmul(cconj(v[i]), sc);
+  }
+  __syncwarp();  // every lane has read alpha = conj(v[0])
+  if (lane == 0) {
+    v[0] = mk<S>(1, 0);
+    e[j] = beta;
+    tau[j] = t;
+    d[j] = A[(size_t)j * lda + j].re;
+  }
+  __syncwarp();
+}
+
+// Step 1.  A: n x n Hermitian (both triangles), row-major with leading dimension lda, in shared memory.  On
+// return row j right of the diagonal holds the reflector: A[j][j+1+i] = v_j[i] (v_j[0] = 1), i < n-1-j (row j
+// is dead once column j has been reduced, and a row is contiguous for the products that use v_j).  d[n], e[n-1]
+// receive T; tau[n-1] the reflector scalars; p[n] is scratch.  All threads of the block call it; blockDim.x is
+// a multiple of 32.  Two barriers a step: the matrix-vector product, then the rank-2 update, during which warp 0
+// updates the next pivot row first and forms the next reflector from it while the other warps update the rest.
+template <class S>
+__device__ void tridiag_cta(cplx<S>* A, int lda, int n, S* d, S* e, cplx<S>* tau, cplx<S>* p) {
+  constexpr int TM = 4;  // lanes per row of the matrix-vector product
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+  const int tl = tid & (TM - 1), team = tid / TM, nteam = nt / TM;
+  if (n > 1 && warp == 0) reflector_warp<S>(A, lda, n, 0, d, e, tau);
+  __syncthreads();
   for (int j = 0; j < n - 1; ++j) {
     const int L = n - 1 - j;
-    cplx<S>* vcol = A + (size_t)(j + 1) * lda + j;  // v_j[i] = vcol[i * lda]
-    if (warp == 0) {
-      S sig = 0;
-      for (int i = 1 + lane; i < L; i += 32) {
-        const cplx<S> x = vcol[(size_t)i * lda];
-        sig += x.re * x.re + x.im * x.im;
-      }
-      sig = warp_allsum(sig);
-      const cplx<S> alpha = vcol[0];
-      bool skip = false;
-      S beta;
-      cplx<S> t = mk<S>(0, 0), sc = mk<S>(0, 0);
-      if (sig == (S)0 && alpha.im == (S)0) {
-        skip = true;
-        beta = alpha.re;
-      } else {
-        const S an = sqrt(alpha.re * alpha.re + alpha.im * alpha.im + sig);
-        beta = alpha.re >= (S)0 ? -an : an;
-        t = mk<S>((beta - alpha.re) / beta, -alpha.im / beta);
-        const S dr = alpha.re - beta, di = alpha.im, dd = dr * dr + di * di;
-        sc = mk<S>(dr / dd, -di / dd);  // 1 / (alpha - beta)
-      }
-      if (!skip)
-        for (int i = 1 + lane; i < L; i += 32) vcol[(size_t)i * lda] = cmul(vcol[(size_t)i * lda], sc);
-      if (lane == 0) {
-        vcol[0] = mk<S>(1, 0);
-        e[j] = beta;
-        tau[j] = t;
-        d[j] = A[(size_t)j * lda + j].re;
-        flag[0] = skip ? 1 : 0;
-      }
-    }
-    __syncthreads();
-    const bool skip = flag[0] != 0;
-    if (skip) {
-      __syncthreads();  // every thread has read the flag before warp 0 rewrites it
+    const cplx<S>* v = A + (size_t)j * lda + (j + 1);
+    cplx<S>* A22 = A + (size_t)(j + 1) * lda + (j + 1);
+    const cplx<S> tj = tau[j];
+    if (tj.re == (S)0 && tj.im == (S)0) {  // column j needs no reflection: A22 is unchanged
+      if (warp == 0 && j + 1 < n - 1) reflector_warp<S>(A, lda, n, j + 1, d, e, tau);
+      __syncthreads();
       continue;
     }
-    const cplx<S> tj = tau[j];
-    // p = tau A22 v (A22 = rows/columns j+1..n-1), one thread per row (no reduction on the critical path)
-    for (int r = tid; r < L; r += nt) {
-      const cplx<S>* row = A + (size_t)(j + 1 + r) * lda + (j + 1);
-      cplx<S> acc = mk<S>(0, 0);
-      for (int c = 0; c < L; ++c) cfma(acc, row[c], vcol[(size_t)c * lda]);
-      p[r] = cmul(tj, acc);
+    // p = tau A22 v: TM lanes per row, partial sums combined by shuffles inside the lane group (the loop
+    // bound is uniform, so every lane of a warp reaches the shuffles)
+    for (int r0 = 0; r0 < L; r0 += nteam) {
+      const int r = r0 + team;
+      cplx<S> a0 = mk<S>(0, 0), a1 = mk<S>(0, 0);
+      if (r < L) {
+        const cplx<S>* row = A22 + (size_t)r * lda;
+        int c = tl;
+        for (; c + TM < L; c += 2 * TM) {
+          cfma(a0, row[c], v[c]);
+          cfma(a1, row[c + TM], v[c + TM]);
+        }
+        if (c < L) cfma(a0, row[c], v[c]);
+      }
+      cplx<S> acc = mk<S>(a0.re + a1.re, a0.im + a1.im);
+#pragma unroll
+      for (int o = TM / 2; o > 0; o >>= 1) {
+        acc.re += __shfl_xor_sync(0xffffffffu, acc.re, o);
+        acc.im += __shfl_xor_sync(0xffffffffu, acc.im, o);
+      }
+      if (r < L && tl == 0) p[r] = cmul(tj, acc);
     }
     __syncthreads();
-    // K = -1/2 tau (p^H v), every warp for itself; w = p + K v;  A22 -= v w^H + w v^H
+    // K = -1/2 tau (p^H v), every warp for itself; w = p + K v;  A22 -= v w^H + w v^H, one warp per row
     cplx<S> sdot = mk<S>(0, 0);
-    for (int c = lane; c < L; c += 32) cfmac(sdot, p[c], vcol[(size_t)c * lda]);
+    for (int c = lane; c < L; c += 32) cfmac(sdot, p[c], v[c]);
     sdot.re = warp_allsum(sdot.re);
     sdot.im = warp_allsum(sdot.im);
     const cplx<S> K = cmul(mk<S>((S)-0.5 * tj.re, (S)-0.5 * tj.im), sdot);
-    for (int q = tid; q < L * L; q += nt) {
-      const int r = q / L, c = q - r * L;
-      const cplx<S> vr = vcol[(size_t)r * lda], vc = vcol[(size_t)c * lda];
+    auto update_row = [&](int r) {
+      const cplx<S> vr = v[r];
       const cplx<S> wr = mk<S>(p[r].re + K.re * vr.re - K.im * vr.im, p[r].im + K.re * vr.im + K.im * vr.re);
-      const cplx<S> wc = mk<S>(p[c].re + K.re * vc.re - K.im * vc.im, p[c].im + K.re * vc.im + K.im * vc.re);
-      // v_r conj(w_c) + w_r conj(v_c)
-      const S re = vr.re * wc.re + vr.im * wc.im + wr.re * vc.re + wr.im * vc.im;
-      const S im = vr.im * wc.re - vr.re * wc.im + wr.im * vc.re - wr.re * vc.im;
-      cplx<S>& a = A[(size_t)(j + 1 + r) * lda + (j + 1 + c)];
-      a.re -= re;
-      a.im -= im;
+      cplx<S>* arow = A22 + (size_t)r * lda;
+      for (int c = lane; c < L; c += 32) {
+        const cplx<S> vc = v[c];
+        const cplx<S> wc = mk<S>(p[c].re + K.re * vc.re - K.im * vc.im, p[c].im + K.re * vc.im + K.im * vc.re);
+        // v_r conj(w_c) + w_r conj(v_c)
+        const S re = vr.re * wc.re + vr.im * wc.im + wr.re * vc.re + wr.im * vc.im;
+        const S im = vr.im * wc.re - vr.re * wc.im + wr.im * vc.re - wr.re * vc.im;
+        arow[c].re -= re;
+        arow[c].im -= im;
+      }
+    };
+    if (nwarp == 1) {
+      for (int r = 0; r < L; ++r) update_row(r);
+      __syncwarp();
+      if (j + 1 < n - 1) reflector_warp<S>(A, lda, n, j + 1, d, e, tau);
+    } else if (warp == 0) {
+      update_row(0);
+      __syncwarp();
+      if (j + 1 < n - 1) reflector_warp<S>(A, lda, n, j + 1, d, e, tau);
+    } else {
+      for (int r = warp; r < L; r += nwarp - 1) update_row(r);
     }
     __syncthreads();
   }
@@ -136,15 +174,17 @@ __device__ __forceinline__ int sturm_count(const S* d, const S* e2, int n, S x, 
   return c;
 }
 
-// Steps 2-4 after tridiag_cta.  Computes the nwant lowest eigenpairs: lam[k] ascending, U[i * ldu + k] the
-// eigenvectors of A (complex, in shared memory).  Scratch (shared): e2[n], Z[n * nwant], Dv[n * nwant],
-// Lv[n * nwant] (Lv directly after Dv: U may alias Dv with ldu = nwant, both being dead by step 4),
+// Steps 2-4 after tridiag_cta.  Computes the nwant lowest eigenpairs: lam[k] ascending and the eigenvectors
+// of A column by column, U[k * ldu + i] (complex, shared memory, ldu >= n).  Scratch (shared): e2[n], and Z, Dv,
+// Lv of nwant * (n + 1) each (vector k at offset k * (n + 1): one thread per vector and one warp per vector
+// both read them without bank conflicts), Lv directly after Dv (U may alias Dv, both being dead by step 4),
 // cl[nwant] (ints), red[4].
 template <class S>
 __device__ void tridiag_eigvecs_cta(const cplx<S>* A, int lda, int n, int nwant, const S* d, const S* e,
                                     const cplx<S>* tau, S* e2, S* lam, S* Z, S* Dv, S* Lv, int* cl, cplx<S>* U,
                                     int ldu, S* red) {
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  const int ldz = n + 1;
   const S eps = sizeof(S) == 4 ? (S)5.96e-8 : (S)1.11e-16;
   for (int i = tid; i < n - 1; i += nt) e2[i] = e[i] * e[i];
   // Gershgorin interval and the scale of T (one warp)
@@ -164,7 +204,7 @@ __device__ void tridiag_eigvecs_cta(const cplx<S>* A, int lda, int n, int nwant,
     }
     if (lane == 0) {
       const S tn = fmax(fabs(lo), fabs(hi));
-      const S tiny = sizeof(S) == 4 ? (S)1e-30 : (S)1e-290;
+      const S tiny = tiny_of<S>();
       const S pivmin = fmax(emax2, (S)1) * tiny;
       red[0] = lo - (S)2 * eps * tn - pivmin;
       red[1] = hi + (S)2 * eps * tn + pivmin;
@@ -174,50 +214,67 @@ __device__ void tridiag_eigvecs_cta(const cplx<S>* A, int lda, int n, int nwant,
   }
   __syncthreads();
   const S tnorm = red[2], pivmin = red[3];
-  // step 2: bisection.  In FP64 it runs in FP32 on the rounded T (an FP64 instruction costs a warp dozens of
-  // FP32 ones on this part); the FP32 eigenvalue is then only the shift of the FP64 inverse iteration, and
-  // the FP64 eigenvalue is the Rayleigh quotient of the FP64 vector (step 3).
-  if constexpr (sizeof(S) == 8) {
-    float* df = reinterpret_cast<float*>(Z);  // Z is free until step 3
-    float* e2f = df + n;
-    for (int i = tid; i < n; i += nt) {
-      df[i] = (float)d[i];
-      if (i < n - 1) e2f[i] = (float)e2[i];
+  // step 2: multisection.  G lanes per eigenvalue (a power of two, G * nwant <= blockDim.x where possible) each
+  // evaluate the Sturm count at one of G interior points of the current interval; the first point whose count
+  // exceeds k closes the new interval, which shrinks by G + 1 per round.  In FP64 it runs in FP32 on the rounded
+  // T (an FP64 instruction costs a warp dozens of FP32 ones on this part): the FP32 eigenvalue is then only the
+  // shift of the FP64 inverse iteration, and the FP64 eigenvalue is the Rayleigh quotient of the FP64 vector.
+  {
+    using B = float;
+    const B* db;
+    const B* e2b;
+    B pivb;
+    if constexpr (sizeof(S) == 8) {
+      float* df = reinterpret_cast<float*>(Z);  // Z is free until step 3
+      float* e2f = df + n;
+      for (int i = tid; i < n; i += nt) {
+        df[i] = (float)d[i];
+        if (i < n - 1) e2f[i] = (float)e2[i];
+      }
+      __syncthreads();
+      db = df;
+      e2b = e2f;
+      pivb = fmaxf((float)(pivmin / tiny_of<S>() * 1e-30), 1e-30f);
+    } else {
+      db = reinterpret_cast<const B*>(d);
+      e2b = reinterpret_cast<const B*>(e2);
+      pivb = (B)pivmin;
     }
-    __syncthreads();
-    const float epsf = 5.96e-8f;
-    const float pivf = fmaxf((float)(pivmin / tiny_of<S>() * 1e-30), 1e-30f);
-    for (int k = tid; k < nwant; k += nt) {
-      float a = (float)red[0], b = (float)red[1];
-      const float w0 = b - a;
-      a -= 4.f * epsf * fabsf(w0) + pivf;
-      b += 4.f * epsf * fabsf(w0) + pivf;
+    const B epsb = 5.96e-8f;
+    int G = 1;
+    while (G < 32 && 2 * G * nwant <= nt) G *= 2;
+    const int gl = tid & (G - 1), grp = tid / G, ngrp = nt / G;
+    const unsigned gsh = (unsigned)(lane & ~(G - 1));
+    const unsigned gmask = G == 32 ? 0xffffffffu : ((1u << G) - 1u);
+    for (int k0 = 0; k0 < nwant; k0 += ngrp) {  // uniform loop: every lane reaches the warp votes
+      const int k = k0 + grp;
+      B a = (B)red[0], b = (B)red[1];
+      {
+        const B w0 = b - a;
+        a -= (B)4 * epsb * fabsf(w0) + pivb;
+        b += (B)4 * epsb * fabsf(w0) + pivb;
+      }
+      bool done = k >= nwant;
       for (int it = 0; it < 128; ++it) {
-        const float mid = 0.5f * (a + b);
-        if (b - a <= 2.f * epsf * fmaxf(fabsf(a), fabsf(b)) + pivf || mid <= a || mid >= b) break;
-        if (sturm_count<float>(df, e2f, n, mid, pivf) > k)
-          b = mid;
-        else
-          a = mid;
+        if (!__any_sync(0xffffffffu, !done)) break;
+        const B h = (b - a) / (B)(G + 1);
+        bool gt = false;
+        if (!done) gt = sturm_count<B>(db, e2b, n, a + h * (B)(gl + 1), pivb) > k;
+        const unsigned gm = (__ballot_sync(0xffffffffu, gt) >> gsh) & gmask;
+        if (!done) {
+          const int f = gm ? __ffs(gm) - 1 : G;  // first interior point with more than k eigenvalues below
+          const B na = f > 0 ? a + h * (B)f : a;
+          const B nb = f < G ? a + h * (B)(f + 1) : b;
+          if (!(na > a || nb < b) || nb - na <= (B)2 * epsb * fmaxf(fabsf(na), fabsf(nb)) + pivb) done = true;
+          a = na;
+          b = nb;
+        }
       }
-      lam[k] = (S)(0.5f * (a + b));
-    }
-  } else {
-    for (int k = tid; k < nwant; k += nt) {
-      S a = red[0], b = red[1];
-      for (int it = 0; it < 256; ++it) {
-        const S mid = (S)0.5 * (a + b);
-        if (b - a <= (S)2 * eps * fmax(fabs(a), fabs(b)) + pivmin || mid <= a || mid >= b) break;
-        if (sturm_count<S>(d, e2, n, mid, pivmin) > k)
-          b = mid;
-        else
-          a = mid;
-      }
-      lam[k] = (S)0.5 * (a + b);
+      if (k < nwant && gl == 0) lam[k] = (S)((B)0.5 * (a + b));
     }
   }
   __syncthreads();
-  // step 3: inverse iteration, one thread per eigenvector; column k of Z, Dv, Lv (stride nwant)
+  // step 3: inverse iteration, one thread per eigenvector (vector k at offset k * ldz of Z, Dv, Lv)
   const S tiny = eps * tnorm;
   // clusters from the (shift) eigenvalues: runs closer than 1e-3 ||T|| to their neighbour
   for (int k = tid; k < nwant; k += nt) {
@@ -225,20 +282,24 @@ __device__ void tridiag_eigvecs_cta(const cplx<S>* A, int lda, int n, int nwant,
     while (s0 > 0 && lam[s0] - lam[s0 - 1] <= (S)1e-3 * tnorm) --s0;
     cl[k] = s0;
   }
+  // FP32 shifts carry about 1e-7 of the spread of T: two passes reach FP32 accuracy, three FP64's
+  constexpr int kPasses = sizeof(S) == 4 ? 2 : 3;
   for (int k = tid; k < nwant; k += nt) {
-    // Dv holds the reciprocal pivots (one division per pivot; the solves multiply)
-    const S lk = lam[k];
-    S Dp = d[0] - lk;
+    S* zk = Z + (size_t)k * ldz;
+    S* dk = Dv + (size_t)k * ldz;  // reciprocal pivots (one division per pivot; the solves multiply)
+    S* lk = Lv + (size_t)k * ldz;
+    const S sh = lam[k];
+    S Dp = d[0] - sh;
     if (fabs(Dp) < tiny) Dp = tiny;
     S Dr = (S)1 / Dp;
-    Dv[k] = Dr;
+    dk[0] = Dr;
     for (int i = 1; i < n; ++i) {
       const S l = e[i - 1] * Dr;
-      Lv[(size_t)(i - 1) * nwant + k] = l;
-      Dp = (d[i] - lk) - l * e[i - 1];
+      lk[i - 1] = l;
+      Dp = (d[i] - sh) - l * e[i - 1];
       if (fabs(Dp) < tiny) Dp = tiny;
       Dr = (S)1 / Dp;
-      Dv[(size_t)i * nwant + k] = Dr;
+      dk[i] = Dr;
     }
     // start: deterministic pseudo-random entries in [-1, 1) (distinct for every k)
     for (int i = 0; i < n; ++i) {
@@ -246,33 +307,31 @@ __device__ void tridiag_eigvecs_cta(const cplx<S>* A, int lda, int n, int nwant,
       h ^= h >> 15;
       h *= 0x2c1b3c6du;
       h ^= h >> 12;
-      Z[(size_t)i * nwant + k] = (S)((double)(h & 0xffffffu) / 8388608.0 - 1.0);
+      zk[i] = (S)((double)(h & 0xffffffu) / 8388608.0 - 1.0);
     }
-    for (int pass = 0; pass < 3; ++pass) {
-      // L y = b (in place), y /= D, L^T x = y (in place)
-      S y = Z[k];
+    for (int pass = 0; pass < kPasses; ++pass) {
+      // L y = b (in place) and y /= D; L^T x = y (in place) with the largest magnitude on the way
+      S y = zk[0];
+      zk[0] = y * dk[0];
       for (int i = 1; i < n; ++i) {
-        const S v = Z[(size_t)i * nwant + k] - Lv[(size_t)(i - 1) * nwant + k] * y;
-        Z[(size_t)i * nwant + k] = v;
-        y = v;
+        y = zk[i] - lk[i - 1] * y;
+        zk[i] = y * dk[i];
       }
-      for (int i = 0; i < n; ++i) Z[(size_t)i * nwant + k] *= Dv[(size_t)i * nwant + k];
-      S x = Z[(size_t)(n - 1) * nwant + k];
+      S x = zk[n - 1], mx = fabs(x);
       for (int i = n - 2; i >= 0; --i) {
-        const S v = Z[(size_t)i * nwant + k] - Lv[(size_t)i * nwant + k] * x;
-        Z[(size_t)i * nwant + k] = v;
-        x = v;
+        x = zk[i] - lk[i] * x;
+        zk[i] = x;
+        mx = fmax(mx, fabs(x));
       }
-      S nrm = 0, mx = 0;
-      for (int i = 0; i < n; ++i) mx = fmax(mx, fabs(Z[(size_t)i * nwant + k]));
       if (!(mx > (S)0)) mx = (S)1;
       const S imx = (S)1 / mx;
+      S nrm = 0;
       for (int i = 0; i < n; ++i) {
-        const S v = Z[(size_t)i * nwant + k] * imx;
+        const S v = zk[i] * imx;
         nrm += v * v;
       }
       const S sc = imx / sqrt(nrm);
-      for (int i = 0; i < n; ++i) Z[(size_t)i * nwant + k] *= sc;
+      for (int i = 0; i < n; ++i) zk[i] *= sc;
     }
   }
   __syncthreads();
@@ -282,18 +341,20 @@ __device__ void tridiag_eigvecs_cta(const cplx<S>* A, int lda, int n, int nwant,
     int k1 = k0 + 1;
     while (k1 < nwant && cl[k1] == k0) ++k1;
     for (int jv = k0 + 1; jv < k1; ++jv) {
+      S* zj = Z + (size_t)jv * ldz;
       for (int iv = k0; iv < jv; ++iv) {
+        const S* zi = Z + (size_t)iv * ldz;
         S dot = 0;
-        for (int i = lane; i < n; i += 32) dot += Z[(size_t)i * nwant + iv] * Z[(size_t)i * nwant + jv];
+        for (int i = lane; i < n; i += 32) dot += zi[i] * zj[i];
         dot = warp_allsum(dot);
-        for (int i = lane; i < n; i += 32) Z[(size_t)i * nwant + jv] -= dot * Z[(size_t)i * nwant + iv];
+        for (int i = lane; i < n; i += 32) zj[i] -= dot * zi[i];
         __syncwarp();
       }
       S nrm = 0;
-      for (int i = lane; i < n; i += 32) nrm += Z[(size_t)i * nwant + jv] * Z[(size_t)i * nwant + jv];
+      for (int i = lane; i < n; i += 32) nrm += zj[i] * zj[i];
       nrm = warp_allsum(nrm);
       const S sc = nrm > (S)0 ? (S)1 / sqrt(nrm) : (S)0;
-      for (int i = lane; i < n; i += 32) Z[(size_t)i * nwant + jv] *= sc;
+      for (int i = lane; i < n; i += 32) zj[i] *= sc;
       __syncwarp();
     }
   }
@@ -301,22 +362,24 @@ __device__ void tridiag_eigvecs_cta(const cplx<S>* A, int lda, int n, int nwant,
   if constexpr (sizeof(S) == 8) {
     // FP64 eigenvalues: Rayleigh quotients z^T T z; inside a cluster the Rayleigh-Ritz of T on the cluster's
     // vectors (one warp per cluster; the small symmetric problem by cyclic Jacobi on lane 0; its matrices
-    // use the dead L D L^T storage at offset k0 n, which clusters starting at different k0 cannot overlap)
+    // use the dead L D L^T storage at offset k0 ldz, which clusters starting at different k0 cannot overlap)
     for (int k0 = warp; k0 < nwant; k0 += nw) {
       if (cl[k0] != k0) continue;
       int k1 = k0 + 1;
       while (k1 < nwant && cl[k1] == k0) ++k1;
       const int kc = k1 - k0;
-      S* Tc = Dv + (size_t)k0 * n;
-      S* Yc = Lv + (size_t)k0 * n;
+      S* Tc = Dv + (size_t)k0 * ldz;
+      S* Yc = Lv + (size_t)k0 * ldz;
       for (int a = 0; a < kc; ++a)
         for (int b = a; b < kc; ++b) {
+          const S* za = Z + (size_t)(k0 + a) * ldz;
+          const S* zb = Z + (size_t)(k0 + b) * ldz;
           S acc = 0;
           for (int i = lane; i < n; i += 32) {
-            S tz = d[i] * Z[(size_t)i * nwant + k0 + b];
-            if (i > 0) tz += e[i - 1] * Z[(size_t)(i - 1) * nwant + k0 + b];
-            if (i < n - 1) tz += e[i] * Z[(size_t)(i + 1) * nwant + k0 + b];
-            acc += Z[(size_t)i * nwant + k0 + a] * tz;
+            S tz = d[i] * zb[i];
+            if (i > 0) tz += e[i - 1] * zb[i - 1];
+            if (i < n - 1) tz += e[i] * zb[i + 1];
+            acc += za[i] * tz;
           }
           acc = warp_allsum(acc);
           if (lane == 0) {
@@ -388,36 +451,57 @@ __device__ void tridiag_eigvecs_cta(const cplx<S>* A, int lda, int n, int nwant,
       // Z_c <- Z_c Yc, row by row (each lane owns rows)
       for (int i = lane; i < n; i += 32) {
         S zrow[32];
-        for (int b = 0; b < kc; ++b) zrow[b] = Z[(size_t)i * nwant + k0 + b];
+        for (int b = 0; b < kc; ++b) zrow[b] = Z[(size_t)(k0 + b) * ldz + i];
         for (int a = 0; a < kc; ++a) {
           S acc = 0;
           for (int b = 0; b < kc; ++b) acc += zrow[b] * Yc[b * kc + a];
-          Z[(size_t)i * nwant + k0 + a] = acc;
+          Z[(size_t)(k0 + a) * ldz + i] = acc;
         }
       }
       __syncwarp();
     }
     __syncthreads();
   }
-  // step 4: u_k = H_0 (H_1 (... H_{n-2} z_k)), one warp per eigenvector
-  for (int k = warp; k < nwant; k += nw) {
-    for (int i = lane; i < n; i += 32) U[(size_t)i * ldu + k] = mk<S>(Z[(size_t)i * nwant + k], 0);
+  // step 4: u_k = H_0 (H_1 (... H_{n-2} z_k)), one warp per pair of eigenvectors (two independent reductions
+  // per reflector); v_j is row j of A right of the diagonal, contiguous
+  for (int k = 2 * warp; k < nwant; k += 2 * nw) {
+    const bool two = k + 1 < nwant;
+    cplx<S>* u0 = U + (size_t)k * ldu;
+    cplx<S>* u1 = U + (size_t)(two ? k + 1 : k) * ldu;
+    for (int i = lane; i < n; i += 32) {
+      u0[i] = mk<S>(Z[(size_t)k * ldz + i], 0);
+      if (two) u1[i] = mk<S>(Z[(size_t)(k + 1) * ldz + i], 0);
+    }
     __syncwarp();
     for (int j = n - 2; j >= 0; --j) {
       const cplx<S> tj = tau[j];
       if (tj.re == (S)0 && tj.im == (S)0) continue;
-      const cplx<S>* vcol = A + (size_t)(j + 1) * lda + j;
+      const cplx<S>* vj = A + (size_t)j * lda + (j + 1);
       const int L = n - 1 - j;
-      cplx<S> dot = mk<S>(0, 0);
-      for (int i = lane; i < L; i += 32) cfmac(dot, vcol[(size_t)i * lda], U[(size_t)(j + 1 + i) * ldu + k]);
-      dot.re = warp_allsum(dot.re);
-      dot.im = warp_allsum(dot.im);
-      const cplx<S> f = cmul(tj, dot);
+      cplx<S> d0 = mk<S>(0, 0), d1 = mk<S>(0, 0);
       for (int i = lane; i < L; i += 32) {
-        const cplx<S> v = vcol[(size_t)i * lda];
-        cplx<S>& u = U[(size_t)(j + 1 + i) * ldu + k];
-        u.re -= f.re * v.re - f.im * v.im;
-        u.im -= f.re * v.im + f.im * v.re;
+        const cplx<S> vv = vj[i];
+        cfmac(d0, vv, u0[j + 1 + i]);
+        if (two) cfmac(d1, vv, u1[j + 1 + i]);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        d0.re += __shfl_xor_sync(0xffffffffu, d0.re, o);
+        d0.im += __shfl_xor_sync(0xffffffffu, d0.im, o);
+        d1.re += __shfl_xor_sync(0xffffffffu, d1.re, o);
+        d1.im += __shfl_xor_sync(0xffffffffu, d1.im, o);
+      }
+      const cplx<S> f0 = cmul(tj, d0), f1 = cmul(tj, d1);
+      for (int i = lane; i < L; i += 32) {
+        const cplx<S> vv = vj[i];
+        cplx<S>& a0 = u0[j + 1 + i];
+        a0.re -= f0.re * vv.re - f0.im * vv.im;
+        a0.im -= f0.re * vv.im + f0.im * vv.re;
+        if (two) {
+          cplx<S>& a1 = u1[j + 1 + i];
+          a1.re -= f1.re * vv.re - f1.im * vv.im;
+          a1.im -= f1.re * vv.im + f1.im * vv.re;
+        }
       }
       __syncwarp();
     }

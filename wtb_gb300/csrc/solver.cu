@@ -203,33 +203,33 @@ struct Small {
   int* keep;
 };
 
-// Rayleigh-Ritz on the basis Sb (dim x nb, ld) with ASb = H Sb: returns C (nb x m) and theta (m).
+// Rayleigh-Ritz on the basis Sb (nrow x nb, ld) with ASb = H Sb: returns C (nb x m) and theta (m) of every
+// system of bm (small matrices nn = nb^2 apart, theta nb apart).
 // Orthonormalisation: Cholesky of the scaled Gram matrix in [X W P] order with deflation (directions whose
 // residual diagonal falls below tau are dropped; the r kept ones come first in B); the projected r x r
-// problem B^H G B is solved
-// by the tridiagonal route (small_eig.cuh).  The small problems run in precision S, or FP64 for
-// small_in_fp64.  A missing Ritz pair (r < m) has theta = 1e30 and a zero column in C.
+// problem B^H G B is solved by the tridiagonal route (small_eig.cuh).  The small problems run in precision S,
+// or FP64 for small_in_fp64.  A missing Ritz pair (r < m) has theta = 1e30 and a zero column in C.
 template <class S>
-int rayleigh_ritz(const cplx<S>* Sb, const cplx<S>* ASb, int ld, int nb, int m, int dim, double tau, Small& sm,
-                  double* partial, int npart, DevStatus* st, cudaStream_t s, std::string* msg,
-                  bool small_in_fp64) {
+int rayleigh_ritz(const cplx<S>* Sb, const cplx<S>* ASb, int ld, int nb, int m, int nrow, double tau, Small& sm,
+                  double* partial, int npart, DevStatus* st, cudaStream_t s, std::string* msg, bool small_in_fp64,
+                  const BatchMap& bm, long nn) {
   (void)st;
-  CK(launch_gram<S>(Sb, ld, nb, Sb, ld, nb, dim, sm.M, partial, npart, s));
-  CK(launch_gram<S>(Sb, ld, nb, ASb, ld, nb, dim, sm.G, partial, npart, s));
+  CK(launch_gram<S>(Sb, ld, nb, Sb, ld, nb, nrow, sm.M, partial, npart, s, bm, nn));
+  CK(launch_gram<S>(Sb, ld, nb, ASb, ld, nb, nrow, sm.G, partial, npart, s, bm, nn));
   if (small_in_fp64)
-    CK(launch_pchol_basis<double>(sm.M, nb, nb, tau, sm.B, nb, sm.keep, s));
+    CK(launch_pchol_basis<double>(sm.M, nb, nb, tau, sm.B, nb, sm.keep, s, bm, nn, nn));
   else
-    CK(launch_pchol_basis<S>(sm.M, nb, nb, tau, sm.B, nb, sm.keep, s));
+    CK(launch_pchol_basis<S>(sm.M, nb, nb, tau, sm.B, nb, sm.keep, s, bm, nn, nn));
   // the projected matrix B^H G B stays FP64 (its rounding would mix near-degenerate Ritz vectors); the basis
   // combination C = B Y may run in FP32 when the iteration does
   const bool f32 = !small_in_fp64 && sizeof(S) == 4;
-  CK(launch_small_gemm(sm.G, nb, 0, sm.B, nb, sm.T, nb, nb, nb, nb, s, false));
-  CK(launch_small_gemm(sm.B, nb, 1, sm.T, nb, sm.Gp, nb, nb, nb, nb, s, false));
+  CK(launch_small_gemm(sm.G, nb, 0, sm.B, nb, sm.T, nb, nb, nb, nb, s, false, bm, nn, nn, nn));
+  CK(launch_small_gemm(sm.B, nb, 1, sm.T, nb, sm.Gp, nb, nb, nb, nb, s, false, bm, nn, nn, nn));
   if (small_in_fp64)
-    CK(launch_heev_small<double>(sm.Gp, nb, sm.keep, nb, m, sm.theta, sm.Y, nb, s));
+    CK(launch_heev_small<double>(sm.Gp, nb, sm.keep, nb, m, sm.theta, sm.Y, nb, s, bm, nn, nb, nn));
   else
-    CK(launch_heev_small<S>(sm.Gp, nb, sm.keep, nb, m, sm.theta, sm.Y, nb, s));
-  CK(launch_small_gemm(sm.B, nb, 0, sm.Y, nb, sm.C, m, nb, m, nb, s, f32));
+    CK(launch_heev_small<S>(sm.Gp, nb, sm.keep, nb, m, sm.theta, sm.Y, nb, s, bm, nn, nb, nn));
+  CK(launch_small_gemm(sm.B, nb, 0, sm.Y, nb, sm.C, m, nb, m, nb, s, f32, bm, nn, nn, nn));
   return WTB_OK;
 }
 
@@ -245,11 +245,14 @@ int rayleigh_ritz(const cplx<S>* Sb, const cplx<S>* ASb, int ld, int nb, int m, 
 // orthonormalisation drops zero columns, so the first iteration needs no separate 2m-column path.
 
 struct LobCtl {
-  int it, total_it, nconv, stop, converged, restore, save, failed, best_it, pad[3];
+  int it, total_it, nconv, stop, converged, restore, save, failed, best_it, nworse, pad[2];
   double maxrel, best_maxrel, saved_rel, tol;
 };
 
-__global__ void lob_ctl_reset_kernel(LobCtl* c, double tol, int keep_total) {
+// One thread per system; block 0 also clears the loop's completion counter.
+__global__ void lob_ctl_reset_kernel(LobCtl* ctl, double tol, int keep_total, int* frozen, int* counter) {
+  const int q = blockIdx.x;
+  LobCtl* c = ctl + q;
   c->it = 0;
   if (!keep_total) {
     c->total_it = 0;
@@ -261,123 +264,176 @@ __global__ void lob_ctl_reset_kernel(LobCtl* c, double tol, int keep_total) {
   c->restore = 0;
   c->save = 0;
   c->best_it = 0;
+  c->nworse = 0;
   c->maxrel = 1e300;
   c->best_maxrel = 1e300;
   c->saved_rel = 1e300;
   c->tol = tol;
+  frozen[q] = 0;
+  if (q == 0) {
+    counter[0] = 0;
+    counter[1] = 0;
+  }
 }
 
-// One warp.  rel_j = ||r_j|| / |theta_j|; converged columns leave the active set (soft locking).
+// One warp per system.  rel_j = ||r_j|| / |theta_j|; converged columns leave the active set (soft locking).
 //  - breakdown guard: near the operator's rounding floor the running AX drifts from H X and LOBPCG can lose
 //    consistency (Ritz values falling far below the spectrum): the block with the lowest residual of the
 //    phase is kept (save), and a residual 10x above it after reaching 100 x tol restores it and ends the
 //    phase (restore);
+//  - floor guard (reduced precision): a best block within 1.5 x tol followed by one iteration that does not
+//    improve on it, or within 3 x tol followed by two, sits at the rounding floor of the FP32 iteration: the
+//    best block is restored and the FP64 Rayleigh-Ritz takes over;
 //  - stagnation guard (reduced precision): residuals within 100 x tol that have not improved by 10% over
 //    15 iterations are at the operator's rounding floor; the FP64 Rayleigh-Ritz takes over;
 //  - the iteration cap, a non-finite residual and a device status word end the loop as well.
+// A system that stops is frozen: the iteration kernels leave it alone until the next phase.  The last warp
+// to finish (a completion counter) sets the loop's condition: another pass while any system is running;
+// counter[1] holds the same answer for the host-driven loop.
 // Monitor lines follow the reference's MyEPSMonitor (src/module_slepc_solver.F90:101-116).
-__global__ void lob_control_kernel(LobCtl* c, const double* __restrict__ norms2, const double* __restrict__ theta,
-                                   int m, int nev, int maxit, int reduced, int* __restrict__ active,
-                                   const DevStatus* __restrict__ st, cudaGraphConditionalHandle h, int in_graph,
-                                   int monitor) {
+__global__ void lob_control_kernel(LobCtl* ctl, const double* __restrict__ norms2, const double* __restrict__ theta,
+                                   int theta_stride, int m, int nev, int maxit, int reduced, int* __restrict__ active,
+                                   const DevStatus* __restrict__ st, int* __restrict__ frozen, int* counter, int nsys,
+                                   cudaGraphConditionalHandle h, int in_graph, int monitor) {
   const int lane = threadIdx.x;
-  const double tol = c->tol;
-  double rel = 0.0;
-  int conv = 1, bad = 0;
-  if (lane < m) {
-    const double rn = sqrt(fmax(norms2[lane], 0.0));
-    const double th = theta[lane];
-    bad = !(isfinite(rn) && isfinite(th));
-    rel = rn / fmax(fabs(th), 1e-12);
-    conv = rel <= tol;
-    active[lane] = conv ? 0 : 1;
-  }
-  double mr = lane < nev ? rel : 0.0;
-  int nc = lane < nev ? conv : 0;
-  int first = lane < nev && !conv ? lane : 1 << 20;
+  const int q = blockIdx.x;
+  LobCtl* c = ctl + q;
+  if (!frozen[q]) {
+    norms2 += 32 * q;
+    theta += (size_t)q * theta_stride;
+    active += 32 * q;
+    const double tol = c->tol;
+    double rel = 0.0;
+    int conv = 1, bad = 0;
+    if (lane < m) {
+      const double rn = sqrt(fmax(norms2[lane], 0.0));
+      const double th = theta[lane];
+      bad = !(isfinite(rn) && isfinite(th));
+      rel = rn / fmax(fabs(th), 1e-12);
+      conv = rel <= tol;
+      active[lane] = conv ? 0 : 1;
+    }
+    double mr = lane < nev ? rel : 0.0;
+    int nc = lane < nev ? conv : 0;
+    int first = lane < nev && !conv ? lane : 1 << 20;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
-    nc += __shfl_xor_sync(0xffffffffu, nc, o);
-    bad |= __shfl_xor_sync(0xffffffffu, bad, o);
-    first = min(first, __shfl_xor_sync(0xffffffffu, first, o));
-  }
-  if (lane != 0) return;
-  int stop = 0;
-  c->save = 0;
-  if (st->code) {
-    stop = 1;
-  } else if (bad) {
-    c->failed = WTB_ENAN;
-    stop = 1;
-  } else {
-    c->maxrel = mr;
-    c->nconv = nc;
-    if (mr < c->saved_rel) {
-      c->saved_rel = mr;
-      c->save = 1;
-    } else if (c->saved_rel <= 100.0 * tol && mr > 10.0 * c->saved_rel) {
-      c->restore = 1;
-      c->converged = 1;
-      stop = 1;
+    for (int o = 16; o > 0; o >>= 1) {
+      mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+      nc += __shfl_xor_sync(0xffffffffu, nc, o);
+      bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+      first = min(first, __shfl_xor_sync(0xffffffffu, first, o));
     }
-    if (!stop && nc == nev) {
-      c->converged = 1;
-      stop = 1;
-    }
-    if (!stop) {
-      if (mr < 0.9 * c->best_maxrel) {
-        c->best_maxrel = mr;
-        c->best_it = c->it;
-      } else if (reduced && mr <= 100.0 * tol && c->it - c->best_it >= 15) {
-        c->converged = 1;
+    if (lane == 0) {
+      int stop = 0;
+      c->save = 0;
+      if (st->code) {
         stop = 1;
+      } else if (bad) {
+        c->failed = WTB_ENAN;
+        stop = 1;
+      } else {
+        c->maxrel = mr;
+        c->nconv = nc;
+        if (mr < c->saved_rel) {
+          c->saved_rel = mr;
+          c->save = 1;
+          c->nworse = 0;
+        } else {
+          c->nworse += 1;
+          if ((c->saved_rel <= 100.0 * tol && mr > 10.0 * c->saved_rel) ||
+              (reduced && ((c->saved_rel <= 1.5 * tol && c->nworse >= 1) || (c->saved_rel <= 3.0 * tol && c->nworse >= 2)))) {
+            c->restore = 1;
+            c->converged = 1;
+            stop = 1;
+          }
+        }
+        if (!stop && nc == nev) {
+          c->converged = 1;
+          stop = 1;
+        }
+        if (!stop) {
+          if (mr < 0.9 * c->best_maxrel) {
+            c->best_maxrel = mr;
+            c->best_it = c->it;
+          } else if (reduced && mr <= 100.0 * tol && c->it - c->best_it >= 15) {
+            c->converged = 1;
+            stop = 1;
+          }
+        }
+        if (!stop && c->total_it >= maxit) stop = 1;
       }
+      if (monitor) {
+        const int f = first < nev ? first : nev - 1;
+        if (nsys > 1)
+          printf("WTB-EPS system %4d %5d EPS pair=%4d value (error) %15.8E (%10.3E) max %10.3E\n", q, c->total_it,
+                 nc + 1, theta[f], sqrt(fmax(norms2[f], 0.0)) / fmax(fabs(theta[f]), 1e-12), mr);
+        else
+          printf("WTB-EPS %5d EPS pair=%4d value (error) %15.8E (%10.3E) max %10.3E\n", c->total_it, nc + 1, theta[f],
+                 sqrt(fmax(norms2[f], 0.0)) / fmax(fabs(theta[f]), 1e-12), mr);
+      }
+      if (!stop) {
+        c->it += 1;
+        c->total_it += 1;
+      }
+      c->stop = stop;
+      if (stop) frozen[q] = 1;
     }
-    if (!stop && c->total_it >= maxit) stop = 1;
+  } else if (lane == 0) {
+    c->save = 0;
   }
-  if (monitor) {
-    const int f = first < nev ? first : nev - 1;
-    printf("WTB-EPS %5d EPS pair=%4d value (error) %15.8E (%10.3E) max %10.3E\n", c->total_it, nc + 1, theta[f],
-           sqrt(fmax(norms2[f], 0.0)) / fmax(fabs(theta[f]), 1e-12), mr);
+  if (lane == 0) {
+    __threadfence();
+    if (atomicAdd(counter, 1) == nsys - 1) {
+      __threadfence();
+      int any = 0;
+      for (int i = 0; i < nsys; ++i) any |= (((volatile LobCtl*)ctl)[i].stop == 0) ? 1 : 0;
+      counter[0] = 0;
+      counter[1] = any;
+      if (in_graph) cudaGraphSetConditional(h, any ? 1u : 0u);
+    }
   }
-  if (!stop) {
-    c->it += 1;
-    c->total_it += 1;
-  }
-  c->stop = stop;
-  if (in_graph) cudaGraphSetConditional(h, stop ? 0u : 1u);
 }
 
-// dst[:, 0:ncol] = src[:, 0:ncol] when *flag is set
+// dst[:, 0:ncol] = src[:, 0:ncol] on the rows of the systems whose save (which = 0) or restore (1) flag is set
 template <class S>
-__global__ void cond_copy_kernel(const int* __restrict__ flag, const cplx<S>* __restrict__ src, int lds,
-                                 cplx<S>* __restrict__ dst, int ldd, int ncol, int nrow) {
-  if (!*flag) return;
+__global__ void cond_copy_kernel(const LobCtl* __restrict__ ctl, int which, const cplx<S>* __restrict__ src, int lds,
+                                 cplx<S>* __restrict__ dst, int ldd, int ncol, int nrow, BatchMap bm) {
   const long n = (long)nrow * ncol;
   for (long e = (long)blockIdx.x * blockDim.x + threadIdx.x; e < n; e += (long)gridDim.x * blockDim.x) {
     const long r = e / ncol;
     const int c = (int)(e % ncol);
+    const LobCtl& cq = ctl[bm_sys_of_row(bm, r)];
+    if (!(which ? cq.restore : cq.save)) continue;
     dst[r * ldd + c] = src[r * lds + c];
   }
 }
 
 // In place: X <- [X W P] C and P <- [W P] C[m:3m, :] for the basis and for its image under H.  A CTA stages
-// kUpdRows rows of the block in shared memory (so the in-place writes cannot overtake reads), then threads
-// (row, group of four output columns) form their outputs from the staged row and C.
-constexpr int kUpdRows = 32;
+// kUpdRows rows (one row tile) of the block in shared memory (so the in-place writes cannot overtake reads),
+// then threads (row, group of four output columns) form their outputs from the staged row and the C of the
+// tile's system (staged again only when the system changes from one tile to the next).
+constexpr int kUpdRows = kTileRows;
 template <class S>
 __global__ void __launch_bounds__(256) lob_update_kernel(cplx<S>* __restrict__ Sb, cplx<S>* __restrict__ ASb, int ld,
-                                                         int m, const zd* __restrict__ C, int dim) {
+                                                         int m, const zd* __restrict__ C, int nrow, BatchMap bm,
+                                                         long c_stride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nb = 3 * m;
   cplx<S>* Cs = reinterpret_cast<cplx<S>*>(smem_raw);  // [3m][m]
   cplx<S>* Rs = Cs + nb * m;                           // [kUpdRows][3m]
-  for (int e = threadIdx.x; e < nb * m; e += blockDim.x) Cs[e] = mk<S>((S)C[e].re, (S)C[e].im);
   const int ngrp = (m + 3) >> 2;       // groups of 4 output columns
   const int items = kUpdRows * ngrp;   // (row, group) pairs per pass
-  for (long r0 = (long)blockIdx.x * kUpdRows; r0 < dim; r0 += (long)gridDim.x * kUpdRows) {
-    const int nr = (int)min((long)kUpdRows, dim - r0);
+  int staged = -1;
+  for (long r0 = (long)blockIdx.x * kUpdRows; r0 < nrow; r0 += (long)gridDim.x * kUpdRows) {
+    const int sys = bm_sys_of_row(bm, r0);  // uniform over the CTA
+    if (bm_frozen(bm, sys)) continue;
+    if (sys != staged) {
+      __syncthreads();
+      const zd* Cq = C + (size_t)sys * c_stride;
+      for (int e = threadIdx.x; e < nb * m; e += blockDim.x) Cs[e] = mk<S>((S)Cq[e].re, (S)Cq[e].im);
+      staged = sys;
+    }
+    const int nr = (int)min((long)kUpdRows, nrow - r0);
     for (int which = 0; which < 2; ++which) {
       cplx<S>* base = (which ? ASb : Sb) + r0 * ld;
       __syncthreads();
@@ -436,12 +492,21 @@ struct CaptureSeg {
 };
 
 template <class S>
-int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, double tol, int maxit, Workspace& ws,
-                 DevStatus* st, cudaStream_t s, std::vector<double>* E, zd* Xout, SolveStats* stats,
-                 std::string* msg, double tol_refine) {
+int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L, int nev, int m, double tol,
+                       int maxit, Workspace& ws, DevStatus* st, cudaStream_t s, std::vector<double>* E, zd* Xout,
+                       std::vector<SolveStats>* stats, std::vector<int>* sys_status, std::string* msg,
+                       double tol_refine) {
+  const int nsys = L.bm.nsys;
+  const int nrow = L.nrow;
+  int mindim = nrow;
+  for (int d : L.dims) mindim = std::min(mindim, d);
+  if (nsys < 1 || (int)L.dims.size() != nsys || (nsys > 1 && (!L.bm.rows || !L.bm.parts || !L.bm.tile_sys))) {
+    if (msg) *msg = "inconsistent batch layout";
+    return WTB_EBADARG;
+  }
   if (m < nev) m = nev;
-  if (m > dim) m = dim;
-  if (nev < 1 || nev > dim) {
+  if (m > mindim) m = mindim;
+  if (nev < 1 || nev > mindim) {
     if (msg) *msg = "nev must be between 1 and the BSE dimension";
     return WTB_EBADARG;
   }
@@ -451,39 +516,45 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
     if (msg) *msg = "eigensolver block too large (3*block must be <= 96 in FP32, <= 78 in FP64)";
     return WTB_EBADARG;
   }
+  const int npart = nsys > 1 ? L.nparts : std::max(1, std::min(304, (nrow + 127) / 128));
   cudaError_t err = cudaSuccess;
-  cplx<S>* Sb = ws.get<cplx<S>>("lob_S", (size_t)dim * ld, &err, true);
-  cplx<S>* ASb = ws.get<cplx<S>>("lob_AS", (size_t)dim * ld, &err, true);
-  cplx<S>* Xbest = ws.get<cplx<S>>("lob_Xbest", (size_t)dim * m, &err);
+  cplx<S>* Sb = ws.get<cplx<S>>("lob_S", (size_t)nrow * ld, &err, true);
+  cplx<S>* ASb = ws.get<cplx<S>>("lob_AS", (size_t)nrow * ld, &err, true);
+  cplx<S>* Xbest = ws.get<cplx<S>>("lob_Xbest", (size_t)nrow * m, &err);
   Small sm;
-  const size_t nn = (size_t)nb * nb;
-  sm.M = ws.get<zd>("lob_M", nn, &err);
-  sm.G = ws.get<zd>("lob_G", nn, &err);
-  sm.B = ws.get<zd>("lob_B", nn, &err);
-  sm.Gp = ws.get<zd>("lob_Gp", nn, &err);
+  const long nn = (long)nb * nb;
+  sm.M = ws.get<zd>("lob_M", (size_t)nsys * nn, &err);
+  sm.G = ws.get<zd>("lob_G", (size_t)nsys * nn, &err);
+  sm.B = ws.get<zd>("lob_B", (size_t)nsys * nn, &err);
+  sm.Gp = ws.get<zd>("lob_Gp", (size_t)nsys * nn, &err);
   sm.U = nullptr;
-  sm.Y = ws.get<zd>("lob_Y", nn, &err);
-  sm.C = ws.get<zd>("lob_C", nn, &err);
-  sm.T = ws.get<zd>("lob_T", nn, &err);
+  sm.Y = ws.get<zd>("lob_Y", (size_t)nsys * nn, &err);
+  sm.C = ws.get<zd>("lob_C", (size_t)nsys * nn, &err);
+  sm.T = ws.get<zd>("lob_T", (size_t)nsys * nn, &err);
   sm.lam = nullptr;
   sm.dinv = nullptr;
-  sm.theta = ws.get<double>("lob_theta", nb, &err);
-  sm.keep = ws.get<int>("lob_keep", nb, &err);
-  // partial sums of the tall-skinny reductions: about 128 rows per part, at most two per SM
-  const int npart = std::max(1, std::min(304, (dim + 127) / 128));
+  sm.theta = ws.get<double>("lob_theta", (size_t)nsys * nb, &err);
+  sm.keep = ws.get<int>("lob_keep", nsys, &err);
   double* partial = ws.get<double>("lob_partial", (size_t)npart * nn * 2, &err);
-  double* norms2 = ws.get<double>("lob_norms2", 32, &err);
-  int* active = ws.get<int>("lob_active", 32, &err);
-  int* idx = ws.get<int>("lob_idx", 65 * 128, &err);
-  double* cand = ws.get<double>("lob_cand", 65 * 128, &err);
-  double* th_dev = ws.get<double>("lob_thcur", nb, &err);
-  LobCtl* ctl = ws.get<LobCtl>("lob_ctl", 1, &err);
-  zd* X64 = ws.get<zd>("fin_X", (size_t)dim * 2 * m, &err);
-  zd* T64 = ws.get<zd>("fin_T", (size_t)dim * m, &err);
+  double* norms2 = ws.get<double>("lob_norms2", (size_t)nsys * 32, &err);
+  int* active = ws.get<int>("lob_active", (size_t)nsys * 32, &err);
+  int* idx = ws.get<int>("lob_idx", nsys > 1 ? (size_t)nsys * m : 65 * 128, &err);
+  double* cand = ws.get<double>("lob_cand", nsys > 1 ? (size_t)nsys * m : 65 * 128, &err);
+  double* th_dev = ws.get<double>("lob_thcur", (size_t)nsys * nb, &err);
+  LobCtl* ctl = ws.get<LobCtl>("lob_ctl", nsys, &err);
+  int* frozen = ws.get<int>("lob_frozen", nsys, &err);
+  int* counter = ws.get<int>("lob_counter", 2, &err);
+  zd* X64 = ws.get<zd>("fin_X", (size_t)nrow * 2 * m, &err);
+  zd* T64 = ws.get<zd>("fin_T", (size_t)nrow * m, &err);
   if (err != cudaSuccess) {
     if (msg) *msg = std::string("device allocation failed: ") + cudaGetErrorString(err);
     return WTB_ENOMEM;
   }
+  BatchMap bm = L.bm;  // iteration kernels: frozen systems are left alone
+  bm.frozen = frozen;
+  bm.nparts = npart;
+  BatchMap bmf = bm;   // set-up and final step: every system
+  bmf.frozen = nullptr;
   cplx<S>* X = Sb;
   cplx<S>* W = Sb + m;
   cplx<S>* P = Sb + 2 * m;
@@ -501,70 +572,92 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
   // bodies); the default runs the whole solve as one graph launch
   const bool stream_mode = std::getenv("WTB_SOLVER_STREAM") != nullptr;
   const size_t upd_smem = (size_t)(nb * m + kUpdRows * nb) * sizeof(cplx<S>);
-  const int upd_grid = std::max(1, std::min(152 * 8, (dim + kUpdRows - 1) / kUpdRows));
-  const unsigned cp_grid = (unsigned)std::max(1, std::min(152 * 4, (int)(((long)dim * m + 255) / 256)));
+  const int upd_grid = std::max(1, std::min(152 * 8, (nrow + kUpdRows - 1) / kUpdRows));
+  const unsigned cp_grid = (unsigned)std::max(1, std::min(152 * 4, (int)(((long)nrow * m + 255) / 256)));
 
   // the pieces of one iteration, as stream launches (captured below)
   auto rr_and_update = [&]() -> int {
-    int r = rayleigh_ritz<S>(Sb, ASb, ld, nb, m, dim, tau, sm, partial, npart, st, s, msg, false);
+    int r = rayleigh_ritz<S>(Sb, ASb, ld, nb, m, nrow, tau, sm, partial, npart, st, s, msg, false, bm, nn);
     if (r) return r;
     CK(raise_smem_limit(reinterpret_cast<const void*>(lob_update_kernel<S>), upd_smem));
-    lob_update_kernel<S><<<upd_grid, 256, upd_smem, s>>>(Sb, ASb, ld, m, sm.C, dim);
+    lob_update_kernel<S><<<upd_grid, 256, upd_smem, s>>>(Sb, ASb, ld, m, sm.C, nrow, bm, nn);
     ++g_launch_count;
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(th_dev, sm.theta, sizeof(double) * m, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(th_dev, sm.theta, sizeof(double) * nsys * nb, cudaMemcpyDeviceToDevice, s));
     return WTB_OK;
   };
   auto check_and_decide = [&](cudaGraphConditionalHandle h) -> int {
-    CK(launch_residual<S>(AX, ld, X, ld, th_dev, m, dim, W, ld, partial, npart, norms2, s));
-    lob_control_kernel<<<1, 32, 0, s>>>(ctl, norms2, th_dev, m, nev, maxit, reduced ? 1 : 0, active, st, h,
-                                        stream_mode ? 0 : 1, monitor ? 1 : 0);
+    CK(launch_residual<S>(AX, ld, X, ld, th_dev, m, nrow, W, ld, partial, npart, norms2, s, bm, nb));
+    lob_control_kernel<<<nsys, 32, 0, s>>>(ctl, norms2, th_dev, nb, m, nev, maxit, reduced ? 1 : 0, active, st, frozen,
+                                           counter, nsys, h, stream_mode ? 0 : 1, monitor ? 1 : 0);
     ++g_launch_count;
     CK(cudaGetLastError());
-    cond_copy_kernel<S><<<cp_grid, 256, 0, s>>>(&ctl->save, X, ld, Xbest, m, m, dim);
+    cond_copy_kernel<S><<<cp_grid, 256, 0, s>>>(ctl, 0, X, ld, Xbest, m, m, nrow, bmf);
     ++g_launch_count;
     CK(cudaGetLastError());
     return WTB_OK;
   };
   auto restart_from_x = [&](cudaGraphConditionalHandle h) -> int {
-    CK(cudaMemset2DAsync(W, sizeof(cplx<S>) * ld, 0, sizeof(cplx<S>) * 2 * m, dim, s));
-    CK(cudaMemset2DAsync(AW, sizeof(cplx<S>) * ld, 0, sizeof(cplx<S>) * 2 * m, dim, s));
+    CK(cudaMemset2DAsync(W, sizeof(cplx<S>) * ld, 0, sizeof(cplx<S>) * 2 * m, nrow, s));
+    CK(cudaMemset2DAsync(AW, sizeof(cplx<S>) * ld, 0, sizeof(cplx<S>) * 2 * m, nrow, s));
     CK(op.apply(X, ld, 0, m, AX, ld, s));
     int r = rr_and_update();
     if (r) return r;
     return check_and_decide(h);
   };
   auto iteration = [&](cudaGraphConditionalHandle h) -> int {
-    CK(launch_precond<S>(W, ld, diag, th_dev, active, m, dim, s));
+    CK(launch_precond<S>(W, ld, diag, th_dev, active, m, nrow, s, bm, nb));
     // W <- W - X (X^H W);  P <- P - X (X^H P), AP <- AP - AX (X^H P)
-    CK(launch_gram<S>(X, ld, m, W, ld, m, dim, sm.T, partial, npart, s));
-    CK(launch_update<S>(X, ld, m, sm.T, m, m, dim, W, ld, -1.0, 1.0, s));
+    CK(launch_gram<S>(X, ld, m, W, ld, m, nrow, sm.T, partial, npart, s, bm, nn));
+    CK(launch_update<S>(X, ld, m, sm.T, m, m, nrow, W, ld, -1.0, 1.0, s, bm, nn));
     CK(op.apply(W, ld, 0, m, AW, ld, s));
-    CK(launch_gram<S>(X, ld, m, P, ld, m, dim, sm.T, partial, npart, s));
-    CK(launch_update<S>(X, ld, m, sm.T, m, m, dim, P, ld, -1.0, 1.0, s));
-    CK(launch_update<S>(AX, ld, m, sm.T, m, m, dim, AP, ld, -1.0, 1.0, s));
+    CK(launch_gram<S>(X, ld, m, P, ld, m, nrow, sm.T, partial, npart, s, bm, nn));
+    CK(launch_update<S>(X, ld, m, sm.T, m, m, nrow, P, ld, -1.0, 1.0, s, bm, nn));
+    CK(launch_update<S>(AX, ld, m, sm.T, m, m, nrow, AP, ld, -1.0, 1.0, s, bm, nn));
     int r = rr_and_update();
     if (r) return r;
     return check_and_decide(h);
   };
+  auto setup = [&]() -> int {
+    lob_ctl_reset_kernel<<<nsys, 1, 0, s>>>(ctl, tol, 0, frozen, counter);
+    ++g_launch_count;
+    CK(cudaMemset2DAsync(Sb, sizeof(cplx<S>) * ld, 0, sizeof(cplx<S>) * ld, nrow, s));
+    CK(cudaMemset2DAsync(ASb, sizeof(cplx<S>) * ld, 0, sizeof(cplx<S>) * ld, nrow, s));
+    if (nsys > 1) {
+      CK(launch_select_lowest_batch(diag, bmf, m, idx, m, cand, s));
+      CK(launch_init_guess<S>(X, ld, nrow, m, idx, 12345u, s, bmf, m));
+    } else {
+      CK(launch_select_lowest(diag, nrow, m, idx, cand, s));
+      CK(launch_init_guess<S>(X, ld, nrow, m, idx + 64 * m, 12345u, s));
+    }
+    return WTB_OK;
+  };
+  auto phase2_start = [&]() -> int {
+    cond_copy_kernel<S><<<cp_grid, 256, 0, s>>>(ctl, 1, Xbest, m, X, ld, m, nrow, bmf);
+    ++g_launch_count;
+    lob_ctl_reset_kernel<<<nsys, 1, 0, s>>>(ctl, tol_refine, 1, frozen, counter);
+    ++g_launch_count;
+    CK(cudaGetLastError());
+    return WTB_OK;
+  };
   // final FP64 Rayleigh-Ritz on a fresh application of the operator's most accurate arithmetic (the
   // iteration's AX is a running linear combination of cheaper applications)
   std::function<int()> final_step = [&]() -> int {
-    cond_copy_kernel<S><<<cp_grid, 256, 0, s>>>(&ctl->restore, Xbest, m, X, ld, m, dim);
+    cond_copy_kernel<S><<<cp_grid, 256, 0, s>>>(ctl, 1, Xbest, m, X, ld, m, nrow, bmf);
     ++g_launch_count;
     op.begin_refine();
     op.set_final(true);
     const cudaError_t fe = op.apply(X, ld, 0, m, AX, ld, s);
     op.set_final(false);
     CK(fe);
-    CK((launch_convert_cols<S, double>(X, ld, X64, 2 * m, m, dim, s)));
-    CK((launch_convert_cols<S, double>(AX, ld, X64 + m, 2 * m, m, dim, s)));
-    int r = rayleigh_ritz<double>(X64, X64 + m, 2 * m, m, m, dim, 1e-13, sm, partial, npart, st, s, msg, true);
+    CK((launch_convert_cols<S, double>(X, ld, X64, 2 * m, m, nrow, s)));
+    CK((launch_convert_cols<S, double>(AX, ld, X64 + m, 2 * m, m, nrow, s)));
+    int r = rayleigh_ritz<double>(X64, X64 + m, 2 * m, m, m, nrow, 1e-13, sm, partial, npart, st, s, msg, true, bmf, nn);
     if (r) return r;
     // Xout = X64 C[:, :nev]; residual = (AX64 C - Xout theta)
-    CK(launch_update<double>(X64, 2 * m, m, sm.C, m, nev, dim, Xout, nev, 1.0, 0.0, s));
-    CK(launch_update<double>(X64 + m, 2 * m, m, sm.C, m, nev, dim, T64, nev, 1.0, 0.0, s));
-    CK(launch_residual<double>(T64, nev, Xout, nev, sm.theta, nev, dim, T64, nev, partial, npart, norms2, s));
+    CK(launch_update<double>(X64, 2 * m, m, sm.C, m, nev, nrow, Xout, nev, 1.0, 0.0, s, bmf, nn));
+    CK(launch_update<double>(X64 + m, 2 * m, m, sm.C, m, nev, nrow, T64, nev, 1.0, 0.0, s, bmf, nn));
+    CK(launch_residual<double>(T64, nev, Xout, nev, sm.theta, nev, nrow, T64, nev, partial, npart, norms2, s, bmf, nb));
     return WTB_OK;
   };
 
@@ -573,9 +666,9 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
   if (stream_mode) {
     auto stopped = [&](bool* stop) -> int {
       int h = 0;
-      CK(cudaMemcpyAsync(&h, &ctl->stop, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(&h, counter + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
       CK(cudaStreamSynchronize(s));
-      *stop = h != 0;
+      *stop = h == 0;
       return WTB_OK;
     };
     auto run_loop = [&]() -> int {
@@ -588,26 +681,22 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
         if (r) return r;
       }
     };
-    lob_ctl_reset_kernel<<<1, 1, 0, s>>>(ctl, tol, 0);
-    ++g_launch_count;
-    CK(cudaMemset2DAsync(Sb, sizeof(cplx<S>) * ld, 0, sizeof(cplx<S>) * ld, dim, s));
-    CK(launch_select_lowest(diag, dim, m, idx, cand, s));
-    CK(launch_init_guess<S>(X, ld, dim, m, idx + 64 * m, 12345u, s));
+    if ((rc = setup())) return rc;
     if ((rc = restart_from_x(0))) return rc;
     if ((rc = run_loop())) return rc;
     if (two_phase) {
       op.begin_refine();
-      cond_copy_kernel<S><<<cp_grid, 256, 0, s>>>(&ctl->restore, Xbest, m, X, ld, m, dim);
-      ++g_launch_count;
-      lob_ctl_reset_kernel<<<1, 1, 0, s>>>(ctl, tol_refine, 1);
-      ++g_launch_count;
+      if ((rc = phase2_start())) return rc;
       if ((rc = restart_from_x(0))) return rc;
       if ((rc = run_loop())) return rc;
     }
     if ((rc = final_step())) return rc;
   } else {
   // the graph of this solve is reused when nothing it was captured with has changed
-  std::vector<uint64_t> sig = {(uint64_t)dim, (uint64_t)nev, (uint64_t)m, (uint64_t)maxit, (uint64_t)sizeof(S),
+  std::vector<uint64_t> sig = {(uint64_t)nrow, (uint64_t)nev, (uint64_t)m, (uint64_t)maxit, (uint64_t)sizeof(S),
+                               (uint64_t)nsys, (uint64_t)npart, (uint64_t)(uintptr_t)L.bm.tile_sys,
+                               (uint64_t)(uintptr_t)L.bm.rows, (uint64_t)(uintptr_t)L.bm.parts,
+                               (uint64_t)(uintptr_t)L.bm.part_sys, (uint64_t)(uintptr_t)L.bm.sys_parts,
                                (uint64_t)(uintptr_t)diag, (uint64_t)(uintptr_t)Xout, (uint64_t)(uintptr_t)st,
                                (uint64_t)(uintptr_t)s, (uint64_t)(uintptr_t)Sb, (uint64_t)(uintptr_t)ASb,
                                (uint64_t)(uintptr_t)Xbest, (uint64_t)(uintptr_t)sm.M, (uint64_t)(uintptr_t)sm.G,
@@ -615,8 +704,9 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
                                (uint64_t)(uintptr_t)sm.C, (uint64_t)(uintptr_t)sm.T, (uint64_t)(uintptr_t)sm.theta,
                                (uint64_t)(uintptr_t)sm.keep, (uint64_t)(uintptr_t)partial, (uint64_t)(uintptr_t)norms2,
                                (uint64_t)(uintptr_t)active, (uint64_t)(uintptr_t)idx, (uint64_t)(uintptr_t)cand,
-                               (uint64_t)(uintptr_t)th_dev, (uint64_t)(uintptr_t)ctl, (uint64_t)(uintptr_t)X64,
-                               (uint64_t)(uintptr_t)T64, (uint64_t)monitor};
+                               (uint64_t)(uintptr_t)th_dev, (uint64_t)(uintptr_t)ctl, (uint64_t)(uintptr_t)frozen,
+                               (uint64_t)(uintptr_t)counter, (uint64_t)(uintptr_t)X64, (uint64_t)(uintptr_t)T64,
+                               (uint64_t)monitor};
   {
     uint64_t tb, tr;
     std::memcpy(&tb, &tol, 8);
@@ -688,11 +778,8 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
     }
     // set-up: unit vectors at the m lowest transition energies (+ deterministic noise), W = P = 0
     rc = segment(G, {}, &tail, [&]() -> int {
-      lob_ctl_reset_kernel<<<1, 1, 0, s>>>(ctl, tol, 0);
-      ++g_launch_count;
-      CK(cudaMemset2DAsync(Sb, sizeof(cplx<S>) * ld, 0, sizeof(cplx<S>) * ld, dim, s));
-      CK(launch_select_lowest(diag, dim, m, idx, cand, s));
-      CK(launch_init_guess<S>(X, ld, dim, m, idx + 64 * m, 12345u, s));
+      int r = setup();
+      if (r) return r;
       return restart_from_x(h1);
     });
     if (rc) break;
@@ -707,10 +794,8 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
       // second phase: the accurate operator; fresh AX from the (best) block, search directions dropped
       op.begin_refine();
       rc = segment(G, tail, &tail, [&]() -> int {
-        cond_copy_kernel<S><<<cp_grid, 256, 0, s>>>(&ctl->restore, Xbest, m, X, ld, m, dim);
-        ++g_launch_count;
-        lob_ctl_reset_kernel<<<1, 1, 0, s>>>(ctl, tol_refine, 1);
-        ++g_launch_count;
+        int r = phase2_start();
+        if (r) return r;
         return restart_from_x(h2);
       });
       if (rc) break;
@@ -746,52 +831,87 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
   ws.graph_launches = g_launch_count.load() - captured0;
   }
   }
-  std::vector<double> th(nev), th_it(nev), nrm(nev);
-  LobCtl hc;
-  CK(cudaMemcpyAsync(th.data(), sm.theta, sizeof(double) * nev, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(th_it.data(), th_dev, sizeof(double) * nev, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(nrm.data(), norms2, sizeof(double) * nev, cudaMemcpyDeviceToHost, s));
-  CK(cudaMemcpyAsync(&hc, ctl, sizeof(hc), cudaMemcpyDeviceToHost, s));
+  // per system: final Ritz values, the iteration's last Ritz values, residual norms, loop state
+  std::vector<double> th((size_t)nsys * nb), th_it((size_t)nsys * nb), nrm((size_t)nsys * 32);
+  std::vector<LobCtl> hc(nsys);
+  CK(cudaMemcpyAsync(th.data(), sm.theta, sizeof(double) * nsys * nb, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(th_it.data(), th_dev, sizeof(double) * nsys * nb, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(nrm.data(), norms2, sizeof(double) * nsys * 32, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(hc.data(), ctl, sizeof(LobCtl) * nsys, cudaMemcpyDeviceToHost, s));
   DevStatus hst;
   CK(cudaMemcpyAsync(&hst, st, sizeof(hst), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   if (!stream_mode) {
-    const int it2 = two_phase ? hc.it : 0, it1 = hc.total_it - it2;
-    g_launch_count += body_launches[0] * (it1 - 1) + (two_phase ? body_launches[1] * (it2 - 1) : 0);
+    // the loop bodies ran once per pass of the slowest system
+    int pass1 = 0, pass2 = 0;
+    for (int q = 0; q < nsys; ++q) {
+      const int it2 = two_phase ? hc[q].it : 0;
+      pass1 = std::max(pass1, hc[q].total_it - it2);
+      pass2 = std::max(pass2, it2);
+    }
+    g_launch_count += body_launches[0] * (pass1 - 1) + (two_phase ? body_launches[1] * (pass2 - 1) : 0);
   }
-  if (stats) {
-    stats->iterations = hc.total_it;
-    stats->launches = 0;
-    stats->matvec_columns = (long)m * (hc.total_it + (two_phase ? 3 : 2));
-  }
+  if (stats) stats->assign(nsys, SolveStats());
+  if (sys_status) sys_status->assign(nsys, WTB_OK);
+  E->assign((size_t)nsys * nev, 0.0);
   if (hst.code) {
     if (msg) *msg = "device status " + std::to_string(hst.code) + " during the eigensolve";
     return hst.code >= 400 && hst.code < 500 ? WTB_ETIMEOUT : WTB_ENOCONV;
   }
-  if (hc.failed == WTB_ENAN) {
-    if (msg) *msg = "non-finite residual in the eigensolve";
-    return WTB_ENAN;
-  }
-  double maxrel = 0.0, shift = 0.0;
-  for (int j = 0; j < nev; ++j) {
-    const double rel = std::sqrt(std::max(nrm[j], 0.0)) / std::max(std::fabs(th[j]), 1e-12);
-    if (!std::isfinite(rel) || !std::isfinite(th[j])) {
-      if (msg) *msg = "non-finite eigenpair after the final Rayleigh-Ritz";
-      return WTB_ENAN;
+  int first_bad = WTB_OK;
+  for (int q = 0; q < nsys; ++q) {
+    int code = WTB_OK;
+    std::string why;
+    double maxrel = 0.0, shift = 0.0;
+    if (hc[q].failed == WTB_ENAN) {
+      code = WTB_ENAN;
+      why = "non-finite residual in the eigensolve";
     }
-    maxrel = std::max(maxrel, rel);
-    shift = std::max(shift, std::fabs(th[j] - th_it[j]));
+    for (int j = 0; j < nev && code == WTB_OK; ++j) {
+      const double t = th[(size_t)q * nb + j];
+      const double rel = std::sqrt(std::max(nrm[(size_t)q * 32 + j], 0.0)) / std::max(std::fabs(t), 1e-12);
+      if (!std::isfinite(rel) || !std::isfinite(t)) {
+        code = WTB_ENAN;
+        why = "non-finite eigenpair after the final Rayleigh-Ritz";
+        break;
+      }
+      maxrel = std::max(maxrel, rel);
+      shift = std::max(shift, std::fabs(t - th_it[(size_t)q * nb + j]));
+      (*E)[(size_t)q * nev + j] = t;
+    }
+    if (code == WTB_OK && !hc[q].converged) {
+      code = WTB_ENOCONV;
+      why = "eigensolver did not converge in " + std::to_string(maxit) + " iterations";
+    }
+    if (stats) {
+      SolveStats& st1 = (*stats)[q];
+      st1.iterations = hc[q].total_it;
+      st1.launches = 0;
+      st1.matvec_columns = (long)m * (hc[q].total_it + (two_phase ? 3 : 2));
+      st1.max_rel_residual = maxrel;
+      st1.refine_shift_max = shift;
+    }
+    if (sys_status) (*sys_status)[q] = code;
+    if (code != WTB_OK && first_bad == WTB_OK) {
+      first_bad = code;
+      if (msg) *msg = nsys > 1 ? "system " + std::to_string(q) + ": " + why : why;
+    }
   }
-  *E = th;
-  if (stats) {
-    stats->max_rel_residual = maxrel;
-    stats->refine_shift_max = shift;
-  }
-  if (!hc.converged) {
-    if (msg) *msg = "eigensolver did not converge in " + std::to_string(maxit) + " iterations";
-    return WTB_ENOCONV;
-  }
-  return WTB_OK;
+  return first_bad;
+}
+
+template <class S>
+int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, double tol, int maxit, Workspace& ws,
+                 DevStatus* st, cudaStream_t s, std::vector<double>* E, zd* Xout, SolveStats* stats,
+                 std::string* msg, double tol_refine) {
+  BatchLayout L;
+  L.nrow = dim;
+  L.dims.assign(1, dim);
+  std::vector<SolveStats> sv;
+  const int rc = lobpcg_solve_batch<S>(op, diag, L, nev, m, tol, maxit, ws, st, s, E, Xout, &sv, nullptr, msg,
+                                       tol_refine);
+  if (stats && !sv.empty()) *stats = sv[0];
+  return rc;
 }
 
 template int lobpcg_solve<float>(Operator<float>&, const double*, int, int, int, double, int, Workspace&, DevStatus*,
@@ -799,5 +919,11 @@ template int lobpcg_solve<float>(Operator<float>&, const double*, int, int, int,
 template int lobpcg_solve<double>(Operator<double>&, const double*, int, int, int, double, int, Workspace&,
                                   DevStatus*, cudaStream_t, std::vector<double>*, zd*, SolveStats*, std::string*,
                                   double);
+template int lobpcg_solve_batch<float>(Operator<float>&, const double*, const BatchLayout&, int, int, double, int,
+                                       Workspace&, DevStatus*, cudaStream_t, std::vector<double>*, zd*,
+                                       std::vector<SolveStats>*, std::vector<int>*, std::string*, double);
+template int lobpcg_solve_batch<double>(Operator<double>&, const double*, const BatchLayout&, int, int, double, int,
+                                        Workspace&, DevStatus*, cudaStream_t, std::vector<double>*, zd*,
+                                        std::vector<SolveStats>*, std::vector<int>*, std::string*, double);
 
 }  // namespace wtb

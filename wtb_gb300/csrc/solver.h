@@ -203,15 +203,39 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
                  Workspace& ws, DevStatus* st, cudaStream_t s, std::vector<double>* E, zd* Xout, SolveStats* stats,
                  std::string* msg, double tol_refine = 0.0);
 
+// A ragged batch of independent eigenproblems in one concatenated row space (BatchMap, device tables; the
+// solver sets its frozen flags and part count): nrow rows in all, nparts reduction parts, dims[q] the rows of
+// system q.  A single system needs only nrow and dims = {nrow}.
+struct BatchLayout {
+  BatchMap bm;
+  int nrow = 0;
+  int nparts = 0;
+  std::vector<int> dims;
+};
+
+// The lowest nev eigenpairs of every system of the batch, iterated together: one launch of each kernel covers
+// all systems still running, a system that has converged is frozen, and the loop ends when the last one
+// has.  diag and Xout in the concatenated rows; E (host) nsys x nev; per-system statistics and status codes.
+template <class S>
+int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L, int nev, int m, double tol,
+                       int maxit, Workspace& ws, DevStatus* st, cudaStream_t s, std::vector<double>* E, zd* Xout,
+                       std::vector<SolveStats>* stats, std::vector<int>* sys_status, std::string* msg,
+                       double tol_refine = 0.0);
+
 // extra launchers used by the solver
 template <class S>
 cudaError_t launch_heev_small(const zd* A, int lda, const int* nptr, int nmax, int nwant, double* evals, zd* evecs,
-                              int ldv, cudaStream_t s);
+                              int ldv, cudaStream_t s, const BatchMap& bm = BatchMap(), long a_stride = 0,
+                              long e_stride = 0, long v_stride = 0);
 template <class S>
-cudaError_t launch_pchol_basis(const zd* M, int ldm, int n, double drop, zd* B, int ldb, int* r_out, cudaStream_t s);
+cudaError_t launch_pchol_basis(const zd* M, int ldm, int n, double drop, zd* B, int ldb, int* r_out, cudaStream_t s,
+                               const BatchMap& bm = BatchMap(), long m_stride = 0, long b_stride = 0);
 cudaError_t launch_select_lowest(const double* diag, int dim, int m, int* idx, double* cand_val, cudaStream_t s);
+cudaError_t launch_select_lowest_batch(const double* diag, const BatchMap& bm, int m, int* idx, long idx_stride,
+                                       double* cand_val, cudaStream_t s);
 template <class S>
-cudaError_t launch_init_guess(cplx<S>* X, int ldx, int dim, int m, const int* idx, unsigned seed, cudaStream_t s);
+cudaError_t launch_init_guess(cplx<S>* X, int ldx, int nrow, int m, const int* idx, unsigned seed, cudaStream_t s,
+                              const BatchMap& bm = BatchMap(), long idx_stride = 0);
 void tc_gemm_set_valid(TcGemmPlan* p, int m_valid, int n_valid);
 
 }  // namespace wtb

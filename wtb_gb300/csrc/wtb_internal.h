@@ -118,27 +118,71 @@ template <class S>
 cudaError_t launch_dense_mv(const cplx<S>* H, int dim, const cplx<S>* X, int ldx, cplx<S>* Y, int ldy, int ncol,
                             cudaStream_t s);
 
+// ----------------------------------------------------------------------------- ragged batches
+// Independent eigenproblems solved together share one concatenated row space: system q owns rows
+// [rows[q].x, rows[q].x + rows[q].y), followed by zero rows up to a multiple of kTileRows, and row tile t
+// (kTileRows rows) belongs to system tile_sys[t].  Reductions over rows run in parts that never straddle two
+// systems: part p covers rows [parts[p].x, parts[p].y) of system part_sys[p], and system q owns parts
+// [sys_parts[q].x, sys_parts[q].x + sys_parts[q].y).  frozen[q] != 0: system q has left the iteration, whose
+// kernels then leave its rows and small matrices alone.  The default map is one system whose parts are
+// npart equal row ranges.  Small per-system matrices sit at a fixed stride from system to system.
+constexpr int kTileRows = 32;
+struct BatchMap {
+  int nsys = 1;
+  int nparts = 0;
+  const int* tile_sys = nullptr;
+  const int2* rows = nullptr;
+  const int2* parts = nullptr;
+  const int* part_sys = nullptr;
+  const int2* sys_parts = nullptr;
+  const int* frozen = nullptr;
+};
+
+__device__ __forceinline__ int bm_sys_of_row(const BatchMap& bm, long r) {
+  return bm.tile_sys ? bm.tile_sys[r / kTileRows] : 0;
+}
+__device__ __forceinline__ bool bm_frozen(const BatchMap& bm, int q) { return bm.frozen && bm.frozen[q] != 0; }
+// rows [*r0, *r1) and system of reduction part p (uniform parts of rpp rows when the map has no table)
+__device__ __forceinline__ int bm_part(const BatchMap& bm, int p, long nrow, long rpp, long* r0, long* r1) {
+  if (bm.parts) {
+    const int2 pr = bm.parts[p];
+    *r0 = pr.x;
+    *r1 = pr.y;
+    return bm.part_sys[p];
+  }
+  *r0 = (long)p * rpp;
+  *r1 = *r0 + rpp < nrow ? *r0 + rpp : nrow;
+  return 0;
+}
+
 // ----------------------------------------------------------------------------- block linear algebra
+// Batched forms: bm describes the systems (default: one); out_stride, c_stride, ... are the per-system
+// strides (in elements) of the small matrices.
 template <class S>
 cudaError_t launch_gram(const cplx<S>* A, int lda, int p, const cplx<S>* B, int ldb, int q, int nrow,
-                        zd* out, double* partial, int npart, cudaStream_t s);
+                        zd* out, double* partial, int npart, cudaStream_t s, const BatchMap& bm = BatchMap(),
+                        long out_stride = 0);
 template <class S>
 cudaError_t launch_update(const cplx<S>* Sx, int lds, int nin, const zd* C, int ldc, int nout, int nrow,
-                          cplx<S>* Out, int ldo, double alpha, double beta, cudaStream_t s);
+                          cplx<S>* Out, int ldo, double alpha, double beta, cudaStream_t s,
+                          const BatchMap& bm = BatchMap(), long c_stride = 0);
+// norms2 of system q at norms2 + 32 q
 template <class S>
 cudaError_t launch_residual(const cplx<S>* AX, int ldax, const cplx<S>* X, int ldx, const double* theta, int m,
                             int nrow, cplx<S>* R, int ldr, double* partial, int npart, double* norms2,
-                            cudaStream_t s);
+                            cudaStream_t s, const BatchMap& bm = BatchMap(), long theta_stride = 0);
+// active flags of system q at active + 32 q
 template <class S>
 cudaError_t launch_precond(cplx<S>* R, int ldr, const double* diag, const double* theta, const int* active, int m,
-                           int nrow, cudaStream_t s);
+                           int nrow, cudaStream_t s, const BatchMap& bm = BatchMap(), long theta_stride = 0);
 template <class S>
 cudaError_t launch_copy_cols(const cplx<S>* A, int lda, cplx<S>* B, int ldb, int ncol, int nrow, cudaStream_t s);
 template <class Sa, class Sb>
 cudaError_t launch_convert_cols(const cplx<Sa>* A, int lda, cplx<Sb>* B, int ldb, int ncol, int nrow,
                                 cudaStream_t s);
 cudaError_t launch_small_gemm(const zd* A, int lda, int transA, const zd* B, int ldb, zd* C, int ldc, int m, int n,
-                              int k, cudaStream_t s, bool fp32 = false);
+                              int k, cudaStream_t s, bool fp32 = false, const BatchMap& bm = BatchMap(),
+                              long a_stride = 0, long b_stride = 0, long c_stride = 0);
 
 // ----------------------------------------------------------------------------- matrix-free operator
 // Z[n][k'] with n = ((b*w + o)*w + p)*2 + ri (K-major for the V*Z contraction).
@@ -151,6 +195,26 @@ cudaError_t launch_mf_scatter(const T* Tm, int ldt, const cplx<S>* X, int ldx, c
 template <class S>
 cudaError_t launch_simt_gemm_tn(const S* A, int lda, const S* B, int ldb, S* C, int ldc, int M, int N, int K,
                                 cudaStream_t s);
+// The split-BF16 operator of one system of a batch (device array, one entry per system): its rows start at row0
+// of the concatenated block vectors; Z panel zt (nslices x [Npad][ldk] bf16, slice_stride apart), contraction
+// result Tm ([Mpad][ldt] fp32).
+struct MfSys {
+  long row0;
+  int nk, nv, nc, w;
+  int ldk, ldt;
+  long slice_stride;
+  const zd* vec_win;
+  const double* dE;
+  uint16_t* zt;
+  const float* Tm;
+};
+// gather over tiles (system, first k-point of 8), scatter over k-points (system, k)
+cudaError_t launch_mf_gather_batch(const zf* X, int ldx, int c0, int nb, const MfSys* sys, const int2* tiles,
+                                   int ntiles, int max_nv, int max_nc, int w, int nslices, const int* frozen,
+                                   cudaStream_t s);
+cudaError_t launch_mf_scatter_batch(const zf* X, int ldx, const MfSys* sys, const int2* kpts, int nkpts, int max_nv,
+                                    int max_nc, int w, int nb, zf* Y, int ldy, int c0, const int* frozen,
+                                    cudaStream_t s);
 cudaError_t launch_split_bf16(const double* V, int ldv, int rows, int cols, uint16_t* out, int ldo, long slice_stride,
                               int nslices, cudaStream_t s);
 cudaError_t launch_round_f32(const double* V, int ldv, int rows, int cols, float* out, int ldo, cudaStream_t s);
@@ -165,6 +229,21 @@ cudaError_t tc_gemm_run(TcGemmPlan* plan, DevStatus* st, cudaStream_t s);
 cudaError_t tc_gemm_run_split(TcGemmPlan* plan, DevStatus* st, cudaStream_t s, int kb_chunk);
 void tc_gemm_plan_destroy(TcGemmPlan* plan);
 int tc_gemm_available();
+// A group of independent products of that kind (one per system of a batch) in one launch.  Products of
+// systems with frozen[q] set are skipped (frozen may be null); npairs: slice products of this launch.
+struct TcGroupDesc {
+  const uint16_t* A;  // [nslices][M][K]
+  const uint16_t* B;  // [nslices][N][K]
+  float* C;
+  int M, N, K, ldc, m_valid, n_valid;
+};
+struct TcGroupPlan;
+int tc_gemm_group_create(TcGroupPlan** plan, int n, const TcGroupDesc* descs, int nslices, int npairs,
+                         const int* pair_a, const int* pair_b, std::string* msg);
+cudaError_t tc_gemm_group_run(TcGroupPlan* plan, int npairs, const int* frozen, DevStatus* st, cudaStream_t s);
+cudaError_t tc_gemm_group_run_split(TcGroupPlan* plan, int npairs, const int* frozen, DevStatus* st, cudaStream_t s,
+                                    int kb_chunk);
+void tc_gemm_group_destroy(TcGroupPlan* plan);
 
 // ----------------------------------------------------------------------------- spectrum
 cudaError_t launch_oscillators(const zd* A, int lda, int nev, int dim, const zd* hr, double* osc /*[8][nev]*/,
