@@ -219,15 +219,18 @@ typedef struct wtb_system {
 
 typedef struct wtb_batch wtb_batch;
 
-/* A pool of nworkers contexts on one device, each with its own stream and host thread, so that the solves of
- * several small systems overlap on the GPU.  The reference runs one bsesolver per process and input; a batch
- * of independent inputs is what its strain scans and mesh-convergence series do by relaunching it. */
+/* A batch solver on one device: one context per system plus one for the joint eigensolve.  The reference runs
+ * one bsesolver per process and input; a batch of independent inputs is what its strain scans and
+ * mesh-convergence series do by relaunching it.  nworkers (1..64) is kept for the ABI and not used. */
 int wtb_batch_create(wtb_batch** batch, int device, int nworkers);
 int wtb_batch_destroy(wtb_batch* batch);
 
-/* wtb_bsesolver for nsys independent systems: system i uses sys[i] and p[i] (p[i].nev <= nev_stride).  Systems
- * are handed to the workers largest first (cost ~ Nk^2 w^2 nev of the matrix-free operator).  Outputs, for the
- * first p[i].nev excitons of system i:
+/* wtb_bsesolver for nsys independent systems: system i uses sys[i] and p[i] (p[i].nev <= nev_stride).  With the
+ * split-BF16 matrix-free forms (every p[i] the same precision, tol, maxit and block) the whole batch is one CUDA
+ * graph launch: per-system set-up branches, one block eigensolve over all systems (each kernel launch covers
+ * every system still iterating; converged systems are frozen), per-system oscillator strengths; the graph is
+ * kept and relaunched while the batch keeps its shapes.  Other forms are solved system by system, largest
+ * first.  Outputs, for the first p[i].nev excitons of system i:
  *   E[i * nev_stride + n]               exciton energies (eV)
  *   act[(i * 8 + a) * nev_stride + n]   activities a = xx yy zz xy xz yz sp sm (dielbsev/dielbsep)
  *   status[i]                           WTB_OK or the system's error (text: wtb_batch_error(batch, i))
@@ -237,6 +240,10 @@ int wtb_batch_destroy(wtb_batch* batch);
 int wtb_batch_bsesolver(wtb_batch* batch, int nsys, const wtb_system* sys, const wtb_bse_params* p, int nev_stride,
                         double* E, double* act, int* status, int* iterations, double* wall_ms);
 const char* wtb_batch_error(const wtb_batch* batch, int i);
+/* The joint split-BF16 operator of the last wtb_batch_bsesolver call (its accurate arithmetic, as in the final
+ * Rayleigh-Ritz step) applied to ncol (1..16) vectors of every system: X and Y hold, system after system, the
+ * dim_i x ncol complex(8) column-major blocks (wtb_bse_matvec's layout). */
+int wtb_batch_matvec(wtb_batch* batch, int ncol, const double* X, double* Y);
 
 /* Number of CUDA kernels this library has launched in the process (instrumentation for benchmarks). */
 long long wtb_kernel_launch_count(void);

@@ -88,6 +88,7 @@ def _load():
         "wtb_batch_create": [C.POINTER(P), C.c_int, C.c_int],
         "wtb_batch_destroy": [P],
         "wtb_batch_bsesolver": [P, C.c_int, C.POINTER(CSystem), C.POINTER(CParams), C.c_int, dp, dp, ip, ip, dp],
+        "wtb_batch_matvec": [P, C.c_int, dp, dp],
     }
     for name, args in sigs.items():
         f = getattr(lib, name)
@@ -354,8 +355,8 @@ class Context:
 
 
 class Batch:
-    """A pool of ``nworkers`` contexts on one device solving independent systems concurrently
-    (``wtb_batch_*``)."""
+    """Independent systems solved together on one device (``wtb_batch_*``): the split-BF16 forms as one joint
+    eigensolve in one graph launch, other forms system by system."""
 
     def __init__(self, device: int = 0, nworkers: int = 8):
         h = C.c_void_p()
@@ -407,3 +408,19 @@ class Batch:
             bad = next(i for i in range(n) if status[i])
             raise WTBError(int(r), f"wtb_batch_bsesolver: system {bad}: {out[bad]['error']}")
         return out, float(wall[0])
+
+    def matvec(self, Xs):
+        """The joint operator of the last ``bsesolver`` call applied to one block per system: Xs[i] is
+        (dim_i, ncol) complex; returns the list of H_i X_i."""
+        ncol = Xs[0].shape[1]
+        X = np.concatenate([np.asfortranarray(x, dtype=np.complex128).reshape(-1, order="F") for x in Xs])
+        Y = np.zeros_like(X)
+        r = _lib.wtb_batch_matvec(self._h, int(ncol), _dp(X), _dp(Y))
+        if r:
+            raise WTBError(r, "wtb_batch_matvec failed")
+        out, off = [], 0
+        for x in Xs:
+            n = x.shape[0] * ncol
+            out.append(Y[off:off + n].reshape(x.shape[0], ncol, order="F"))
+            off += n
+        return out

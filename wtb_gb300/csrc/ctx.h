@@ -57,4 +57,7 @@ CoulParams ctx_coul_params(wtb_ctx* c, const wtb_bse_params* p);
 int ctx_coulomb_table(wtb_ctx* c, const wtb_bse_params* p, double* V, int ldv, bool deriv_r0);
 int ctx_make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob, const std::string& tag,
                       bool deriv_r0);
+int ctx_stage_system(wtb_ctx* c, const wtb_bse_params* p);
+int ctx_enqueue_system(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob);
+int ctx_auto_block(const wtb_bse_params* p, int dim, bool fp64);
 }  // namespace wtb

@@ -195,6 +195,23 @@ cudaError_t MatFreeOperator<S>::contract(const cplx<S>* X, int ldx, int ncol, cu
 template struct MatFreeOperator<float>;
 template struct MatFreeOperator<double>;
 
+cudaError_t BatchMatFreeOperator::apply(const zf* X, int ldx, int c0, int ncol, zf* Y, int ldy, cudaStream_t s) {
+  this->matvec_columns += ncol;
+  const int* skip = final_apply ? nullptr : frozen;
+  for (int b0 = 0; b0 < ncol; b0 += nbmax) {
+    const int nb = ncol - b0 < nbmax ? ncol - b0 : nbmax;
+    cudaError_t e = launch_mf_gather_batch(X, ldx, c0 + b0, nb, d_sys, d_gtiles, ngtiles, max_nv, max_nc, max_w,
+                                           nslices, skip, s);
+    if (e != cudaSuccess) return e;
+    e = final_apply ? tc_gemm_group_run_split(gemm, npairs, nullptr, st, s, kchunk_final)
+                    : tc_gemm_group_run(gemm, npairs, skip, st, s);
+    if (e != cudaSuccess) return e;
+    e = launch_mf_scatter_batch(X, ldx, d_sys, d_kpts, nkpts, max_nv, max_nc, max_w, nb, Y, ldy, c0 + b0, skip, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 namespace {
 
 struct Small {
@@ -204,7 +221,7 @@ struct Small {
 };
 
 // Rayleigh-Ritz on the basis Sb (nrow x nb, ld) with ASb = H Sb: returns C (nb x m) and theta (m) of every
-// system of bm (small matrices nn = nb^2 apart, theta nb apart).
+// system of bm (small matrices nn apart, theta ts apart).
 // Orthonormalisation: Cholesky of the scaled Gram matrix in [X W P] order with deflation (directions whose
 // residual diagonal falls below tau are dropped; the r kept ones come first in B); the projected r x r
 // problem B^H G B is solved by the tridiagonal route (small_eig.cuh).  The small problems run in precision S,
@@ -212,7 +229,7 @@ struct Small {
 template <class S>
 int rayleigh_ritz(const cplx<S>* Sb, const cplx<S>* ASb, int ld, int nb, int m, int nrow, double tau, Small& sm,
                   double* partial, int npart, DevStatus* st, cudaStream_t s, std::string* msg, bool small_in_fp64,
-                  const BatchMap& bm, long nn) {
+                  const BatchMap& bm, long nn, long ts) {
   (void)st;
   CK(launch_gram<S>(Sb, ld, nb, Sb, ld, nb, nrow, sm.M, partial, npart, s, bm, nn));
   CK(launch_gram<S>(Sb, ld, nb, ASb, ld, nb, nrow, sm.G, partial, npart, s, bm, nn));
@@ -226,9 +243,9 @@ int rayleigh_ritz(const cplx<S>* Sb, const cplx<S>* ASb, int ld, int nb, int m, 
   CK(launch_small_gemm(sm.G, nb, 0, sm.B, nb, sm.T, nb, nb, nb, nb, s, false, bm, nn, nn, nn));
   CK(launch_small_gemm(sm.B, nb, 1, sm.T, nb, sm.Gp, nb, nb, nb, nb, s, false, bm, nn, nn, nn));
   if (small_in_fp64)
-    CK(launch_heev_small<double>(sm.Gp, nb, sm.keep, nb, m, sm.theta, sm.Y, nb, s, bm, nn, nb, nn));
+    CK(launch_heev_small<double>(sm.Gp, nb, sm.keep, nb, m, sm.theta, sm.Y, nb, s, bm, nn, ts, nn));
   else
-    CK(launch_heev_small<S>(sm.Gp, nb, sm.keep, nb, m, sm.theta, sm.Y, nb, s, bm, nn, nb, nn));
+    CK(launch_heev_small<S>(sm.Gp, nb, sm.keep, nb, m, sm.theta, sm.Y, nb, s, bm, nn, ts, nn));
   CK(launch_small_gemm(sm.B, nb, 0, sm.Y, nb, sm.C, m, nb, m, nb, s, f32, bm, nn, nn, nn));
   return WTB_OK;
 }
@@ -495,12 +512,13 @@ template <class S>
 int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L, int nev, int m, double tol,
                        int maxit, Workspace& ws, DevStatus* st, cudaStream_t s, std::vector<double>* E, zd* Xout,
                        std::vector<SolveStats>* stats, std::vector<int>* sys_status, std::string* msg,
-                       double tol_refine) {
+                       double tol_refine, SolveGraph* sg) {
   const int nsys = L.bm.nsys;
   const int nrow = L.nrow;
   int mindim = nrow;
   for (int d : L.dims) mindim = std::min(mindim, d);
-  if (nsys < 1 || (int)L.dims.size() != nsys || (nsys > 1 && (!L.bm.rows || !L.bm.parts || !L.bm.tile_sys))) {
+  if (nsys < 1 || (int)L.dims.size() != nsys || (nsys > 1 && !L.bm.rows) ||
+      (L.bm.rows && (!L.bm.parts || !L.bm.part_sys || !L.bm.sys_parts || !L.bm.tile_sys || L.nparts < 1))) {
     if (msg) *msg = "inconsistent batch layout";
     return WTB_EBADARG;
   }
@@ -516,7 +534,10 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
     if (msg) *msg = "eigensolver block too large (3*block must be <= 96 in FP32, <= 78 in FP64)";
     return WTB_EBADARG;
   }
-  const int npart = nsys > 1 ? L.nparts : std::max(1, std::min(304, (nrow + 127) / 128));
+  // a ragged layout (row tables present) selects its start vectors per system over the systems' own rows and
+  // keeps the padding rows zero; its reductions run over its part table
+  const bool ragged = L.bm.rows != nullptr;
+  const int npart = ragged ? L.nparts : std::max(1, std::min(304, (nrow + 127) / 128));
   cudaError_t err = cudaSuccess;
   cplx<S>* Sb = ws.get<cplx<S>>("lob_S", (size_t)nrow * ld, &err, true);
   cplx<S>* ASb = ws.get<cplx<S>>("lob_AS", (size_t)nrow * ld, &err, true);
@@ -538,8 +559,8 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
   double* partial = ws.get<double>("lob_partial", (size_t)npart * nn * 2, &err);
   double* norms2 = ws.get<double>("lob_norms2", (size_t)nsys * 32, &err);
   int* active = ws.get<int>("lob_active", (size_t)nsys * 32, &err);
-  int* idx = ws.get<int>("lob_idx", nsys > 1 ? (size_t)nsys * m : 65 * 128, &err);
-  double* cand = ws.get<double>("lob_cand", nsys > 1 ? (size_t)nsys * m : 65 * 128, &err);
+  int* idx = ws.get<int>("lob_idx", ragged ? (size_t)nsys * m : 65 * 128, &err);
+  double* cand = ws.get<double>("lob_cand", ragged ? (size_t)nsys * m : 65 * 128, &err);
   double* th_dev = ws.get<double>("lob_thcur", (size_t)nsys * nb, &err);
   LobCtl* ctl = ws.get<LobCtl>("lob_ctl", nsys, &err);
   int* frozen = ws.get<int>("lob_frozen", nsys, &err);
@@ -570,14 +591,14 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
   // WTB_SOLVER_STREAM: the same kernels launched directly on the stream, the host reading the loop state
   // between iterations (for kernel-level profilers, which do not replay kernels inside conditional graph
   // bodies); the default runs the whole solve as one graph launch
-  const bool stream_mode = std::getenv("WTB_SOLVER_STREAM") != nullptr;
+  const bool stream_mode = std::getenv("WTB_SOLVER_STREAM") != nullptr && !sg;
   const size_t upd_smem = (size_t)(nb * m + kUpdRows * nb) * sizeof(cplx<S>);
   const int upd_grid = std::max(1, std::min(152 * 8, (nrow + kUpdRows - 1) / kUpdRows));
   const unsigned cp_grid = (unsigned)std::max(1, std::min(152 * 4, (int)(((long)nrow * m + 255) / 256)));
 
   // the pieces of one iteration, as stream launches (captured below)
   auto rr_and_update = [&]() -> int {
-    int r = rayleigh_ritz<S>(Sb, ASb, ld, nb, m, nrow, tau, sm, partial, npart, st, s, msg, false, bm, nn);
+    int r = rayleigh_ritz<S>(Sb, ASb, ld, nb, m, nrow, tau, sm, partial, npart, st, s, msg, false, bm, nn, nb);
     if (r) return r;
     CK(raise_smem_limit(reinterpret_cast<const void*>(lob_update_kernel<S>), upd_smem));
     lob_update_kernel<S><<<upd_grid, 256, upd_smem, s>>>(Sb, ASb, ld, m, sm.C, nrow, bm, nn);
@@ -623,7 +644,7 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
     ++g_launch_count;
     CK(cudaMemset2DAsync(Sb, sizeof(cplx<S>) * ld, 0, sizeof(cplx<S>) * ld, nrow, s));
     CK(cudaMemset2DAsync(ASb, sizeof(cplx<S>) * ld, 0, sizeof(cplx<S>) * ld, nrow, s));
-    if (nsys > 1) {
+    if (ragged) {
       CK(launch_select_lowest_batch(diag, bmf, m, idx, m, cand, s));
       CK(launch_init_guess<S>(X, ld, nrow, m, idx, 12345u, s, bmf, m));
     } else {
@@ -652,7 +673,8 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
     CK(fe);
     CK((launch_convert_cols<S, double>(X, ld, X64, 2 * m, m, nrow, s)));
     CK((launch_convert_cols<S, double>(AX, ld, X64 + m, 2 * m, m, nrow, s)));
-    int r = rayleigh_ritz<double>(X64, X64 + m, 2 * m, m, m, nrow, 1e-13, sm, partial, npart, st, s, msg, true, bmf, nn);
+    int r = rayleigh_ritz<double>(X64, X64 + m, 2 * m, m, m, nrow, 1e-13, sm, partial, npart, st, s, msg, true, bmf, nn,
+                                  nb);
     if (r) return r;
     // Xout = X64 C[:, :nev]; residual = (AX64 C - Xout theta)
     CK(launch_update<double>(X64, 2 * m, m, sm.C, m, nev, nrow, Xout, nev, 1.0, 0.0, s, bmf, nn));
@@ -663,7 +685,10 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
 
   int rc = WTB_OK;
   long long body_launches[2] = {0, 0};
-  if (stream_mode) {
+  if (sg && sg->collect) {
+    body_launches[0] = sg->body_launches[0];
+    body_launches[1] = sg->body_launches[1];
+  } else if (stream_mode) {
     auto stopped = [&](bool* stop) -> int {
       int h = 0;
       CK(cudaMemcpyAsync(&h, counter + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -722,7 +747,7 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
       key *= 1099511628211ull;
     }
   if (key == 0) key = 1;
-  if (ws.graph_exec && ws.graph_key == key) {
+  if (!sg && ws.graph_exec && ws.graph_key == key) {
     body_launches[0] = ws.graph_body_launches[0];
     body_launches[1] = ws.graph_body_launches[1];
     g_launch_count += ws.graph_launches;  // one pass of every captured kernel; the bodies' repeats are added below
@@ -731,11 +756,14 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
       return WTB_ECUDA;
     }
   } else {
-  ws.drop_graph();
+  if (!sg) ws.drop_graph();
   const long long captured0 = g_launch_count.load();
   cudaGraph_t G = nullptr;
   cudaGraphExec_t GX = nullptr;
-  CK(cudaGraphCreate(&G, 0));
+  if (sg)
+    G = sg->graph;
+  else
+    CK(cudaGraphCreate(&G, 0));
   CaptureSeg cap{s};
   std::vector<cudaGraphNode_t> tail;
   // kernels captured into each loop body (the launch counter counts captured kernels; the bodies then run
@@ -777,7 +805,7 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
       break;
     }
     // set-up: unit vectors at the m lowest transition energies (+ deterministic noise), W = P = 0
-    rc = segment(G, {}, &tail, [&]() -> int {
+    rc = segment(G, sg ? sg->deps : std::vector<cudaGraphNode_t>(), &tail, [&]() -> int {
       int r = setup();
       if (r) return r;
       return restart_from_x(h1);
@@ -807,6 +835,7 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
     }
     rc = segment(G, tail, &tail, final_step);
     if (rc) break;
+    if (sg) break;  // the caller instantiates and launches its graph
     if (cudaGraphInstantiate(&GX, G, 0) != cudaSuccess) {
       if (msg) *msg = "graph instantiation failed";
       rc = WTB_ECUDA;
@@ -818,6 +847,15 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
       break;
     }
   } while (false);
+  if (sg) {
+    if (rc == WTB_OK) {
+      sg->tail = tail;
+      sg->launches = g_launch_count.load() - captured0;
+      sg->body_launches[0] = body_launches[0];
+      sg->body_launches[1] = body_launches[1];
+    }
+    return rc;
+  }
   if (rc) {
     if (GX) cudaGraphExecDestroy(GX);
     if (G) cudaGraphDestroy(G);
@@ -909,7 +947,7 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
   L.dims.assign(1, dim);
   std::vector<SolveStats> sv;
   const int rc = lobpcg_solve_batch<S>(op, diag, L, nev, m, tol, maxit, ws, st, s, E, Xout, &sv, nullptr, msg,
-                                       tol_refine);
+                                       tol_refine, nullptr);
   if (stats && !sv.empty()) *stats = sv[0];
   return rc;
 }
@@ -921,9 +959,11 @@ template int lobpcg_solve<double>(Operator<double>&, const double*, int, int, in
                                   double);
 template int lobpcg_solve_batch<float>(Operator<float>&, const double*, const BatchLayout&, int, int, double, int,
                                        Workspace&, DevStatus*, cudaStream_t, std::vector<double>*, zd*,
-                                       std::vector<SolveStats>*, std::vector<int>*, std::string*, double);
+                                       std::vector<SolveStats>*, std::vector<int>*, std::string*, double,
+                                       SolveGraph*);
 template int lobpcg_solve_batch<double>(Operator<double>&, const double*, const BatchLayout&, int, int, double, int,
                                         Workspace&, DevStatus*, cudaStream_t, std::vector<double>*, zd*,
-                                        std::vector<SolveStats>*, std::vector<int>*, std::string*, double);
+                                        std::vector<SolveStats>*, std::vector<int>*, std::string*, double,
+                                        SolveGraph*);
 
 }  // namespace wtb

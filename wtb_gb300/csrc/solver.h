@@ -60,12 +60,17 @@ struct Workspace {
     graph_key = 0;
   }
   ~Workspace() { drop_graph(); }
+  // incremented whenever a buffer is (re)allocated: a graph captured at one generation holds valid addresses
+  // as long as the generation is unchanged
+  uint64_t generation = 0;
   template <class T>
   T* get(const std::string& name, size_t count, cudaError_t* err, bool zero = false) {
     auto& b = bufs[name];
     if (!b) b.reset(new DevBuf());
+    const void* before = b->p;
     const cudaError_t e = b->ensure(count * sizeof(T), zero, stream);
     if (e != cudaSuccess) *err = e;
+    if (b->p != before) ++generation;
     return b->as<T>();
   }
   // an existing buffer of at least count elements, or nullptr
@@ -213,14 +218,61 @@ struct BatchLayout {
   std::vector<int> dims;
 };
 
+// A solve inside a caller's graph: with build, the solve's nodes are added to graph after deps (tail receives
+// its last nodes, launches and body_launches the kernels captured) and nothing is launched or read back; after
+// the caller has launched its graph, the same call with collect reads the results.
+struct SolveGraph {
+  cudaGraph_t graph = nullptr;
+  std::vector<cudaGraphNode_t> deps, tail;
+  long long launches = 0, body_launches[2] = {0, 0};
+  bool build = false, collect = false;
+};
+
 // The lowest nev eigenpairs of every system of the batch, iterated together: one launch of each kernel covers
 // all systems still running, a system that has converged is frozen, and the loop ends when the last one
 // has.  diag and Xout in the concatenated rows; E (host) nsys x nev; per-system statistics and status codes.
+// The frozen flags live in ws buffer "lob_frozen" (nsys ints), where a batched operator can read them.
 template <class S>
 int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L, int nev, int m, double tol,
                        int maxit, Workspace& ws, DevStatus* st, cudaStream_t s, std::vector<double>* E, zd* Xout,
                        std::vector<SolveStats>* stats, std::vector<int>* sys_status, std::string* msg,
-                       double tol_refine = 0.0);
+                       double tol_refine = 0.0, SolveGraph* sg = nullptr);
+
+// The split-BF16 matrix-free operators of a batch of systems applied together: one gather, one grouped
+// tensor-core contraction and one scatter launch cover every system still iterating (all of them in the final
+// application).  Rows of system q start at sys[q].row0 of the concatenated block vectors.
+struct BatchMatFreeOperator : Operator<float> {
+  int nsys = 0, nbmax = 16, max_nv = 0, max_nc = 0, max_w = 0;
+  int nslices = 3, npairs = 3, npairs_refine = 6;
+  int pa[8] = {0}, pb[8] = {0};
+  int kchunk_final = 4;
+  bool final_apply = false;
+  const MfSys* d_sys = nullptr;
+  const int2* d_gtiles = nullptr;  // gather tiles (system, first k-point)
+  int ngtiles = 0;
+  const int2* d_kpts = nullptr;    // scatter k-points (system, k)
+  int nkpts = 0;
+  TcGroupPlan* gemm = nullptr;     // owned
+  const int* frozen = nullptr;
+  DevStatus* st = nullptr;
+  ~BatchMatFreeOperator() override {
+    if (gemm) tc_gemm_group_destroy(gemm);
+  }
+  cudaError_t apply(const zf* X, int ldx, int c0, int ncol, zf* Y, int ldy, cudaStream_t s) override;
+  bool begin_refine() override {
+    if (npairs_refine <= npairs) return false;
+    npairs = npairs_refine;
+    return true;
+  }
+  void set_final(bool on) override { final_apply = on; }
+  void signature(std::vector<uint64_t>* sig) const override {
+    const uint64_t v[] = {3, (uint64_t)nsys, (uint64_t)nbmax, (uint64_t)nslices, (uint64_t)npairs,
+                          (uint64_t)npairs_refine, (uint64_t)kchunk_final, (uint64_t)(uintptr_t)d_sys,
+                          (uint64_t)(uintptr_t)d_gtiles, (uint64_t)(uintptr_t)d_kpts, (uint64_t)(uintptr_t)gemm,
+                          (uint64_t)(uintptr_t)frozen, (uint64_t)(uintptr_t)st};
+    sig->insert(sig->end(), v, v + sizeof(v) / sizeof(v[0]));
+  }
+};
 
 // extra launchers used by the solver
 template <class S>

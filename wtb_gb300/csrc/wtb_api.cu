@@ -190,33 +190,44 @@ __global__ void expand_acts_kernel(const double* __restrict__ osc, int nev, int 
   acts[e] = i < nev ? osc[(size_t)a * nev + i] : 0.0;
 }
 
-int upload_bands(wtb_ctx* c, int nk, const double* kpt_rm, int nv, int nc) {
+// Host part of a band computation: the k-points go to the device (stream-ordered), the band buffers are
+// sized and the context records the mesh.  enqueue_bands then only launches kernels (a graph can hold it).
+int stage_bands(wtb_ctx* c, int nk, const double* kpt_rm, int nv, int nc) {
   cudaError_t err = cudaSuccess;
   double* dk = c->ws.get<double>("kpt", (size_t)nk * 3, &err);
   CKC(err);
-  CKC(cudaMemcpyAsync(dk, kpt_rm, sizeof(double) * nk * 3, cudaMemcpyHostToDevice, c->s));
+  c->kpt.assign(kpt_rm, kpt_rm + (size_t)nk * 3);
+  CKC(cudaMemcpyAsync(dk, c->kpt.data(), sizeof(double) * nk * 3, cudaMemcpyHostToDevice, c->s));
   const int w = c->w, nb = nv + nc;
-  double* eig_all = c->ws.get<double>("eig_all", (size_t)nk * w, &err);
+  c->ws.get<double>("eig_all", (size_t)nk * w, &err);
+  c->ws.get<zd>("vec_all", (size_t)nk * w * w, &err);
+  c->ws.get<double>("eig_win", (size_t)nk * (nb > 0 ? nb : 1), &err);
+  c->ws.get<zd>("vec_win", (size_t)nk * (nb > 0 ? nb : 1) * w, &err);
+  c->ws.get<int>("nocp", nk, &err);
   CKC(err);
-  zd* vec_all = c->ws.get<zd>("vec_all", (size_t)nk * w * w, &err);
-  CKC(err);
-  double* eig_win = c->ws.get<double>("eig_win", (size_t)nk * (nb > 0 ? nb : 1), &err);
-  CKC(err);
-  zd* vec_win = c->ws.get<zd>("vec_win", (size_t)nk * (nb > 0 ? nb : 1) * w, &err);
-  CKC(err);
-  int* nocp = c->ws.get<int>("nocp", nk, &err);
-  CKC(err);
-  CKC(launch_hk_eig(c->ws.get<zd>("hr", 0, &err), c->ws.get<int>("rvec", 0, &err), c->ws.get<int>("ndegen", 0, &err),
-                    c->nR, w, c->ws.get<double>("rlat", 0, &err), c->efermi, c->scs, dk, nk, nv, nc, eig_all, vec_all,
-                    nb > 0 ? eig_win : nullptr, nb > 0 ? vec_win : nullptr, nocp, c->st, c->s));
-  CKR(check_status(c));
   c->nk = nk;
   c->nv = nv;
   c->nc = nc;
-  c->kpt.assign(kpt_rm, kpt_rm + (size_t)nk * 3);
   c->have_bands = nb > 0;
   c->have_solve = false;  // the stored excitons belong to the previous bands
   return WTB_OK;
+}
+
+int enqueue_bands(wtb_ctx* c) {
+  cudaError_t err = cudaSuccess;
+  const int nk = c->nk, nv = c->nv, nc = c->nc, w = c->w, nb = nv + nc;
+  CKC(launch_hk_eig(c->ws.get<zd>("hr", 0, &err), c->ws.get<int>("rvec", 0, &err), c->ws.get<int>("ndegen", 0, &err),
+                    c->nR, w, c->ws.get<double>("rlat", 0, &err), c->efermi, c->scs, c->ws.get<double>("kpt", 0, &err),
+                    nk, nv, nc, c->ws.get<double>("eig_all", 0, &err), c->ws.get<zd>("vec_all", 0, &err),
+                    nb > 0 ? c->ws.get<double>("eig_win", 0, &err) : nullptr,
+                    nb > 0 ? c->ws.get<zd>("vec_win", 0, &err) : nullptr, c->ws.get<int>("nocp", 0, &err), c->st, c->s));
+  return WTB_OK;
+}
+
+int upload_bands(wtb_ctx* c, int nk, const double* kpt_rm, int nv, int nc) {
+  CKR(stage_bands(c, nk, kpt_rm, nv, nc));
+  CKR(enqueue_bands(c));
+  return check_status(c);
 }
 
 int validate_params(wtb_ctx* c, const wtb_bse_params* p) {
@@ -258,29 +269,12 @@ int coulomb_table_into(wtb_ctx* c, const wtb_bse_params* p, double* V, int ldv, 
   const bool mp = c->mesh_mp && p->ngrid[0] == c->ngrid[0] && p->ngrid[1] == c->ngrid[1] &&
                   p->ngrid[2] == c->ngrid[2] && (long)p->ngrid[0] * p->ngrid[1] * p->ngrid[2] == nk;
   if (mp) {
-    // reciprocal vectors exactly as the mesh was built (recvec, src/module_kmesh.F90:391-407)
-    const double* r = c->rlat_rm;
-    auto cross = [](const double* u, const double* v, double* o) {
-      o[0] = u[1] * v[2] - u[2] * v[1];
-      o[1] = u[2] * v[0] - u[0] * v[2];
-      o[2] = u[0] * v[1] - u[1] * v[0];
-    };
-    double v23[3], v31[3], v12[3], bl[9];
-    cross(r + 3, r + 6, v23);
-    cross(r + 6, r, v31);
-    cross(r, r + 3, v12);
-    const double vol = std::fabs(r[0] * v23[0] + r[1] * v23[1] + r[2] * v23[2]);
-    const double f = (2.0 * (double)3.14159274101257324f) / vol;
-    for (int d = 0; d < 3; ++d) {
-      bl[d] = f * v23[d];
-      bl[3 + d] = f * v31[d];
-      bl[6 + d] = f * v12[d];
-    }
-    double* dbl = c->ws.get<double>("recip", 9, &err);
+    // reciprocal vectors of the mesh, on the device since wtb_set_hr
+    const double* dbl = c->ws.find<double>("recip", 9);
+    if (!dbl) return set_err(c, WTB_ESTATE, "reciprocal vectors not staged");
     const long ns = (2L * p->ngrid[0] - 1) * (2L * p->ngrid[1] - 1) * (2L * p->ngrid[2] - 1);
     double* stn = c->ws.get<double>("vstencil", ns, &err);
     CKC(err);
-    CKC(cudaMemcpyAsync(dbl, bl, sizeof(bl), cudaMemcpyHostToDevice, c->s));
     CKC(launch_coulomb_mesh(cpar, dbl, stn, V, ldv, c->s));
   } else {
     const double* kd = c->ws.get<double>("kpt", 0, &err);
@@ -526,6 +520,27 @@ int wtb_set_hr(wtb_ctx* c, int w90basis, int nvec, const int* rvec, const int* f
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) rl[3 * i + j] = rlat[i + 3 * j];
   if (!std::isfinite(efermi) || !std::isfinite(scs)) return set_err(c, WTB_ENAN, "non-finite efermi or scs");
+  // reciprocal vectors exactly as the mesh is built (recvec, src/module_kmesh.F90:391-407), for the
+  // V(k,k') table on the mesh
+  double bl[9];
+  {
+    auto cross = [](const double* u, const double* v, double* o) {
+      o[0] = u[1] * v[2] - u[2] * v[1];
+      o[1] = u[2] * v[0] - u[0] * v[2];
+      o[2] = u[0] * v[1] - u[1] * v[0];
+    };
+    double v23[3], v31[3], v12[3];
+    cross(rl + 3, rl + 6, v23);
+    cross(rl + 6, rl, v31);
+    cross(rl, rl + 3, v12);
+    const double vol = std::fabs(rl[0] * v23[0] + rl[1] * v23[1] + rl[2] * v23[2]);
+    const double f = (2.0 * (double)3.14159274101257324f) / vol;
+    for (int d = 0; d < 3; ++d) {
+      bl[d] = f * v23[d];
+      bl[3 + d] = f * v31[d];
+      bl[6 + d] = f * v12[d];
+    }
+  }
   cudaError_t err = cudaSuccess;
   zd* dh = c->ws.get<zd>("hr", hr.size(), &err);
   CKC(err);
@@ -534,11 +549,13 @@ int wtb_set_hr(wtb_ctx* c, int w90basis, int nvec, const int* rvec, const int* f
   int* dn = c->ws.get<int>("ndegen", nvec, &err);
   CKC(err);
   double* dl = c->ws.get<double>("rlat", 9, &err);
+  double* db = c->ws.get<double>("recip", 9, &err);
   CKC(err);
   CKC(cudaMemcpyAsync(dh, hr.data(), hr.size() * sizeof(zd), cudaMemcpyHostToDevice, c->s));
   CKC(cudaMemcpyAsync(dr, rvec, sizeof(int) * nvec * 3, cudaMemcpyHostToDevice, c->s));
   CKC(cudaMemcpyAsync(dn, ffactor, sizeof(int) * nvec, cudaMemcpyHostToDevice, c->s));
   CKC(cudaMemcpyAsync(dl, rl, sizeof(rl), cudaMemcpyHostToDevice, c->s));
+  CKC(cudaMemcpyAsync(db, bl, sizeof(bl), cudaMemcpyHostToDevice, c->s));
   CKC(cudaStreamSynchronize(c->s));
   c->w = w;
   c->nR = nvec;
@@ -664,14 +681,21 @@ int wtb_coulomb_table(wtb_ctx* c, const wtb_bse_params* p, int n1, const double*
   return check_status(c);
 }
 
-static int ensure_bands_for(wtb_ctx* c, const wtb_bse_params* p) {
+// the Monkhorst-Pack mesh of p staged for the band computation
+static int stage_mesh(wtb_ctx* c, const wtb_bse_params* p) {
   const int nk = p->ngrid[0] * p->ngrid[1] * p->ngrid[2];
   std::vector<double> k((size_t)nk * 3);
   mp_mesh(p->ngrid[0], p->ngrid[1], p->ngrid[2], p->mshift, c->rlat_rm, c->rlat_rm + 3, c->rlat_rm + 6, k.data());
-  CKR(upload_bands(c, nk, k.data(), p->nv, p->nc));
+  CKR(stage_bands(c, nk, k.data(), p->nv, p->nc));
   for (int d = 0; d < 3; ++d) c->ngrid[d] = p->ngrid[d];
   c->mesh_mp = true;
   return WTB_OK;
+}
+
+static int ensure_bands_for(wtb_ctx* c, const wtb_bse_params* p) {
+  CKR(stage_mesh(c, p));
+  CKR(enqueue_bands(c));
+  return check_status(c);
 }
 
 static int compute_optics(wtb_ctx* c, const wtb_bse_params* p) {
@@ -978,3 +1002,26 @@ int wtb_profile_read(wtb_ctx* c, double* total_ms, long long* launches, double* 
 }
 
 }  // extern "C"
+
+namespace wtb {
+// Batch solves (batch.cu): the host part of one system's set-up (validation, mesh, k-points to the device)
+// and its device part as kernel launches only (bands, optical matrix elements, operator), which a graph
+// can hold.
+int ctx_stage_system(wtb_ctx* c, const wtb_bse_params* p) {
+  CKR(prep_device(c));
+  if (!c->have_hr) return set_err(c, WTB_ESTATE, "H(R) not set (call wtb_set_hr first)");
+  CKR(validate_params(c, p));
+  if (p->nv + p->nc > c->w) return set_err(c, WTB_EBADARG, "nv + nc exceeds w90basis");
+  const long dim = (long)p->ngrid[0] * p->ngrid[1] * p->ngrid[2] * p->nc * p->nv;
+  if (p->nev < 1 || p->nev > dim) return set_err(c, WTB_EBADARG, "nev must be between 1 and the BSE dimension");
+  return stage_mesh(c, p);
+}
+
+int ctx_enqueue_system(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob) {
+  CKR(enqueue_bands(c));
+  CKR(compute_optics(c, p));
+  return make_operator(c, p, nbmax, ob);
+}
+
+int ctx_auto_block(const wtb_bse_params* p, int dim, bool fp64) { return auto_block(p, dim, fp64); }
+}  // namespace wtb
