@@ -210,8 +210,9 @@ def run_reference(args):
 
 
 def run_batch(args, torch, api, S, world, local):
-    """systems/s over the 64-system batch: one step = the whole batch through wtb_batch_bsesolver (its
-    workers' streams overlap on the device; the call returns when every system is done)."""
+    """systems/s over the 64-system batch: one step = the whole batch through wtb_batch_bsesolver (inputs
+    staged from host memory, then one CUDA graph launch: per-system set-up branches, one joint eigensolve
+    over all systems, per-system oscillator strengths; the call returns when every system is done)."""
     from wtb_gb300 import batch as B
 
     everything = S.strained_batch(nsys=64)
@@ -220,7 +221,7 @@ def run_batch(args, torch, api, S, world, local):
     # data path; only the step time is reduced)
     part = B.lpt_partition([B.system_cost(p, s.w90basis) for s, p in everything], world)[rank]
     items = [everything[i] for i in part]
-    b = api.Batch(local, nworkers=args.workers)
+    b = api.Batch(local)
     kw = dict(precision=args.precision, op="matfree", tol=args.tol)
     for _ in range(args.warmup):
         b.bsesolver(items, **kw)
@@ -241,6 +242,7 @@ def run_batch(args, torch, api, S, world, local):
     launches = api.kernel_launch_count() - launches0
     clk = clocks.stop()
     tot = sum(ms)
+    phases = b.timings()
     b.close()
     if world > 1:
         import torch.distributed as dist
@@ -255,9 +257,11 @@ def run_batch(args, torch, api, S, world, local):
             "unit": "systems/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": tot / args.steps, "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
             "dtype": args.precision, "data": "synthetic (seeded H(R))",
-            "config": {"workload": "batch64", "systems_this_rank": len(items), "sharding": "LPT over ranks", "description": WORKLOADS["batch64"], "workers": args.workers,
+            "config": {"workload": "batch64", "systems_this_rank": len(items), "sharding": "LPT over ranks", "description": WORKLOADS["batch64"],
+                       "form": "one graph launch per batch (joint ragged-batch eigensolve, grouped tcgen05 contraction)",
                        "precision": args.precision, "l2": "inputs and operators of 64 systems exceed L2 per step",
                        "timing": "events on a side stream around the blocking batch call"},
+            "phases_ms": {k: round(v, 3) for k, v in phases.items()},
             "e2e": {"value": value, "unit": "systems/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches), "clocks": clk,
             "iterations": {"max": max(o["iterations"] for o in out), "mean": float(np.mean([o["iterations"] for o in out]))}}
@@ -279,7 +283,6 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--ref-matvecs", type=int, default=800)
     ap.add_argument("--ref-budget", type=float, default=12.0)
-    ap.add_argument("--workers", type=int, default=8, help="batch64: concurrent contexts")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

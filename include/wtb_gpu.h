@@ -244,6 +244,11 @@ const char* wtb_batch_error(const wtb_batch* batch, int i);
  * Rayleigh-Ritz step) applied to ncol (1..16) vectors of every system: X and Y hold, system after system, the
  * dim_i x ncol complex(8) column-major blocks (wtb_bse_matvec's layout). */
 int wtb_batch_matvec(wtb_batch* batch, int ncol, const double* X, double* Y);
+/* Times (ms) of the last wtb_batch_bsesolver call of the joint form (t_ms has 7 entries).  Host wall:
+ * t_ms[0] staging of the inputs, t_ms[1] graph capture (0 when the cached graph was reused), t_ms[2] graph run,
+ * t_ms[3] read-back.  Device (events in the graph): t_ms[4] per-system set-up (bands, optics, operator data),
+ * t_ms[5] joint eigensolve, t_ms[6] oscillator strengths. */
+int wtb_batch_timings(const wtb_batch* batch, double* t_ms);
 
 /* Number of CUDA kernels this library has launched in the process (instrumentation for benchmarks). */
 long long wtb_kernel_launch_count(void);

@@ -89,6 +89,7 @@ def _load():
         "wtb_batch_destroy": [P],
         "wtb_batch_bsesolver": [P, C.c_int, C.POINTER(CSystem), C.POINTER(CParams), C.c_int, dp, dp, ip, ip, dp],
         "wtb_batch_matvec": [P, C.c_int, dp, dp],
+        "wtb_batch_timings": [P, dp],
     }
     for name, args in sigs.items():
         f = getattr(lib, name)
@@ -358,7 +359,7 @@ class Batch:
     """Independent systems solved together on one device (``wtb_batch_*``): the split-BF16 forms as one joint
     eigensolve in one graph launch, other forms system by system."""
 
-    def __init__(self, device: int = 0, nworkers: int = 8):
+    def __init__(self, device: int = 0, nworkers: int = 1):
         h = C.c_void_p()
         r = _lib.wtb_batch_create(C.byref(h), int(device), int(nworkers))
         if r:
@@ -408,6 +409,13 @@ class Batch:
             bad = next(i for i in range(n) if status[i])
             raise WTBError(int(r), f"wtb_batch_bsesolver: system {bad}: {out[bad]['error']}")
         return out, float(wall[0])
+
+    def timings(self):
+        """Times (ms) of the last joint batch call: host stage, build, run, collect; device set-up, solve and
+        oscillator phases."""
+        t = np.zeros(7)
+        _lib.wtb_batch_timings(self._h, _dp(t))
+        return dict(zip(("stage", "build", "run", "collect", "dev_setup", "dev_solve", "dev_oscillators"), t.tolist()))
 
     def matvec(self, Xs):
         """The joint operator of the last ``bsesolver`` call applied to one block per system: Xs[i] is

@@ -44,6 +44,12 @@ struct wtb_batch {
   double tol = 0.0, tol_refine = 0.0;
   int maxit = 200;
   std::vector<int> row0, dims;
+  // host wall time of the last call's phases (ms): staging, graph build (0 when reused), graph run, read-back
+  double t_stage = 0, t_build = 0, t_run = 0, t_collect = 0;
+  // device time of the graph's phases (ms): per-system set-up, joint eigensolve, oscillator strengths; from
+  // event-record nodes at the two joins and events around the launch
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  double t_front = 0, t_solve = 0, t_back = 0;
   void drop_graph() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
@@ -328,6 +334,15 @@ int build_graph(wtb_batch* b, int nsys, const wtb_bse_params* p, std::string* ms
     // the operator objects of the first pass own the same buffers; keep those
     joins.insert(joins.end(), tail.begin(), tail.end());
   }
+  // event-record node after the set-up branches (device time of the phases)
+  auto mark = [&](cudaEvent_t e, const std::vector<cudaGraphNode_t>& deps, std::vector<cudaGraphNode_t>* out) {
+    Capture cap{mc->s};
+    if (cap.begin(G, deps) != cudaSuccess) return ctx_set_err(mc, WTB_ECUDA, "batch: capture failed");
+    const cudaError_t e1 = cudaEventRecordWithFlags(e, mc->s, cudaEventRecordExternal);
+    if (cap.end(out) != cudaSuccess || e1 != cudaSuccess) return ctx_set_err(mc, WTB_ECUDA, "batch: capture failed");
+    return WTB_OK;
+  };
+  if (rc == WTB_OK) rc = mark(b->ev[1], joins, &joins);
   if (rc == WTB_OK) {
     b->op = std::move(op);
     b->sg = SolveGraph();
@@ -338,10 +353,12 @@ int build_graph(wtb_batch* b, int nsys, const wtb_bse_params* p, std::string* ms
     rc = lobpcg_solve_batch<float>(*b->op, diag, L, nevmax, b->m, b->tol, b->maxit, ws, mc->st, mc->s, &E, Xout,
                                    nullptr, nullptr, msg, b->tol_refine, &b->sg);
   }
+  std::vector<cudaGraphNode_t> solved;
+  if (rc == WTB_OK) rc = mark(b->ev[2], b->sg.tail, &solved);
   for (int q = 0; q < nsys && rc == WTB_OK; ++q) {
     wtb_ctx* c = b->slots[q];
     Capture cap{c->s};
-    if (cap.begin(G, b->sg.tail) != cudaSuccess) {
+    if (cap.begin(G, solved) != cudaSuccess) {
       rc = ctx_set_err(mc, WTB_ECUDA, "batch: capture failed");
       break;
     }
@@ -376,6 +393,11 @@ extern "C" int wtb_batch_create(wtb_batch** out, int device, int nworkers) {
     delete b;
     return WTB_ENODEV;
   }
+  for (auto& e : b->ev)
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      wtb_batch_destroy(b);
+      return WTB_ENODEV;
+    }
   *out = b;
   return WTB_OK;
 }
@@ -385,6 +407,8 @@ extern "C" int wtb_batch_destroy(wtb_batch* b) {
   if (b->main) cudaStreamSynchronize(b->main->s);
   b->drop_graph();
   for (wtb_ctx* w : b->slots) wtb_ctx_destroy(w);
+  for (auto& e : b->ev)
+    if (e) cudaEventDestroy(e);
   wtb_ctx_destroy(b->main);
   delete b;
   return WTB_OK;
@@ -439,6 +463,12 @@ extern "C" int wtb_batch_bsesolver(wtb_batch* b, int nsys, const wtb_system* sys
   }
   if (first_bad != WTB_OK) return finish(first_bad);
 
+  auto ms_since = [](std::chrono::steady_clock::time_point a) {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - a).count();
+  };
+  b->t_stage = ms_since(t0);
+  b->t_build = 0;
+  const auto t1 = std::chrono::steady_clock::now();
   // the graph: reused while every baked-in size, parameter and device address is unchanged
   uint64_t key = 1469598103934665603ull;
   key = fnv(key, &nsys, sizeof(nsys));
@@ -482,8 +512,11 @@ extern "C" int wtb_batch_bsesolver(wtb_batch* b, int nsys, const wtb_system* sys
     b->key = k2 == 0 ? 1 : k2;
   }
   wtb_ctx* mc = b->main;
+  b->t_build = ms_since(t1);
+  const auto t2 = std::chrono::steady_clock::now();
   g_launch_count += b->graph_launches;
-  if (cudaGraphLaunch(b->exec, mc->s) != cudaSuccess || cudaStreamSynchronize(mc->s) != cudaSuccess) {
+  if (cudaEventRecord(b->ev[0], mc->s) != cudaSuccess || cudaGraphLaunch(b->exec, mc->s) != cudaSuccess ||
+      cudaEventRecord(b->ev[3], mc->s) != cudaSuccess || cudaStreamSynchronize(mc->s) != cudaSuccess) {
     b->drop_graph();
     for (int q = 0; q < nsys; ++q) {
       status[q] = WTB_ECUDA;
@@ -491,6 +524,17 @@ extern "C" int wtb_batch_bsesolver(wtb_batch* b, int nsys, const wtb_system* sys
     }
     return finish(WTB_ECUDA);
   }
+  b->t_run = ms_since(t2);
+  {
+    float a = 0.f, c2 = 0.f, d = 0.f;
+    cudaEventElapsedTime(&a, b->ev[0], b->ev[1]);
+    cudaEventElapsedTime(&c2, b->ev[1], b->ev[2]);
+    cudaEventElapsedTime(&d, b->ev[2], b->ev[3]);
+    b->t_front = a;
+    b->t_solve = c2;
+    b->t_back = d;
+  }
+  const auto t3 = std::chrono::steady_clock::now();
   // results: joint eigensolve, set-up status of every system, oscillator strengths
   std::vector<double> Eall;
   std::vector<SolveStats> stats;
@@ -543,7 +587,20 @@ extern "C" int wtb_batch_bsesolver(wtb_batch* b, int nsys, const wtb_system* sys
     c->have_solve = false;  // the slot holds no single-system solve for the backward pass
   }
   if (ctx_check_status(mc) != WTB_OK && first_bad == WTB_OK) first_bad = WTB_ECUDA;
+  b->t_collect = ms_since(t3);
   return finish(first_bad);
+}
+
+extern "C" int wtb_batch_timings(const wtb_batch* b, double* t_ms) {
+  if (!b || !t_ms) return WTB_EBADARG;
+  t_ms[0] = b->t_stage;
+  t_ms[1] = b->t_build;
+  t_ms[2] = b->t_run;
+  t_ms[3] = b->t_collect;
+  t_ms[4] = b->t_front;
+  t_ms[5] = b->t_solve;
+  t_ms[6] = b->t_back;
+  return WTB_OK;
 }
 
 // The joint operator of the last batch call (its accurate arithmetic, as in the final Rayleigh-Ritz) applied to
