@@ -263,7 +263,7 @@ def run_batch(args, torch, api, S, world, local):
                        "timing": "events on a side stream around the blocking batch call"},
             "phases_ms": {k: round(v, 3) for k, v in phases.items()},
             "e2e": {"value": value, "unit": "systems/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-            "gpu_launches": int(launches), "clocks": clk,
+            "gpu_launches": int(launches), "clocks": clk, "autotune": api.autotune_report(),
             "iterations": {"max": max(o["iterations"] for o in out), "mean": float(np.mean([o["iterations"] for o in out]))}}
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -403,7 +403,8 @@ def main():
                        "stage_ms": {k: last["timings"][k] for k in ("t_bands_ms", "t_build_ms", "t_solve_ms",
                                                                      "t_optics_ms", "t_total_ms")}},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-            "gpu_launches": int(launches), "roofline": roofline, "clocks": clk}
+            "gpu_launches": int(launches), "roofline": roofline, "clocks": clk,
+            "autotune": api.autotune_report()}
 
     fp64_cols = args.ref_matvecs
     if rank == 0 and not args.no_fp64:

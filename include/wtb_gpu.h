@@ -250,6 +250,10 @@ int wtb_batch_matvec(wtb_batch* batch, int ncol, const double* X, double* Y);
  * t_ms[5] joint eigensolve, t_ms[6] oscillator strengths. */
 int wtb_batch_timings(const wtb_batch* batch, double* t_ms);
 
+/* The contraction tiles the autotuner chose in this process (one entry per operator shape: the tile and the
+ * measured time of each candidate), as text into buf (len bytes, NUL-terminated).  Returns the full length. */
+int wtb_autotune_report(char* buf, int len);
+
 /* Number of CUDA kernels this library has launched in the process (instrumentation for benchmarks). */
 long long wtb_kernel_launch_count(void);
 

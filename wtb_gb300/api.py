@@ -90,6 +90,7 @@ def _load():
         "wtb_batch_bsesolver": [P, C.c_int, C.POINTER(CSystem), C.POINTER(CParams), C.c_int, dp, dp, ip, ip, dp],
         "wtb_batch_matvec": [P, C.c_int, dp, dp],
         "wtb_batch_timings": [P, dp],
+        "wtb_autotune_report": [C.c_char_p, C.c_int],
     }
     for name, args in sigs.items():
         f = getattr(lib, name)
@@ -149,6 +150,14 @@ def cparams(p: BSEParams, precision="fp64", op="dense", tol=0.0, maxit=0, block=
     c.op = OPS[op] if isinstance(op, str) else int(op)
     c.tol, c.maxit, c.block = float(tol), int(maxit), int(block)
     return c
+
+
+def autotune_report() -> str:
+    """The contraction tiles chosen by the autotuner in this process (wtb_autotune_report)."""
+    n = _lib.wtb_autotune_report(None, 0)
+    buf = C.create_string_buffer(n + 1)
+    _lib.wtb_autotune_report(buf, n + 1)
+    return buf.value.decode()
 
 
 def kernel_launch_count() -> int:

@@ -16,6 +16,7 @@
 // Precisions other than the split-BF16 matrix-free forms are solved system by system on the slots.
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -309,9 +310,29 @@ int build_graph(wtb_batch* b, int nsys, const wtb_bse_params* p, std::string* ms
   op->st = mc->st;
   if (err != cudaSuccess || cudaStreamSynchronize(mc->s) != cudaSuccess)
     return ctx_set_err(mc, WTB_ENOMEM, "batch: operator tables");
+  // the grouped contraction's column tile: measured on this batch's own operands (once per batch shape)
   std::string m2;
-  if (tc_gemm_group_create(&op->gemm, nsys, gd.data(), 3, 6, op->pa, op->pb, &m2) != WTB_OK)
-    return ctx_set_err(mc, WTB_ECUDA, "batch: " + m2);
+  TcGroupPlan* gp[2] = {nullptr, nullptr};  // bn = 256, 128
+  auto group_of = [&](int bn) -> TcGroupPlan* {
+    TcGroupPlan*& g = gp[bn == 128 ? 1 : 0];
+    if (!g && tc_gemm_group_create(&g, nsys, gd.data(), 3, 6, op->pa, op->pb, &m2, bn) != WTB_OK) g = nullptr;
+    return g;
+  };
+  uint64_t tkey = 1469598103934665603ull;
+  for (int q = 0; q < nsys; ++q) {
+    const int v[5] = {gd[q].M, gd[q].K, gd[q].N, gd[q].m_valid, gd[q].n_valid};
+    tkey = fnv(tkey, v, sizeof(v));
+  }
+  char what[96];
+  std::snprintf(what, sizeof(what), "grouped contraction of %d systems (%d slice products)", nsys, op->npairs);
+  const int bn = tc_autotune(tkey, what, [&](int cand) -> cudaError_t {
+    TcGroupPlan* g = group_of(cand);
+    return g ? tc_gemm_group_run(g, op->npairs, nullptr, mc->st, mc->s) : cudaErrorInvalidValue;
+  }, mc->s);
+  op->gemm = group_of(bn);
+  if (gp[0] && gp[0] != op->gemm) tc_gemm_group_destroy(gp[0]);
+  if (gp[1] && gp[1] != op->gemm) tc_gemm_group_destroy(gp[1]);
+  if (!op->gemm || cudaStreamSynchronize(mc->s) != cudaSuccess) return ctx_set_err(mc, WTB_ECUDA, "batch: " + m2);
 
   // the graph: set-up branches, joint eigensolve after all of them, oscillator branches after it
   cudaGraph_t G = nullptr;

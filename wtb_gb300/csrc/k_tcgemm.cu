@@ -14,7 +14,11 @@
 // Every mbarrier wait is bounded (2 s of %globaltimer); a wait that gives up sets the device status
 // word and an abort flag, the other roles stop at their next wait, and TMEM is freed before exit.
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
+#include <functional>
+#include <map>
+#include <mutex>
 #include <utility>
 
 #include <cuda.h>
@@ -26,20 +30,27 @@ namespace wtb {
 
 namespace {
 
-constexpr int BM = 128, BN = 256, BK = 64, STAGES = 4;
+constexpr int BM = 128, BK = 64;
 constexpr int A_BYTES = BM * BK * 2;
-constexpr int B_BYTES = BN * BK * 2;
-constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
-// room for two FP32 accumulators of BN columns: in split runs even K blocks go to the first, odd ones to
-// the second, and the epilogue adds them (halves the number of MMA accumulation steps each one takes)
-constexpr int TMEM_COLS = 2 * BN;
 constexpr unsigned long long kTimeoutNs = 2000000000ull;
-constexpr uint32_t kIdesc = (1u << 4)                       // D format: f32
-                            | (1u << 7)                     // A format: bf16
-                            | (1u << 10)                    // B format: bf16
-                            | ((uint32_t)(BN >> 3) << 17)   // N / 8
-                            | ((uint32_t)(BM >> 4) << 24);  // M / 16
-constexpr size_t kSmemBytes = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
+// Column tile BN (256 or 128, chosen per operator shape by the autotuner): the pipeline depth fills the same
+// shared memory with either.
+template <int BN_>
+struct TcShape {
+  static constexpr int BN = BN_;
+  static constexpr int STAGES = BN_ == 256 ? 4 : 6;
+  static constexpr int B_BYTES = BN * BK * 2;
+  static constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+  // room for two FP32 accumulators of BN columns: in split runs even K blocks go to the first, odd ones to
+  // the second, and the epilogue adds them (halves the number of MMA accumulation steps each one takes)
+  static constexpr int TMEM_COLS = 2 * BN;
+  static constexpr uint32_t IDESC = (1u << 4)                       // D format: f32
+                                    | (1u << 7)                     // A format: bf16
+                                    | (1u << 10)                    // B format: bf16
+                                    | ((uint32_t)(BN >> 3) << 17)   // N / 8
+                                    | ((uint32_t)(BM >> 4) << 24);  // M / 16
+  static constexpr size_t SMEM = (size_t)STAGES * STAGE_BYTES + 1024 + 256;
+};
 
 struct TcArgs {
   int K, kblocks, m_valid, n_valid, ldc, npairs;
@@ -137,8 +148,12 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 
 // One 128 x 256 output tile at (m0, n0) of the product described by args, operands through the tensor maps
 // (kernel parameter or global memory).
+template <int BN_>
 __device__ __forceinline__ void tc_gemm_tile(const CUtensorMap* mapA_p, const CUtensorMap* mapB_p,
                                              const TcArgs& args, int m0, int n0) {
+  using Sh = TcShape<BN_>;
+  constexpr int BN = Sh::BN, STAGES = Sh::STAGES, STAGE_BYTES = Sh::STAGE_BYTES, TMEM_COLS = Sh::TMEM_COLS;
+  constexpr uint32_t kIdesc = Sh::IDESC;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   const CUtensorMap& mapA = *mapA_p;
   const CUtensorMap& mapB = *mapB_p;
@@ -283,9 +298,10 @@ __device__ __forceinline__ void tc_gemm_tile(const CUtensorMap* mapA_p, const CU
   }
 }
 
+template <int BN>
 __global__ void __launch_bounds__(256, 1) tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA,
                                                          const __grid_constant__ CUtensorMap mapB, TcArgs args) {
-  tc_gemm_tile(&mapA, &mapB, args, blockIdx.y * BM, blockIdx.x * BN);
+  tc_gemm_tile<BN>(&mapA, &mapB, args, blockIdx.y * BM, blockIdx.x * BN);
 }
 
 // A group of independent products (the operators of a batch of systems): tensor maps and arguments per
@@ -299,6 +315,7 @@ struct TcGroup {
 // kb_chunk > 0: this launch is range `chunk` of a split run (K blocks [chunk kb_chunk, (chunk + 1) kb_chunk) of
 // each product, added to C from the second range on, even and odd K blocks in two accumulators).  Products of
 // frozen systems are skipped; the CTA returns before it touches shared memory or TMEM.
+template <int BN>
 __global__ void __launch_bounds__(256, 1) tc_gemm_grouped_kernel(const TcGroup* __restrict__ groups,
                                                                  const int4* __restrict__ tiles, int npairs,
                                                                  int chunk, int kb_chunk,
@@ -322,7 +339,7 @@ __global__ void __launch_bounds__(256, 1) tc_gemm_grouped_kernel(const TcGroup* 
     a.accumulate = 0;
     a.dual = 0;
   }
-  tc_gemm_tile(&g->mapA, &g->mapB, a, t.y * BM, t.z * BN);
+  tc_gemm_tile<BN>(&g->mapA, &g->mapB, a, t.y * BM, t.z * BN);
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
@@ -364,7 +381,24 @@ struct TcGemmPlan {
   CUtensorMap mapA, mapB;
   TcArgs args;
   dim3 grid;
+  int bn = 256;
 };
+
+namespace {
+template <int BN>
+void launch_tile_kernel(TcGemmPlan* p, const TcArgs& a, cudaStream_t s) {
+  tc_gemm_kernel<BN><<<p->grid, 256, TcShape<BN>::SMEM, s>>>(p->mapA, p->mapB, a);
+}
+cudaError_t raise_limits() {
+  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(tc_gemm_kernel<256>), TcShape<256>::SMEM);
+  if (e == cudaSuccess) e = raise_smem_limit(reinterpret_cast<const void*>(tc_gemm_kernel<128>), TcShape<128>::SMEM);
+  if (e == cudaSuccess)
+    e = raise_smem_limit(reinterpret_cast<const void*>(tc_gemm_grouped_kernel<256>), TcShape<256>::SMEM);
+  if (e == cudaSuccess)
+    e = raise_smem_limit(reinterpret_cast<const void*>(tc_gemm_grouped_kernel<128>), TcShape<128>::SMEM);
+  return e;
+}
+}  // namespace
 
 int tc_gemm_available() {
   int dev = 0, major = 0, minor = 0;
@@ -374,12 +408,12 @@ int tc_gemm_available() {
   return (major == 10 && minor == 3) ? 1 : 0;
 }
 
-// A: [na_slices][M][K] bf16 (M multiple of 128, K multiple of 64); B: [nb_slices][N][K] bf16 (N multiple of 256);
-// C: fp32 rows of length ldc; only rows < m_valid and columns < n_valid are written.
+// A: [na_slices][M][K] bf16 (M multiple of 128, K multiple of 64); B: [nb_slices][N][K] bf16 (N multiple of bn,
+// bn = 256 or 128); C: fp32 rows of length ldc; only rows < m_valid and columns < n_valid are written.
 int tc_gemm_plan_create(TcGemmPlan** plan, const uint16_t* A, int M, int K, long a_slice_stride, int na_slices,
                         const uint16_t* B, int N, long b_slice_stride, int nb_slices, float* C, int ldc, int npairs,
-                        const int* pair_a, const int* pair_b, std::string* msg) {
-  if (M % BM || N % BN || K % BK || npairs < 1 || npairs > 8 || ldc % 4) {
+                        const int* pair_a, const int* pair_b, std::string* msg, int bn) {
+  if ((bn != 256 && bn != 128) || M % BM || N % bn || K % BK || npairs < 1 || npairs > 8 || ldc % 4) {
     *msg = "tc_gemm: unsupported shape";
     return WTB_EBADARG;
   }
@@ -388,7 +422,8 @@ int tc_gemm_plan_create(TcGemmPlan** plan, const uint16_t* A, int M, int K, long
     return WTB_EBADARG;
   }
   TcGemmPlan* p = new TcGemmPlan();
-  if (!make_map(&p->mapA, A, K, M, na_slices, BM, msg) || !make_map(&p->mapB, B, K, N, nb_slices, BN, msg)) {
+  p->bn = bn;
+  if (!make_map(&p->mapA, A, K, M, na_slices, BM, msg) || !make_map(&p->mapB, B, K, N, nb_slices, bn, msg)) {
     delete p;
     return WTB_ECUDA;
   }
@@ -407,10 +442,9 @@ int tc_gemm_plan_create(TcGemmPlan** plan, const uint16_t* A, int M, int K, long
   p->args.C = C;
   p->args.m_valid = M;
   p->args.n_valid = N;
-  p->grid = dim3(N / BN, M / BM);
+  p->grid = dim3(N / bn, M / BM);
   // per device and thread-safe in the runtime; plans are cached, so this runs once per operator shape
-  if (raise_smem_limit(reinterpret_cast<const void*>(tc_gemm_kernel), (size_t)kSmemBytes) !=
-      cudaSuccess) {
+  if (raise_limits() != cudaSuccess) {
     *msg = "tc_gemm: shared memory attribute rejected";
     delete p;
     return WTB_ECUDA;
@@ -430,7 +464,11 @@ cudaError_t tc_gemm_run(TcGemmPlan* plan, DevStatus* st, cudaStream_t s) {
   plan->args.kbn = plan->args.kblocks;
   plan->args.accumulate = 0;
   plan->args.dual = 0;
-  tc_gemm_kernel<<<plan->grid, 256, kSmemBytes, s>>>(plan->mapA, plan->mapB, plan->args); ++g_launch_count;
+  if (plan->bn == 128)
+    launch_tile_kernel<128>(plan, plan->args, s);
+  else
+    launch_tile_kernel<256>(plan, plan->args, s);
+  ++g_launch_count;
   return cudaGetLastError();
 }
 
@@ -450,7 +488,11 @@ cudaError_t tc_gemm_run_split(TcGemmPlan* plan, DevStatus* st, cudaStream_t s, i
     a.kbn = std::min(kb_chunk, plan->args.kblocks - kb0);
     a.accumulate = kb0 > 0 ? 1 : 0;
     a.dual = 1;
-    tc_gemm_kernel<<<plan->grid, 256, kSmemBytes, s>>>(plan->mapA, plan->mapB, a); ++g_launch_count;
+    if (plan->bn == 128)
+      launch_tile_kernel<128>(plan, a, s);
+    else
+      launch_tile_kernel<256>(plan, a, s);
+    ++g_launch_count;
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -464,6 +506,7 @@ struct TcGroupPlan {
   int4* d_tiles = nullptr;
   int ntiles = 0;
   int max_kblocks = 0;
+  int bn = 256;
   ~TcGroupPlan() {
     if (d_groups) cudaFree(d_groups);
     if (d_tiles) cudaFree(d_tiles);
@@ -471,8 +514,8 @@ struct TcGroupPlan {
 };
 
 int tc_gemm_group_create(TcGroupPlan** plan, int n, const TcGroupDesc* d, int nslices, int npairs, const int* pair_a,
-                         const int* pair_b, std::string* msg) {
-  if (n < 1 || npairs < 1 || npairs > 8) {
+                         const int* pair_b, std::string* msg, int bn) {
+  if (n < 1 || npairs < 1 || npairs > 8 || (bn != 256 && bn != 128)) {
     *msg = "tc_gemm_group: bad arguments";
     return WTB_EBADARG;
   }
@@ -481,12 +524,12 @@ int tc_gemm_group_create(TcGroupPlan** plan, int n, const TcGroupDesc* d, int ns
   std::vector<std::pair<int, int>> order;  // (K blocks, product): the longest tiles go first
   for (int i = 0; i < n; ++i) {
     const TcGroupDesc& q = d[i];
-    if (q.M % BM || q.N % BN || q.K % BK || q.ldc % 4) {
+    if (q.M % BM || q.N % bn || q.K % BK || q.ldc % 4) {
       *msg = "tc_gemm_group: unsupported shape";
       return WTB_EBADARG;
     }
     std::memset(&h[i], 0, sizeof(TcGroup));
-    if (!make_map(&h[i].mapA, q.A, q.K, q.M, nslices, BM, msg) || !make_map(&h[i].mapB, q.B, q.K, q.N, nslices, BN, msg))
+    if (!make_map(&h[i].mapA, q.A, q.K, q.M, nslices, BM, msg) || !make_map(&h[i].mapB, q.B, q.K, q.N, nslices, bn, msg))
       return WTB_ECUDA;
     TcArgs& a = h[i].args;
     a.K = q.K;
@@ -510,12 +553,12 @@ int tc_gemm_group_create(TcGroupPlan** plan, int n, const TcGroupDesc* d, int ns
   int maxkb = 0;
   for (const auto& o : order) {
     const TcGroupDesc& q = d[o.second];
-    const int mt = (q.m_valid + BM - 1) / BM, nt = (q.n_valid + BN - 1) / BN;
+    const int mt = (q.m_valid + BM - 1) / BM, nt = (q.n_valid + bn - 1) / bn;
     for (int y = 0; y < mt; ++y)
       for (int x = 0; x < nt; ++x) tiles.push_back(make_int4(o.second, y, x, 0));
     maxkb = std::max(maxkb, o.first);
   }
-  if (raise_smem_limit(reinterpret_cast<const void*>(tc_gemm_grouped_kernel), (size_t)kSmemBytes) != cudaSuccess) {
+  if (raise_limits() != cudaSuccess) {
     *msg = "tc_gemm_group: shared memory attribute rejected";
     return WTB_ECUDA;
   }
@@ -530,13 +573,26 @@ int tc_gemm_group_create(TcGroupPlan** plan, int n, const TcGroupDesc* d, int ns
   }
   p->ntiles = (int)tiles.size();
   p->max_kblocks = maxkb;
+  p->bn = bn;
   *plan = p;
   return WTB_OK;
 }
 
-cudaError_t tc_gemm_group_run(TcGroupPlan* plan, int npairs, const int* frozen, DevStatus* st, cudaStream_t s) {
-  tc_gemm_grouped_kernel<<<plan->ntiles, 256, kSmemBytes, s>>>(plan->d_groups, plan->d_tiles, npairs, 0, 0, frozen, st);
+namespace {
+void launch_group(TcGroupPlan* plan, int npairs, int chunk, int kb_chunk, const int* frozen, DevStatus* st,
+                  cudaStream_t s) {
+  if (plan->bn == 128)
+    tc_gemm_grouped_kernel<128><<<plan->ntiles, 256, TcShape<128>::SMEM, s>>>(plan->d_groups, plan->d_tiles, npairs,
+                                                                               chunk, kb_chunk, frozen, st);
+  else
+    tc_gemm_grouped_kernel<256><<<plan->ntiles, 256, TcShape<256>::SMEM, s>>>(plan->d_groups, plan->d_tiles, npairs,
+                                                                               chunk, kb_chunk, frozen, st);
   ++g_launch_count;
+}
+}  // namespace
+
+cudaError_t tc_gemm_group_run(TcGroupPlan* plan, int npairs, const int* frozen, DevStatus* st, cudaStream_t s) {
+  launch_group(plan, npairs, 0, 0, frozen, st, s);
   return cudaGetLastError();
 }
 
@@ -544,9 +600,7 @@ cudaError_t tc_gemm_group_run_split(TcGroupPlan* plan, int npairs, const int* fr
                                     int kb_chunk) {
   if (kb_chunk < 1) kb_chunk = plan->max_kblocks;
   for (int c = 0; c * kb_chunk < plan->max_kblocks; ++c) {
-    tc_gemm_grouped_kernel<<<plan->ntiles, 256, kSmemBytes, s>>>(plan->d_groups, plan->d_tiles, npairs, c, kb_chunk,
-                                                                 frozen, st);
-    ++g_launch_count;
+    launch_group(plan, npairs, c, kb_chunk, frozen, st, s);
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }
@@ -554,5 +608,62 @@ cudaError_t tc_gemm_group_run_split(TcGroupPlan* plan, int npairs, const int* fr
 }
 
 void tc_gemm_group_destroy(TcGroupPlan* plan) { delete plan; }
+
+// ------------------------------------------------------------------------------------------------ autotuner
+// The column tile of the contraction is chosen by measurement: run(bn) launches the caller's own product with
+// that tile; each candidate gets one warm-up launch and three timed ones (CUDA events on the caller's stream)
+// and the fastest mean wins.  Results are kept per shape key for the life of the process, so a shape is
+// measured once (and never while a stream is being captured: the default tile is used then).
+namespace {
+struct TuneEntry {
+  int bn;
+  double ms[2];  // mean ms of bn = 256 and bn = 128
+  std::string what;
+};
+std::mutex g_tune_mu;
+std::map<uint64_t, TuneEntry> g_tune;
+}  // namespace
+
+int tc_autotune(uint64_t key, const std::string& what, const std::function<cudaError_t(int)>& run, cudaStream_t s) {
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) return it->second.bn;
+  }
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return 256;
+  const int cand[2] = {256, 128};
+  double ms[2] = {1e30, 1e30};
+  cudaEvent_t a = nullptr, b = nullptr;
+  if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return 256;
+  for (int i = 0; i < 2; ++i) {
+    if (run(cand[i]) != cudaSuccess) continue;
+    if (cudaEventRecord(a, s) != cudaSuccess) continue;
+    bool ok = true;
+    for (int r = 0; r < 3 && ok; ++r) ok = run(cand[i]) == cudaSuccess;
+    float t = 0.f;
+    if (ok && cudaEventRecord(b, s) == cudaSuccess && cudaEventSynchronize(b) == cudaSuccess &&
+        cudaEventElapsedTime(&t, a, b) == cudaSuccess)
+      ms[i] = t / 3.0;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  const int bn = ms[1] < ms[0] ? 128 : 256;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = TuneEntry{bn, {ms[0], ms[1]}, what};
+  return bn;
+}
+
+std::string tc_autotune_report() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  std::string out;
+  char buf[256];
+  for (const auto& kv : g_tune) {
+    std::snprintf(buf, sizeof(buf), "%s%s: tile 128x%d (128x256 %.4f ms, 128x128 %.4f ms)", out.empty() ? "" : "; ",
+                  kv.second.what.c_str(), kv.second.bn, kv.second.ms[0], kv.second.ms[1]);
+    out += buf;
+  }
+  return out;
+}
 
 }  // namespace wtb

@@ -15,6 +15,7 @@
 // EPS_SMALLEST_MAGNITUDE, tol 1e-8, 200 iterations); for the positive BSE spectra of this path the
 // smallest-magnitude and smallest-algebraic eigenvalues coincide.
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <functional>
 #include <cstdlib>
@@ -45,21 +46,8 @@ cudaError_t MatFreeOperator<S>::apply(const cplx<S>* X, int ldx, int c0, int nco
         e = launch_mf_gather<float, uint16_t>(X, ldx, c0 + b0, nb, vec_win, nk, nv, nc, w, Zs, Kpad, nslices,
                                               (long)Npad * Kpad, s);
         if (e != cudaSuccess) return e;
-        const long key = (long)N * 16 + npairs;
-        auto it = plans.find(key);
-        TcGemmPlan* plan = nullptr;
-        if (it == plans.end()) {
-          std::string m2;
-          if (tc_gemm_plan_create(&plan, Vs, Mpad, Kpad, (long)Mpad * Kpad, nslices, Zs, Npad, (long)Npad * Kpad,
-                                  nslices, reinterpret_cast<float*>(Tm), Npad, npairs, pa, pb, &m2) != WTB_OK) {
-            if (msg) *msg = m2;
-            return cudaErrorInvalidValue;
-          }
-          tc_gemm_set_valid(plan, nk, N);
-          plans[key] = plan;
-        } else {
-          plan = it->second;
-        }
+        TcGemmPlan* plan = plan_for(N, npairs, tile_n);
+        if (!plan) return cudaErrorInvalidValue;
         cudaEvent_t ea = nullptr, eb = nullptr;
         // the live profile covers the iteration's contraction launches (the final split run is a
         // different launch configuration and is left out of it)
@@ -119,18 +107,8 @@ cudaError_t MatFreeOperator<S>::time_contraction(int reps, int ncol, cudaStream_
   const int np = npairs0 > 0 ? npairs0 : npairs;
   TcGemmPlan* plan = nullptr;
   if (kind == GEMM_TC_BF16) {
-    const long key = (long)N * 16 + np;
-    auto it = plans.find(key);
-    if (it == plans.end()) {
-      std::string m2;
-      if (tc_gemm_plan_create(&plan, Vs, Mpad, Kpad, (long)Mpad * Kpad, nslices, Zs, Npad, (long)Npad * Kpad, nslices,
-                              reinterpret_cast<float*>(Tm), Npad, np, pa, pb, &m2) != WTB_OK)
-        return cudaErrorInvalidValue;
-      tc_gemm_set_valid(plan, nk, N);
-      plans[key] = plan;
-    } else {
-      plan = it->second;
-    }
+    plan = plan_for(N, np, tile_n);
+    if (!plan) return cudaErrorInvalidValue;
   }
   for (int r = 0; r < reps; ++r) {
     cudaEvent_t ea, eb;
@@ -167,21 +145,8 @@ cudaError_t MatFreeOperator<S>::contract(const cplx<S>* X, int ldx, int ncol, cu
       cudaError_t e = launch_mf_gather<float, uint16_t>(X, ldx, 0, ncol, vec_win, nk, nv, nc, w, Zs, Kpad, nslices,
                                                         (long)Npad * Kpad, s);
       if (e != cudaSuccess) return e;
-      const long key = (long)N * 16 + npairs;
-      TcGemmPlan* plan = nullptr;
-      auto it = plans.find(key);
-      if (it == plans.end()) {
-        std::string m2;
-        if (tc_gemm_plan_create(&plan, Vs, Mpad, Kpad, (long)Mpad * Kpad, nslices, Zs, Npad, (long)Npad * Kpad,
-                                nslices, reinterpret_cast<float*>(Tm), Npad, npairs, pa, pb, &m2) != WTB_OK) {
-          if (msg) *msg = m2;
-          return cudaErrorInvalidValue;
-        }
-        tc_gemm_set_valid(plan, nk, N);
-        plans[key] = plan;
-      } else {
-        plan = it->second;
-      }
+      TcGemmPlan* plan = plan_for(N, npairs, tile_n);
+      if (!plan) return cudaErrorInvalidValue;
       return tc_gemm_run(plan, st, s);
     } else {
       return cudaErrorInvalidValue;
@@ -190,6 +155,44 @@ cudaError_t MatFreeOperator<S>::contract(const cplx<S>* X, int ldx, int ncol, cu
   cudaError_t e = launch_mf_gather<S, S>(X, ldx, 0, ncol, vec_win, nk, nv, nc, w, Zr, Kpad, 1, 0, s);
   if (e != cudaSuccess) return e;
   return launch_simt_gemm_tn<S>(Vr, Kpad, Zr, Kpad, reinterpret_cast<S*>(Tm), Npad, nk, N, Kpad, s);
+}
+
+template <class S>
+TcGemmPlan* MatFreeOperator<S>::plan_for(int N, int np, int bn) {
+  const long key = ((long)N * 16 + np) * 2 + (bn == 128 ? 1 : 0);
+  auto it = plans.find(key);
+  if (it != plans.end()) return it->second;
+  std::string m2;
+  TcGemmPlan* plan = nullptr;
+  if (tc_gemm_plan_create(&plan, Vs, Mpad, Kpad, (long)Mpad * Kpad, nslices, Zs, Npad, (long)Npad * Kpad, nslices,
+                          reinterpret_cast<float*>(Tm), Npad, np, pa, pb, &m2, bn) != WTB_OK) {
+    if (msg) *msg = m2;
+    return nullptr;
+  }
+  tc_gemm_set_valid(plan, nk, N);
+  plans[key] = plan;
+  return plan;
+}
+
+template <class S>
+cudaError_t MatFreeOperator<S>::autotune(cudaStream_t s) {
+  if (kind != GEMM_TC_BF16) return cudaSuccess;
+  const int N = 2 * w * w * nbmax;
+  const int np = npairs;
+  uint64_t key = 1469598103934665603ull;
+  const long v[] = {1, Mpad, Kpad, Npad, nk, N, np, nslices};
+  for (long x : v)
+    for (int b = 0; b < 8; ++b) {
+      key ^= ((uint64_t)x >> (8 * b)) & 0xffu;
+      key *= 1099511628211ull;
+    }
+  char what[96];
+  std::snprintf(what, sizeof(what), "contraction %dx%dx%d (%d slice products)", nk, N, nk, np);
+  tile_n = tc_autotune(key, what, [&](int bn) -> cudaError_t {
+    TcGemmPlan* plan = plan_for(N, np, bn);
+    return plan ? tc_gemm_run(plan, st, s) : cudaErrorInvalidValue;
+  }, s);
+  return cudaSuccess;
 }
 
 template struct MatFreeOperator<float>;

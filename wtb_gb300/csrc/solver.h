@@ -175,6 +175,7 @@ struct MatFreeOperator : Operator<S> {
   void signature(std::vector<uint64_t>* sig) const override {
     const uint64_t v[] = {2, (uint64_t)kind, (uint64_t)nk, (uint64_t)nv, (uint64_t)nc, (uint64_t)w, (uint64_t)nbmax,
                           (uint64_t)nslices, (uint64_t)npairs, (uint64_t)npairs_refine, (uint64_t)kchunk_final,
+                          (uint64_t)tile_n,
                           (uint64_t)Mpad, (uint64_t)Kpad, (uint64_t)Npad, (uint64_t)(uintptr_t)vec_win,
                           (uint64_t)(uintptr_t)dE, (uint64_t)(uintptr_t)Vs, (uint64_t)(uintptr_t)Zs,
                           (uint64_t)(uintptr_t)Vr, (uint64_t)(uintptr_t)Zr, (uint64_t)(uintptr_t)Tm,
@@ -189,6 +190,10 @@ struct MatFreeOperator : Operator<S> {
   int kchunk_final = 4;
   bool final_apply = false;
   void set_final(bool on) override { final_apply = on; }
+  // column tile of the contraction (tensor-core kind), chosen by autotune() for the operator's shape
+  int tile_n = 256;
+  TcGemmPlan* plan_for(int N, int np, int bn);
+  cudaError_t autotune(cudaStream_t s);
 };
 
 struct SolveStats {

@@ -295,8 +295,9 @@ int auto_block(const wtb_bse_params* p, int dim, bool fp64) {
 
 // tag: suffix of the buffers holding the V table and its forms (a second operator, e.g. the dV/dr0 one,
 // must not overwrite the first); deriv_r0: build the operator of dV/dr0 with no diagonal term.
+// tune: choose the contraction's column tile by timing (not for the operators a batch contracts jointly)
 int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob, const std::string& tag = "",
-                  bool deriv_r0 = false) {
+                  bool deriv_r0 = false, bool tune = true) {
   const int nk = c->nk, nv = c->nv, nc = c->nc, w = c->w;
   const int dim = nk * nc * nv;
   cudaError_t err = cudaSuccess;
@@ -384,6 +385,8 @@ int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob, 
   op->Tm = c->ws.get<float>("Tbf", (size_t)Mpad * Npad, &err);
   CKC(err);
   if (const char* kc = std::getenv("WTB_FINAL_KCHUNK")) op->kchunk_final = std::atoi(kc);
+  // column tile of the contraction: measured once per shape (skipped while a graph is being captured)
+  if (tune) CKC(op->autotune(c->s));
   return WTB_OK;
 }
 
@@ -982,6 +985,16 @@ int wtb_bse_matvec(wtb_ctx* c, const wtb_bse_params* p, int ncol, const double* 
 
 long long wtb_kernel_launch_count(void) { return g_launch_count.load(); }
 
+int wtb_autotune_report(char* buf, int len) {
+  const std::string r = tc_autotune_report();
+  if (buf && len > 0) {
+    const size_t n = std::min((size_t)len - 1, r.size());
+    std::memcpy(buf, r.data(), n);
+    buf[n] = '\0';
+  }
+  return (int)r.size();
+}
+
 void* wtb_ctx_stream(wtb_ctx* c) { return c ? (void*)c->s : nullptr; }
 
 int wtb_profile_enable(wtb_ctx* c, int on) {
@@ -1020,7 +1033,7 @@ int ctx_stage_system(wtb_ctx* c, const wtb_bse_params* p) {
 int ctx_enqueue_system(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob) {
   CKR(enqueue_bands(c));
   CKR(compute_optics(c, p));
-  return make_operator(c, p, nbmax, ob);
+  return make_operator(c, p, nbmax, ob, "", false, false);
 }
 
 int ctx_auto_block(const wtb_bse_params* p, int dim, bool fp64) { return auto_block(p, dim, fp64); }

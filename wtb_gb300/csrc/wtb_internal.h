@@ -9,6 +9,7 @@
 //   V table     V[k][k'] real, padded rows/cols for the tensor-core GEMM
 #pragma once
 #include <atomic>
+#include <functional>
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
@@ -221,9 +222,10 @@ cudaError_t launch_round_f32(const double* V, int ldv, int rows, int cols, float
 
 // tcgen05 split-bf16 GEMM: C[M][N] (fp32, ldc) = sum over slice pairs of A_sa[M][K] * B_sb[N][K]^T.
 struct TcGemmPlan;
+// bn: column tile of the output (256 or 128)
 int tc_gemm_plan_create(TcGemmPlan** plan, const uint16_t* A, int M, int K, long a_slice_stride, int na_slices,
                         const uint16_t* B, int N, long b_slice_stride, int nb_slices, float* C, int ldc,
-                        int npairs, const int* pair_a, const int* pair_b, std::string* msg);
+                        int npairs, const int* pair_a, const int* pair_b, std::string* msg, int bn = 256);
 cudaError_t tc_gemm_run(TcGemmPlan* plan, DevStatus* st, cudaStream_t s);
 // the same product with K split into ranges of kb_chunk 64-wide blocks, summed in FP32 round-to-nearest
 cudaError_t tc_gemm_run_split(TcGemmPlan* plan, DevStatus* st, cudaStream_t s, int kb_chunk);
@@ -239,11 +241,15 @@ struct TcGroupDesc {
 };
 struct TcGroupPlan;
 int tc_gemm_group_create(TcGroupPlan** plan, int n, const TcGroupDesc* descs, int nslices, int npairs,
-                         const int* pair_a, const int* pair_b, std::string* msg);
+                         const int* pair_a, const int* pair_b, std::string* msg, int bn = 256);
 cudaError_t tc_gemm_group_run(TcGroupPlan* plan, int npairs, const int* frozen, DevStatus* st, cudaStream_t s);
 cudaError_t tc_gemm_group_run_split(TcGroupPlan* plan, int npairs, const int* frozen, DevStatus* st, cudaStream_t s,
                                     int kb_chunk);
 void tc_gemm_group_destroy(TcGroupPlan* plan);
+// Chooses the column tile (256 or 128) of a contraction shape by timing run(bn) on the caller's stream; cached
+// per key for the process (what: a label for the report).
+int tc_autotune(uint64_t key, const std::string& what, const std::function<cudaError_t(int)>& run, cudaStream_t s);
+std::string tc_autotune_report();
 
 // ----------------------------------------------------------------------------- spectrum
 cudaError_t launch_oscillators(const zd* A, int lda, int nev, int dim, const zd* hr, double* osc /*[8][nev]*/,
