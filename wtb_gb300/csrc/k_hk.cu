@@ -3,9 +3,10 @@
 // table.  Follows eigsys (src/module_hamiltonian.F90:200-320), the bsesolver band loop
 // (src/module_bse.F90:2230-2245), hlm/optsp (src/module_optics.F90:12-167) and module_coulomb.
 //
-// Eigensolver: cyclic two-sided Jacobi for complex Hermitian matrices with the round-robin (circle)
-// pair ordering, so the n/2 rotations of a step touch disjoint rows/columns and are applied by all
-// threads at once.  The matrix and the accumulated rotations live in shared memory (w <= 64).
+// Eigensolver: the CTA routine of small_eig.cuh (Householder tridiagonalisation, bisection, inverse iteration),
+// in FP64; for the tensor-core forms in FP32 followed by FP64 Rayleigh quotients against the FP64 H(k), which
+// leaves the band energies FP64-accurate and the vectors FP32-accurate (the FP64 pipe is the bound of this
+// kernel on GB300).
 // Gauge: every eigenvector is rotated so its first component is real and >= 0, the gauge ZHEEV('L')
 // produces up to a sign (the Householder reflectors of ZHETRD('L') leave e1 invariant).
 #include "small_eig.cuh"
@@ -42,6 +43,7 @@ __device__ __forceinline__ double rcomp_f32(const int* rvec, int nR, int iR, con
   return (double)__double2float_rn(rcart(r1, r2, r3, rl, a));
 }
 
+template <bool kMixed>
 __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict__ hr, const int* __restrict__ rvec,
                                                             const int* __restrict__ ndegen, int nR, int w,
                                                             const double* __restrict__ rlat, double efermi, double scs,
@@ -67,6 +69,18 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
   double* Lv = Dv + n * (n + 1);  // reuse both
   int* cl = reinterpret_cast<int*>(Lv + n * (n + 1));
   zd* U = reinterpret_cast<zd*>(Dv);
+  // mixed: FP32 eigensolver workspace after the FP64 one, and the FP64 eigenvectors and eigenvalues
+  zf* A32 = reinterpret_cast<zf*>(cl + ((n + 1) & ~1));
+  zf* p32 = A32 + n * ld;
+  zf* tau32 = p32 + n;
+  float* d32 = reinterpret_cast<float*>(tau32 + n);
+  float* e32 = d32 + n;
+  float* e2_32 = e32 + n;
+  float* lam32 = e2_32 + n;
+  float* red32 = lam32 + n;
+  float* Z32 = red32 + 4;
+  float* Dv32 = Z32 + n * (n + 1);
+  float* Lv32 = Dv32 + n * (n + 1);
   __shared__ double rl[9];
   __shared__ int s_nocp;
   const int tid = threadIdx.x;
@@ -97,8 +111,50 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
     if (m != c) A[c * ld + m] = mk<double>(acc.re, -acc.im);
   }
   __syncthreads();
-  tridiag_cta<double>(A, ld, n, d, e, tau, p);
-  tridiag_eigvecs_cta<double>(A, ld, n, n, d, e, tau, e2, lam, Z, Dv, Lv, cl, U, n, red);
+  if constexpr (kMixed) {
+    // FP32 eigensolve of the rounded H(k), then FP64 Rayleigh quotients of the normalised vectors against
+    // the FP64 H(k): eigenvalues carry the square of the vectors' FP32 error (FP64-accurate), vectors FP32's
+    for (int q = tid; q < n * ld; q += blockDim.x) A32[q] = mk<float>((float)A[q].re, (float)A[q].im);
+    __syncthreads();
+    zf* U32 = reinterpret_cast<zf*>(Dv32);
+    tridiag_cta<float>(A32, ld, n, d32, e32, tau32, p32);
+    tridiag_eigvecs_cta<float>(A32, ld, n, n, d32, e32, tau32, e2_32, lam32, Z32, Dv32, Lv32, cl, U32, n, red32);
+    // U (FP64, column j = vector j) = U32 normalised in FP64; H U (n x n complex, column-major) after the FP32
+    // workspace
+    zd* HU = reinterpret_cast<zd*>((reinterpret_cast<uintptr_t>(Lv32 + n * (n + 1)) + 15) & ~(uintptr_t)15);
+    for (int q = tid; q < n * n; q += blockDim.x) {
+      const int i = q / n, j = q % n;  // row i of H, column j of U
+      zd acc = mk<double>(0.0, 0.0);
+      for (int c = 0; c < n; ++c) {
+        const zf u = U32[j * n + c];
+        cfma(acc, A[i * ld + c], mk<double>((double)u.re, (double)u.im));
+      }
+      HU[j * n + i] = acc;
+    }
+    __syncthreads();
+    const int lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+    for (int j = warp; j < n; j += nwarp) {
+      double nn = 0.0, rq = 0.0;
+      for (int i = lane; i < n; i += 32) {
+        const zf u = U32[j * n + i];
+        const zd ud = mk<double>((double)u.re, (double)u.im), h = HU[j * n + i];
+        nn += ud.re * ud.re + ud.im * ud.im;
+        rq += ud.re * h.re + ud.im * h.im;  // Re(conj(u_i) (H u)_i)
+      }
+      nn = warp_allsum(nn);
+      rq = warp_allsum(rq);
+      const double inv = nn > 0.0 ? 1.0 / sqrt(nn) : 0.0;
+      if (lane == 0) lam[j] = nn > 0.0 ? rq / nn : (double)lam32[j];
+      for (int i = lane; i < n; i += 32) {
+        const zf u = U32[j * n + i];
+        U[j * n + i] = mk<double>((double)u.re * inv, (double)u.im * inv);
+      }
+    }
+    __syncthreads();
+  } else {
+    tridiag_cta<double>(A, ld, n, d, e, tau, p);
+    tridiag_eigvecs_cta<double>(A, ld, n, n, d, e, tau, e2, lam, Z, Dv, Lv, cl, U, n, red);
+  }
   if (tid == 0) {
     int cnt = 0;
     for (int j = 0; j < n; ++j) cnt += (lam[j] <= 0.0);
@@ -137,6 +193,7 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
 }
 
 // ----------------------------------------------------------------------------- optics (hlm + optsp)
+template <class T>
 __global__ void __launch_bounds__(kHkThreads) optics_kernel(const zd* __restrict__ hr, const int* __restrict__ rvec,
                                                             const int* __restrict__ ndegen, int nR, int w,
                                                             const double* __restrict__ rlat,
@@ -174,17 +231,19 @@ __global__ void __launch_bounds__(kHkThreads) optics_kernel(const zd* __restrict
     __syncthreads();
     for (int r = tid; r < nR; r += blockDim.x) Ra[r] = rcomp_f32(rvec, nR, r, rl, a);
     __syncthreads();
-    // M = sum_R i R_a e^{i phi} H(R)/ndegen; the on-site diagonal at R = 0 is removed (R_a = 0 there)
+    // M = sum_R i R_a e^{i phi} H(R)/ndegen (the R = 0 term vanishes with R_a = 0, its diagonal is skipped as
+    // in hlm), in arithmetic T: FP32 for the tensor-core forms, whose oscillator strengths need 1e-4
     for (int e = tid; e < w * w; e += blockDim.x) {
       const int m = e / w, c = e % w;
-      zd acc = mk<double>(0.0, 0.0);
+      cplx<T> acc = mk<T>(0, 0);
       for (int r = 0; r < nR; ++r) {
         const bool r0 = rvec[r] == 0 && rvec[nR + r] == 0 && rvec[2 * nR + r] == 0;
         if (r0 && m == c) continue;
-        const zd f = mk<double>(-Ra[r] * eph[r].im, Ra[r] * eph[r].re);  // i R_a e
-        cfma(acc, f, hr[((size_t)r * w + m) * w + c]);
+        const cplx<T> f = mk<T>((T)(-Ra[r] * eph[r].im), (T)(Ra[r] * eph[r].re));  // i R_a e
+        const zd h = hr[((size_t)r * w + m) * w + c];
+        cfma(acc, f, mk<T>((T)h.re, (T)h.im));
       }
-      M[e] = acc;
+      M[e] = mk<double>((double)acc.re, (double)acc.im);
     }
     __syncthreads();
     for (int e = tid; e < nv * w; e += blockDim.x) {
@@ -389,29 +448,47 @@ __global__ void transition_kernel(const double* __restrict__ eig_win, int nk, in
 
 cudaError_t launch_hk_eig(const zd* hr, const int* rvec, const int* ndegen, int nR, int w, const double* rlat_rm,
                           double efermi, double scs, const double* kpt, int nk, int nv, int nc, double* eig_all,
-                          zd* vec_all, double* eig_win, zd* vec_win, int* nocp, DevStatus* st, cudaStream_t s) {
+                          zd* vec_all, double* eig_win, zd* vec_win, int* nocp, DevStatus* st, cudaStream_t s,
+                          bool mixed) {
   if (w > 64 || w < 1) return cudaErrorInvalidValue;
   const int n = w;
   // A, phases, p, tau (complex); d, e, e2, lam, red; Z, Dv, Lv (n x (n + 1) each); cluster ids
-  const size_t smem = (size_t)(n * (n + 1) + nR + 2 * n) * sizeof(zd) + (size_t)(4 * n + 4 + 3 * n * (n + 1)) * sizeof(double) +
-                      (size_t)(n + 4) * sizeof(int) + 64;
+  size_t smem = (size_t)(n * (n + 1) + nR + 2 * n) * sizeof(zd) + (size_t)(4 * n + 4 + 3 * n * (n + 1)) * sizeof(double) +
+                (size_t)((n + 1) & ~1) * sizeof(int);
+  // mixed: the FP32 copy and workspace, then H U
+  const size_t smem_mixed = smem + (size_t)(n * (n + 1) + 2 * n) * sizeof(zf) +
+                            (size_t)(4 * n + 4 + 3 * n * (n + 1)) * sizeof(float) + 16 + (size_t)n * n * sizeof(zd);
+  if (mixed && smem_mixed > 200 * 1024) mixed = false;  // the FP64 route for very wide bases
+  smem = (mixed ? smem_mixed : smem) + 64;
   if (smem > 220 * 1024) return cudaErrorInvalidValue;
-  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(hk_eig_kernel), (size_t)smem);
+  const void* fn = mixed ? reinterpret_cast<const void*>(hk_eig_kernel<true>) : reinterpret_cast<const void*>(hk_eig_kernel<false>);
+  cudaError_t e = raise_smem_limit(fn, (size_t)smem);
   if (e != cudaSuccess) return e;
-  hk_eig_kernel<<<nk, kHkThreads, smem, s>>>(hr, rvec, ndegen, nR, w, rlat_rm, efermi, scs, kpt, nk, nv, nc, eig_all,
-                                             vec_all, eig_win, vec_win, nocp, st); ++g_launch_count;
+  if (mixed)
+    hk_eig_kernel<true><<<nk, kHkThreads, smem, s>>>(hr, rvec, ndegen, nR, w, rlat_rm, efermi, scs, kpt, nk, nv, nc,
+                                                     eig_all, vec_all, eig_win, vec_win, nocp, st);
+  else
+    hk_eig_kernel<false><<<nk, kHkThreads, smem, s>>>(hr, rvec, ndegen, nR, w, rlat_rm, efermi, scs, kpt, nk, nv, nc,
+                                                      eig_all, vec_all, eig_win, vec_win, nocp, st);
+  ++g_launch_count;
   return cudaGetLastError();
 }
 
 cudaError_t launch_optics(const zd* hr, const int* rvec, const int* ndegen, int nR, int w, const double* rlat_rm,
                           const double* kpt, int nk, int nv, int nc, const double* eig_win, const zd* vec_win,
-                          double cshift, zd* hout, cudaStream_t s) {
+                          double cshift, zd* hout, cudaStream_t s, bool mixed) {
   const int nb = nv + nc;
   const size_t smem = (size_t)(w * w + nb * w + nv * w + nR) * sizeof(zd) + nR * sizeof(double) + 16;
-  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(optics_kernel), (size_t)smem);
+  const void* fn = mixed ? reinterpret_cast<const void*>(optics_kernel<float>) : reinterpret_cast<const void*>(optics_kernel<double>);
+  cudaError_t e = raise_smem_limit(fn, (size_t)smem);
   if (e != cudaSuccess) return e;
-  optics_kernel<<<nk, kHkThreads, smem, s>>>(hr, rvec, ndegen, nR, w, rlat_rm, kpt, nk, nv, nc, eig_win, vec_win,
-                                             (float)cshift, hout); ++g_launch_count;
+  if (mixed)
+    optics_kernel<float><<<nk, kHkThreads, smem, s>>>(hr, rvec, ndegen, nR, w, rlat_rm, kpt, nk, nv, nc, eig_win,
+                                                      vec_win, (float)cshift, hout);
+  else
+    optics_kernel<double><<<nk, kHkThreads, smem, s>>>(hr, rvec, ndegen, nR, w, rlat_rm, kpt, nk, nv, nc, eig_win,
+                                                       vec_win, (float)cshift, hout);
+  ++g_launch_count;
   return cudaGetLastError();
 }
 

@@ -213,14 +213,20 @@ int stage_bands(wtb_ctx* c, int nk, const double* kpt_rm, int nv, int nc) {
   return WTB_OK;
 }
 
-int enqueue_bands(wtb_ctx* c) {
+// The split-BF16 (tensor-core) forms take their bands from the mixed band solver (FP32 eigensolve, FP64
+// Rayleigh quotients) and their velocity matrix elements from FP32 Fourier sums: their operator carries
+// about 1e-7 relative error already, and on this GPU those set-up kernels are bound by the FP64 pipe.
+bool tc_form(const wtb_bse_params* p) { return p && p->op == WTB_OP_MATFREE && p->precision >= WTB_PREC_BF16X3; }
+
+int enqueue_bands(wtb_ctx* c, bool mixed = false) {
   cudaError_t err = cudaSuccess;
   const int nk = c->nk, nv = c->nv, nc = c->nc, w = c->w, nb = nv + nc;
   CKC(launch_hk_eig(c->ws.get<zd>("hr", 0, &err), c->ws.get<int>("rvec", 0, &err), c->ws.get<int>("ndegen", 0, &err),
                     c->nR, w, c->ws.get<double>("rlat", 0, &err), c->efermi, c->scs, c->ws.get<double>("kpt", 0, &err),
                     nk, nv, nc, c->ws.get<double>("eig_all", 0, &err), c->ws.get<zd>("vec_all", 0, &err),
                     nb > 0 ? c->ws.get<double>("eig_win", 0, &err) : nullptr,
-                    nb > 0 ? c->ws.get<zd>("vec_win", 0, &err) : nullptr, c->ws.get<int>("nocp", 0, &err), c->st, c->s));
+                    nb > 0 ? c->ws.get<zd>("vec_win", 0, &err) : nullptr, c->ws.get<int>("nocp", 0, &err), c->st, c->s,
+                    mixed));
   return WTB_OK;
 }
 
@@ -697,7 +703,7 @@ static int stage_mesh(wtb_ctx* c, const wtb_bse_params* p) {
 
 static int ensure_bands_for(wtb_ctx* c, const wtb_bse_params* p) {
   CKR(stage_mesh(c, p));
-  CKR(enqueue_bands(c));
+  CKR(enqueue_bands(c, tc_form(p)));
   return check_status(c);
 }
 
@@ -709,7 +715,7 @@ static int compute_optics(wtb_ctx* c, const wtb_bse_params* p) {
   CKC(launch_optics(c->ws.get<zd>("hr", 0, &err), c->ws.get<int>("rvec", 0, &err), c->ws.get<int>("ndegen", 0, &err),
                     c->nR, c->w, c->ws.get<double>("rlat", 0, &err), c->ws.get<double>("kpt", 0, &err), c->nk, c->nv,
                     c->nc, c->ws.get<double>("eig_win", 0, &err), c->ws.get<zd>("vec_win", 0, &err), p->cshift, hout,
-                    c->s));
+                    c->s, tc_form(p)));
   c->have_hr_optics = true;
   c->have_solve = false;  // hrvel now follows p->cshift; wtb_bsesolver sets it again after its solve
   return WTB_OK;
@@ -1031,7 +1037,7 @@ int ctx_stage_system(wtb_ctx* c, const wtb_bse_params* p) {
 }
 
 int ctx_enqueue_system(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob) {
-  CKR(enqueue_bands(c));
+  CKR(enqueue_bands(c, tc_form(p)));
   CKR(compute_optics(c, p));
   return make_operator(c, p, nbmax, ob, "", false, false);
 }

@@ -93,14 +93,15 @@ struct CoulParams {
 
 // ----------------------------------------------------------------------------- kernels (launchers)
 // H(k) + Hermitian eigensolve + gauge + band window.  Returns 0 or a launch error.
+// mixed: FP32 eigensolve + FP64 Rayleigh quotients (energies FP64-accurate, vectors FP32-accurate)
 cudaError_t launch_hk_eig(const zd* hr, const int* rvec, const int* ndegen, int nR, int w,
                           const double* rlat_rm, double efermi, double scs, const double* kpt, int nk,
                           int nv, int nc, double* eig_all, zd* vec_all, double* eig_win, zd* vec_win,
-                          int* nocp, DevStatus* st, cudaStream_t s);
-// Velocity matrix elements hr[5][dim] (x, y, z, sigma+, sigma-).
+                          int* nocp, DevStatus* st, cudaStream_t s, bool mixed = false);
+// Velocity matrix elements hr[5][dim] (x, y, z, sigma+, sigma-); mixed: the Fourier sums in FP32.
 cudaError_t launch_optics(const zd* hr, const int* rvec, const int* ndegen, int nR, int w,
                           const double* rlat_rm, const double* kpt, int nk, int nv, int nc,
-                          const double* eig_win, const zd* vec_win, double cshift, zd* hout, cudaStream_t s);
+                          const double* eig_win, const zd* vec_win, double cshift, zd* hout, cudaStream_t s, bool mixed = false);
 // V(k,k') table, double, leading dimension ldv (>= nk), zero padding left as is.
 cudaError_t launch_coulomb(const CoulParams& p, const double* kpt1, int n1, const double* kpt2, int n2,
                            double* V, int ldv, cudaStream_t s);
