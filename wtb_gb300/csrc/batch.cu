@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -173,7 +174,12 @@ T* upload(Workspace& ws, const char* name, const std::vector<T>& h, cudaStream_t
 }
 
 // Builds the batch graph (set-up branches, joint eigensolve, oscillator branches) for the staged systems.
-int build_graph(wtb_batch* b, int nsys, const wtb_bse_params* p, std::string* msg) {
+// eager (WTB_SOLVER_STREAM, for kernel profilers, which do not see kernels inside conditional graph bodies):
+// no graph; the joint eigensolve runs with the host driving its loop and the oscillator kernels follow it,
+// results into *E, *stats, *sst.
+int build_graph(wtb_batch* b, int nsys, const wtb_bse_params* p, std::string* msg, bool eager = false,
+                std::vector<double>* E = nullptr, std::vector<SolveStats>* stats = nullptr,
+                std::vector<int>* sst = nullptr) {
   wtb_ctx* mc = b->main;
   cudaError_t err = cudaSuccess;
   const bool x6 = p[0].precision == WTB_PREC_BF16X6;
@@ -272,7 +278,7 @@ int build_graph(wtb_batch* b, int nsys, const wtb_bse_params* p, std::string* ms
     s.dE = mf->dE;
     s.zt = mf->Zs;
     s.Tm = reinterpret_cast<const float*>(mf->Tm);
-    for (int k = 0; k < s.nk; k += 8) gtiles.push_back(make_int2(q, k));
+    for (int k = 0; k < s.nk; k += 16) gtiles.push_back(make_int2(q, k));  // refined below to the tile size
     for (int k = 0; k < s.nk; ++k) kpts.push_back(make_int2(q, k));
     gd[q].A = mf->Vs;
     gd[q].B = mf->Zs;
@@ -287,6 +293,11 @@ int build_graph(wtb_batch* b, int nsys, const wtb_bse_params* p, std::string* ms
     max_nc = std::max(max_nc, s.nc);
     max_w = std::max(max_w, s.w);
   }
+  // gather tiles of the tile size the launcher picks for this batch's widest system
+  const int gkt = mf_gather_batch_tile(max_nv, max_nc, max_w, nbmax);
+  gtiles.clear();
+  for (int q = 0; q < nsys; ++q)
+    for (int k = 0; k < ms[q].nk; k += gkt) gtiles.push_back(make_int2(q, k));
   auto op = std::make_unique<BatchMatFreeOperator>();
   op->nsys = nsys;
   op->nbmax = nbmax;
@@ -334,6 +345,18 @@ int build_graph(wtb_batch* b, int nsys, const wtb_bse_params* p, std::string* ms
   if (gp[1] && gp[1] != op->gemm) tc_gemm_group_destroy(gp[1]);
   if (!op->gemm || cudaStreamSynchronize(mc->s) != cudaSuccess) return ctx_set_err(mc, WTB_ECUDA, "batch: " + m2);
 
+  if (eager) {
+    b->op = std::move(op);
+    int r = lobpcg_solve_batch<float>(*b->op, diag, L, nevmax, b->m, b->tol, b->maxit, ws, mc->st, mc->s, E, Xout,
+                                      stats, sst, msg, b->tol_refine, nullptr);
+    if (cudaStreamSynchronize(mc->s) != cudaSuccess) r = ctx_set_err(mc, WTB_ECUDA, "batch: eigensolve failed");
+    for (int q = 0; q < nsys && r != WTB_ECUDA; ++q) {
+      wtb_ctx* c = b->slots[q];
+      const int rb = enqueue_back(c, Xout + (size_t)b->row0[q] * nevmax, nevmax, b->dims[q], osc + (size_t)q * 8 * nevmax);
+      if (rb != WTB_OK || cudaStreamSynchronize(c->s) != cudaSuccess) r = ctx_set_err(mc, WTB_ECUDA, "batch: oscillators");
+    }
+    return r;
+  }
   // the graph: set-up branches, joint eigensolve after all of them, oscillator branches after it
   cudaGraph_t G = nullptr;
   if (cudaGraphCreate(&G, 0) != cudaSuccess) return ctx_set_err(mc, WTB_ECUDA, "batch: graph creation failed");
@@ -506,6 +529,24 @@ extern "C" int wtb_batch_bsesolver(wtb_batch* b, int nsys, const wtb_system* sys
   key = fnv(key, &b->main->ws.generation, sizeof(uint64_t));
   if (key == 0) key = 1;
   std::string msg;
+  wtb_ctx* mc = b->main;
+  std::vector<double> Eall;
+  std::vector<SolveStats> stats;
+  std::vector<int> sst;
+  int rc = WTB_OK;
+  const bool eager = std::getenv("WTB_SOLVER_STREAM") != nullptr;
+  if (eager) {
+    b->drop_graph();
+    rc = build_graph(b, nsys, p, &msg, true, &Eall, &stats, &sst);
+    if (!b->op) {
+      for (int q = 0; q < nsys; ++q) {
+        status[q] = rc;
+        if (b->errors[q].empty()) b->errors[q] = msg;
+      }
+      return finish(rc);
+    }
+    b->t_build = b->t_run = ms_since(t1);
+  } else {
   if (!(b->exec && b->key == key)) {
     b->drop_graph();
     const int r = build_graph(b, nsys, p, &msg);
@@ -532,7 +573,6 @@ extern "C" int wtb_batch_bsesolver(wtb_batch* b, int nsys, const wtb_system* sys
     k2 = fnv(k2, &b->main->ws.generation, sizeof(uint64_t));
     b->key = k2 == 0 ? 1 : k2;
   }
-  wtb_ctx* mc = b->main;
   b->t_build = ms_since(t1);
   const auto t2 = std::chrono::steady_clock::now();
   g_launch_count += b->graph_launches;
@@ -555,19 +595,19 @@ extern "C" int wtb_batch_bsesolver(wtb_batch* b, int nsys, const wtb_system* sys
     b->t_solve = c2;
     b->t_back = d;
   }
-  const auto t3 = std::chrono::steady_clock::now();
-  // results: joint eigensolve, set-up status of every system, oscillator strengths
-  std::vector<double> Eall;
-  std::vector<SolveStats> stats;
-  std::vector<int> sst;
+  // results: joint eigensolve
   SolveGraph sgc = b->sg;
   sgc.build = false;
   sgc.collect = true;
+  cudaError_t err0 = cudaSuccess;
+  zd* Xout = mc->ws.get<zd>("b_Xout", (size_t)b->L.nrow * b->nev, &err0);
+  double* diag = mc->ws.get<double>("b_diag", b->L.nrow, &err0);
+  rc = lobpcg_solve_batch<float>(*b->op, diag, b->L, b->nev, b->m, b->tol, b->maxit, mc->ws, mc->st, mc->s, &Eall,
+                                 Xout, &stats, &sst, &msg, b->tol_refine, &sgc);
+  }
+  const auto t3 = std::chrono::steady_clock::now();
+  // set-up status of every system, oscillator strengths
   cudaError_t err = cudaSuccess;
-  zd* Xout = mc->ws.get<zd>("b_Xout", (size_t)b->L.nrow * b->nev, &err);
-  double* diag = mc->ws.get<double>("b_diag", b->L.nrow, &err);
-  const int rc = lobpcg_solve_batch<float>(*b->op, diag, b->L, b->nev, b->m, b->tol, b->maxit, mc->ws, mc->st, mc->s,
-                                           &Eall, Xout, &stats, &sst, &msg, b->tol_refine, &sgc);
   std::vector<double> osc((size_t)nsys * 8 * b->nev, 0.0);
   double* dosc = mc->ws.get<double>("b_osc", osc.size(), &err);
   if (err != cudaSuccess || cudaMemcpy(osc.data(), dosc, sizeof(double) * osc.size(), cudaMemcpyDeviceToHost) != cudaSuccess) {

@@ -193,8 +193,11 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
 }
 
 // ----------------------------------------------------------------------------- optics (hlm + optsp)
+// T = double: FP64 throughout (hr_t = hr).  T = float: the Fourier sums in FP32 over an FP32 copy hr_t of H(R),
+// with the per-R factors i R_a e^{i phi}/ndegen formed once per direction (FP64, then rounded).
 template <class T>
-__global__ void __launch_bounds__(kHkThreads) optics_kernel(const zd* __restrict__ hr, const int* __restrict__ rvec,
+__global__ void __launch_bounds__(kHkThreads) optics_kernel(const cplx<T>* __restrict__ hr_t,
+                                                            const int* __restrict__ rvec,
                                                             const int* __restrict__ ndegen, int nR, int w,
                                                             const double* __restrict__ rlat,
                                                             const double* __restrict__ kpt, int nk, int nv, int nc,
@@ -210,7 +213,8 @@ __global__ void __launch_bounds__(kHkThreads) optics_kernel(const zd* __restrict
   zd* B = M + w * w;                         // nb*w band vectors
   zd* Mv = B + nb * w;                       // nv*w
   zd* eph = Mv + nv * w;                     // nR
-  double* Ra = reinterpret_cast<double*>(eph + nR);  // nR
+  cplx<T>* fr = reinterpret_cast<cplx<T>*>(eph + nR);  // nR (16-byte aligned after the complex(8) arrays)
+  double* Ra = reinterpret_cast<double*>(fr + nR);     // nR
   __shared__ double rl[9];
   if (tid < 9) rl[tid] = rlat[tid];
   for (int e = tid; e < nb * w; e += blockDim.x) B[e] = vec_win[(size_t)k * nb * w + e];
@@ -229,20 +233,18 @@ __global__ void __launch_bounds__(kHkThreads) optics_kernel(const zd* __restrict
   (void)hxyz;
   for (int a = 0; a < 3; ++a) {
     __syncthreads();
-    for (int r = tid; r < nR; r += blockDim.x) Ra[r] = rcomp_f32(rvec, nR, r, rl, a);
+    for (int r = tid; r < nR; r += blockDim.x) {
+      Ra[r] = rcomp_f32(rvec, nR, r, rl, a);
+      fr[r] = mk<T>((T)(-Ra[r] * eph[r].im), (T)(Ra[r] * eph[r].re));  // i R_a e
+    }
     __syncthreads();
-    // M = sum_R i R_a e^{i phi} H(R)/ndegen (the R = 0 term vanishes with R_a = 0, its diagonal is skipped as
-    // in hlm), in arithmetic T: FP32 for the tensor-core forms, whose oscillator strengths need 1e-4
+    // M = sum_R i R_a e^{i phi} H(R)/ndegen, in arithmetic T (FP32 for the tensor-core forms, whose oscillator
+    // strengths need 1e-4).  hlm skips the diagonal of the R = 0 term, whose factor R_a = 0 makes it vanish
+    // exactly here as well.
     for (int e = tid; e < w * w; e += blockDim.x) {
       const int m = e / w, c = e % w;
       cplx<T> acc = mk<T>(0, 0);
-      for (int r = 0; r < nR; ++r) {
-        const bool r0 = rvec[r] == 0 && rvec[nR + r] == 0 && rvec[2 * nR + r] == 0;
-        if (r0 && m == c) continue;
-        const cplx<T> f = mk<T>((T)(-Ra[r] * eph[r].im), (T)(Ra[r] * eph[r].re));  // i R_a e
-        const zd h = hr[((size_t)r * w + m) * w + c];
-        cfma(acc, f, mk<T>((T)h.re, (T)h.im));
-      }
+      for (int r = 0; r < nR; ++r) cfma(acc, fr[r], hr_t[((size_t)r * w + m) * w + c]);
       M[e] = mk<double>((double)acc.re, (double)acc.im);
     }
     __syncthreads();
@@ -476,14 +478,15 @@ cudaError_t launch_hk_eig(const zd* hr, const int* rvec, const int* ndegen, int 
 
 cudaError_t launch_optics(const zd* hr, const int* rvec, const int* ndegen, int nR, int w, const double* rlat_rm,
                           const double* kpt, int nk, int nv, int nc, const double* eig_win, const zd* vec_win,
-                          double cshift, zd* hout, cudaStream_t s, bool mixed) {
+                          double cshift, zd* hout, cudaStream_t s, const zf* hr32) {
   const int nb = nv + nc;
-  const size_t smem = (size_t)(w * w + nb * w + nv * w + nR) * sizeof(zd) + nR * sizeof(double) + 16;
+  const size_t smem = (size_t)(w * w + nb * w + nv * w + nR) * sizeof(zd) + nR * sizeof(double) + nR * sizeof(zd) + 16;
+  const bool mixed = hr32 != nullptr;
   const void* fn = mixed ? reinterpret_cast<const void*>(optics_kernel<float>) : reinterpret_cast<const void*>(optics_kernel<double>);
   cudaError_t e = raise_smem_limit(fn, (size_t)smem);
   if (e != cudaSuccess) return e;
   if (mixed)
-    optics_kernel<float><<<nk, kHkThreads, smem, s>>>(hr, rvec, ndegen, nR, w, rlat_rm, kpt, nk, nv, nc, eig_win,
+    optics_kernel<float><<<nk, kHkThreads, smem, s>>>(hr32, rvec, ndegen, nR, w, rlat_rm, kpt, nk, nv, nc, eig_win,
                                                       vec_win, (float)cshift, hout);
   else
     optics_kernel<double><<<nk, kHkThreads, smem, s>>>(hr, rvec, ndegen, nR, w, rlat_rm, kpt, nk, nv, nc, eig_win,

@@ -104,24 +104,24 @@ __global__ void __launch_bounds__(256) mf_gather_kernel(const cplx<S>* __restric
   }
 }
 
-// bf16-slice variant: one CTA per tile of 8 consecutive k' and all nb block columns.  The X rows of the tile
-// (nb contiguous columns each) and the tile's band vectors are read once; Y1 = Vb x is staged in shared
-// memory; each thread then forms Z[k'][o][p][b] for its (b, o, p) items over the 8 k' of the tile and writes
-// the re and im rows of every slice as one 16-byte vector of 8 bf16 (the K-major rows of zt are 16-byte
-// aligned: ldk and the tile start are multiples of 8).  k' >= nk inside the last tile give zeros (x = 0).
-constexpr int kGatherKT = 8;
-__device__ __forceinline__ void gather_bf16_tile(const zf* __restrict__ X, int ldx, int c0, int nbc,
+// bf16-slice variant: one CTA per tile of KT consecutive k' (8 or 16) and all nb block columns, the columns in
+// passes of nbp.  The tile's band vectors are read once; per pass the X rows of the tile are staged, Y1 = Vb x
+// is formed in shared memory, and each thread then forms Z[k'][o][p][b] for its (b, o, p) items over the KT k'
+// of the tile and writes the re and im rows of every slice as KT/8 16-byte vectors of 8 bf16 (with KT = 16 a
+// row segment is a whole 32-byte sector; the K-major rows of zt are 16-byte aligned: ldk and the tile start
+// are multiples of KT).  k' >= nk inside the last tile give zeros (x = 0).
+template <int KT>
+__device__ __forceinline__ void gather_bf16_tile(const zf* __restrict__ X, int ldx, int c0, int nbc, int nbp,
                                                  const zd* __restrict__ vec_win, int nk, int nv, int nc, int w,
                                                  uint16_t* __restrict__ zt, int ldk, int nslices, long slice_stride,
                                                  int kt0) {
-  constexpr int KT = kGatherKT;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nbnd = nv + nc, ncv = nc * nv, ww = w * w;
   const int tkn = min(KT, nk - kt0);
   zf* Cs = reinterpret_cast<zf*>(smem_raw);  // [KT][nc][w]
   zf* Vs = Cs + KT * nc * w;                 // [KT][nv][w]
-  zf* xs = Vs + KT * nv * w;                 // [KT][ncv][nbc]
-  zf* Y1 = xs + KT * ncv * nbc;              // [KT][nc][w][nbc]
+  zf* xs = Vs + KT * nv * w;                 // [KT][ncv][nbp]
+  zf* Y1 = xs + KT * ncv * nbp;              // [KT][nc][w][nbp]
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int e = tid; e < KT * nbnd * w; e += nt) {
     const int kk = e / (nbnd * w), sb = (e / w) % nbnd, o = e % w;
@@ -133,72 +133,105 @@ __device__ __forceinline__ void gather_bf16_tile(const zf* __restrict__ X, int l
     else
       Cs[(kk * nc + sb - nv) * w + o] = as;
   }
-  for (int e = tid; e < KT * ncv * nbc; e += nt) {
-    const int b = e % nbc, r = e / nbc;  // r = kk * ncv + cv
-    const int kk = r / ncv;
-    xs[e] = kk < tkn ? X[((size_t)kt0 * ncv + r) * ldx + c0 + b] : mk<float>(0.f, 0.f);
-  }
-  __syncthreads();
-  // Y1[kk][c][p][b] = sum_v Vb[kk][v][p] x[kk][c][v][b]
-  for (int e = tid; e < KT * nc * w * nbc; e += nt) {
-    const int b = e % nbc, p = (e / nbc) % w, c = (e / (nbc * w)) % nc, kk = e / (nbc * w * nc);
-    zf acc = mk<float>(0.f, 0.f);
-    for (int v = 0; v < nv; ++v) cfma(acc, Vs[(kk * nv + v) * w + p], xs[(kk * ncv + c * nv + v) * nbc + b]);
-    Y1[e] = acc;
-  }
-  __syncthreads();
-  // items (b, o, p), b fastest across lanes (Y1 reads are then consecutive in shared memory): Z over the
-  // tile's 8 k', re and im rows, every slice
-  for (int it = tid; it < nbc * ww; it += nt) {
-    const int b = it % nbc, op = it / nbc, o = op / w, p = op % w;
-    float zr[KT], zi[KT];
-#pragma unroll
-    for (int kk = 0; kk < KT; ++kk) {
-      zf acc = mk<float>(0.f, 0.f);
-      for (int c = 0; c < nc; ++c)
-        cfma(acc, Cs[(kk * nc + c) * w + o], Y1[((kk * nc + c) * w + p) * nbc + b]);
-      zr[kk] = acc.re;
-      zi[kk] = acc.im;
+  for (int b0 = 0; b0 < nbc; b0 += nbp) {
+    const int nbl = min(nbp, nbc - b0);
+    __syncthreads();  // the previous pass is done with xs and Y1
+    for (int e = tid; e < KT * ncv * nbl; e += nt) {
+      const int bb = e % nbl, r = e / nbl;  // r = kk * ncv + cv
+      const int kk = r / ncv;
+      xs[r * nbp + bb] = kk < tkn ? X[((size_t)kt0 * ncv + r) * ldx + c0 + b0 + bb] : mk<float>(0.f, 0.f);
     }
-    const long row = ((long)(b * w + o) * w + p) * 2;
-    const long off_re = row * ldk + kt0, off_im = off_re + ldk;
-    for (int sl = 0; sl < nslices; ++sl) {
-      uint32_t pr[4], pi[4];
+    __syncthreads();
+    // Y1[kk][c][p][bb] = sum_v Vb[kk][v][p] x[kk][c][v][bb]
+    for (int e = tid; e < KT * nc * w * nbl; e += nt) {
+      const int bb = e % nbl, q = e / nbl;  // q = (kk * nc + c) * w + p
+      const int p = q % w, c = (q / w) % nc, kk = q / (w * nc);
+      zf acc = mk<float>(0.f, 0.f);
+      for (int v = 0; v < nv; ++v) cfma(acc, Vs[(kk * nv + v) * w + p], xs[(kk * ncv + c * nv + v) * nbp + bb]);
+      Y1[q * nbp + bb] = acc;
+    }
+    __syncthreads();
+    // items (bb, o, p), bb fastest across lanes (Y1 reads are then consecutive in shared memory): Z over the
+    // tile's KT k', re and im rows, every slice
+    for (int it = tid; it < nbl * ww; it += nt) {
+      const int bb = it % nbl, op = it / nbl, o = op / w, p = op % w;
+      float zr[KT], zi[KT];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const __nv_bfloat16 r0 = __float2bfloat16_rn(zr[2 * q]), r1 = __float2bfloat16_rn(zr[2 * q + 1]);
-        const __nv_bfloat16 i0 = __float2bfloat16_rn(zi[2 * q]), i1 = __float2bfloat16_rn(zi[2 * q + 1]);
-        zr[2 * q] -= __bfloat162float(r0);
-        zr[2 * q + 1] -= __bfloat162float(r1);
-        zi[2 * q] -= __bfloat162float(i0);
-        zi[2 * q + 1] -= __bfloat162float(i1);
-        pr[q] = (uint32_t)__bfloat16_as_ushort(r0) | ((uint32_t)__bfloat16_as_ushort(r1) << 16);
-        pi[q] = (uint32_t)__bfloat16_as_ushort(i0) | ((uint32_t)__bfloat16_as_ushort(i1) << 16);
+      for (int kk = 0; kk < KT; ++kk) {
+        zf acc = mk<float>(0.f, 0.f);
+        for (int c = 0; c < nc; ++c)
+          cfma(acc, Cs[(kk * nc + c) * w + o], Y1[((kk * nc + c) * w + p) * nbp + bb]);
+        zr[kk] = acc.re;
+        zi[kk] = acc.im;
       }
-      *reinterpret_cast<uint4*>(zt + sl * slice_stride + off_re) = make_uint4(pr[0], pr[1], pr[2], pr[3]);
-      *reinterpret_cast<uint4*>(zt + sl * slice_stride + off_im) = make_uint4(pi[0], pi[1], pi[2], pi[3]);
+      const long row = ((long)((b0 + bb) * w + o) * w + p) * 2;
+      const long off_re = row * ldk + kt0, off_im = off_re + ldk;
+      for (int sl = 0; sl < nslices; ++sl) {
+#pragma unroll
+        for (int h = 0; h < KT / 8; ++h) {
+          uint32_t pr[4], pi[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int k0 = 8 * h + 2 * q;
+            const __nv_bfloat16 r0 = __float2bfloat16_rn(zr[k0]), r1 = __float2bfloat16_rn(zr[k0 + 1]);
+            const __nv_bfloat16 i0 = __float2bfloat16_rn(zi[k0]), i1 = __float2bfloat16_rn(zi[k0 + 1]);
+            zr[k0] -= __bfloat162float(r0);
+            zr[k0 + 1] -= __bfloat162float(r1);
+            zi[k0] -= __bfloat162float(i0);
+            zi[k0 + 1] -= __bfloat162float(i1);
+            pr[q] = (uint32_t)__bfloat16_as_ushort(r0) | ((uint32_t)__bfloat16_as_ushort(r1) << 16);
+            pi[q] = (uint32_t)__bfloat16_as_ushort(i0) | ((uint32_t)__bfloat16_as_ushort(i1) << 16);
+          }
+          *reinterpret_cast<uint4*>(zt + sl * slice_stride + off_re + 8 * h) = make_uint4(pr[0], pr[1], pr[2], pr[3]);
+          *reinterpret_cast<uint4*>(zt + sl * slice_stride + off_im + 8 * h) = make_uint4(pi[0], pi[1], pi[2], pi[3]);
+        }
+      }
     }
   }
 }
 
+// shared memory of a gather tile: band vectors, then the staged X rows and Y1 of one pass of nbp columns
+inline size_t gather_smem(int KT, int nv, int nc, int w, int nbp) {
+  return (size_t)(KT * nc * w + KT * nv * w + KT * nc * nv * nbp + KT * nc * w * nbp) * sizeof(zf);
+}
+
+// The tile shape of a gather: 16 k' per tile when two CTAs of it fit an SM with the columns in one or two
+// passes, else 8 k' (the column passes as few as fit); *nbp receives the columns per pass.
+inline int gather_tile(int nv, int nc, int w, int nbc, int* nbp) {
+  constexpr size_t kTwoPerSm = 110 * 1024;
+  for (int KT : {16, 8})
+    for (int passes = 1; passes <= 2; ++passes) {
+      const int p = (nbc + passes - 1) / passes;
+      if (gather_smem(KT, nv, nc, w, p) <= kTwoPerSm) {
+        *nbp = p;
+        return KT;
+      }
+    }
+  *nbp = nbc;
+  while (*nbp > 1 && gather_smem(8, nv, nc, w, *nbp) > 200 * 1024) *nbp = (*nbp + 1) / 2;
+  return 8;
+}
+
+template <int KT>
 __global__ void __launch_bounds__(256) mf_gather_bf16_kernel(const zf* __restrict__ X, int ldx, int c0, int nbc,
-                                                             const zd* __restrict__ vec_win, int nk, int nv, int nc,
-                                                             int w, uint16_t* __restrict__ zt, int ldk, int nslices,
-                                                             long slice_stride) {
-  gather_bf16_tile(X, ldx, c0, nbc, vec_win, nk, nv, nc, w, zt, ldk, nslices, slice_stride, blockIdx.x * kGatherKT);
+                                                             int nbp, const zd* __restrict__ vec_win, int nk, int nv,
+                                                             int nc, int w, uint16_t* __restrict__ zt, int ldk,
+                                                             int nslices, long slice_stride) {
+  gather_bf16_tile<KT>(X, ldx, c0, nbc, nbp, vec_win, nk, nv, nc, w, zt, ldk, nslices, slice_stride, blockIdx.x * KT);
 }
 
 // batch: CTA b takes tile tiles[b] = (system, first k-point) of the systems' Z panels; frozen systems are
 // skipped unless all (the final application) are wanted
+template <int KT>
 __global__ void __launch_bounds__(256) mf_gather_bf16_batch_kernel(const zf* __restrict__ X, int ldx, int c0, int nbc,
-                                                                   const MfSys* __restrict__ sys,
+                                                                   int nbp, const MfSys* __restrict__ sys,
                                                                    const int2* __restrict__ tiles, int nslices,
                                                                    const int* __restrict__ frozen) {
   const int2 t = tiles[blockIdx.x];
   if (frozen && frozen[t.x]) return;
   const MfSys& q = sys[t.x];
-  gather_bf16_tile(X + (size_t)q.row0 * ldx, ldx, c0, nbc, q.vec_win, q.nk, q.nv, q.nc, q.w, q.zt, q.ldk, nslices,
-                   q.slice_stride, t.y);
+  gather_bf16_tile<KT>(X + (size_t)q.row0 * ldx, ldx, c0, nbc, nbp, q.vec_win, q.nk, q.nv, q.nc, q.w, q.zt, q.ldk,
+                       nslices, q.slice_stride, t.y);
 }
 
 template <class S, class T>
@@ -359,15 +392,24 @@ template <class S, class Z>
 cudaError_t launch_mf_gather(const cplx<S>* X, int ldx, int c0, int nb, const zd* vec_win, int nk, int nv, int nc,
                              int w, Z* zt, int ldk, int nslices, long slice_stride, cudaStream_t s) {
   if constexpr (sizeof(S) == 4 && sizeof(Z) == 2) {
-    const int KT = kGatherKT;
-    const size_t smem = (size_t)(KT * nc * w + KT * nv * w + KT * nc * nv * nb + KT * nc * w * nb) * sizeof(zf);
+    int nbp = nb;
+    const int KT = gather_tile(nv, nc, w, nb, &nbp);
+    const size_t smem = gather_smem(KT, nv, nc, w, nbp);
     if (smem <= 200 * 1024 && ldk % KT == 0 && slice_stride % 8 == 0) {
-      cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(mf_gather_bf16_kernel), smem);
+      const void* fn = KT == 16 ? reinterpret_cast<const void*>(mf_gather_bf16_kernel<16>)
+                                : reinterpret_cast<const void*>(mf_gather_bf16_kernel<8>);
+      cudaError_t e = raise_smem_limit(fn, smem);
       if (e != cudaSuccess) return e;
-      mf_gather_bf16_kernel<<<(nk + KT - 1) / KT, 256, smem, s>>>(reinterpret_cast<const zf*>(X), ldx, c0, nb,
-                                                                   vec_win, nk, nv, nc, w,
-                                                                   reinterpret_cast<uint16_t*>(zt), ldk, nslices,
-                                                                   slice_stride);
+      if (KT == 16)
+        mf_gather_bf16_kernel<16><<<(nk + 15) / 16, 256, smem, s>>>(reinterpret_cast<const zf*>(X), ldx, c0, nb, nbp,
+                                                                     vec_win, nk, nv, nc, w,
+                                                                     reinterpret_cast<uint16_t*>(zt), ldk, nslices,
+                                                                     slice_stride);
+      else
+        mf_gather_bf16_kernel<8><<<(nk + 7) / 8, 256, smem, s>>>(reinterpret_cast<const zf*>(X), ldx, c0, nb, nbp,
+                                                                  vec_win, nk, nv, nc, w,
+                                                                  reinterpret_cast<uint16_t*>(zt), ldk, nslices,
+                                                                  slice_stride);
       ++g_launch_count;
       return cudaGetLastError();
     }
@@ -400,16 +442,27 @@ cudaError_t launch_mf_scatter(const T* Tm, int ldt, const cplx<S>* X, int ldx, c
   return cudaGetLastError();
 }
 
+int mf_gather_batch_tile(int max_nv, int max_nc, int w, int nb) {
+  int nbp = nb;
+  return gather_tile(max_nv, max_nc, w, nb, &nbp);
+}
+
+// tiles hold (system, first k-point) of tiles of mf_gather_batch_tile() k-points
 cudaError_t launch_mf_gather_batch(const zf* X, int ldx, int c0, int nb, const MfSys* sys, const int2* tiles,
                                    int ntiles, int max_nv, int max_nc, int w, int nslices, const int* frozen,
                                    cudaStream_t s) {
-  const int KT = kGatherKT;
-  const size_t smem =
-      (size_t)(KT * max_nc * w + KT * max_nv * w + KT * max_nc * max_nv * nb + KT * max_nc * w * nb) * sizeof(zf);
+  int nbp = nb;
+  const int KT = gather_tile(max_nv, max_nc, w, nb, &nbp);
+  const size_t smem = gather_smem(KT, max_nv, max_nc, w, nbp);
   if (smem > 200 * 1024) return cudaErrorInvalidValue;
-  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(mf_gather_bf16_batch_kernel), smem);
+  const void* fn = KT == 16 ? reinterpret_cast<const void*>(mf_gather_bf16_batch_kernel<16>)
+                            : reinterpret_cast<const void*>(mf_gather_bf16_batch_kernel<8>);
+  cudaError_t e = raise_smem_limit(fn, smem);
   if (e != cudaSuccess) return e;
-  mf_gather_bf16_batch_kernel<<<ntiles, 256, smem, s>>>(X, ldx, c0, nb, sys, tiles, nslices, frozen);
+  if (KT == 16)
+    mf_gather_bf16_batch_kernel<16><<<ntiles, 256, smem, s>>>(X, ldx, c0, nb, nbp, sys, tiles, nslices, frozen);
+  else
+    mf_gather_bf16_batch_kernel<8><<<ntiles, 256, smem, s>>>(X, ldx, c0, nb, nbp, sys, tiles, nslices, frozen);
   ++g_launch_count;
   return cudaGetLastError();
 }

@@ -430,8 +430,8 @@ __global__ void cond_copy_kernel(const LobCtl* __restrict__ ctl, int which, cons
 
 // In place: X <- [X W P] C and P <- [W P] C[m:3m, :] for the basis and for its image under H.  A CTA stages
 // kUpdRows rows (one row tile) of the block in shared memory (so the in-place writes cannot overtake reads),
-// then threads (row, group of four output columns) form their outputs from the staged row and the C of the
-// tile's system (staged again only when the system changes from one tile to the next).
+// then threads (row, pair of output columns: 256 threads for m = 16) form their outputs from the staged row
+// and the C of the tile's system (staged again only when the system changes from one tile to the next).
 constexpr int kUpdRows = kTileRows;
 template <class S>
 __global__ void __launch_bounds__(256) lob_update_kernel(cplx<S>* __restrict__ Sb, cplx<S>* __restrict__ ASb, int ld,
@@ -441,8 +441,8 @@ __global__ void __launch_bounds__(256) lob_update_kernel(cplx<S>* __restrict__ S
   const int nb = 3 * m;
   cplx<S>* Cs = reinterpret_cast<cplx<S>*>(smem_raw);  // [3m][m]
   cplx<S>* Rs = Cs + nb * m;                           // [kUpdRows][3m]
-  const int ngrp = (m + 3) >> 2;       // groups of 4 output columns
-  const int items = kUpdRows * ngrp;   // (row, group) pairs per pass
+  const int ngrp = (m + 1) >> 1;       // pairs of output columns
+  const int items = kUpdRows * ngrp;   // (row, pair) items per pass
   int staged = -1;
   for (long r0 = (long)blockIdx.x * kUpdRows; r0 < nrow; r0 += (long)gridDim.x * kUpdRows) {
     const int sys = bm_sys_of_row(bm, r0);  // uniform over the CTA
@@ -465,29 +465,29 @@ __global__ void __launch_bounds__(256) lob_update_kernel(cplx<S>* __restrict__ S
       for (int it = threadIdx.x; it < items; it += blockDim.x) {
         const int rr = it / ngrp, g = it - rr * ngrp;
         if (rr >= nr) continue;
-        const int j0 = g * 4;
-        cplx<S> x[4], pn[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) x[q] = pn[q] = mk<S>(0, 0);
+        const int j0 = g * 2;
+        const bool two = j0 + 1 < m;
+        cplx<S> x0 = mk<S>(0, 0), x1 = mk<S>(0, 0), p0 = mk<S>(0, 0), p1 = mk<S>(0, 0);
         const cplx<S>* row = Rs + rr * nb;
-        for (int i = 0; i < nb; ++i) {
+        for (int i = 0; i < m; ++i) {  // the X block contributes to X only
           const cplx<S> ri = row[i];
           const cplx<S>* crow = Cs + i * m + j0;
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            if (j0 + q < m) {
-              cfma(x[q], ri, crow[q]);
-              if (i >= m) cfma(pn[q], ri, crow[q]);
-            }
-          }
+          cfma(x0, ri, crow[0]);
+          if (two) cfma(x1, ri, crow[1]);
+        }
+        for (int i = m; i < nb; ++i) {  // W and P contribute to X and to the new P
+          const cplx<S> ri = row[i];
+          const cplx<S>* crow = Cs + i * m + j0;
+          cfma(p0, ri, crow[0]);
+          if (two) cfma(p1, ri, crow[1]);
         }
         cplx<S>* out = base + (size_t)rr * ld;
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-          if (j0 + q < m) {
-            out[j0 + q] = x[q];
-            out[2 * m + j0 + q] = pn[q];
-          }
+        out[j0] = mk<S>(x0.re + p0.re, x0.im + p0.im);
+        out[2 * m + j0] = p0;
+        if (two) {
+          out[j0 + 1] = mk<S>(x1.re + p1.re, x1.im + p1.im);
+          out[2 * m + j0 + 1] = p1;
+        }
       }
     }
   }

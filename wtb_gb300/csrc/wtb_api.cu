@@ -712,10 +712,18 @@ static int compute_optics(wtb_ctx* c, const wtb_bse_params* p) {
   const int dim = c->nk * c->nc * c->nv;
   zd* hout = c->ws.get<zd>("hrvel", (size_t)5 * dim, &err);
   CKC(err);
+  // the tensor-core forms: Fourier sums in FP32 over an FP32 copy of H(R)
+  zf* hr32 = nullptr;
+  if (tc_form(p)) {
+    const size_t nh = (size_t)c->nR * c->w * c->w;
+    hr32 = c->ws.get<zf>("hr32", nh, &err);
+    CKC(err);
+    CKC((launch_convert_cols<double, float>(c->ws.get<zd>("hr", 0, &err), 1, hr32, 1, 1, (int)nh, c->s)));
+  }
   CKC(launch_optics(c->ws.get<zd>("hr", 0, &err), c->ws.get<int>("rvec", 0, &err), c->ws.get<int>("ndegen", 0, &err),
                     c->nR, c->w, c->ws.get<double>("rlat", 0, &err), c->ws.get<double>("kpt", 0, &err), c->nk, c->nv,
                     c->nc, c->ws.get<double>("eig_win", 0, &err), c->ws.get<zd>("vec_win", 0, &err), p->cshift, hout,
-                    c->s, tc_form(p)));
+                    c->s, hr32));
   c->have_hr_optics = true;
   c->have_solve = false;  // hrvel now follows p->cshift; wtb_bsesolver sets it again after its solve
   return WTB_OK;

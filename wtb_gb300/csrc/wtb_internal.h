@@ -98,10 +98,12 @@ cudaError_t launch_hk_eig(const zd* hr, const int* rvec, const int* ndegen, int 
                           const double* rlat_rm, double efermi, double scs, const double* kpt, int nk,
                           int nv, int nc, double* eig_all, zd* vec_all, double* eig_win, zd* vec_win,
                           int* nocp, DevStatus* st, cudaStream_t s, bool mixed = false);
-// Velocity matrix elements hr[5][dim] (x, y, z, sigma+, sigma-); mixed: the Fourier sums in FP32.
+// Velocity matrix elements hr[5][dim] (x, y, z, sigma+, sigma-); with hr32 (an FP32 copy of H(R)) the Fourier
+// sums run in FP32.
 cudaError_t launch_optics(const zd* hr, const int* rvec, const int* ndegen, int nR, int w,
                           const double* rlat_rm, const double* kpt, int nk, int nv, int nc,
-                          const double* eig_win, const zd* vec_win, double cshift, zd* hout, cudaStream_t s, bool mixed = false);
+                          const double* eig_win, const zd* vec_win, double cshift, zd* hout, cudaStream_t s,
+                          const zf* hr32 = nullptr);
 // V(k,k') table, double, leading dimension ldv (>= nk), zero padding left as is.
 cudaError_t launch_coulomb(const CoulParams& p, const double* kpt1, int n1, const double* kpt2, int n2,
                            double* V, int ldv, cudaStream_t s);
@@ -210,7 +212,9 @@ struct MfSys {
   uint16_t* zt;
   const float* Tm;
 };
-// gather over tiles (system, first k-point of 8), scatter over k-points (system, k)
+// gather over tiles (system, first k-point of a tile of mf_gather_batch_tile() k-points), scatter over k-points
+// (system, k)
+int mf_gather_batch_tile(int max_nv, int max_nc, int w, int nb);
 cudaError_t launch_mf_gather_batch(const zf* X, int ldx, int c0, int nb, const MfSys* sys, const int2* tiles,
                                    int ntiles, int max_nv, int max_nc, int w, int nslices, const int* frozen,
                                    cudaStream_t s);
