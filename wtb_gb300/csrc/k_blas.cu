@@ -320,13 +320,27 @@ __global__ void __launch_bounds__(256) select_lowest_kernel(const double* __rest
   select_m_smallest(val, ids, r0, r1, m, out_val + blockIdx.x * m, out_idx + blockIdx.x * m);
 }
 
-// one CTA per system: indices relative to the system's first row, at out_idx + idx_stride q
+// batch, first level: CTA (g, q) takes the m smallest of slice g of system q's rows (indices relative to the
+// system's first row) into cand_val/cand_idx [q][g][m]
 __global__ void __launch_bounds__(256) select_lowest_batch_kernel(const double* __restrict__ diag, BatchMap bm, int m,
                                                                   double* __restrict__ cand_val,
-                                                                  int* __restrict__ out_idx, long idx_stride) {
-  const int q = blockIdx.x;
+                                                                  int* __restrict__ cand_idx) {
+  const int q = blockIdx.y, g = blockIdx.x, ng = gridDim.x;
   const int2 rw = bm.rows[q];
-  select_m_smallest(diag + rw.x, nullptr, 0, rw.y, m, cand_val + (size_t)q * m, out_idx + (size_t)q * idx_stride);
+  const int per = (rw.y + ng - 1) / ng;
+  const int r0 = min(rw.y, g * per), r1 = min(rw.y, r0 + per);
+  const size_t o = ((size_t)q * ng + g) * m;
+  select_m_smallest(diag + rw.x, nullptr, r0, r1, m, cand_val + o, cand_idx + o);
+}
+
+// batch, second level: one CTA per system over its ng * m candidates, into out_idx + idx_stride q
+__global__ void __launch_bounds__(256) select_lowest_batch2_kernel(const double* __restrict__ cand_val,
+                                                                   const int* __restrict__ cand_idx, int ng, int m,
+                                                                   double* __restrict__ out_val,
+                                                                   int* __restrict__ out_idx, long idx_stride) {
+  const int q = blockIdx.x;
+  const size_t o = (size_t)q * ng * m;
+  select_m_smallest(cand_val + o, cand_idx + o, 0, ng * m, m, out_val + (size_t)q * m, out_idx + (size_t)q * idx_stride);
 }
 
 // rows of every system (nrow in all); the noise depends on the row within its system, so a system gets the
@@ -670,11 +684,16 @@ cudaError_t launch_select_lowest(const double* diag, int dim, int m, int* idx, d
   return cudaGetLastError();
 }
 
-// batch: the m lowest rows of every system, relative indices at idx + idx_stride q (cand_val: nsys * m)
+// batch: the m lowest rows of every system, relative indices at idx + idx_stride q; cand_val and cand_idx hold
+// kSelSlices * m candidates per system, cand_val m more
 cudaError_t launch_select_lowest_batch(const double* diag, const BatchMap& bm, int m, int* idx, long idx_stride,
-                                       double* cand_val, cudaStream_t s) {
+                                       double* cand_val, int* cand_idx, cudaStream_t s) {
   if (m > 128 || !bm.rows) return cudaErrorInvalidValue;
-  select_lowest_batch_kernel<<<bm.nsys, 256, 0, s>>>(diag, bm, m, cand_val, idx, idx_stride); ++g_launch_count;
+  select_lowest_batch_kernel<<<dim3(kSelSlices, bm.nsys), 256, 0, s>>>(diag, bm, m, cand_val, cand_idx);
+  ++g_launch_count;
+  select_lowest_batch2_kernel<<<bm.nsys, 256, 0, s>>>(cand_val, cand_idx, kSelSlices, m,
+                                                       cand_val + (size_t)bm.nsys * kSelSlices * m, idx, idx_stride);
+  ++g_launch_count;
   return cudaGetLastError();
 }
 

@@ -258,7 +258,18 @@ __device__ __forceinline__ void scatter_k(const T* __restrict__ Tm, int ldt, con
   }
   const int row = nbl * w * w * 2;
   const T* trow = Tm + (size_t)k * ldt + (size_t)b0 * w * w * 2;
-  for (int e = tid; e < row; e += nt) Ts[e] = trow[e];
+  if constexpr (sizeof(T) == 4) {
+    // 16-byte loads when the row segment allows (row starts and lengths are multiples of 4 floats)
+    if (((reinterpret_cast<uintptr_t>(trow) | reinterpret_cast<uintptr_t>(Ts)) & 15) == 0 && (row & 3) == 0) {
+      const float4* t4 = reinterpret_cast<const float4*>(trow);
+      float4* s4 = reinterpret_cast<float4*>(Ts);
+      for (int e = tid; e < row / 4; e += nt) s4[e] = t4[e];
+    } else {
+      for (int e = tid; e < row; e += nt) Ts[e] = trow[e];
+    }
+  } else {
+    for (int e = tid; e < row; e += nt) Ts[e] = trow[e];
+  }
   __syncthreads();
   // U[b][o][v] = sum_p conj(Vb[v][p]) T[b][o][p]
   for (int e = tid; e < nbl * w * nv; e += nt) {

@@ -563,7 +563,8 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
   double* norms2 = ws.get<double>("lob_norms2", (size_t)nsys * 32, &err);
   int* active = ws.get<int>("lob_active", (size_t)nsys * 32, &err);
   int* idx = ws.get<int>("lob_idx", ragged ? (size_t)nsys * m : 65 * 128, &err);
-  double* cand = ws.get<double>("lob_cand", ragged ? (size_t)nsys * m : 65 * 128, &err);
+  double* cand = ws.get<double>("lob_cand", ragged ? (size_t)nsys * (kSelSlices + 1) * m : 65 * 128, &err);
+  int* cand_idx = ws.get<int>("lob_cand_idx", ragged ? (size_t)nsys * kSelSlices * m : 1, &err);
   double* th_dev = ws.get<double>("lob_thcur", (size_t)nsys * nb, &err);
   LobCtl* ctl = ws.get<LobCtl>("lob_ctl", nsys, &err);
   int* frozen = ws.get<int>("lob_frozen", nsys, &err);
@@ -648,7 +649,7 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
     CK(cudaMemset2DAsync(Sb, sizeof(cplx<S>) * ld, 0, sizeof(cplx<S>) * ld, nrow, s));
     CK(cudaMemset2DAsync(ASb, sizeof(cplx<S>) * ld, 0, sizeof(cplx<S>) * ld, nrow, s));
     if (ragged) {
-      CK(launch_select_lowest_batch(diag, bmf, m, idx, m, cand, s));
+      CK(launch_select_lowest_batch(diag, bmf, m, idx, m, cand, cand_idx, s));
       CK(launch_init_guess<S>(X, ld, nrow, m, idx, 12345u, s, bmf, m));
     } else {
       CK(launch_select_lowest(diag, nrow, m, idx, cand, s));
@@ -732,6 +733,7 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
                                (uint64_t)(uintptr_t)sm.C, (uint64_t)(uintptr_t)sm.T, (uint64_t)(uintptr_t)sm.theta,
                                (uint64_t)(uintptr_t)sm.keep, (uint64_t)(uintptr_t)partial, (uint64_t)(uintptr_t)norms2,
                                (uint64_t)(uintptr_t)active, (uint64_t)(uintptr_t)idx, (uint64_t)(uintptr_t)cand,
+                               (uint64_t)(uintptr_t)cand_idx,
                                (uint64_t)(uintptr_t)th_dev, (uint64_t)(uintptr_t)ctl, (uint64_t)(uintptr_t)frozen,
                                (uint64_t)(uintptr_t)counter, (uint64_t)(uintptr_t)X64, (uint64_t)(uintptr_t)T64,
                                (uint64_t)monitor};

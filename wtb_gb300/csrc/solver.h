@@ -289,7 +289,7 @@ cudaError_t launch_pchol_basis(const zd* M, int ldm, int n, double drop, zd* B, 
                                const BatchMap& bm = BatchMap(), long m_stride = 0, long b_stride = 0);
 cudaError_t launch_select_lowest(const double* diag, int dim, int m, int* idx, double* cand_val, cudaStream_t s);
 cudaError_t launch_select_lowest_batch(const double* diag, const BatchMap& bm, int m, int* idx, long idx_stride,
-                                       double* cand_val, cudaStream_t s);
+                                       double* cand_val, int* cand_idx, cudaStream_t s);
 template <class S>
 cudaError_t launch_init_guess(cplx<S>* X, int ldx, int nrow, int m, const int* idx, unsigned seed, cudaStream_t s,
                               const BatchMap& bm = BatchMap(), long idx_stride = 0);

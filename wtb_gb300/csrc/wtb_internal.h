@@ -131,6 +131,7 @@ cudaError_t launch_dense_mv(const cplx<S>* H, int dim, const cplx<S>* X, int ldx
 // kernels then leave its rows and small matrices alone.  The default map is one system whose parts are
 // npart equal row ranges.  Small per-system matrices sit at a fixed stride from system to system.
 constexpr int kTileRows = 32;
+constexpr int kSelSlices = 8;  // first-level slices per system of the batched start-vector selection
 struct BatchMap {
   int nsys = 1;
   int nparts = 0;
