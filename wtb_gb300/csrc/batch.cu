@@ -184,7 +184,7 @@ int build_graph(wtb_batch* b, int nsys, const wtb_bse_params* p, std::string* ms
   cudaError_t err = cudaSuccess;
   const bool x6 = p[0].precision == WTB_PREC_BF16X6;
   // the concatenated row space: systems padded to whole row tiles, reduction parts of up to kPartRows rows
-  constexpr int kPartRows = 512;
+  constexpr int kPartRows = 256;
   b->row0.assign(nsys, 0);
   b->dims.assign(nsys, 0);
   std::vector<int> tile_sys;

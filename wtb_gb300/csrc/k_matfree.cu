@@ -104,16 +104,17 @@ __global__ void __launch_bounds__(256) mf_gather_kernel(const cplx<S>* __restric
   }
 }
 
-// bf16-slice variant: one CTA per tile of KT consecutive k' (8 or 16) and all nb block columns, the columns in
-// passes of nbp.  The tile's band vectors are read once; per pass the X rows of the tile are staged, Y1 = Vb x
-// is formed in shared memory, and each thread then forms Z[k'][o][p][b] for its (b, o, p) items over the KT k'
-// of the tile and writes the re and im rows of every slice as KT/8 16-byte vectors of 8 bf16 (with KT = 16 a
-// row segment is a whole 32-byte sector; the K-major rows of zt are 16-byte aligned: ldk and the tile start
-// are multiples of KT).  k' >= nk inside the last tile give zeros (x = 0).
+// bf16-slice variant: one CTA per tile of KT consecutive k' (8 or 16) and one chunk of nbp block columns (grid.y:
+// the chunks, so that a panel of a few thousand k' still spreads over many CTAs).  The tile's band vectors and X
+// rows are staged, Y1 = Vb x is formed in shared memory, and each thread then forms Z[k'][o][p][b] for its
+// (b, o, p) items over the KT k' of the tile and writes the re and im rows of every slice as KT/8 16-byte
+// vectors of 8 bf16.  zt is stored in 64-wide K blocks, zt[slice][kb][n][64] (ldn rows per block): the tile's
+// row segments of one block sit side by side, so a warp's stores cover contiguous memory.  k' >= nk inside the
+// last tile give zeros (x = 0).
 template <int KT>
 __device__ __forceinline__ void gather_bf16_tile(const zf* __restrict__ X, int ldx, int c0, int nbc, int nbp,
                                                  const zd* __restrict__ vec_win, int nk, int nv, int nc, int w,
-                                                 uint16_t* __restrict__ zt, int ldk, int nslices, long slice_stride,
+                                                 uint16_t* __restrict__ zt, int ldn, int nslices, long slice_stride,
                                                  int kt0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nbnd = nv + nc, ncv = nc * nv, ww = w * w;
@@ -133,9 +134,10 @@ __device__ __forceinline__ void gather_bf16_tile(const zf* __restrict__ X, int l
     else
       Cs[(kk * nc + sb - nv) * w + o] = as;
   }
-  for (int b0 = 0; b0 < nbc; b0 += nbp) {
+  {
+    const int b0 = blockIdx.y * nbp;
     const int nbl = min(nbp, nbc - b0);
-    __syncthreads();  // the previous pass is done with xs and Y1
+    if (nbl <= 0) return;  // uniform over the CTA
     for (int e = tid; e < KT * ncv * nbl; e += nt) {
       const int bb = e % nbl, r = e / nbl;  // r = kk * ncv + cv
       const int kk = r / ncv;
@@ -165,7 +167,7 @@ __device__ __forceinline__ void gather_bf16_tile(const zf* __restrict__ X, int l
         zi[kk] = acc.im;
       }
       const long row = ((long)((b0 + bb) * w + o) * w + p) * 2;
-      const long off_re = row * ldk + kt0, off_im = off_re + ldk;
+      const long off_re = ((long)(kt0 >> 6) * ldn + row) * 64 + (kt0 & 63), off_im = off_re + 64;
       for (int sl = 0; sl < nslices; ++sl) {
 #pragma unroll
         for (int h = 0; h < KT / 8; ++h) {
@@ -195,29 +197,26 @@ inline size_t gather_smem(int KT, int nv, int nc, int w, int nbp) {
   return (size_t)(KT * nc * w + KT * nv * w + KT * nc * nv * nbp + KT * nc * w * nbp) * sizeof(zf);
 }
 
-// The tile shape of a gather: 16 k' per tile when two CTAs of it fit an SM with the columns in one or two
-// passes, else 8 k' (the column passes as few as fit); *nbp receives the columns per pass.
+// The tile shape of a gather: 16 k' per tile and chunks of (at most) 4 block columns, smaller chunks or 8 k'
+// when the shared memory of a CTA would exceed 56 KB (four CTAs per SM); *nbp receives the columns per chunk.
 inline int gather_tile(int nv, int nc, int w, int nbc, int* nbp) {
-  constexpr size_t kTwoPerSm = 110 * 1024;
+  constexpr size_t kFourPerSm = 56 * 1024;
   for (int KT : {16, 8})
-    for (int passes = 1; passes <= 2; ++passes) {
-      const int p = (nbc + passes - 1) / passes;
-      if (gather_smem(KT, nv, nc, w, p) <= kTwoPerSm) {
+    for (int p = std::min(nbc, 4); p >= 1; --p)
+      if (gather_smem(KT, nv, nc, w, p) <= kFourPerSm) {
         *nbp = p;
         return KT;
       }
-    }
-  *nbp = nbc;
-  while (*nbp > 1 && gather_smem(8, nv, nc, w, *nbp) > 200 * 1024) *nbp = (*nbp + 1) / 2;
+  *nbp = 1;
   return 8;
 }
 
 template <int KT>
 __global__ void __launch_bounds__(256) mf_gather_bf16_kernel(const zf* __restrict__ X, int ldx, int c0, int nbc,
                                                              int nbp, const zd* __restrict__ vec_win, int nk, int nv,
-                                                             int nc, int w, uint16_t* __restrict__ zt, int ldk,
+                                                             int nc, int w, uint16_t* __restrict__ zt, int ldn,
                                                              int nslices, long slice_stride) {
-  gather_bf16_tile<KT>(X, ldx, c0, nbc, nbp, vec_win, nk, nv, nc, w, zt, ldk, nslices, slice_stride, blockIdx.x * KT);
+  gather_bf16_tile<KT>(X, ldx, c0, nbc, nbp, vec_win, nk, nv, nc, w, zt, ldn, nslices, slice_stride, blockIdx.x * KT);
 }
 
 // batch: CTA b takes tile tiles[b] = (system, first k-point) of the systems' Z panels; frozen systems are
@@ -230,8 +229,8 @@ __global__ void __launch_bounds__(256) mf_gather_bf16_batch_kernel(const zf* __r
   const int2 t = tiles[blockIdx.x];
   if (frozen && frozen[t.x]) return;
   const MfSys& q = sys[t.x];
-  gather_bf16_tile<KT>(X + (size_t)q.row0 * ldx, ldx, c0, nbc, nbp, q.vec_win, q.nk, q.nv, q.nc, q.w, q.zt, q.ldk,
-                       nslices, q.slice_stride, t.y);
+  gather_bf16_tile<KT>(X + (size_t)q.row0 * ldx, ldx, c0, nbc, nbp, q.vec_win, q.nk, q.nv, q.nc, q.w, q.zt,
+                       (int)(q.slice_stride / q.ldk), nslices, q.slice_stride, t.y);
 }
 
 template <class S, class T>
@@ -242,10 +241,13 @@ __device__ __forceinline__ void scatter_k(const T* __restrict__ Tm, int ldt, con
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nbl = min(nbg, nb - b0);
   const int nbnd = nv + nc, ncv = nc * nv;
+  // shared rows are padded by one element (U: one complex per column b, Ts: one value per (b, o) row) so that
+  // the strided reads of both products hit distinct banks
+  const int us = w * nv + 1, ts = 2 * w + 1;
   cplx<S>* Cs = reinterpret_cast<cplx<S>*>(smem_raw);  // [nc][w]
   cplx<S>* Vs = Cs + nc * w;                           // [nv][w]
-  cplx<S>* U = Vs + nv * w;                            // [nbg][w][nv]
-  T* Ts = reinterpret_cast<T*>(U + nbg * w * nv);     // [nbg][w][w][2]
+  cplx<S>* U = Vs + nv * w;                            // [nbg][us]: U[b][o][v] at b * us + o * nv + v
+  T* Ts = reinterpret_cast<T*>(U + nbg * us);          // [nbg][w][ts]: T[b][o][p][ri] at (b * w + o) * ts + 2p + ri
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int e = tid; e < nbnd * w; e += nt) {
     const int s = e / w, o = e % w;
@@ -256,28 +258,35 @@ __device__ __forceinline__ void scatter_k(const T* __restrict__ Tm, int ldt, con
     else
       Cs[(s - nv) * w + o] = as;
   }
-  const int row = nbl * w * w * 2;
+  const int row = nbl * w * w * 2, tw = 2 * w;
   const T* trow = Tm + (size_t)k * ldt + (size_t)b0 * w * w * 2;
   if constexpr (sizeof(T) == 4) {
     // 16-byte loads when the row segment allows (row starts and lengths are multiples of 4 floats)
-    if (((reinterpret_cast<uintptr_t>(trow) | reinterpret_cast<uintptr_t>(Ts)) & 15) == 0 && (row & 3) == 0) {
+    if ((reinterpret_cast<uintptr_t>(trow) & 15) == 0 && (row & 3) == 0) {
       const float4* t4 = reinterpret_cast<const float4*>(trow);
-      float4* s4 = reinterpret_cast<float4*>(Ts);
-      for (int e = tid; e < row / 4; e += nt) s4[e] = t4[e];
+      for (int e = tid; e < row / 4; e += nt) {
+        const float4 v4 = t4[e];
+        const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int f = 4 * e + q;
+          Ts[(f / tw) * ts + f % tw] = vv[q];
+        }
+      }
     } else {
-      for (int e = tid; e < row; e += nt) Ts[e] = trow[e];
+      for (int f = tid; f < row; f += nt) Ts[(f / tw) * ts + f % tw] = trow[f];
     }
   } else {
-    for (int e = tid; e < row; e += nt) Ts[e] = trow[e];
+    for (int f = tid; f < row; f += nt) Ts[(f / tw) * ts + f % tw] = trow[f];
   }
   __syncthreads();
   // U[b][o][v] = sum_p conj(Vb[v][p]) T[b][o][p]
   for (int e = tid; e < nbl * w * nv; e += nt) {
     const int bb = e / (w * nv), o = (e / nv) % w, v = e % nv;
     cplx<S> acc = mk<S>(0, 0);
-    const T* tp = Ts + ((size_t)bb * w + o) * w * 2;
+    const T* tp = Ts + ((size_t)bb * w + o) * ts;
     for (int p = 0; p < w; ++p) cfmac(acc, Vs[v * w + p], mk<S>((S)tp[2 * p], (S)tp[2 * p + 1]));
-    U[e] = acc;
+    U[bb * us + o * nv + v] = acc;
   }
   __syncthreads();
   // y[c][v][b] = dE x + sum_o conj(C[c][o]) U[b][o][v]
@@ -285,7 +294,7 @@ __device__ __forceinline__ void scatter_k(const T* __restrict__ Tm, int ldt, con
     const int cv = e / nbl, bb = e % nbl;
     const int c = cv / nv, v = cv % nv;
     cplx<S> acc = mk<S>(0, 0);
-    for (int o = 0; o < w; ++o) cfmac(acc, Cs[c * w + o], U[((size_t)bb * w + o) * nv + v]);
+    for (int o = 0; o < w; ++o) cfmac(acc, Cs[c * w + o], U[bb * us + o * nv + v]);
     const size_t I = (size_t)k * ncv + cv;
     const cplx<S> x = X[I * ldx + c0 + b0 + bb];
     const S d = (S)dE[I];
@@ -406,25 +415,29 @@ cudaError_t launch_mf_gather(const cplx<S>* X, int ldx, int c0, int nb, const zd
     int nbp = nb;
     const int KT = gather_tile(nv, nc, w, nb, &nbp);
     const size_t smem = gather_smem(KT, nv, nc, w, nbp);
-    if (smem <= 200 * 1024 && ldk % KT == 0 && slice_stride % 8 == 0) {
+    // the K-blocked panel: ldk a multiple of 64, ldn = rows per K block
+    const int ldn = (int)(slice_stride / ldk);
+    if (smem <= 200 * 1024 && ldk % 64 == 0 && slice_stride == (long)ldn * ldk) {
       const void* fn = KT == 16 ? reinterpret_cast<const void*>(mf_gather_bf16_kernel<16>)
                                 : reinterpret_cast<const void*>(mf_gather_bf16_kernel<8>);
       cudaError_t e = raise_smem_limit(fn, smem);
       if (e != cudaSuccess) return e;
+      const unsigned nch = (unsigned)((nb + nbp - 1) / nbp);
       if (KT == 16)
-        mf_gather_bf16_kernel<16><<<(nk + 15) / 16, 256, smem, s>>>(reinterpret_cast<const zf*>(X), ldx, c0, nb, nbp,
+        mf_gather_bf16_kernel<16><<<dim3((nk + 15) / 16, nch), 256, smem, s>>>(reinterpret_cast<const zf*>(X), ldx, c0, nb, nbp,
                                                                      vec_win, nk, nv, nc, w,
-                                                                     reinterpret_cast<uint16_t*>(zt), ldk, nslices,
+                                                                     reinterpret_cast<uint16_t*>(zt), ldn, nslices,
                                                                      slice_stride);
       else
-        mf_gather_bf16_kernel<8><<<(nk + 7) / 8, 256, smem, s>>>(reinterpret_cast<const zf*>(X), ldx, c0, nb, nbp,
+        mf_gather_bf16_kernel<8><<<dim3((nk + 7) / 8, nch), 256, smem, s>>>(reinterpret_cast<const zf*>(X), ldx, c0, nb, nbp,
                                                                   vec_win, nk, nv, nc, w,
-                                                                  reinterpret_cast<uint16_t*>(zt), ldk, nslices,
+                                                                  reinterpret_cast<uint16_t*>(zt), ldn, nslices,
                                                                   slice_stride);
       ++g_launch_count;
       return cudaGetLastError();
     }
   }
+  if constexpr (sizeof(Z) == 2) return cudaErrorInvalidValue;  // the bf16 panel exists only in the K-blocked layout
   int KT = 32;
   auto smem_of = [&](int kt) { return (size_t)(2 * kt * nc * w + kt * nv * w + kt * nc * nv) * sizeof(cplx<S>); };
   while (KT > 4 && smem_of(KT) > 160 * 1024) KT /= 2;
@@ -442,7 +455,7 @@ cudaError_t launch_mf_scatter(const T* Tm, int ldt, const cplx<S>* X, int ldx, c
                               int nk, int nv, int nc, int w, int nb, cplx<S>* Y, int ldy, int c0, cudaStream_t s) {
   int nbg = nb;
   auto smem_of = [&](int g) {
-    return (size_t)((nc + nv) * w + g * w * nv) * sizeof(cplx<S>) + (size_t)g * w * w * 2 * sizeof(T) + 16;
+    return (size_t)((nc + nv) * w + g * (w * nv + 1)) * sizeof(cplx<S>) + (size_t)g * w * (2 * w + 1) * sizeof(T) + 16;
   };
   while (nbg > 1 && smem_of(nbg) > 96 * 1024) nbg = (nbg + 1) / 2;
   const size_t smem = smem_of(nbg);
@@ -470,10 +483,11 @@ cudaError_t launch_mf_gather_batch(const zf* X, int ldx, int c0, int nb, const M
                             : reinterpret_cast<const void*>(mf_gather_bf16_batch_kernel<8>);
   cudaError_t e = raise_smem_limit(fn, smem);
   if (e != cudaSuccess) return e;
+  const dim3 grid(ntiles, (nb + nbp - 1) / nbp);
   if (KT == 16)
-    mf_gather_bf16_batch_kernel<16><<<ntiles, 256, smem, s>>>(X, ldx, c0, nb, nbp, sys, tiles, nslices, frozen);
+    mf_gather_bf16_batch_kernel<16><<<grid, 256, smem, s>>>(X, ldx, c0, nb, nbp, sys, tiles, nslices, frozen);
   else
-    mf_gather_bf16_batch_kernel<8><<<ntiles, 256, smem, s>>>(X, ldx, c0, nb, nbp, sys, tiles, nslices, frozen);
+    mf_gather_bf16_batch_kernel<8><<<grid, 256, smem, s>>>(X, ldx, c0, nb, nbp, sys, tiles, nslices, frozen);
   ++g_launch_count;
   return cudaGetLastError();
 }
@@ -483,7 +497,8 @@ cudaError_t launch_mf_scatter_batch(const zf* X, int ldx, const MfSys* sys, cons
                                     cudaStream_t s) {
   int nbg = nb;
   auto smem_of = [&](int g) {
-    return (size_t)((max_nc + max_nv) * w + g * w * max_nv) * sizeof(zf) + (size_t)g * w * w * 2 * sizeof(float) + 16;
+    return (size_t)((max_nc + max_nv) * w + g * (w * max_nv + 1)) * sizeof(zf) + (size_t)g * w * (2 * w + 1) * sizeof(float) +
+           16;
   };
   while (nbg > 1 && smem_of(nbg) > 96 * 1024) nbg = (nbg + 1) / 2;
   const size_t smem = smem_of(nbg);

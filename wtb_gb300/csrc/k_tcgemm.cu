@@ -109,6 +109,18 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
       : "memory");
 }
 
+// B operand: the Z panel is stored in 64-wide K blocks, zt[slice][kb][n][64], so that the rows of one K block
+// are adjacent in memory (the gather writes them side by side); the 4-D box {64, rows, 1, 1} lands in shared
+// memory exactly as a K-major 64 x rows tile of a plain [n][K] panel would.
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2,
+                                            int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // UMMA shared-memory descriptor: K-major, 128-byte swizzle, 8-row core groups 1024 bytes apart.
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   uint64_t d = 0;
@@ -206,7 +218,7 @@ __device__ __forceinline__ void tc_gemm_tile(const CUtensorMap* mapA_p, const CU
         uint8_t* sb = sa + A_BYTES;
         mbar_expect_tx(&full[s], STAGE_BYTES);
         tma_load_3d(sa, &mapA, &full[s], kb * BK, m0, args.pa[pair]);
-        tma_load_3d(sb, &mapB, &full[s], kb * BK, n0, args.pb[pair]);
+        tma_load_4d(sb, &mapB, &full[s], 0, n0, kb, args.pb[pair]);
         *issued = it + 1;
       }
     }
@@ -355,6 +367,28 @@ PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
   return fn;
 }
 
+// B: [slices][K / 64][rows][64] bf16 (K-blocked panel)
+bool make_map_kblocked(CUtensorMap* map, const uint16_t* ptr, int K, int rows, int slices, int box_rows,
+                       std::string* msg) {
+  auto enc = get_encode();
+  if (!enc) {
+    *msg = "cuTensorMapEncodeTiled unavailable";
+    return false;
+  }
+  cuuint64_t dims[4] = {(cuuint64_t)BK, (cuuint64_t)rows, (cuuint64_t)(K / BK), (cuuint64_t)slices};
+  cuuint64_t strides[3] = {(cuuint64_t)BK * 2, (cuuint64_t)BK * 2 * rows, (cuuint64_t)K * 2 * rows};
+  cuuint32_t box[4] = {(cuuint32_t)BK, (cuuint32_t)box_rows, 1, 1};
+  cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<uint16_t*>(ptr), dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    *msg = "cuTensorMapEncodeTiled failed with code " + std::to_string((int)r);
+    return false;
+  }
+  return true;
+}
+
 bool make_map(CUtensorMap* map, const uint16_t* ptr, int K, int rows, int slices, int box_rows, std::string* msg) {
   auto enc = get_encode();
   if (!enc) {
@@ -408,8 +442,8 @@ int tc_gemm_available() {
   return (major == 10 && minor == 3) ? 1 : 0;
 }
 
-// A: [na_slices][M][K] bf16 (M multiple of 128, K multiple of 64); B: [nb_slices][N][K] bf16 (N multiple of bn,
-// bn = 256 or 128); C: fp32 rows of length ldc; only rows < m_valid and columns < n_valid are written.
+// A: [na_slices][M][K] bf16 (M multiple of 128, K multiple of 64); B: [nb_slices][K / 64][N][64] bf16 (N multiple
+// of bn, bn = 256 or 128); C: fp32 rows of length ldc; only rows < m_valid and columns < n_valid are written.
 int tc_gemm_plan_create(TcGemmPlan** plan, const uint16_t* A, int M, int K, long a_slice_stride, int na_slices,
                         const uint16_t* B, int N, long b_slice_stride, int nb_slices, float* C, int ldc, int npairs,
                         const int* pair_a, const int* pair_b, std::string* msg, int bn) {
@@ -423,7 +457,7 @@ int tc_gemm_plan_create(TcGemmPlan** plan, const uint16_t* A, int M, int K, long
   }
   TcGemmPlan* p = new TcGemmPlan();
   p->bn = bn;
-  if (!make_map(&p->mapA, A, K, M, na_slices, BM, msg) || !make_map(&p->mapB, B, K, N, nb_slices, bn, msg)) {
+  if (!make_map(&p->mapA, A, K, M, na_slices, BM, msg) || !make_map_kblocked(&p->mapB, B, K, N, nb_slices, bn, msg)) {
     delete p;
     return WTB_ECUDA;
   }
@@ -529,7 +563,8 @@ int tc_gemm_group_create(TcGroupPlan** plan, int n, const TcGroupDesc* d, int ns
       return WTB_EBADARG;
     }
     std::memset(&h[i], 0, sizeof(TcGroup));
-    if (!make_map(&h[i].mapA, q.A, q.K, q.M, nslices, BM, msg) || !make_map(&h[i].mapB, q.B, q.K, q.N, nslices, bn, msg))
+    if (!make_map(&h[i].mapA, q.A, q.K, q.M, nslices, BM, msg) ||
+        !make_map_kblocked(&h[i].mapB, q.B, q.K, q.N, nslices, bn, msg))
       return WTB_ECUDA;
     TcArgs& a = h[i].args;
     a.K = q.K;

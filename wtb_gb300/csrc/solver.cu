@@ -540,7 +540,8 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
   // a ragged layout (row tables present) selects its start vectors per system over the systems' own rows and
   // keeps the padding rows zero; its reductions run over its part table
   const bool ragged = L.bm.rows != nullptr;
-  const int npart = ragged ? L.nparts : std::max(1, std::min(304, (nrow + 127) / 128));
+  // reduction parts: about 96 rows each, at most four per SM (the Gram kernel needs the CTAs to hide latency)
+  const int npart = ragged ? L.nparts : std::max(1, std::min(608, (nrow + 95) / 96));
   cudaError_t err = cudaSuccess;
   cplx<S>* Sb = ws.get<cplx<S>>("lob_S", (size_t)nrow * ld, &err, true);
   cplx<S>* ASb = ws.get<cplx<S>>("lob_AS", (size_t)nrow * ld, &err, true);

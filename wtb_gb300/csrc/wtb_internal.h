@@ -226,7 +226,8 @@ cudaError_t launch_split_bf16(const double* V, int ldv, int rows, int cols, uint
                               int nslices, cudaStream_t s);
 cudaError_t launch_round_f32(const double* V, int ldv, int rows, int cols, float* out, int ldo, cudaStream_t s);
 
-// tcgen05 split-bf16 GEMM: C[M][N] (fp32, ldc) = sum over slice pairs of A_sa[M][K] * B_sb[N][K]^T.
+// tcgen05 split-bf16 GEMM: C[M][N] (fp32, ldc) = sum over slice pairs of A_sa[M][K] * B_sb[N][K]^T, with A stored
+// [slice][M][K] and B in 64-wide K blocks, [slice][K / 64][N][64].
 struct TcGemmPlan;
 // bn: column tile of the output (256 or 128)
 int tc_gemm_plan_create(TcGemmPlan** plan, const uint16_t* A, int M, int K, long a_slice_stride, int na_slices,
@@ -241,7 +242,7 @@ int tc_gemm_available();
 // systems with frozen[q] set are skipped (frozen may be null); npairs: slice products of this launch.
 struct TcGroupDesc {
   const uint16_t* A;  // [nslices][M][K]
-  const uint16_t* B;  // [nslices][N][K]
+  const uint16_t* B;  // [nslices][K / 64][N][64]
   float* C;
   int M, N, K, ldc, m_valid, n_valid;
 };
