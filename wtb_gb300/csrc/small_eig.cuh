@@ -462,48 +462,41 @@ __device__ void tridiag_eigvecs_cta(const cplx<S>* A, int lda, int n, int nwant,
     }
     __syncthreads();
   }
-  // step 4: u_k = H_0 (H_1 (... H_{n-2} z_k)), one warp per pair of eigenvectors (two independent reductions
-  // per reflector); v_j is row j of A right of the diagonal, contiguous
-  for (int k = 2 * warp; k < nwant; k += 2 * nw) {
-    const bool two = k + 1 < nwant;
-    cplx<S>* u0 = U + (size_t)k * ldu;
-    cplx<S>* u1 = U + (size_t)(two ? k + 1 : k) * ldu;
-    for (int i = lane; i < n; i += 32) {
-      u0[i] = mk<S>(Z[(size_t)k * ldz + i], 0);
-      if (two) u1[i] = mk<S>(Z[(size_t)(k + 1) * ldz + i], 0);
-    }
-    __syncwarp();
-    for (int j = n - 2; j >= 0; --j) {
-      const cplx<S> tj = tau[j];
-      if (tj.re == (S)0 && tj.im == (S)0) continue;
-      const cplx<S>* vj = A + (size_t)j * lda + (j + 1);
-      const int L = n - 1 - j;
-      cplx<S> d0 = mk<S>(0, 0), d1 = mk<S>(0, 0);
-      for (int i = lane; i < L; i += 32) {
-        const cplx<S> vv = vj[i];
-        cfmac(d0, vv, u0[j + 1 + i]);
-        if (two) cfmac(d1, vv, u1[j + 1 + i]);
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        d0.re += __shfl_xor_sync(0xffffffffu, d0.re, o);
-        d0.im += __shfl_xor_sync(0xffffffffu, d0.im, o);
-        d1.re += __shfl_xor_sync(0xffffffffu, d1.re, o);
-        d1.im += __shfl_xor_sync(0xffffffffu, d1.im, o);
-      }
-      const cplx<S> f0 = cmul(tj, d0), f1 = cmul(tj, d1);
-      for (int i = lane; i < L; i += 32) {
-        const cplx<S> vv = vj[i];
-        cplx<S>& a0 = u0[j + 1 + i];
-        a0.re -= f0.re * vv.re - f0.im * vv.im;
-        a0.im -= f0.re * vv.im + f0.im * vv.re;
-        if (two) {
-          cplx<S>& a1 = u1[j + 1 + i];
-          a1.re -= f1.re * vv.re - f1.im * vv.im;
-          a1.im -= f1.re * vv.im + f1.im * vv.re;
-        }
-      }
+  // step 4: u_k = H_0 (H_1 (... H_{n-2} z_k)), one team of TS lanes per eigenvector (teams inside warps, so a
+  // reflector costs a few shuffles and no block barrier); v_j is row j of A right of the diagonal, contiguous
+  {
+    const int TS = n > 16 ? 16 : 8;
+    const int tl = tid & (TS - 1), team = tid / TS, nteam = nt / TS;
+    const int kmax = (nwant + nteam - 1) / nteam * nteam;  // uniform trip count: every lane reaches the shuffles
+    for (int k = team; k < kmax; k += nteam) {
+      const bool on = k < nwant;
+      cplx<S>* u = U + (size_t)(on ? k : 0) * ldu;
+      if (on)
+        for (int i = tl; i < n; i += TS) u[i] = mk<S>(Z[(size_t)k * ldz + i], 0);
       __syncwarp();
+      for (int j = n - 2; j >= 0; --j) {
+        const cplx<S> tj = tau[j];
+        if (tj.re == (S)0 && tj.im == (S)0) continue;  // uniform: tau is shared
+        const cplx<S>* vj = A + (size_t)j * lda + (j + 1);
+        const int L = n - 1 - j;
+        cplx<S> dt = mk<S>(0, 0);
+        if (on)
+          for (int i = tl; i < L; i += TS) cfmac(dt, vj[i], u[j + 1 + i]);
+#pragma unroll
+        for (int o = TS / 2; o > 0; o >>= 1) {
+          dt.re += __shfl_xor_sync(0xffffffffu, dt.re, o);
+          dt.im += __shfl_xor_sync(0xffffffffu, dt.im, o);
+        }
+        const cplx<S> f = cmul(tj, dt);
+        if (on)
+          for (int i = tl; i < L; i += TS) {
+            const cplx<S> vv = vj[i];
+            cplx<S>& a0 = u[j + 1 + i];
+            a0.re -= f.re * vv.re - f.im * vv.im;
+            a0.im -= f.re * vv.im + f.im * vv.re;
+          }
+        __syncwarp();
+      }
     }
   }
   __syncthreads();
