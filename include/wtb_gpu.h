@@ -163,9 +163,38 @@ int wtb_bsesolver(wtb_ctx* ctx, const wtb_bse_params* p, double* Ws, double* act
 int wtb_bsedielraw(wtb_ctx* ctx, const wtb_bse_params* p, int dimse, const double* Ws, const double* acts,
                    double* dielf);
 
+/* Replaces bsedielrawpol (src/module_bse.F90:1043-1199): dielf(numbse, 3, 5) = (omega, eps1, eps2) for the
+ * xx yy zz sp sm (sigma+/sigma-) components from Ws and acts(dimse, 5) (the columns of bse_opt_diel-pol.dat);
+ * every component takes optdiel's rtype 1 (eps1 = 1 + ...), then imagrenorm and the spin factor. */
+int wtb_bsedielrawpol(wtb_ctx* ctx, const wtb_bse_params* p, int dimse, const double* Ws, const double* acts,
+                      double* dielf);
+
+/* Replaces spoptics (src/module_bse.F90:4802-5071) without its text files; bsesolver writes the same records
+ * (:2317-2357).  For the Monkhorst-Pack mesh of p (ngrid, mshift, nv, nc; cshift is optsp's sme): bands and
+ * velocity matrix elements on the device, then the dimsp = Nk nc nv independent-particle transitions as
+ * REAL(4) records, column-major like the reference's vecres(dimsp, 15):
+ *   kx ky kz, nocp, nocp-nv+c, nocp-nv+v, E_c-E_v, xx yy zz xy xz yz, sp sm
+ * (xx = |h_x|^2, xy = Re(h_x h_y*), sp = |h_+|^2, ...), stably sorted by E_c-E_v as Bubblem sorts them
+ * (src/module_math.F90:287-308).  Columns 7-13 are sp_optics.dat, columns 7-10 and 14-15 sp_optics-pol.dat. */
+int wtb_spoptics(wtb_ctx* ctx, const wtb_bse_params* p, float* rec);
+
+/* Replace spdielraw and spdielrawpol (src/module_bse.F90:4090-4308, :4318-4524): the broadened
+ * independent-particle spectrum of the dimsp transitions esp with acts(dimsp, 6) = xx yy zz xy xz yz
+ * (dielf(numbse, 3, 6), rtype 1 for xx yy zz) or acts(dimsp, 5) = xx yy zz sp sm (dielf(numbse, 3, 5),
+ * rtype 1 for all); optdiel, avgsme, imagrenorm and the spin factor as in bsedielraw. */
+int wtb_spdielraw(wtb_ctx* ctx, const wtb_bse_params* p, int dimsp, const double* esp, const double* acts,
+                  double* dielf);
+int wtb_spdielrawpol(wtb_ctx* ctx, const wtb_bse_params* p, int dimsp, const double* esp, const double* acts,
+                     double* dielf);
+
 /* Replaces bseoptprop (src/module_bse.F90:3766-3931, formulas :5075-5124): props(numbse, 6, 5) =
- * refractive index, extinction coefficient, reflectivity, absorption coefficient, energy-loss function. */
+ * refractive index, extinction coefficient, reflectivity, absorption coefficient, energy-loss function.
+ * spoptprop (:3438-3602) applies the same formulas to the spdielraw spectrum. */
 int wtb_bseoptprop(wtb_ctx* ctx, int numbse, const double* dielf, double* props);
+
+/* Replaces bseoptproppol and spoptproppol (src/module_bse.F90:3937-4084, :3608-3760): props(numbse, 5, 5)
+ * for the xx yy zz sp sm spectrum dielf(numbse, 3, 5). */
+int wtb_bseoptproppol(wtb_ctx* ctx, int numbse, const double* dielf, double* props);
 
 /* Allocation-free variant of wtb_dielbse, for callers that cannot allocate device memory: their device
  * memory belongs to another allocator (a framework's caching pool, a host program's preallocated arena)

@@ -448,20 +448,20 @@ def imagrenorm(E1, dielf):
 
 
 COMPONENTS = ("xx", "yy", "zz", "xy", "xz", "yz")
+POL_COMPONENTS = ("xx", "yy", "zz", "sp", "sm")
 
 
-def bsedielraw(Ws, acts, ngrid, rlat, p, spinf=1.0):
-    """epsilon(omega) for the six components (src/module_bse.F90:835-1036).
-
-    ``Ws`` and ``acts`` are the dim-row arrays that bsesolver writes (rows past nev hold E = 0 and
-    zero activities).  Returns dict comp -> (numbse, 3) array [omega, spinf*eps1, spinf*eps2]."""
+def dielraw(Ws, acts, comps, rtype1, ngrid, rlat, p, spinf=1.0):
+    """optdiel over the given activity columns, then imagrenorm and the spin factor: the common body of
+    bsedielraw (src/module_bse.F90:835-1036), bsedielrawpol (:1043-1199), spdielraw (:4090-4308) and
+    spdielrawpol (:4318-4524).  ``rtype1`` holds the components optdiel gets with rtype 1."""
     vc = vcell3D(rlat)
     N = int(p.numbse)
     j = np.arange(N, dtype=np.float64)
     elux = p.ebse0 + ((p.ebsef - p.ebse0) * j) / (float(N) - 1.0)
     out = {}
-    for comp in COMPONENTS:
-        rtype = 1 if comp in ("xx", "yy", "zz") else 0
+    for comp in comps:
+        rtype = 1 if comp in rtype1 else 0
         r, im = optdiel_grid(rtype, vc, ngrid, elux, Ws, acts[comp], p.cshift)
         d = np.stack([elux, r, im], axis=1)
         if p.renorm:
@@ -470,6 +470,78 @@ def bsedielraw(Ws, acts, ngrid, rlat, p, spinf=1.0):
         d[:, 2] *= spinf
         out[comp] = d
     return out
+
+
+def bsedielraw(Ws, acts, ngrid, rlat, p, spinf=1.0):
+    """epsilon(omega) for the six components (src/module_bse.F90:835-1036).
+
+    ``Ws`` and ``acts`` are the dim-row arrays that bsesolver writes (rows past nev hold E = 0 and
+    zero activities).  Returns dict comp -> (numbse, 3) array [omega, spinf*eps1, spinf*eps2]."""
+    return dielraw(Ws, acts, COMPONENTS, ("xx", "yy", "zz"), ngrid, rlat, p, spinf)
+
+
+def bsedielrawpol(Ws, acts, ngrid, rlat, p, spinf=1.0):
+    """xx yy zz sp sm, every one with optdiel rtype 1 (src/module_bse.F90:1043-1199)."""
+    return dielraw(Ws, acts, POL_COMPONENTS, POL_COMPONENTS, ngrid, rlat, p, spinf)
+
+
+def spdielraw(esp, acts, ngrid, rlat, p, spinf=1.0):
+    """The independent-particle spectrum (src/module_bse.F90:4090-4308): bsedielraw's sums over the
+    transitions of spoptics."""
+    return dielraw(esp, acts, COMPONENTS, ("xx", "yy", "zz"), ngrid, rlat, p, spinf)
+
+
+def spdielrawpol(esp, acts, ngrid, rlat, p, spinf=1.0):
+    """src/module_bse.F90:4318-4524."""
+    return dielraw(esp, acts, POL_COMPONENTS, POL_COMPONENTS, ngrid, rlat, p, spinf)
+
+
+def bubblem(vec, a):
+    """Bubblem(a, b, vec, n) (src/module_math.F90:287-308) literally: for i = 1..n, for j = n..i+1 step -1,
+    swap rows j-1 and j when vec(j-1, a) > vec(j, a).  Pure Python, O(n^2): small cases only.  ``a`` is
+    0-based here."""
+    v = np.array(vec, copy=True)
+    n = v.shape[0]
+    for i in range(n):
+        for j in range(n - 1, i, -1):
+            if v[j - 1, a] > v[j, a]:
+                t = v[j - 1].copy()
+                v[j - 1] = v[j]
+                v[j] = t
+    return v
+
+
+def stable_sort_rows(vec, a):
+    """The result of Bubblem: a stable ascending sort of the rows by column ``a`` (ties, including -0 and
+    +0, keep their order)."""
+    return np.asarray(vec)[np.argsort(np.asarray(vec)[:, a], kind="stable")]
+
+
+def spoptics_records(eigv, kpt, nocpk, hr, nv, nc):
+    """spoptics' vecres(dimsp, 15) in REAL(4) (src/module_bse.F90:4962-4991; bsesolver :2317-2348), sorted
+    by Bubblem on column 7 (:4992).  hr = (hrx, hry, hrz, hrsp, hrsm) of optsp_all."""
+    F = np.float32
+    nk = len(kpt)
+    dim = nk * nc * nv
+    rec = np.zeros((dim, 15), dtype=F)
+    hx, hy, hz, hsp, hsm = hr
+
+    def rp(a, b):
+        return (a * np.conj(b)).real
+
+    for k in range(nk):
+        for c in range(nc):
+            for v in range(nv):
+                I = k * nc * nv + c * nv + v
+                rec[I, 0:3] = F(kpt[k, 0]), F(kpt[k, 1]), F(kpt[k, 2])
+                rec[I, 3] = F(nocpk[k])
+                rec[I, 4] = F(nocpk[k] - nv + (nv + c + 1))
+                rec[I, 5] = F(nocpk[k] - nv + (v + 1))
+                rec[I, 6] = F(eigv[k, nv + c] - eigv[k, v])
+                rec[I, 7:15] = [F(rp(hx[I], hx[I])), F(rp(hy[I], hy[I])), F(rp(hz[I], hz[I])),
+                                F(rp(hx[I], hy[I])), F(rp(hx[I], hz[I])), F(rp(hy[I], hz[I])),
+                                F(rp(hsp[I], hsp[I])), F(rp(hsm[I], hsm[I]))]
+    return stable_sort_rows(rec, 6)
 
 
 def abscoef(e1, e2, efoton):

@@ -76,3 +76,35 @@ def test_fit_screening_length_to_target_spectrum(ctx):
     # the target's noise alone leaves numbse * 1e-6 = 1e-3 in the loss
     noise_floor = p.numbse * 1e-6
     assert Lb < L0 and Lb < 1.2 * noise_floor, (Lb, L0)
+
+
+def test_ipa_spectrum_at_full_size(ctx):
+    """spoptics + spdielraw on the 57,600-transition mesh: the records are sorted and hold every (k, c, v)
+    once, and the IPA spectrum obeys the Lorentzian sum rule over the window,
+    int eps2 = C sum_n f_n [atan((b - E_n)/g) - atan((a - E_n)/g)], g = CSHIFT + avgsme (renormalisation off),
+    to the trapezoid rule's 1e-5."""
+    from oracle import wtb_oracle as O
+
+    sysm, p = S.workload("hex12_60x60")
+    ctx.set_hr(sysm)
+    rec = ctx.spoptics(p)
+    assert rec.shape == (p.dim, 15)
+    assert np.all(np.diff(rec[:, 6]) >= 0)
+    nk = p.ngrid[0] * p.ngrid[1] * p.ngrid[2]
+    ids = np.unique(np.stack([rec[:, 4] - rec[:, 3], rec[:, 3] - rec[:, 5]], axis=1), axis=0)
+    assert len(ids) == p.nc * p.nv
+    kid = np.unique(np.round(rec[:, :3].astype(np.float64), 4), axis=0)
+    assert len(kid) == nk
+    q = S.BSEParams(**{**p.__dict__})
+    q.renorm, q.numbse, q.ebse0, q.ebsef = False, 40001, 0.0, 12.0
+    esp = rec[:, 6].astype(np.float64)
+    acts = {c: rec[:, 7 + i].astype(np.float64) for i, c in enumerate(O.COMPONENTS)}
+    d = ctx.spdielraw(q, esp, acts)["xx"]
+    spinf = 2.0 if sysm.systype == "NP" else 1.0
+    C = O.GAMA / (float(np.float32(nk)) * O.vcell3D(sysm.rlat))
+    g = q.cshift + O.avgsme(esp)
+    f = acts["xx"]
+    expect = spinf * C * np.sum(f * (np.arctan((q.ebsef - esp) / g) - np.arctan((q.ebse0 - esp) / g)))
+    integral = np.trapezoid(d[:, 2], d[:, 0])
+    assert abs(integral - expect) / expect < 1e-5, (integral, expect)
+    assert np.all(np.isfinite(d))

@@ -181,6 +181,67 @@ def test_optprops_kernel(ctx, c1):
             np.testing.assert_allclose(props[nm][c], pr[nm], rtol=1e-9, atol=1e-12)
 
 
+def test_spectrum_pol_kernel(ctx, c1):
+    """bsedielrawpol: xx yy zz sp sm all with rtype 1."""
+    sysm, p, ref = c1
+    ctx.set_hr(sysm)
+    d = ctx.bsedielrawpol(p, ref["Ws"], ref["acts"])
+    d_ref = O.bsedielrawpol(ref["Ws"], ref["acts"], p.ngrid, sysm.rlat, p)
+    for c in O.POL_COMPONENTS:
+        np.testing.assert_allclose(d[c], d_ref[c], rtol=1e-10, atol=1e-12 * max(1.0, np.abs(d_ref[c]).max()))
+    props = ctx.bseoptproppol(d_ref)
+    for c in O.POL_COMPONENTS:
+        om, e1, e2 = d_ref[c][:, 0], d_ref[c][:, 1], d_ref[c][:, 2]
+        pr = O.optprops(e1, e2, om)
+        for nm in ("refr", "ext", "refl", "abs", "eloss"):
+            np.testing.assert_allclose(props[nm][c], pr[nm], rtol=1e-9, atol=1e-12)
+
+
+def _by_transition(rec):
+    """rows keyed by (k-point, conduction slot, valence slot)"""
+    return {(round(float(r[0]), 4), round(float(r[1]), 4), round(float(r[2]), 4), int(r[4]), int(r[5])): r
+            for r in rec}
+
+
+@pytest.mark.parametrize("precision,op", [("fp64", "matfree"), ("bf16x3", "matfree")])
+def test_spoptics_records(ctx, small, precision, op):
+    """spoptics: REAL(4) records sorted by transition energy; every (k, c, v) once; activities within the
+    band solver's accuracy (FP64 bands: 1e-6 of the largest; mixed FP32/FP64 set-up: 1e-4)."""
+    sysm, p, ref = small
+    ctx.set_hr(sysm)
+    q = S.BSEParams(**{**p.__dict__})
+    q.precision, q.op = precision, op
+    rec = ctx.spoptics(q)
+    rr = O.spoptics_records(ref["eigv"], ref["kpt"], ref["nocpk"], ref["hr"], p.nv, p.nc)
+    assert rec.dtype == np.float32 and rec.shape == rr.shape
+    assert np.all(np.diff(rec[:, 6]) >= 0)
+    np.testing.assert_allclose(rec[:, 6], rr[:, 6], rtol=2e-7, atol=1e-6)
+    a, b = _by_transition(rec), _by_transition(rr)
+    assert a.keys() == b.keys() and len(a) == p.dim
+    tol = 1e-6 if precision == "fp64" else 1e-4
+    amax = np.abs(rr[:, 7:15]).max(axis=0)
+    for key, y in b.items():
+        x = a[key]
+        np.testing.assert_array_equal(x[3:6], y[3:6])
+        np.testing.assert_allclose(x[7:15], y[7:15], rtol=0, atol=tol * amax.max())
+
+
+def test_spdielraw_kernels(ctx, small):
+    """spdielraw / spdielrawpol over the IPA transitions (every row carries activity)."""
+    sysm, p, ref = small
+    ctx.set_hr(sysm)
+    rr = O.spoptics_records(ref["eigv"], ref["kpt"], ref["nocpk"], ref["hr"], p.nv, p.nc).astype(np.float64)
+    esp = rr[:, 6]
+    acts = {c: rr[:, 7 + i] for i, c in enumerate(O.COMPONENTS)}
+    acts.update(sp=rr[:, 13], sm=rr[:, 14])
+    for fn, ofn, comps in ((ctx.spdielraw, O.spdielraw, O.COMPONENTS),
+                           (ctx.spdielrawpol, O.spdielrawpol, O.POL_COMPONENTS)):
+        d = fn(p, esp, acts)
+        d_ref = ofn(esp, acts, p.ngrid, sysm.rlat, p)
+        for c in comps:
+            np.testing.assert_allclose(d[c], d_ref[c], rtol=1e-10, atol=1e-12 * max(1.0, np.abs(d_ref[c]).max()))
+
+
 def test_dielbse(ctx, small):
     sysm, p, ref = small
     A = ref["A"]

@@ -169,6 +169,66 @@ def test_imagrenorm_baseline():
     assert np.all(d2 == 1.0)
 
 
+def test_bubblem_is_a_stable_sort():
+    """Bubblem swaps only on a strictly greater key: its result is the stable ascending sort, with ties
+    (including -0 and +0) in their original order."""
+    rng = np.random.default_rng(7)
+    v = np.zeros((60, 3), dtype=np.float32)
+    v[:, 0] = rng.integers(0, 6, 60).astype(np.float32) * np.float32(0.25)
+    v[:5, 0] = [0.0, -0.0, 0.0, -0.0, 0.5]
+    v[:, 1] = np.arange(60)
+    v[:, 2] = rng.standard_normal(60)
+    a = O.bubblem(v, 0)
+    b = O.stable_sort_rows(v, 0)
+    np.testing.assert_array_equal(a, b)
+    assert np.all(np.diff(a[:, 0]) >= 0)
+    for key in np.unique(v[:, 0]):             # ties keep their input order
+        rows = a[a[:, 0] == key, 1]
+        assert np.all(np.diff(rows) > 0)
+
+
+def test_pol_spectrum_shares_the_lorentzian_sum():
+    """bsedielrawpol's sp/sm columns get the rtype-1 sum of bsedielraw's xx (eps1 offset 1); spdielraw is
+    bsedielraw over the transition list."""
+    p = S.BSEParams(ngrid=(4, 4, 1), nc=1, nv=1, numbse=301, ebse0=0.0, ebsef=4.0, cshift=0.05, renorm=True)
+    rlat = S.hex_lattice()
+    rng = np.random.default_rng(3)
+    Ws = np.sort(rng.uniform(1.0, 3.0, 40))
+    f = {c: rng.uniform(0.0, 1.0, 40) for c in O.COMPONENTS + ("sp", "sm")}
+    six = O.bsedielraw(Ws, f, p.ngrid, rlat, p, spinf=2.0)
+    pol = O.bsedielrawpol(Ws, f, p.ngrid, rlat, p, spinf=2.0)
+    for c in ("xx", "yy", "zz"):
+        np.testing.assert_array_equal(pol[c], six[c])
+    same = dict(f, xx=f["sp"])
+    np.testing.assert_array_equal(pol["sp"], O.bsedielraw(Ws, same, p.ngrid, rlat, p, spinf=2.0)["xx"])
+    off = O.bsedielraw(Ws, dict(f, xy=f["sm"]), p.ngrid, rlat, p, spinf=1.0)["xy"]
+    pm = O.bsedielrawpol(Ws, f, p.ngrid, rlat, p, spinf=1.0)["sm"]
+    np.testing.assert_allclose(pm[:, 1], off[:, 1] + 1.0, rtol=1e-14)   # rtype 1 vs 0: eps1 offset only
+    np.testing.assert_array_equal(pm[:, 2], off[:, 2])
+    sp = O.spdielraw(Ws, f, p.ngrid, rlat, p, spinf=2.0)
+    for c in O.COMPONENTS:
+        np.testing.assert_array_equal(sp[c], six[c])
+
+
+def test_spoptics_records(small):
+    """The IPA records: sorted by transition energy, one per (k, c, v), quantum numbers from nocp, and the
+    circular activities obey |h+|^2 + |h-|^2 = 2 s^2 (|hx|^2 + |hy|^2) with s = 1/sqrt(2) in REAL(4)."""
+    sysm, p, kpt, eigv, vec, nocp = small
+    hr = O.optsp_all(eigv, vec, kpt, sysm, p)
+    rec = O.spoptics_records(eigv, kpt, nocp, hr, p.nv, p.nc)
+    assert rec.dtype == np.float32 and rec.shape == (p.dim, 15)
+    assert np.all(np.diff(rec[:, 6]) >= 0)
+    ids = {(int(r[4]) - int(r[3]), int(r[3]) - int(r[5])) for r in rec}
+    assert ids == {(c + 1, p.nv - v - 1) for c in range(p.nc) for v in range(p.nv)}
+    np.testing.assert_allclose(rec[:, 6].min(), np.float32((eigv[:, p.nv] - eigv[:, p.nv - 1]).min()), rtol=1e-7)
+    s2 = O.INV_SQRT2_F32 ** 2
+    lhs = rec[:, 13].astype(np.float64) + rec[:, 14]
+    rhs = 2.0 * s2 * (rec[:, 7].astype(np.float64) + rec[:, 8])
+    np.testing.assert_allclose(lhs, rhs, rtol=1e-5, atol=1e-6 * rhs.max())
+    assert np.all(rec[:, 7:10] >= 0)
+    assert np.all(rec[:, 10] ** 2 <= rec[:, 7] * rec[:, 8] * (1 + 1e-5) + 1e-12)   # Cauchy-Schwarz
+
+
 @pytest.mark.parametrize("name", ["hex8_6x6", "hex8_24x24"])
 def test_golden_fixtures(name):
     from tests.golden.make_golden import input_digest

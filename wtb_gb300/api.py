@@ -2,7 +2,8 @@
 
 The names and argument meanings follow the Fortran subroutines the library replaces
 (``eigsys``, ``monhkhorst_pack``, ``bsesolver``, ``slepc_solver``, ``dielbsev``/``dielbsep``,
-``bsedielraw``, ``bseoptprop`` and the ``module_coulomb`` potentials); arrays cross the boundary in
+``bsedielraw``/``bsedielrawpol``, ``spoptics``, ``spdielraw``/``spdielrawpol``, ``bseoptprop``/``bseoptproppol``
+and the ``module_coulomb`` potentials); arrays cross the boundary in
 Fortran column-major order exactly as the Fortran caller would pass them.  There is no CPU
 fallback: if the shared library is missing, importing this module raises.
 """
@@ -27,6 +28,9 @@ PREC = {"fp64": 0, "fp32": 1, "bf16x3": 2, "bf16x6": 3}
 OPS = {"dense": 0, "matfree": 1}
 COULTYPES = {"V2DK": 0, "V3D": 1, "V3DL": 2, "V2DT": 3, "V2DT2": 4, "V2DOH": 5, "V2DRK": 6, "V1DT": 7, "V0DT": 8}
 COMPONENTS = ("xx", "yy", "zz", "xy", "xz", "yz", "sp", "sm")
+POL_COMPONENTS = ("xx", "yy", "zz", "sp", "sm")
+# the columns of spoptics' vecres records (src/module_bse.F90:4969-4990)
+SP_COLUMNS = ("kx", "ky", "kz", "nocp", "ic", "iv", "energy", "xx", "yy", "zz", "xy", "xz", "yz", "sp", "sm")
 
 
 class WTBError(RuntimeError):
@@ -83,6 +87,11 @@ def _load():
         "wtb_bsesolver": [P, C.POINTER(CParams), dp, dp, dp, C.POINTER(CTimings)],
         "wtb_bsedielraw": [P, C.POINTER(CParams), C.c_int, dp, dp, dp],
         "wtb_bseoptprop": [P, C.c_int, dp, dp],
+        "wtb_bsedielrawpol": [P, C.POINTER(CParams), C.c_int, dp, dp, dp],
+        "wtb_spdielraw": [P, C.POINTER(CParams), C.c_int, dp, dp, dp],
+        "wtb_spdielrawpol": [P, C.POINTER(CParams), C.c_int, dp, dp, dp],
+        "wtb_bseoptproppol": [P, C.c_int, dp, dp],
+        "wtb_spoptics": [P, C.POINTER(CParams), C.POINTER(C.c_float)],
         "wtb_bse_backward": [P, C.POINTER(CParams), dp, dp, dp, dp, dp, C.POINTER(CTimings)],
         "wtb_spectrum_loss": [P, C.POINTER(CParams), C.c_int, C.c_int, dp, dp, dp, dp, dp, dp],
         "wtb_batch_create": [C.POINTER(P), C.c_int, C.c_int],
@@ -339,29 +348,61 @@ class Context:
                   "wtb_spectrum_loss")
         return L.value, gE, gf
 
-    def bsedielraw(self, p: BSEParams, Ws, acts):
-        """Returns dict comp -> (numbse, 3) [omega, eps1, eps2] for xx yy zz xy xz yz."""
+    def _dielraw(self, fn, name, p: BSEParams, Ws, acts, comps):
         Ws = np.asarray(Ws, dtype=np.float64)
         dimse = len(Ws)
-        A = np.zeros((dimse, 6), order="F")
-        for i, cname in enumerate(COMPONENTS[:6]):
+        nc = len(comps)
+        A = np.zeros((dimse, nc), order="F")
+        for i, cname in enumerate(comps):
             A[:, i] = acts[cname]
-        dielf = np.zeros((p.numbse, 3, 6), order="F")
+        dielf = np.zeros((p.numbse, 3, nc), order="F")
         cp = cparams(p)
-        self._chk(_lib.wtb_bsedielraw(self._h, C.byref(cp), dimse, _dp(_f64(Ws)), _dp(A), _dp(dielf)),
-                  "wtb_bsedielraw")
-        return {cname: dielf[:, :, i].copy() for i, cname in enumerate(COMPONENTS[:6])}
+        self._chk(fn(self._h, C.byref(cp), dimse, _dp(_f64(Ws)), _dp(A), _dp(dielf)), name)
+        return {cname: dielf[:, :, i].copy() for i, cname in enumerate(comps)}
+
+    def bsedielraw(self, p: BSEParams, Ws, acts):
+        """Returns dict comp -> (numbse, 3) [omega, eps1, eps2] for xx yy zz xy xz yz."""
+        return self._dielraw(_lib.wtb_bsedielraw, "wtb_bsedielraw", p, Ws, acts, COMPONENTS[:6])
+
+    def bsedielrawpol(self, p: BSEParams, Ws, acts):
+        """bsedielrawpol: dict comp -> (numbse, 3) for xx yy zz sp sm (acts: dict with those keys)."""
+        return self._dielraw(_lib.wtb_bsedielrawpol, "wtb_bsedielrawpol", p, Ws, acts, POL_COMPONENTS)
+
+    def spdielraw(self, p: BSEParams, esp, acts):
+        """spdielraw: the independent-particle spectrum of the transitions esp, acts xx yy zz xy xz yz."""
+        return self._dielraw(_lib.wtb_spdielraw, "wtb_spdielraw", p, esp, acts, COMPONENTS[:6])
+
+    def spdielrawpol(self, p: BSEParams, esp, acts):
+        """spdielrawpol: the independent-particle spectrum for xx yy zz sp sm."""
+        return self._dielraw(_lib.wtb_spdielrawpol, "wtb_spdielrawpol", p, esp, acts, POL_COMPONENTS)
+
+    def spoptics(self, p: BSEParams):
+        """spoptics: the (dimsp, 15) float32 records (columns SP_COLUMNS) sorted by transition energy."""
+        dim = p.ngrid[0] * p.ngrid[1] * p.ngrid[2] * p.nc * p.nv
+        rec = np.zeros((dim, 15), dtype=np.float32, order="F")
+        cp = cparams(p)
+        self._chk(_lib.wtb_spoptics(self._h, C.byref(cp), rec.ctypes.data_as(C.POINTER(C.c_float))),
+                  "wtb_spoptics")
+        return rec
+
+    def _optprop(self, fn, name, dielf: dict, comps):
+        n = next(iter(dielf.values())).shape[0]
+        nc = len(comps)
+        D = np.zeros((n, 3, nc), order="F")
+        for i, cname in enumerate(comps):
+            D[:, :, i] = dielf[cname]
+        props = np.zeros((n, nc, 5), order="F")
+        self._chk(fn(self._h, n, _dp(D), _dp(props)), name)
+        names = ("refr", "ext", "refl", "abs", "eloss")
+        return {nm: {cname: props[:, i, q].copy() for i, cname in enumerate(comps)}
+                for q, nm in enumerate(names)}
 
     def bseoptprop(self, dielf: dict):
-        n = next(iter(dielf.values())).shape[0]
-        D = np.zeros((n, 3, 6), order="F")
-        for i, cname in enumerate(COMPONENTS[:6]):
-            D[:, :, i] = dielf[cname]
-        props = np.zeros((n, 6, 5), order="F")
-        self._chk(_lib.wtb_bseoptprop(self._h, n, _dp(D), _dp(props)), "wtb_bseoptprop")
-        names = ("refr", "ext", "refl", "abs", "eloss")
-        return {nm: {cname: props[:, i, q].copy() for i, cname in enumerate(COMPONENTS[:6])}
-                for q, nm in enumerate(names)}
+        return self._optprop(_lib.wtb_bseoptprop, "wtb_bseoptprop", dielf, COMPONENTS[:6])
+
+    def bseoptproppol(self, dielf: dict):
+        """bseoptproppol / spoptproppol: the optical constants of an xx yy zz sp sm spectrum."""
+        return self._optprop(_lib.wtb_bseoptproppol, "wtb_bseoptproppol", dielf, POL_COMPONENTS)
 
 
 class Batch:

@@ -6,7 +6,9 @@
 //   omega_j = E0 + (Ef - E0)(j-1)/(N-1),   gamma = CSHIFT + 10 * (sum_{i>=2} (E_i - E_{i-1})) / nrows,
 //   eps2(omega) = C sum_n f_n gamma / ((omega - E_n)^2 + gamma^2),
 //   eps1(omega) = delta + C sum_n f_n (E_n - omega) / ((omega - E_n)^2 + gamma^2),  C = 180.90_f32 / (Nk Vol)
-// then the optional baseline renormalisation of eps2 and the spin factor.
+// then the optional baseline renormalisation of eps2 and the spin factor.  bsedielrawpol, spdielraw and
+// spdielrawpol (src/module_bse.F90:1043-1199, :4090-4524) run the same sums over other columns: xx yy zz sp sm
+// all with rtype 1, and the IPA records of spoptics (:4802-5071) sorted by Bubblem (src/module_math.F90:287-308).
 // bseoptprop (src/module_bse.F90:3766-3931, :5075-5124): refractive index, extinction, reflectivity,
 // absorption coefficient sqrt(2)_f32 * omega / hc_f32 * sqrt(|eps| - eps1), loss function.
 #include "wtb_internal.h"
@@ -88,7 +90,8 @@ __global__ void osc_final_kernel(const double* __restrict__ partial, int nblk, i
 // Also records in smef[1] the end of the last row with a nonzero activity in any component: rows past it add
 // exactly zero to every Lorentzian sum (bsesolver leaves the rows past nev at zero).
 __global__ void __launch_bounds__(1024) avgsme_kernel(const double* __restrict__ Ws, int nrows, double sme,
-                                                      const double* __restrict__ f, double* __restrict__ smef) {
+                                                      const double* __restrict__ f, int ncomp,
+                                                      double* __restrict__ smef) {
   __shared__ double red[1024];
   __shared__ int s_last;
   if (threadIdx.x == 0) s_last = 0;
@@ -98,7 +101,7 @@ __global__ void __launch_bounds__(1024) avgsme_kernel(const double* __restrict__
   int last = 0;
   for (int i = max(i0, 1); i < min(nrows, i0 + chunk); ++i) acc = acc + Ws[i] - Ws[i - 1];
   for (int i = i0; i < min(nrows, i0 + chunk); ++i)
-    for (int c = 0; c < 6; ++c)
+    for (int c = 0; c < ncomp; ++c)
       if (f[(size_t)c * nrows + i] != 0.0) last = i + 1;
   red[threadIdx.x] = acc;
   __syncthreads();
@@ -113,29 +116,86 @@ __global__ void __launch_bounds__(1024) avgsme_kernel(const double* __restrict__
   }
 }
 
-__global__ void lorentz_kernel(const double* __restrict__ Ws, int nrows, const double* __restrict__ f,
-                               const double* __restrict__ smef_p, double caux, double e0, double ef, int nesp,
-                               double* __restrict__ dielf) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= 6 * nesp) return;
-  const int comp = e / nesp, j = e % nesp;
-  const double elux = e0 + ((ef - e0) * (double)j) / ((double)nesp - 1.0);
-  const double smef = smef_p[0];
+constexpr int kLorOmega = 128;  // photon energies per CTA (one per thread)
+constexpr int kLorRows = 256;   // rows staged in shared memory at a time
+
+__device__ __forceinline__ double omega_of(double e0, double ef, int nesp, int j) {
+  return e0 + ((ef - e0) * (double)j) / ((double)nesp - 1.0);
+}
+
+// Partial Lorentzian sums of optdiel over one chunk of the rows, all NC components at once: the two
+// quotients (E - omega) / eaux and gamma / eaux do not depend on the component, so each (row, omega) pair
+// costs two FP64 divisions instead of two per component, and the products f_c * quotient are the
+// reference's own.  A thread owns one photon energy; the chunk's rows pass through shared memory.
+// part[chunk][c][0: real, 1: imaginary][nesp].
+template <int NC>
+__global__ void __launch_bounds__(kLorOmega) lorentz_partial_kernel(const double* __restrict__ Ws, int nrows,
+                                                                    const double* __restrict__ f,
+                                                                    const double* __restrict__ smef_p, double e0,
+                                                                    double ef, int nesp, double* __restrict__ part) {
+  __shared__ double sW[kLorRows];
+  __shared__ double sf[NC][kLorRows];
+  const int j = blockIdx.x * kLorOmega + threadIdx.x;
+  const int nchunk = gridDim.y, ch = blockIdx.y;
   const int nuse = min(nrows, (int)smef_p[1]);
-  const double* fc = f + (size_t)comp * nrows;
-  double rpart = 0.0, ipart = 0.0;
-  for (int i = 0; i < nuse; ++i) {
-    const double fi = fc[i];
-    if (fi == 0.0) continue;  // zero activities add exactly zero (the denominator is >= gamma^2 > 0)
-    const double ex = Ws[i];
-    const double eaux = ((elux - ex) * (elux - ex)) + (smef * smef);
-    rpart += fi * ((ex - elux) / eaux);
-    ipart += fi * (smef / eaux);
+  const int per = (nuse + nchunk - 1) / nchunk;
+  const int r0 = min(nuse, ch * per), r1 = min(nuse, r0 + per);
+  const double smef = smef_p[0];
+  const double elux = omega_of(e0, ef, nesp, j);
+  double rp[NC], ip[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) rp[c] = ip[c] = 0.0;
+  for (int t0 = r0; t0 < r1; t0 += kLorRows) {
+    const int nt = min(kLorRows, r1 - t0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < (NC + 1) * kLorRows; e += kLorOmega) {
+      const int q = e / kLorRows, r = e % kLorRows;
+      if (r >= nt) continue;
+      if (q == 0)
+        sW[r] = Ws[t0 + r];
+      else
+        sf[q - 1][r] = f[(size_t)(q - 1) * nrows + t0 + r];
+    }
+    __syncthreads();
+    if (j < nesp)
+      for (int r = 0; r < nt; ++r) {
+        const double ex = sW[r];
+        const double eaux = ((elux - ex) * (elux - ex)) + (smef * smef);
+        const double q1 = (ex - elux) / eaux;
+        const double q2 = smef / eaux;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          rp[c] += sf[c][r] * q1;
+          ip[c] += sf[c][r] * q2;
+        }
+      }
   }
-  const double delta = comp < 3 ? 1.0 : 0.0;
-  // Fortran layout dielf(nesp, 3, 6): (j, c, comp) at j + nesp*(c + 3*comp)
+  if (j >= nesp) return;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    double* o = part + ((size_t)ch * NC + c) * 2 * nesp + j;
+    o[0] = rp[c];
+    o[nesp] = ip[c];
+  }
+}
+
+// Adds the chunks in order and applies optdiel's epilogue: eps1 = delta + C * rpart, eps2 = C * ipart, with
+// delta = 1 for the components whose bit is set in delta_mask (rtype 1) and 0 otherwise.
+// Fortran layout dielf(nesp, 3, ncomp): (j, c, comp) at j + nesp*(c + 3*comp).
+__global__ void lorentz_final_kernel(const double* __restrict__ part, int nchunk, int ncomp, unsigned delta_mask,
+                                     double caux, double e0, double ef, int nesp, double* __restrict__ dielf) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ncomp * nesp) return;
+  const int comp = e / nesp, j = e % nesp;
+  double rpart = 0.0, ipart = 0.0;
+  for (int ch = 0; ch < nchunk; ++ch) {
+    const double* o = part + ((size_t)ch * ncomp + comp) * 2 * nesp + j;
+    rpart += o[0];
+    ipart += o[nesp];
+  }
+  const double delta = (delta_mask >> comp) & 1u ? 1.0 : 0.0;
   double* d = dielf + (size_t)comp * 3 * nesp + j;
-  d[0] = elux;
+  d[0] = omega_of(e0, ef, nesp, j);
   d[nesp] = delta + rpart * caux;
   d[2 * nesp] = ipart * caux;
 }
@@ -184,9 +244,9 @@ __global__ void renorm_kernel(const double* __restrict__ Ws, int nesp, int renor
   }
 }
 
-__global__ void optprops_kernel(const double* __restrict__ dielf, int nesp, double* __restrict__ props) {
+__global__ void optprops_kernel(const double* __restrict__ dielf, int nesp, int ncomp, double* __restrict__ props) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;  // e = comp * nesp + j
-  if (e >= 6 * nesp) return;
+  if (e >= ncomp * nesp) return;
   const int comp = e / nesp, j = e % nesp;
   const double* d = dielf + (size_t)comp * 3 * nesp + j;
   const double om = d[0], e1 = d[nesp], e2 = d[2 * nesp];
@@ -197,12 +257,91 @@ __global__ void optprops_kernel(const double* __restrict__ dielf, int nesp, doub
   const double hc = (double)19.746E-06f;
   const double absc = ((double)1.41421354f * om) * (1.0 / hc) * sqrt(aux - e1);
   const double eloss = e2 / ((e1 * e1) + (e2 * e2));
-  const size_t plane = (size_t)6 * nesp;
+  const size_t plane = (size_t)ncomp * nesp;
   props[0 * plane + e] = n;
   props[1 * plane + e] = kap;
   props[2 * plane + e] = refl;
   props[3 * plane + e] = absc;
   props[4 * plane + e] = eloss;
+}
+
+// The IPA transition records of spoptics (src/module_bse.F90:4969-4990; bsesolver writes the same,
+// :2317-2348) in REAL(4), column-major rec(dim, 15):
+//   kx ky kz, nocp, nocp - nv + c, nocp - nv + v, E_c - E_v, |hx|^2 |hy|^2 |hz|^2, Re(hx hy*) Re(hx hz*)
+//   Re(hy hz*), |hsp|^2 |hsm|^2
+// with c = nv+1..nv+nc and v = 1..nv the band slots of basis row I = (k, c, v) (quantumnumbers2).  key(I) is
+// column 7, the sort key of Bubblem.
+__global__ void sp_records_kernel(const double* __restrict__ kpt, const int* __restrict__ nocp,
+                                  const double* __restrict__ eig_win, const zd* __restrict__ hr, int nk, int nv,
+                                  int nc, float* __restrict__ rec, float* __restrict__ key) {
+  const long I = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long dim = (long)nk * nc * nv;
+  if (I >= dim) return;
+  const int k = (int)(I / (nc * nv)), c = (int)((I / nv) % nc), v = (int)(I % nv);
+  const int nb = nv + nc, no = nocp[k];
+  const double de = eig_win[(size_t)k * nb + nv + c] - eig_win[(size_t)k * nb + v];
+  zd h[5];
+#pragma unroll
+  for (int a = 0; a < 5; ++a) h[a] = hr[(size_t)a * dim + I];
+  auto re_prod = [](zd a, zd b) { return a.re * b.re + a.im * b.im; };  // Re(a conj(b))
+  float* r = rec + I;
+  r[0 * dim] = (float)kpt[3 * k];
+  r[1 * dim] = (float)kpt[3 * k + 1];
+  r[2 * dim] = (float)kpt[3 * k + 2];
+  r[3 * dim] = (float)no;
+  r[4 * dim] = (float)(no + c + 1);
+  r[5 * dim] = (float)(no - nv + v + 1);
+  r[6 * dim] = (float)de;
+  r[7 * dim] = (float)re_prod(h[0], h[0]);
+  r[8 * dim] = (float)re_prod(h[1], h[1]);
+  r[9 * dim] = (float)re_prod(h[2], h[2]);
+  r[10 * dim] = (float)re_prod(h[0], h[1]);
+  r[11 * dim] = (float)re_prod(h[0], h[2]);
+  r[12 * dim] = (float)re_prod(h[1], h[2]);
+  r[13 * dim] = (float)re_prod(h[3], h[3]);
+  r[14 * dim] = (float)re_prod(h[4], h[4]);
+  key[I] = (float)de;
+}
+
+constexpr int kRankThreads = 256;
+constexpr int kRankTile = 2048;
+
+// Bubblem (src/module_math.F90:287-308) is a bubble sort that swaps adjacent rows only when the upper key is
+// strictly greater: a stable ascending sort.  Row i therefore lands at
+//   rank(i) = #{j : key_j < key_i} + #{j < i : key_j == key_i}
+// (float comparisons, so -0 and +0 tie as in the reference).  Every count is exact whatever the order of
+// the additions; the keys pass through shared memory in tiles and blockIdx.y splits the j range.
+__global__ void __launch_bounds__(kRankThreads) stable_rank_kernel(const float* __restrict__ key, int n,
+                                                                   int* __restrict__ rank) {
+  __shared__ float sk[kRankTile];
+  const int i = blockIdx.x * kRankThreads + threadIdx.x;
+  const float ki = i < n ? key[i] : 0.0f;
+  const int per = (n + gridDim.y - 1) / gridDim.y;
+  const int j0 = min(n, (int)blockIdx.y * per), j1 = min(n, j0 + per);
+  int cnt = 0;
+  for (int t0 = j0; t0 < j1; t0 += kRankTile) {
+    const int nt = min(kRankTile, j1 - t0);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nt; e += kRankThreads) sk[e] = key[t0 + e];
+    __syncthreads();
+    if (i < n) {
+      const int lim = i - t0;  // tile rows below this bound come before row i
+      for (int r = 0; r < nt; ++r) {
+        const float kj = sk[r];
+        cnt += (kj < ki) | ((kj == ki) & (r < lim));
+      }
+    }
+  }
+  if (i < n && cnt) atomicAdd(&rank[i], cnt);
+}
+
+__global__ void permute_rows_kernel(const float* __restrict__ in, const int* __restrict__ rank, int n, int ncol,
+                                    float* __restrict__ out) {
+  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long)n * ncol) return;
+  const int q = (int)(e / n), i = (int)(e % n);
+  const int r = rank[i];
+  if (r >= 0 && r < n) out[(size_t)q * n + r] = in[e];
 }
 
 }  // namespace
@@ -216,20 +355,60 @@ cudaError_t launch_oscillators(const zd* A, int lda, int nev, int dim, const zd*
   return cudaGetLastError();
 }
 
-cudaError_t launch_spectrum(const double* Ws, int nrows, const double* f, double sme, double vc, int ng, double e0,
-                            double ef, int nesp, int renorm, double spinf, double* dielf, double* partial, int npart,
-                            cudaStream_t s) {
-  (void)npart;
-  avgsme_kernel<<<1, 1024, 0, s>>>(Ws, nrows, sme, f, partial); ++g_launch_count;
+namespace {
+// Row chunks of the Lorentzian sums: at least 512 rows each, and about four CTAs per SM over the photon grid.
+int lorentz_chunks(int nrows, int nesp) {
+  const int gx = (nesp + kLorOmega - 1) / kLorOmega;
+  const int want = (nrows + 2 * kLorRows - 1) / (2 * kLorRows);
+  return std::max(1, std::min(want, std::max(1, 4 * 152 / gx)));
+}
+}  // namespace
+
+size_t spectrum_partial_len(int nrows, int nesp, int ncomp) {
+  return 2 + (size_t)lorentz_chunks(nrows, nesp) * ncomp * 2 * nesp;
+}
+
+cudaError_t launch_spectrum(const double* Ws, int nrows, const double* f, int ncomp, unsigned delta_mask, double sme,
+                            double vc, int ng, double e0, double ef, int nesp, int renorm, double spinf,
+                            double* dielf, double* partial, size_t partial_len, cudaStream_t s) {
+  if ((ncomp != 5 && ncomp != 6) || nrows < 1 || nesp < 2) return cudaErrorInvalidValue;
+  if (partial_len < spectrum_partial_len(nrows, nesp, ncomp)) return cudaErrorInvalidValue;
+  const int nchunk = lorentz_chunks(nrows, nesp);
+  avgsme_kernel<<<1, 1024, 0, s>>>(Ws, nrows, sme, f, ncomp, partial); ++g_launch_count;
+  const dim3 grid((nesp + kLorOmega - 1) / kLorOmega, nchunk);
+  if (ncomp == 5)
+    lorentz_partial_kernel<5><<<grid, kLorOmega, 0, s>>>(Ws, nrows, f, partial, e0, ef, nesp, partial + 2);
+  else
+    lorentz_partial_kernel<6><<<grid, kLorOmega, 0, s>>>(Ws, nrows, f, partial, e0, ef, nesp, partial + 2);
+  ++g_launch_count;
   const double baux = (double)(float)ng * vc;  // real(ngrid product) * vc
   const double caux = (double)180.90f / (baux * 1.0);
-  lorentz_kernel<<<(6 * nesp + 127) / 128, 128, 0, s>>>(Ws, nrows, f, partial, caux, e0, ef, nesp, dielf); ++g_launch_count;
-  renorm_kernel<<<6, 256, 0, s>>>(Ws, nesp, renorm, spinf, dielf); ++g_launch_count;
+  lorentz_final_kernel<<<(ncomp * nesp + 127) / 128, 128, 0, s>>>(partial + 2, nchunk, ncomp, delta_mask, caux, e0,
+                                                                  ef, nesp, dielf); ++g_launch_count;
+  renorm_kernel<<<ncomp, 256, 0, s>>>(Ws, nesp, renorm, spinf, dielf); ++g_launch_count;
   return cudaGetLastError();
 }
 
-cudaError_t launch_optprops(const double* dielf, int nesp, double* props, cudaStream_t s) {
-  optprops_kernel<<<(6 * nesp + 255) / 256, 256, 0, s>>>(dielf, nesp, props); ++g_launch_count;
+cudaError_t launch_optprops(const double* dielf, int nesp, int ncomp, double* props, cudaStream_t s) {
+  optprops_kernel<<<(ncomp * nesp + 255) / 256, 256, 0, s>>>(dielf, nesp, ncomp, props); ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sp_records(const double* kpt, const int* nocp, const double* eig_win, const zd* hr, int nk, int nv,
+                              int nc, float* rec, float* key, int* rank, float* sorted, cudaStream_t s) {
+  const long dim = (long)nk * nc * nv;
+  if (dim < 1 || dim > (1L << 30) / 15) return cudaErrorInvalidValue;
+  const int n = (int)dim;
+  sp_records_kernel<<<(n + 255) / 256, 256, 0, s>>>(kpt, nocp, eig_win, hr, nk, nv, nc, rec, key); ++g_launch_count;
+  cudaError_t e = cudaMemsetAsync(rank, 0, sizeof(int) * n, s);
+  if (e != cudaSuccess) return e;
+  const int gx = (n + kRankThreads - 1) / kRankThreads;
+  // split the compared range so that a small sort still fills the GPU (at least one key tile per split)
+  const int gy = std::max(1, std::min((2 * 152 + gx - 1) / gx, (n + kRankTile - 1) / kRankTile));
+  stable_rank_kernel<<<dim3(gx, gy), kRankThreads, 0, s>>>(key, n, rank); ++g_launch_count;
+  e = cudaMemsetAsync(sorted, 0, sizeof(float) * 15 * n, s);
+  if (e != cudaSuccess) return e;
+  permute_rows_kernel<<<(unsigned)((15L * n + 255) / 256), 256, 0, s>>>(rec, rank, n, 15, sorted); ++g_launch_count;
   return cudaGetLastError();
 }
 

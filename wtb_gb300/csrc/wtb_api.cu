@@ -1,7 +1,7 @@
 // C ABI of libwtb_gb300 (declared in include/wtb_gpu.h): the context, the state the Fortran modules
 // kept in globals, and the entry points that stand in for eigsys, monhkhorst_pack, the module_coulomb
-// potentials, matrizelbse's build loop, slepc_solver, dielbsev/dielbsep, bsesolver, bsedielraw and
-// bseoptprop.  Everything numeric runs in the CUDA kernels of this library; host code only moves
+// potentials, matrizelbse's build loop, slepc_solver, dielbsev/dielbsep, bsesolver, bsedielraw(pol),
+// spoptics, spdielraw(pol) and bseoptprop(pol).  Everything numeric runs in the CUDA kernels of this library; host code only moves
 // arguments, checks them, and orchestrates launches on the context's stream.
 #include <cmath>
 #include <cstdlib>
@@ -922,38 +922,96 @@ int wtb_bsesolver(wtb_ctx* c, const wtb_bse_params* p, double* Ws, double* acts,
   return check_status(c);
 }
 
-int wtb_bsedielraw(wtb_ctx* c, const wtb_bse_params* p, int dimse, const double* Ws, const double* acts,
-                   double* dielf) {
+// optdiel over ncomp activity columns, then imagrenorm and the spin factor: bsedielraw, bsedielrawpol,
+// spdielraw and spdielrawpol differ only in their columns and in which of them carry rtype 1.
+static int dielraw(wtb_ctx* c, const wtb_bse_params* p, int dimse, const double* Ws, const double* acts, int ncomp,
+                   unsigned delta_mask, double* dielf) {
   if (!c) return WTB_EBADARG;
   CKR(prep_device(c));
   if (!c->have_hr) return set_err(c, WTB_ESTATE, "lattice not set (call wtb_set_hr first)");
   if (!p || dimse < 1 || !Ws || !acts || !dielf || p->numbse < 2) return set_err(c, WTB_EBADARG, "bad arguments");
   cudaError_t err = cudaSuccess;
+  const size_t plen = spectrum_partial_len(dimse, p->numbse, ncomp);
   double* dW = c->ws.get<double>("sp_W", dimse, &err);
-  double* df = c->ws.get<double>("sp_f", (size_t)6 * dimse, &err);
-  double* dd = c->ws.get<double>("sp_d", (size_t)18 * p->numbse, &err);
-  double* dp = c->ws.get<double>("sp_p", 16, &err);
+  double* df = c->ws.get<double>("sp_f", (size_t)ncomp * dimse, &err);
+  double* dd = c->ws.get<double>("sp_d", (size_t)3 * ncomp * p->numbse, &err);
+  double* dp = c->ws.get<double>("sp_p", plen, &err);
   CKC(err);
   CKC(cudaMemcpyAsync(dW, Ws, sizeof(double) * dimse, cudaMemcpyHostToDevice, c->s));
-  CKC(cudaMemcpyAsync(df, acts, sizeof(double) * 6 * dimse, cudaMemcpyHostToDevice, c->s));
+  CKC(cudaMemcpyAsync(df, acts, sizeof(double) * ncomp * dimse, cudaMemcpyHostToDevice, c->s));
   const int ng = p->ngrid[0] * p->ngrid[1] * p->ngrid[2];
-  CKC(launch_spectrum(dW, dimse, df, p->cshift, vcell3D(c->rlat_rm), ng, p->ebse0, p->ebsef, p->numbse, p->renorm,
-                      c->systype_np ? 2.0 : 1.0, dd, dp, 1, c->s));
-  CKC(cudaMemcpyAsync(dielf, dd, sizeof(double) * 18 * p->numbse, cudaMemcpyDeviceToHost, c->s));
+  CKC(launch_spectrum(dW, dimse, df, ncomp, delta_mask, p->cshift, vcell3D(c->rlat_rm), ng, p->ebse0, p->ebsef,
+                      p->numbse, p->renorm, c->systype_np ? 2.0 : 1.0, dd, dp, plen, c->s));
+  CKC(cudaMemcpyAsync(dielf, dd, sizeof(double) * 3 * ncomp * p->numbse, cudaMemcpyDeviceToHost, c->s));
   return check_status(c);
 }
 
-int wtb_bseoptprop(wtb_ctx* c, int numbse, const double* dielf, double* props) {
+int wtb_bsedielraw(wtb_ctx* c, const wtb_bse_params* p, int dimse, const double* Ws, const double* acts,
+                   double* dielf) {
+  return dielraw(c, p, dimse, Ws, acts, 6, 0x7u, dielf);  // xx yy zz rtype 1; xy xz yz rtype 0
+}
+
+int wtb_bsedielrawpol(wtb_ctx* c, const wtb_bse_params* p, int dimse, const double* Ws, const double* acts,
+                      double* dielf) {
+  return dielraw(c, p, dimse, Ws, acts, 5, 0x1Fu, dielf);  // xx yy zz sp sm, all rtype 1
+}
+
+int wtb_spdielraw(wtb_ctx* c, const wtb_bse_params* p, int dimsp, const double* esp, const double* acts,
+                  double* dielf) {
+  return dielraw(c, p, dimsp, esp, acts, 6, 0x7u, dielf);
+}
+
+int wtb_spdielrawpol(wtb_ctx* c, const wtb_bse_params* p, int dimsp, const double* esp, const double* acts,
+                     double* dielf) {
+  return dielraw(c, p, dimsp, esp, acts, 5, 0x1Fu, dielf);
+}
+
+static int optprop(wtb_ctx* c, int numbse, const double* dielf, int ncomp, double* props) {
   if (!c) return WTB_EBADARG;
   CKR(prep_device(c));
   if (numbse < 1 || !dielf || !props) return set_err(c, WTB_EBADARG, "bad arguments");
   cudaError_t err = cudaSuccess;
-  double* dd = c->ws.get<double>("op_d", (size_t)18 * numbse, &err);
-  double* dp = c->ws.get<double>("op_p", (size_t)30 * numbse, &err);
+  double* dd = c->ws.get<double>("op_d", (size_t)3 * ncomp * numbse, &err);
+  double* dp = c->ws.get<double>("op_p", (size_t)5 * ncomp * numbse, &err);
   CKC(err);
-  CKC(cudaMemcpyAsync(dd, dielf, sizeof(double) * 18 * numbse, cudaMemcpyHostToDevice, c->s));
-  CKC(launch_optprops(dd, numbse, dp, c->s));
-  CKC(cudaMemcpyAsync(props, dp, sizeof(double) * 30 * numbse, cudaMemcpyDeviceToHost, c->s));
+  CKC(cudaMemcpyAsync(dd, dielf, sizeof(double) * 3 * ncomp * numbse, cudaMemcpyHostToDevice, c->s));
+  CKC(launch_optprops(dd, numbse, ncomp, dp, c->s));
+  CKC(cudaMemcpyAsync(props, dp, sizeof(double) * 5 * ncomp * numbse, cudaMemcpyDeviceToHost, c->s));
+  return check_status(c);
+}
+
+int wtb_bseoptprop(wtb_ctx* c, int numbse, const double* dielf, double* props) {
+  return optprop(c, numbse, dielf, 6, props);
+}
+
+int wtb_bseoptproppol(wtb_ctx* c, int numbse, const double* dielf, double* props) {
+  return optprop(c, numbse, dielf, 5, props);
+}
+
+int wtb_spoptics(wtb_ctx* c, const wtb_bse_params* p, float* rec) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (!c->have_hr) return set_err(c, WTB_ESTATE, "H(R) not set (call wtb_set_hr first)");
+  if (!p || !rec) return set_err(c, WTB_EBADARG, "bad arguments");
+  if (p->ngrid[0] < 1 || p->ngrid[1] < 1 || p->ngrid[2] < 1) return set_err(c, WTB_EBADARG, "ngrid must be >= 1");
+  if (p->nc < 1 || p->nv < 1) return set_err(c, WTB_EBADARG, "nc and nv must be >= 1");
+  if (p->nv + p->nc > c->w) return set_err(c, WTB_EBADARG, "nv + nc exceeds w90basis");
+  if (p->precision < 0 || p->precision > 3 || p->op < 0 || p->op > 1)
+    return set_err(c, WTB_EBADARG, "unknown precision or operator mode");
+  const long dim = (long)p->ngrid[0] * p->ngrid[1] * p->ngrid[2] * p->nc * p->nv;
+  if (dim > (1L << 30) / 15) return set_err(c, WTB_EBADARG, "too many transitions");
+  CKR(ensure_bands_for(c, p));
+  CKR(compute_optics(c, p));
+  cudaError_t err = cudaSuccess;
+  float* raw = c->ws.get<float>("spo_raw", (size_t)15 * dim, &err);
+  float* out = c->ws.get<float>("spo_out", (size_t)15 * dim, &err);
+  float* key = c->ws.get<float>("spo_key", dim, &err);
+  int* rank = c->ws.get<int>("spo_rank", dim, &err);
+  CKC(err);
+  CKC(launch_sp_records(c->ws.get<double>("kpt", 0, &err), c->ws.get<int>("nocp", 0, &err),
+                        c->ws.get<double>("eig_win", 0, &err), c->ws.get<zd>("hrvel", 0, &err), c->nk, c->nv, c->nc,
+                        raw, key, rank, out, c->s));
+  CKC(cudaMemcpyAsync(rec, out, sizeof(float) * 15 * dim, cudaMemcpyDeviceToHost, c->s));
   return check_status(c);
 }
 

@@ -261,11 +261,19 @@ std::string tc_autotune_report();
 // ----------------------------------------------------------------------------- spectrum
 cudaError_t launch_oscillators(const zd* A, int lda, int nev, int dim, const zd* hr, double* osc /*[8][nev]*/,
                                double* partial, int npart, cudaStream_t s);
-// dielf in the Fortran layout dielf(nesp, 3, 6); props(nesp, 6, 5)
-cudaError_t launch_spectrum(const double* Ws, int nrows, const double* f /*[6][nrows]*/, double sme, double vc,
-                            int ng, double e0, double ef, int nesp, int renorm, double spinf, double* dielf,
-                            double* partial, int npart, cudaStream_t s);
-cudaError_t launch_optprops(const double* dielf, int nesp, double* props, cudaStream_t s);
+// The broadened spectrum of ncomp (5 or 6) activity columns f[ncomp][nrows]: dielf in the Fortran layout
+// dielf(nesp, 3, ncomp); delta_mask bit c set = component c has optdiel's rtype 1 (eps1 offset 1).  partial
+// holds spectrum_partial_len(nrows, nesp, ncomp) doubles.
+size_t spectrum_partial_len(int nrows, int nesp, int ncomp);
+cudaError_t launch_spectrum(const double* Ws, int nrows, const double* f, int ncomp, unsigned delta_mask, double sme,
+                            double vc, int ng, double e0, double ef, int nesp, int renorm, double spinf,
+                            double* dielf, double* partial, size_t partial_len, cudaStream_t s);
+// props(nesp, ncomp, 5) from dielf(nesp, 3, ncomp)
+cudaError_t launch_optprops(const double* dielf, int nesp, int ncomp, double* props, cudaStream_t s);
+// The IPA transition records rec(dim, 15) (REAL(4), column-major) of the bands and velocity matrix elements
+// hr[5][dim], stably sorted by transition energy into sorted; key(dim), rank(dim) and rec(dim, 15) are scratch.
+cudaError_t launch_sp_records(const double* kpt, const int* nocp, const double* eig_win, const zd* hr, int nk, int nv,
+                              int nc, float* rec, float* key, int* rank, float* sorted, cudaStream_t s);
 
 // Raises (never lowers) a kernel's dynamic shared-memory limit on the current device.  Launchers run on
 // several host threads at once (batch workers): setting the limit to each launch's own need would let one
