@@ -6,6 +6,10 @@
 !   wtb_gpu_slepc_solver  <- slepc_solver  (src/module_slepc_solver.F90:12-97)
 !   wtb_gpu_bsesolver     <- bsesolver     (src/module_bse.F90:2023-2594)
 !   wtb_gpu_bsedielraw    <- bsedielraw    (src/module_bse.F90:835-1036)
+!   wtb_gpu_bsedielrawpol <- bsedielrawpol (src/module_bse.F90:1043-1199)
+!   wtb_gpu_spoptics      <- spoptics      (src/module_bse.F90:4802-5071), records before the writes
+!   wtb_gpu_spdielraw     <- spdielraw     (src/module_bse.F90:4090-4308)
+!   wtb_gpu_spdielrawpol  <- spdielrawpol  (src/module_bse.F90:4318-4524)
 ! A non-zero status from the library is turned into the reference's behaviour: print the message
 ! (the reference's STOP text where it has one) and STOP.
 ! No Fortran compiler exists in the build image, so this file is not compiled by the project's build.
@@ -14,7 +18,8 @@ module wtb_gpu
   implicit none
   private
   public :: wtb_bse_params_t, wtb_timings_t, wtb_gpu_init, wtb_gpu_eigsys, wtb_gpu_slepc_solver, &
-            wtb_gpu_bsesolver, wtb_gpu_bsedielraw, wtb_gpu_set_hr
+            wtb_gpu_bsesolver, wtb_gpu_bsedielraw, wtb_gpu_set_hr, wtb_gpu_bsedielrawpol, &
+            wtb_gpu_spoptics, wtb_gpu_spdielraw, wtb_gpu_spdielrawpol
 
   type, bind(C) :: wtb_bse_params_t
     integer(c_int)  :: ngrid(3)
@@ -83,6 +88,33 @@ module wtb_gpu
       type(wtb_bse_params_t) :: p
       integer(c_int), value :: dimse
       real(c_double) :: ws(*), acts(*), dielf(*)
+    end function
+    integer(c_int) function c_wtb_bsedielrawpol(ctx, p, dimse, ws, acts, dielf) bind(C, name="wtb_bsedielrawpol")
+      import :: c_ptr, c_int, c_double, wtb_bse_params_t
+      type(c_ptr), value :: ctx
+      type(wtb_bse_params_t) :: p
+      integer(c_int), value :: dimse
+      real(c_double) :: ws(*), acts(*), dielf(*)
+    end function
+    integer(c_int) function c_wtb_spdielraw(ctx, p, dimsp, esp, acts, dielf) bind(C, name="wtb_spdielraw")
+      import :: c_ptr, c_int, c_double, wtb_bse_params_t
+      type(c_ptr), value :: ctx
+      type(wtb_bse_params_t) :: p
+      integer(c_int), value :: dimsp
+      real(c_double) :: esp(*), acts(*), dielf(*)
+    end function
+    integer(c_int) function c_wtb_spdielrawpol(ctx, p, dimsp, esp, acts, dielf) bind(C, name="wtb_spdielrawpol")
+      import :: c_ptr, c_int, c_double, wtb_bse_params_t
+      type(c_ptr), value :: ctx
+      type(wtb_bse_params_t) :: p
+      integer(c_int), value :: dimsp
+      real(c_double) :: esp(*), acts(*), dielf(*)
+    end function
+    integer(c_int) function c_wtb_spoptics(ctx, p, rec) bind(C, name="wtb_spoptics")
+      import :: c_ptr, c_int, c_float, wtb_bse_params_t
+      type(c_ptr), value :: ctx
+      type(wtb_bse_params_t) :: p
+      real(c_float) :: rec(*)
     end function
     integer(c_int) function c_wtb_spectrum_loss(ctx, p, dimse, nev, e, fxx, target, l, dl_de, dl_df) &
         bind(C, name="wtb_spectrum_loss")
@@ -188,6 +220,41 @@ contains
     double precision :: Ws(dimse), acts(dimse,6), dielf(p%numbse,3,6)
     call wtb_gpu_init(0)
     call check(c_wtb_bsedielraw(ctx, p, dimse, Ws, acts, dielf), 'bsedielraw')
+  end subroutine
+
+  ! acts(:,1:5) = xx yy zz sp sm (the columns of bse_opt_diel-pol.dat)
+  subroutine wtb_gpu_bsedielrawpol(p, dimse, Ws, acts, dielf)
+    type(wtb_bse_params_t) :: p
+    integer :: dimse
+    double precision :: Ws(dimse), acts(dimse,5), dielf(p%numbse,3,5)
+    call wtb_gpu_init(0)
+    call check(c_wtb_bsedielrawpol(ctx, p, dimse, Ws, acts, dielf), 'bsedielrawpol')
+  end subroutine
+
+  ! vecres(dimsp,15) of spoptics, already sorted as Bubblem(7,15,vecres,dimsp) leaves it; the caller keeps
+  ! its writes of sp_optics.dat (columns 7-13) and sp_optics-pol.dat (columns 7-10, 14-15)
+  subroutine wtb_gpu_spoptics(p, dimsp, vecres)
+    type(wtb_bse_params_t) :: p
+    integer :: dimsp
+    real :: vecres(dimsp,15)
+    call wtb_gpu_init(0)
+    call check(c_wtb_spoptics(ctx, p, vecres), 'spoptics')
+  end subroutine
+
+  subroutine wtb_gpu_spdielraw(p, dimsp, esp, acts, dielf)
+    type(wtb_bse_params_t) :: p
+    integer :: dimsp
+    double precision :: esp(dimsp), acts(dimsp,6), dielf(p%numbse,3,6)
+    call wtb_gpu_init(0)
+    call check(c_wtb_spdielraw(ctx, p, dimsp, esp, acts, dielf), 'spdielraw')
+  end subroutine
+
+  subroutine wtb_gpu_spdielrawpol(p, dimsp, esp, acts, dielf)
+    type(wtb_bse_params_t) :: p
+    integer :: dimsp
+    double precision :: esp(dimsp), acts(dimsp,5), dielf(p%numbse,3,5)
+    call wtb_gpu_init(0)
+    call check(c_wtb_spdielrawpol(ctx, p, dimsp, esp, acts, dielf), 'spdielrawpol')
   end subroutine
 
   ! gradient of L = sum_j (spinf eps2_xx(omega_j) - target_j)^2 with respect to H(R) and R_0, through the last
