@@ -187,6 +187,29 @@ int wtb_spdielraw(wtb_ctx* ctx, const wtb_bse_params* p, int dimsp, const double
 int wtb_spdielrawpol(wtb_ctx* ctx, const wtb_bse_params* p, int dimsp, const double* esp, const double* acts,
                      double* dielf);
 
+/* Replaces kpathbse (src/module_kmesh.F90:124-193), host arithmetic: the Q path of bsebnds from nks corner
+ * points ks(nks, 3) (reduced coordinates, column-major; taken in pairs (start, end) of segments) with npts
+ * points per segment: qpath(nq, 4), nq = (nks/2) npts, column 1 the normalised path coordinate, columns 2-4
+ * the Cartesian Q. */
+int wtb_kpathbse(const double* rlat1, const double* rlat2, const double* rlat3, int nks, const double* ks, int npts,
+                 double* qpath);
+
+/* Replaces the matrizelbsekq build loop of bsebnds (src/module_bse.F90:452-569, :1400-1410) for one Q-path row
+ * q4 = (path coordinate, Qx, Qy, Qz): the dense finite-Q BSE matrix over the mesh of p, conduction states on
+ * the Q-shifted mesh (monhkhorst_packq), the exchange term -V(Q,0)<c_i|v_i><v_j|c_j> for |Q| != 0.
+ * hbse(dim, dim) complex(8), full Hermitian (the reference fills the upper triangle).  dim <= 20000. */
+int wtb_bse_build_q(wtb_ctx* ctx, const wtb_bse_params* p, const double* q4, double* hbse);
+
+/* Replaces the Q loop of bsebnds (src/module_bse.F90:1206-1566, ZHEEV 'N' at :1439-1447): for each of the nq
+ * rows of qpath (as wtb_kpathbse writes it), all dim eigenvalues of the finite-Q matrix, ascending, into
+ * exk(dim, nq) (the columns of bands_bse.dat).  FP64 throughout. */
+int wtb_bsebnds(wtb_ctx* ctx, const wtb_bse_params* p, int nq, const double* qpath, double* exk);
+
+/* Replaces LAPACK ZHEEV('N', 'U', n, A, lda, W, ...) of the dense full-spectrum paths: all eigenvalues of the
+ * Hermitian n x n matrix whose upper triangle A (host, complex(8), column-major, leading dimension lda) holds,
+ * ascending, in W(n).  Householder tridiagonalisation and bisection on the device, FP64. */
+int wtb_zheev(wtb_ctx* ctx, int n, const double* A, int lda, double* W);
+
 /* Replaces bseoptprop (src/module_bse.F90:3766-3931, formulas :5075-5124): props(numbse, 6, 5) =
  * refractive index, extinction coefficient, reflectivity, absorption coefficient, energy-loss function.
  * spoptprop (:3438-3602) applies the same formulas to the spdielraw spectrum. */

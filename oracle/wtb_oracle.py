@@ -315,6 +315,92 @@ def bse_build(eigv, vec, kpt, p, rlat):
     return H
 
 
+def kpathbse(rlat, ks, npts):
+    """The Q path of bsebnds (src/module_kmesh.F90:124-193): ks (nks, 3) in reduced coordinates, taken in
+    pairs (start, end) of segments; returns qpath ((nks//2)*npts, 4) = (normalised path coordinate, Q
+    Cartesian)."""
+    b1, b2, b3 = recvec(rlat[0], rlat[1], rlat[2])
+    ks = np.asarray(ks, dtype=np.float64)
+    nks = len(ks)
+    ksaux = np.array([[k[0] * b1[d] + k[1] * b2[d] + k[2] * b3[d] for d in range(3)] for k in ks])
+    nseg = nks // 2
+    kdis = np.empty(nseg)
+    kdistot = 0.0
+    for i in range(nseg):
+        a, b = ksaux[2 * i + 1], ksaux[2 * i]
+        kdis[i] = np.sqrt((a[0] - b[0]) ** 2 + (a[1] - b[1]) ** 2 + (a[2] - b[2]) ** 2)   # distvec
+        kdistot = kdistot + kdis[i]
+    kdis = kdis / kdistot
+    q = np.empty((nseg * npts, 4))
+    kdisaux = 0.0
+    for j in range(nseg):
+        for i in range(npts):
+            r = j * npts + i
+            q[r, 0] = kdisaux + kdis[j] * float(i) / (npts - 1.0)
+            for d in range(3):
+                q[r, 1 + d] = ksaux[2 * j, d] + (ksaux[2 * j + 1, d] - ksaux[2 * j, d]) * float(i) / (npts - 1.0)
+        kdisaux = kdisaux + kdis[j]
+    return q
+
+
+def monhkhorst_packq(q, n1, n2, n3, shift, rlat):
+    """The mesh shifted by Q (src/module_kmesh.F90:281-334): q(2:4) + (b1/n1) i + (b2/n2) j + (b3/n3) l +
+    kshift, summed in that order."""
+    b1, b2, b3 = recvec(rlat[0], rlat[1], rlat[2])
+    ks = np.array([b1[d] * shift[0] + b2[d] * shift[1] + b3[d] * shift[2] for d in range(3)])
+    out = np.empty((n1 * n2 * n3, 3))
+    c = 0
+    for i in range(n1):
+        for j in range(n2):
+            for l in range(n3):
+                for d in range(3):
+                    out[c, d] = (q[1 + d] + (b1[d] / float(n1)) * float(i) + (b2[d] / float(n2)) * float(j)
+                                 + (b3[d] / float(n3)) * float(l) + ks[d])
+                c += 1
+    return out
+
+
+def bse_build_q(eigv, vec, eigvq, vecq, kpt, q, p, rlat):
+    """Dense finite-Q hbse (matrizelbsekq, src/module_bse.F90:452-569, build loop :1400-1410): conduction
+    states from the Q-shifted mesh (eigvq, vecq), valence states from the plain mesh.  Direct term as at
+    Q = 0, V(k_i, k_j) <c_i|c_j> <v_i|v_j>, with the diagonal (E_c - E_v) + V(k_i, k_i); for |Q| != 0 the
+    exchange term - V(Q, 0) <c_i|v_i> <v_j|c_j> on every element (diagonal included).  The reference fills
+    the upper triangle; the Hermitian mirror is returned here."""
+    nk = len(kpt)
+    kk, cs, vs = basis(nk, p.nc, p.nv)
+    V = coulomb_table(kpt, kpt, p, rlat)
+    Cv = vecq[kk, cs]
+    Vv = vec[kk, vs]
+    gc = np.conj(Cv) @ Cv.T
+    gv = np.conj(Vv) @ Vv.T
+    H = V[kk[:, None], kk[None, :]] * gc * gv
+    dE = eigvq[kk, cs] - eigv[kk, vs]
+    d = np.arange(len(kk))
+    H[d, d] = dE + V[kk, kk]
+    modq = np.sqrt(q[1] ** 2 + q[2] ** 2 + q[3] ** 2)
+    if modq != 0.0:
+        vq = coulomb_table(np.array([q[1:4]]), np.zeros((1, 3)), p, rlat)[0, 0]
+        u = np.einsum("iw,iw->i", np.conj(Cv), Vv)           # vcv = <c_i|v_i>; vvc = <v_j|c_j> = conj(u_j)
+        H = H - vq * np.outer(u, np.conj(u))
+    iu = np.triu_indices(len(kk), 1)
+    H[iu[1], iu[0]] = np.conj(H[iu[0], iu[1]])
+    return H
+
+
+def bsebnds(sysm, p, qpath):
+    """The Q loop of bsebnds (src/module_bse.F90:1206-1566): for each row of qpath, bands on the Q-shifted
+    mesh, the matrizelbsekq matrix and all its eigenvalues (ZHEEV 'N', ascending).  Returns exk (dim, nq)."""
+    kpt = monhkhorst_pack(p.ngrid[0], p.ngrid[1], p.ngrid[2], p.mshift, sysm.rlat)
+    eigv, vec, nocpk = bands(sysm, p, kpt)
+    out = np.empty((p.dim, len(qpath)))
+    for i, q in enumerate(qpath):
+        kq = monhkhorst_packq(q, p.ngrid[0], p.ngrid[1], p.ngrid[2], p.mshift, sysm.rlat)
+        eigvq, vecq, _ = bands(sysm, p, kq)
+        H = bse_build_q(eigv, vec, eigvq, vecq, kpt, q, p, sysm.rlat)
+        out[:, i] = np.linalg.eigvalsh(H)
+    return out
+
+
 def bse_matvec_factored(x, eigv, vec, kpt, p, rlat, V=None):
     """Matrix-free y = H x through V(k,k') and the orbital factorisation; same operator as bse_build."""
     nk = len(kpt)

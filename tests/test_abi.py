@@ -40,6 +40,22 @@ def test_host_only_entry_points(built):
     np.testing.assert_allclose(k, ref, rtol=0, atol=1e-14)
 
 
+def test_kpathbse_host_entry_matches_oracle(built):
+    """kpathbse is host arithmetic: the library's Q path equals the oracle's bit for bit."""
+    import numpy as np
+
+    from oracle import wtb_oracle as O
+    from wtb_gb300 import api, synthetic
+
+    rlat = synthetic.hex_lattice()
+    ks = np.array([[0.0, 0.0, 0.0], [0.5, 0.0, 0.0], [0.5, 0.0, 0.0], [1 / 3, 1 / 3, 0.0], [1 / 3, 1 / 3, 0.0],
+                   [0.0, 0.0, 0.0]])
+    q = api.kpathbse(rlat[0], rlat[1], rlat[2], ks, 7)
+    ref = O.kpathbse(rlat, ks, 7)
+    assert q.shape == ref.shape == (21, 4)
+    assert np.array_equal(q, ref)
+
+
 def test_no_device_is_an_error_not_a_fallback(built):
     torch = pytest.importorskip("torch")
     if torch.cuda.is_available():

@@ -229,6 +229,48 @@ def test_spoptics_records(small):
     assert np.all(rec[:, 10] ** 2 <= rec[:, 7] * rec[:, 8] * (1 + 1e-5) + 1e-12)   # Cauchy-Schwarz
 
 
+def test_q_mesh_and_path():
+    """monhkhorst_packq at Q = 0 is the plain mesh bit for bit (0 + t == t); the path coordinate runs 0..1
+    over the segments and each segment interpolates its corner points."""
+    rlat = S.hex_lattice()
+    kp = O.monhkhorst_pack(4, 3, 1, (0.1, 0.0, 0.0), rlat)
+    kq = O.monhkhorst_packq(np.zeros(4), 4, 3, 1, (0.1, 0.0, 0.0), rlat)
+    assert np.array_equal(kp, kq)
+    q = np.array([0.0, 0.01, -0.02, 0.0])
+    np.testing.assert_allclose(O.monhkhorst_packq(q, 4, 3, 1, (0.1, 0.0, 0.0), rlat), kp + q[1:], atol=1e-15)
+    ks = np.array([[0.0, 0.0, 0.0], [0.5, 0.0, 0.0], [0.5, 0.0, 0.0], [1 / 3, 1 / 3, 0.0]])
+    path = O.kpathbse(rlat, ks, 5)
+    assert path.shape == (10, 4)
+    assert path[0, 0] == 0.0 and abs(path[-1, 0] - 1.0) < 1e-15
+    assert np.all(np.diff(path[:5, 0]) > 0) and np.all(np.diff(path[5:, 0]) > 0)
+    b1, b2, b3 = O.recvec(rlat[0], rlat[1], rlat[2])
+    np.testing.assert_allclose(path[4, 1:], 0.5 * b1, atol=1e-15)
+    np.testing.assert_allclose(path[9, 1:], (b1 + b2) / 3.0, atol=1e-15)
+
+
+def test_finite_q_matrix(small):
+    """matrizelbsekq: at Q = 0 the plain BSE matrix; for Q != 0 Hermitian, and the exchange part is the rank-1
+    term -V(Q,0) u u^H (its one nonzero eigenvalue is -V(Q,0)|u|^2 > 0 for an attractive V)."""
+    sysm, p, kpt, eigv, vec, nocp = small
+    H0 = O.bse_build(eigv, vec, kpt, p, sysm.rlat)
+    Hq0 = O.bse_build_q(eigv, vec, eigv, vec, kpt, np.zeros(4), p, sysm.rlat)
+    assert np.array_equal(H0, Hq0)
+    q = np.array([0.1, 0.05, 0.02, 0.0])
+    kq = O.monhkhorst_packq(q, *p.ngrid, p.mshift, sysm.rlat)
+    eq, vq, _ = O.bands(sysm, p, kq)
+    Hq = O.bse_build_q(eigv, vec, eq, vq, kpt, q, p, sysm.rlat)
+    np.testing.assert_allclose(Hq, np.conj(Hq.T), atol=1e-14)
+    # the direct part alone: the same shifted conduction states with |Q| read as zero
+    Hd = O.bse_build_q(eigv, vec, eq, vq, kpt, np.array([0.1, 0.0, 0.0, 0.0]), p, sysm.rlat)
+    ev = np.linalg.eigvalsh(Hq - Hd)
+    vQ = O.coulomb_table(np.array([q[1:]]), np.zeros((1, 3)), p, sysm.rlat)[0, 0]
+    assert vQ < 0
+    assert np.sum(np.abs(ev) > 1e-12 * np.abs(ev).max()) == 1
+    kk, cs, vs = O.basis(len(kpt), p.nc, p.nv)
+    u = np.einsum("iw,iw->i", np.conj(vq[kk, cs]), vec[kk, vs])
+    np.testing.assert_allclose(ev.max(), -vQ * np.vdot(u, u).real, rtol=1e-10)
+
+
 @pytest.mark.parametrize("name", ["hex8_6x6", "hex8_24x24"])
 def test_golden_fixtures(name):
     from tests.golden.make_golden import input_digest

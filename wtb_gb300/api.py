@@ -92,6 +92,10 @@ def _load():
         "wtb_spdielrawpol": [P, C.POINTER(CParams), C.c_int, dp, dp, dp],
         "wtb_bseoptproppol": [P, C.c_int, dp, dp],
         "wtb_spoptics": [P, C.POINTER(CParams), C.POINTER(C.c_float)],
+        "wtb_kpathbse": [dp, dp, dp, C.c_int, dp, C.c_int, dp],
+        "wtb_bse_build_q": [P, C.POINTER(CParams), dp, dp],
+        "wtb_bsebnds": [P, C.POINTER(CParams), C.c_int, dp, dp],
+        "wtb_zheev": [P, C.c_int, dp, C.c_int, dp],
         "wtb_bse_backward": [P, C.POINTER(CParams), dp, dp, dp, dp, dp, C.POINTER(CTimings)],
         "wtb_spectrum_loss": [P, C.POINTER(CParams), C.c_int, C.c_int, dp, dp, dp, dp, dp, dp],
         "wtb_batch_create": [C.POINTER(P), C.c_int, C.c_int],
@@ -183,6 +187,19 @@ def monhkhorst_pack(n1, n2, n3, shift, rlat1, rlat2, rlat3):
     return np.ascontiguousarray(kpt)
 
 
+def kpathbse(rlat1, rlat2, rlat3, ks, npts):
+    """kpathbse (src/module_kmesh.F90:124-193): ks (nks, 3) reduced corner points in (start, end) pairs; returns
+    qpath ((nks//2)*npts, 4) = (path coordinate, Qx, Qy, Qz)."""
+    ks = np.asfortranarray(np.asarray(ks, dtype=np.float64))
+    nq = (ks.shape[0] // 2) * int(npts)
+    q = np.zeros((nq, 4), order="F")
+    r = _lib.wtb_kpathbse(_dp(_f64(rlat1)), _dp(_f64(rlat2)), _dp(_f64(rlat3)), ks.shape[0], _dp(ks), int(npts),
+                          _dp(q))
+    if r:
+        raise WTBError(r, "kpathbse: bad arguments")
+    return np.ascontiguousarray(q)
+
+
 def eigsys(nthreads, scs, exc, nocp, ffactor, kx, ky, kz, w90basis, nvec, rlat, rvec, hopmatrices, ihopmatrices,
            efermi):
     """eigsys (src/module_hamiltonian.F90:200-320), same argument list; H(R) arrays with the reference's
@@ -270,6 +287,31 @@ class Context:
         cp = cparams(p, precision=precision)
         self._chk(_lib.wtb_bse_build(self._h, C.byref(cp), _dp(H)), "wtb_bse_build")
         return H
+
+    def bse_build_q(self, p: BSEParams, q4):
+        """The finite-Q BSE matrix (matrizelbsekq) for one Q-path row q4 = (path coordinate, Qx, Qy, Qz)."""
+        dim = p.dim
+        H = np.zeros((dim, dim), dtype=np.complex128, order="F")
+        cp = cparams(p)
+        self._chk(_lib.wtb_bse_build_q(self._h, C.byref(cp), _dp(_f64(q4)), _dp(H)), "wtb_bse_build_q")
+        return H
+
+    def bsebnds(self, p: BSEParams, qpath):
+        """bsebnds: all finite-Q exciton energies, exk (dim, nq), for the rows of qpath."""
+        qpath = np.asfortranarray(np.asarray(qpath, dtype=np.float64))
+        nq = qpath.shape[0]
+        exk = np.zeros((p.dim, nq), order="F")
+        cp = cparams(p)
+        self._chk(_lib.wtb_bsebnds(self._h, C.byref(cp), nq, _dp(qpath), _dp(exk)), "wtb_bsebnds")
+        return exk
+
+    def zheev(self, A):
+        """ZHEEV('N', 'U'): all eigenvalues (ascending) of the Hermitian matrix held in A's upper triangle."""
+        A = np.asfortranarray(np.asarray(A, dtype=np.complex128))
+        n = A.shape[0]
+        W = np.zeros(n)
+        self._chk(_lib.wtb_zheev(self._h, n, A.ctypes.data_as(C.POINTER(C.c_double)), n, _dp(W)), "wtb_zheev")
+        return W
 
     def bse_matvec(self, p: BSEParams, X, precision="fp64", op="matfree"):
         """Y = H X for the bands of the last set-up (X: dim x ncol complex)."""

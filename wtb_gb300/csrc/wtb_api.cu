@@ -89,10 +89,8 @@ double vcell3D(const double* r) {
   return std::fabs(vx0 * r[6] + vx1 * r[7] + vx2 * r[8]);
 }
 
-// Gamma-anchored mesh, i outer, j, l inner; reciprocal vectors with single-precision pi
-// (monhkhorst_pack + recvec, src/module_kmesh.F90:338-407).  kpt row-major nk x 3.
-void mp_mesh(int n1, int n2, int n3, const double* shift, const double* a1, const double* a2, const double* a3,
-             double* kpt) {
+// Reciprocal vectors with single-precision pi (recvec, src/module_kmesh.F90:391-407).
+void recvec(const double* a1, const double* a2, const double* a3, double* b1, double* b2, double* b3) {
   auto cross = [](const double* u, const double* v, double* o) {
     o[0] = u[1] * v[2] - u[2] * v[1];
     o[1] = u[2] * v[0] - u[0] * v[2];
@@ -105,20 +103,33 @@ void mp_mesh(int n1, int n2, int n3, const double* shift, const double* a1, cons
   const double vol = std::fabs(a1[0] * v23[0] + a1[1] * v23[1] + a1[2] * v23[2]);
   const double pi32 = (double)3.14159274101257324f;
   const double f = (2.0 * pi32) / vol;
-  double b1[3], b2[3], b3[3], ks[3];
   for (int d = 0; d < 3; ++d) {
     b1[d] = f * v23[d];
     b2[d] = f * v31[d];
     b3[d] = f * v12[d];
   }
+}
+
+// Gamma-anchored mesh, i outer, j, l inner (monhkhorst_pack, src/module_kmesh.F90:338-386); with q, the mesh
+// shifted by Q = q(2:4) of a Q-path row, summed in monhkhorst_packq's order (src/module_kmesh.F90:281-334).
+// kpt row-major nk x 3.
+void mp_mesh(int n1, int n2, int n3, const double* shift, const double* a1, const double* a2, const double* a3,
+             double* kpt, const double* q = nullptr) {
+  double b1[3], b2[3], b3[3], ks[3];
+  recvec(a1, a2, a3, b1, b2, b3);
   for (int d = 0; d < 3; ++d) ks[d] = b1[d] * shift[0] + b2[d] * shift[1] + b3[d] * shift[2];
   long cnt = 0;
   for (int i = 0; i < n1; ++i)
     for (int j = 0; j < n2; ++j)
       for (int l = 0; l < n3; ++l) {
-        for (int d = 0; d < 3; ++d)
-          kpt[3 * cnt + d] = (b1[d] / (double)n1) * (double)i + (b2[d] / (double)n2) * (double)j +
-                             (b3[d] / (double)n3) * (double)l + ks[d];
+        for (int d = 0; d < 3; ++d) {
+          if (q)
+            kpt[3 * cnt + d] = q[1 + d] + (b1[d] / (double)n1) * (double)i + (b2[d] / (double)n2) * (double)j +
+                               (b3[d] / (double)n3) * (double)l + ks[d];
+          else
+            kpt[3 * cnt + d] = (b1[d] / (double)n1) * (double)i + (b2[d] / (double)n2) * (double)j +
+                               (b3[d] / (double)n3) * (double)l + ks[d];
+        }
         ++cnt;
       }
 }
@@ -785,6 +796,163 @@ int wtb_bse_build(wtb_ctx* c, const wtb_bse_params* p, double* hbse) {
   }
   CKC(cudaGetLastError());
   if (hbse) CKC(cudaMemcpyAsync(hbse, staging, sizeof(zd) * dim * dim, cudaMemcpyDeviceToHost, c->s));
+  return check_status(c);
+}
+
+int wtb_kpathbse(const double* rlat1, const double* rlat2, const double* rlat3, int nks, const double* ks, int npts,
+                 double* qpath) {
+  if (!rlat1 || !rlat2 || !rlat3 || !ks || !qpath || nks < 2 || npts < 2) return WTB_EBADARG;
+  double b1[3], b2[3], b3[3];
+  recvec(rlat1, rlat2, rlat3, b1, b2, b3);
+  std::vector<double> ksaux((size_t)nks * 3);
+  for (int i = 0; i < nks; ++i)
+    for (int d = 0; d < 3; ++d)
+      ksaux[3 * i + d] = ks[i] * b1[d] + ks[i + nks] * b2[d] + ks[i + 2 * nks] * b3[d];
+  const int nseg = nks / 2, nq = nseg * npts;
+  std::vector<double> kdis(nseg);
+  double kdistot = 0.0;
+  for (int i = 0; i < nseg; ++i) {
+    const double* a = &ksaux[3 * (2 * i + 1)];
+    const double* b = &ksaux[3 * (2 * i)];
+    kdis[i] = std::sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]));
+    kdistot = kdistot + kdis[i];
+  }
+  for (int i = 0; i < nseg; ++i) kdis[i] = kdis[i] / kdistot;
+  double kdisaux = 0.0;
+  for (int j = 0; j < nseg; ++j) {
+    for (int i = 0; i < npts; ++i) {
+      const int r = j * npts + i;
+      const double ti = (double)i, tn = (double)npts - 1.0;
+      qpath[r] = kdisaux + kdis[j] * ti / tn;
+      for (int d = 0; d < 3; ++d)
+        qpath[r + (size_t)nq * (1 + d)] =
+            ksaux[3 * (2 * j) + d] + (ksaux[3 * (2 * j + 1) + d] - ksaux[3 * (2 * j) + d]) * ti / tn;
+    }
+    kdisaux = kdisaux + kdis[j];
+  }
+  return WTB_OK;
+}
+
+// The finite-Q matrix of one Q-path row q4 = (path coordinate, Q) into the row-major dim x dim "HQ" buffer:
+// bands on the Q-shifted mesh, the merged window, the direct build over V (leading dimension ldv) and, for
+// |Q| != 0, the exchange term.  The plain-mesh bands must be current.
+static int build_q_matrix(wtb_ctx* c, const wtb_bse_params* p, const double* q4, const double* V, int ldv, zd** Hout) {
+  const int nk = c->nk, nv = c->nv, nc = c->nc, w = c->w, nb = nv + nc;
+  const long dim = (long)nk * nc * nv;
+  cudaError_t err = cudaSuccess;
+  std::vector<double> kq((size_t)nk * 3);
+  mp_mesh(p->ngrid[0], p->ngrid[1], p->ngrid[2], p->mshift, c->rlat_rm, c->rlat_rm + 3, c->rlat_rm + 6, kq.data(), q4);
+  double* dkq = c->ws.get<double>("kptq", (size_t)nk * 3 + 6, &err);
+  double* eq_all = c->ws.get<double>("eigq_all", (size_t)nk * w, &err);
+  zd* vq_all = c->ws.get<zd>("vecq_all", (size_t)nk * w * w, &err);
+  double* eq_win = c->ws.get<double>("eigq_win", (size_t)nk * nb, &err);
+  zd* vq_win = c->ws.get<zd>("vecq_win", (size_t)nk * nb * w, &err);
+  int* nocpq = c->ws.get<int>("nocpq", nk, &err);
+  double* em = c->ws.get<double>("eigm_win", (size_t)nk * nb, &err);
+  zd* vm = c->ws.get<zd>("vecm_win", (size_t)nk * nb * w, &err);
+  double* dE = c->ws.get<double>("dEq", dim, &err);
+  zd* u = c->ws.get<zd>("xq_u", dim, &err);
+  double* dvq = c->ws.get<double>("xq_v", 2, &err);
+  zd* H = c->ws.get<zd>("HQ", (size_t)dim * dim, &err);
+  CKC(err);
+  // the Q point and the origin follow the mesh in the same buffer (coulomb pair V(Q, 0))
+  for (int d = 0; d < 3; ++d) {
+    kq.push_back(q4[1 + d]);
+  }
+  for (int d = 0; d < 3; ++d) kq.push_back(0.0);
+  CKC(cudaMemcpyAsync(dkq, kq.data(), sizeof(double) * kq.size(), cudaMemcpyHostToDevice, c->s));
+  CKC(launch_hk_eig(c->ws.get<zd>("hr", 0, &err), c->ws.get<int>("rvec", 0, &err), c->ws.get<int>("ndegen", 0, &err),
+                    c->nR, w, c->ws.get<double>("rlat", 0, &err), c->efermi, c->scs, dkq, nk, nv, nc, eq_all, vq_all,
+                    eq_win, vq_win, nocpq, c->st, c->s, false));
+  CKC(launch_merge_windows(c->ws.get<double>("eig_win", 0, &err), c->ws.get<zd>("vec_win", 0, &err), eq_win, vq_win,
+                           nk, nv, nc, w, em, vm, c->s));
+  CKC(launch_transition_energies(em, nk, nv, nc, dE, c->s));
+  CKC(launch_bse_build<double>(vm, dE, V, ldv, nk, nv, nc, w, H, c->s));
+  const double modq = std::sqrt(q4[1] * q4[1] + q4[2] * q4[2] + q4[3] * q4[3]);  // modvecq
+  if (modq != 0.0) {
+    CKC(launch_coulomb(coul_of(c, p), dkq + (size_t)nk * 3, 1, dkq + (size_t)nk * 3 + 3, 1, dvq, 1, c->s));
+    CKC(launch_exchange(vm, nk, nv, nc, w, dvq, u, H, c->s));
+  }
+  *Hout = H;
+  return WTB_OK;
+}
+
+static int check_q_params(wtb_ctx* c, const wtb_bse_params* p) {
+  if (!c->have_hr) return set_err(c, WTB_ESTATE, "H(R) not set (call wtb_set_hr first)");
+  CKR(validate_params(c, p));
+  if (p->nv + p->nc > c->w) return set_err(c, WTB_EBADARG, "nv + nc exceeds w90basis");
+  const long dim = (long)p->ngrid[0] * p->ngrid[1] * p->ngrid[2] * p->nc * p->nv;
+  if (dim > 20000) return set_err(c, WTB_EBADARG, "the finite-Q dense solve holds dim^2 complex entries: dim <= 20000");
+  return WTB_OK;
+}
+
+int wtb_bse_build_q(wtb_ctx* c, const wtb_bse_params* p, const double* q4, double* hbse) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (!p || !q4) return set_err(c, WTB_EBADARG, "bad arguments");
+  CKR(check_q_params(c, p));
+  CKR(stage_mesh(c, p));
+  CKR(enqueue_bands(c, false));
+  const int nk = c->nk;
+  const long dim = (long)nk * c->nc * c->nv;
+  cudaError_t err = cudaSuccess;
+  const int Kpad = (nk + 63) / 64 * 64;
+  double* V = c->ws.get<double>("V", (size_t)((nk + 127) / 128 * 128) * Kpad, &err, true);
+  CKC(err);
+  CKR(coulomb_table_into(c, p, V, Kpad));
+  zd* H = nullptr;
+  CKR(build_q_matrix(c, p, q4, V, Kpad, &H));
+  if (hbse) {
+    zd* staging = c->ws.get<zd>("Hout", (size_t)dim * dim, &err);
+    CKC(err);
+    conj_convert_kernel<double><<<(unsigned)((dim * dim + 255) / 256), 256, 0, c->s>>>(H, dim * dim, staging); ++g_launch_count;
+    CKC(cudaGetLastError());
+    CKC(cudaMemcpyAsync(hbse, staging, sizeof(zd) * dim * dim, cudaMemcpyDeviceToHost, c->s));
+  }
+  return check_status(c);
+}
+
+int wtb_bsebnds(wtb_ctx* c, const wtb_bse_params* p, int nq, const double* qpath, double* exk) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (!p || nq < 1 || !qpath || !exk) return set_err(c, WTB_EBADARG, "bad arguments");
+  CKR(check_q_params(c, p));
+  CKR(stage_mesh(c, p));
+  CKR(enqueue_bands(c, false));
+  const int nk = c->nk;
+  const long dim = (long)nk * c->nc * c->nv;
+  cudaError_t err = cudaSuccess;
+  const int Kpad = (nk + 63) / 64 * 64;
+  double* V = c->ws.get<double>("V", (size_t)((nk + 127) / 128 * 128) * Kpad, &err, true);
+  void* scratch = c->ws.get<zd>("deig_scratch", (dense_eig_scratch((int)dim) + sizeof(zd) - 1) / sizeof(zd), &err);
+  double* W = c->ws.get<double>("deig_W", dim, &err);
+  CKC(err);
+  CKR(coulomb_table_into(c, p, V, Kpad));
+  for (int i = 0; i < nq; ++i) {
+    const double q4[4] = {qpath[i], qpath[i + nq], qpath[i + 2 * (size_t)nq], qpath[i + 3 * (size_t)nq]};
+    zd* H = nullptr;
+    CKR(build_q_matrix(c, p, q4, V, Kpad, &H));
+    // H is row-major Hermitian, i.e. conj(H) column-major: the same eigenvalues
+    CKC(launch_dense_eigvals(H, (int)dim, (int)dim, false, W, scratch, c->s));
+    CKC(cudaMemcpyAsync(exk + (size_t)i * dim, W, sizeof(double) * dim, cudaMemcpyDeviceToHost, c->s));
+    CKR(check_status(c));
+  }
+  c->have_solve = false;
+  return check_status(c);
+}
+
+int wtb_zheev(wtb_ctx* c, int n, const double* A, int lda, double* W) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (n < 1 || lda < n || !A || !W) return set_err(c, WTB_EBADARG, "bad matrix size");
+  cudaError_t err = cudaSuccess;
+  zd* dA = c->ws.get<zd>("zh_A", (size_t)n * n, &err);
+  void* scratch = c->ws.get<zd>("deig_scratch", (dense_eig_scratch(n) + sizeof(zd) - 1) / sizeof(zd), &err);
+  double* dW = c->ws.get<double>("deig_W", n, &err);
+  CKC(err);
+  CKC(cudaMemcpy2DAsync(dA, sizeof(zd) * n, A, sizeof(zd) * lda, sizeof(zd) * n, n, cudaMemcpyHostToDevice, c->s));
+  CKC(launch_dense_eigvals(dA, n, n, true, dW, scratch, c->s));
+  CKC(cudaMemcpyAsync(W, dW, sizeof(double) * n, cudaMemcpyDeviceToHost, c->s));
   return check_status(c);
 }
 

@@ -275,6 +275,23 @@ cudaError_t launch_optprops(const double* dielf, int nesp, int ncomp, double* pr
 cudaError_t launch_sp_records(const double* kpt, const int* nocp, const double* eig_win, const zd* hr, int nk, int nv,
                               int nc, float* rec, float* key, int* rank, float* sorted, cudaStream_t s);
 
+// ----------------------------------------------------------------------------- finite-Q BSE
+// Merged band window of the finite-Q basis: valence slots from the plain mesh, conduction slots from the
+// Q-shifted mesh (eig (nk, nb), vec (nk, nb, w)).
+cudaError_t launch_merge_windows(const double* eig_k, const zd* vec_k, const double* eig_q, const zd* vec_q, int nk,
+                                 int nv, int nc, int w, double* eig_m, zd* vec_m, cudaStream_t s);
+// Exchange term of matrizelbsekq on the row-major dense H: H -= V(Q,0) u u^H, u_i = <c_i|v_i> (u: dim scratch).
+cudaError_t launch_exchange(const zd* vec_m, int nk, int nv, int nc, int w, const double* vq, zd* u, zd* H,
+                            cudaStream_t s);
+
+// ----------------------------------------------------------------------------- dense Hermitian eigenvalues
+// All eigenvalues (ascending) of the n x n Hermitian A (column-major, leading dimension lda; destroyed: its
+// strictly lower part ends holding the Householder vectors).  upper_only: only the upper triangle holds the
+// matrix (ZHEEV 'U'); it is mirrored first.  scratch: dense_eig_scratch(n) bytes, 16-byte aligned.
+constexpr int kDenseEigChunks = 16;
+size_t dense_eig_scratch(int n);
+cudaError_t launch_dense_eigvals(zd* A, int n, int lda, bool upper_only, double* W, void* scratch, cudaStream_t s);
+
 // Raises (never lowers) a kernel's dynamic shared-memory limit on the current device.  Launchers run on
 // several host threads at once (batch workers): setting the limit to each launch's own need would let one
 // thread lower it under another thread's larger launch.
