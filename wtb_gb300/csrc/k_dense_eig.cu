@@ -3,15 +3,14 @@
 //
 // 1. Householder tridiagonalisation A = Q T Q^H in FP64, the unblocked zhetd2 sequence (lower form): for
 //    column j, the reflector H = I - tau v v^H of zlarfg annihilates A(j+2:n, j); x = tau A22 v;
-//    w = x - (tau/2)(x^H v) v; A22 -= v w^H + w v^H.  A is kept in full storage (both triangles updated), so
-//    the matrix-vector product reads columns with coalesced loads.  Three launches per column: the product
-//    over row blocks x column chunks (every CTA forms the reflector itself from column j, so no launch is
-//    spent on it), a one-CTA reduction of the chunks with the w correction, and the rank-2 update.  Each
-//    column reads the trailing block twice and writes it once: 16 n^3 bytes in all (HBM-bound; the block
-//    falls into L2 once it is below ~100 MB).
+//    w = x - (tau/2)(x^H v) v; A22 -= v w^H + w v^H, on the lower triangle only.  Four launches per column:
+//    the reflector (one CTA), the Hermitian product by 64 x 64 lower tiles (each off-diagonal tile staged
+//    in shared memory serves A v and A^H v), the fixed-order sum of the tile partials with the x^H v dots,
+//    and the rank-2 update of the lower tiles.  On this GPU the FP64 pipe, not HBM, bounds both: 8 FMAs per
+//    stored element and column, 8/3 n^3 FMAs in all.
 // 2. Eigenvalues of the real symmetric tridiagonal T by bisection on Sturm counts (dstebz's method), as
-//    32-point multisection with one warp per eigenvalue index, the count with LAPACK's pivot guard pivmin,
-//    to the FP64 resolution of the Gershgorin interval.  Backward stable: |lambda - lambda_exact| <~ n eps ||A||.
+//    multisection with a few lanes per eigenvalue index where n alone would leave SMs idle, the count with
+//    LAPACK's pivot guard pivmin, to the FP64 resolution of the Gershgorin interval.  Backward stable: |lambda - lambda_exact| <~ n eps ||A||.
 #include <cfloat>
 
 #include "wtb_internal.h"
@@ -20,8 +19,25 @@ namespace wtb {
 
 namespace {
 
-constexpr int kHvRows = 128;   // rows per CTA of the product
-constexpr int kH2Tile = 32;    // rank-2 update tile (32 x 32, 256 threads x 4 elements)
+// Tile edge of the Hermitian product and the rank-2 update: 64 while the trailing block gives at least three
+// tiles per SM, then 32, then 16 (the late columns would otherwise run on a handful of CTAs).
+constexpr int kMinTiles = 3 * 152;
+inline int pick_tile(int m) {
+  auto tiles = [m](int t) { const long nt = (m + t - 1) / t; return nt * (nt + 1) / 2; };
+  if (tiles(64) >= kMinTiles) return 64;
+  if (tiles(32) >= kMinTiles) return 32;
+  return 16;
+}
+// partial-sum buffer: (tiles per column) x m entries, largest over the three tile sizes (from m = 4096 on the
+// tile is always 64)
+inline size_t p_capacity(int n) {
+  size_t cap = (size_t)((n + 63) / 64) * n;
+  for (int m = 1; m < std::min(n, 4096); ++m) {
+    const int t = pick_tile(m);
+    cap = std::max(cap, (size_t)((m + t - 1) / t) * m);
+  }
+  return cap;
+}
 
 // zlarfg for x = A(j+1:n, j): returns tau, beta and the scale 1/(alpha - beta) applied to x(2:m).
 struct Reflector {
@@ -48,108 +64,219 @@ __device__ Reflector make_reflector(zd alpha, double xnorm2) {
   return r;
 }
 
-// Block-wide sum of one double (blockDim.x a multiple of 32, <= 1024).
-__device__ double block_sum(double v, double* red) {
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  __syncthreads();
-  if (lane == 0) red[warp] = v;
-  __syncthreads();
-  double t = 0.0;
-  for (int i = 0; i < nw; ++i) t += red[i];
-  return t;
+// Tile (R, C), R >= C, of the lower triangle of an nT x nT tile grid from the linear index b.
+__device__ __forceinline__ void lower_tile(int b, int* R, int* C) {
+  int r = (int)((sqrtf(8.0f * (float)b + 1.0f) - 1.0f) * 0.5f);  // FP32 guess, corrected exactly below
+  while ((r + 1) * (r + 2) / 2 <= b) ++r;
+  while (r * (r + 1) / 2 > b) --r;
+  *R = r;
+  *C = b - r * (r + 1) / 2;
 }
 
-// Partial products p[chunk][r] = sum_{c in chunk} A22(r, c) v(c) with A22 = A(j+1:n, j+1:n), v the reflector
-// of column j.  Every CTA forms the reflector from column j; CTA (0, 0) records tau, e(j) and v.
-__global__ void __launch_bounds__(kHvRows) tri_hemv_kernel(const zd* __restrict__ A, int n, int lda, int j,
-                                                           zd* __restrict__ vout, zd* __restrict__ tau_out,
-                                                           double* __restrict__ e_out, zd* __restrict__ part) {
-  __shared__ double red[32];
-  __shared__ zd vs[kHvRows];
+// zlarfg on column j (one CTA): v(0) = 1, v(1:) = x(1:) / (alpha - beta), stored in v and below the
+// subdiagonal of column j; tau(j), e(j) = beta.
+__global__ void __launch_bounds__(256) tri_reflector_kernel(zd* __restrict__ A, int n, int lda, int j,
+                                                            zd* __restrict__ v, zd* __restrict__ tau_out,
+                                                            double* __restrict__ e_out) {
+  __shared__ double red[8];
+  __shared__ zd s_scale;
+  __shared__ int s_skip;
   const int m = n - j - 1;
-  const zd* x = A + (size_t)j * lda + j + 1;
+  zd* x = A + (size_t)j * lda + j + 1;
   double s2 = 0.0;
-  for (int i = 1 + threadIdx.x; i < m; i += blockDim.x) s2 += x[i].re * x[i].re + x[i].im * x[i].im;
-  s2 = block_sum(s2, red);
-  const Reflector R = make_reflector(x[0], s2);
-  const bool first = blockIdx.x == 0 && blockIdx.y == 0;
-  if (first && threadIdx.x == 0) {
+  for (int i = 1 + threadIdx.x; i < m; i += blockDim.x) s2 = fma(x[i].re, x[i].re, fma(x[i].im, x[i].im, s2));
+  for (int o = 16; o > 0; o >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s2;
+  __syncthreads();
+  // the scalar FP64 work (sqrt, divisions) on one thread: every warp repeating it would queue on the FP64 pipe
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    const Reflector R = make_reflector(x[0], t);
     tau_out[j] = R.tau;
     e_out[j] = R.beta;
+    s_scale = R.scale;
+    s_skip = R.tau.re == 0.0 && R.tau.im == 0.0;
   }
-  if (R.tau.re == 0.0 && R.tau.im == 0.0) return;
-  if (first)
-    for (int i = threadIdx.x; i < m; i += blockDim.x) vout[i] = i == 0 ? mk<double>(1.0, 0.0) : cmul(x[i], R.scale);
-  const int nchunk = gridDim.y;
-  const int per = (m + nchunk - 1) / nchunk;
-  const int c0 = min(m, (int)blockIdx.y * per), c1 = min(m, c0 + per);
-  const int r = blockIdx.x * kHvRows + threadIdx.x;
-  zd acc = mk<double>(0.0, 0.0);
-  const zd* a22 = A + (size_t)(j + 1) * lda + j + 1;
-  for (int t0 = c0; t0 < c1; t0 += kHvRows) {
-    const int nt = min(kHvRows, c1 - t0);
-    __syncthreads();
-    if (threadIdx.x < nt) {
-      const int c = t0 + threadIdx.x;
-      vs[threadIdx.x] = c == 0 ? mk<double>(1.0, 0.0) : cmul(x[c], R.scale);
-    }
-    __syncthreads();
-    if (r < m)
-      for (int q = 0; q < nt; ++q) cfma(acc, a22[(size_t)(t0 + q) * lda + r], vs[q]);
-  }
-  if (r < m) part[(size_t)blockIdx.y * m + r] = acc;
-}
-
-// w = tau p - (tau/2)(tau p)^H v v, one CTA.
-__global__ void __launch_bounds__(1024) tri_w_kernel(const zd* __restrict__ part, int nchunk, int m,
-                                                     const zd* __restrict__ tau_p, int j,
-                                                     const zd* __restrict__ v, zd* __restrict__ w) {
-  __shared__ double red[32];
-  const zd tau = tau_p[j];
-  if (tau.re == 0.0 && tau.im == 0.0) return;
-  double dre = 0.0, dim_ = 0.0;
-  for (int r = threadIdx.x; r < m; r += blockDim.x) {
-    zd p = mk<double>(0.0, 0.0);
-    for (int c = 0; c < nchunk; ++c) p = cadd(p, part[(size_t)c * m + r]);
-    const zd xr = cmul(tau, p);
-    w[r] = xr;
-    const zd t = cmulc(xr, v[r]);  // conj(x_r) v_r
-    dre += t.re;
-    dim_ += t.im;
-  }
-  dre = block_sum(dre, red);
-  dim_ = block_sum(dim_, red);
-  const zd alpha = cscale(cmul(tau, mk<double>(dre, dim_)), -0.5);
   __syncthreads();
-  for (int r = threadIdx.x; r < m; r += blockDim.x) w[r] = cadd(w[r], cmul(alpha, v[r]));
+  if (s_skip) return;
+  const zd sc = s_scale;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    const zd vi = i == 0 ? mk<double>(1.0, 0.0) : cmul(x[i], sc);
+    v[i] = vi;
+    x[i] = vi;
+  }
 }
 
-// A22 -= v w^H + w v^H (full storage); CTA (0, 0) also stores v below the subdiagonal of column j.
-__global__ void __launch_bounds__(256) tri_her2_kernel(zd* __restrict__ A, int n, int lda, int j,
-                                                       const zd* __restrict__ tau_p, const zd* __restrict__ v,
-                                                       const zd* __restrict__ w) {
+// Lower-triangle Hermitian product p = A22 v by tiles: an off-diagonal tile (R, C) gives A_RC v_C to the rows of
+// block R and A_RC^H v_R to the rows of block C; a diagonal tile supplies its upper half from the lower one.
+// Each (row block, other block) pair receives exactly one partial, P[other][row], so the sum over the tile
+// index is a fixed-order reduction.  4T threads: row (or column) t % T, a quarter of the tile's width each.
+template <int T>
+__global__ void __launch_bounds__(4 * T) tri_symv_kernel(const zd* __restrict__ A, int n, int lda, int j,
+                                                         const zd* __restrict__ v, const zd* __restrict__ tau_p,
+                                                         zd* __restrict__ P) {
+  constexpr int kSymTile = T, kTPad = T + 1;  // padded column stride: conflict-free transposed reads
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  zd* tile = reinterpret_cast<zd*>(smem_raw);    // [kSymTile][kTPad], column-major
+  zd* vR = tile + kSymTile * kTPad;
+  zd* vC = vR + kSymTile;
+  zd* ry = vC + kSymTile;                         // [4][kSymTile]
+  zd* rz = ry + 4 * kSymTile;                     // [4][kSymTile]
   const zd tau = tau_p[j];
   if (tau.re == 0.0 && tau.im == 0.0) return;
   const int m = n - j - 1;
-  const int r = blockIdx.x * kH2Tile + (threadIdx.x & 31);
-  const int cb = blockIdx.y * kH2Tile + (threadIdx.x >> 5) * 4;
-  zd* a22 = A + (size_t)(j + 1) * lda + j + 1;
-  if (blockIdx.x == 0 && blockIdx.y == 0)
-    for (int i = threadIdx.x; i < m; i += blockDim.x) A[(size_t)j * lda + j + 1 + i] = v[i];
+  int R, C;
+  lower_tile(blockIdx.x, &R, &C);
+  const int r0 = R * kSymTile, c0 = C * kSymTile;
+  const zd* a22 = A + (size_t)(j + 1) * lda + j + 1;
+  for (int e = threadIdx.x; e < kSymTile * kSymTile; e += blockDim.x) {
+    const int ii = e % kSymTile, jj = e / kSymTile;
+    const int r = r0 + ii, c = c0 + jj;
+    tile[jj * kTPad + ii] = (r < m && c < m) ? a22[(size_t)c * lda + r] : mk<double>(0.0, 0.0);
+  }
+  if (threadIdx.x < kSymTile) {
+    const int r = r0 + threadIdx.x, c = c0 + threadIdx.x;
+    vR[threadIdx.x] = r < m ? v[r] : mk<double>(0.0, 0.0);
+    vC[threadIdx.x] = c < m ? v[c] : mk<double>(0.0, 0.0);
+  }
+  __syncthreads();
+  const bool diag = R == C;
+  const int i = threadIdx.x % kSymTile, g = threadIdx.x / kSymTile;
+  const int q0 = g * (kSymTile / 4), q1 = q0 + kSymTile / 4;
+  zd acc = mk<double>(0.0, 0.0);
+  if (!diag) {
+    for (int jj = q0; jj < q1; ++jj) cfma(acc, tile[jj * kTPad + i], vC[jj]);
+  } else {
+    for (int jj = q0; jj < q1; ++jj) {
+      zd a;
+      if (jj < i)
+        a = tile[jj * kTPad + i];
+      else if (jj == i)
+        a = mk<double>(tile[i * kTPad + i].re, 0.0);
+      else
+        a = cconj(tile[i * kTPad + jj]);
+      cfma(acc, a, vC[jj]);
+    }
+  }
+  ry[g * kSymTile + i] = acc;
+  if (!diag) {
+    zd accz = mk<double>(0.0, 0.0);
+    for (int ii = q0; ii < q1; ++ii) cfmac(accz, tile[i * kTPad + ii], vR[ii]);  // conj(A(ii, i)) vR(ii)
+    rz[g * kSymTile + i] = accz;
+  }
+  __syncthreads();
+  if (threadIdx.x < kSymTile) {
+    const int t = threadIdx.x;
+    zd y = ry[t];
+    for (int q = 1; q < 4; ++q) y = cadd(y, ry[q * kSymTile + t]);
+    if (r0 + t < m) P[(size_t)C * m + r0 + t] = y;
+  } else if (!diag && threadIdx.x < 2 * kSymTile) {
+    const int t = threadIdx.x - kSymTile;
+    zd z = rz[t];
+    for (int q = 1; q < 4; ++q) z = cadd(z, rz[q * kSymTile + t]);
+    if (c0 + t < m) P[(size_t)R * m + c0 + t] = z;
+  }
+}
+
+// x = tau sum_k P[k] and the partial dots conj(x) . v of each CTA.  256 threads = 32 rows x 8 slices of the
+// tile index (slice l sums k = l, l+8, ...), the slices then added in order: a fixed-order sum whose serial
+// chain is nT/8 loads long.
+constexpr int kXRows = 32;
+__global__ void __launch_bounds__(256) tri_x_kernel(const zd* __restrict__ P, int nT, int m,
+                                                    const zd* __restrict__ tau_p, int j, const zd* __restrict__ v,
+                                                    zd* __restrict__ x, zd* __restrict__ dots) {
+  __shared__ zd red[8][kXRows];
+  const zd tau = tau_p[j];
+  if (tau.re == 0.0 && tau.im == 0.0) return;
+  const int rr = threadIdx.x % kXRows, sl = threadIdx.x / kXRows;
+  const int r = blockIdx.x * kXRows + rr;
+  zd p = mk<double>(0.0, 0.0);
+  if (r < m)
+    for (int k = sl; k < nT; k += 8) p = cadd(p, P[(size_t)k * m + r]);
+  red[sl][rr] = p;
+  __syncthreads();
+  if (threadIdx.x < kXRows) {
+    zd t = mk<double>(0.0, 0.0);
+    if (r < m) {
+      zd q = red[0][rr];
+      for (int l = 1; l < 8; ++l) q = cadd(q, red[l][rr]);
+      const zd xr = cmul(tau, q);
+      x[r] = xr;
+      t = cmulc(xr, v[r]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      t.re += __shfl_xor_sync(0xffffffffu, t.re, o);
+      t.im += __shfl_xor_sync(0xffffffffu, t.im, o);
+    }
+    if (threadIdx.x == 0) dots[blockIdx.x] = t;
+  }
+}
+
+// alpha = -(tau/2) sum_b dots[b], the sum split over one warp's lanes in a fixed order.
+__device__ __forceinline__ zd her2_alpha(const zd* __restrict__ dots, int ndots, zd tau) {
+  zd d = mk<double>(0.0, 0.0);
+  for (int b = threadIdx.x; b < ndots; b += 32) d = cadd(d, dots[b]);
+  for (int o = 16; o > 0; o >>= 1) {
+    d.re += __shfl_xor_sync(0xffffffffu, d.re, o);
+    d.im += __shfl_xor_sync(0xffffffffu, d.im, o);
+  }
+  return cscale(cmul(tau, d), -0.5);
+}
+
+// A22 -= v w^H + w v^H on the lower triangle, w = x - (tau/2)(x^H v) v formed per tile from x and the dots.
+// Eight FP64 FMAs per element.
+template <int T>
+__global__ void __launch_bounds__(4 * T) tri_her2l_kernel(zd* __restrict__ A, int n, int lda, int j,
+                                                          const zd* __restrict__ tau_p, const zd* __restrict__ v,
+                                                          const zd* __restrict__ x, const zd* __restrict__ dots,
+                                                          int ndots) {
+  constexpr int kSymTile = T;
+  __shared__ zd s_alpha;
+  __shared__ zd vR[kSymTile], wR[kSymTile], vC[kSymTile], wC[kSymTile];
+  const zd tau = tau_p[j];
+  if (tau.re == 0.0 && tau.im == 0.0) return;
+  const int m = n - j - 1;
+  int R, C;
+  lower_tile(blockIdx.x, &R, &C);
+  const int r0 = R * kSymTile, c0 = C * kSymTile;
+  if (threadIdx.x < 32) {
+    const zd al = her2_alpha(dots, ndots, tau);
+    if (threadIdx.x == 0) s_alpha = al;
+  }
+  __syncthreads();
+  const zd alpha = s_alpha;
+  if (threadIdx.x < kSymTile) {
+    const int t = threadIdx.x, r = r0 + t, c = c0 + t;
+    const zd z = mk<double>(0.0, 0.0);
+    const zd vr = r < m ? v[r] : z, vc = c < m ? v[c] : z;
+    vR[t] = vr;
+    vC[t] = vc;
+    wR[t] = r < m ? cadd(x[r], cmul(alpha, vr)) : z;
+    wC[t] = c < m ? cadd(x[c], cmul(alpha, vc)) : z;
+  }
+  __syncthreads();
+  const int i = threadIdx.x % kSymTile, g = threadIdx.x / kSymTile;
+  const int r = r0 + i;
   if (r >= m) return;
-  const zd vr = v[r], wr = w[r];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int c = cb + q;
+  zd* a22 = A + (size_t)(j + 1) * lda + j + 1;
+  const zd vr = vR[i], wr = wR[i];
+  const int q0 = g * (kSymTile / 4);
+  const int q1 = min(q0 + kSymTile / 4, R == C ? i + 1 : kSymTile);
+  for (int jj = q0; jj < q1; ++jj) {
+    const int c = c0 + jj;
     if (c >= m) break;
-    const zd vc = v[c], wc = w[c];
+    const zd vc = vC[jj], wc = wC[jj];
     zd a = a22[(size_t)c * lda + r];
     // a -= vr conj(wc) + wr conj(vc)
-    const zd t1 = mk<double>(vr.re * wc.re + vr.im * wc.im, vr.im * wc.re - vr.re * wc.im);
-    const zd t2 = mk<double>(wr.re * vc.re + wr.im * vc.im, wr.im * vc.re - wr.re * vc.im);
-    a.re -= t1.re + t2.re;
-    a.im -= t1.im + t2.im;
+    a.re = fma(-vr.re, wc.re, a.re);
+    a.re = fma(-vr.im, wc.im, a.re);
+    a.re = fma(-wr.re, vc.re, a.re);
+    a.re = fma(-wr.im, vc.im, a.re);
+    a.im = fma(-vr.im, wc.re, a.im);
+    a.im = fma(vr.re, wc.im, a.im);
+    a.im = fma(-wr.im, vc.re, a.im);
+    a.im = fma(wr.re, vc.im, a.im);
     a22[(size_t)c * lda + r] = a;
   }
 }
@@ -223,52 +350,90 @@ __global__ void e2_kernel(const double* __restrict__ e, int n, double* __restric
   if (i < n - 1) e2[i] = e[i] * e[i];
 }
 
-// The k-th smallest eigenvalue (k = 0..n-1), one warp per k: multisection, the 32 lanes evaluating the Sturm
-// count at 32 interior points of the bracket, which shrinks 33-fold per pass (about 11 passes from the
-// Gershgorin interval to the resolution 2 eps max|bound|).  The count is non-decreasing in x, so the points
-// with count <= k form a prefix of the lanes and the new bracket is read off the ballot.
+// The k-th smallest eigenvalue (k = 0..n-1) by multisection with L lanes per k (L a power of two <= 32): the L
+// lanes evaluate the Sturm count at L interior points of the bracket, which shrinks (L+1)-fold per pass, to the
+// resolution 2 eps max|bound|.  The count is non-decreasing in x, so the points with count <= k form a prefix
+// of the group and the new bracket is read off the ballot.  L = 1 is plain bisection (the fewest counts); the
+// launcher raises L only until the GPU's SMs all have work, since a Sturm count (one FP64 division per row)
+// queues on the SM's FP64 pipe.  Groups that have converged idle until their whole warp has.
 __global__ void __launch_bounds__(128) tri_multisect_kernel(const double* __restrict__ d,
                                                             const double* __restrict__ e2, int n,
                                                             const double* __restrict__ bounds,
-                                                            double* __restrict__ W) {
-  const int k = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+                                                            double* __restrict__ W, int L) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
-  if (k >= n) return;  // whole warps
+  const int k = tid / L, g = lane % L, base = lane - g;
+  const unsigned gmask = L == 32 ? 0xffffffffu : (((1u << L) - 1u) << base);
   double lo = bounds[0], hi = bounds[1];
   const double pivmin = bounds[2];
   const double tol = 2.0 * DBL_EPSILON * fmax(fabs(lo), fabs(hi)) + pivmin;
-  for (int it = 0; it < 64 && hi - lo > tol; ++it) {
-    const double h = (hi - lo) / 33.0;
-    const double x = lo + h * (double)(lane + 1);
-    const int cnt = sturm_count(d, e2, n, x, pivmin);
-    const unsigned below = __ballot_sync(0xffffffffu, cnt <= k);
-    const int nlo = __popc(below);
-    const double xlo = __shfl_sync(0xffffffffu, x, max(nlo - 1, 0));
-    const double xhi = __shfl_sync(0xffffffffu, x, min(nlo, 31));
-    const double nl = nlo > 0 ? xlo : lo;
-    const double nh = nlo < 32 ? xhi : hi;
-    if (nl == lo && nh == hi) break;  // no representable progress
-    lo = nl;
-    hi = nh;
+  bool done = k >= n;
+  for (int it = 0; it < 256; ++it) {
+    if (!done && !(hi - lo > tol)) done = true;
+    if (__all_sync(0xffffffffu, done)) break;
+    const double h = (hi - lo) / (double)(L + 1);
+    const double x = lo + h * (double)(g + 1);
+    const int cnt = done ? 0 : sturm_count(d, e2, n, x, pivmin);
+    const unsigned bal = __ballot_sync(0xffffffffu, !done && cnt <= k);
+    const int nlo = __popc(bal & gmask);
+    const double xlo = __shfl_sync(0xffffffffu, x, base + max(nlo - 1, 0));
+    const double xhi = __shfl_sync(0xffffffffu, x, base + min(nlo, L - 1));
+    if (!done) {
+      const double nl = nlo > 0 ? xlo : lo;
+      const double nh = nlo < L ? xhi : hi;
+      if (nl == lo && nh == hi)
+        done = true;  // no representable progress
+      else {
+        lo = nl;
+        hi = nh;
+      }
+    }
   }
-  if (lane == 0) W[k] = 0.5 * (lo + hi);
+  if (k < n && g == 0) W[k] = 0.5 * (lo + hi);
 }
 
 }  // namespace
 
 size_t dense_eig_scratch(int n) {
-  // v, w, tau (n each, complex), part (chunks x n complex), e, d, e2 (n doubles), bounds
-  return sizeof(zd) * ((size_t)3 * n + (size_t)kDenseEigChunks * n) + sizeof(double) * ((size_t)3 * n + 4);
+  // v, x, tau (n each), dots, P, all complex; e, d, e2 (n doubles); bounds
+  const size_t nd = (size_t)(n + kXRows - 1) / kXRows;
+  return sizeof(zd) * ((size_t)3 * n + nd + p_capacity(n)) + sizeof(double) * ((size_t)3 * n + 4);
+}
+
+cudaError_t dense_eig_prepare() {
+  cudaError_t err = raise_smem_limit(reinterpret_cast<const void*>(tri_symv_kernel<64>), sizeof(zd) * (64 * 65 + 640));
+  if (err == cudaSuccess)
+    err = raise_smem_limit(reinterpret_cast<const void*>(tri_symv_kernel<32>), sizeof(zd) * (32 * 33 + 320));
+  if (err == cudaSuccess)
+    err = raise_smem_limit(reinterpret_cast<const void*>(tri_symv_kernel<16>), sizeof(zd) * (16 * 17 + 160));
+  return err;
+}
+
+template <int T>
+static cudaError_t tri_step(zd* A, int n, int lda, int j, zd* v, zd* tau, zd* P, zd* x, zd* dots, cudaStream_t s) {
+  const int m = n - j - 1;
+  const int nT = (m + T - 1) / T;
+  const unsigned ntiles = (unsigned)((long)nT * (nT + 1) / 2);
+  const int nd = (m + kXRows - 1) / kXRows;
+  const size_t smem = sizeof(zd) * ((size_t)T * (T + 1) + 10 * T);
+  cudaError_t err = raise_smem_limit(reinterpret_cast<const void*>(tri_symv_kernel<T>), smem);
+  if (err != cudaSuccess) return err;
+  tri_symv_kernel<T><<<ntiles, 4 * T, smem, s>>>(A, n, lda, j, v, tau, P); ++g_launch_count;
+  tri_x_kernel<<<nd, 8 * kXRows, 0, s>>>(P, nT, m, tau, j, v, x, dots); ++g_launch_count;
+  tri_her2l_kernel<T><<<ntiles, 4 * T, 0, s>>>(A, n, lda, j, tau, v, x, dots, nd); ++g_launch_count;
+  return cudaSuccess;
 }
 
 cudaError_t launch_dense_eigvals(zd* A, int n, int lda, bool upper_only, double* W, void* scratch,
                                  cudaStream_t s) {
   if (n < 1 || lda < n) return cudaErrorInvalidValue;
+  const size_t ndmax = (size_t)(n + kXRows - 1) / kXRows;
   zd* v = reinterpret_cast<zd*>(scratch);
-  zd* w = v + n;
-  zd* tau = w + n;
-  zd* part = tau + n;
-  double* e = reinterpret_cast<double*>(part + (size_t)kDenseEigChunks * n);
+  zd* x = v + n;
+  zd* tau = x + n;
+  zd* dots = tau + n;
+  zd* P = dots + ndmax;
+  double* e = reinterpret_cast<double*>(P + p_capacity(n));
   double* d = e + n;
   double* e2 = d + n;
   double* bounds = e2 + n;
@@ -277,19 +442,20 @@ cudaError_t launch_dense_eigvals(zd* A, int n, int lda, bool upper_only, double*
   }
   for (int j = 0; j + 1 < n; ++j) {
     const int m = n - j - 1;
-    const int rb = (m + kHvRows - 1) / kHvRows;
-    // about four CTAs per SM, at least 64 columns per chunk
-    const int nchunk = std::max(1, std::min({kDenseEigChunks, (m + 63) / 64, std::max(1, 4 * 152 / rb)}));
-    tri_hemv_kernel<<<dim3(rb, nchunk), kHvRows, 0, s>>>(A, n, lda, j, v, tau, e, part); ++g_launch_count;
-    tri_w_kernel<<<1, 1024, 0, s>>>(part, nchunk, m, tau, j, v, w); ++g_launch_count;
-    const int tb = (m + kH2Tile - 1) / kH2Tile;
-    tri_her2_kernel<<<dim3(tb, tb), 256, 0, s>>>(A, n, lda, j, tau, v, w); ++g_launch_count;
+    tri_reflector_kernel<<<1, 256, 0, s>>>(A, n, lda, j, v, tau, e); ++g_launch_count;
+    const int T = pick_tile(m);
+    const cudaError_t err = T == 64 ? tri_step<64>(A, n, lda, j, v, tau, P, x, dots, s)
+                            : T == 32 ? tri_step<32>(A, n, lda, j, v, tau, P, x, dots, s)
+                                      : tri_step<16>(A, n, lda, j, v, tau, P, x, dots, s);
+    if (err != cudaSuccess) return err;
   }
   tri_finish_kernel<<<1, 1024, 0, s>>>(A, n, lda, d, e, bounds); ++g_launch_count;
   if (n > 1) {
     e2_kernel<<<(n + 255) / 256, 256, 0, s>>>(e, n, e2); ++g_launch_count;
   }
-  tri_multisect_kernel<<<(unsigned)(((long)n * 32 + 127) / 128), 128, 0, s>>>(d, e2, n, bounds, W); ++g_launch_count;
+  int L = 1;  // about two warps per SM
+  while (L < 32 && (long)n * L < 152L * 64) L *= 2;
+  tri_multisect_kernel<<<(unsigned)(((long)n * L + 127) / 128), 128, 0, s>>>(d, e2, n, bounds, W, L); ++g_launch_count;
   return cudaGetLastError();
 }
 

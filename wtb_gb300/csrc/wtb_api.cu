@@ -928,16 +928,45 @@ int wtb_bsebnds(wtb_ctx* c, const wtb_bse_params* p, int nq, const double* qpath
   double* W = c->ws.get<double>("deig_W", dim, &err);
   CKC(err);
   CKR(coulomb_table_into(c, p, V, Kpad));
-  for (int i = 0; i < nq; ++i) {
+  CKC(dense_eig_prepare());
+  // the eigenvalue sequence (4 launches per column) is captured once and replayed for every Q: same buffers
+  cudaGraphExec_t ge = nullptr;
+  zd* Hcap = nullptr;
+  int rc = WTB_OK;
+  for (int i = 0; i < nq && rc == WTB_OK; ++i) {
     const double q4[4] = {qpath[i], qpath[i + nq], qpath[i + 2 * (size_t)nq], qpath[i + 3 * (size_t)nq]};
     zd* H = nullptr;
-    CKR(build_q_matrix(c, p, q4, V, Kpad, &H));
-    // H is row-major Hermitian, i.e. conj(H) column-major: the same eigenvalues
-    CKC(launch_dense_eigvals(H, (int)dim, (int)dim, false, W, scratch, c->s));
-    CKC(cudaMemcpyAsync(exk + (size_t)i * dim, W, sizeof(double) * dim, cudaMemcpyDeviceToHost, c->s));
-    CKR(check_status(c));
+    rc = build_q_matrix(c, p, q4, V, Kpad, &H);
+    if (rc != WTB_OK) break;
+    if (!ge || H != Hcap) {
+      if (ge) cudaGraphExecDestroy(ge);
+      ge = nullptr;
+      cudaGraph_t graph = nullptr;
+      cudaError_t e1 = cudaStreamBeginCapture(c->s, cudaStreamCaptureModeThreadLocal);
+      // H is row-major Hermitian, i.e. conj(H) column-major: the same eigenvalues
+      cudaError_t e2 = e1 == cudaSuccess ? launch_dense_eigvals(H, (int)dim, (int)dim, false, W, scratch, c->s) : e1;
+      cudaError_t e3 = e1 == cudaSuccess ? cudaStreamEndCapture(c->s, &graph) : e1;
+      cudaError_t e4 = (e2 == cudaSuccess && e3 == cudaSuccess) ? cudaGraphInstantiate(&ge, graph, 0) : e2;
+      if (graph) cudaGraphDestroy(graph);
+      const cudaError_t e = e2 != cudaSuccess ? e2 : e3 != cudaSuccess ? e3 : e4;
+      if (e != cudaSuccess) {
+        rc = set_err(c, WTB_ECUDA, std::string("dense eigenvalue graph: ") + cudaGetErrorString(e));
+        break;
+      }
+      Hcap = H;
+    }
+    cudaError_t e = cudaGraphLaunch(ge, c->s);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(exk + (size_t)i * dim, W, sizeof(double) * dim, cudaMemcpyDeviceToHost, c->s);
+    if (e != cudaSuccess) {
+      rc = set_err(c, WTB_ECUDA, std::string("bsebnds: ") + cudaGetErrorString(e));
+      break;
+    }
+    rc = check_status(c);
   }
+  if (ge) cudaGraphExecDestroy(ge);
   c->have_solve = false;
+  if (rc != WTB_OK) return rc;
   return check_status(c);
 }
 

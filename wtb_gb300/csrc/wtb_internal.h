@@ -291,6 +291,8 @@ cudaError_t launch_exchange(const zd* vec_m, int nk, int nv, int nc, int w, cons
 constexpr int kDenseEigChunks = 16;
 size_t dense_eig_scratch(int n);
 cudaError_t launch_dense_eigvals(zd* A, int n, int lda, bool upper_only, double* W, void* scratch, cudaStream_t s);
+// Sets the kernels' shared-memory limits ahead of a stream capture of launch_dense_eigvals.
+cudaError_t dense_eig_prepare();
 
 // Raises (never lowers) a kernel's dynamic shared-memory limit on the current device.  Launchers run on
 // several host threads at once (batch workers): setting the limit to each launch's own need would let one
