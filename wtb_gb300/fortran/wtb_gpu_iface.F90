@@ -10,6 +10,7 @@
 !   wtb_gpu_spoptics      <- spoptics      (src/module_bse.F90:4802-5071), records before the writes
 !   wtb_gpu_spdielraw     <- spdielraw     (src/module_bse.F90:4090-4308)
 !   wtb_gpu_spdielrawpol  <- spdielrawpol  (src/module_bse.F90:4318-4524)
+!   wtb_gpu_bsebnds       <- the Q loop of bsebnds (src/module_bse.F90:1206-1566)
 ! A non-zero status from the library is turned into the reference's behaviour: print the message
 ! (the reference's STOP text where it has one) and STOP.
 ! No Fortran compiler exists in the build image, so this file is not compiled by the project's build.
@@ -19,7 +20,7 @@ module wtb_gpu
   private
   public :: wtb_bse_params_t, wtb_timings_t, wtb_gpu_init, wtb_gpu_eigsys, wtb_gpu_slepc_solver, &
             wtb_gpu_bsesolver, wtb_gpu_bsedielraw, wtb_gpu_set_hr, wtb_gpu_bsedielrawpol, &
-            wtb_gpu_spoptics, wtb_gpu_spdielraw, wtb_gpu_spdielrawpol
+            wtb_gpu_spoptics, wtb_gpu_spdielraw, wtb_gpu_spdielrawpol, wtb_gpu_bsebnds
 
   type, bind(C) :: wtb_bse_params_t
     integer(c_int)  :: ngrid(3)
@@ -109,6 +110,13 @@ module wtb_gpu
       type(wtb_bse_params_t) :: p
       integer(c_int), value :: dimsp
       real(c_double) :: esp(*), acts(*), dielf(*)
+    end function
+    integer(c_int) function c_wtb_bsebnds(ctx, p, nq, qpath, exk) bind(C, name="wtb_bsebnds")
+      import :: c_ptr, c_int, c_double, wtb_bse_params_t
+      type(c_ptr), value :: ctx
+      type(wtb_bse_params_t) :: p
+      integer(c_int), value :: nq
+      real(c_double) :: qpath(*), exk(*)
     end function
     integer(c_int) function c_wtb_spoptics(ctx, p, rec) bind(C, name="wtb_spoptics")
       import :: c_ptr, c_int, c_float, wtb_bse_params_t
@@ -239,6 +247,15 @@ contains
     real :: vecres(dimsp,15)
     call wtb_gpu_init(0)
     call check(c_wtb_spoptics(ctx, p, vecres), 'spoptics')
+  end subroutine
+
+  ! qauxv(nq,4) of kpathbse; exk(dimbse,nq) all eigenvalues per Q, ascending (ZHEEV 'N')
+  subroutine wtb_gpu_bsebnds(p, nq, qauxv, exk)
+    type(wtb_bse_params_t) :: p
+    integer :: nq
+    double precision :: qauxv(nq,4), exk(*)
+    call wtb_gpu_init(0)
+    call check(c_wtb_bsebnds(ctx, p, nq, qauxv, exk), 'bsebnds')
   end subroutine
 
   subroutine wtb_gpu_spdielraw(p, dimsp, esp, acts, dielf)
