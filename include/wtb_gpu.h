@@ -210,6 +210,30 @@ int wtb_bsebnds(wtb_ctx* ctx, const wtb_bse_params* p, int nq, const double* qpa
  * ascending, in W(n).  Householder tridiagonalisation and bisection on the device, FP64. */
 int wtb_zheev(wtb_ctx* ctx, int n, const double* A, int lda, double* W);
 
+/* Replaces LAPACK ZHEEV('V', 'U', n, A, lda, W, ...): all eigenvalues W(n), ascending, and the orthonormal
+ * eigenvectors Z(n, n) (complex(8), column-major, column k for W(k)) of the Hermitian matrix in A's upper
+ * triangle.  Householder tridiagonalisation, bisection, inverse iteration (near-degenerate clusters
+ * reorthogonalised) and the back-transformation on the device, FP64.  Eigenvectors carry an arbitrary phase
+ * each, as LAPACK's do. */
+int wtb_zheev_vectors(wtb_ctx* ctx, int n, const double* A, int lda, double* W, double* Z);
+
+/* Temperature run keys of bsesolvertemp (src/module_bse.F90:2649-2652). */
+typedef struct {
+  double temp;  /* K; 0 is read as 1e-8 as fermidisteh does */
+  int ta;       /* gap correction: 0 "FA" none, 1 "VE" gapcortemp, 2 "BE" gapcortemp2 (src/module_math.F90:383-403) */
+  double st, phavg;  /* their parameters */
+  int dtfull;   /* 1: xy xz yz activities computed, 0: written as zero */
+  int cpol;     /* 1: sp sm activities computed, 0: written as zero */
+} wtb_temp_params;
+
+/* Replaces bsesolvertemp (src/module_bse.F90:2649-3263) without its text files: bands with the scissor
+ * scs + tcor, the (f_v - f_c)-weighted BSE matrix of matrizelbsetemp (:575-660) as ZHEEV 'U' reads its upper
+ * triangle, ALL its dim eigenpairs (ZHEEV 'V'), and dielbseptemp's activities (:784-810) of every exciton.
+ * Outputs (each may be NULL): Ws(dim) ascending; acts(dim, 8) xx yy zz xy xz yz sp sm; HE(dim, dim)
+ * complex(8) eigenvectors; fdeh(dim) the occupation differences.  FP64; dim <= 20000. */
+int wtb_bsesolvertemp(wtb_ctx* ctx, const wtb_bse_params* p, const wtb_temp_params* tp, double* Ws, double* acts,
+                      double* HE, double* fdeh);
+
 /* Replaces bseoptprop (src/module_bse.F90:3766-3931, formulas :5075-5124): props(numbse, 6, 5) =
  * refractive index, extinction coefficient, reflectivity, absorption coefficient, energy-loss function.
  * spoptprop (:3438-3602) applies the same formulas to the spdielraw spectrum. */

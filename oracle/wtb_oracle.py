@@ -401,6 +401,62 @@ def bsebnds(sysm, p, qpath):
     return out
 
 
+KB_F32 = float(F32(8.617330350e-5))                  # kb = 8.617330350E-5 (single), src/module_math.F90:386
+
+
+def fermidisteh(ec, ev, temp):
+    """f_v - f_c, Fermi level 0; temp = 0 is read as 1E-8 (single) (src/module_math.F90:407-421)."""
+    t = float(F32(1e-8)) if temp == 0.0 else temp
+    beta = 1.0 / (KB_F32 * t)
+    with np.errstate(over="ignore"):
+        fv = 1.0 / (np.exp(np.asarray(ev) * beta) + 1.0)
+        fc = 1.0 / (np.exp(np.asarray(ec) * beta) + 1.0)
+    return fv - fc
+
+
+def gapcortemp(st, phavg, temp):
+    """Varshni-type gap correction (src/module_math.F90:383-391)."""
+    aux1 = phavg / ((2.0 * KB_F32) * temp)
+    return -st * phavg * (1.0 / np.tanh(aux1) - 1.0)
+
+
+def gapcortemp2(st, phavg, temp):
+    """Bose-Einstein gap correction (src/module_math.F90:395-403)."""
+    return -((2.0 * st) / (np.exp(phavg / temp) - 1.0))
+
+
+def bsesolvertemp(sysm, p, temp, ta="FA", st=0.0, phavg=0.0, dtfull=True, cpol=True):
+    """bsesolvertemp (src/module_bse.F90:2649-3263): bands with scs + tcor, the matrizelbsetemp matrix
+    (:575-660) completed from its upper triangle as ZHEEV 'U' reads it, E(i,j) = D(i,j) f_min(i,j) and
+    E(i,i) = dE_i + V(k_i,k_i) f_i, all eigenpairs, and dielbseptemp's activities (:784-810) of every exciton."""
+    import dataclasses
+    tcor = {"VE": lambda: gapcortemp(st, phavg, temp), "BE": lambda: gapcortemp2(st, phavg, temp)}.get(ta, lambda: 0.0)()
+    s2 = dataclasses.replace(sysm, scs=sysm.scs + tcor)
+    kpt = monhkhorst_pack(p.ngrid[0], p.ngrid[1], p.ngrid[2], p.mshift, s2.rlat)
+    eigv, vec, nocpk = bands(s2, p, kpt)
+    hx, hy, hz, hsp, hsm = optsp_all(eigv, vec, kpt, s2, p)
+    nk = len(kpt)
+    kk, cs, vs = basis(nk, p.nc, p.nv)
+    f = fermidisteh(eigv[kk, cs], eigv[kk, vs], temp)
+    D = bse_build(eigv, vec, kpt, p, s2.rlat)
+    V = coulomb_table(kpt, kpt, p, s2.rlat)
+    idx = np.arange(len(kk))
+    E = D * f[np.minimum(idx[:, None], idx[None, :])]
+    E[idx, idx] = (eigv[kk, cs] - eigv[kk, vs]) + V[kk, kk] * f
+    W, A = np.linalg.eigh(E)
+
+    def act(h1, h2):
+        s1 = A.T @ h1
+        s2_ = A.T @ (h2 * f)
+        return (s1 * np.conj(s2_)).real
+
+    z = np.zeros(len(W))
+    acts = {"xx": act(hx, hx), "yy": act(hy, hy), "zz": act(hz, hz),
+            "xy": act(hx, hy) if dtfull else z, "xz": act(hx, hz) if dtfull else z,
+            "yz": act(hy, hz) if dtfull else z, "sp": act(hsp, hsp) if cpol else z, "sm": act(hsm, hsm) if cpol else z}
+    return {"Ws": W, "A": A, "acts": acts, "fdeh": f, "E": E, "tcor": tcor}
+
+
 def bse_matvec_factored(x, eigv, vec, kpt, p, rlat, V=None):
     """Matrix-free y = H x through V(k,k') and the orbital factorisation; same operator as bse_build."""
     nk = len(kpt)

@@ -271,6 +271,35 @@ def test_finite_q_matrix(small):
     np.testing.assert_allclose(ev.max(), -vQ * np.vdot(u, u).real, rtol=1e-10)
 
 
+def test_fermi_weights_and_gap_corrections():
+    """fermidisteh: f_v - f_c = tanh(x/2) for E_v = -E_c with x = E_c/(kb T); T = 0 reads as 1e-8 K (a step);
+    the gap corrections vanish as T -> 0 and are negative above."""
+    kb = O.KB_F32
+    for T in (50.0, 300.0, 3000.0):
+        ec = np.array([0.01, 0.1, 0.75])
+        np.testing.assert_allclose(O.fermidisteh(ec, -ec, T), np.tanh(ec / (kb * T) / 2), rtol=1e-12)
+    assert np.all(O.fermidisteh(np.array([0.5, 2.0]), np.array([-0.5, -1.0]), 0.0) == 1.0)
+    assert O.fermidisteh(np.array([0.3]), np.array([0.2]), 0.0)[0] == 0.0   # both empty
+    assert abs(O.gapcortemp(2.0, 0.02, 1e-3)) < 1e-12 and O.gapcortemp(2.0, 0.02, 300.0) < 0
+    assert abs(O.gapcortemp2(0.1, 300.0, 1.0)) < 1e-12 and O.gapcortemp2(0.1, 300.0, 600.0) < 0
+
+
+def test_temperature_bse_reduces_to_full_spectrum_at_low_temperature(small):
+    """f = 1 for every transition of a 1.5 eV gap at 10 K: the temperature matrix is the plain BSE matrix and
+    its eigenvalues its full spectrum; the activities sum to sum_j f_j |h_j|^2 (completeness of A)."""
+    sysm, p, kpt, eigv, vec, nocp = small
+    r = O.bsesolvertemp(sysm, p, 10.0)
+    assert np.all(r["fdeh"] == 1.0)
+    H = O.bse_build(eigv, vec, kpt, p, sysm.rlat)
+    np.testing.assert_allclose(r["Ws"], np.linalg.eigvalsh(H), atol=1e-11)
+    hx = O.optsp_all(eigv, vec, kpt, sysm, p)[0]
+    # sum_n s_n conj(t_n) = h^T A A^H conj(h f) = h^T conj(h f) (A unitary)
+    np.testing.assert_allclose(r["acts"]["xx"].sum(), np.sum(np.abs(hx) ** 2 * r["fdeh"]), rtol=1e-10)
+    hot = O.bsesolvertemp(sysm, p, 4000.0, ta="BE", st=0.05, phavg=300.0)
+    assert hot["tcor"] < 0 and np.all(hot["fdeh"] < 1.0)
+    np.testing.assert_allclose(hot["E"], np.conj(hot["E"].T), atol=1e-15)
+
+
 @pytest.mark.parametrize("name", ["hex8_6x6", "hex8_24x24"])
 def test_golden_fixtures(name):
     from tests.golden.make_golden import input_digest

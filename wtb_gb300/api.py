@@ -50,6 +50,14 @@ class CParams(C.Structure):
                 ("maxit", C.c_int), ("block", C.c_int)]
 
 
+class CTempParams(C.Structure):
+    _fields_ = [("temp", C.c_double), ("ta", C.c_int), ("st", C.c_double), ("phavg", C.c_double),
+                ("dtfull", C.c_int), ("cpol", C.c_int)]
+
+
+TEMP_GAP_CORRECTIONS = {"FA": 0, "VE": 1, "BE": 2}
+
+
 class CSystem(C.Structure):
     _fields_ = [("w90basis", C.c_int), ("nvec", C.c_int), ("rvec", C.POINTER(C.c_int)), ("ffactor", C.POINTER(C.c_int)),
                 ("hopmatrices", C.POINTER(C.c_double)), ("ihopmatrices", C.POINTER(C.c_double)),
@@ -96,6 +104,8 @@ def _load():
         "wtb_bse_build_q": [P, C.POINTER(CParams), dp, dp],
         "wtb_bsebnds": [P, C.POINTER(CParams), C.c_int, dp, dp],
         "wtb_zheev": [P, C.c_int, dp, C.c_int, dp],
+        "wtb_zheev_vectors": [P, C.c_int, dp, C.c_int, dp, dp],
+        "wtb_bsesolvertemp": [P, C.POINTER(CParams), C.POINTER(CTempParams), dp, dp, dp, dp],
         "wtb_bse_backward": [P, C.POINTER(CParams), dp, dp, dp, dp, dp, C.POINTER(CTimings)],
         "wtb_spectrum_loss": [P, C.POINTER(CParams), C.c_int, C.c_int, dp, dp, dp, dp, dp, dp],
         "wtb_batch_create": [C.POINTER(P), C.c_int, C.c_int],
@@ -312,6 +322,35 @@ class Context:
         W = np.zeros(n)
         self._chk(_lib.wtb_zheev(self._h, n, A.ctypes.data_as(C.POINTER(C.c_double)), n, _dp(W)), "wtb_zheev")
         return W
+
+    def zheev_vectors(self, A):
+        """ZHEEV('V', 'U'): (W ascending, Z (n, n) eigenvectors in columns) of the matrix in A's upper triangle."""
+        A = np.asfortranarray(np.asarray(A, dtype=np.complex128))
+        n = A.shape[0]
+        W = np.zeros(n)
+        Z = np.zeros((n, n), dtype=np.complex128, order="F")
+        self._chk(_lib.wtb_zheev_vectors(self._h, n, A.ctypes.data_as(C.POINTER(C.c_double)), n, _dp(W),
+                                         Z.ctypes.data_as(C.POINTER(C.c_double))), "wtb_zheev_vectors")
+        return W, Z
+
+    def bsesolvertemp(self, p: BSEParams, temp, ta="FA", st=0.0, phavg=0.0, dtfull=True, cpol=True,
+                      want_vectors=False):
+        """bsesolvertemp: all dim exciton energies Ws, the activities {comp: (dim,)}, fdeh, and (optionally) HE."""
+        dim = p.dim
+        Ws = np.zeros(dim)
+        acts = np.zeros((dim, 8), order="F")
+        f = np.zeros(dim)
+        HE = np.zeros((dim, dim), dtype=np.complex128, order="F") if want_vectors else None
+        tp = CTempParams(float(temp), TEMP_GAP_CORRECTIONS[ta] if isinstance(ta, str) else int(ta), float(st),
+                         float(phavg), int(bool(dtfull)), int(bool(cpol)))
+        cp = cparams(p)
+        self._chk(_lib.wtb_bsesolvertemp(self._h, C.byref(cp), C.byref(tp), _dp(Ws), _dp(acts),
+                                         None if HE is None else HE.ctypes.data_as(C.POINTER(C.c_double)),
+                                         _dp(f)), "wtb_bsesolvertemp")
+        out = {"Ws": Ws, "acts": {c: acts[:, i].copy() for i, c in enumerate(COMPONENTS)}, "fdeh": f}
+        if want_vectors:
+            out["HE"] = HE
+        return out
 
     def bse_matvec(self, p: BSEParams, X, precision="fp64", op="matfree"):
         """Y = H X for the bands of the last set-up (X: dim x ncol complex)."""

@@ -392,6 +392,170 @@ __global__ void __launch_bounds__(128) tri_multisect_kernel(const double* __rest
   if (k < n && g == 0) W[k] = 0.5 * (lo + hi);
 }
 
+// ----------------------------------------------------------------------------- eigenvectors
+// Inverse iteration on T for every eigenvalue (dstein's method): Gaussian elimination with partial pivoting of
+// T - lambda I, three solves from a deterministic start vector, each normalised.  Eigenvalues closer than
+// 1e-7 ||T|| to their predecessor form a cluster, handled by one thread in order: later members are shifted
+// apart by 10 eps ||T|| and reorthogonalised against the earlier ones after every solve (a degenerate pair
+// then spans its eigenspace).  Outside clusters the vectors are orthogonal to eps ||T|| / gap <= 2e-9.
+// One thread per cluster start; its scratch (6 arrays of n) is interleaved across the batch's threads so the
+// row loops are coalesced.  Zt(i, k) = Zt[i * n + k] (row-major real).
+constexpr int kInvIters = 3;
+
+// deterministic start entries in [-1, 1): splitmix64 of (k, i)
+__device__ __forceinline__ double start_entry(unsigned long long k, unsigned long long i) {
+  unsigned long long z = k * 0x9E3779B97F4A7C15ull + (i + 1) * 0xD1B54A32D192ED03ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+}
+
+__global__ void __launch_bounds__(128) tri_invit_kernel(const double* __restrict__ d, const double* __restrict__ e,
+                                                        int n, const double* __restrict__ W,
+                                                        const double* __restrict__ bounds, int k0, int nb,
+                                                        double* __restrict__ work, double* __restrict__ Zt) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = k0 + t;
+  if (t >= nb || k >= n) return;
+  const double tnorm = fmax(fmax(fabs(bounds[0]), fabs(bounds[1])), DBL_MIN);
+  const double ortol = 1e-7 * tnorm;
+  if (k > 0 && W[k] - W[k - 1] < ortol) return;  // inside a cluster started by an earlier thread
+  int kend = k + 1;
+  while (kend < n && W[kend] - W[kend - 1] < ortol) ++kend;
+  const size_t st = (size_t)nb;
+  double* a = work + t;             // diagonal of U
+  double* b = a + (size_t)n * st;   // first superdiagonal of U
+  double* dd = b + (size_t)n * st;  // second superdiagonal of U
+  double* c = dd + (size_t)n * st;  // multipliers
+  double* pv = c + (size_t)n * st;  // 1 where rows i, i+1 were swapped
+  double* y = pv + (size_t)n * st;  // iterate
+#define AT(arr, i) arr[(size_t)(i) * st]
+  const double tiny = DBL_EPSILON * tnorm;
+  double lam_prev = 0.0;
+  for (int q = k; q < kend; ++q) {
+    double lam = W[q];
+    if (q > k && lam - lam_prev < 10.0 * DBL_EPSILON * tnorm) lam = lam_prev + 10.0 * DBL_EPSILON * tnorm;
+    lam_prev = lam;
+    // T - lam I = P L U
+    for (int i = 0; i < n; ++i) {
+      AT(a, i) = d[i] - lam;
+      AT(b, i) = i < n - 1 ? e[i] : 0.0;
+    }
+    for (int i = 0; i + 1 < n; ++i) {
+      const double sub = e[i], ai = AT(a, i);
+      if (fabs(ai) >= fabs(sub)) {
+        const double m = ai == 0.0 ? 0.0 : sub / ai;
+        AT(c, i) = m;
+        AT(pv, i) = 0.0;
+        AT(dd, i) = 0.0;
+        AT(a, i + 1) = AT(a, i + 1) - m * AT(b, i);
+      } else {
+        const double m = ai / sub;
+        const double a1 = AT(a, i + 1), bi = AT(b, i), b1 = i + 2 < n ? AT(b, i + 1) : 0.0;
+        AT(a, i) = sub;
+        AT(b, i) = a1;
+        AT(dd, i) = b1;
+        AT(a, i + 1) = bi - m * a1;
+        if (i + 2 < n) AT(b, i + 1) = -m * b1;
+        AT(c, i) = m;
+        AT(pv, i) = 1.0;
+      }
+    }
+    for (int i = 0; i < n; ++i)
+      if (fabs(AT(a, i)) < tiny) AT(a, i) = AT(a, i) < 0.0 ? -tiny : tiny;
+    for (int i = 0; i < n; ++i) AT(y, i) = start_entry((unsigned long long)q, (unsigned long long)i);
+    for (int it = 0; it < kInvIters; ++it) {
+      for (int i = 0; i + 1 < n; ++i) {
+        if (AT(pv, i) != 0.0) {
+          const double tmp = AT(y, i);
+          AT(y, i) = AT(y, i + 1);
+          AT(y, i + 1) = tmp;
+        }
+        AT(y, i + 1) = AT(y, i + 1) - AT(c, i) * AT(y, i);
+      }
+      for (int i = n - 1; i >= 0; --i) {
+        double r = AT(y, i);
+        if (i + 1 < n) r -= AT(b, i) * AT(y, i + 1);
+        if (i + 2 < n) r -= AT(dd, i) * AT(y, i + 2);
+        AT(y, i) = r / AT(a, i);
+      }
+      // against the cluster's earlier members, then to unit length
+      for (int p = k; p < q; ++p) {
+        double dot = 0.0;
+        for (int i = 0; i < n; ++i) dot += AT(y, i) * Zt[(size_t)i * n + p];
+        for (int i = 0; i < n; ++i) AT(y, i) -= dot * Zt[(size_t)i * n + p];
+      }
+      double mx = 0.0;
+      for (int i = 0; i < n; ++i) mx = fmax(mx, fabs(AT(y, i)));
+      const double sc = mx > 0.0 ? 1.0 / mx : 1.0;
+      double nrm2 = 0.0;
+      for (int i = 0; i < n; ++i) {
+        const double v = AT(y, i) * sc;
+        AT(y, i) = v;
+        nrm2 += v * v;
+      }
+      const double inv = 1.0 / sqrt(nrm2);
+      for (int i = 0; i < n; ++i) AT(y, i) *= inv;
+    }
+    for (int i = 0; i < n; ++i) Zt[(size_t)i * n + q] = AT(y, i);
+  }
+#undef AT
+}
+
+constexpr int kBtCols = 8;  // eigenvector columns per CTA of the back-transformation
+
+// Z = Q Zt with Q = H_0 H_1 ... H_{n-2}, H_j = I - tau_j v_j v_j^H (v_j in A(j+1:n, j), v_j(0) = 1): the
+// reflectors applied from j = n-2 down to 0 to every column.  A CTA owns 8 columns and 32 row slices (row i in
+// slice i % 32) for the whole sweep, so the columns need no synchronisation between CTAs; per reflector a
+// two-barrier reduction of v^H z.  Z(i, k) = Z[i * n + k] (row-major), conjugated at the end when the solver
+// worked on conj(H).
+__global__ void __launch_bounds__(256) tri_backtransform_kernel(const zd* __restrict__ A, int n, int lda,
+                                                                const zd* __restrict__ tau,
+                                                                const double* __restrict__ Zt, zd* __restrict__ Z,
+                                                                int conj_out) {
+  __shared__ zd red[8][kBtCols];
+  __shared__ zd dots[kBtCols];
+  const int c = threadIdx.x % kBtCols, sl = threadIdx.x / kBtCols;
+  const int k = blockIdx.x * kBtCols + c;
+  const bool kv = k < n;
+  for (int i = sl; i < n; i += 32)
+    if (kv) Z[(size_t)i * n + k] = mk<double>(Zt[(size_t)i * n + k], 0.0);
+  for (int j = n - 2; j >= 0; --j) {
+    const zd tj = tau[j];
+    if (tj.re == 0.0 && tj.im == 0.0) continue;
+    const zd* v = A + (size_t)j * lda + j + 1;  // v(i - j - 1) for rows i > j
+    const int i0 = j + 1 + (((sl - (j + 1)) % 32) + 32) % 32;
+    zd p = mk<double>(0.0, 0.0);
+    if (kv)
+      for (int i = i0; i < n; i += 32) cfmac(p, v[i - j - 1], Z[(size_t)i * n + k]);
+    for (int o = kBtCols; o < 32; o <<= 1) {
+      p.re += __shfl_xor_sync(0xffffffffu, p.re, o);
+      p.im += __shfl_xor_sync(0xffffffffu, p.im, o);
+    }
+    if ((threadIdx.x & 31) < kBtCols) red[threadIdx.x >> 5][c] = p;
+    __syncthreads();
+    if (threadIdx.x < kBtCols) {
+      zd t = red[0][threadIdx.x];
+      for (int w = 1; w < 8; ++w) t = cadd(t, red[w][threadIdx.x]);
+      dots[threadIdx.x] = cmul(tj, t);
+    }
+    __syncthreads();
+    const zd f = dots[c];
+    if (kv)
+      for (int i = i0; i < n; i += 32) {
+        zd z = Z[(size_t)i * n + k];
+        const zd vi = v[i - j - 1];
+        // z -= vi * f
+        z.re = fma(-vi.re, f.re, fma(vi.im, f.im, z.re));
+        z.im = fma(-vi.re, f.im, fma(-vi.im, f.re, z.im));
+        Z[(size_t)i * n + k] = z;
+      }
+  }
+  if (conj_out && kv)
+    for (int i = sl; i < n; i += 32) Z[(size_t)i * n + k].im = -Z[(size_t)i * n + k].im;
+}
+
 }  // namespace
 
 size_t dense_eig_scratch(int n) {
@@ -424,8 +588,23 @@ static cudaError_t tri_step(zd* A, int n, int lda, int j, zd* v, zd* tau, zd* P,
   return cudaSuccess;
 }
 
+static int invit_batch(int n) {
+  const long nb = (1L << 25) / (6L * n);  // the inverse-iteration scratch stays near 256 MB
+  return (int)std::max(1L, std::min((long)n, nb));
+}
+
+size_t dense_eigvec_scratch(int n) {
+  return sizeof(double) * ((size_t)n * n + (size_t)6 * n * invit_batch(n));
+}
+
 cudaError_t launch_dense_eigvals(zd* A, int n, int lda, bool upper_only, double* W, void* scratch,
                                  cudaStream_t s) {
+  return launch_dense_eig(A, n, lda, upper_only, W, nullptr, false, scratch, nullptr, s);
+}
+
+cudaError_t launch_dense_eig(zd* A, int n, int lda, bool upper_only, double* W, zd* Z, bool conj_vectors,
+                             void* scratch, void* vscratch, cudaStream_t s) {
+  if (Z && !vscratch) return cudaErrorInvalidValue;
   if (n < 1 || lda < n) return cudaErrorInvalidValue;
   const size_t ndmax = (size_t)(n + kXRows - 1) / kXRows;
   zd* v = reinterpret_cast<zd*>(scratch);
@@ -456,6 +635,16 @@ cudaError_t launch_dense_eigvals(zd* A, int n, int lda, bool upper_only, double*
   int L = 1;  // about two warps per SM
   while (L < 32 && (long)n * L < 152L * 64) L *= 2;
   tri_multisect_kernel<<<(unsigned)(((long)n * L + 127) / 128), 128, 0, s>>>(d, e2, n, bounds, W, L); ++g_launch_count;
+  if (Z) {
+    double* Zt = reinterpret_cast<double*>(vscratch);
+    double* work = Zt + (size_t)n * n;
+    const int nb = invit_batch(n);
+    for (int k0 = 0; k0 < n; k0 += nb) {
+      tri_invit_kernel<<<(nb + 127) / 128, 128, 0, s>>>(d, e, n, W, bounds, k0, nb, work, Zt); ++g_launch_count;
+    }
+    tri_backtransform_kernel<<<(n + kBtCols - 1) / kBtCols, 256, 0, s>>>(A, n, lda, tau, Zt, Z, conj_vectors ? 1 : 0);
+    ++g_launch_count;
+  }
   return cudaGetLastError();
 }
 

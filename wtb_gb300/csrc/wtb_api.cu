@@ -985,6 +985,101 @@ int wtb_zheev(wtb_ctx* c, int n, const double* A, int lda, double* W) {
   return check_status(c);
 }
 
+int wtb_zheev_vectors(wtb_ctx* c, int n, const double* A, int lda, double* W, double* Z) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (n < 1 || lda < n || !A || !W || !Z) return set_err(c, WTB_EBADARG, "bad matrix size");
+  cudaError_t err = cudaSuccess;
+  zd* dA = c->ws.get<zd>("zh_A", (size_t)n * n, &err);
+  zd* dZ = c->ws.get<zd>("zh_Z", (size_t)n * n, &err);
+  zd* dZc = c->ws.get<zd>("zh_Zc", (size_t)n * n, &err);
+  void* scratch = c->ws.get<zd>("deig_scratch", (dense_eig_scratch(n) + sizeof(zd) - 1) / sizeof(zd), &err);
+  void* vscratch = c->ws.get<double>("deig_vscratch", dense_eigvec_scratch(n) / sizeof(double), &err);
+  double* dW = c->ws.get<double>("deig_W", n, &err);
+  CKC(err);
+  CKC(cudaMemcpy2DAsync(dA, sizeof(zd) * n, A, sizeof(zd) * lda, sizeof(zd) * n, n, cudaMemcpyHostToDevice, c->s));
+  CKC(dense_eig_prepare());
+  CKC(launch_dense_eig(dA, n, n, true, dW, dZ, false, scratch, vscratch, c->s));
+  transpose_z_kernel<<<(unsigned)(((long)n * n + 255) / 256), 256, 0, c->s>>>(dZ, n, n, n, dZc, 0); ++g_launch_count;
+  CKC(cudaGetLastError());
+  CKC(cudaMemcpyAsync(W, dW, sizeof(double) * n, cudaMemcpyDeviceToHost, c->s));
+  CKC(cudaMemcpyAsync(Z, dZc, sizeof(zd) * n * n, cudaMemcpyDeviceToHost, c->s));
+  return check_status(c);
+}
+
+// Gap corrections of bsesolvertemp's ta key (gapcortemp, gapcortemp2: src/module_math.F90:383-403); kb is the
+// single-precision literal of the reference.
+static double temp_gap_correction(const wtb_temp_params* tp) {
+  const double kb = (double)8.617330350E-5f;
+  if (tp->ta == 1) {
+    const double aux1 = tp->phavg / ((2.0 * kb) * tp->temp);  // 2.0*kb is a single-precision product, exact
+    const double aux2 = 1 / std::tanh(aux1);
+    return -tp->st * tp->phavg * (aux2 - 1.0);
+  }
+  if (tp->ta == 2) {
+    const double aux1 = 2.0 * tp->st;
+    const double aux2 = std::exp(tp->phavg / tp->temp);
+    return -(aux1 / (aux2 - 1.0));
+  }
+  return 0.0;
+}
+
+int wtb_bsesolvertemp(wtb_ctx* c, const wtb_bse_params* p, const wtb_temp_params* tp, double* Ws, double* acts,
+                      double* HE, double* fdeh) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (!p || !tp) return set_err(c, WTB_EBADARG, "bad arguments");
+  if (tp->ta < 0 || tp->ta > 2 || !(tp->temp >= 0.0)) return set_err(c, WTB_EBADARG, "bad temperature keys");
+  CKR(check_q_params(c, p));
+  wtb_bse_params pp = *p;  // the full-spectrum path is FP64 throughout
+  pp.precision = WTB_PREC_FP64;
+  pp.op = WTB_OP_DENSE;
+  const double tcor = temp_gap_correction(tp);
+  CKR(stage_mesh(c, &pp));
+  const double scs0 = c->scs;
+  c->scs = scs0 + tcor;
+  const int rb = enqueue_bands(c, false);
+  c->scs = scs0;
+  CKR(rb);
+  CKR(compute_optics(c, &pp));
+  const int nk = c->nk, nv = c->nv, nc = c->nc, w = c->w;
+  const long dim = (long)nk * nc * nv;
+  cudaError_t err = cudaSuccess;
+  const int Kpad = (nk + 63) / 64 * 64;
+  double* V = c->ws.get<double>("V", (size_t)((nk + 127) / 128 * 128) * Kpad, &err, true);
+  double* dE = c->ws.get<double>("dE", dim, &err);
+  double* f = c->ws.get<double>("T_f", dim, &err);
+  zd* H = c->ws.get<zd>("HT", (size_t)dim * dim, &err);
+  zd* Z = c->ws.get<zd>("T_Z", (size_t)dim * dim, &err);
+  double* W = c->ws.get<double>("deig_W", dim, &err);
+  double* dacts = c->ws.get<double>("T_acts", (size_t)8 * dim, &err);
+  void* scratch = c->ws.get<zd>("deig_scratch", (dense_eig_scratch((int)dim) + sizeof(zd) - 1) / sizeof(zd), &err);
+  void* vscratch = c->ws.get<double>("deig_vscratch", dense_eigvec_scratch((int)dim) / sizeof(double), &err);
+  CKC(err);
+  const double* eig_win = c->ws.get<double>("eig_win", 0, &err);
+  CKC(launch_transition_energies(eig_win, nk, nv, nc, dE, c->s));
+  CKR(coulomb_table_into(c, &pp, V, Kpad));
+  CKC(launch_bse_build<double>(c->ws.get<zd>("vec_win", 0, &err), dE, V, Kpad, nk, nv, nc, w, H, c->s));
+  CKC(launch_fermi_weights(eig_win, nk, nv, nc, tp->temp, f, c->s));
+  CKC(launch_temp_weight(H, dim, f, dE, V, Kpad, nc * nv, c->s));
+  CKC(dense_eig_prepare());
+  // H is row-major, i.e. conj(H) column-major: its eigenvectors are conjugated back
+  CKC(launch_dense_eig(H, (int)dim, (int)dim, false, W, Z, true, scratch, vscratch, c->s));
+  CKC(launch_temp_acts(Z, (int)dim, c->ws.get<zd>("hrvel", 0, &err), f, tp->dtfull, tp->cpol, dacts, c->s));
+  if (Ws) CKC(cudaMemcpyAsync(Ws, W, sizeof(double) * dim, cudaMemcpyDeviceToHost, c->s));
+  if (acts) CKC(cudaMemcpyAsync(acts, dacts, sizeof(double) * 8 * dim, cudaMemcpyDeviceToHost, c->s));
+  if (fdeh) CKC(cudaMemcpyAsync(fdeh, f, sizeof(double) * dim, cudaMemcpyDeviceToHost, c->s));
+  if (HE) {
+    // the column-major copy reuses the matrix buffer (H is no longer needed)
+    transpose_z_kernel<<<(unsigned)((dim * dim + 255) / 256), 256, 0, c->s>>>(Z, (int)dim, (int)dim, (int)dim, H, 0);
+    ++g_launch_count;
+    CKC(cudaGetLastError());
+    CKC(cudaMemcpyAsync(HE, H, sizeof(zd) * dim * dim, cudaMemcpyDeviceToHost, c->s));
+  }
+  c->have_solve = false;
+  return check_status(c);
+}
+
 int wtb_slepc_solver(wtb_ctx* c, const double* HX, double* EX, double* HE, int NX, int NE) {
   if (!c) return WTB_EBADARG;
   CKR(prep_device(c));

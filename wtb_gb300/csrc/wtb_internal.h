@@ -284,6 +284,17 @@ cudaError_t launch_merge_windows(const double* eig_k, const zd* vec_k, const dou
 cudaError_t launch_exchange(const zd* vec_m, int nk, int nv, int nc, int w, const double* vq, zd* u, zd* H,
                             cudaStream_t s);
 
+// ----------------------------------------------------------------------------- temperature BSE
+// f[I] = f_v - f_c of transition I at temp (K) (fermidisteh).
+cudaError_t launch_fermi_weights(const double* eig_win, int nk, int nv, int nc, double temp, double* f,
+                                 cudaStream_t s);
+// The row-major direct matrix H (dim x dim) weighted in place as ZHEEV 'U' reads matrizelbsetemp's upper triangle.
+cudaError_t launch_temp_weight(zd* H, long dim, const double* f, const double* dE, const double* V, int ldv, int nvc,
+                               cudaStream_t s);
+// dielbseptemp's eight activities acts(dim, 8) of the eigenvectors Z (row-major) and hr[5][dim].
+cudaError_t launch_temp_acts(const zd* Z, int dim, const zd* hr, const double* f, int dtfull, int cpol, double* acts,
+                             cudaStream_t s);
+
 // ----------------------------------------------------------------------------- dense Hermitian eigenvalues
 // All eigenvalues (ascending) of the n x n Hermitian A (column-major, leading dimension lda; destroyed: its
 // strictly lower part ends holding the Householder vectors).  upper_only: only the upper triangle holds the
@@ -291,6 +302,13 @@ cudaError_t launch_exchange(const zd* vec_m, int nk, int nv, int nc, int w, cons
 constexpr int kDenseEigChunks = 16;
 size_t dense_eig_scratch(int n);
 cudaError_t launch_dense_eigvals(zd* A, int n, int lda, bool upper_only, double* W, void* scratch, cudaStream_t s);
+// All eigenpairs: W ascending and Z(i, k) = Z[i * n + k] (row-major, complex) the eigenvector of W[k]; inverse
+// iteration on the tridiagonal (clusters reorthogonalised) and the Householder back-transformation.  With
+// conj_vectors the conjugates are returned (for A holding conj(H), e.g. a row-major H read column-major).
+// vscratch: dense_eigvec_scratch(n) bytes.
+size_t dense_eigvec_scratch(int n);
+cudaError_t launch_dense_eig(zd* A, int n, int lda, bool upper_only, double* W, zd* Z, bool conj_vectors,
+                             void* scratch, void* vscratch, cudaStream_t s);
 // Sets the kernels' shared-memory limits ahead of a stream capture of launch_dense_eigvals.
 cudaError_t dense_eig_prepare();
 
