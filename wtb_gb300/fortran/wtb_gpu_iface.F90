@@ -11,6 +11,7 @@
 !   wtb_gpu_spdielraw     <- spdielraw     (src/module_bse.F90:4090-4308)
 !   wtb_gpu_spdielrawpol  <- spdielrawpol  (src/module_bse.F90:4318-4524)
 !   wtb_gpu_bsebnds       <- the Q loop of bsebnds (src/module_bse.F90:1206-1566)
+!   wtb_gpu_bsesolvertemp <- bsesolvertemp (src/module_bse.F90:2649-3263) before its writes
 ! A non-zero status from the library is turned into the reference's behaviour: print the message
 ! (the reference's STOP text where it has one) and STOP.
 ! No Fortran compiler exists in the build image, so this file is not compiled by the project's build.
@@ -20,7 +21,8 @@ module wtb_gpu
   private
   public :: wtb_bse_params_t, wtb_timings_t, wtb_gpu_init, wtb_gpu_eigsys, wtb_gpu_slepc_solver, &
             wtb_gpu_bsesolver, wtb_gpu_bsedielraw, wtb_gpu_set_hr, wtb_gpu_bsedielrawpol, &
-            wtb_gpu_spoptics, wtb_gpu_spdielraw, wtb_gpu_spdielrawpol, wtb_gpu_bsebnds
+            wtb_gpu_spoptics, wtb_gpu_spdielraw, wtb_gpu_spdielrawpol, wtb_gpu_bsebnds, &
+            wtb_temp_params_t, wtb_gpu_bsesolvertemp
 
   type, bind(C) :: wtb_bse_params_t
     integer(c_int)  :: ngrid(3)
@@ -38,6 +40,13 @@ module wtb_gpu
     integer(c_int)  :: iterations, matvec_columns
     real(c_double)  :: max_rel_residual, refine_shift_max
     integer(c_int)  :: kernel_launches
+  end type
+
+  type, bind(C) :: wtb_temp_params_t
+    real(c_double)  :: temp
+    integer(c_int)  :: ta
+    real(c_double)  :: st, phavg
+    integer(c_int)  :: dtfull, cpol
   end type
 
   interface
@@ -117,6 +126,14 @@ module wtb_gpu
       type(wtb_bse_params_t) :: p
       integer(c_int), value :: nq
       real(c_double) :: qpath(*), exk(*)
+    end function
+    integer(c_int) function c_wtb_bsesolvertemp(ctx, p, tp, ws, acts, he, fdeh) bind(C, name="wtb_bsesolvertemp")
+      import :: c_ptr, c_int, c_double, wtb_bse_params_t, wtb_temp_params_t
+      type(c_ptr), value :: ctx
+      type(wtb_bse_params_t) :: p
+      type(wtb_temp_params_t) :: tp
+      real(c_double) :: ws(*), acts(*)
+      type(c_ptr), value :: he, fdeh
     end function
     integer(c_int) function c_wtb_spoptics(ctx, p, rec) bind(C, name="wtb_spoptics")
       import :: c_ptr, c_int, c_float, wtb_bse_params_t
@@ -256,6 +273,16 @@ contains
     double precision :: qauxv(nq,4), exk(*)
     call wtb_gpu_init(0)
     call check(c_wtb_bsebnds(ctx, p, nq, qauxv, exk), 'bsebnds')
+  end subroutine
+
+  ! W(dimbse) all exciton energies ascending, acts(dimbse,8) xx yy zz xy xz yz sp sm of dielbseptemp
+  subroutine wtb_gpu_bsesolvertemp(p, tp, dimbse, W, acts)
+    type(wtb_bse_params_t) :: p
+    type(wtb_temp_params_t) :: tp
+    integer :: dimbse
+    double precision :: W(dimbse), acts(dimbse,8)
+    call wtb_gpu_init(0)
+    call check(c_wtb_bsesolvertemp(ctx, p, tp, W, acts, c_null_ptr, c_null_ptr), 'bsesolvertemp')
   end subroutine
 
   subroutine wtb_gpu_spdielraw(p, dimsp, esp, acts, dielf)
