@@ -234,6 +234,33 @@ typedef struct {
 int wtb_bsesolvertemp(wtb_ctx* ctx, const wtb_bse_params* p, const wtb_temp_params* tp, double* Ws, double* acts,
                       double* HE, double* fdeh);
 
+/* ---- Output files (host writers; path = the file to create).  Records byte for byte in the reference's
+ * formats: Fw.d / Ew.d / Iw.m edit descriptors as the Fortran standard defines them (the width-less I of excwf2
+ * as I12), IEEE infinities as "Infinity"; the '#' header lines as list-directed records of character items
+ * (a leading blank, no separators) with integers in 12-character fields.  Return WTB_EBADARG when the file
+ * cannot be written. */
+/* bse_opt_diel.dat (pol = 0: Ws, xx yy zz xy xz yz, 7F15.4) or bse_opt_diel-pol.dat (pol = 1: Ws, xx yy zz sp sm,
+ * 6F15.4) from the Ws(dim) and acts(dim, 8) of wtb_bsesolver / wtb_bsesolvertemp (src/module_bse.F90:2132-2133,
+ * :2556-2567). */
+int wtb_write_bse_opt_diel(const char* path, int dim, const double* Ws, const double* acts, int pol);
+/* sp_optics.dat / sp_optics-pol.dat from wtb_spoptics' rec(dimsp, 15) (src/module_bse.F90:2296-2297, :2366-2367). */
+int wtb_write_sp_optics(const char* path, int dimsp, const float* rec, int pol);
+/* tm_coef.dat / tm_coef-pol.dat (3F10.4,3I10.0,7F10.4 / ...,6F10.4) from the same records (:2300-2311, :2370-2377). */
+int wtb_write_tm_coef(const char* path, int nk, int nc, int nv, const float* rec, int pol);
+/* exc_wf_<n>.dat of excwf2 (src/module_bse.F90:374-408): nocpk(nk), kpt(nk, 3) column-major, the exciton's
+ * energy and its dim = nk nc nv coefficients ewf (complex(8)). */
+int wtb_write_exc_wf(const char* path, int nk, int nc, int nv, const int* nocpk, const double* kpt, int excnum,
+                     double energy, const double* ewf);
+/* Replaces exclft over the rows of lifetime (src/module_bse.F90:326-370, :3271-3349): fosc(dim, 7) the columns of
+ * bse_opt_diel.dat, sysdim "3D" / "2D" / "1D" with the lattice of wtb_set_hr; lft(dim, 4) radiative lifetimes (s)
+ * for xx+yy+zz, xx, yy, zz. */
+int wtb_exciton_lifetime(wtb_ctx* ctx, const char* sysdim, const int* ngrid, int dim, const double* fosc,
+                         double* lft);
+/* exciton_lifetime.dat (1F15.4,4E15.4) from the energies and lft(dim, 4). */
+int wtb_write_exciton_lifetime(const char* path, int dim, const double* energy, const double* lft);
+/* One Fortran edit descriptor applied to x (kind 'F', 'E' or 'I' with w, d (m for I)) into out (>= w+1 bytes). */
+int wtb_fortran_format(char kind, double x, int w, int d, char* out, int outlen);
+
 /* Replaces bseoptprop (src/module_bse.F90:3766-3931, formulas :5075-5124): props(numbse, 6, 5) =
  * refractive index, extinction coefficient, reflectivity, absorption coefficient, energy-loss function.
  * spoptprop (:3438-3602) applies the same formulas to the spdielraw spectrum. */

@@ -738,3 +738,93 @@ def bsesolver(sysm, p, dense_solver=True, nev=None, with_vectors=False):
 def round_f15_4(x):
     """The 7F15.4 text handoff of bse_opt_diel.dat (src/module_bse.F90:2556-2567)."""
     return np.round(np.asarray(x, dtype=np.float64), 4)
+
+
+# ----------------------------------------------------------------------------- output records
+def _fortran_special(x, w):
+    s = "NaN" if np.isnan(x) else ("Infinity" if w >= 8 + (x < 0) else "Inf")
+    if np.isinf(x) and x < 0:
+        s = "-" + s
+    return "*" * w if len(s) > w else s.rjust(w)
+
+
+def fortran_F(x, w, d):
+    """Fw.d editing of the binary value x, restated with exact decimal arithmetic: rounded to d decimals
+    (nearest, ties to even), right-justified; the optional leading zero dropped when it does not fit; w
+    asterisks when the number does not fit."""
+    from decimal import ROUND_HALF_EVEN, Decimal
+    x = float(x)
+    if not np.isfinite(x):
+        return _fortran_special(x, w)
+    from decimal import localcontext
+    with localcontext() as ctx:
+        ctx.prec = 1200                            # every double has an exact decimal expansion of < 800 digits
+        q = Decimal(x).quantize(Decimal(1).scaleb(-d), rounding=ROUND_HALF_EVEN)
+    neg = np.signbit(x)
+    mag = format(abs(q), "f")
+    if d > 0 and "." not in mag:
+        mag += "." + "0" * d
+    s = ("-" if neg else "") + mag
+    if len(s) > w and mag.startswith("0."):
+        s = ("-" if neg else "") + mag[1:]
+    return "*" * w if len(s) > w else s.rjust(w)
+
+
+def fortran_E(x, w, d):
+    """Ew.d editing: 0.d1..dd E+xx (the E dropped for a three-digit exponent), d significant digits rounded
+    from the exact binary value (nearest, ties to even)."""
+    from decimal import ROUND_HALF_EVEN, Decimal
+    x = float(x)
+    if not np.isfinite(x):
+        return _fortran_special(x, w)
+    neg = np.signbit(x)
+    if x == 0.0:
+        digits, e10 = "0" * d, 0
+    else:
+        from decimal import localcontext
+        with localcontext() as ctx:
+            ctx.prec = 1200
+            dx = abs(Decimal(x))
+            e = dx.adjusted()                  # dx = m * 10**e with 1 <= m < 10
+            m = (dx.scaleb(-e)).quantize(Decimal(1).scaleb(-(d - 1)), rounding=ROUND_HALF_EVEN)
+            if m >= 10:
+                m = (m / 10).quantize(Decimal(1).scaleb(-(d - 1)), rounding=ROUND_HALF_EVEN)
+                e += 1
+        digits = format(m, "f").replace(".", "")[:d].ljust(d, "0")
+        e10 = e + 1
+    exp = f"E{'-' if e10 < 0 else '+'}{abs(e10):02d}" if abs(e10) <= 99 else f"{'-' if e10 < 0 else '+'}{abs(e10):03d}"
+    s = ("-" if neg else "") + "0." + digits + exp
+    if len(s) > w:
+        s = ("-" if neg else "") + "." + digits + exp
+    return "*" * w if len(s) > w else s.rjust(w)
+
+
+def fortran_I(v, w, m=1):
+    """Iw.m editing (Iw.0 of zero is blank)."""
+    v = int(v)
+    if m == 0 and v == 0:
+        return " " * w
+    s = str(abs(v)).rjust(m, "0")
+    s = ("-" if v < 0 else "") + s
+    return "*" * w if len(s) > w else s.rjust(w)
+
+
+def exclft(sysdim, ngrid, rlat, fosc, enexc):
+    """Radiative lifetime (src/module_bse.F90:326-370) with the reference's single-precision constants."""
+    cfe, lspd, hbar = float(F32(7.297e-3)), float(F32(299.792e16)), float(F32(6.582e-16))
+    ng = float(ngrid[0] * ngrid[1] * ngrid[2])
+    with np.errstate(divide="ignore"):
+        if sysdim == "3D":
+            aux1 = (4.0 * cfe) * (enexc * enexc * enexc)
+            aux2 = fosc / ng
+            aux3 = 3.0 * (lspd * lspd) * (hbar * hbar * hbar)
+            return 1.0 / ((aux1 * aux2) / aux3)
+        if sysdim == "2D":
+            aux1 = ng * vcell2D(rlat) * hbar
+            aux2 = (8.0 * PI_F32 * cfe * enexc) * fosc
+            return aux1 / aux2
+        if sysdim == "1D":
+            aux2 = (2.0 * PI_F32 * cfe * enexc * enexc) * fosc
+            aux1 = ng * rlat[0, 0] * hbar * hbar * lspd
+            return aux1 / aux2
+    raise OracleError("Wrong System dimension")

@@ -295,3 +295,25 @@ def test_determinism_fp64(ctx, small):
     a = ctx.bsesolver(p, precision="fp64", op="dense", tol=1e-8)
     b = ctx.bsesolver(p, precision="fp64", op="dense", tol=1e-8)
     assert np.array_equal(a["E"], b["E"])
+
+
+@pytest.mark.parametrize("sysdim", ["3D", "2D", "1D"])
+def test_exciton_lifetime(ctx, small, sysdim):
+    """exclft over bse_opt_diel.dat's rows (zero activity: an infinite lifetime, as the reference divides)."""
+    from wtb_gb300 import api
+
+    sysm, p, _ = small
+    ctx.set_hr(sysm)
+    rng = np.random.default_rng(11)
+    fosc = np.zeros((40, 7))
+    fosc[:, 0] = rng.uniform(1.0, 4.0, 40)
+    fosc[:, 1:] = rng.uniform(0.0, 30.0, (40, 6))
+    fosc[30:, 1:4] = 0.0
+    lft = ctx.exciton_lifetime(sysdim, p.ngrid, fosc)
+    ref = np.stack([O.exclft(sysdim, p.ngrid, sysm.rlat, fosc[:, 1] + fosc[:, 2] + fosc[:, 3], fosc[:, 0])]
+                   + [O.exclft(sysdim, p.ngrid, sysm.rlat, fosc[:, c], fosc[:, 0]) for c in (1, 2, 3)], axis=1)
+    np.testing.assert_allclose(lft, ref, rtol=1e-14)
+    assert np.all(np.isinf(lft[30:]))
+    with pytest.raises(api.WTBError) as e:
+        ctx.exciton_lifetime("4D", p.ngrid, fosc)
+    assert "Wrong System dimension" in str(e.value)

@@ -105,6 +105,13 @@ def _load():
         "wtb_bsebnds": [P, C.POINTER(CParams), C.c_int, dp, dp],
         "wtb_zheev": [P, C.c_int, dp, C.c_int, dp],
         "wtb_zheev_vectors": [P, C.c_int, dp, C.c_int, dp, dp],
+        "wtb_write_bse_opt_diel": [C.c_char_p, C.c_int, dp, dp, C.c_int],
+        "wtb_write_sp_optics": [C.c_char_p, C.c_int, C.POINTER(C.c_float), C.c_int],
+        "wtb_write_tm_coef": [C.c_char_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_int],
+        "wtb_write_exc_wf": [C.c_char_p, C.c_int, C.c_int, C.c_int, ip, dp, C.c_int, C.c_double, dp],
+        "wtb_exciton_lifetime": [P, C.c_char_p, ip, C.c_int, dp, dp],
+        "wtb_write_exciton_lifetime": [C.c_char_p, C.c_int, dp, dp],
+        "wtb_fortran_format": [C.c_char, C.c_double, C.c_int, C.c_int, C.c_char_p, C.c_int],
         "wtb_bsesolvertemp": [P, C.POINTER(CParams), C.POINTER(CTempParams), dp, dp, dp, dp],
         "wtb_bse_backward": [P, C.POINTER(CParams), dp, dp, dp, dp, dp, C.POINTER(CTimings)],
         "wtb_spectrum_loss": [P, C.POINTER(CParams), C.c_int, C.c_int, dp, dp, dp, dp, dp, dp],
@@ -208,6 +215,56 @@ def kpathbse(rlat1, rlat2, rlat3, ks, npts):
     if r:
         raise WTBError(r, "kpathbse: bad arguments")
     return np.ascontiguousarray(q)
+
+
+def fortran_format(kind, x, w, d):
+    """One Fortran edit descriptor (F, E or I) as the output writers apply it."""
+    buf = C.create_string_buffer(w + 1)
+    r = _lib.wtb_fortran_format(kind.encode(), float(x), int(w), int(d), buf, w + 1)
+    if r:
+        raise WTBError(r, "fortran_format: bad arguments")
+    return buf.value.decode()
+
+
+def _w(r, what):
+    if r:
+        raise WTBError(r, what + ": cannot write the file")
+
+
+def write_bse_opt_diel(path, Ws, acts, pol=False):
+    """bse_opt_diel.dat (pol=False) or bse_opt_diel-pol.dat from Ws (dim,) and acts {comp: (dim,)}."""
+    Ws = np.ascontiguousarray(Ws, dtype=np.float64)
+    A = np.zeros((len(Ws), 8), order="F")
+    for i, c in enumerate(COMPONENTS):
+        A[:, i] = acts[c]
+    _w(_lib.wtb_write_bse_opt_diel(os.fsencode(path), len(Ws), _dp(Ws), _dp(A), int(bool(pol))),
+       "wtb_write_bse_opt_diel")
+
+
+def write_sp_optics(path, rec, pol=False):
+    rec = np.asfortranarray(rec, dtype=np.float32)
+    _w(_lib.wtb_write_sp_optics(os.fsencode(path), rec.shape[0], rec.ctypes.data_as(C.POINTER(C.c_float)),
+                                int(bool(pol))), "wtb_write_sp_optics")
+
+
+def write_tm_coef(path, nk, nc, nv, rec, pol=False):
+    rec = np.asfortranarray(rec, dtype=np.float32)
+    _w(_lib.wtb_write_tm_coef(os.fsencode(path), nk, nc, nv, rec.ctypes.data_as(C.POINTER(C.c_float)),
+                              int(bool(pol))), "wtb_write_tm_coef")
+
+
+def write_exc_wf(path, nocpk, kpt, nc, nv, excnum, energy, ewf):
+    nocp = np.ascontiguousarray(nocpk, dtype=np.int32)
+    k = np.asfortranarray(kpt, dtype=np.float64)
+    e = np.ascontiguousarray(ewf, dtype=np.complex128)
+    _w(_lib.wtb_write_exc_wf(os.fsencode(path), len(nocp), nc, nv, nocp.ctypes.data_as(C.POINTER(C.c_int)), _dp(k),
+                             int(excnum), float(energy), e.ctypes.data_as(C.POINTER(C.c_double))), "wtb_write_exc_wf")
+
+
+def write_exciton_lifetime(path, energy, lft):
+    e = np.ascontiguousarray(energy, dtype=np.float64)
+    L = np.asfortranarray(lft, dtype=np.float64)
+    _w(_lib.wtb_write_exciton_lifetime(os.fsencode(path), len(e), _dp(e), _dp(L)), "wtb_write_exciton_lifetime")
 
 
 def eigsys(nthreads, scs, exc, nocp, ffactor, kx, ky, kz, w90basis, nvec, rlat, rvec, hopmatrices, ihopmatrices,
@@ -351,6 +408,15 @@ class Context:
         if want_vectors:
             out["HE"] = HE
         return out
+
+    def exciton_lifetime(self, sysdim, ngrid, fosc):
+        """exclft over the rows fosc (dim, 7) of bse_opt_diel.dat: lft (dim, 4) for xx+yy+zz, xx, yy, zz."""
+        F = np.asfortranarray(fosc, dtype=np.float64)
+        g = np.ascontiguousarray(ngrid, dtype=np.int32)
+        L = np.zeros((F.shape[0], 4), order="F")
+        self._chk(_lib.wtb_exciton_lifetime(self._h, sysdim.encode(), g.ctypes.data_as(C.POINTER(C.c_int)),
+                                            F.shape[0], _dp(F), _dp(L)), "wtb_exciton_lifetime")
+        return L
 
     def bse_matvec(self, p: BSEParams, X, precision="fp64", op="matfree"):
         """Y = H X for the bands of the last set-up (X: dim x ncol complex)."""
