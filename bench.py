@@ -351,13 +351,31 @@ def main():
     api.lib().wtb_profile_enable(ctx._h, 0)
     value = world * args.steps / (tot_ms / 1000.0)
 
-    # end to end through the C ABI with host buffers: H(R) host -> device, Ws/acts/HE device -> host
+    # end to end through the C ABI with host buffers: H(R) host -> device, Ws/acts/HE device -> host, both in
+    # page-locked host memory allocated once (the device copies straight into and out of it)
+    def pinned(shape, dtype, order="C"):
+        n = int(np.prod(shape))
+        t = torch.empty(n, dtype={np.float64: torch.float64, np.complex128: torch.complex128}[dtype], pin_memory=True)
+        a = t.numpy()
+        return a.reshape(shape[::-1]).T if order == "F" else a.reshape(shape)
+
+    def pinned_copy(a):
+        b = pinned(a.shape, np.float64, "F")
+        b[...] = a
+        return b
+
+    import dataclasses
+    sys_pin = dataclasses.replace(sysm, hop=pinned_copy(np.asfortranarray(sysm.hop, dtype=np.float64)),
+                                  ihop=pinned_copy(np.asfortranarray(sysm.ihop, dtype=np.float64)))
+    outs = {"Ws": pinned((p.dim,), np.float64), "acts": pinned((p.dim, 8), np.float64, "F"),
+            "HE": pinned((p.dim, p.nev), np.complex128, "F")}
     e2e_ms = []
     for i in range(max(1, min(args.steps, 3))):
+        flush_l2(torch, l2buf)  # as between the device-timed steps; outside the timed window
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        ctx.set_hr(sysm)
-        out = ctx.bsesolver(p, want_vectors=True, **solve_kw)
+        ctx.set_hr(sys_pin)
+        out = ctx.bsesolver(p, want_vectors=True, out=outs, **solve_kw)
         torch.cuda.synchronize()
         e2e_ms.append(1000.0 * (time.perf_counter() - t0))
     h2d = sysm.hop.nbytes + sysm.ihop.nbytes + sysm.rvec.astype(np.int32).nbytes + \

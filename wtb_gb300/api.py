@@ -447,15 +447,25 @@ class Context:
         return act
 
     def bsesolver(self, p: BSEParams, precision="fp64", op="dense", tol=0.0, maxit=0, block=0,
-                  want_vectors=False):
-        """The bsesolver path; returns dict with Ws (dim,), acts {comp: (dim,)}, E (nev,), timings, HE."""
+                  want_vectors=False, out=None):
+        """The bsesolver path; returns dict with Ws (dim,), acts {comp: (dim,)}, E (nev,), timings, HE.
+        out: optional caller-owned output arrays {"Ws": (dim,), "acts": (dim, 8) Fortran order, "HE": (dim, nev)
+        complex128 Fortran order} (e.g. page-locked memory, which the device copies into directly)."""
         dim = p.dim
-        Ws = np.zeros(dim)
-        acts = np.zeros((dim, 8), order="F")
-        HE = np.zeros((dim, p.nev), dtype=np.complex128, order="F") if want_vectors else None
+        if out is not None:
+            Ws, acts = out["Ws"], out["acts"]
+            HE = out.get("HE") if want_vectors else None
+            assert Ws.dtype == np.float64 and Ws.shape == (dim,) and Ws.flags.c_contiguous
+            assert acts.dtype == np.float64 and acts.shape == (dim, 8) and acts.flags.f_contiguous
+            assert HE is None or (HE.dtype == np.complex128 and HE.shape == (dim, p.nev) and HE.flags.f_contiguous)
+        else:
+            Ws = np.zeros(dim)
+            acts = np.zeros((dim, 8), order="F")
+            HE = np.zeros((dim, p.nev), dtype=np.complex128, order="F") if want_vectors else None
         t = CTimings()
         cp = cparams(p, precision=precision, op=op, tol=tol, maxit=maxit, block=block)
-        self._chk(_lib.wtb_bsesolver(self._h, C.byref(cp), _dp(Ws), _dp(acts), _dp(HE), C.byref(t)),
+        self._chk(_lib.wtb_bsesolver(self._h, C.byref(cp), _dp(Ws), _dp(acts),
+                                     None if HE is None else HE.ctypes.data_as(C.POINTER(C.c_double)), C.byref(t)),
                   "wtb_bsesolver")
         out = {"Ws": Ws, "E": Ws[: p.nev].copy(), "acts": {c: acts[:, i].copy() for i, c in enumerate(COMPONENTS)},
                "timings": {f: getattr(t, f) for f, _ in CTimings._fields_}}
