@@ -175,3 +175,17 @@ def test_bsesolvertemp_small(ctx, small_bands, temp, ta, st, phavg):
     E[idx, idx] = D[idx, idx] + Vkk * (f - 1.0)
     assert np.abs(E @ HE - HE * out["Ws"]).max() <= 1e-10
     assert np.abs(HE.conj().T @ HE - np.eye(p.dim)).max() <= 1e-10
+
+
+def test_bsesolvertemp_2304(ctx):
+    """dim 2304 (24 x 24 mesh, 2v2c) at 600 K: every exciton energy 1e-9 eV and the broadened spectra 1e-8
+    against the oracle's dense eigendecomposition."""
+    sysm, p = S.workload("hex8_24x24")
+    ctx.set_hr(sysm)
+    out = ctx.bsesolvertemp(p, 600.0, "VE", 3.0e-4, 0.03)
+    ref = O.bsesolvertemp(sysm, p, 600.0, "VE", 3.0e-4, 0.03)
+    np.testing.assert_allclose(out["Ws"], ref["Ws"], atol=1e-9)
+    spec = O.bsedielraw(out["Ws"], out["acts"], p.ngrid, sysm.rlat, p)
+    spec_ref = O.bsedielraw(ref["Ws"], ref["acts"], p.ngrid, sysm.rlat, p)
+    for c in ("xx", "yy", "zz", "xy"):
+        np.testing.assert_allclose(spec[c], spec_ref[c], rtol=1e-8, atol=1e-9 * np.abs(spec_ref[c]).max())
