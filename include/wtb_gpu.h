@@ -234,6 +234,17 @@ typedef struct {
 int wtb_bsesolvertemp(wtb_ctx* ctx, const wtb_bse_params* p, const wtb_temp_params* tp, double* Ws, double* acts,
                       double* HE, double* fdeh);
 
+/* Replaces the Q loop of bsebndstemp (src/module_bse.F90:1572-1990): wtb_bsebnds with the temperature keys of
+ * tp — bands with the scissor scs + tcor on both meshes, the finite-Q matrix of matrizelbsekqtemp (:664-780,
+ * the direct and exchange couplings weighted by f_v - f_c of the row's transition, as ZHEEV 'U' reads its upper
+ * triangle) — all dim eigenvalues per Q in exk(dim, nq). */
+int wtb_bsebndstemp(wtb_ctx* ctx, const wtb_bse_params* p, const wtb_temp_params* tp, int nq, const double* qpath,
+                    double* exk);
+
+/* The IPA records bsesolvertemp writes to sp_optics.dat / tm_coef.dat (src/module_bse.F90:2649-3263): as
+ * wtb_spoptics, with the bands' scissor scs + tcor and the eight activity columns multiplied by f_v - f_c. */
+int wtb_spoptics_temp(wtb_ctx* ctx, const wtb_bse_params* p, const wtb_temp_params* tp, float* rec);
+
 /* ---- Output files (host writers; path = the file to create).  Records byte for byte in the reference's
  * formats: Fw.d / Ew.d / Iw.m edit descriptors as the Fortran standard defines them (the width-less I of excwf2
  * as I12), IEEE infinities as "Infinity"; the '#' header lines as list-directed records of character items

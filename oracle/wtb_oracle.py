@@ -457,6 +457,32 @@ def bsesolvertemp(sysm, p, temp, ta="FA", st=0.0, phavg=0.0, dtfull=True, cpol=T
     return {"Ws": W, "A": A, "acts": acts, "fdeh": f, "E": E, "tcor": tcor}
 
 
+def bsebndstemp(sysm, p, qpath, temp, ta="FA", st=0.0, phavg=0.0):
+    """The Q loop of bsebndstemp (src/module_bse.F90:1572-1990): bsebnds with scs + tcor and
+    matrizelbsekqtemp (:664-780), i.e. the finite-Q couplings weighted by f_v - f_c of the row's transition
+    (E(i,j) = H(i,j) f_min(i,j), E(i,i) = dE_i + (H(i,i) - dE_i) f_i for the Hermitian completion of the upper
+    triangle).  Returns exk (dim, nq)."""
+    import dataclasses
+    tcor = {"VE": lambda: gapcortemp(st, phavg, temp), "BE": lambda: gapcortemp2(st, phavg, temp)}.get(ta, lambda: 0.0)()
+    s2 = dataclasses.replace(sysm, scs=sysm.scs + tcor)
+    kpt = monhkhorst_pack(p.ngrid[0], p.ngrid[1], p.ngrid[2], p.mshift, s2.rlat)
+    eigv, vec, _ = bands(s2, p, kpt)
+    nk = len(kpt)
+    kk, cs, vs = basis(nk, p.nc, p.nv)
+    idx = np.arange(p.dim)
+    out = np.empty((p.dim, len(qpath)))
+    for i, q in enumerate(qpath):
+        kq = monhkhorst_packq(q, p.ngrid[0], p.ngrid[1], p.ngrid[2], p.mshift, s2.rlat)
+        eigvq, vecq, _ = bands(s2, p, kq)
+        H = bse_build_q(eigv, vec, eigvq, vecq, kpt, q, p, s2.rlat)
+        dE = eigvq[kk, cs] - eigv[kk, vs]
+        f = fermidisteh(eigvq[kk, cs], eigv[kk, vs], temp)
+        E = H * f[np.minimum(idx[:, None], idx[None, :])]
+        E[idx, idx] = dE + (H[idx, idx].real - dE) * f
+        out[:, i] = np.linalg.eigvalsh(E)
+    return out
+
+
 def bse_matvec_factored(x, eigv, vec, kpt, p, rlat, V=None):
     """Matrix-free y = H x through V(k,k') and the orbital factorisation; same operator as bse_build."""
     nk = len(kpt)
@@ -659,9 +685,10 @@ def stable_sort_rows(vec, a):
     return np.asarray(vec)[np.argsort(np.asarray(vec)[:, a], kind="stable")]
 
 
-def spoptics_records(eigv, kpt, nocpk, hr, nv, nc):
+def spoptics_records(eigv, kpt, nocpk, hr, nv, nc, f=None):
     """spoptics' vecres(dimsp, 15) in REAL(4) (src/module_bse.F90:4962-4991; bsesolver :2317-2348), sorted
-    by Bubblem on column 7 (:4992).  hr = (hrx, hry, hrz, hrsp, hrsm) of optsp_all."""
+    by Bubblem on column 7 (:4992).  hr = (hrx, hry, hrz, hrsp, hrsm) of optsp_all.  With f (dim,), the
+    activity columns times f_v - f_c before the rounding, as bsesolvertemp writes them."""
     F = np.float32
     nk = len(kpt)
     dim = nk * nc * nv
@@ -680,9 +707,10 @@ def spoptics_records(eigv, kpt, nocpk, hr, nv, nc):
                 rec[I, 4] = F(nocpk[k] - nv + (nv + c + 1))
                 rec[I, 5] = F(nocpk[k] - nv + (v + 1))
                 rec[I, 6] = F(eigv[k, nv + c] - eigv[k, v])
-                rec[I, 7:15] = [F(rp(hx[I], hx[I])), F(rp(hy[I], hy[I])), F(rp(hz[I], hz[I])),
-                                F(rp(hx[I], hy[I])), F(rp(hx[I], hz[I])), F(rp(hy[I], hz[I])),
-                                F(rp(hsp[I], hsp[I])), F(rp(hsm[I], hsm[I]))]
+                w = 1.0 if f is None else f[I]
+                rec[I, 7:15] = [F(rp(hx[I], hx[I]) * w), F(rp(hy[I], hy[I]) * w), F(rp(hz[I], hz[I]) * w),
+                                F(rp(hx[I], hy[I]) * w), F(rp(hx[I], hz[I]) * w), F(rp(hy[I], hz[I]) * w),
+                                F(rp(hsp[I], hsp[I]) * w), F(rp(hsm[I], hsm[I]) * w)]
     return stable_sort_rows(rec, 6)
 
 

@@ -189,3 +189,41 @@ def test_bsesolvertemp_2304(ctx):
     spec_ref = O.bsedielraw(ref["Ws"], ref["acts"], p.ngrid, sysm.rlat, p)
     for c in ("xx", "yy", "zz", "xy"):
         np.testing.assert_allclose(spec[c], spec_ref[c], rtol=1e-8, atol=1e-9 * np.abs(spec_ref[c]).max())
+
+
+@pytest.mark.parametrize("temp,ta,st,phavg", [(300.0, "FA", 0.0, 0.0), (3000.0, "BE", 0.05, 300.0)])
+def test_bsebndstemp_small(ctx, small_bands, temp, ta, st, phavg):
+    """bsebndstemp: the finite-Q Q loop with the temperature weighting and gap correction, against the oracle."""
+    sysm, p, kpt, eigv, vec = small_bands
+    ctx.set_hr(sysm)
+    ks = np.array([[0.0, 0.0, 0.0], [0.5, 0.0, 0.0]])
+    qpath = O.kpathbse(sysm.rlat, ks, 3)
+    exk = ctx.bsebndstemp(p, qpath, temp, ta, st, phavg)
+    ref = O.bsebndstemp(sysm, p, qpath, temp, ta, st, phavg)
+    assert np.max(np.abs(exk - ref)) <= 1e-9, np.max(np.abs(exk - ref))
+    if temp < 1000:   # f = 1 for a 1.5 eV gap: the plain finite-Q spectrum
+        np.testing.assert_allclose(exk, O.bsebnds(sysm, p, qpath), atol=1e-9)
+
+
+def test_spoptics_temp(ctx, small_bands):
+    """bsesolvertemp's IPA records: bands with scs + tcor, activity columns weighted by f_v - f_c."""
+    sysm, p, kpt, eigv, vec = small_bands
+    import dataclasses
+    ctx.set_hr(sysm)
+    temp, st, phavg = 3000.0, 0.05, 300.0
+    rec = ctx.spoptics_temp(p, temp, "BE", st, phavg)
+    s2 = dataclasses.replace(sysm, scs=sysm.scs + O.gapcortemp2(st, phavg, temp))
+    e2, v2, nocp = O.bands(s2, p, kpt)
+    hr = O.optsp_all(e2, v2, kpt, s2, p)
+    kk, cs, vs = O.basis(len(kpt), p.nc, p.nv)
+    f = O.fermidisteh(e2[kk, cs], e2[kk, vs], temp)
+    assert np.all(f < 1.0)
+    ref = O.spoptics_records(e2, kpt, nocp, hr, p.nv, p.nc, f)
+    assert np.all(np.diff(rec[:, 6]) >= 0)
+    np.testing.assert_allclose(rec[:, 6], ref[:, 6], rtol=2e-7, atol=1e-6)
+    amax = np.abs(ref[:, 7:15]).max()
+    # rows matched by (k-point, c, v)
+    key = lambda r: (round(float(r[0]), 4), round(float(r[1]), 4), round(float(r[2]), 4), int(r[4]), int(r[5]))
+    a = {key(r): r for r in rec}
+    for r in ref:
+        np.testing.assert_allclose(a[key(r)][7:15], r[7:15], rtol=0, atol=1e-6 * amax)

@@ -113,6 +113,8 @@ def _load():
         "wtb_write_exciton_lifetime": [C.c_char_p, C.c_int, dp, dp],
         "wtb_fortran_format": [C.c_char, C.c_double, C.c_int, C.c_int, C.c_char_p, C.c_int],
         "wtb_bsesolvertemp": [P, C.POINTER(CParams), C.POINTER(CTempParams), dp, dp, dp, dp],
+        "wtb_bsebndstemp": [P, C.POINTER(CParams), C.POINTER(CTempParams), C.c_int, dp, dp],
+        "wtb_spoptics_temp": [P, C.POINTER(CParams), C.POINTER(CTempParams), C.POINTER(C.c_float)],
         "wtb_bse_backward": [P, C.POINTER(CParams), dp, dp, dp, dp, dp, C.POINTER(CTimings)],
         "wtb_spectrum_loss": [P, C.POINTER(CParams), C.c_int, C.c_int, dp, dp, dp, dp, dp, dp],
         "wtb_batch_create": [C.POINTER(P), C.c_int, C.c_int],
@@ -372,6 +374,18 @@ class Context:
         self._chk(_lib.wtb_bsebnds(self._h, C.byref(cp), nq, _dp(qpath), _dp(exk)), "wtb_bsebnds")
         return exk
 
+    def bsebndstemp(self, p: BSEParams, qpath, temp, ta="FA", st=0.0, phavg=0.0):
+        """bsebndstemp: all finite-Q exciton energies at temperature temp, exk (dim, nq)."""
+        qpath = np.asfortranarray(np.asarray(qpath, dtype=np.float64))
+        nq = qpath.shape[0]
+        exk = np.zeros((p.dim, nq), order="F")
+        tp = CTempParams(float(temp), TEMP_GAP_CORRECTIONS[ta] if isinstance(ta, str) else int(ta), float(st),
+                         float(phavg), 1, 1)
+        cp = cparams(p)
+        self._chk(_lib.wtb_bsebndstemp(self._h, C.byref(cp), C.byref(tp), nq, _dp(qpath), _dp(exk)),
+                  "wtb_bsebndstemp")
+        return exk
+
     def zheev(self, A):
         """ZHEEV('N', 'U'): all eigenvalues (ascending) of the Hermitian matrix held in A's upper triangle."""
         A = np.asfortranarray(np.asarray(A, dtype=np.complex128))
@@ -532,6 +546,17 @@ class Context:
     def spdielrawpol(self, p: BSEParams, esp, acts):
         """spdielrawpol: the independent-particle spectrum for xx yy zz sp sm."""
         return self._dielraw(_lib.wtb_spdielrawpol, "wtb_spdielrawpol", p, esp, acts, POL_COMPONENTS)
+
+    def spoptics_temp(self, p: BSEParams, temp, ta="FA", st=0.0, phavg=0.0):
+        """bsesolvertemp's IPA records: spoptics with scs + tcor and f-weighted activity columns."""
+        dim = p.ngrid[0] * p.ngrid[1] * p.ngrid[2] * p.nc * p.nv
+        rec = np.zeros((dim, 15), dtype=np.float32, order="F")
+        tp = CTempParams(float(temp), TEMP_GAP_CORRECTIONS[ta] if isinstance(ta, str) else int(ta), float(st),
+                         float(phavg), 1, 1)
+        cp = cparams(p)
+        self._chk(_lib.wtb_spoptics_temp(self._h, C.byref(cp), C.byref(tp), rec.ctypes.data_as(C.POINTER(C.c_float))),
+                  "wtb_spoptics_temp")
+        return rec
 
     def spoptics(self, p: BSEParams):
         """spoptics: the (dimsp, 15) float32 records (columns SP_COLUMNS) sorted by transition energy."""

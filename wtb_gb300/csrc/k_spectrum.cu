@@ -271,9 +271,12 @@ __global__ void optprops_kernel(const double* __restrict__ dielf, int nesp, int 
 //   Re(hy hz*), |hsp|^2 |hsm|^2
 // with c = nv+1..nv+nc and v = 1..nv the band slots of basis row I = (k, c, v) (quantumnumbers2).  key(I) is
 // column 7, the sort key of Bubblem.
+// With f (bsesolvertemp's records, src/module_bse.F90:2649-3263, lines 299-306 of its body) the eight activity
+// columns are weighted by f_v - f_c before the rounding to REAL(4).
 __global__ void sp_records_kernel(const double* __restrict__ kpt, const int* __restrict__ nocp,
                                   const double* __restrict__ eig_win, const zd* __restrict__ hr, int nk, int nv,
-                                  int nc, float* __restrict__ rec, float* __restrict__ key) {
+                                  int nc, const double* __restrict__ f, float* __restrict__ rec,
+                                  float* __restrict__ key) {
   const long I = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const long dim = (long)nk * nc * nv;
   if (I >= dim) return;
@@ -292,14 +295,16 @@ __global__ void sp_records_kernel(const double* __restrict__ kpt, const int* __r
   r[4 * dim] = (float)(no + c + 1);
   r[5 * dim] = (float)(no - nv + v + 1);
   r[6 * dim] = (float)de;
-  r[7 * dim] = (float)re_prod(h[0], h[0]);
-  r[8 * dim] = (float)re_prod(h[1], h[1]);
-  r[9 * dim] = (float)re_prod(h[2], h[2]);
-  r[10 * dim] = (float)re_prod(h[0], h[1]);
-  r[11 * dim] = (float)re_prod(h[0], h[2]);
-  r[12 * dim] = (float)re_prod(h[1], h[2]);
-  r[13 * dim] = (float)re_prod(h[3], h[3]);
-  r[14 * dim] = (float)re_prod(h[4], h[4]);
+  const double w = f ? f[I] : 1.0;
+  auto act = [w, f](double v) { return (float)(f ? v * w : v); };
+  r[7 * dim] = act(re_prod(h[0], h[0]));
+  r[8 * dim] = act(re_prod(h[1], h[1]));
+  r[9 * dim] = act(re_prod(h[2], h[2]));
+  r[10 * dim] = act(re_prod(h[0], h[1]));
+  r[11 * dim] = act(re_prod(h[0], h[2]));
+  r[12 * dim] = act(re_prod(h[1], h[2]));
+  r[13 * dim] = act(re_prod(h[3], h[3]));
+  r[14 * dim] = act(re_prod(h[4], h[4]));
   key[I] = (float)de;
 }
 
@@ -395,11 +400,12 @@ cudaError_t launch_optprops(const double* dielf, int nesp, int ncomp, double* pr
 }
 
 cudaError_t launch_sp_records(const double* kpt, const int* nocp, const double* eig_win, const zd* hr, int nk, int nv,
-                              int nc, float* rec, float* key, int* rank, float* sorted, cudaStream_t s) {
+                              int nc, const double* f, float* rec, float* key, int* rank, float* sorted,
+                              cudaStream_t s) {
   const long dim = (long)nk * nc * nv;
   if (dim < 1 || dim > (1L << 30) / 15) return cudaErrorInvalidValue;
   const int n = (int)dim;
-  sp_records_kernel<<<(n + 255) / 256, 256, 0, s>>>(kpt, nocp, eig_win, hr, nk, nv, nc, rec, key); ++g_launch_count;
+  sp_records_kernel<<<(n + 255) / 256, 256, 0, s>>>(kpt, nocp, eig_win, hr, nk, nv, nc, f, rec, key); ++g_launch_count;
   cudaError_t e = cudaMemsetAsync(rank, 0, sizeof(int) * n, s);
   if (e != cudaSuccess) return e;
   const int gx = (n + kRankThreads - 1) / kRankThreads;

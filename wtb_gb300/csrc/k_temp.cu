@@ -1,10 +1,11 @@
-// Temperature BSE of bsesolvertemp (src/module_bse.F90:2649-3263): the transitions weighted by the occupation
-// difference f_v - f_c (fermidisteh, src/module_math.F90:407-421), the matrix of matrizelbsetemp
-// (src/module_bse.F90:575-660)
-//   H(i,j) = V(k_i,k_j) <c_i|c_j> <v_i|v_j> f_i   (i != j),   H(i,i) = (E_c - E_v) + V(k_i,k_i) f_i
-// of which the reference fills the upper triangle and ZHEEV('V', 'U') reads the Hermitian completion:
-// E(i,j) = D(i,j) f_min(i,j) with D the Q = 0 direct matrix; then the activities of dielbseptemp
-// (src/module_bse.F90:784-810) for every exciton: Re[(sum_j A(j,n) h1(j)) conj(sum_j A(j,n) h2(j) f_j)].
+// Temperature BSE of bsesolvertemp and bsebndstemp (src/module_bse.F90:2649-3263, :1572-1990): the couplings
+// weighted by the occupation difference f_v - f_c of the row's transition (fermidisteh, src/module_math.F90:407-421).
+// matrizelbsetemp / matrizelbsekqtemp (src/module_bse.F90:575-660, :664-780) give
+//   H(i,j) = C(i,j) f_i  (i != j),   H(i,i) = (E_c - E_v) + C(i,i) f_i
+// with C the Coulomb part (direct, and at finite Q the exchange); the reference fills the upper triangle and
+// ZHEEV 'U' reads its Hermitian completion, E(i,j) = D(i,j) f_min(i,j) with D the unweighted matrix.  Then the
+// activities of dielbseptemp (src/module_bse.F90:784-810) for every exciton:
+// Re[(sum_j A(j,n) h1(j)) conj(sum_j A(j,n) h2(j) f_j)].
 #include "wtb_internal.h"
 
 namespace wtb {
@@ -29,15 +30,16 @@ __global__ void fermi_weight_kernel(const double* __restrict__ eig_win, int nk, 
   f[I] = fv - fc;
 }
 
-// E = D f_min(i,j) off the diagonal, E(i,i) = dE_i + V(k_i,k_i) f_i, on the row-major dim x dim D in place.
+// E = D f_min(i,j) off the diagonal, E(i,i) = dE_i + (D(i,i) - dE_i) f_i (the coupling part of the diagonal
+// weighted: V(k_i,k_i) at Q = 0, V(k_i,k_i) - V(Q,0)|<c_i|v_i>|^2 for the finite-Q matrix of matrizelbsekqtemp),
+// on the row-major dim x dim D in place.
 __global__ void temp_weight_kernel(zd* __restrict__ H, long dim, const double* __restrict__ f,
-                                   const double* __restrict__ dE, const double* __restrict__ V, int ldv, int nvc) {
+                                   const double* __restrict__ dE) {
   const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= dim * dim) return;
   const long I = e / dim, J = e % dim;
   if (I == J) {
-    const long k = I / nvc;
-    H[e] = mk<double>(dE[I] + V[(size_t)k * ldv + k] * f[I], 0.0);
+    H[e] = mk<double>(dE[I] + (H[e].re - dE[I]) * f[I], 0.0);
   } else {
     const double w = f[I < J ? I : J];
     H[e].re *= w;
@@ -87,9 +89,8 @@ cudaError_t launch_fermi_weights(const double* eig_win, int nk, int nv, int nc, 
   return cudaGetLastError();
 }
 
-cudaError_t launch_temp_weight(zd* H, long dim, const double* f, const double* dE, const double* V, int ldv, int nvc,
-                               cudaStream_t s) {
-  temp_weight_kernel<<<(unsigned)((dim * dim + 255) / 256), 256, 0, s>>>(H, dim, f, dE, V, ldv, nvc); ++g_launch_count;
+cudaError_t launch_temp_weight(zd* H, long dim, const double* f, const double* dE, cudaStream_t s) {
+  temp_weight_kernel<<<(unsigned)((dim * dim + 255) / 256), 256, 0, s>>>(H, dim, f, dE); ++g_launch_count;
   return cudaGetLastError();
 }
 

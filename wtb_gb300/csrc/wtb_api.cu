@@ -836,7 +836,8 @@ int wtb_kpathbse(const double* rlat1, const double* rlat2, const double* rlat3, 
 // The finite-Q matrix of one Q-path row q4 = (path coordinate, Q) into the row-major dim x dim "HQ" buffer:
 // bands on the Q-shifted mesh, the merged window, the direct build over V (leading dimension ldv) and, for
 // |Q| != 0, the exchange term.  The plain-mesh bands must be current.
-static int build_q_matrix(wtb_ctx* c, const wtb_bse_params* p, const double* q4, const double* V, int ldv, zd** Hout) {
+static int build_q_matrix(wtb_ctx* c, const wtb_bse_params* p, const double* q4, const double* V, int ldv, double scs,
+                          zd** Hout) {
   const int nk = c->nk, nv = c->nv, nc = c->nc, w = c->w, nb = nv + nc;
   const long dim = (long)nk * nc * nv;
   cudaError_t err = cudaSuccess;
@@ -862,7 +863,7 @@ static int build_q_matrix(wtb_ctx* c, const wtb_bse_params* p, const double* q4,
   for (int d = 0; d < 3; ++d) kq.push_back(0.0);
   CKC(cudaMemcpyAsync(dkq, kq.data(), sizeof(double) * kq.size(), cudaMemcpyHostToDevice, c->s));
   CKC(launch_hk_eig(c->ws.get<zd>("hr", 0, &err), c->ws.get<int>("rvec", 0, &err), c->ws.get<int>("ndegen", 0, &err),
-                    c->nR, w, c->ws.get<double>("rlat", 0, &err), c->efermi, c->scs, dkq, nk, nv, nc, eq_all, vq_all,
+                    c->nR, w, c->ws.get<double>("rlat", 0, &err), c->efermi, scs, dkq, nk, nv, nc, eq_all, vq_all,
                     eq_win, vq_win, nocpq, c->st, c->s, false));
   CKC(launch_merge_windows(c->ws.get<double>("eig_win", 0, &err), c->ws.get<zd>("vec_win", 0, &err), eq_win, vq_win,
                            nk, nv, nc, w, em, vm, c->s));
@@ -901,7 +902,7 @@ int wtb_bse_build_q(wtb_ctx* c, const wtb_bse_params* p, const double* q4, doubl
   CKC(err);
   CKR(coulomb_table_into(c, p, V, Kpad));
   zd* H = nullptr;
-  CKR(build_q_matrix(c, p, q4, V, Kpad, &H));
+  CKR(build_q_matrix(c, p, q4, V, Kpad, c->scs, &H));
   if (hbse) {
     zd* staging = c->ws.get<zd>("Hout", (size_t)dim * dim, &err);
     CKC(err);
@@ -912,13 +913,24 @@ int wtb_bse_build_q(wtb_ctx* c, const wtb_bse_params* p, const double* q4, doubl
   return check_status(c);
 }
 
-int wtb_bsebnds(wtb_ctx* c, const wtb_bse_params* p, int nq, const double* qpath, double* exk) {
+static double temp_gap_correction(const wtb_temp_params* tp);
+
+// The Q loop of bsebnds, or of bsebndstemp with tp (scissor scs + tcor on both meshes, matrizelbsekqtemp's
+// weighting by f_v - f_c of the row's transition).
+static int bsebnds_impl(wtb_ctx* c, const wtb_bse_params* p, const wtb_temp_params* tp, int nq, const double* qpath,
+                        double* exk) {
   if (!c) return WTB_EBADARG;
   CKR(prep_device(c));
   if (!p || nq < 1 || !qpath || !exk) return set_err(c, WTB_EBADARG, "bad arguments");
   CKR(check_q_params(c, p));
+  if (tp && (tp->ta < 0 || tp->ta > 2 || !(tp->temp >= 0.0))) return set_err(c, WTB_EBADARG, "bad temperature keys");
+  const double scs = c->scs + (tp ? temp_gap_correction(tp) : 0.0);
   CKR(stage_mesh(c, p));
-  CKR(enqueue_bands(c, false));
+  const double scs0 = c->scs;
+  c->scs = scs;
+  const int rb = enqueue_bands(c, false);
+  c->scs = scs0;
+  CKR(rb);
   const int nk = c->nk;
   const long dim = (long)nk * c->nc * c->nv;
   cudaError_t err = cudaSuccess;
@@ -936,8 +948,20 @@ int wtb_bsebnds(wtb_ctx* c, const wtb_bse_params* p, int nq, const double* qpath
   for (int i = 0; i < nq && rc == WTB_OK; ++i) {
     const double q4[4] = {qpath[i], qpath[i + nq], qpath[i + 2 * (size_t)nq], qpath[i + 3 * (size_t)nq]};
     zd* H = nullptr;
-    rc = build_q_matrix(c, p, q4, V, Kpad, &H);
+    rc = build_q_matrix(c, p, q4, V, Kpad, scs, &H);
     if (rc != WTB_OK) break;
+    if (tp) {
+      cudaError_t e = cudaSuccess;
+      double* f = c->ws.get<double>("T_fq", dim, &e);
+      const double* em = c->ws.get<double>("eigm_win", 0, &e);
+      const double* dEq = c->ws.get<double>("dEq", 0, &e);
+      if (e == cudaSuccess) e = launch_fermi_weights(em, nk, c->nv, c->nc, tp->temp, f, c->s);
+      if (e == cudaSuccess) e = launch_temp_weight(H, dim, f, dEq, c->s);
+      if (e != cudaSuccess) {
+        rc = set_err(c, WTB_ECUDA, std::string("bsebndstemp weights: ") + cudaGetErrorString(e));
+        break;
+      }
+    }
     if (!ge || H != Hcap) {
       if (ge) cudaGraphExecDestroy(ge);
       ge = nullptr;
@@ -968,6 +992,16 @@ int wtb_bsebnds(wtb_ctx* c, const wtb_bse_params* p, int nq, const double* qpath
   c->have_solve = false;
   if (rc != WTB_OK) return rc;
   return check_status(c);
+}
+
+int wtb_bsebnds(wtb_ctx* c, const wtb_bse_params* p, int nq, const double* qpath, double* exk) {
+  return bsebnds_impl(c, p, nullptr, nq, qpath, exk);
+}
+
+int wtb_bsebndstemp(wtb_ctx* c, const wtb_bse_params* p, const wtb_temp_params* tp, int nq, const double* qpath,
+                    double* exk) {
+  if (!tp) return set_err(c, WTB_EBADARG, "temperature keys are NULL");
+  return bsebnds_impl(c, p, tp, nq, qpath, exk);
 }
 
 int wtb_zheev(wtb_ctx* c, int n, const double* A, int lda, double* W) {
@@ -1061,7 +1095,7 @@ int wtb_bsesolvertemp(wtb_ctx* c, const wtb_bse_params* p, const wtb_temp_params
   CKR(coulomb_table_into(c, &pp, V, Kpad));
   CKC(launch_bse_build<double>(c->ws.get<zd>("vec_win", 0, &err), dE, V, Kpad, nk, nv, nc, w, H, c->s));
   CKC(launch_fermi_weights(eig_win, nk, nv, nc, tp->temp, f, c->s));
-  CKC(launch_temp_weight(H, dim, f, dE, V, Kpad, nc * nv, c->s));
+  CKC(launch_temp_weight(H, dim, f, dE, c->s));
   CKC(dense_eig_prepare());
   // H is row-major, i.e. conj(H) column-major: its eigenvectors are conjugated back
   CKC(launch_dense_eig(H, (int)dim, (int)dim, false, W, Z, true, scratch, vscratch, c->s));
@@ -1280,7 +1314,11 @@ int wtb_bseoptproppol(wtb_ctx* c, int numbse, const double* dielf, double* props
   return optprop(c, numbse, dielf, 5, props);
 }
 
-int wtb_spoptics(wtb_ctx* c, const wtb_bse_params* p, float* rec) {
+static double temp_gap_correction(const wtb_temp_params* tp);
+
+// spoptics' records, or with tp the records bsesolvertemp writes (bands with scs + tcor, activities weighted by
+// f_v - f_c).
+static int spoptics_impl(wtb_ctx* c, const wtb_bse_params* p, const wtb_temp_params* tp, float* rec) {
   if (!c) return WTB_EBADARG;
   CKR(prep_device(c));
   if (!c->have_hr) return set_err(c, WTB_ESTATE, "H(R) not set (call wtb_set_hr first)");
@@ -1292,9 +1330,22 @@ int wtb_spoptics(wtb_ctx* c, const wtb_bse_params* p, float* rec) {
     return set_err(c, WTB_EBADARG, "unknown precision or operator mode");
   const long dim = (long)p->ngrid[0] * p->ngrid[1] * p->ngrid[2] * p->nc * p->nv;
   if (dim > (1L << 30) / 15) return set_err(c, WTB_EBADARG, "too many transitions");
-  CKR(ensure_bands_for(c, p));
+  if (tp && (tp->ta < 0 || tp->ta > 2 || !(tp->temp >= 0.0))) return set_err(c, WTB_EBADARG, "bad temperature keys");
+  CKR(stage_mesh(c, p));
+  const double scs0 = c->scs;
+  c->scs = scs0 + (tp ? temp_gap_correction(tp) : 0.0);
+  const int rb = enqueue_bands(c, tc_form(p));
+  c->scs = scs0;
+  CKR(rb);
+  CKR(check_status(c));
   CKR(compute_optics(c, p));
   cudaError_t err = cudaSuccess;
+  double* f = nullptr;
+  if (tp) {
+    f = c->ws.get<double>("spo_f", dim, &err);
+    CKC(err);
+    CKC(launch_fermi_weights(c->ws.get<double>("eig_win", 0, &err), c->nk, c->nv, c->nc, tp->temp, f, c->s));
+  }
   float* raw = c->ws.get<float>("spo_raw", (size_t)15 * dim, &err);
   float* out = c->ws.get<float>("spo_out", (size_t)15 * dim, &err);
   float* key = c->ws.get<float>("spo_key", dim, &err);
@@ -1302,9 +1353,16 @@ int wtb_spoptics(wtb_ctx* c, const wtb_bse_params* p, float* rec) {
   CKC(err);
   CKC(launch_sp_records(c->ws.get<double>("kpt", 0, &err), c->ws.get<int>("nocp", 0, &err),
                         c->ws.get<double>("eig_win", 0, &err), c->ws.get<zd>("hrvel", 0, &err), c->nk, c->nv, c->nc,
-                        raw, key, rank, out, c->s));
+                        f, raw, key, rank, out, c->s));
   CKC(cudaMemcpyAsync(rec, out, sizeof(float) * 15 * dim, cudaMemcpyDeviceToHost, c->s));
   return check_status(c);
+}
+
+int wtb_spoptics(wtb_ctx* c, const wtb_bse_params* p, float* rec) { return spoptics_impl(c, p, nullptr, rec); }
+
+int wtb_spoptics_temp(wtb_ctx* c, const wtb_bse_params* p, const wtb_temp_params* tp, float* rec) {
+  if (!tp) return set_err(c, WTB_EBADARG, "temperature keys are NULL");
+  return spoptics_impl(c, p, tp, rec);
 }
 
 int wtb_bse_matvec(wtb_ctx* c, const wtb_bse_params* p, int ncol, const double* X, double* Y) {

@@ -272,8 +272,10 @@ cudaError_t launch_spectrum(const double* Ws, int nrows, const double* f, int nc
 cudaError_t launch_optprops(const double* dielf, int nesp, int ncomp, double* props, cudaStream_t s);
 // The IPA transition records rec(dim, 15) (REAL(4), column-major) of the bands and velocity matrix elements
 // hr[5][dim], stably sorted by transition energy into sorted; key(dim), rank(dim) and rec(dim, 15) are scratch.
+// f (nullable): the activity columns weighted by f_v - f_c (the temperature solver's records).
 cudaError_t launch_sp_records(const double* kpt, const int* nocp, const double* eig_win, const zd* hr, int nk, int nv,
-                              int nc, float* rec, float* key, int* rank, float* sorted, cudaStream_t s);
+                              int nc, const double* f, float* rec, float* key, int* rank, float* sorted,
+                              cudaStream_t s);
 
 // ----------------------------------------------------------------------------- finite-Q BSE
 // Merged band window of the finite-Q basis: valence slots from the plain mesh, conduction slots from the
@@ -288,9 +290,9 @@ cudaError_t launch_exchange(const zd* vec_m, int nk, int nv, int nc, int w, cons
 // f[I] = f_v - f_c of transition I at temp (K) (fermidisteh).
 cudaError_t launch_fermi_weights(const double* eig_win, int nk, int nv, int nc, double temp, double* f,
                                  cudaStream_t s);
-// The row-major direct matrix H (dim x dim) weighted in place as ZHEEV 'U' reads matrizelbsetemp's upper triangle.
-cudaError_t launch_temp_weight(zd* H, long dim, const double* f, const double* dE, const double* V, int ldv, int nvc,
-                               cudaStream_t s);
+// The row-major BSE matrix H (dim x dim, Q = 0 or finite Q) weighted in place as ZHEEV 'U' reads the upper
+// triangle of matrizelbsetemp / matrizelbsekqtemp; dE the transition energies of H's diagonal.
+cudaError_t launch_temp_weight(zd* H, long dim, const double* f, const double* dE, cudaStream_t s);
 // dielbseptemp's eight activities acts(dim, 8) of the eigenvectors Z (row-major) and hr[5][dim].
 cudaError_t launch_temp_acts(const zd* Z, int dim, const zd* hr, const double* f, int dtfull, int cpol, double* acts,
                              cudaStream_t s);
