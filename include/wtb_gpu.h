@@ -178,6 +178,13 @@ int wtb_bsedielrawpol(wtb_ctx* ctx, const wtb_bse_params* p, int dimse, const do
  * (src/module_math.F90:287-308).  Columns 7-13 are sp_optics.dat, columns 7-10 and 14-15 sp_optics-pol.dat. */
 int wtb_spoptics(wtb_ctx* ctx, const wtb_bse_params* p, float* rec);
 
+/* Replaces spoptpolbz (src/module_bse.F90:4532-4797) without its text files: for each k-point of the mesh of p
+ * (column-major act(nk, 6)) the BZ-resolved optical activity summed over the nc x nv transitions,
+ * |<c|dH/dk_a|v> / (E_c - E_v + i sme)|^2 for x y z (optspbz, src/module_optics.F90:257-311; sme = p->cshift),
+ * the circular sp / sm activities and the dichroism (sp - sm)/(sp + sm) — the last column of bz_act_*.dat and
+ * dichroism.dat.  An insulator is required (the same occupied count at every k-point). */
+int wtb_spoptpolbz(wtb_ctx* ctx, const wtb_bse_params* p, double* act);
+
 /* Replace spdielraw and spdielrawpol (src/module_bse.F90:4090-4308, :4318-4524): the broadened
  * independent-particle spectrum of the dimsp transitions esp with acts(dimsp, 6) = xx yy zz xy xz yz
  * (dielf(numbse, 3, 6), rtype 1 for xx yy zz) or acts(dimsp, 5) = xx yy zz sp sm (dielf(numbse, 3, 5),
@@ -264,11 +271,13 @@ int wtb_write_exc_wf(const char* path, int nk, int nc, int nv, const int* nocpk,
                      double energy, const double* ewf);
 /* Replaces exclft over the rows of lifetime (src/module_bse.F90:326-370, :3271-3349): fosc(dim, 7) the columns of
  * bse_opt_diel.dat, sysdim "3D" / "2D" / "1D" with the lattice of wtb_set_hr; lft(dim, 4) radiative lifetimes (s)
- * for xx+yy+zz, xx, yy, zz. */
-int wtb_exciton_lifetime(wtb_ctx* ctx, const char* sysdim, const int* ngrid, int dim, const double* fosc,
+ * for xx+yy+zz, xx, yy, zz.  pol = 1 replaces lifetimepol (:3353-3432): fosc(dim, 6) the columns of
+ * bse_opt_diel-pol.dat, lft(dim, 6) adding sp and sm. */
+int wtb_exciton_lifetime(wtb_ctx* ctx, const char* sysdim, const int* ngrid, int dim, const double* fosc, int pol,
                          double* lft);
-/* exciton_lifetime.dat (1F15.4,4E15.4) from the energies and lft(dim, 4). */
-int wtb_write_exciton_lifetime(const char* path, int dim, const double* energy, const double* lft);
+/* exciton_lifetime.dat (1F15.4,4E15.4) from the energies and lft(dim, 4), or exciton_lifetime-pol.dat
+ * (1F15.4,6E15.4) from lft(dim, 6) with pol = 1. */
+int wtb_write_exciton_lifetime(const char* path, int dim, const double* energy, const double* lft, int pol);
 /* One Fortran edit descriptor applied to x (kind 'F', 'E' or 'I' with w, d (m for I)) into out (>= w+1 bytes). */
 int wtb_fortran_format(char kind, double x, int w, int d, char* out, int outlen);
 

@@ -483,6 +483,30 @@ def bsebndstemp(sysm, p, qpath, temp, ta="FA", st=0.0, phavg=0.0):
     return out
 
 
+def spoptpolbz(sysm, p):
+    """BZ-resolved optical activity (src/module_bse.F90:4532-4797): per k-point the sums over the nc x nv
+    transitions of |h_a|^2, h_a = <c|dH/dk_a|v> / (E_c - E_v + i sme) (optspbz, src/module_optics.F90:257-311,
+    then a complex division; sme = CSHIFT in double), the circular |n (h_x +- i h_y)|^2 with n = 1/sqrt(2) in
+    single precision, and (sp - sm)/(sp + sm).  Returns act (nk, 6)."""
+    kpt = monhkhorst_pack(p.ngrid[0], p.ngrid[1], p.ngrid[2], p.mshift, sysm.rlat)
+    eigv, vec, nocpk = bands(sysm, p, kpt)
+    act = np.zeros((len(kpt), 6))
+    n = INV_SQRT2_F32
+    for k in range(len(kpt)):
+        dx, dy, dz = hlm(kpt[k], sysm)
+        s = np.zeros(5)
+        for c in range(p.nc):
+            for v in range(p.nv):
+                cv, vv = vec[k, p.nv + c], vec[k, v]
+                d = (eigv[k, p.nv + c] - eigv[k, v]) + 1j * p.cshift
+                hx, hy, hz = [(np.conj(cv) @ (D @ vv)) / d for D in (dx, dy, dz)]
+                s += [abs(hx) ** 2, abs(hy) ** 2, abs(hz) ** 2, abs(n * (hx + 1j * hy)) ** 2,
+                      abs(n * (hx - 1j * hy)) ** 2]
+        act[k, :5] = s
+        act[k, 5] = (s[3] - s[4]) / (s[3] + s[4])
+    return act
+
+
 def bse_matvec_factored(x, eigv, vec, kpt, p, rlat, V=None):
     """Matrix-free y = H x through V(k,k') and the orbital factorisation; same operator as bse_build."""
     nk = len(kpt)

@@ -317,3 +317,20 @@ def test_exciton_lifetime(ctx, small, sysdim):
     with pytest.raises(api.WTBError) as e:
         ctx.exciton_lifetime("4D", p.ngrid, fosc)
     assert "Wrong System dimension" in str(e.value)
+    # lifetimepol: the six columns of bse_opt_diel-pol.dat (energy, xx, yy, zz, sp, sm)
+    fp = fosc[:, :6].copy()
+    lp = ctx.exciton_lifetime(sysdim, p.ngrid, fp, pol=True)
+    np.testing.assert_allclose(lp[:, :4], ref, rtol=1e-14)
+    for c in (4, 5):
+        np.testing.assert_allclose(lp[:, c], O.exclft(sysdim, p.ngrid, sysm.rlat, fp[:, c], fp[:, 0]), rtol=1e-14)
+
+
+def test_spoptpolbz(ctx, small):
+    """BZ-resolved x y z sp sm activity and dichroism per k-point against the oracle; sp + sm = 2 n^2 (x + y)
+    with n = 1/sqrt(2) rounded to single precision."""
+    sysm, p, _ = small
+    ctx.set_hr(sysm)
+    act = ctx.spoptpolbz(p)
+    ref = O.spoptpolbz(sysm, p)
+    np.testing.assert_allclose(act, ref, rtol=1e-9, atol=1e-12 * np.abs(ref[:, :5]).max())
+    np.testing.assert_allclose(act[:, 3] + act[:, 4], 2 * O.INV_SQRT2_F32 ** 2 * (act[:, 0] + act[:, 1]), rtol=1e-12)

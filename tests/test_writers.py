@@ -127,3 +127,16 @@ def test_writer_rejects_unwritable_path(built):
 
     with pytest.raises(api.WTBError):
         api.write_exciton_lifetime("/nonexistent-dir/x.dat", np.ones(2), np.ones((2, 4)))
+
+
+def test_lifetime_pol_file(built, tmp_path):
+    from wtb_gb300 import api
+
+    e = np.array([1.5, 2.25])
+    lft = np.array([[1e-12, 2e-12, 3e-12, 4e-12, 5e-12, 6e-12], [7e-9, 8e-9, 9e-9, np.inf, 1e-8, 2e-8]])
+    path = os.path.join(tmp_path, "exciton_lifetime-pol.dat")
+    api.write_exciton_lifetime(path, e, lft, pol=True)
+    lines = open(path).read().splitlines()
+    assert lines[0] == " #energy(eV) sum-lft(s)  x-lft(s) y-lft(s) z-lft(s) sp-lft(s) sm-lft(s)"
+    for i in range(2):
+        assert lines[1 + i] == O.fortran_F(e[i], 15, 4) + "".join(O.fortran_E(lft[i, c], 15, 4) for c in range(6))

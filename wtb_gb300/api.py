@@ -100,6 +100,7 @@ def _load():
         "wtb_spdielrawpol": [P, C.POINTER(CParams), C.c_int, dp, dp, dp],
         "wtb_bseoptproppol": [P, C.c_int, dp, dp],
         "wtb_spoptics": [P, C.POINTER(CParams), C.POINTER(C.c_float)],
+        "wtb_spoptpolbz": [P, C.POINTER(CParams), dp],
         "wtb_kpathbse": [dp, dp, dp, C.c_int, dp, C.c_int, dp],
         "wtb_bse_build_q": [P, C.POINTER(CParams), dp, dp],
         "wtb_bsebnds": [P, C.POINTER(CParams), C.c_int, dp, dp],
@@ -109,8 +110,8 @@ def _load():
         "wtb_write_sp_optics": [C.c_char_p, C.c_int, C.POINTER(C.c_float), C.c_int],
         "wtb_write_tm_coef": [C.c_char_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_int],
         "wtb_write_exc_wf": [C.c_char_p, C.c_int, C.c_int, C.c_int, ip, dp, C.c_int, C.c_double, dp],
-        "wtb_exciton_lifetime": [P, C.c_char_p, ip, C.c_int, dp, dp],
-        "wtb_write_exciton_lifetime": [C.c_char_p, C.c_int, dp, dp],
+        "wtb_exciton_lifetime": [P, C.c_char_p, ip, C.c_int, dp, C.c_int, dp],
+        "wtb_write_exciton_lifetime": [C.c_char_p, C.c_int, dp, dp, C.c_int],
         "wtb_fortran_format": [C.c_char, C.c_double, C.c_int, C.c_int, C.c_char_p, C.c_int],
         "wtb_bsesolvertemp": [P, C.POINTER(CParams), C.POINTER(CTempParams), dp, dp, dp, dp],
         "wtb_bsebndstemp": [P, C.POINTER(CParams), C.POINTER(CTempParams), C.c_int, dp, dp],
@@ -263,10 +264,13 @@ def write_exc_wf(path, nocpk, kpt, nc, nv, excnum, energy, ewf):
                              int(excnum), float(energy), e.ctypes.data_as(C.POINTER(C.c_double))), "wtb_write_exc_wf")
 
 
-def write_exciton_lifetime(path, energy, lft):
+def write_exciton_lifetime(path, energy, lft, pol=False):
+    """exciton_lifetime.dat (lft (dim, 4)) or exciton_lifetime-pol.dat (pol=True, lft (dim, 6))."""
     e = np.ascontiguousarray(energy, dtype=np.float64)
     L = np.asfortranarray(lft, dtype=np.float64)
-    _w(_lib.wtb_write_exciton_lifetime(os.fsencode(path), len(e), _dp(e), _dp(L)), "wtb_write_exciton_lifetime")
+    assert L.shape == (len(e), 6 if pol else 4)
+    _w(_lib.wtb_write_exciton_lifetime(os.fsencode(path), len(e), _dp(e), _dp(L), int(bool(pol))),
+       "wtb_write_exciton_lifetime")
 
 
 def eigsys(nthreads, scs, exc, nocp, ffactor, kx, ky, kz, w90basis, nvec, rlat, rvec, hopmatrices, ihopmatrices,
@@ -423,13 +427,15 @@ class Context:
             out["HE"] = HE
         return out
 
-    def exciton_lifetime(self, sysdim, ngrid, fosc):
-        """exclft over the rows fosc (dim, 7) of bse_opt_diel.dat: lft (dim, 4) for xx+yy+zz, xx, yy, zz."""
+    def exciton_lifetime(self, sysdim, ngrid, fosc, pol=False):
+        """exclft over the rows fosc (dim, 7) of bse_opt_diel.dat: lft (dim, 4) for xx+yy+zz, xx, yy, zz; with
+        pol the rows (dim, 6) of bse_opt_diel-pol.dat and lft (dim, 6) adding sp, sm (lifetimepol)."""
         F = np.asfortranarray(fosc, dtype=np.float64)
+        assert F.shape[1] == (6 if pol else 7)
         g = np.ascontiguousarray(ngrid, dtype=np.int32)
-        L = np.zeros((F.shape[0], 4), order="F")
+        L = np.zeros((F.shape[0], 6 if pol else 4), order="F")
         self._chk(_lib.wtb_exciton_lifetime(self._h, sysdim.encode(), g.ctypes.data_as(C.POINTER(C.c_int)),
-                                            F.shape[0], _dp(F), _dp(L)), "wtb_exciton_lifetime")
+                                            F.shape[0], _dp(F), int(bool(pol)), _dp(L)), "wtb_exciton_lifetime")
         return L
 
     def bse_matvec(self, p: BSEParams, X, precision="fp64", op="matfree"):
@@ -557,6 +563,14 @@ class Context:
         self._chk(_lib.wtb_spoptics_temp(self._h, C.byref(cp), C.byref(tp), rec.ctypes.data_as(C.POINTER(C.c_float))),
                   "wtb_spoptics_temp")
         return rec
+
+    def spoptpolbz(self, p: BSEParams):
+        """spoptpolbz: act (nk, 6) = x y z sp sm activity per k-point of the mesh and the dichroism."""
+        nk = p.ngrid[0] * p.ngrid[1] * p.ngrid[2]
+        act = np.zeros((nk, 6), order="F")
+        cp = cparams(p)
+        self._chk(_lib.wtb_spoptpolbz(self._h, C.byref(cp), _dp(act)), "wtb_spoptpolbz")
+        return act
 
     def spoptics(self, p: BSEParams):
         """spoptics: the (dimsp, 15) float32 records (columns SP_COLUMNS) sorted by transition energy."""

@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(kHkThreads) optics_kernel(const cplx<T>* __res
                                                             const double* __restrict__ kpt, int nk, int nv, int nc,
                                                             const double* __restrict__ eig_win,
                                                             const zd* __restrict__ vec_win, float s32,
-                                                            zd* __restrict__ hout) {
+                                                            zd* __restrict__ hout, int raw) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int k = blockIdx.x;
   if (k >= nk) return;
@@ -262,7 +262,7 @@ __global__ void __launch_bounds__(kHkThreads) optics_kernel(const cplx<T>* __res
       // factor = Re(1/(E_c - E_v + i*CSHIFT_f32)) (a complex assigned to a real in optsp)
       const double de = eig_win[(size_t)k * nb + nv + c] - eig_win[(size_t)k * nb + v];
       const double sf = (double)s32;
-      const double factor = de / (de * de + sf * sf);
+      const double factor = raw ? 1.0 : de / (de * de + sf * sf);  // raw: <c|dH/dk_a|v> unscaled (optspbz)
       hout[a * dim + (size_t)k * dimk + e] = cscale(acc, factor);
     }
   }
@@ -478,7 +478,7 @@ cudaError_t launch_hk_eig(const zd* hr, const int* rvec, const int* ndegen, int 
 
 cudaError_t launch_optics(const zd* hr, const int* rvec, const int* ndegen, int nR, int w, const double* rlat_rm,
                           const double* kpt, int nk, int nv, int nc, const double* eig_win, const zd* vec_win,
-                          double cshift, zd* hout, cudaStream_t s, const zf* hr32) {
+                          double cshift, zd* hout, cudaStream_t s, const zf* hr32, bool raw) {
   const int nb = nv + nc;
   const size_t smem = (size_t)(w * w + nb * w + nv * w + nR) * sizeof(zd) + nR * sizeof(double) + nR * sizeof(zd) + 16;
   const bool mixed = hr32 != nullptr;
@@ -487,10 +487,10 @@ cudaError_t launch_optics(const zd* hr, const int* rvec, const int* ndegen, int 
   if (e != cudaSuccess) return e;
   if (mixed)
     optics_kernel<float><<<nk, kHkThreads, smem, s>>>(hr32, rvec, ndegen, nR, w, rlat_rm, kpt, nk, nv, nc, eig_win,
-                                                      vec_win, (float)cshift, hout);
+                                                      vec_win, (float)cshift, hout, raw ? 1 : 0);
   else
     optics_kernel<double><<<nk, kHkThreads, smem, s>>>(hr, rvec, ndegen, nR, w, rlat_rm, kpt, nk, nv, nc, eig_win,
-                                                       vec_win, (float)cshift, hout);
+                                                       vec_win, (float)cshift, hout, raw ? 1 : 0);
   ++g_launch_count;
   return cudaGetLastError();
 }

@@ -349,6 +349,50 @@ __global__ void permute_rows_kernel(const float* __restrict__ in, const int* __r
   if (r >= 0 && r < n) out[(size_t)q * n + r] = in[e];
 }
 
+// spoptpolbz (src/module_bse.F90:4532-4797) per k-point: h_a = <c|dH/dk_a|v> / (E_c - E_v + i sme) (optspbz and
+// the complex division, src/module_optics.F90:257-311), summed |h_a|^2 over the nc x nv transitions for a = x y z,
+// |n (h_x +- i h_y)|^2 with n = 1/sqrt(2) in single precision for sp / sm, and (sp - sm)/(sp + sm).  The reference
+// takes the valence bands up to nocp of the first k-point at every k; the window here is each k-point's own, so
+// a mesh whose occupied count varies (a metal) is refused (status 103).
+__global__ void bz_activity_kernel(const zd* __restrict__ hraw, const double* __restrict__ eig_win,
+                                   const int* __restrict__ nocp, int nk, int nv, int nc, double sme,
+                                   double* __restrict__ act, DevStatus* st) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nk) return;
+  if (nocp[k] != nocp[0]) {
+    dev_fail(st, 103, k);
+    return;
+  }
+  const int nb = nv + nc, dimk = nc * nv;
+  const size_t dim = (size_t)nk * dimk;
+  const double nrm = (double)0.70710677f;
+  double sx = 0.0, sy = 0.0, sz = 0.0, sp = 0.0, sm = 0.0;
+  for (int e = 0; e < dimk; ++e) {
+    const int c = e / nv, v = e % nv;
+    const double de = eig_win[(size_t)k * nb + nv + c] - eig_win[(size_t)k * nb + v];
+    const double den = de * de + sme * sme;
+    zd h[3];
+    for (int a = 0; a < 3; ++a) {
+      const zd r = hraw[(size_t)a * dim + (size_t)k * dimk + e];
+      // r / (de + i sme) = r (de - i sme) / den
+      h[a] = mk<double>((r.re * de + r.im * sme) / den, (r.im * de - r.re * sme) / den);
+    }
+    sx += h[0].re * h[0].re + h[0].im * h[0].im;
+    sy += h[1].re * h[1].re + h[1].im * h[1].im;
+    sz += h[2].re * h[2].re + h[2].im * h[2].im;
+    const zd p = mk<double>(nrm * (h[0].re - h[1].im), nrm * (h[0].im + h[1].re));  // n (hx + i hy)
+    const zd q = mk<double>(nrm * (h[0].re + h[1].im), nrm * (h[0].im - h[1].re));  // n (hx - i hy)
+    sp += p.re * p.re + p.im * p.im;
+    sm += q.re * q.re + q.im * q.im;
+  }
+  act[0 * (size_t)nk + k] = sx;
+  act[1 * (size_t)nk + k] = sy;
+  act[2 * (size_t)nk + k] = sz;
+  act[3 * (size_t)nk + k] = sp;
+  act[4 * (size_t)nk + k] = sm;
+  act[5 * (size_t)nk + k] = (sp - sm) / (sp + sm);
+}
+
 }  // namespace
 
 cudaError_t launch_oscillators(const zd* A, int lda, int nev, int dim, const zd* hr, double* osc, double* partial,
@@ -415,6 +459,12 @@ cudaError_t launch_sp_records(const double* kpt, const int* nocp, const double* 
   e = cudaMemsetAsync(sorted, 0, sizeof(float) * 15 * n, s);
   if (e != cudaSuccess) return e;
   permute_rows_kernel<<<(unsigned)((15L * n + 255) / 256), 256, 0, s>>>(rec, rank, n, 15, sorted); ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bz_activity(const zd* hraw, const double* eig_win, const int* nocp, int nk, int nv, int nc,
+                               double sme, double* act, DevStatus* st, cudaStream_t s) {
+  bz_activity_kernel<<<(nk + 127) / 128, 128, 0, s>>>(hraw, eig_win, nocp, nk, nv, nc, sme, act, st); ++g_launch_count;
   return cudaGetLastError();
 }
 

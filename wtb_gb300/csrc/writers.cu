@@ -15,7 +15,7 @@
 //   sp_optics.dat / -pol      :2296-2297, :2366-2367 (7F15.4 / 6F15.4)
 //   tm_coef.dat / -pol        :2300-2311, :2370-2377 (3F10.4,3I10.0,7F10.4 / ...,6F10.4)
 //   exc_wf_<n>.dat            excwf2, :374-408 ((I,3F15.4,2I,2E15.4))
-//   exciton_lifetime.dat      lifetime, :3271-3349 ((1F15.4,4E15.4))
+//   exciton_lifetime.dat      lifetime, :3271-3349 ((1F15.4,4E15.4)); -pol: lifetimepol, :3353-3432 ((1F15.4,6E15.4))
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -95,19 +95,26 @@ std::string fortran_I(long v, int w, int m) {
 namespace {
 
 // Radiative lifetimes of exclft (src/module_bse.F90:326-370) for the rows of bse_opt_diel.dat as lifetime reads
-// them (src/module_bse.F90:3271-3349): fosc(dim, 7) = energy, xx, yy, zz, ...; lft(dim, 4) = for xx+yy+zz, xx, yy,
-// zz.  The constants are the reference's single-precision literals; sysdim 3 / 2 / 1.
-__global__ void lifetime_kernel(const double* __restrict__ fosc, int dim, int sysdim, double ng, double vc2d,
-                                double a11, double* __restrict__ lft) {
+// them (src/module_bse.F90:3271-3349): fosc(dim, 7) = energy, xx, yy, zz, ...; lft(dim, 4) = for xx+yy+zz, xx,
+// yy, zz.  pol: the rows of bse_opt_diel-pol.dat as lifetimepol reads them (:3353-3432), fosc(dim, 6) = energy,
+// xx, yy, zz, sp, sm and lft(dim, 6) adding sp, sm.  The constants are the reference's single-precision
+// literals; sysdim 3 / 2 / 1.
+__global__ void lifetime_kernel(const double* __restrict__ fosc, int dim, int pol, int sysdim, double ng,
+                                double vc2d, double a11, double* __restrict__ lft) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= dim) return;
   const double cfe = (double)7.297E-3f, lspd = (double)299.792E16f, hbar = (double)6.582E-16f;
   const double pi = (double)3.14159274101257324f;
   const size_t n = (size_t)dim;
   const double e = fosc[i];
-  const double f[4] = {fosc[n + i] + fosc[2 * n + i] + fosc[3 * n + i], fosc[n + i], fosc[2 * n + i],
-                       fosc[3 * n + i]};
-  for (int c = 0; c < 4; ++c) {
+  const int nout = pol ? 6 : 4;
+  double f[6] = {fosc[n + i] + fosc[2 * n + i] + fosc[3 * n + i], fosc[n + i], fosc[2 * n + i], fosc[3 * n + i],
+                 0.0, 0.0};
+  if (pol) {
+    f[4] = fosc[4 * n + i];
+    f[5] = fosc[5 * n + i];
+  }
+  for (int c = 0; c < nout; ++c) {
     double l;
     if (sysdim == 3) {
       const double aux1 = (4.0 * cfe) * (e * e * e);
@@ -285,21 +292,23 @@ int wtb_write_exc_wf(const char* path, int nk, int nc, int nv, const int* nocpk,
   return std::ferror(f.f) ? WTB_EBADARG : WTB_OK;
 }
 
-int wtb_write_exciton_lifetime(const char* path, int dim, const double* energy, const double* lft) {
+int wtb_write_exciton_lifetime(const char* path, int dim, const double* energy, const double* lft, int pol) {
   if (!path || dim < 1 || !energy || !lft) return WTB_EBADARG;
   File f(path);
   if (!f.f) return WTB_EBADARG;
   const size_t n = (size_t)dim;
-  f.line(ld_chars({"#energy(eV) sum-lft(s)  x-lft(s) y-lft(s) z-lft(s)"}));
+  const int nout = pol ? 6 : 4;
+  f.line(pol ? ld_chars({"#energy(eV) sum-lft(s)  x-lft(s) y-lft(s) z-lft(s) sp-lft(s) sm-lft(s)"})
+             : ld_chars({"#energy(eV) sum-lft(s)  x-lft(s) y-lft(s) z-lft(s)"}));
   for (size_t i = 0; i < n; ++i) {
     std::string s = fortran_F(energy[i], 15, 4);
-    for (int c = 0; c < 4; ++c) s += fortran_E(lft[c * n + i], 15, 4);
+    for (int c = 0; c < nout; ++c) s += fortran_E(lft[c * n + i], 15, 4);
     f.line(s);
   }
   return std::ferror(f.f) ? WTB_EBADARG : WTB_OK;
 }
 
-int wtb_exciton_lifetime(wtb_ctx* c, const char* sysdim, const int* ngrid, int dim, const double* fosc,
+int wtb_exciton_lifetime(wtb_ctx* c, const char* sysdim, const int* ngrid, int dim, const double* fosc, int pol,
                          double* lft) {
   if (!c) return WTB_EBADARG;
   if (cudaSetDevice(c->device) != cudaSuccess) return WTB_ENODEV;
@@ -315,15 +324,16 @@ int wtb_exciton_lifetime(wtb_ctx* c, const char* sysdim, const int* ngrid, int d
   const double vc2d = std::sqrt(vx * vx + vy * vy + vz * vz);  // vcell2D
   const double ng = (double)(ngrid[0] * ngrid[1] * ngrid[2]);
   cudaError_t err = cudaSuccess;
-  double* df = c->ws.get<double>("lft_in", (size_t)7 * dim, &err);
-  double* dl = c->ws.get<double>("lft_out", (size_t)4 * dim, &err);
-  if (err == cudaSuccess) err = cudaMemcpyAsync(df, fosc, sizeof(double) * 7 * dim, cudaMemcpyHostToDevice, c->s);
+  const int nin = pol ? 6 : 7, nout = pol ? 6 : 4;
+  double* df = c->ws.get<double>("lft_in", (size_t)nin * dim, &err);
+  double* dl = c->ws.get<double>("lft_out", (size_t)nout * dim, &err);
+  if (err == cudaSuccess) err = cudaMemcpyAsync(df, fosc, sizeof(double) * nin * dim, cudaMemcpyHostToDevice, c->s);
   if (err == cudaSuccess) {
-    wtb::lifetime_kernel<<<(dim + 255) / 256, 256, 0, c->s>>>(df, dim, sd, ng, vc2d, r[0], dl);
+    wtb::lifetime_kernel<<<(dim + 255) / 256, 256, 0, c->s>>>(df, dim, pol ? 1 : 0, sd, ng, vc2d, r[0], dl);
     ++wtb::g_launch_count;
     err = cudaGetLastError();
   }
-  if (err == cudaSuccess) err = cudaMemcpyAsync(lft, dl, sizeof(double) * 4 * dim, cudaMemcpyDeviceToHost, c->s);
+  if (err == cudaSuccess) err = cudaMemcpyAsync(lft, dl, sizeof(double) * nout * dim, cudaMemcpyDeviceToHost, c->s);
   if (err != cudaSuccess) return wtb::ctx_set_err(c, WTB_ECUDA, std::string("lifetime: ") + cudaGetErrorString(err));
   return wtb::ctx_check_status(c);
 }

@@ -70,6 +70,9 @@ int check_status(wtb_ctx* c) {
     case 102:
       return set_err(c, WTB_EBADARG, "Number of conduction states higher then unocuppied states (k-point " +
                                          std::to_string(h.info + 1) + ")");
+    case 103:
+      return set_err(c, WTB_EBADARG, "spoptpolbz: the number of occupied states differs between k-points (k-point " +
+                                         std::to_string(h.info + 1) + "); the BZ-resolved activity needs an insulator");
     case 201:
       return set_err(c, WTB_ENOCONV, "The algorithm failed to compute eigenvalues.");
     default:
@@ -1359,6 +1362,33 @@ static int spoptics_impl(wtb_ctx* c, const wtb_bse_params* p, const wtb_temp_par
 }
 
 int wtb_spoptics(wtb_ctx* c, const wtb_bse_params* p, float* rec) { return spoptics_impl(c, p, nullptr, rec); }
+
+int wtb_spoptpolbz(wtb_ctx* c, const wtb_bse_params* p, double* act) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (!c->have_hr) return set_err(c, WTB_ESTATE, "H(R) not set (call wtb_set_hr first)");
+  if (!p || !act) return set_err(c, WTB_EBADARG, "bad arguments");
+  if (p->ngrid[0] < 1 || p->ngrid[1] < 1 || p->ngrid[2] < 1) return set_err(c, WTB_EBADARG, "ngrid must be >= 1");
+  if (p->nc < 1 || p->nv < 1) return set_err(c, WTB_EBADARG, "nc and nv must be >= 1");
+  if (p->nv + p->nc > c->w) return set_err(c, WTB_EBADARG, "nv + nc exceeds w90basis");
+  CKR(stage_mesh(c, p));
+  CKR(enqueue_bands(c, false));
+  CKR(check_status(c));
+  const int nk = c->nk;
+  const long dim = (long)nk * c->nc * c->nv;
+  cudaError_t err = cudaSuccess;
+  zd* hraw = c->ws.get<zd>("hrraw", (size_t)5 * dim, &err);
+  double* dact = c->ws.get<double>("bz_act", (size_t)6 * nk, &err);
+  CKC(err);
+  CKC(launch_optics(c->ws.get<zd>("hr", 0, &err), c->ws.get<int>("rvec", 0, &err), c->ws.get<int>("ndegen", 0, &err),
+                    c->nR, c->w, c->ws.get<double>("rlat", 0, &err), c->ws.get<double>("kpt", 0, &err), nk, c->nv,
+                    c->nc, c->ws.get<double>("eig_win", 0, &err), c->ws.get<zd>("vec_win", 0, &err), p->cshift, hraw,
+                    c->s, nullptr, true));
+  CKC(launch_bz_activity(hraw, c->ws.get<double>("eig_win", 0, &err), c->ws.get<int>("nocp", 0, &err), nk, c->nv,
+                         c->nc, p->cshift, dact, c->st, c->s));
+  CKC(cudaMemcpyAsync(act, dact, sizeof(double) * 6 * nk, cudaMemcpyDeviceToHost, c->s));
+  return check_status(c);
+}
 
 int wtb_spoptics_temp(wtb_ctx* c, const wtb_bse_params* p, const wtb_temp_params* tp, float* rec) {
   if (!tp) return set_err(c, WTB_EBADARG, "temperature keys are NULL");

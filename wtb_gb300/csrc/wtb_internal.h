@@ -103,7 +103,12 @@ cudaError_t launch_hk_eig(const zd* hr, const int* rvec, const int* ndegen, int 
 cudaError_t launch_optics(const zd* hr, const int* rvec, const int* ndegen, int nR, int w,
                           const double* rlat_rm, const double* kpt, int nk, int nv, int nc,
                           const double* eig_win, const zd* vec_win, double cshift, zd* hout, cudaStream_t s,
-                          const zf* hr32 = nullptr);
+                          const zf* hr32 = nullptr, bool raw = false);
+// BZ-resolved optical activity of spoptpolbz: per k-point the sums over the window's transitions of
+// |<c|dH/dk_a|v>/(E_c - E_v + i sme)|^2 for x y z and the circular sp sm, and the dichroism (sp-sm)/(sp+sm):
+// act(nk, 6), from the unscaled matrix elements hraw[3][dim] of launch_optics(raw).
+cudaError_t launch_bz_activity(const zd* hraw, const double* eig_win, const int* nocp, int nk, int nv, int nc,
+                               double sme, double* act, DevStatus* st, cudaStream_t s);
 // V(k,k') table, double, leading dimension ldv (>= nk), zero padding left as is.
 cudaError_t launch_coulomb(const CoulParams& p, const double* kpt1, int n1, const double* kpt2, int n2,
                            double* V, int ldv, cudaStream_t s);
