@@ -207,6 +207,12 @@ int wtb_kpathbse(const double* rlat1, const double* rlat2, const double* rlat3, 
  * hbse(dim, dim) complex(8), full Hermitian (the reference fills the upper triangle).  dim <= 20000. */
 int wtb_bse_build_q(wtb_ctx* ctx, const wtb_bse_params* p, const double* q4, double* hbse);
 
+/* bsebnds with bsewf (src/module_bse.F90:1427-1438, ZHEEV 'V'): for one Q-path row q4 all dim eigenvalues W of the
+ * finite-Q matrix and the eigenvectors il .. il+nvec-1 (1-based, the reference's excwf0..excwff) into Z(dim, nvec)
+ * (complex(8), column-major), for excwfi2. */
+int wtb_bse_q_eigenpairs(wtb_ctx* ctx, const wtb_bse_params* p, const double* q4, int il, int nvec, double* W,
+                         double* Z);
+
 /* Replaces the Q loop of bsebnds (src/module_bse.F90:1206-1566, ZHEEV 'N' at :1439-1447): for each of the nq
  * rows of qpath (as wtb_kpathbse writes it), all dim eigenvalues of the finite-Q matrix, ascending, into
  * exk(dim, nq) (the columns of bands_bse.dat).  FP64 throughout. */
@@ -266,9 +272,10 @@ int wtb_write_sp_optics(const char* path, int dimsp, const float* rec, int pol);
 /* tm_coef.dat / tm_coef-pol.dat (3F10.4,3I10.0,7F10.4 / ...,6F10.4) from the same records (:2300-2311, :2370-2377). */
 int wtb_write_tm_coef(const char* path, int nk, int nc, int nv, const float* rec, int pol);
 /* exc_wf_<n>.dat of excwf2 (src/module_bse.F90:374-408): nocpk(nk), kpt(nk, 3) column-major, the exciton's
- * energy and its dim = nk nc nv coefficients ewf (complex(8)). */
-int wtb_write_exc_wf(const char* path, int nk, int nc, int nv, const int* nocpk, const double* kpt, int excnum,
-                     double energy, const double* ewf);
+ * energy and its dim = nk nc nv coefficients ewf (complex(8)).  With q4 (a Q-path row) the exc_wf_<n>_<q>.dat of
+ * excwfi2 (:412-448), which adds the momentum line. */
+int wtb_write_exc_wf(const char* path, int nk, int nc, int nv, const int* nocpk, const double* kpt, const double* q4,
+                     int excnum, double energy, const double* ewf);
 /* Replaces exclft over the rows of lifetime (src/module_bse.F90:326-370, :3271-3349): fosc(dim, 7) the columns of
  * bse_opt_diel.dat, sysdim "3D" / "2D" / "1D" with the lattice of wtb_set_hr; lft(dim, 4) radiative lifetimes (s)
  * for xx+yy+zz, xx, yy, zz.  pol = 1 replaces lifetimepol (:3353-3432): fosc(dim, 6) the columns of

@@ -227,3 +227,16 @@ def test_spoptics_temp(ctx, small_bands):
     a = {key(r): r for r in rec}
     for r in ref:
         np.testing.assert_allclose(a[key(r)][7:15], r[7:15], rtol=0, atol=1e-6 * amax)
+
+
+def test_bse_q_eigenpairs(ctx, small_bands):
+    """bsebnds with bsewf: eigenvalues as wtb_bsebnds, the selected eigenvectors satisfy H_Q z = w z for the
+    finite-Q matrix of the same bands, orthonormal."""
+    sysm, p, kpt, eigv, vec = small_bands
+    ctx.set_hr(sysm)
+    q = np.array([0.3, 0.05, 0.02, 0.0])
+    W, Z = ctx.bse_q_eigenpairs(p, q, il=2, nvec=5)
+    np.testing.assert_allclose(W, ctx.bsebnds(p, q.reshape(1, 4))[:, 0], atol=1e-12)
+    H = ctx.bse_build_q(p, q)
+    assert np.abs(H @ Z - Z * W[1:6]).max() <= 1e-11
+    assert np.abs(Z.conj().T @ Z - np.eye(5)).max() <= 1e-11

@@ -140,3 +140,16 @@ def test_lifetime_pol_file(built, tmp_path):
     assert lines[0] == " #energy(eV) sum-lft(s)  x-lft(s) y-lft(s) z-lft(s) sp-lft(s) sm-lft(s)"
     for i in range(2):
         assert lines[1 + i] == O.fortran_F(e[i], 15, 4) + "".join(O.fortran_E(lft[i, c], 15, 4) for c in range(6))
+
+
+def test_exc_wf_finite_q_header(built, tmp_path):
+    from wtb_gb300 import api
+
+    path = os.path.join(tmp_path, "exc_wf_2_5.dat")
+    api.write_exc_wf(path, np.full(2, 4, dtype=np.int32), np.zeros((2, 3)), 1, 1, 2, 1.75, np.ones(2, complex),
+                     q4=[0.25, 0.1, -0.2, 0.0])
+    lines = open(path).read().splitlines()
+    assert lines[0].startswith(" # excitonic momentum")
+    assert [float(t) for t in lines[0].split()[3:]] == [np.float32(0.1), np.float32(-0.2), 0.0]
+    assert lines[1] == " # excitonic state" + O.fortran_I(2, 12)
+    assert len(lines) == 8 + 2

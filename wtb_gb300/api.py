@@ -109,7 +109,8 @@ def _load():
         "wtb_write_bse_opt_diel": [C.c_char_p, C.c_int, dp, dp, C.c_int],
         "wtb_write_sp_optics": [C.c_char_p, C.c_int, C.POINTER(C.c_float), C.c_int],
         "wtb_write_tm_coef": [C.c_char_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_int],
-        "wtb_write_exc_wf": [C.c_char_p, C.c_int, C.c_int, C.c_int, ip, dp, C.c_int, C.c_double, dp],
+        "wtb_write_exc_wf": [C.c_char_p, C.c_int, C.c_int, C.c_int, ip, dp, dp, C.c_int, C.c_double, dp],
+        "wtb_bse_q_eigenpairs": [P, C.POINTER(CParams), dp, C.c_int, C.c_int, dp, dp],
         "wtb_exciton_lifetime": [P, C.c_char_p, ip, C.c_int, dp, C.c_int, dp],
         "wtb_write_exciton_lifetime": [C.c_char_p, C.c_int, dp, dp, C.c_int],
         "wtb_fortran_format": [C.c_char, C.c_double, C.c_int, C.c_int, C.c_char_p, C.c_int],
@@ -256,12 +257,15 @@ def write_tm_coef(path, nk, nc, nv, rec, pol=False):
                               int(bool(pol))), "wtb_write_tm_coef")
 
 
-def write_exc_wf(path, nocpk, kpt, nc, nv, excnum, energy, ewf):
+def write_exc_wf(path, nocpk, kpt, nc, nv, excnum, energy, ewf, q4=None):
+    """exc_wf_<n>.dat (excwf2), or with q4 (a Q-path row) exc_wf_<n>_<q>.dat (excwfi2)."""
     nocp = np.ascontiguousarray(nocpk, dtype=np.int32)
     k = np.asfortranarray(kpt, dtype=np.float64)
     e = np.ascontiguousarray(ewf, dtype=np.complex128)
+    q = None if q4 is None else np.ascontiguousarray(q4, dtype=np.float64)
     _w(_lib.wtb_write_exc_wf(os.fsencode(path), len(nocp), nc, nv, nocp.ctypes.data_as(C.POINTER(C.c_int)), _dp(k),
-                             int(excnum), float(energy), e.ctypes.data_as(C.POINTER(C.c_double))), "wtb_write_exc_wf")
+                             _dp(q), int(excnum), float(energy), e.ctypes.data_as(C.POINTER(C.c_double))),
+       "wtb_write_exc_wf")
 
 
 def write_exciton_lifetime(path, energy, lft, pol=False):
@@ -368,6 +372,15 @@ class Context:
         cp = cparams(p)
         self._chk(_lib.wtb_bse_build_q(self._h, C.byref(cp), _dp(_f64(q4)), _dp(H)), "wtb_bse_build_q")
         return H
+
+    def bse_q_eigenpairs(self, p: BSEParams, q4, il=1, nvec=1):
+        """All eigenvalues W of the finite-Q matrix and the eigenvectors il..il+nvec-1 (1-based) as Z (dim, nvec)."""
+        W = np.zeros(p.dim)
+        Z = np.zeros((p.dim, nvec), dtype=np.complex128, order="F")
+        cp = cparams(p)
+        self._chk(_lib.wtb_bse_q_eigenpairs(self._h, C.byref(cp), _dp(_f64(q4)), int(il), int(nvec), _dp(W),
+                                            Z.ctypes.data_as(C.POINTER(C.c_double))), "wtb_bse_q_eigenpairs")
+        return W, Z
 
     def bsebnds(self, p: BSEParams, qpath):
         """bsebnds: all finite-Q exciton energies, exk (dim, nq), for the rows of qpath."""

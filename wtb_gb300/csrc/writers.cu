@@ -14,7 +14,7 @@
 //   bse_opt_diel.dat / -pol   src/module_bse.F90:2132-2133, :2556-2567 (7F15.4 / 6F15.4)
 //   sp_optics.dat / -pol      :2296-2297, :2366-2367 (7F15.4 / 6F15.4)
 //   tm_coef.dat / -pol        :2300-2311, :2370-2377 (3F10.4,3I10.0,7F10.4 / ...,6F10.4)
-//   exc_wf_<n>.dat            excwf2, :374-408 ((I,3F15.4,2I,2E15.4))
+//   exc_wf_<n>.dat            excwf2, :374-408 ((I,3F15.4,2I,2E15.4)); exc_wf_<n>_<q>.dat excwfi2, :412-448
 //   exciton_lifetime.dat      lifetime, :3271-3349 ((1F15.4,4E15.4)); -pol: lifetimepol, :3353-3432 ((1F15.4,6E15.4))
 #include <cmath>
 #include <cstdio>
@@ -161,6 +161,13 @@ std::string ld_real8(double v) {
   return buf;
 }
 
+// a list-directed REAL(4) item: 7 significant digits in a 15-character field
+std::string ld_real4(double v) {
+  char buf[64];
+  std::snprintf(buf, sizeof(buf), "%15.7G", (double)(float)v);
+  return buf;
+}
+
 struct File {
   FILE* f = nullptr;
   explicit File(const char* path) : f(path ? std::fopen(path, "w") : nullptr) {}
@@ -262,12 +269,14 @@ int wtb_write_tm_coef(const char* path, int nk, int nc, int nv, const float* rec
   return std::ferror(f.f) ? WTB_EBADARG : WTB_OK;
 }
 
-int wtb_write_exc_wf(const char* path, int nk, int nc, int nv, const int* nocpk, const double* kpt, int excnum,
-                     double energy, const double* ewf) {
+int wtb_write_exc_wf(const char* path, int nk, int nc, int nv, const int* nocpk, const double* kpt, const double* q4,
+                     int excnum, double energy, const double* ewf) {
   if (!path || nk < 1 || nc < 1 || nv < 1 || !nocpk || !kpt || !ewf) return WTB_EBADARG;
   File f(path);
   if (!f.f) return WTB_EBADARG;
   const size_t nkk = (size_t)nk;
+  if (q4)  // excwfi2's momentum line: three REAL(4) list-directed items
+    f.line(ld_chars({"#", " ", "excitonic momentum"}) + ld_real4(q4[1]) + ld_real4(q4[2]) + ld_real4(q4[3]));
   f.line(ld_chars({"#", " ", "excitonic state"}) + ld_int(excnum));
   f.line(ld_chars({"#", " ", "exciton energy:"}) + ld_real8(energy));
   f.line(ld_chars({"#", " ", "number occupied states"}) + ld_int(nocpk[0]) + "(not valid for metallic systems)");

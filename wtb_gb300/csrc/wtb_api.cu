@@ -916,6 +916,43 @@ int wtb_bse_build_q(wtb_ctx* c, const wtb_bse_params* p, const double* q4, doubl
   return check_status(c);
 }
 
+int wtb_bse_q_eigenpairs(wtb_ctx* c, const wtb_bse_params* p, const double* q4, int il, int nvec, double* W,
+                         double* Z) {
+  if (!c) return WTB_EBADARG;
+  CKR(prep_device(c));
+  if (!p || !q4 || !W || (nvec > 0 && !Z)) return set_err(c, WTB_EBADARG, "bad arguments");
+  CKR(check_q_params(c, p));
+  const long dim = (long)p->ngrid[0] * p->ngrid[1] * p->ngrid[2] * p->nc * p->nv;
+  if (nvec < 0 || il < 1 || il - 1 + nvec > dim) return set_err(c, WTB_EBADARG, "eigenvector range outside 1..dim");
+  CKR(stage_mesh(c, p));
+  CKR(enqueue_bands(c, false));
+  const int nk = c->nk;
+  cudaError_t err = cudaSuccess;
+  const int Kpad = (nk + 63) / 64 * 64;
+  double* V = c->ws.get<double>("V", (size_t)((nk + 127) / 128 * 128) * Kpad, &err, true);
+  void* scratch = c->ws.get<zd>("deig_scratch", (dense_eig_scratch((int)dim) + sizeof(zd) - 1) / sizeof(zd), &err);
+  void* vscratch = c->ws.get<double>("deig_vscratch", dense_eigvec_scratch((int)dim) / sizeof(double), &err);
+  double* dW = c->ws.get<double>("deig_W", dim, &err);
+  zd* dZ = c->ws.get<zd>("T_Z", (size_t)dim * dim, &err);
+  CKC(err);
+  CKR(coulomb_table_into(c, p, V, Kpad));
+  zd* H = nullptr;
+  CKR(build_q_matrix(c, p, q4, V, Kpad, c->scs, &H));
+  CKC(dense_eig_prepare());
+  // H row-major is conj(H) column-major: the vectors are conjugated back
+  CKC(launch_dense_eig(H, (int)dim, (int)dim, false, dW, dZ, true, scratch, vscratch, c->s));
+  CKC(cudaMemcpyAsync(W, dW, sizeof(double) * dim, cudaMemcpyDeviceToHost, c->s));
+  if (nvec > 0) {
+    // columns il..il+nvec-1 of the row-major Z into the column-major Z(dim, nvec) over the dead matrix H
+    transpose_z_kernel<<<(unsigned)((dim * nvec + 255) / 256), 256, 0, c->s>>>(dZ + (il - 1), (int)dim, nvec, (int)dim,
+                                                                              H, 0);
+    ++g_launch_count;
+    CKC(cudaGetLastError());
+    CKC(cudaMemcpyAsync(Z, H, sizeof(zd) * dim * nvec, cudaMemcpyDeviceToHost, c->s));
+  }
+  return check_status(c);
+}
+
 static double temp_gap_correction(const wtb_temp_params* tp);
 
 // The Q loop of bsebnds, or of bsebndstemp with tp (scissor scs + tcor on both meshes, matrizelbsekqtemp's
