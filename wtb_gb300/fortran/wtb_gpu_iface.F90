@@ -12,6 +12,8 @@
 !   wtb_gpu_spdielrawpol  <- spdielrawpol  (src/module_bse.F90:4318-4524)
 !   wtb_gpu_bsebnds       <- the Q loop of bsebnds (src/module_bse.F90:1206-1566)
 !   wtb_gpu_bsesolvertemp <- bsesolvertemp (src/module_bse.F90:2649-3263) before its writes
+!   wtb_gpu_bsebndstemp   <- the Q loop of bsebndstemp (src/module_bse.F90:1572-1990)
+!   wtb_gpu_zheev         <- ZHEEV('N'/'V', 'U', n, A, lda, W, ...) of the full-spectrum paths
 ! A non-zero status from the library is turned into the reference's behaviour: print the message
 ! (the reference's STOP text where it has one) and STOP.
 ! No Fortran compiler exists in the build image, so this file is not compiled by the project's build.
@@ -22,7 +24,7 @@ module wtb_gpu
   public :: wtb_bse_params_t, wtb_timings_t, wtb_gpu_init, wtb_gpu_eigsys, wtb_gpu_slepc_solver, &
             wtb_gpu_bsesolver, wtb_gpu_bsedielraw, wtb_gpu_set_hr, wtb_gpu_bsedielrawpol, &
             wtb_gpu_spoptics, wtb_gpu_spdielraw, wtb_gpu_spdielrawpol, wtb_gpu_bsebnds, &
-            wtb_temp_params_t, wtb_gpu_bsesolvertemp
+            wtb_temp_params_t, wtb_gpu_bsesolvertemp, wtb_gpu_bsebndstemp, wtb_gpu_zheev
 
   type, bind(C) :: wtb_bse_params_t
     integer(c_int)  :: ngrid(3)
@@ -134,6 +136,28 @@ module wtb_gpu
       type(wtb_temp_params_t) :: tp
       real(c_double) :: ws(*), acts(*)
       type(c_ptr), value :: he, fdeh
+    end function
+    integer(c_int) function c_wtb_bsebndstemp(ctx, p, tp, nq, qpath, exk) bind(C, name="wtb_bsebndstemp")
+      import :: c_ptr, c_int, c_double, wtb_bse_params_t, wtb_temp_params_t
+      type(c_ptr), value :: ctx
+      type(wtb_bse_params_t) :: p
+      type(wtb_temp_params_t) :: tp
+      integer(c_int), value :: nq
+      real(c_double) :: qpath(*), exk(*)
+    end function
+    integer(c_int) function c_wtb_zheev(ctx, n, a, lda, w) bind(C, name="wtb_zheev")
+      import :: c_ptr, c_int, c_double, c_double_complex
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: n, lda
+      complex(c_double_complex) :: a(*)
+      real(c_double) :: w(*)
+    end function
+    integer(c_int) function c_wtb_zheev_vectors(ctx, n, a, lda, w, z) bind(C, name="wtb_zheev_vectors")
+      import :: c_ptr, c_int, c_double, c_double_complex
+      type(c_ptr), value :: ctx
+      integer(c_int), value :: n, lda
+      complex(c_double_complex) :: a(*), z(*)
+      real(c_double) :: w(*)
     end function
     integer(c_int) function c_wtb_spoptics(ctx, p, rec) bind(C, name="wtb_spoptics")
       import :: c_ptr, c_int, c_float, wtb_bse_params_t
@@ -283,6 +307,33 @@ contains
     double precision :: W(dimbse), acts(dimbse,8)
     call wtb_gpu_init(0)
     call check(c_wtb_bsesolvertemp(ctx, p, tp, W, acts, c_null_ptr, c_null_ptr), 'bsesolvertemp')
+  end subroutine
+
+  subroutine wtb_gpu_bsebndstemp(p, tp, nq, qauxv, exk)
+    type(wtb_bse_params_t) :: p
+    type(wtb_temp_params_t) :: tp
+    integer :: nq
+    double precision :: qauxv(nq,4), exk(*)
+    call wtb_gpu_init(0)
+    call check(c_wtb_bsebndstemp(ctx, p, tp, nq, qauxv, exk), 'bsebndstemp')
+  end subroutine
+
+  ! jobz 'N': W only (A is left unchanged); jobz 'V': the eigenvectors overwrite A, as ZHEEV's do
+  subroutine wtb_gpu_zheev(jobz, n, A, lda, W)
+    character :: jobz
+    integer :: n, lda
+    complex(8) :: A(lda,n)
+    double precision :: W(n)
+    complex(8), allocatable :: Z(:,:)
+    call wtb_gpu_init(0)
+    if (jobz == 'V' .or. jobz == 'v') then
+      allocate(Z(n,n))
+      call check(c_wtb_zheev_vectors(ctx, n, A, lda, W, Z), 'zheev')
+      A(1:n,1:n) = Z
+      deallocate(Z)
+    else
+      call check(c_wtb_zheev(ctx, n, A, lda, W), 'zheev')
+    end if
   end subroutine
 
   subroutine wtb_gpu_spdielraw(p, dimsp, esp, acts, dielf)
