@@ -240,3 +240,31 @@ def test_bse_q_eigenpairs(ctx, small_bands):
     H = ctx.bse_build_q(p, q)
     assert np.abs(H @ Z - Z * W[1:6]).max() <= 1e-11
     assert np.abs(Z.conj().T @ Z - np.eye(5)).max() <= 1e-11
+
+
+def test_next_rows_argument_errors(ctx, small_bands):
+    """bad arguments of the full-spectrum entry points come back as WTB_EBADARG with a message, not a fault"""
+    from wtb_gb300 import api
+
+    sysm, p, kpt, eigv, vec = small_bands
+    ctx.set_hr(sysm)
+    with pytest.raises(api.WTBError) as e:
+        ctx.bsesolvertemp(p, 300.0, ta=5)
+    assert e.value.code == api.WTB_EBADARG and "temperature" in str(e.value)
+    with pytest.raises(api.WTBError) as e:
+        ctx.bsesolvertemp(p, -1.0)
+    assert e.value.code == api.WTB_EBADARG
+    with pytest.raises(api.WTBError) as e:
+        ctx.bsebnds(p, np.zeros((0, 4)))
+    assert e.value.code == api.WTB_EBADARG
+    big = S.BSEParams(**{**p.__dict__})
+    big.ngrid = (80, 80, 1)                            # dim 25,600 > 20,000: refused before any allocation
+    with pytest.raises(api.WTBError) as e:
+        ctx.bsebnds(big, np.zeros((1, 4)))
+    assert e.value.code == api.WTB_EBADARG and "dim <= 20000" in str(e.value)
+    with pytest.raises(api.WTBError):
+        ctx.bse_q_eigenpairs(p, np.zeros(4), il=p.dim, nvec=2)
+    with pytest.raises(api.WTBError):
+        api.kpathbse(sysm.rlat[0], sysm.rlat[1], sysm.rlat[2], np.zeros((2, 3)), 1)
+    # the context stays usable
+    np.testing.assert_allclose(ctx.zheev(np.diag([3.0, 1.0, 2.0]).astype(complex)), [1.0, 2.0, 3.0], atol=1e-14)
