@@ -59,7 +59,32 @@ def make_fit_target(name="hex8_36x36", r0_true=44.0, noise=1e-3, seed=2024):
     print(name, "fit target at r0 =", r0_true, r["E"])
 
 
+def make_next_rows(name="hex8_6x6"):
+    """The (f) rows on the small case: the finite-Q spectrum on a Gamma-M path (bsebnds), the same at 3000 K
+    with the Bose-Einstein gap correction (bsebndstemp), the temperature solver's energies and summed
+    activities at 300 K and 4000 K (bsesolvertemp), the sorted IPA records (spoptics) and the BZ-resolved
+    activity (spoptpolbz)."""
+    sysm, p = S.workload(name)
+    ks = np.array([[0.0, 0.0, 0.0], [0.5, 0.0, 0.0]])
+    qpath = O.kpathbse(sysm.rlat, ks, 3)
+    out = {"digest": np.array(input_digest(sysm)), "qpath": qpath, "exk": O.bsebnds(sysm, p, qpath),
+           "exk_temp": O.bsebndstemp(sysm, p, qpath, 3000.0, "BE", 0.05, 300.0)}
+    for T, ta, st, ph in ((300.0, "FA", 0.0, 0.0), (4000.0, "VE", 2.0e-4, 0.02)):
+        r = O.bsesolvertemp(sysm, p, T, ta, st, ph)
+        out[f"W_{int(T)}"] = r["Ws"]
+        out[f"fdeh_{int(T)}"] = r["fdeh"]
+        for c in ("xx", "yy", "zz", "sp", "sm"):
+            out[f"actsum_{c}_{int(T)}"] = np.array(r["acts"][c].sum())
+    kpt = O.monhkhorst_pack(*p.ngrid, p.mshift, sysm.rlat)
+    eigv, vec, nocp = O.bands(sysm, p, kpt)
+    out["sp_records"] = O.spoptics_records(eigv, kpt, nocp, O.optsp_all(eigv, vec, kpt, sysm, p), p.nv, p.nc)
+    out["bz_act"] = O.spoptpolbz(sysm, p)
+    np.savez_compressed(os.path.join(HERE, name + "_next_rows.npz"), **out)
+    print(name, "next rows: lowest finite-Q", out["exk"][:2, :].T)
+
+
 if __name__ == "__main__":
     for n in ("hex8_6x6", "hex8_24x24"):
         make(n)
     make_fit_target()
+    make_next_rows()

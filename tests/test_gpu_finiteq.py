@@ -268,3 +268,25 @@ def test_next_rows_argument_errors(ctx, small_bands):
         api.kpathbse(sysm.rlat[0], sysm.rlat[1], sysm.rlat[2], np.zeros((2, 3)), 1)
     # the context stays usable
     np.testing.assert_allclose(ctx.zheev(np.diag([3.0, 1.0, 2.0]).astype(complex)), [1.0, 2.0, 3.0], atol=1e-14)
+
+
+def test_next_rows_against_golden_fixture(ctx):
+    """The GPU's finite-Q, temperature, IPA-record and BZ-activity outputs against the committed fixture made
+    by the oracle (tests/golden/hex8_6x6_next_rows.npz)."""
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "hex8_6x6_next_rows.npz"))
+    sysm, p = S.workload("hex8_6x6")
+    ctx.set_hr(sysm)
+    np.testing.assert_allclose(ctx.bsebnds(p, g["qpath"]), g["exk"], atol=1e-9)
+    np.testing.assert_allclose(ctx.bsebndstemp(p, g["qpath"], 3000.0, "BE", 0.05, 300.0), g["exk_temp"], atol=1e-9)
+    for T, ta, st, ph in ((300.0, "FA", 0.0, 0.0), (4000.0, "VE", 2.0e-4, 0.02)):
+        out = ctx.bsesolvertemp(p, T, ta, st, ph)
+        np.testing.assert_allclose(out["Ws"], g[f"W_{int(T)}"], atol=1e-9)
+        np.testing.assert_allclose(out["fdeh"], g[f"fdeh_{int(T)}"], atol=1e-12)
+        for c in ("xx", "yy", "zz", "sp", "sm"):
+            ref = float(g[f"actsum_{c}_{int(T)}"])
+            assert abs(out["acts"][c].sum() - ref) <= 1e-8 * max(1.0, abs(ref)), (T, c)
+    rec = ctx.spoptics(p)
+    np.testing.assert_allclose(rec[:, 6], g["sp_records"][:, 6], rtol=2e-7, atol=1e-6)
+    np.testing.assert_allclose(ctx.spoptpolbz(p), g["bz_act"], rtol=1e-9, atol=1e-12 * np.abs(g["bz_act"]).max())

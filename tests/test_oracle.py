@@ -315,6 +315,26 @@ def test_golden_fixtures(name):
         np.testing.assert_allclose(spec[c], g["spec_" + c], rtol=1e-8, atol=1e-10)
 
 
+def test_next_rows_golden_fixture():
+    """The oracle's finite-Q, temperature, IPA-record and BZ-activity outputs on the small case against the
+    committed fixture (tests/golden/hex8_6x6_next_rows.npz)."""
+    from tests.golden.make_golden import input_digest
+
+    g = np.load(os.path.join(HERE, "golden", "hex8_6x6_next_rows.npz"))
+    sysm, p = S.workload("hex8_6x6")
+    assert str(g["digest"]) == input_digest(sysm), "the seeded input generator changed"
+    qpath = O.kpathbse(sysm.rlat, np.array([[0.0, 0.0, 0.0], [0.5, 0.0, 0.0]]), 3)
+    np.testing.assert_array_equal(qpath, g["qpath"])
+    np.testing.assert_allclose(O.bsebnds(sysm, p, qpath), g["exk"], atol=1e-11)
+    np.testing.assert_allclose(O.bsebndstemp(sysm, p, qpath, 3000.0, "BE", 0.05, 300.0), g["exk_temp"], atol=1e-11)
+    r = O.bsesolvertemp(sysm, p, 4000.0, "VE", 2.0e-4, 0.02)
+    np.testing.assert_allclose(r["Ws"], g["W_4000"], atol=1e-11)
+    np.testing.assert_allclose(r["fdeh"], g["fdeh_4000"], atol=1e-14)
+    for c in ("xx", "yy", "zz", "sp", "sm"):
+        np.testing.assert_allclose(r["acts"][c].sum(), g[f"actsum_{c}_4000"], rtol=1e-10)
+    np.testing.assert_allclose(O.spoptpolbz(sysm, p), g["bz_act"], rtol=1e-10, atol=1e-13)
+
+
 def test_c_restatement_matches_numpy(built, small):
     """The element-by-element C loop (the timed CPU baseline) equals the vectorised oracle."""
     import __graft_entry__ as g
