@@ -125,7 +125,7 @@ __device__ __forceinline__ double omega_of(double e0, double ef, int nesp, int j
 
 // Partial Lorentzian sums of optdiel over one chunk of the rows, all NC components at once: the two
 // quotients (E - omega) / eaux and gamma / eaux do not depend on the component, so each (row, omega) pair
-// costs two FP64 divisions instead of two per component, and the products f_c * quotient are the
+// costs one FP64 division (1/eaux) instead of two per component, and the products f_c * quotient are the
 // reference's own.  A thread owns one photon energy; the chunk's rows pass through shared memory.
 // part[chunk][c][0: real, 1: imaginary][nesp].
 template <int NC>
@@ -161,8 +161,11 @@ __global__ void __launch_bounds__(kLorOmega) lorentz_partial_kernel(const double
       for (int r = 0; r < nt; ++r) {
         const double ex = sW[r];
         const double eaux = ((elux - ex) * (elux - ex)) + (smef * smef);
-        const double q1 = (ex - elux) / eaux;
-        const double q2 = smef / eaux;
+        // one FP64 division per pair (the FP64 pipe bounds this kernel): the quotients as products with 1/eaux,
+        // within an ulp of the reference's two divisions
+        const double ie = 1.0 / eaux;
+        const double q1 = (ex - elux) * ie;
+        const double q2 = smef * ie;
 #pragma unroll
         for (int c = 0; c < NC; ++c) {
           rp[c] += sf[c][r] * q1;
