@@ -24,6 +24,8 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <cstdlib>
+
 #include "wtb_internal.h"
 
 namespace wtb {
@@ -667,6 +669,14 @@ int tc_autotune(uint64_t key, const std::string& what, const std::function<cudaE
   }
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return 256;
+  // WTB_TC_TILE=256|128 pins the choice without timing: a kernel profiler serialises and replays the timed runs,
+  // which makes the timing (and so the tile a profiled run would use) differ from a normal run's
+  if (const char* pin = std::getenv("WTB_TC_TILE")) {
+    const int bn = std::atoi(pin) == 128 ? 128 : 256;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = TuneEntry{bn, {0.0, 0.0}, what + " (pinned)"};
+    return bn;
+  }
   const int cand[2] = {256, 128};
   double ms[2] = {1e30, 1e30};
   cudaEvent_t a = nullptr, b = nullptr;

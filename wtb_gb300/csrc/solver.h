@@ -186,8 +186,12 @@ struct MatFreeOperator : Operator<S> {
   // with CUDA events around each, into prof (the eigensolve itself runs as one graph launch)
   int npairs0 = 0;
   cudaError_t time_contraction(int reps, int ncol, cudaStream_t s);
-  // tensor-core kind: K blocks per accumulation range in the final applications (0: one range)
-  int kchunk_final = 4;
+  // tensor-core kind: K blocks per accumulation range in the final applications (0: one range).  The FP32
+  // accumulation error of the final application grows about linearly with the range: on the 57,600-dim
+  // workload the exciton energies moved by 3.7e-7 / 7.2e-7 / 1.5e-6 / 5.3e-6 eV from the FP64 form with 4 / 8
+  // / 16 / 64 blocks per range, and the solve took 15.58 / 15.21 / 15.00 / 14.77 ms; 8 keeps a 14x margin to
+  // the 1e-5 eV bound
+  int kchunk_final = 8;
   bool final_apply = false;
   void set_final(bool on) override { final_apply = on; }
   // column tile of the contraction (tensor-core kind), chosen by autotune() for the operator's shape
@@ -250,7 +254,7 @@ struct BatchMatFreeOperator : Operator<float> {
   int nsys = 0, nbmax = 16, max_nv = 0, max_nc = 0, max_w = 0;
   int nslices = 3, npairs = 3, npairs_refine = 6;
   int pa[8] = {0}, pb[8] = {0};
-  int kchunk_final = 4;
+  int kchunk_final = 8;  // K blocks per accumulation range of the final application (as the single operator)
   bool final_apply = false;
   const MfSys* d_sys = nullptr;
   const int2* d_gtiles = nullptr;  // gather tiles (system, first k-point)
