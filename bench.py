@@ -397,7 +397,11 @@ def main():
                 "traffic": None, "launches_timed": int(nl.value), "avg_launch_ms": g_ms,
                 "flops_per_launch": g_flops, "algorithmic_bytes_per_launch": by.value / max(nl.value, 1),
                 # the iteration-phase contractions (one per iteration plus the set-up application) over the step
-                "share_of_step": (g_ms * (last["timings"]["iterations"] + 1) / (tot_ms / args.steps))
+                # the full-K contraction launches of one solve (the initial block, one per iteration, the
+                # refinement's first application: iterations + 2) at the live per-launch time; the final
+                # application's K-split launches (about 6 % of a step in the ncu launch list) are not in it
+                "full_k_launches_per_step": last["timings"]["iterations"] + 2,
+                "share_of_step": (g_ms * (last["timings"]["iterations"] + 2) / (tot_ms / args.steps))
                 if tot_ms > 0 and g_ms > 0 else None}
     if args.precision not in ("bf16x3", "bf16x6"):
         roofline["bound"] = "simt"
