@@ -541,7 +541,10 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
   // keeps the padding rows zero; its reductions run over its part table
   const bool ragged = L.bm.rows != nullptr;
   // reduction parts: about 96 rows each, at most four per SM (the Gram kernel needs the CTAs to hide latency)
-  const int npart = ragged ? L.nparts : std::max(1, std::min(608, (nrow + 95) / 96));
+  // reduction parts of the tall-skinny Grams and residual norms: two CTAs per SM at most (each part's FP64
+  // partial of a 48 x 48 Gram is 36 KB, and the sum over parts reads all of them: 608 parts made that sum
+  // about 7 % of a solve)
+  const int npart = ragged ? L.nparts : std::max(1, std::min(304, (nrow + 191) / 192));
   cudaError_t err = cudaSuccess;
   cplx<S>* Sb = ws.get<cplx<S>>("lob_S", (size_t)nrow * ld, &err, true);
   cplx<S>* ASb = ws.get<cplx<S>>("lob_AS", (size_t)nrow * ld, &err, true);
