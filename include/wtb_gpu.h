@@ -285,7 +285,24 @@ int wtb_exciton_lifetime(wtb_ctx* ctx, const char* sysdim, const int* ngrid, int
 /* exciton_lifetime.dat (1F15.4,4E15.4) from the energies and lft(dim, 4), or exciton_lifetime-pol.dat
  * (1F15.4,6E15.4) from lft(dim, 6) with pol = 1. */
 int wtb_write_exciton_lifetime(const char* path, int dim, const double* energy, const double* lft, int pol);
-/* One Fortran edit descriptor applied to x (kind 'F', 'E' or 'I' with w, d (m for I)) into out (>= w+1 bytes). */
+/* List-directed files, written as gfortran's runtime writes list-directed records (a blank before the first
+ * item, one blank between items except between two character items; REAL(8) as 1PG25.17E3, REAL(4) as
+ * 1PG16.9E2, 4-byte integers as I11).
+ * One component of bse_diel_*.dat (bsedielraw, src/module_bse.F90:926-931, :1004-1009; bsedielrawpol
+ * :1130-1134, :1174-1178) or sp_diel_*.dat / sp_diel-pol_*.dat (spdielraw, spdielrawpol): the header record and
+ * per photon energy the REAL(8) energy and the REAL(4) eps1, eps2 from dielf(numbse, 3) (column-major: omega,
+ * eps1, eps2 — one component block of what wtb_bsedielraw / wtb_spdielraw return). */
+int wtb_write_diel(const char* path, int numbse, const double* dielf);
+/* bands_bse.dat of bsebnds (src/module_bse.F90:1536-1543) and bsebndstemp (:1981-1990): for each of the dim
+ * bands, per Q-path point the REAL(4) path coordinate qpath(i, 1) and the REAL(8) energy exk(b, i) (column-major
+ * exk(dim, nq), as wtb_bsebnds returns it), then an empty record. */
+int wtb_write_bands_bse(const char* path, int nq, int dim, const double* qpath, const double* exk);
+/* One of bz_act_x/y/z/sp/sm.dat or dichroism.dat of spoptpolbz (src/module_bse.F90:4754-4759): per k-point the
+ * REAL(4) coordinates kpt(k, 1:3) (column-major kpt(nk, 3)) and the REAL(8) value(k) (one column of what
+ * wtb_spoptpolbz returns). */
+int wtb_write_bz_act(const char* path, int nk, const double* kpt, const double* value);
+/* One Fortran edit descriptor applied to x (kind 'F', 'E' or 'I' with w, d (m for I)) into out (>= w+1 bytes).
+ * Kind 'G' with (w, d) = (25, 17) or (16, 9): one REAL(8) or REAL(4) item of a list-directed record as above. */
 int wtb_fortran_format(char kind, double x, int w, int d, char* out, int outlen);
 
 /* Replaces bseoptprop (src/module_bse.F90:3766-3931, formulas :5075-5124): props(numbse, 6, 5) =

@@ -861,6 +861,55 @@ def fortran_I(v, w, m=1):
     return "*" * w if len(s) > w else s.rjust(w)
 
 
+def list_directed_real(x, kind):
+    """One real item of a list-directed WRITE as gfortran's runtime edits it (the reference's top-level README
+    names the GNU compiler): G editing with scale factor 1P, 1PG25.17E3 for REAL(8) and 1PG16.9E2 for REAL(4)
+    (of the single-precision value, as real(x) rounds it).  The G rule of the Fortran standard: with the value
+    rounded to d significant digits (nearest, ties to even) and 10**(k-1) <= |r| < 10**k, F(w-n).(d-k) and
+    n = e+2 blanks when 0 <= k <= d, else 1PEw.dEe (one digit before the point, d-1 after); zero as
+    F(w-n).(d-1) and n blanks.  Exact decimal arithmetic."""
+    from decimal import ROUND_HALF_EVEN, Decimal, localcontext
+    w, d, e = (25, 17, 3) if kind == 8 else (16, 9, 2)
+    x = float(np.float32(x)) if kind == 4 else float(x)
+    if not np.isfinite(x):
+        return _fortran_special(x, w)
+    n = e + 2
+    sign = "-" if np.signbit(x) else ""
+    if x == 0.0:
+        return (sign + "0." + "0" * (d - 1)).rjust(w - n) + " " * n
+    with localcontext() as ctx:
+        ctx.prec = 1200
+        dx = abs(Decimal(x))
+        ex = dx.adjusted()
+        m = dx.scaleb(-ex).quantize(Decimal(1).scaleb(-(d - 1)), rounding=ROUND_HALF_EVEN)
+        if m >= 10:
+            m = (m / 10).quantize(Decimal(1).scaleb(-(d - 1)), rounding=ROUND_HALF_EVEN)
+            ex += 1
+        k = ex + 1
+        if 0 <= k <= d:
+            q = dx.quantize(Decimal(1).scaleb(-(d - k)), rounding=ROUND_HALF_EVEN)
+            mag = format(q, "f")
+            if "." not in mag:
+                mag += "."
+            return (sign + mag).rjust(w - n) + " " * n
+        s = sign + format(m, "f") + "E" + ("-" if ex < 0 else "+") + str(abs(ex)).rjust(e, "0")
+    return s.rjust(w)
+
+
+def list_directed_record(items):
+    """One list-directed output record as gfortran writes it: a blank before the first item, one blank before
+    every later item except a character item that follows a character item; character items as they are,
+    4-byte integers as I11, reals by list_directed_real.  items: ("c", str), ("i", int), ("r8", x), ("r4", x).
+    A WRITE with no items is an empty record."""
+    s, prev_char = "", None
+    for t, v in items:
+        is_char = t == "c"
+        s += " " if prev_char is None or not (is_char and prev_char) else ""
+        prev_char = is_char
+        s += v if is_char else (fortran_I(v, 11) if t == "i" else list_directed_real(v, 8 if t == "r8" else 4))
+    return s
+
+
 def exclft(sysdim, ngrid, rlat, fosc, enexc):
     """Radiative lifetime (src/module_bse.F90:326-370) with the reference's single-precision constants."""
     cfe, lspd, hbar = float(F32(7.297e-3)), float(F32(299.792e16)), float(F32(6.582e-16))

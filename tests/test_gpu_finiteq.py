@@ -75,8 +75,9 @@ def test_bse_build_q(ctx, small_bands, q):
     np.testing.assert_allclose(np.linalg.eigvalsh(H), np.linalg.eigvalsh(ref), atol=1e-11 * np.abs(ref).max())
 
 
-def test_bsebnds_small(ctx, small_bands):
-    """The whole Q loop on a path through Gamma (Q = 0: no exchange) against the oracle's ZHEEV spectrum."""
+def test_bsebnds_small(ctx, small_bands, tmp_path):
+    """The whole Q loop on a path through Gamma (Q = 0: no exchange) against the oracle's ZHEEV spectrum, and
+    its bands_bse.dat read back."""
     sysm, p, kpt, eigv, vec = small_bands
     ctx.set_hr(sysm)
     ks = np.array([[0.0, 0.0, 0.0], [0.5, 0.0, 0.0], [0.5, 0.0, 0.0], [1 / 3, 1 / 3, 0.0]])
@@ -88,6 +89,15 @@ def test_bsebnds_small(ctx, small_bands):
     # Q = 0 reproduces the plain BSE spectrum
     H0 = O.bse_build(eigv, vec, kpt, p, sysm.rlat)
     np.testing.assert_allclose(exk[:, 0], np.linalg.eigvalsh(H0), atol=1e-9)
+    from wtb_gb300 import api
+    path = str(tmp_path / "bands_bse.dat")
+    api.write_bands_bse(path, qpath, exk)
+    lines = open(path).read().splitlines()
+    assert len(lines) == p.dim * (len(qpath) + 1)
+    assert lines[len(qpath)] == "" and lines[1] == O.list_directed_record([("r4", qpath[1, 0]), ("r8", exk[0, 1])])
+    back = np.array([[float(t) for t in ln.split()] for ln in lines if ln])
+    assert np.array_equal(back[:, 1], exk.reshape(-1))          # band-major, every REAL(8) energy exactly
+    assert np.array_equal(back[: len(qpath), 0].astype(np.float32), qpath[:, 0].astype(np.float32))
 
 
 def test_bsebnds_2304(ctx):

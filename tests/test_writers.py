@@ -101,6 +101,9 @@ def test_exc_wf_and_lifetime_files(built, tmp_path):
     api.write_exc_wf(path, nocp, kpt, nc, nv, 3, 2.5, ewf)
     lines = open(path).read().splitlines()
     assert lines[0] == " # excitonic state" + O.fortran_I(3, 12)
+    assert lines[1] == O.list_directed_record([("c", "#"), ("c", " "), ("c", "exciton energy:"), ("r8", 2.5)])
+    assert lines[2] == O.list_directed_record([("c", "#"), ("c", " "), ("c", "number occupied states"), ("i", 6),
+                                               ("c", "(not valid for metallic systems)")])
     I = 0
     for k in range(nk):
         for c in range(nc):
@@ -149,7 +152,94 @@ def test_exc_wf_finite_q_header(built, tmp_path):
     api.write_exc_wf(path, np.full(2, 4, dtype=np.int32), np.zeros((2, 3)), 1, 1, 2, 1.75, np.ones(2, complex),
                      q4=[0.25, 0.1, -0.2, 0.0])
     lines = open(path).read().splitlines()
-    assert lines[0].startswith(" # excitonic momentum")
+    assert lines[0] == O.list_directed_record([("c", "#"), ("c", " "), ("c", "excitonic momentum"), ("r4", 0.1),
+                                               ("r4", -0.2), ("r4", 0.0)])
     assert [float(t) for t in lines[0].split()[3:]] == [np.float32(0.1), np.float32(-0.2), 0.0]
     assert lines[1] == " # excitonic state" + O.fortran_I(2, 12)
     assert len(lines) == 8 + 2
+
+
+def _ld_values(rng, n, kind):
+    mag = 10.0 ** rng.uniform(-40 if kind == 4 else -300, 38 if kind == 4 else 300, n)
+    v = np.where(rng.random(n) < 0.5, -mag, mag)
+    d = 17 if kind == 8 else 9
+    b = [0.1, 10.0 ** d, 1.0, 10.0, 0.5]                # the G rule's F / E boundaries and neighbours
+    if kind == 8:
+        edge = [x for c in b for x in (np.nextafter(c, 0), c, np.nextafter(c, np.inf))]
+    else:
+        edge = [float(x) for c in b for x in (np.nextafter(np.float32(c), np.float32(0)), np.float32(c),
+                                                np.nextafter(np.float32(c), np.float32(np.inf)))]
+    edge += [0.0, -0.0, 1.03125, 123.456, 1e-3, 5e-324, 1.7976931348623157e308, np.inf, -np.inf, np.nan]
+    if kind == 4:
+        edge = [x for x in edge if not np.isfinite(x) or abs(x) < 3.4e38]
+    return np.concatenate([v, np.array(edge)])
+
+
+@pytest.mark.parametrize("kind", [8, 4])
+def test_list_directed_items_match_restatement(built, kind):
+    from wtb_gb300 import api
+
+    rng = np.random.default_rng(11 + kind)
+    w, d = (25, 17) if kind == 8 else (16, 9)
+    for x in _ld_values(rng, 3000, kind):
+        assert api.fortran_format("G", x, w, d) == O.list_directed_real(x, kind), (kind, repr(x))
+
+
+def test_list_directed_known_outputs(built):
+    """gfortran's list-directed output of a few values (a blank, then the item's field)."""
+    from wtb_gb300 import api
+
+    known8 = {1.0: "   1.0000000000000000     ", 0.1: "  0.10000000000000001     ",
+              1e-3: "   1.0000000000000000E-003", -1.0: "  -1.0000000000000000     ",
+              0.0: "   0.0000000000000000     ", 123.456: "   123.45600000000000     "}
+    known4 = {1.0: "   1.00000000    ", 0.1: "  0.100000001    ", 1e-3: "   1.00000005E-03"}
+    for x, s in known8.items():
+        assert O.list_directed_record([("r8", x)]) == s
+        assert " " + api.fortran_format("G", x, 25, 17) == s
+    for x, s in known4.items():
+        assert O.list_directed_record([("r4", x)]) == s
+        assert " " + api.fortran_format("G", x, 16, 9) == s
+    assert O.list_directed_record([("i", 1), ("i", -2)]) == "           1          -2"
+    assert O.list_directed_record([("c", "#"), ("c", "  "), ("c", "energy"), ("i", 3), ("c", "x")]) == \
+        " #  energy           3 x"
+    assert O.list_directed_record([]) == ""
+
+
+def test_list_directed_files(built, tmp_path):
+    from wtb_gb300 import api
+
+    rng = np.random.default_rng(12)
+    numbse = 41
+    dielf = np.stack([np.linspace(0.0, 6.0, numbse), rng.uniform(-3, 30, numbse), rng.uniform(0, 25, numbse)], 1)
+    dielf[3, 2] = 1e-7                                    # an E-form item
+    path = os.path.join(tmp_path, "bse_diel_xx.dat")
+    api.write_diel(path, dielf)
+    want = [O.list_directed_record([("c", "#"), ("c", "  "), ("c", "energy"), ("c", "  "), ("c", "real"),
+                                    ("c", "  "), ("c", "imag")])]
+    want += [O.list_directed_record([("r8", r[0]), ("r4", r[1]), ("r4", r[2])]) for r in dielf]
+    assert open(path).read() == "\n".join(want) + "\n"
+    back = _read_table(path, 1)                           # bseoptprop's list-directed read of the file
+    assert np.array_equal(back[:, 0], dielf[:, 0])        # 17 significant digits: REAL(8) round-trips
+    assert np.array_equal(back[:, 1:].astype(np.float32), dielf[:, 1:].astype(np.float32))
+
+    nq, dim = 7, 5
+    qpath = np.zeros((nq, 4))
+    qpath[:, 0] = np.linspace(0.0, 1.0, nq)
+    exk = np.sort(rng.uniform(1.5, 4.0, (dim, nq)), axis=0)
+    path = os.path.join(tmp_path, "bands_bse.dat")
+    api.write_bands_bse(path, qpath, exk)
+    want = []
+    for b in range(dim):
+        want += [O.list_directed_record([("r4", qpath[i, 0]), ("r8", exk[b, i])]) for i in range(nq)] + [""]
+    assert open(path).read() == "\n".join(want) + "\n"
+
+    nk = 9
+    kpt = rng.uniform(-0.5, 0.5, (nk, 3))
+    act = rng.uniform(0, 5, (nk, 6))
+    act[2, 5] = np.nan                                     # (sp - sm)/(sp + sm) of a k-point with no activity
+    path = os.path.join(tmp_path, "dichroism.dat")
+    api.write_bz_act(path, kpt, act[:, 5])
+    want = [O.list_directed_record([("r4", k[0]), ("r4", k[1]), ("r4", k[2]), ("r8", a)])
+            for k, a in zip(kpt, act[:, 5])]
+    assert open(path).read() == "\n".join(want) + "\n"
+    assert open(path).read().splitlines()[2].endswith("NaN")

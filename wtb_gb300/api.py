@@ -113,6 +113,9 @@ def _load():
         "wtb_bse_q_eigenpairs": [P, C.POINTER(CParams), dp, C.c_int, C.c_int, dp, dp],
         "wtb_exciton_lifetime": [P, C.c_char_p, ip, C.c_int, dp, C.c_int, dp],
         "wtb_write_exciton_lifetime": [C.c_char_p, C.c_int, dp, dp, C.c_int],
+        "wtb_write_diel": [C.c_char_p, C.c_int, dp],
+        "wtb_write_bands_bse": [C.c_char_p, C.c_int, C.c_int, dp, dp],
+        "wtb_write_bz_act": [C.c_char_p, C.c_int, dp, dp],
         "wtb_fortran_format": [C.c_char, C.c_double, C.c_int, C.c_int, C.c_char_p, C.c_int],
         "wtb_bsesolvertemp": [P, C.POINTER(CParams), C.POINTER(CTempParams), dp, dp, dp, dp],
         "wtb_bsebndstemp": [P, C.POINTER(CParams), C.POINTER(CTempParams), C.c_int, dp, dp],
@@ -222,7 +225,8 @@ def kpathbse(rlat1, rlat2, rlat3, ks, npts):
 
 
 def fortran_format(kind, x, w, d):
-    """One Fortran edit descriptor (F, E or I) as the output writers apply it."""
+    """One Fortran edit descriptor (F, E or I) as the output writers apply it; kind G with (w, d) = (25, 17) or
+    (16, 9) is one REAL(8) or REAL(4) item of a list-directed record."""
     buf = C.create_string_buffer(w + 1)
     r = _lib.wtb_fortran_format(kind.encode(), float(x), int(w), int(d), buf, w + 1)
     if r:
@@ -275,6 +279,30 @@ def write_exciton_lifetime(path, energy, lft, pol=False):
     assert L.shape == (len(e), 6 if pol else 4)
     _w(_lib.wtb_write_exciton_lifetime(os.fsencode(path), len(e), _dp(e), _dp(L), int(bool(pol))),
        "wtb_write_exciton_lifetime")
+
+
+def write_diel(path, dielf):
+    """One component of bse_diel_*.dat or sp_diel*.dat from dielf (numbse, 3) = omega, eps1, eps2 (one value of
+    the dict bsedielraw / spdielraw return)."""
+    D = np.asfortranarray(dielf, dtype=np.float64)
+    assert D.ndim == 2 and D.shape[1] == 3
+    _w(_lib.wtb_write_diel(os.fsencode(path), D.shape[0], _dp(D)), "wtb_write_diel")
+
+
+def write_bands_bse(path, qpath, exk):
+    """bands_bse.dat from qpath (nq, 4) (kpathbse) and exk (dim, nq) (bsebnds / bsebndstemp)."""
+    q = np.asfortranarray(qpath, dtype=np.float64)
+    E = np.asfortranarray(exk, dtype=np.float64)
+    assert q.ndim == 2 and E.ndim == 2 and E.shape[1] == q.shape[0]
+    _w(_lib.wtb_write_bands_bse(os.fsencode(path), q.shape[0], E.shape[0], _dp(q), _dp(E)), "wtb_write_bands_bse")
+
+
+def write_bz_act(path, kpt, value):
+    """One of bz_act_x/y/z/sp/sm.dat or dichroism.dat from kpt (nk, 3) and one column of spoptpolbz's act."""
+    k = np.asfortranarray(kpt, dtype=np.float64)
+    v = np.ascontiguousarray(value, dtype=np.float64)
+    assert k.shape == (len(v), 3)
+    _w(_lib.wtb_write_bz_act(os.fsencode(path), len(v), _dp(k), _dp(v)), "wtb_write_bz_act")
 
 
 def eigsys(nthreads, scs, exc, nocp, ffactor, kx, ky, kz, w90basis, nvec, rlat, rvec, hopmatrices, ihopmatrices,

@@ -9,13 +9,20 @@
 //   Ew.d  0.d1...dd E+xx (E dropped for a three-digit exponent), same justification rules;
 //   Iw, Iw.m  right-justified integers, Iw.0 of zero is all blanks; the reference's width-less I is read as
 //         I12, the default width of a 4-byte integer.
-// List-directed records (the '#' header lines) are written as a blank followed by the character items with no
-// separators, and integers in 12-character fields.
+// List-directed records (the '#' header lines, and the whole of bse_diel_*.dat, sp_diel*.dat, bands_bse.dat,
+// bz_act_*.dat and dichroism.dat) are written as gfortran's runtime writes them (the reference's README names the
+// GNU compiler): a blank before the first item, one blank between items except between two character items,
+// 4-byte integers as I11, REAL(8) as 1PG25.17E3 and REAL(4) as 1PG16.9E2.
 //   bse_opt_diel.dat / -pol   src/module_bse.F90:2132-2133, :2556-2567 (7F15.4 / 6F15.4)
 //   sp_optics.dat / -pol      :2296-2297, :2366-2367 (7F15.4 / 6F15.4)
 //   tm_coef.dat / -pol        :2300-2311, :2370-2377 (3F10.4,3I10.0,7F10.4 / ...,6F10.4)
 //   exc_wf_<n>.dat            excwf2, :374-408 ((I,3F15.4,2I,2E15.4)); exc_wf_<n>_<q>.dat excwfi2, :412-448
 //   exciton_lifetime.dat      lifetime, :3271-3349 ((1F15.4,4E15.4)); -pol: lifetimepol, :3353-3432 ((1F15.4,6E15.4))
+//   bse_diel_*.dat            bsedielraw, :926-931, :1004-1009; bsedielrawpol :1130-1134, :1174-1178;
+//   sp_diel_*.dat             spdielraw / spdielrawpol (same records): REAL(8) energy, two REAL(4)
+//   bands_bse.dat             bsebnds, :1536-1543 / bsebndstemp :1981-1990: REAL(4) path coordinate, REAL(8)
+//                             energy, an empty record after each band
+//   bz_act_*.dat, dichroism   spoptpolbz, :4754-4759: three REAL(4) k coordinates, one REAL(8)
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -143,29 +150,74 @@ namespace {
 using wtb::fortran_E;
 using wtb::fortran_F;
 using wtb::fortran_I;
+using wtb::fortran_special;
 
-// a list-directed record of character items: a leading blank, the items without separators
-std::string ld_chars(std::initializer_list<const char*> items) {
-  std::string s = " ";
-  for (const char* it : items) s += it;
-  return s;
+// One real item of a list-directed WRITE as gfortran's runtime edits it: G editing with scale factor 1P,
+// 1PG25.17E3 for REAL(8) (kind 8) and 1PG16.9E2 for REAL(4) (kind 4, of the value rounded to single precision).
+// With r the value rounded to d significant digits and 10^(k-1) <= |r| < 10^k: F(w-n).(d-k) followed by n = e+2
+// blanks when 0 <= k <= d, else one digit, the point, d-1 digits and E+-e digits; zero as F(w-n).(d-1).
+// The C library's conversions round the exact binary value to nearest, ties to even.
+std::string ld_real(double x, int kind) {
+  const int w = kind == 8 ? 25 : 16, d = kind == 8 ? 17 : 9, e = kind == 8 ? 3 : 2, n = e + 2;
+  if (kind != 8) x = (double)(float)x;
+  if (std::isnan(x) || std::isinf(x)) return fortran_special(x, w);
+  const std::string sign = std::signbit(x) ? "-" : "";
+  auto pad = [](const std::string& t, int width) {
+    return (int)t.size() >= width ? t : std::string((size_t)(width - (int)t.size()), ' ') + t;
+  };
+  char buf[128];
+  if (x == 0.0) return pad(sign + "0." + std::string((size_t)(d - 1), '0'), w - n) + std::string((size_t)n, ' ');
+  std::snprintf(buf, sizeof(buf), "%.*e", d - 1, std::fabs(x));  // "D.DDDe+XX", rounded to d digits
+  const char* ep = std::strchr(buf, 'e');
+  const int ex = std::atoi(ep + 1), k = ex + 1;
+  if (k >= 0 && k <= d) {
+    char fb[128];
+    std::snprintf(fb, sizeof(fb), "%#.*f", d - k, std::fabs(x));  // '#': the point also with no decimals
+    return pad(sign + fb, w - n) + std::string((size_t)n, ' ');
+  }
+  char xb[16];
+  std::snprintf(xb, sizeof(xb), "E%c%0*d", ex < 0 ? '-' : '+', e, std::abs(ex));
+  return pad(sign + std::string(buf, (size_t)(ep - buf)) + xb, w);
 }
 
-// a list-directed 4-byte integer item
-std::string ld_int(long v) { return fortran_I(v, 12, 1); }
+// One list-directed output record as gfortran writes it: a blank before the first item, one blank before
+// every later item except a character item that follows a character item; character items as they are,
+// 4-byte integers as I11, reals by ld_real.  A WRITE with no items is an empty record.
+struct LdRecord {
+  std::string s;
+  bool first = true, prev_char = false;
+  void sep(bool is_char) {
+    if (first || !(is_char && prev_char)) s += ' ';
+    first = false;
+    prev_char = is_char;
+  }
+  LdRecord& c(const char* t) {
+    sep(true);
+    s += t;
+    return *this;
+  }
+  LdRecord& i(long v) {
+    sep(false);
+    s += fortran_I(v, 11, 1);
+    return *this;
+  }
+  LdRecord& r8(double v) {
+    sep(false);
+    s += ld_real(v, 8);
+    return *this;
+  }
+  LdRecord& r4(double v) {
+    sep(false);
+    s += ld_real(v, 4);
+    return *this;
+  }
+};
 
-// a list-directed REAL(8) item: 15 significant digits in a 25-character field
-std::string ld_real8(double v) {
-  char buf[64];
-  std::snprintf(buf, sizeof(buf), "%25.15G", v);
-  return buf;
-}
-
-// a list-directed REAL(4) item: 7 significant digits in a 15-character field
-std::string ld_real4(double v) {
-  char buf[64];
-  std::snprintf(buf, sizeof(buf), "%15.7G", (double)(float)v);
-  return buf;
+// a record of character items only
+LdRecord ld_chars(std::initializer_list<const char*> items) {
+  LdRecord r;
+  for (const char* it : items) r.c(it);
+  return r;
 }
 
 struct File {
@@ -175,6 +227,7 @@ struct File {
     if (f) std::fclose(f);
   }
   void line(const std::string& s) { std::fputs((s + "\n").c_str(), f); }
+  void line(const LdRecord& r) { line(r.s); }
 };
 
 }  // namespace
@@ -190,6 +243,10 @@ int wtb_fortran_format(char kind, double x, int w, int d, char* out, int outlen)
     s = fortran_E(x, w, d);
   else if (kind == 'I')
     s = fortran_I((long)x, w, d);
+  else if (kind == 'G' && w == 25 && d == 17)
+    s = ld_real(x, 8);
+  else if (kind == 'G' && w == 16 && d == 9)
+    s = ld_real(x, 4);
   else
     return WTB_EBADARG;
   std::memcpy(out, s.c_str(), s.size() + 1);
@@ -246,9 +303,9 @@ int wtb_write_tm_coef(const char* path, int nk, int nc, int nv, const float* rec
   File f(path);
   if (!f.f) return WTB_EBADARG;
   const size_t n = (size_t)nk * nc * nv;
-  f.line(ld_chars({"number of kpoints:"}) + ld_int(nk));
-  f.line(ld_chars({"number of conduction states"}) + ld_int(nc));
-  f.line(ld_chars({"number of valence states"}) + ld_int(nv));
+  f.line(ld_chars({"number of kpoints:"}).i(nk));
+  f.line(ld_chars({"number of conduction states"}).i(nc));
+  f.line(ld_chars({"number of valence states"}).i(nv));
   if (!pol)
     f.line(ld_chars({"#", " ", "kx", " ", "ky", " ", "kz", " ", "nocp", " ", "nc", " ", "nv", "  ", "energy", "  ",
                      "xx", "  ", "yy", "  ", "zz", "  ", "xy", "  ", "xz", "  ", "yz"}));
@@ -276,13 +333,13 @@ int wtb_write_exc_wf(const char* path, int nk, int nc, int nv, const int* nocpk,
   if (!f.f) return WTB_EBADARG;
   const size_t nkk = (size_t)nk;
   if (q4)  // excwfi2's momentum line: three REAL(4) list-directed items
-    f.line(ld_chars({"#", " ", "excitonic momentum"}) + ld_real4(q4[1]) + ld_real4(q4[2]) + ld_real4(q4[3]));
-  f.line(ld_chars({"#", " ", "excitonic state"}) + ld_int(excnum));
-  f.line(ld_chars({"#", " ", "exciton energy:"}) + ld_real8(energy));
-  f.line(ld_chars({"#", " ", "number occupied states"}) + ld_int(nocpk[0]) + "(not valid for metallic systems)");
-  f.line(ld_chars({"#", " ", "Number of conduction states", ""}) + ld_int(nc));
-  f.line(ld_chars({"#", " ", "Number of valence states", ""}) + ld_int(nv));
-  f.line(ld_chars({"#", " ", "Number of kpoints", ""}) + ld_int(nk));
+    f.line(ld_chars({"#", " ", "excitonic momentum"}).r4(q4[1]).r4(q4[2]).r4(q4[3]));
+  f.line(ld_chars({"#", " ", "excitonic state"}).i(excnum));
+  f.line(ld_chars({"#", " ", "exciton energy:"}).r8(energy));
+  f.line(ld_chars({"#", " ", "number occupied states"}).i(nocpk[0]).c("(not valid for metallic systems)"));
+  f.line(ld_chars({"#", " ", "Number of conduction states", ""}).i(nc));
+  f.line(ld_chars({"#", " ", "Number of valence states", ""}).i(nv));
+  f.line(ld_chars({"#", " ", "Number of kpoints", ""}).i(nk));
   f.line(ld_chars({"#", " ", "nocpk", " ", "kx", " ", "ky", " ", "kz", " ", "nc", " ", "nv", " ", "re_wf", " ",
                    "imag_wf"}));
   size_t I = 0;
@@ -314,6 +371,36 @@ int wtb_write_exciton_lifetime(const char* path, int dim, const double* energy, 
     for (int c = 0; c < nout; ++c) s += fortran_E(lft[c * n + i], 15, 4);
     f.line(s);
   }
+  return std::ferror(f.f) ? WTB_EBADARG : WTB_OK;
+}
+
+int wtb_write_diel(const char* path, int numbse, const double* dielf) {
+  if (!path || numbse < 1 || !dielf) return WTB_EBADARG;
+  File f(path);
+  if (!f.f) return WTB_EBADARG;
+  const size_t n = (size_t)numbse;
+  f.line(ld_chars({"#", "  ", "energy", "  ", "real", "  ", "imag"}));
+  for (size_t i = 0; i < n; ++i) f.line(LdRecord().r8(dielf[i]).r4(dielf[n + i]).r4(dielf[2 * n + i]));
+  return std::ferror(f.f) ? WTB_EBADARG : WTB_OK;
+}
+
+int wtb_write_bands_bse(const char* path, int nq, int dim, const double* qpath, const double* exk) {
+  if (!path || nq < 1 || dim < 1 || !qpath || !exk) return WTB_EBADARG;
+  File f(path);
+  if (!f.f) return WTB_EBADARG;
+  for (size_t b = 0; b < (size_t)dim; ++b) {
+    for (size_t i = 0; i < (size_t)nq; ++i) f.line(LdRecord().r4(qpath[i]).r8(exk[i * (size_t)dim + b]));
+    f.line(LdRecord());
+  }
+  return std::ferror(f.f) ? WTB_EBADARG : WTB_OK;
+}
+
+int wtb_write_bz_act(const char* path, int nk, const double* kpt, const double* value) {
+  if (!path || nk < 1 || !kpt || !value) return WTB_EBADARG;
+  File f(path);
+  if (!f.f) return WTB_EBADARG;
+  const size_t n = (size_t)nk;
+  for (size_t k = 0; k < n; ++k) f.line(LdRecord().r4(kpt[k]).r4(kpt[n + k]).r4(kpt[2 * n + k]).r8(value[k]));
   return std::ferror(f.f) ? WTB_EBADARG : WTB_OK;
 }
 
