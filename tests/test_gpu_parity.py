@@ -160,13 +160,23 @@ def test_bsesolver_hex8_24x24(ctx, c1, precision, op):
         assert rel_l2(spec[c][:, 2], spec_ref[c][:, 2]) <= 1e-4, c
 
 
-def test_spectrum_kernel(ctx, c1):
+def test_spectrum_kernel(ctx, c1, tmp_path):
+    """bsedielraw's spectra against the oracle, and bse_diel_xx.dat written from them and read back as
+    bseoptprop reads it (energies exactly, eps1 and eps2 at single precision)."""
     sysm, p, ref = c1
     ctx.set_hr(sysm)
     d = ctx.bsedielraw(p, ref["Ws"], ref["acts"])
     d_ref = O.bsedielraw(ref["Ws"], ref["acts"], p.ngrid, sysm.rlat, p)
     for c in O.COMPONENTS:
         np.testing.assert_allclose(d[c], d_ref[c], rtol=1e-10, atol=1e-12 * max(1.0, np.abs(d_ref[c]).max()))
+    from wtb_gb300 import api
+    path = str(tmp_path / "bse_diel_xx.dat")
+    api.write_diel(path, d["xx"])
+    lines = open(path).read().splitlines()
+    back = np.array([[float(t) for t in ln.split()] for ln in lines[1:]])
+    assert lines[0] == " #  energy  real  imag" and back.shape == d["xx"].shape
+    assert np.array_equal(back[:, 0], d["xx"][:, 0])
+    assert np.array_equal(back[:, 1:].astype(np.float32), d["xx"][:, 1:].astype(np.float32))
 
 
 def test_optprops_kernel(ctx, c1):
