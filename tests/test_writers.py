@@ -203,6 +203,8 @@ def test_list_directed_known_outputs(built):
     assert O.list_directed_record([("c", "#"), ("c", "  "), ("c", "energy"), ("i", 3), ("c", "x")]) == \
         " #  energy           3 x"
     assert O.list_directed_record([]) == ""
+    with pytest.raises(api.WTBError):                     # only the two list-directed real kinds exist
+        api.fortran_format("G", 1.0, 20, 10)
 
 
 def test_list_directed_files(built, tmp_path):
