@@ -511,16 +511,24 @@ def bse_matvec_factored(x, eigv, vec, kpt, p, rlat, V=None):
     """Matrix-free y = H x through V(k,k') and the orbital factorisation; same operator as bse_build."""
     nk = len(kpt)
     nc, nv = p.nc, p.nv
+    w = vec.shape[2]
     if V is None:
         V = coulomb_table(kpt, kpt, p, rlat)
     C = vec[:, nv:nv + nc]        # (nk, nc, w)
     Vb = vec[:, :nv]              # (nk, nv, w)
-    X = x.reshape(nk, nc, nv, -1)
-    Z = np.einsum("kco,kvp,kcvb->kopb", C, Vb, X)
-    T = np.einsum("kq,qopb->kopb", V, Z)
-    Y = np.einsum("kco,kvp,kopb->kcvb", np.conj(C), np.conj(Vb), T)
+    nb = x.size // (nk * nc * nv)
+    X = x.reshape(nk, nc, nv, nb)
+    # Z[k,o,p,b] = sum_{c,v} C[k,c,o] Vb[k,v,p] X[k,c,v,b], as two batched products over k
+    U = np.matmul(np.swapaxes(Vb, 1, 2)[:, None], X)                     # (nk, nc, w_p, nb)
+    Z = np.matmul(np.swapaxes(C, 1, 2), U.reshape(nk, nc, w * nb))       # (nk, w_o, w_p*nb)
+    # T = V Z with V real: one real product on the interleaved re/im panel
+    Zr = np.ascontiguousarray(Z).view(np.float64).reshape(nk, -1)
+    T = (V @ Zr).view(np.complex128).reshape(nk, w, w, nb)               # (nk, o, p, b)
+    # Y[k,c,v,b] = sum_{o,p} conj(C[k,c,o]) conj(Vb[k,v,p]) T[k,o,p,b]
+    R = np.matmul(np.conj(C), T.reshape(nk, w, w * nb)).reshape(nk, nc, w, nb)
+    Y = np.matmul(np.conj(Vb)[:, None], R)                               # (nk, nc, nv, nb)
     dE = (eigv[:, nv:nv + nc][:, :, None] - eigv[:, :nv][:, None, :])
-    Y += dE[..., None] * X
+    Y = Y + dE[..., None] * X
     return Y.reshape(x.shape)
 
 

@@ -83,8 +83,112 @@ def make_next_rows(name="hex8_6x6"):
     print(name, "next rows: lowest finite-Q", out["exk"][:2, :].T)
 
 
+def system_arrays(sysm):
+    """The seeded system itself, stored beside the results: the generator bisects the gap with LAPACK, whose
+    last bits may differ between machines, so the full-size tests rebuild the system from these arrays."""
+    return {"hop": sysm.hop, "ihop": sysm.ihop, "rvec": sysm.rvec.astype(np.int32),
+            "ffactor": sysm.ffactor.astype(np.int32), "rlat": sysm.rlat, "efermi": np.array(sysm.efermi),
+            "scs": np.array(sysm.scs), "systype": np.array(sysm.systype)}
+
+
+def make_fullsize(name, ncv_factor=4, tol=1e-10):
+    """Lowest nev excitons of a full-size workload from the oracle's FP64 factored operator
+    (bse_matvec_factored: the matrix of the reference's element-by-element build, never formed) under
+    ARPACK's implicitly restarted Lanczos (which='SA', tol 1e-10), standing in for SLEPc Krylov-Schur.
+    Two runs from different start vectors must agree to 1e-9 eV and every residual ||Hx - Ex|| must be
+    below 1e-8 eV; then the activities (dielbsev/dielbsep) and the three bsedielraw spectra."""
+    import time
+
+    import scipy.sparse.linalg as sla
+
+    sysm, p = S.workload(name)
+    kpt = O.monhkhorst_pack(p.ngrid[0], p.ngrid[1], p.ngrid[2], p.mshift, sysm.rlat)
+    eigv, vec, nocpk = O.bands(sysm, p, kpt)
+    V = O.coulomb_table(kpt, kpt, p, sysm.rlat)
+    hrx, hry, hrz, hrsp, hrsm = O.optsp_all(eigv, vec, kpt, sysm, p)
+    dim, nev = p.dim, p.nev
+
+    def mv(x):
+        return O.bse_matvec_factored(x.reshape(dim, -1), eigv, vec, kpt, p, sysm.rlat, V).reshape(x.shape)
+
+    op = sla.LinearOperator((dim, dim), dtype=np.complex128, matvec=mv, matmat=mv)
+    runs = []
+    for seed in (1, 2):
+        v0 = np.random.default_rng(seed).normal(size=dim) + 1j * np.random.default_rng(seed + 10).normal(size=dim)
+        t0 = time.time()
+        E, A = sla.eigsh(op, k=nev, which="SA", tol=tol, ncv=ncv_factor * nev, v0=v0)
+        o = np.argsort(E)
+        runs.append((E[o], A[:, o]))
+        print(f"{name}: ARPACK run {seed}: {time.time() - t0:.1f} s, E = {E[o]}")
+    E, A = runs[0]
+    assert np.max(np.abs(runs[1][0] - E)) < 1e-9, runs[1][0] - E
+    res = np.linalg.norm(mv(A) - A * E[None, :], axis=0)
+    assert res.max() < 1e-8, res
+    Ws = np.zeros(dim)
+    Ws[:nev] = E
+    acts = {"xx": O.dielbsev(A, hrx, dim), "yy": O.dielbsev(A, hry, dim), "zz": O.dielbsev(A, hrz, dim),
+            "xy": O.dielbsep(A, hrx, hry, dim), "xz": O.dielbsep(A, hrx, hrz, dim),
+            "yz": O.dielbsep(A, hry, hrz, dim), "sp": O.dielbsev(A, hrsp, dim), "sm": O.dielbsev(A, hrsm, dim)}
+    spec = O.bsedielraw(Ws, acts, p.ngrid, sysm.rlat, p)
+    out = {"digest": np.array(input_digest(sysm)), "E": E, "residual": res, "eigv_min_gap": np.array(
+        np.min(np.diff(E))), **system_arrays(sysm)}
+    for c in ("xx", "yy", "zz", "xy", "xz", "yz", "sp", "sm"):
+        out["act_" + c] = acts[c][:nev]
+    for c in ("xx", "yy", "zz"):
+        out["spec_" + c] = spec[c]
+    np.savez_compressed(os.path.join(HERE, name + "_oracle.npz"), **out)
+    print(name, "residuals", res.max(), "smallest gap", np.min(np.diff(E)))
+
+
+def lowest_factored(sysm, p, nev, tol=1e-10):
+    """Lowest nev excitons (energies, vectors) of the FP64 factored operator under ARPACK, with the bands."""
+    import scipy.sparse.linalg as sla
+
+    kpt = O.monhkhorst_pack(p.ngrid[0], p.ngrid[1], p.ngrid[2], p.mshift, sysm.rlat)
+    eigv, vec, _ = O.bands(sysm, p, kpt)
+    V = O.coulomb_table(kpt, kpt, p, sysm.rlat)
+    dim = p.dim
+
+    def mv(x):
+        return O.bse_matvec_factored(x.reshape(dim, -1), eigv, vec, kpt, p, sysm.rlat, V).reshape(x.shape)
+
+    op = sla.LinearOperator((dim, dim), dtype=np.complex128, matvec=mv, matmat=mv)
+    v0 = np.random.default_rng(5).normal(size=dim) + 0.5j
+    E, A = sla.eigsh(op, k=nev, which="SA", tol=tol, ncv=max(4 * nev, 20), v0=v0)
+    o = np.argsort(E)
+    E, A = E[o], A[:, o]
+    res = np.linalg.norm(mv(A) - A * E[None, :], axis=0)
+    assert res.max() < 1e-8, res
+    return E, A, res
+
+
+def make_batch_subset():
+    """Three systems of the 64-system strained batch (the smallest, a middle and the largest BSE dimension):
+    their lowest 6 excitons from the FP64 factored operator under ARPACK (tol 1e-10)."""
+    batch = S.strained_batch(nsys=64)
+    dims = np.array([p.dim for _, p in batch])
+    order = np.argsort(dims, kind="stable")
+    pick = sorted({int(order[0]), int(order[len(order) // 2]), int(order[-1])})
+    out = {"systems": np.array(pick)}
+    for i in pick:
+        sysm, p = batch[i]
+        E, _, res = lowest_factored(sysm, p, p.nev)
+        out[f"E_{i}"] = E
+        out[f"dim_{i}"] = np.array(p.dim)
+        out[f"digest_{i}"] = np.array(input_digest(sysm))
+        print("batch system", i, "dim", p.dim, "E", E, "residual", res.max())
+    np.savez_compressed(os.path.join(HERE, "batch64_subset_oracle.npz"), **out)
+
+
 if __name__ == "__main__":
-    for n in ("hex8_6x6", "hex8_24x24"):
-        make(n)
-    make_fit_target()
-    make_next_rows()
+    which = sys.argv[1:] or ["small"]
+    if "batch64" in which:
+        make_batch_subset()
+    if "small" in which:
+        for n in ("hex8_6x6", "hex8_24x24"):
+            make(n)
+        make_fit_target()
+        make_next_rows()
+    for n in ("hex12_60x60", "cubic16_16x16x16"):
+        if n in which:
+            make_fullsize(n)

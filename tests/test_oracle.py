@@ -364,3 +364,27 @@ def test_c_restatement_matches_numpy(built, small):
     H = O.bse_build(eigv, vec, kpt, p, sysm.rlat)
     iu = np.triu_indices(dim)
     np.testing.assert_allclose(out[iu], H[iu], rtol=0, atol=1e-14)
+
+
+@pytest.mark.parametrize("name", ["hex12_60x60", "cubic16_16x16x16"])
+def test_fullsize_fixture_consistent(name):
+    """The full-size oracle fixtures: the stored system is the seeded one, the stored ARPACK residuals are
+    below 1e-8 eV, and the stored spectra are bsedielraw of the stored energies and activities."""
+    import os
+
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", name + "_oracle.npz")
+    g = np.load(path)
+    sysm = S.system_from_arrays(g)
+    regen, p = S.workload(name)
+    np.testing.assert_allclose(sysm.hop, regen.hop, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(sysm.ihop, regen.ihop, rtol=0, atol=1e-12)
+    np.testing.assert_array_equal(sysm.rvec, regen.rvec)
+    assert abs(sysm.efermi - regen.efermi) < 1e-12
+    assert g["E"].shape == (p.nev,) and np.all(np.diff(g["E"]) > 0)
+    assert np.all(g["residual"] < 1e-8)
+    Ws = np.zeros(p.dim)
+    Ws[: p.nev] = g["E"]
+    acts = {c: np.concatenate([g["act_" + c], np.zeros(p.dim - p.nev)]) for c in O.COMPONENTS}
+    spec = O.bsedielraw(Ws, acts, p.ngrid, sysm.rlat, p)
+    for c in ("xx", "yy", "zz"):
+        np.testing.assert_allclose(spec[c], g["spec_" + c], rtol=1e-12, atol=1e-14)

@@ -228,8 +228,9 @@ def rk_params(ngrid, nc, nv, nev, r0=40.0) -> BSEParams:
                      ebse0=0.0, ebsef=5.0, numbse=1000, nev=nev, renorm=True)
 
 
-def workload(name: str, seed: int | None = None):
-    """The named workloads: returns (TBSystem, BSEParams).
+def workload(name: str, seed: int | None = None, params_only: bool = False):
+    """The named workloads: returns (TBSystem, BSEParams); with params_only the system is not generated and
+    (None, BSEParams) is returned.
 
     * ``hex8_24x24``   : 2D hexagonal, w=8, |R|<=3a (37), 24x24x1, 2v+2c, dim 2304, V2DRK r0=40 A,
                          10 excitons, spectrum 0-5 eV at 1000 points, CSHIFT 0.05.
@@ -240,33 +241,40 @@ def workload(name: str, seed: int | None = None):
     * ``hex8_6x6``     : a small 2D case (dim 144) for fast checks.
     """
     if name == "hex8_24x24":
-        s = 11 if seed is None else seed
-        ng = (24, 24, 1)
-        return make_system(s, 8, "hex", 3, 1.5, ng), rk_params(ng, 2, 2, 10)
-    if name == "cubic16_16x16x16":
-        s = 12 if seed is None else seed
+        spec, p = (11, 8, "hex", 3, 1.5, (24, 24, 1)), rk_params((24, 24, 1), 2, 2, 10)
+    elif name == "cubic16_16x16x16":
         ng = (16, 16, 16)
-        sysm = make_system(s, 16, "cubic", 2, 2.0, ng)
+        spec = (12, 16, "cubic", 2, 2.0, ng)
         p = BSEParams(ngrid=ng, nc=3, nv=3, coultype="V3DL", ktol=1e-3, ediel=(1.0, 8.0, 1.0),
                       cshift=0.05, ebse0=0.0, ebsef=5.0, numbse=1000, nev=20)
-        return sysm, p
-    if name == "hex12_60x60":
-        s = 13 if seed is None else seed
-        ng = (60, 60, 1)
-        return make_system(s, 12, "hex", 3, 1.5, ng), rk_params(ng, 4, 4, 10)
-    if name == "hex8_36x36":
-        s = 15 if seed is None else seed
-        ng = (36, 36, 1)
-        return make_system(s, 8, "hex", 3, 1.5, ng), rk_params(ng, 2, 2, 4)
-    if name.startswith("hex"):
+    elif name == "hex12_60x60":
+        spec, p = (13, 12, "hex", 3, 1.5, (60, 60, 1)), rk_params((60, 60, 1), 4, 4, 10)
+    elif name == "hex8_36x36":
+        spec, p = (15, 8, "hex", 3, 1.5, (36, 36, 1)), rk_params((36, 36, 1), 2, 2, 4)
+    elif name.startswith("hex"):
         # generic "hex{w}_{n}x{n}" with 2v+2c
-        body = name[3:]
-        w_s, mesh = body.split("_")
+        w_s, mesh = name[3:].split("_")
         n = int(mesh.split("x")[0])
-        s = 17 if seed is None else seed
-        ng = (n, n, 1)
-        return make_system(s, int(w_s), "hex", 3, 1.5, ng), rk_params(ng, 2, 2, 4)
-    raise KeyError(name)
+        spec, p = (17, int(w_s), "hex", 3, 1.5, (n, n, 1)), rk_params((n, n, 1), 2, 2, 4)
+    else:
+        raise KeyError(name)
+    if params_only:
+        return None, p
+    s0, w, lattice, rmax, gap, ng = spec
+    return make_system(s0 if seed is None else seed, w, lattice, rmax, gap, ng), p
+
+
+def system_from_arrays(a) -> TBSystem:
+    """A TBSystem from stored arrays (a mapping such as an opened .npz with hop, ihop, rvec, ffactor, rlat,
+    efermi and optionally scs and systype)."""
+    keys = set(a.keys()) if hasattr(a, "keys") else set(a.files)
+    return TBSystem(w90basis=int(a["hop"].shape[1]), rvec=np.ascontiguousarray(a["rvec"], dtype=np.int32),
+                    ffactor=np.ascontiguousarray(a["ffactor"], dtype=np.int32),
+                    hop=np.ascontiguousarray(a["hop"], dtype=np.float64),
+                    ihop=np.ascontiguousarray(a["ihop"], dtype=np.float64),
+                    rlat=np.ascontiguousarray(a["rlat"], dtype=np.float64), efermi=float(a["efermi"]),
+                    scs=float(a["scs"]) if "scs" in keys else 0.0,
+                    systype=str(a["systype"]) if "systype" in keys else "2D")
 
 
 def strained_batch(seed: int = 14, nsys: int = 64, base_w: int = 8):
