@@ -180,8 +180,104 @@ def make_batch_subset():
     np.savez_compressed(os.path.join(HERE, "batch64_subset_oracle.npz"), **out)
 
 
+def make_grad_c5(name="hex8_36x36", nentries=24, h=1e-6, seed=77):
+    """The differentiation form at its own size (dim 5184, lowest 4): the FP64 gradient oracle's
+    (oracle/wtb_oracle_grad.py) gradients with respect to every H(R) entry and r0 of five losses -- each of the
+    lowest 4 exciton energies and the L2 spectrum loss against the fitting case's target spectrum -- and
+    central differences (step h = 1e-6) of the oracle's forward for the same five losses on a seeded sample
+    of H(R) entries and on r0.  The forward of the differences is the factored operator under ARPACK at
+    machine precision (energies and xx activities of the lowest 4)."""
+    import copy
+    import time
+
+    import scipy.sparse.linalg as sla
+
+    from oracle import wtb_oracle_grad as OG
+
+    sysm, p = S.workload(name)
+    target = np.load(os.path.join(HERE, name + "_fit_target.npz"))["target"]
+    vc = O.vcell3D(sysm.rlat)
+    spinf = 2.0 if sysm.systype == "NP" else 1.0
+    nev = p.nev
+    t0 = time.time()
+    d = OG.forward(sysm, p)
+    print("forward", time.time() - t0, "E", d["E"])
+
+    def loss_spec(E, f):
+        return OG.spectrum_loss(E, f, p.dim, p, vc, target, spinf)
+
+    # cotangents of the spectrum loss in (E, f): central differences of the scalar loss of 2 nev numbers
+    gE, gf = np.zeros(nev), np.zeros(nev)
+    for n in range(nev):
+        for arr, g in ((d["E"], gE), (d["f"], gf)):
+            hh = 1e-6 * max(1.0, abs(arr[n]))
+            ap, am = arr.copy(), arr.copy()
+            ap[n] += hh
+            am[n] -= hh
+            lp = loss_spec(ap, d["f"]) if arr is d["E"] else loss_spec(d["E"], ap)
+            lm = loss_spec(am, d["f"]) if arr is d["E"] else loss_spec(d["E"], am)
+            g[n] = (lp - lm) / (2 * hh)
+    cot = {f"E{n}": (np.eye(nev)[n], np.zeros(nev)) for n in range(nev)}
+    cot["spec"] = (gE, gf)
+    out = {"digest": np.array(input_digest(sysm)), "E": d["E"], "f": d["f"], "target": target,
+           "spec_loss": np.array(loss_spec(d["E"], d["f"])), "gE_spec": gE, "gf_spec": gf, **system_arrays(sysm)}
+    for key, (a, b) in cot.items():
+        t0 = time.time()
+        dh, di, dr, _ = OG.backward(sysm, p, a, b, d=d)
+        out[f"dhop_{key}"], out[f"dihop_{key}"], out[f"dr0_{key}"] = dh, di, np.array(dr)
+        print("backward", key, time.time() - t0, "dr0", dr)
+
+    def fwd(s, q):
+        kpt = O.monhkhorst_pack(q.ngrid[0], q.ngrid[1], q.ngrid[2], q.mshift, s.rlat)
+        eigv, vec, _ = O.bands(s, q, kpt)
+        V = O.coulomb_table(kpt, kpt, q, s.rlat)
+        hx = O.optsp_all(eigv, vec, kpt, s, q)[0]
+        dim = q.dim
+
+        def mv(x):
+            return O.bse_matvec_factored(x.reshape(dim, -1), eigv, vec, kpt, q, s.rlat, V).reshape(x.shape)
+
+        op = sla.LinearOperator((dim, dim), dtype=np.complex128, matvec=mv, matmat=mv)
+        v0 = np.random.default_rng(3).normal(size=dim) + 0.25j
+        E, A = sla.eigsh(op, k=nev, which="SA", tol=0, ncv=24, v0=v0)
+        o = np.argsort(E)
+        E, A = E[o], A[:, o]
+        f = np.abs(A.T @ hx) ** 2
+        return np.concatenate([E, [loss_spec(E, f)]])
+
+    rng = np.random.default_rng(seed)
+    entries = []
+    while len(entries) < nentries:
+        which = "hop" if len(entries) % 2 == 0 else "ihop"
+        r, m, n = int(rng.integers(sysm.nvec)), int(rng.integers(sysm.w90basis)), int(rng.integers(sysm.w90basis))
+        if (which, r, m, n) not in entries:
+            entries.append((which, r, m, n))
+    fd = np.zeros((nentries + 1, nev + 1))
+    t0 = time.time()
+    for i, (which, r, m, n) in enumerate(entries):
+        sp, sm = copy.deepcopy(sysm), copy.deepcopy(sysm)
+        getattr(sp, which)[r, m, n] += h
+        getattr(sm, which)[r, m, n] -= h
+        fd[i] = (fwd(sp, p) - fwd(sm, p)) / (2 * h)
+    pp, pm = copy.deepcopy(p), copy.deepcopy(p)
+    pp.r0 += h
+    pm.r0 -= h
+    fd[nentries] = (fwd(sysm, pp) - fwd(sysm, pm)) / (2 * h)
+    print("finite differences", time.time() - t0)
+    out["fd_entries"] = np.array([[0 if w == "hop" else 1, r, m, n] for w, r, m, n in entries], dtype=np.int32)
+    out["fd"] = fd  # rows: entries then r0; columns: E0..E3, spectrum loss
+    out["fd_h"] = np.array(h)
+    for i, (which, r, m, n) in enumerate(entries + [("r0", 0, 0, 0)]):
+        for j, key in enumerate(list(cot)):
+            g = out[f"dr0_{key}"] if which == "r0" else out[f"d{which}_{key}"][r, m, n]
+            print(f"{which:4s} {r:2d} {m} {n} {key:5s} grad {float(g): .10e} fd {fd[i, j]: .10e}")
+    np.savez_compressed(os.path.join(HERE, name + "_grad_oracle.npz"), **out)
+
+
 if __name__ == "__main__":
     which = sys.argv[1:] or ["small"]
+    if "grad_c5" in which:
+        make_grad_c5()
     if "batch64" in which:
         make_batch_subset()
     if "small" in which:

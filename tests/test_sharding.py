@@ -2,6 +2,7 @@
 import os
 import socket
 
+import numpy as np
 import pytest
 
 from wtb_gb300.batch import lpt_partition, solve_sharded
@@ -67,3 +68,74 @@ def test_two_rank_gather_gloo():
     assert out[0] == out[1]
     assert [v for v, _ in out[0]] == [i * i for i in range(11)]
     assert {r for _, r in out[0]} == {0, 1}
+
+
+def _lowest_transitions(item):
+    """CPU stand-in for one system's solve: the oracle's bands on the system's mesh and its lowest nev
+    transition energies E_c - E_v (the exciton energies with the Coulomb kernel switched off)."""
+    from oracle import wtb_oracle as O
+
+    sysm, p = item
+    kpt = O.monhkhorst_pack(p.ngrid[0], p.ngrid[1], p.ngrid[2], p.mshift, sysm.rlat)
+    eigv, _, _ = O.bands(sysm, p, kpt)
+    de = (eigv[:, p.nv:p.nv + p.nc][:, :, None] - eigv[:, :p.nv][:, None, :]).ravel()
+    return np.sort(de)[: p.nev]
+
+
+def _batch_worker(rank, world, port, q):
+    import torch.distributed as dist
+
+    from wtb_gb300 import batch as B
+    from wtb_gb300 import synthetic as S
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+
+    def gather(local):
+        out = [None] * world
+        dist.all_gather_object(out, local)
+        return out
+
+    items = S.strained_batch(nsys=64)
+    cost = [B.system_cost(p, s.w90basis) for s, p in items]
+    mine = B.lpt_partition(cost, world)[rank]
+    res = solve_sharded(items, _lowest_transitions, rank, world, cost=lambda it: B.system_cost(it[1], it[0].w90basis),
+                        gather=gather)
+    q.put((rank, mine, [r.tolist() for r in res]))
+    dist.destroy_process_group()
+
+
+def test_strained_batch_sharded_over_two_gloo_ranks():
+    """The 64-system strained batch split over 2 ranks by the LPT partition of system_cost, each system solved by
+    the rank that owns it, the results gathered on every rank: equal to a 1-rank run, item for item."""
+    import torch.multiprocessing as mp
+
+    from wtb_gb300 import batch as B
+    from wtb_gb300 import synthetic as S
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_batch_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = {}
+    for _ in range(2):
+        r, mine, res = q.get(timeout=300)
+        out[r] = (mine, res)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    items = S.strained_batch(nsys=64)
+    ref = solve_sharded(items, _lowest_transitions, 0, 1)
+    assert out[0][1] == out[1][1]
+    assert len(out[0][1]) == len(items)
+    for got, want in zip(out[0][1], ref):
+        np.testing.assert_array_equal(np.array(got), want)
+    # the two ranks own disjoint halves of the batch whose costs differ by at most the largest system's
+    a, b = set(out[0][0]), set(out[1][0])
+    assert a.isdisjoint(b) and a | b == set(range(len(items)))
+    cost = [B.system_cost(p, s.w90basis) for s, p in items]
+    la, lb = sum(cost[i] for i in a), sum(cost[i] for i in b)
+    assert abs(la - lb) <= max(cost)
