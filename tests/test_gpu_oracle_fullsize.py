@@ -45,10 +45,14 @@ def test_energies_spectra_against_oracle(ctx, full, precision, op):
     ctx.set_hr(sysm)
     out = ctx.bsesolver(p, precision=precision, op=op)
     dE = np.abs(out["E"] - g["E"])
-    print(f"{name} {precision}/{op}: |dE| vs oracle (eV) = {np.array2string(dE, precision=2)}")
+    spec = ctx.bsedielraw(p, out["Ws"], out["acts"])
+    sl2 = {c: rel_l2(spec[c][:, 2], g["spec_" + c][:, 2]) for c in ("xx", "yy", "zz")}
+    t = out["timings"]
+    print(f"{name} {precision}/{op}: |dE| vs oracle (eV) = {np.array2string(dE, precision=2)}; spectrum rel L2 "
+          f"{ {c: f'{v:.2e}' for c, v in sl2.items()} }; iterations {t['iterations']}, residual "
+          f"{t['max_rel_residual']:.2e}")
     assert dE.shape == (p.nev,)
     assert np.all(dE <= 1e-5), (name, precision, op, dE)
-    spec = ctx.bsedielraw(p, out["Ws"], out["acts"])
     for c in ("xx", "yy", "zz"):
         np.testing.assert_array_equal(spec[c][:, 0], g["spec_" + c][:, 0])
         assert rel_l2(spec[c][:, 2], g["spec_" + c][:, 2]) <= 1e-4, (name, precision, op, c)
