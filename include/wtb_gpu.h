@@ -125,9 +125,38 @@ int wtb_eigsys_mesh(wtb_ctx* ctx, int nk, const double* kpt, int nv, int nc, dou
 int wtb_coulomb_table(wtb_ctx* ctx, const wtb_bse_params* p, int n1, const double* kpt1, int n2,
                       const double* kpt2, double* V);
 
+/* Replaces one call of a scalar potential of module_coulomb with its explicit lattice argument, e.g.
+ * real(8) function v2drk(kpt1,kpt2,ngrid,rlat,ediel,lc,ez,w,r0,tolr) (src/module_coulomb.F90:286) or
+ * v3diel(kpt1,kpt2,ediel,rlat,ngrid,tolr) (:98): v = V(kpt1, kpt2) for the potential p->coultype with the keys
+ * of p (ngrid, ktol = tolr, ediel, ez, w_coul, r0, lc) and rlat(3, 3) (rlat(i,:) = a_i).  Evaluated by the
+ * library's Coulomb kernel on the process-wide default context (device 0), like wtb_eigsys. */
+int wtb_coulomb_pair(const wtb_bse_params* p, const double* rlat, const double* kpt1, const double* kpt2, double* v);
+
 /* Replaces the optsp/hlm loop of bsesolver (src/module_bse.F90:2317-2348; src/module_optics.F90:12-167):
  * hr(dim, 5) = hrx, hry, hrz, hrsp, hrsm for the bands of the last wtb_eigsys_mesh/wtb_bsesolver call. */
 int wtb_optsp(wtb_ctx* ctx, const wtb_bse_params* p, double* hr);
+
+/* Replaces hlm(kx,ky,kz,ffactor,w90basis,nvec,rlat,rvec,hopmatrices,ihopmatrices,hx,hy,hz)
+ * (src/module_optics.F90:12-108) with its argument list: hx, hy, hz (w x w complex(8), column-major) =
+ * sum_R i R_a e^{ik.R} H(R)/ndegen at one k-point, phases and R_a rounded to single precision.  Stateless, on the
+ * process-wide default context (device 0), like wtb_eigsys. */
+int wtb_hlm(double kx, double ky, double kz, const int* ffactor, int w90basis, int nvec, const double* rlat,
+            const int* rvec, const double* hopmatrices, const double* ihopmatrices, double* hx, double* hy, double* hz);
+
+/* Replaces optsp(ev,vv,ec,vc,kx,ky,kz,ffactor,sme,w90basis,nvec,rlat,rvec,hopmatrices,ihopmatrices,hrx,hry,hrz)
+ * (src/module_optics.F90:113-167) with its argument list: for the valence and conduction vectors vv, vc (w
+ * complex(8)) with energies ev, ec, hr_a = <c|dH/dk_a|v> Re(1/(ec - ev + i sme)) (sme in single precision, the
+ * reference's 1./esp assigned to a real), each one complex(8).  Stateless, on the default context. */
+int wtb_optsp_pair(double ev, const double* vv, double ec, const double* vc, double kx, double ky, double kz,
+                   const int* ffactor, double sme, int w90basis, int nvec, const double* rlat, const int* rvec,
+                   const double* hopmatrices, const double* ihopmatrices, double* hrx, double* hry, double* hrz);
+
+/* Replaces optdiel(rtype,vc,dimse,ngrid,elux,exciton,fosc,sme,rpart,ipart) (src/module_optics.F90:171-255) with
+ * its argument list: the Lorentzian sums at one photon energy elux over the dimse energies exciton and strengths
+ * fosc, width sme + avgsme(exciton) (:313-335); rpart = delta + C sum f (E - elux)/eaux, ipart = C sum f smef/eaux,
+ * delta = 1 for rtype 1.  On the default context. */
+int wtb_optdiel(int rtype, double vc, int dimse, const int* ngrid, double elux, const double* exciton,
+                const double* fosc, double sme, double* rpart, double* ipart);
 
 /* Replaces the matrizelbse build loop and Hermitian mirror (src/module_bse.F90:24-83, :2392-2415):
  * builds the dense BSE Hamiltonian on the device in p->precision (FP64 or FP32) from the bands of the

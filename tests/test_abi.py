@@ -38,6 +38,13 @@ def test_host_only_entry_points(built):
     k = api.monhkhorst_pack(5, 4, 1, [0.1, 0.0, 0.0], rlat[0], rlat[1], rlat[2])
     ref = synthetic.monkhorst_pack((5, 4, 1), rlat, (0.1, 0.0, 0.0))
     np.testing.assert_allclose(k, ref, rtol=0, atol=1e-14)
+    # against the oracle's restatement of monhkhorst_pack/recvec (single-precision pi): bit for bit
+    from oracle import wtb_oracle as O
+
+    for ng, shift in (((5, 4, 1), (0.1, 0.0, 0.0)), ((60, 60, 1), (0.0, 0.0, 0.0)), ((16, 16, 16), (0.0, 0.0, 0.0)),
+                      ((7, 3, 2), (0.25, 0.5, 0.125))):
+        k = api.monhkhorst_pack(ng[0], ng[1], ng[2], list(shift), rlat[0], rlat[1], rlat[2])
+        np.testing.assert_array_equal(k, O.monhkhorst_pack(ng[0], ng[1], ng[2], shift, rlat))
 
 
 def test_kpathbse_host_entry_matches_oracle(built):

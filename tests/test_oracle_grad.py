@@ -57,3 +57,22 @@ def test_grad_oracle_r0_zero_for_other_potentials(coul):
     p.ediel = (1.0, 4.0, 1.0)
     _, _, dr0, _ = OG.backward(sysm, p, a, b)
     assert dr0 == 0.0
+
+
+def test_grad_oracle_pinned_by_finite_differences_at_dim_5184():
+    """The differentiation form at its own size (tests/golden/hex8_36x36_grad_oracle.npz): the gradient oracle's
+    gradients of the lowest 4 energies and of the spectrum loss against central differences (h = 1e-6) of the
+    oracle's forward on 24 seeded H(R) entries and r0, within 1e-4 relative (floor 1e-3 of the largest entry)."""
+    import os
+
+    import numpy as np
+
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "hex8_36x36_grad_oracle.npz"))
+    assert g["fd_entries"].shape == (24, 4) and float(g["fd_h"]) == 1e-6
+    for j, k in enumerate(["E0", "E1", "E2", "E3", "spec"]):
+        oh, oi = g["dhop_" + k], g["dihop_" + k]
+        scale = max(np.abs(oh).max(), np.abs(oi).max())
+        for i, (w, r, m, n) in enumerate(g["fd_entries"]):
+            v = (oh if w == 0 else oi)[r, m, n]
+            assert abs(v - g["fd"][i, j]) <= 1e-4 * max(abs(g["fd"][i, j]), 1e-3 * scale), (k, w, r, m, n)
+        assert abs(float(g["dr0_" + k]) - g["fd"][-1, j]) <= 1e-4 * abs(g["fd"][-1, j]), k

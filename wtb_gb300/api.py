@@ -128,6 +128,11 @@ def _load():
         "wtb_batch_matvec": [P, C.c_int, dp, dp],
         "wtb_batch_timings": [P, dp],
         "wtb_autotune_report": [C.c_char_p, C.c_int],
+        "wtb_coulomb_pair": [C.POINTER(CParams), dp, dp, dp, dp],
+        "wtb_hlm": [C.c_double, C.c_double, C.c_double, ip, C.c_int, C.c_int, dp, ip, dp, dp, dp, dp, dp],
+        "wtb_optsp_pair": [C.c_double, dp, C.c_double, dp, C.c_double, C.c_double, C.c_double, ip, C.c_double,
+                           C.c_int, C.c_int, dp, ip, dp, dp, dp, dp, dp],
+        "wtb_optdiel": [C.c_int, C.c_double, C.c_int, ip, C.c_double, dp, dp, C.c_double, dp, dp],
     }
     for name, args in sigs.items():
         f = getattr(lib, name)
@@ -320,6 +325,60 @@ def eigsys(nthreads, scs, exc, nocp, ffactor, kx, ky, kz, w90basis, nvec, rlat, 
     if r:
         raise WTBError(r, "eigsys failed")
     return n.value, en, av
+
+
+def coulomb_pair(p: BSEParams, rlat, kpt1, kpt2) -> float:
+    """One value of the potential p.coultype at (kpt1, kpt2) with the lattice rlat (rlat[i] = a_(i+1)), as the
+    scalar functions of module_coulomb return it (v2drk, v3diel, ...; src/module_coulomb.F90:11-442)."""
+    v = C.c_double()
+    cp = cparams(p)
+    r = _lib.wtb_coulomb_pair(C.byref(cp), _dp(_f64(rlat)), _dp(np.ascontiguousarray(kpt1, dtype=np.float64)),
+                              _dp(np.ascontiguousarray(kpt2, dtype=np.float64)), C.byref(v))
+    if r:
+        raise WTBError(r, "wtb_coulomb_pair failed")
+    return v.value
+
+
+def _hr_args(sysm):
+    return (_ip(np.asfortranarray(np.asarray(sysm.ffactor, dtype=np.int32))), int(sysm.w90basis), int(sysm.nvec),
+            _dp(_f64(sysm.rlat)), _ip(np.asfortranarray(np.asarray(sysm.rvec, dtype=np.int32))),
+            _dp(_f64(sysm.hop)), _dp(_f64(sysm.ihop)))
+
+
+def hlm(k, sysm):
+    """hlm (src/module_optics.F90:12-108) at one k-point: (hx, hy, hz), each (w, w) complex."""
+    w = sysm.w90basis
+    out = [np.zeros((w, w), dtype=np.complex128, order="F") for _ in range(3)]
+    ff, w_, nv_, rl, rv, hp, ih = _hr_args(sysm)
+    r = _lib.wtb_hlm(float(k[0]), float(k[1]), float(k[2]), ff, w_, nv_, rl, rv, hp, ih, *(_dp(o) for o in out))
+    if r:
+        raise WTBError(r, "wtb_hlm failed")
+    return tuple(out)
+
+
+def optsp_pair(ev, vv, ec, vc, k, sme, sysm):
+    """optsp (src/module_optics.F90:113-167) for one (valence, conduction) pair: (hrx, hry, hrz)."""
+    out = [np.zeros(1, dtype=np.complex128) for _ in range(3)]
+    ff, w_, nv_, rl, rv, hp, ih = _hr_args(sysm)
+    r = _lib.wtb_optsp_pair(float(ev), _dp(np.ascontiguousarray(vv, dtype=np.complex128)), float(ec),
+                            _dp(np.ascontiguousarray(vc, dtype=np.complex128)), float(k[0]), float(k[1]), float(k[2]),
+                            ff, float(sme), w_, nv_, rl, rv, hp, ih, *(_dp(o) for o in out))
+    if r:
+        raise WTBError(r, "wtb_optsp_pair failed")
+    return tuple(complex(o[0]) for o in out)
+
+
+def optdiel(rtype, vc, ngrid, elux, exciton, fosc, sme):
+    """optdiel (src/module_optics.F90:171-255) at one photon energy: (rpart, ipart)."""
+    E = np.ascontiguousarray(exciton, dtype=np.float64)
+    f = np.ascontiguousarray(fosc, dtype=np.float64)
+    g = np.ascontiguousarray(ngrid, dtype=np.int32)
+    rp, ipart = C.c_double(), C.c_double()
+    r = _lib.wtb_optdiel(int(rtype), float(vc), len(E), _ip(g), float(elux), _dp(E), _dp(f), float(sme), C.byref(rp),
+                         C.byref(ipart))
+    if r:
+        raise WTBError(r, "wtb_optdiel failed")
+    return rp.value, ipart.value
 
 
 class Context:

@@ -602,4 +602,123 @@ cudaError_t launch_transition_energies(const double* eig_win, int nk, int nv, in
   return cudaGetLastError();
 }
 
+// ----------------------------------------------------------------------------- hlm / optsp / optdiel, one call each
+// The scalar routines of module_optics for callers that keep their own loops.  hlm_kernel, one CTA: the three
+// velocity matrices dH/dk_a = sum_R i R_a e^{i phi_R} H(R)/ndegen at one k-point (hlm, src/module_optics.F90:12-108;
+// phases and R_a rounded to single precision as there; the R = 0 term vanishes with its factor R_a = 0), written
+// column-major w x w; or, given band vectors cv and vv (optsp, :113-167), the three elements
+// <c|dH/dk_a|v> Re(1/(E_c - E_v + i sme)) with sme in single precision (factor = 1./esp assigned to a real).
+__global__ void __launch_bounds__(kHkThreads) hlm_kernel(const zd* __restrict__ hr, const int* __restrict__ rvec,
+                                                         const int* __restrict__ ndegen, int nR, int w,
+                                                         const double* __restrict__ rlat, double kx, double ky,
+                                                         double kz, const zd* __restrict__ cv,
+                                                         const zd* __restrict__ vv, double ev, double ec, float s32,
+                                                         zd* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  zd* M = reinterpret_cast<zd*>(smem_raw);  // w*w
+  zd* eph = M + w * w;                      // nR: e^{i phi}/ndegen
+  zd* fr = eph + nR;                        // nR: i R_a e^{i phi}/ndegen
+  zd* rowv = fr + nR;                       // w: per-row sandwich terms
+  __shared__ double rl[9];
+  const int tid = threadIdx.x;
+  if (tid < 9) rl[tid] = rlat[tid];
+  __syncthreads();
+  for (int r = tid; r < nR; r += blockDim.x) {
+    const double phi = phase_f32(rvec, nR, r, rl, kx, ky, kz);
+    double sn, cs;
+    sincos(phi, &sn, &cs);
+    const double inv = 1.0 / (double)ndegen[r];
+    eph[r] = mk<double>(cs * inv, sn * inv);
+  }
+  for (int a = 0; a < 3; ++a) {
+    __syncthreads();
+    for (int r = tid; r < nR; r += blockDim.x) {
+      const double Ra = rcomp_f32(rvec, nR, r, rl, a);
+      fr[r] = mk<double>(-Ra * eph[r].im, Ra * eph[r].re);
+    }
+    __syncthreads();
+    for (int e = tid; e < w * w; e += blockDim.x) {
+      const int m = e / w, n = e % w;
+      zd acc = mk<double>(0.0, 0.0);
+      for (int r = 0; r < nR; ++r) cfma(acc, fr[r], hr[((size_t)r * w + m) * w + n]);
+      M[e] = acc;
+      if (!cv) out[(size_t)a * w * w + m + (size_t)w * n] = acc;
+    }
+    if (!cv) continue;
+    __syncthreads();
+    for (int m = tid; m < w; m += blockDim.x) {
+      zd mv = mk<double>(0.0, 0.0);
+      for (int n = 0; n < w; ++n) cfma(mv, M[m * w + n], vv[n]);
+      zd t = mk<double>(0.0, 0.0);
+      cfmac(t, cv[m], mv);
+      rowv[m] = t;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      zd sum = mk<double>(0.0, 0.0);
+      for (int m = 0; m < w; ++m) sum = mk<double>(sum.re + rowv[m].re, sum.im + rowv[m].im);
+      const double de = ec - ev, sf = (double)s32;
+      out[a] = cscale(sum, de / (de * de + sf * sf));
+    }
+  }
+}
+
+// optdiel (src/module_optics.F90:171-255) at one photon energy, one CTA: avgsme's telescoped spacing over the dimse
+// energies (:313-335), then the two Lorentzian sums, each summed per thread in row order and the 256 partials in
+// thread order.  out = (rpart, ipart).
+__global__ void __launch_bounds__(256) optdiel_kernel(int rtype, double caux, int dimse, double elux,
+                                                      const double* __restrict__ E, const double* __restrict__ f,
+                                                      double sme, double* __restrict__ out) {
+  __shared__ double red[3][256];
+  __shared__ double s_smef;
+  const int tid = threadIdx.x;
+  double acc = 0.0;
+  for (int i = 1 + tid; i < dimse; i += blockDim.x) acc += E[i] - E[i - 1];
+  red[0][tid] = acc;
+  __syncthreads();
+  if (tid == 0) {
+    double t = 0.0;
+    for (int i = 0; i < (int)blockDim.x; ++i) t += red[0][i];
+    s_smef = 10.0 * (t / (double)dimse) + sme;
+  }
+  __syncthreads();
+  const double smef = s_smef;
+  double rp = 0.0, ip = 0.0;
+  for (int i = tid; i < dimse; i += blockDim.x) {
+    const double eaux = ((elux - E[i]) * (elux - E[i])) + (smef * smef);
+    rp += f[i] * ((E[i] - elux) / eaux);
+    ip += f[i] * (smef / eaux);
+  }
+  red[1][tid] = rp;
+  red[2][tid] = ip;
+  __syncthreads();
+  if (tid == 0) {
+    double r = 0.0, im = 0.0;
+    for (int i = 0; i < (int)blockDim.x; ++i) {
+      r += red[1][i];
+      im += red[2][i];
+    }
+    out[0] = (rtype == 1 ? 1.0 : 0.0) + r * caux;
+    out[1] = im * caux;
+  }
+}
+
+cudaError_t launch_hlm(const zd* hr, const int* rvec, const int* ndegen, int nR, int w, const double* rlat_rm, double kx,
+                       double ky, double kz, const zd* cv, const zd* vv, double ev, double ec, double sme, zd* out,
+                       cudaStream_t s) {
+  const size_t smem = (size_t)(w * w + 2 * nR + w) * sizeof(zd);
+  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(hlm_kernel), smem);
+  if (e != cudaSuccess) return e;
+  hlm_kernel<<<1, kHkThreads, smem, s>>>(hr, rvec, ndegen, nR, w, rlat_rm, kx, ky, kz, cv, vv, ev, ec, (float)sme, out);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_optdiel(int rtype, double caux, int dimse, double elux, const double* E, const double* f, double sme,
+                           double* out, cudaStream_t s) {
+  optdiel_kernel<<<1, 256, 0, s>>>(rtype, caux, dimse, elux, E, f, sme, out);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
 }  // namespace wtb

@@ -707,6 +707,123 @@ int wtb_coulomb_table(wtb_ctx* c, const wtb_bse_params* p, int n1, const double*
   return check_status(c);
 }
 
+int wtb_coulomb_pair(const wtb_bse_params* p, const double* rlat, const double* kpt1, const double* kpt2, double* v) {
+  if (!p || !rlat || !kpt1 || !kpt2 || !v) return WTB_EBADARG;
+  std::lock_guard<std::mutex> lock(g_default_mu);
+  if (!g_default) {
+    int r = wtb_ctx_create(&g_default, 0);
+    if (r) return r;
+  }
+  wtb_ctx* c = g_default;
+  CKR(prep_device(c));
+  if (p->coultype < 0 || p->coultype > 8) return set_err(c, WTB_EBADARG, "Wrong Coulomb Potential");
+  // the lattice of this call (rlat(i,:) = a_i, column-major) rather than the context's
+  CoulParams cp = coul_of(c, p);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) cp.rlat[3 * i + j] = rlat[i + 3 * j];
+  cudaError_t err = cudaSuccess;
+  double* dk = c->ws.get<double>("cp_k", 6, &err);
+  double* dv = c->ws.get<double>("cp_v", 1, &err);
+  CKC(err);
+  const double k[6] = {kpt1[0], kpt1[1], kpt1[2], kpt2[0], kpt2[1], kpt2[2]};
+  CKC(cudaMemcpyAsync(dk, k, sizeof(k), cudaMemcpyHostToDevice, c->s));
+  CKC(launch_coulomb(cp, dk + 3, 1, dk, 1, dv, 1, c->s));
+  CKC(cudaMemcpyAsync(v, dv, sizeof(double), cudaMemcpyDeviceToHost, c->s));
+  CKC(cudaStreamSynchronize(c->s));
+  return check_status(c);
+}
+
+// hlm / optsp at one k-point on the default context: H(R) staged as wtb_eigsys stages it, then one hlm_kernel
+static int hlm_common(double kx, double ky, double kz, const int* ffactor, int w90basis, int nvec, const double* rlat,
+                      const int* rvec, const double* hop, const double* ihop, const double* cv, const double* vv,
+                      double ev, double ec, double sme, double* out, int nout) {
+  std::lock_guard<std::mutex> lock(g_default_mu);
+  if (!g_default) {
+    int r = wtb_ctx_create(&g_default, 0);
+    if (r) return r;
+  }
+  wtb_ctx* c = g_default;
+  CKR(wtb_set_hr(c, w90basis, nvec, rvec, ffactor, hop, ihop, rlat, 0.0, 0.0, 0));
+  const int w = w90basis;
+  cudaError_t err = cudaSuccess;
+  zd* dvec = c->ws.get<zd>("hlm_vec", (size_t)2 * w, &err);
+  zd* dout = c->ws.get<zd>("hlm_out", (size_t)nout, &err);
+  double* drl = c->ws.get<double>("hlm_rlat", 9, &err);
+  CKC(err);
+  double rl[9];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) rl[3 * i + j] = rlat[i + 3 * j];
+  CKC(cudaMemcpyAsync(drl, rl, sizeof(rl), cudaMemcpyHostToDevice, c->s));
+  if (cv) {
+    CKC(cudaMemcpyAsync(dvec, cv, sizeof(zd) * w, cudaMemcpyHostToDevice, c->s));
+    CKC(cudaMemcpyAsync(dvec + w, vv, sizeof(zd) * w, cudaMemcpyHostToDevice, c->s));
+  }
+  CKC(launch_hlm(c->ws.get<zd>("hr", 0, &err), c->ws.get<int>("rvec", 0, &err), c->ws.get<int>("ndegen", 0, &err), nvec, w,
+                 drl, kx, ky, kz, cv ? dvec : nullptr, cv ? dvec + w : nullptr, ev, ec, sme, dout, c->s));
+  CKC(cudaMemcpyAsync(out, dout, sizeof(zd) * nout, cudaMemcpyDeviceToHost, c->s));
+  CKC(cudaStreamSynchronize(c->s));
+  return check_status(c);
+}
+
+int wtb_hlm(double kx, double ky, double kz, const int* ffactor, int w90basis, int nvec, const double* rlat,
+            const int* rvec, const double* hop, const double* ihop, double* hx, double* hy, double* hz) {
+  if (!ffactor || !rlat || !rvec || !hop || !ihop || !hx || !hy || !hz || w90basis < 1 || w90basis > 64 || nvec < 1)
+    return WTB_EBADARG;
+  const int w = w90basis;
+  std::vector<double> out((size_t)6 * w * w);
+  CKR(hlm_common(kx, ky, kz, ffactor, w, nvec, rlat, rvec, hop, ihop, nullptr, nullptr, 0.0, 0.0, 0.0, out.data(),
+                 3 * w * w));
+  std::memcpy(hx, out.data(), sizeof(double) * 2 * w * w);
+  std::memcpy(hy, out.data() + 2 * w * w, sizeof(double) * 2 * w * w);
+  std::memcpy(hz, out.data() + 4 * w * w, sizeof(double) * 2 * w * w);
+  return WTB_OK;
+}
+
+int wtb_optsp_pair(double ev, const double* vv, double ec, const double* vc, double kx, double ky, double kz,
+                   const int* ffactor, double sme, int w90basis, int nvec, const double* rlat, const int* rvec,
+                   const double* hop, const double* ihop, double* hrx, double* hry, double* hrz) {
+  if (!vv || !vc || !ffactor || !rlat || !rvec || !hop || !ihop || !hrx || !hry || !hrz || w90basis < 1 ||
+      w90basis > 64 || nvec < 1)
+    return WTB_EBADARG;
+  double out[6];
+  CKR(hlm_common(kx, ky, kz, ffactor, w90basis, nvec, rlat, rvec, hop, ihop, vc, vv, ev, ec, sme, out, 3));
+  hrx[0] = out[0];
+  hrx[1] = out[1];
+  hry[0] = out[2];
+  hry[1] = out[3];
+  hrz[0] = out[4];
+  hrz[1] = out[5];
+  return WTB_OK;
+}
+
+int wtb_optdiel(int rtype, double vc, int dimse, const int* ngrid, double elux, const double* exciton,
+                const double* fosc, double sme, double* rpart, double* ipart) {
+  if (dimse < 1 || !ngrid || !exciton || !fosc || !rpart || !ipart) return WTB_EBADARG;
+  std::lock_guard<std::mutex> lock(g_default_mu);
+  if (!g_default) {
+    int r = wtb_ctx_create(&g_default, 0);
+    if (r) return r;
+  }
+  wtb_ctx* c = g_default;
+  CKR(prep_device(c));
+  cudaError_t err = cudaSuccess;
+  double* dE = c->ws.get<double>("od_E", dimse, &err);
+  double* df = c->ws.get<double>("od_f", dimse, &err);
+  double* dout = c->ws.get<double>("od_out", 2, &err);
+  CKC(err);
+  CKC(cudaMemcpyAsync(dE, exciton, sizeof(double) * dimse, cudaMemcpyHostToDevice, c->s));
+  CKC(cudaMemcpyAsync(df, fosc, sizeof(double) * dimse, cudaMemcpyHostToDevice, c->s));
+  // caux = gama/(real(ngrid(1)*ngrid(2)*ngrid(3))*vc), gama the single-precision literal 180.90
+  const double baux = (double)(float)(ngrid[0] * ngrid[1] * ngrid[2]) * vc;
+  CKC(launch_optdiel(rtype, (double)180.90f / (baux * 1.0), dimse, elux, dE, df, sme, dout, c->s));
+  double o[2];
+  CKC(cudaMemcpyAsync(o, dout, sizeof(o), cudaMemcpyDeviceToHost, c->s));
+  CKC(cudaStreamSynchronize(c->s));
+  *rpart = o[0];
+  *ipart = o[1];
+  return check_status(c);
+}
+
 // the Monkhorst-Pack mesh of p staged for the band computation
 static int stage_mesh(wtb_ctx* c, const wtb_bse_params* p) {
   const int nk = p->ngrid[0] * p->ngrid[1] * p->ngrid[2];

@@ -118,6 +118,13 @@ cudaError_t launch_coulomb_mesh(const CoulParams& p, const double* bl, double* s
                                 cudaStream_t s);
 // Transition energies dE[I] = E_c - E_v.
 cudaError_t launch_transition_energies(const double* eig_win, int nk, int nv, int nc, double* dE, cudaStream_t s);
+// hlm at one k-point (out: 3 column-major w x w matrices), or with band vectors cv, vv the optsp elements (out: 3)
+cudaError_t launch_hlm(const zd* hr, const int* rvec, const int* ndegen, int nR, int w, const double* rlat_rm, double kx,
+                       double ky, double kz, const zd* cv, const zd* vv, double ev, double ec, double sme, zd* out,
+                       cudaStream_t s);
+// optdiel at one photon energy: out = (rpart, ipart); caux = 180.90 / (real(ngrid product) * vc)
+cudaError_t launch_optdiel(int rtype, double caux, int dimse, double elux, const double* E, const double* f, double sme,
+                           double* out, cudaStream_t s);
 
 // Dense build: H[I][J] (row-major, ld = dim) = delta_IJ dE_I + V(k_I,k_J) <c_I|c_J> <v_I|v_J>.
 template <class S>
