@@ -351,7 +351,9 @@ int wtb_bseoptproppol(wtb_ctx* ctx, int numbse, const double* dielf, double* pro
  * partial sums live in one fixed 2 MiB device array per GPU (held until the process exits), so
  * ceil(dimse/1024) * dimse1 * 4 must not exceed 262144; larger calls return WTB_EBADARG (reason on stderr).
  * All calls share that array: calls that overlap on the GPU race and must be ordered.  The first call on
- * a device looks up the array's address; make it before any stream capture. */
+ * a device looks up the array's address; make it before any stream capture.  That address belongs to the
+ * device's primary context (the CUDA runtime's): call it with the primary context current, and do not reset
+ * the device (cudaDeviceReset) after the first call. */
 int wtb_dielbse_noalloc(int dimse, int dimse1, const double* excitonvec, const double* hopt1,
                         const double* hopt2, int pair, double* activity, void* stream);
 

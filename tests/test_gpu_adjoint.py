@@ -3,7 +3,7 @@ pinned to finite differences of the forward oracle (tests/test_oracle_grad.py), 
 differences of the library's own FP64 forward.
 
 Tolerances: FP64 gradients 1e-6 of the largest |dL/dhop| entry (the adjoint solve stops at 1e-10 relative
-residual, the forward eigensolve at 1e-8); mixed-precision gradients 2e-3 relative in the Frobenius norm;
+residual, the forward eigensolve at 1e-8); mixed-precision gradients 1e-4 relative in the Frobenius norm;
 spectrum loss 1e-10 relative, its cotangents 1e-5 relative to central differences."""
 import copy
 
@@ -103,8 +103,10 @@ def test_backward_mixed_precision_against_fp64(ctx, c1_grad, prec):
     g = ctx.bse_backward(p, a, b, precision=prec)
     for key in ("dhop", "dihop"):
         err = np.linalg.norm(g[key] - g64[key]) / np.linalg.norm(g64[key])
-        assert err <= 2e-3, (prec, key, err)
-    assert abs(g["dr0"] - g64["dr0"]) <= 2e-3 * abs(g64["dr0"])
+        print(f"{prec} {key}: relative Frobenius error against FP64 {err:.2e}")
+        assert err <= 1e-4, (prec, key, err)
+    print(f"{prec} dr0: relative error against FP64 {abs(g['dr0'] - g64['dr0']) / abs(g64['dr0']):.2e}")
+    assert abs(g["dr0"] - g64["dr0"]) <= 1e-4 * abs(g64["dr0"])
 
 
 def test_spectrum_loss_and_chain_rule(ctx, small_grad):

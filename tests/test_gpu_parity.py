@@ -344,3 +344,40 @@ def test_spoptpolbz(ctx, small):
     ref = O.spoptpolbz(sysm, p)
     np.testing.assert_allclose(act, ref, rtol=1e-9, atol=1e-12 * np.abs(ref[:, :5]).max())
     np.testing.assert_allclose(act[:, 3] + act[:, 4], 2 * O.INV_SQRT2_F32 ** 2 * (act[:, 0] + act[:, 1]), rtol=1e-12)
+
+
+def test_scalar_routines_with_reference_argument_lists(built, small):
+    """hlm, optsp, optdiel and the scalar potentials, one call each through their stateless entries
+    (wtb_hlm, wtb_optsp_pair, wtb_optdiel, wtb_coulomb_pair), against the oracle: 1e-12 relative."""
+    from wtb_gb300 import api
+
+    sysm, p, ref = small
+    kpt, eigv, vec = ref["kpt"], ref["eigv"], ref["vec"]
+    for k in (0, 5, 17):
+        got = api.hlm(kpt[k], sysm)
+        want = O.hlm(kpt[k], sysm)
+        for a in range(3):
+            np.testing.assert_allclose(got[a], want[a], rtol=0, atol=1e-12 * max(1.0, np.abs(want[a]).max()))
+    s32 = float(np.float32(p.cshift))
+    for k, c, v in ((3, 0, 0), (11, 1, 0), (20, 1, 1)):
+        ev, ec, vv, vc = eigv[k, v], eigv[k, p.nv + c], vec[k, v], vec[k, p.nv + c]
+        got = api.optsp_pair(ev, vv, ec, vc, kpt[k], p.cshift, sysm)
+        hs = O.hlm(kpt[k], sysm)
+        factor = (1.0 / ((ec - ev) + 1j * s32)).real
+        for a in range(3):
+            want = factor * (np.conj(vc) @ (hs[a] @ vv))
+            assert abs(got[a] - want) <= 1e-12 * max(1.0, abs(want)), (k, c, v, a, got[a], want)
+    vc3 = O.vcell3D(sysm.rlat)
+    E, f = ref["Ws"], ref["acts"]["xx"]
+    for rtype in (0, 1):
+        for elux in (0.7, 2.31, 4.9):
+            rp, ip = api.optdiel(rtype, vc3, p.ngrid, elux, E, f, p.cshift)
+            wr, wi = O.optdiel_grid(rtype, vc3, p.ngrid, np.array([elux]), E, f, p.cshift)
+            assert abs(rp - wr[0]) <= 1e-12 * max(1.0, abs(wr[0])) and abs(ip - wi[0]) <= 1e-12 * max(1.0, abs(wi[0]))
+    for coul, ediel in (("V2DRK", (1.0, 1.0, 1.0)), ("V3DL", (1.0, 8.0, 1.0)), ("V2DK", (1.0, 3.0, 2.0))):
+        q = S.BSEParams(**{**p.__dict__})
+        q.coultype, q.ediel = coul, ediel
+        for i, j in ((0, 7), (3, 3), (12, 30)):
+            got = api.coulomb_pair(q, sysm.rlat, kpt[i], kpt[j])
+            want = O.coulomb_table(kpt[i:i + 1], kpt[j:j + 1], q, sysm.rlat)[0, 0]
+            assert abs(got - want) <= 1e-12 * max(1e-300, abs(want)), (coul, i, j, got, want)

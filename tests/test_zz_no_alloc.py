@@ -36,8 +36,9 @@ def test_noalloc_matches_dielbse_on_consecutive_calls(built):
     f = _entry()
     ctx = api.Context(0)
     rng = np.random.default_rng(21)
-    dimse, dimse1 = 3100, 12
-    for pair in (1, 0):  # the second call must not see the first call's partial sums
+    # the second call changes the geometry (partial-sum blocks per row and rows), so a final kernel that read
+    # slots the current call did not write would see the first call's stale sums
+    for dimse, dimse1, pair in ((3100, 12, 1), (1500, 20, 0)):
         A = rng.normal(size=(dimse, dimse1)) + 1j * rng.normal(size=(dimse, dimse1))
         h1 = rng.normal(size=dimse) + 1j * rng.normal(size=dimse)
         h2 = rng.normal(size=dimse) + 1j * rng.normal(size=dimse)
@@ -45,10 +46,17 @@ def test_noalloc_matches_dielbse_on_consecutive_calls(built):
         dA, d1, d2 = _device_complex(torch, A), _device_complex(torch, h1), _device_complex(torch, h2)
         out = torch.full((dimse,), 7.0, dtype=torch.float64, device="cuda")
         torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        launches0 = api.kernel_launch_count()
         rc = f(dimse, dimse1, dA.data_ptr(), d1.data_ptr(), d2.data_ptr() if pair else None, pair, out.data_ptr(),
                None)
         torch.cuda.synchronize()
         assert rc == api.WTB_OK
+        # the call allocates nothing on the device (its first call may load the module, hence from the second
+        # call on) and launches its two kernels
+        if pair == 0:
+            assert torch.cuda.mem_get_info()[0] == free0
+        assert api.kernel_launch_count() - launches0 == 2
         np.testing.assert_allclose(out.cpu().numpy(), ref, rtol=1e-12, atol=1e-14)
     ctx.close()
 

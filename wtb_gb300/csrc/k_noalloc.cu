@@ -93,7 +93,9 @@ extern "C" int wtb_dielbse_noalloc(int dimse, int dimse1, const double* excitonv
                                    const double* hopt2, int pair, double* activity, void* stream) {
   if (dimse < 1 || dimse1 < 0 || dimse1 > dimse || !excitonvec || !hopt1 || (pair && !hopt2) || !activity)
     return fail(WTB_EBADARG, "wtb_dielbse_noalloc: bad arguments");
-  const long nblk = (dimse + WTB_NOALLOC_ROWS_PER_BLOCK - 1) / WTB_NOALLOC_ROWS_PER_BLOCK;
+  // sizes in long before any arithmetic, so no dimse up to INT_MAX can wrap
+  const long nblk = ((long)dimse + WTB_NOALLOC_ROWS_PER_BLOCK - 1) / WTB_NOALLOC_ROWS_PER_BLOCK;
+  const long final_grid = ((long)dimse + 255) / 256;
   if (nblk * (long)dimse1 * 4 > WTB_NOALLOC_SCRATCH_DOUBLES)
     return fail(WTB_EBADARG, "wtb_dielbse_noalloc: ceil(dimse/1024) * dimse1 * 4 = " +
                                  std::to_string(nblk * (long)dimse1 * 4) + " exceeds the fixed scratch of " +
@@ -123,7 +125,8 @@ extern "C" int wtb_dielbse_noalloc(int dimse, int dimse1, const double* excitonv
     dielbse_partial_kernel<<<dim3((unsigned)nblk, (unsigned)dimse1), 256, 0, s>>>(A, dimse, h1, h2, pair, (int)nblk,
                                                                                   scratch); ++g_launch_count;
   }
-  dielbse_final_kernel<<<(dimse + 255) / 256, 256, 0, s>>>(scratch, (int)nblk, dimse, dimse1, pair, activity); ++g_launch_count;
+  dielbse_final_kernel<<<(unsigned)final_grid, 256, 0, s>>>(scratch, (int)nblk, dimse, dimse1, pair, activity);
+  ++g_launch_count;
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(WTB_ECUDA, std::string("wtb_dielbse_noalloc: ") + cudaGetErrorString(e));
   return WTB_OK;
