@@ -72,15 +72,129 @@ __global__ void __launch_bounds__(256) gram_partial_kernel(const cplx<S>* __rest
     }
 }
 
+// M = A^H A and G = A^H B in one pass over the rows (the Gram pair of the Rayleigh-Ritz step): every staged row of
+// A feeds both products, so A is read once, and a thread's 3 x 3 entries of both matrices take 9 shared-memory
+// loads per row for 72 multiply-adds.  Rows are staged 32 (FP32) or 8 (FP64) at a time, two stages deep, by
+// cp.async (one copy per element, so any leading dimension works): the loads of the next stage are in flight while
+// the current one is multiplied.  Each thread adds the rows in the order of gram_partial_kernel, so the sums are
+// bitwise the same as two separate launches.  One CTA per reduction part; partials [part][p][p] of M, then of G at
+// partial + npart p p 2.
+template <int BYTES>
+__device__ __forceinline__ void cp_async_elem(void* dst, const void* src) {
+  static_assert(BYTES == 8 || BYTES == 16, "cp.async copies 4, 8 or 16 bytes");
+  if constexpr (BYTES == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+  else
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+
+template <class S, int TI>
+__global__ void __launch_bounds__(256) gram_pair_partial_kernel(const cplx<S>* __restrict__ A,
+                                                                const cplx<S>* __restrict__ B, int ld, int p,
+                                                                int nrow, double* __restrict__ partial,
+                                                                int rows_per_part, int npart, BatchMap bm) {
+  constexpr int W = 16 * TI;
+  // rows per stage: both stages of both operands within 48 KB of static shared memory
+  constexpr int kPairRows = sizeof(S) == 4 ? 32 : 8;
+  __shared__ cplx<S> As[2][kPairRows][W];
+  __shared__ cplx<S> Bs[2][kPairRows][W];
+  const int tid = threadIdx.x, tx = tid % kGramTile, ty = tid / kGramTile;
+  long r_begin, r_end;
+  const int sys = bm_part(bm, blockIdx.x, nrow, rows_per_part, &r_begin, &r_end);
+  if (bm_frozen(bm, sys)) return;
+  // columns p .. W - 1 are never copied: zero them in both stages once
+  for (int e = tid; e < 2 * kPairRows * W; e += 256) {
+    if (e % W >= p) {
+      (&As[0][0][0])[e] = mk<S>(0, 0);
+      (&Bs[0][0][0])[e] = mk<S>(0, 0);
+    }
+  }
+  const int rr0 = tid / p, c0 = tid - rr0 * p, drr = 256 / p, dc = 256 - drr * p;  // stride 256 in (row, column)
+  auto stage = [&](int buf, long r0) {
+    const int nr = (int)min((long)kPairRows, r_end - r0);
+    int rr = rr0, c = c0;
+    for (int e = tid; e < nr * p; e += 256) {
+      cp_async_elem<sizeof(cplx<S>)>(&As[buf][rr][c], A + (r0 + rr) * ld + c);
+      cp_async_elem<sizeof(cplx<S>)>(&Bs[buf][rr][c], B + (r0 + rr) * ld + c);
+      rr += drr;
+      c += dc;
+      if (c >= p) {
+        c -= p;
+        ++rr;
+      }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  cplx<S> am[TI][TI], ag[TI][TI];
+#pragma unroll
+  for (int i = 0; i < TI; ++i)
+#pragma unroll
+    for (int j = 0; j < TI; ++j) am[i][j] = ag[i][j] = mk<S>(0, 0);
+  const long nst = (r_end - r_begin + kPairRows - 1) / kPairRows;
+  if (nst > 0) stage(0, r_begin);
+  for (long t = 0; t < nst; ++t) {
+    const int buf = (int)(t & 1);
+    if (t + 1 < nst) {
+      stage(buf ^ 1, r_begin + (t + 1) * kPairRows);
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    }
+    __syncthreads();
+    const int nr = (int)min((long)kPairRows, r_end - (r_begin + t * kPairRows));
+    for (int rr = 0; rr < nr; ++rr) {
+      cplx<S> a[TI], b[TI], c[TI];
+#pragma unroll
+      for (int i = 0; i < TI; ++i) a[i] = As[buf][rr][ty + kGramTile * i];
+#pragma unroll
+      for (int j = 0; j < TI; ++j) {
+        b[j] = As[buf][rr][tx + kGramTile * j];
+        c[j] = Bs[buf][rr][tx + kGramTile * j];
+      }
+#pragma unroll
+      for (int i = 0; i < TI; ++i)
+#pragma unroll
+        for (int j = 0; j < TI; ++j) {
+          cfmac(am[i][j], a[i], b[j]);
+          cfmac(ag[i][j], a[i], c[j]);
+        }
+    }
+    __syncthreads();  // the next stage's copies overwrite this buffer
+  }
+  const size_t n = (size_t)p * p * 2;
+  double* om = partial + (size_t)blockIdx.x * n;
+  double* og = partial + ((size_t)npart + blockIdx.x) * n;
+#pragma unroll
+  for (int i = 0; i < TI; ++i)
+#pragma unroll
+    for (int j = 0; j < TI; ++j) {
+      const int ii = ty + kGramTile * i, jj = tx + kGramTile * j;
+      if (ii < p && jj < p) {
+        om[2 * (ii * p + jj)] = (double)am[i][j].re;
+        om[2 * (ii * p + jj) + 1] = (double)am[i][j].im;
+        og[2 * (ii * p + jj)] = (double)ag[i][j].re;
+        og[2 * (ii * p + jj) + 1] = (double)ag[i][j].im;
+      }
+    }
+}
+
 // out[e] = sum over b of partial[b][e] over the parts of system blockIdx.y (out at a stride of out_stride per
 // system): a CTA owns 32 consecutive e; its 8 warps take every 8th part (lane = e, so reads coalesce), then the
 // 8 warp sums are added in a fixed order.
+// With out2: blockIdx.z = 1 sums the second set of partials (npart parts further on) into out2.
 __global__ void __launch_bounds__(256) sum_partials_kernel(const double* __restrict__ partial, int npart, int n,
-                                                           double* __restrict__ out, BatchMap bm, long out_stride) {
+                                                           double* __restrict__ out, BatchMap bm, long out_stride,
+                                                           double* __restrict__ out2 = nullptr) {
   __shared__ double red[8][33];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int e = blockIdx.x * 32 + lane;
   const int sys = blockIdx.y;
+  if (blockIdx.z == 1) {
+    partial += (size_t)npart * n;
+    out = out2;
+  }
   if (bm_frozen(bm, sys)) return;
   int b0 = 0, nbp = npart;
   if (bm.sys_parts) {
@@ -89,8 +203,11 @@ __global__ void __launch_bounds__(256) sum_partials_kernel(const double* __restr
   }
   out += (size_t)sys * out_stride;
   double s = 0.0;
-  if (e < n)
+  // unrolled so the loads of eight parts are in flight together; the additions keep the part order
+  if (e < n) {
+#pragma unroll 8
     for (int b = warp; b < nbp; b += 8) s += partial[(size_t)(b0 + b) * n + e];
+  }
   red[warp][lane] = s;
   __syncthreads();
   if (warp == 0 && e < n) {
@@ -567,6 +684,27 @@ cudaError_t launch_gram(const cplx<S>* A, int lda, int p, const cplx<S>* B, int 
 }
 
 template <class S>
+cudaError_t launch_gram_pair(const cplx<S>* A, const cplx<S>* B, int ld, int p, int nrow, zd* outM, zd* outG,
+                             double* partial, int npart, cudaStream_t s, const BatchMap& bm, long out_stride) {
+  if (p > 48) return cudaErrorInvalidValue;
+  if (bm.parts) npart = bm.nparts;
+  const int rpp = (nrow + npart - 1) / npart;
+  switch ((p + 15) / 16) {
+    case 1: gram_pair_partial_kernel<S, 1><<<npart, 256, 0, s>>>(A, B, ld, p, nrow, partial, rpp, npart, bm); break;
+    case 2: gram_pair_partial_kernel<S, 2><<<npart, 256, 0, s>>>(A, B, ld, p, nrow, partial, rpp, npart, bm); break;
+    default: gram_pair_partial_kernel<S, 3><<<npart, 256, 0, s>>>(A, B, ld, p, nrow, partial, rpp, npart, bm); break;
+  }
+  ++g_launch_count;
+  const int n = p * p * 2;
+  // both sets in one launch (the G partials keep the part numbering, npart parts further on)
+  sum_partials_kernel<<<dim3((n + 31) / 32, bm.nsys, 2), 256, 0, s>>>(partial, npart, n,
+                                                                       reinterpret_cast<double*>(outM), bm,
+                                                                       2 * out_stride, reinterpret_cast<double*>(outG));
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+template <class S>
 cudaError_t launch_update(const cplx<S>* Sx, int lds, int nin, const zd* C, int ldc, int nout, int nrow,
                           cplx<S>* Out, int ldo, double alpha, double beta, cudaStream_t s, const BatchMap& bm,
                           long c_stride) {
@@ -709,6 +847,8 @@ cudaError_t launch_init_guess(cplx<S>* X, int ldx, int nrow, int m, const int* i
 #define WTB_INST_BLAS(S)                                                                                          \
   template cudaError_t launch_gram<S>(const cplx<S>*, int, int, const cplx<S>*, int, int, int, zd*, double*, int,  \
                                       cudaStream_t, const BatchMap&, long);                                       \
+  template cudaError_t launch_gram_pair<S>(const cplx<S>*, const cplx<S>*, int, int, int, zd*, zd*, double*, int,    \
+                                           cudaStream_t, const BatchMap&, long);                                   \
   template cudaError_t launch_update<S>(const cplx<S>*, int, int, const zd*, int, int, int, cplx<S>*, int, double, \
                                         double, cudaStream_t, const BatchMap&, long);                             \
   template cudaError_t launch_residual<S>(const cplx<S>*, int, const cplx<S>*, int, const double*, int, int,       \

@@ -234,8 +234,13 @@ int rayleigh_ritz(const cplx<S>* Sb, const cplx<S>* ASb, int ld, int nb, int m, 
                   double* partial, int npart, DevStatus* st, cudaStream_t s, std::string* msg, bool small_in_fp64,
                   const BatchMap& bm, long nn, long ts) {
   (void)st;
-  CK(launch_gram<S>(Sb, ld, nb, Sb, ld, nb, nrow, sm.M, partial, npart, s, bm, nn));
-  CK(launch_gram<S>(Sb, ld, nb, ASb, ld, nb, nrow, sm.G, partial, npart, s, bm, nn));
+  if (nb <= 48) {
+    // both Grams in one pass over the basis (bitwise the same sums as two separate launches)
+    CK(launch_gram_pair<S>(Sb, ASb, ld, nb, nrow, sm.M, sm.G, partial, npart, s, bm, nn));
+  } else {
+    CK(launch_gram<S>(Sb, ld, nb, Sb, ld, nb, nrow, sm.M, partial, npart, s, bm, nn));
+    CK(launch_gram<S>(Sb, ld, nb, ASb, ld, nb, nrow, sm.G, partial, npart, s, bm, nn));
+  }
   if (small_in_fp64)
     CK(launch_pchol_basis<double>(sm.M, nb, nb, tau, sm.B, nb, sm.keep, s, bm, nn, nn));
   else
@@ -563,7 +568,7 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
   sm.dinv = nullptr;
   sm.theta = ws.get<double>("lob_theta", (size_t)nsys * nb, &err);
   sm.keep = ws.get<int>("lob_keep", nsys, &err);
-  double* partial = ws.get<double>("lob_partial", (size_t)npart * nn * 2, &err);
+  double* partial = ws.get<double>("lob_partial", (size_t)npart * nn * 4, &err);  // the Gram pair's two sets
   double* norms2 = ws.get<double>("lob_norms2", (size_t)nsys * 32, &err);
   int* active = ws.get<int>("lob_active", (size_t)nsys * 32, &err);
   int* idx = ws.get<int>("lob_idx", ragged ? (size_t)nsys * m : 65 * 128, &err);

@@ -179,6 +179,11 @@ template <class S>
 cudaError_t launch_gram(const cplx<S>* A, int lda, int p, const cplx<S>* B, int ldb, int q, int nrow,
                         zd* out, double* partial, int npart, cudaStream_t s, const BatchMap& bm = BatchMap(),
                         long out_stride = 0);
+// outM = A^H A and outG = A^H B in one pass over the rows (p <= 48 columns); partial holds 2 * npart p p doubles
+template <class S>
+cudaError_t launch_gram_pair(const cplx<S>* A, const cplx<S>* B, int ld, int p, int nrow, zd* outM, zd* outG,
+                             double* partial, int npart, cudaStream_t s, const BatchMap& bm = BatchMap(),
+                             long out_stride = 0);
 template <class S>
 cudaError_t launch_update(const cplx<S>* Sx, int lds, int nin, const zd* C, int ldc, int nout, int nrow,
                           cplx<S>* Out, int ldo, double alpha, double beta, cudaStream_t s,
