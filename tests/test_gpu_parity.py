@@ -381,3 +381,34 @@ def test_scalar_routines_with_reference_argument_lists(built, small):
             got = api.coulomb_pair(q, sysm.rlat, kpt[i], kpt[j])
             want = O.coulomb_table(kpt[i:i + 1], kpt[j:j + 1], q, sysm.rlat)[0, 0]
             assert abs(got - want) <= 1e-12 * max(1e-300, abs(want)), (coul, i, j, got, want)
+
+
+@pytest.mark.parametrize("precision,nev", [("fp64", 100), ("bf16x3", 40), ("fp32", 100)])
+def test_more_excitons_than_one_block(ctx, c1, precision, nev):
+    """nev beyond one eigensolver block (the reference's bsesolver asks 100, src/module_bse.F90:2432): chunks of 16
+    eigenpairs with deflation; every energy within 1e-5 eV of the oracle's dense solve, the spectrum within 1e-4."""
+    sysm, p, _ = c1
+    q = S.BSEParams(**{**p.__dict__})
+    q.nev = nev
+    ref = O.bsesolver(sysm, q)
+    ctx.set_hr(sysm)
+    out = ctx.bsesolver(q, precision=precision, op="matfree")
+    err = np.abs(out["E"] - ref["E"])
+    assert err.max() <= 1e-5, (precision, nev, err.max(), int(np.argmax(err)))
+    assert np.all(np.diff(out["E"]) >= 0)
+    spec = O.bsedielraw(out["Ws"], out["acts"], q.ngrid, sysm.rlat, q)
+    spec_ref = O.bsedielraw(ref["Ws"], ref["acts"], q.ngrid, sysm.rlat, q)
+    for c in ("xx", "yy", "zz"):
+        assert rel_l2(spec[c][:, 2], spec_ref[c][:, 2]) <= 1e-4, c
+
+
+def test_slepc_solver_with_the_reference_ne(ctx, c1):
+    """slepc_solver(HX, EX, HE, NX, NE) with the reference's NE = 100: the lowest 100 eigenpairs of the dense matrix,
+    eigenvalues within 1e-9 eV of LAPACK's, every residual ||HX x - e x|| / |e| within 1e-8 (SLEPc's tolerance)."""
+    sysm, p, ref = c1
+    H = O.bse_build(ref["eigv"], ref["vec"], ref["kpt"], p, sysm.rlat)
+    EX, HE = ctx.slepc_solver(H, 100)
+    w = np.linalg.eigvalsh(H)[:100]
+    np.testing.assert_allclose(EX, w, rtol=0, atol=1e-9)
+    res = np.linalg.norm(H @ HE - HE * EX[None, :], axis=0) / np.abs(EX)
+    assert res.max() <= 1e-8, res.max()

@@ -14,6 +14,7 @@
 // residual norms.  It replaces slepc_solver (src/module_slepc_solver.F90:12-97: Krylov-Schur,
 // EPS_SMALLEST_MAGNITUDE, tol 1e-8, 200 iterations); for the positive BSE spectra of this path the
 // smallest-magnitude and smallest-algebraic eigenvalues coincide.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -965,6 +966,145 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
   if (stats && !sv.empty()) *stats = sv[0];
   return rc;
 }
+
+namespace {
+
+// P H P + sigma Q Q^H with P = I - Q Q^H (Q orthonormal, dim x nq): span(Q) is an exactly invariant subspace with
+// eigenvalue sigma, so the eigenpairs still sought are those of H in the complement, up to the residuals of the
+// vectors in Q themselves (a shift alone, H + sigma Q Q^H, would perturb them by sigma times the error of Q).
+// Applied to a block: T1 = Q^H X, Xp = X - Q T1, Y = H Xp, T2 = Q^H Y, Y += Q (sigma T1 - T2); Q in blocks of at
+// most 96 columns, the Gram kernel's limit.
+template <class S>
+struct DeflatedOperator : Operator<S> {
+  Operator<S>* base = nullptr;
+  const cplx<S>* Q = nullptr;
+  int ldq = 0, nq = 0, dim = 0, npart = 1;
+  double sigma = 0.0;
+  zd* T1 = nullptr;  // [96][ncol] per Q block, blocks side by side
+  zd* T2 = nullptr;
+  cplx<S>* Xp = nullptr;  // dim x ncol
+  double* partial = nullptr;
+  cudaError_t apply(const cplx<S>* X, int ldx, int c0, int ncol, cplx<S>* Y, int ldy, cudaStream_t s) override {
+    base->capturing = this->capturing;
+    this->matvec_columns += ncol;
+    if (nq == 0) return base->apply(X, ldx, c0, ncol, Y, ldy, s);
+    cudaError_t e = launch_copy_cols<S>(X + c0, ldx, Xp, ncol, ncol, dim, s);
+    for (int q0 = 0; q0 < nq && e == cudaSuccess; q0 += 96) {
+      const int qn = std::min(96, nq - q0);
+      zd* t1 = T1 + (size_t)q0 * ncol;
+      e = launch_gram<S>(Q + q0, ldq, qn, X + c0, ldx, ncol, dim, t1, partial, npart, s);
+      if (e == cudaSuccess) e = launch_update<S>(Q + q0, ldq, qn, t1, ncol, ncol, dim, Xp, ncol, -1.0, 1.0, s);
+    }
+    if (e == cudaSuccess) e = base->apply(Xp, ncol, 0, ncol, Y + c0, ldy, s);
+    for (int q0 = 0; q0 < nq && e == cudaSuccess; q0 += 96) {
+      const int qn = std::min(96, nq - q0);
+      zd* t1 = T1 + (size_t)q0 * ncol;
+      zd* t2 = T2 + (size_t)q0 * ncol;
+      e = launch_gram<S>(Q + q0, ldq, qn, Y + c0, ldy, ncol, dim, t2, partial, npart, s);
+      if (e == cudaSuccess) e = launch_update<S>(Q + q0, ldq, qn, t2, ncol, ncol, dim, Y + c0, ldy, -1.0, 1.0, s);
+      if (e == cudaSuccess) e = launch_update<S>(Q + q0, ldq, qn, t1, ncol, ncol, dim, Y + c0, ldy, sigma, 1.0, s);
+    }
+    return e;
+  }
+  bool begin_refine() override { return base->begin_refine(); }
+  void set_final(bool on) override { base->set_final(on); }
+  void signature(std::vector<uint64_t>* sig) const override {
+    base->signature(sig);
+    uint64_t sb;
+    std::memcpy(&sb, &sigma, 8);
+    for (uint64_t v : {(uint64_t)7, (uint64_t)(uintptr_t)Q, (uint64_t)ldq, (uint64_t)nq, sb, (uint64_t)(uintptr_t)T1,
+                       (uint64_t)(uintptr_t)T2, (uint64_t)(uintptr_t)Xp, (uint64_t)(uintptr_t)partial,
+                       (uint64_t)npart})
+      sig->push_back(v);
+  }
+};
+
+}  // namespace
+
+template <class S>
+int lobpcg_solve_deflated(Operator<S>& op, const double* diag, int dim, int nev, int chunk, int m, double tol,
+                          int maxit, double sigma, Workspace& ws, DevStatus* st, cudaStream_t s, std::vector<double>* E,
+                          zd* Xout, SolveStats* stats, std::string* msg, double tol_refine) {
+  if (nev < 1 || nev > dim || chunk < 1 || m < chunk) {
+    if (msg) *msg = "bad deflated-solve sizes";
+    return WTB_EBADARG;
+  }
+  cudaError_t err = cudaSuccess;
+  const int npart = std::max(1, std::min(304, (dim + 191) / 192));
+  cplx<S>* Q = ws.get<cplx<S>>("defl_Q", (size_t)dim * nev, &err);
+  zd* Xc = ws.get<zd>("defl_X", (size_t)dim * chunk, &err);
+  const int qcap = (nev + 95) / 96 * 96;
+  zd* T1 = ws.get<zd>("defl_T1", (size_t)qcap * m, &err);
+  zd* T2 = ws.get<zd>("defl_T2", (size_t)qcap * m, &err);
+  cplx<S>* Xp = ws.get<cplx<S>>("defl_Xp", (size_t)dim * m, &err);
+  double* partial = ws.get<double>("defl_partial", (size_t)npart * 96 * m * 2, &err);
+  if (err != cudaSuccess) {
+    if (msg) *msg = std::string("device allocation failed: ") + cudaGetErrorString(err);
+    return WTB_ENOMEM;
+  }
+  DeflatedOperator<S> dop;
+  dop.base = &op;
+  dop.Q = Q;
+  dop.ldq = nev;
+  dop.dim = dim;
+  dop.npart = npart;
+  dop.sigma = sigma;
+  dop.T1 = T1;
+  dop.T2 = T2;
+  dop.Xp = Xp;
+  dop.partial = partial;
+  E->assign(nev, 0.0);
+  SolveStats tot;
+  for (int k0 = 0; k0 < nev; k0 += chunk) {
+    const int kc = std::min(chunk, nev - k0);
+    dop.nq = k0;
+    std::vector<double> Ec;
+    SolveStats sc;
+    const int rc = lobpcg_solve<S>(dop, diag, dim, kc, std::min(m, dim - k0), tol, maxit, ws, st, s, &Ec, Xc, &sc, msg,
+                                   tol_refine);
+    if (rc != WTB_OK) {
+      if (msg) *msg = "eigenpairs " + std::to_string(k0 + 1) + "-" + std::to_string(k0 + kc) + ": " + *msg;
+      return rc;
+    }
+    for (int j = 0; j < kc; ++j) (*E)[k0 + j] = Ec[j];
+    CK(launch_copy_cols<double>(Xc, kc, Xout + k0, nev, kc, dim, s));
+    CK((launch_convert_cols<double, S>(Xc, kc, Q + k0, nev, kc, dim, s)));
+    tot.iterations += sc.iterations;
+    tot.matvec_columns += sc.matvec_columns;
+    tot.max_rel_residual = std::max(tot.max_rel_residual, sc.max_rel_residual);
+    tot.refine_shift_max = std::max(tot.refine_shift_max, sc.refine_shift_max);
+  }
+  // ascending order across the chunks (a pair close to a chunk boundary may come out of order): sort, moving
+  // the vectors' columns with their values
+  std::vector<int> perm(nev);
+  for (int j = 0; j < nev; ++j) perm[j] = j;
+  std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return (*E)[a] < (*E)[b]; });
+  bool sorted = true;
+  for (int j = 0; j < nev; ++j) sorted &= perm[j] == j;
+  if (!sorted) {
+    zd* tmp = ws.get<zd>("defl_sort", (size_t)dim * nev, &err);
+    if (err != cudaSuccess) {
+      if (msg) *msg = "device allocation failed";
+      return WTB_ENOMEM;
+    }
+    CK(launch_copy_cols<double>(Xout, nev, tmp, nev, nev, dim, s));
+    std::vector<double> Es(nev);
+    for (int j = 0; j < nev; ++j) {
+      Es[j] = (*E)[perm[j]];
+      CK(launch_copy_cols<double>(tmp + perm[j], nev, Xout + j, nev, 1, dim, s));
+    }
+    *E = Es;
+  }
+  if (stats) *stats = tot;
+  return WTB_OK;
+}
+
+template int lobpcg_solve_deflated<float>(Operator<float>&, const double*, int, int, int, int, double, int, double,
+                                          Workspace&, DevStatus*, cudaStream_t, std::vector<double>*, zd*, SolveStats*,
+                                          std::string*, double);
+template int lobpcg_solve_deflated<double>(Operator<double>&, const double*, int, int, int, int, double, int, double,
+                                           Workspace&, DevStatus*, cudaStream_t, std::vector<double>*, zd*,
+                                           SolveStats*, std::string*, double);
 
 template int lobpcg_solve<float>(Operator<float>&, const double*, int, int, int, double, int, Workspace&, DevStatus*,
                                  cudaStream_t, std::vector<double>*, zd*, SolveStats*, std::string*, double);

@@ -217,6 +217,14 @@ int lobpcg_solve(Operator<S>& op, const double* diag, int dim, int nev, int m, d
                  Workspace& ws, DevStatus* st, cudaStream_t s, std::vector<double>* E, zd* Xout, SolveStats* stats,
                  std::string* msg, double tol_refine = 0.0);
 
+// The lowest nev eigenpairs for nev beyond one block (the reference asks 100): chunks of `chunk` eigenpairs,
+// each an ordinary solve with block m of P H P + sigma Q Q^H, Q the eigenvectors of the chunks before it and
+// P = I - Q Q^H (sigma moves span(Q) above the eigenvalues still sought).  Same outputs as lobpcg_solve, ascending.
+template <class S>
+int lobpcg_solve_deflated(Operator<S>& op, const double* diag, int dim, int nev, int chunk, int m, double tol,
+                          int maxit, double sigma, Workspace& ws, DevStatus* st, cudaStream_t s, std::vector<double>* E,
+                          zd* Xout, SolveStats* stats, std::string* msg, double tol_refine = 0.0);
+
 // A ragged batch of independent eigenproblems in one concatenated row space (BatchMap, device tables; the
 // solver sets its frozen flags and part count): nrow rows in all, nparts reduction parts, dims[q] the rows of
 // system q.  A single system needs only nrow and dims = {nrow}.

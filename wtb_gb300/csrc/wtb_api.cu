@@ -303,10 +303,26 @@ int coulomb_table_into(wtb_ctx* c, const wtb_bse_params* p, double* V, int ldv, 
   return WTB_OK;
 }
 
+// the largest block the block eigensolver takes (3 m columns in its projected problems)
+int block_cap(bool fp64) { return fp64 ? 26 : 32; }
+
+// shift of the deflated solves: the spread of the diagonal plus 2 eV moves a found eigenpair above every
+// eigenvalue still sought (the lowest excitons lie below the largest transition energy)
+int deflation_shift(wtb_ctx* c, const double* d_diag, int dim, double* sigma) {
+  std::vector<double> h(dim);
+  CKC(cudaMemcpyAsync(h.data(), d_diag, sizeof(double) * dim, cudaMemcpyDeviceToHost, c->s));
+  CKC(cudaStreamSynchronize(c->s));
+  const auto mm = std::minmax_element(h.begin(), h.end());
+  *sigma = (*mm.second - *mm.first) + 2.0;
+  return WTB_OK;
+}
+
 int auto_block(const wtb_bse_params* p, int dim, bool fp64) {
-  int m = p->block > 0 ? p->block : std::max(p->nev + 6, (3 * p->nev + 1) / 2);
-  if (p->block <= 0) m = (m + 7) / 8 * 8;
-  const int cap = fp64 ? 26 : 32;
+  // automatic: nev + 4 rounded up to a multiple of 8, at least 16 (measured on the 57,600 workload with nev = 10:
+  // blocks 12 / 14 / 16 / 24 took 13.6 (not converged) / 15.0 / 13.5 / 22.4 ms; on the 36,864 one with nev = 20:
+  // blocks 20 / 24 / 32 took 20.8 / 20.0 / 23.4 ms)
+  int m = p->block > 0 ? p->block : std::max(16, (p->nev + 4 + 7) / 8 * 8);
+  const int cap = block_cap(fp64);
   if (m > cap) m = cap;
   if (m < p->nev) m = p->nev;
   if (m > dim) m = dim;
@@ -436,11 +452,22 @@ int run_solve(wtb_ctx* c, const wtb_bse_params* p, std::vector<double>* E, wtb_t
   CKC(cudaEventRecord(ev[1], c->s));
   int rc;
   std::string msg;
-  if (ob.o64)
+  if (p->nev > block_cap(fp64)) {
+    // more excitons than one block holds (the reference asks 100): chunks of 16 with deflation
+    double sigma = 0.0;
+    CKR(deflation_shift(c, ob.dE, dim, &sigma));
+    if (ob.o64)
+      rc = lobpcg_solve_deflated<double>(*ob.o64, ob.dE, dim, p->nev, 16, 24, tol, maxit, sigma, c->ws, c->st, c->s, E,
+                                         Xout, stats, &msg);
+    else
+      rc = lobpcg_solve_deflated<float>(*ob.o32, ob.dE, dim, p->nev, 16, 24, tol, maxit, sigma, c->ws, c->st, c->s, E,
+                                        Xout, stats, &msg, tol_refine);
+  } else if (ob.o64) {
     rc = lobpcg_solve<double>(*ob.o64, ob.dE, dim, p->nev, m, tol, maxit, c->ws, c->st, c->s, E, Xout, stats, &msg);
-  else
+  } else {
     rc = lobpcg_solve<float>(*ob.o32, ob.dE, dim, p->nev, m, tol, maxit, c->ws, c->st, c->s, E, Xout, stats, &msg,
                              tol_refine);
+  }
   if (!ob.msg.empty()) msg += " (" + ob.msg + ")";
   CKC(cudaEventRecord(ev[2], c->s));
   CKC(cudaEventSynchronize(ev[2]));
@@ -1299,7 +1326,15 @@ int wtb_slepc_solver(wtb_ctx* c, const double* HX, double* EX, double* HE, int N
   std::vector<double> E;
   SolveStats stats;
   std::string msg;
-  int rc = lobpcg_solve<double>(op, d, NX, NE, m, 1e-8, 200, c->ws, c->st, c->s, &E, X, &stats, &msg);
+  int rc;
+  if (NE > block_cap(true)) {
+    // the reference's NE = 100: chunks of 16 with deflation
+    double sigma = 0.0;
+    CKR(deflation_shift(c, d, NX, &sigma));
+    rc = lobpcg_solve_deflated<double>(op, d, NX, NE, 16, 24, 1e-8, 200, sigma, c->ws, c->st, c->s, &E, X, &stats, &msg);
+  } else {
+    rc = lobpcg_solve<double>(op, d, NX, NE, m, 1e-8, 200, c->ws, c->st, c->s, &E, X, &stats, &msg);
+  }
   if (rc != WTB_OK) return set_err(c, rc, msg);
   for (int i = 0; i < NE; ++i)
     if (EX) EX[i] = E[i];
