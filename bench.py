@@ -116,6 +116,24 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# the arithmetic of the exciton solve per precision form (operator / iteration, final Rayleigh-Ritz)
+DTYPES = {"fp32": "f32 operator (FFT convolution on a 2D mesh), f32 iteration, f64 Rayleigh-Ritz",
+          "bf16x3": "bf16x3+f32 operator, f64 Rayleigh-Ritz", "bf16x6": "bf16x6+f32 operator, f64 Rayleigh-Ritz",
+          "fp64": "f64"}
+
+
+def form_for(args, p, batch=False):
+    """The precision form a workload runs in: the requested one, or with "auto" the fastest: fp32 where the FP32
+    operator is the FFT convolution (a 2D mesh of at most 64 x 64 points), bf16x3 (tensor cores) otherwise and
+    for the batch's joint graph."""
+    if args.precision != "auto":
+        return args.precision
+    if batch:
+        return "bf16x3"
+    g = p.ngrid
+    return "fp32" if (g[2] == 1 and max(g[0], g[1]) <= 64) else "bf16x3"
+
+
 def measured_peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -322,7 +340,8 @@ def batch_line(args, torch, api, S, world, local, steps, warmup):
     part = B.lpt_partition([B.system_cost(p, s.w90basis) for s, p in everything], world)[rank]
     items = [everything[i] for i in part]
     b = api.Batch(local)
-    kw = dict(precision=args.precision, op="matfree", tol=args.tol)
+    prec = form_for(args, None, batch=True)
+    kw = dict(precision=prec, op="matfree", tol=args.tol)
     for _ in range(warmup):
         b.bsesolver(items, **kw)
     torch.cuda.synchronize()
@@ -357,11 +376,11 @@ def batch_line(args, torch, api, S, world, local, steps, warmup):
     line = {"metric": "exciton systems/s (BSE build + lowest-6 solve, 64-system batch)", "value": value,
             "unit": "systems/s", "n_gpus": world, "steps": steps, "warmup": warmup,
             "ms_per_step": tot / steps, "higher_is_better": True, "scaling": "strong", "vs_baseline": None,
-            "dtype": args.precision, "data": "synthetic (seeded H(R))",
+            "dtype": prec, "data": "synthetic (seeded H(R))",
             "config": {"workload": "batch64", "systems_this_rank": len(items), "sharding": "LPT over ranks",
                        "description": WORKLOADS["batch64"],
                        "form": "one graph launch per batch (joint ragged-batch eigensolve, grouped tcgen05 contraction)",
-                       "precision": args.precision, "l2": "inputs and operators of 64 systems exceed L2 per step",
+                       "precision": prec, "l2": "inputs and operators of 64 systems exceed L2 per step",
                        "timing": "events on a side stream around the blocking batch call"},
             "phases_ms": {k: round(v, 3) for k, v in phases.items()},
             "e2e": {"value": value, "unit": "systems/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
@@ -436,6 +455,9 @@ def contraction_roofline(api, ctx, p, kw, sysm, peaks, step_ms, last, precision)
     n = max(nl.value, 1)
     g_ms = tms.value / n
     issued = fl.value / n
+    form = ctx.operator_form()
+    if form == "FP32 FFT convolution":
+        return fft_roofline(p, peaks, step_ms, last, g_ms, issued, by.value / n, int(nl.value))
     nk, w = p.nk, sysm.w90basis
     nb = 16  # the operator's block width (the eigensolver block)
     algo = 4.0 * nk * nk * w * w * nb  # one real V (nk x nk) times a complex panel (nk x w^2 nb)
@@ -469,6 +491,35 @@ def contraction_roofline(api, ctx, p, kw, sysm, peaks, step_ms, last, precision)
     return r
 
 
+# FP32 issue rate of the CUDA cores: 152 SMs x 128 lanes x 2 flops (FMA) at the 2070 MHz maximum SM clock
+FP32_NOMINAL_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12
+
+
+def fft_roofline(p, peaks, step_ms, last, g_ms, flops, algo_bytes, launches):
+    """Roofline of the FP32 FFT convolution (the contraction of the FP32 matrix-free form on a 2D mesh): against
+    the measured HBM copy rate with its algorithmic bytes (Z read and T written once in FP32, the P x P spectrum
+    once), and its FFT flop rate (5 P log2 P per transform) against the CUDA cores' nominal FP32 rate."""
+    hbm = peaks.get("hbm_gbs") if peaks else 6800.0
+    ach = algo_bytes / (g_ms * 1e-3) / 1e9 if g_ms > 0 else None
+    tfl = flops / (g_ms * 1e-3) / 1e12 if g_ms > 0 else None
+    return {"bound": "hbm", "kernel": "fft_conv_kernel (FP32 FFT convolution of the gathered Z with the Coulomb "
+                                      "stencil, one 128 x 128 transform pair per column pair)",
+            "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": (ach / hbm) if ach else None,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback",
+            "achieved_definition": "algorithmic bytes per launch (Z read and T written once in FP32, the spectrum "
+                                   "once) / CUDA-event launch time",
+            "algorithmic_bytes_per_launch": algo_bytes,
+            "fft_flops_per_launch": flops, "fp32_tflops": tfl, "fp32_nominal_tflops": FP32_NOMINAL_TFLOPS,
+            "frac_fp32_nominal": (tfl / FP32_NOMINAL_TFLOPS) if tfl else None,
+            "limiter": "the shared-memory pipe (transposes and the transforms' passes through the shared grid), "
+                       "not HBM: see profiles/fft_conv_hex12_60x60.md",
+            "launches_timed": launches, "avg_launch_ms": g_ms,
+            "launches_per_step": last["timings"]["iterations"] + 3,
+            "share_of_step": (g_ms * (last["timings"]["iterations"] + 3) / step_ms) if step_ms > 0 and g_ms > 0
+            else None,
+            "traffic": None, "traffic_source": "not captured for this kernel"}
+
+
 def p_name_of(p, sysm):
     return "hex12_60x60" if (p.nk == 3600 and sysm.w90basis == 12) else "other"
 
@@ -479,14 +530,16 @@ def c2_line(torch, api, ctx, args, stream, l2buf, local):
     name = "cubic16_16x16x16"
     sysm, p, g = load_workload(name)
     ctx.set_hr(sysm)
-    kw = dict(precision=args.precision, op="matfree", tol=args.tol)
+    prec = form_for(args, p)
+    kw = dict(precision=prec, op="matfree", tol=args.tol)
     clocks = ClockSampler(local)
     clocks.start()
     ms, last = timed_solves(torch, ctx, p, kw, args.steps, args.warmup, stream, l2buf)
     clk = clocks.stop()
     step = float(np.mean(ms))
     d = {"workload": name, "description": WORKLOADS[name], "unit": UNIT, "value": 1000.0 / step,
-         "ms_per_step": step, "steps": args.steps, "precision": args.precision, "clocks": clk,
+         "ms_per_step": step, "steps": args.steps, "precision": prec, "contraction": ctx.operator_form(),
+         "clocks": clk,
          "solver": {"iterations": last["timings"]["iterations"], "max_rel_residual": last["timings"]["max_rel_residual"]}}
     d.update(oracle_errors(ctx, p, last, g))
     d["fp64_gpu_form"] = fp64_forms(torch, ctx, p, g, step / 1000.0, last)
@@ -500,7 +553,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--workload", default="hex12_60x60")
-    ap.add_argument("--precision", default="bf16x3")
+    ap.add_argument("--precision", default="auto",
+                    help="auto (per workload: fp32 on a 2D mesh of at most 64 x 64 points, whose FP32 operator is the "
+                         "FFT convolution, else bf16x3; bf16x3 for the batch), fp32, bf16x3, bf16x6 or fp64")
     ap.add_argument("--tol", type=float, default=0.0, help="residual target (0: the library's per-precision default)")
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain FP64 GPU forms")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
@@ -535,7 +590,8 @@ def main():
     ctx.set_hr(sysm)
     stream = torch.cuda.ExternalStream(api.lib().wtb_ctx_stream(ctx._h))
     l2buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
-    solve_kw = dict(precision=args.precision, op="matfree", tol=args.tol)
+    prec = form_for(args, p)
+    solve_kw = dict(precision=prec, op="matfree", tol=args.tol)
 
     def pinned(shape, dtype, order="C"):
         n = int(np.prod(shape))
@@ -570,7 +626,8 @@ def main():
     value = world * args.steps / (tot_ms / 1000.0)
     mean_step = tot_ms / args.steps
     errs = oracle_errors(ctx, p, last, g)
-    roofline = contraction_roofline(api, ctx, p, solve_kw, sysm, measured_peaks(), mean_step, last, args.precision)
+    form = ctx.operator_form()
+    roofline = contraction_roofline(api, ctx, p, solve_kw, sysm, measured_peaks(), mean_step, last, prec)
 
     # end to end through the C ABI with host buffers: H(R) host -> device, Ws/acts/HE device -> host, both in
     # page-locked host memory (allocated before the timed loop); every step of the device-timed loop again
@@ -593,10 +650,11 @@ def main():
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": mean_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "bf16x3+f32 operator, f64 Rayleigh-Ritz" if args.precision == "bf16x3"
-            else args.precision, "data": "synthetic (seeded H(R), stored with the oracle's results)",
+            "vs_baseline": None, "dtype": DTYPES.get(prec, prec),
+            "data": "synthetic (seeded H(R), stored with the oracle's results)",
             "config": {"workload": args.workload, "description": WORKLOADS.get(args.workload, args.workload),
-                       "operator": "matrix-free", "precision": args.precision, "eigensolver_tol": args.tol,
+                       "operator": "matrix-free, contraction: " + form, "precision": prec,
+                       "eigensolver_tol": args.tol,
                        "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{world}"},
             "build_plus_solve_s": mean_step / 1000.0,
             **errs,

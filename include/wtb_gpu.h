@@ -428,9 +428,19 @@ int wtb_batch_matvec(wtb_batch* batch, int ncol, const double* X, double* Y);
  * t_ms[5] joint eigensolve, t_ms[6] oscillator strengths. */
 int wtb_batch_timings(const wtb_batch* batch, double* t_ms);
 
-/* The contraction tiles the autotuner chose in this process (one entry per operator shape: the tile and the
- * measured time of each candidate), as text into buf (len bytes, NUL-terminated).  Returns the full length. */
+/* The launch shapes the autotuner chose in this process, as JSON into buf (len bytes, NUL-terminated):
+ * {"build": the source hash the cache is keyed by, "cache": the cache file or null, "choices": [{"shape",
+ * "param" (tile_n, gather_tile, scatter_cols), "choice", "source" (measured | cache | pinned |
+ * default), "ms": [[candidate, mean ms], ...]}, ...]}.  Returns the full length.  Needs no device.
+ * The cache file is WTB_TUNE_CACHE ("off": none), else $XDG_CACHE_HOME or $HOME/.cache + /wtb_gb300/autotune.json;
+ * WTB_TUNE=off skips every measurement and WTB_TUNE_PIN="param=value,..." pins choices. */
 int wtb_autotune_report(char* buf, int len);
+
+/* The contraction form of the context's last BSE operator: WTB_FORM_NONE (dense operator, or none built),
+ * the split-BF16 tensor-core product, the FP32 or FP64 CUDA-core product, or the FP32 FFT convolution that
+ * the FP32 matrix-free operator uses on a two-dimensional Monkhorst-Pack mesh of at most 64 x 64 points. */
+enum { WTB_FORM_NONE = 0, WTB_FORM_TC_BF16 = 1, WTB_FORM_SIMT_F32 = 2, WTB_FORM_SIMT_F64 = 3, WTB_FORM_FFT_F32 = 4 };
+int wtb_operator_form(const wtb_ctx* ctx);
 
 /* Number of CUDA kernels this library has launched in the process (instrumentation for benchmarks). */
 long long wtb_kernel_launch_count(void);

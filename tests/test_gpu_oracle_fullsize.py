@@ -62,3 +62,25 @@ def test_energies_spectra_against_oracle(ctx, full, precision, op):
         ref = g["act_" + c]
         scale = max(np.abs(ref).max(), 1e-300)
         assert np.max(np.abs(out["acts"][c][: p.nev] - ref)) <= tol * scale, (name, precision, op, c)
+
+
+def test_fft_operator_at_full_size(ctx):
+    """The FP32 matrix-free operator of the 60 x 60 mesh is the FFT convolution (P = 128): 16 applications against
+    the oracle's FP64 factored operator, relative to ||H x||."""
+    from oracle import wtb_oracle as O
+
+    g = np.load(os.path.join(HERE, "golden", "hex12_60x60_oracle.npz"))
+    sysm = S.system_from_arrays(g)
+    _, p = S.workload("hex12_60x60", params_only=True)
+    ctx.set_hr(sysm)
+    ctx.bsesolver(p, precision="fp32", op="matfree")  # stages the mesh and its bands
+    kpt = O.monhkhorst_pack(p.ngrid[0], p.ngrid[1], p.ngrid[2], p.mshift, sysm.rlat)
+    eigv, vec, _ = O.bands(sysm, p, kpt)
+    rng = np.random.default_rng(128)
+    X = rng.normal(size=(p.dim, 16)) + 1j * rng.normal(size=(p.dim, 16))
+    Y = ctx.bse_matvec(p, X, precision="fp32", op="matfree")
+    assert ctx.operator_form() == "FP32 FFT convolution"
+    Yref = O.bse_matvec_factored(X, eigv, O.gauge_fix(vec), kpt, p, sysm.rlat)
+    err = np.linalg.norm(Y - Yref, axis=0) / np.linalg.norm(Yref, axis=0)
+    print(f"hex12_60x60 FFT operator: max relative error {err.max():.2e}")
+    assert err.max() <= 2e-6, err

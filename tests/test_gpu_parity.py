@@ -124,6 +124,25 @@ def test_operator_matvec(ctx, small, precision, op, ncol):
     assert err.max() <= MATVEC_TOL[(precision, op)], err
 
 
+@pytest.mark.parametrize("name,P", [("hex8_6x6", 32), ("hex8_24x24", 64)])
+def test_fft_operator_on_the_mesh(ctx, name, P):
+    """On a Monkhorst-Pack mesh (bands of the mesh itself, not a k-point list) the FP32 matrix-free operator is the
+    FFT convolution of the Coulomb stencil (transform size P): against the oracle's FP64 factored operator,
+    relative to ||H x|| (the bound of the CUDA-core FP32 product)."""
+    sysm, p = S.workload(name)
+    ctx.set_hr(sysm)
+    ctx.bsesolver(p, precision="fp64", op="matfree")  # stages the mesh and its bands
+    kpt = O.monhkhorst_pack(p.ngrid[0], p.ngrid[1], p.ngrid[2], p.mshift, sysm.rlat)
+    eigv, vec, _ = O.bands(sysm, p, kpt)
+    rng = np.random.default_rng(P)
+    X = rng.normal(size=(p.dim, 20)) + 1j * rng.normal(size=(p.dim, 20))
+    Y = ctx.bse_matvec(p, X, precision="fp32", op="matfree")
+    assert ctx.operator_form() == "FP32 FFT convolution"
+    Yref = O.bse_matvec_factored(X, eigv, O.gauge_fix(vec), kpt, p, sysm.rlat)
+    err = np.linalg.norm(Y - Yref, axis=0) / np.linalg.norm(Yref, axis=0)
+    assert err.max() <= 2e-6, err
+
+
 def test_slepc_solver_dense(ctx, small):
     sysm, p, ref = small
     Href = O.bse_build(ref["eigv"], ref["vec"], ref["kpt"], p, sysm.rlat)

@@ -10,6 +10,7 @@ fallback: if the shared library is missing, importing this module raises.
 from __future__ import annotations
 
 import ctypes as C
+import json
 import os
 from dataclasses import dataclass
 
@@ -133,6 +134,7 @@ def _load():
         "wtb_optsp_pair": [C.c_double, dp, C.c_double, dp, C.c_double, C.c_double, C.c_double, ip, C.c_double,
                            C.c_int, C.c_int, dp, ip, dp, dp, dp, dp, dp],
         "wtb_optdiel": [C.c_int, C.c_double, C.c_int, ip, C.c_double, dp, dp, C.c_double, dp, dp],
+        "wtb_operator_form": [P],
     }
     for name, args in sigs.items():
         f = getattr(lib, name)
@@ -194,12 +196,17 @@ def cparams(p: BSEParams, precision="fp64", op="dense", tol=0.0, maxit=0, block=
     return c
 
 
-def autotune_report() -> str:
-    """The contraction tiles chosen by the autotuner in this process (wtb_autotune_report)."""
+def autotune_report() -> dict:
+    """The launch shapes chosen by the autotuner in this process (wtb_autotune_report): the source hash its
+    cache is keyed by, the cache file, and one entry per (shape, parameter)."""
     n = _lib.wtb_autotune_report(None, 0)
     buf = C.create_string_buffer(n + 1)
     _lib.wtb_autotune_report(buf, n + 1)
-    return buf.value.decode()
+    return json.loads(buf.value.decode())
+
+
+OPERATOR_FORMS = ("none", "tensor-core split-BF16 product", "FP32 CUDA-core product", "FP64 CUDA-core product",
+                  "FP32 FFT convolution")
 
 
 def kernel_launch_count() -> int:
@@ -537,6 +544,10 @@ class Context:
         self._chk(_lib.wtb_exciton_lifetime(self._h, sysdim.encode(), g.ctypes.data_as(C.POINTER(C.c_int)),
                                             F.shape[0], _dp(F), int(bool(pol)), _dp(L)), "wtb_exciton_lifetime")
         return L
+
+    def operator_form(self) -> str:
+        """The contraction form of the last BSE operator (wtb_operator_form)."""
+        return OPERATOR_FORMS[int(_lib.wtb_operator_form(self._h))]
 
     def bse_matvec(self, p: BSEParams, X, precision="fp64", op="matfree"):
         """Y = H X for the bands of the last set-up (X: dim x ncol complex)."""

@@ -336,9 +336,11 @@ int build_graph(wtb_batch* b, int nsys, const wtb_bse_params* p, std::string* ms
     const int v[5] = {gd[q].M, gd[q].K, gd[q].N, gd[q].m_valid, gd[q].n_valid};
     tkey = fnv(tkey, v, sizeof(v));
   }
-  char what[96];
-  std::snprintf(what, sizeof(what), "grouped contraction of %d systems (%d slice products)", nsys, op->npairs);
-  const int bn = tc_autotune(tkey, what, [&](int cand) -> cudaError_t {
+  // the batch's shape: its system count, slice products and a hash of every system's contraction extents
+  char shape[128];
+  std::snprintf(shape, sizeof(shape), "grouped contraction systems=%d products=%d extents=%016llx", nsys, op->npairs,
+                (unsigned long long)tkey);
+  const int bn = tune_choice(shape, "tile_n", {256, 128}, 256, [&](int cand) -> cudaError_t {
     TcGroupPlan* g = group_of(cand);
     return g ? tc_gemm_group_run(g, op->npairs, nullptr, mc->st, mc->s) : cudaErrorInvalidValue;
   }, mc->s);

@@ -29,6 +29,8 @@ struct wtb_ctx {
   bool mesh_mp = false;
   // last BSE operator data (for wtb_optsp)
   bool have_hr_optics = false;
+  // contraction form of the last operator built (WTB_FORM_*)
+  int last_form = 0;
   wtb::KernelProfile prof;
   // the last wtb_bsesolver call (for wtb_bse_backward): its parameters and exciton energies
   bool have_solve = false;

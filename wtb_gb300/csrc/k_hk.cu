@@ -507,6 +507,15 @@ cudaError_t launch_coulomb(const CoulParams& p, const double* kpt1, int n1, cons
   return cudaGetLastError();
 }
 
+cudaError_t launch_coulomb_stencil(const CoulParams& p, const double* bl, double* stencil, cudaStream_t s) {
+  CoulConst cc{};
+  if (!coul_const(p, &cc)) return cudaErrorInvalidValue;
+  const int n1 = p.ngrid[0], n2 = p.ngrid[1], n3 = p.ngrid[2];
+  const int ns = (2 * n1 - 1) * (2 * n2 - 1) * (2 * n3 - 1);
+  coulomb_stencil_kernel<<<(ns + 127) / 128, 128, 0, s>>>(cc, bl, n1, n2, n3, stencil); ++g_launch_count;
+  return cudaGetLastError();
+}
+
 cudaError_t launch_coulomb_mesh(const CoulParams& p, const double* bl, double* stencil, double* V, int ldv,
                                 cudaStream_t s) {
   CoulConst cc{};

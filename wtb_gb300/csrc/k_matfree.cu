@@ -111,11 +111,13 @@ __global__ void __launch_bounds__(256) mf_gather_kernel(const cplx<S>* __restric
 // vectors of 8 bf16.  zt is stored in 64-wide K blocks, zt[slice][kb][n][64] (ldn rows per block): the tile's
 // row segments of one block sit side by side, so a warp's stores cover contiguous memory.  k' >= nk inside the
 // last tile give zeros (x = 0).
-template <int KT>
+// F32: the same tile writes FP32 Z rows instead, z32[n][ldk] (n = ((b w + o) w + p) 2 + ri, k' contiguous; ldk a
+// multiple of 64, so the tile's KT values are 16-byte aligned; k' >= nk inside the last tile get zeros).
+template <int KT, bool F32 = false>
 __device__ __forceinline__ void gather_bf16_tile(const zf* __restrict__ X, int ldx, int c0, int nbc, int nbp,
                                                  const zd* __restrict__ vec_win, int nk, int nv, int nc, int w,
                                                  uint16_t* __restrict__ zt, int ldn, int nslices, long slice_stride,
-                                                 int kt0) {
+                                                 int kt0, float* __restrict__ z32 = nullptr, int ldk = 0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nbnd = nv + nc, ncv = nc * nv, ww = w * w;
   const int tkn = min(KT, nk - kt0);
@@ -167,6 +169,16 @@ __device__ __forceinline__ void gather_bf16_tile(const zf* __restrict__ X, int l
         zi[kk] = acc.im;
       }
       const long row = ((long)((b0 + bb) * w + o) * w + p) * 2;
+      if constexpr (F32) {
+        float4* dre = reinterpret_cast<float4*>(z32 + row * ldk + kt0);
+        float4* dim = reinterpret_cast<float4*>(z32 + (row + 1) * ldk + kt0);
+#pragma unroll
+        for (int h = 0; h < KT / 4; ++h) {
+          dre[h] = make_float4(zr[4 * h], zr[4 * h + 1], zr[4 * h + 2], zr[4 * h + 3]);
+          dim[h] = make_float4(zi[4 * h], zi[4 * h + 1], zi[4 * h + 2], zi[4 * h + 3]);
+        }
+        continue;
+      }
       const long off_re = ((long)(kt0 >> 6) * ldn + row) * 64 + (kt0 & 63), off_im = off_re + 64;
       for (int sl = 0; sl < nslices; ++sl) {
 #pragma unroll
@@ -217,6 +229,14 @@ __global__ void __launch_bounds__(256) mf_gather_bf16_kernel(const zf* __restric
                                                              int nc, int w, uint16_t* __restrict__ zt, int ldn,
                                                              int nslices, long slice_stride) {
   gather_bf16_tile<KT>(X, ldx, c0, nbc, nbp, vec_win, nk, nv, nc, w, zt, ldn, nslices, slice_stride, blockIdx.x * KT);
+}
+
+template <int KT>
+__global__ void __launch_bounds__(256) mf_gather_f32_kernel(const zf* __restrict__ X, int ldx, int c0, int nbc,
+                                                            int nbp, const zd* __restrict__ vec_win, int nk, int nv,
+                                                            int nc, int w, float* __restrict__ z32, int ldk) {
+  gather_bf16_tile<KT, true>(X, ldx, c0, nbc, nbp, vec_win, nk, nv, nc, w, nullptr, 0, 0, 0, blockIdx.x * KT, z32,
+                             ldk);
 }
 
 // batch: CTA b takes tile tiles[b] = (system, first k-point) of the systems' Z panels; frozen systems are
@@ -410,10 +430,16 @@ __global__ void round_f32_kernel(const double* __restrict__ V, int ldv, int rows
 
 template <class S, class Z>
 cudaError_t launch_mf_gather(const cplx<S>* X, int ldx, int c0, int nb, const zd* vec_win, int nk, int nv, int nc,
-                             int w, Z* zt, int ldk, int nslices, long slice_stride, cudaStream_t s) {
+                             int w, Z* zt, int ldk, int nslices, long slice_stride, cudaStream_t s, int tile) {
   if constexpr (sizeof(S) == 4 && sizeof(Z) == 2) {
     int nbp = nb;
-    const int KT = gather_tile(nv, nc, w, nb, &nbp);
+    int KT = gather_tile(nv, nc, w, nb, &nbp);
+    // a requested tile KT * 100 + nbp (16 or 8 k' per CTA, 1..8 block columns per chunk)
+    if (tile > 0) {
+      KT = tile / 100;
+      nbp = std::min(tile % 100, nb);
+      if ((KT != 16 && KT != 8) || nbp < 1 || nbp > 8) return cudaErrorInvalidValue;
+    }
     const size_t smem = gather_smem(KT, nv, nc, w, nbp);
     // the K-blocked panel: ldk a multiple of 64, ldn = rows per K block
     const int ldn = (int)(slice_stride / ldk);
@@ -437,6 +463,32 @@ cudaError_t launch_mf_gather(const cplx<S>* X, int ldx, int c0, int nb, const zd
       return cudaGetLastError();
     }
   }
+  if constexpr (sizeof(S) == 4 && sizeof(Z) == 4) {
+    // FP32 rows through the tiled gather (the band vectors and X rows of a tile staged once for nbp columns)
+    int nbp = nb;
+    int KT = gather_tile(nv, nc, w, nb, &nbp);
+    if (tile > 0) {
+      KT = tile / 100;
+      nbp = std::min(tile % 100, nb);
+      if ((KT != 16 && KT != 8) || nbp < 1 || nbp > 8) return cudaErrorInvalidValue;
+    }
+    const size_t smem = gather_smem(KT, nv, nc, w, nbp);
+    if (smem <= 200 * 1024 && ldk % 64 == 0 && nslices == 1) {
+      const void* fn = KT == 16 ? reinterpret_cast<const void*>(mf_gather_f32_kernel<16>)
+                                : reinterpret_cast<const void*>(mf_gather_f32_kernel<8>);
+      cudaError_t e = raise_smem_limit(fn, smem);
+      if (e != cudaSuccess) return e;
+      const unsigned nch = (unsigned)((nb + nbp - 1) / nbp);
+      if (KT == 16)
+        mf_gather_f32_kernel<16><<<dim3((nk + 15) / 16, nch), 256, smem, s>>>(
+            reinterpret_cast<const zf*>(X), ldx, c0, nb, nbp, vec_win, nk, nv, nc, w, reinterpret_cast<float*>(zt), ldk);
+      else
+        mf_gather_f32_kernel<8><<<dim3((nk + 7) / 8, nch), 256, smem, s>>>(
+            reinterpret_cast<const zf*>(X), ldx, c0, nb, nbp, vec_win, nk, nv, nc, w, reinterpret_cast<float*>(zt), ldk);
+      ++g_launch_count;
+      return cudaGetLastError();
+    }
+  }
   if constexpr (sizeof(Z) == 2) return cudaErrorInvalidValue;  // the bf16 panel exists only in the K-blocked layout
   int KT = 32;
   auto smem_of = [&](int kt) { return (size_t)(2 * kt * nc * w + kt * nv * w + kt * nc * nv) * sizeof(cplx<S>); };
@@ -452,8 +504,10 @@ cudaError_t launch_mf_gather(const cplx<S>* X, int ldx, int c0, int nb, const zd
 
 template <class S, class T>
 cudaError_t launch_mf_scatter(const T* Tm, int ldt, const cplx<S>* X, int ldx, const zd* vec_win, const double* dE,
-                              int nk, int nv, int nc, int w, int nb, cplx<S>* Y, int ldy, int c0, cudaStream_t s) {
-  int nbg = nb;
+                              int nk, int nv, int nc, int w, int nb, cplx<S>* Y, int ldy, int c0, cudaStream_t s,
+                              int cols) {
+  // block columns per CTA: all (or the requested count), halved until the CTA's tiles fit in 96 KB
+  int nbg = cols > 0 ? std::min(cols, nb) : nb;
   auto smem_of = [&](int g) {
     return (size_t)((nc + nv) * w + g * (w * nv + 1)) * sizeof(cplx<S>) + (size_t)g * w * (2 * w + 1) * sizeof(T) + 16;
   };
@@ -532,17 +586,17 @@ cudaError_t launch_round_f32(const double* V, int ldv, int rows, int cols, float
 }
 
 template cudaError_t launch_mf_gather<float, float>(const cplx<float>*, int, int, int, const zd*, int, int, int, int,
-                                                    float*, int, int, long, cudaStream_t);
+                                                    float*, int, int, long, cudaStream_t, int);
 template cudaError_t launch_mf_gather<float, uint16_t>(const cplx<float>*, int, int, int, const zd*, int, int, int,
-                                                       int, uint16_t*, int, int, long, cudaStream_t);
+                                                       int, uint16_t*, int, int, long, cudaStream_t, int);
 template cudaError_t launch_mf_gather<double, double>(const cplx<double>*, int, int, int, const zd*, int, int, int,
-                                                      int, double*, int, int, long, cudaStream_t);
+                                                      int, double*, int, int, long, cudaStream_t, int);
 template cudaError_t launch_mf_scatter<float, float>(const float*, int, const cplx<float>*, int, const zd*,
                                                      const double*, int, int, int, int, int, cplx<float>*, int, int,
-                                                     cudaStream_t);
+                                                     cudaStream_t, int);
 template cudaError_t launch_mf_scatter<double, double>(const double*, int, const cplx<double>*, int, const zd*,
                                                        const double*, int, int, int, int, int, cplx<double>*, int, int,
-                                                       cudaStream_t);
+                                                       cudaStream_t, int);
 template cudaError_t launch_simt_gemm_tn<float>(const float*, int, const float*, int, float*, int, int, int, int,
                                                 cudaStream_t);
 template cudaError_t launch_simt_gemm_tn<double>(const double*, int, const double*, int, double*, int, int, int, int,

@@ -17,8 +17,6 @@
 #include <cstdio>
 #include <cstring>
 #include <functional>
-#include <map>
-#include <mutex>
 #include <utility>
 
 #include <cuda.h>
@@ -645,70 +643,5 @@ cudaError_t tc_gemm_group_run_split(TcGroupPlan* plan, int npairs, const int* fr
 }
 
 void tc_gemm_group_destroy(TcGroupPlan* plan) { delete plan; }
-
-// ------------------------------------------------------------------------------------------------ autotuner
-// The column tile of the contraction is chosen by measurement: run(bn) launches the caller's own product with
-// that tile; each candidate gets one warm-up launch and three timed ones (CUDA events on the caller's stream)
-// and the fastest mean wins.  Results are kept per shape key for the life of the process, so a shape is
-// measured once (and never while a stream is being captured: the default tile is used then).
-namespace {
-struct TuneEntry {
-  int bn;
-  double ms[2];  // mean ms of bn = 256 and bn = 128
-  std::string what;
-};
-std::mutex g_tune_mu;
-std::map<uint64_t, TuneEntry> g_tune;
-}  // namespace
-
-int tc_autotune(uint64_t key, const std::string& what, const std::function<cudaError_t(int)>& run, cudaStream_t s) {
-  {
-    std::lock_guard<std::mutex> lk(g_tune_mu);
-    auto it = g_tune.find(key);
-    if (it != g_tune.end()) return it->second.bn;
-  }
-  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return 256;
-  // WTB_TC_TILE=256|128 pins the choice without timing: a kernel profiler serialises and replays the timed runs,
-  // which makes the timing (and so the tile a profiled run would use) differ from a normal run's
-  if (const char* pin = std::getenv("WTB_TC_TILE")) {
-    const int bn = std::atoi(pin) == 128 ? 128 : 256;
-    std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tune[key] = TuneEntry{bn, {0.0, 0.0}, what + " (pinned)"};
-    return bn;
-  }
-  const int cand[2] = {256, 128};
-  double ms[2] = {1e30, 1e30};
-  cudaEvent_t a = nullptr, b = nullptr;
-  if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) return 256;
-  for (int i = 0; i < 2; ++i) {
-    if (run(cand[i]) != cudaSuccess) continue;
-    if (cudaEventRecord(a, s) != cudaSuccess) continue;
-    bool ok = true;
-    for (int r = 0; r < 3 && ok; ++r) ok = run(cand[i]) == cudaSuccess;
-    float t = 0.f;
-    if (ok && cudaEventRecord(b, s) == cudaSuccess && cudaEventSynchronize(b) == cudaSuccess &&
-        cudaEventElapsedTime(&t, a, b) == cudaSuccess)
-      ms[i] = t / 3.0;
-  }
-  cudaEventDestroy(a);
-  cudaEventDestroy(b);
-  const int bn = ms[1] < ms[0] ? 128 : 256;
-  std::lock_guard<std::mutex> lk(g_tune_mu);
-  g_tune[key] = TuneEntry{bn, {ms[0], ms[1]}, what};
-  return bn;
-}
-
-std::string tc_autotune_report() {
-  std::lock_guard<std::mutex> lk(g_tune_mu);
-  std::string out;
-  char buf[256];
-  for (const auto& kv : g_tune) {
-    std::snprintf(buf, sizeof(buf), "%s%s: tile 128x%d (128x256 %.4f ms, 128x128 %.4f ms)", out.empty() ? "" : "; ",
-                  kv.second.what.c_str(), kv.second.bn, kv.second.ms[0], kv.second.ms[1]);
-    out += buf;
-  }
-  return out;
-}
 
 }  // namespace wtb

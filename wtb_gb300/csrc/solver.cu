@@ -45,7 +45,7 @@ cudaError_t MatFreeOperator<S>::apply(const cplx<S>* X, int ldx, int c0, int nco
     if (kind == GEMM_TC_BF16) {
       if constexpr (sizeof(S) == 4) {
         e = launch_mf_gather<float, uint16_t>(X, ldx, c0 + b0, nb, vec_win, nk, nv, nc, w, Zs, Kpad, nslices,
-                                              (long)Npad * Kpad, s);
+                                              (long)Npad * Kpad, s, gather_tile);
         if (e != cudaSuccess) return e;
         TcGemmPlan* plan = plan_for(N, npairs, tile_n);
         if (!plan) return cudaErrorInvalidValue;
@@ -69,7 +69,7 @@ cudaError_t MatFreeOperator<S>::apply(const cplx<S>* X, int ldx, int c0, int nco
           prof->bytes += 2.0 * nslices * ((double)nk * nk + (double)N * nk) + 4.0 * nk * (double)N;
         }
         e = launch_mf_scatter<float, float>(reinterpret_cast<const float*>(Tm), Npad, X, ldx, vec_win, dE, nk, nv, nc,
-                                            w, nb, Y, ldy, c0 + b0, s);
+                                            w, nb, Y, ldy, c0 + b0, s, scatter_cols);
         if (e != cudaSuccess) return e;
       } else {
         return cudaErrorInvalidValue;
@@ -84,14 +84,14 @@ cudaError_t MatFreeOperator<S>::apply(const cplx<S>* X, int ldx, int c0, int nco
         cudaEventCreate(&eb);
         cudaEventRecord(ea, s);
       }
-      e = launch_simt_gemm_tn<S>(Vr, Kpad, Zr, Kpad, reinterpret_cast<S*>(Tm), Npad, nk, N, Kpad, s);
+      e = contract_z(N, s);
       if (e != cudaSuccess) return e;
       if (profiled) {
         cudaEventRecord(eb, s);
         prof->pending.emplace_back(ea, eb);
         prof->launches += 1;
-        prof->flops += 2.0 * nk * (double)N * nk;
-        prof->bytes += sizeof(S) * ((double)nk * nk + (double)N * nk + (double)nk * N);
+        prof->flops += contraction_flops(N);
+        prof->bytes += contraction_bytes(N);
       }
       e = launch_mf_scatter<S, S>(reinterpret_cast<const S*>(Tm), Npad, X, ldx, vec_win, dE, nk, nv, nc, w, nb, Y, ldy,
                                   c0 + b0, s);
@@ -121,7 +121,7 @@ cudaError_t MatFreeOperator<S>::time_contraction(int reps, int ncol, cudaStream_
     if (plan)
       e = tc_gemm_run(plan, st, s);
     else
-      e = launch_simt_gemm_tn<S>(Vr, Kpad, Zr, Kpad, reinterpret_cast<S*>(Tm), Npad, nk, N, Kpad, s);
+      e = contract_z(N, s);
     if (e != cudaSuccess) return e;
     cudaEventRecord(eb, s);
     prof->pending.emplace_back(ea, eb);
@@ -130,8 +130,8 @@ cudaError_t MatFreeOperator<S>::time_contraction(int reps, int ncol, cudaStream_
       prof->flops += 2.0 * nk * (double)N * nk * np;
       prof->bytes += 2.0 * nslices * ((double)nk * nk + (double)N * nk) + 4.0 * nk * (double)N;
     } else {
-      prof->flops += 2.0 * nk * (double)N * nk;
-      prof->bytes += sizeof(S) * ((double)nk * nk + (double)N * nk + (double)nk * N);
+      prof->flops += contraction_flops(N);
+      prof->bytes += contraction_bytes(N);
     }
   }
   return cudaSuccess;
@@ -144,7 +144,7 @@ cudaError_t MatFreeOperator<S>::contract(const cplx<S>* X, int ldx, int ncol, cu
   if (kind == GEMM_TC_BF16) {
     if constexpr (sizeof(S) == 4) {
       cudaError_t e = launch_mf_gather<float, uint16_t>(X, ldx, 0, ncol, vec_win, nk, nv, nc, w, Zs, Kpad, nslices,
-                                                        (long)Npad * Kpad, s);
+                                                        (long)Npad * Kpad, s, gather_tile);
       if (e != cudaSuccess) return e;
       TcGemmPlan* plan = plan_for(N, npairs, tile_n);
       if (!plan) return cudaErrorInvalidValue;
@@ -155,7 +155,38 @@ cudaError_t MatFreeOperator<S>::contract(const cplx<S>* X, int ldx, int ncol, cu
   }
   cudaError_t e = launch_mf_gather<S, S>(X, ldx, 0, ncol, vec_win, nk, nv, nc, w, Zr, Kpad, 1, 0, s);
   if (e != cudaSuccess) return e;
+  return contract_z(N, s);
+}
+
+// T = V Z for the N gathered columns in Zr: FP32 FFT convolutions (FFT kind) or the CUDA-core product
+template <class S>
+cudaError_t MatFreeOperator<S>::contract_z(int N, cudaStream_t s) {
+  if (kind == GEMM_FFT_F32) {
+    if constexpr (sizeof(S) == 4)
+      return launch_fft_conv(reinterpret_cast<const float*>(Zr), Kpad, N / 2, mesh1, mesh2, fft_p, fft_spec, fft_tw,
+                             reinterpret_cast<float*>(Tm), Npad, s);
+    return cudaErrorInvalidValue;
+  }
   return launch_simt_gemm_tn<S>(Vr, Kpad, Zr, Kpad, reinterpret_cast<S*>(Tm), Npad, nk, N, Kpad, s);
+}
+
+// algorithmic flops and bytes of one contraction of N columns: the product's 2 nk^2 N, or for the FFT kind
+// 5 P log2(P) per P-point transform, (2 n1 + 2 P) transforms per column pair, plus the spectrum products
+template <class S>
+double MatFreeOperator<S>::contraction_flops(int N) const {
+  if (kind == GEMM_FFT_F32) {
+    const double lg = std::log2((double)fft_p);
+    return (N / 2) * ((2.0 * mesh1 + 2.0 * fft_p) * 5.0 * fft_p * lg + 6.0 * fft_p * fft_p);
+  }
+  return 2.0 * nk * (double)N * nk;
+}
+
+// Z read and T written once (FP32 for the FFT kind, with its P x P FP32 spectrum read once; every column pair
+// rereads it from L2), and the nk x nk table for the product
+template <class S>
+double MatFreeOperator<S>::contraction_bytes(int N) const {
+  if (kind == GEMM_FFT_F32) return 4.0 * 2.0 * N * nk + 8.0 * (double)fft_p * fft_p;
+  return sizeof(S) * ((double)nk * nk + (double)N * nk + (double)nk * N);
 }
 
 template <class S>
@@ -175,25 +206,45 @@ TcGemmPlan* MatFreeOperator<S>::plan_for(int N, int np, int bn) {
   return plan;
 }
 
+// The three launch shapes of an application, one parameter at a time: the contraction tile, then the gather
+// tile, then the scatter's column group, each timed as whole nbmax-column applications (gather, contraction and
+// scatter) with the choices made so far.  The three kernels are separate launches whose times add, so this
+// coordinate order finds the best combination of the candidates.  None of the choices changes a result: each
+// output element is summed in the same order whatever the tile.
 template <class S>
-cudaError_t MatFreeOperator<S>::autotune(cudaStream_t s) {
+cudaError_t MatFreeOperator<S>::autotune(cudaStream_t s, const cplx<S>* X, cplx<S>* Y) {
   if (kind != GEMM_TC_BF16) return cudaSuccess;
-  const int N = 2 * w * w * nbmax;
-  const int np = npairs;
-  uint64_t key = 1469598103934665603ull;
-  const long v[] = {1, Mpad, Kpad, Npad, nk, N, np, nslices};
-  for (long x : v)
-    for (int b = 0; b < 8; ++b) {
-      key ^= ((uint64_t)x >> (8 * b)) & 0xffu;
-      key *= 1099511628211ull;
-    }
-  char what[96];
-  std::snprintf(what, sizeof(what), "contraction %dx%dx%d (%d slice products)", nk, N, nk, np);
-  tile_n = tc_autotune(key, what, [&](int bn) -> cudaError_t {
-    TcGemmPlan* plan = plan_for(N, np, bn);
-    return plan ? tc_gemm_run(plan, st, s) : cudaErrorInvalidValue;
+  char shape[160];
+  std::snprintf(shape, sizeof(shape), "matfree nk=%d nv=%d nc=%d w=%d cols=%d slices=%d products=%d", nk, nv, nc, w,
+                nbmax, nslices, npairs);
+  auto run = [&]() -> cudaError_t {
+    const long mv = this->matvec_columns;
+    const cudaError_t e = apply(X, nbmax, 0, nbmax, Y, nbmax, s);
+    this->matvec_columns = mv;
+    return e;
+  };
+  tile_n = tune_choice(shape, "tile_n", {256, 128}, 256, [&](int c) {
+    tile_n = c;
+    return run();
   }, s);
-  return cudaSuccess;
+  // gather tiles: 16 or 8 k' per CTA, chunks of 1, 2 or 4 block columns (those within 200 KB of shared memory)
+  std::vector<int> gt;
+  for (int kt : {16, 8})
+    for (int p : {4, 2, 1})
+      if (p <= nbmax &&
+          (size_t)(kt * nc * w + kt * nv * w + kt * nc * nv * p + kt * nc * w * p) * sizeof(zf) <= 200 * 1024)
+        gt.push_back(kt * 100 + p);
+  gather_tile = tune_choice(shape, "gather_tile", gt, 0, [&](int c) {
+    gather_tile = c;
+    return run();
+  }, s);
+  std::vector<int> sc;
+  for (int g = nbmax; g >= 1 && sc.size() < 3; g = g > 1 ? (g + 1) / 2 : 0) sc.push_back(g);
+  scatter_cols = tune_choice(shape, "scatter_cols", sc, 0, [&](int c) {
+    scatter_cols = c;
+    return run();
+  }, s);
+  return cudaGetLastError();
 }
 
 template struct MatFreeOperator<float>;
@@ -546,10 +597,11 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
   // a ragged layout (row tables present) selects its start vectors per system over the systems' own rows and
   // keeps the padding rows zero; its reductions run over its part table
   const bool ragged = L.bm.rows != nullptr;
-  // reduction parts: about 96 rows each, at most four per SM (the Gram kernel needs the CTAs to hide latency)
-  // reduction parts of the tall-skinny Grams and residual norms: two CTAs per SM at most (each part's FP64
-  // partial of a 48 x 48 Gram is 36 KB, and the sum over parts reads all of them: 608 parts made that sum
-  // about 7 % of a solve)
+  // reduction parts of the tall-skinny Grams and residual norms: parts of 192 rows, at most 304 (each part's
+  // FP64 partial of a 48 x 48 Gram is 36 KB, and the sum over parts reads all of them).  Not autotuned: a part
+  // sums its rows in FP32, so the part count sets the Grams' rounding.  Measured on the 57,600 workload: 304
+  // parts made the Gram pair 0.8 us faster than 300 (63.7 against 64.5 us), and the solve took 12 iterations
+  // instead of 10.  A ragged batch keeps its own part table.
   const int npart = ragged ? L.nparts : std::max(1, std::min(304, (nrow + 191) / 192));
   cudaError_t err = cudaSuccess;
   cplx<S>* Sb = ws.get<cplx<S>>("lob_S", (size_t)nrow * ld, &err, true);

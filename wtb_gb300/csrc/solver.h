@@ -114,7 +114,8 @@ struct DenseOperator : Operator<S> {
   }
 };
 
-enum GemmKind { GEMM_TC_BF16 = 0, GEMM_SIMT_F32 = 1, GEMM_SIMT_F64 = 2 };
+// GEMM_FFT_F32: the contraction as FP32 FFT convolutions over a two-dimensional mesh (k_fftconv.cu)
+enum GemmKind { GEMM_TC_BF16 = 0, GEMM_SIMT_F32 = 1, GEMM_SIMT_F64 = 2, GEMM_FFT_F32 = 3 };
 
 // Event pairs around the contraction launches (enabled by wtb_profile_enable).
 struct KernelProfile {
@@ -155,7 +156,11 @@ struct MatFreeOperator : Operator<S> {
   uint16_t* Zs = nullptr;         // [nslices][Npad][Kpad] bf16
   const S* Vr = nullptr;          // [nk][Kpad] (SIMT)
   S* Zr = nullptr;                // [Npad][Kpad] (SIMT)
-  void* Tm = nullptr;             // [Mpad][Npad] float (TC) or S (SIMT)
+  void* Tm = nullptr;             // [Mpad][Npad] float (TC, FFT) or S (SIMT)
+  // FFT kind: the n1 x n2 mesh, the transform size and the stencil's spectrum and twiddles (k_fftconv.cu)
+  int mesh1 = 0, mesh2 = 0, fft_p = 0;
+  const float2* fft_spec = nullptr;
+  const float2* fft_tw = nullptr;
   DevStatus* st = nullptr;
   KernelProfile* prof = nullptr;
   std::map<long, TcGemmPlan*> plans;  // keyed by (N of the chunk, slice products)
@@ -167,6 +172,9 @@ struct MatFreeOperator : Operator<S> {
   // gather + contraction only: leaves T = V Z(X[:, 0:ncol]) in Tm (row k, column ((b w + o) w + p) 2 + ri,
   // leading dimension Npad; float for the tensor-core kind, S otherwise); ncol <= nbmax
   cudaError_t contract(const cplx<S>* X, int ldx, int ncol, cudaStream_t s);
+  cudaError_t contract_z(int N, cudaStream_t s);
+  double contraction_flops(int N) const;
+  double contraction_bytes(int N) const;
   bool begin_refine() override {
     if (npairs_refine <= npairs) return false;
     npairs = npairs_refine;
@@ -175,11 +183,12 @@ struct MatFreeOperator : Operator<S> {
   void signature(std::vector<uint64_t>* sig) const override {
     const uint64_t v[] = {2, (uint64_t)kind, (uint64_t)nk, (uint64_t)nv, (uint64_t)nc, (uint64_t)w, (uint64_t)nbmax,
                           (uint64_t)nslices, (uint64_t)npairs, (uint64_t)npairs_refine, (uint64_t)kchunk_final,
-                          (uint64_t)tile_n,
+                          (uint64_t)tile_n, (uint64_t)gather_tile, (uint64_t)scatter_cols,
                           (uint64_t)Mpad, (uint64_t)Kpad, (uint64_t)Npad, (uint64_t)(uintptr_t)vec_win,
                           (uint64_t)(uintptr_t)dE, (uint64_t)(uintptr_t)Vs, (uint64_t)(uintptr_t)Zs,
                           (uint64_t)(uintptr_t)Vr, (uint64_t)(uintptr_t)Zr, (uint64_t)(uintptr_t)Tm,
-                          (uint64_t)(uintptr_t)st};
+                          (uint64_t)(uintptr_t)st, (uint64_t)mesh1, (uint64_t)mesh2, (uint64_t)fft_p,
+                          (uint64_t)(uintptr_t)fft_spec, (uint64_t)(uintptr_t)fft_tw};
     sig->insert(sig->end(), v, v + sizeof(v) / sizeof(v[0]));
   }
   // launches the contraction of an ncol-column application (the first phase's slice products) reps times
@@ -194,10 +203,15 @@ struct MatFreeOperator : Operator<S> {
   int kchunk_final = 8;
   bool final_apply = false;
   void set_final(bool on) override { final_apply = on; }
-  // column tile of the contraction (tensor-core kind), chosen by autotune() for the operator's shape
+  // launch shapes chosen by autotune() for the operator's shape (tensor-core kind): the contraction's column
+  // tile, the gather tile (KT * 100 + block columns per chunk; 0 = the shared-memory rule) and the scatter's
+  // block columns per CTA (0 = all that fit)
   int tile_n = 256;
+  int gather_tile = 0;
+  int scatter_cols = 0;
   TcGemmPlan* plan_for(int N, int np, int bn);
-  cudaError_t autotune(cudaStream_t s);
+  // X, Y: row-major dim x nbmax scratch blocks (row stride nbmax) that the timed applications use
+  cudaError_t autotune(cudaStream_t s, const cplx<S>* X, cplx<S>* Y);
 };
 
 struct SolveStats {

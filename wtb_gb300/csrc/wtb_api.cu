@@ -227,10 +227,11 @@ int stage_bands(wtb_ctx* c, int nk, const double* kpt_rm, int nv, int nc) {
   return WTB_OK;
 }
 
-// The split-BF16 (tensor-core) forms take their bands from the mixed band solver (FP32 eigensolve, FP64
-// Rayleigh quotients) and their velocity matrix elements from FP32 Fourier sums: their operator carries
-// about 1e-7 relative error already, and on this GPU those set-up kernels are bound by the FP64 pipe.
-bool tc_form(const wtb_bse_params* p) { return p && p->op == WTB_OP_MATFREE && p->precision >= WTB_PREC_BF16X3; }
+// The reduced-precision matrix-free forms (FP32 and split-BF16) take their bands from the mixed band solver
+// (FP32 eigensolve, FP64 Rayleigh quotients) and their velocity matrix elements from FP32 Fourier sums: their
+// operator carries about 1e-7 relative error already, and on this GPU those set-up kernels are bound by the
+// FP64 pipe (57,600 workload: 1.9 ms for the FP64 bands against 0.7 ms mixed).
+bool reduced_form(const wtb_bse_params* p) { return p && p->op == WTB_OP_MATFREE && p->precision != WTB_PREC_FP64; }
 
 int enqueue_bands(wtb_ctx* c, bool mixed = false) {
   cudaError_t err = cudaSuccess;
@@ -342,6 +343,47 @@ int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob, 
   CKC(err);
   if (!deriv_r0) CKC(launch_transition_energies(c->ws.get<double>("eig_win", 0, &err), nk, nv, nc, dE, c->s));
   const int Kpad = (nk + 63) / 64 * 64, Mpad = (nk + 127) / 128 * 128;
+  // FP32 matrix-free operator on a two-dimensional Monkhorst-Pack mesh: the contraction as FFT convolutions with
+  // the Coulomb stencil (no nk x nk table).  WTB_FFT=0 selects the CUDA-core product instead.
+  const bool mesh2d = c->mesh_mp && p->ngrid[0] == c->ngrid[0] && p->ngrid[1] == c->ngrid[1] &&
+                      p->ngrid[2] == c->ngrid[2] && p->ngrid[2] == 1 && (long)p->ngrid[0] * p->ngrid[1] == nk;
+  const char* fft_env = std::getenv("WTB_FFT");
+  const int fftP = (p->op == WTB_OP_MATFREE && p->precision == WTB_PREC_FP32 && mesh2d &&
+                    !(fft_env && std::strcmp(fft_env, "0") == 0))
+                       ? fft_conv_size(p->ngrid[0], p->ngrid[1])
+                       : 0;
+  if (fftP) {
+    const double* dbl = c->ws.find<double>("recip", 9);
+    if (!dbl) return set_err(c, WTB_ESTATE, "reciprocal vectors not staged");
+    CoulParams cpar = coul_of(c, p);
+    cpar.deriv_r0 = deriv_r0 ? 1 : 0;
+    const int n1 = p->ngrid[0], n2 = p->ngrid[1];
+    double* stn = c->ws.get<double>("vstencil" + tag, (size_t)(2 * n1 - 1) * (2 * n2 - 1), &err);
+    zd* work = c->ws.get<zd>("fft_work", (size_t)(2 * n1 - 1) * fftP, &err);
+    float2* spec = c->ws.get<float2>("fft_spec" + tag, (size_t)fftP * fftP, &err);
+    float2* tw = c->ws.get<float2>("fft_tw", 128, &err);
+    CKC(err);
+    CKC(launch_coulomb_stencil(cpar, dbl, stn, c->s));
+    CKC(launch_fft_spectrum(stn, n1, n2, fftP, work, spec, tw, c->s));
+    const int N = 2 * w * w * nbmax;
+    const int Npad = (N + 255) / 256 * 256;
+    auto op = new MatFreeOperator<float>();
+    ob->o32.reset(op);
+    ob->dE = dE;
+    ob->dim = dim;
+    op->kind = GEMM_FFT_F32;
+    op->nk = nk; op->nv = nv; op->nc = nc; op->w = w; op->nbmax = nbmax;
+    op->vec_win = vec_win; op->dE = dE; op->st = c->st; op->msg = &ob->msg; op->prof = &c->prof;
+    op->Kpad = Kpad; op->Mpad = Mpad; op->Npad = Npad;
+    op->mesh1 = n1; op->mesh2 = n2; op->fft_p = fftP;
+    op->fft_spec = spec; op->fft_tw = tw;
+    op->Zr = c->ws.get<float>("Zr32", (size_t)Npad * Kpad, &err, true);
+    op->Tm = c->ws.get<float>("T32", (size_t)Mpad * Npad, &err);
+    CKC(err);
+    c->last_form = WTB_FORM_FFT_F32;
+    return WTB_OK;
+  }
+  c->last_form = WTB_FORM_NONE;
   double* V = c->ws.get<double>("V" + tag, (size_t)Mpad * Kpad, &err, true);
   CKC(err);
   CKR(coulomb_table_into(c, p, V, Kpad, deriv_r0));
@@ -381,6 +423,7 @@ int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob, 
     op->Zr = c->ws.get<double>("Zr64", (size_t)Npad * Kpad, &err, true);
     op->Tm = c->ws.get<double>("T64", (size_t)Mpad * Npad, &err);
     CKC(err);
+    c->last_form = WTB_FORM_SIMT_F64;
     return WTB_OK;
   }
   auto op = new MatFreeOperator<float>();
@@ -397,6 +440,7 @@ int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob, 
     op->Zr = c->ws.get<float>("Zr32", (size_t)Npad * Kpad, &err, true);
     op->Tm = c->ws.get<float>("T32", (size_t)Mpad * Npad, &err);
     CKC(err);
+    c->last_form = WTB_FORM_SIMT_F32;
     return WTB_OK;
   }
   if (!tc_gemm_available()) return set_err(c, WTB_ENODEV, "the split-BF16 tensor-core path needs an sm_103 device");
@@ -421,8 +465,15 @@ int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob, 
   op->Tm = c->ws.get<float>("Tbf", (size_t)Mpad * Npad, &err);
   CKC(err);
   if (const char* kc = std::getenv("WTB_FINAL_KCHUNK")) op->kchunk_final = std::atoi(kc);
-  // column tile of the contraction: measured once per shape (skipped while a graph is being captured)
-  if (tune) CKC(op->autotune(c->s));
+  // launch shapes of the application: measured once per shape and device (skipped while a graph is being
+  // captured), on two zeroed scratch blocks
+  c->last_form = WTB_FORM_TC_BF16;
+  if (tune) {
+    zf* tx = c->ws.get<zf>("tune_X", (size_t)dim * nbmax, &err, true);
+    zf* ty = c->ws.get<zf>("tune_Y", (size_t)dim * nbmax, &err);
+    CKC(err);
+    CKC(op->autotune(c->s, tx, ty));
+  }
   return WTB_OK;
 }
 
@@ -864,7 +915,7 @@ static int stage_mesh(wtb_ctx* c, const wtb_bse_params* p) {
 
 static int ensure_bands_for(wtb_ctx* c, const wtb_bse_params* p) {
   CKR(stage_mesh(c, p));
-  CKR(enqueue_bands(c, tc_form(p)));
+  CKR(enqueue_bands(c, reduced_form(p)));
   return check_status(c);
 }
 
@@ -873,9 +924,9 @@ static int compute_optics(wtb_ctx* c, const wtb_bse_params* p) {
   const int dim = c->nk * c->nc * c->nv;
   zd* hout = c->ws.get<zd>("hrvel", (size_t)5 * dim, &err);
   CKC(err);
-  // the tensor-core forms: Fourier sums in FP32 over an FP32 copy of H(R)
+  // the reduced-precision matrix-free forms: Fourier sums in FP32 over an FP32 copy of H(R)
   zf* hr32 = nullptr;
-  if (tc_form(p)) {
+  if (reduced_form(p)) {
     const size_t nh = (size_t)c->nR * c->w * c->w;
     hr32 = c->ws.get<zf>("hr32", nh, &err);
     CKC(err);
@@ -1529,7 +1580,7 @@ static int spoptics_impl(wtb_ctx* c, const wtb_bse_params* p, const wtb_temp_par
   CKR(stage_mesh(c, p));
   const double scs0 = c->scs;
   c->scs = scs0 + (tp ? temp_gap_correction(tp) : 0.0);
-  const int rb = enqueue_bands(c, tc_form(p));
+  const int rb = enqueue_bands(c, reduced_form(p));
   c->scs = scs0;
   CKR(rb);
   CKR(check_status(c));
@@ -1629,8 +1680,10 @@ int wtb_bse_matvec(wtb_ctx* c, const wtb_bse_params* p, int ncol, const double* 
 
 long long wtb_kernel_launch_count(void) { return g_launch_count.load(); }
 
+int wtb_operator_form(const wtb_ctx* ctx) { return ctx ? ctx->last_form : WTB_FORM_NONE; }
+
 int wtb_autotune_report(char* buf, int len) {
-  const std::string r = tc_autotune_report();
+  const std::string r = tune_report();
   if (buf && len > 0) {
     const size_t n = std::min((size_t)len - 1, r.size());
     std::memcpy(buf, r.data(), n);
@@ -1675,7 +1728,7 @@ int ctx_stage_system(wtb_ctx* c, const wtb_bse_params* p) {
 }
 
 int ctx_enqueue_system(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob) {
-  CKR(enqueue_bands(c, tc_form(p)));
+  CKR(enqueue_bands(c, reduced_form(p)));
   CKR(compute_optics(c, p));
   return make_operator(c, p, nbmax, ob, "", false, false);
 }

@@ -114,6 +114,17 @@ cudaError_t launch_coulomb(const CoulParams& p, const double* kpt1, int n1, cons
                            double* V, int ldv, cudaStream_t s);
 // The same table on a Monkhorst-Pack mesh from the reciprocal vectors bl (3 x 3 row-major), through the
 // (2n1-1)(2n2-1)(2n3-1) distinct values of k - k' (stencil scratch of that size).
+// the stencil s of a mesh alone: s[(di + n1 - 1) (2 n2 - 1) (2 n3 - 1) + ...] = V at the index difference
+cudaError_t launch_coulomb_stencil(const CoulParams& p, const double* bl, double* stencil, cudaStream_t s);
+// FFT form of the contraction on a two-dimensional mesh (k_fftconv.cu): the transform size P (32, 64 or 128)
+// for an n1 x n2 mesh, or 0 when the mesh is too large; the stencil's spectrum (work: (2 n1 - 1) P complex
+// doubles; spec: P x P; tw: 128 twiddles); T[k][2q + (0, 1)] = (V Z)[k][2q + (0, 1)] for the npairs column
+// pairs of Z (column n at Z + n ldz, k' = i n2 + j)
+int fft_conv_size(int n1, int n2);
+cudaError_t launch_fft_spectrum(const double* stencil, int n1, int n2, int P, zd* work, float2* spec, float2* tw,
+                                cudaStream_t s);
+cudaError_t launch_fft_conv(const float* Z, int ldz, int npairs, int n1, int n2, int P, const float2* spec,
+                            const float2* tw, float* T, int ldt, cudaStream_t s);
 cudaError_t launch_coulomb_mesh(const CoulParams& p, const double* bl, double* stencil, double* V, int ldv,
                                 cudaStream_t s);
 // Transition energies dE[I] = E_c - E_v.
@@ -207,13 +218,16 @@ cudaError_t launch_small_gemm(const zd* A, int lda, int transA, const zd* B, int
                               long a_stride = 0, long b_stride = 0, long c_stride = 0);
 
 // ----------------------------------------------------------------------------- matrix-free operator
-// Z[n][k'] with n = ((b*w + o)*w + p)*2 + ri (K-major for the V*Z contraction).
+// Z[n][k'] with n = ((b*w + o)*w + p)*2 + ri (K-major for the V*Z contraction).  tile (split-BF16 panel only):
+// 0 = the shared-memory rule, else KT * 100 + nbp (KT = 16 or 8 k' per CTA, nbp block columns per chunk).
 template <class S, class Z>
 cudaError_t launch_mf_gather(const cplx<S>* X, int ldx, int c0, int nb, const zd* vec_win, int nk, int nv, int nc,
-                             int w, Z* zt, int ldk, int nslices, long slice_stride, cudaStream_t s);
+                             int w, Z* zt, int ldk, int nslices, long slice_stride, cudaStream_t s, int tile = 0);
+// cols: block columns per CTA (0 = all that fit in 96 KB of shared memory)
 template <class S, class T>
 cudaError_t launch_mf_scatter(const T* Tm, int ldt, const cplx<S>* X, int ldx, const zd* vec_win, const double* dE,
-                              int nk, int nv, int nc, int w, int nb, cplx<S>* Y, int ldy, int c0, cudaStream_t s);
+                              int nk, int nv, int nc, int w, int nb, cplx<S>* Y, int ldy, int c0, cudaStream_t s,
+                              int cols = 0);
 template <class S>
 cudaError_t launch_simt_gemm_tn(const S* A, int lda, const S* B, int ldb, S* C, int ldc, int M, int N, int K,
                                 cudaStream_t s);
@@ -270,10 +284,13 @@ cudaError_t tc_gemm_group_run(TcGroupPlan* plan, int npairs, const int* frozen, 
 cudaError_t tc_gemm_group_run_split(TcGroupPlan* plan, int npairs, const int* frozen, DevStatus* st, cudaStream_t s,
                                     int kb_chunk);
 void tc_gemm_group_destroy(TcGroupPlan* plan);
-// Chooses the column tile (256 or 128) of a contraction shape by timing run(bn) on the caller's stream; cached
-// per key for the process (what: a label for the report).
-int tc_autotune(uint64_t key, const std::string& what, const std::function<cudaError_t(int)>& run, cudaStream_t s);
-std::string tc_autotune_report();
+// autotuner (autotune.cu): the fastest of cands for (shape, param), measured with run(candidate) on stream s the
+// first time the pair is seen on this device and build (or read from the JSON cache); dflt while s is capturing
+int tune_choice(const std::string& shape, const char* param, const std::vector<int>& cands, int dflt,
+                const std::function<cudaError_t(int)>& run, cudaStream_t s);
+// {"build": source hash, "cache": file or null, "choices": [{shape, param, choice, source, ms}, ...]} (JSON)
+std::string tune_report();
+std::string tune_cache_path();
 
 // ----------------------------------------------------------------------------- spectrum
 cudaError_t launch_oscillators(const zd* A, int lda, int nev, int dim, const zd* hr, double* osc /*[8][nev]*/,
