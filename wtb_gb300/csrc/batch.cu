@@ -215,7 +215,7 @@ int build_graph(wtb_batch* b, int nsys, const wtb_bse_params* p, std::string* ms
   b->nev = nevmax;
   b->m = ctx_auto_block(&pm, mindim, false);
   const int nbmax = std::min(b->m, 16);
-  const double tol_final = p[0].tol > 0 ? p[0].tol : 1e-5;
+  const double tol_final = p[0].tol > 0 ? p[0].tol : kReducedTol;
   // two phases in every form (see run_solve): to 1e-4, then from the best block with a fresh operator
   // application (and 6 slice products for bf16x3) to the target
   b->tol = std::max(tol_final, 1e-4);

@@ -265,6 +265,69 @@ __global__ void __launch_bounds__(256) update_kernel(const cplx<S>* __restrict__
   }
 }
 
+// The projections of one iteration in one pass: W -= X T_W, P -= X T_P and AP -= AX T_P, with T_W = T[:, 0:m] and
+// T_P = T[:, m:2m] of T = X^H [W P] (m x 2m).  A CTA stages a row tile of X and AX and both coefficient blocks in
+// shared memory; each output keeps update_kernel's arithmetic (the sum over i in order, then old minus it), so
+// the results are bitwise those of three update_kernel launches.
+template <class S>
+__global__ void __launch_bounds__(256) orth_update_kernel(const cplx<S>* __restrict__ X, const cplx<S>* __restrict__ AX,
+                                                          int ld, int m, const zd* __restrict__ T,
+                                                          cplx<S>* __restrict__ W, cplx<S>* __restrict__ P,
+                                                          cplx<S>* __restrict__ AP, int nrow, BatchMap bm,
+                                                          long t_stride) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int RS = m + 1;                                // padded row of the staged blocks
+  cplx<S>* Tw = reinterpret_cast<cplx<S>*>(smem_raw);  // [m][m]
+  cplx<S>* Tp = Tw + m * m;                            // [m][m]
+  cplx<S>* Xs = Tp + m * m;                            // [kTileRows][RS]
+  cplx<S>* As = Xs + kTileRows * RS;                   // [kTileRows][RS]
+  const int tid = threadIdx.x;
+  const long ntile = ((long)nrow + kTileRows - 1) / kTileRows;
+  int staged = -1;
+  for (long t = blockIdx.x; t < ntile; t += gridDim.x) {
+    const int sys = bm_sys_of_row(bm, t * kTileRows);  // uniform over the CTA
+    if (bm_frozen(bm, sys)) continue;
+    __syncthreads();  // the previous tile's reads are done
+    if (sys != staged) {
+      const zd* Tq = T + (size_t)sys * t_stride;
+      for (int e = tid; e < m * m; e += blockDim.x) {
+        const int i = e / m, j = e - i * m;
+        const zd a = Tq[(size_t)i * 2 * m + j], b = Tq[(size_t)i * 2 * m + m + j];
+        Tw[e] = mk<S>((S)a.re, (S)a.im);
+        Tp[e] = mk<S>((S)b.re, (S)b.im);
+      }
+      staged = sys;
+    }
+    const long r0 = t * kTileRows;
+    const int nr = (int)min((long)kTileRows, nrow - r0);
+    for (int e = tid; e < nr * m; e += blockDim.x) {
+      const int rr = e / m, i = e - rr * m;
+      Xs[rr * RS + i] = X[(r0 + rr) * ld + i];
+      As[rr * RS + i] = AX[(r0 + rr) * ld + i];
+    }
+    __syncthreads();
+    for (int e = tid; e < nr * m; e += blockDim.x) {
+      const int rr = e / m, j = e - rr * m;
+      const cplx<S>* xr = Xs + rr * RS;
+      const cplx<S>* ar = As + rr * RS;
+      cplx<S> aw = mk<S>(0, 0), ap = mk<S>(0, 0), aa = mk<S>(0, 0);
+      for (int i = 0; i < m; ++i) {
+        const cplx<S> xi = xr[i], tw = Tw[i * m + j], tp = Tp[i * m + j];
+        cfma(aw, xi, tw);
+        cfma(ap, xi, tp);
+        cfma(aa, ar[i], tp);
+      }
+      const long r = r0 + rr;
+      cplx<S>* ow = W + r * ld + j;
+      cplx<S>* op = P + r * ld + j;
+      cplx<S>* oa = AP + r * ld + j;
+      *ow = mk<S>(ow->re - aw.re, ow->im - aw.im);
+      *op = mk<S>(op->re - ap.re, op->im - ap.im);
+      *oa = mk<S>(oa->re - aa.re, oa->im - aa.im);
+    }
+  }
+}
+
 // ----------------------------------------------------------------------------- residual and preconditioner
 template <class S>
 __global__ void __launch_bounds__(256) residual_kernel(const cplx<S>* __restrict__ AX, int ldax,
@@ -721,6 +784,20 @@ cudaError_t launch_update(const cplx<S>* Sx, int lds, int nin, const zd* C, int 
 }
 
 template <class S>
+cudaError_t launch_orth_update(const cplx<S>* X, const cplx<S>* AX, int ld, int m, const zd* T, cplx<S>* W,
+                               cplx<S>* P, cplx<S>* AP, int nrow, cudaStream_t s, const BatchMap& bm, long t_stride) {
+  if (m < 1 || m > 32) return cudaErrorInvalidValue;
+  const size_t smem = (size_t)(2 * m * m + 2 * kTileRows * (m + 1)) * sizeof(cplx<S>);
+  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(orth_update_kernel<S>), smem);
+  if (e != cudaSuccess) return e;
+  long nblk = ((long)nrow + kTileRows - 1) / kTileRows;
+  if (nblk > 152 * 16) nblk = 152 * 16;
+  orth_update_kernel<S><<<(unsigned)nblk, 256, smem, s>>>(X, AX, ld, m, T, W, P, AP, nrow, bm, t_stride);
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
+template <class S>
 cudaError_t launch_residual(const cplx<S>* AX, int ldax, const cplx<S>* X, int ldx, const double* theta, int m,
                             int nrow, cplx<S>* R, int ldr, double* partial, int npart, double* norms2, cudaStream_t s,
                             const BatchMap& bm, long theta_stride) {
@@ -851,6 +928,8 @@ cudaError_t launch_init_guess(cplx<S>* X, int ldx, int nrow, int m, const int* i
                                            cudaStream_t, const BatchMap&, long);                                   \
   template cudaError_t launch_update<S>(const cplx<S>*, int, int, const zd*, int, int, int, cplx<S>*, int, double, \
                                         double, cudaStream_t, const BatchMap&, long);                             \
+  template cudaError_t launch_orth_update<S>(const cplx<S>*, const cplx<S>*, int, int, const zd*, cplx<S>*,        \
+                                             cplx<S>*, cplx<S>*, int, cudaStream_t, const BatchMap&, long);       \
   template cudaError_t launch_residual<S>(const cplx<S>*, int, const cplx<S>*, int, const double*, int, int,       \
                                           cplx<S>*, int, double*, int, double*, cudaStream_t, const BatchMap&,     \
                                           long);                                                                   \

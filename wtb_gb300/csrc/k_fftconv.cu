@@ -216,11 +216,12 @@ __device__ __forceinline__ void fft_inv(float2 (&x)[16], int r, float2* scr, con
 
 constexpr int kFftThreads = 256;
 
+// t_kn: T as [k][ldt] rows (column pair 2q, 2q + 1 of row k); otherwise T as [n][ldt] rows like Z
 template <int P>
 __global__ void __launch_bounds__(kFftThreads, 2) fft_conv_kernel(const float* __restrict__ Z, int ldz, int n1, int n2,
                                                                   const float2* __restrict__ spec,
                                                                   const float2* __restrict__ tw_g,
-                                                                  float* __restrict__ T, int ldt) {
+                                                                  float* __restrict__ T, int ldt, int t_kn) {
   constexpr int G = P / 16, TT = 16 / G, NG = kFftThreads / G, LDS = P + 1, TS = 128 / P;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* scr_all = reinterpret_cast<float2*>(smem_raw);  // [NG][G * kScr]
@@ -286,7 +287,6 @@ __global__ void __launch_bounds__(kFftThreads, 2) fft_conv_kernel(const float* _
   }
   __syncthreads();
   // C. inverse row transforms (as conj(DFT(conj(.)))), the mesh's n2 outputs of each row to T
-  float* tq = T + 2 * q;
   for (int i0 = 0; i0 < n1; i0 += NG) {
     const int i = i0 + g;
     const bool act = i < n1;
@@ -295,13 +295,39 @@ __global__ void __launch_bounds__(kFftThreads, 2) fft_conv_kernel(const float* _
     for (int m = 0; m < 16; ++m) x[m] = act ? conj2(Sb[i * LDS + r + G * m]) : zero;
     fft_fwd<P>(x, r, scr, tw);
     if (act) {
+      if (t_kn) {  // T[k][2q + (0, 1)]: one 8-byte (re, im) store per output
+        float* tq = T + 2 * q;
 #pragma unroll
-      for (int t = 0; t < TT; ++t)
+        for (int t = 0; t < TT; ++t)
 #pragma unroll
-        for (int k1 = 0; k1 < G; ++k1) {
-          const int j = r * TT + t + 16 * k1;
-          if (j < n2) *reinterpret_cast<float2*>(tq + (size_t)(i * n2 + j) * ldt) = conj2(x[t * G + k1]);
-        }
+          for (int k1 = 0; k1 < G; ++k1) {
+            const int j = r * TT + t + 16 * k1;
+            if (j < n2) *reinterpret_cast<float2*>(tq + (size_t)(i * n2 + j) * ldt) = conj2(x[t * G + k1]);
+          }
+      } else {  // rows of Z's layout, T[2q][k] and T[2q + 1][k]: a lane's outputs j, j + 1 are adjacent
+        float* tre = T + (size_t)(2 * q) * ldt + i * n2;
+        float* tim = tre + ldt;
+#pragma unroll
+        for (int t = 0; t < TT; t += 2)
+#pragma unroll
+          for (int k1 = 0; k1 < G; ++k1) {
+            const int j = r * TT + t + 16 * k1;  // even
+            const float2 a = conj2(x[t * G + k1]), b = conj2(x[(t + 1) * G + k1]);
+            if (((i * n2) & 1) == 0 && j + 1 < n2) {
+              *reinterpret_cast<float2*>(tre + j) = c2(a.x, b.x);
+              *reinterpret_cast<float2*>(tim + j) = c2(a.y, b.y);
+            } else {
+              if (j < n2) {
+                tre[j] = a.x;
+                tim[j] = a.y;
+              }
+              if (j + 1 < n2) {
+                tre[j + 1] = b.x;
+                tim[j + 1] = b.y;
+              }
+            }
+          }
+      }
     }
   }
 }
@@ -395,29 +421,30 @@ cudaError_t launch_fft_spectrum(const double* stencil, int n1, int n2, int P, zd
 }
 
 cudaError_t launch_fft_conv(const float* Z, int ldz, int npairs, int n1, int n2, int P, const float2* spec,
-                            const float2* tw, float* T, int ldt, cudaStream_t s) {
+                            const float2* tw, float* T, int ldt, bool t_kn, cudaStream_t s) {
   if (npairs < 1) return cudaSuccess;
   if (2 * n1 - 1 > P || 2 * n2 - 1 > P || (ldt & 1)) return cudaErrorInvalidValue;
+  const int kn = t_kn ? 1 : 0;
   switch (P) {
     case 32: {
       const size_t smem = conv_smem<32>(n1);
       cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(fft_conv_kernel<32>), smem);
       if (e != cudaSuccess) return e;
-      fft_conv_kernel<32><<<npairs, kFftThreads, smem, s>>>(Z, ldz, n1, n2, spec, tw, T, ldt);
+      fft_conv_kernel<32><<<npairs, kFftThreads, smem, s>>>(Z, ldz, n1, n2, spec, tw, T, ldt, kn);
       break;
     }
     case 64: {
       const size_t smem = conv_smem<64>(n1);
       cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(fft_conv_kernel<64>), smem);
       if (e != cudaSuccess) return e;
-      fft_conv_kernel<64><<<npairs, kFftThreads, smem, s>>>(Z, ldz, n1, n2, spec, tw, T, ldt);
+      fft_conv_kernel<64><<<npairs, kFftThreads, smem, s>>>(Z, ldz, n1, n2, spec, tw, T, ldt, kn);
       break;
     }
     case 128: {
       const size_t smem = conv_smem<128>(n1);
       cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(fft_conv_kernel<128>), smem);
       if (e != cudaSuccess) return e;
-      fft_conv_kernel<128><<<npairs, kFftThreads, smem, s>>>(Z, ldz, n1, n2, spec, tw, T, ldt);
+      fft_conv_kernel<128><<<npairs, kFftThreads, smem, s>>>(Z, ldz, n1, n2, spec, tw, T, ldt, kn);
       break;
     }
     default:

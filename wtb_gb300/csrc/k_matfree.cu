@@ -126,8 +126,11 @@ __device__ __forceinline__ void gather_bf16_tile(const zf* __restrict__ X, int l
   zf* xs = Vs + KT * nv * w;                 // [KT][ncv][nbp]
   zf* Y1 = xs + KT * ncv * nbp;              // [KT][nc][w][nbp]
   const int tid = threadIdx.x, nt = blockDim.x;
+  // index quotients by the runtime extents through qdiv (all numerators < 2^21)
+  const float r_w = 1.0f / w, r_nbnd = 1.0f / nbnd, r_ncv = 1.0f / ncv, r_nc = 1.0f / nc;
   for (int e = tid; e < KT * nbnd * w; e += nt) {
-    const int kk = e / (nbnd * w), sb = (e / w) % nbnd, o = e % w;
+    const int q = qdiv(e, r_w), o = e - q * w;  // q = kk * nbnd + sb
+    const int kk = qdiv(q, r_nbnd), sb = q - kk * nbnd;
     zd a = mk<double>(0.0, 0.0);
     if (kk < tkn) a = vec_win[((size_t)(kt0 + kk) * nbnd + sb) * w + o];
     const zf as = mk<float>((float)a.re, (float)a.im);
@@ -140,16 +143,18 @@ __device__ __forceinline__ void gather_bf16_tile(const zf* __restrict__ X, int l
     const int b0 = blockIdx.y * nbp;
     const int nbl = min(nbp, nbc - b0);
     if (nbl <= 0) return;  // uniform over the CTA
+    const float r_nbl = 1.0f / nbl;
     for (int e = tid; e < KT * ncv * nbl; e += nt) {
-      const int bb = e % nbl, r = e / nbl;  // r = kk * ncv + cv
-      const int kk = r / ncv;
+      const int r = qdiv(e, r_nbl), bb = e - r * nbl;  // r = kk * ncv + cv
+      const int kk = qdiv(r, r_ncv);
       xs[r * nbp + bb] = kk < tkn ? X[((size_t)kt0 * ncv + r) * ldx + c0 + b0 + bb] : mk<float>(0.f, 0.f);
     }
     __syncthreads();
     // Y1[kk][c][p][bb] = sum_v Vb[kk][v][p] x[kk][c][v][bb]
     for (int e = tid; e < KT * nc * w * nbl; e += nt) {
-      const int bb = e % nbl, q = e / nbl;  // q = (kk * nc + c) * w + p
-      const int p = q % w, c = (q / w) % nc, kk = q / (w * nc);
+      const int q = qdiv(e, r_nbl), bb = e - q * nbl;  // q = (kk * nc + c) * w + p
+      const int kc = qdiv(q, r_w), p = q - kc * w;       // kc = kk * nc + c
+      const int kk = qdiv(kc, r_nc), c = kc - kk * nc;
       zf acc = mk<float>(0.f, 0.f);
       for (int v = 0; v < nv; ++v) cfma(acc, Vs[(kk * nv + v) * w + p], xs[(kk * ncv + c * nv + v) * nbp + bb]);
       Y1[q * nbp + bb] = acc;
@@ -158,7 +163,7 @@ __device__ __forceinline__ void gather_bf16_tile(const zf* __restrict__ X, int l
     // items (bb, o, p), bb fastest across lanes (Y1 reads are then consecutive in shared memory): Z over the
     // tile's KT k', re and im rows, every slice
     for (int it = tid; it < nbl * ww; it += nt) {
-      const int bb = it % nbl, op = it / nbl, o = op / w, p = op % w;
+      const int op = qdiv(it, r_nbl), bb = it - op * nbl, o = qdiv(op, r_w), p = op - o * w;
       float zr[KT], zi[KT];
 #pragma unroll
       for (int kk = 0; kk < KT; ++kk) {
@@ -261,16 +266,18 @@ __device__ __forceinline__ void scatter_k(const T* __restrict__ Tm, int ldt, con
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int nbl = min(nbg, nb - b0);
   const int nbnd = nv + nc, ncv = nc * nv;
-  // shared rows are padded by one element (U: one complex per column b, Ts: one value per (b, o) row) so that
-  // the strided reads of both products hit distinct banks
-  const int us = w * nv + 1, ts = 2 * w + 1;
+  // U rows padded by one complex per column b; T rows of 2w values padded to 2w + 2, so that the eight (b, o) rows
+  // a warp reads at one p fall in distinct bank pairs and every (re, im) pair is one 8-byte load.  Index
+  // quotients by the runtime extents go through qdiv (all numerators < 2^21).
+  const int us = w * nv + 1, tw = 2 * w, ts = tw + 2;
   cplx<S>* Cs = reinterpret_cast<cplx<S>*>(smem_raw);  // [nc][w]
   cplx<S>* Vs = Cs + nc * w;                           // [nv][w]
   cplx<S>* U = Vs + nv * w;                            // [nbg][us]: U[b][o][v] at b * us + o * nv + v
   T* Ts = reinterpret_cast<T*>(U + nbg * us);          // [nbg][w][ts]: T[b][o][p][ri] at (b * w + o) * ts + 2p + ri
   const int tid = threadIdx.x, nt = blockDim.x;
+  const float r_w = 1.0f / w, r_nv = 1.0f / nv, r_nbl = 1.0f / nbl;
   for (int e = tid; e < nbnd * w; e += nt) {
-    const int s = e / w, o = e % w;
+    const int s = qdiv(e, r_w), o = e - s * w;
     const zd a = vec_win[((size_t)k * nbnd + s) * w + o];
     const cplx<S> as = mk<S>((S)a.re, (S)a.im);
     if (s < nv)
@@ -278,43 +285,56 @@ __device__ __forceinline__ void scatter_k(const T* __restrict__ Tm, int ldt, con
     else
       Cs[(s - nv) * w + o] = as;
   }
-  const int row = nbl * w * w * 2, tw = 2 * w;
-  const T* trow = Tm + (size_t)k * ldt + (size_t)b0 * w * w * 2;
+  const int row = nbl * w * tw;
+  const T* trow = Tm + (size_t)k * ldt + (size_t)b0 * w * tw;
   if constexpr (sizeof(T) == 4) {
-    // 16-byte loads when the row segment allows (row starts and lengths are multiples of 4 floats)
-    if ((reinterpret_cast<uintptr_t>(trow) & 15) == 0 && (row & 3) == 0) {
+    // 16-byte loads when the row segment allows (its start a multiple of 16 bytes, w even so that a load stays
+    // within one (b, o) row of 2w values), each stored as two 8-byte pairs
+    if ((reinterpret_cast<uintptr_t>(trow) & 15) == 0 && (w & 1) == 0) {
       const float4* t4 = reinterpret_cast<const float4*>(trow);
+      const int hw = w >> 1;  // 16-byte loads per (b, o) row
+      const float r_hw = 1.0f / hw;
       for (int e = tid; e < row / 4; e += nt) {
         const float4 v4 = t4[e];
-        const float vv[4] = {v4.x, v4.y, v4.z, v4.w};
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int f = 4 * e + q;
-          Ts[(f / tw) * ts + f % tw] = vv[q];
-        }
+        const int r = qdiv(e, r_hw), c = (e - r * hw) * 4;
+        float2* d = reinterpret_cast<float2*>(Ts + r * ts + c);
+        d[0] = make_float2(v4.x, v4.y);
+        d[1] = make_float2(v4.z, v4.w);
       }
     } else {
-      for (int f = tid; f < row; f += nt) Ts[(f / tw) * ts + f % tw] = trow[f];
+      const float r_tw = 1.0f / tw;
+      for (int f = tid; f < row; f += nt) {
+        const int r = qdiv(f, r_tw);
+        Ts[r * ts + f - r * tw] = trow[f];
+      }
     }
   } else {
-    for (int f = tid; f < row; f += nt) Ts[(f / tw) * ts + f % tw] = trow[f];
+    const float r_tw = 1.0f / tw;
+    for (int f = tid; f < row; f += nt) {
+      const int r = qdiv(f, r_tw);
+      Ts[r * ts + f - r * tw] = trow[f];
+    }
   }
   __syncthreads();
   // U[b][o][v] = sum_p conj(Vb[v][p]) T[b][o][p]
   for (int e = tid; e < nbl * w * nv; e += nt) {
-    const int bb = e / (w * nv), o = (e / nv) % w, v = e % nv;
+    const int q = qdiv(e, r_nv), v = e - q * nv;  // q = bb * w + o
     cplx<S> acc = mk<S>(0, 0);
-    const T* tp = Ts + ((size_t)bb * w + o) * ts;
-    for (int p = 0; p < w; ++p) cfmac(acc, Vs[v * w + p], mk<S>((S)tp[2 * p], (S)tp[2 * p + 1]));
+    const T* tp = Ts + (size_t)q * ts;
+    const cplx<S>* vr = Vs + v * w;
+    for (int p = 0; p < w; ++p) cfmac(acc, vr[p], mk<S>((S)tp[2 * p], (S)tp[2 * p + 1]));
+    const int bb = qdiv(q, r_w), o = q - bb * w;
     U[bb * us + o * nv + v] = acc;
   }
   __syncthreads();
   // y[c][v][b] = dE x + sum_o conj(C[c][o]) U[b][o][v]
   for (int e = tid; e < ncv * nbl; e += nt) {
-    const int cv = e / nbl, bb = e % nbl;
-    const int c = cv / nv, v = cv % nv;
+    const int cv = qdiv(e, r_nbl), bb = e - cv * nbl;
+    const int c = qdiv(cv, r_nv), v = cv - c * nv;
     cplx<S> acc = mk<S>(0, 0);
-    for (int o = 0; o < w; ++o) cfmac(acc, Cs[c * w + o], U[bb * us + o * nv + v]);
+    const cplx<S>* cr = Cs + c * w;
+    const cplx<S>* ur = U + bb * us + v;
+    for (int o = 0; o < w; ++o) cfmac(acc, cr[o], ur[o * nv]);
     const size_t I = (size_t)k * ncv + cv;
     const cplx<S> x = X[I * ldx + c0 + b0 + bb];
     const S d = (S)dE[I];
@@ -331,6 +351,89 @@ __global__ void __launch_bounds__(128) mf_scatter_kernel(const T* __restrict__ T
                                                          int nk, int nv, int nc, int w, int nb, int nbg,
                                                          cplx<S>* __restrict__ Y, int ldy, int c0) {
   scatter_k<S, T>(Tm, ldt, X, ldx, vec_win, dE, nk, nv, nc, w, nb, nbg, Y, ldy, c0, blockIdx.x, blockIdx.y * nbg);
+}
+
+// Scatter from T in Z's layout, T[n][k] (the FFT form): a CTA takes a tile of kScatK consecutive k-points and
+// nbg block columns.  It reads each of its T rows' kScatK values (32 bytes, one sector) at once and stages them
+// as Ts[kk][(b w + o) (2w + 2) + 2p + ri] (rows padded as in mf_scatter), then forms U and y for every k-point
+// of the tile with the same sums, in the same order, as mf_scatter.
+constexpr int kScatK = 8;
+__global__ void __launch_bounds__(256) mf_scatter_t_kernel(const float* __restrict__ Tt, int ldt,
+                                                           const zf* __restrict__ X, int ldx,
+                                                           const zd* __restrict__ vec_win,
+                                                           const double* __restrict__ dE, int nk, int nv, int nc,
+                                                           int w, int nb, int nbg, zf* __restrict__ Y, int ldy,
+                                                           int c0) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int k0 = blockIdx.x * kScatK, kn = min(kScatK, nk - k0);
+  const int b0 = blockIdx.y * nbg, nbl = min(nbg, nb - b0);
+  const int nbnd = nv + nc, ncv = nc * nv, tw = 2 * w, ts = tw + 2, us = w * nv + 1;
+  const int nrow = nbl * w;  // (b, o) rows per k-point
+  zf* Cs = reinterpret_cast<zf*>(smem_raw);             // [kScatK][nc][w]
+  zf* Vs = Cs + kScatK * nc * w;                        // [kScatK][nv][w]
+  zf* U = Vs + kScatK * nv * w;                         // [kScatK][nbg][us]
+  float* Ts = reinterpret_cast<float*>(U + kScatK * nbg * us);  // [kScatK][nbg w][ts]
+  const int TSK = nbg * w * ts;                         // floats per k-point
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const float r_w = 1.0f / w, r_nbnd = 1.0f / nbnd, r_tw = 1.0f / tw, r_nv = 1.0f / nv, r_nrow = 1.0f / nrow,
+              r_nbl = 1.0f / nbl, r_ncv = 1.0f / ncv;
+  for (int e = tid; e < kScatK * nbnd * w; e += nt) {
+    const int q = qdiv(e, r_w), o = e - q * w;  // q = kk * nbnd + sb
+    const int kk = qdiv(q, r_nbnd), sb = q - kk * nbnd;
+    zd a = mk<double>(0.0, 0.0);
+    if (kk < kn) a = vec_win[((size_t)(k0 + kk) * nbnd + sb) * w + o];
+    const zf as = mk<float>((float)a.re, (float)a.im);
+    if (sb < nv)
+      Vs[(kk * nv + sb) * w + o] = as;
+    else
+      Cs[(kk * nc + sb - nv) * w + o] = as;
+  }
+  // T rows n = b0 2w^2 + nl: kScatK values at Tt[n ldt + k0] (ldt a multiple of 64, k0 of 8: 32-byte aligned;
+  // values past nk are padding, staged and never used)
+  const float* tbase = Tt + (size_t)b0 * w * tw * ldt + k0;
+  for (int nl = tid; nl < nrow * tw; nl += nt) {
+    const float4* src = reinterpret_cast<const float4*>(tbase + (size_t)nl * ldt);
+    const float4 a = src[0], b = src[1];
+    const int row = qdiv(nl, r_tw), c = nl - row * tw;  // row = b w + o, c = 2p + ri
+    float* d = Ts + row * ts + c;
+    d[0] = a.x;
+    d[TSK] = a.y;
+    d[2 * TSK] = a.z;
+    d[3 * TSK] = a.w;
+    d[4 * TSK] = b.x;
+    d[5 * TSK] = b.y;
+    d[6 * TSK] = b.z;
+    d[7 * TSK] = b.w;
+  }
+  __syncthreads();
+  // U[kk][b][o][v] = sum_p conj(Vb[kk][v][p]) T[kk][b][o][p]
+  for (int e = tid; e < kn * nrow * nv; e += nt) {
+    const int q = qdiv(e, r_nv), v = e - q * nv;  // q = kk nrow + (b w + o)
+    const int kk = qdiv(q, r_nrow), ro = q - kk * nrow;
+    const float* tp = Ts + kk * TSK + ro * ts;
+    const zf* vr = Vs + (kk * nv + v) * w;
+    zf acc = mk<float>(0.f, 0.f);
+    for (int p = 0; p < w; ++p) cfmac(acc, vr[p], mk<float>(tp[2 * p], tp[2 * p + 1]));
+    const int bb = qdiv(ro, r_w), o = ro - bb * w;
+    U[(kk * nbg + bb) * us + o * nv + v] = acc;
+  }
+  __syncthreads();
+  // y[k][c][v][b] = dE x + sum_o conj(C[k][c][o]) U[k][b][o][v]
+  for (int e = tid; e < kn * ncv * nbl; e += nt) {
+    const int q = qdiv(e, r_nbl), bb = e - q * nbl;  // q = kk ncv + cv
+    const int kk = qdiv(q, r_ncv), cv = q - kk * ncv;
+    const int c = qdiv(cv, r_nv), v = cv - c * nv;
+    const zf* cr = Cs + (kk * nc + c) * w;
+    const zf* ur = U + (kk * nbg + bb) * us + v;
+    zf acc = mk<float>(0.f, 0.f);
+    for (int o = 0; o < w; ++o) cfmac(acc, cr[o], ur[o * nv]);
+    const size_t I = (size_t)(k0 + kk) * ncv + cv;
+    const zf x = X[I * ldx + c0 + b0 + bb];
+    const float d = (float)dE[I];
+    acc.re += d * x.re;
+    acc.im += d * x.im;
+    Y[I * ldy + c0 + b0 + bb] = acc;
+  }
 }
 
 // batch: CTA (b, g) takes k-point kpts[b] = (system, k) and column group g
@@ -509,7 +612,7 @@ cudaError_t launch_mf_scatter(const T* Tm, int ldt, const cplx<S>* X, int ldx, c
   // block columns per CTA: all (or the requested count), halved until the CTA's tiles fit in 96 KB
   int nbg = cols > 0 ? std::min(cols, nb) : nb;
   auto smem_of = [&](int g) {
-    return (size_t)((nc + nv) * w + g * (w * nv + 1)) * sizeof(cplx<S>) + (size_t)g * w * (2 * w + 1) * sizeof(T) + 16;
+    return (size_t)((nc + nv) * w + g * (w * nv + 1)) * sizeof(cplx<S>) + (size_t)g * w * (2 * w + 2) * sizeof(T) + 16;
   };
   while (nbg > 1 && smem_of(nbg) > 96 * 1024) nbg = (nbg + 1) / 2;
   const size_t smem = smem_of(nbg);
@@ -517,6 +620,26 @@ cudaError_t launch_mf_scatter(const T* Tm, int ldt, const cplx<S>* X, int ldx, c
   if (e != cudaSuccess) return e;
   dim3 grid(nk, (nb + nbg - 1) / nbg);
   mf_scatter_kernel<S, T><<<grid, 128, smem, s>>>(Tm, ldt, X, ldx, vec_win, dE, nk, nv, nc, w, nb, nbg, Y, ldy, c0); ++g_launch_count;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mf_scatter_t(const float* Tt, int ldt, const zf* X, int ldx, const zd* vec_win, const double* dE,
+                                int nk, int nv, int nc, int w, int nb, zf* Y, int ldy, int c0, cudaStream_t s,
+                                int cols) {
+  if (ldt % 64 != 0 || (reinterpret_cast<uintptr_t>(Tt) & 31) != 0) return cudaErrorInvalidValue;
+  int nbg = std::min(cols > 0 ? cols : 4, nb);
+  auto smem_of = [&](int g) {
+    return (size_t)kScatK * ((nc + nv) * w + g * (w * nv + 1)) * sizeof(zf) +
+           (size_t)kScatK * g * w * (2 * w + 2) * sizeof(float);
+  };
+  while (nbg > 1 && smem_of(nbg) > 160 * 1024) nbg = (nbg + 1) / 2;
+  const size_t smem = smem_of(nbg);
+  if (smem > 200 * 1024) return cudaErrorInvalidValue;
+  cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(mf_scatter_t_kernel), smem);
+  if (e != cudaSuccess) return e;
+  mf_scatter_t_kernel<<<dim3((nk + kScatK - 1) / kScatK, (nb + nbg - 1) / nbg), 256, smem, s>>>(
+      Tt, ldt, X, ldx, vec_win, dE, nk, nv, nc, w, nb, nbg, Y, ldy, c0);
+  ++g_launch_count;
   return cudaGetLastError();
 }
 
@@ -551,7 +674,7 @@ cudaError_t launch_mf_scatter_batch(const zf* X, int ldx, const MfSys* sys, cons
                                     cudaStream_t s) {
   int nbg = nb;
   auto smem_of = [&](int g) {
-    return (size_t)((max_nc + max_nv) * w + g * (w * max_nv + 1)) * sizeof(zf) + (size_t)g * w * (2 * w + 1) * sizeof(float) +
+    return (size_t)((max_nc + max_nv) * w + g * (w * max_nv + 1)) * sizeof(zf) + (size_t)g * w * (2 * w + 2) * sizeof(float) +
            16;
   };
   while (nbg > 1 && smem_of(nbg) > 96 * 1024) nbg = (nbg + 1) / 2;

@@ -84,7 +84,7 @@ cudaError_t MatFreeOperator<S>::apply(const cplx<S>* X, int ldx, int c0, int nco
         cudaEventCreate(&eb);
         cudaEventRecord(ea, s);
       }
-      e = contract_z(N, s);
+      e = contract_z(N, s, false);
       if (e != cudaSuccess) return e;
       if (profiled) {
         cudaEventRecord(eb, s);
@@ -93,8 +93,14 @@ cudaError_t MatFreeOperator<S>::apply(const cplx<S>* X, int ldx, int c0, int nco
         prof->flops += contraction_flops(N);
         prof->bytes += contraction_bytes(N);
       }
-      e = launch_mf_scatter<S, S>(reinterpret_cast<const S*>(Tm), Npad, X, ldx, vec_win, dE, nk, nv, nc, w, nb, Y, ldy,
-                                  c0 + b0, s);
+      if (kind == GEMM_FFT_F32) {
+        if constexpr (sizeof(S) == 4)
+          e = launch_mf_scatter_t(reinterpret_cast<const float*>(Tm), Kpad, X, ldx, vec_win, dE, nk, nv, nc, w, nb, Y,
+                                  ldy, c0 + b0, s, scatter_cols);
+      } else {
+        e = launch_mf_scatter<S, S>(reinterpret_cast<const S*>(Tm), Npad, X, ldx, vec_win, dE, nk, nv, nc, w, nb, Y,
+                                    ldy, c0 + b0, s);
+      }
       if (e != cudaSuccess) return e;
     }
   }
@@ -121,7 +127,7 @@ cudaError_t MatFreeOperator<S>::time_contraction(int reps, int ncol, cudaStream_
     if (plan)
       e = tc_gemm_run(plan, st, s);
     else
-      e = contract_z(N, s);
+      e = contract_z(N, s, false);
     if (e != cudaSuccess) return e;
     cudaEventRecord(eb, s);
     prof->pending.emplace_back(ea, eb);
@@ -155,16 +161,18 @@ cudaError_t MatFreeOperator<S>::contract(const cplx<S>* X, int ldx, int ncol, cu
   }
   cudaError_t e = launch_mf_gather<S, S>(X, ldx, 0, ncol, vec_win, nk, nv, nc, w, Zr, Kpad, 1, 0, s);
   if (e != cudaSuccess) return e;
-  return contract_z(N, s);
+  return contract_z(N, s, true);
 }
 
 // T = V Z for the N gathered columns in Zr: FP32 FFT convolutions (FFT kind) or the CUDA-core product
 template <class S>
-cudaError_t MatFreeOperator<S>::contract_z(int N, cudaStream_t s) {
+cudaError_t MatFreeOperator<S>::contract_z(int N, cudaStream_t s, bool t_kn) {
   if (kind == GEMM_FFT_F32) {
+    // contract() leaves T[k][n] (row k, leading dimension Npad) as the other kinds do; the applications keep
+    // Z's layout T[n][k] (leading dimension Kpad), which the FFT writes and the scatter reads contiguously
     if constexpr (sizeof(S) == 4)
       return launch_fft_conv(reinterpret_cast<const float*>(Zr), Kpad, N / 2, mesh1, mesh2, fft_p, fft_spec, fft_tw,
-                             reinterpret_cast<float*>(Tm), Npad, s);
+                             reinterpret_cast<float*>(Tm), t_kn ? Npad : Kpad, t_kn, s);
     return cudaErrorInvalidValue;
   }
   return launch_simt_gemm_tn<S>(Vr, Kpad, Zr, Kpad, reinterpret_cast<S*>(Tm), Npad, nk, N, Kpad, s);
@@ -213,20 +221,26 @@ TcGemmPlan* MatFreeOperator<S>::plan_for(int N, int np, int bn) {
 // output element is summed in the same order whatever the tile.
 template <class S>
 cudaError_t MatFreeOperator<S>::autotune(cudaStream_t s, const cplx<S>* X, cplx<S>* Y) {
-  if (kind != GEMM_TC_BF16) return cudaSuccess;
+  if (kind != GEMM_TC_BF16 && kind != GEMM_FFT_F32) return cudaSuccess;
+  const bool fft = kind == GEMM_FFT_F32;
   char shape[160];
-  std::snprintf(shape, sizeof(shape), "matfree nk=%d nv=%d nc=%d w=%d cols=%d slices=%d products=%d", nk, nv, nc, w,
-                nbmax, nslices, npairs);
+  if (fft)
+    std::snprintf(shape, sizeof(shape), "matfree-fft nk=%d nv=%d nc=%d w=%d cols=%d mesh=%dx%d P=%d", nk, nv, nc, w,
+                  nbmax, mesh1, mesh2, fft_p);
+  else
+    std::snprintf(shape, sizeof(shape), "matfree nk=%d nv=%d nc=%d w=%d cols=%d slices=%d products=%d", nk, nv, nc, w,
+                  nbmax, nslices, npairs);
   auto run = [&]() -> cudaError_t {
     const long mv = this->matvec_columns;
     const cudaError_t e = apply(X, nbmax, 0, nbmax, Y, nbmax, s);
     this->matvec_columns = mv;
     return e;
   };
-  tile_n = tune_choice(shape, "tile_n", {256, 128}, 256, [&](int c) {
-    tile_n = c;
-    return run();
-  }, s);
+  if (!fft)
+    tile_n = tune_choice(shape, "tile_n", {256, 128}, 256, [&](int c) {
+      tile_n = c;
+      return run();
+    }, s);
   // gather tiles: 16 or 8 k' per CTA, chunks of 1, 2 or 4 block columns (those within 200 KB of shared memory)
   std::vector<int> gt;
   for (int kt : {16, 8})
@@ -238,8 +252,14 @@ cudaError_t MatFreeOperator<S>::autotune(cudaStream_t s, const cplx<S>* X, cplx<
     gather_tile = c;
     return run();
   }, s);
+  // scatter columns per CTA: the k-point scatter from nbmax down, the FFT form's k-tiled scatter 2, 4 or 8
   std::vector<int> sc;
-  for (int g = nbmax; g >= 1 && sc.size() < 3; g = g > 1 ? (g + 1) / 2 : 0) sc.push_back(g);
+  if (fft) {
+    for (int g : {2, 4, 8})
+      if (g <= nbmax) sc.push_back(g);
+  } else {
+    for (int g = nbmax; g >= 1 && sc.size() < 3; g = g > 1 ? (g + 1) / 2 : 0) sc.push_back(g);
+  }
   scatter_cols = tune_choice(shape, "scatter_cols", sc, 0, [&](int c) {
     scatter_cols = c;
     return run();
@@ -485,66 +505,92 @@ __global__ void cond_copy_kernel(const LobCtl* __restrict__ ctl, int which, cons
   }
 }
 
-// In place: X <- [X W P] C and P <- [W P] C[m:3m, :] for the basis and for its image under H.  A CTA stages
-// kUpdRows rows (one row tile) of the block in shared memory (so the in-place writes cannot overtake reads),
-// then threads (row, pair of output columns: 256 threads for m = 16) form their outputs from the staged row
-// and the C of the tile's system (staged again only when the system changes from one tile to the next).
+// In place: X <- [X W P] C and P <- [W P] C[m:3m, :] for the basis and for its image under H.  A CTA takes one
+// row tile (kUpdRows rows) of both blocks at once: it stages the tile's rows of S and of AS in shared memory (so
+// the in-place writes cannot overtake reads; rows padded to nb + 2 complex, so that the four rows a warp reads
+// at one column fall in distinct banks and 16-byte copies stay aligned), then each thread forms one pair of
+// output columns of the same row of S and of AS: per input column one load from each staged row and one 16-byte
+// load of C serve four complex FMAs.  Each output keeps the summation order of a plain loop (X block, then
+// [W P]), independent of the tiling.  C of the tile's system is staged again only when the system changes.
 constexpr int kUpdRows = kTileRows;
 template <class S>
 __global__ void __launch_bounds__(256) lob_update_kernel(cplx<S>* __restrict__ Sb, cplx<S>* __restrict__ ASb, int ld,
                                                          int m, const zd* __restrict__ C, int nrow, BatchMap bm,
                                                          long c_stride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int nb = 3 * m;
+  const int nb = 3 * m, RS = nb + 2;
   cplx<S>* Cs = reinterpret_cast<cplx<S>*>(smem_raw);  // [3m][m]
-  cplx<S>* Rs = Cs + nb * m;                           // [kUpdRows][3m]
-  const int ngrp = (m + 1) >> 1;       // pairs of output columns
-  const int items = kUpdRows * ngrp;   // (row, pair) items per pass
+  cplx<S>* Rs = Cs + ((nb * m + 1) & ~1);              // [2][kUpdRows][RS]: rows of S, then of AS
+  const int ngrp = (m + 1) >> 1;      // pairs of output columns
+  const int items = kUpdRows * ngrp;  // (row, pair) items per tile
+  const bool vec = sizeof(S) == 4 && (ld & 1) == 0 && (nb & 1) == 0;
   int staged = -1;
   for (long r0 = (long)blockIdx.x * kUpdRows; r0 < nrow; r0 += (long)gridDim.x * kUpdRows) {
     const int sys = bm_sys_of_row(bm, r0);  // uniform over the CTA
     if (bm_frozen(bm, sys)) continue;
+    __syncthreads();  // the previous tile's reads of Rs (and of Cs) are done
     if (sys != staged) {
-      __syncthreads();
       const zd* Cq = C + (size_t)sys * c_stride;
       for (int e = threadIdx.x; e < nb * m; e += blockDim.x) Cs[e] = mk<S>((S)Cq[e].re, (S)Cq[e].im);
       staged = sys;
     }
     const int nr = (int)min((long)kUpdRows, nrow - r0);
     for (int which = 0; which < 2; ++which) {
-      cplx<S>* base = (which ? ASb : Sb) + r0 * ld;
-      __syncthreads();
-      for (int e = threadIdx.x; e < nr * nb; e += blockDim.x) {
-        const int rr = e / nb, c = e - rr * nb;
-        Rs[rr * nb + c] = base[(size_t)rr * ld + c];
+      const cplx<S>* base = (which ? ASb : Sb) + r0 * ld;
+      cplx<S>* dst = Rs + which * kUpdRows * RS;
+      if (vec) {  // two complex FP32 per 16-byte copy
+        const int hp = nb >> 1;
+        for (int e = threadIdx.x; e < nr * hp; e += blockDim.x) {
+          const int rr = e / hp, c2 = e - rr * hp;
+          *reinterpret_cast<float4*>(dst + rr * RS + 2 * c2) =
+              *reinterpret_cast<const float4*>(base + (size_t)rr * ld + 2 * c2);
+        }
+      } else {
+        for (int e = threadIdx.x; e < nr * nb; e += blockDim.x) {
+          const int rr = e / nb, c = e - rr * nb;
+          dst[rr * RS + c] = base[(size_t)rr * ld + c];
+        }
       }
-      __syncthreads();
-      for (int it = threadIdx.x; it < items; it += blockDim.x) {
-        const int rr = it / ngrp, g = it - rr * ngrp;
-        if (rr >= nr) continue;
-        const int j0 = g * 2;
-        const bool two = j0 + 1 < m;
-        cplx<S> x0 = mk<S>(0, 0), x1 = mk<S>(0, 0), p0 = mk<S>(0, 0), p1 = mk<S>(0, 0);
-        const cplx<S>* row = Rs + rr * nb;
-        for (int i = 0; i < m; ++i) {  // the X block contributes to X only
-          const cplx<S> ri = row[i];
-          const cplx<S>* crow = Cs + i * m + j0;
-          cfma(x0, ri, crow[0]);
-          if (two) cfma(x1, ri, crow[1]);
-        }
-        for (int i = m; i < nb; ++i) {  // W and P contribute to X and to the new P
-          const cplx<S> ri = row[i];
-          const cplx<S>* crow = Cs + i * m + j0;
-          cfma(p0, ri, crow[0]);
-          if (two) cfma(p1, ri, crow[1]);
-        }
-        cplx<S>* out = base + (size_t)rr * ld;
-        out[j0] = mk<S>(x0.re + p0.re, x0.im + p0.im);
-        out[2 * m + j0] = p0;
-        if (two) {
-          out[j0 + 1] = mk<S>(x1.re + p1.re, x1.im + p1.im);
-          out[2 * m + j0 + 1] = p1;
-        }
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+      const int rr = it / ngrp, g = it - rr * ngrp;
+      if (rr >= nr) continue;
+      const int j0 = g * 2;
+      const bool two = j0 + 1 < m;
+      const cplx<S>* rs = Rs + rr * RS;
+      const cplx<S>* ra = Rs + (kUpdRows + rr) * RS;
+      cplx<S> xs0 = mk<S>(0, 0), xs1 = mk<S>(0, 0), ps0 = mk<S>(0, 0), ps1 = mk<S>(0, 0);
+      cplx<S> xa0 = mk<S>(0, 0), xa1 = mk<S>(0, 0), pa0 = mk<S>(0, 0), pa1 = mk<S>(0, 0);
+      for (int i = 0; i < m; ++i) {  // the X block contributes to X only
+        const cplx<S> si = rs[i], ai = ra[i];
+        const cplx<S>* crow = Cs + i * m + j0;
+        const cplx<S> c0 = crow[0], c1 = two ? crow[1] : mk<S>(0, 0);
+        cfma(xs0, si, c0);
+        cfma(xa0, ai, c0);
+        cfma(xs1, si, c1);
+        cfma(xa1, ai, c1);
+      }
+      for (int i = m; i < nb; ++i) {  // W and P contribute to X and to the new P
+        const cplx<S> si = rs[i], ai = ra[i];
+        const cplx<S>* crow = Cs + i * m + j0;
+        const cplx<S> c0 = crow[0], c1 = two ? crow[1] : mk<S>(0, 0);
+        cfma(ps0, si, c0);
+        cfma(pa0, ai, c0);
+        cfma(ps1, si, c1);
+        cfma(pa1, ai, c1);
+      }
+      cplx<S>* os = Sb + (r0 + rr) * ld;
+      cplx<S>* oa = ASb + (r0 + rr) * ld;
+      os[j0] = mk<S>(xs0.re + ps0.re, xs0.im + ps0.im);
+      os[2 * m + j0] = ps0;
+      oa[j0] = mk<S>(xa0.re + pa0.re, xa0.im + pa0.im);
+      oa[2 * m + j0] = pa0;
+      if (two) {
+        os[j0 + 1] = mk<S>(xs1.re + ps1.re, xs1.im + ps1.im);
+        os[2 * m + j0 + 1] = ps1;
+        oa[j0 + 1] = mk<S>(xa1.re + pa1.re, xa1.im + pa1.im);
+        oa[2 * m + j0 + 1] = pa1;
       }
     }
   }
@@ -658,7 +704,7 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
   // between iterations (for kernel-level profilers, which do not replay kernels inside conditional graph
   // bodies); the default runs the whole solve as one graph launch
   const bool stream_mode = std::getenv("WTB_SOLVER_STREAM") != nullptr && !sg;
-  const size_t upd_smem = (size_t)(nb * m + kUpdRows * nb) * sizeof(cplx<S>);
+  const size_t upd_smem = (size_t)(((nb * m + 1) & ~1) + 2 * kUpdRows * (nb + 2)) * sizeof(cplx<S>);
   const int upd_grid = std::max(1, std::min(152 * 8, (nrow + kUpdRows - 1) / kUpdRows));
   const unsigned cp_grid = (unsigned)std::max(1, std::min(152 * 4, (int)(((long)nrow * m + 255) / 256)));
 
@@ -694,13 +740,11 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
   };
   auto iteration = [&](cudaGraphConditionalHandle h) -> int {
     CK(launch_precond<S>(W, ld, diag, th_dev, active, m, nrow, s, bm, nb));
-    // W <- W - X (X^H W);  P <- P - X (X^H P), AP <- AP - AX (X^H P)
-    CK(launch_gram<S>(X, ld, m, W, ld, m, nrow, sm.T, partial, npart, s, bm, nn));
-    CK(launch_update<S>(X, ld, m, sm.T, m, m, nrow, W, ld, -1.0, 1.0, s, bm, nn));
+    // W <- W - X (X^H W);  P <- P - X (X^H P), AP <- AP - AX (X^H P): one Gram X^H [W P] (W and P are adjacent
+    // column blocks) and one pass for the three projections; P and AP do not depend on W's image
+    CK(launch_gram<S>(X, ld, m, W, ld, 2 * m, nrow, sm.T, partial, npart, s, bm, nn));
+    CK(launch_orth_update<S>(X, AX, ld, m, sm.T, W, P, AP, nrow, s, bm, nn));
     CK(op.apply(W, ld, 0, m, AW, ld, s));
-    CK(launch_gram<S>(X, ld, m, P, ld, m, nrow, sm.T, partial, npart, s, bm, nn));
-    CK(launch_update<S>(X, ld, m, sm.T, m, m, nrow, P, ld, -1.0, 1.0, s, bm, nn));
-    CK(launch_update<S>(AX, ld, m, sm.T, m, m, nrow, AP, ld, -1.0, 1.0, s, bm, nn));
     int r = rr_and_update();
     if (r) return r;
     return check_and_decide(h);

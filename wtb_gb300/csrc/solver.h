@@ -172,7 +172,9 @@ struct MatFreeOperator : Operator<S> {
   // gather + contraction only: leaves T = V Z(X[:, 0:ncol]) in Tm (row k, column ((b w + o) w + p) 2 + ri,
   // leading dimension Npad; float for the tensor-core kind, S otherwise); ncol <= nbmax
   cudaError_t contract(const cplx<S>* X, int ldx, int ncol, cudaStream_t s);
-  cudaError_t contract_z(int N, cudaStream_t s);
+  // T = V Z for the N gathered columns; t_kn: T[k][n] (leading dimension Npad) for every kind, else the FFT kind
+  // writes T[n][k] (leading dimension Kpad)
+  cudaError_t contract_z(int N, cudaStream_t s, bool t_kn);
   double contraction_flops(int N) const;
   double contraction_bytes(int N) const;
   bool begin_refine() override {

@@ -381,6 +381,12 @@ int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob, 
     op->Tm = c->ws.get<float>("T32", (size_t)Mpad * Npad, &err);
     CKC(err);
     c->last_form = WTB_FORM_FFT_F32;
+    if (tune) {
+      zf* tx = c->ws.get<zf>("tune_X", (size_t)dim * nbmax, &err, true);
+      zf* ty = c->ws.get<zf>("tune_Y", (size_t)dim * nbmax, &err);
+      CKC(err);
+      CKC(op->autotune(c->s, tx, ty));
+    }
     return WTB_OK;
   }
   c->last_form = WTB_FORM_NONE;
@@ -486,13 +492,13 @@ int run_solve(wtb_ctx* c, const wtb_bse_params* p, std::vector<double>* E, wtb_t
   CKC(cudaEventRecord(ev[0], c->s));
   const bool fp64 = p->precision == WTB_PREC_FP64;
   const int m = auto_block(p, dim, fp64);
-  // residual targets: SLEPc's 1e-8 in FP64; 1e-5 (about the FP32 rounding floor of the operator) otherwise.
+  // residual targets: SLEPc's 1e-8 in FP64; kReducedTol (just above the FP32 rounding floor) otherwise.
   // The reduced-precision forms run in two phases: to 1e-4, then -- from the best block, with a freshly applied
   // operator and the search directions dropped -- to the target (bf16x3 switches to its 6-product operator
   // there).  The restart removes the drift of the FP32 iteration's running H X, which otherwise stalls the
   // residual between 1e-5 and 1e-4 on the 57,600 workload.
   const bool two_phase = !fp64;
-  const double tol_final = p->tol > 0 ? p->tol : (fp64 ? 1e-8 : 1e-5);
+  const double tol_final = p->tol > 0 ? p->tol : (fp64 ? 1e-8 : kReducedTol);
   const double tol = two_phase ? std::max(tol_final, 1e-4) : tol_final;
   const double tol_refine = two_phase && tol_final < tol ? tol_final : 0.0;
   const int maxit = p->maxit > 0 ? p->maxit : 200;

@@ -49,6 +49,19 @@ template <class S>
 __host__ __device__ __forceinline__ cplx<S> cconj(cplx<S> a) { return mk<S>(a.re, -a.im); }
 template <class S>
 __host__ __device__ __forceinline__ cplx<S> cscale(cplx<S> a, S s) { return mk<S>(a.re * s, a.im * s); }
+// Relative residual target of the reduced-precision (FP32 and split-BF16) solves.  It sits above the FP32
+// iteration's rounding floor (about 1.2e-5 on the 57,600-dimensional workload), where a target at the floor made
+// the iteration count depend on the last bits.  Measured against the FP64 oracle on that workload (FP32 FFT
+// form): targets 1e-5 / 2e-5 / 3e-5 took 11 / 10 / 9 iterations with exciton energies within 9.9e-8 / 9.0e-8 /
+// 6.6e-8 eV and spectra within 3.2e-5 / 5.2e-5 / 7.2e-5 relative L2; on the 36,864 cubic workload (bf16x3) 3e-5
+// put a spectrum 1.3e-4 off, 2e-5 2.8e-5.
+constexpr double kReducedTol = 2e-5;
+
+// n / d for 0 <= n < 2^21 and d >= 1, with rinv = 1.0f / d: (n + 1/2) / d lies at least 1 / (2 d) from an
+// integer, and the two FP32 roundings move it by at most 2^-23 (n + 1/2) / d < 1 / (4 d), so truncation gives
+// the quotient.  Two instructions instead of an integer division by a runtime divisor.
+__device__ __forceinline__ int qdiv(int n, float rinv) { return __float2int_rz(((float)n + 0.5f) * rinv); }
+
 // acc += a*b
 template <class S>
 __host__ __device__ __forceinline__ void cfma(cplx<S>& acc, cplx<S> a, cplx<S> b) {
@@ -118,13 +131,13 @@ cudaError_t launch_coulomb(const CoulParams& p, const double* kpt1, int n1, cons
 cudaError_t launch_coulomb_stencil(const CoulParams& p, const double* bl, double* stencil, cudaStream_t s);
 // FFT form of the contraction on a two-dimensional mesh (k_fftconv.cu): the transform size P (32, 64 or 128)
 // for an n1 x n2 mesh, or 0 when the mesh is too large; the stencil's spectrum (work: (2 n1 - 1) P complex
-// doubles; spec: P x P; tw: 128 twiddles); T[k][2q + (0, 1)] = (V Z)[k][2q + (0, 1)] for the npairs column
-// pairs of Z (column n at Z + n ldz, k' = i n2 + j)
+// doubles; spec: P x P; tw: 128 twiddles); (V Z) for the npairs column pairs of Z (column n at Z + n ldz,
+// k' = i n2 + j) into T: t_kn ? T[k][2q + (0, 1)] (row k at T + k ldt) : T[2q + (0, 1)][k] (Z's layout)
 int fft_conv_size(int n1, int n2);
 cudaError_t launch_fft_spectrum(const double* stencil, int n1, int n2, int P, zd* work, float2* spec, float2* tw,
                                 cudaStream_t s);
 cudaError_t launch_fft_conv(const float* Z, int ldz, int npairs, int n1, int n2, int P, const float2* spec,
-                            const float2* tw, float* T, int ldt, cudaStream_t s);
+                            const float2* tw, float* T, int ldt, bool t_kn, cudaStream_t s);
 cudaError_t launch_coulomb_mesh(const CoulParams& p, const double* bl, double* stencil, double* V, int ldv,
                                 cudaStream_t s);
 // Transition energies dE[I] = E_c - E_v.
@@ -195,6 +208,11 @@ template <class S>
 cudaError_t launch_gram_pair(const cplx<S>* A, const cplx<S>* B, int ld, int p, int nrow, zd* outM, zd* outG,
                              double* partial, int npart, cudaStream_t s, const BatchMap& bm = BatchMap(),
                              long out_stride = 0);
+// W -= X T[:, 0:m], P -= X T[:, m:2m], AP -= AX T[:, m:2m] (T: m x 2m FP64, per system at t_stride)
+template <class S>
+cudaError_t launch_orth_update(const cplx<S>* X, const cplx<S>* AX, int ld, int m, const zd* T, cplx<S>* W,
+                               cplx<S>* P, cplx<S>* AP, int nrow, cudaStream_t s, const BatchMap& bm = BatchMap(),
+                               long t_stride = 0);
 template <class S>
 cudaError_t launch_update(const cplx<S>* Sx, int lds, int nin, const zd* C, int ldc, int nout, int nrow,
                           cplx<S>* Out, int ldo, double alpha, double beta, cudaStream_t s,
@@ -223,6 +241,11 @@ cudaError_t launch_small_gemm(const zd* A, int lda, int transA, const zd* B, int
 template <class S, class Z>
 cudaError_t launch_mf_gather(const cplx<S>* X, int ldx, int c0, int nb, const zd* vec_win, int nk, int nv, int nc,
                              int w, Z* zt, int ldk, int nslices, long slice_stride, cudaStream_t s, int tile = 0);
+// scatter from T in Z's layout, T[n][k] (row n at Tt + n ldt; the FFT form), over tiles of 8 k-points and cols
+// block columns per CTA (0: 4)
+cudaError_t launch_mf_scatter_t(const float* Tt, int ldt, const zf* X, int ldx, const zd* vec_win, const double* dE,
+                                int nk, int nv, int nc, int w, int nb, zf* Y, int ldy, int c0, cudaStream_t s,
+                                int cols = 0);
 // cols: block columns per CTA (0 = all that fit in 96 KB of shared memory)
 template <class S, class T>
 cudaError_t launch_mf_scatter(const T* Tm, int ldt, const cplx<S>* X, int ldx, const zd* vec_win, const double* dE,
