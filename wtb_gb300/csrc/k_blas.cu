@@ -767,6 +767,15 @@ cudaError_t launch_gram_pair(const cplx<S>* A, const cplx<S>* B, int ld, int p, 
   return cudaGetLastError();
 }
 
+cudaError_t launch_sum_partials_pair(const double* partial, int npart, int n, zd* outM, zd* outG, cudaStream_t s,
+                                     const BatchMap& bm, long out_stride) {
+  sum_partials_kernel<<<dim3((n + 31) / 32, bm.nsys, 2), 256, 0, s>>>(partial, npart, n,
+                                                                       reinterpret_cast<double*>(outM), bm,
+                                                                       2 * out_stride, reinterpret_cast<double*>(outG));
+  ++g_launch_count;
+  return cudaGetLastError();
+}
+
 template <class S>
 cudaError_t launch_update(const cplx<S>* Sx, int lds, int nin, const zd* C, int ldc, int nout, int nrow,
                           cplx<S>* Out, int ldo, double alpha, double beta, cudaStream_t s, const BatchMap& bm,

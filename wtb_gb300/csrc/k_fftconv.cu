@@ -216,10 +216,15 @@ __device__ __forceinline__ void fft_inv(float2 (&x)[16], int r, float2* scr, con
 
 constexpr int kFftThreads = 256;
 
-// t_kn: T as [k][ldt] rows (column pair 2q, 2q + 1 of row k); otherwise T as [n][ldt] rows like Z
+// t_kn: T as [k][ldt] rows (column pair 2q, 2q + 1 of row k); otherwise T as [n][ldt] rows like Z.
+// spec: the complex spectrum; spec_re its real parts (the same layout, FP32) and *even != 0 when the stencil is
+// even, s(-d) = s(d) bitwise (every potential of the reference depends on q through |q| or squared components),
+// so that the spectrum is real and the column pass multiplies by (and loads) its real parts only.
 template <int P>
 __global__ void __launch_bounds__(kFftThreads, 2) fft_conv_kernel(const float* __restrict__ Z, int ldz, int n1, int n2,
                                                                   const float2* __restrict__ spec,
+                                                                  const float* __restrict__ spec_re,
+                                                                  const int* __restrict__ even,
                                                                   const float2* __restrict__ tw_g,
                                                                   float* __restrict__ T, int ldt, int t_kn) {
   constexpr int G = P / 16, TT = 16 / G, NG = kFftThreads / G, LDS = P + 1, TS = 128 / P;
@@ -232,6 +237,7 @@ __global__ void __launch_bounds__(kFftThreads, 2) fft_conv_kernel(const float* _
   const float* zre = Z + (size_t)(2 * q) * ldz;
   const float* zim = zre + ldz;
   const LaneTw tw{tw_g[r * TS], tw_g[2 * r * TS], tw_g[4 * r * TS], tw_g[8 * r * TS]};
+  const bool real_spec = *even != 0;  // uniform
   const float2 zero = c2(0.f, 0.f);
   // A. row transforms over j
   for (int i0 = 0; i0 < n1; i0 += NG) {
@@ -268,12 +274,23 @@ __global__ void __launch_bounds__(kFftThreads, 2) fft_conv_kernel(const float* _
     for (int m = 8; m < 16; ++m) x[m] = zero;
     fft_fwd<P, true>(x, r, scr, tw);  // n1 <= P / 2
     if (act) {
-      const float4* sv = reinterpret_cast<const float4*>(spec + (size_t)v * P + r * 16);
+      if (real_spec) {
+        const float4* sv = reinterpret_cast<const float4*>(spec_re + (size_t)v * P + r * 16);
 #pragma unroll
-      for (int h = 0; h < 8; ++h) {
-        const float4 s4 = sv[h];
-        x[2 * h] = cmul2(x[2 * h], c2(s4.x, s4.y));
-        x[2 * h + 1] = cmul2(x[2 * h + 1], c2(s4.z, s4.w));
+        for (int h = 0; h < 4; ++h) {
+          const float4 s4 = sv[h];
+          const float sr[4] = {s4.x, s4.y, s4.z, s4.w};
+#pragma unroll
+          for (int u = 0; u < 4; ++u) x[4 * h + u] = c2(x[4 * h + u].x * sr[u], x[4 * h + u].y * sr[u]);
+        }
+      } else {
+        const float4* sv = reinterpret_cast<const float4*>(spec + (size_t)v * P + r * 16);
+#pragma unroll
+        for (int h = 0; h < 8; ++h) {
+          const float4 s4 = sv[h];
+          x[2 * h] = cmul2(x[2 * h], c2(s4.x, s4.y));
+          x[2 * h + 1] = cmul2(x[2 * h + 1], c2(s4.z, s4.w));
+        }
       }
     }
     fft_inv<P>(x, r, scr, tw);
@@ -360,7 +377,8 @@ __global__ void spec_rows_kernel(const double* __restrict__ st, int n1, int n2, 
 
 // S[u][v] = sum_a R[a][v] W_P^(u (a - (n1 - 1))) / P^2, stored in FP32 in the distributed layout of the
 // column pass: column v's P values, value u = k2 + 16 k1 at v P + r 16 + t G + k1 with k2 = r (16 / G) + t
-__global__ void spec_cols_kernel(const zd* __restrict__ R, int n1, int P, float2* __restrict__ spec) {
+__global__ void spec_cols_kernel(const zd* __restrict__ R, int n1, int P, float2* __restrict__ spec,
+                                 float* __restrict__ spec_re) {
   __shared__ double wr[128], wi[128];
   const int u = blockIdx.x, v = threadIdx.x;
   if (v < P) {
@@ -384,6 +402,19 @@ __global__ void spec_cols_kernel(const zd* __restrict__ R, int n1, int P, float2
   const double sc = 1.0 / ((double)P * P);
   const int k2 = u % 16, k1 = u / 16, r = k2 / T, t = k2 % T;
   spec[(size_t)v * P + r * 16 + t * G + k1] = make_float2((float)(re * sc), (float)(im * sc));
+  spec_re[(size_t)v * P + r * 16 + t * G + k1] = (float)(re * sc);
+}
+
+// *even = 1 when s[d] == s[-d] bitwise for every index difference d of the (2 n1 - 1) x (2 n2 - 1) stencil
+__global__ void stencil_even_kernel(const double* __restrict__ st, int n1, int n2, int* __restrict__ even) {
+  const int s1 = 2 * n1 - 1, s2 = 2 * n2 - 1, n = s1 * s2;
+  int ok = 1;
+  for (int e = threadIdx.x; e < n; e += blockDim.x) {
+    const int a = e / s2, b = e - a * s2;
+    ok &= st[e] == st[(size_t)(s1 - 1 - a) * s2 + (s2 - 1 - b)] ? 1 : 0;
+  }
+  ok = __syncthreads_and(ok);
+  if (threadIdx.x == 0) *even = ok;
 }
 
 // the transforms' twiddles W_128^m, m < 128, rounded to FP32 from FP64
@@ -414,8 +445,11 @@ cudaError_t launch_fft_spectrum(const double* stencil, int n1, int n2, int P, zd
                                 cudaStream_t s) {
   if (P != 32 && P != 64 && P != 128) return cudaErrorInvalidValue;
   if (2 * n1 - 1 > P || 2 * n2 - 1 > P) return cudaErrorInvalidValue;
+  float* spec_re = reinterpret_cast<float*>(spec + (size_t)P * P);
+  int* even = reinterpret_cast<int*>(spec_re + (size_t)P * P);
   spec_rows_kernel<<<2 * n1 - 1, 128, 0, s>>>(stencil, n1, n2, P, work); ++g_launch_count;
-  spec_cols_kernel<<<P, 128, 0, s>>>(work, n1, P, spec); ++g_launch_count;
+  spec_cols_kernel<<<P, 128, 0, s>>>(work, n1, P, spec, spec_re); ++g_launch_count;
+  stencil_even_kernel<<<1, 256, 0, s>>>(stencil, n1, n2, even); ++g_launch_count;
   twiddle_kernel<<<1, 128, 0, s>>>(tw); ++g_launch_count;
   return cudaGetLastError();
 }
@@ -425,26 +459,28 @@ cudaError_t launch_fft_conv(const float* Z, int ldz, int npairs, int n1, int n2,
   if (npairs < 1) return cudaSuccess;
   if (2 * n1 - 1 > P || 2 * n2 - 1 > P || (ldt & 1)) return cudaErrorInvalidValue;
   const int kn = t_kn ? 1 : 0;
+  const float* spec_re = reinterpret_cast<const float*>(spec + (size_t)P * P);
+  const int* even = reinterpret_cast<const int*>(spec_re + (size_t)P * P);
   switch (P) {
     case 32: {
       const size_t smem = conv_smem<32>(n1);
       cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(fft_conv_kernel<32>), smem);
       if (e != cudaSuccess) return e;
-      fft_conv_kernel<32><<<npairs, kFftThreads, smem, s>>>(Z, ldz, n1, n2, spec, tw, T, ldt, kn);
+      fft_conv_kernel<32><<<npairs, kFftThreads, smem, s>>>(Z, ldz, n1, n2, spec, spec_re, even, tw, T, ldt, kn);
       break;
     }
     case 64: {
       const size_t smem = conv_smem<64>(n1);
       cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(fft_conv_kernel<64>), smem);
       if (e != cudaSuccess) return e;
-      fft_conv_kernel<64><<<npairs, kFftThreads, smem, s>>>(Z, ldz, n1, n2, spec, tw, T, ldt, kn);
+      fft_conv_kernel<64><<<npairs, kFftThreads, smem, s>>>(Z, ldz, n1, n2, spec, spec_re, even, tw, T, ldt, kn);
       break;
     }
     case 128: {
       const size_t smem = conv_smem<128>(n1);
       cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(fft_conv_kernel<128>), smem);
       if (e != cudaSuccess) return e;
-      fft_conv_kernel<128><<<npairs, kFftThreads, smem, s>>>(Z, ldz, n1, n2, spec, tw, T, ldt, kn);
+      fft_conv_kernel<128><<<npairs, kFftThreads, smem, s>>>(Z, ldz, n1, n2, spec, spec_re, even, tw, T, ldt, kn);
       break;
     }
     default:

@@ -360,7 +360,7 @@ int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob, 
     const int n1 = p->ngrid[0], n2 = p->ngrid[1];
     double* stn = c->ws.get<double>("vstencil" + tag, (size_t)(2 * n1 - 1) * (2 * n2 - 1), &err);
     zd* work = c->ws.get<zd>("fft_work", (size_t)(2 * n1 - 1) * fftP, &err);
-    float2* spec = c->ws.get<float2>("fft_spec" + tag, (size_t)fftP * fftP, &err);
+    float2* spec = c->ws.get<float2>("fft_spec" + tag, fft_spec_size(fftP), &err);
     float2* tw = c->ws.get<float2>("fft_tw", 128, &err);
     CKC(err);
     CKC(launch_coulomb_stencil(cpar, dbl, stn, c->s));

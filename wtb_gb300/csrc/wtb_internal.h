@@ -131,9 +131,11 @@ cudaError_t launch_coulomb(const CoulParams& p, const double* kpt1, int n1, cons
 cudaError_t launch_coulomb_stencil(const CoulParams& p, const double* bl, double* stencil, cudaStream_t s);
 // FFT form of the contraction on a two-dimensional mesh (k_fftconv.cu): the transform size P (32, 64 or 128)
 // for an n1 x n2 mesh, or 0 when the mesh is too large; the stencil's spectrum (work: (2 n1 - 1) P complex
-// doubles; spec: P x P; tw: 128 twiddles); (V Z) for the npairs column pairs of Z (column n at Z + n ldz,
+// doubles; spec: fft_spec_size(P) complex (the P x P spectrum, its real parts and the stencil's evenness flag);
+// tw: 128 twiddles); (V Z) for the npairs column pairs of Z (column n at Z + n ldz,
 // k' = i n2 + j) into T: t_kn ? T[k][2q + (0, 1)] (row k at T + k ldt) : T[2q + (0, 1)][k] (Z's layout)
 int fft_conv_size(int n1, int n2);
+inline size_t fft_spec_size(int P) { return (size_t)P * P + (size_t)P * P / 2 + 1; }
 cudaError_t launch_fft_spectrum(const double* stencil, int n1, int n2, int P, zd* work, float2* spec, float2* tw,
                                 cudaStream_t s);
 cudaError_t launch_fft_conv(const float* Z, int ldz, int npairs, int n1, int n2, int P, const float2* spec,
@@ -208,6 +210,16 @@ template <class S>
 cudaError_t launch_gram_pair(const cplx<S>* A, const cplx<S>* B, int ld, int p, int nrow, zd* outM, zd* outG,
                              double* partial, int npart, cudaStream_t s, const BatchMap& bm = BatchMap(),
                              long out_stride = 0);
+// outM, outG: the sums over npart parts of the two partial sets [part][n] at partial and partial + npart n
+cudaError_t launch_sum_partials_pair(const double* partial, int npart, int n, zd* outM, zd* outG, cudaStream_t s,
+                                     const BatchMap& bm, long out_stride);
+// the final Rayleigh-Ritz of the reduced forms (k_final.cu): M = A^H A and G = A^H B of FP32 blocks (p <= 32
+// columns) summed with compensated FP32 arithmetic; and the small FP64 problem from M, G (n <= 32): theta (m
+// lowest, ascending; 1e30 for a dropped direction) and C (n x m, leading dimension m), keep = kept directions
+cudaError_t launch_gram_pair_dot2(const zf* A, const zf* B, int ld, int p, int nrow, zd* outM, zd* outG,
+                                  double* partial, int npart, cudaStream_t s, const BatchMap& bm, long out_stride);
+cudaError_t launch_small_rr(const zd* M, const zd* G, int n, int m, double drop, double* theta, zd* C, int* keep,
+                            cudaStream_t s, const BatchMap& bm, long mat_stride, long theta_stride);
 // W -= X T[:, 0:m], P -= X T[:, m:2m], AP -= AX T[:, m:2m] (T: m x 2m FP64, per system at t_stride)
 template <class S>
 cudaError_t launch_orth_update(const cplx<S>* X, const cplx<S>* AX, int ld, int m, const zd* T, cplx<S>* W,
