@@ -9,7 +9,7 @@ tests/golden/make_golden.py.
 
 Gates (the acceptance bounds): every exciton energy within 1e-5 eV of the oracle's, in every precision form;
 the xx, yy, zz spectra within 1e-4 relative L2.  Activities: 1e-4 of the largest in the FP64 forms; in the
-reduced-precision forms the eigenvectors carry the 2e-5 residual divided by the smallest gap between the
+reduced-precision forms the eigenvectors carry the 1e-5 residual divided by the smallest gap between the
 excitons (9 meV at 57,600), so 2e-2 of the largest.
 """
 import os

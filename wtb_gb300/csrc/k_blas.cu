@@ -633,6 +633,7 @@ __global__ void __launch_bounds__(256) pchol_basis_kernel(const zd* __restrict__
   S* dinv = reinterpret_cast<S*>(R + (size_t)n * lds);
   S* rinv = dinv + n;                                  // 1 / R[k][k]
   int* perm = reinterpret_cast<int*>(rinv + n);
+  cplx<S>* tri_scr = reinterpret_cast<cplx<S>*>((reinterpret_cast<uintptr_t>(perm + n) + 15) & ~(uintptr_t)15);
   __shared__ int s_r;
   for (int i = tid; i < n; i += nt) {
     const double m = Mg[(size_t)i * ldm + i].re;
@@ -665,7 +666,8 @@ __global__ void __launch_bounds__(256) pchol_basis_kernel(const zd* __restrict__
       perm[r] = k;
       rinv[r] = irk;
     }
-    // Schur complement on the trailing block: W[i][j] -= conj(W[k][i]) W[k][j] / dk
+    // Schur complement on the trailing block: W[i][j] -= conj(W[k][i]) W[k][j] / dk (a 16 x 16 thread grid;
+    // flattened over the CTA with one element per index step it measured slower: 64K against 53K cycles)
     for (int i = k + 1 + ty; i < n; i += 16) {
       const cplx<S> ri = wk[i];
       const cplx<S> rs = mk<S>(ri.re * idk, ri.im * idk);
@@ -685,26 +687,55 @@ __global__ void __launch_bounds__(256) pchol_basis_kernel(const zd* __restrict__
   for (int k = ty; k < r; k += 16)
     for (int l = tx; l < r; l += 16) Rk[(size_t)k * lds + l] = l >= k ? R[(size_t)k * lds + perm[l]] : mk<S>(0, 0);
   __syncthreads();
-  // R^-1 (r x r upper triangular), one thread per column c, over R's rows (dead); two partial sums per
-  // element halve the dependent chain
+  // R^-1 (r x r upper triangular) over R's rows (dead), by blocks of kTriB: the diagonal blocks by back
+  // substitution (one thread per column), then superdiagonal s of blocks at once,
+  // Ri[I][J] = -Ri[I][I] sum_{K = I+1..J} Rk[I][K] Ri[K][J], from blocks of lower superdiagonals (two barriers a
+  // superdiagonal instead of a dependent chain of r^2/4 products per column).  The sums go to the scratch after
+  // perm ((n + 7) / 8 blocks of 8 x 8).
   cplx<S>* Ri = R;
-  for (int c = tid; c < r; c += nt) {
-    for (int k = c + 1; k < r; ++k) Ri[(size_t)k * lds + c] = mk<S>(0, 0);
-    Ri[(size_t)c * lds + c] = mk<S>(rinv[c], 0);
-    for (int k = c - 1; k >= 0; --k) {
-      const cplx<S>* rk = Rk + (size_t)k * lds;
-      cplx<S> a0 = mk<S>(0, 0), a1 = mk<S>(0, 0);
-      int l = k + 1;
-      for (; l + 1 <= c; l += 2) {
-        cfma(a0, rk[l], Ri[(size_t)l * lds + c]);
-        cfma(a1, rk[l + 1], Ri[(size_t)(l + 1) * lds + c]);
+  {
+    constexpr int kTriB = 8;
+    const int nbk = (r + kTriB - 1) / kTriB;
+    for (int e = tid; e < r * r; e += nt) {
+      const int k = e / r, c = e - k * r;
+      if (k > c) Ri[(size_t)k * lds + c] = mk<S>(0, 0);
+    }
+    for (int c = tid; c < r; c += nt) {  // diagonal blocks
+      const int k0 = (c / kTriB) * kTriB;
+      Ri[(size_t)c * lds + c] = mk<S>(rinv[c], 0);
+      for (int k = c - 1; k >= k0; --k) {
+        const cplx<S>* rk = Rk + (size_t)k * lds;
+        cplx<S> a = mk<S>(0, 0);
+        for (int l = k + 1; l <= c; ++l) cfma(a, rk[l], Ri[(size_t)l * lds + c]);
+        const S ir = rinv[k];
+        Ri[(size_t)k * lds + c] = mk<S>(-a.re * ir, -a.im * ir);
       }
-      if (l <= c) cfma(a0, rk[l], Ri[(size_t)l * lds + c]);
-      const S ir = rinv[k];
-      Ri[(size_t)k * lds + c] = mk<S>(-(a0.re + a1.re) * ir, -(a0.im + a1.im) * ir);
+    }
+    __syncthreads();
+    cplx<S>* Tsum = tri_scr;  // [nbk - 1][kTriB][kTriB]
+    for (int sd = 1; sd < nbk; ++sd) {
+      const int nblk = nbk - sd;  // blocks (I, I + sd)
+      for (int e = tid; e < nblk * kTriB * kTriB; e += nt) {
+        const int bi = e / (kTriB * kTriB), ij = e - bi * kTriB * kTriB, i = ij / kTriB, j = ij - i * kTriB;
+        const int I = bi, J = bi + sd, row = I * kTriB + i, col = J * kTriB + j;
+        cplx<S> a = mk<S>(0, 0);
+        if (row < r && col < r)
+          for (int l = (I + 1) * kTriB; l <= col; ++l) cfma(a, Rk[(size_t)row * lds + l], Ri[(size_t)l * lds + col]);
+        Tsum[e] = a;
+      }
+      __syncthreads();
+      for (int e = tid; e < nblk * kTriB * kTriB; e += nt) {
+        const int bi = e / (kTriB * kTriB), ij = e - bi * kTriB * kTriB, i = ij / kTriB, j = ij - i * kTriB;
+        const int I = bi, J = bi + sd, row = I * kTriB + i, col = J * kTriB + j;
+        if (row >= r || col >= r) continue;
+        cplx<S> a = mk<S>(0, 0);
+        for (int q = i; q < kTriB && I * kTriB + q < r; ++q)
+          cfma(a, Ri[(size_t)row * lds + I * kTriB + q], Tsum[bi * kTriB * kTriB + q * kTriB + j]);
+        Ri[(size_t)row * lds + col] = mk<S>(-a.re, -a.im);
+      }
+      __syncthreads();
     }
   }
-  __syncthreads();
   // B[perm[k]][c] = dinv[perm[k]] Ri[k][c] (k <= c < r); everything else zero
   for (int i = ty; i < n; i += 16)
     for (int c = tx; c < n; c += 16) B[(size_t)i * ldb + c] = mk<double>(0.0, 0.0);
@@ -867,7 +898,9 @@ template <class S>
 cudaError_t launch_pchol_basis(const zd* M, int ldm, int n, double drop, zd* B, int ldb, int* r_out, cudaStream_t s,
                                const BatchMap& bm, long m_stride, long b_stride) {
   if (n < 1 || n > 96) return cudaErrorInvalidValue;
-  const size_t smem = (size_t)2 * n * (n + 1) * sizeof(cplx<S>) + (size_t)2 * n * sizeof(S) + (size_t)n * sizeof(int) + 64;
+  // W, R (n x (n + 1) each), dinv, rinv, perm, and the triangular inverse's scratch (11 blocks of 8 x 8 for n <= 96)
+  const size_t smem = (size_t)2 * n * (n + 1) * sizeof(cplx<S>) + (size_t)2 * n * sizeof(S) + (size_t)n * sizeof(int) +
+                      16 + (size_t)((n + 7) / 8) * 64 * sizeof(cplx<S>) + 64;
   if (smem > 220 * 1024) return cudaErrorInvalidValue;
   cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(pchol_basis_kernel<S>), smem);
   if (e != cudaSuccess) return e;

@@ -9,13 +9,17 @@
 //                          compensated dot product of Ogita, Rump and Oishi, "Accurate sum and dot product",
 //                          SIAM J. Sci. Comput. 26, 2005): per entry and part the result is as accurate as an
 //                          FP64 accumulation of the FP32 products, which are exact in FP64;
-//   small_rr_kernel        one CTA per system: the scaled Cholesky basis with the drop rule of
-//                          pchol_basis_kernel, the projected matrix B^H G B and its eigenpairs by cyclic Jacobi
-//                          rotations (a complex Hermitian rotation per pair, n/2 disjoint pairs per round), all
-//                          in FP64 on at most 32 x 32 matrices, with C = B Y for the lowest m.  The final
-//                          projected matrix is diagonal to the iteration's residual, so Jacobi ends in a few
-//                          sweeps; it replaces the Cholesky, two products, the tridiagonal eigensolver and a
-//                          third product (five launches).
+//   small_rr_kernel        one CTA per system, FP64, at most 32 x 32: the orthonormalising basis B, the
+//                          projected matrix B^H G B and its eigenpairs by cyclic Jacobi rotations (a complex
+//                          Hermitian rotation per pair, n/2 disjoint pairs per round), with C = B Y for the
+//                          lowest m.  The final block is orthonormal to FP32 rounding, M = I + E with |E| ~ 1e-7:
+//                          then B = M^(-1/2) = I - E/2 + 3/8 E^2 (exact to |E|^3) from products alone, and the
+//                          projected matrix is diagonal to the iteration's residual, so one Jacobi sweep does
+//                          nearly all the rotations and later ones skip those below 1e-10 (FP64 square roots
+//                          and divisions cost this GPU hundreds of cycles each).  Otherwise: the scaled Cholesky
+//                          basis with the drop rule of pchol_basis_kernel.  It replaces the Cholesky, two
+//                          products, the tridiagonal eigensolver and a third product (five launches).
+//   update_dot2_kernel     X C and AX C for the reported vectors and residuals, FP64-accurate from FP32 X.
 #include <cfloat>
 
 #include "solver.h"
@@ -108,6 +112,59 @@ __global__ void __launch_bounds__(256) gram_pair_dot2_kernel(const zf* __restric
     }
 }
 
+// Out (nrow x nout, complex(8)) = X C for FP32 rows X (nin <= 32 columns) and FP64 C (nin x nout, nout <= 32):
+// C = Ch + Cl with Ch = fl32(C) and Cl = fl32(C - Ch); the X Ch products enter compensated FP32 sums of their
+// exact splits, the X Cl products (2^-24 smaller) a plain FP32 sum, which leaves an error near 2^-48 of the
+// terms, as an FP64 product would.  Row tiles of kTileRows rows; C of the tile's system staged in shared memory.
+__global__ void __launch_bounds__(256) update_dot2_kernel(const zf* __restrict__ X, int ldx, int nin,
+                                                          const zd* __restrict__ C, int ldc, int nout, int nrow,
+                                                          zd* __restrict__ Out, int ldo, BatchMap bm, long c_stride) {
+  __shared__ zf Ch[32 * 32], Cl[32 * 32];
+  __shared__ zf Xs[kTileRows][33];
+  const int tid = threadIdx.x;
+  const long ntile = ((long)nrow + kTileRows - 1) / kTileRows;
+  int staged = -1;
+  for (long t = blockIdx.x; t < ntile; t += gridDim.x) {
+    const int sys = bm_sys_of_row(bm, t * kTileRows);  // uniform over the CTA
+    if (bm_frozen(bm, sys)) continue;
+    __syncthreads();  // the previous tile's reads are done
+    if (sys != staged) {
+      const zd* Cq = C + (size_t)sys * c_stride;
+      for (int e = tid; e < nin * nout; e += blockDim.x) {
+        const int i = e / nout, j = e - i * nout;
+        const zd c = Cq[(size_t)i * ldc + j];
+        const float hr = (float)c.re, hi = (float)c.im;
+        Ch[e] = mk<float>(hr, hi);
+        Cl[e] = mk<float>((float)(c.re - (double)hr), (float)(c.im - (double)hi));
+      }
+      staged = sys;
+    }
+    const long r0 = t * kTileRows;
+    const int nr = (int)min((long)kTileRows, nrow - r0);
+    for (int e = tid; e < nr * nin; e += blockDim.x) {
+      const int rr = e / nin, i = e - rr * nin;
+      Xs[rr][i] = X[(r0 + rr) * ldx + i];
+    }
+    __syncthreads();
+    for (int e = tid; e < nr * nout; e += blockDim.x) {
+      const int rr = e / nout, j = e - rr * nout;
+      Acc2 re, im;
+      float lre = 0.f, lim = 0.f;
+      for (int i = 0; i < nin; ++i) {
+        const zf x = Xs[rr][i], h = Ch[i * nout + j], l = Cl[i * nout + j];
+        dot2_add(re.s, re.c, x.re, h.re);
+        dot2_add(re.s, re.c, -x.im, h.im);
+        dot2_add(im.s, im.c, x.re, h.im);
+        dot2_add(im.s, im.c, x.im, h.re);
+        lre = fmaf(x.re, l.re, fmaf(-x.im, l.im, lre));
+        lim = fmaf(x.re, l.im, fmaf(x.im, l.re, lim));
+      }
+      Out[(r0 + rr) * ldo + j] = mk<double>((double)re.s + (double)re.c + (double)lre,
+                                            (double)im.s + (double)im.c + (double)lim);
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------------------- small Rayleigh-Ritz
 constexpr int kRRMax = 32;
 
@@ -130,21 +187,129 @@ __device__ __forceinline__ void rr_pair(int N, int t, int i, int* p, int* q) {
   *q = max(a, b);
 }
 
+constexpr int kRRL = kRRMax + 1;
+
+// Cyclic Jacobi on the r x r Hermitian A (shared, rows of kRRL), accumulating V <- V U: N (r rounded up to even)
+// players, N - 1 rounds of N / 2 disjoint pairs per sweep; a pair with the padding player is skipped.  Rotation
+// of pair (p, q): with A_pq = g e (g = |A_pq|, |e| = 1) and zeta = (A_qq - A_pp) / (2 g),
+// t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)), c = 1 / sqrt(1 + t^2), s = t c, U = [[c, s], [-s conj(e), c conj(e)]]
+// on (p, q) makes (U^H A U)_pq = 0; A <- U^H A U.  Stops when the off-diagonal mass is below tol2 times the
+// diagonal's (or after 40 sweeps).  All threads of the CTA call it.
+template <class T>
+__device__ void jacobi_cta(cplx<T> (*A)[kRRL], cplx<T> (*V)[kRRL], int r, T tol2, T skip_rel, T* rot_c, T* rot_s,
+                           cplx<T>* rot_e, T* offs, T* dias, int* s_done, int* s_any, int* s_sweep) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int N = (r + 1) & ~1;
+  for (int sweep = 0; sweep < 40 && r > 1; ++sweep) {
+    T off = 0, dia = 0;
+    for (int e = tid; e < r * r; e += nt) {
+      const int a = e / r, b = e - a * r;
+      const T v = A[a][b].re * A[a][b].re + A[a][b].im * A[a][b].im;
+      if (a == b)
+        dia += v;
+      else
+        off += v;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      off += __shfl_xor_sync(0xffffffffu, off, o);
+      dia += __shfl_xor_sync(0xffffffffu, dia, o);
+    }
+    if ((tid & 31) == 0) {
+      offs[tid >> 5] = off;
+      dias[tid >> 5] = dia;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      T o = 0, d = 0;
+      for (int w = 0; w < (nt >> 5); ++w) {
+        o += offs[w];
+        d += dias[w];
+      }
+      *s_done = o <= tol2 * d ? 1 : 0;
+      *s_sweep = 0;  // after a barrier: every thread has read the previous sweep's flag
+    }
+    __syncthreads();
+    if (*s_done) break;
+    for (int t = 0; t < N - 1; ++t) {
+      if (tid == 0) *s_any = 0;
+      __syncthreads();
+      if (tid < N / 2) {
+        int p, q;
+        rr_pair(N, t, tid, &p, &q);
+        T c = 1, sn = 0;
+        cplx<T> ee = mk<T>(1, 0);
+        if (q < r) {
+          const cplx<T> apq = A[p][q];
+          const T g = sqrt(apq.re * apq.re + apq.im * apq.im);
+          // a rotation whose angle (about g / |A_qq - A_pp|) is below skip_rel is left out: it would move the
+          // vectors by less than that and the eigenvalues by its square times the gap
+          if (g > (sizeof(T) == 4 ? (T)1e-30 : (T)1e-300) && g > skip_rel * fabs(A[q][q].re - A[p][p].re)) {
+            *s_any = 1;  // benign race: every writer stores 1
+            ee = mk<T>(apq.re / g, apq.im / g);
+            const T zeta = (A[q][q].re - A[p][p].re) / (2 * g);
+            const T tt = (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
+            c = (T)1 / sqrt((T)1 + tt * tt);
+            sn = tt * c;
+          }
+        }
+        rot_c[tid] = c;
+        rot_s[tid] = sn;
+        rot_e[tid] = ee;
+      }
+      __syncthreads();
+      const int any = *s_any;
+      __syncthreads();  // every thread has read the flag before the next round resets it
+      if (!any) continue;  // uniform: no pair of this round rotates
+      if (tid == 0) *s_sweep = 1;
+      // columns: A[k][p], A[k][q] <- (A_kp c - A_kq s conj(e), A_kp s + A_kq c conj(e)); V likewise
+      for (int e = tid; e < r * (N / 2); e += nt) {
+        const int i = e / r, k = e - i * r;
+        int p, q;
+        rr_pair(N, t, i, &p, &q);
+        if (q >= r) continue;
+        const T c = rot_c[i], sn = rot_s[i];
+        const cplx<T> ce = cconj(rot_e[i]);
+        const cplx<T> akp = A[k][p], kq_ce = cmul(A[k][q], ce);
+        A[k][p] = mk<T>(akp.re * c - kq_ce.re * sn, akp.im * c - kq_ce.im * sn);
+        A[k][q] = mk<T>(akp.re * sn + kq_ce.re * c, akp.im * sn + kq_ce.im * c);
+        const cplx<T> vkp = V[k][p], vq_ce = cmul(V[k][q], ce);
+        V[k][p] = mk<T>(vkp.re * c - vq_ce.re * sn, vkp.im * c - vq_ce.im * sn);
+        V[k][q] = mk<T>(vkp.re * sn + vq_ce.re * c, vkp.im * sn + vq_ce.im * c);
+      }
+      __syncthreads();
+      // rows: A[p][k], A[q][k] <- (c A_pk - s e A_qk, s A_pk + c e A_qk)  (U^H from the left)
+      for (int e = tid; e < r * (N / 2); e += nt) {
+        const int i = e / r, k = e - i * r;
+        int p, q;
+        rr_pair(N, t, i, &p, &q);
+        if (q >= r) continue;
+        const T c = rot_c[i], sn = rot_s[i];
+        const cplx<T> apk = A[p][k], e_qk = cmul(rot_e[i], A[q][k]);
+        A[p][k] = mk<T>(apk.re * c - e_qk.re * sn, apk.im * c - e_qk.im * sn);
+        A[q][k] = mk<T>(apk.re * sn + e_qk.re * c, apk.im * sn + e_qk.im * c);
+      }
+      __syncthreads();
+    }
+    __syncthreads();
+    if (!*s_sweep) break;  // uniform: a sweep without rotations leaves nothing to do
+  }
+}
+
 __global__ void __launch_bounds__(256) small_rr_kernel(const zd* __restrict__ Mg, const zd* __restrict__ Gg, int n,
                                                        int m, double drop, double* __restrict__ theta,
                                                        zd* __restrict__ Cg, int* __restrict__ keep, BatchMap bm,
                                                        long mat_stride, long theta_stride) {
-  constexpr int L = kRRMax + 1;
+  constexpr int L = kRRL;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   zd(*W)[L] = reinterpret_cast<zd(*)[L]>(smem_raw);  // scaled Gram, its Schur complements; the compact R; G B
   zd(*R)[L] = W + kRRMax;                           // Cholesky rows in kept order; then the basis B (n x r)
   zd(*Gs)[L] = R + kRRMax;                          // G, then B^H G B
-  zd(*A)[L] = Gs + kRRMax;                          // R^-1; then the projected matrix, diagonalised in place
-  zd(*V)[L] = A + kRRMax;                           // eigenvectors of A
+  zd(*A)[L] = Gs + kRRMax;                          // R^-1; then the projected matrix
+  zd(*V)[L] = A + kRRMax;                           // eigenvectors of A (FP64 route)
   __shared__ double dinv[kRRMax], rinv[kRRMax], rot_c[kRRMax / 2], rot_s[kRRMax / 2], offs[8], dias[8];
   __shared__ zd rot_e[kRRMax / 2];
   __shared__ int perm[kRRMax], order[kRRMax];
-  __shared__ int s_r, s_done;
+  __shared__ int s_r, s_done, s_near, s_any, s_sweep;
   const int sys = blockIdx.x;
   if (bm_frozen(bm, sys)) return;
   Mg += (size_t)sys * mat_stride;
@@ -152,6 +317,86 @@ __global__ void __launch_bounds__(256) small_rr_kernel(const zd* __restrict__ Mg
   Cg += (size_t)sys * mat_stride;
   theta += (size_t)sys * theta_stride;
   const int tid = threadIdx.x, nt = blockDim.x;
+  // near-identity route when M = I + E with max |E| < 1e-5 (the final block is orthonormal to FP32 rounding):
+  // B = M^(-1/2) = I - E/2 + 3/8 E^2 to O(|E|^3) < 1e-15, from products alone (no FP64 division or square root,
+  // which this GPU issues at a fraction of the FP32 rate)
+  if (tid == 0) s_near = 1;
+  __syncthreads();
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e / n, j = e - i * n;
+    const zd a = Mg[(size_t)i * n + j];
+    const double dr = a.re - (i == j ? 1.0 : 0.0);
+    if (!(fabs(dr) < 1e-5 && fabs(a.im) < 1e-5)) s_near = 0;  // benign race: every writer stores 0
+  }
+  __syncthreads();
+  if (s_near) {
+    for (int e = tid; e < n * n; e += nt) {
+      const int i = e / n, j = e - i * n;
+      const zd a = Mg[(size_t)i * n + j], b = Mg[(size_t)j * n + i];
+      W[i][j] = mk<double>(0.5 * (a.re + b.re) - (i == j ? 1.0 : 0.0), i == j ? 0.0 : 0.5 * (a.im - b.im));  // E
+      const zd g = Gg[(size_t)i * n + j], h = Gg[(size_t)j * n + i];
+      Gs[i][j] = mk<double>(0.5 * (g.re + h.re), i == j ? 0.0 : 0.5 * (g.im - h.im));
+    }
+    __syncthreads();
+    for (int e = tid; e < n * n; e += nt) {  // B = I - E/2 + 3/8 E^2
+      const int i = e / n, j = e - i * n;
+      zd e2 = mk<double>(0.0, 0.0);
+      for (int k = 0; k < n; ++k) e2 = zadd(e2, zmul(W[i][k], W[k][j]));
+      R[i][j] = mk<double>((i == j ? 1.0 : 0.0) - 0.5 * W[i][j].re + 0.375 * e2.re, -0.5 * W[i][j].im + 0.375 * e2.im);
+    }
+    __syncthreads();
+    for (int e = tid; e < n * n; e += nt) {  // T = G B
+      const int i = e / n, j = e - i * n;
+      zd acc = mk<double>(0.0, 0.0);
+      for (int k = 0; k < n; ++k) acc = zadd(acc, zmul(Gs[i][k], R[k][j]));
+      W[i][j] = acc;
+    }
+    __syncthreads();
+    for (int e = tid; e < n * n; e += nt) {  // Gp = B T (B Hermitian)
+      const int i = e / n, j = e - i * n;
+      zd acc = mk<double>(0.0, 0.0);
+      for (int k = 0; k < n; ++k) acc = zadd(acc, zmul(R[i][k], W[k][j]));
+      A[i][j] = acc;
+    }
+    __syncthreads();
+    for (int e = tid; e < n * n; e += nt) {  // Hermitian part
+      const int i = e / n, j = e - i * n;
+      const zd x = A[i][j], y = A[j][i];
+      Gs[i][j] = mk<double>(0.5 * (x.re + y.re), i == j ? 0.0 : 0.5 * (x.im - y.im));
+    }
+    __syncthreads();
+    for (int e = tid; e < n * n; e += nt) {
+      const int i = e / n, j = e - i * n;
+      A[i][j] = Gs[i][j];
+      V[i][j] = mk<double>(i == j ? 1.0 : 0.0, 0.0);
+    }
+    __syncthreads();
+    // the final projected matrix is diagonal to the iteration's residual: one sweep does nearly all the rotations
+    // and the next ones skip the negligible ones (angles below 1e-10)
+    jacobi_cta<double>(A, V, n, 1e-30, 1e-10, rot_c, rot_s, rot_e, offs, dias, &s_done, &s_any, &s_sweep);
+    for (int a = tid; a < n; a += nt) {
+      const double va = A[a][a].re;
+      int rank = 0;
+      for (int b = 0; b < n; ++b) {
+        const double vb = A[b][b].re;
+        rank += (vb < va || (vb == va && b < a)) ? 1 : 0;
+      }
+      order[rank] = a;
+    }
+    __syncthreads();
+    // C = B Y[:, order[0:m]]
+    for (int e = tid; e < n * m; e += nt) {
+      const int i = e / m, k = e - i * m;
+      const int col = order[k];
+      zd acc = mk<double>(0.0, 0.0);
+      for (int c = 0; c < n; ++c) acc = zadd(acc, zmul(R[i][c], V[c][col]));
+      Cg[(size_t)i * m + k] = acc;
+    }
+    for (int k = tid; k < m; k += nt) theta[k] = A[order[k]][order[k]].re;
+    if (tid == 0 && keep) keep[sys] = n;
+    return;
+  }
+  // general route: FP64 scaled Cholesky with drops, R^-1, projection and Jacobi
   for (int i = tid; i < n; i += nt) {
     const double d = Mg[(size_t)i * n + i].re;
     dinv[i] = d > 1e-300 ? 1.0 / sqrt(d) : 0.0;
@@ -244,95 +489,7 @@ __global__ void __launch_bounds__(256) small_rr_kernel(const zd* __restrict__ Mg
   // the padding player is skipped.  Rotation of pair (p, q): with A_pq = g e (g = |A_pq|, |e| = 1) and
   // zeta = (A_qq - A_pp) / (2 g), t = sign(zeta) / (|zeta| + sqrt(1 + zeta^2)), c = 1 / sqrt(1 + t^2), s = t c,
   // U = [[c, s], [-s conj(e), c conj(e)]] on (p, q) makes (U^H A U)_pq = 0; A <- U^H A U, V <- V U.
-  const int N = (r + 1) & ~1;
-  for (int sweep = 0; sweep < 40 && r > 1; ++sweep) {
-    // convergence: off-diagonal mass against the diagonal's
-    double off = 0.0, dia = 0.0;
-    for (int e = tid; e < r * r; e += nt) {
-      const int a = e / r, b = e - a * r;
-      const double v = A[a][b].re * A[a][b].re + A[a][b].im * A[a][b].im;
-      if (a == b)
-        dia += v;
-      else
-        off += v;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      off += __shfl_xor_sync(0xffffffffu, off, o);
-      dia += __shfl_xor_sync(0xffffffffu, dia, o);
-    }
-    if ((tid & 31) == 0) {
-      offs[tid >> 5] = off;
-      dias[tid >> 5] = dia;
-    }
-    __syncthreads();
-    if (tid == 0) {
-      double o = 0.0, d = 0.0;
-      for (int w = 0; w < (nt >> 5); ++w) {
-        o += offs[w];
-        d += dias[w];
-      }
-      // off-diagonal mass below (1e-15)^2 of the diagonal's: rotations no longer change any value by more than
-      // an FP64 rounding
-      s_done = o <= 1e-30 * d ? 1 : 0;
-    }
-    __syncthreads();
-    if (s_done) break;
-    for (int t = 0; t < N - 1; ++t) {
-      if (tid < N / 2) {
-        int p, q;
-        rr_pair(N, t, tid, &p, &q);
-        double c = 1.0, sn = 0.0;
-        zd ee = mk<double>(1.0, 0.0);
-        if (q < r) {
-          const zd apq = A[p][q];
-          const double g = sqrt(apq.re * apq.re + apq.im * apq.im);
-          if (g > 1e-300) {
-            ee = mk<double>(apq.re / g, apq.im / g);
-            const double zeta = (A[q][q].re - A[p][p].re) / (2.0 * g);
-            const double tt = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-            c = 1.0 / sqrt(1.0 + tt * tt);
-            sn = tt * c;
-          }
-        }
-        rot_c[tid] = c;
-        rot_s[tid] = sn;
-        rot_e[tid] = ee;
-      }
-      __syncthreads();
-      // columns: A[k][p], A[k][q] <- (A_kp c - A_kq s conj(e), A_kp s + A_kq c conj(e)); V likewise
-      for (int e = tid; e < r * (N / 2); e += nt) {
-        const int i = e / r, k = e - i * r;
-        int p, q;
-        rr_pair(N, t, i, &p, &q);
-        if (q >= r) continue;
-        const double c = rot_c[i], sn = rot_s[i];
-        const zd ce = zconj(rot_e[i]);
-        const zd akp = A[k][p], akq = A[k][q];
-        const zd kq_ce = zmul(akq, ce);
-        A[k][p] = mk<double>(akp.re * c - kq_ce.re * sn, akp.im * c - kq_ce.im * sn);
-        A[k][q] = mk<double>(akp.re * sn + kq_ce.re * c, akp.im * sn + kq_ce.im * c);
-        const zd vkp = V[k][p], vkq = V[k][q];
-        const zd vq_ce = zmul(vkq, ce);
-        V[k][p] = mk<double>(vkp.re * c - vq_ce.re * sn, vkp.im * c - vq_ce.im * sn);
-        V[k][q] = mk<double>(vkp.re * sn + vq_ce.re * c, vkp.im * sn + vq_ce.im * c);
-      }
-      __syncthreads();
-      // rows: A[p][k], A[q][k] <- (c A_pk - s e A_qk, s A_pk + c e A_qk)  (U^H from the left)
-      for (int e = tid; e < r * (N / 2); e += nt) {
-        const int i = e / r, k = e - i * r;
-        int p, q;
-        rr_pair(N, t, i, &p, &q);
-        if (q >= r) continue;
-        const double c = rot_c[i], sn = rot_s[i];
-        const zd ev = rot_e[i];
-        const zd apk = A[p][k], aqk = A[q][k];
-        const zd e_qk = zmul(ev, aqk);
-        A[p][k] = mk<double>(apk.re * c - e_qk.re * sn, apk.im * c - e_qk.im * sn);
-        A[q][k] = mk<double>(apk.re * sn + e_qk.re * c, apk.im * sn + e_qk.im * c);
-      }
-      __syncthreads();
-    }
-  }
+  jacobi_cta<double>(A, V, r, 1e-30, 0.0, rot_c, rot_s, rot_e, offs, dias, &s_done, &s_any, &s_sweep);
   // ascending order of the eigenvalues (rank by comparison; ties by index)
   for (int a = tid; a < r; a += nt) {
     const double va = A[a][a].re;
@@ -371,6 +528,16 @@ cudaError_t launch_gram_pair_dot2(const zf* A, const zf* B, int ld, int p, int n
     gram_pair_dot2_kernel<2><<<npart, 256, 0, s>>>(A, B, ld, p, nrow, partial, rpp, npart, bm);
   ++g_launch_count;
   return launch_sum_partials_pair(partial, npart, p * p * 2, outM, outG, s, bm, out_stride);
+}
+
+cudaError_t launch_update_dot2(const zf* X, int ldx, int nin, const zd* C, int ldc, int nout, int nrow, zd* Out,
+                               int ldo, cudaStream_t s, const BatchMap& bm, long c_stride) {
+  if (nin < 1 || nin > 32 || nout < 1 || nout > 32) return cudaErrorInvalidValue;
+  long nblk = ((long)nrow + kTileRows - 1) / kTileRows;
+  if (nblk > 152 * 16) nblk = 152 * 16;
+  update_dot2_kernel<<<(unsigned)nblk, 256, 0, s>>>(X, ldx, nin, C, ldc, nout, nrow, Out, ldo, bm, c_stride);
+  ++g_launch_count;
+  return cudaGetLastError();
 }
 
 cudaError_t launch_small_rr(const zd* M, const zd* G, int n, int m, double drop, double* theta, zd* C, int* keep,

@@ -152,7 +152,22 @@ __device__ void tridiag_cta(cplx<S>* A, int lda, int n, S* d, S* e, cplx<S>* tau
       __syncwarp();
       if (j + 1 < n - 1) reflector_warp<S>(A, lda, n, j + 1, d, e, tau);
     } else {
-      for (int r = warp; r < L; r += nwarp - 1) update_row(r);
+      // rows 1 .. L-1 element by element over the other warps' threads: independent updates, several in flight
+      // per thread (each element's arithmetic is update_row's)
+      const int nt1 = nt - 32, t1 = tid - 32, ne = (L - 1) * L;
+      const float rL = 1.0f / (float)L;
+#pragma unroll 4
+      for (int e = t1; e < ne; e += nt1) {
+        const int r = 1 + qdiv(e, rL), c = e - (r - 1) * L;
+        const cplx<S> vr = v[r], pr = p[r], vc = v[c], pc = p[c];
+        const cplx<S> wr = mk<S>(pr.re + K.re * vr.re - K.im * vr.im, pr.im + K.re * vr.im + K.im * vr.re);
+        const cplx<S> wc = mk<S>(pc.re + K.re * vc.re - K.im * vc.im, pc.im + K.re * vc.im + K.im * vc.re);
+        const S re = vr.re * wc.re + vr.im * wc.im + wr.re * vc.re + wr.im * vc.im;
+        const S im = vr.im * wc.re - vr.re * wc.im + wr.im * vc.re - wr.re * vc.im;
+        cplx<S>& a = A22[(size_t)r * lda + c];
+        a.re -= re;
+        a.im -= im;
+      }
     }
     __syncthreads();
   }

@@ -781,22 +781,26 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
     const cudaError_t fe = op.apply(X, ld, 0, m, AX, ld, s);
     op.set_final(false);
     CK(fe);
-    CK((launch_convert_cols<S, double>(X, ld, X64, 2 * m, m, nrow, s)));
-    CK((launch_convert_cols<S, double>(AX, ld, X64 + m, 2 * m, m, nrow, s)));
     if (sizeof(S) == 4 && m <= 32) {
-      // FP32 data: Grams by compensated FP32 sums of the exact products, then the small problem by Jacobi, both
-      // FP64-accurate (k_final.cu)
-      CK(launch_gram_pair_dot2(reinterpret_cast<const zf*>(X), reinterpret_cast<const zf*>(AX), ld, m, nrow, sm.M,
-                               sm.G, partial, npart, s, bmf, nn));
+      // FP32 data: the Grams, the small problem and the combinations X C, AX C with FP64 accuracy from FP32
+      // instructions (k_final.cu)
+      const zf* Xf = reinterpret_cast<const zf*>(X);
+      const zf* AXf = reinterpret_cast<const zf*>(AX);
+      CK(launch_gram_pair_dot2(Xf, AXf, ld, m, nrow, sm.M, sm.G, partial, npart, s, bmf, nn));
       CK(launch_small_rr(sm.M, sm.G, m, m, 1e-13, sm.theta, sm.C, sm.keep, s, bmf, nn, nb));
+      // Xout = X C[:, :nev]; residual = (AX C - Xout theta)
+      CK(launch_update_dot2(Xf, ld, m, sm.C, m, nev, nrow, Xout, nev, s, bmf, nn));
+      CK(launch_update_dot2(AXf, ld, m, sm.C, m, nev, nrow, T64, nev, s, bmf, nn));
     } else {
+      CK((launch_convert_cols<S, double>(X, ld, X64, 2 * m, m, nrow, s)));
+      CK((launch_convert_cols<S, double>(AX, ld, X64 + m, 2 * m, m, nrow, s)));
       int r = rayleigh_ritz<double>(X64, X64 + m, 2 * m, m, m, nrow, 1e-13, sm, partial, npart, st, s, msg, true, bmf,
                                     nn, nb);
       if (r) return r;
+      // Xout = X64 C[:, :nev]; residual = (AX64 C - Xout theta)
+      CK(launch_update<double>(X64, 2 * m, m, sm.C, m, nev, nrow, Xout, nev, 1.0, 0.0, s, bmf, nn));
+      CK(launch_update<double>(X64 + m, 2 * m, m, sm.C, m, nev, nrow, T64, nev, 1.0, 0.0, s, bmf, nn));
     }
-    // Xout = X64 C[:, :nev]; residual = (AX64 C - Xout theta)
-    CK(launch_update<double>(X64, 2 * m, m, sm.C, m, nev, nrow, Xout, nev, 1.0, 0.0, s, bmf, nn));
-    CK(launch_update<double>(X64 + m, 2 * m, m, sm.C, m, nev, nrow, T64, nev, 1.0, 0.0, s, bmf, nn));
     CK(launch_residual<double>(T64, nev, Xout, nev, sm.theta, nev, nrow, T64, nev, partial, npart, norms2, s, bmf, nb));
     return WTB_OK;
   };

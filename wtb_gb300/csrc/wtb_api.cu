@@ -492,7 +492,7 @@ int run_solve(wtb_ctx* c, const wtb_bse_params* p, std::vector<double>* E, wtb_t
   CKC(cudaEventRecord(ev[0], c->s));
   const bool fp64 = p->precision == WTB_PREC_FP64;
   const int m = auto_block(p, dim, fp64);
-  // residual targets: SLEPc's 1e-8 in FP64; kReducedTol (just above the FP32 rounding floor) otherwise.
+  // residual targets: SLEPc's 1e-8 in FP64; kReducedTol (1e-5, at the FP32 rounding floor) otherwise.
   // The reduced-precision forms run in two phases: to 1e-4, then -- from the best block, with a freshly applied
   // operator and the search directions dropped -- to the target (bf16x3 switches to its 6-product operator
   // there).  The restart removes the drift of the FP32 iteration's running H X, which otherwise stalls the
