@@ -517,7 +517,14 @@ def fft_roofline(p, peaks, step_ms, last, g_ms, flops, algo_bytes, launches):
             "launches_per_step": last["timings"]["iterations"] + 3,
             "share_of_step": (g_ms * (last["timings"]["iterations"] + 3) / step_ms) if step_ms > 0 and g_ms > 0
             else None,
-            "traffic": None, "traffic_source": "not captured for this kernel"}
+            "traffic": FFT_TRAFFIC.get("hex12_60x60") if (p.nk == 3600 and p.ngrid[0] == 60) else None,
+            "traffic_source": FFT_TRAFFIC.get("source") if p.nk == 3600 else "not captured for this workload"}
+
+
+# DRAM bytes (read + write) of one fft_conv_kernel<128> launch on the 60 x 60 mesh from one ncu capture
+# (profiles/fft_conv_hex12_60x60.md): below the algorithmic bytes because the L2 absorbs most of T's write
+FFT_TRAFFIC = {"hex12_60x60": 66770176 + 19405568,
+               "source": "profiles/fft_conv_hex12_60x60.md (an ncu --set full capture, not this run)"}
 
 
 def p_name_of(p, sysm):

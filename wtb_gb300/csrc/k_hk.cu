@@ -43,13 +43,56 @@ __device__ __forceinline__ double rcomp_f32(const int* rvec, int nR, int iR, con
   return (double)__double2float_rn(rcart(r1, r2, r3, rl, a));
 }
 
+// Double-float (FP32 pair, value = hi + lo) sums for the mixed band route, where the FP64 pipe (1/64 of the FP32
+// rate on this GPU) bounds the FP64 sums: each product keeps its exact rounding error (FMA) and each running sum
+// its exact TwoSum error, the low parts added without renormalisation (the Dot2 scheme of Ogita, Rump and
+// Oishi, "Accurate sum and dot product", SIAM J. Sci. Comput. 26 (2005), with double-float inputs): about 2^-48
+// relative to the sum of |terms| per term.  The _rn intrinsics keep the compiler from contracting the steps.
+__device__ __forceinline__ void df_split(double x, float& h, float& l) {
+  h = __double2float_rn(x);
+  l = __double2float_rn(x - (double)h);
+}
+// (ah, al) += (xh, xl) (yh, yl)
+__device__ __forceinline__ void df_mac(float& ah, float& al, float xh, float xl, float yh, float yl) {
+  const float p = __fmul_rn(xh, yh);
+  const float e = __fmaf_rn(xh, yl, __fmaf_rn(xl, yh, __fmaf_rn(xh, yh, -p)));
+  const float sm = __fadd_rn(ah, p);
+  const float bv = __fsub_rn(sm, ah);
+  const float err = __fadd_rn(__fsub_rn(ah, __fsub_rn(sm, bv)), __fsub_rn(p, bv));
+  al = __fadd_rn(al, __fadd_rn(err, e));
+  ah = sm;
+}
+// (ah, al) += (xh, xl) y for an FP32 y
+__device__ __forceinline__ void df_mac1(float& ah, float& al, float xh, float xl, float y) {
+  const float p = __fmul_rn(xh, y);
+  const float e = __fmaf_rn(xl, y, __fmaf_rn(xh, y, -p));
+  const float sm = __fadd_rn(ah, p);
+  const float bv = __fsub_rn(sm, ah);
+  const float err = __fadd_rn(__fsub_rn(ah, __fsub_rn(sm, bv)), __fsub_rn(p, bv));
+  al = __fadd_rn(al, __fadd_rn(err, e));
+  ah = sm;
+}
+__device__ __forceinline__ double df_val(float h, float l) { return (double)h + (double)l; }
+
+// H(R) / 1 split into double-float parts once per band solve: (re hi, re lo, im hi, im lo)
+__global__ void hr_split_kernel(const zd* __restrict__ hr, long n, float4* __restrict__ out) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const zd h = hr[i];
+  float rh, rl, ih, il;
+  df_split(h.re, rh, rl);
+  df_split(h.im, ih, il);
+  out[i] = make_float4(rh, rl, ih, il);
+}
+
 template <bool kMixed>
 __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict__ hr, const int* __restrict__ rvec,
                                                             const int* __restrict__ ndegen, int nR, int w,
                                                             const double* __restrict__ rlat, double efermi, double scs,
                                                             const double* __restrict__ kpt, int nk, int nv, int nc,
                                                             double* eig_all, zd* vec_all, double* eig_win,
-                                                            zd* vec_win, int* nocp_out, DevStatus* st) {
+                                                            zd* vec_win, int* nocp_out, DevStatus* st,
+                                                            const float4* __restrict__ hr_df) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int k = blockIdx.x;
   if (k >= nk) return;
@@ -93,11 +136,40 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
     sincos(phi, &sn, &cs);
     const double inv = 1.0 / (double)ndegen[r];
     eph[r] = mk<double>(cs * inv, sn * inv);
+    if constexpr (kMixed) {
+      float ch, cl, sh, sl;
+      df_split(cs * inv, ch, cl);
+      df_split(sn * inv, sh, sl);
+      reinterpret_cast<float4*>(eph)[r] = make_float4(ch, cl, sh, sl);
+    }
   }
   __syncthreads();
   // ZHEEV('V','L') reads the lower triangle and the real part of the diagonal only: the matrix that is
   // diagonalised is the Hermitian completion of the lower triangle (identical to H(k) when the H(R) set
   // is Hermitian-consistent; a perturbation of an upper-triangle entry does not reach the eigensolve)
+  if constexpr (kMixed) {
+    // the mixed route: H(k) in double-float, Ad[m][c] = (re hi, re lo, im hi, im lo) over A's storage
+    const float4* ephd = reinterpret_cast<const float4*>(eph);
+    float4* Ad = reinterpret_cast<float4*>(A);
+    for (int q = tid; q < n * n; q += blockDim.x) {
+      const int m = q / n, c = q % n;
+      if (m < c) continue;
+      float rh = 0.f, rlo = 0.f, ih = 0.f, il = 0.f;
+      for (int r = 0; r < nR; ++r) {
+        const float4 ph = ephd[r], h = hr_df[((size_t)r * w + m) * w + c];
+        df_mac(rh, rlo, ph.x, ph.y, h.x, h.y);    // cos h.re
+        df_mac(rh, rlo, -ph.z, -ph.w, h.z, h.w);  // - sin h.im
+        df_mac(ih, il, ph.x, ph.y, h.z, h.w);     // cos h.im
+        df_mac(ih, il, ph.z, ph.w, h.x, h.y);     // sin h.re
+      }
+      if (m == c) {
+        df_split(df_val(rh, rlo) - efermi, rh, rlo);
+        ih = il = 0.f;
+      }
+      Ad[m * ld + c] = make_float4(rh, rlo, ih, il);
+      if (m != c) Ad[c * ld + m] = make_float4(rh, rlo, -ih, -il);
+    }
+  } else {
   for (int q = tid; q < n * n; q += blockDim.x) {
     const int m = q / n, c = q % n;
     if (m < c) continue;
@@ -110,11 +182,16 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
     A[m * ld + c] = acc;
     if (m != c) A[c * ld + m] = mk<double>(acc.re, -acc.im);
   }
+  }
   __syncthreads();
   if constexpr (kMixed) {
-    // FP32 eigensolve of the rounded H(k), then FP64 Rayleigh quotients of the normalised vectors against
-    // the FP64 H(k): eigenvalues carry the square of the vectors' FP32 error (FP64-accurate), vectors FP32's
-    for (int q = tid; q < n * ld; q += blockDim.x) A32[q] = mk<float>((float)A[q].re, (float)A[q].im);
+    // FP32 eigensolve of the rounded H(k), then Rayleigh quotients of the normalised vectors against the
+    // double-float H(k): eigenvalues carry the square of the vectors' FP32 error (FP64-accurate), vectors FP32's
+    const float4* Ad = reinterpret_cast<const float4*>(A);
+    for (int q = tid; q < n * ld; q += blockDim.x) {
+      const float4 a = Ad[q];
+      A32[q] = mk<float>(__fadd_rn(a.x, a.y), __fadd_rn(a.z, a.w));
+    }
     __syncthreads();
     zf* U32 = reinterpret_cast<zf*>(Dv32);
     tridiag_cta<float>(A32, ld, n, d32, e32, tau32, p32);
@@ -124,12 +201,16 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
     zd* HU = reinterpret_cast<zd*>((reinterpret_cast<uintptr_t>(Lv32 + n * (n + 1)) + 15) & ~(uintptr_t)15);
     for (int q = tid; q < n * n; q += blockDim.x) {
       const int i = q / n, j = q % n;  // row i of H, column j of U
-      zd acc = mk<double>(0.0, 0.0);
+      float rh = 0.f, rlo = 0.f, ih = 0.f, il = 0.f;
       for (int c = 0; c < n; ++c) {
         const zf u = U32[j * n + c];
-        cfma(acc, A[i * ld + c], mk<double>((double)u.re, (double)u.im));
+        const float4 a = Ad[i * ld + c];
+        df_mac1(rh, rlo, a.x, a.y, u.re);
+        df_mac1(rh, rlo, -a.z, -a.w, u.im);
+        df_mac1(ih, il, a.x, a.y, u.im);
+        df_mac1(ih, il, a.z, a.w, u.re);
       }
-      HU[j * n + i] = acc;
+      HU[j * n + i] = mk<double>(df_val(rh, rlo), df_val(ih, il));
     }
     __syncthreads();
     const int lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
@@ -164,14 +245,18 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
   const int nocp = s_nocp;
   // outputs in ascending order; eigenvector j = column j of U, rotated so that its first component is real
   // and >= 0 (ZHEEV('L') returns it real; the sign does not reach any output)
-  for (int q = tid; q < w * w; q += blockDim.x) {
-    const int j = q / w, o = q % w;
+  // the gauge factor of each vector once (p and d are free after the eigensolve)
+  for (int j = tid; j < w; j += blockDim.x) {
     const zd a0 = U[j * n];
     const double m0 = sqrt(cabs2(a0));
-    zd g = mk<double>(1.0, 0.0);
-    if (m0 > 0.0) g = mk<double>(a0.re / m0, -a0.im / m0);
-    zd val = cmul(U[j * n + o], g);
-    if (o == 0) val = mk<double>(m0, 0.0);
+    p[j] = m0 > 0.0 ? mk<double>(a0.re / m0, -a0.im / m0) : mk<double>(1.0, 0.0);
+    d[j] = m0;
+  }
+  __syncthreads();
+  for (int q = tid; q < w * w; q += blockDim.x) {
+    const int j = q / w, o = q % w;
+    zd val = cmul(U[j * n + o], p[j]);
+    if (o == 0) val = mk<double>(d[j], 0.0);
     if (vec_all) vec_all[((size_t)k * w + j) * w + o] = val;
     const int sl = j - (nocp - nv);
     if (vec_win && sl >= 0 && sl < nv + nc) vec_win[((size_t)k * (nv + nc) + sl) * w + o] = val;
@@ -193,8 +278,9 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
 }
 
 // ----------------------------------------------------------------------------- optics (hlm + optsp)
-// T = double: FP64 throughout (hr_t = hr).  T = float: the Fourier sums in FP32 over an FP32 copy hr_t of H(R),
-// with the per-R factors i R_a e^{i phi}/ndegen formed once per direction (FP64, then rounded).
+// T = double: FP64 throughout (hr_t = hr).  T = float: the Fourier sums and the band contractions in FP32 (an FP32
+// copy hr_t of H(R), the band vectors rounded once per k-point), with the per-R factors i R_a e^{i phi}/ndegen
+// formed once per direction (FP64, then rounded) and the energy factors in FP64.
 template <class T>
 __global__ void __launch_bounds__(kHkThreads) optics_kernel(const cplx<T>* __restrict__ hr_t,
                                                             const int* __restrict__ rvec,
@@ -209,15 +295,19 @@ __global__ void __launch_bounds__(kHkThreads) optics_kernel(const cplx<T>* __res
   if (k >= nk) return;
   const int tid = threadIdx.x;
   const int nb = nv + nc;
-  zd* M = reinterpret_cast<zd*>(smem_raw);   // w*w
-  zd* B = M + w * w;                         // nb*w band vectors
-  zd* Mv = B + nb * w;                       // nv*w
-  zd* eph = Mv + nv * w;                     // nR
+  // M, B, Mv in precision T over regions sized for complex(8)
+  cplx<T>* M = reinterpret_cast<cplx<T>*>(smem_raw);                    // w*w
+  cplx<T>* B = reinterpret_cast<cplx<T>*>(reinterpret_cast<zd*>(M) + w * w);   // nb*w band vectors
+  cplx<T>* Mv = reinterpret_cast<cplx<T>*>(reinterpret_cast<zd*>(B) + nb * w);  // nv*w
+  zd* eph = reinterpret_cast<zd*>(Mv) + nv * w;                          // nR
   cplx<T>* fr = reinterpret_cast<cplx<T>*>(eph + nR);  // nR (16-byte aligned after the complex(8) arrays)
   double* Ra = reinterpret_cast<double*>(fr + nR);     // nR
   __shared__ double rl[9];
   if (tid < 9) rl[tid] = rlat[tid];
-  for (int e = tid; e < nb * w; e += blockDim.x) B[e] = vec_win[(size_t)k * nb * w + e];
+  for (int e = tid; e < nb * w; e += blockDim.x) {
+    const zd b = vec_win[(size_t)k * nb * w + e];
+    B[e] = mk<T>((T)b.re, (T)b.im);
+  }
   __syncthreads();
   const double kx = kpt[3 * k], ky = kpt[3 * k + 1], kz = kpt[3 * k + 2];
   for (int r = tid; r < nR; r += blockDim.x) {
@@ -245,20 +335,21 @@ __global__ void __launch_bounds__(kHkThreads) optics_kernel(const cplx<T>* __res
       const int m = e / w, c = e % w;
       cplx<T> acc = mk<T>(0, 0);
       for (int r = 0; r < nR; ++r) cfma(acc, fr[r], hr_t[((size_t)r * w + m) * w + c]);
-      M[e] = mk<double>((double)acc.re, (double)acc.im);
+      M[e] = acc;
     }
     __syncthreads();
     for (int e = tid; e < nv * w; e += blockDim.x) {
       const int v = e / w, m = e % w;
-      zd acc = mk<double>(0.0, 0.0);
+      cplx<T> acc = mk<T>(0, 0);
       for (int c = 0; c < w; ++c) cfma(acc, M[m * w + c], B[v * w + c]);
       Mv[e] = acc;
     }
     __syncthreads();
     for (int e = tid; e < dimk; e += blockDim.x) {
       const int c = e / nv, v = e % nv;
-      zd acc = mk<double>(0.0, 0.0);
-      for (int m = 0; m < w; ++m) cfmac(acc, B[(nv + c) * w + m], Mv[v * w + m]);
+      cplx<T> acct = mk<T>(0, 0);
+      for (int m = 0; m < w; ++m) cfmac(acct, B[(nv + c) * w + m], Mv[v * w + m]);
+      const zd acc = mk<double>((double)acct.re, (double)acct.im);
       // factor = Re(1/(E_c - E_v + i*CSHIFT_f32)) (a complex assigned to a real in optsp)
       const double de = eig_win[(size_t)k * nb + nv + c] - eig_win[(size_t)k * nb + v];
       const double sf = (double)s32;
@@ -451,8 +542,9 @@ __global__ void transition_kernel(const double* __restrict__ eig_win, int nk, in
 cudaError_t launch_hk_eig(const zd* hr, const int* rvec, const int* ndegen, int nR, int w, const double* rlat_rm,
                           double efermi, double scs, const double* kpt, int nk, int nv, int nc, double* eig_all,
                           zd* vec_all, double* eig_win, zd* vec_win, int* nocp, DevStatus* st, cudaStream_t s,
-                          bool mixed) {
+                          bool mixed, float4* hr_df) {
   if (w > 64 || w < 1) return cudaErrorInvalidValue;
+  if (mixed && !hr_df) return cudaErrorInvalidValue;
   const int n = w;
   // A, phases, p, tau (complex); d, e, e2, lam, red; Z, Dv, Lv (n x (n + 1) each); cluster ids
   size_t smem = (size_t)(n * (n + 1) + nR + 2 * n) * sizeof(zd) + (size_t)(4 * n + 4 + 3 * n * (n + 1)) * sizeof(double) +
@@ -466,12 +558,16 @@ cudaError_t launch_hk_eig(const zd* hr, const int* rvec, const int* ndegen, int 
   const void* fn = mixed ? reinterpret_cast<const void*>(hk_eig_kernel<true>) : reinterpret_cast<const void*>(hk_eig_kernel<false>);
   cudaError_t e = raise_smem_limit(fn, (size_t)smem);
   if (e != cudaSuccess) return e;
-  if (mixed)
+  if (mixed) {
+    const long nh = (long)nR * w * w;
+    hr_split_kernel<<<(unsigned)((nh + 255) / 256), 256, 0, s>>>(hr, nh, hr_df);
+    ++g_launch_count;
     hk_eig_kernel<true><<<nk, kHkThreads, smem, s>>>(hr, rvec, ndegen, nR, w, rlat_rm, efermi, scs, kpt, nk, nv, nc,
-                                                     eig_all, vec_all, eig_win, vec_win, nocp, st);
-  else
+                                                     eig_all, vec_all, eig_win, vec_win, nocp, st, hr_df);
+  } else {
     hk_eig_kernel<false><<<nk, kHkThreads, smem, s>>>(hr, rvec, ndegen, nR, w, rlat_rm, efermi, scs, kpt, nk, nv, nc,
-                                                      eig_all, vec_all, eig_win, vec_win, nocp, st);
+                                                      eig_all, vec_all, eig_win, vec_win, nocp, st, nullptr);
+  }
   ++g_launch_count;
   return cudaGetLastError();
 }

@@ -53,7 +53,7 @@ struct ZStore<uint16_t> {
 
 template <class S, class Z>
 __global__ void __launch_bounds__(256) mf_gather_kernel(const cplx<S>* __restrict__ X, int ldx, int c0,
-                                                        const zd* __restrict__ vec_win, int nk, int nv, int nc, int w,
+                                                        const cplx<S>* __restrict__ vec_win, int nk, int nv, int nc, int w,
                                                         int KT, Z* __restrict__ zt, int ldk, int nslices,
                                                         long slice_stride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -68,9 +68,7 @@ __global__ void __launch_bounds__(256) mf_gather_kernel(const cplx<S>* __restric
   const int tid = threadIdx.x, nt = blockDim.x;
   for (int e = tid; e < KT * nb * w; e += nt) {
     const int kk = e / (nb * w), s = (e / w) % nb, o = e % w;
-    zd a = mk<double>(0.0, 0.0);
-    if (kk < tkn) a = vec_win[((size_t)(kt0 + kk) * nb + s) * w + o];
-    const cplx<S> as = mk<S>((S)a.re, (S)a.im);
+    const cplx<S> as = kk < tkn ? vec_win[((size_t)(kt0 + kk) * nb + s) * w + o] : mk<S>(0, 0);
     if (s < nv)
       Vs[(kk * nv + s) * w + o] = as;
     else
@@ -113,9 +111,9 @@ __global__ void __launch_bounds__(256) mf_gather_kernel(const cplx<S>* __restric
 // last tile give zeros (x = 0).
 // F32: the same tile writes FP32 Z rows instead, z32[n][ldk] (n = ((b w + o) w + p) 2 + ri, k' contiguous; ldk a
 // multiple of 64, so the tile's KT values are 16-byte aligned; k' >= nk inside the last tile get zeros).
-template <int KT, bool F32 = false>
+template <int KT, bool F32 = false, class VT = zd>
 __device__ __forceinline__ void gather_bf16_tile(const zf* __restrict__ X, int ldx, int c0, int nbc, int nbp,
-                                                 const zd* __restrict__ vec_win, int nk, int nv, int nc, int w,
+                                                 const VT* __restrict__ vec_win, int nk, int nv, int nc, int w,
                                                  uint16_t* __restrict__ zt, int ldn, int nslices, long slice_stride,
                                                  int kt0, float* __restrict__ z32 = nullptr, int ldk = 0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -131,9 +129,11 @@ __device__ __forceinline__ void gather_bf16_tile(const zf* __restrict__ X, int l
   for (int e = tid; e < KT * nbnd * w; e += nt) {
     const int q = qdiv(e, r_w), o = e - q * w;  // q = kk * nbnd + sb
     const int kk = qdiv(q, r_nbnd), sb = q - kk * nbnd;
-    zd a = mk<double>(0.0, 0.0);
-    if (kk < tkn) a = vec_win[((size_t)(kt0 + kk) * nbnd + sb) * w + o];
-    const zf as = mk<float>((float)a.re, (float)a.im);
+    zf as = mk<float>(0.f, 0.f);
+    if (kk < tkn) {
+      const VT a = vec_win[((size_t)(kt0 + kk) * nbnd + sb) * w + o];
+      as = mk<float>((float)a.re, (float)a.im);
+    }
     if (sb < nv)
       Vs[(kk * nv + sb) * w + o] = as;
     else
@@ -150,59 +150,93 @@ __device__ __forceinline__ void gather_bf16_tile(const zf* __restrict__ X, int l
       xs[r * nbp + bb] = kk < tkn ? X[((size_t)kt0 * ncv + r) * ldx + c0 + b0 + bb] : mk<float>(0.f, 0.f);
     }
     __syncthreads();
-    // Y1[kk][c][p][bb] = sum_v Vb[kk][v][p] x[kk][c][v][bb]
-    for (int e = tid; e < KT * nc * w * nbl; e += nt) {
-      const int q = qdiv(e, r_nbl), bb = e - q * nbl;  // q = (kk * nc + c) * w + p
-      const int kc = qdiv(q, r_w), p = q - kc * w;       // kc = kk * nc + c
-      const int kk = qdiv(kc, r_nc), c = kc - kk * nc;
-      zf acc = mk<float>(0.f, 0.f);
-      for (int v = 0; v < nv; ++v) cfma(acc, Vs[(kk * nv + v) * w + p], xs[(kk * ncv + c * nv + v) * nbp + bb]);
-      Y1[q * nbp + bb] = acc;
+    // Y1[kk][c][p][bb] = sum_v Vb[kk][v][p] x[kk][c][v][bb]: a thread takes one (kk, p, bb) and four c at a time,
+    // each band-vector value loaded once for them (every sum runs over v in the same order as one c alone)
+    for (int e = tid; e < KT * w * nbl; e += nt) {
+      const int q = qdiv(e, r_nbl), bb = e - q * nbl;  // q = kk * w + p
+      const int kk = qdiv(q, r_w), p = q - kk * w;
+      for (int cb = 0; cb < nc; cb += 4) {
+        zf acc[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) acc[i] = mk<float>(0.f, 0.f);
+        for (int v = 0; v < nv; ++v) {
+          const zf a = Vs[(kk * nv + v) * w + p];
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+            if (cb + i < nc) cfma(acc[i], a, xs[(kk * ncv + (cb + i) * nv + v) * nbp + bb]);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (cb + i < nc) Y1[((kk * nc + cb + i) * w + p) * nbp + bb] = acc[i];
+      }
     }
     __syncthreads();
-    // items (bb, o, p), bb fastest across lanes (Y1 reads are then consecutive in shared memory): Z over the
-    // tile's KT k', re and im rows, every slice
-    for (int it = tid; it < nbl * ww; it += nt) {
-      const int op = qdiv(it, r_nbl), bb = it - op * nbl, o = qdiv(op, r_w), p = op - o * w;
-      float zr[KT], zi[KT];
+    // items (bb, o group, p), bb fastest across lanes (Y1 reads are then consecutive in shared memory): Z over the
+    // tile's KT k' for OG consecutive o (each Y1 value loaded once for them; OG = 2 for the 8-wide tile, whose
+    // accumulators then take the registers of the 16-wide tile's single o), re and im rows, every slice
+    constexpr int OG = KT <= 8 ? 2 : 1;
+    const int wo = (w + OG - 1) / OG;  // o groups
+    for (int it = tid; it < nbl * wo * w; it += nt) {
+      const int op = qdiv(it, r_nbl), bb = it - op * nbl, o2 = qdiv(op, r_w), p = op - o2 * w;
+      float zr[OG][KT], zi[OG][KT];
+      const int nog = min(OG, w - OG * o2);
 #pragma unroll
       for (int kk = 0; kk < KT; ++kk) {
-        zf acc = mk<float>(0.f, 0.f);
-        for (int c = 0; c < nc; ++c)
-          cfma(acc, Cs[(kk * nc + c) * w + o], Y1[((kk * nc + c) * w + p) * nbp + bb]);
-        zr[kk] = acc.re;
-        zi[kk] = acc.im;
-      }
-      const long row = ((long)((b0 + bb) * w + o) * w + p) * 2;
-      if constexpr (F32) {
-        float4* dre = reinterpret_cast<float4*>(z32 + row * ldk + kt0);
-        float4* dim = reinterpret_cast<float4*>(z32 + (row + 1) * ldk + kt0);
+        zf acc[OG];
 #pragma unroll
-        for (int h = 0; h < KT / 4; ++h) {
-          dre[h] = make_float4(zr[4 * h], zr[4 * h + 1], zr[4 * h + 2], zr[4 * h + 3]);
-          dim[h] = make_float4(zi[4 * h], zi[4 * h + 1], zi[4 * h + 2], zi[4 * h + 3]);
+        for (int g = 0; g < OG; ++g) acc[g] = mk<float>(0.f, 0.f);
+        for (int c = 0; c < nc; ++c) {
+          const zf y = Y1[((kk * nc + c) * w + p) * nbp + bb];
+          const zf* cr = Cs + (kk * nc + c) * w + OG * o2;
+#pragma unroll
+          for (int g = 0; g < OG; ++g)
+            if (g < nog) cfma(acc[g], cr[g], y);
         }
-        continue;
+#pragma unroll
+        for (int g = 0; g < OG; ++g) {
+          zr[g][kk] = acc[g].re;
+          zi[g][kk] = acc[g].im;
+        }
       }
-      const long off_re = ((long)(kt0 >> 6) * ldn + row) * 64 + (kt0 & 63), off_im = off_re + 64;
-      for (int sl = 0; sl < nslices; ++sl) {
 #pragma unroll
-        for (int h = 0; h < KT / 8; ++h) {
-          uint32_t pr[4], pi[4];
+      for (int ho = 0; ho < OG; ++ho) {
+        if (ho >= nog) break;
+        const int o = OG * o2 + ho;
+        const long row = ((long)((b0 + bb) * w + o) * w + p) * 2;
+        if constexpr (F32) {
+          float4* dre = reinterpret_cast<float4*>(z32 + row * ldk + kt0);
+          float4* dim = reinterpret_cast<float4*>(z32 + (row + 1) * ldk + kt0);
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const int k0 = 8 * h + 2 * q;
-            const __nv_bfloat16 r0 = __float2bfloat16_rn(zr[k0]), r1 = __float2bfloat16_rn(zr[k0 + 1]);
-            const __nv_bfloat16 i0 = __float2bfloat16_rn(zi[k0]), i1 = __float2bfloat16_rn(zi[k0 + 1]);
-            zr[k0] -= __bfloat162float(r0);
-            zr[k0 + 1] -= __bfloat162float(r1);
-            zi[k0] -= __bfloat162float(i0);
-            zi[k0 + 1] -= __bfloat162float(i1);
-            pr[q] = (uint32_t)__bfloat16_as_ushort(r0) | ((uint32_t)__bfloat16_as_ushort(r1) << 16);
-            pi[q] = (uint32_t)__bfloat16_as_ushort(i0) | ((uint32_t)__bfloat16_as_ushort(i1) << 16);
+          for (int h = 0; h < KT / 4; ++h) {
+            dre[h] = make_float4(zr[ho][4 * h], zr[ho][4 * h + 1], zr[ho][4 * h + 2], zr[ho][4 * h + 3]);
+            dim[h] = make_float4(zi[ho][4 * h], zi[ho][4 * h + 1], zi[ho][4 * h + 2], zi[ho][4 * h + 3]);
           }
-          *reinterpret_cast<uint4*>(zt + sl * slice_stride + off_re + 8 * h) = make_uint4(pr[0], pr[1], pr[2], pr[3]);
-          *reinterpret_cast<uint4*>(zt + sl * slice_stride + off_im + 8 * h) = make_uint4(pi[0], pi[1], pi[2], pi[3]);
+        } else {
+          const long off_re = ((long)(kt0 >> 6) * ldn + row) * 64 + (kt0 & 63), off_im = off_re + 64;
+          for (int sl = 0; sl < nslices; ++sl) {
+#pragma unroll
+            for (int h = 0; h < KT / 8; ++h) {
+              uint32_t pr[4], pi[4];
+#pragma unroll
+              for (int q = 0; q < 4; ++q) {
+                const int k0 = 8 * h + 2 * q;
+                float* zrr = zr[ho];
+                float* zii = zi[ho];
+                const __nv_bfloat16 r0 = __float2bfloat16_rn(zrr[k0]), r1 = __float2bfloat16_rn(zrr[k0 + 1]);
+                const __nv_bfloat16 i0 = __float2bfloat16_rn(zii[k0]), i1 = __float2bfloat16_rn(zii[k0 + 1]);
+                zrr[k0] -= __bfloat162float(r0);
+                zrr[k0 + 1] -= __bfloat162float(r1);
+                zii[k0] -= __bfloat162float(i0);
+                zii[k0 + 1] -= __bfloat162float(i1);
+                pr[q] = (uint32_t)__bfloat16_as_ushort(r0) | ((uint32_t)__bfloat16_as_ushort(r1) << 16);
+                pi[q] = (uint32_t)__bfloat16_as_ushort(i0) | ((uint32_t)__bfloat16_as_ushort(i1) << 16);
+              }
+              *reinterpret_cast<uint4*>(zt + sl * slice_stride + off_re + 8 * h) =
+                  make_uint4(pr[0], pr[1], pr[2], pr[3]);
+              *reinterpret_cast<uint4*>(zt + sl * slice_stride + off_im + 8 * h) =
+                  make_uint4(pi[0], pi[1], pi[2], pi[3]);
+            }
+          }
         }
       }
     }
@@ -230,17 +264,17 @@ inline int gather_tile(int nv, int nc, int w, int nbc, int* nbp) {
 
 template <int KT>
 __global__ void __launch_bounds__(256) mf_gather_bf16_kernel(const zf* __restrict__ X, int ldx, int c0, int nbc,
-                                                             int nbp, const zd* __restrict__ vec_win, int nk, int nv,
+                                                             int nbp, const zf* __restrict__ vec_win, int nk, int nv,
                                                              int nc, int w, uint16_t* __restrict__ zt, int ldn,
                                                              int nslices, long slice_stride) {
-  gather_bf16_tile<KT>(X, ldx, c0, nbc, nbp, vec_win, nk, nv, nc, w, zt, ldn, nslices, slice_stride, blockIdx.x * KT);
+  gather_bf16_tile<KT, false, zf>(X, ldx, c0, nbc, nbp, vec_win, nk, nv, nc, w, zt, ldn, nslices, slice_stride, blockIdx.x * KT);
 }
 
 template <int KT>
 __global__ void __launch_bounds__(256) mf_gather_f32_kernel(const zf* __restrict__ X, int ldx, int c0, int nbc,
-                                                            int nbp, const zd* __restrict__ vec_win, int nk, int nv,
+                                                            int nbp, const zf* __restrict__ vec_win, int nk, int nv,
                                                             int nc, int w, float* __restrict__ z32, int ldk) {
-  gather_bf16_tile<KT, true>(X, ldx, c0, nbc, nbp, vec_win, nk, nv, nc, w, nullptr, 0, 0, 0, blockIdx.x * KT, z32,
+  gather_bf16_tile<KT, true, zf>(X, ldx, c0, nbc, nbp, vec_win, nk, nv, nc, w, nullptr, 0, 0, 0, blockIdx.x * KT, z32,
                              ldk);
 }
 
@@ -258,9 +292,9 @@ __global__ void __launch_bounds__(256) mf_gather_bf16_batch_kernel(const zf* __r
                        (int)(q.slice_stride / q.ldk), nslices, q.slice_stride, t.y);
 }
 
-template <class S, class T>
+template <class S, class T, class VT, class ET>
 __device__ __forceinline__ void scatter_k(const T* __restrict__ Tm, int ldt, const cplx<S>* __restrict__ X, int ldx,
-                                          const zd* __restrict__ vec_win, const double* __restrict__ dE, int nk,
+                                          const VT* __restrict__ vec_win, const ET* __restrict__ dE, int nk,
                                           int nv, int nc, int w, int nb, int nbg, cplx<S>* __restrict__ Y, int ldy,
                                           int c0, int k, int b0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -278,7 +312,7 @@ __device__ __forceinline__ void scatter_k(const T* __restrict__ Tm, int ldt, con
   const float r_w = 1.0f / w, r_nv = 1.0f / nv, r_nbl = 1.0f / nbl;
   for (int e = tid; e < nbnd * w; e += nt) {
     const int s = qdiv(e, r_w), o = e - s * w;
-    const zd a = vec_win[((size_t)k * nbnd + s) * w + o];
+    const VT a = vec_win[((size_t)k * nbnd + s) * w + o];
     const cplx<S> as = mk<S>((S)a.re, (S)a.im);
     if (s < nv)
       Vs[s * w + o] = as;
@@ -316,15 +350,26 @@ __device__ __forceinline__ void scatter_k(const T* __restrict__ Tm, int ldt, con
     }
   }
   __syncthreads();
-  // U[b][o][v] = sum_p conj(Vb[v][p]) T[b][o][p]
-  for (int e = tid; e < nbl * w * nv; e += nt) {
-    const int q = qdiv(e, r_nv), v = e - q * nv;  // q = bb * w + o
-    cplx<S> acc = mk<S>(0, 0);
+  // U[b][o][v] = sum_p conj(Vb[v][p]) T[b][o][p]: a thread takes one (b, o) row and four v at a time, each T value
+  // loaded once for them (every sum runs over p in the same order as one v alone)
+  for (int q = tid; q < nbl * w; q += nt) {  // q = bb * w + o
     const T* tp = Ts + (size_t)q * ts;
-    const cplx<S>* vr = Vs + v * w;
-    for (int p = 0; p < w; ++p) cfmac(acc, vr[p], mk<S>((S)tp[2 * p], (S)tp[2 * p + 1]));
     const int bb = qdiv(q, r_w), o = q - bb * w;
-    U[bb * us + o * nv + v] = acc;
+    cplx<S>* up = U + bb * us + o * nv;
+    for (int v0 = 0; v0 < nv; v0 += 4) {
+      cplx<S> acc[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc[i] = mk<S>(0, 0);
+      for (int p = 0; p < w; ++p) {
+        const cplx<S> tc = mk<S>((S)tp[2 * p], (S)tp[2 * p + 1]);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (v0 + i < nv) cfmac(acc[i], Vs[(v0 + i) * w + p], tc);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        if (v0 + i < nv) up[v0 + i] = acc[i];
+    }
   }
   __syncthreads();
   // y[c][v][b] = dE x + sum_o conj(C[c][o]) U[b][o][v]
@@ -347,10 +392,10 @@ __device__ __forceinline__ void scatter_k(const T* __restrict__ Tm, int ldt, con
 template <class S, class T>
 __global__ void __launch_bounds__(128) mf_scatter_kernel(const T* __restrict__ Tm, int ldt,
                                                          const cplx<S>* __restrict__ X, int ldx,
-                                                         const zd* __restrict__ vec_win, const double* __restrict__ dE,
+                                                         const cplx<S>* __restrict__ vec_win, const S* __restrict__ dE,
                                                          int nk, int nv, int nc, int w, int nb, int nbg,
                                                          cplx<S>* __restrict__ Y, int ldy, int c0) {
-  scatter_k<S, T>(Tm, ldt, X, ldx, vec_win, dE, nk, nv, nc, w, nb, nbg, Y, ldy, c0, blockIdx.x, blockIdx.y * nbg);
+  scatter_k<S, T, cplx<S>, S>(Tm, ldt, X, ldx, vec_win, dE, nk, nv, nc, w, nb, nbg, Y, ldy, c0, blockIdx.x, blockIdx.y * nbg);
 }
 
 // Scatter from T in Z's layout, T[n][k] (the FFT form): a CTA takes a tile of kScatK consecutive k-points and
@@ -360,8 +405,8 @@ __global__ void __launch_bounds__(128) mf_scatter_kernel(const T* __restrict__ T
 constexpr int kScatK = 8;
 __global__ void __launch_bounds__(256) mf_scatter_t_kernel(const float* __restrict__ Tt, int ldt,
                                                            const zf* __restrict__ X, int ldx,
-                                                           const zd* __restrict__ vec_win,
-                                                           const double* __restrict__ dE, int nk, int nv, int nc,
+                                                           const zf* __restrict__ vec_win,
+                                                           const float* __restrict__ dE, int nk, int nv, int nc,
                                                            int w, int nb, int nbg, zf* __restrict__ Y, int ldy,
                                                            int c0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -380,9 +425,7 @@ __global__ void __launch_bounds__(256) mf_scatter_t_kernel(const float* __restri
   for (int e = tid; e < kScatK * nbnd * w; e += nt) {
     const int q = qdiv(e, r_w), o = e - q * w;  // q = kk * nbnd + sb
     const int kk = qdiv(q, r_nbnd), sb = q - kk * nbnd;
-    zd a = mk<double>(0.0, 0.0);
-    if (kk < kn) a = vec_win[((size_t)(k0 + kk) * nbnd + sb) * w + o];
-    const zf as = mk<float>((float)a.re, (float)a.im);
+    const zf as = kk < kn ? vec_win[((size_t)(k0 + kk) * nbnd + sb) * w + o] : mk<float>(0.f, 0.f);
     if (sb < nv)
       Vs[(kk * nv + sb) * w + o] = as;
     else
@@ -406,16 +449,29 @@ __global__ void __launch_bounds__(256) mf_scatter_t_kernel(const float* __restri
     d[7 * TSK] = b.w;
   }
   __syncthreads();
-  // U[kk][b][o][v] = sum_p conj(Vb[kk][v][p]) T[kk][b][o][p]
-  for (int e = tid; e < kn * nrow * nv; e += nt) {
-    const int q = qdiv(e, r_nv), v = e - q * nv;  // q = kk nrow + (b w + o)
+  // U[kk][b][o][v] = sum_p conj(Vb[kk][v][p]) T[kk][b][o][p]: a thread takes one (kk, b, o) row and four v at a
+  // time, so that each T value is loaded once for them (every sum runs over p in the same order as one v alone)
+  for (int q = tid; q < kn * nrow; q += nt) {  // q = kk nrow + (b w + o)
     const int kk = qdiv(q, r_nrow), ro = q - kk * nrow;
-    const float* tp = Ts + kk * TSK + ro * ts;
-    const zf* vr = Vs + (kk * nv + v) * w;
-    zf acc = mk<float>(0.f, 0.f);
-    for (int p = 0; p < w; ++p) cfmac(acc, vr[p], mk<float>(tp[2 * p], tp[2 * p + 1]));
+    const float2* tp = reinterpret_cast<const float2*>(Ts + kk * TSK + ro * ts);  // ts, TSK even: 8-byte aligned
     const int bb = qdiv(ro, r_w), o = ro - bb * w;
-    U[(kk * nbg + bb) * us + o * nv + v] = acc;
+    zf* up = U + (kk * nbg + bb) * us + o * nv;
+    for (int v0 = 0; v0 < nv; v0 += 4) {
+      const zf* vr = Vs + (kk * nv + v0) * w;
+      zf acc[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc[i] = mk<float>(0.f, 0.f);
+      for (int p = 0; p < w; ++p) {
+        const float2 t = tp[p];
+        const zf tc = mk<float>(t.x, t.y);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (v0 + i < nv) cfmac(acc[i], vr[i * w + p], tc);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        if (v0 + i < nv) up[v0 + i] = acc[i];
+    }
   }
   __syncthreads();
   // y[k][c][v][b] = dE x + sum_o conj(C[k][c][o]) U[k][b][o][v]
@@ -429,10 +485,172 @@ __global__ void __launch_bounds__(256) mf_scatter_t_kernel(const float* __restri
     for (int o = 0; o < w; ++o) cfmac(acc, cr[o], ur[o * nv]);
     const size_t I = (size_t)(k0 + kk) * ncv + cv;
     const zf x = X[I * ldx + c0 + b0 + bb];
-    const float d = (float)dE[I];
+    const float d = dE[I];
     acc.re += d * x.re;
     acc.im += d * x.im;
     Y[I * ldy + c0 + b0 + bb] = acc;
+  }
+}
+
+// The FFT form's gather and scatter with the lanes of a warp along k (Z and T are [n][k] rows, k contiguous):
+// a CTA takes 32 consecutive k-points and a chunk of block columns, and every load of T and store of Z is then one
+// 128-byte line per warp instruction (the row-per-thread kernels above touch 32 lines per instruction).  The
+// per-k operands are staged k-innermost with the k extent padded to 33, so that lane k's accesses are
+// conflict-free.  The sums are those of the tiles above, term for term and in the same order.
+constexpr int kLaneK = 32;
+constexpr int kLaneKp = 33;
+
+// shared memory of the lane-k gather: Vs, Cs, xs, Y1
+inline size_t gather32_smem(int nv, int nc, int w, int nbp) {
+  return (size_t)(nv * w + nc * w + nc * nv * nbp + nc * w * nbp) * kLaneKp * sizeof(zf);
+}
+
+__global__ void __launch_bounds__(256) mf_gather_k32_kernel(const zf* __restrict__ X, int ldx, int c0, int nbc,
+                                                            int nbp, const zf* __restrict__ vec, int nk, int nv,
+                                                            int nc, int w, float* __restrict__ z32, int ldk) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nbnd = nv + nc, ncv = nc * nv;
+  const int k0 = blockIdx.x * kLaneK, b0 = blockIdx.y * nbp;
+  const int nbl = min(nbp, nbc - b0);
+  if (nbl <= 0) return;  // uniform over the CTA
+  zf* Vs = reinterpret_cast<zf*>(smem_raw);  // [v][p][33]
+  zf* Cs = Vs + nv * w * kLaneKp;             // [c][o][33]
+  zf* xs = Cs + nc * w * kLaneKp;             // [c][v][bb][33]
+  zf* Y1 = xs + ncv * nbp * kLaneKp;          // [c][p][bb][33]
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+  const float r_bw = 1.0f / (nbnd * w), r_w = 1.0f / w, r_ncvb = 1.0f / (ncv * nbl), r_nbl = 1.0f / nbl;
+  // band vectors: reads follow memory (one k-point's nbnd w values after another)
+  for (int e = tid; e < kLaneK * nbnd * w; e += nt) {
+    const int kk = qdiv(e, r_bw), sw = e - kk * nbnd * w;  // sw = sb w + o
+    const int sb = qdiv(sw, r_w), o = sw - sb * w;
+    const zf a = k0 + kk < nk ? vec[(size_t)(k0 + kk) * nbnd * w + sw] : mk<float>(0.f, 0.f);
+    if (sb < nv)
+      Vs[(sb * w + o) * kLaneKp + kk] = a;
+    else
+      Cs[((sb - nv) * w + o) * kLaneKp + kk] = a;
+  }
+  // x rows (k, c, v): the chunk's nbl values of each
+  for (int e = tid; e < kLaneK * ncv * nbl; e += nt) {
+    const int kk = qdiv(e, r_ncvb), r = e - kk * ncv * nbl;  // r = cv nbl + bb
+    const int cv = qdiv(r, r_nbl), bb = r - cv * nbl;
+    xs[(cv * nbp + bb) * kLaneKp + kk] =
+        k0 + kk < nk ? X[((size_t)(k0 + kk) * ncv + cv) * ldx + c0 + b0 + bb] : mk<float>(0.f, 0.f);
+  }
+  __syncthreads();
+  // Y1[c][p][bb] = sum_v Vb[v][p] x[c][v][bb] for lane k: a warp takes (p, bb) items and every c
+  for (int it = warp; it < w * nbl; it += nwarp) {
+    const int p = qdiv(it, r_nbl), bb = it - p * nbl;
+    for (int cb = 0; cb < nc; cb += 4) {
+      zf acc[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc[i] = mk<float>(0.f, 0.f);
+      for (int v = 0; v < nv; ++v) {
+        const zf a = Vs[(v * w + p) * kLaneKp + lane];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (cb + i < nc) cfma(acc[i], a, xs[(((cb + i) * nv + v) * nbp + bb) * kLaneKp + lane]);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        if (cb + i < nc) Y1[(((cb + i) * w + p) * nbp + bb) * kLaneKp + lane] = acc[i];
+    }
+  }
+  __syncthreads();
+  // Z[o][p][bb] = sum_c C[c][o] Y1[c][p][bb] for lane k: a warp takes (bb, p, o group of 4) items; the re and im
+  // rows of each output are one 128-byte store each (k >= nk inside the last tile: zeros, x = 0 there)
+  const int wo = (w + 3) >> 2;
+  const float r_wo = 1.0f / wo;
+  for (int it = warp; it < nbl * w * wo; it += nwarp) {
+    const int q = qdiv(it, r_wo), og = it - q * wo;  // q = bb w + p
+    const int bb = qdiv(q, r_w), p = q - bb * w;
+    zf acc[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) acc[i] = mk<float>(0.f, 0.f);
+    for (int c = 0; c < nc; ++c) {
+      const zf y = Y1[((c * w + p) * nbp + bb) * kLaneKp + lane];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        if (4 * og + i < w) cfma(acc[i], Cs[(c * w + 4 * og + i) * kLaneKp + lane], y);
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int o = 4 * og + i;
+      if (o < w) {
+        const long row = ((long)((b0 + bb) * w + o) * w + p) * 2;
+        z32[row * ldk + k0 + lane] = acc[i].re;
+        z32[(row + 1) * ldk + k0 + lane] = acc[i].im;
+      }
+    }
+  }
+}
+
+// shared memory of the lane-k scatter: Vs, Cs, U
+inline size_t scatter32_smem(int nv, int nc, int w, int nbg) {
+  return (size_t)(nv * w + nc * w + nbg * w * nv) * kLaneKp * sizeof(zf);
+}
+
+// y[k][c][v][b] = dE x + sum_o conj(C[k][c][o]) sum_p conj(Vb[k][v][p]) T[k][b][o][p] for 32 k-points (lanes) and
+// nbg block columns
+__global__ void __launch_bounds__(256) mf_scatter_k32_kernel(const float* __restrict__ Tt, int ldt,
+                                                             const zf* __restrict__ X, int ldx,
+                                                             const zf* __restrict__ vec,
+                                                             const float* __restrict__ dE, int nk, int nv, int nc,
+                                                             int w, int nb, int nbg, zf* __restrict__ Y, int ldy,
+                                                             int c0) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nbnd = nv + nc, ncv = nc * nv, tw = 2 * w;
+  const int k0 = blockIdx.x * kLaneK, b0 = blockIdx.y * nbg;
+  const int nbl = min(nbg, nb - b0);
+  zf* Vs = reinterpret_cast<zf*>(smem_raw);  // [v][p][33]
+  zf* Cs = Vs + nv * w * kLaneKp;             // [c][o][33]
+  zf* U = Cs + nc * w * kLaneKp;              // [bb][o][v][33]
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+  const float r_bw = 1.0f / (nbnd * w), r_w = 1.0f / w, r_nv = 1.0f / nv, r_nbl = 1.0f / nbl;
+  for (int e = tid; e < kLaneK * nbnd * w; e += nt) {
+    const int kk = qdiv(e, r_bw), sw = e - kk * nbnd * w;
+    const int sb = qdiv(sw, r_w), o = sw - sb * w;
+    const zf a = k0 + kk < nk ? vec[(size_t)(k0 + kk) * nbnd * w + sw] : mk<float>(0.f, 0.f);
+    if (sb < nv)
+      Vs[(sb * w + o) * kLaneKp + kk] = a;
+    else
+      Cs[((sb - nv) * w + o) * kLaneKp + kk] = a;
+  }
+  __syncthreads();
+  // U[bb][o][v] = sum_p conj(Vb[v][p]) T[bb][o][p] for lane k: a warp takes (bb, o) rows; T's re and im rows
+  // n = ((b0 + bb) w + o) 2w + 2p (+1) are read at columns k0 .. k0 + 31 (ldt >= the tile's end: padding columns)
+  for (int it = warp; it < nbl * w; it += nwarp) {  // it = bb w + o
+    const float* trow = Tt + (size_t)(b0 * w + it) * tw * ldt + k0 + lane;
+    for (int v0 = 0; v0 < nv; v0 += 4) {
+      zf acc[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) acc[i] = mk<float>(0.f, 0.f);
+      for (int p = 0; p < w; ++p) {
+        const zf tc = mk<float>(trow[(size_t)(2 * p) * ldt], trow[(size_t)(2 * p + 1) * ldt]);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (v0 + i < nv) cfmac(acc[i], Vs[((v0 + i) * w + p) * kLaneKp + lane], tc);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        if (v0 + i < nv) U[(it * nv + v0 + i) * kLaneKp + lane] = acc[i];
+    }
+  }
+  __syncthreads();
+  // y for lane k: a warp takes (c v, bb) items
+  for (int it = warp; it < ncv * nbl; it += nwarp) {
+    const int cv = qdiv(it, r_nbl), bb = it - cv * nbl;
+    const int c = qdiv(cv, r_nv), v = cv - c * nv;
+    zf acc = mk<float>(0.f, 0.f);
+    for (int o = 0; o < w; ++o)
+      cfmac(acc, Cs[(c * w + o) * kLaneKp + lane], U[((bb * w + o) * nv + v) * kLaneKp + lane]);
+    if (k0 + lane < nk) {
+      const size_t I = (size_t)(k0 + lane) * ncv + cv;
+      const zf x = X[I * ldx + c0 + b0 + bb];
+      const float d = dE[I];
+      acc.re += d * x.re;
+      acc.im += d * x.im;
+      Y[I * ldy + c0 + b0 + bb] = acc;
+    }
   }
 }
 
@@ -445,7 +663,7 @@ __global__ void __launch_bounds__(128) mf_scatter_batch_kernel(const zf* __restr
   const int2 t = kpts[blockIdx.x];
   if (frozen && frozen[t.x]) return;
   const MfSys& q = sys[t.x];
-  scatter_k<float, float>(q.Tm, q.ldt, X + (size_t)q.row0 * ldx, ldx, q.vec_win, q.dE, q.nk, q.nv, q.nc, q.w, nb, nbg,
+  scatter_k<float, float, zd, double>(q.Tm, q.ldt, X + (size_t)q.row0 * ldx, ldx, q.vec_win, q.dE, q.nk, q.nv, q.nc, q.w, nb, nbg,
                           Y + (size_t)q.row0 * ldy, ldy, c0, t.y, blockIdx.y * nbg);
 }
 
@@ -532,7 +750,7 @@ __global__ void round_f32_kernel(const double* __restrict__ V, int ldv, int rows
 }  // namespace
 
 template <class S, class Z>
-cudaError_t launch_mf_gather(const cplx<S>* X, int ldx, int c0, int nb, const zd* vec_win, int nk, int nv, int nc,
+cudaError_t launch_mf_gather(const cplx<S>* X, int ldx, int c0, int nb, const cplx<S>* vec_win, int nk, int nv, int nc,
                              int w, Z* zt, int ldk, int nslices, long slice_stride, cudaStream_t s, int tile) {
   if constexpr (sizeof(S) == 4 && sizeof(Z) == 2) {
     int nbp = nb;
@@ -573,7 +791,18 @@ cudaError_t launch_mf_gather(const cplx<S>* X, int ldx, int c0, int nb, const zd
     if (tile > 0) {
       KT = tile / 100;
       nbp = std::min(tile % 100, nb);
-      if ((KT != 16 && KT != 8) || nbp < 1 || nbp > 8) return cudaErrorInvalidValue;
+      if ((KT != 16 && KT != 8 && KT != 32) || nbp < 1 || nbp > 8) return cudaErrorInvalidValue;
+    }
+    if (KT == 32) {
+      // the lane-k gather: 32 k' per CTA along the lanes
+      const size_t smem = gather32_smem(nv, nc, w, nbp);
+      if (smem > 200 * 1024 || ldk % kLaneK != 0 || nslices != 1) return cudaErrorInvalidValue;
+      cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(mf_gather_k32_kernel), smem);
+      if (e != cudaSuccess) return e;
+      mf_gather_k32_kernel<<<dim3((nk + kLaneK - 1) / kLaneK, (nb + nbp - 1) / nbp), 256, smem, s>>>(
+          reinterpret_cast<const zf*>(X), ldx, c0, nb, nbp, vec_win, nk, nv, nc, w, reinterpret_cast<float*>(zt), ldk);
+      ++g_launch_count;
+      return cudaGetLastError();
     }
     const size_t smem = gather_smem(KT, nv, nc, w, nbp);
     if (smem <= 200 * 1024 && ldk % 64 == 0 && nslices == 1) {
@@ -606,7 +835,7 @@ cudaError_t launch_mf_gather(const cplx<S>* X, int ldx, int c0, int nb, const zd
 }
 
 template <class S, class T>
-cudaError_t launch_mf_scatter(const T* Tm, int ldt, const cplx<S>* X, int ldx, const zd* vec_win, const double* dE,
+cudaError_t launch_mf_scatter(const T* Tm, int ldt, const cplx<S>* X, int ldx, const cplx<S>* vec_win, const S* dE,
                               int nk, int nv, int nc, int w, int nb, cplx<S>* Y, int ldy, int c0, cudaStream_t s,
                               int cols) {
   // block columns per CTA: all (or the requested count), halved until the CTA's tiles fit in 96 KB
@@ -623,10 +852,22 @@ cudaError_t launch_mf_scatter(const T* Tm, int ldt, const cplx<S>* X, int ldx, c
   return cudaGetLastError();
 }
 
-cudaError_t launch_mf_scatter_t(const float* Tt, int ldt, const zf* X, int ldx, const zd* vec_win, const double* dE,
+cudaError_t launch_mf_scatter_t(const float* Tt, int ldt, const zf* X, int ldx, const zf* vec_win, const float* dE,
                                 int nk, int nv, int nc, int w, int nb, zf* Y, int ldy, int c0, cudaStream_t s,
                                 int cols) {
   if (ldt % 64 != 0 || (reinterpret_cast<uintptr_t>(Tt) & 31) != 0) return cudaErrorInvalidValue;
+  if (cols > 100) {
+    // the lane-k scatter: 32 k-points per CTA along the lanes, cols - 100 block columns
+    const int g = std::min(cols - 100, nb);
+    const size_t smem = scatter32_smem(nv, nc, w, g);
+    if (smem > 200 * 1024 || ldt < (nk + kLaneK - 1) / kLaneK * kLaneK) return cudaErrorInvalidValue;
+    cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(mf_scatter_k32_kernel), smem);
+    if (e != cudaSuccess) return e;
+    mf_scatter_k32_kernel<<<dim3((nk + kLaneK - 1) / kLaneK, (nb + g - 1) / g), 256, smem, s>>>(
+        Tt, ldt, X, ldx, vec_win, dE, nk, nv, nc, w, nb, g, Y, ldy, c0);
+    ++g_launch_count;
+    return cudaGetLastError();
+  }
   int nbg = std::min(cols > 0 ? cols : 4, nb);
   auto smem_of = [&](int g) {
     return (size_t)kScatK * ((nc + nv) * w + g * (w * nv + 1)) * sizeof(zf) +
@@ -708,14 +949,14 @@ cudaError_t launch_round_f32(const double* V, int ldv, int rows, int cols, float
   return cudaGetLastError();
 }
 
-template cudaError_t launch_mf_gather<float, float>(const cplx<float>*, int, int, int, const zd*, int, int, int, int,
+template cudaError_t launch_mf_gather<float, float>(const cplx<float>*, int, int, int, const zf*, int, int, int, int,
                                                     float*, int, int, long, cudaStream_t, int);
-template cudaError_t launch_mf_gather<float, uint16_t>(const cplx<float>*, int, int, int, const zd*, int, int, int,
+template cudaError_t launch_mf_gather<float, uint16_t>(const cplx<float>*, int, int, int, const zf*, int, int, int,
                                                        int, uint16_t*, int, int, long, cudaStream_t, int);
 template cudaError_t launch_mf_gather<double, double>(const cplx<double>*, int, int, int, const zd*, int, int, int,
                                                       int, double*, int, int, long, cudaStream_t, int);
-template cudaError_t launch_mf_scatter<float, float>(const float*, int, const cplx<float>*, int, const zd*,
-                                                     const double*, int, int, int, int, int, cplx<float>*, int, int,
+template cudaError_t launch_mf_scatter<float, float>(const float*, int, const cplx<float>*, int, const zf*,
+                                                     const float*, int, int, int, int, int, cplx<float>*, int, int,
                                                      cudaStream_t, int);
 template cudaError_t launch_mf_scatter<double, double>(const double*, int, const cplx<double>*, int, const zd*,
                                                        const double*, int, int, int, int, int, cplx<double>*, int, int,

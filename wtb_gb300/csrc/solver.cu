@@ -37,6 +37,7 @@ namespace wtb {
 template <class S>
 cudaError_t MatFreeOperator<S>::apply(const cplx<S>* X, int ldx, int c0, int ncol, cplx<S>* Y, int ldy,
                                       cudaStream_t s) {
+  if (!vec_s || !dE_s) return cudaErrorInvalidValue;  // the operator's precision copies were never set
   this->matvec_columns += ncol;
   for (int b0 = 0; b0 < ncol; b0 += nbmax) {
     const int nb = ncol - b0 < nbmax ? ncol - b0 : nbmax;
@@ -44,7 +45,7 @@ cudaError_t MatFreeOperator<S>::apply(const cplx<S>* X, int ldx, int c0, int nco
     cudaError_t e;
     if (kind == GEMM_TC_BF16) {
       if constexpr (sizeof(S) == 4) {
-        e = launch_mf_gather<float, uint16_t>(X, ldx, c0 + b0, nb, vec_win, nk, nv, nc, w, Zs, Kpad, nslices,
+        e = launch_mf_gather<float, uint16_t>(X, ldx, c0 + b0, nb, vec_s, nk, nv, nc, w, Zs, Kpad, nslices,
                                               (long)Npad * Kpad, s, gather_tile);
         if (e != cudaSuccess) return e;
         TcGemmPlan* plan = plan_for(N, npairs, tile_n);
@@ -68,14 +69,14 @@ cudaError_t MatFreeOperator<S>::apply(const cplx<S>* X, int ldx, int c0, int nco
           prof->flops += 2.0 * nk * (double)N * nk * npairs;
           prof->bytes += 2.0 * nslices * ((double)nk * nk + (double)N * nk) + 4.0 * nk * (double)N;
         }
-        e = launch_mf_scatter<float, float>(reinterpret_cast<const float*>(Tm), Npad, X, ldx, vec_win, dE, nk, nv, nc,
+        e = launch_mf_scatter<float, float>(reinterpret_cast<const float*>(Tm), Npad, X, ldx, vec_s, dE_s, nk, nv, nc,
                                             w, nb, Y, ldy, c0 + b0, s, scatter_cols);
         if (e != cudaSuccess) return e;
       } else {
         return cudaErrorInvalidValue;
       }
     } else {
-      e = launch_mf_gather<S, S>(X, ldx, c0 + b0, nb, vec_win, nk, nv, nc, w, Zr, Kpad, 1, 0, s);
+      e = launch_mf_gather<S, S>(X, ldx, c0 + b0, nb, vec_s, nk, nv, nc, w, Zr, Kpad, 1, 0, s, gather_tile);
       if (e != cudaSuccess) return e;
       cudaEvent_t ea = nullptr, eb = nullptr;
       const bool profiled = prof && prof->on && !this->capturing;
@@ -95,10 +96,10 @@ cudaError_t MatFreeOperator<S>::apply(const cplx<S>* X, int ldx, int c0, int nco
       }
       if (kind == GEMM_FFT_F32) {
         if constexpr (sizeof(S) == 4)
-          e = launch_mf_scatter_t(reinterpret_cast<const float*>(Tm), Kpad, X, ldx, vec_win, dE, nk, nv, nc, w, nb, Y,
+          e = launch_mf_scatter_t(reinterpret_cast<const float*>(Tm), Kpad, X, ldx, vec_s, dE_s, nk, nv, nc, w, nb, Y,
                                   ldy, c0 + b0, s, scatter_cols);
       } else {
-        e = launch_mf_scatter<S, S>(reinterpret_cast<const S*>(Tm), Npad, X, ldx, vec_win, dE, nk, nv, nc, w, nb, Y,
+        e = launch_mf_scatter<S, S>(reinterpret_cast<const S*>(Tm), Npad, X, ldx, vec_s, dE_s, nk, nv, nc, w, nb, Y,
                                     ldy, c0 + b0, s);
       }
       if (e != cudaSuccess) return e;
@@ -145,11 +146,11 @@ cudaError_t MatFreeOperator<S>::time_contraction(int reps, int ncol, cudaStream_
 
 template <class S>
 cudaError_t MatFreeOperator<S>::contract(const cplx<S>* X, int ldx, int ncol, cudaStream_t s) {
-  if (ncol > nbmax) return cudaErrorInvalidValue;
+  if (ncol > nbmax || !vec_s) return cudaErrorInvalidValue;
   const int N = 2 * w * w * ncol;
   if (kind == GEMM_TC_BF16) {
     if constexpr (sizeof(S) == 4) {
-      cudaError_t e = launch_mf_gather<float, uint16_t>(X, ldx, 0, ncol, vec_win, nk, nv, nc, w, Zs, Kpad, nslices,
+      cudaError_t e = launch_mf_gather<float, uint16_t>(X, ldx, 0, ncol, vec_s, nk, nv, nc, w, Zs, Kpad, nslices,
                                                         (long)Npad * Kpad, s, gather_tile);
       if (e != cudaSuccess) return e;
       TcGemmPlan* plan = plan_for(N, npairs, tile_n);
@@ -159,7 +160,7 @@ cudaError_t MatFreeOperator<S>::contract(const cplx<S>* X, int ldx, int ncol, cu
       return cudaErrorInvalidValue;
     }
   }
-  cudaError_t e = launch_mf_gather<S, S>(X, ldx, 0, ncol, vec_win, nk, nv, nc, w, Zr, Kpad, 1, 0, s);
+  cudaError_t e = launch_mf_gather<S, S>(X, ldx, 0, ncol, vec_s, nk, nv, nc, w, Zr, Kpad, 1, 0, s, gather_tile);
   if (e != cudaSuccess) return e;
   return contract_z(N, s, true);
 }
@@ -241,13 +242,18 @@ cudaError_t MatFreeOperator<S>::autotune(cudaStream_t s, const cplx<S>* X, cplx<
       tile_n = c;
       return run();
     }, s);
-  // gather tiles: 16 or 8 k' per CTA, chunks of 1, 2 or 4 block columns (those within 200 KB of shared memory)
+  // gather tiles: 16 or 8 k' per CTA, chunks of 1, 2 or 4 block columns (those within 200 KB of shared memory);
+  // the FFT form also the lane-k gather over 32 k' (its Z rows are k-contiguous)
   std::vector<int> gt;
   for (int kt : {16, 8})
     for (int p : {4, 2, 1})
       if (p <= nbmax &&
           (size_t)(kt * nc * w + kt * nv * w + kt * nc * nv * p + kt * nc * w * p) * sizeof(zf) <= 200 * 1024)
         gt.push_back(kt * 100 + p);
+  if (fft)
+    for (int p : {4, 2, 1})
+      if (p <= nbmax && (size_t)(nv * w + nc * w + nc * nv * p + nc * w * p) * 33 * sizeof(zf) <= 200 * 1024)
+        gt.push_back(3200 + p);
   gather_tile = tune_choice(shape, "gather_tile", gt, 0, [&](int c) {
     gather_tile = c;
     return run();
@@ -257,6 +263,9 @@ cudaError_t MatFreeOperator<S>::autotune(cudaStream_t s, const cplx<S>* X, cplx<
   if (fft) {
     for (int g : {2, 4, 8})
       if (g <= nbmax) sc.push_back(g);
+    // the lane-k scatter over 32 k-points, 2, 4 or 8 block columns (coded 100 + columns)
+    for (int g : {2, 4, 8})
+      if (g <= nbmax && (size_t)(nv * w + nc * w + g * w * nv) * 33 * sizeof(zf) <= 200 * 1024) sc.push_back(100 + g);
   } else {
     for (int g = nbmax; g >= 1 && sc.size() < 3; g = g > 1 ? (g + 1) / 2 : 0) sc.push_back(g);
   }

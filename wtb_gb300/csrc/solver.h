@@ -146,6 +146,10 @@ struct MatFreeOperator : Operator<S> {
   int nk = 0, nv = 0, nc = 0, w = 0, nbmax = 16;
   const zd* vec_win = nullptr;
   const double* dE = nullptr;
+  // the same band vectors and transition energies in precision S, which the gather and scatter read (FP32 copies
+  // rounded once per operator for the FP32 forms: bitwise the values the tiles would convert)
+  const cplx<S>* vec_s = nullptr;
+  const S* dE_s = nullptr;
   GemmKind kind = GEMM_SIMT_F32;
   int nslices = 2, npairs = 3;
   int npairs_refine = 0;  // > npairs: slice products used by begin_refine() (needs nslices = 3)
@@ -187,7 +191,8 @@ struct MatFreeOperator : Operator<S> {
                           (uint64_t)nslices, (uint64_t)npairs, (uint64_t)npairs_refine, (uint64_t)kchunk_final,
                           (uint64_t)tile_n, (uint64_t)gather_tile, (uint64_t)scatter_cols,
                           (uint64_t)Mpad, (uint64_t)Kpad, (uint64_t)Npad, (uint64_t)(uintptr_t)vec_win,
-                          (uint64_t)(uintptr_t)dE, (uint64_t)(uintptr_t)Vs, (uint64_t)(uintptr_t)Zs,
+                          (uint64_t)(uintptr_t)dE, (uint64_t)(uintptr_t)vec_s, (uint64_t)(uintptr_t)dE_s,
+                          (uint64_t)(uintptr_t)Vs, (uint64_t)(uintptr_t)Zs,
                           (uint64_t)(uintptr_t)Vr, (uint64_t)(uintptr_t)Zr, (uint64_t)(uintptr_t)Tm,
                           (uint64_t)(uintptr_t)st, (uint64_t)mesh1, (uint64_t)mesh2, (uint64_t)fft_p,
                           (uint64_t)(uintptr_t)fft_spec, (uint64_t)(uintptr_t)fft_tw};

@@ -241,7 +241,8 @@ int enqueue_bands(wtb_ctx* c, bool mixed = false) {
                     nk, nv, nc, c->ws.get<double>("eig_all", 0, &err), c->ws.get<zd>("vec_all", 0, &err),
                     nb > 0 ? c->ws.get<double>("eig_win", 0, &err) : nullptr,
                     nb > 0 ? c->ws.get<zd>("vec_win", 0, &err) : nullptr, c->ws.get<int>("nocp", 0, &err), c->st, c->s,
-                    mixed));
+                    mixed, mixed ? c->ws.get<float4>("hr_df", (size_t)c->nR * w * w, &err) : nullptr));
+  CKC(err);
   return WTB_OK;
 }
 
@@ -343,6 +344,20 @@ int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob, 
   CKC(err);
   if (!deriv_r0) CKC(launch_transition_energies(c->ws.get<double>("eig_win", 0, &err), nk, nv, nc, dE, c->s));
   const int Kpad = (nk + 63) / 64 * 64, Mpad = (nk + 127) / 128 * 128;
+  // the FP32 forms' gather and scatter read the band vectors and transition energies rounded to FP32 once here
+  // (the values their tiles would otherwise convert from FP64 in every CTA)
+  auto f32_inputs = [&](MatFreeOperator<float>* op) -> int {
+    const int nvals = (nv + nc) * w;
+    zf* vf = c->ws.get<zf>("vec_win_f32", (size_t)nk * nvals, &err);
+    float* ef = c->ws.get<float>(deriv_r0 ? "dE0_f32" : "dE_f32", dim, &err);
+    CKC(err);
+    CKC(launch_round_f32(reinterpret_cast<const double*>(vec_win), 2 * nvals, nk, 2 * nvals,
+                         reinterpret_cast<float*>(vf), 2 * nvals, c->s));
+    CKC(launch_round_f32(dE, dim, 1, dim, ef, dim, c->s));
+    op->vec_s = vf;
+    op->dE_s = ef;
+    return WTB_OK;
+  };
   // FP32 matrix-free operator on a two-dimensional Monkhorst-Pack mesh: the contraction as FFT convolutions with
   // the Coulomb stencil (no nk x nk table).  WTB_FFT=0 selects the CUDA-core product instead.
   const bool mesh2d = c->mesh_mp && p->ngrid[0] == c->ngrid[0] && p->ngrid[1] == c->ngrid[1] &&
@@ -374,6 +389,7 @@ int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob, 
     op->kind = GEMM_FFT_F32;
     op->nk = nk; op->nv = nv; op->nc = nc; op->w = w; op->nbmax = nbmax;
     op->vec_win = vec_win; op->dE = dE; op->st = c->st; op->msg = &ob->msg; op->prof = &c->prof;
+    CKR(f32_inputs(op));
     op->Kpad = Kpad; op->Mpad = Mpad; op->Npad = Npad;
     op->mesh1 = n1; op->mesh2 = n2; op->fft_p = fftP;
     op->fft_spec = spec; op->fft_tw = tw;
@@ -424,6 +440,8 @@ int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob, 
     op->kind = GEMM_SIMT_F64;
     op->nk = nk; op->nv = nv; op->nc = nc; op->w = w; op->nbmax = nbmax;
     op->vec_win = vec_win; op->dE = dE; op->st = c->st; op->msg = &ob->msg; op->prof = &c->prof;
+    op->vec_s = vec_win;
+    op->dE_s = dE;
     op->Kpad = Kpad; op->Mpad = Mpad; op->Npad = Npad;
     op->Vr = V;
     op->Zr = c->ws.get<double>("Zr64", (size_t)Npad * Kpad, &err, true);
@@ -436,6 +454,7 @@ int make_operator(wtb_ctx* c, const wtb_bse_params* p, int nbmax, OpBundle* ob, 
   ob->o32.reset(op);
   op->nk = nk; op->nv = nv; op->nc = nc; op->w = w; op->nbmax = nbmax;
   op->vec_win = vec_win; op->dE = dE; op->st = c->st; op->msg = &ob->msg; op->prof = &c->prof;
+  CKR(f32_inputs(op));
   op->Kpad = Kpad; op->Mpad = Mpad; op->Npad = Npad;
   if (p->precision == WTB_PREC_FP32) {
     op->kind = GEMM_SIMT_F32;

@@ -107,11 +107,12 @@ struct CoulParams {
 
 // ----------------------------------------------------------------------------- kernels (launchers)
 // H(k) + Hermitian eigensolve + gauge + band window.  Returns 0 or a launch error.
-// mixed: FP32 eigensolve + FP64 Rayleigh quotients (energies FP64-accurate, vectors FP32-accurate)
+// mixed: FP32 eigensolve + Rayleigh quotients against H(k) summed in double-float (energies FP64-accurate,
+// vectors FP32-accurate); hr_df: scratch of nR w^2 float4 for the split H(R) (mixed only)
 cudaError_t launch_hk_eig(const zd* hr, const int* rvec, const int* ndegen, int nR, int w,
                           const double* rlat_rm, double efermi, double scs, const double* kpt, int nk,
                           int nv, int nc, double* eig_all, zd* vec_all, double* eig_win, zd* vec_win,
-                          int* nocp, DevStatus* st, cudaStream_t s, bool mixed = false);
+                          int* nocp, DevStatus* st, cudaStream_t s, bool mixed = false, float4* hr_df = nullptr);
 // Velocity matrix elements hr[5][dim] (x, y, z, sigma+, sigma-); with hr32 (an FP32 copy of H(R)) the Fourier
 // sums run in FP32.
 cudaError_t launch_optics(const zd* hr, const int* rvec, const int* ndegen, int nR, int w,
@@ -252,19 +253,20 @@ cudaError_t launch_small_gemm(const zd* A, int lda, int transA, const zd* B, int
                               long a_stride = 0, long b_stride = 0, long c_stride = 0);
 
 // ----------------------------------------------------------------------------- matrix-free operator
-// Z[n][k'] with n = ((b*w + o)*w + p)*2 + ri (K-major for the V*Z contraction).  tile (split-BF16 panel only):
-// 0 = the shared-memory rule, else KT * 100 + nbp (KT = 16 or 8 k' per CTA, nbp block columns per chunk).
+// Z[n][k'] with n = ((b*w + o)*w + p)*2 + ri (K-major for the V*Z contraction).  tile (split-BF16 panel and FP32
+// rows): 0 = the shared-memory rule, else KT * 100 + nbp (KT = 16 or 8 k' per CTA, nbp block columns per chunk;
+// FP32 rows also KT = 32: the gather with the warp's lanes along k').
 template <class S, class Z>
-cudaError_t launch_mf_gather(const cplx<S>* X, int ldx, int c0, int nb, const zd* vec_win, int nk, int nv, int nc,
+cudaError_t launch_mf_gather(const cplx<S>* X, int ldx, int c0, int nb, const cplx<S>* vec_win, int nk, int nv, int nc,
                              int w, Z* zt, int ldk, int nslices, long slice_stride, cudaStream_t s, int tile = 0);
 // scatter from T in Z's layout, T[n][k] (row n at Tt + n ldt; the FFT form), over tiles of 8 k-points and cols
-// block columns per CTA (0: 4)
-cudaError_t launch_mf_scatter_t(const float* Tt, int ldt, const zf* X, int ldx, const zd* vec_win, const double* dE,
+// block columns per CTA (0: 4); cols = 100 + g: tiles of 32 k-points along the warp's lanes, g block columns
+cudaError_t launch_mf_scatter_t(const float* Tt, int ldt, const zf* X, int ldx, const zf* vec_win, const float* dE,
                                 int nk, int nv, int nc, int w, int nb, zf* Y, int ldy, int c0, cudaStream_t s,
                                 int cols = 0);
 // cols: block columns per CTA (0 = all that fit in 96 KB of shared memory)
 template <class S, class T>
-cudaError_t launch_mf_scatter(const T* Tm, int ldt, const cplx<S>* X, int ldx, const zd* vec_win, const double* dE,
+cudaError_t launch_mf_scatter(const T* Tm, int ldt, const cplx<S>* X, int ldx, const cplx<S>* vec_win, const S* dE,
                               int nk, int nv, int nc, int w, int nb, cplx<S>* Y, int ldy, int c0, cudaStream_t s,
                               int cols = 0);
 template <class S>
