@@ -102,3 +102,47 @@ def test_launch_shapes_leave_results_unchanged(built):
         for prm in OPERATOR_PARAMS:
             assert ch[prm]["source"] == "pinned" and ch[prm]["choice"] == int(want[prm]), (prm, ch)
     np.testing.assert_array_equal(runs[0][0], runs[1][0])
+
+
+_CHILD_FFT = """
+import json, sys
+import numpy as np
+sys.path.insert(0, {root!r})
+from wtb_gb300 import api, synthetic as S
+sysm, p = S.workload("hex8_24x24")
+ctx = api.Context(0)
+ctx.set_hr(sysm)
+ctx.bsesolver(p, precision="fp64", op="matfree")
+rng = np.random.default_rng(5)
+X = rng.normal(size=(p.dim, 16)) + 1j * rng.normal(size=(p.dim, 16))
+Y = ctx.bse_matvec(p, X, precision="fp32", op="matfree")
+np.save({out!r}, Y)
+print("RESULT " + json.dumps({{"form": ctx.operator_form(), "report": api.autotune_report()}}))
+"""
+
+
+@pytest.mark.gpu
+def test_fft_launch_shapes_leave_results_unchanged(built, tmp_path):
+    """The FFT form's gather and scatter: the row-per-thread tiles and the lane-k tiles (32 k along a warp's
+    lanes) form every sum term for term in the same order, so H X is bitwise the same for every launch shape."""
+    pins = ("gather_tile=1604,scatter_cols=2", "gather_tile=3201,scatter_cols=102",
+            "gather_tile=3204,scatter_cols=108", "gather_tile=802,scatter_cols=104")
+    Ys = []
+    for i, pin in enumerate(pins):
+        out = str(tmp_path / f"y{i}.npy")
+        env = dict(os.environ)
+        for k in ("WTB_TC_TILE", "WTB_TUNE_PIN", "WTB_TUNE", "WTB_FFT"):
+            env.pop(k, None)
+        env.update({"WTB_TUNE_CACHE": "off", "WTB_TUNE_PIN": pin})
+        r = subprocess.run([sys.executable, "-c", _CHILD_FFT.format(root=ROOT, out=out)], env=env,
+                           capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+        d = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("RESULT ")][-1][len("RESULT "):])
+        assert d["form"] == "FP32 FFT convolution"
+        ch = {c["param"]: c for c in d["report"]["choices"] if c["shape"].startswith("matfree-fft ")}
+        want = dict(kv.split("=") for kv in pin.split(","))
+        for prm, v in want.items():
+            assert ch[prm]["source"] == "pinned" and ch[prm]["choice"] == int(v), (prm, ch)
+        Ys.append(np.load(out))
+    for Y in Ys[1:]:
+        np.testing.assert_array_equal(Y, Ys[0])

@@ -117,7 +117,7 @@ __device__ __forceinline__ void gather_bf16_tile(const zf* __restrict__ X, int l
                                                  uint16_t* __restrict__ zt, int ldn, int nslices, long slice_stride,
                                                  int kt0, float* __restrict__ z32 = nullptr, int ldk = 0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int nbnd = nv + nc, ncv = nc * nv, ww = w * w;
+  const int nbnd = nv + nc, ncv = nc * nv;
   const int tkn = min(KT, nk - kt0);
   zf* Cs = reinterpret_cast<zf*>(smem_raw);  // [KT][nc][w]
   zf* Vs = Cs + KT * nc * w;                 // [KT][nv][w]
@@ -125,7 +125,7 @@ __device__ __forceinline__ void gather_bf16_tile(const zf* __restrict__ X, int l
   zf* Y1 = xs + KT * ncv * nbp;              // [KT][nc][w][nbp]
   const int tid = threadIdx.x, nt = blockDim.x;
   // index quotients by the runtime extents through qdiv (all numerators < 2^21)
-  const float r_w = 1.0f / w, r_nbnd = 1.0f / nbnd, r_ncv = 1.0f / ncv, r_nc = 1.0f / nc;
+  const float r_w = 1.0f / w, r_nbnd = 1.0f / nbnd, r_ncv = 1.0f / ncv;
   for (int e = tid; e < KT * nbnd * w; e += nt) {
     const int q = qdiv(e, r_w), o = e - q * w;  // q = kk * nbnd + sb
     const int kk = qdiv(q, r_nbnd), sb = q - kk * nbnd;
@@ -636,15 +636,18 @@ __global__ void __launch_bounds__(256) mf_scatter_k32_kernel(const float* __rest
     }
   }
   __syncthreads();
-  // y for lane k: a warp takes (c v, bb) items
-  for (int it = warp; it < ncv * nbl; it += nwarp) {
-    const int cv = qdiv(it, r_nbl), bb = it - cv * nbl;
+  // y: the lanes along (c v, bb) of one k-point, so that a warp's X loads and Y stores cover consecutive rows
+  // (c v) of the k-point (lanes along k would put every lane in a different row)
+  const float r_ib = 1.0f / (ncv * nbl);
+  for (int e = tid; e < kLaneK * ncv * nbl; e += nt) {
+    const int kk = qdiv(e, r_ib), r = e - kk * ncv * nbl;  // r = cv nbl + bb
+    const int cv = qdiv(r, r_nbl), bb = r - cv * nbl;
     const int c = qdiv(cv, r_nv), v = cv - c * nv;
     zf acc = mk<float>(0.f, 0.f);
     for (int o = 0; o < w; ++o)
-      cfmac(acc, Cs[(c * w + o) * kLaneKp + lane], U[((bb * w + o) * nv + v) * kLaneKp + lane]);
-    if (k0 + lane < nk) {
-      const size_t I = (size_t)(k0 + lane) * ncv + cv;
+      cfmac(acc, Cs[(c * w + o) * kLaneKp + kk], U[((bb * w + o) * nv + v) * kLaneKp + kk]);
+    if (k0 + kk < nk) {
+      const size_t I = (size_t)(k0 + kk) * ncv + cv;
       const zf x = X[I * ldx + c0 + b0 + bb];
       const float d = dE[I];
       acc.re += d * x.re;

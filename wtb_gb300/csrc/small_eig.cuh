@@ -5,7 +5,7 @@
 // bisection and inverse iteration for the tridiagonal stage because their work is independent per
 // eigenpair and spreads over the CTA's threads):
 //   1. Householder reduction to a real symmetric tridiagonal T = Q^H A Q with Q = H_0 H_1 ... H_{n-2},
-//      H_j = I - tau_j v_j v_j^H (the lower-triangle convention of ZHETD2; v_j[0] = 1), three barriers a step;
+//      H_j = I - tau_j v_j v_j^H (the lower-triangle convention of ZHETD2; v_j[0] = 1), two barriers a step;
 //   2. the k-th smallest eigenvalue of T by Sturm-count bisection, one thread per eigenvalue;
 //   3. its eigenvector z_k by inverse iteration (L D L^T of T - lam_k I with safeguarded pivots, three
 //      solves from a fixed pseudo-random start), one thread per eigenvector, then modified Gram-Schmidt
@@ -62,9 +62,11 @@ __device__ __forceinline__ void reflector_warp(cplx<S>* A, int lda, int n, int j
   } else {
     const S an = sqrt(alpha.re * alpha.re + alpha.im * alpha.im + sig);
     beta = alpha.re >= (S)0 ? -an : an;
-    t = mk<S>((beta - alpha.re) / beta, -alpha.im / beta);
+    const S ib = (S)1 / beta;
+    t = mk<S>((beta - alpha.re) * ib, -alpha.im * ib);
     const S dr = alpha.re - beta, di = alpha.im, dd = dr * dr + di * di;
-    sc = mk<S>(dr / dd, -di / dd);  // 1 / (alpha - beta)
+    const S idd = (S)1 / dd;
+    sc = mk<S>(dr * idd, -di * idd);  // 1 / (alpha - beta)
     for (int i = 1 + lane; i < L; i += 32) v[i] = cmul(cconj(v[i]), sc);
   }
   __syncwarp();  // every lane has read alpha = conj(v[0])
@@ -77,15 +79,18 @@ __device__ __forceinline__ void reflector_warp(cplx<S>* A, int lda, int n, int j
   __syncwarp();
 }
 
-// Step 1.  A: n x n Hermitian (both triangles), row-major with leading dimension lda, in shared memory.  On
-// return row j right of the diagonal holds the reflector: A[j][j+1+i] = v_j[i] (v_j[0] = 1), i < n-1-j (row j
+// Step 1.  A: n x n Hermitian (both triangles, n <= 97), row-major with leading dimension lda, in shared memory.
+// On return row j right of the diagonal holds the reflector: A[j][j+1+i] = v_j[i] (v_j[0] = 1), i < n-1-j (row j
 // is dead once column j has been reduced, and a row is contiguous for the products that use v_j).  d[n], e[n-1]
 // receive T; tau[n-1] the reflector scalars; p[n] is scratch.  All threads of the block call it; blockDim.x is
-// a multiple of 32.  Two barriers a step: the matrix-vector product, then the rank-2 update, during which warp 0
-// updates the next pivot row first and forms the next reflector from it while the other warps update the rest.
+// a multiple of 32.  Two barriers a step.  The matrix-vector product p = tau A22 v (two lanes per row) also sums
+// q = Re(v^H A22 v), so that K = -1/2 tau (p^H v) = -1/2 |tau|^2 q needs no second pass over p.  Then the
+// rank-2 update: warp 0 updates the next pivot row in registers and forms the next reflector from them while
+// the other warps update the remaining rows.
 template <class S>
 __device__ void tridiag_cta(cplx<S>* A, int lda, int n, S* d, S* e, cplx<S>* tau, cplx<S>* p) {
-  constexpr int TM = 4;  // lanes per row of the matrix-vector product
+  constexpr int TM = 2;  // lanes per row of the matrix-vector product
+  __shared__ S qpart[32];
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
   const int tl = tid & (TM - 1), team = tid / TM, nteam = nt / TM;
   if (n > 1 && warp == 0) reflector_warp<S>(A, lda, n, 0, d, e, tau);
@@ -100,8 +105,8 @@ __device__ void tridiag_cta(cplx<S>* A, int lda, int n, S* d, S* e, cplx<S>* tau
       __syncthreads();
       continue;
     }
-    // p = tau A22 v: TM lanes per row, partial sums combined by shuffles inside the lane group (the loop
-    // bound is uniform, so every lane of a warp reaches the shuffles)
+    // p = tau A22 v and q (the loop bound is uniform, so every lane of a warp reaches the shuffles)
+    S q = 0;
     for (int r0 = 0; r0 < L; r0 += nteam) {
       const int r = r0 + team;
       cplx<S> a0 = mk<S>(0, 0), a1 = mk<S>(0, 0);
@@ -120,53 +125,97 @@ __device__ void tridiag_cta(cplx<S>* A, int lda, int n, S* d, S* e, cplx<S>* tau
         acc.re += __shfl_xor_sync(0xffffffffu, acc.re, o);
         acc.im += __shfl_xor_sync(0xffffffffu, acc.im, o);
       }
-      if (r < L && tl == 0) p[r] = cmul(tj, acc);
-    }
-    __syncthreads();
-    // K = -1/2 tau (p^H v), every warp for itself; w = p + K v;  A22 -= v w^H + w v^H, one warp per row
-    cplx<S> sdot = mk<S>(0, 0);
-    for (int c = lane; c < L; c += 32) cfmac(sdot, p[c], v[c]);
-    sdot.re = warp_allsum(sdot.re);
-    sdot.im = warp_allsum(sdot.im);
-    const cplx<S> K = cmul(mk<S>((S)-0.5 * tj.re, (S)-0.5 * tj.im), sdot);
-    auto update_row = [&](int r) {
-      const cplx<S> vr = v[r];
-      const cplx<S> wr = mk<S>(p[r].re + K.re * vr.re - K.im * vr.im, p[r].im + K.re * vr.im + K.im * vr.re);
-      cplx<S>* arow = A22 + (size_t)r * lda;
-      for (int c = lane; c < L; c += 32) {
-        const cplx<S> vc = v[c];
-        const cplx<S> wc = mk<S>(p[c].re + K.re * vc.re - K.im * vc.im, p[c].im + K.re * vc.im + K.im * vc.re);
-        // v_r conj(w_c) + w_r conj(v_c)
-        const S re = vr.re * wc.re + vr.im * wc.im + wr.re * vc.re + wr.im * vc.im;
-        const S im = vr.im * wc.re - vr.re * wc.im + wr.im * vc.re - wr.re * vc.im;
-        arow[c].re -= re;
-        arow[c].im -= im;
+      if (r < L && tl == 0) {
+        p[r] = cmul(tj, acc);
+        q += v[r].re * acc.re + v[r].im * acc.im;
       }
+    }
+#pragma unroll
+    for (int o = TM; o < 32; o <<= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+    if (lane == 0) qpart[warp] = q;
+    __syncthreads();
+    S qs = 0;
+    for (int w = 0; w < nwarp; ++w) qs += qpart[w];
+    const S K = (S)-0.5 * (tj.re * tj.re + tj.im * tj.im) * qs;
+    // A22 -= v w^H + w v^H with w = p + K v: element (r, c) -= v_r conj(w_c) + w_r conj(v_c)
+    auto upd = [&](cplx<S>& a, const cplx<S>& vr, const cplx<S>& wr, const cplx<S>& vc, const cplx<S>& pc) {
+      const cplx<S> wc = mk<S>(pc.re + K * vc.re, pc.im + K * vc.im);
+      a.re -= vr.re * wc.re + vr.im * wc.im + wr.re * vc.re + wr.im * vc.im;
+      a.im -= vr.im * wc.re - vr.re * wc.im + wr.im * vc.re - wr.re * vc.im;
     };
-    if (nwarp == 1) {
-      for (int r = 0; r < L; ++r) update_row(r);
-      __syncwarp();
-      if (j + 1 < n - 1) reflector_warp<S>(A, lda, n, j + 1, d, e, tau);
-    } else if (warp == 0) {
-      update_row(0);
-      __syncwarp();
-      if (j + 1 < n - 1) reflector_warp<S>(A, lda, n, j + 1, d, e, tau);
-    } else {
-      // rows 1 .. L-1 element by element over the other warps' threads: independent updates, several in flight
-      // per thread (each element's arithmetic is update_row's)
-      const int nt1 = nt - 32, t1 = tid - 32, ne = (L - 1) * L;
+    const bool rows_by_warp0 = nwarp == 1;
+    if (warp == 0) {
+      // pivot row 0 of A22 in registers (c = lane + 32 h), then the reflector of column j + 1 from it:
+      // x_i = conj(A22[0][1 + i]); row j + 1 right of the diagonal becomes v_{j+1} (v[0] = 1 at c = 1)
+      const cplx<S> vr = v[0], pr = p[0];
+      const cplx<S> wr = mk<S>(pr.re + K * vr.re, pr.im + K * vr.im);
+      cplx<S> a[3];
+#pragma unroll
+      for (int h = 0; h < 3; ++h) {
+        const int c = lane + 32 * h;
+        a[h] = mk<S>(0, 0);
+        if (c < L) {
+          a[h] = A22[c];
+          upd(a[h], vr, wr, v[c], p[c]);
+        }
+      }
+      if (j + 1 < n - 1) {
+        S sg = 0;
+#pragma unroll
+        for (int h = 0; h < 3; ++h) {
+          const int c = lane + 32 * h;
+          if (c >= 2 && c < L) sg += a[h].re * a[h].re + a[h].im * a[h].im;
+        }
+        sg = warp_allsum(sg);
+        const cplx<S> alpha = mk<S>(__shfl_sync(0xffffffffu, a[0].re, 1), -__shfl_sync(0xffffffffu, a[0].im, 1));
+        S beta;
+        cplx<S> t = mk<S>(0, 0), sc = mk<S>(0, 0);
+        const bool refl = !(sg == (S)0 && alpha.im == (S)0);
+        if (!refl) {
+          beta = alpha.re;
+        } else {
+          const S an = sqrt(alpha.re * alpha.re + alpha.im * alpha.im + sg);
+          beta = alpha.re >= (S)0 ? -an : an;
+          const S ib = (S)1 / beta;
+          t = mk<S>((beta - alpha.re) * ib, -alpha.im * ib);
+          const S dr = alpha.re - beta, di = alpha.im, dd = dr * dr + di * di;
+          const S idd = (S)1 / dd;
+          sc = mk<S>(dr * idd, -di * idd);  // 1 / (alpha - beta)
+        }
+#pragma unroll
+        for (int h = 0; h < 3; ++h) {
+          const int c = lane + 32 * h;
+          if (c < L) {
+            cplx<S> o = a[h];  // c = 0: the diagonal
+            if (c == 1) o = mk<S>(1, 0);
+            else if (c >= 2 && refl) o = cmul(cconj(a[h]), sc);
+            A22[c] = o;
+          }
+        }
+        if (lane == 0) {
+          e[j + 1] = beta;
+          tau[j + 1] = t;
+          d[j + 1] = a[0].re;
+        }
+      } else {
+#pragma unroll
+        for (int h = 0; h < 3; ++h) {
+          const int c = lane + 32 * h;
+          if (c < L) A22[c] = a[h];
+        }
+      }
+    }
+    if (warp > 0 || rows_by_warp0) {
+      // rows 1 .. L-1 element by element over the other warps' threads (or warp 0's, for one warp): independent
+      // updates, several in flight per thread
+      const int nt1 = rows_by_warp0 ? 32 : nt - 32, t1 = rows_by_warp0 ? lane : tid - 32, ne = (L - 1) * L;
       const float rL = 1.0f / (float)L;
 #pragma unroll 4
-      for (int e = t1; e < ne; e += nt1) {
-        const int r = 1 + qdiv(e, rL), c = e - (r - 1) * L;
-        const cplx<S> vr = v[r], pr = p[r], vc = v[c], pc = p[c];
-        const cplx<S> wr = mk<S>(pr.re + K.re * vr.re - K.im * vr.im, pr.im + K.re * vr.im + K.im * vr.re);
-        const cplx<S> wc = mk<S>(pc.re + K.re * vc.re - K.im * vc.im, pc.im + K.re * vc.im + K.im * vc.re);
-        const S re = vr.re * wc.re + vr.im * wc.im + wr.re * vc.re + wr.im * vc.im;
-        const S im = vr.im * wc.re - vr.re * wc.im + wr.im * vc.re - wr.re * vc.im;
-        cplx<S>& a = A22[(size_t)r * lda + c];
-        a.re -= re;
-        a.im -= im;
+      for (int e2 = t1; e2 < ne; e2 += nt1) {
+        const int r = 1 + qdiv(e2, rL), c = e2 - (r - 1) * L;
+        const cplx<S> vr = v[r], pr = p[r];
+        const cplx<S> wr = mk<S>(pr.re + K * vr.re, pr.im + K * vr.im);
+        upd(A22[(size_t)r * lda + c], vr, wr, v[c], p[c]);
       }
     }
     __syncthreads();
