@@ -18,46 +18,77 @@ namespace {
 // ----------------------------------------------------------------------------- gram: out = A^H B
 constexpr int kGramTile = 16;
 
+template <int BYTES>
+__device__ __forceinline__ void cp_async_elem(void* dst, const void* src) {
+  static_assert(BYTES == 8 || BYTES == 16, "cp.async copies 4, 8 or 16 bytes");
+  if constexpr (BYTES == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+  else
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+
 template <class S, int TI>
 __global__ void __launch_bounds__(256) gram_partial_kernel(const cplx<S>* __restrict__ A, int lda, int p,
                                                            const cplx<S>* __restrict__ B, int ldb, int q, int nrow,
                                                            double* __restrict__ partial, int rows_per_part,
                                                            BatchMap bm) {
   // the p x q output is covered by a 16 x 16 thread grid with TI x TI entries per thread (16 TI >= p, q);
-  // one CTA per reduction part
-  constexpr int RT = 16;  // rows of A/B staged per step (8: 14.2 ms per 57,600 solve, 16: 13.9, 32: 14.0)
+  // one CTA per reduction part.  Rows are staged by cp.async, two stages of RT rows deep (both stages of both
+  // operands within 33 KB of static shared memory), so the next stage's loads are in flight while the current
+  // one is multiplied; each thread adds the rows in order, one running sum per entry.
   constexpr int W = 16 * TI;
-  __shared__ cplx<S> As[RT][W];
-  __shared__ cplx<S> Bs[RT][W];
+  constexpr int RT = (sizeof(S) == 4 ? 2 : 1) * (W <= 32 ? 16 : W <= 64 ? 8 : 4);
+  __shared__ cplx<S> As[2][RT][W];
+  __shared__ cplx<S> Bs[2][RT][W];
   const int tid = threadIdx.x, tx = tid % kGramTile, ty = tid / kGramTile;
   long r_begin, r_end;
   const int sys = bm_part(bm, blockIdx.x, nrow, rows_per_part, &r_begin, &r_end);
   if (bm_frozen(bm, sys)) return;
+  // columns past p (A) and q (B) are never copied: zero them in both stages once
+  for (int e = tid; e < 2 * RT * W; e += 256) {
+    if (e % W >= p) (&As[0][0][0])[e] = mk<S>(0, 0);
+    if (e % W >= q) (&Bs[0][0][0])[e] = mk<S>(0, 0);
+  }
+  auto stage = [&](int buf, long r0) {
+    const int nr = (int)min((long)RT, r_end - r0);
+    for (int e = tid; e < nr * W; e += 256) {
+      const int rr = e / W, c = e - rr * W;
+      if (c < p) cp_async_elem<sizeof(cplx<S>)>(&As[buf][rr][c], A + (r0 + rr) * lda + c);
+      if (c < q) cp_async_elem<sizeof(cplx<S>)>(&Bs[buf][rr][c], B + (r0 + rr) * ldb + c);
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
   cplx<S> acc[TI][TI];
 #pragma unroll
   for (int a = 0; a < TI; ++a)
 #pragma unroll
     for (int b = 0; b < TI; ++b) acc[a][b] = mk<S>(0, 0);
-  for (long r0 = r_begin; r0 < r_end; r0 += RT) {
-    for (int e = tid; e < RT * W; e += 256) {
-      const int rr = e / W, c = e % W;
-      const long gr = r0 + rr;
-      As[rr][c] = (gr < r_end && c < p) ? A[gr * lda + c] : mk<S>(0, 0);
-      Bs[rr][c] = (gr < r_end && c < q) ? B[gr * ldb + c] : mk<S>(0, 0);
+  const long nst = (r_end - r_begin + RT - 1) / RT;
+  if (nst > 0) stage(0, r_begin);
+  for (long t = 0; t < nst; ++t) {
+    const int buf = (int)(t & 1);
+    if (t + 1 < nst) {
+      stage(buf ^ 1, r_begin + (t + 1) * RT);
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
     }
     __syncthreads();
-    for (int rr = 0; rr < RT; ++rr) {
+    const int nr = (int)min((long)RT, r_end - (r_begin + t * RT));
+    for (int rr = 0; rr < nr; ++rr) {
       cplx<S> a[TI], b[TI];
 #pragma unroll
-      for (int i = 0; i < TI; ++i) a[i] = As[rr][ty + kGramTile * i];
+      for (int i = 0; i < TI; ++i) a[i] = As[buf][rr][ty + kGramTile * i];
 #pragma unroll
-      for (int j = 0; j < TI; ++j) b[j] = Bs[rr][tx + kGramTile * j];
+      for (int j = 0; j < TI; ++j) b[j] = Bs[buf][rr][tx + kGramTile * j];
 #pragma unroll
       for (int i = 0; i < TI; ++i)
 #pragma unroll
         for (int j = 0; j < TI; ++j) cfmac(acc[i][j], a[i], b[j]);
     }
-    __syncthreads();
+    __syncthreads();  // the next stage's copies overwrite this buffer
   }
   double* out = partial + (size_t)blockIdx.x * p * q * 2;
 #pragma unroll
@@ -78,17 +109,9 @@ __global__ void __launch_bounds__(256) gram_partial_kernel(const cplx<S>* __rest
 // cp.async (one copy per element, so any leading dimension works): the loads of the next stage are in flight while
 // the current one is multiplied.  Each thread adds the rows in the order of gram_partial_kernel, so the sums are
 // bitwise the same as two separate launches.  One CTA per reduction part; partials [part][p][p] of M, then of G at
-// partial + npart p p 2.
-template <int BYTES>
-__device__ __forceinline__ void cp_async_elem(void* dst, const void* src) {
-  static_assert(BYTES == 8 || BYTES == 16, "cp.async copies 4, 8 or 16 bytes");
-  if constexpr (BYTES == 8)
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
-                 : "memory");
-  else
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
-                 : "memory");
-}
+// partial + npart p p 2.  (Measured and rejected: thread-block clusters of 6 parts adding their FP64 partials
+// through distributed shared memory before writing.  Clusters must fit inside one GPC, which left room for 288
+// of the 300 CTAs at a time, and the second wave took the Gram pair from 52.6 to 92.0 us.)
 
 template <class S, int TI>
 __global__ void __launch_bounds__(256) gram_pair_partial_kernel(const cplx<S>* __restrict__ A,
@@ -633,24 +656,52 @@ __global__ void __launch_bounds__(256) pchol_basis_kernel(const zd* __restrict__
   S* dinv = reinterpret_cast<S*>(R + (size_t)n * lds);
   S* rinv = dinv + n;                                  // 1 / R[k][k]
   int* perm = reinterpret_cast<int*>(rinv + n);
-  cplx<S>* tri_scr = reinterpret_cast<cplx<S>*>((reinterpret_cast<uintptr_t>(perm + n) + 15) & ~(uintptr_t)15);
+  int* iperm = perm + n;                               // kept position of column i, or -1
+  cplx<S>* tri_scr = reinterpret_cast<cplx<S>*>((reinterpret_cast<uintptr_t>(iperm + n) + 15) & ~(uintptr_t)15);
   __shared__ int s_r;
-  for (int i = tid; i < n; i += nt) {
-    const double m = Mg[(size_t)i * ldm + i].re;
-    dinv[i] = m > 1e-300 ? (S)(1.0 / sqrt(m)) : (S)0;
-  }
-  __syncthreads();
-  for (int i = ty; i < n; i += 16)
-    for (int j = tx; j < n; j += 16) {
-      const zd a = Mg[(size_t)i * ldm + j], b = Mg[(size_t)j * ldm + i];
-      const S sc = dinv[i] * dinv[j];
-      W[(size_t)i * lds + j] = mk<S>((S)(0.5 * (a.re + b.re)) * sc, i == j ? (S)0 : (S)(0.5 * (a.im - b.im)) * sc);
+  // Ms, 48 x 48 entries per pass: a thread issues all of its (i, j) and (j, i) loads first (the diagonal scales
+  // are formed while they are in flight), then scales and symmetrises
+  constexpr int kLd = 3;
+  for (int i0 = 0; i0 < n; i0 += 16 * kLd)
+    for (int j0 = 0; j0 < n; j0 += 16 * kLd) {
+      zd av[kLd][kLd], bv[kLd][kLd];
+#pragma unroll
+      for (int ii = 0; ii < kLd; ++ii)
+#pragma unroll
+        for (int jj = 0; jj < kLd; ++jj) {
+          const int i = i0 + ty + 16 * ii, j = j0 + tx + 16 * jj;
+          if (i < n && j < n) {
+            av[ii][jj] = Mg[(size_t)i * ldm + j];
+            bv[ii][jj] = Mg[(size_t)j * ldm + i];
+          }
+        }
+      if (i0 == 0 && j0 == 0)
+        for (int i = tid; i < n; i += nt) {
+          const double m = Mg[(size_t)i * ldm + i].re;
+          dinv[i] = m > 1e-300 ? (S)(1.0 / sqrt(m)) : (S)0;
+        }
+      __syncthreads();  // dinv (uniform loop bounds)
+#pragma unroll
+      for (int ii = 0; ii < kLd; ++ii)
+#pragma unroll
+        for (int jj = 0; jj < kLd; ++jj) {
+          const int i = i0 + ty + 16 * ii, j = j0 + tx + 16 * jj;
+          if (i < n && j < n) {
+            const zd a = av[ii][jj], b = bv[ii][jj];
+            const S sc = dinv[i] * dinv[j];
+            W[(size_t)i * lds + j] =
+                mk<S>((S)(0.5 * (a.re + b.re)) * sc, i == j ? (S)0 : (S)(0.5 * (a.im - b.im)) * sc);
+          }
+        }
     }
   __syncthreads();
   int r = 0;  // kept so far (uniform across the block)
   for (int k = 0; k < n; ++k) {
     const S dk = W[(size_t)k * lds + k].re;
-    if (!(dk > (S)drop)) continue;  // uniform decision: every thread reads the same settled value
+    if (!(dk > (S)drop)) {  // uniform decision: every thread reads the same settled value
+      if (tid == 0) iperm[k] = -1;
+      continue;
+    }
     const S rkk = sqrt(dk), irk = (S)1 / rkk, idk = irk * irk;
     const cplx<S>* wk = W + (size_t)k * lds;
     // row r of R: columns k+1.. of the residual row k, scaled
@@ -664,6 +715,7 @@ __global__ void __launch_bounds__(256) pchol_basis_kernel(const zd* __restrict__
     }
     if (tid == 0) {
       perm[r] = k;
+      iperm[k] = r;
       rinv[r] = irk;
     }
     // Schur complement on the trailing block: W[i][j] -= conj(W[k][i]) W[k][j] / dk (a 16 x 16 thread grid;
@@ -736,17 +788,19 @@ __global__ void __launch_bounds__(256) pchol_basis_kernel(const zd* __restrict__
       __syncthreads();
     }
   }
-  // B[perm[k]][c] = dinv[perm[k]] Ri[k][c] (k <= c < r); everything else zero
-  for (int i = ty; i < n; i += 16)
-    for (int c = tx; c < n; c += 16) B[(size_t)i * ldb + c] = mk<double>(0.0, 0.0);
-  __syncthreads();
-  for (int k = ty; k < r; k += 16)
-    for (int c = tx; c < r; c += 16) {
-      if (k > c) continue;
-      const int i = perm[k];
-      const cplx<S> v = Ri[(size_t)k * lds + c];
-      B[(size_t)i * ldb + c] = mk<double>((double)v.re * (double)dinv[i], (double)v.im * (double)dinv[i]);
+  // B[perm[k]][c] = dinv[perm[k]] Ri[k][c] (k <= c < r); everything else zero (one pass over B)
+  for (int i = ty; i < n; i += 16) {
+    const int k = iperm[i];
+    const double di = (double)dinv[i];
+    for (int c = tx; c < n; c += 16) {
+      zd v = mk<double>(0.0, 0.0);
+      if (k >= 0 && k <= c && c < r) {
+        const cplx<S> x = Ri[(size_t)k * lds + c];
+        v = mk<double>((double)x.re * di, (double)x.im * di);
+      }
+      B[(size_t)i * ldb + c] = v;
     }
+  }
   if (tid == 0) *r_out = s_r;
 }
 
@@ -783,7 +837,8 @@ cudaError_t launch_gram_pair(const cplx<S>* A, const cplx<S>* B, int ld, int p, 
   if (p > 48) return cudaErrorInvalidValue;
   if (bm.parts) npart = bm.nparts;
   const int rpp = (nrow + npart - 1) / npart;
-  switch ((p + 15) / 16) {
+  const int ti = (p + 15) / 16;
+  switch (ti) {
     case 1: gram_pair_partial_kernel<S, 1><<<npart, 256, 0, s>>>(A, B, ld, p, nrow, partial, rpp, npart, bm); break;
     case 2: gram_pair_partial_kernel<S, 2><<<npart, 256, 0, s>>>(A, B, ld, p, nrow, partial, rpp, npart, bm); break;
     default: gram_pair_partial_kernel<S, 3><<<npart, 256, 0, s>>>(A, B, ld, p, nrow, partial, rpp, npart, bm); break;
@@ -898,9 +953,10 @@ template <class S>
 cudaError_t launch_pchol_basis(const zd* M, int ldm, int n, double drop, zd* B, int ldb, int* r_out, cudaStream_t s,
                                const BatchMap& bm, long m_stride, long b_stride) {
   if (n < 1 || n > 96) return cudaErrorInvalidValue;
-  // W, R (n x (n + 1) each), dinv, rinv, perm, and the triangular inverse's scratch (11 blocks of 8 x 8 for n <= 96)
-  const size_t smem = (size_t)2 * n * (n + 1) * sizeof(cplx<S>) + (size_t)2 * n * sizeof(S) + (size_t)n * sizeof(int) +
-                      16 + (size_t)((n + 7) / 8) * 64 * sizeof(cplx<S>) + 64;
+  // W, R (n x (n + 1) each), dinv, rinv, perm, iperm, and the triangular inverse's scratch (11 blocks of 8 x 8 for
+  // n <= 96)
+  const size_t smem = (size_t)2 * n * (n + 1) * sizeof(cplx<S>) + (size_t)2 * n * sizeof(S) +
+                      (size_t)2 * n * sizeof(int) + 16 + (size_t)((n + 7) / 8) * 64 * sizeof(cplx<S>) + 64;
   if (smem > 220 * 1024) return cudaErrorInvalidValue;
   cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(pchol_basis_kernel<S>), smem);
   if (e != cudaSuccess) return e;

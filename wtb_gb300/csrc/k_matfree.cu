@@ -499,6 +499,7 @@ __global__ void __launch_bounds__(256) mf_scatter_t_kernel(const float* __restri
 // conflict-free.  The sums are those of the tiles above, term for term and in the same order.
 constexpr int kLaneK = 32;
 constexpr int kLaneKp = 33;
+constexpr int kScatMaxW = 16;  // orbitals per k-point of the lane-k scatter (its T row values live in registers)
 
 // shared memory of the lane-k gather: Vs, Cs, xs, Y1
 inline size_t gather32_smem(int nv, int nc, int w, int nbp) {
@@ -620,16 +621,26 @@ __global__ void __launch_bounds__(256) mf_scatter_k32_kernel(const float* __rest
   // n = ((b0 + bb) w + o) 2w + 2p (+1) are read at columns k0 .. k0 + 31 (ldt >= the tile's end: padding columns)
   for (int it = warp; it < nbl * w; it += nwarp) {  // it = bb w + o
     const float* trow = Tt + (size_t)(b0 * w + it) * tw * ldt + k0 + lane;
+    // the row's 2w values of lane k, all loads issued before the first use (w <= kScatMaxW)
+    float tre[kScatMaxW], tim[kScatMaxW];
+#pragma unroll
+    for (int p = 0; p < kScatMaxW; ++p)
+      if (p < w) {
+        tre[p] = trow[(size_t)(2 * p) * ldt];
+        tim[p] = trow[(size_t)(2 * p + 1) * ldt];
+      }
     for (int v0 = 0; v0 < nv; v0 += 4) {
       zf acc[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) acc[i] = mk<float>(0.f, 0.f);
-      for (int p = 0; p < w; ++p) {
-        const zf tc = mk<float>(trow[(size_t)(2 * p) * ldt], trow[(size_t)(2 * p + 1) * ldt]);
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
-          if (v0 + i < nv) cfmac(acc[i], Vs[((v0 + i) * w + p) * kLaneKp + lane], tc);
-      }
+      for (int p = 0; p < kScatMaxW; ++p)
+        if (p < w) {
+          const zf tc = mk<float>(tre[p], tim[p]);
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+            if (v0 + i < nv) cfmac(acc[i], Vs[((v0 + i) * w + p) * kLaneKp + lane], tc);
+        }
 #pragma unroll
       for (int i = 0; i < 4; ++i)
         if (v0 + i < nv) U[(it * nv + v0 + i) * kLaneKp + lane] = acc[i];
@@ -863,7 +874,7 @@ cudaError_t launch_mf_scatter_t(const float* Tt, int ldt, const zf* X, int ldx, 
     // the lane-k scatter: 32 k-points per CTA along the lanes, cols - 100 block columns
     const int g = std::min(cols - 100, nb);
     const size_t smem = scatter32_smem(nv, nc, w, g);
-    if (smem > 200 * 1024 || ldt < (nk + kLaneK - 1) / kLaneK * kLaneK) return cudaErrorInvalidValue;
+    if (smem > 200 * 1024 || w > kScatMaxW || ldt < (nk + kLaneK - 1) / kLaneK * kLaneK) return cudaErrorInvalidValue;
     cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(mf_scatter_k32_kernel), smem);
     if (e != cudaSuccess) return e;
     mf_scatter_k32_kernel<<<dim3((nk + kLaneK - 1) / kLaneK, (nb + g - 1) / g), 256, smem, s>>>(
