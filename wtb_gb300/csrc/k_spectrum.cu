@@ -26,7 +26,7 @@ constexpr int kOscRows = 256;
 __global__ void __launch_bounds__(256) osc_partial_kernel(const zd* __restrict__ A, int lda, int nev, int dim,
                                                           const zd* __restrict__ hr, double* __restrict__ partial) {
   __shared__ zd hs[5][kOscRows];
-  __shared__ double red[8][32][10];
+  __shared__ double red[8][32][2];
   const int r0 = blockIdx.x * kOscRows;
   const int nr = min(kOscRows, dim - r0);
   for (int e = threadIdx.x; e < 5 * kOscRows; e += blockDim.x) {
@@ -34,47 +34,53 @@ __global__ void __launch_bounds__(256) osc_partial_kernel(const zd* __restrict__
     hs[a][r] = r < nr ? hr[(size_t)a * dim + r0 + r] : mk<double>(0.0, 0.0);
   }
   __syncthreads();
+  // lanes along (exciton n, component a) pairs, 32 per pass (the FP64 pipe then serves up to 32 useful lanes of a
+  // warp instruction, not nev); each warp adds its rows r = warp, warp + 8, ... in order, then the 8 warp sums
+  // are added in warp order
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int n0 = 0; n0 < nev; n0 += 32) {
-    const int n = n0 + lane;
-    zd acc[5];
-#pragma unroll
-    for (int a = 0; a < 5; ++a) acc[a] = mk<double>(0.0, 0.0);
-    if (n < nev)
-      for (int r = warp; r < nr; r += 8) {
-        const zd x = A[(size_t)(r0 + r) * lda + n];
-#pragma unroll
-        for (int a = 0; a < 5; ++a) cfma(acc[a], x, hs[a][r]);
-      }
-#pragma unroll
-    for (int a = 0; a < 5; ++a) {
-      red[warp][lane][2 * a] = acc[a].re;
-      red[warp][lane][2 * a + 1] = acc[a].im;
-    }
+  const int npair = nev * 5;
+  for (int q0 = 0; q0 < npair; q0 += 32) {
+    const int q = q0 + lane, n = q / 5, a = q - 5 * n;
+    zd acc = mk<double>(0.0, 0.0);
+    if (q < npair)
+      for (int r = warp; r < nr; r += 8) cfma(acc, A[(size_t)(r0 + r) * lda + n], hs[a][r]);
+    red[warp][lane][0] = acc.re;
+    red[warp][lane][1] = acc.im;
     __syncthreads();
-    for (int e = threadIdx.x; e < 32 * 10; e += blockDim.x) {
-      const int l = e / 10, q = e % 10;
-      if (n0 + l >= nev) continue;
+    for (int e = threadIdx.x; e < 32 * 2; e += blockDim.x) {
+      const int l = e >> 1, ri = e & 1, qq = q0 + l;
+      if (qq >= npair) continue;
       double t = 0.0;
-      for (int w = 0; w < 8; ++w) t += red[w][l][q];
-      partial[((size_t)blockIdx.x * nev + n0 + l) * 10 + q] = t;
+      for (int w = 0; w < 8; ++w) t += red[w][l][ri];
+      const int nn = qq / 5, aa = qq - 5 * nn;
+      partial[((size_t)blockIdx.x * nev + nn) * 10 + 2 * aa + ri] = t;
     }
     __syncthreads();
   }
 }
 
-__global__ void osc_final_kernel(const double* __restrict__ partial, int nblk, int nev, double* __restrict__ osc) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= nev) return;
-  zd s[5];
-  for (int a = 0; a < 5; ++a) s[a] = mk<double>(0.0, 0.0);
-  for (int b = 0; b < nblk; ++b) {
+// one warp per exciton: lane l adds the blocks b = l, l + 32, ... in order, then a fixed butterfly over the lanes
+__global__ void __launch_bounds__(256) osc_final_kernel(const double* __restrict__ partial, int nblk, int nev,
+                                                        double* __restrict__ osc) {
+  const int lane = threadIdx.x & 31;
+  const int n = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (n >= nev) return;  // warp-uniform
+  double v[10];
+#pragma unroll
+  for (int q = 0; q < 10; ++q) v[q] = 0.0;
+  for (int b = lane; b < nblk; b += 32) {
     const double* p = partial + ((size_t)b * nev + n) * 10;
-    for (int a = 0; a < 5; ++a) {
-      s[a].re += p[2 * a];
-      s[a].im += p[2 * a + 1];
-    }
+#pragma unroll
+    for (int q = 0; q < 10; ++q) v[q] += p[q];
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int q = 0; q < 10; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+  if (lane != 0) return;
+  zd s[5];
+#pragma unroll
+  for (int a = 0; a < 5; ++a) s[a] = mk<double>(v[2 * a], v[2 * a + 1]);
   auto re_prod = [](zd a, zd b) { return a.re * b.re + a.im * b.im; };  // Re(a conj(b))
   osc[0 * nev + n] = re_prod(s[0], s[0]);
   osc[1 * nev + n] = re_prod(s[1], s[1]);
@@ -403,7 +409,7 @@ cudaError_t launch_oscillators(const zd* A, int lda, int nev, int dim, const zd*
   const int nblk = (dim + kOscRows - 1) / kOscRows;
   if (nblk > npart) return cudaErrorInvalidValue;
   osc_partial_kernel<<<nblk, 256, 0, s>>>(A, lda, nev, dim, hr, partial); ++g_launch_count;
-  osc_final_kernel<<<(nev + 127) / 128, 128, 0, s>>>(partial, nblk, nev, osc); ++g_launch_count;
+  osc_final_kernel<<<(nev + 7) / 8, 256, 0, s>>>(partial, nblk, nev, osc); ++g_launch_count;
   return cudaGetLastError();
 }
 
