@@ -109,7 +109,9 @@ __global__ void __launch_bounds__(256) gram_partial_kernel(const cplx<S>* __rest
 // cp.async (one copy per element, so any leading dimension works): the loads of the next stage are in flight while
 // the current one is multiplied.  Each thread adds the rows in the order of gram_partial_kernel, so the sums are
 // bitwise the same as two separate launches.  One CTA per reduction part; partials [part][p][p] of M, then of G at
-// partial + npart p p 2.  (Measured and rejected: thread-block clusters of 6 parts adding their FP64 partials
+// partial + npart p p 2.  (Measured and rejected: the complex multiply-adds as packed fma.rn.f32x2 pairs, bitwise
+// the same sums with half the FMA instructions, took 58.8 us against 52.5 (the pair packing costs more than it
+// saves); and thread-block clusters of 6 parts adding their FP64 partials
 // through distributed shared memory before writing.  Clusters must fit inside one GPC, which left room for 288
 // of the 300 CTAs at a time, and the second wave took the Gram pair from 52.6 to 92.0 us.)
 
@@ -515,12 +517,116 @@ __device__ void select_m_smallest(const double* __restrict__ val, const int* __r
   }
 }
 
+// The same selection for m <= M: every thread keeps a sorted list of the M smallest (value, index) pairs of its
+// rows (registers, insertion by compare-and-swap), then m rounds take the smallest head over the CTA (a warp
+// butterfly, then the 8 warp winners) and its owner pops it.  The order is the lexicographic (value, index) order
+// of select_m_smallest, so both give the same indices in the same order; 256 threads.  Values are compared as
+// order-preserving unsigned keys (sign bit set for x >= 0, all bits flipped for x < 0, -0 taken as +0: the
+// floating-point order of non-NaN doubles), integer work instead of FP64 compares.
+__device__ __forceinline__ unsigned long long order_key(double x) {
+  unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  if ((u << 1) == 0ull) u = 0ull;  // -0 == +0
+  return (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+}
+__device__ __forceinline__ double key_value(unsigned long long k) {
+  return __longlong_as_double((long long)((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k));
+}
+__device__ __forceinline__ bool vi_less(unsigned long long a, int ia, unsigned long long b, int ib) {
+  return a < b || (a == b && ia < ib);
+}
+
+template <int M>
+__device__ void select_m_smallest_lists(const double* __restrict__ val, const int* __restrict__ ids, int r0, int r1,
+                                        int m, double* __restrict__ out_val, int* __restrict__ out_idx) {
+  constexpr unsigned long long kNone = 0xffffffffffffffffull;  // above every key of a non-NaN double
+  __shared__ unsigned long long wv[8];
+  __shared__ int wi[8];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  unsigned long long lv[M];
+  int li[M];
+#pragma unroll
+  for (int k = 0; k < M; ++k) {
+    lv[k] = kNone;
+    li[k] = 0x7fffffff;
+  }
+  for (int r = r0 + tid; r < r1; r += blockDim.x) {
+    const int id = ids ? ids[r] : r;
+    if (id < 0) continue;
+    const unsigned long long d = order_key(val[r]);
+    if (vi_less(d, id, lv[M - 1], li[M - 1])) {
+      lv[M - 1] = d;
+      li[M - 1] = id;
+#pragma unroll
+      for (int k = M - 1; k > 0; --k)
+        if (vi_less(lv[k], li[k], lv[k - 1], li[k - 1])) {
+          const unsigned long long tv = lv[k];
+          lv[k] = lv[k - 1];
+          lv[k - 1] = tv;
+          const int ti = li[k];
+          li[k] = li[k - 1];
+          li[k - 1] = ti;
+        }
+    }
+  }
+  for (int s = 0; s < m; ++s) {
+    unsigned long long bv = lv[0];
+    int bi = li[0];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long ov = __shfl_xor_sync(0xffffffffu, bv, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (vi_less(ov, oi, bv, bi)) {
+        bv = ov;
+        bi = oi;
+      }
+    }
+    if (lane == 0) {
+      wv[warp] = bv;
+      wi[warp] = bi;
+    }
+    __syncthreads();
+    bv = wv[0];
+    bi = wi[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+      if (vi_less(wv[w], wi[w], bv, bi)) {
+        bv = wv[w];
+        bi = wi[w];
+      }
+    if (tid == 0) {
+      out_val[s] = bi == 0x7fffffff ? 1e300 : key_value(bv);
+      out_idx[s] = bi == 0x7fffffff ? -1 : bi;
+    }
+    if (bi != 0x7fffffff && li[0] == bi) {  // the owner (indices are distinct) pops its head
+#pragma unroll
+      for (int k = 0; k < M - 1; ++k) {
+        lv[k] = lv[k + 1];
+        li[k] = li[k + 1];
+      }
+      lv[M - 1] = kNone;
+      li[M - 1] = 0x7fffffff;
+    }
+    __syncthreads();  // wv / wi are rewritten next round
+  }
+}
+
+// m smallest by lists when m <= 32, else by rounds of full scans
+__device__ __forceinline__ void select_m_smallest_any(const double* __restrict__ val, const int* __restrict__ ids,
+                                                      int r0, int r1, int m, double* __restrict__ out_val,
+                                                      int* __restrict__ out_idx) {
+  if (m <= 16)
+    select_m_smallest_lists<16>(val, ids, r0, r1, m, out_val, out_idx);
+  else if (m <= 32)
+    select_m_smallest_lists<32>(val, ids, r0, r1, m, out_val, out_idx);
+  else
+    select_m_smallest(val, ids, r0, r1, m, out_val, out_idx);
+}
+
 __global__ void __launch_bounds__(256) select_lowest_kernel(const double* __restrict__ val, const int* __restrict__ ids,
                                                             int count, int m, double* __restrict__ out_val,
                                                             int* __restrict__ out_idx) {
   const int per = (count + gridDim.x - 1) / gridDim.x;
   const int r0 = blockIdx.x * per, r1 = min(count, r0 + per);
-  select_m_smallest(val, ids, r0, r1, m, out_val + blockIdx.x * m, out_idx + blockIdx.x * m);
+  select_m_smallest_any(val, ids, r0, r1, m, out_val + blockIdx.x * m, out_idx + blockIdx.x * m);
 }
 
 // batch, first level: CTA (g, q) takes the m smallest of slice g of system q's rows (indices relative to the
@@ -533,7 +639,7 @@ __global__ void __launch_bounds__(256) select_lowest_batch_kernel(const double* 
   const int per = (rw.y + ng - 1) / ng;
   const int r0 = min(rw.y, g * per), r1 = min(rw.y, r0 + per);
   const size_t o = ((size_t)q * ng + g) * m;
-  select_m_smallest(diag + rw.x, nullptr, r0, r1, m, cand_val + o, cand_idx + o);
+  select_m_smallest_any(diag + rw.x, nullptr, r0, r1, m, cand_val + o, cand_idx + o);
 }
 
 // batch, second level: one CTA per system over its ng * m candidates, into out_idx + idx_stride q
@@ -543,7 +649,8 @@ __global__ void __launch_bounds__(256) select_lowest_batch2_kernel(const double*
                                                                    int* __restrict__ out_idx, long idx_stride) {
   const int q = blockIdx.x;
   const size_t o = (size_t)q * ng * m;
-  select_m_smallest(cand_val + o, cand_idx + o, 0, ng * m, m, out_val + (size_t)q * m, out_idx + (size_t)q * idx_stride);
+  select_m_smallest_any(cand_val + o, cand_idx + o, 0, ng * m, m, out_val + (size_t)q * m,
+                        out_idx + (size_t)q * idx_stride);
 }
 
 // rows of every system (nrow in all); the noise depends on the row within its system, so a system gets the
