@@ -506,10 +506,13 @@ inline size_t gather32_smem(int nv, int nc, int w, int nbp) {
   return (size_t)(nv * w + nc * w + nc * nv * nbp + nc * w * nbp) * kLaneKp * sizeof(zf);
 }
 
+// NV, NC > 0: the band counts fixed at compile time (the loops over them unroll), else taken from nv_rt, nc_rt
+template <int NV, int NC>
 __global__ void __launch_bounds__(256) mf_gather_k32_kernel(const zf* __restrict__ X, int ldx, int c0, int nbc,
-                                                            int nbp, const zf* __restrict__ vec, int nk, int nv,
-                                                            int nc, int w, float* __restrict__ z32, int ldk) {
+                                                            int nbp, const zf* __restrict__ vec, int nk, int nv_rt,
+                                                            int nc_rt, int w, float* __restrict__ z32, int ldk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nv = NV > 0 ? NV : nv_rt, nc = NC > 0 ? NC : nc_rt;
   const int nbnd = nv + nc, ncv = nc * nv;
   const int k0 = blockIdx.x * kLaneK, b0 = blockIdx.y * nbp;
   const int nbl = min(nbp, nbc - b0);
@@ -541,10 +544,12 @@ __global__ void __launch_bounds__(256) mf_gather_k32_kernel(const zf* __restrict
   // Y1[c][p][bb] = sum_v Vb[v][p] x[c][v][bb] for lane k: a warp takes (p, bb) items and every c
   for (int it = warp; it < w * nbl; it += nwarp) {
     const int p = qdiv(it, r_nbl), bb = it - p * nbl;
+#pragma unroll
     for (int cb = 0; cb < nc; cb += 4) {
       zf acc[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) acc[i] = mk<float>(0.f, 0.f);
+#pragma unroll
       for (int v = 0; v < nv; ++v) {
         const zf a = Vs[(v * w + p) * kLaneKp + lane];
 #pragma unroll
@@ -567,6 +572,7 @@ __global__ void __launch_bounds__(256) mf_gather_k32_kernel(const zf* __restrict
     zf acc[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) acc[i] = mk<float>(0.f, 0.f);
+#pragma unroll
     for (int c = 0; c < nc; ++c) {
       const zf y = Y1[((c * w + p) * nbp + bb) * kLaneKp + lane];
 #pragma unroll
@@ -586,25 +592,31 @@ __global__ void __launch_bounds__(256) mf_gather_k32_kernel(const zf* __restrict
 }
 
 // shared memory of the lane-k scatter: Vs, Cs, U
+// U's column groups are ustride(w, nv) complex apart: w nv 33 rounded up to 4 mod 16, so that lanes of different
+// groups at one (o, v) fall in different bank pairs (w nv 33 itself is a multiple of 16 at w = 12, nv = 4)
+inline int scatter32_ustride(int w, int nv) { return w * nv * kLaneKp + ((4 - (w * nv * kLaneKp) % 16) + 16) % 16; }
 inline size_t scatter32_smem(int nv, int nc, int w, int nbg) {
-  return (size_t)(nv * w + nc * w + nbg * w * nv) * kLaneKp * sizeof(zf);
+  return ((size_t)(nv * w + nc * w) * kLaneKp + (size_t)nbg * scatter32_ustride(w, nv)) * sizeof(zf);
 }
 
 // y[k][c][v][b] = dE x + sum_o conj(C[k][c][o]) sum_p conj(Vb[k][v][p]) T[k][b][o][p] for 32 k-points (lanes) and
 // nbg block columns
+template <int NV, int NC>
 __global__ void __launch_bounds__(256) mf_scatter_k32_kernel(const float* __restrict__ Tt, int ldt,
                                                              const zf* __restrict__ X, int ldx,
                                                              const zf* __restrict__ vec,
-                                                             const float* __restrict__ dE, int nk, int nv, int nc,
-                                                             int w, int nb, int nbg, zf* __restrict__ Y, int ldy,
-                                                             int c0) {
+                                                             const float* __restrict__ dE, int nk, int nv_rt,
+                                                             int nc_rt, int w, int nb, int nbg, zf* __restrict__ Y,
+                                                             int ldy, int c0) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nv = NV > 0 ? NV : nv_rt, nc = NC > 0 ? NC : nc_rt;
   const int nbnd = nv + nc, ncv = nc * nv, tw = 2 * w;
   const int k0 = blockIdx.x * kLaneK, b0 = blockIdx.y * nbg;
   const int nbl = min(nbg, nb - b0);
   zf* Vs = reinterpret_cast<zf*>(smem_raw);  // [v][p][33]
   zf* Cs = Vs + nv * w * kLaneKp;             // [c][o][33]
-  zf* U = Cs + nc * w * kLaneKp;              // [bb][o][v][33]
+  zf* U = Cs + nc * w * kLaneKp;              // [bb][o][v][33], column groups ust apart
+  const int ust = w * nv * kLaneKp + ((4 - (w * nv * kLaneKp) % 16) + 16) % 16;
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
   const float r_bw = 1.0f / (nbnd * w), r_w = 1.0f / w, r_nv = 1.0f / nv, r_nbl = 1.0f / nbl;
   for (int e = tid; e < kLaneK * nbnd * w; e += nt) {
@@ -619,7 +631,9 @@ __global__ void __launch_bounds__(256) mf_scatter_k32_kernel(const float* __rest
   __syncthreads();
   // U[bb][o][v] = sum_p conj(Vb[v][p]) T[bb][o][p] for lane k: a warp takes (bb, o) rows; T's re and im rows
   // n = ((b0 + bb) w + o) 2w + 2p (+1) are read at columns k0 .. k0 + 31 (ldt >= the tile's end: padding columns)
+  const float r_wu = 1.0f / w;
   for (int it = warp; it < nbl * w; it += nwarp) {  // it = bb w + o
+    const int bbit = qdiv(it, r_wu), oit = it - bbit * w;
     const float* trow = Tt + (size_t)(b0 * w + it) * tw * ldt + k0 + lane;
     // the row's 2w values of lane k, all loads issued before the first use (w <= kScatMaxW)
     float tre[kScatMaxW], tim[kScatMaxW];
@@ -629,6 +643,7 @@ __global__ void __launch_bounds__(256) mf_scatter_k32_kernel(const float* __rest
         tre[p] = trow[(size_t)(2 * p) * ldt];
         tim[p] = trow[(size_t)(2 * p + 1) * ldt];
       }
+#pragma unroll
     for (int v0 = 0; v0 < nv; v0 += 4) {
       zf acc[4];
 #pragma unroll
@@ -643,7 +658,7 @@ __global__ void __launch_bounds__(256) mf_scatter_k32_kernel(const float* __rest
         }
 #pragma unroll
       for (int i = 0; i < 4; ++i)
-        if (v0 + i < nv) U[(it * nv + v0 + i) * kLaneKp + lane] = acc[i];
+        if (v0 + i < nv) U[bbit * ust + (oit * nv + v0 + i) * kLaneKp + lane] = acc[i];
     }
   }
   __syncthreads();
@@ -656,7 +671,7 @@ __global__ void __launch_bounds__(256) mf_scatter_k32_kernel(const float* __rest
     const int c = qdiv(cv, r_nv), v = cv - c * nv;
     zf acc = mk<float>(0.f, 0.f);
     for (int o = 0; o < w; ++o)
-      cfmac(acc, Cs[(c * w + o) * kLaneKp + kk], U[((bb * w + o) * nv + v) * kLaneKp + kk]);
+      cfmac(acc, Cs[(c * w + o) * kLaneKp + kk], U[bb * ust + (o * nv + v) * kLaneKp + kk]);
     if (k0 + kk < nk) {
       const size_t I = (size_t)(k0 + kk) * ncv + cv;
       const zf x = X[I * ldx + c0 + b0 + bb];
@@ -811,9 +826,12 @@ cudaError_t launch_mf_gather(const cplx<S>* X, int ldx, int c0, int nb, const cp
       // the lane-k gather: 32 k' per CTA along the lanes
       const size_t smem = gather32_smem(nv, nc, w, nbp);
       if (smem > 200 * 1024 || ldk % kLaneK != 0 || nslices != 1) return cudaErrorInvalidValue;
-      cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(mf_gather_k32_kernel), smem);
+      auto kern = nv == 4 && nc == 4 ? mf_gather_k32_kernel<4, 4>
+                  : nv == 2 && nc == 2 ? mf_gather_k32_kernel<2, 2>
+                                       : mf_gather_k32_kernel<0, 0>;
+      cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(kern), smem);
       if (e != cudaSuccess) return e;
-      mf_gather_k32_kernel<<<dim3((nk + kLaneK - 1) / kLaneK, (nb + nbp - 1) / nbp), 256, smem, s>>>(
+      kern<<<dim3((nk + kLaneK - 1) / kLaneK, (nb + nbp - 1) / nbp), 256, smem, s>>>(
           reinterpret_cast<const zf*>(X), ldx, c0, nb, nbp, vec_win, nk, nv, nc, w, reinterpret_cast<float*>(zt), ldk);
       ++g_launch_count;
       return cudaGetLastError();
@@ -875,9 +893,12 @@ cudaError_t launch_mf_scatter_t(const float* Tt, int ldt, const zf* X, int ldx, 
     const int g = std::min(cols - 100, nb);
     const size_t smem = scatter32_smem(nv, nc, w, g);
     if (smem > 200 * 1024 || w > kScatMaxW || ldt < (nk + kLaneK - 1) / kLaneK * kLaneK) return cudaErrorInvalidValue;
-    cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(mf_scatter_k32_kernel), smem);
+    auto kern = nv == 4 && nc == 4 ? mf_scatter_k32_kernel<4, 4>
+                : nv == 2 && nc == 2 ? mf_scatter_k32_kernel<2, 2>
+                                     : mf_scatter_k32_kernel<0, 0>;
+    cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(kern), smem);
     if (e != cudaSuccess) return e;
-    mf_scatter_k32_kernel<<<dim3((nk + kLaneK - 1) / kLaneK, (nb + g - 1) / g), 256, smem, s>>>(
+    kern<<<dim3((nk + kLaneK - 1) / kLaneK, (nb + g - 1) / g), 256, smem, s>>>(
         Tt, ldt, X, ldx, vec_win, dE, nk, nv, nc, w, nb, g, Y, ldy, c0);
     ++g_launch_count;
     return cudaGetLastError();
