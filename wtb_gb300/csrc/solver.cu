@@ -522,86 +522,124 @@ __global__ void cond_copy_kernel(const LobCtl* __restrict__ ctl, int which, cons
 // load of C serve four complex FMAs.  Each output keeps the summation order of a plain loop (X block, then
 // [W P]), independent of the tiling.  C of the tile's system is staged again only when the system changes.
 constexpr int kUpdRows = kTileRows;
+template <int BYTES>
+__device__ __forceinline__ void upd_cp_async(void* dst, const void* src) {
+  if constexpr (BYTES == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+  else
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+
+// Stages of the row tiles: two for FP32 (the next tile's rows are copied by cp.async while the current one is
+// combined), one for FP64 (two would not fit in shared memory)
+template <class S>
+__host__ __device__ constexpr int upd_stages() { return sizeof(S) == 4 ? 2 : 1; }
+
 template <class S>
 __global__ void __launch_bounds__(256) lob_update_kernel(cplx<S>* __restrict__ Sb, cplx<S>* __restrict__ ASb, int ld,
                                                          int m, const zd* __restrict__ C, int nrow, BatchMap bm,
                                                          long c_stride) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int NST = upd_stages<S>();
   const int nb = 3 * m, RS = nb + 2;
   cplx<S>* Cs = reinterpret_cast<cplx<S>*>(smem_raw);  // [3m][m]
-  cplx<S>* Rs = Cs + ((nb * m + 1) & ~1);              // [2][kUpdRows][RS]: rows of S, then of AS
+  cplx<S>* Rs = Cs + ((nb * m + 1) & ~1);              // [NST][2][kUpdRows][RS]: rows of S, then of AS
+  const int STG = 2 * kUpdRows * RS;                   // one stage
   const int ngrp = (m + 1) >> 1;      // pairs of output columns
   const int items = kUpdRows * ngrp;  // (row, pair) items per tile
   const bool vec = sizeof(S) == 4 && (ld & 1) == 0 && (nb & 1) == 0;
+  auto tile_r0 = [&](long t) { return ((long)blockIdx.x + t * gridDim.x) * kUpdRows; };
+  // copies of a tile's rows of S and AS into stage buf (none for a tile past the end or of a frozen system; every
+  // call commits one group, so that the wait counts stay in step)
+  auto stage = [&](int buf, long r0) {
+    if (r0 < nrow && !bm_frozen(bm, bm_sys_of_row(bm, r0))) {
+      const int nr = (int)min((long)kUpdRows, nrow - r0);
+      for (int which = 0; which < 2; ++which) {
+        const cplx<S>* base = (which ? ASb : Sb) + r0 * ld;
+        cplx<S>* dst = Rs + buf * STG + which * kUpdRows * RS;
+        if (vec) {  // two complex FP32 per 16-byte copy
+          const int hp = nb >> 1;
+          for (int e = threadIdx.x; e < nr * hp; e += blockDim.x) {
+            const int rr = e / hp, c2 = e - rr * hp;
+            upd_cp_async<16>(dst + rr * RS + 2 * c2, base + (size_t)rr * ld + 2 * c2);
+          }
+        } else {
+          for (int e = threadIdx.x; e < nr * nb; e += blockDim.x) {
+            const int rr = e / nb, c = e - rr * nb;
+            upd_cp_async<sizeof(cplx<S>)>(dst + rr * RS + c, base + (size_t)rr * ld + c);
+          }
+        }
+      }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
   int staged = -1;
-  for (long r0 = (long)blockIdx.x * kUpdRows; r0 < nrow; r0 += (long)gridDim.x * kUpdRows) {
+  if (NST == 2) stage(0, tile_r0(0));
+  for (long t = 0; tile_r0(t) < nrow; ++t) {
+    const long r0 = tile_r0(t);
+    const int buf = NST == 2 ? (int)(t & 1) : 0;
+    if (NST == 2) {
+      stage(buf ^ 1, tile_r0(t + 1));  // the next tile's copies in flight
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    } else {
+      stage(0, r0);
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    }
     const int sys = bm_sys_of_row(bm, r0);  // uniform over the CTA
-    if (bm_frozen(bm, sys)) continue;
-    __syncthreads();  // the previous tile's reads of Rs (and of Cs) are done
-    if (sys != staged) {
+    const bool live = !bm_frozen(bm, sys);
+    if (live && sys != staged) {  // the previous tile's reads of Cs ended at the last barrier
       const zd* Cq = C + (size_t)sys * c_stride;
       for (int e = threadIdx.x; e < nb * m; e += blockDim.x) Cs[e] = mk<S>((S)Cq[e].re, (S)Cq[e].im);
       staged = sys;
     }
+    __syncthreads();  // every thread's copies of this tile (and Cs) are visible
     const int nr = (int)min((long)kUpdRows, nrow - r0);
-    for (int which = 0; which < 2; ++which) {
-      const cplx<S>* base = (which ? ASb : Sb) + r0 * ld;
-      cplx<S>* dst = Rs + which * kUpdRows * RS;
-      if (vec) {  // two complex FP32 per 16-byte copy
-        const int hp = nb >> 1;
-        for (int e = threadIdx.x; e < nr * hp; e += blockDim.x) {
-          const int rr = e / hp, c2 = e - rr * hp;
-          *reinterpret_cast<float4*>(dst + rr * RS + 2 * c2) =
-              *reinterpret_cast<const float4*>(base + (size_t)rr * ld + 2 * c2);
+    const cplx<S>* Rb = Rs + buf * STG;
+    if (live) {
+      for (int it = threadIdx.x; it < items; it += blockDim.x) {
+        const int rr = it / ngrp, g = it - rr * ngrp;
+        if (rr >= nr) continue;
+        const int j0 = g * 2;
+        const bool two = j0 + 1 < m;
+        const cplx<S>* rs = Rb + rr * RS;
+        const cplx<S>* ra = Rb + (kUpdRows + rr) * RS;
+        cplx<S> xs0 = mk<S>(0, 0), xs1 = mk<S>(0, 0), ps0 = mk<S>(0, 0), ps1 = mk<S>(0, 0);
+        cplx<S> xa0 = mk<S>(0, 0), xa1 = mk<S>(0, 0), pa0 = mk<S>(0, 0), pa1 = mk<S>(0, 0);
+        for (int i = 0; i < m; ++i) {  // the X block contributes to X only
+          const cplx<S> si = rs[i], ai = ra[i];
+          const cplx<S>* crow = Cs + i * m + j0;
+          const cplx<S> c0 = crow[0], c1 = two ? crow[1] : mk<S>(0, 0);
+          cfma(xs0, si, c0);
+          cfma(xa0, ai, c0);
+          cfma(xs1, si, c1);
+          cfma(xa1, ai, c1);
         }
-      } else {
-        for (int e = threadIdx.x; e < nr * nb; e += blockDim.x) {
-          const int rr = e / nb, c = e - rr * nb;
-          dst[rr * RS + c] = base[(size_t)rr * ld + c];
+        for (int i = m; i < nb; ++i) {  // W and P contribute to X and to the new P
+          const cplx<S> si = rs[i], ai = ra[i];
+          const cplx<S>* crow = Cs + i * m + j0;
+          const cplx<S> c0 = crow[0], c1 = two ? crow[1] : mk<S>(0, 0);
+          cfma(ps0, si, c0);
+          cfma(pa0, ai, c0);
+          cfma(ps1, si, c1);
+          cfma(pa1, ai, c1);
+        }
+        cplx<S>* os = Sb + (r0 + rr) * ld;
+        cplx<S>* oa = ASb + (r0 + rr) * ld;
+        os[j0] = mk<S>(xs0.re + ps0.re, xs0.im + ps0.im);
+        os[2 * m + j0] = ps0;
+        oa[j0] = mk<S>(xa0.re + pa0.re, xa0.im + pa0.im);
+        oa[2 * m + j0] = pa0;
+        if (two) {
+          os[j0 + 1] = mk<S>(xs1.re + ps1.re, xs1.im + ps1.im);
+          os[2 * m + j0 + 1] = ps1;
+          oa[j0 + 1] = mk<S>(xa1.re + pa1.re, xa1.im + pa1.im);
+          oa[2 * m + j0 + 1] = pa1;
         }
       }
     }
-    __syncthreads();
-    for (int it = threadIdx.x; it < items; it += blockDim.x) {
-      const int rr = it / ngrp, g = it - rr * ngrp;
-      if (rr >= nr) continue;
-      const int j0 = g * 2;
-      const bool two = j0 + 1 < m;
-      const cplx<S>* rs = Rs + rr * RS;
-      const cplx<S>* ra = Rs + (kUpdRows + rr) * RS;
-      cplx<S> xs0 = mk<S>(0, 0), xs1 = mk<S>(0, 0), ps0 = mk<S>(0, 0), ps1 = mk<S>(0, 0);
-      cplx<S> xa0 = mk<S>(0, 0), xa1 = mk<S>(0, 0), pa0 = mk<S>(0, 0), pa1 = mk<S>(0, 0);
-      for (int i = 0; i < m; ++i) {  // the X block contributes to X only
-        const cplx<S> si = rs[i], ai = ra[i];
-        const cplx<S>* crow = Cs + i * m + j0;
-        const cplx<S> c0 = crow[0], c1 = two ? crow[1] : mk<S>(0, 0);
-        cfma(xs0, si, c0);
-        cfma(xa0, ai, c0);
-        cfma(xs1, si, c1);
-        cfma(xa1, ai, c1);
-      }
-      for (int i = m; i < nb; ++i) {  // W and P contribute to X and to the new P
-        const cplx<S> si = rs[i], ai = ra[i];
-        const cplx<S>* crow = Cs + i * m + j0;
-        const cplx<S> c0 = crow[0], c1 = two ? crow[1] : mk<S>(0, 0);
-        cfma(ps0, si, c0);
-        cfma(pa0, ai, c0);
-        cfma(ps1, si, c1);
-        cfma(pa1, ai, c1);
-      }
-      cplx<S>* os = Sb + (r0 + rr) * ld;
-      cplx<S>* oa = ASb + (r0 + rr) * ld;
-      os[j0] = mk<S>(xs0.re + ps0.re, xs0.im + ps0.im);
-      os[2 * m + j0] = ps0;
-      oa[j0] = mk<S>(xa0.re + pa0.re, xa0.im + pa0.im);
-      oa[2 * m + j0] = pa0;
-      if (two) {
-        os[j0 + 1] = mk<S>(xs1.re + ps1.re, xs1.im + ps1.im);
-        os[2 * m + j0 + 1] = ps1;
-        oa[j0 + 1] = mk<S>(xa1.re + pa1.re, xa1.im + pa1.im);
-        oa[2 * m + j0 + 1] = pa1;
-      }
-    }
+    __syncthreads();  // this stage's rows (and Cs) are read before the next copies into it
   }
 }
 
@@ -713,8 +751,11 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
   // between iterations (for kernel-level profilers, which do not replay kernels inside conditional graph
   // bodies); the default runs the whole solve as one graph launch
   const bool stream_mode = std::getenv("WTB_SOLVER_STREAM") != nullptr && !sg;
-  const size_t upd_smem = (size_t)(((nb * m + 1) & ~1) + 2 * kUpdRows * (nb + 2)) * sizeof(cplx<S>);
-  const int upd_grid = std::max(1, std::min(152 * 8, (nrow + kUpdRows - 1) / kUpdRows));
+  const size_t upd_smem =
+      (size_t)(((nb * m + 1) & ~1) + upd_stages<S>() * 2 * kUpdRows * (nb + 2)) * sizeof(cplx<S>);
+  // FP32: a few tiles per CTA, so that the copies of the next overlap the combination of the current one
+  const int upd_grid =
+      std::max(1, std::min(upd_stages<S>() == 2 ? 152 * 3 : 152 * 8, (nrow + kUpdRows - 1) / kUpdRows));
   const unsigned cp_grid = (unsigned)std::max(1, std::min(152 * 4, (int)(((long)nrow * m + 255) / 256)));
 
   // the pieces of one iteration, as stream launches (captured below)
