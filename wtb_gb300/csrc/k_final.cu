@@ -189,6 +189,27 @@ __device__ __forceinline__ void rr_pair(int N, int t, int i, int* p, int* q) {
 
 constexpr int kRRL = kRRMax + 1;
 
+// FP64 1/sqrt(x) and 1/d for arguments inside the FP32 normal range, without the FP64 division and square-root
+// sequences (the FP64 pipe runs at 1/64 of the FP32 rate here): an FP32 estimate, then two Newton-Raphson steps
+// in FP64, y <- y (3 - x y^2) / 2 and z <- z (2 - d z); the error falls quadratically from the estimate's 2^-23
+// to a few FP64 ulp (checked on the host from estimates up to 4 FP32 ulp off: <= 4.1e-16 relative).
+__device__ __forceinline__ double rsqrt_nr(double x) {
+  double y = (double)rsqrtf((float)x);
+  y = y * fma(-0.5 * x, y * y, 1.5);
+  y = y * fma(-0.5 * x, y * y, 1.5);
+  return y;
+}
+__device__ __forceinline__ double rcp_nr(double d) {
+  double z = (double)(1.0f / (float)d);
+  z = z * fma(-d, z, 2.0);
+  z = z * fma(-d, z, 2.0);
+  return z;
+}
+__device__ __forceinline__ bool in_f32_range(double x) {  // |x| (nonzero) with room for a square in FP32
+  const double a = fabs(x);
+  return a > 1e-18 && a < 1e18;
+}
+
 // Cyclic Jacobi on the r x r Hermitian A (shared, rows of kRRL), accumulating V <- V U: N (r rounded up to even)
 // players, N - 1 rounds of N / 2 disjoint pairs per sweep; a pair with the padding player is skipped.  Rotation
 // of pair (p, q): with A_pq = g e (g = |A_pq|, |e| = 1) and zeta = (A_qq - A_pp) / (2 g),
@@ -245,11 +266,33 @@ __device__ void jacobi_cta(cplx<T> (*A)[kRRL], cplx<T> (*V)[kRRL], int r, T tol2
           // vectors by less than that and the eigenvalues by its square times the gap
           if (g > (sizeof(T) == 4 ? (T)1e-30 : (T)1e-300) && g > skip_rel * fabs(A[q][q].re - A[p][p].re)) {
             *s_any = 1;  // benign race: every writer stores 1
-            ee = mk<T>(apq.re / g, apq.im / g);
-            const T zeta = (A[q][q].re - A[p][p].re) / (2 * g);
-            const T tt = (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
-            c = (T)1 / sqrt((T)1 + tt * tt);
-            sn = tt * c;
+            const T dqp = A[q][q].re - A[p][p].re;
+            bool done = false;
+            if constexpr (sizeof(T) == 8) {
+              // the same rotation from Newton-refined reciprocals and reciprocal square roots (the inputs in
+              // the FP32 range, else the division and square-root route below)
+              const double g2 = apq.re * apq.re + apq.im * apq.im;
+              if (in_f32_range(g)) {
+                const double rg = rsqrt_nr(g2);  // 1 / g
+                const double zeta = 0.5 * dqp * rg;
+                if (fabs(zeta) < 1e17) {
+                  const double z2 = fma(zeta, zeta, 1.0);
+                  const double h = z2 * rsqrt_nr(z2);  // sqrt(1 + zeta^2)
+                  const double tt = (zeta >= 0 ? 1.0 : -1.0) * rcp_nr(fabs(zeta) + h);
+                  ee = mk<T>(apq.re * rg, apq.im * rg);
+                  c = rsqrt_nr(fma(tt, tt, 1.0));
+                  sn = tt * c;
+                  done = true;
+                }
+              }
+            }
+            if (!done) {
+              ee = mk<T>(apq.re / g, apq.im / g);
+              const T zeta = dqp / (2 * g);
+              const T tt = (zeta >= 0 ? (T)1 : (T)-1) / (fabs(zeta) + sqrt((T)1 + zeta * zeta));
+              c = (T)1 / sqrt((T)1 + tt * tt);
+              sn = tt * c;
+            }
           }
         }
         rot_c[tid] = c;
@@ -309,7 +352,7 @@ __global__ void __launch_bounds__(256) small_rr_kernel(const zd* __restrict__ Mg
   __shared__ double dinv[kRRMax], rinv[kRRMax], rot_c[kRRMax / 2], rot_s[kRRMax / 2], offs[8], dias[8];
   __shared__ zd rot_e[kRRMax / 2];
   __shared__ int perm[kRRMax], order[kRRMax];
-  __shared__ int s_r, s_done, s_near, s_any, s_sweep;
+  __shared__ int s_done, s_near, s_any, s_sweep;
   const int sys = blockIdx.x;
   if (bm_frozen(bm, sys)) return;
   Mg += (size_t)sys * mat_stride;
@@ -433,8 +476,7 @@ __global__ void __launch_bounds__(256) small_rr_kernel(const zd* __restrict__ Mg
     ++r;
     __syncthreads();
   }
-  if (tid == 0) s_r = r;
-  __syncthreads();
+  __syncthreads();  // the last (dropped) columns' reads of W are done before it is overwritten
   // compact upper-triangular Rk (r x r) into W, then its inverse by back substitution, one thread per column
   for (int e = tid; e < r * r; e += nt) {
     const int k = e / r, l = e - k * r;
