@@ -299,7 +299,7 @@ __global__ void __launch_bounds__(256) orth_update_kernel(const cplx<S>* __restr
                                                           int ld, int m, const zd* __restrict__ T,
                                                           cplx<S>* __restrict__ W, cplx<S>* __restrict__ P,
                                                           cplx<S>* __restrict__ AP, int nrow, BatchMap bm,
-                                                          long t_stride) {
+                                                          long t_stride, const int* __restrict__ active) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int RS = m + 1;                                // padded row of the staged blocks
   cplx<S>* Tw = reinterpret_cast<cplx<S>*>(smem_raw);  // [m][m]
@@ -346,7 +346,8 @@ __global__ void __launch_bounds__(256) orth_update_kernel(const cplx<S>* __restr
       cplx<S>* ow = W + r * ld + j;
       cplx<S>* op = P + r * ld + j;
       cplx<S>* oa = AP + r * ld + j;
-      *ow = mk<S>(ow->re - aw.re, ow->im - aw.im);
+      // active: the search direction of a locked column is zero (the preconditioner's mask)
+      *ow = active && !active[32 * sys + j] ? mk<S>(0, 0) : mk<S>(ow->re - aw.re, ow->im - aw.im);
       *op = mk<S>(op->re - ap.re, op->im - ap.im);
       *oa = mk<S>(oa->re - aa.re, oa->im - aa.im);
     }
@@ -359,7 +360,8 @@ __global__ void __launch_bounds__(256) residual_kernel(const cplx<S>* __restrict
                                                        const cplx<S>* __restrict__ X, int ldx,
                                                        const double* __restrict__ theta, int m, int nrow,
                                                        cplx<S>* __restrict__ R, int ldr, double* __restrict__ partial,
-                                                       int rows_per_part, BatchMap bm, long theta_stride) {
+                                                       int rows_per_part, BatchMap bm, long theta_stride,
+                                                       const double* __restrict__ diag) {
   __shared__ double red[8][32];
   const int tid = threadIdx.x;
   const int j = tid % 32, rr = tid / 32;  // 8 rows per step, up to 32 columns; one CTA per reduction part
@@ -371,10 +373,20 @@ __global__ void __launch_bounds__(256) residual_kernel(const cplx<S>* __restrict
   S acc = 0;
   if (j < m) {
     const S th = (S)theta[(size_t)sys * theta_stride + j];
+    // diag: store the preconditioned residual |diag - theta|^-1 (AX - X theta), the denominator floored at
+    // 1e-2 max(|theta|, 1e-3) (the diagonal preconditioner of the iteration); the norms are of the residual itself
+    const S fl = (S)1e-2 * (fabs(th) > (S)1e-3 ? fabs(th) : (S)1e-3);
     for (long r = r_begin + rr; r < r_end; r += 8) {
       const cplx<S> ax = AX[r * ldax + j], x = X[r * ldx + j];
       const cplx<S> v = mk<S>(ax.re - th * x.re, ax.im - th * x.im);
-      R[r * ldr + j] = v;
+      if (diag) {
+        S d = (S)diag[r] - th;
+        if (fabs(d) < fl) d = fl;
+        const S inv = (S)1 / fabs(d);
+        R[r * ldr + j] = mk<S>(v.re * inv, v.im * inv);
+      } else {
+        R[r * ldr + j] = v;
+      }
       acc += v.re * v.re + v.im * v.im;
     }
   }
@@ -385,29 +397,6 @@ __global__ void __launch_bounds__(256) residual_kernel(const cplx<S>* __restrict
     for (int i = 0; i < 8; ++i) s += red[i][j];
     partial[(size_t)blockIdx.x * 32 + j] = s;
   }
-}
-
-template <class S>
-__global__ void precond_kernel(cplx<S>* __restrict__ R, int ldr, const double* __restrict__ diag,
-                               const double* __restrict__ theta, const int* __restrict__ active, int m, int nrow,
-                               BatchMap bm, long theta_stride) {
-  const long e = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= (long)nrow * m) return;
-  const long r = e / m;
-  const int j = (int)(e % m);
-  const int sys = bm_sys_of_row(bm, r);
-  if (bm_frozen(bm, sys)) return;
-  cplx<S>& v = R[r * ldr + j];
-  if (!active[32 * sys + j]) {
-    v = mk<S>(0, 0);
-    return;
-  }
-  const S th = (S)theta[(size_t)sys * theta_stride + j];
-  S d = (S)diag[r] - th;
-  const S fl = (S)1e-2 * (fabs(th) > (S)1e-3 ? fabs(th) : (S)1e-3);
-  if (fabs(d) < fl) d = fl;
-  const S inv = (S)1 / fabs(d);
-  v = mk<S>(v.re * inv, v.im * inv);
 }
 
 template <class Sa, class Sb>
@@ -987,14 +976,15 @@ cudaError_t launch_update(const cplx<S>* Sx, int lds, int nin, const zd* C, int 
 
 template <class S>
 cudaError_t launch_orth_update(const cplx<S>* X, const cplx<S>* AX, int ld, int m, const zd* T, cplx<S>* W,
-                               cplx<S>* P, cplx<S>* AP, int nrow, cudaStream_t s, const BatchMap& bm, long t_stride) {
+                               cplx<S>* P, cplx<S>* AP, int nrow, cudaStream_t s, const BatchMap& bm, long t_stride,
+                               const int* active) {
   if (m < 1 || m > 32) return cudaErrorInvalidValue;
   const size_t smem = (size_t)(2 * m * m + 2 * kTileRows * (m + 1)) * sizeof(cplx<S>);
   cudaError_t e = raise_smem_limit(reinterpret_cast<const void*>(orth_update_kernel<S>), smem);
   if (e != cudaSuccess) return e;
   long nblk = ((long)nrow + kTileRows - 1) / kTileRows;
   if (nblk > 152 * 16) nblk = 152 * 16;
-  orth_update_kernel<S><<<(unsigned)nblk, 256, smem, s>>>(X, AX, ld, m, T, W, P, AP, nrow, bm, t_stride);
+  orth_update_kernel<S><<<(unsigned)nblk, 256, smem, s>>>(X, AX, ld, m, T, W, P, AP, nrow, bm, t_stride, active);
   ++g_launch_count;
   return cudaGetLastError();
 }
@@ -1002,24 +992,15 @@ cudaError_t launch_orth_update(const cplx<S>* X, const cplx<S>* AX, int ld, int 
 template <class S>
 cudaError_t launch_residual(const cplx<S>* AX, int ldax, const cplx<S>* X, int ldx, const double* theta, int m,
                             int nrow, cplx<S>* R, int ldr, double* partial, int npart, double* norms2, cudaStream_t s,
-                            const BatchMap& bm, long theta_stride) {
+                            const BatchMap& bm, long theta_stride, const double* diag) {
   if (m > 32) return cudaErrorInvalidValue;
   if (bm.parts) npart = bm.nparts;
   const int rpp = (nrow + npart - 1) / npart;
-  residual_kernel<S><<<npart, 256, 0, s>>>(AX, ldax, X, ldx, theta, m, nrow, R, ldr, partial, rpp, bm, theta_stride);
+  residual_kernel<S><<<npart, 256, 0, s>>>(AX, ldax, X, ldx, theta, m, nrow, R, ldr, partial, rpp, bm, theta_stride,
+                                           diag);
   ++g_launch_count;
   // partial is [part][32]; summed column-wise per system
   sum_partials_kernel<<<dim3(1, bm.nsys), 256, 0, s>>>(partial, npart, 32, norms2, bm, 32);
-  ++g_launch_count;
-  return cudaGetLastError();
-}
-
-template <class S>
-cudaError_t launch_precond(cplx<S>* R, int ldr, const double* diag, const double* theta, const int* active, int m,
-                           int nrow, cudaStream_t s, const BatchMap& bm, long theta_stride) {
-  const long n = (long)nrow * m;
-  precond_kernel<S><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(R, ldr, diag, theta, active, m, nrow, bm,
-                                                                theta_stride);
   ++g_launch_count;
   return cudaGetLastError();
 }
@@ -1134,12 +1115,11 @@ cudaError_t launch_init_guess(cplx<S>* X, int ldx, int nrow, int m, const int* i
   template cudaError_t launch_update<S>(const cplx<S>*, int, int, const zd*, int, int, int, cplx<S>*, int, double, \
                                         double, cudaStream_t, const BatchMap&, long);                             \
   template cudaError_t launch_orth_update<S>(const cplx<S>*, const cplx<S>*, int, int, const zd*, cplx<S>*,        \
-                                             cplx<S>*, cplx<S>*, int, cudaStream_t, const BatchMap&, long);       \
+                                             cplx<S>*, cplx<S>*, int, cudaStream_t, const BatchMap&, long,        \
+                                             const int*);                                                         \
   template cudaError_t launch_residual<S>(const cplx<S>*, int, const cplx<S>*, int, const double*, int, int,       \
                                           cplx<S>*, int, double*, int, double*, cudaStream_t, const BatchMap&,     \
-                                          long);                                                                   \
-  template cudaError_t launch_precond<S>(cplx<S>*, int, const double*, const double*, const int*, int, int,        \
-                                         cudaStream_t, const BatchMap&, long);                                    \
+                                          long, const double*);                                                    \
   template cudaError_t launch_copy_cols<S>(const cplx<S>*, int, cplx<S>*, int, int, int, cudaStream_t);           \
   template cudaError_t launch_init_guess<S>(cplx<S>*, int, int, int, const int*, unsigned, cudaStream_t,           \
                                             const BatchMap&, long);

@@ -770,7 +770,8 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
     return WTB_OK;
   };
   auto check_and_decide = [&](cudaGraphConditionalHandle h) -> int {
-    CK(launch_residual<S>(AX, ld, X, ld, th_dev, m, nrow, W, ld, partial, npart, norms2, s, bm, nb));
+    // W <- the preconditioned residual (the inactive columns are zeroed by the next iteration's projections)
+    CK(launch_residual<S>(AX, ld, X, ld, th_dev, m, nrow, W, ld, partial, npart, norms2, s, bm, nb, diag));
     lob_control_kernel<<<nsys, 32, 0, s>>>(ctl, norms2, th_dev, nb, m, nev, maxit, reduced ? 1 : 0, active, st, frozen,
                                            counter, nsys, h, stream_mode ? 0 : 1, monitor ? 1 : 0);
     ++g_launch_count;
@@ -789,11 +790,10 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
     return check_and_decide(h);
   };
   auto iteration = [&](cudaGraphConditionalHandle h) -> int {
-    CK(launch_precond<S>(W, ld, diag, th_dev, active, m, nrow, s, bm, nb));
     // W <- W - X (X^H W);  P <- P - X (X^H P), AP <- AP - AX (X^H P): one Gram X^H [W P] (W and P are adjacent
     // column blocks) and one pass for the three projections; P and AP do not depend on W's image
     CK(launch_gram<S>(X, ld, m, W, ld, 2 * m, nrow, sm.T, partial, npart, s, bm, nn));
-    CK(launch_orth_update<S>(X, AX, ld, m, sm.T, W, P, AP, nrow, s, bm, nn));
+    CK(launch_orth_update<S>(X, AX, ld, m, sm.T, W, P, AP, nrow, s, bm, nn, active));
     CK(op.apply(W, ld, 0, m, AW, ld, s));
     int r = rr_and_update();
     if (r) return r;

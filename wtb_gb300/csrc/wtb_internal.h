@@ -225,24 +225,23 @@ cudaError_t launch_small_rr(const zd* M, const zd* G, int n, int m, double drop,
 // Out = X C with FP32 X (nin <= 32 columns) and FP64 C, to FP64 accuracy in FP32 instructions
 cudaError_t launch_update_dot2(const zf* X, int ldx, int nin, const zd* C, int ldc, int nout, int nrow, zd* Out,
                                int ldo, cudaStream_t s, const BatchMap& bm, long c_stride);
-// W -= X T[:, 0:m], P -= X T[:, m:2m], AP -= AX T[:, m:2m] (T: m x 2m FP64, per system at t_stride)
+// W -= X T[:, 0:m], P -= X T[:, m:2m], AP -= AX T[:, m:2m] (T: m x 2m FP64, per system at t_stride); with active
+// (flags of system q at active + 32 q) the W columns of inactive vectors are set to zero
 template <class S>
 cudaError_t launch_orth_update(const cplx<S>* X, const cplx<S>* AX, int ld, int m, const zd* T, cplx<S>* W,
                                cplx<S>* P, cplx<S>* AP, int nrow, cudaStream_t s, const BatchMap& bm = BatchMap(),
-                               long t_stride = 0);
+                               long t_stride = 0, const int* active = nullptr);
 template <class S>
 cudaError_t launch_update(const cplx<S>* Sx, int lds, int nin, const zd* C, int ldc, int nout, int nrow,
                           cplx<S>* Out, int ldo, double alpha, double beta, cudaStream_t s,
                           const BatchMap& bm = BatchMap(), long c_stride = 0);
-// norms2 of system q at norms2 + 32 q
+// norms2 of system q at norms2 + 32 q (of AX - X theta); with diag, R receives the preconditioned residual
+// |diag - theta|^-1 (AX - X theta), the denominator floored at 1e-2 max(|theta|, 1e-3)
 template <class S>
 cudaError_t launch_residual(const cplx<S>* AX, int ldax, const cplx<S>* X, int ldx, const double* theta, int m,
                             int nrow, cplx<S>* R, int ldr, double* partial, int npart, double* norms2,
-                            cudaStream_t s, const BatchMap& bm = BatchMap(), long theta_stride = 0);
-// active flags of system q at active + 32 q
-template <class S>
-cudaError_t launch_precond(cplx<S>* R, int ldr, const double* diag, const double* theta, const int* active, int m,
-                           int nrow, cudaStream_t s, const BatchMap& bm = BatchMap(), long theta_stride = 0);
+                            cudaStream_t s, const BatchMap& bm = BatchMap(), long theta_stride = 0,
+                            const double* diag = nullptr);
 template <class S>
 cudaError_t launch_copy_cols(const cplx<S>* A, int lda, cplx<S>* B, int ldb, int ncol, int nrow, cudaStream_t s);
 template <class Sa, class Sb>
