@@ -74,9 +74,21 @@ __device__ __forceinline__ void df_mac1(float& ah, float& al, float xh, float xl
 }
 __device__ __forceinline__ double df_val(float h, float l) { return (double)h + (double)l; }
 
-// H(R) / 1 split into double-float parts once per band solve: (re hi, re lo, im hi, im lo)
-__global__ void hr_split_kernel(const zd* __restrict__ hr, long n, float4* __restrict__ out) {
+// H(R) / 1 split into double-float parts once per band solve: (re hi, re lo, im hi, im lo); and the k-independent
+// factors of the phases, R's Cartesian components and 1 / ndegen (rtab[2r] = (Rx, Ry), rtab[2r + 1] = (Rz, 1 / ndegen),
+// the same expressions as the per-k route)
+__global__ void hr_split_kernel(const zd* __restrict__ hr, long n, float4* __restrict__ out,
+                                const int* __restrict__ rvec, const int* __restrict__ ndegen, int nR,
+                                const double* __restrict__ rlat, double2* __restrict__ rtab) {
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nR) {
+    double lat[9];
+#pragma unroll
+    for (int a = 0; a < 9; ++a) lat[a] = rlat[a];
+    const int r1 = rvec[i], r2 = rvec[nR + i], r3 = rvec[2 * nR + i];
+    rtab[2 * i] = make_double2(rcart(r1, r2, r3, lat, 0), rcart(r1, r2, r3, lat, 1));
+    rtab[2 * i + 1] = make_double2(rcart(r1, r2, r3, lat, 2), 1.0 / (double)ndegen[i]);
+  }
   if (i >= n) return;
   const zd h = hr[i];
   float rh, rl, ih, il;
@@ -131,10 +143,19 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
   __syncthreads();
   const double kx = kpt[3 * k], ky = kpt[3 * k + 1], kz = kpt[3 * k + 2];
   for (int r = tid; r < nR; r += blockDim.x) {
-    const double phi = phase_f32(rvec, nR, r, rl, kx, ky, kz);
+    double phi, inv;
+    if constexpr (kMixed) {
+      // R's components and 1 / ndegen from the table after the split H(R) (FP64 instructions are the scarce ones)
+      const double2* rtab = reinterpret_cast<const double2*>(hr_df + (size_t)nR * w * w);
+      const double2 a = rtab[2 * r], b = rtab[2 * r + 1];
+      phi = (double)__double2float_rn(__dadd_rn(__dadd_rn(__dmul_rn(kx, a.x), __dmul_rn(ky, a.y)), __dmul_rn(kz, b.x)));
+      inv = b.y;
+    } else {
+      phi = phase_f32(rvec, nR, r, rl, kx, ky, kz);
+      inv = 1.0 / (double)ndegen[r];
+    }
     double sn, cs;
     sincos(phi, &sn, &cs);
-    const double inv = 1.0 / (double)ndegen[r];
     eph[r] = mk<double>(cs * inv, sn * inv);
     if constexpr (kMixed) {
       float ch, cl, sh, sl;
@@ -213,23 +234,28 @@ __global__ void __launch_bounds__(kHkThreads) hk_eig_kernel(const zd* __restrict
       HU[j * n + i] = mk<double>(df_val(rh, rlo), df_val(ih, il));
     }
     __syncthreads();
-    const int lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
-    for (int j = warp; j < n; j += nwarp) {
+    // vector j's norm and quotient on thread j, its components in order (one FP64 square root and two divisions
+    // per vector, no warp reductions: the FP64 pipe is the scarce one), then U = U32 / |u| on every thread;
+    // e (n doubles) is free on this route
+    for (int j = tid; j < n; j += blockDim.x) {
       double nn = 0.0, rq = 0.0;
-      for (int i = lane; i < n; i += 32) {
+      for (int i = 0; i < n; ++i) {
         const zf u = U32[j * n + i];
-        const zd ud = mk<double>((double)u.re, (double)u.im), h = HU[j * n + i];
-        nn += ud.re * ud.re + ud.im * ud.im;
-        rq += ud.re * h.re + ud.im * h.im;  // Re(conj(u_i) (H u)_i)
+        const double ur = (double)u.re, ui = (double)u.im;
+        const zd h = HU[j * n + i];
+        nn = fma(ur, ur, nn);
+        nn = fma(ui, ui, nn);
+        rq = fma(ur, h.re, rq);  // Re(conj(u_i) (H u)_i)
+        rq = fma(ui, h.im, rq);
       }
-      nn = warp_allsum(nn);
-      rq = warp_allsum(rq);
-      const double inv = nn > 0.0 ? 1.0 / sqrt(nn) : 0.0;
-      if (lane == 0) lam[j] = nn > 0.0 ? rq / nn : (double)lam32[j];
-      for (int i = lane; i < n; i += 32) {
-        const zf u = U32[j * n + i];
-        U[j * n + i] = mk<double>((double)u.re * inv, (double)u.im * inv);
-      }
+      lam[j] = nn > 0.0 ? rq / nn : (double)lam32[j];
+      e[j] = nn > 0.0 ? 1.0 / sqrt(nn) : 0.0;
+    }
+    __syncthreads();
+    for (int q = tid; q < n * n; q += blockDim.x) {
+      const zf u = U32[q];
+      const double inv = e[q / n];
+      U[q] = mk<double>((double)u.re * inv, (double)u.im * inv);
     }
     __syncthreads();
   } else {
@@ -560,7 +586,9 @@ cudaError_t launch_hk_eig(const zd* hr, const int* rvec, const int* ndegen, int 
   if (e != cudaSuccess) return e;
   if (mixed) {
     const long nh = (long)nR * w * w;
-    hr_split_kernel<<<(unsigned)((nh + 255) / 256), 256, 0, s>>>(hr, nh, hr_df);
+    // the split H(R), then the per-R table (2 nR float4 = nR (Rx, Ry, Rz, 1 / ndegen) in FP64)
+    hr_split_kernel<<<(unsigned)((nh + 255) / 256), 256, 0, s>>>(hr, nh, hr_df, rvec, ndegen, nR, rlat_rm,
+                                                                 reinterpret_cast<double2*>(hr_df + nh));
     ++g_launch_count;
     hk_eig_kernel<true><<<nk, kHkThreads, smem, s>>>(hr, rvec, ndegen, nR, w, rlat_rm, efermi, scs, kpt, nk, nv, nc,
                                                      eig_all, vec_all, eig_win, vec_win, nocp, st, hr_df);

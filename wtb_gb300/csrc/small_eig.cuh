@@ -371,7 +371,7 @@ __device__ void tridiag_eigvecs_cta(const cplx<S>* A, int lda, int n, int nwant,
       h ^= h >> 15;
       h *= 0x2c1b3c6du;
       h ^= h >> 12;
-      zk[i] = (S)((double)(h & 0xffffffu) / 8388608.0 - 1.0);
+      zk[i] = (S)(h & 0xffffffu) * (S)(1.0 / 8388608.0) - (S)1;  // exact in FP32 too (24-bit integer, 2^-23)
     }
     for (int pass = 0; pass < kPasses; ++pass) {
       // L y = b (in place) and y /= D; L^T x = y (in place) with the largest magnitude on the way

@@ -241,7 +241,7 @@ int enqueue_bands(wtb_ctx* c, bool mixed = false) {
                     nk, nv, nc, c->ws.get<double>("eig_all", 0, &err), c->ws.get<zd>("vec_all", 0, &err),
                     nb > 0 ? c->ws.get<double>("eig_win", 0, &err) : nullptr,
                     nb > 0 ? c->ws.get<zd>("vec_win", 0, &err) : nullptr, c->ws.get<int>("nocp", 0, &err), c->st, c->s,
-                    mixed, mixed ? c->ws.get<float4>("hr_df", (size_t)c->nR * w * w, &err) : nullptr));
+                    mixed, mixed ? c->ws.get<float4>("hr_df", (size_t)c->nR * (w * w + 2), &err) : nullptr));
   CKC(err);
   return WTB_OK;
 }

@@ -108,7 +108,8 @@ struct CoulParams {
 // ----------------------------------------------------------------------------- kernels (launchers)
 // H(k) + Hermitian eigensolve + gauge + band window.  Returns 0 or a launch error.
 // mixed: FP32 eigensolve + Rayleigh quotients against H(k) summed in double-float (energies FP64-accurate,
-// vectors FP32-accurate); hr_df: scratch of nR w^2 float4 for the split H(R) (mixed only)
+// vectors FP32-accurate); hr_df: scratch of nR (w^2 + 2) float4 for the split H(R) and the
+// per-R phase factors (mixed only)
 cudaError_t launch_hk_eig(const zd* hr, const int* rvec, const int* ndegen, int nR, int w,
                           const double* rlat_rm, double efermi, double scs, const double* kpt, int nk,
                           int nv, int nc, double* eig_all, zd* vec_all, double* eig_win, zd* vec_win,
