@@ -206,40 +206,21 @@ __global__ void __launch_bounds__(256) gram_pair_partial_kernel(const cplx<S>* _
 }
 
 // out[e] = sum over b of partial[b][e] over the parts of system blockIdx.y (out at a stride of out_stride per
-// system): a CTA owns 32 consecutive e; its 8 warps take every 8th part (lane = e, so reads coalesce), then the
-// 8 warp sums are added in a fixed order.
+// system): a CTA owns 32 consecutive e (sum_parts_cta).
 // With out2: blockIdx.z = 1 sums the second set of partials (npart parts further on) into out2.
 __global__ void __launch_bounds__(256) sum_partials_kernel(const double* __restrict__ partial, int npart, int n,
                                                            double* __restrict__ out, BatchMap bm, long out_stride,
                                                            double* __restrict__ out2 = nullptr) {
   __shared__ double red[8][33];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int e = blockIdx.x * 32 + lane;
+  const int e = blockIdx.x * 32 + (threadIdx.x & 31);
   const int sys = blockIdx.y;
   if (blockIdx.z == 1) {
     partial += (size_t)npart * n;
     out = out2;
   }
   if (bm_frozen(bm, sys)) return;
-  int b0 = 0, nbp = npart;
-  if (bm.sys_parts) {
-    b0 = bm.sys_parts[sys].x;
-    nbp = bm.sys_parts[sys].y;
-  }
-  out += (size_t)sys * out_stride;
-  double s = 0.0;
-  // unrolled so the loads of eight parts are in flight together; the additions keep the part order
-  if (e < n) {
-#pragma unroll 8
-    for (int b = warp; b < nbp; b += 8) s += partial[(size_t)(b0 + b) * n + e];
-  }
-  red[warp][lane] = s;
-  __syncthreads();
-  if (warp == 0 && e < n) {
-    double t = 0.0;
-    for (int w = 0; w < 8; ++w) t += red[w][lane];
-    out[e] = t;
-  }
+  const double t = sum_parts_cta(partial, npart, n, e, sys, bm, red);
+  if (threadIdx.x < 32 && e < n) out[(size_t)sys * out_stride + e] = t;
 }
 
 // ----------------------------------------------------------------------------- update: Out = beta Out + S C
@@ -992,7 +973,7 @@ cudaError_t launch_orth_update(const cplx<S>* X, const cplx<S>* AX, int ld, int 
 template <class S>
 cudaError_t launch_residual(const cplx<S>* AX, int ldax, const cplx<S>* X, int ldx, const double* theta, int m,
                             int nrow, cplx<S>* R, int ldr, double* partial, int npart, double* norms2, cudaStream_t s,
-                            const BatchMap& bm, long theta_stride, const double* diag) {
+                            const BatchMap& bm, long theta_stride, const double* diag, bool sum_parts) {
   if (m > 32) return cudaErrorInvalidValue;
   if (bm.parts) npart = bm.nparts;
   const int rpp = (nrow + npart - 1) / npart;
@@ -1000,8 +981,10 @@ cudaError_t launch_residual(const cplx<S>* AX, int ldax, const cplx<S>* X, int l
                                            diag);
   ++g_launch_count;
   // partial is [part][32]; summed column-wise per system
-  sum_partials_kernel<<<dim3(1, bm.nsys), 256, 0, s>>>(partial, npart, 32, norms2, bm, 32);
-  ++g_launch_count;
+  if (sum_parts) {
+    sum_partials_kernel<<<dim3(1, bm.nsys), 256, 0, s>>>(partial, npart, 32, norms2, bm, 32);
+    ++g_launch_count;
+  }
   return cudaGetLastError();
 }
 
@@ -1119,7 +1102,7 @@ cudaError_t launch_init_guess(cplx<S>* X, int ldx, int nrow, int m, const int* i
                                              const int*);                                                         \
   template cudaError_t launch_residual<S>(const cplx<S>*, int, const cplx<S>*, int, const double*, int, int,       \
                                           cplx<S>*, int, double*, int, double*, cudaStream_t, const BatchMap&,     \
-                                          long, const double*);                                                    \
+                                          long, const double*, bool);                                              \
   template cudaError_t launch_copy_cols<S>(const cplx<S>*, int, cplx<S>*, int, int, int, cudaStream_t);           \
   template cudaError_t launch_init_guess<S>(cplx<S>*, int, int, int, const int*, unsigned, cudaStream_t,           \
                                             const BatchMap&, long);

@@ -397,13 +397,25 @@ __global__ void lob_ctl_reset_kernel(LobCtl* ctl, double tol, int keep_total, in
 // to finish (a completion counter) sets the loop's condition: another pass while any system is running;
 // counter[1] holds the same answer for the host-driven loop.
 // Monitor lines follow the reference's MyEPSMonitor (src/module_slepc_solver.F90:101-116).
-__global__ void lob_control_kernel(LobCtl* ctl, const double* __restrict__ norms2, const double* __restrict__ theta,
-                                   int theta_stride, int m, int nev, int maxit, int reduced, int* __restrict__ active,
-                                   const DevStatus* __restrict__ st, int* __restrict__ frozen, int* counter, int nsys,
-                                   cudaGraphConditionalHandle h, int in_graph, int monitor) {
+// One CTA of 256 threads per system: first the residual norms of system q from the residual kernel's parts
+// ([npart][32] in partial, written to norms2), then warp 0 decides.
+__global__ void __launch_bounds__(256) lob_control_kernel(LobCtl* ctl, double* __restrict__ norms2,
+                                                          const double* __restrict__ partial, int npart, BatchMap bm,
+                                                          const double* __restrict__ theta, int theta_stride, int m,
+                                                          int nev, int maxit, int reduced, int* __restrict__ active,
+                                                          const DevStatus* __restrict__ st, int* __restrict__ frozen,
+                                                          int* counter, int nsys, cudaGraphConditionalHandle h,
+                                                          int in_graph, int monitor) {
+  __shared__ double red[8][33];
   const int lane = threadIdx.x;
   const int q = blockIdx.x;
   LobCtl* c = ctl + q;
+  if (!frozen[q]) {  // uniform over the CTA
+    const double t = sum_parts_cta(partial, npart, 32, lane & 31, q, bm, red);
+    if (lane < 32) norms2[32 * q + lane] = t;
+  }
+  if (lane >= 32) return;
+  __syncwarp();
   if (!frozen[q]) {
     norms2 += 32 * q;
     theta += (size_t)q * theta_stride;
@@ -759,21 +771,25 @@ int lobpcg_solve_batch(Operator<S>& op, const double* diag, const BatchLayout& L
   const unsigned cp_grid = (unsigned)std::max(1, std::min(152 * 4, (int)(((long)nrow * m + 255) / 256)));
 
   // the pieces of one iteration, as stream launches (captured below)
+  // the iteration's Ritz values go straight to th_dev (the final step's to sm.theta)
+  Small smi = sm;
+  smi.theta = th_dev;
   auto rr_and_update = [&]() -> int {
-    int r = rayleigh_ritz<S>(Sb, ASb, ld, nb, m, nrow, tau, sm, partial, npart, st, s, msg, false, bm, nn, nb);
+    int r = rayleigh_ritz<S>(Sb, ASb, ld, nb, m, nrow, tau, smi, partial, npart, st, s, msg, false, bm, nn, nb);
     if (r) return r;
     CK(raise_smem_limit(reinterpret_cast<const void*>(lob_update_kernel<S>), upd_smem));
     lob_update_kernel<S><<<upd_grid, 256, upd_smem, s>>>(Sb, ASb, ld, m, sm.C, nrow, bm, nn);
     ++g_launch_count;
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(th_dev, sm.theta, sizeof(double) * nsys * nb, cudaMemcpyDeviceToDevice, s));
     return WTB_OK;
   };
   auto check_and_decide = [&](cudaGraphConditionalHandle h) -> int {
     // W <- the preconditioned residual (the inactive columns are zeroed by the next iteration's projections)
-    CK(launch_residual<S>(AX, ld, X, ld, th_dev, m, nrow, W, ld, partial, npart, norms2, s, bm, nb, diag));
-    lob_control_kernel<<<nsys, 32, 0, s>>>(ctl, norms2, th_dev, nb, m, nev, maxit, reduced ? 1 : 0, active, st, frozen,
-                                           counter, nsys, h, stream_mode ? 0 : 1, monitor ? 1 : 0);
+    // the residual's parts are summed by the control kernel
+    CK(launch_residual<S>(AX, ld, X, ld, th_dev, m, nrow, W, ld, partial, npart, norms2, s, bm, nb, diag, false));
+    lob_control_kernel<<<nsys, 256, 0, s>>>(ctl, norms2, partial, bm.parts ? bm.nparts : npart, bm, th_dev, nb, m, nev,
+                                            maxit, reduced ? 1 : 0, active, st, frozen, counter, nsys, h,
+                                            stream_mode ? 0 : 1, monitor ? 1 : 0);
     ++g_launch_count;
     CK(cudaGetLastError());
     cond_copy_kernel<S><<<cp_grid, 256, 0, s>>>(ctl, 0, X, ld, Xbest, m, m, nrow, bmf);

@@ -188,6 +188,37 @@ __device__ __forceinline__ int bm_sys_of_row(const BatchMap& bm, long r) {
   return bm.tile_sys ? bm.tile_sys[r / kTileRows] : 0;
 }
 __device__ __forceinline__ bool bm_frozen(const BatchMap& bm, int q) { return bm.frozen && bm.frozen[q] != 0; }
+// Sum over the reduction parts of system sys of partial[b][e] for the e of this lane (lane = e - e0, e < n): the
+// CTA's 8 warps take every 8th part, in rounds of up to 16 loads issued together (no serial remainder) with the
+// additions in part order, then warp 0 adds the 8 warp sums in a fixed order.  All 256 threads call it; the result
+// is valid on warp 0's lanes with e < n.  red: 8 x 33 doubles of shared memory.
+__device__ __forceinline__ double sum_parts_cta(const double* __restrict__ partial, int npart, int n, int e, int sys,
+                                                const BatchMap& bm, double (*red)[33]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int b0 = 0, nbp = npart;
+  if (bm.sys_parts) {
+    b0 = bm.sys_parts[sys].x;
+    nbp = bm.sys_parts[sys].y;
+  }
+  constexpr int kDeep = 16;
+  double s = 0.0;
+  if (e < n) {
+    for (int b = warp; b < nbp; b += 8 * kDeep) {
+      double v[kDeep];
+#pragma unroll
+      for (int u = 0; u < kDeep; ++u) v[u] = b + 8 * u < nbp ? partial[(size_t)(b0 + b + 8 * u) * n + e] : 0.0;
+#pragma unroll
+      for (int u = 0; u < kDeep; ++u)
+        if (b + 8 * u < nbp) s += v[u];
+    }
+  }
+  red[warp][lane] = s;
+  __syncthreads();
+  double t = 0.0;
+  if (warp == 0)
+    for (int w = 0; w < 8; ++w) t += red[w][lane];
+  return t;
+}
 // rows [*r0, *r1) and system of reduction part p (uniform parts of rpp rows when the map has no table)
 __device__ __forceinline__ int bm_part(const BatchMap& bm, int p, long nrow, long rpp, long* r0, long* r1) {
   if (bm.parts) {
@@ -236,13 +267,14 @@ template <class S>
 cudaError_t launch_update(const cplx<S>* Sx, int lds, int nin, const zd* C, int ldc, int nout, int nrow,
                           cplx<S>* Out, int ldo, double alpha, double beta, cudaStream_t s,
                           const BatchMap& bm = BatchMap(), long c_stride = 0);
-// norms2 of system q at norms2 + 32 q (of AX - X theta); with diag, R receives the preconditioned residual
+// norms2 of system q at norms2 + 32 q (of AX - X theta; without sum_parts only the parts [npart][32] in partial,
+// summed by the caller's next kernel); with diag, R receives the preconditioned residual
 // |diag - theta|^-1 (AX - X theta), the denominator floored at 1e-2 max(|theta|, 1e-3)
 template <class S>
 cudaError_t launch_residual(const cplx<S>* AX, int ldax, const cplx<S>* X, int ldx, const double* theta, int m,
                             int nrow, cplx<S>* R, int ldr, double* partial, int npart, double* norms2,
                             cudaStream_t s, const BatchMap& bm = BatchMap(), long theta_stride = 0,
-                            const double* diag = nullptr);
+                            const double* diag = nullptr, bool sum_parts = true);
 template <class S>
 cudaError_t launch_copy_cols(const cplx<S>* A, int lda, cplx<S>* B, int ldb, int ncol, int nrow, cudaStream_t s);
 template <class Sa, class Sb>
