@@ -205,6 +205,144 @@ __global__ void __launch_bounds__(256) gram_pair_partial_kernel(const cplx<S>* _
     }
 }
 
+// The Gram pair for 33..48 FP32 columns over the upper triangle only (M and G are Hermitian: the lower triangle is
+// the conjugate, written by sum_partials_herm_kernel).  The 48 x 48 matrices are 16 x 16 blocks of 3 x 3; thread
+// t < 136 owns upper block t (block row a <= block column b) of both, so a staged row costs it the same 9
+// shared-memory loads and 18 complex multiply-adds as in gram_pair_partial_kernel, with about half the work.  Its
+// entries are added in the same row order with the same operand roles, so they are bitwise the entries of
+// gram_pair_partial_kernel.  160 threads a CTA; the partials are [part][136][9] complex of M, then of G at
+// partial + npart * kHermN.
+constexpr int kHermBlocks = 136;            // 3 x 3 blocks on and above the diagonal of a 48 x 48 matrix
+constexpr int kHermN = kHermBlocks * 18;    // doubles per part and matrix
+constexpr int kHermThreads = 160;
+
+__device__ __forceinline__ void herm_block(int t, int& a, int& b) {
+  int r = 0;
+  while (t >= 16 - r) {
+    t -= 16 - r;
+    ++r;
+  }
+  a = r;
+  b = r + t;
+}
+
+__global__ void __launch_bounds__(kHermThreads) gram_pair_upper_kernel(const zf* __restrict__ A,
+                                                                       const zf* __restrict__ B, int ld, int p,
+                                                                       int nrow, double* __restrict__ partial,
+                                                                       int rows_per_part, int npart, BatchMap bm) {
+  constexpr int W = 48, kRows = 32;
+  __shared__ zf As[2][kRows][W];
+  __shared__ zf Bs[2][kRows][W];
+  const int tid = threadIdx.x;
+  long r_begin, r_end;
+  const int sys = bm_part(bm, blockIdx.x, nrow, rows_per_part, &r_begin, &r_end);
+  if (bm_frozen(bm, sys)) return;
+  for (int e = tid; e < 2 * kRows * W; e += kHermThreads) {
+    if (e % W >= p) {
+      (&As[0][0][0])[e] = mk<float>(0.f, 0.f);
+      (&Bs[0][0][0])[e] = mk<float>(0.f, 0.f);
+    }
+  }
+  const int rr0 = tid / p, c0 = tid - rr0 * p, drr = kHermThreads / p, dc = kHermThreads - drr * p;
+  auto stage = [&](int buf, long r0) {
+    const int nr = (int)min((long)kRows, r_end - r0);
+    int rr = rr0, c = c0;
+    for (int e = tid; e < nr * p; e += kHermThreads) {
+      cp_async_elem<sizeof(zf)>(&As[buf][rr][c], A + (r0 + rr) * ld + c);
+      cp_async_elem<sizeof(zf)>(&Bs[buf][rr][c], B + (r0 + rr) * ld + c);
+      rr += drr;
+      c += dc;
+      if (c >= p) {
+        c -= p;
+        ++rr;
+      }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+  };
+  const bool worker = tid < kHermBlocks;
+  int ba = 0, bb = 0;
+  if (worker) herm_block(tid, ba, bb);
+  const int i0 = 3 * ba, j0 = 3 * bb;
+  zf am[3][3], ag[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) am[i][j] = ag[i][j] = mk<float>(0.f, 0.f);
+  const long nst = (r_end - r_begin + kRows - 1) / kRows;
+  if (nst > 0) stage(0, r_begin);
+  for (long t = 0; t < nst; ++t) {
+    const int buf = (int)(t & 1);
+    if (t + 1 < nst) {
+      stage(buf ^ 1, r_begin + (t + 1) * kRows);
+      asm volatile("cp.async.wait_group 1;" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;" ::: "memory");
+    }
+    __syncthreads();
+    if (worker) {
+      const int nr = (int)min((long)kRows, r_end - (r_begin + t * kRows));
+      for (int rr = 0; rr < nr; ++rr) {
+        zf a[3], b[3], c[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) a[i] = As[buf][rr][i0 + i];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          b[j] = As[buf][rr][j0 + j];
+          c[j] = Bs[buf][rr][j0 + j];
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            cfmac(am[i][j], a[i], b[j]);
+            cfmac(ag[i][j], a[i], c[j]);
+          }
+      }
+    }
+    __syncthreads();  // the next stage's copies overwrite this buffer
+  }
+  if (!worker) return;
+  double* om = partial + (size_t)blockIdx.x * kHermN + tid * 18;
+  double* og = partial + ((size_t)npart + blockIdx.x) * kHermN + tid * 18;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      om[2 * (3 * i + j)] = (double)am[i][j].re;
+      om[2 * (3 * i + j) + 1] = (double)am[i][j].im;
+      og[2 * (3 * i + j)] = (double)ag[i][j].re;
+      og[2 * (3 * i + j) + 1] = (double)ag[i][j].im;
+    }
+}
+
+// Sums the upper-block partials of gram_pair_upper_kernel over the parts (sum_parts_cta; blockIdx.z = 1: the G set)
+// and writes the p x p matrix: the entries on and above the diagonal, and their conjugates below it.
+__global__ void __launch_bounds__(256) sum_partials_herm_kernel(const double* __restrict__ partial, int npart, int p,
+                                                                double* __restrict__ outM, double* __restrict__ outG,
+                                                                BatchMap bm, long out_stride) {
+  __shared__ double red[8][33];
+  const int e = blockIdx.x * 32 + (threadIdx.x & 31);
+  const int sys = blockIdx.y;
+  double* out = outM;
+  if (blockIdx.z == 1) {
+    partial += (size_t)npart * kHermN;
+    out = outG;
+  }
+  if (bm_frozen(bm, sys)) return;
+  const double t = sum_parts_cta(partial, npart, kHermN, e, sys, bm, red);
+  if (threadIdx.x < 32 && e < kHermN) {
+    const int blk = e / 18, w = e - 18 * blk, ij = w >> 1, im = w & 1;
+    int ba, bb;
+    herm_block(blk, ba, bb);
+    const int ii = 3 * ba + ij / 3, jj = 3 * bb + ij % 3;
+    if (ii <= jj && jj < p) {  // the strictly lower entries of the diagonal blocks come from their mirrors
+      out += (size_t)sys * out_stride;
+      out[2 * (ii * p + jj) + im] = t;
+      if (ii != jj) out[2 * (jj * p + ii) + im] = im ? -t : t;
+    }
+  }
+}
+
 // out[e] = sum over b of partial[b][e] over the parts of system blockIdx.y (out at a stride of out_stride per
 // system): a CTA owns 32 consecutive e (sum_parts_cta).
 // With out2: blockIdx.z = 1 sums the second set of partials (npart parts further on) into out2.
@@ -914,6 +1052,17 @@ cudaError_t launch_gram_pair(const cplx<S>* A, const cplx<S>* B, int ld, int p, 
   if (p > 48) return cudaErrorInvalidValue;
   if (bm.parts) npart = bm.nparts;
   const int rpp = (nrow + npart - 1) / npart;
+  if constexpr (sizeof(S) == 4) {
+    if (p > 32) {
+      // upper triangle only; the reduction writes both
+      gram_pair_upper_kernel<<<npart, kHermThreads, 0, s>>>(A, B, ld, p, nrow, partial, rpp, npart, bm);
+      ++g_launch_count;
+      sum_partials_herm_kernel<<<dim3((kHermN + 31) / 32, bm.nsys, 2), 256, 0, s>>>(
+          partial, npart, p, reinterpret_cast<double*>(outM), reinterpret_cast<double*>(outG), bm, 2 * out_stride);
+      ++g_launch_count;
+      return cudaGetLastError();
+    }
+  }
   const int ti = (p + 15) / 16;
   switch (ti) {
     case 1: gram_pair_partial_kernel<S, 1><<<npart, 256, 0, s>>>(A, B, ld, p, nrow, partial, rpp, npart, bm); break;

@@ -316,7 +316,8 @@ int rayleigh_ritz(const cplx<S>* Sb, const cplx<S>* ASb, int ld, int nb, int m, 
                   const BatchMap& bm, long nn, long ts) {
   (void)st;
   if (nb <= 48) {
-    // both Grams in one pass over the basis (bitwise the same sums as two separate launches)
+    // both Grams in one pass over the basis (bitwise the same sums as two separate launches; with 33..48 FP32
+    // columns the upper triangles only, the lower ones their conjugates)
     CK(launch_gram_pair<S>(Sb, ASb, ld, nb, nrow, sm.M, sm.G, partial, npart, s, bm, nn));
   } else {
     CK(launch_gram<S>(Sb, ld, nb, Sb, ld, nb, nrow, sm.M, partial, npart, s, bm, nn));
