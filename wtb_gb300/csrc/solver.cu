@@ -383,7 +383,9 @@ __global__ void lob_ctl_reset_kernel(LobCtl* ctl, double tol, int keep_total, in
   }
 }
 
-// One warp per system.  rel_j = ||r_j|| / |theta_j|; converged columns leave the active set (soft locking).
+// One CTA of 256 threads per system: the residual norms of system q are first summed from the residual kernel's
+// parts ([npart][32] in partial, written to norms2), then warp 0 decides.  rel_j = ||r_j|| / |theta_j|;
+// converged columns leave the active set (soft locking).
 //  - breakdown guard: near the operator's rounding floor the running AX drifts from H X and LOBPCG can lose
 //    consistency (Ritz values falling far below the spectrum): the block with the lowest residual of the
 //    phase is kept (save), and a residual 10x above it after reaching 100 x tol restores it and ends the
@@ -394,12 +396,10 @@ __global__ void lob_ctl_reset_kernel(LobCtl* ctl, double tol, int keep_total, in
 //  - stagnation guard (reduced precision): residuals within 100 x tol that have not improved by 10% over
 //    15 iterations are at the operator's rounding floor; the FP64 Rayleigh-Ritz takes over;
 //  - the iteration cap, a non-finite residual and a device status word end the loop as well.
-// A system that stops is frozen: the iteration kernels leave it alone until the next phase.  The last warp
+// A system that stops is frozen: the iteration kernels leave it alone until the next phase.  The last CTA
 // to finish (a completion counter) sets the loop's condition: another pass while any system is running;
 // counter[1] holds the same answer for the host-driven loop.
 // Monitor lines follow the reference's MyEPSMonitor (src/module_slepc_solver.F90:101-116).
-// One CTA of 256 threads per system: first the residual norms of system q from the residual kernel's parts
-// ([npart][32] in partial, written to norms2), then warp 0 decides.
 __global__ void __launch_bounds__(256) lob_control_kernel(LobCtl* ctl, double* __restrict__ norms2,
                                                           const double* __restrict__ partial, int npart, BatchMap bm,
                                                           const double* __restrict__ theta, int theta_stride, int m,
